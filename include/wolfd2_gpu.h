@@ -1,0 +1,196 @@
+/*
+ * wolfd2_gpu.h -- C-ABI of the GB300 (sm_103a) projection-method time step.
+ *
+ * The library replaces the hot-path subroutines of the wolfd2 Fortran code.
+ * Every drop-in entry point takes the same arguments as the Fortran routine
+ * it replaces, in the same order and by reference (F77 implicit interfaces
+ * pass everything by address), preceded by a context handle.  Arrays are the
+ * Fortran driver's own static arrays: REAL*8 (0:mnx,0:mny) column-major,
+ * INTEGER*4 region tables (mgri,mgrj[,4]), REAL*8 dBCVal(mgri,mgrj,4,4).
+ * mnx/mny/mgri/mgrj are the driver's compile-time sizes (include/config.f)
+ * and are given once to wolfd2gpu_create.
+ *
+ * Data movement: metric arrays and region tables are uploaded once by
+ * wolfd2gpu_create / wolfd2gpu_set_metrics (they are constant after Grid and
+ * SetUpBCs).  Field arguments of the drop-ins are copied host->device on
+ * entry and device->host on exit, so each call is a self-contained
+ * replacement.  The device-resident path (wolfd2gpu_load_fields,
+ * wolfd2gpu_step, wolfd2gpu_store_fields) keeps the fields on the GPU and
+ * runs the whole time-loop body of main.f:690-972 per step.
+ *
+ * Errors: every function returns an int status, 0 on success (see
+ * W2_E_* below).  Convergence results come back through the same out
+ * arguments as the reference (nSorConv, the nAuxMomentum value).
+ * Threading: one host thread per context; calls on a context are
+ * serialised on the context's CUDA stream.
+ */
+#ifndef WOLFD2_GPU_H
+#define WOLFD2_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define W2_OK              0
+#define W2_E_ARG           1  /* bad argument or size                          */
+#define W2_E_CUDA          2  /* CUDA runtime error                           */
+#define W2_E_TIMEOUT       3  /* a device-side wait ran out its time limit    */
+#define W2_E_DIVERGED      4  /* max step difference > 1e12 (main.f:969-972)  */
+#define W2_E_BCFLAG        5  /* invalid boundary flag (bound_cond.f 'stop')  */
+#define W2_E_UNSUPPORTED   6  /* configuration outside this library's scope   */
+#define W2_E_FALLBACK      7  /* chain recurrence needed the sequential path  */
+
+/* Region / boundary enums, identical to include/wolfd2.h:15-60 of the
+ * reference. */
+#define W2_RM_BLOCKG 0
+#define W2_RM_INTERN 1
+#define W2_RM_POROUS 2
+#define W2_BM_INTERN 0
+#define W2_BM_WALL1  1
+#define W2_BM_WALL2  2
+#define W2_BM_INLET  3
+#define W2_BM_OUTLT1 4
+#define W2_BM_OUTLT2 5
+#define W2_WEST  1
+#define W2_EAST  2
+#define W2_SOUTH 3
+#define W2_NORTH 4
+
+/* Arithmetic of the hot path. */
+#define W2_PREC_FP64  0   /* plain FP64, op-by-op as the reference source  */
+#define W2_PREC_MIXED 1   /* FP32 momentum + FP32 Poisson sweeps with FP64
+                             residual/correction refinement               */
+
+typedef struct w2_ctx w2_ctx;
+
+/* Metric arrays in the argument order of grid.f:Grid (src/grid.f:31-42):
+ * rau rbu rbv rgv ran rbn rgn rac rbc rgc dju djv djc djn xen yen xzn yzn
+ * xec yec xzc yzc xeu yeu xzv yzv xzu yzu xev yev -- 30 host pointers,
+ * each REAL*8 (0:mnx,0:mny). */
+#define W2_NMETRIC 30
+
+/* Create a context for an nx x ny natural-point grid.  Uploads the region
+ * tables (output of SetUpBCs, src/bound_cond.f:34-443).  Fields are zero.
+ * No reference counterpart (the reference keeps these as static arrays). */
+int wolfd2gpu_create(w2_ctx **ctx, int mnx, int mny, int mgri, int mgrj,
+                     int nx, int ny, const int *nReg, const int *nRegBrd,
+                     const int *nRegType, const int *nMomBdTp,
+                     const double *dBCVal, const double *dPRporos,
+                     const double *dPRporc1, const double *dPRporc2);
+int wolfd2gpu_destroy(w2_ctx *ctx);
+
+/* Upload the 30 metric arrays computed by the driver's Grid
+ * (src/grid.f:368-535), in the order listed above. */
+int wolfd2gpu_set_metrics(w2_ctx *ctx, const double *const *metrics);
+
+/* Compute the metric arrays on the device from natural grid points gx, gy
+ * (0:mnx,0:mny) with nodes (1..nx,1..ny) filled and already divided by
+ * dlref: MirrorPts + FullGrid + Metric, src/grid.f:258-535.  If metrics_out
+ * is non-NULL the 30 arrays are also copied back to those host arrays. */
+int wolfd2gpu_grid_metric(w2_ctx *ctx, const double *gx, const double *gy,
+                          double *const *metrics_out);
+
+/* ---- Drop-in replacements (arguments as in the reference) ------------ */
+
+/* nAuxMomentum, src/momentum.f:33-48: returns the number of Q-L iterations
+ * (or -1) through *nQLiter.  Metric arguments are accepted for signature
+ * parity and ignored: the copies uploaded at set-up are used. */
+int wolfd2gpu_naux_momentum(w2_ctx *ctx, const int *nx, const int *ny,
+                            const int *mqiter, const double *dk,
+                            const double *re, const double *fr,
+                            const double *qtol, const double *d,
+                            const double *dn, const double *un,
+                            const double *vn, double *us, double *vs,
+                            int *nQLiter);
+
+/* Ppe, src/pressure.f:30-38: solves for p in place; nSorConv out. */
+int wolfd2gpu_ppe(w2_ctx *ctx, const int *nx, const int *ny,
+                  const int *lCartesGrid, const int *nPpeSolver,
+                  const int *msorit, int *nSorConv, const double *dk,
+                  const double *sortol, const double *sorrel, const double *u,
+                  const double *v, double *p);
+
+/* Project, src/utility.f:253-259. */
+int wolfd2gpu_project(w2_ctx *ctx, const int *nx, const int *ny,
+                      const double *dk, const double *p, double *u, double *v);
+
+/* VelBoundCond, src/bound_cond.f:511-513. */
+int wolfd2gpu_vel_bound_cond(w2_ctx *ctx, const int *nx, const int *ny,
+                             double *u, double *v);
+
+/* PresBoundCond, src/bound_cond.f:853-856. */
+int wolfd2gpu_pres_bound_cond(w2_ctx *ctx, const int *nx, const int *ny,
+                              double *p);
+
+/* VelOutflowBCs, src/bound_cond.f:1656-1659. */
+int wolfd2gpu_vel_outflow_bcs(w2_ctx *ctx, const int *nx, const int *ny,
+                              double *u, double *v);
+
+/* DiffMaxNorm, src/utility.f:446: *result = max |un - u| over the
+ * reference's index range. */
+int wolfd2gpu_diff_max_norm(w2_ctx *ctx, const int *nx, const int *ny,
+                            const double *un, const double *u,
+                            double *result);
+
+/* Filter, src/utility.f:33-36, velocity components (ncomp 1 = u, 2 = v). */
+int wolfd2gpu_filter(w2_ctx *ctx, const int *nx, const int *ny,
+                     const int *ncomp, const double *fp, double *qu);
+
+/* ---- Device-resident time loop ---------------------------------------- */
+
+/* Run parameters of the time loop (main.f with nthermen = 0). */
+typedef struct {
+  double dk, re, fr, qtol, sortol, sorrel, fpu, fpv;
+  int mqiter, npsolver, msorit, nfiltu, nfiltv, lcartes;
+  int precision;      /* W2_PREC_*                                        */
+  int refine_sweeps;  /* mixed: FP32 sweeps per refinement pass (0=auto) */
+  double refine_tol;  /* mixed: FP64 residual target (0 = auto)          */
+} w2_params;
+
+/* Per-step results of main.f:753-966. */
+typedef struct {
+  int nQLiter, nSorConv;
+  double dif[4];      /* DiffMaxNorm of (pn,p), (un,u), (vn,v), (tn,t)  */
+} w2_stepstat;
+
+/* Copy u, v, p (0:mnx,0:mny host arrays) to / from the device state. */
+int wolfd2gpu_load_fields(w2_ctx *ctx, const double *u, const double *v,
+                          const double *p);
+int wolfd2gpu_store_fields(w2_ctx *ctx, double *u, double *v, double *p);
+
+/* Cold-start projection, main.f:606-641; *nSorConv out. */
+int wolfd2gpu_cold_start(w2_ctx *ctx, const w2_params *prm, int *nSorConv);
+
+/* nsteps passes of the time loop body, main.f:693-972, on device-resident
+ * fields.  stats (may be NULL) receives one record per step.  Returns
+ * W2_E_DIVERGED at the first step whose max difference exceeds 1e12. */
+int wolfd2gpu_step(w2_ctx *ctx, const w2_params *prm, int nsteps,
+                   w2_stepstat *stats);
+
+/* Synchronise the context stream; returns the first pending error. */
+int wolfd2gpu_sync(w2_ctx *ctx);
+
+/* Last error message of this context (static storage of the context). */
+const char *wolfd2gpu_last_error(w2_ctx *ctx);
+
+/* Library configuration knobs (segment length and warm-up of the chain
+ * recurrence, threads per block, blocks per SM); 0 keeps the default.
+ * Takes effect on the next launch. */
+int wolfd2gpu_tune(w2_ctx *ctx, int chain_seg, int chain_warm, int threads,
+                   int blocks_per_sm);
+
+/* Device pointers of the resident u, v, p fields and the device leading
+ * dimension (elements), for callers that bring their own device buffers. */
+int wolfd2gpu_device_fields(w2_ctx *ctx, double **u, double **v, double **p,
+                            int *ld);
+
+/* Kernel launches issued so far by this context (for accounting). */
+long long wolfd2gpu_launch_count(w2_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,243 @@
+"""ctypes front end of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Loads oracle/_build/libwolfd2_oracle.so (building it with ``make`` when it is
+missing) and exposes the restated reference routines on Fortran-layout numpy
+arrays of shape (mnx+1, mny+1).  Used by tests/, by the smoke check and by the
+CPU-baseline leg of bench.py, never by the product.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+from typing import Dict, Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libwolfd2_oracle.so")
+_lock = threading.Lock()
+_lib = None
+
+METRIC_NAMES = ("ran rbn rgn rac rbc rgc rau rbu rbv rgv dju djv djc djn "
+                "xen yen xzn yzn xec yec xzc yzc xeu yeu xzv yzv xzu yzu xev yev").split()
+FIELD_NAMES = "u v p t un vn pn tn us vs ts d dn".split()
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class _Regions(C.Structure):
+    _fields_ = [("mgri", C.c_int), ("mgrj", C.c_int), ("nReg", _ip),
+                ("nRegBrd", _ip), ("nRegType", _ip), ("nMomBdTp", _ip),
+                ("dBCVal", _dp), ("dPRporos", _dp), ("dPRporc1", _dp),
+                ("dPRporc2", _dp)]
+
+
+class _Metrics(C.Structure):
+    _fields_ = [(n, _dp) for n in METRIC_NAMES]
+
+
+class _Params(C.Structure):
+    _fields_ = [(n, C.c_double) for n in "dk re fr qtol sortol sorrel fpu fpv".split()] + \
+               [(n, C.c_int) for n in "mqiter npsolver msorit nfiltu nfiltv lcartes".split()]
+
+
+class _Fields(C.Structure):
+    _fields_ = [(n, _dp) for n in FIELD_NAMES]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle library (gcc, no FMA contraction)."""
+    if force or not os.path.exists(LIB_PATH) or \
+            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "wolfd2_oracle.c")):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = C.CDLL(LIB_PATH)
+            L.w2o_create.restype = C.c_void_p
+            L.w2o_create.argtypes = [C.c_int, C.c_int]
+            L.w2o_destroy.argtypes = [C.c_void_p]
+            L.w2o_grid.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, C.POINTER(_Metrics)]
+            L.w2o_naux_momentum.restype = C.c_int
+            L.w2o_naux_momentum.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                            C.POINTER(_Regions), C.c_double, C.c_double,
+                                            C.c_double, C.c_double, C.POINTER(_Metrics),
+                                            _dp, _dp, _dp, _dp, _dp, _dp]
+            L.w2o_ppe.restype = C.c_int
+            L.w2o_ppe.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions), C.c_int,
+                                  C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                  C.POINTER(_Metrics), _dp, _dp, _dp]
+            L.w2o_project.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions),
+                                      C.c_double, C.POINTER(_Metrics), _dp, _dp, _dp]
+            for nm in ("w2o_vel_bound_cond", "w2o_vel_outflow_bcs"):
+                getattr(L, nm).argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions), _dp, _dp]
+            L.w2o_pres_bound_cond.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions), _dp]
+            L.w2o_filter.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(_Regions),
+                                     C.c_double, _dp]
+            L.w2o_diff_max_norm.restype = C.c_double
+            L.w2o_diff_max_norm.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp]
+            L.w2o_dmax_norm.restype = C.c_double
+            L.w2o_dmax_norm.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp]
+            L.w2o_alt_trid_lu.argtypes = [C.c_int, _dp, _dp]
+            L.w2o_cold_start.restype = C.c_int
+            L.w2o_cold_start.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions),
+                                         C.POINTER(_Params), C.POINTER(_Metrics), C.POINTER(_Fields)]
+            L.w2o_step.restype = C.c_int
+            L.w2o_step.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions),
+                                   C.POINTER(_Params), C.POINTER(_Metrics), C.POINTER(_Fields),
+                                   _ip, _ip, _dp]
+            _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray, ct=C.c_double):
+    assert a.flags["F_CONTIGUOUS"] or a.ndim == 1, "oracle arrays must be Fortran-ordered"
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def alt_trid_lu(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """AltTridLU on copies; a has shape (3, n) (Fortran a(3,n))."""
+    a = np.asfortranarray(a, np.float64).copy(order="F")
+    b = np.ascontiguousarray(b, np.float64).copy()
+    lib().w2o_alt_trid_lu(int(b.size), _ptr(a), b.ctypes.data_as(_dp))
+    return b
+
+
+class Oracle:
+    """One oracle context: persistent work arrays for a (0:mnx, 0:mny) box."""
+
+    def __init__(self, mnx: int, mny: int):
+        self.mnx, self.mny = mnx, mny
+        self.L = lib()
+        self.h = C.c_void_p(self.L.w2o_create(mnx, mny))
+        self._keep = []
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.L.w2o_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def field(self) -> np.ndarray:
+        return np.zeros((self.mnx + 1, self.mny + 1), np.float64, order="F")
+
+    # -- setup --------------------------------------------------------------
+    def grid(self, nx: int, ny: int, x_nodes: np.ndarray, y_nodes: np.ndarray) -> Dict[str, np.ndarray]:
+        """grid.f Grid minus file reading; returns the 30 metric arrays."""
+        gx, gy = self.field(), self.field()
+        gx[1:nx + 1, 1:ny + 1] = x_nodes
+        gy[1:nx + 1, 1:ny + 1] = y_nodes
+        met = {n: self.field() for n in METRIC_NAMES}
+        ms = _Metrics(*[_ptr(met[n]) for n in METRIC_NAMES])
+        self.L.w2o_grid(self.h, nx, ny, _ptr(gx), _ptr(gy), C.byref(ms))
+        met["gx"], met["gy"] = gx, gy
+        return met
+
+    @staticmethod
+    def regions_struct(regs) -> _Regions:
+        arrs = [np.asfortranarray(getattr(regs, n)) for n in
+                ("nReg", "nRegBrd", "nRegType", "nMomBdTp")]
+        darrs = [np.asfortranarray(getattr(regs, n)) for n in
+                 ("dBCVal", "dPRporos", "dPRporc1", "dPRporc2")]
+        s = _Regions(regs.nRegBrd.shape[0], regs.nRegBrd.shape[1],
+                     *[_ptr(a, C.c_int) for a in arrs], *[_ptr(a) for a in darrs])
+        s._keep = (arrs, darrs)
+        return s
+
+    @staticmethod
+    def metrics_struct(met: Dict[str, np.ndarray]) -> _Metrics:
+        return _Metrics(*[_ptr(met[n]) for n in METRIC_NAMES])
+
+    @staticmethod
+    def params_struct(p) -> _Params:
+        return _Params(p.dk, p.re, p.fr, p.qtol, p.sortol, p.sorrel, p.fpu, p.fpv,
+                       p.mqiter, p.npsolver, p.msorit, p.nfiltu, p.nfiltv, p.lcartes)
+
+    # -- routines -----------------------------------------------------------
+    def naux_momentum(self, nx, ny, regs, prm, met, d, dn, un, vn, us, vs) -> int:
+        rs = self.regions_struct(regs)
+        return self.L.w2o_naux_momentum(self.h, nx, ny, prm.mqiter, C.byref(rs), prm.dk,
+                                        prm.re, prm.fr, prm.qtol,
+                                        C.byref(self.metrics_struct(met)),
+                                        _ptr(d), _ptr(dn), _ptr(un), _ptr(vn), _ptr(us), _ptr(vs))
+
+    def ppe(self, nx, ny, regs, prm, met, u, v, p, npsolver=None, msorit=None) -> int:
+        rs = self.regions_struct(regs)
+        return self.L.w2o_ppe(self.h, nx, ny, C.byref(rs), prm.lcartes,
+                              prm.npsolver if npsolver is None else npsolver,
+                              prm.msorit if msorit is None else msorit,
+                              prm.dk, prm.sortol, prm.sorrel,
+                              C.byref(self.metrics_struct(met)), _ptr(u), _ptr(v), _ptr(p))
+
+    def project(self, nx, ny, regs, dk, met, p, u, v) -> None:
+        rs = self.regions_struct(regs)
+        self.L.w2o_project(self.h, nx, ny, C.byref(rs), dk, C.byref(self.metrics_struct(met)),
+                           _ptr(p), _ptr(u), _ptr(v))
+
+    def vel_bound_cond(self, nx, ny, regs, u, v) -> None:
+        rs = self.regions_struct(regs)
+        self.L.w2o_vel_bound_cond(self.h, nx, ny, C.byref(rs), _ptr(u), _ptr(v))
+
+    def vel_outflow_bcs(self, nx, ny, regs, u, v) -> None:
+        rs = self.regions_struct(regs)
+        self.L.w2o_vel_outflow_bcs(self.h, nx, ny, C.byref(rs), _ptr(u), _ptr(v))
+
+    def pres_bound_cond(self, nx, ny, regs, p) -> None:
+        rs = self.regions_struct(regs)
+        self.L.w2o_pres_bound_cond(self.h, nx, ny, C.byref(rs), _ptr(p))
+
+    def filter(self, nx, ny, ncomp, regs, fp, q) -> None:
+        rs = self.regions_struct(regs)
+        self.L.w2o_filter(self.h, nx, ny, ncomp, C.byref(rs), fp, _ptr(q))
+
+    def diff_max_norm(self, nx, ny, un, u) -> float:
+        return self.L.w2o_diff_max_norm(self.h, nx, ny, _ptr(un), _ptr(u))
+
+    def dmax_norm(self, nx, ny, u) -> float:
+        return self.L.w2o_dmax_norm(self.h, nx, ny, _ptr(u))
+
+
+class OracleRun:
+    """A whole case advanced by the oracle's time loop (main.f:690-972)."""
+
+    def __init__(self, case, fields: Optional[Dict[str, np.ndarray]] = None, cold_start: bool = True):
+        self.case = case
+        self.nx, self.ny = case.nx, case.ny
+        self.o = Oracle(case.nx + 1, case.ny + 1)
+        self.met = self.o.grid(case.nx, case.ny, case.x, case.y)
+        self.f = {n: self.o.field() for n in FIELD_NAMES}
+        if fields:
+            for k, v in fields.items():
+                self.f[k][...] = v
+        self._rs = Oracle.regions_struct(case.regions)
+        self._ms = Oracle.metrics_struct(self.met)
+        self._ps = Oracle.params_struct(case.params)
+        self._fs = _Fields(*[_ptr(self.f[n]) for n in FIELD_NAMES])
+        self.history = []
+        self.cold_nconv = None
+        if cold_start:
+            self.cold_nconv = self.o.L.w2o_cold_start(self.o.h, self.nx, self.ny, C.byref(self._rs),
+                                                      C.byref(self._ps), C.byref(self._ms),
+                                                      C.byref(self._fs))
+
+    def step(self, n: int = 1):
+        nql, nsor = C.c_int(), C.c_int()
+        dif = (C.c_double * 4)()
+        for _ in range(n):
+            rc = self.o.L.w2o_step(self.o.h, self.nx, self.ny, C.byref(self._rs), C.byref(self._ps),
+                                   C.byref(self._ms), C.byref(self._fs), C.byref(nql),
+                                   C.byref(nsor), dif)
+            self.history.append((nql.value, nsor.value, tuple(dif)))
+            if rc:
+                raise FloatingPointError("Solution diverged. Please reduce CFL number.")
+        return self.history[-1]

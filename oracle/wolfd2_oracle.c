@@ -1,0 +1,1439 @@
+/*
+ * wolfd2_oracle.c -- TEST INFRASTRUCTURE: CPU restatement of the reference's
+ * projection-method time step.  See wolfd2_oracle.h for the scope, the
+ * storage conventions and the parity-pinning status.
+ *
+ * Every routine names the reference file:line it restates.  Expressions keep
+ * the reference's evaluation order (Fortran evaluates same-precedence
+ * operators left to right and this file is compiled without FMA
+ * contraction), so results are the IEEE-double results of the reference
+ * source as written.
+ */
+#include "wolfd2_oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* Region and boundary enums, include/wolfd2.h:15-60 */
+enum { RM_BLOCKG = 0, RM_INTERN = 1, RM_POROUS = 2 };
+enum { BM_INTERN = 0, BM_WALL1 = 1, BM_WALL2 = 2, BM_INLET = 3,
+       BM_OUTLT1 = 4, BM_OUTLT2 = 5 };
+enum { WEST = 1, EAST = 2, SOUTH = 3, NORTH = 4 };
+enum { VU = 1, VV = 2, VP = 3, VT = 4 };
+
+/* Persistent work storage (the reference's static locals). */
+typedef struct {
+  double *cj1, *cj2, *c1s, *c2s, *c1n, *c2n, *cps, *cpn, *cpj;
+  double *cnvs, *difs, *cnvn, *difn;
+  double *a; /* a(3,mn) */
+  double *b; /* b(mn)   */
+} w2o_mom_ws;
+
+struct w2o_ctx {
+  int mnx, mny;
+  size_t ld, nf; /* leading dimension mnx+1 and field size */
+  size_t mn;     /* mnx*mny (chain workspace length) */
+  w2o_mom_ws wx, wy;       /* XMomentum / YMomentum statics            */
+  double *dus, *dvs;       /* nAuxMomentum statics                     */
+  double *div, *pa, *pb;   /* Ppe statics: div, a(mn,5), b(mn)         */
+  double *rbp_pn;          /* SlorRBP static pn(0:mnx,0:mny)           */
+  double *qh;              /* Filter static qh                         */
+  double *xu, *yu, *xv, *yv, *xc, *yc; /* Grid statics              */
+  double *lin;             /* aline/bline/plold for the line solvers   */
+  double *rbp_dif;         /* SorRBP dif(0:nx+1,0:ny+1)                */
+};
+
+#define IX(i, j) ((size_t)(i) + (size_t)(j) * c->ld)
+#define F(a, i, j) (a)[IX(i, j)]
+
+/* Region-table accessors (Fortran column-major, 1-based). */
+#define RBRD(r, ir, jr, s) \
+  (r)->nRegBrd[((ir)-1) + ((jr)-1) * (r)->mgri + ((s)-1) * (r)->mgri * (r)->mgrj]
+#define RTYP(r, ir, jr) (r)->nRegType[((ir)-1) + ((jr)-1) * (r)->mgri]
+#define MBTP(r, ir, jr, s) \
+  (r)->nMomBdTp[((ir)-1) + ((jr)-1) * (r)->mgri + ((s)-1) * (r)->mgri * (r)->mgrj]
+#define BCV(r, ir, jr, s, var)                                            \
+  (r)->dBCVal[((ir)-1) + ((jr)-1) * (r)->mgri + ((s)-1) * (r)->mgri * (r)->mgrj + \
+              ((var)-1) * (r)->mgri * (r)->mgrj * 4]
+#define RPAR(arr, r, ir, jr) (r)->arr[((ir)-1) + ((jr)-1) * (r)->mgri]
+
+static void die(const char *msg, int ir, int jr) {
+  fprintf(stderr, "%s in region %d,%d\n", msg, ir, jr);
+  exit(2);
+}
+
+static double *zalloc(size_t n) {
+  double *p = (double *)calloc(n ? n : 1, sizeof(double));
+  if (!p) {
+    fprintf(stderr, "oracle: out of memory\n");
+    exit(3);
+  }
+  return p;
+}
+
+static void mom_ws_init(w2o_mom_ws *w, size_t nf, size_t mn) {
+  w->cj1 = zalloc(nf); w->cj2 = zalloc(nf); w->c1s = zalloc(nf);
+  w->c2s = zalloc(nf); w->c1n = zalloc(nf); w->c2n = zalloc(nf);
+  w->cps = zalloc(nf); w->cpn = zalloc(nf); w->cpj = zalloc(nf);
+  w->cnvs = zalloc(nf); w->difs = zalloc(nf); w->cnvn = zalloc(nf);
+  w->difn = zalloc(nf);
+  w->a = zalloc(3 * mn); w->b = zalloc(mn);
+}
+
+static void mom_ws_free(w2o_mom_ws *w) {
+  free(w->cj1); free(w->cj2); free(w->c1s); free(w->c2s); free(w->c1n);
+  free(w->c2n); free(w->cps); free(w->cpn); free(w->cpj); free(w->cnvs);
+  free(w->difs); free(w->cnvn); free(w->difn); free(w->a); free(w->b);
+}
+
+w2o_ctx *w2o_create(int mnx, int mny) {
+  w2o_ctx *c = (w2o_ctx *)calloc(1, sizeof(w2o_ctx));
+  c->mnx = mnx; c->mny = mny;
+  c->ld = (size_t)mnx + 1;
+  c->nf = c->ld * ((size_t)mny + 1);
+  c->mn = (size_t)mnx * (size_t)mny;
+  mom_ws_init(&c->wx, c->nf, c->mn);
+  mom_ws_init(&c->wy, c->nf, c->mn);
+  c->dus = zalloc(c->nf); c->dvs = zalloc(c->nf);
+  c->div = zalloc(c->nf); c->pa = zalloc(5 * c->mn); c->pb = zalloc(c->mn);
+  c->rbp_pn = zalloc(c->nf); c->qh = zalloc(c->nf);
+  c->xu = zalloc(c->nf); c->yu = zalloc(c->nf); c->xv = zalloc(c->nf);
+  c->yv = zalloc(c->nf); c->xc = zalloc(c->nf); c->yc = zalloc(c->nf);
+  size_t mnl = (size_t)(mnx > mny ? mnx : mny);
+  c->lin = zalloc(5 * mnl);
+  c->rbp_dif = zalloc(c->nf);
+  return c;
+}
+
+void w2o_destroy(w2o_ctx *c) {
+  if (!c) return;
+  mom_ws_free(&c->wx); mom_ws_free(&c->wy);
+  free(c->dus); free(c->dvs); free(c->div); free(c->pa); free(c->pb);
+  free(c->rbp_pn); free(c->qh); free(c->xu); free(c->yu); free(c->xv);
+  free(c->yv); free(c->xc); free(c->yc); free(c->lin); free(c->rbp_dif);
+  free(c);
+}
+
+/* ------------------------------------------------------------------ */
+/* grid.f                                                              */
+/* ------------------------------------------------------------------ */
+
+void w2o_grid(w2o_ctx *c, int nx, int ny, double *x, double *y,
+              w2o_metrics *m) {
+  int i, j;
+  /* MirrorPts, grid.f:258-306 */
+  for (i = 1; i <= nx; i++) {
+    F(x, i, 0) = 2.0 * F(x, i, 1) - F(x, i, 2);
+    F(x, i, ny + 1) = 2.0 * F(x, i, ny) - F(x, i, ny - 1);
+    F(y, i, 0) = 2.0 * F(y, i, 1) - F(y, i, 2);
+    F(y, i, ny + 1) = 2.0 * F(y, i, ny) - F(y, i, ny - 1);
+  }
+  for (j = 1; j <= ny; j++) {
+    F(x, 0, j) = 2.0 * F(x, 1, j) - F(x, 2, j);
+    F(x, nx + 1, j) = 2.0 * F(x, nx, j) - F(x, nx - 1, j);
+    F(y, 0, j) = 2.0 * F(y, 1, j) - F(y, 2, j);
+    F(y, nx + 1, j) = 2.0 * F(y, nx, j) - F(y, nx - 1, j);
+  }
+  F(x, 0, 0) = 2.0 * F(x, 1, 1) - F(x, 2, 2);
+  F(y, 0, 0) = 2.0 * F(y, 1, 1) - F(y, 2, 2);
+  F(x, 0, ny + 1) = 2.0 * F(x, 1, ny) - F(x, 2, ny - 1);
+  F(y, 0, ny + 1) = 2.0 * F(y, 1, ny) - F(y, 2, ny - 1);
+  F(x, nx + 1, 0) = 2.0 * F(x, nx, 1) - F(x, nx - 1, 2);
+  F(y, nx + 1, 0) = 2.0 * F(y, nx, 1) - F(y, nx - 1, 2);
+  F(x, nx + 1, ny + 1) = 2.0 * F(x, nx, ny) - F(x, nx - 1, ny - 1);
+  F(y, nx + 1, ny + 1) = 2.0 * F(y, nx, ny) - F(y, nx - 1, ny - 1);
+
+  /* FullGrid, grid.f:312-362 */
+  double *xu = c->xu, *yu = c->yu, *xv = c->xv, *yv = c->yv, *xc = c->xc,
+         *yc = c->yc;
+  for (j = 1; j <= ny + 1; j++)
+    for (i = 0; i <= nx + 1; i++) {
+      F(xu, i, j) = 0.5 * (F(x, i, j) + F(x, i, j - 1));
+      F(yu, i, j) = 0.5 * (F(y, i, j) + F(y, i, j - 1));
+    }
+  for (j = 0; j <= ny + 1; j++)
+    for (i = 1; i <= nx + 1; i++) {
+      F(xv, i, j) = 0.5 * (F(x, i, j) + F(x, i - 1, j));
+      F(yv, i, j) = 0.5 * (F(y, i, j) + F(y, i - 1, j));
+    }
+  for (j = 1; j <= ny + 1; j++)
+    for (i = 1; i <= nx + 1; i++) {
+      F(xc, i, j) = 0.5 * (F(xu, i, j) + F(xu, i - 1, j));
+      F(yc, i, j) = 0.5 * (F(yv, i, j) + F(yv, i, j - 1));
+    }
+
+  /* Metric, grid.f:368-535 */
+  double g11, g12, g22;
+  for (j = 1; j <= ny; j++)
+    for (i = 1; i <= nx; i++) {
+      F(m->xzn, i, j) = F(xv, i + 1, j) - F(xv, i, j);
+      F(m->xen, i, j) = F(xu, i, j + 1) - F(xu, i, j);
+      F(m->yzn, i, j) = F(yv, i + 1, j) - F(yv, i, j);
+      F(m->yen, i, j) = F(yu, i, j + 1) - F(yu, i, j);
+      F(m->djn, i, j) = 1.0 / (F(m->xzn, i, j) * F(m->yen, i, j) -
+                               F(m->xen, i, j) * F(m->yzn, i, j));
+      g11 = F(m->xzn, i, j) * F(m->xzn, i, j) + F(m->yzn, i, j) * F(m->yzn, i, j);
+      g12 = F(m->xzn, i, j) * F(m->xen, i, j) + F(m->yzn, i, j) * F(m->yen, i, j);
+      g22 = F(m->xen, i, j) * F(m->xen, i, j) + F(m->yen, i, j) * F(m->yen, i, j);
+      F(m->ran, i, j) = F(m->djn, i, j) * g22;
+      F(m->rbn, i, j) = -F(m->djn, i, j) * g12 * 0.25;
+      F(m->rgn, i, j) = F(m->djn, i, j) * g11;
+    }
+  for (j = 1; j <= ny; j++)
+    for (i = 1; i <= nx; i++) {
+      F(m->xzu, i, j) = F(xc, i + 1, j) - F(xc, i, j);
+      F(m->xeu, i, j) = F(x, i, j) - F(x, i, j - 1);
+      F(m->yzu, i, j) = F(yc, i + 1, j) - F(yc, i, j);
+      F(m->yeu, i, j) = F(y, i, j) - F(y, i, j - 1);
+      F(m->dju, i, j) = 1.0 / (F(m->xzu, i, j) * F(m->yeu, i, j) -
+                               F(m->xeu, i, j) * F(m->yzu, i, j));
+      g11 = F(m->xzu, i, j) * F(m->xzu, i, j) + F(m->yzu, i, j) * F(m->yzu, i, j);
+      g12 = F(m->xzu, i, j) * F(m->xeu, i, j) + F(m->yzu, i, j) * F(m->yeu, i, j);
+      g22 = F(m->xeu, i, j) * F(m->xeu, i, j) + F(m->yeu, i, j) * F(m->yeu, i, j);
+      (void)g11;
+      F(m->rau, i, j) = F(m->dju, i, j) * g22;
+      F(m->rbu, i, j) = -F(m->dju, i, j) * g12 * 0.25;
+    }
+  for (j = 1; j <= ny; j++)
+    for (i = 1; i <= nx; i++) {
+      F(m->xzv, i, j) = F(x, i, j) - F(x, i - 1, j);
+      F(m->xev, i, j) = F(xc, i, j + 1) - F(xc, i, j);
+      F(m->yzv, i, j) = F(y, i, j) - F(y, i - 1, j);
+      F(m->yev, i, j) = F(yc, i, j + 1) - F(yc, i, j);
+      F(m->djv, i, j) = 1.0 / (F(m->xzv, i, j) * F(m->yev, i, j) -
+                               F(m->xev, i, j) * F(m->yzv, i, j));
+      g11 = F(m->xzv, i, j) * F(m->xzv, i, j) + F(m->yzv, i, j) * F(m->yzv, i, j);
+      g12 = F(m->xzv, i, j) * F(m->xev, i, j) + F(m->yzv, i, j) * F(m->yev, i, j);
+      g22 = F(m->xev, i, j) * F(m->xev, i, j) + F(m->yev, i, j) * F(m->yev, i, j);
+      (void)g22;
+      F(m->rbv, i, j) = -F(m->djv, i, j) * g12 * 0.25;
+      F(m->rgv, i, j) = F(m->djv, i, j) * g11;
+    }
+  for (j = 1; j <= ny; j++)
+    for (i = 1; i <= nx; i++) {
+      F(m->xzc, i, j) = F(xu, i, j) - F(xu, i - 1, j);
+      F(m->xec, i, j) = F(xv, i, j) - F(xv, i, j - 1);
+      F(m->yzc, i, j) = F(yu, i, j) - F(yu, i - 1, j);
+      F(m->yec, i, j) = F(yv, i, j) - F(yv, i, j - 1);
+      F(m->djc, i, j) = 1.0 / (F(m->xzc, i, j) * F(m->yec, i, j) -
+                               F(m->xec, i, j) * F(m->yzc, i, j));
+      g11 = F(m->xzc, i, j) * F(m->xzc, i, j) + F(m->yzc, i, j) * F(m->yzc, i, j);
+      g12 = F(m->xzc, i, j) * F(m->xec, i, j) + F(m->yzc, i, j) * F(m->yec, i, j);
+      g22 = F(m->xec, i, j) * F(m->xec, i, j) + F(m->yec, i, j) * F(m->yec, i, j);
+      F(m->rac, i, j) = F(m->djc, i, j) * g22;
+      F(m->rbc, i, j) = -F(m->djc, i, j) * g12 * 0.25;
+      F(m->rgc, i, j) = F(m->djc, i, j) * g11;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* momentum.f                                                          */
+/* ------------------------------------------------------------------ */
+
+/* AltTridLU, momentum.f:1307-1339.  a is a(3,n) column-major: a(k,i) at
+ * a[(k-1) + 3*(i-1)].  Row 1's super-diagonal is divided by the ORIGINAL
+ * diagonal of row 2 (momentum.f:1319). */
+void w2o_alt_trid_lu(int n, double *a, double *b) {
+#define A(k, i) a[((k)-1) + 3 * (size_t)((i)-1)]
+#define B(i) b[(i)-1]
+  int i;
+  A(3, 1) = A(3, 1) / A(2, 2);
+  B(1) = B(1) / A(2, 1);
+  for (i = 2; i <= n - 1; i++) {
+    A(2, i) = A(2, i) - (A(1, i) * A(3, i - 1));
+    A(3, i) = A(3, i) / A(2, i);
+    B(i) = (B(i) - A(1, i) * B(i - 1)) / A(2, i);
+  }
+  A(2, n) = A(2, n) - (A(1, n) * A(3, n - 1));
+  B(n) = (B(n) - A(1, n) * B(n - 1)) / A(2, n);
+  for (i = n - 1; i >= 1; i--) B(i) = B(i) - (A(3, i) * B(i + 1));
+#undef A
+#undef B
+}
+
+/* ConvCoef, momentum.f:864-981 (cases 1, 2, 4, 5). */
+static void conv_coef(w2o_ctx *c, int nx, int ny, int ncomp, int njacob,
+                      const double *xzi, const double *xet, const double *yzi,
+                      const double *yet, const double *u, const double *v,
+                      double *cc1, double *cc2) {
+  int i, j;
+  double djac = 1.0;
+  if (njacob == 1) djac = 2.0;
+  switch (ncomp) {
+    case 1:
+      for (j = 1; j <= ny + 1; j++)
+        for (i = 1; i <= nx + 1; i++)
+          F(cc1, i, j) = (djac * F(yet, i, j) * (F(u, i, j) + F(u, i - 1, j)) -
+                          F(xet, i, j) * (F(v, i, j) + F(v, i, j - 1))) * 0.5;
+      for (j = 1; j <= ny; j++)
+        for (i = 1; i <= nx; i++)
+          F(cc2, i, j) = (F(xzi, i, j) * (F(v, i + 1, j) + F(v, i, j)) -
+                          djac * F(yzi, i, j) * (F(u, i, j + 1) + F(u, i, j))) * 0.5;
+      break;
+    case 2:
+      for (j = 1; j <= ny; j++)
+        for (i = 1; i <= nx; i++)
+          F(cc1, i, j) = (F(yet, i, j) * (F(u, i, j + 1) + F(u, i, j)) -
+                          djac * F(xet, i, j) * (F(v, i + 1, j) + F(v, i, j))) * 0.5;
+      for (j = 1; j <= ny + 1; j++)
+        for (i = 1; i <= nx + 1; i++)
+          F(cc2, i, j) = (djac * F(xzi, i, j) * (F(v, i, j) + F(v, i, j - 1)) -
+                          F(yzi, i, j) * (F(u, i, j) + F(u, i - 1, j))) * 0.5;
+      break;
+    case 4:
+      for (j = 1; j <= ny; j++)
+        for (i = 0; i <= nx; i++) {
+          F(cc1, i, j) = djac * F(yet, i, j) * F(u, i, j) -
+                         F(xet, i, j) * (F(v, i + 1, j) + F(v, i, j) +
+                                         F(v, i + 1, j - 1) + F(v, i, j - 1)) / 4.0;
+          F(cc2, i, j) = F(xzi, i, j) * (F(v, i + 1, j) + F(v, i, j) +
+                                         F(v, i + 1, j - 1) + F(v, i, j - 1)) / 4.0 -
+                         djac * F(yzi, i, j) * F(u, i, j);
+        }
+      break;
+    case 5:
+      for (j = 0; j <= ny; j++)
+        for (i = 1; i <= nx; i++) {
+          F(cc1, i, j) = F(yet, i, j) * (F(u, i, j + 1) + F(u, i - 1, j + 1) +
+                                         F(u, i, j) + F(u, i - 1, j)) / 4.0 -
+                         djac * F(xet, i, j) * F(v, i, j);
+          F(cc2, i, j) = djac * F(xzi, i, j) * F(v, i, j) -
+                         F(yzi, i, j) * (F(u, i, j + 1) + F(u, i - 1, j + 1) +
+                                         F(u, i, j) + F(u, i - 1, j)) / 4.0;
+        }
+      break;
+    default:
+      die("Error: Wrong component flag passed to ConvCoef", ncomp, 0);
+  }
+}
+
+/* DConvU, momentum.f:987-1009 */
+static void dconv_u(w2o_ctx *c, int nx, int ny, const double *c1,
+                    const double *c2, const double *u, double *cv) {
+  for (int j = 2; j <= ny; j++)
+    for (int i = 1; i <= nx; i++)
+      F(cv, i, j) = -F(c2, i, j - 1) * F(u, i, j - 1) - F(c1, i, j) * F(u, i - 1, j) +
+                    (F(c1, i + 1, j) - F(c1, i, j) + F(c2, i, j) - F(c2, i, j - 1)) *
+                        F(u, i, j) +
+                    F(c1, i + 1, j) * F(u, i + 1, j) + F(c2, i, j) * F(u, i, j + 1);
+}
+
+/* DDiffU, momentum.f:1015-1045 */
+static void ddiff_u(w2o_ctx *c, int nx, int ny, const double *ac,
+                    const double *bc, const double *bn, const double *gn,
+                    const double *u, double *d) {
+  double s1, s2;
+  for (int j = 2; j <= ny; j++)
+    for (int i = 1; i <= nx; i++) {
+      s1 = F(ac, i + 1, j) * (F(u, i + 1, j) - F(u, i, j)) -
+           F(ac, i, j) * (F(u, i, j) - F(u, i - 1, j)) +
+           F(bc, i + 1, j) * (F(u, i + 1, j + 1) + F(u, i, j + 1) -
+                              F(u, i + 1, j - 1) - F(u, i, j - 1)) -
+           F(bc, i, j) * (F(u, i, j + 1) + F(u, i - 1, j + 1) - F(u, i, j - 1) -
+                          F(u, i - 1, j - 1));
+      s2 = F(bn, i, j) * (F(u, i + 1, j + 1) + F(u, i + 1, j) -
+                          F(u, i - 1, j + 1) - F(u, i - 1, j)) -
+           F(bn, i, j - 1) * (F(u, i + 1, j) + F(u, i + 1, j - 1) -
+                              F(u, i - 1, j) - F(u, i - 1, j - 1)) +
+           F(gn, i, j) * (F(u, i, j + 1) - F(u, i, j)) -
+           F(gn, i, j - 1) * (F(u, i, j) - F(u, i, j - 1));
+      F(d, i, j) = s1 + s2;
+    }
+}
+
+/* DConvV, momentum.f:1051-1073 */
+static void dconv_v(w2o_ctx *c, int nx, int ny, const double *c1,
+                    const double *c2, const double *v, double *cv) {
+  for (int j = 1; j <= ny; j++)
+    for (int i = 2; i <= nx; i++)
+      F(cv, i, j) = -F(c2, i, j) * F(v, i, j - 1) - F(c1, i - 1, j) * F(v, i - 1, j) +
+                    (F(c1, i, j) - F(c1, i - 1, j) + F(c2, i, j + 1) - F(c2, i, j)) *
+                        F(v, i, j) +
+                    F(c1, i, j) * F(v, i + 1, j) + F(c2, i, j + 1) * F(v, i, j + 1);
+}
+
+/* DDiffV, momentum.f:1079-1109 */
+static void ddiff_v(w2o_ctx *c, int nx, int ny, const double *an,
+                    const double *bc, const double *bn, const double *gc,
+                    const double *v, double *d) {
+  double s1, s2;
+  for (int j = 1; j <= ny; j++)
+    for (int i = 2; i <= nx; i++) {
+      s1 = F(an, i, j) * (F(v, i + 1, j) - F(v, i, j)) -
+           F(an, i - 1, j) * (F(v, i, j) - F(v, i - 1, j)) +
+           F(bn, i, j) * (F(v, i + 1, j + 1) + F(v, i, j + 1) -
+                          F(v, i + 1, j - 1) - F(v, i, j - 1)) -
+           F(bn, i - 1, j) * (F(v, i, j + 1) + F(v, i - 1, j + 1) -
+                              F(v, i, j - 1) - F(v, i - 1, j - 1));
+      s2 = F(bc, i, j + 1) * (F(v, i + 1, j + 1) + F(v, i + 1, j) -
+                              F(v, i - 1, j + 1) - F(v, i - 1, j)) -
+           F(bc, i, j) * (F(v, i + 1, j) + F(v, i + 1, j - 1) - F(v, i - 1, j) -
+                          F(v, i - 1, j - 1)) +
+           F(gc, i, j + 1) * (F(v, i, j + 1) - F(v, i, j)) -
+           F(gc, i, j) * (F(v, i, j) - F(v, i, j - 1));
+      F(d, i, j) = s1 + s2;
+    }
+}
+
+/* PorosCoef, momentum.f:1115-1226 */
+static void poros_coef(w2o_ctx *c, int nx, int ny, int ncomp, int njacob,
+                       const w2o_regions *r, const double *u, const double *v,
+                       double *cp) {
+  (void)nx; (void)ny;
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      if (RTYP(r, ireg, jreg) != RM_POROUS) {
+        for (int j = jS; j <= jN; j++)
+          for (int i = iW; i <= iE; i++) F(cp, i, j) = 0.0;
+        continue;
+      }
+      double porc1 = RPAR(dPRporc1, r, ireg, jreg);
+      double porc2 = RPAR(dPRporc2, r, ireg, jreg);
+      double unorm, unrm1, t;
+      if (ncomp == 1) {
+        for (int j = jS + 1; j <= jN; j++)
+          for (int i = iW; i <= iE; i++) {
+            /* the reference divides only the last v term by 4 */
+            t = F(v, i, j) + F(v, i + 1, j) + F(v, i, j - 1) + F(v, i + 1, j - 1) / 4.0;
+            unorm = sqrt(F(u, i, j) * F(u, i, j) + t * t);
+            unrm1 = 0.0;
+            if (unorm > 1.0e-8) unrm1 = (F(u, i, j) * F(u, i, j)) / unorm;
+            if (njacob == 1) unorm = unrm1 + unorm;
+            F(cp, i, j) = porc1 + porc2 * unorm;
+          }
+      } else if (ncomp == 2) {
+        for (int j = jS; j <= jN; j++)
+          for (int i = iW + 1; i <= iE; i++) {
+            t = (F(u, i - 1, j + 1) + F(u, i, j + 1) + F(u, i - 1, j) + F(u, i, j)) / 4.0;
+            unorm = sqrt(t * t + F(v, i, j) * F(v, i, j));
+            unrm1 = 0.0;
+            if (unorm > 1.0e-8) unrm1 = (F(v, i, j) * F(v, i, j)) / unorm;
+            if (njacob == 1) unorm = unrm1 + unorm;
+            F(cp, i, j) = porc1 + porc2 * unorm;
+          }
+      } else {
+        die("Error: Wrong ncomp flag passed to PorosCoef", ncomp, 0);
+      }
+    }
+}
+
+/* Porosity division of convective coefficients, momentum.f:296-324 (X) and
+ * 621-649 (Y). */
+static void poros_scale(w2o_ctx *c, const w2o_regions *r, w2o_mom_ws *w,
+                        int yflag) {
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      if (RTYP(r, ireg, jreg) != RM_POROUS) continue;
+      int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      double por = RPAR(dPRporos, r, ireg, jreg);
+      int j0 = yflag ? jS : jS + 1, i0 = yflag ? iW + 1 : iW;
+      for (int j = j0; j <= jN; j++)
+        for (int i = i0; i <= iE; i++) {
+          F(w->cj1, i, j) = F(w->cj1, i, j) / por;
+          F(w->cj2, i, j) = F(w->cj2, i, j) / por;
+          F(w->c1s, i, j) = F(w->c1s, i, j) / por;
+          F(w->c2s, i, j) = F(w->c2s, i, j) / por;
+          F(w->c1n, i, j) = F(w->c1n, i, j) / por;
+          F(w->c2n, i, j) = F(w->c2n, i, j) / por;
+        }
+    }
+}
+
+#define CA(k, ind) w->a[((k)-1) + 3 * (size_t)((ind)-1)]
+#define CB(ind) w->b[(ind)-1]
+
+static void set_identity_row(w2o_mom_ws *w, int ind) {
+  CA(1, ind) = 0.0; CA(2, ind) = 1.0; CA(3, ind) = 0.0; CB(ind) = 0.0;
+}
+
+/* XMomentum, momentum.f:199-514 */
+static void x_momentum(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                       double dk, double re, const w2o_metrics *m,
+                       const double *us, const double *vs, const double *un,
+                       const double *vn, double *dus) {
+  w2o_mom_ws *w = &c->wx;
+  int i, j, ind;
+  double re1 = 1.0 / re, dk2 = dk * 0.5, rkj;
+
+  conv_coef(c, nx, ny, 4, 1, m->xzu, m->xeu, m->yzu, m->yeu, us, vs, w->cj1, w->cj2);
+  conv_coef(c, nx, ny, 1, 0, m->xzn, m->xec, m->yzn, m->yec, us, vs, w->c1s, w->c2s);
+  conv_coef(c, nx, ny, 1, 0, m->xzn, m->xec, m->yzn, m->yec, un, vn, w->c1n, w->c2n);
+  poros_scale(c, r, w, 0);
+
+  dconv_u(c, nx, ny, w->c1s, w->c2s, us, w->cnvs);
+  dconv_u(c, nx, ny, w->c1n, w->c2n, un, w->cnvn);
+  ddiff_u(c, nx, ny, m->rac, m->rbc, m->rbn, m->rgn, us, w->difs);
+  ddiff_u(c, nx, ny, m->rac, m->rbc, m->rbn, m->rgn, un, w->difn);
+
+  poros_coef(c, nx, ny, 1, 1, r, us, vs, w->cpj);
+  poros_coef(c, nx, ny, 1, 0, r, us, vs, w->cps);
+  poros_coef(c, nx, ny, 1, 0, r, un, vn, w->cpn);
+
+  /* First split step, momentum.f:350-384 */
+  for (j = 2; j <= ny; j++)
+    for (i = 1; i <= nx; i++) {
+      ind = (j - 2) * nx + i;
+      rkj = dk2 * F(m->dju, i, j);
+      if (F(w->cj1, i, j) >= 0.0) {
+        CA(1, ind) = rkj * (-F(w->cj1, i - 1, j) - re1 * F(m->rac, i, j));
+        CA(2, ind) = 1.0 + rkj * (F(w->cj1, i, j) +
+                                  re1 * (F(m->rac, i + 1, j) + F(m->rac, i, j))) +
+                     dk2 * F(w->cpj, i, j);
+        CA(3, ind) = rkj * (-re1 * F(m->rac, i + 1, j));
+      } else {
+        CA(1, ind) = rkj * (-re1 * F(m->rac, i, j));
+        CA(2, ind) = 1.0 + rkj * (-F(w->cj1, i, j) +
+                                  re1 * (F(m->rac, i + 1, j) + F(m->rac, i, j))) +
+                     dk2 * F(w->cpj, i, j);
+        CA(3, ind) = rkj * (F(w->cj1, i + 1, j) - re1 * F(m->rac, i + 1, j));
+      }
+      CB(ind) = F(un, i, j) - F(us, i, j) +
+                rkj * (-F(w->cnvs, i, j) - F(w->cnvn, i, j)) +
+                rkj * re1 * (F(w->difs, i, j) + F(w->difn, i, j)) -
+                dk2 * (F(w->cps, i, j) * F(us, i, j) + F(w->cpn, i, j) * F(un, i, j));
+    }
+  w2o_alt_trid_lu(nx * (ny - 1), w->a, w->b);
+
+  /* Second split step, momentum.f:396-428 */
+  for (j = 2; j <= ny; j++)
+    for (i = 1; i <= nx; i++) {
+      ind = (j - 2) * nx + i;
+      rkj = dk2 * F(m->dju, i, j);
+      if (F(w->cj2, i, j) >= 0.0) {
+        CA(1, ind) = rkj * (-F(w->cj2, i, j - 1) - re1 * F(m->rgn, i, j - 1));
+        CA(2, ind) = 1.0 + rkj * (F(w->cj2, i, j) +
+                                  re1 * (F(m->rgn, i, j) + F(m->rgn, i, j - 1))) +
+                     dk2 * F(w->cpj, i, j);
+        CA(3, ind) = rkj * (-re1 * F(m->rgn, i, j));
+      } else {
+        CA(1, ind) = rkj * (-re1 * F(m->rgn, i, j - 1));
+        CA(2, ind) = 1.0 + rkj * (-F(w->cj2, i, j) +
+                                  re1 * (F(m->rgn, i, j) + F(m->rgn, i, j - 1))) +
+                     dk2 * F(w->cpj, i, j);
+        CA(3, ind) = rkj * (F(w->cj2, i, j + 1) - re1 * F(m->rgn, i, j));
+      }
+    }
+
+  /* Blockage and W/E boundary identity rows, momentum.f:434-496 */
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      if (RTYP(r, ireg, jreg) == RM_BLOCKG)
+        for (j = jS + 1; j <= jN; j++)
+          for (i = iW; i <= iE; i++) set_identity_row(w, (j - 2) * nx + i);
+      switch (MBTP(r, ireg, jreg, WEST)) {
+        case BM_INTERN: case BM_OUTLT1: case BM_OUTLT2: break;
+        case BM_WALL1: case BM_WALL2: case BM_INLET:
+          for (j = jS + 1; j <= jN; j++) set_identity_row(w, (j - 2) * nx + iW);
+          break;
+        default: die("Wrong nBdTypeW flag", ireg, jreg);
+      }
+      switch (MBTP(r, ireg, jreg, EAST)) {
+        case BM_INTERN: case BM_OUTLT1: case BM_OUTLT2: break;
+        case BM_WALL1: case BM_WALL2: case BM_INLET:
+          for (j = jS + 1; j <= jN; j++) set_identity_row(w, (j - 2) * nx + iE);
+          break;
+        default: die("Wrong nBdTypeE flag", ireg, jreg);
+      }
+    }
+  w2o_alt_trid_lu(nx * (ny - 1), w->a, w->b);
+
+  for (j = 2; j <= ny; j++)
+    for (i = 1; i <= nx; i++) F(dus, i, j) = CB((j - 2) * nx + i);
+}
+
+/* YMomentum, momentum.f:520-838 */
+static void y_momentum(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                       double dk, double re, double fr, const w2o_metrics *m,
+                       const double *d, const double *dn, const double *us,
+                       const double *vs, const double *un, const double *vn,
+                       double *dvs) {
+  w2o_mom_ws *w = &c->wy;
+  int i, j, ind;
+  double re1 = 1.0 / re, dk2 = dk * 0.5, fr1 = 1.0 / fr, rkj, buoy;
+  (void)fr1;
+
+  conv_coef(c, nx, ny, 5, 1, m->xzv, m->xev, m->yzv, m->yev, us, vs, w->cj1, w->cj2);
+  conv_coef(c, nx, ny, 2, 0, m->xzc, m->xen, m->yzc, m->yen, us, vs, w->c1s, w->c2s);
+  conv_coef(c, nx, ny, 2, 0, m->xzc, m->xen, m->yzc, m->yen, un, vn, w->c1n, w->c2n);
+  poros_scale(c, r, w, 1);
+
+  dconv_v(c, nx, ny, w->c1s, w->c2s, vs, w->cnvs);
+  dconv_v(c, nx, ny, w->c1n, w->c2n, vn, w->cnvn);
+  ddiff_v(c, nx, ny, m->ran, m->rbc, m->rbn, m->rgc, vs, w->difs);
+  ddiff_v(c, nx, ny, m->ran, m->rbc, m->rbn, m->rgc, vn, w->difn);
+
+  poros_coef(c, nx, ny, 2, 1, r, us, vs, w->cpj);
+  poros_coef(c, nx, ny, 2, 0, r, us, vs, w->cps);
+  poros_coef(c, nx, ny, 2, 0, r, un, vn, w->cpn);
+
+  /* First split step, momentum.f:675-711 */
+  for (j = 1; j <= ny; j++)
+    for (i = 2; i <= nx; i++) {
+      ind = (j - 1) * (nx - 1) + i - 1;
+      rkj = dk2 * F(m->djv, i, j);
+      if (F(w->cj1, i, j) >= 0.0) {
+        CA(1, ind) = rkj * (-F(w->cj1, i - 1, j) - re1 * F(m->ran, i - 1, j));
+        CA(2, ind) = rkj * (F(w->cj1, i, j) +
+                            re1 * (F(m->ran, i, j) + F(m->ran, i - 1, j))) +
+                     dk2 * F(w->cpj, i, j) + 1.0;
+        CA(3, ind) = rkj * (-re1 * F(m->ran, i, j));
+      } else {
+        CA(1, ind) = rkj * (-re1 * F(m->ran, i - 1, j));
+        CA(2, ind) = rkj * (-F(w->cj1, i, j) +
+                            re1 * (F(m->ran, i, j) + F(m->ran, i - 1, j))) +
+                     dk2 * F(w->cpj, i, j) + 1.0;
+        CA(3, ind) = rkj * (F(w->cj1, i + 1, j) - re1 * F(m->ran, i, j));
+      }
+      buoy = dk * (F(d, i, j + 1) + F(d, i, j) + F(dn, i, j + 1) + F(dn, i, j)) /
+             (4.0 * fr);
+      CB(ind) = F(vn, i, j) - F(vs, i, j) +
+                rkj * (-F(w->cnvs, i, j) - F(w->cnvn, i, j)) +
+                rkj * re1 * (F(w->difs, i, j) + F(w->difn, i, j)) -
+                dk2 * (F(w->cps, i, j) * F(vs, i, j) + F(w->cpn, i, j) * F(vn, i, j)) -
+                buoy;
+    }
+  w2o_alt_trid_lu((nx - 1) * ny, w->a, w->b);
+
+  /* Second split step, momentum.f:723-754 */
+  for (j = 1; j <= ny; j++)
+    for (i = 2; i <= nx; i++) {
+      ind = (j - 1) * (nx - 1) + i - 1;
+      rkj = dk2 * F(m->djv, i, j);
+      if (F(w->cj2, i, j) >= 0.0) {
+        CA(1, ind) = rkj * (-F(w->cj2, i, j - 1) - re1 * F(m->rgc, i, j));
+        CA(2, ind) = rkj * (F(w->cj2, i, j) +
+                            re1 * (F(m->rgc, i, j + 1) + F(m->rgc, i, j))) +
+                     dk2 * F(w->cpj, i, j) + 1.0;
+        CA(3, ind) = rkj * (-re1 * F(m->rgc, i, j + 1));
+      } else {
+        CA(1, ind) = rkj * (-re1 * F(m->rgc, i, j));
+        CA(2, ind) = rkj * (-F(w->cj2, i, j) +
+                            re1 * (F(m->rgc, i, j + 1) + F(m->rgc, i, j))) +
+                     dk2 * F(w->cpj, i, j) + 1.0;
+        CA(3, ind) = rkj * (F(w->cj2, i, j + 1) - re1 * F(m->rgc, i, j + 1));
+      }
+    }
+
+  /* Blockage and S/N boundary identity rows, momentum.f:760-821 */
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      if (RTYP(r, ireg, jreg) == RM_BLOCKG)
+        for (j = jS; j <= jN; j++)
+          for (i = iW + 1; i <= iE; i++) set_identity_row(w, (j - 1) * (nx - 1) + i - 1);
+      switch (MBTP(r, ireg, jreg, SOUTH)) {
+        case BM_INTERN: case BM_OUTLT1: case BM_OUTLT2: break;
+        case BM_WALL1: case BM_WALL2: case BM_INLET:
+          for (i = iW + 1; i <= iE; i++) set_identity_row(w, (jS - 1) * (nx - 1) + i - 1);
+          break;
+        default: die("Wrong nBdTypeS flag", ireg, jreg);
+      }
+      switch (MBTP(r, ireg, jreg, NORTH)) {
+        case BM_INTERN: case BM_OUTLT1: case BM_OUTLT2: break;
+        case BM_WALL1: case BM_WALL2: case BM_INLET:
+          for (i = iW + 1; i <= iE; i++) set_identity_row(w, (jN - 1) * (nx - 1) + i - 1);
+          break;
+        default: die("Wrong nBdTypeN flag", ireg, jreg);
+      }
+    }
+  w2o_alt_trid_lu((nx - 1) * ny, w->a, w->b);
+
+  for (j = 1; j <= ny; j++)
+    for (i = 2; i <= nx; i++) F(dvs, i, j) = CB((j - 1) * (nx - 1) + i - 1);
+}
+#undef CA
+#undef CB
+
+/* DMaxNorm, utility.f:479-507 */
+double w2o_dmax_norm(w2o_ctx *c, int nx, int ny, const double *u) {
+  double diff = fabs(F(u, 5, 5));
+  for (int j = 2; j <= ny - 1; j++)
+    for (int i = 2; i <= nx - 1; i++) {
+      double a = fabs(F(u, i, j));
+      if (a > diff) diff = a;
+    }
+  return diff;
+}
+
+/* DiffMaxNorm, utility.f:446-473 */
+double w2o_diff_max_norm(w2o_ctx *c, int nx, int ny, const double *un,
+                         const double *u) {
+  double diff = fabs(F(un, 2, 2) - F(u, 2, 2));
+  for (int j = 2; j <= ny - 1; j++)
+    for (int i = 2; i <= nx - 1; i++) {
+      double a = fabs(F(un, i, j) - F(u, i, j));
+      if (a > diff) diff = a;
+    }
+  return diff;
+}
+
+/* nAuxMomentum, momentum.f:33-193 */
+int w2o_naux_momentum(w2o_ctx *c, int nx, int ny, int mqiter,
+                      const w2o_regions *r, double dk, double re, double fr,
+                      double qtol, const w2o_metrics *m, const double *d,
+                      const double *dn, const double *un, const double *vn,
+                      double *us, double *vs) {
+  int i, j, mm;
+  for (j = 1; j <= ny + 1; j++)
+    for (i = 1; i <= nx + 1; i++) {
+      F(us, i, j) = F(un, i, j);
+      F(vs, i, j) = F(vn, i, j);
+    }
+  for (mm = 1; mm <= mqiter; mm++) {
+    w2o_vel_outflow_bcs(c, nx, ny, r, us, vs);
+    for (j = 0; j <= ny + 1; j++)
+      for (i = 0; i <= nx + 1; i++) {
+        F(c->dus, i, j) = 0.0;
+        F(c->dvs, i, j) = 0.0;
+      }
+    x_momentum(c, nx, ny, r, dk, re, m, us, vs, un, vn, c->dus);
+    y_momentum(c, nx, ny, r, dk, re, fr, m, d, dn, us, vs, un, vn, c->dvs);
+    for (j = 1; j <= ny; j++)
+      for (i = 1; i <= nx; i++) {
+        F(us, i, j) = F(us, i, j) + F(c->dus, i, j);
+        F(vs, i, j) = F(vs, i, j) + F(c->dvs, i, j);
+      }
+    double d1 = w2o_dmax_norm(c, nx, ny, c->dus);
+    double d2 = w2o_dmax_norm(c, nx, ny, c->dvs);
+    double difmax = d1 > d2 ? d1 : d2;
+    if (difmax <= qtol) return mm;
+  }
+  return -1;
+}
+
+/* ------------------------------------------------------------------ */
+/* pressure.f                                                          */
+/* ------------------------------------------------------------------ */
+
+#define PA(ind, k) c->pa[((ind)-1) + (size_t)((k)-1) * c->mn]
+#define PB(ind) c->pb[(ind)-1]
+
+/* Divergence nloc=1, pressure.f:265-300 */
+static void divergence1(w2o_ctx *c, int nx, int ny, const double *xet,
+                        const double *yet, const double *xzi,
+                        const double *yzi, const double *u, const double *v,
+                        double *div) {
+  double ucij, uci1j, vcij, vcij1;
+  for (int j = 1; j <= ny; j++)
+    for (int i = 1; i <= nx; i++) {
+      ucij = F(yet, i, j) * F(u, i, j) -
+             F(xet, i, j) * (F(v, i + 1, j) + F(v, i, j) + F(v, i + 1, j - 1) +
+                             F(v, i, j - 1)) / 4.0;
+      uci1j = F(yet, i - 1, j) * F(u, i - 1, j) -
+              F(xet, i - 1, j) * (F(v, i, j) + F(v, i - 1, j) + F(v, i, j - 1) +
+                                  F(v, i - 1, j - 1)) / 4.0;
+      vcij = F(xzi, i, j) * F(v, i, j) -
+             F(yzi, i, j) * (F(u, i, j + 1) + F(u, i - 1, j + 1) + F(u, i, j) +
+                             F(u, i - 1, j)) / 4.0;
+      vcij1 = F(xzi, i, j - 1) * F(v, i, j - 1) -
+              F(yzi, i, j - 1) * (F(u, i, j) + F(u, i - 1, j) + F(u, i, j - 1) +
+                                  F(u, i - 1, j - 1)) / 4.0;
+      F(div, i, j) = ucij - uci1j + vcij - vcij1;
+    }
+}
+
+/* RhsPpe, pressure.f:329-378 */
+static void rhs_ppe(w2o_ctx *c, int nx, int ny, int lcartes, double dk,
+                    const w2o_metrics *m, const double *div, const double *p) {
+  int i, j, ind;
+  for (j = 2; j <= ny; j++)
+    for (i = 2; i <= nx; i++) {
+      ind = (j - 2) * (nx - 1) + i - 1;
+      PB(ind) = F(div, i, j) / dk;
+    }
+  if (!lcartes) {
+    const double *rbu = m->rbu, *rbv = m->rbv;
+    for (j = 2; j <= ny; j++)
+      for (i = 2; i <= nx; i++) {
+        ind = (j - 2) * (nx - 1) + i - 1;
+        PB(ind) = PB(ind) -
+                  (F(rbu, i, j) * (F(p, i + 1, j + 1) + F(p, i, j + 1) -
+                                   F(p, i + 1, j - 1) - F(p, i, j - 1)) -
+                   F(rbu, i - 1, j) * (F(p, i, j + 1) + F(p, i - 1, j + 1) -
+                                       F(p, i, j - 1) - F(p, i - 1, j - 1)) +
+                   F(rbv, i, j) * (F(p, i + 1, j + 1) + F(p, i + 1, j) -
+                                   F(p, i - 1, j + 1) - F(p, i - 1, j)) -
+                   F(rbv, i, j - 1) * (F(p, i + 1, j) + F(p, i + 1, j - 1) -
+                                       F(p, i - 1, j) - F(p, i - 1, j - 1)));
+      }
+  }
+}
+
+/* One point update shared by Sor/SorRB/SorRBP (pressure.f:434-439);
+ * returns |delta| and updates p in place. */
+static inline double sor_point(w2o_ctx *c, int nx, double *p, int i, int j,
+                               double sorrel) {
+  int ind = (j - 2) * (nx - 1) + i - 1;
+  double sum = PB(ind) - PA(ind, 1) * F(p, i, j - 1) - PA(ind, 2) * F(p, i - 1, j) -
+               PA(ind, 4) * F(p, i + 1, j) - PA(ind, 5) * F(p, i, j + 1);
+  sum = sum / PA(ind, 3) - F(p, i, j);
+  F(p, i, j) = F(p, i, j) + sorrel * sum;
+  return fabs(sum);
+}
+
+/* Sor, pressure.f:384-450 */
+static int sor(w2o_ctx *c, int nx, int ny, int lcartes, int msorit, double dk,
+               double sortol, double sorrel, const w2o_metrics *m,
+               const double *div, double *p) {
+  if (lcartes) rhs_ppe(c, nx, ny, lcartes, dk, m, div, p);
+  for (int it = 1; it <= msorit; it++) {
+    if (!lcartes) rhs_ppe(c, nx, ny, lcartes, dk, m, div, p);
+    double dif = 0.0;
+    for (int j = 2; j <= ny; j++)
+      for (int i = 2; i <= nx; i++) {
+        double s = sor_point(c, nx, p, i, j, sorrel);
+        dif = (s > dif) ? s : dif;
+      }
+    if (it > 1 && dif < sortol) return it;
+  }
+  return 0;
+}
+
+/* SorRB, pressure.f:457-541 */
+static int sor_rb(w2o_ctx *c, int nx, int ny, int lcartes, int msorit,
+                  double dk, double sortol, double sorrel,
+                  const w2o_metrics *m, const double *div, double *p) {
+  if (lcartes) rhs_ppe(c, nx, ny, lcartes, dk, m, div, p);
+  for (int it = 1; it <= msorit; it++) {
+    if (!lcartes) rhs_ppe(c, nx, ny, lcartes, dk, m, div, p);
+    double dif = 0.0;
+    for (int j = 2; j <= ny; j++)
+      for (int i = 2 + j % 2; i <= nx; i += 2) {
+        double s = sor_point(c, nx, p, i, j, sorrel);
+        dif = (s > dif) ? s : dif;
+      }
+    for (int j = 2; j <= ny; j++)
+      for (int i = 2 + (j + 1) % 2; i <= nx; i += 2) {
+        double s = sor_point(c, nx, p, i, j, sorrel);
+        dif = (s > dif) ? s : dif;
+      }
+    if (it > 1 && dif < sortol) return it;
+  }
+  return 0;
+}
+
+/* SorRBP, pressure.f:548-656 (per-point dif array, then its max) */
+static int sor_rbp(w2o_ctx *c, int nx, int ny, int lcartes, int msorit,
+                   double dk, double sortol, double sorrel,
+                   const w2o_metrics *m, const double *div, double *p) {
+  double *dif = c->rbp_dif;
+  if (lcartes) rhs_ppe(c, nx, ny, lcartes, dk, m, div, p);
+  for (int it = 1; it <= msorit; it++) {
+    if (!lcartes) rhs_ppe(c, nx, ny, lcartes, dk, m, div, p);
+    for (int j = 1; j <= ny; j++)
+      for (int i = 1; i <= nx; i++) F(dif, i, j) = 0.0;
+    for (int j = 2; j <= ny; j++)
+      for (int i = 2 + j % 2; i <= nx; i += 2) {
+        double s = sor_point(c, nx, p, i, j, sorrel);
+        F(dif, i, j) = (s > F(dif, i, j)) ? s : F(dif, i, j);
+      }
+    for (int j = 2; j <= ny; j++)
+      for (int i = 2 + (j + 1) % 2; i <= nx; i += 2) {
+        double s = sor_point(c, nx, p, i, j, sorrel);
+        F(dif, i, j) = (s > F(dif, i, j)) ? s : F(dif, i, j);
+      }
+    double difmax = 0.0;
+    for (int j = 2; j <= ny; j++)
+      for (int i = 2; i <= nx; i++)
+        difmax = (F(dif, i, j) > difmax) ? F(dif, i, j) : difmax;
+    if (it > 1 && difmax < sortol) return it;
+  }
+  return 0;
+}
+
+/* Line solve of line nl (j = nl) along i, shared by Slor / SlorRB with
+ * ndir = 1 (pressure.f:750-790, 905-945).  Returns the line's max |delta|. */
+static double slor_line(w2o_ctx *c, int nx, double *p, int nl, double sorrel) {
+  int ncomps = nx - 1;
+  size_t mnl = (size_t)(c->mnx > c->mny ? c->mnx : c->mny);
+  double *aline = c->lin, *bline = c->lin + 3 * mnl, *plold = c->lin + 4 * mnl;
+  double dif = 0.0;
+  for (int nc = 2; nc <= ncomps + 1; nc++) {
+    int ind = (nl - 2) * ncomps + nc - 1;
+    plold[nc - 2] = F(p, nc, nl);
+    double plprev = F(p, nc, nl - 1), plnext = F(p, nc, nl + 1);
+    aline[0 + 3 * (nc - 2)] = PA(ind, 2);
+    aline[1 + 3 * (nc - 2)] = PA(ind, 3);
+    aline[2 + 3 * (nc - 2)] = PA(ind, 4);
+    bline[nc - 2] = PB(ind) - (PA(ind, 1) * plprev + PA(ind, 5) * plnext);
+  }
+  w2o_alt_trid_lu(ncomps, aline, bline);
+  for (int nc = 1; nc <= ncomps; nc++) {
+    double sum = bline[nc - 1] - plold[nc - 1];
+    bline[nc - 1] = plold[nc - 1] + sorrel * sum;
+    sum = fabs(sum);
+    dif = (sum > dif) ? sum : dif;
+  }
+  for (int nc = 2; nc <= ncomps + 1; nc++) F(p, nc, nl) = bline[nc - 2];
+  return dif;
+}
+
+/* Slor with ndir = 1, pressure.f:673-802 */
+static int slor(w2o_ctx *c, int nx, int ny, int lcartes, int msorit,
+                double dk, double sortol, double sorrel, const w2o_metrics *m,
+                const double *div, double *p) {
+  int nlines = ny - 1;
+  if (lcartes) rhs_ppe(c, nx, ny, lcartes, dk, m, div, p);
+  for (int it = 1; it <= msorit; it++) {
+    double dif = 0.0;
+    if (!lcartes) rhs_ppe(c, nx, ny, lcartes, dk, m, div, p);
+    for (int nl = 2; nl <= nlines + 1; nl++) {
+      double s = slor_line(c, nx, p, nl, sorrel);
+      dif = (s > dif) ? s : dif;
+    }
+    if (it > 1 && dif < sortol) return it;
+  }
+  return 0;
+}
+
+/* SlorRB with ndir = 1, pressure.f:819-959 */
+static int slor_rb(w2o_ctx *c, int nx, int ny, int lcartes, int msorit,
+                   double dk, double sortol, double sorrel,
+                   const w2o_metrics *m, const double *div, double *p) {
+  int nlines = ny - 1;
+  if (lcartes) rhs_ppe(c, nx, ny, lcartes, dk, m, div, p);
+  for (int it = 1; it <= msorit; it++) {
+    double dif = 0.0;
+    for (int k = 2; k <= 3; k++) {
+      if (!lcartes) rhs_ppe(c, nx, ny, lcartes, dk, m, div, p);
+      for (int nl = k; nl <= nlines + 1; nl += 2) {
+        double s = slor_line(c, nx, p, nl, sorrel);
+        dif = (s > dif) ? s : dif;
+      }
+    }
+    if (it > 1 && dif < sortol) return it;
+  }
+  return 0;
+}
+
+/* SlorRBP, pressure.f:976-1138 */
+static int slor_rbp(w2o_ctx *c, int nx, int ny, int lcartes, int msorit,
+                    double dk, double sortol, double sorrel,
+                    const w2o_metrics *m, const double *div, double *p) {
+  int nlines = ny - 1, ncomps = nx - 1;
+  size_t mnl = (size_t)(c->mnx > c->mny ? c->mnx : c->mny);
+  double *aline = c->lin, *bline = c->lin + 3 * mnl;
+  double *pn = c->rbp_pn;
+  if (lcartes) rhs_ppe(c, nx, ny, lcartes, dk, m, div, p);
+  for (int it = 1; it <= msorit; it++) {
+    for (int nl = 1; nl <= nlines + 2; nl++)
+      for (int nc = 1; nc <= ncomps + 2; nc++) F(pn, nc, nl) = F(p, nc, nl);
+    for (int color = 2; color <= 3; color++) {
+      if (!lcartes) rhs_ppe(c, nx, ny, lcartes, dk, m, div, p);
+      for (int nl = color; nl <= nlines + 1; nl += 2) {
+        for (int nc = 2; nc <= ncomps + 1; nc++) {
+          int ind = (nl - 2) * ncomps + nc - 1;
+          aline[0 + 3 * (nc - 2)] = PA(ind, 2);
+          aline[1 + 3 * (nc - 2)] = PA(ind, 3);
+          aline[2 + 3 * (nc - 2)] = PA(ind, 4);
+          bline[nc - 2] = PB(ind) - (PA(ind, 1) * F(p, nc, nl - 1) +
+                                     PA(ind, 5) * F(p, nc, nl + 1));
+        }
+        w2o_alt_trid_lu(ncomps, aline, bline);
+        for (int nc = 2; nc <= ncomps + 1; nc++) F(p, nc, nl) = bline[nc - 2];
+      }
+      for (int nl = color; nl <= nlines + 1; nl += 2)
+        for (int nc = 2; nc <= ncomps + 1; nc++)
+          F(p, nc, nl) = F(pn, nc, nl) + sorrel * (F(p, nc, nl) - F(pn, nc, nl));
+    }
+    double dif = 0.0;
+    for (int nl = 2; nl <= nlines + 1; nl++)
+      for (int nc = 2; nc <= ncomps + 1; nc++) {
+        double s = fabs(F(pn, nc, nl) - F(p, nc, nl));
+        dif = (s > dif) ? s : dif;
+      }
+    if (it > 1 && dif < sortol) return it;
+  }
+  return 0;
+}
+
+static void ppe_identity(w2o_ctx *c, int ind) {
+  PA(ind, 1) = 0.0; PA(ind, 2) = 0.0; PA(ind, 3) = 1.0;
+  PA(ind, 4) = 0.0; PA(ind, 5) = 0.0;
+}
+
+/* Ppe, pressure.f:30-249 */
+int w2o_ppe(w2o_ctx *c, int nx, int ny, const w2o_regions *r, int lcartes,
+            int npsolver, int msorit, double dk, double sortol, double sorrel,
+            const w2o_metrics *m, const double *u, const double *v, double *p) {
+  int i, j, ind;
+  double *div = c->div;
+  divergence1(c, nx, ny, m->xeu, m->yeu, m->xzv, m->yzv, u, v, div);
+  for (j = 2; j <= ny; j++)
+    for (i = 2; i <= nx; i++) {
+      ind = (j - 2) * (nx - 1) + i - 1;
+      PA(ind, 1) = F(m->rgv, i, j - 1);
+      PA(ind, 2) = F(m->rau, i - 1, j);
+      PA(ind, 3) = -F(m->rau, i, j) - F(m->rau, i - 1, j) - F(m->rgv, i, j) -
+                   F(m->rgv, i, j - 1);
+      PA(ind, 4) = F(m->rau, i, j);
+      PA(ind, 5) = F(m->rgv, i, j);
+    }
+  /* Blockage rows, pressure.f:109-196 */
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      if (RTYP(r, ireg, jreg) != RM_BLOCKG) continue;
+      int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      for (j = jS + 2; j <= jN - 1; j++)
+        for (i = iW + 2; i <= iE - 1; i++) {
+          ppe_identity(c, (j - 2) * (nx - 1) + i - 1);
+          F(div, i, j) = 0.0;
+        }
+      if (ireg > 1 && RTYP(r, ireg - 1, jreg) == RM_BLOCKG)
+        for (j = jS + 1; j <= jN; j++) {
+          ppe_identity(c, (j - 2) * (nx - 1) + iW);
+          F(div, iW + 1, j) = 0.0;
+        }
+      if (ireg < r->nReg[0] && RTYP(r, ireg + 1, jreg) == RM_BLOCKG)
+        for (j = jS + 1; j <= jN; j++) {
+          ppe_identity(c, (j - 2) * (nx - 1) + iE - 1);
+          F(div, iE, j) = 0.0;
+        }
+      if (jreg > 1 && RTYP(r, ireg, jreg - 1) == RM_BLOCKG)
+        for (i = iW + 1; i <= iE; i++) {
+          ppe_identity(c, (jS - 1) * (nx - 1) + i - 1);
+          F(div, i, jS + 1) = 0.0;
+        }
+      if (jreg < r->nReg[1] && RTYP(r, ireg, jreg + 1) == RM_BLOCKG)
+        for (i = iW + 1; i <= iE; i++) {
+          ppe_identity(c, (jN - 2) * (nx - 1) + i - 1);
+          F(div, i, jN) = 0.0;
+        }
+    }
+  int nconv = 0;
+  switch (npsolver) {
+    case 1: nconv = sor(c, nx, ny, lcartes, msorit, dk, sortol, sorrel, m, div, p); break;
+    case 2: nconv = slor(c, nx, ny, lcartes, msorit, dk, sortol, sorrel, m, div, p); break;
+    case 3: nconv = slor_rb(c, nx, ny, lcartes, msorit, dk, sortol, sorrel, m, div, p); break;
+    case 4: nconv = slor_rbp(c, nx, ny, lcartes, msorit, dk, sortol, sorrel, m, div, p); break;
+    case 5: nconv = sor_rb(c, nx, ny, lcartes, msorit, dk, sortol, sorrel, m, div, p); break;
+    case 6: nconv = sor_rbp(c, nx, ny, lcartes, msorit, dk, sortol, sorrel, m, div, p); break;
+    default: fprintf(stderr, "Wrong nPpeSolver flag passed to Ppe\n");
+  }
+  if (nconv < 1) nconv = msorit;
+  return nconv;
+}
+#undef PA
+#undef PB
+
+/* ------------------------------------------------------------------ */
+/* utility.f                                                           */
+/* ------------------------------------------------------------------ */
+
+/* Project, utility.f:253-440 */
+void w2o_project(w2o_ctx *c, int nx, int ny, const w2o_regions *r, double dk,
+                 const w2o_metrics *m, const double *p, double *u, double *v) {
+  (void)nx; (void)ny;
+  double pzi, pet, djk;
+  const double *dju = m->dju, *djv = m->djv, *yeu = m->yeu, *xzv = m->xzv,
+               *yzu = m->yzu, *xev = m->xev;
+#define UPD_U(i, j)                                                                  \
+  do {                                                                               \
+    pzi = F(p, (i) + 1, j) - F(p, i, j);                                             \
+    pet = (F(p, (i) + 1, (j) + 1) + F(p, i, (j) + 1) - F(p, (i) + 1, (j)-1) -        \
+           F(p, i, (j)-1)) / 4.0;                                                    \
+    djk = F(dju, i, j) * dk;                                                         \
+    F(u, i, j) = F(u, i, j) - djk * (F(yeu, i, j) * pzi - F(yzu, i, j) * pet);       \
+  } while (0)
+#define UPD_V(i, j)                                                                  \
+  do {                                                                               \
+    pzi = (F(p, (i) + 1, (j) + 1) + F(p, (i) + 1, j) - F(p, (i)-1, (j) + 1) -        \
+           F(p, (i)-1, j)) / 4.0;                                                    \
+    pet = F(p, i, (j) + 1) - F(p, i, j);                                             \
+    djk = F(djv, i, j) * dk;                                                         \
+    F(v, i, j) = F(v, i, j) - djk * (-F(xev, i, j) * pzi + F(xzv, i, j) * pet);      \
+  } while (0)
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      if (RTYP(r, ireg, jreg) == RM_BLOCKG) continue;
+      int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      for (int j = jS + 1; j <= jN; j++)
+        for (int i = iW + 1; i <= iE - 1; i++) UPD_U(i, j);
+      int t = MBTP(r, ireg, jreg, WEST);
+      if (t == BM_OUTLT1)
+        for (int j = jS + 1; j <= jN; j++) UPD_U(iW, j);
+      t = MBTP(r, ireg, jreg, EAST);
+      if (t == BM_INTERN || t == BM_OUTLT1)
+        for (int j = jS + 1; j <= jN; j++) UPD_U(iE, j);
+    }
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      if (RTYP(r, ireg, jreg) == RM_BLOCKG) continue;
+      int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      for (int j = jS + 1; j <= jN - 1; j++)
+        for (int i = iW + 1; i <= iE; i++) UPD_V(i, j);
+      int t = MBTP(r, ireg, jreg, SOUTH);
+      if (t == BM_OUTLT1)
+        for (int i = iW + 1; i <= iE; i++) UPD_V(i, jS);
+      t = MBTP(r, ireg, jreg, NORTH);
+      if (t == BM_INTERN || t == BM_OUTLT1)
+        for (int i = iW + 1; i <= iE; i++) UPD_V(i, jN);
+    }
+#undef UPD_U
+#undef UPD_V
+}
+
+/* Filter, utility.f:33-247 (velocity components only) */
+void w2o_filter(w2o_ctx *c, int nx, int ny, int ncomp, const w2o_regions *r,
+                double fp, double *qu) {
+  double *qh = c->qh;
+  for (int j = 0; j <= ny + 1; j++)
+    for (int i = 0; i <= nx + 1; i++) F(qh, i, j) = F(qu, i, j);
+#define FILT(i, j)                                                                 \
+  F(qh, i, j) = (F(qu, i, (j)-1) + F(qu, (i)-1, j) + F(qu, i, (j) + 1) +            \
+                 F(qu, (i) + 1, j) + fp * F(qu, i, j)) / (fp + 4.0)
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      if (RTYP(r, ireg, jreg) == RM_BLOCKG) continue;
+      int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      if (ncomp == VU) {
+        for (int j = jS + 1; j <= jN; j++)
+          for (int i = iW + 1; i <= iE - 1; i++) FILT(i, j);
+        if (MBTP(r, ireg, jreg, WEST) == BM_OUTLT1)
+          for (int j = jS + 1; j <= jN; j++) FILT(iW, j);
+        int t = MBTP(r, ireg, jreg, EAST);
+        if (t == BM_INTERN || t == BM_OUTLT1)
+          for (int j = jS + 1; j <= jN; j++) FILT(iE, j);
+      } else {
+        for (int j = jS + 1; j <= jN - 1; j++)
+          for (int i = iW + 1; i <= iE; i++) FILT(i, j);
+        if (MBTP(r, ireg, jreg, SOUTH) == BM_OUTLT1)
+          for (int i = iW + 1; i <= iE; i++) FILT(i, jS);
+        int t = MBTP(r, ireg, jreg, NORTH);
+        if (t == BM_INTERN || t == BM_OUTLT1)
+          for (int i = iW + 1; i <= iE; i++) FILT(i, jN);
+      }
+    }
+#undef FILT
+  for (int j = 0; j <= ny + 1; j++)
+    for (int i = 0; i <= nx + 1; i++) F(qu, i, j) = F(qh, i, j);
+}
+
+/* ------------------------------------------------------------------ */
+/* bound_cond.f                                                        */
+/* ------------------------------------------------------------------ */
+
+/* VelBoundCond, bound_cond.f:511-847 */
+void w2o_vel_bound_cond(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                        double *u, double *v) {
+  (void)nx; (void)ny;
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      int i, j;
+      switch (MBTP(r, ireg, jreg, WEST)) {
+        case BM_INTERN: break;
+        case BM_WALL1:
+          for (j = jS; j <= jN; j++) F(u, iW, j) = 0.0;
+          for (j = jS + 1; j <= jN; j++)
+            F(v, iW, j) = 2.0 * BCV(r, ireg, jreg, WEST, VV) - F(v, iW + 1, j);
+          break;
+        case BM_WALL2:
+          for (j = jS; j <= jN; j++) F(u, iW, j) = 0.0;
+          for (j = jS + 1; j <= jN; j++) F(v, iW, j) = F(v, iW + 1, j);
+          break;
+        case BM_INLET:
+          for (j = jS; j <= jN; j++) F(u, iW, j) = BCV(r, ireg, jreg, WEST, VU);
+          for (j = jS + 1; j <= jN; j++)
+            F(v, iW, j) = 2.0 * BCV(r, ireg, jreg, WEST, VV) - F(v, iW + 1, j);
+          break;
+        case BM_OUTLT1:
+          for (j = jS; j <= jN; j++) F(u, iW - 1, j) = BCV(r, ireg, jreg, WEST, VU) + F(u, iW, j);
+          for (j = jS + 1; j <= jN; j++) F(v, iW, j) = -F(v, iW + 1, j);
+          break;
+        case BM_OUTLT2:
+          for (j = jS + 1; j <= jN; j++)
+            F(u, iW, j) = F(u, iW + 1, j) + F(v, iW + 1, j) - F(v, iW + 1, j - 1);
+          for (j = jS + 1; j <= jN; j++)
+            F(v, iW, j) = -F(v, iW, j - 1) + 5.0 * (F(v, iW + 1, j) - F(v, iW + 1, j - 1)) +
+                          8.0 * (F(u, iW + 1, j) - F(u, iW, j));
+          break;
+        default: die("Wrong nBdTypeW flag", ireg, jreg);
+      }
+      switch (MBTP(r, ireg, jreg, EAST)) {
+        case BM_INTERN: break;
+        case BM_WALL1:
+          for (j = jS; j <= jN; j++) F(u, iE, j) = 0.0;
+          for (j = jS + 1; j <= jN; j++)
+            F(v, iE + 1, j) = 2.0 * BCV(r, ireg, jreg, EAST, VV) - F(v, iE, j);
+          break;
+        case BM_WALL2:
+          for (j = jS; j <= jN; j++) F(u, iE, j) = 0.0;
+          for (j = jS + 1; j <= jN; j++) F(v, iE + 1, j) = F(v, iE, j);
+          break;
+        case BM_INLET:
+          for (j = jS; j <= jN; j++) F(u, iE, j) = BCV(r, ireg, jreg, EAST, VU);
+          for (j = jS + 1; j <= jN; j++)
+            F(v, iE + 1, j) = 2.0 * BCV(r, ireg, jreg, EAST, VV) - F(v, iE, j);
+          break;
+        case BM_OUTLT1:
+          for (j = jS; j <= jN; j++) F(u, iE + 1, j) = BCV(r, ireg, jreg, EAST, VU) + F(u, iE, j);
+          for (j = jS + 1; j <= jN; j++) F(v, iE + 1, j) = -F(v, iE, j);
+          break;
+        case BM_OUTLT2:
+          for (j = jS + 1; j <= jN; j++)
+            F(u, iE, j) = F(u, iE - 1, j) - (F(v, iE, j) - F(v, iE, j - 1));
+          for (j = jS + 1; j <= jN - 1; j++)
+            F(v, iE + 1, j) = F(v, iE + 1, j - 1) + 3.0 * (F(v, iE, j - 1) - F(v, iE, j)) -
+                              4.0 * (F(u, iE, j) - F(u, iE - 1, j));
+          break;
+        default: die("Wrong nBdTypeE flag", ireg, jreg);
+      }
+      switch (MBTP(r, ireg, jreg, SOUTH)) {
+        case BM_INTERN: break;
+        case BM_WALL1:
+          for (i = iW + 1; i <= iE; i++)
+            F(u, i, jS) = 2.0 * BCV(r, ireg, jreg, SOUTH, VU) - F(u, i, jS + 1);
+          for (i = iW; i <= iE; i++) F(v, i, jS) = 0.0;
+          break;
+        case BM_WALL2:
+          for (i = iW + 1; i <= iE; i++) F(u, i, jS) = F(u, i, jS + 1);
+          for (i = iW; i <= iE; i++) F(v, i, jS) = 0.0;
+          break;
+        case BM_INLET:
+          for (i = iW + 1; i <= iE; i++)
+            F(u, i, jS) = 2.0 * BCV(r, ireg, jreg, SOUTH, VU) - F(u, i, jS + 1);
+          for (i = iW; i <= iE; i++) F(v, i, jS) = BCV(r, ireg, jreg, SOUTH, VV);
+          break;
+        case BM_OUTLT1:
+          for (i = iW + 1; i <= iE; i++) F(u, i, jS) = -F(u, i, jS + 1);
+          for (i = iW; i <= iE; i++) F(v, i, jS) = BCV(r, ireg, jreg, SOUTH, VV) + F(v, i, jS);
+          break;
+        case BM_OUTLT2:
+          for (i = iW + 1; i <= iE; i++)
+            F(v, i, jS) = F(v, i, jS + 1) + (F(u, i, jS + 1) - F(u, i - 1, jS + 1));
+          for (i = iW + 1; i <= iE - 1; i++)
+            F(u, i, jS) = F(u, i - 1, jS) + 3.0 * (F(u, i - 1, jS + 1) - F(u, i, jS + 1)) -
+                          4.0 * (F(v, i, jS + 1) - F(v, i, jS));
+          break;
+        default: die("Wrong nBdTypeS flag", ireg, jreg);
+      }
+      switch (MBTP(r, ireg, jreg, NORTH)) {
+        case BM_INTERN: break;
+        case BM_WALL1:
+          for (i = iW + 1; i <= iE; i++)
+            F(u, i, jN + 1) = 2.0 * BCV(r, ireg, jreg, NORTH, VU) - F(u, i, jN);
+          for (i = iW; i <= iE; i++) F(v, i, jN) = 0.0;
+          break;
+        case BM_WALL2:
+          for (i = iW + 1; i <= iE; i++) F(u, i, jN + 1) = F(u, i, jN);
+          for (i = iW; i <= iE; i++) F(v, i, jN) = 0.0;
+          break;
+        case BM_INLET:
+          for (i = iW + 1; i <= iE; i++)
+            F(u, i, jN + 1) = 2.0 * BCV(r, ireg, jreg, NORTH, VU) - F(u, i, jN);
+          for (i = iW; i <= iE; i++) F(v, i, jN) = BCV(r, ireg, jreg, NORTH, VV);
+          break;
+        case BM_OUTLT1:
+          for (i = iW + 1; i <= iE; i++) F(u, i, jN + 1) = -F(u, i, jN);
+          for (i = iW; i <= iE; i++) F(v, i, jN + 1) = BCV(r, ireg, jreg, NORTH, VV) + F(v, i, jN);
+          break;
+        case BM_OUTLT2:
+          for (i = iW; i <= iE; i++)
+            F(v, i, jN) = F(v, i, jN - 1) - (F(u, i, jN) - F(u, i - 1, jN));
+          for (i = iW + 1; i <= iE - 1; i++)
+            F(u, i, jN + 1) = F(u, i - 1, jN + 1) + 3.0 * (F(u, i - 1, jN) - F(u, i, jN)) -
+                              4.0 * (F(v, i, jN) - F(v, i, jN - 1));
+          break;
+        default: die("Wrong nBdTypeN flag", ireg, jreg);
+      }
+    }
+}
+
+/* PresBoundCond, bound_cond.f:853-1024 */
+void w2o_pres_bound_cond(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                         double *p) {
+  (void)nx; (void)ny;
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      int i, j, t;
+      if (RTYP(r, ireg, jreg) == RM_BLOCKG) {
+        for (j = jS + 1; j <= jN; j++)
+          for (i = iW + 1; i <= iE; i++) F(p, i, j) = 0.0;
+        for (j = jS + 1; j <= jN; j++) F(p, iW + 1, j) = BCV(r, ireg, jreg, WEST, VP) + F(p, iW, j);
+        for (j = jS + 1; j <= jN; j++) F(p, iE, j) = BCV(r, ireg, jreg, EAST, VP) + F(p, iE + 1, j);
+        for (i = iW + 1; i <= iE; i++) F(p, i, jS + 1) = BCV(r, ireg, jreg, SOUTH, VP) + F(p, i, jS);
+        for (i = iW + 1; i <= iE; i++) F(p, i, jN) = BCV(r, ireg, jreg, NORTH, VP) + F(p, i, jN + 1);
+        continue;
+      }
+      t = MBTP(r, ireg, jreg, WEST);
+      if (t == BM_WALL1 || t == BM_WALL2 || t == BM_INLET) {
+        for (j = jS + 1; j <= jN; j++) F(p, iW, j) = BCV(r, ireg, jreg, WEST, VP) + F(p, iW + 1, j);
+      } else if (t == BM_OUTLT1 || t == BM_OUTLT2) {
+        for (j = jS + 1; j <= jN; j++) F(p, iW, j) = 2.0 * BCV(r, ireg, jreg, WEST, VP) - F(p, iW + 1, j);
+      } else if (t != BM_INTERN) die("Wrong nBdTypeW flag", ireg, jreg);
+      t = MBTP(r, ireg, jreg, EAST);
+      if (t == BM_WALL1 || t == BM_WALL2 || t == BM_INLET) {
+        for (j = jS + 1; j <= jN; j++) F(p, iE + 1, j) = BCV(r, ireg, jreg, EAST, VP) + F(p, iE, j);
+      } else if (t == BM_OUTLT1 || t == BM_OUTLT2) {
+        for (j = jS + 1; j <= jN; j++) F(p, iE + 1, j) = 2.0 * BCV(r, ireg, jreg, EAST, VP) - F(p, iE, j);
+      } else if (t != BM_INTERN) die("Wrong nBdTypeE flag", ireg, jreg);
+      t = MBTP(r, ireg, jreg, SOUTH);
+      if (t == BM_WALL1 || t == BM_WALL2 || t == BM_INLET) {
+        for (i = iW + 1; i <= iE; i++) F(p, i, jS) = BCV(r, ireg, jreg, SOUTH, VP) + F(p, i, jS + 1);
+      } else if (t == BM_OUTLT1 || t == BM_OUTLT2) {
+        for (i = iW + 1; i <= iE; i++) F(p, i, jS) = 2.0 * BCV(r, ireg, jreg, SOUTH, VP) - F(p, i, jS + 1);
+      } else if (t != BM_INTERN) die("Wrong nBdTypeS flag", ireg, jreg);
+      t = MBTP(r, ireg, jreg, NORTH);
+      if (t == BM_WALL1 || t == BM_WALL2 || t == BM_INLET) {
+        for (i = iW + 1; i <= iE; i++) F(p, i, jN + 1) = BCV(r, ireg, jreg, NORTH, VP) + F(p, i, jN);
+      } else if (t == BM_OUTLT1 || t == BM_OUTLT2) {
+        for (i = iW + 1; i <= iE; i++) F(p, i, jN + 1) = 2.0 * BCV(r, ireg, jreg, NORTH, VP) - F(p, i, jN);
+      } else if (t != BM_INTERN) die("Wrong nBdTypeN flag", ireg, jreg);
+    }
+}
+
+/* VelOutflowBCs, bound_cond.f:1656-1874 */
+void w2o_vel_outflow_bcs(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                         double *u, double *v) {
+  (void)nx; (void)ny;
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      int i, j;
+      switch (MBTP(r, ireg, jreg, WEST)) {
+        case BM_INTERN: case BM_WALL1: case BM_WALL2: case BM_INLET: break;
+        case BM_OUTLT1:
+          for (j = jS; j <= jN; j++) F(u, iW - 1, j) = BCV(r, ireg, jreg, WEST, VU) + F(u, iW, j);
+          for (j = jS + 1; j <= jN; j++) F(v, iW, j) = -F(v, iW + 1, j);
+          break;
+        case BM_OUTLT2:
+          for (j = jS + 1; j <= jN; j++)
+            F(u, iW, j) = F(u, iW + 1, j) - F(v, iW + 1, j) + F(v, iW + 1, j - 1);
+          for (j = jS + 1; j <= jN; j++)
+            F(v, iW, j) = -F(v, iW, j - 1) + 5.0 * (F(v, iW + 1, j) - F(v, iW + 1, j - 1)) +
+                          8.0 * (F(u, iW + 1, j) - F(u, iW, j));
+          break;
+        default: die("Wrong nBdTypeW flag", ireg, jreg);
+      }
+      switch (MBTP(r, ireg, jreg, EAST)) {
+        case BM_INTERN: case BM_WALL1: case BM_WALL2: case BM_INLET: break;
+        case BM_OUTLT1:
+          for (j = jS; j <= jN; j++) F(u, iE + 1, j) = BCV(r, ireg, jreg, EAST, VU) + F(u, iE, j);
+          for (j = jS + 1; j <= jN; j++) F(v, iE + 1, j) = -F(v, iE, j);
+          break;
+        case BM_OUTLT2:
+          for (j = jS + 1; j <= jN; j++)
+            F(u, iE, j) = F(u, iE - 1, j) - (F(v, iE, j) - F(v, iE, j - 1));
+          for (j = jS + 1; j <= jN - 1; j++)
+            F(v, iE + 1, j) = F(v, iE + 1, j - 1) + 3.0 * (F(v, iE, j - 1) - F(v, iE, j)) -
+                              4.0 * (F(u, iE, j) - F(u, iE - 1, j));
+          break;
+        default: die("Wrong nBdTypeE flag", ireg, jreg);
+      }
+      switch (MBTP(r, ireg, jreg, SOUTH)) {
+        case BM_INTERN: case BM_WALL1: case BM_WALL2: case BM_INLET: break;
+        case BM_OUTLT1:
+          for (i = iW + 1; i <= iE; i++) F(u, i, jS) = -F(u, i, jS + 1);
+          for (i = iW; i <= iE; i++) F(v, i, jS) = BCV(r, ireg, jreg, SOUTH, VV) + F(v, i, jS);
+          break;
+        case BM_OUTLT2:
+          for (i = iW + 1; i <= iE; i++)
+            F(v, i, jS) = F(v, i, jS + 1) + (F(u, i, jS + 1) - F(u, i - 1, jS + 1));
+          for (i = iW + 1; i <= iE - 1; i++)
+            F(u, i, jS) = F(u, i - 1, jS) + 3.0 * (F(u, i - 1, jS + 1) - F(u, i, jS + 1)) -
+                          4.0 * (F(v, i, jS + 1) - F(v, i, jS));
+          break;
+        default: die("Wrong nBdTypeS flag", ireg, jreg);
+      }
+      switch (MBTP(r, ireg, jreg, NORTH)) {
+        case BM_INTERN: case BM_WALL1: case BM_WALL2: case BM_INLET: break;
+        case BM_OUTLT1:
+          for (i = iW + 1; i <= iE; i++) F(u, i, jN + 1) = -F(u, i, jN);
+          for (i = iW; i <= iE; i++) F(v, i, jN + 1) = BCV(r, ireg, jreg, NORTH, VV) + F(v, i, jN);
+          break;
+        case BM_OUTLT2:
+          for (i = iW; i <= iE; i++)
+            F(v, i, jN) = F(v, i, jN - 1) - (F(u, i, jN) - F(u, i - 1, jN));
+          for (i = iW + 1; i <= iE - 1; i++)
+            F(u, i, jN + 1) = F(u, i - 1, jN + 1) + 3.0 * (F(u, i - 1, jN) - F(u, i, jN)) -
+                              4.0 * (F(v, i, jN) - F(v, i, jN - 1));
+          break;
+        default: die("Wrong nBdTypeN flag", ireg, jreg);
+      }
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* main.f                                                              */
+/* ------------------------------------------------------------------ */
+
+/* Cold start, main.f:606-641 */
+int w2o_cold_start(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                   const w2o_params *prm, const w2o_metrics *m,
+                   w2o_fields *f) {
+  w2o_vel_bound_cond(c, nx, ny, r, f->u, f->v);
+  int nconv = w2o_ppe(c, nx, ny, r, prm->lcartes, prm->npsolver, prm->msorit,
+                      prm->dk, prm->sortol, prm->sorrel, m, f->u, f->v, f->p);
+  w2o_pres_bound_cond(c, nx, ny, r, f->p);
+  w2o_project(c, nx, ny, r, prm->dk, m, f->p, f->u, f->v);
+  w2o_vel_bound_cond(c, nx, ny, r, f->u, f->v);
+  return nconv;
+}
+
+/* One pass of the time loop, main.f:690-972 (nthermen = nsmallscl = 0, so the
+ * momentum/energy loop runs once, main.f:736). */
+int w2o_step(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+             const w2o_params *prm, const w2o_metrics *m, w2o_fields *f,
+             int *nQLiter, int *nSorConv, double dif[4]) {
+  int i, j;
+  for (j = 0; j <= ny + 1; j++)
+    for (i = 0; i <= nx + 1; i++) {
+      F(f->pn, i, j) = F(f->p, i, j);
+      F(f->un, i, j) = F(f->u, i, j);
+      F(f->vn, i, j) = F(f->v, i, j);
+      F(f->tn, i, j) = F(f->t, i, j);
+    }
+  for (j = 0; j <= ny + 1; j++)
+    for (i = 0; i <= nx + 1; i++) {
+      F(f->us, i, j) = F(f->u, i, j);
+      F(f->vs, i, j) = F(f->v, i, j);
+      F(f->ts, i, j) = F(f->t, i, j);
+    }
+  *nQLiter = w2o_naux_momentum(c, nx, ny, prm->mqiter, r, prm->dk, prm->re,
+                               prm->fr, prm->qtol, m, f->d, f->dn, f->un,
+                               f->vn, f->us, f->vs);
+  if (prm->nfiltu == 1) w2o_filter(c, nx, ny, VU, r, prm->fpu, f->us);
+  if (prm->nfiltv == 1) w2o_filter(c, nx, ny, VV, r, prm->fpv, f->vs);
+  w2o_vel_bound_cond(c, nx, ny, r, f->us, f->vs);
+  w2o_pres_bound_cond(c, nx, ny, r, f->p);
+  *nSorConv = w2o_ppe(c, nx, ny, r, prm->lcartes, prm->npsolver, prm->msorit,
+                      prm->dk, prm->sortol, prm->sorrel, m, f->us, f->vs, f->p);
+  w2o_pres_bound_cond(c, nx, ny, r, f->p);
+  w2o_project(c, nx, ny, r, prm->dk, m, f->p, f->us, f->vs);
+  w2o_vel_bound_cond(c, nx, ny, r, f->us, f->vs);
+  w2o_pres_bound_cond(c, nx, ny, r, f->p);
+  /* main.f:857-859 computes dif(1..3) here; with one momentum/energy pass
+   * they are overwritten below before any use. */
+  for (j = 0; j <= ny + 1; j++)
+    for (i = 0; i <= nx + 1; i++) {
+      F(f->u, i, j) = F(f->us, i, j);
+      F(f->v, i, j) = F(f->vs, i, j);
+      F(f->t, i, j) = F(f->ts, i, j);
+    }
+  w2o_vel_bound_cond(c, nx, ny, r, f->u, f->v);
+  w2o_pres_bound_cond(c, nx, ny, r, f->p);
+  dif[0] = w2o_diff_max_norm(c, nx, ny, f->pn, f->p);
+  dif[1] = w2o_diff_max_norm(c, nx, ny, f->un, f->u);
+  dif[2] = w2o_diff_max_norm(c, nx, ny, f->vn, f->v);
+  dif[3] = w2o_diff_max_norm(c, nx, ny, f->tn, f->t);
+  double difmax = dif[0];
+  for (int k = 1; k < 4; k++) difmax = dif[k] > difmax ? dif[k] : difmax;
+  return difmax > 1.0e12 ? 1 : 0;
+}

@@ -1,0 +1,132 @@
+/*
+ * wolfd2_oracle.h -- CPU oracle for the wolfd2 projection-method time step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * Fortran routines on the hot path (momentum.f, pressure.f, utility.f,
+ * bound_cond.f and the time-loop body of main.f).  It exists so the tests,
+ * the smoke check and the CPU-baseline leg of the benchmark can check the
+ * CUDA library against an independent implementation.  Nothing in the
+ * product (wolfd2_gb300/, include/) links or calls it.
+ *
+ * Parity pinning: the reference ships no tests, golden vectors or sample
+ * decks, and no Fortran compiler exists on the build or GPU machines, so the
+ * restatement cannot be checked against the compiled reference.  It is
+ * checked instead against a mechanical Fortran-77-to-C translation of the
+ * reference's own source files (oracle/f77c.py, output in oracle/_ref/, built
+ * only where the reference source tree is present) -- see the tests.  Where
+ * that translation is absent, parity is unpinned.
+ *
+ * Storage follows the reference: every field is REAL*8 (0:mnx,0:mny),
+ * column-major, element (i,j) at offset i + j*(mnx+1).  Region tables keep
+ * their Fortran shapes: nRegBrd(mgri,mgrj,4), nRegType(mgri,mgrj),
+ * nMomBdTp(mgri,mgrj,4), dBCVal(mgri,mgrj,4,4), porous coefficients
+ * (mgri,mgrj).  All work arrays live in an oracle context, zero-initialised
+ * once and persistent across calls, which reproduces the static storage the
+ * reference's large local arrays get from gfortran (some entries, e.g.
+ * cj1(nx+1,j), are read but never written and must stay zero).
+ *
+ * Build: cc -O2 -ffp-contract=off (op-by-op IEEE double, no FMA), see
+ * oracle/Makefile.
+ */
+#ifndef WOLFD2_ORACLE_H
+#define WOLFD2_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct w2o_ctx w2o_ctx;
+
+/* Region / boundary tables, Fortran layout (see include/wolfd2.h). */
+typedef struct {
+  int mgri, mgrj;          /* leading dimensions (20, 10 in config.f) */
+  const int *nReg;         /* nReg(2)                                  */
+  const int *nRegBrd;      /* nRegBrd(mgri,mgrj,4)                     */
+  const int *nRegType;     /* nRegType(mgri,mgrj)                      */
+  const int *nMomBdTp;     /* nMomBdTp(mgri,mgrj,4)                    */
+  const double *dBCVal;    /* dBCVal(mgri,mgrj,4,4)                    */
+  const double *dPRporos;  /* dPRporos(mgri,mgrj)                      */
+  const double *dPRporc1;
+  const double *dPRporc2;
+} w2o_regions;
+
+/* The 30 metric arrays produced by grid.f:Metric, each (0:mnx,0:mny). */
+typedef struct {
+  double *ran, *rbn, *rgn, *rac, *rbc, *rgc, *rau, *rbu, *rbv, *rgv;
+  double *dju, *djv, *djc, *djn;
+  double *xen, *yen, *xzn, *yzn, *xec, *yec, *xzc, *yzc;
+  double *xeu, *yeu, *xzv, *yzv, *xzu, *yzu, *xev, *yev;
+} w2o_metrics;
+
+w2o_ctx *w2o_create(int mnx, int mny);
+void w2o_destroy(w2o_ctx *c);
+
+/* grid.f:31-127 minus file reading: gx,gy hold nodes (1..nx,1..ny), already
+ * divided by dlref; mirror points are added in place. */
+void w2o_grid(w2o_ctx *c, int nx, int ny, double *gx, double *gy,
+              w2o_metrics *m);
+
+/* momentum.f:33-193 */
+int w2o_naux_momentum(w2o_ctx *c, int nx, int ny, int mqiter,
+                      const w2o_regions *r, double dk, double re, double fr,
+                      double qtol, const w2o_metrics *m, const double *d,
+                      const double *dn, const double *un, const double *vn,
+                      double *us, double *vs);
+
+/* pressure.f:30-249; returns nSorConv */
+int w2o_ppe(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+            int lcartes, int npsolver, int msorit, double dk, double sortol,
+            double sorrel, const w2o_metrics *m, const double *u,
+            const double *v, double *p);
+
+/* utility.f:253-440 */
+void w2o_project(w2o_ctx *c, int nx, int ny, const w2o_regions *r, double dk,
+                 const w2o_metrics *m, const double *p, double *u, double *v);
+
+/* bound_cond.f:511-847, 853-1024, 1656-1874 */
+void w2o_vel_bound_cond(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                        double *u, double *v);
+void w2o_pres_bound_cond(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                         double *p);
+void w2o_vel_outflow_bcs(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                         double *u, double *v);
+
+/* utility.f:33-247 (ncomp 1=u, 2=v) */
+void w2o_filter(w2o_ctx *c, int nx, int ny, int ncomp, const w2o_regions *r,
+                double fp, double *q);
+
+/* utility.f:446-507 */
+double w2o_diff_max_norm(w2o_ctx *c, int nx, int ny, const double *un,
+                         const double *u);
+double w2o_dmax_norm(w2o_ctx *c, int nx, int ny, const double *u);
+
+/* momentum.f:1307-1339 (exported for unit tests) */
+void w2o_alt_trid_lu(int n, double *a /* a(3,n) */, double *b);
+
+/* Time-loop parameters (main.f with nthermen = nsmallscl = 0). */
+typedef struct {
+  double dk, re, fr, qtol, sortol, sorrel, fpu, fpv;
+  int mqiter, npsolver, msorit, nfiltu, nfiltv, lcartes;
+} w2o_params;
+
+/* Fields of the time loop, each (0:mnx,0:mny). */
+typedef struct {
+  double *u, *v, *p, *t, *un, *vn, *pn, *tn, *us, *vs, *ts, *d, *dn;
+} w2o_fields;
+
+/* main.f:606-641 (cold-start projection) */
+int w2o_cold_start(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                   const w2o_params *prm, const w2o_metrics *m,
+                   w2o_fields *f);
+
+/* main.f:690-972 for one step; returns 0, or 1 when 'Solution diverged'. */
+int w2o_step(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+             const w2o_params *prm, const w2o_metrics *m, w2o_fields *f,
+             int *nQLiter, int *nSorConv, double dif[4]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

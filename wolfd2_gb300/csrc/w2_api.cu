@@ -1,0 +1,778 @@
+// w2_api.cu -- host side of the wolfd2 GB300 library: context, device memory,
+// region masks, launches, and the C-ABI declared in include/wolfd2_gpu.h.
+//
+// Compiled for sm_103a with -fmad=false: the FP64 kernels evaluate every
+// reference expression operation by operation, so their results are the
+// IEEE-double results of the reference source as written.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "w2_kernels.cuh"
+
+using namespace w2;
+
+struct w2_ctx {
+  int mnx = 0, mny = 0, mgri = 0, mgrj = 0, nx = 0, ny = 0, ld = 0;
+  int device = 0, nsm = 0;
+  cudaStream_t st = nullptr;
+  size_t nf = 0;  // device field length (elements)
+  std::vector<void *> allocs;
+  Dev dev{};
+  double *met[W2_NMETRIC] = {};
+  double *U[2] = {}, *V[2] = {}, *P[2] = {};
+  int cur = 0;
+  double *stage[6] = {};  // drop-in staging: a, b, c, d, e, f
+  StepOut *d_out = nullptr;
+  StepOut *h_out = nullptr;  // pinned
+  int threads = 256, blocks_per_sm = 2, seg_req = 0, warm_req = 0;
+  bool metrics_ok = false, porous = false;
+  long long launches = 0;
+  char err[512] = {0};
+  std::vector<int> tab_brd, tab_rtype, tab_btype;
+  std::vector<double> tab_bcv;
+  int nri = 0, nrj = 0;
+};
+
+namespace {
+
+int fail(w2_ctx *c, int code, const char *fmt, ...) {
+  if (c) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(c->err, sizeof(c->err), fmt, ap);
+    va_end(ap);
+  }
+  return code;
+}
+
+#define CK(call)                                                                   \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess)                                                         \
+      return fail(c, W2_E_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));   \
+  } while (0)
+
+template <class T>
+T *dalloc(w2_ctx *c, size_t n) {
+  void *p = nullptr;
+  if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return nullptr;
+  cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(T));
+  c->allocs.push_back(p);
+  return (T *)p;
+}
+
+// Metric order of the C-ABI (grid.f:Grid argument order).
+enum {
+  M_RAU, M_RBU, M_RBV, M_RGV, M_RAN, M_RBN, M_RGN, M_RAC, M_RBC, M_RGC, M_DJU, M_DJV, M_DJC,
+  M_DJN, M_XEN, M_YEN, M_XZN, M_YZN, M_XEC, M_YEC, M_XZC, M_YZC, M_XEU, M_YEU, M_XZV, M_YZV,
+  M_XZU, M_YZU, M_XEV, M_YEV
+};
+
+void bind_metrics(w2_ctx *c) {
+  Metrics &m = c->dev.m;
+  double **a = c->met;
+  m.rau = a[M_RAU]; m.rbu = a[M_RBU]; m.rbv = a[M_RBV]; m.rgv = a[M_RGV];
+  m.ran = a[M_RAN]; m.rbn = a[M_RBN]; m.rgn = a[M_RGN];
+  m.rac = a[M_RAC]; m.rbc = a[M_RBC]; m.rgc = a[M_RGC];
+  m.dju = a[M_DJU]; m.djv = a[M_DJV]; m.djc = a[M_DJC]; m.djn = a[M_DJN];
+  m.xen = a[M_XEN]; m.yen = a[M_YEN]; m.xzn = a[M_XZN]; m.yzn = a[M_YZN];
+  m.xec = a[M_XEC]; m.yec = a[M_YEC]; m.xzc = a[M_XZC]; m.yzc = a[M_YZC];
+  m.xeu = a[M_XEU]; m.yeu = a[M_YEU]; m.xzv = a[M_XZV]; m.yzv = a[M_YZV];
+  m.xzu = a[M_XZU]; m.yzu = a[M_YZU]; m.xev = a[M_XEV]; m.yev = a[M_YEV];
+}
+
+// Host replay of the reference's region loops into per-cell mask bits.
+int build_masks(w2_ctx *c, std::vector<uint16_t> &mk) {
+  const int nx = c->nx, ny = c->ny, ld = c->ld, mgri = c->mgri, mgrj = c->mgrj;
+  mk.assign(c->nf, 0);
+  std::vector<uint8_t> pu(c->nf, 0), pv(c->nf, 0);
+  auto B = [&](int ir, int jr, int s) { return c->tab_brd[(ir - 1) + (jr - 1) * mgri + (s - 1) * mgri * mgrj]; };
+  auto RT = [&](int ir, int jr) { return c->tab_rtype[(ir - 1) + (jr - 1) * mgri]; };
+  auto BT = [&](int ir, int jr, int s) { return c->tab_btype[(ir - 1) + (jr - 1) * mgri + (s - 1) * mgri * mgrj]; };
+  auto at = [&](int i, int j) -> uint16_t & { return mk[(size_t)i + (size_t)j * ld]; };
+  auto inb = [&](int i, int j) { return i >= 0 && i <= nx + 1 && j >= 0 && j <= ny + 1; };
+  for (int jr = 1; jr <= c->nrj; jr++)
+    for (int ir = 1; ir <= c->nri; ir++) {
+      const int iW = B(ir, jr, W2_WEST), iE = B(ir, jr, W2_EAST);
+      const int jS = B(ir, jr, W2_SOUTH), jN = B(ir, jr, W2_NORTH);
+      if (iW < 1 || iE > nx || jS < 1 || jN > ny || iW >= iE || jS >= jN)
+        return fail(c, W2_E_ARG, "region %d,%d borders out of range", ir, jr);
+      for (int s = 1; s <= 4; ++s) {
+        int t = BT(ir, jr, s);
+        if (t < W2_BM_INTERN || t > W2_BM_OUTLT2)
+          return fail(c, W2_E_BCFLAG, "Wrong nBdType flag in region %d,%d", ir, jr);
+      }
+      const int rt = RT(ir, jr);
+      if (rt == W2_RM_POROUS) c->porous = true;
+      // X split-2 identity rows, momentum.f:444-496
+      if (rt == W2_RM_BLOCKG)
+        for (int j = jS + 1; j <= jN; j++)
+          for (int i = iW; i <= iE; i++) at(i, j) |= MK_XID;
+      int tw = BT(ir, jr, W2_WEST), te = BT(ir, jr, W2_EAST);
+      int ts = BT(ir, jr, W2_SOUTH), tn = BT(ir, jr, W2_NORTH);
+      auto wall = [](int t) { return t == W2_BM_WALL1 || t == W2_BM_WALL2 || t == W2_BM_INLET; };
+      if (wall(tw)) for (int j = jS + 1; j <= jN; j++) at(iW, j) |= MK_XID;
+      if (wall(te)) for (int j = jS + 1; j <= jN; j++) at(iE, j) |= MK_XID;
+      // Y split-2 identity rows, momentum.f:770-821
+      if (rt == W2_RM_BLOCKG)
+        for (int j = jS; j <= jN; j++)
+          for (int i = iW + 1; i <= iE; i++) at(i, j) |= MK_YID;
+      if (wall(ts)) for (int i = iW + 1; i <= iE; i++) at(i, jS) |= MK_YID;
+      if (wall(tn)) for (int i = iW + 1; i <= iE; i++) at(i, jN) |= MK_YID;
+      if (rt != W2_RM_BLOCKG) {
+        // Project / Filter u, utility.f:313-363 and 94-137
+        for (int j = jS + 1; j <= jN; j++)
+          for (int i = iW + 1; i <= iE - 1; i++) { pu[i + (size_t)j * ld]++; at(i, j) |= MK_FU; }
+        if (tw == W2_BM_OUTLT1)
+          for (int j = jS + 1; j <= jN; j++) { pu[iW + (size_t)j * ld]++; at(iW, j) |= MK_FU; }
+        if (te == W2_BM_INTERN || te == W2_BM_OUTLT1)
+          for (int j = jS + 1; j <= jN; j++) { pu[iE + (size_t)j * ld]++; at(iE, j) |= MK_FU; }
+        // Project / Filter v, utility.f:384-432 and 157-201
+        for (int j = jS + 1; j <= jN - 1; j++)
+          for (int i = iW + 1; i <= iE; i++) { pv[i + (size_t)j * ld]++; at(i, j) |= MK_FV; }
+        if (ts == W2_BM_OUTLT1)
+          for (int i = iW + 1; i <= iE; i++) { pv[i + (size_t)jS * ld]++; at(i, jS) |= MK_FV; }
+        if (tn == W2_BM_INTERN || tn == W2_BM_OUTLT1)
+          for (int i = iW + 1; i <= iE; i++) { pv[i + (size_t)jN * ld]++; at(i, jN) |= MK_FV; }
+      } else {
+        // PPE identity rows and div zeroing, pressure.f:109-196
+        auto pid = [&](int i, int j) {
+          if (inb(i, j) && i >= 2 && i <= nx && j >= 2 && j <= ny) at(i, j) |= MK_PID;
+        };
+        auto dz = [&](int i, int j) { if (inb(i, j)) at(i, j) |= MK_DIVZ; };
+        for (int j = jS + 2; j <= jN - 1; j++)
+          for (int i = iW + 2; i <= iE - 1; i++) { pid(i, j); dz(i, j); }
+        // a(ind,.) rows addressed through ind in the reference map back to
+        // (i,j) = (ind mod (nx-1) + 1, ind div (nx-1) + 2)
+        auto pid_ind = [&](int ind) {
+          int i = (ind - 1) % (nx - 1) + 2, j = (ind - 1) / (nx - 1) + 2;
+          pid(i, j);
+        };
+        if (ir > 1 && RT(ir - 1, jr) == W2_RM_BLOCKG)
+          for (int j = jS + 1; j <= jN; j++) { pid_ind((j - 2) * (nx - 1) + iW); dz(iW + 1, j); }
+        if (ir < c->nri && RT(ir + 1, jr) == W2_RM_BLOCKG)
+          for (int j = jS + 1; j <= jN; j++) { pid_ind((j - 2) * (nx - 1) + iE - 1); dz(iE, j); }
+        if (jr > 1 && RT(ir, jr - 1) == W2_RM_BLOCKG)
+          for (int i = iW + 1; i <= iE; i++) { pid_ind((jS - 1) * (nx - 1) + i - 1); dz(i, jS + 1); }
+        if (jr < c->nrj && RT(ir, jr + 1) == W2_RM_BLOCKG)
+          for (int i = iW + 1; i <= iE; i++) { pid_ind((jN - 2) * (nx - 1) + i - 1); dz(i, jN); }
+      }
+    }
+  for (size_t k = 0; k < c->nf; ++k) {
+    if (pu[k] > 1 || pv[k] > 1)
+      return fail(c, W2_E_UNSUPPORTED, "overlapping projection faces in the region layout");
+    if (pu[k]) mk[k] |= MK_PU;
+    if (pv[k]) mk[k] |= MK_PV;
+  }
+  return W2_OK;
+}
+
+int pick_blocks(w2_ctx *c, const void *kern, long work) {
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, c->threads, 0);
+  occ = std::max(1, std::min(occ, c->blocks_per_sm));
+  long want = (work + 4095) / 4096;
+  long nb = std::max<long>(1, std::min<long>(want, (long)occ * c->nsm));
+  return (int)nb;
+}
+
+int coop(w2_ctx *c, const void *kern, int blocks, void **args) {
+  c->launches++;
+  cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(c->threads), args, 0, c->st);
+  if (e != cudaSuccess) return fail(c, W2_E_CUDA, "cooperative launch: %s", cudaGetErrorString(e));
+  return W2_OK;
+}
+
+int check_sync(w2_ctx *c) {
+  CK(cudaStreamSynchronize(c->st));
+  Sync s;
+  CK(cudaMemcpy(&s, c->dev.sync, sizeof(Sync), cudaMemcpyDeviceToHost));
+  if (s.error) {
+    int code = s.error;
+    // clear the sticky error and barrier state so the context stays usable
+    Sync z;
+    memset(&z, 0, sizeof(z));
+    cudaMemcpy(c->dev.sync, &z, sizeof(Sync), cudaMemcpyHostToDevice);
+    if (code == W2_E_TIMEOUT) return fail(c, code, "device wait exceeded its time limit");
+    if (code == W2_E_BCFLAG) return fail(c, code, "invalid boundary flag");
+    return fail(c, code, "device error %d", code);
+  }
+  return W2_OK;
+}
+
+// Chain buffers for a chain of n rows.
+int make_chain(w2_ctx *c, Chain &ch, int n, bool with_b) {
+  ch.n = n;
+  ch.a1 = dalloc<double>(c, n);
+  ch.a2 = dalloc<double>(c, n);
+  ch.a3 = dalloc<double>(c, n);
+  ch.b = with_b ? dalloc<double>(c, n) : nullptr;
+  ch.a3p = dalloc<double>(c, n);
+  ch.bp = dalloc<double>(c, n);
+  ch.x = dalloc<double>(c, n);
+  ch.bzero = nullptr;
+  if (!ch.a1 || !ch.a2 || !ch.a3 || !ch.a3p || !ch.bp || !ch.x || (with_b && !ch.b))
+    return fail(c, W2_E_CUDA, "out of device memory (chains)");
+  return W2_OK;
+}
+
+int set_segments(w2_ctx *c) {
+  Dev &d = c->dev;
+  const int nX = c->nx * (c->ny - 1), nY = (c->nx - 1) * c->ny;
+  int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny);
+  long threads = (long)blocks * c->threads;
+  int seg = c->seg_req > 0 ? c->seg_req : (int)std::max<long>(8, (nX + nY + threads - 1) / threads);
+  seg = std::min(seg, 4096);
+  d.seg = seg;
+  d.warm = c->warm_req > 0 ? c->warm_req : 64;
+  auto setn = [&](Chain &ch, int n) {
+    ch.nseg = (n + seg - 1) / seg;
+  };
+  setn(d.x1, nX); setn(d.x2, nX); setn(d.y1, nY); setn(d.y2, nY);
+  // end-state buffers, sized for the smallest segment length we allow (8)
+  return W2_OK;
+}
+
+int copy_in(w2_ctx *c, double *dst, const double *src) {
+  CK(cudaMemcpy2DAsync(dst, (size_t)c->ld * 8, src, (size_t)(c->mnx + 1) * 8, (size_t)(c->nx + 2) * 8,
+                       c->ny + 2, cudaMemcpyHostToDevice, c->st));
+  return W2_OK;
+}
+
+int copy_out(w2_ctx *c, double *dst, const double *src) {
+  CK(cudaMemcpy2DAsync(dst, (size_t)(c->mnx + 1) * 8, src, (size_t)c->ld * 8, (size_t)(c->nx + 2) * 8,
+                       c->ny + 2, cudaMemcpyDeviceToHost, c->st));
+  return W2_OK;
+}
+
+bool dims_match(w2_ctx *c, const int *nx, const int *ny) {
+  return nx && ny && *nx == c->nx && *ny == c->ny;
+}
+
+int ready(w2_ctx *c) {
+  if (!c) return W2_E_ARG;
+  if (!c->metrics_ok) return fail(c, W2_E_ARG, "metrics not set (wolfd2gpu_set_metrics or wolfd2gpu_grid_metric)");
+  if (c->porous) return fail(c, W2_E_UNSUPPORTED, "porous regions are not supported by the GPU path");
+  return W2_OK;
+}
+
+// ---- launch helpers on explicit device buffers ---------------------------
+int launch_bc(w2_ctx *c, int ops, double *u, double *v, double *p) {
+  c->launches++;
+  k_bc<<<1, c->threads, 0, c->st>>>(c->dev, ops, u, v, p);
+  CK(cudaGetLastError());
+  return W2_OK;
+}
+
+int launch_naux(w2_ctx *c, int mqiter, double dk, double re, double qtol, const double *un,
+                const double *vn, double *us, double *vs) {
+  int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny);
+  Dev d = c->dev;
+  StepOut *out = c->d_out;
+  void *args[] = {&d, &mqiter, &dk, &re, &qtol, (void *)&un, (void *)&vn, &us, &vs, &out};
+  return coop(c, (const void *)k_naux, blocks, args);
+}
+
+int launch_ppe(w2_ctx *c, int lcartes, int npsolver, int msorit, double dk, double sortol,
+               double sorrel, const double *u, const double *v, double *p) {
+  int blocks = (npsolver == 1 || npsolver == 2) ? 1 : pick_blocks(c, (const void *)k_ppe, (long)c->nx * c->ny);
+  Dev d = c->dev;
+  StepOut *out = c->d_out;
+  void *args[] = {&d, &lcartes, &npsolver, &msorit, &dk, &sortol, &sorrel, (void *)&u, (void *)&v, &p, &out};
+  return coop(c, (const void *)k_ppe, blocks, args);
+}
+
+int grid_blocks(w2_ctx *c) {
+  long work = (long)(c->nx + 2) * (c->ny + 2);
+  return (int)std::max<long>(1, std::min<long>((work + c->threads - 1) / c->threads, (long)c->nsm * 8));
+}
+
+}  // namespace
+
+extern "C" {
+
+int wolfd2gpu_create(w2_ctx **out, int mnx, int mny, int mgri, int mgrj, int nx, int ny,
+                     const int *nReg, const int *nRegBrd, const int *nRegType,
+                     const int *nMomBdTp, const double *dBCVal, const double *dPRporos,
+                     const double *dPRporc1, const double *dPRporc2) {
+  (void)dPRporos; (void)dPRporc1; (void)dPRporc2;
+  if (!out) return W2_E_ARG;
+  *out = nullptr;
+  if (nx < 6 || ny < 6 || nx + 1 > mnx || ny + 1 > mny || mgri < 1 || mgrj < 1 || !nReg ||
+      !nRegBrd || !nRegType || !nMomBdTp || !dBCVal)
+    return W2_E_ARG;
+  if (nReg[0] < 1 || nReg[0] > mgri || nReg[1] < 1 || nReg[1] > mgrj) return W2_E_ARG;
+  w2_ctx *c = new w2_ctx();
+  c->mnx = mnx; c->mny = mny; c->mgri = mgri; c->mgrj = mgrj; c->nx = nx; c->ny = ny;
+  c->ld = ((nx + 2 + 31) / 32) * 32;
+  c->nf = (size_t)c->ld * (size_t)(ny + 2);
+  c->nri = nReg[0]; c->nrj = nReg[1];
+  const size_t nt = (size_t)mgri * mgrj;
+  c->tab_brd.assign(nRegBrd, nRegBrd + nt * 4);
+  c->tab_rtype.assign(nRegType, nRegType + nt);
+  c->tab_btype.assign(nMomBdTp, nMomBdTp + nt * 4);
+  c->tab_bcv.assign(dBCVal, dBCVal + nt * 16);
+  auto bad = [&](int code) { int r = code; wolfd2gpu_destroy(c); return r; };
+  if (cudaGetDevice(&c->device) != cudaSuccess) return bad(W2_E_CUDA);
+  cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device);
+  int coopok = 0;
+  cudaDeviceGetAttribute(&coopok, cudaDevAttrCooperativeLaunch, c->device);
+  if (!coopok) return bad(W2_E_UNSUPPORTED);
+  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) return bad(W2_E_CUDA);
+  std::vector<uint16_t> mk;
+  int rc = build_masks(c, mk);
+  if (rc) { fprintf(stderr, "wolfd2gpu_create: %s\n", c->err); return bad(rc); }
+  Dev &d = c->dev;
+  d.nx = nx; d.ny = ny; d.ld = c->ld;
+  for (int k = 0; k < W2_NMETRIC; ++k)
+    if (!(c->met[k] = dalloc<double>(c, c->nf))) return bad(W2_E_CUDA);
+  bind_metrics(c);
+  int *brd = dalloc<int>(c, nt * 4), *rty = dalloc<int>(c, nt), *bty = dalloc<int>(c, nt * 4);
+  double *bcv = dalloc<double>(c, nt * 16);
+  uint16_t *dmk = dalloc<uint16_t>(c, c->nf);
+  if (!brd || !rty || !bty || !bcv || !dmk) return bad(W2_E_CUDA);
+  cudaMemcpy(brd, c->tab_brd.data(), nt * 4 * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMemcpy(rty, c->tab_rtype.data(), nt * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMemcpy(bty, c->tab_btype.data(), nt * 4 * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMemcpy(bcv, c->tab_bcv.data(), nt * 16 * sizeof(double), cudaMemcpyHostToDevice);
+  cudaMemcpy(dmk, mk.data(), c->nf * sizeof(uint16_t), cudaMemcpyHostToDevice);
+  d.r = Regions{c->nri, c->nrj, mgri, mgrj, brd, rty, bty, bcv};
+  d.mask = dmk;
+  d.has_outflow = 0;
+  for (int jr = 1; jr <= c->nrj; ++jr)
+    for (int ir = 1; ir <= c->nri; ++ir)
+      for (int s = 1; s <= 4; ++s) {
+        int t = c->tab_btype[(ir - 1) + (jr - 1) * mgri + (s - 1) * nt];
+        if (t == W2_BM_OUTLT1 || t == W2_BM_OUTLT2) d.has_outflow = 1;
+      }
+  for (int k = 0; k < 2; ++k) {
+    if (!(c->U[k] = dalloc<double>(c, c->nf)) || !(c->V[k] = dalloc<double>(c, c->nf)) ||
+        !(c->P[k] = dalloc<double>(c, c->nf)))
+      return bad(W2_E_CUDA);
+  }
+  for (int k = 0; k < 6; ++k)
+    if (!(c->stage[k] = dalloc<double>(c, c->nf))) return bad(W2_E_CUDA);
+  double **wa[] = {&d.cj1x, &d.cj2x, &d.c1sx, &d.c2sx, &d.c1nx, &d.c2nx, &d.cj1y, &d.cj2y,
+                   &d.c1sy, &d.c2sy, &d.c1ny, &d.c2ny, &d.pa1, &d.pa2, &d.pa3, &d.pa4,
+                   &d.pa5, &d.div, &d.pb, &d.ppn, &d.la3p, &d.lbp, &d.qh};
+  for (double **w : wa)
+    if (!(*w = dalloc<double>(c, c->nf))) return bad(W2_E_CUDA);
+  const int nX = nx * (ny - 1), nY = (nx - 1) * ny;
+  if (make_chain(c, d.x1, nX, true) || make_chain(c, d.x2, nX, false) ||
+      make_chain(c, d.y1, nY, true) || make_chain(c, d.y2, nY, false))
+    return bad(W2_E_CUDA);
+  // split-2 rhs = split-1 solution, zero on identity rows
+  d.x2.b = d.x1.x;
+  d.y2.b = d.y1.x;
+  {
+    std::vector<uint8_t> zx(nX), zy(nY);
+    for (int j = 2; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) zx[(j - 2) * nx + i - 1] = (mk[i + (size_t)j * c->ld] & MK_XID) ? 1 : 0;
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 2; i <= nx; ++i) zy[(j - 1) * (nx - 1) + i - 2] = (mk[i + (size_t)j * c->ld] & MK_YID) ? 1 : 0;
+    uint8_t *dzx = dalloc<uint8_t>(c, nX), *dzy = dalloc<uint8_t>(c, nY);
+    if (!dzx || !dzy) return bad(W2_E_CUDA);
+    cudaMemcpy(dzx, zx.data(), nX, cudaMemcpyHostToDevice);
+    cudaMemcpy(dzy, zy.data(), nY, cudaMemcpyHostToDevice);
+    d.x2.bzero = dzx;
+    d.y2.bzero = dzy;
+  }
+  // end-state buffers for the smallest allowed segment length (8)
+  {
+    const int maxsegX = (nX + 7) / 8, maxsegY = (nY + 7) / 8;
+    Chain *chs[] = {&d.x1, &d.x2, &d.y1, &d.y2};
+    for (Chain *ch : chs) {
+      int ms = ch->n == nX ? maxsegX : maxsegY;
+      ch->ef = dalloc<double>(c, (size_t)4 * ms);
+      ch->eb = dalloc<double>(c, (size_t)2 * ms);
+      if (!ch->ef || !ch->eb) return bad(W2_E_CUDA);
+    }
+  }
+  d.sync = dalloc<Sync>(c, 1);
+  c->d_out = dalloc<StepOut>(c, 1);
+  if (!d.sync || !c->d_out) return bad(W2_E_CUDA);
+  if (cudaMallocHost(&c->h_out, sizeof(StepOut)) != cudaSuccess) return bad(W2_E_CUDA);
+  c->threads = 256;
+  c->blocks_per_sm = 2;
+  set_segments(c);
+  d.u = c->U[0]; d.v = c->V[0]; d.p = c->P[0];
+  if (cudaDeviceSynchronize() != cudaSuccess) return bad(W2_E_CUDA);
+  *out = c;
+  return W2_OK;
+}
+
+int wolfd2gpu_destroy(w2_ctx *c) {
+  if (!c) return W2_OK;
+  if (c->st) cudaStreamSynchronize(c->st);
+  for (void *p : c->allocs) cudaFree(p);
+  if (c->h_out) cudaFreeHost(c->h_out);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return W2_OK;
+}
+
+const char *wolfd2gpu_last_error(w2_ctx *c) { return c ? c->err : "null context"; }
+
+long long wolfd2gpu_launch_count(w2_ctx *c) { return c ? c->launches : 0; }
+
+int wolfd2gpu_tune(w2_ctx *c, int chain_seg, int chain_warm, int threads, int blocks_per_sm) {
+  if (!c) return W2_E_ARG;
+  if (chain_seg < 0 || chain_warm < 0 || threads < 0 || blocks_per_sm < 0) return W2_E_ARG;
+  if (chain_seg > 0 && chain_seg < 8) return fail(c, W2_E_ARG, "chain segment length must be >= 8");
+  if (threads > 0) {
+    if (threads % 32 || threads > kMaxThreads) return fail(c, W2_E_ARG, "threads must be a multiple of 32 <= %d", kMaxThreads);
+    c->threads = threads;
+  }
+  if (blocks_per_sm > 0) c->blocks_per_sm = blocks_per_sm;
+  c->seg_req = chain_seg;
+  c->warm_req = chain_warm;
+  return set_segments(c);
+}
+
+int wolfd2gpu_set_metrics(w2_ctx *c, const double *const *metrics) {
+  if (!c || !metrics) return W2_E_ARG;
+  for (int k = 0; k < W2_NMETRIC; ++k) {
+    if (!metrics[k]) return fail(c, W2_E_ARG, "metric %d is null", k);
+    int rc = copy_in(c, c->met[k], metrics[k]);
+    if (rc) return rc;
+  }
+  c->launches++;
+  k_ppe_coef<<<grid_blocks(c), c->threads, 0, c->st>>>(c->dev);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->st));
+  c->metrics_ok = true;
+  return W2_OK;
+}
+
+int wolfd2gpu_grid_metric(w2_ctx *c, const double *gx, const double *gy, double *const *metrics_out) {
+  if (!c || !gx || !gy) return W2_E_ARG;
+  double *x = c->stage[0], *y = c->stage[1], *xu = c->stage[2], *yu = c->stage[3], *xv = c->stage[4],
+         *yv = c->stage[5];
+  double *xc = c->dev.pa1, *yc = c->dev.pa2;  // free until the PPE coefficients are formed
+  for (int k = 0; k < 6; ++k) CK(cudaMemsetAsync(c->stage[k], 0, c->nf * 8, c->st));
+  CK(cudaMemsetAsync(xc, 0, c->nf * 8, c->st));
+  CK(cudaMemsetAsync(yc, 0, c->nf * 8, c->st));
+  for (int k = 0; k < W2_NMETRIC; ++k) CK(cudaMemsetAsync(c->met[k], 0, c->nf * 8, c->st));
+  int rc = copy_in(c, x, gx);
+  if (!rc) rc = copy_in(c, y, gy);
+  if (rc) return rc;
+  const int gb = grid_blocks(c);
+  k_mirror<<<1, 256, 0, c->st>>>(c->dev, x, y);
+  k_fullgrid_uv<<<gb, c->threads, 0, c->st>>>(c->dev, x, y, xu, yu, xv, yv);
+  k_fullgrid_c<<<gb, c->threads, 0, c->st>>>(c->dev, xu, yv, xc, yc);
+  MetricOut mo;
+  double **a = c->met;
+  mo.rau = a[M_RAU]; mo.rbu = a[M_RBU]; mo.rbv = a[M_RBV]; mo.rgv = a[M_RGV];
+  mo.ran = a[M_RAN]; mo.rbn = a[M_RBN]; mo.rgn = a[M_RGN];
+  mo.rac = a[M_RAC]; mo.rbc = a[M_RBC]; mo.rgc = a[M_RGC];
+  mo.dju = a[M_DJU]; mo.djv = a[M_DJV]; mo.djc = a[M_DJC]; mo.djn = a[M_DJN];
+  mo.xen = a[M_XEN]; mo.yen = a[M_YEN]; mo.xzn = a[M_XZN]; mo.yzn = a[M_YZN];
+  mo.xec = a[M_XEC]; mo.yec = a[M_YEC]; mo.xzc = a[M_XZC]; mo.yzc = a[M_YZC];
+  mo.xeu = a[M_XEU]; mo.yeu = a[M_YEU]; mo.xzv = a[M_XZV]; mo.yzv = a[M_YZV];
+  mo.xzu = a[M_XZU]; mo.yzu = a[M_YZU]; mo.xev = a[M_XEV]; mo.yev = a[M_YEV];
+  k_metric<<<gb, c->threads, 0, c->st>>>(c->dev, mo, x, y, xu, yu, xv, yv, xc, yc);
+  c->launches += 4;
+  CK(cudaGetLastError());
+  if (metrics_out)
+    for (int k = 0; k < W2_NMETRIC; ++k)
+      if (metrics_out[k]) {
+        rc = copy_out(c, metrics_out[k], c->met[k]);
+        if (rc) return rc;
+      }
+  CK(cudaMemsetAsync(xc, 0, c->nf * 8, c->st));
+  CK(cudaMemsetAsync(yc, 0, c->nf * 8, c->st));
+  c->launches++;
+  k_ppe_coef<<<gb, c->threads, 0, c->st>>>(c->dev);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->st));
+  c->metrics_ok = true;
+  return W2_OK;
+}
+
+// ---- drop-ins -------------------------------------------------------------
+
+int wolfd2gpu_naux_momentum(w2_ctx *c, const int *nx, const int *ny, const int *mqiter,
+                            const double *dk, const double *re, const double *fr,
+                            const double *qtol, const double *d, const double *dn,
+                            const double *un, const double *vn, double *us, double *vs,
+                            int *nQLiter) {
+  (void)fr;
+  int rc = ready(c);
+  if (rc) return rc;
+  if (!dims_match(c, nx, ny) || !mqiter || !dk || !re || !qtol || !un || !vn || !us || !vs || !nQLiter)
+    return fail(c, W2_E_ARG, "bad argument");
+  if (d || dn) {
+    // density enters only through the buoyancy term (momentum.f:703), which
+    // needs the equation of state (thermal energy, outside this library)
+    const double *arrs[2] = {d, dn};
+    for (const double *a : arrs)
+      if (a)
+        for (int j = 0; j <= c->ny + 1; ++j)
+          for (int i = 0; i <= c->nx + 1; ++i)
+            if (a[i + (size_t)j * (c->mnx + 1)] != 0.0)
+              return fail(c, W2_E_UNSUPPORTED, "nonzero density (buoyancy) is not supported");
+  }
+  double *dun = c->stage[0], *dvn = c->stage[1], *dus = c->stage[2], *dvs = c->stage[3];
+  if ((rc = copy_in(c, dun, un)) || (rc = copy_in(c, dvn, vn)) || (rc = copy_in(c, dus, us)) ||
+      (rc = copy_in(c, dvs, vs)))
+    return rc;
+  c->launches++;
+  k_naux_init<<<grid_blocks(c), c->threads, 0, c->st>>>(c->dev, dun, dvn, dus, dvs);
+  CK(cudaGetLastError());
+  if ((rc = launch_naux(c, *mqiter, *dk, *re, *qtol, dun, dvn, dus, dvs))) return rc;
+  if ((rc = copy_out(c, us, dus)) || (rc = copy_out(c, vs, dvs))) return rc;
+  CK(cudaMemcpyAsync(c->h_out, c->d_out, sizeof(StepOut), cudaMemcpyDeviceToHost, c->st));
+  if ((rc = check_sync(c))) return rc;
+  *nQLiter = c->h_out->nql;
+  return W2_OK;
+}
+
+int wolfd2gpu_ppe(w2_ctx *c, const int *nx, const int *ny, const int *lCartesGrid,
+                  const int *nPpeSolver, const int *msorit, int *nSorConv, const double *dk,
+                  const double *sortol, const double *sorrel, const double *u, const double *v,
+                  double *p) {
+  int rc = ready(c);
+  if (rc) return rc;
+  if (!dims_match(c, nx, ny) || !lCartesGrid || !nPpeSolver || !msorit || !nSorConv || !dk ||
+      !sortol || !sorrel || !u || !v || !p)
+    return fail(c, W2_E_ARG, "bad argument");
+  double *du = c->stage[0], *dv = c->stage[1], *dp = c->stage[2];
+  if ((rc = copy_in(c, du, u)) || (rc = copy_in(c, dv, v)) || (rc = copy_in(c, dp, p))) return rc;
+  if ((rc = launch_ppe(c, *lCartesGrid ? 1 : 0, *nPpeSolver, *msorit, *dk, *sortol, *sorrel, du, dv, dp)))
+    return rc;
+  if ((rc = copy_out(c, p, dp))) return rc;
+  CK(cudaMemcpyAsync(c->h_out, c->d_out, sizeof(StepOut), cudaMemcpyDeviceToHost, c->st));
+  if ((rc = check_sync(c))) return rc;
+  *nSorConv = c->h_out->nsor;
+  return W2_OK;
+}
+
+int wolfd2gpu_project(w2_ctx *c, const int *nx, const int *ny, const double *dk, const double *p,
+                      double *u, double *v) {
+  int rc = ready(c);
+  if (rc) return rc;
+  if (!dims_match(c, nx, ny) || !dk || !p || !u || !v) return fail(c, W2_E_ARG, "bad argument");
+  double *du = c->stage[0], *dv = c->stage[1], *dp = c->stage[2];
+  if ((rc = copy_in(c, du, u)) || (rc = copy_in(c, dv, v)) || (rc = copy_in(c, dp, p))) return rc;
+  c->launches++;
+  k_project<<<grid_blocks(c), c->threads, 0, c->st>>>(c->dev, *dk, dp, du, dv);
+  CK(cudaGetLastError());
+  if ((rc = copy_out(c, u, du)) || (rc = copy_out(c, v, dv))) return rc;
+  return check_sync(c);
+}
+
+static int bc_dropin(w2_ctx *c, const int *nx, const int *ny, int ops, double *u, double *v, double *p) {
+  if (!c) return W2_E_ARG;
+  if (!dims_match(c, nx, ny)) return fail(c, W2_E_ARG, "bad argument");
+  double *du = c->stage[0], *dv = c->stage[1], *dp = c->stage[2];
+  int rc;
+  if (u && (rc = copy_in(c, du, u))) return rc;
+  if (v && (rc = copy_in(c, dv, v))) return rc;
+  if (p && (rc = copy_in(c, dp, p))) return rc;
+  if ((rc = launch_bc(c, ops, du, dv, dp))) return rc;
+  if (u && (rc = copy_out(c, u, du))) return rc;
+  if (v && (rc = copy_out(c, v, dv))) return rc;
+  if (p && (rc = copy_out(c, p, dp))) return rc;
+  return check_sync(c);
+}
+
+int wolfd2gpu_vel_bound_cond(w2_ctx *c, const int *nx, const int *ny, double *u, double *v) {
+  if (!u || !v) return fail(c, W2_E_ARG, "bad argument");
+  return bc_dropin(c, nx, ny, BC_VEL, u, v, nullptr);
+}
+
+int wolfd2gpu_pres_bound_cond(w2_ctx *c, const int *nx, const int *ny, double *p) {
+  if (!p) return fail(c, W2_E_ARG, "bad argument");
+  return bc_dropin(c, nx, ny, BC_PRES, nullptr, nullptr, p);
+}
+
+int wolfd2gpu_vel_outflow_bcs(w2_ctx *c, const int *nx, const int *ny, double *u, double *v) {
+  if (!u || !v) return fail(c, W2_E_ARG, "bad argument");
+  return bc_dropin(c, nx, ny, BC_OUTFLOW, u, v, nullptr);
+}
+
+int wolfd2gpu_diff_max_norm(w2_ctx *c, const int *nx, const int *ny, const double *un,
+                            const double *u, double *result) {
+  if (!c) return W2_E_ARG;
+  if (!dims_match(c, nx, ny) || !un || !u || !result) return fail(c, W2_E_ARG, "bad argument");
+  int rc;
+  double *da = c->stage[0], *db = c->stage[1];
+  if ((rc = copy_in(c, da, un)) || (rc = copy_in(c, db, u))) return rc;
+  unsigned long long *slot = &c->dev.sync->red[9];
+  CK(cudaMemsetAsync(slot, 0, 8, c->st));
+  c->launches++;
+  k_diff_norm<<<grid_blocks(c), c->threads, 0, c->st>>>(c->dev, da, db, slot);
+  CK(cudaGetLastError());
+  unsigned long long bits = 0;
+  CK(cudaMemcpyAsync(&bits, slot, 8, cudaMemcpyDeviceToHost, c->st));
+  if ((rc = check_sync(c))) return rc;
+  memcpy(result, &bits, 8);
+  return W2_OK;
+}
+
+int wolfd2gpu_filter(w2_ctx *c, const int *nx, const int *ny, const int *ncomp, const double *fp,
+                     double *qu) {
+  int rc = ready(c);
+  if (rc) return rc;
+  if (!dims_match(c, nx, ny) || !ncomp || !fp || !qu || (*ncomp != 1 && *ncomp != 2))
+    return fail(c, W2_E_ARG, "bad argument");
+  double *dq = c->stage[0], *dh = c->stage[1];
+  if ((rc = copy_in(c, dq, qu))) return rc;
+  c->launches++;
+  k_filter<<<grid_blocks(c), c->threads, 0, c->st>>>(c->dev, *ncomp == 1 ? MK_FU : MK_FV, *fp, dq, dh);
+  CK(cudaGetLastError());
+  if ((rc = copy_out(c, qu, dh))) return rc;
+  return check_sync(c);
+}
+
+// ---- device-resident time loop ----------------------------------------------
+
+int wolfd2gpu_load_fields(w2_ctx *c, const double *u, const double *v, const double *p) {
+  if (!c || !u || !v || !p) return W2_E_ARG;
+  int rc;
+  if ((rc = copy_in(c, c->U[c->cur], u)) || (rc = copy_in(c, c->V[c->cur], v)) ||
+      (rc = copy_in(c, c->P[c->cur], p)))
+    return rc;
+  return W2_OK;
+}
+
+int wolfd2gpu_store_fields(w2_ctx *c, double *u, double *v, double *p) {
+  if (!c) return W2_E_ARG;
+  int rc;
+  if (u && (rc = copy_out(c, u, c->U[c->cur]))) return rc;
+  if (v && (rc = copy_out(c, v, c->V[c->cur]))) return rc;
+  if (p && (rc = copy_out(c, p, c->P[c->cur]))) return rc;
+  CK(cudaStreamSynchronize(c->st));
+  return W2_OK;
+}
+
+int wolfd2gpu_device_fields(w2_ctx *c, double **u, double **v, double **p, int *ld) {
+  if (!c) return W2_E_ARG;
+  if (u) *u = c->U[c->cur];
+  if (v) *v = c->V[c->cur];
+  if (p) *p = c->P[c->cur];
+  if (ld) *ld = c->ld;
+  return W2_OK;
+}
+
+int wolfd2gpu_sync(w2_ctx *c) {
+  if (!c) return W2_E_ARG;
+  return check_sync(c);
+}
+
+static int check_params(w2_ctx *c, const w2_params *prm) {
+  if (!prm) return fail(c, W2_E_ARG, "null params");
+  if (prm->npsolver < 1 || prm->npsolver > 6 || prm->msorit < 1 || prm->mqiter < 1)
+    return fail(c, W2_E_ARG, "bad solver parameters");
+  if (prm->precision != W2_PREC_FP64)
+    return fail(c, W2_E_UNSUPPORTED, "precision mode %d not available in this build", prm->precision);
+  return W2_OK;
+}
+
+int wolfd2gpu_cold_start(w2_ctx *c, const w2_params *prm, int *nSorConv) {
+  int rc = ready(c);
+  if (rc) return rc;
+  if ((rc = check_params(c, prm))) return rc;
+  double *u = c->U[c->cur], *v = c->V[c->cur], *p = c->P[c->cur];
+  if ((rc = launch_bc(c, BC_VEL, u, v, p))) return rc;
+  if ((rc = launch_ppe(c, prm->lcartes, prm->npsolver, prm->msorit, prm->dk, prm->sortol, prm->sorrel, u, v, p)))
+    return rc;
+  if ((rc = launch_bc(c, BC_PRES, u, v, p))) return rc;
+  c->launches++;
+  k_project<<<grid_blocks(c), c->threads, 0, c->st>>>(c->dev, prm->dk, p, u, v);
+  CK(cudaGetLastError());
+  if ((rc = launch_bc(c, BC_VEL, u, v, p))) return rc;
+  CK(cudaMemcpyAsync(c->h_out, c->d_out, sizeof(StepOut), cudaMemcpyDeviceToHost, c->st));
+  if ((rc = check_sync(c))) return rc;
+  if (nSorConv) *nSorConv = c->h_out->nsor;
+  return W2_OK;
+}
+
+int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *stats) {
+  int rc = ready(c);
+  if (rc) return rc;
+  if ((rc = check_params(c, prm))) return rc;
+  if (nsteps < 0) return fail(c, W2_E_ARG, "nsteps < 0");
+  std::vector<StepOut> outs((size_t)std::max(nsteps, 1));
+  StepOut *d_outs = nullptr;
+  CK(cudaMallocAsync((void **)&d_outs, sizeof(StepOut) * std::max(nsteps, 1), c->st));
+  const int gb = grid_blocks(c);
+  for (int s = 0; s < nsteps && rc == W2_OK; ++s) {
+    const int a = c->cur, b = 1 - a;
+    double *un = c->U[a], *vn = c->V[a], *pn = c->P[a];
+    double *us = c->U[b], *vs = c->V[b], *p = c->P[b];
+    StepOut *o = d_outs + s;
+    Dev d = c->dev;
+    c->launches++;
+    k_copy3<<<gb, c->threads, 0, c->st>>>(d, us, un, vs, vn, p, pn);
+    CK(cudaGetLastError());
+    // nAuxMomentum on (un, vn) -> (us, vs); us = un already (main.f:741-747)
+    {
+      int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny);
+      int mq = prm->mqiter;
+      double dk = prm->dk, re = prm->re, qtol = prm->qtol;
+      void *args[] = {&d, &mq, &dk, &re, &qtol, &un, &vn, &us, &vs, &o};
+      if ((rc = coop(c, (const void *)k_naux, blocks, args))) break;
+    }
+    if (prm->nfiltu == 1 || prm->nfiltv == 1) {
+      double *h = c->stage[5];
+      if (prm->nfiltu == 1) {
+        k_filter<<<gb, c->threads, 0, c->st>>>(d, MK_FU, prm->fpu, us, h);
+        CK(cudaMemcpyAsync(us, h, c->nf * 8, cudaMemcpyDeviceToDevice, c->st));
+        c->launches++;
+      }
+      if (prm->nfiltv == 1) {
+        k_filter<<<gb, c->threads, 0, c->st>>>(d, MK_FV, prm->fpv, vs, h);
+        CK(cudaMemcpyAsync(vs, h, c->nf * 8, cudaMemcpyDeviceToDevice, c->st));
+        c->launches++;
+      }
+    }
+    if ((rc = launch_bc(c, BC_VEL | BC_PRES, us, vs, p))) break;
+    {
+      int blocks = (prm->npsolver == 1 || prm->npsolver == 2)
+                       ? 1 : pick_blocks(c, (const void *)k_ppe, (long)c->nx * c->ny);
+      int lc = prm->lcartes, ns = prm->npsolver, ms = prm->msorit;
+      double dk = prm->dk, st = prm->sortol, sr = prm->sorrel;
+      void *args[] = {&d, &lc, &ns, &ms, &dk, &st, &sr, &us, &vs, &p, &o};
+      if ((rc = coop(c, (const void *)k_ppe, blocks, args))) break;
+    }
+    {
+      int blocks = pick_blocks(c, (const void *)k_step_post, (long)c->nx * c->ny);
+      double dk = prm->dk;
+      void *args[] = {&d, &dk, &p, &pn, &un, &vn, &us, &vs, &o};
+      if ((rc = coop(c, (const void *)k_step_post, blocks, args))) break;
+    }
+    c->cur = b;
+  }
+  if (nsteps > 0)
+    cudaMemcpyAsync(outs.data(), d_outs, sizeof(StepOut) * nsteps, cudaMemcpyDeviceToHost, c->st);
+  cudaFreeAsync(d_outs, c->st);
+  int rs = check_sync(c);
+  if (rc == W2_OK) rc = rs;
+  int diverged_at = -1;
+  for (int s = 0; s < nsteps; ++s) {
+    double mx = std::max(std::max(outs[s].dif[0], outs[s].dif[1]), outs[s].dif[2]);
+    if (stats) {
+      stats[s].nQLiter = outs[s].nql;
+      stats[s].nSorConv = outs[s].nsor;
+      for (int k = 0; k < 4; ++k) stats[s].dif[k] = outs[s].dif[k];
+    }
+    if (diverged_at < 0 && mx > 1.0e12) diverged_at = s;
+  }
+  if (rc == W2_OK && diverged_at >= 0) {
+    // clear the halt flag so the context can be reloaded
+    Sync z;
+    memset(&z, 0, sizeof(z));
+    cudaMemcpy(c->dev.sync, &z, sizeof(Sync), cudaMemcpyHostToDevice);
+    return fail(c, W2_E_DIVERGED, "Solution diverged at step %d. Please reduce CFL number.", diverged_at + 1);
+  }
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,286 @@
+// w2_chain.cuh -- exact parallel solve of AltTridLU chains (momentum.f:1307-1339).
+//
+// The reference solves each momentum split step as ONE Thomas recurrence over
+// the concatenation of all grid lines, including a first-row quirk (row 1's
+// super-diagonal is divided by row 2's ORIGINAL diagonal).  Neighbouring
+// lines couple through the chain wherever the end rows are not identity rows,
+// so a per-line solve would change the numbers.
+//
+// This solver reproduces the sequential recurrence bit for bit with parallel
+// work.  The chain is cut into segments of `seg` rows, one thread each:
+//   F1  every segment runs the forward recurrence (factorisation + forward
+//       substitution, state (a3', b')) starting `warm` rows early from the
+//       state (0, 0), so by its first own row the state has usually converged
+//       to the true one (the recurrence contracts);
+//   F2  verification rounds: each segment re-runs its rows from the exact end
+//       state of its predecessor and stops at the first row whose recomputed
+//       state equals the stored one bit for bit -- from there on the stored
+//       values ARE the sequential ones.  A segment that never re-joins its
+//       stored trajectory publishes a new end state and another round runs.
+//       When a round changes nothing, every segment provably holds the values
+//       of the sequential recurrence (induction from row 0, which is exact).
+//   B1/B2  the same for the back substitution x(k) = b'(k) - a3'(k) x(k+1),
+//       running from the last row down.
+// If rounds do not settle within kMaxRounds, one thread finishes the
+// recurrence sequentially (always exact, slow) and the fallback flag is set.
+#pragma once
+#include "w2_common.cuh"
+
+namespace w2 {
+
+constexpr int kMaxRounds = 8;
+
+__device__ __forceinline__ bool same_bits(double a, double b) {
+  return __double_as_longlong(a) == __double_as_longlong(b);
+}
+
+__device__ __forceinline__ double chain_rhs(const Chain &c, int k) {
+  return (c.bzero != nullptr && c.bzero[k]) ? 0.0 : c.b[k];
+}
+
+// One forward row k >= 1 of AltTridLU: a2' = a2 - a1 a3'(k-1); a3' = a3/a2'
+// (not formed on the last row); b' = (b - a1 b'(k-1)) / a2'.
+__device__ __forceinline__ void fwd_row(const Chain &c, int k, double &a3p, double &bp) {
+  const double a1 = c.a1[k];
+  const double a2p = c.a2[k] - a1 * a3p;
+  const double nb = (chain_rhs(c, k) - a1 * bp) / a2p;
+  a3p = (k < c.n - 1) ? c.a3[k] / a2p : 0.0;
+  bp = nb;
+}
+
+// Row 0 with the reference's first-row quirk.
+__device__ __forceinline__ void fwd_row0(const Chain &c, double &a3p, double &bp) {
+  a3p = c.a3[0] / c.a2[1];
+  bp = chain_rhs(c, 0) / c.a2[0];
+}
+
+__device__ void chain_f1(const Chain &c, int s, int L, int W) {
+  const int k0 = s * L, k1 = min(c.n, k0 + L);
+  double a3p, bp;
+  int k;
+  if (k0 == 0) {
+    fwd_row0(c, a3p, bp);
+    c.a3p[0] = a3p;
+    c.bp[0] = bp;
+    k = 1;
+  } else {
+    int kw = k0 - W;
+    if (kw <= 0) {
+      fwd_row0(c, a3p, bp);
+      for (int q = 1; q < k0; ++q) fwd_row(c, q, a3p, bp);
+    } else {
+      a3p = 0.0;
+      bp = 0.0;
+      for (int q = kw; q < k0; ++q) fwd_row(c, q, a3p, bp);
+    }
+    k = k0;
+  }
+  for (; k < k1; ++k) {
+    fwd_row(c, k, a3p, bp);
+    c.a3p[k] = a3p;
+    c.bp[k] = bp;
+  }
+  c.ef[2 * s] = a3p;
+  c.ef[2 * s + 1] = bp;
+}
+
+// Verification round; reads end states from `ein`, writes `eout`.
+// Returns true when the segment's end state changed.
+__device__ bool chain_f2(const Chain &c, int s, int L, const double *ein, double *eout) {
+  if (s == 0) {
+    eout[0] = ein[0];
+    eout[1] = ein[1];
+    return false;
+  }
+  const int k0 = s * L, k1 = min(c.n, k0 + L);
+  double a3p = ein[2 * (s - 1)], bp = ein[2 * (s - 1) + 1];
+  for (int k = k0; k < k1; ++k) {
+    fwd_row(c, k, a3p, bp);
+    if (same_bits(a3p, c.a3p[k]) && same_bits(bp, c.bp[k])) {
+      eout[2 * s] = ein[2 * s];
+      eout[2 * s + 1] = ein[2 * s + 1];
+      return false;
+    }
+    c.a3p[k] = a3p;
+    c.bp[k] = bp;
+  }
+  eout[2 * s] = a3p;
+  eout[2 * s + 1] = bp;
+  return true;
+}
+
+__device__ void chain_b1(const Chain &c, int s, int L, int W) {
+  const int k0 = s * L, k1 = min(c.n, k0 + L);
+  double xn;
+  int k;
+  if (k1 == c.n) {
+    xn = c.bp[c.n - 1];
+    c.x[c.n - 1] = xn;
+    k = c.n - 2;
+  } else {
+    int kw = k1 - 1 + W;
+    if (kw >= c.n - 1) {
+      xn = c.bp[c.n - 1];
+      for (int q = c.n - 2; q >= k1; --q) xn = c.bp[q] - c.a3p[q] * xn;
+    } else {
+      xn = 0.0;
+      for (int q = kw; q >= k1; --q) xn = c.bp[q] - c.a3p[q] * xn;
+    }
+    k = k1 - 1;
+  }
+  for (; k >= k0; --k) {
+    xn = c.bp[k] - c.a3p[k] * xn;
+    c.x[k] = xn;
+  }
+  c.eb[s] = c.x[k0];
+}
+
+__device__ bool chain_b2(const Chain &c, int s, int L, const double *ein, double *eout) {
+  const int k0 = s * L, k1 = min(c.n, k0 + L);
+  if (k1 == c.n) {
+    eout[s] = ein[s];
+    return false;
+  }
+  double xn = ein[s + 1];
+  for (int k = k1 - 1; k >= k0; --k) {
+    xn = c.bp[k] - c.a3p[k] * xn;
+    if (same_bits(xn, c.x[k])) {
+      eout[s] = ein[s];
+      return false;
+    }
+    c.x[k] = xn;
+  }
+  eout[s] = xn;
+  return true;
+}
+
+// Sequential completion used when verification rounds do not settle.
+__device__ void chain_sequential(const Chain &c) {
+  double a3p, bp;
+  fwd_row0(c, a3p, bp);
+  c.a3p[0] = a3p;
+  c.bp[0] = bp;
+  for (int k = 1; k < c.n; ++k) {
+    fwd_row(c, k, a3p, bp);
+    c.a3p[k] = a3p;
+    c.bp[k] = bp;
+  }
+  double xn = c.bp[c.n - 1];
+  c.x[c.n - 1] = xn;
+  for (int k = c.n - 2; k >= 0; --k) {
+    xn = c.bp[k] - c.a3p[k] * xn;
+    c.x[k] = xn;
+  }
+}
+
+// Views of a chain whose end-state buffers are swapped per round.
+__device__ __forceinline__ const double *ef_buf(const Chain &c, int b) {
+  return c.ef + (size_t)b * 2 * c.nseg;
+}
+__device__ __forceinline__ const double *eb_buf(const Chain &c, int b) {
+  return c.eb + (size_t)b * c.nseg;
+}
+
+// Solve up to two independent chains together (segments of both share the
+// grid).  Every block must call this.  Returns false if a barrier failed.
+__device__ bool solve_chains(const Dev &d, Chain c0, Chain c1, int nchains) {
+  Sync *sy = d.sync;
+  const int L = d.seg, W = d.warm;
+  const int nseg0 = c0.nseg, nseg1 = nchains > 1 ? c1.nseg : 0;
+  const int nsegt = nseg0 + nseg1;
+  // ---- F1
+  for (int g = gtid(); g < nsegt; g += gthreads()) {
+    if (g < nseg0) chain_f1(c0, g, L, W);
+    else chain_f1(c1, g - nseg0, L, W);
+  }
+  // ---- F2 rounds (end-state buffers alternate 0 -> 1 -> 0 ...)
+  int cur = 0;
+  bool settled = false;
+  for (int round = 0; round < kMaxRounds; ++round) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      if (round == 0) sy->iout[0] = 0;
+      sy->iout[(round + 1) % 3] = 0;
+    }
+    if (!grid_sync(sy)) return false;
+    int any = 0;
+    for (int g = gtid(); g < nsegt; g += gthreads()) {
+      const Chain &c = g < nseg0 ? c0 : c1;
+      int s = g < nseg0 ? g : g - nseg0;
+      double *eo = const_cast<double *>(ef_buf(c, cur ^ 1));
+      if (chain_f2(c, s, L, ef_buf(c, cur), eo)) any = 1;
+    }
+    if (any) atomicOr(&sy->iout[round % 3], 1);
+    if (!grid_sync(sy)) return false;
+    int ch = cuda::atomic_ref<int, cuda::thread_scope_device>(sy->iout[round % 3])
+                 .load(cuda::memory_order_acquire);
+    cur ^= 1;
+    if (!ch) {
+      settled = true;
+      break;
+    }
+  }
+  if (!settled) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      chain_sequential(c0);
+      if (nchains > 1) chain_sequential(c1);
+      atomicAdd(&sy->fallback, 1);
+    }
+    if (!grid_sync(sy)) return false;
+    return true;  // sequential pass produced a3p, bp and x
+  }
+  // ---- B1
+  for (int g = gtid(); g < nsegt; g += gthreads()) {
+    if (g < nseg0) {
+      Chain c = c0;
+      c.eb = const_cast<double *>(eb_buf(c0, 0));
+      chain_b1(c, g, L, W);
+    } else {
+      Chain c = c1;
+      c.eb = const_cast<double *>(eb_buf(c1, 0));
+      chain_b1(c, g - nseg0, L, W);
+    }
+  }
+  cur = 0;
+  settled = false;
+  for (int round = 0; round < kMaxRounds; ++round) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      if (round == 0) sy->iout[3] = 0;
+      sy->iout[3 + (round + 1) % 3] = 0;
+    }
+    if (!grid_sync(sy)) return false;
+    int any = 0;
+    for (int g = gtid(); g < nsegt; g += gthreads()) {
+      const Chain &c = g < nseg0 ? c0 : c1;
+      int s = g < nseg0 ? g : g - nseg0;
+      if (chain_b2(c, s, L, eb_buf(c, cur), const_cast<double *>(eb_buf(c, cur ^ 1)))) any = 1;
+    }
+    if (any) atomicOr(&sy->iout[3 + round % 3], 1);
+    if (!grid_sync(sy)) return false;
+    int ch = cuda::atomic_ref<int, cuda::thread_scope_device>(sy->iout[3 + round % 3])
+                 .load(cuda::memory_order_acquire);
+    cur ^= 1;
+    if (!ch) {
+      settled = true;
+      break;
+    }
+  }
+  if (!settled) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      // forward values are exact here; redo the back substitution serially
+      for (int t = 0; t < nchains; ++t) {
+        const Chain &c = t == 0 ? c0 : c1;
+        double xn = c.bp[c.n - 1];
+        c.x[c.n - 1] = xn;
+        for (int k = c.n - 2; k >= 0; --k) {
+          xn = c.bp[k] - c.a3p[k] * xn;
+          c.x[k] = xn;
+        }
+      }
+      atomicAdd(&sy->fallback, 1);
+    }
+    if (!grid_sync(sy)) return false;
+  }
+  return true;
+}
+
+}  // namespace w2

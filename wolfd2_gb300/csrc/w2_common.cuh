@@ -1,0 +1,216 @@
+// w2_common.cuh -- device-side context, bounded grid barrier and reductions
+// shared by every persistent kernel of the wolfd2 GB300 time step.
+//
+// Field layout on the device: REAL*8 (0:nx+1, 0:ny+1) with i fastest and a
+// padded leading dimension ld (a multiple of 32 elements, so every row starts
+// on a 256-byte boundary).  Element (i,j) lives at i + j*ld.  Work arrays that
+// the reference keeps as static locals are allocated zeroed once and reused,
+// which gives the same "never written => 0" entries the reference reads
+// (for example cj1(nx+1,j) in momentum.f:374).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cuda/atomic>
+
+#include "../../include/wolfd2_gpu.h"
+
+namespace w2 {
+
+// Bits of the per-cell mask, built on the host from the region tables by
+// replaying the reference's region loops.
+enum : uint16_t {
+  MK_XID = 1u << 0,   // X split-2 identity row   (momentum.f:444-496)
+  MK_YID = 1u << 1,   // Y split-2 identity row   (momentum.f:770-821)
+  MK_PU = 1u << 2,    // Project updates u(i,j)   (utility.f:301-366)
+  MK_PV = 1u << 3,    // Project updates v(i,j)   (utility.f:371-437)
+  MK_PID = 1u << 4,   // PPE identity row         (pressure.f:109-196)
+  MK_DIVZ = 1u << 5,  // div(i,j) zeroed          (pressure.f:109-196)
+  MK_FU = 1u << 6,    // Filter u at (i,j)        (utility.f:79-140)
+  MK_FV = 1u << 7,    // Filter v at (i,j)        (utility.f:142-204)
+};
+
+// Metric arrays (grid.f:368-535), device copies in the padded layout.
+struct Metrics {
+  const double *ran, *rbn, *rgn, *rac, *rbc, *rgc, *rau, *rbu, *rbv, *rgv;
+  const double *dju, *djv, *djc, *djn;
+  const double *xen, *yen, *xzn, *yzn, *xec, *yec, *xzc, *yzc;
+  const double *xeu, *yeu, *xzv, *yzv, *xzu, *yzu, *xev, *yev;
+};
+
+// Region tables, Fortran layout (include/wolfd2.h, src/main.f:211-239).
+struct Regions {
+  int nri, nrj, mgri, mgrj;
+  const int *brd;     // nRegBrd(mgri,mgrj,4)
+  const int *rtype;   // nRegType(mgri,mgrj)
+  const int *btype;   // nMomBdTp(mgri,mgrj,4)
+  const double *bcv;  // dBCVal(mgri,mgrj,4,4)
+  __device__ __forceinline__ int B(int ir, int jr, int s) const {
+    return brd[(ir - 1) + (jr - 1) * mgri + (s - 1) * mgri * mgrj];
+  }
+  __device__ __forceinline__ int RT(int ir, int jr) const {
+    return rtype[(ir - 1) + (jr - 1) * mgri];
+  }
+  __device__ __forceinline__ int BT(int ir, int jr, int s) const {
+    return btype[(ir - 1) + (jr - 1) * mgri + (s - 1) * mgri * mgrj];
+  }
+  __device__ __forceinline__ double BV(int ir, int jr, int s, int var) const {
+    return bcv[(ir - 1) + (jr - 1) * mgri + (s - 1) * mgri * mgrj +
+               (var - 1) * mgri * mgrj * 4];
+  }
+};
+
+// A concatenated tridiagonal chain solved by AltTridLU semantics
+// (momentum.f:1307-1339): forward elimination over all n rows in order,
+// row 1's super-diagonal divided by row 2's original diagonal.
+struct Chain {
+  int n;           // rows
+  int nseg;        // segments of length seg
+  double *a1, *a2, *a3, *b;        // sub, diag, super, rhs
+  const uint8_t *bzero;            // rows whose rhs is forced to 0 (or null)
+  double *a3p, *bp, *x;            // factorised super, forward rhs, solution
+  double *ef;      // forward end states: 2 per segment x 2 buffers
+  double *eb;      // backward end states: 1 per segment x 2 buffers
+};
+
+// Grid-wide synchronisation state in device memory.
+struct Sync {
+  unsigned int count;
+  unsigned int gen;
+  int error;          // sticky W2_E_* code
+  int changed;        // chain verification rounds: "some segment moved"
+  int fallback;       // chain recurrence needed a sequential pass
+  int pad0;
+  int halt;           // a step diverged: later stages of the run are skipped
+  int pad1;
+  unsigned long long red[16];  // max-reductions (bit patterns of doubles >= 0):
+                               // [0..2] momentum ring, [3..5] PPE ring,
+                               // [6..8] step norms, [9..] scratch
+  int iout[8];                 // chain verification flags ([0..2] fwd, [3..5] bwd)
+  double dout[8];              // small double results
+};
+
+struct Dev {
+  int nx, ny, ld;
+  Metrics m;
+  Regions r;
+  const uint16_t *mask;
+  // fields of the device-resident time loop
+  double *u, *v, *p, *un, *vn, *pn, *us, *vs;
+  // momentum work arrays (X: cj1x..c2nx; Y: cj1y..c2ny)
+  double *cj1x, *cj2x, *c1sx, *c2sx, *c1nx, *c2nx;
+  double *cj1y, *cj2y, *c1sy, *c2sy, *c1ny, *c2ny;
+  Chain x1, x2, y1, y2;
+  // PPE: coefficients a(ind,1..5) and rhs/divergence, field layout
+  double *pa1, *pa2, *pa3, *pa4, *pa5;
+  double *div, *pb, *ppn;
+  double *la3p, *lbp;  // line-solver scratch (field layout)
+  double *qh;          // filter scratch
+  Sync *sync;
+  int seg, warm;       // chain segment length and warm-up rows
+  int has_outflow;     // any OUTLT1/OUTLT2 face (VelOutflowBCs not a no-op)
+};
+
+__device__ __forceinline__ size_t IX(const Dev &d, int i, int j) {
+  return (size_t)i + (size_t)j * (size_t)d.ld;
+}
+
+__device__ __forceinline__ unsigned long long gtime_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Time limit of every device-side wait.
+constexpr unsigned long long kWaitLimitNs = 4000000000ull;
+
+__device__ __forceinline__ void set_error(Sync *s, int code) {
+  atomicCAS(&s->error, 0, code);
+}
+
+__device__ __forceinline__ int read_error(Sync *s) {
+  return cuda::atomic_ref<int, cuda::thread_scope_device>(s->error).load(
+      cuda::memory_order_acquire);
+}
+
+// Grid barrier with a time limit.  All blocks of a cooperative launch call
+// it the same number of times.  On timeout the sticky error is set and every
+// caller returns false; callers then leave the kernel.
+__device__ __noinline__ bool grid_sync(Sync *s) {
+  __shared__ int ok;
+  __syncthreads();
+  if (gridDim.x == 1) {
+    if (threadIdx.x == 0) ok = (read_error(s) == 0);
+    __syncthreads();
+    return ok;
+  }
+  if (threadIdx.x == 0) {
+    cuda::atomic_ref<unsigned, cuda::thread_scope_device> gen(s->gen), cnt(s->count);
+    __threadfence();
+    unsigned g = gen.load(cuda::memory_order_acquire);
+    unsigned a = cnt.fetch_add(1u, cuda::memory_order_acq_rel);
+    if (a == gridDim.x - 1) {
+      cnt.store(0u, cuda::memory_order_relaxed);
+      gen.fetch_add(1u, cuda::memory_order_acq_rel);
+    } else {
+      unsigned long long t0 = gtime_ns();
+      unsigned spins = 0;
+      while (gen.load(cuda::memory_order_acquire) == g) {
+        if ((++spins & 31u) == 0) {
+          if (read_error(s) != 0) break;
+          if (gtime_ns() - t0 > kWaitLimitNs) {
+            set_error(s, W2_E_TIMEOUT);
+            break;
+          }
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    ok = (read_error(s) == 0);
+  }
+  __syncthreads();
+  return ok;
+}
+
+// Block-wide max of non-negative doubles, then one atomicMax per block on the
+// IEEE bit pattern (order-preserving for values >= 0, so the max is exact).
+__device__ __forceinline__ unsigned long long dbits(double x) {
+  return (unsigned long long)__double_as_longlong(x);
+}
+
+__device__ __noinline__ void block_max_to(unsigned long long *slot, double v) {
+  __shared__ unsigned long long wmax[32];
+  unsigned long long b = dbits(v);
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long t = __shfl_down_sync(0xffffffffu, b, o);
+    b = t > b ? t : b;
+  }
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) wmax[w] = b;
+  __syncthreads();
+  if (w == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    b = lane < nw ? wmax[lane] : 0ull;
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long t = __shfl_down_sync(0xffffffffu, b, o);
+      b = t > b ? t : b;
+    }
+    if (lane == 0 && b != 0ull) atomicMax(slot, b);
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ double slot_value(const unsigned long long *slot) {
+  unsigned long long b = cuda::atomic_ref<const unsigned long long, cuda::thread_scope_device>(*slot)
+                             .load(cuda::memory_order_relaxed);
+  return __longlong_as_double((long long)b);
+}
+
+// Max helper matching the reference's dmax1/max on non-NaN values.
+__device__ __forceinline__ double dmax(double a, double b) { return b > a ? b : a; }
+
+__device__ __forceinline__ int gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ int gthreads() { return gridDim.x * blockDim.x; }
+
+}  // namespace w2

@@ -1,0 +1,311 @@
+// w2_kernels.cuh -- __global__ entry points of the plain FP64 path.
+#pragma once
+#include "w2_bc.cuh"
+#include "w2_momentum.cuh"
+#include "w2_ppe.cuh"
+
+namespace w2 {
+
+constexpr int kMaxThreads = 512;
+
+// Per-launch step record written by the kernels.
+struct StepOut {
+  int nql, nsor;
+  double dif[4];
+};
+
+// ---- grid metrics (grid.f:258-535) ------------------------------------
+__global__ void k_mirror(Dev d, double *x, double *y) {
+  const int nx = d.nx, ny = d.ny;
+#define X(i, j) x[IX(d, i, j)]
+#define Y(i, j) y[IX(d, i, j)]
+  for (int i = 1 + threadIdx.x; i <= nx; i += blockDim.x) {
+    X(i, 0) = 2.0 * X(i, 1) - X(i, 2);
+    X(i, ny + 1) = 2.0 * X(i, ny) - X(i, ny - 1);
+    Y(i, 0) = 2.0 * Y(i, 1) - Y(i, 2);
+    Y(i, ny + 1) = 2.0 * Y(i, ny) - Y(i, ny - 1);
+  }
+  for (int j = 1 + threadIdx.x; j <= ny; j += blockDim.x) {
+    X(0, j) = 2.0 * X(1, j) - X(2, j);
+    X(nx + 1, j) = 2.0 * X(nx, j) - X(nx - 1, j);
+    Y(0, j) = 2.0 * Y(1, j) - Y(2, j);
+    Y(nx + 1, j) = 2.0 * Y(nx, j) - Y(nx - 1, j);
+  }
+  if (threadIdx.x == 0) {
+    X(0, 0) = 2.0 * X(1, 1) - X(2, 2);
+    Y(0, 0) = 2.0 * Y(1, 1) - Y(2, 2);
+    X(0, ny + 1) = 2.0 * X(1, ny) - X(2, ny - 1);
+    Y(0, ny + 1) = 2.0 * Y(1, ny) - Y(2, ny - 1);
+    X(nx + 1, 0) = 2.0 * X(nx, 1) - X(nx - 1, 2);
+    Y(nx + 1, 0) = 2.0 * Y(nx, 1) - Y(nx - 1, 2);
+    X(nx + 1, ny + 1) = 2.0 * X(nx, ny) - X(nx - 1, ny - 1);
+    Y(nx + 1, ny + 1) = 2.0 * Y(nx, ny) - Y(nx - 1, ny - 1);
+  }
+}
+
+__global__ void k_fullgrid_uv(Dev d, const double *x, const double *y, double *xu, double *yu,
+                              double *xv, double *yv) {
+  const int nx = d.nx, ny = d.ny, W = nx + 2, H = ny + 2;
+  for (int t = gtid(); t < W * H; t += gthreads()) {
+    const int i = t % W, j = t / W;
+    const size_t o = IX(d, i, j);
+    if (j >= 1) {
+      xu[o] = 0.5 * (x[o] + x[IX(d, i, j - 1)]);
+      yu[o] = 0.5 * (y[o] + y[IX(d, i, j - 1)]);
+    }
+    if (i >= 1) {
+      xv[o] = 0.5 * (x[o] + x[IX(d, i - 1, j)]);
+      yv[o] = 0.5 * (y[o] + y[IX(d, i - 1, j)]);
+    }
+  }
+}
+
+__global__ void k_fullgrid_c(Dev d, const double *xu, const double *yv, double *xc, double *yc) {
+  const int nx = d.nx, ny = d.ny;
+  for (int t = gtid(); t < (nx + 1) * (ny + 1); t += gthreads()) {
+    const int i = t % (nx + 1) + 1, j = t / (nx + 1) + 1;
+    const size_t o = IX(d, i, j);
+    xc[o] = 0.5 * (xu[o] + xu[IX(d, i - 1, j)]);
+    yc[o] = 0.5 * (yv[o] + yv[IX(d, i, j - 1)]);
+  }
+}
+
+struct MetricOut {
+  double *ran, *rbn, *rgn, *rac, *rbc, *rgc, *rau, *rbu, *rbv, *rgv;
+  double *dju, *djv, *djc, *djn;
+  double *xen, *yen, *xzn, *yzn, *xec, *yec, *xzc, *yzc;
+  double *xeu, *yeu, *xzv, *yzv, *xzu, *yzu, *xev, *yev;
+};
+
+__global__ void k_metric(Dev d, MetricOut m, const double *xn, const double *yn, const double *xu,
+                         const double *yu, const double *xv, const double *yv, const double *xc,
+                         const double *yc) {
+  const int nx = d.nx, ny = d.ny;
+  for (int t = gtid(); t < nx * ny; t += gthreads()) {
+    const int i = t % nx + 1, j = t / nx + 1;
+    const size_t o = IX(d, i, j);
+    double g11, g12, g22;
+    // natural points (N), grid.f:425-448
+    m.xzn[o] = xv[IX(d, i + 1, j)] - xv[o];
+    m.xen[o] = xu[IX(d, i, j + 1)] - xu[o];
+    m.yzn[o] = yv[IX(d, i + 1, j)] - yv[o];
+    m.yen[o] = yu[IX(d, i, j + 1)] - yu[o];
+    m.djn[o] = 1.0 / (m.xzn[o] * m.yen[o] - m.xen[o] * m.yzn[o]);
+    g11 = m.xzn[o] * m.xzn[o] + m.yzn[o] * m.yzn[o];
+    g12 = m.xzn[o] * m.xen[o] + m.yzn[o] * m.yen[o];
+    g22 = m.xen[o] * m.xen[o] + m.yen[o] * m.yen[o];
+    m.ran[o] = m.djn[o] * g22;
+    m.rbn[o] = -m.djn[o] * g12 * 0.25;
+    m.rgn[o] = m.djn[o] * g11;
+    // U cells, grid.f:451-477
+    m.xzu[o] = xc[IX(d, i + 1, j)] - xc[o];
+    m.xeu[o] = xn[o] - xn[IX(d, i, j - 1)];
+    m.yzu[o] = yc[IX(d, i + 1, j)] - yc[o];
+    m.yeu[o] = yn[o] - yn[IX(d, i, j - 1)];
+    m.dju[o] = 1.0 / (m.xzu[o] * m.yeu[o] - m.xeu[o] * m.yzu[o]);
+    g12 = m.xzu[o] * m.xeu[o] + m.yzu[o] * m.yeu[o];
+    g22 = m.xeu[o] * m.xeu[o] + m.yeu[o] * m.yeu[o];
+    m.rau[o] = m.dju[o] * g22;
+    m.rbu[o] = -m.dju[o] * g12 * 0.25;
+    // V cells, grid.f:480-506
+    m.xzv[o] = xn[o] - xn[IX(d, i - 1, j)];
+    m.xev[o] = xc[IX(d, i, j + 1)] - xc[o];
+    m.yzv[o] = yn[o] - yn[IX(d, i - 1, j)];
+    m.yev[o] = yc[IX(d, i, j + 1)] - yc[o];
+    m.djv[o] = 1.0 / (m.xzv[o] * m.yev[o] - m.xev[o] * m.yzv[o]);
+    g11 = m.xzv[o] * m.xzv[o] + m.yzv[o] * m.yzv[o];
+    g12 = m.xzv[o] * m.xev[o] + m.yzv[o] * m.yev[o];
+    m.rbv[o] = -m.djv[o] * g12 * 0.25;
+    m.rgv[o] = m.djv[o] * g11;
+    // P cells, grid.f:509-532
+    m.xzc[o] = xu[o] - xu[IX(d, i - 1, j)];
+    m.xec[o] = xv[o] - xv[IX(d, i, j - 1)];
+    m.yzc[o] = yu[o] - yu[IX(d, i - 1, j)];
+    m.yec[o] = yv[o] - yv[IX(d, i, j - 1)];
+    m.djc[o] = 1.0 / (m.xzc[o] * m.yec[o] - m.xec[o] * m.yzc[o]);
+    g11 = m.xzc[o] * m.xzc[o] + m.yzc[o] * m.yzc[o];
+    g12 = m.xzc[o] * m.xec[o] + m.yzc[o] * m.yec[o];
+    g22 = m.xec[o] * m.xec[o] + m.yec[o] * m.yec[o];
+    m.rac[o] = m.djc[o] * g22;
+    m.rbc[o] = -m.djc[o] * g12 * 0.25;
+    m.rgc[o] = m.djc[o] * g11;
+  }
+#undef X
+#undef Y
+}
+
+__global__ void k_ppe_coef(Dev d) { ppe_coefficients(d); }
+
+// ---- field copies -------------------------------------------------------
+__global__ void k_copy3(Dev d, double *a, const double *a0, double *b, const double *b0,
+                        double *c, const double *c0) {
+  if (d.sync->halt) return;
+  const int W = d.nx + 2, H = d.ny + 2;
+  for (int t = gtid(); t < W * H; t += gthreads()) {
+    const size_t o = IX(d, t % W, t / W);
+    a[o] = a0[o];
+    b[o] = b0[o];
+    if (c) c[o] = c0[o];
+  }
+}
+
+// us(1..nx+1,1..ny+1) = un, vs = vn (momentum.f:114-119)
+__global__ void k_naux_init(Dev d, const double *un, const double *vn, double *us, double *vs) {
+  const int W = d.nx + 1, H = d.ny + 1;
+  for (int t = gtid(); t < W * H; t += gthreads()) {
+    const size_t o = IX(d, t % W + 1, t / W + 1);
+    us[o] = un[o];
+    vs[o] = vn[o];
+  }
+}
+
+// ---- nAuxMomentum --------------------------------------------------------
+__global__ void __launch_bounds__(kMaxThreads) k_naux(Dev d, int mqiter, double dk, double re,
+                                                      double qtol, const double *un,
+                                                      const double *vn, double *us, double *vs,
+                                                      StepOut *out) {
+  if (d.sync->halt) return;
+  int res = -1;
+  if (!naux_momentum(d, mqiter, dk, re, qtol, un, vn, us, vs, &res)) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) out->nql = res;
+}
+
+// ---- boundary programs (one block) -------------------------------------
+enum : int { BC_VEL = 1, BC_PRES = 2, BC_OUTFLOW = 4 };
+
+__global__ void k_bc(Dev d, int ops, double *u, double *v, double *p) {
+  if (d.sync->halt) return;
+  bool ok = true;
+  if (ops & BC_OUTFLOW) ok = ok && vel_outflow_bcs_block(d, u, v);
+  if (ops & BC_VEL) ok = ok && vel_bound_cond_block(d, u, v);
+  if (ops & BC_PRES) ok = ok && pres_bound_cond_block(d, p);
+  if (!ok && threadIdx.x == 0) set_error(d.sync, W2_E_BCFLAG);
+}
+
+// ---- Ppe -----------------------------------------------------------------
+// Multi-block form (solvers 3, 4, 5, 6) and single-block form (1, 2).
+__global__ void __launch_bounds__(kMaxThreads) k_ppe(Dev d, int lcartes, int npsolver, int msorit,
+                                                     double dk, double sortol, double sorrel,
+                                                     const double *u, const double *v, double *p,
+                                                     StepOut *out) {
+  if (d.sync->halt) return;
+  Sync *sy = d.sync;
+  ppe_divergence(d, u, v);
+  if (!grid_sync(sy)) return;
+  if (lcartes) {
+    ppe_rhs_grid(d, lcartes, dk, p);
+    if (!grid_sync(sy)) return;
+  }
+  int nconv = 0;
+  if (npsolver == 1 || npsolver == 2) {
+    if (blockIdx.x == 0) {
+      nconv = npsolver == 1 ? sor_lex_block(d, p, lcartes, msorit, dk, sortol, sorrel)
+                            : slor_block(d, p, lcartes, msorit, dk, sortol, sorrel);
+    }
+  } else if (npsolver >= 3 && npsolver <= 6) {
+    nconv = ppe_parallel(d, p, npsolver, lcartes, msorit, dk, sortol, sorrel);
+    if (nconv < 0) return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? msorit : nconv;
+}
+
+// ---- Project (utility.f:253-440), masked -------------------------------
+__device__ void project_grid(const Dev &d, double dk, const double *p, double *u, double *v) {
+  const int nx = d.nx, ny = d.ny, W = nx + 2, H = ny + 2;
+  const Metrics &m = d.m;
+  for (int t = gtid(); t < W * H; t += gthreads()) {
+    const int i = t % W, j = t / W;
+    const size_t o = IX(d, i, j);
+    const uint16_t mk = d.mask[o];
+    if (mk & MK_PU) {
+      const double pzi = p[IX(d, i + 1, j)] - p[o];
+      const double pet = (p[IX(d, i + 1, j + 1)] + p[IX(d, i, j + 1)] - p[IX(d, i + 1, j - 1)] -
+                          p[IX(d, i, j - 1)]) / 4.0;
+      const double djk = m.dju[o] * dk;
+      u[o] = u[o] - djk * (m.yeu[o] * pzi - m.yzu[o] * pet);
+    }
+    if (mk & MK_PV) {
+      const double pzi = (p[IX(d, i + 1, j + 1)] + p[IX(d, i + 1, j)] - p[IX(d, i - 1, j + 1)] -
+                          p[IX(d, i - 1, j)]) / 4.0;
+      const double pet = p[IX(d, i, j + 1)] - p[o];
+      const double djk = m.djv[o] * dk;
+      v[o] = v[o] - djk * (-m.xev[o] * pzi + m.xzv[o] * pet);
+    }
+  }
+}
+
+__global__ void k_project(Dev d, double dk, const double *p, double *u, double *v) {
+  if (d.sync->halt) return;
+  project_grid(d, dk, p, u, v);
+}
+
+// DiffMaxNorm (utility.f:446-473) into red[slot]
+__device__ double diff_norm_local(const Dev &d, const double *a, const double *b) {
+  const int nx = d.nx, ny = d.ny;
+  double mx = 0.0;
+  for (int t = gtid(); t < (nx - 2) * (ny - 2); t += gthreads()) {
+    const int i = t % (nx - 2) + 2, j = t / (nx - 2) + 2;
+    const size_t o = IX(d, i, j);
+    mx = dmax(mx, fabs(a[o] - b[o]));
+  }
+  if (gtid() == 0) mx = dmax(mx, fabs(a[IX(d, 2, 2)] - b[IX(d, 2, 2)]));
+  return mx;
+}
+
+__global__ void k_diff_norm(Dev d, const double *a, const double *b, unsigned long long *slot) {
+  block_max_to(slot, diff_norm_local(d, a, b));
+}
+
+// Tail of one step, main.f:813-972: PresBoundCond, Project, boundary
+// conditions of the starred and new fields, the three step norms and the
+// divergence guard.
+__global__ void __launch_bounds__(kMaxThreads) k_step_post(Dev d, double dk, double *p,
+                                                           const double *pn, const double *un,
+                                                           const double *vn, double *u,
+                                                           double *v, StepOut *out) {
+  if (d.sync->halt) return;
+  Sync *sy = d.sync;
+  if (blockIdx.x == 0) {
+    if (!pres_bound_cond_block(d, p) && threadIdx.x == 0) set_error(sy, W2_E_BCFLAG);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) sy->red[6] = sy->red[7] = sy->red[8] = 0ull;
+  if (!grid_sync(sy)) return;
+  project_grid(d, dk, p, u, v);
+  if (!grid_sync(sy)) return;
+  if (blockIdx.x == 0) {
+    bool ok = vel_bound_cond_block(d, u, v) && pres_bound_cond_block(d, p);
+    // u = us etc. (main.f:864-870) is a buffer swap on the host; then
+    // main.f:946-953 applies the conditions again to the new level.
+    ok = ok && vel_bound_cond_block(d, u, v) && pres_bound_cond_block(d, p);
+    if (!ok && threadIdx.x == 0) set_error(sy, W2_E_BCFLAG);
+  }
+  if (!grid_sync(sy)) return;
+  block_max_to(&sy->red[6], diff_norm_local(d, pn, p));
+  block_max_to(&sy->red[7], diff_norm_local(d, un, u));
+  block_max_to(&sy->red[8], diff_norm_local(d, vn, v));
+  if (!grid_sync(sy)) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    out->dif[0] = slot_value(&sy->red[6]);
+    out->dif[1] = slot_value(&sy->red[7]);
+    out->dif[2] = slot_value(&sy->red[8]);
+    out->dif[3] = 0.0;
+    double mx = dmax(dmax(out->dif[0], out->dif[1]), out->dif[2]);
+    if (mx > 1.0e12) sy->halt = 1;
+  }
+}
+
+// ---- Filter (utility.f:33-247), velocity components ---------------------
+__global__ void k_filter(Dev d, int bit, double fp, const double *qu, double *qh) {
+  const int W = d.nx + 2, H = d.ny + 2;
+  for (int t = gtid(); t < W * H; t += gthreads()) {
+    const int i = t % W, j = t / W;
+    const size_t o = IX(d, i, j);
+    if (d.mask[o] & bit)
+      qh[o] = (qu[IX(d, i, j - 1)] + qu[IX(d, i - 1, j)] + qu[IX(d, i, j + 1)] + qu[IX(d, i + 1, j)] +
+               fp * qu[o]) / (fp + 4.0);
+    else
+      qh[o] = qu[o];
+  }
+}
+
+}  // namespace w2

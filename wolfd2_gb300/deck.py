@@ -1,0 +1,503 @@
+"""Host-side case setup: region tables, boundary-condition tables and run
+parameters in the reference's own Fortran layouts.
+
+This mirrors the part of the reference's input layer that produces the hot
+path's inputs:
+
+* ``boundary_conditions`` keywords ``number_of_regions``, ``i_borders``,
+  ``j_borders``, ``wall``, ``inlet``, ``outlet``, ``blockage`` and ``porous_region``
+  (src/parse.f:1005-1950), defaults from ``InitBCFlags`` (src/parse.f:2257-2380);
+* the region-border fill and boundary-type consistency passes of
+  ``SetUpBCs`` (src/bound_cond.f:123-223) and the porous constants of
+  ``PorRegCnst`` (src/bound_cond.f:1883-1986);
+* the input-parameter defaults (src/parse.f:117-193) and the
+  Reynolds/Froude/time-step scaling of ``ReadParam``
+  (src/file_manip.f:130-157).
+
+Tables are numpy arrays with Fortran (column-major) order and the
+reference's shapes (mgri=20, mgrj=10 from include/config.f), so the same
+buffers can be handed to the C-ABI exactly as the Fortran driver would.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+# include/config.f:19-26
+MGRI = 20
+MGRJ = 10
+
+# include/wolfd2.h:15-60
+RM_BLOCKG, RM_INTERN, RM_POROUS = 0, 1, 2
+BM_INTERN, BM_WALL1, BM_WALL2, BM_INLET, BM_OUTLT1, BM_OUTLT2 = 0, 1, 2, 3, 4, 5
+WEST, EAST, SOUTH, NORTH = 1, 2, 3, 4
+VAR_U, VAR_V, VAR_P, VAR_T = 1, 2, 3, 4
+
+# ppe_solver keywords, src/parse.f:449-460
+PPE_SOLVERS = {"sor": 1, "lsor": 2, "rb_lsor": 3, "par_rb_lsor": 4,
+               "rb_sor": 5, "par_rb_sor": 6}
+
+_FACES = {"w": WEST, "west": WEST, "e": EAST, "east": EAST,
+          "s": SOUTH, "south": SOUTH, "n": NORTH, "north": NORTH}
+
+
+@dataclasses.dataclass
+class Regions:
+    """Region/boundary tables in Fortran layout (1-based meaning, 0-based
+    storage: element (ireg,jreg,face) lives at [ireg-1, jreg-1, face-1])."""
+    nReg: np.ndarray          # int32 (2,)
+    nRegBrd: np.ndarray       # int32 (mgri, mgrj, 4)
+    nRegType: np.ndarray      # int32 (mgri, mgrj)
+    nMomBdTp: np.ndarray      # int32 (mgri, mgrj, 4)
+    dBCVal: np.ndarray        # float64 (mgri, mgrj, 4, 4)
+    dPRporos: np.ndarray      # float64 (mgri, mgrj)
+    dPRporc1: np.ndarray
+    dPRporc2: np.ndarray
+
+    @property
+    def n_i(self) -> int:
+        return int(self.nReg[0])
+
+    @property
+    def n_j(self) -> int:
+        return int(self.nReg[1])
+
+    def border(self, ireg: int, jreg: int, face: int) -> int:
+        return int(self.nRegBrd[ireg - 1, jreg - 1, face - 1])
+
+    def btype(self, ireg: int, jreg: int, face: int) -> int:
+        return int(self.nMomBdTp[ireg - 1, jreg - 1, face - 1])
+
+    def rtype(self, ireg: int, jreg: int) -> int:
+        return int(self.nRegType[ireg - 1, jreg - 1])
+
+
+def _empty_tables() -> Regions:
+    f = dict(order="F")
+    return Regions(
+        nReg=np.zeros(2, np.int32),
+        nRegBrd=np.zeros((MGRI, MGRJ, 4), np.int32, **f),
+        nRegType=np.zeros((MGRI, MGRJ), np.int32, **f),
+        nMomBdTp=np.zeros((MGRI, MGRJ, 4), np.int32, **f),
+        dBCVal=np.zeros((MGRI, MGRJ, 4, 4), np.float64, **f),
+        dPRporos=np.zeros((MGRI, MGRJ), np.float64, **f),
+        dPRporc1=np.zeros((MGRI, MGRJ), np.float64, **f),
+        dPRporc2=np.zeros((MGRI, MGRJ), np.float64, **f),
+    )
+
+
+class DeckError(ValueError):
+    """A boundary-condition or parameter deck the reference would reject."""
+
+
+def _init_bc_flags(t: Regions) -> None:
+    """InitBCFlags, src/parse.f:2257-2380 (momentum part)."""
+    ni, nj = t.n_i, t.n_j
+    t.dBCVal[:ni, :nj, :, :] = 0.0
+    t.nRegType[:ni, :nj] = RM_INTERN
+    t.nMomBdTp[:ni, :nj, :] = BM_INTERN
+    t.nMomBdTp[0, :nj, WEST - 1] = BM_WALL1
+    t.nMomBdTp[ni - 1, :nj, EAST - 1] = BM_WALL1
+    t.nMomBdTp[:ni, 0, SOUTH - 1] = BM_WALL1
+    t.nMomBdTp[:ni, nj - 1, NORTH - 1] = BM_WALL1
+
+
+def parse_bc_section(text: str, nx: int, ny: int, *, uref: float = 1.0,
+                     densref: float = 1.0, dlref: float = 1.0,
+                     re: float = 1.0) -> Regions:
+    """Parse a ``boundary_conditions`` section body (lines between
+    ``section boundary_conditions`` and ``end section``) and run the
+    ``SetUpBCs`` passes.  Keywords are case-insensitive; ``#`` starts a
+    comment (src/parse.f:1168-1210)."""
+    t = _empty_tables()
+    found_nreg = def_i = def_j = False
+    perm_eq = np.zeros((MGRI, MGRJ), np.int32, order="F")
+    dim_coef = np.zeros((MGRI, MGRJ, 3), np.float64, order="F")
+
+    def need_ij(words: List[str], k: int) -> Tuple[int, int]:
+        try:
+            ir, jr = int(words[k]), int(words[k + 1])
+        except (IndexError, ValueError) as exc:
+            raise DeckError(f"expected region indices in {' '.join(words)!r}") from exc
+        if not (1 <= ir <= MGRI and 1 <= jr <= MGRJ):
+            raise DeckError(f"region index out of range: {ir},{jr}")
+        return ir, jr
+
+    def face_of(word: str) -> int:
+        if word not in _FACES:
+            raise DeckError(f"Unrecognized cell face designation: [{word}]")
+        return _FACES[word]
+
+    for raw in text.splitlines():
+        line = raw.split("#", 1)[0].strip().lower()
+        if not line:
+            continue
+        w = line.split()
+        key = w[0]
+        if key == "number_of_regions":
+            ir, jr = need_ij(w, 1)
+            t.nReg[:] = (ir, jr)
+            found_nreg = True
+        elif key == "i_borders":
+            if not found_nreg:
+                raise DeckError("Error: Number_of_Regions not defined")
+            vals = [int(x) for x in w[1:]]
+            if len(vals) < t.n_i - 1:
+                raise DeckError("i_borders: too few values")
+            for k in range(2, t.n_i + 1):
+                t.nRegBrd[k - 1, 0, WEST - 1] = vals[k - 2]
+            def_i = True
+            if def_j:
+                _init_bc_flags(t)
+        elif key == "j_borders":
+            if not found_nreg:
+                raise DeckError("Error: Number_of_Regions not defined")
+            vals = [int(x) for x in w[1:]]
+            if len(vals) < t.n_j - 1:
+                raise DeckError("j_borders: too few values")
+            for k in range(2, t.n_j + 1):
+                t.nRegBrd[0, k - 1, SOUTH - 1] = vals[k - 2]
+            def_j = True
+            if def_i:
+                _init_bc_flags(t)
+        elif key == "blockage":
+            ir, jr = need_ij(w, 1)
+            t.nRegType[ir - 1, jr - 1] = RM_BLOCKG
+            t.nMomBdTp[ir - 1, jr - 1, :] = BM_WALL1
+            if ir > 1:
+                t.nMomBdTp[ir - 2, jr - 1, EAST - 1] = BM_WALL1
+            if ir < t.n_i:
+                t.nMomBdTp[ir, jr - 1, WEST - 1] = BM_WALL1
+            if jr > 1:
+                t.nMomBdTp[ir - 1, jr - 2, NORTH - 1] = BM_WALL1
+            if jr < t.n_j:
+                t.nMomBdTp[ir - 1, jr, SOUTH - 1] = BM_WALL1
+        elif key == "porous_region":
+            ir, jr = need_ij(w, 1)
+            t.nRegType[ir - 1, jr - 1] = RM_POROUS
+            # permeability equation names, src/parse.f:1422-1432
+            eqs = {"carman-kozeny": 1, "kaviany": 2, "happen-brenner": 3}
+            if len(w) < 7 or w[3] not in eqs:
+                raise DeckError(f"porous: bad syntax {line!r}")
+            perm_eq[ir - 1, jr - 1] = eqs[w[3]]
+            dim_coef[ir - 1, jr - 1, :] = [float(x) for x in w[4:7]]
+        elif key in ("wall", "inlet", "outlet"):
+            ir, jr = need_ij(w, 1)
+            if len(w) < 4:
+                raise DeckError(f"{key}: missing face")
+            face = face_of(w[3])
+            rest = w[4:]
+            i0, j0 = ir - 1, jr - 1
+            if key == "wall":
+                t.nMomBdTp[i0, j0, face - 1] = BM_WALL1
+            elif key == "inlet":
+                t.nMomBdTp[i0, j0, face - 1] = BM_INLET
+                if not rest:
+                    raise DeckError("inlet: needs at least one value")
+            else:
+                t.nMomBdTp[i0, j0, face - 1] = BM_OUTLT2
+            k = 0
+            while k < len(rest):
+                word = rest[k]
+                if key == "wall" and word == "no_slip":
+                    t.nMomBdTp[i0, j0, face - 1] = BM_WALL1
+                elif key == "wall" and word == "no_stress":
+                    t.nMomBdTp[i0, j0, face - 1] = BM_WALL2
+                elif key == "outlet" and word in ("fully_dev", "fd"):
+                    t.nMomBdTp[i0, j0, face - 1] = BM_OUTLT1
+                elif key == "outlet" and word in ("mass_cons", "mc"):
+                    t.nMomBdTp[i0, j0, face - 1] = BM_OUTLT2
+                elif key != "outlet" and word in ("tangent_vel", "tv", "normal_vel", "nv"):
+                    val = float(rest[k + 1]) / uref
+                    normal = word in ("normal_vel", "nv")
+                    if key == "wall" and normal:
+                        raise DeckError("wall: normal velocity not allowed")
+                    ew = face in (WEST, EAST)
+                    var = (VAR_U if ew else VAR_V) if normal else (VAR_V if ew else VAR_U)
+                    t.dBCVal[i0, j0, face - 1, var - 1] = val
+                    k += 1
+                elif key != "inlet" and word in ("press", "p"):
+                    t.dBCVal[i0, j0, face - 1, VAR_P - 1] = float(rest[k + 1]) / (densref * uref * uref)
+                    k += 1
+                elif word in ("temper", "t"):
+                    k += 1  # thermal boundary values: thermal energy is not on this path
+                else:
+                    raise DeckError(f"{key}: unrecognized word {word!r}")
+                k += 1
+        elif key in ("heat_generation_region", "fixed_temperature_region",
+                     "fixed_temperature_wall"):
+            continue  # thermal keywords: accepted, not on the momentum path
+        else:
+            raise DeckError(f"Unrecognized keyword: [{key}]")
+
+    if not (found_nreg and def_i and def_j):
+        raise DeckError("number_of_regions, i_borders and j_borders are required")
+    _setup_bcs(t, nx, ny)
+    _por_reg_cnst(t, perm_eq, dim_coef, dlref, re)
+    return t
+
+
+def _setup_bcs(t: Regions, nx: int, ny: int) -> None:
+    """Border checks, border fill and type consistency,
+    src/bound_cond.f:123-223."""
+    ni, nj = t.n_i, t.n_j
+    B = t.nRegBrd
+    for ir in range(2, ni + 1):
+        b = B[ir - 1, 0, WEST - 1]
+        if b < 2 or b > nx - 2:
+            raise DeckError(f"Bad iRegW index: {b}. Must be >= 2 and <= nx-2.")
+    for ir in range(2, ni):
+        if B[ir, 0, WEST - 1] - B[ir - 1, 0, WEST - 1] < 2:
+            raise DeckError("i borders must increase by at least 2")
+    for jr in range(2, nj + 1):
+        b = B[0, jr - 1, SOUTH - 1]
+        if b < 2 or b > ny - 2:
+            raise DeckError(f"Bad jRegS index: {b}. Must be >= 2 and <= ny-2")
+    for jr in range(2, nj):
+        if B[0, jr, SOUTH - 1] - B[0, jr - 1, SOUTH - 1] < 2:
+            raise DeckError("j borders must increase by at least 2")
+    for jr in range(nj):
+        B[0, jr, WEST - 1] = 1
+        B[ni - 1, jr, EAST - 1] = nx
+    for ir in range(ni):
+        B[ir, 0, SOUTH - 1] = 1
+        B[ir, nj - 1, NORTH - 1] = ny
+    for jr in range(1, nj):
+        for ir in range(1, ni):
+            B[ir, jr, WEST - 1] = B[ir, 0, WEST - 1]
+            B[ir, jr, SOUTH - 1] = B[0, jr, SOUTH - 1]
+    for jr in range(nj):
+        for ir in range(ni - 1):
+            B[ir, jr, EAST - 1] = B[ir + 1, 0, WEST - 1]
+    for jr in range(nj - 1):
+        for ir in range(ni):
+            B[ir, jr, NORTH - 1] = B[0, jr + 1, SOUTH - 1]
+    T = t.nMomBdTp
+    for jr in range(nj):
+        for ir in range(ni - 1):
+            if T[ir, jr, EAST - 1] == BM_INLET:
+                T[ir + 1, jr, WEST - 1] = BM_INLET
+            if T[ir + 1, jr, WEST - 1] == BM_INLET:
+                T[ir, jr, EAST - 1] = BM_INLET
+            if T[ir, jr, EAST - 1] == BM_WALL1:
+                T[ir + 1, jr, WEST - 1] = BM_WALL1
+            if T[ir + 1, jr, WEST - 1] == BM_WALL1:
+                T[ir, jr, EAST - 1] = BM_WALL1
+    for jr in range(nj - 1):
+        for ir in range(ni):
+            if T[ir, jr + 1, SOUTH - 1] == BM_INLET:
+                T[ir, jr, NORTH - 1] = BM_INLET
+            if T[ir, jr, NORTH - 1] == BM_INLET:
+                T[ir, jr + 1, SOUTH - 1] = BM_INLET
+            if T[ir, jr + 1, SOUTH - 1] == BM_WALL1:
+                T[ir, jr, NORTH - 1] = BM_WALL1
+            if T[ir, jr, NORTH - 1] == BM_WALL1:
+                T[ir, jr + 1, SOUTH - 1] = BM_WALL1
+
+
+def _por_reg_cnst(t: Regions, perm_eq, dim_coef, dlref: float, re: float) -> None:
+    """PorRegCnst, src/bound_cond.f:1883-1986."""
+    dpi4 = math.acos(-1.0) / 4.0
+    for jr in range(t.n_j):
+        for ir in range(t.n_i):
+            if t.nRegType[ir, jr] != RM_POROUS:
+                t.dPRporos[ir, jr] = 1.0
+                t.dPRporc1[ir, jr] = 0.0
+                t.dPRporc2[ir, jr] = 0.0
+                continue
+            por, dia, cf = (float(x) for x in dim_coef[ir, jr])
+            if (1.0 - por) < 1.0e-4:
+                por = 0.98
+            eq = int(perm_eq[ir, jr])
+            if eq == 1:
+                perm = (dia ** 2 * por ** 3) / (1.8e2 * (1.0 - por) ** 2)
+            elif eq == 2:
+                perm = 0.0606 * dpi4 * (por ** 5.10) * dia ** 2 / (1.0 - por)
+            elif eq == 3:
+                pors = 1.0 - por
+                pors2 = pors ** 2
+                koz = (2.0 * por ** 3) / pors / (math.log(1.0 / pors) - (1.0 - pors2) / (1.0 + pors2))
+                perm = dia ** 2 * por ** 3 / (16.0 * koz * pors2)
+            else:
+                raise DeckError("Wrong nPermEq flag")
+            t.dPRporos[ir, jr] = float(dim_coef[ir, jr, 0])
+            t.dPRporc1[ir, jr] = (por * dlref ** 2) / (re * perm)
+            t.dPRporc2[ir, jr] = (dlref * cf * por) / math.sqrt(perm)
+
+
+@dataclasses.dataclass
+class RunParams:
+    """Time-loop parameters after ReadParam's scaling (nthermen = 0)."""
+    dk: float                   # dimensionless time step (dk*uref/dlref)
+    re: float
+    fr: float
+    nts: int = 0
+    mqiter: int = 20            # src/parse.f:135-148 defaults
+    qtol: float = 1.0e-4
+    npsolver: int = 1
+    msorit: int = 2000
+    sortol: float = 1.0e-8
+    sorrel: float = 1.0
+    nfiltu: int = 0
+    nfiltv: int = 0
+    fpu: float = 5.0e2
+    fpv: float = 5.0e2
+    lcartes: int = 0
+
+    @staticmethod
+    def scaled(dt: float, dlref: float, uref: float, rho: float, mu: float,
+               **kw) -> "RunParams":
+        """ReadParam scaling, src/file_manip.f:130-157."""
+        kinvisc = mu / rho
+        re = dlref * uref / kinvisc
+        fr = uref ** 2.0 / (dlref * 9.81)
+        return RunParams(dk=dt * uref / dlref, re=re, fr=fr, **kw)
+
+
+@dataclasses.dataclass
+class Case:
+    """Everything the hot path needs for one instance."""
+    name: str
+    nx: int
+    ny: int
+    x: np.ndarray   # node x coordinates, shape (nx, ny), already / dlref
+    y: np.ndarray
+    regions: Regions
+    params: RunParams
+    bc_text: str = ""
+
+    @property
+    def cells(self) -> int:
+        return (self.nx - 1) * (self.ny - 1)
+
+
+def _uniform_nodes(ncx: int, ncy: int, lx: float, ly: float):
+    xi = np.array([lx * i / ncx for i in range(ncx + 1)], np.float64)
+    yj = np.array([ly * j / ncy for j in range(ncy + 1)], np.float64)
+    X = np.repeat(xi[:, None], ncy + 1, axis=1)
+    Y = np.repeat(yj[None, :], ncx + 1, axis=0)
+    return X, Y
+
+
+def cavity(n: int, re: float, dt: float, *, lid: float = 1.0,
+           solver: str = "sor", ny: Optional[int] = None, **kw) -> Case:
+    """Lid-driven cavity on the unit square with n x n uniform cells: no-slip
+    walls, north wall moving at ``lid`` (``wall 1 1 north tv <lid>``), fluid
+    with rho = 1 and mu = 1/re, dlref = uref = 1."""
+    ncy = n if ny is None else ny
+    X, Y = _uniform_nodes(n, ncy, 1.0, float(ncy) / n)
+    nx, nyy = n + 1, ncy + 1
+    bc = ("number_of_regions 1 1\n"
+          "i_borders\n"
+          "j_borders\n"
+          f"wall 1 1 north tv {lid!r}\n")
+    prm = RunParams.scaled(dt, 1.0, 1.0, 1.0, 1.0 / re,
+                           npsolver=PPE_SOLVERS[solver], lcartes=1, **kw)
+    regs = parse_bc_section(bc, nx, nyy, re=prm.re)
+    return Case(f"cavity{n}x{ncy}_re{re:g}", nx, nyy, X, Y, regs, prm, bc)
+
+
+def channel(ncx: int, ncy: int, re: float, dt: float, *, length: float = 4.0,
+            height: float = 1.0, u_in: float = 1.0, solver: str = "rb_sor",
+            **kw) -> Case:
+    """Plane channel: inlet on the west face with normal velocity ``u_in``,
+    fully developed outlet on the east face, no-slip south/north walls."""
+    X, Y = _uniform_nodes(ncx, ncy, length, height)
+    nx, ny = ncx + 1, ncy + 1
+    bc = ("number_of_regions 1 1\n"
+          "i_borders\n"
+          "j_borders\n"
+          f"inlet 1 1 west nv {u_in!r}\n"
+          "outlet 1 1 east fd\n")
+    prm = RunParams.scaled(dt, 1.0, 1.0, 1.0, 1.0 / re,
+                           npsolver=PPE_SOLVERS[solver], lcartes=1, **kw)
+    regs = parse_bc_section(bc, nx, ny, re=prm.re)
+    return Case(f"channel{ncx}x{ncy}_re{re:g}", nx, ny, X, Y, regs, prm, bc)
+
+
+# ---------------------------------------------------------------------------
+# Reference-format files: decks, Plot3D grid, fluid table, restart records.
+# ---------------------------------------------------------------------------
+
+def write_grid_plot3d(path: str, x: np.ndarray, y: np.ndarray) -> None:
+    """2-D formatted Plot3D grid read by ReadGrid (src/grid.f:189-228):
+    first line ``nx ny``, then all x (i fastest), then all y."""
+    nx, ny = x.shape
+    with open(path, "w") as f:
+        f.write(f"{nx} {ny}\n")
+        for arr in (x, y):
+            vals = arr.ravel(order="F")
+            for k in range(0, vals.size, 4):
+                f.write(" ".join(repr(float(v)) for v in vals[k:k + 4]) + "\n")
+
+
+def write_deck(path: str, case: Case, *, grid_file: str = "grid.xyz",
+               nts: int = 1, print_diff: int = 1) -> None:
+    """Input deck with the two sections the reference reads from one file
+    (src/main.f:311-312)."""
+    inv = {v: k for k, v in PPE_SOLVERS.items()}
+    p = case.params
+    with open(path, "w") as f:
+        f.write("section input_parameters\n")
+        f.write(f"  grid_file {grid_file}{' cartesian_grid' if p.lcartes else ''}\n")
+        f.write(f"  n_time_steps {nts}\n")
+        f.write(f"  time_step_size {p.dk!r}\n")
+        f.write(f"  max_ql_iter {p.mqiter}\n  ql_tolerance {p.qtol!r}\n")
+        f.write(f"  ppe_solver {inv[p.npsolver]}\n")
+        f.write(f"  max_sor_iter {p.msorit}\n  sor_tolerance {p.sortol!r}\n")
+        f.write(f"  sor_relaxation {p.sorrel!r}\n")
+        f.write(f"  print_diff_freq {print_diff}\n")
+        f.write("end section\n\n")
+        f.write("section boundary_conditions\n")
+        for line in case.bc_text.splitlines():
+            f.write("  " + line + "\n")
+        f.write("end section\n")
+
+
+def write_fluid_table(path: str, rho: float, mu: float, name: str = "air01") -> None:
+    """Fluid table with two identical rows at T = 200 and 400 so the
+    interpolation at tref returns them exactly (src/utility.f:654-662)."""
+    with open(path, "w") as f:
+        f.write(f"fluid {name}\n")
+        for temp in (200.0, 400.0):
+            f.write(f"{temp!r} {rho!r} 1.0 {mu!r} 1.0 1.0\n")
+        f.write("end\n")
+
+
+def write_restart(path: str, k: int, dtime: float, nx: int, ny: int,
+                  fields: Sequence[np.ndarray]) -> None:
+    """Fortran unformatted sequential restart file (src/file_manip.f:364-401):
+    record 1 ``k, dtime``; record 2 ``nx, ny``; record 3 the eight fields
+    p, u, v, t, pss, uss, vss, tss over (0:nx+1, 0:ny+1).  Each record is
+    framed by 4-byte little-endian length markers (gfortran)."""
+    def rec(buf: bytes) -> bytes:
+        n = np.array([len(buf)], "<i4").tobytes()
+        return n + buf + n
+    body = [rec(np.array([k], "<i4").tobytes() + np.array([dtime], "<f8").tobytes()),
+            rec(np.array([nx, ny], "<i4").tobytes())]
+    parts = []
+    for fld in fields:
+        parts.append(np.asarray(fld[: nx + 2, : ny + 2], "<f8").ravel(order="F").tobytes())
+    body.append(rec(b"".join(parts)))
+    with open(path, "wb") as f:
+        f.write(b"".join(body))
+
+
+def read_restart(path: str):
+    """Inverse of :func:`write_restart`; returns (k, dtime, nx, ny, fields)."""
+    data = open(path, "rb").read()
+    pos = 0
+    recs = []
+    while pos < len(data):
+        n = int(np.frombuffer(data, "<i4", 1, pos)[0])
+        recs.append(data[pos + 4: pos + 4 + n])
+        pos += 8 + n
+    k = int(np.frombuffer(recs[0], "<i4", 1, 0)[0])
+    dtime = float(np.frombuffer(recs[0], "<f8", 1, 4)[0])
+    nx, ny = (int(v) for v in np.frombuffer(recs[1], "<i4", 2, 0))
+    arr = np.frombuffer(recs[2], "<f8").reshape(8, ny + 2, nx + 2)
+    fields = [np.asfortranarray(a.T) for a in arr]
+    return k, dtime, nx, ny, fields

@@ -1,0 +1,262 @@
+"""ctypes binding of the C-ABI in include/wolfd2_gpu.h.
+
+The class :class:`Solver` mirrors the reference's hot-path subroutines by
+name and argument meaning -- ``nAuxMomentum``, ``Ppe``, ``Project``,
+``VelBoundCond``, ``PresBoundCond``, ``VelOutflowBCs``, ``DiffMaxNorm``,
+``Filter`` -- operating on Fortran-layout numpy arrays of shape
+(mnx+1, mny+1) exactly like the Fortran driver's static arrays, plus the
+device-resident time loop (``load_fields`` / ``cold_start`` / ``step`` /
+``store_fields``).
+
+There is no CPU fallback: if the CUDA library is missing or no GPU is
+visible, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+from . import build as _build
+from .deck import Case, Regions, RunParams
+
+W2_OK = 0
+ERRORS = {1: "bad argument", 2: "CUDA error", 3: "device wait timed out",
+          4: "solution diverged", 5: "invalid boundary flag",
+          6: "unsupported configuration", 7: "chain fallback"}
+PREC_FP64, PREC_MIXED = 0, 1
+
+# metric order of the C-ABI = argument order of grid.f:Grid
+METRIC_ORDER = ("rau rbu rbv rgv ran rbn rgn rac rbc rgc dju djv djc djn xen yen xzn yzn "
+                "xec yec xzc yzc xeu yeu xzv yzv xzu yzu xev yev").split()
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class W2Error(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"wolfd2gpu error {code} ({ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [(n, C.c_double) for n in "dk re fr qtol sortol sorrel fpu fpv".split()] + \
+               [(n, C.c_int) for n in "mqiter npsolver msorit nfiltu nfiltv lcartes precision refine_sweeps".split()] + \
+               [("refine_tol", C.c_double)]
+
+    @staticmethod
+    def of(p: RunParams, precision: int = PREC_FP64, refine_sweeps: int = 0,
+           refine_tol: float = 0.0) -> "Params":
+        return Params(p.dk, p.re, p.fr, p.qtol, p.sortol, p.sorrel, p.fpu, p.fpv,
+                      p.mqiter, p.npsolver, p.msorit, p.nfiltu, p.nfiltv, p.lcartes,
+                      precision, refine_sweeps, refine_tol)
+
+
+class StepStat(C.Structure):
+    _fields_ = [("nQLiter", C.c_int), ("nSorConv", C.c_int), ("dif", C.c_double * 4)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """Load libwolfd2gpu.so (building it in-tree when sources are newer)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if _build.needs_build():
+        _build.build_library()
+    if not os.path.exists(_build.LIB):
+        raise RuntimeError(f"CUDA library missing: {_build.LIB}")
+    L = C.CDLL(_build.LIB)
+    vp = C.c_void_p
+    L.wolfd2gpu_create.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                   C.c_int, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp]
+    L.wolfd2gpu_destroy.argtypes = [vp]
+    L.wolfd2gpu_set_metrics.argtypes = [vp, C.POINTER(_dp)]
+    L.wolfd2gpu_grid_metric.argtypes = [vp, _dp, _dp, C.POINTER(_dp)]
+    L.wolfd2gpu_naux_momentum.argtypes = [vp, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp,
+                                          _dp, _dp, _dp, _dp, _ip]
+    L.wolfd2gpu_ppe.argtypes = [vp, _ip, _ip, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp]
+    L.wolfd2gpu_project.argtypes = [vp, _ip, _ip, _dp, _dp, _dp, _dp]
+    L.wolfd2gpu_vel_bound_cond.argtypes = [vp, _ip, _ip, _dp, _dp]
+    L.wolfd2gpu_pres_bound_cond.argtypes = [vp, _ip, _ip, _dp]
+    L.wolfd2gpu_vel_outflow_bcs.argtypes = [vp, _ip, _ip, _dp, _dp]
+    L.wolfd2gpu_diff_max_norm.argtypes = [vp, _ip, _ip, _dp, _dp, _dp]
+    L.wolfd2gpu_filter.argtypes = [vp, _ip, _ip, _ip, _dp, _dp]
+    L.wolfd2gpu_load_fields.argtypes = [vp, _dp, _dp, _dp]
+    L.wolfd2gpu_store_fields.argtypes = [vp, _dp, _dp, _dp]
+    L.wolfd2gpu_cold_start.argtypes = [vp, C.POINTER(Params), _ip]
+    L.wolfd2gpu_step.argtypes = [vp, C.POINTER(Params), C.c_int, C.POINTER(StepStat)]
+    L.wolfd2gpu_sync.argtypes = [vp]
+    L.wolfd2gpu_last_error.argtypes = [vp]
+    L.wolfd2gpu_last_error.restype = C.c_char_p
+    L.wolfd2gpu_tune.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
+    L.wolfd2gpu_device_fields.argtypes = [vp, C.POINTER(_dp), C.POINTER(_dp), C.POINTER(_dp), _ip]
+    L.wolfd2gpu_launch_count.argtypes = [vp]
+    L.wolfd2gpu_launch_count.restype = C.c_longlong
+    _lib = L
+    return L
+
+
+def _p(a: np.ndarray):
+    if a.dtype != np.float64 or not a.flags["F_CONTIGUOUS"]:
+        raise TypeError("expected a Fortran-ordered float64 array")
+    return a.ctypes.data_as(_dp)
+
+
+def _i(v: int):
+    return C.byref(C.c_int(int(v)))
+
+
+def _d(v: float):
+    return C.byref(C.c_double(float(v)))
+
+
+class Solver:
+    """One device context for an nx x ny grid with the given region tables."""
+
+    def __init__(self, nx: int, ny: int, regions: Regions, mnx: Optional[int] = None,
+                 mny: Optional[int] = None):
+        self.L = lib()
+        self.nx, self.ny = nx, ny
+        self.mnx = nx + 1 if mnx is None else mnx
+        self.mny = ny + 1 if mny is None else mny
+        self.regions = regions
+        self._keep = [np.ascontiguousarray(regions.nReg, np.int32)] + \
+            [np.asfortranarray(getattr(regions, n)) for n in ("nRegBrd", "nRegType", "nMomBdTp")] + \
+            [np.asfortranarray(getattr(regions, n)) for n in ("dBCVal", "dPRporos", "dPRporc1", "dPRporc2")]
+        k = self._keep
+        h = C.c_void_p()
+        rc = self.L.wolfd2gpu_create(C.byref(h), self.mnx, self.mny, regions.nRegBrd.shape[0],
+                                     regions.nRegBrd.shape[1], nx, ny,
+                                     k[0].ctypes.data_as(_ip), k[1].ctypes.data_as(_ip),
+                                     k[2].ctypes.data_as(_ip), k[3].ctypes.data_as(_ip),
+                                     _p(k[4]), _p(k[5]), _p(k[6]), _p(k[7]))
+        if rc != W2_OK:
+            raise W2Error(rc, "wolfd2gpu_create failed")
+        self.h = h
+
+    @classmethod
+    def for_case(cls, case: Case, mnx: Optional[int] = None, mny: Optional[int] = None) -> "Solver":
+        s = cls(case.nx, case.ny, case.regions, mnx, mny)
+        s.grid_metric(case.x, case.y)
+        return s
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.wolfd2gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != W2_OK:
+            msg = self.L.wolfd2gpu_last_error(self.h).decode(errors="replace")
+            raise W2Error(rc, msg)
+
+    def field(self) -> np.ndarray:
+        return np.zeros((self.mnx + 1, self.mny + 1), np.float64, order="F")
+
+    # ---- set-up ------------------------------------------------------------
+    def set_metrics(self, met: Dict[str, np.ndarray]) -> None:
+        arr = (_dp * 30)(*[_p(met[n]) for n in METRIC_ORDER])
+        self._check(self.L.wolfd2gpu_set_metrics(self.h, arr))
+
+    def grid_metric(self, x_nodes: np.ndarray, y_nodes: np.ndarray,
+                    want: bool = False) -> Optional[Dict[str, np.ndarray]]:
+        gx, gy = self.field(), self.field()
+        gx[1:self.nx + 1, 1:self.ny + 1] = x_nodes
+        gy[1:self.nx + 1, 1:self.ny + 1] = y_nodes
+        out = None
+        outp = None
+        if want:
+            out = {n: self.field() for n in METRIC_ORDER}
+            outp = (_dp * 30)(*[_p(out[n]) for n in METRIC_ORDER])
+        self._check(self.L.wolfd2gpu_grid_metric(self.h, _p(gx), _p(gy), outp))
+        return out
+
+    def tune(self, seg: int = 0, warm: int = 0, threads: int = 0, blocks_per_sm: int = 0):
+        self._check(self.L.wolfd2gpu_tune(self.h, seg, warm, threads, blocks_per_sm))
+
+    # ---- reference drop-ins ------------------------------------------------
+    def nAuxMomentum(self, mqiter, dk, re, fr, qtol, d, dn, un, vn, us, vs) -> int:
+        out = C.c_int()
+        self._check(self.L.wolfd2gpu_naux_momentum(
+            self.h, _i(self.nx), _i(self.ny), _i(mqiter), _d(dk), _d(re), _d(fr), _d(qtol),
+            None if d is None else _p(d), None if dn is None else _p(dn),
+            _p(un), _p(vn), _p(us), _p(vs), C.byref(out)))
+        return out.value
+
+    def Ppe(self, lCartesGrid, nPpeSolver, msorit, dk, sortol, sorrel, u, v, p) -> int:
+        out = C.c_int()
+        self._check(self.L.wolfd2gpu_ppe(
+            self.h, _i(self.nx), _i(self.ny), _i(1 if lCartesGrid else 0), _i(nPpeSolver),
+            _i(msorit), C.byref(out), _d(dk), _d(sortol), _d(sorrel), _p(u), _p(v), _p(p)))
+        return out.value
+
+    def Project(self, dk, p, u, v) -> None:
+        self._check(self.L.wolfd2gpu_project(self.h, _i(self.nx), _i(self.ny), _d(dk), _p(p), _p(u), _p(v)))
+
+    def VelBoundCond(self, u, v) -> None:
+        self._check(self.L.wolfd2gpu_vel_bound_cond(self.h, _i(self.nx), _i(self.ny), _p(u), _p(v)))
+
+    def PresBoundCond(self, p) -> None:
+        self._check(self.L.wolfd2gpu_pres_bound_cond(self.h, _i(self.nx), _i(self.ny), _p(p)))
+
+    def VelOutflowBCs(self, u, v) -> None:
+        self._check(self.L.wolfd2gpu_vel_outflow_bcs(self.h, _i(self.nx), _i(self.ny), _p(u), _p(v)))
+
+    def DiffMaxNorm(self, un, u) -> float:
+        out = C.c_double()
+        self._check(self.L.wolfd2gpu_diff_max_norm(self.h, _i(self.nx), _i(self.ny), _p(un), _p(u),
+                                                   C.byref(out)))
+        return out.value
+
+    def Filter(self, ncomp, fp, qu) -> None:
+        self._check(self.L.wolfd2gpu_filter(self.h, _i(self.nx), _i(self.ny), _i(ncomp), _d(fp), _p(qu)))
+
+    # ---- device-resident time loop ---------------------------------------
+    def load_fields(self, u, v, p) -> None:
+        self._check(self.L.wolfd2gpu_load_fields(self.h, _p(u), _p(v), _p(p)))
+
+    def store_fields(self):
+        u, v, p = self.field(), self.field(), self.field()
+        self._check(self.L.wolfd2gpu_store_fields(self.h, _p(u), _p(v), _p(p)))
+        return u, v, p
+
+    def cold_start(self, prm: RunParams, **kw) -> int:
+        out = C.c_int()
+        pr = Params.of(prm, **kw)
+        self._check(self.L.wolfd2gpu_cold_start(self.h, C.byref(pr), C.byref(out)))
+        return out.value
+
+    def step(self, prm: RunParams, nsteps: int = 1, **kw) -> List[tuple]:
+        pr = Params.of(prm, **kw)
+        st = (StepStat * max(nsteps, 1))()
+        self._check(self.L.wolfd2gpu_step(self.h, C.byref(pr), nsteps, st))
+        return [(s.nQLiter, s.nSorConv, tuple(s.dif)) for s in st[:nsteps]]
+
+    def sync(self) -> None:
+        self._check(self.L.wolfd2gpu_sync(self.h))
+
+    def launch_count(self) -> int:
+        return int(self.L.wolfd2gpu_launch_count(self.h))
+
+    def device_fields(self):
+        u, v, p = _dp(), _dp(), _dp()
+        ld = C.c_int()
+        self._check(self.L.wolfd2gpu_device_fields(self.h, C.byref(u), C.byref(v), C.byref(p), C.byref(ld)))
+        return (C.cast(u, C.c_void_p).value, C.cast(v, C.c_void_p).value,
+                C.cast(p, C.c_void_p).value, ld.value)
