@@ -1,0 +1,348 @@
+#!/usr/bin/env python3
+"""Throughput benchmark of the wolfd2 projection-method time step on GB300.
+
+Workload (one "step" = one pass of main.f:690-972, the whole time step):
+lid-driven cavity, 1024 x 1024 uniform cells, Re = 1000, seeded divergence-
+free perturbation (16 x 16 streamfunction modes, N(0, 1e-3) amplitudes),
+red/black point SOR, plain FP64.  dt = 5e-4: at the named dt = 1e-3 the
+reference's own Newton-Kantorovich iteration diverges to NaN in the first
+step at this resolution (the CPU oracle and the GPU path agree bit for bit on
+that), so the benchmark halves dt, which keeps every cell and every
+iteration of the reference algorithm (20 Q-L iterations and 2000 SOR sweeps
+per step at this size).
+
+Arms:
+  --impl ours       the CUDA library through its C-ABI (value: device-timed
+                    with CUDA events on the library stream; e2e: host buffers
+                    with the H2D/D2H copies inside the timed region)
+  --impl reference  the reference algorithm on the host cores (the CPU
+                    oracle's restatement; no Fortran compiler exists on the
+                    GPU machines to build the reference itself)
+
+Multi-GPU: the single-case path does not shard (per-sweep halos, global
+max-norms and domain-long chains), so N GPUs run N independent replicas and
+`value` sums them ("replicas only", scaling weak).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+from wolfd2_gb300 import deck  # noqa: E402
+
+METRIC = json.load(open(os.path.join(ROOT, "BASELINE.json")))["metric"]
+UNIT = "cell-steps/s"
+DT_NAMED = 1.0e-3
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples taken while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_case(args):
+    return deck.cavity(args.n, args.re, args.dt, solver=args.solver)
+
+
+def ppe_bytes(cells, nsor):
+    """Algorithmic bytes of one Ppe call: RHS reads us, vs and writes b
+    (3 words); each sweep reads p, b and writes p (3 words)."""
+    return 8.0 * cells * (3 + 3 * nsor)
+
+
+def mom_bytes(cells, nql):
+    """Algorithmic bytes of one nAuxMomentum call: per Q-L iteration read us,
+    vs, un, vn and write us, vs (6 words); chain systems stay on chip."""
+    return 8.0 * cells * 6 * nql
+
+
+def step_bytes(cells, nql, nsor):
+    return 8.0 * cells * (6 * nql + 3 + 3 * nsor + 5 + 3)
+
+
+def cpu_step_sample(case, ic, nsteps=1):
+    """Time `nsteps` oracle steps (the checker restating the reference) on
+    the host; returns (cell-steps/s, seconds, threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    u, v, p = ic
+    r = O.OracleRun(case, fields={"u": u, "v": v, "p": p}, cold_start=False)
+    t0 = time.perf_counter()
+    r.step(nsteps)
+    dt = time.perf_counter() - t0
+    return case.cells * nsteps / dt, dt, O.threads()
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    case = make_case(args)
+    ic = deck.perturbation_ic(case, args.seed)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    u, v, p = ic
+    r = O.OracleRun(case, fields={"u": u, "v": v, "p": p}, cold_start=False)
+    r.step(args.warmup)
+    t0 = time.perf_counter()
+    r.step(args.steps)
+    dt = time.perf_counter() - t0
+    value = case.cells * args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_of(args, case),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.threads(), "kind": "port",
+                         "sample": f"{args.warmup} + {args.steps} full time steps of the same case"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "iterations": [[h[0], h[1]] for h in r.history[-args.steps:]],
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_of(args, case):
+    return {"workload": (f"lid-driven cavity {args.n}x{args.n} cells, Re={args.re:g}, "
+                         f"dt={args.dt:g} (named dt={DT_NAMED:g} diverges in the reference scheme at this size), "
+                         f"seeded 16x16-mode streamfunction perturbation (seed {args.seed}), "
+                         f"ppe_solver {args.solver}, plain FP64"),
+            "cells": case.cells, "nx": case.nx, "ny": case.ny, "re": args.re, "dt": args.dt,
+            "ppe_solver": args.solver,
+            "l2": "flushed between timed steps (256 MiB write); per-step working set > 2x L2"}
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from wolfd2_gb300.gpu import K_COPY, K_MOMENTUM, K_POST, K_PPE, K_BC, KERNEL_NAMES, Solver
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    case = make_case(args)
+    u0, v0, p0 = deck.perturbation_ic(case, args.seed + rank)
+    s = Solver.for_case(case)
+    prm = case.params
+    st = torch.cuda.ExternalStream(s.stream(), device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+
+    # warm-up
+    s.load_fields(u0, v0, p0)
+    hist = s.step(prm, args.warmup) if args.warmup else []
+    barrier()
+
+    # device-timed region: fields resident in HBM
+    s.profile(True)
+    n_launch0 = s.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        barrier()
+        t_wall0 = time.perf_counter()
+        for k in range(args.steps):
+            with torch.cuda.stream(st):
+                flush.fill_(float(k))
+                ev[k][0].record(st)
+            hist += s.step(prm, 1)
+            with torch.cuda.stream(st):
+                ev[k][1].record(st)
+        barrier()
+        t_wall = time.perf_counter() - t_wall0
+    launches = s.launch_count() - n_launch0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_dev = sum(step_ms) / 1e3
+    prof = {k: s.profile_read(k) for k in (K_MOMENTUM, K_PPE, K_POST, K_BC, K_COPY)}
+    s.profile(False)
+    timed = hist[-args.steps:]
+
+    # end-to-end through the C-ABI with host buffers, copies in the timed region
+    u, v, p = s.store_fields()
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s.load_fields(u, v, p)
+        s.step(prm, 1)
+        u, v, p = s.store_fields()
+    barrier()
+    t_e2e = time.perf_counter() - t0
+    field_bytes = (case.nx + 2) * (case.ny + 2) * 8
+
+    # max over ranks
+    t_max = t_dev
+    t_e2e_max = t_e2e
+    if world > 1:
+        tt = torch.tensor([t_dev, t_e2e], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max, t_e2e_max = float(tt[0]), float(tt[1])
+
+    if rank != 0:
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    cells = case.cells
+    value = world * cells * args.steps / t_max
+    e2e_value = world * cells * e2e_steps / t_e2e_max
+    hbm_peak, peak_kind = peaks()
+    # dominant kernel: larger share of device time
+    dom = max((K_MOMENTUM, K_PPE), key=lambda k: prof[k][0])
+    nql = [h[0] if h[0] > 0 else 20 for h in timed]
+    nsor = [h[1] for h in timed]
+    if dom == K_PPE:
+        alg = sum(ppe_bytes(cells, n) for n in nsor)
+    else:
+        alg = sum(mom_bytes(cells, n) for n in nql)
+    dom_ms, dom_n = prof[dom]
+    achieved = alg / (dom_ms / 1e3) / 1e9
+    # FP64 pipe view of the red/black sweep: 11 add/mul + 1 divide per point
+    sweep_pts = sum(cells * n for n in nsor)
+    fp64 = None
+    if prof[K_PPE][0] > 0:
+        ops = sweep_pts * (11 + 8.9)
+        fp64 = {"kernel": "k_ppe", "op_per_point": "11 add/mul + 1 div (div = 8.9 FMA slots)",
+                "achieved_gops": ops / (prof[K_PPE][0] / 1e3) / 1e9, "peak_gops": 628.0,
+                "peak_kind": "measured DFMA probe on this pool's GB300 (2 DFMA/clk/SM)",
+                "frac": ops / (prof[K_PPE][0] / 1e3) / 1e9 / 628.0}
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        tj = json.load(open(tpath)).get(KERNEL_NAMES[dom])
+        if tj:
+            # scale a captured small case by the units processed per launch
+            traffic = tj["bytes_per_unit"] * (alg / dom_n) / tj["alg_bytes_per_unit"]
+    cpu = None
+    if not args.no_cpu_baseline:
+        cv, csec, cores = cpu_step_sample(case, (u0, v0, p0), 1)
+        cpu = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"1 full time step of the same {args.n}x{args.n} case from the same initial state "
+                         f"({csec:.1f} s)"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": config_of(args, case),
+        "parallelism": "replicas only" if world > 1 else "single GPU",
+        "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[dom], "achieved": achieved,
+                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                     "peak_kind": peak_kind, "traffic": traffic,
+                     "alg_bytes_per_launch": alg / dom_n, "avg_launch_ms": dom_ms / dom_n},
+        "fp64_roof": fp64,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 3 * field_bytes,
+                "d2h_bytes_per_step": 3 * field_bytes, "steps": e2e_steps},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+        "kernel_ms": {KERNEL_NAMES[k]: {"total_ms": v[0], "launches": v[1]} for k, v in prof.items()},
+        "iterations": [[h[0], h[1]] for h in timed],
+        "wall_s": t_wall,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=1024, help="cells per side")
+    ap.add_argument("--re", type=float, default=1000.0)
+    ap.add_argument("--dt", type=float, default=5.0e-4)
+    ap.add_argument("--solver", default="rb_sor", choices=sorted(deck.PPE_SOLVERS))
+    ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -190,6 +190,24 @@ int wolfd2gpu_device_fields(w2_ctx *ctx, double **u, double **v, double **p,
 /* Kernel launches issued so far by this context (for accounting). */
 long long wolfd2gpu_launch_count(w2_ctx *ctx);
 
+/* The context's CUDA stream (a cudaStream_t), for callers that time or
+ * order work against it. */
+void *wolfd2gpu_stream(w2_ctx *ctx);
+
+/* Per-kernel timing with CUDA events recorded on the context stream around
+ * every launch of the time loop.  Kinds: */
+#define W2_K_MOMENTUM 0  /* nAuxMomentum persistent kernel        */
+#define W2_K_PPE      1  /* Ppe persistent kernel                 */
+#define W2_K_POST     2  /* Project + boundary rows + step norms  */
+#define W2_K_BC       3  /* one-block boundary programs           */
+#define W2_K_COPY     4  /* time-level copies                     */
+#define W2_K_NKINDS   5
+int wolfd2gpu_profile(w2_ctx *ctx, int enable);
+/* Accumulated device time (ms) and launch count of one kind since the last
+ * wolfd2gpu_profile(ctx, 1); synchronises the context stream. */
+int wolfd2gpu_profile_read(w2_ctx *ctx, int kind, double *total_ms,
+                           long long *count);
+
 #ifdef __cplusplus
 }
 #endif

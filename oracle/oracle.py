@@ -241,3 +241,9 @@ class OracleRun:
             if rc:
                 raise FloatingPointError("Solution diverged. Please reduce CFL number.")
         return self.history[-1]
+
+
+def threads() -> int:
+    """Host threads the oracle library runs on (1: the restatement is serial,
+    like the reference)."""
+    return 1

@@ -37,6 +37,13 @@ struct w2_ctx {
   std::vector<int> tab_brd, tab_rtype, tab_btype;
   std::vector<double> tab_bcv;
   int nri = 0, nrj = 0;
+  // per-kernel event timing (wolfd2gpu_profile)
+  bool prof_on = false;
+  struct Rec { int kind; cudaEvent_t a, b; };
+  std::vector<Rec> prof_pending;
+  std::vector<cudaEvent_t> ev_pool;
+  double prof_ms[W2_K_NKINDS] = {};
+  long long prof_n[W2_K_NKINDS] = {};
 };
 
 namespace {
@@ -173,6 +180,52 @@ int build_masks(w2_ctx *c, std::vector<uint16_t> &mk) {
   return W2_OK;
 }
 
+cudaEvent_t ev_get(w2_ctx *c) {
+  if (!c->ev_pool.empty()) {
+    cudaEvent_t e = c->ev_pool.back();
+    c->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Bracket a launch with events on the context stream when profiling.
+struct ProfScope {
+  w2_ctx *c;
+  int kind;
+  cudaEvent_t a = nullptr;
+  ProfScope(w2_ctx *c_, int k) : c(c_), kind(k) {
+    if (c->prof_on) {
+      a = ev_get(c);
+      cudaEventRecord(a, c->st);
+    }
+  }
+  ~ProfScope() {
+    if (a) {
+      cudaEvent_t b = ev_get(c);
+      cudaEventRecord(b, c->st);
+      c->prof_pending.push_back({kind, a, b});
+    }
+  }
+};
+
+void prof_collect(w2_ctx *c) {
+  if (c->prof_pending.empty()) return;
+  cudaStreamSynchronize(c->st);
+  for (auto &r : c->prof_pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+      c->prof_ms[r.kind] += ms;
+      c->prof_n[r.kind] += 1;
+    }
+    c->ev_pool.push_back(r.a);
+    c->ev_pool.push_back(r.b);
+  }
+  c->prof_pending.clear();
+}
+
 int pick_blocks(w2_ctx *c, const void *kern, long work) {
   int occ = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, c->threads, 0);
@@ -264,6 +317,7 @@ int ready(w2_ctx *c) {
 
 // ---- launch helpers on explicit device buffers ---------------------------
 int launch_bc(w2_ctx *c, int ops, double *u, double *v, double *p) {
+  ProfScope ps(c, W2_K_BC);
   c->launches++;
   k_bc<<<1, c->threads, 0, c->st>>>(c->dev, ops, u, v, p);
   CK(cudaGetLastError());
@@ -273,6 +327,7 @@ int launch_bc(w2_ctx *c, int ops, double *u, double *v, double *p) {
 int launch_naux(w2_ctx *c, int mqiter, double dk, double re, double qtol, const double *un,
                 const double *vn, double *us, double *vs) {
   int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny);
+  ProfScope ps(c, W2_K_MOMENTUM);
   Dev d = c->dev;
   StepOut *out = c->d_out;
   void *args[] = {&d, &mqiter, &dk, &re, &qtol, (void *)&un, (void *)&vn, &us, &vs, &out};
@@ -282,6 +337,7 @@ int launch_naux(w2_ctx *c, int mqiter, double dk, double re, double qtol, const 
 int launch_ppe(w2_ctx *c, int lcartes, int npsolver, int msorit, double dk, double sortol,
                double sorrel, const double *u, const double *v, double *p) {
   int blocks = (npsolver == 1 || npsolver == 2) ? 1 : pick_blocks(c, (const void *)k_ppe, (long)c->nx * c->ny);
+  ProfScope ps(c, W2_K_PPE);
   Dev d = c->dev;
   StepOut *out = c->d_out;
   void *args[] = {&d, &lcartes, &npsolver, &msorit, &dk, &sortol, &sorrel, (void *)&u, (void *)&v, &p, &out};
@@ -410,6 +466,11 @@ int wolfd2gpu_create(w2_ctx **out, int mnx, int mny, int mgri, int mgrj, int nx,
 int wolfd2gpu_destroy(w2_ctx *c) {
   if (!c) return W2_OK;
   if (c->st) cudaStreamSynchronize(c->st);
+  for (auto &r : c->prof_pending) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   for (void *p : c->allocs) cudaFree(p);
   if (c->h_out) cudaFreeHost(c->h_out);
   if (c->st) cudaStreamDestroy(c->st);
@@ -420,6 +481,27 @@ int wolfd2gpu_destroy(w2_ctx *c) {
 const char *wolfd2gpu_last_error(w2_ctx *c) { return c ? c->err : "null context"; }
 
 long long wolfd2gpu_launch_count(w2_ctx *c) { return c ? c->launches : 0; }
+
+void *wolfd2gpu_stream(w2_ctx *c) { return c ? (void *)c->st : nullptr; }
+
+int wolfd2gpu_profile(w2_ctx *c, int enable) {
+  if (!c) return W2_E_ARG;
+  prof_collect(c);
+  for (int k = 0; k < W2_K_NKINDS; ++k) {
+    c->prof_ms[k] = 0.0;
+    c->prof_n[k] = 0;
+  }
+  c->prof_on = enable != 0;
+  return W2_OK;
+}
+
+int wolfd2gpu_profile_read(w2_ctx *c, int kind, double *total_ms, long long *count) {
+  if (!c || kind < 0 || kind >= W2_K_NKINDS) return W2_E_ARG;
+  prof_collect(c);
+  if (total_ms) *total_ms = c->prof_ms[kind];
+  if (count) *count = c->prof_n[kind];
+  return W2_OK;
+}
 
 int wolfd2gpu_tune(w2_ctx *c, int chain_seg, int chain_warm, int threads, int blocks_per_sm) {
   if (!c) return W2_E_ARG;
@@ -709,12 +791,16 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
     double *us = c->U[b], *vs = c->V[b], *p = c->P[b];
     StepOut *o = d_outs + s;
     Dev d = c->dev;
-    c->launches++;
-    k_copy3<<<gb, c->threads, 0, c->st>>>(d, us, un, vs, vn, p, pn);
-    CK(cudaGetLastError());
+    {
+      ProfScope ps(c, W2_K_COPY);
+      c->launches++;
+      k_copy3<<<gb, c->threads, 0, c->st>>>(d, us, un, vs, vn, p, pn);
+      CK(cudaGetLastError());
+    }
     // nAuxMomentum on (un, vn) -> (us, vs); us = un already (main.f:741-747)
     {
       int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny);
+      ProfScope ps(c, W2_K_MOMENTUM);
       int mq = prm->mqiter;
       double dk = prm->dk, re = prm->re, qtol = prm->qtol;
       void *args[] = {&d, &mq, &dk, &re, &qtol, &un, &vn, &us, &vs, &o};
@@ -737,6 +823,7 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
     {
       int blocks = (prm->npsolver == 1 || prm->npsolver == 2)
                        ? 1 : pick_blocks(c, (const void *)k_ppe, (long)c->nx * c->ny);
+      ProfScope ps(c, W2_K_PPE);
       int lc = prm->lcartes, ns = prm->npsolver, ms = prm->msorit;
       double dk = prm->dk, st = prm->sortol, sr = prm->sorrel;
       void *args[] = {&d, &lc, &ns, &ms, &dk, &st, &sr, &us, &vs, &p, &o};
@@ -744,6 +831,7 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
     }
     {
       int blocks = pick_blocks(c, (const void *)k_step_post, (long)c->nx * c->ny);
+      ProfScope ps(c, W2_K_POST);
       double dk = prm->dk;
       void *args[] = {&d, &dk, &p, &pn, &un, &vn, &us, &vs, &o};
       if ((rc = coop(c, (const void *)k_step_post, blocks, args))) break;

@@ -418,6 +418,35 @@ def channel(ncx: int, ncy: int, re: float, dt: float, *, length: float = 4.0,
     return Case(f"channel{ncx}x{ncy}_re{re:g}", nx, ny, X, Y, regs, prm, bc)
 
 
+def perturbation_ic(case: Case, seed: int, modes: int = 16, amp: float = 1.0e-3):
+    """Seeded divergence-free initial velocity on the staggered grid.
+
+    psi(x,y) = sum_{k,l=1..modes} a_kl sin(k pi x/Lx) sin(l pi y/Ly) with
+    a_kl ~ N(0, amp^2) from numpy.random.default_rng(seed); then
+    u(i,j) = (psi(i,j) - psi(i,j-1))/hy and v(i,j) = -(psi(i,j) - psi(i-1,j))/hx
+    at the staggered u/v locations, so the discrete divergence (pressure.f
+    nloc = 1) vanishes up to rounding and the walls see zero normal flow.
+    Returns (u, v, p) as Fortran-ordered (nx+2, ny+2) arrays; p = 0."""
+    rng = np.random.default_rng(seed)
+    a = rng.normal(0.0, amp, size=(modes, modes))
+    x = case.x[:, 0]
+    y = case.y[0, :]
+    lx, ly = x[-1] - x[0], y[-1] - y[0]
+    k = np.arange(1, modes + 1)
+    sx = np.sin(np.pi * np.outer(x - x[0], k) / lx)     # (nx, modes)
+    sy = np.sin(np.pi * np.outer(y - y[0], k) / ly)     # (ny, modes)
+    psi = sx @ a @ sy.T                                  # (nx, ny)
+    nx, ny = case.nx, case.ny
+    hx = np.diff(x)
+    hy = np.diff(y)
+    u = np.zeros((nx + 2, ny + 2), order="F")
+    v = np.zeros((nx + 2, ny + 2), order="F")
+    u[1:nx + 1, 2:ny + 1] = (psi[:, 1:] - psi[:, :-1]) / hy[None, :]
+    v[2:nx + 1, 1:ny + 1] = -(psi[1:, :] - psi[:-1, :]) / hx[:, None]
+    p = np.zeros((nx + 2, ny + 2), order="F")
+    return u, v, p
+
+
 # ---------------------------------------------------------------------------
 # Reference-format files: decks, Plot3D grid, fluid table, restart records.
 # ---------------------------------------------------------------------------

@@ -27,6 +27,9 @@ ERRORS = {1: "bad argument", 2: "CUDA error", 3: "device wait timed out",
           4: "solution diverged", 5: "invalid boundary flag",
           6: "unsupported configuration", 7: "chain fallback"}
 PREC_FP64, PREC_MIXED = 0, 1
+K_MOMENTUM, K_PPE, K_POST, K_BC, K_COPY = range(5)
+KERNEL_NAMES = {K_MOMENTUM: "k_naux", K_PPE: "k_ppe", K_POST: "k_step_post",
+                K_BC: "k_bc", K_COPY: "k_copy3"}
 
 # metric order of the C-ABI = argument order of grid.f:Grid
 METRIC_ORDER = ("rau rbu rbv rgv ran rbn rgn rac rbc rgc dju djv djc djn xen yen xzn yzn "
@@ -102,6 +105,10 @@ def lib():
     L.wolfd2gpu_device_fields.argtypes = [vp, C.POINTER(_dp), C.POINTER(_dp), C.POINTER(_dp), _ip]
     L.wolfd2gpu_launch_count.argtypes = [vp]
     L.wolfd2gpu_launch_count.restype = C.c_longlong
+    L.wolfd2gpu_stream.argtypes = [vp]
+    L.wolfd2gpu_stream.restype = C.c_void_p
+    L.wolfd2gpu_profile.argtypes = [vp, C.c_int]
+    L.wolfd2gpu_profile_read.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_longlong)]
     _lib = L
     return L
 
@@ -250,6 +257,18 @@ class Solver:
 
     def sync(self) -> None:
         self._check(self.L.wolfd2gpu_sync(self.h))
+
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer handle."""
+        return int(self.L.wolfd2gpu_stream(self.h) or 0)
+
+    def profile(self, enable: bool = True) -> None:
+        self._check(self.L.wolfd2gpu_profile(self.h, 1 if enable else 0))
+
+    def profile_read(self, kind: int):
+        ms, n = C.c_double(), C.c_longlong()
+        self._check(self.L.wolfd2gpu_profile_read(self.h, kind, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
 
     def launch_count(self) -> int:
         return int(self.L.wolfd2gpu_launch_count(self.h))
