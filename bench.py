@@ -229,6 +229,7 @@ def run_ours(args):
         barrier()
         t_wall = time.perf_counter() - t_wall0
     launches = s.launch_count() - n_launch0
+    chain_rounds, chain_fallbacks = s.chain_stats()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     t_dev = sum(step_ms) / 1e3
     prof = {k: s.profile_read(k) for k in (K_MOMENTUM, K_PPE, K_POST, K_BC, K_COPY)}
@@ -316,6 +317,8 @@ def run_ours(args):
         "gpu_launches": launches,
         "kernel_ms": {KERNEL_NAMES[k]: {"total_ms": v[0], "launches": v[1]} for k, v in prof.items()},
         "iterations": [[h[0], h[1]] for h in timed],
+        "chain": {"max_verify_rounds": chain_rounds, "sequential_fallbacks": chain_fallbacks,
+                  "segment_rows": s.seg if hasattr(s, "seg") else None},
         "wall_s": t_wall,
     }
     print(json.dumps(line), flush=True)

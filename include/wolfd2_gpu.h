@@ -190,6 +190,11 @@ int wolfd2gpu_device_fields(w2_ctx *ctx, double **u, double **v, double **p,
 /* Kernel launches issued so far by this context (for accounting). */
 long long wolfd2gpu_launch_count(w2_ctx *ctx);
 
+/* Chain-solver statistics since the last call (then reset): the most
+ * verification rounds any chain solve needed (kMaxRounds+1 = it fell back to
+ * the sequential walk) and the number of sequential fallbacks. */
+int wolfd2gpu_chain_stats(w2_ctx *ctx, int *max_rounds, int *fallbacks);
+
 /* The context's CUDA stream (a cudaStream_t), for callers that time or
  * order work against it. */
 void *wolfd2gpu_stream(w2_ctx *ctx);

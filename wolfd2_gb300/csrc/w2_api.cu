@@ -484,6 +484,19 @@ long long wolfd2gpu_launch_count(w2_ctx *c) { return c ? c->launches : 0; }
 
 void *wolfd2gpu_stream(w2_ctx *c) { return c ? (void *)c->st : nullptr; }
 
+int wolfd2gpu_chain_stats(w2_ctx *c, int *max_rounds, int *fallbacks) {
+  if (!c) return W2_E_ARG;
+  CK(cudaStreamSynchronize(c->st));
+  Sync s;
+  CK(cudaMemcpy(&s, c->dev.sync, sizeof(Sync), cudaMemcpyDeviceToHost));
+  if (max_rounds) *max_rounds = s.max_rounds;
+  if (fallbacks) *fallbacks = s.fallback;
+  int zero[2] = {0, 0};
+  CK(cudaMemcpy(&c->dev.sync->max_rounds, &zero[0], sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(&c->dev.sync->fallback, &zero[1], sizeof(int), cudaMemcpyHostToDevice));
+  return W2_OK;
+}
+
 int wolfd2gpu_profile(w2_ctx *c, int enable) {
   if (!c) return W2_E_ARG;
   prof_collect(c);

@@ -28,7 +28,7 @@
 
 namespace w2 {
 
-constexpr int kMaxRounds = 8;
+constexpr int kMaxRounds = 24;
 
 __device__ __forceinline__ bool same_bits(double a, double b) {
   return __double_as_longlong(a) == __double_as_longlong(b);
@@ -154,22 +154,68 @@ __device__ bool chain_b2(const Chain &c, int s, int L, const double *ein, double
   return true;
 }
 
-// Sequential completion used when verification rounds do not settle.
-__device__ void chain_sequential(const Chain &c) {
-  double a3p, bp;
-  fwd_row0(c, a3p, bp);
-  c.a3p[0] = a3p;
-  c.bp[0] = bp;
-  for (int k = 1; k < c.n; ++k) {
-    fwd_row(c, k, a3p, bp);
-    c.a3p[k] = a3p;
-    c.bp[k] = bp;
-  }
-  double xn = c.bp[c.n - 1];
-  c.x[c.n - 1] = xn;
-  for (int k = c.n - 2; k >= 0; --k) {
-    xn = c.bp[k] - c.a3p[k] * xn;
-    c.x[k] = xn;
+// Sequential completion used when verification rounds do not settle: warp 0
+// of block 0 walks the chain in chunks of 32 rows, the lanes staging each
+// chunk's coefficients through shared memory and lane 0 running the
+// recurrence (same arithmetic as fwd_row / the back substitution).
+__device__ void chain_sequential_warp(const Chain &c, bool forward) {
+  __shared__ double s1[32], s2[32], s3[32], sb[32], o3[32], ob[32];
+  const int lane = threadIdx.x & 31;
+  if (forward) {
+    double a3p = 0.0, bp = 0.0;
+    for (int base = 0; base < c.n; base += 32) {
+      const int k = base + lane, cnt = min(32, c.n - base);
+      if (k < c.n) {
+        s1[lane] = c.a1[k];
+        s2[lane] = c.a2[k];
+        s3[lane] = c.a3[k];
+        sb[lane] = chain_rhs(c, k);
+      }
+      __syncwarp();
+      if (lane == 0) {
+        for (int q = 0; q < cnt; ++q) {
+          const int kk = base + q;
+          if (kk == 0) {
+            a3p = s3[0] / c.a2[1];
+            bp = sb[0] / s2[0];
+          } else {
+            const double a1 = s1[q];
+            const double a2p = s2[q] - a1 * a3p;
+            const double nb = (sb[q] - a1 * bp) / a2p;
+            a3p = (kk < c.n - 1) ? s3[q] / a2p : 0.0;
+            bp = nb;
+          }
+          o3[q] = a3p;
+          ob[q] = bp;
+        }
+      }
+      __syncwarp();
+      if (k < c.n) {
+        c.a3p[k] = o3[lane];
+        c.bp[k] = ob[lane];
+      }
+      __syncwarp();
+    }
+  } else {
+    double xn = 0.0;
+    for (int top = c.n - 1; top >= 0; top -= 32) {
+      const int k = top - lane, cnt = min(32, top + 1);
+      if (k >= 0) {
+        s3[lane] = c.a3p[k];
+        sb[lane] = c.bp[k];
+      }
+      __syncwarp();
+      if (lane == 0) {
+        for (int q = 0; q < cnt; ++q) {
+          const int kk = top - q;
+          xn = (kk == c.n - 1) ? sb[q] : sb[q] - s3[q] * xn;
+          ob[q] = xn;
+        }
+      }
+      __syncwarp();
+      if (k >= 0) c.x[k] = ob[lane];
+      __syncwarp();
+    }
   }
 }
 
@@ -216,14 +262,20 @@ __device__ bool solve_chains(const Dev &d, Chain c0, Chain c1, int nchains) {
     cur ^= 1;
     if (!ch) {
       settled = true;
+      if (blockIdx.x == 0 && threadIdx.x == 0) atomicMax(&sy->max_rounds, round + 1);
       break;
     }
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0 && !settled) atomicMax(&sy->max_rounds, kMaxRounds + 1);
   if (!settled) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      chain_sequential(c0);
-      if (nchains > 1) chain_sequential(c1);
-      atomicAdd(&sy->fallback, 1);
+    if (blockIdx.x == 0 && threadIdx.x < 32) {
+      chain_sequential_warp(c0, true);
+      chain_sequential_warp(c0, false);
+      if (nchains > 1) {
+        chain_sequential_warp(c1, true);
+        chain_sequential_warp(c1, false);
+      }
+      if (threadIdx.x == 0) atomicAdd(&sy->fallback, 1);
     }
     if (!grid_sync(sy)) return false;
     return true;  // sequential pass produced a3p, bp and x
@@ -261,22 +313,16 @@ __device__ bool solve_chains(const Dev &d, Chain c0, Chain c1, int nchains) {
     cur ^= 1;
     if (!ch) {
       settled = true;
+      if (blockIdx.x == 0 && threadIdx.x == 0) atomicMax(&sy->max_rounds, round + 1);
       break;
     }
   }
   if (!settled) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (blockIdx.x == 0 && threadIdx.x < 32) {
       // forward values are exact here; redo the back substitution serially
-      for (int t = 0; t < nchains; ++t) {
-        const Chain &c = t == 0 ? c0 : c1;
-        double xn = c.bp[c.n - 1];
-        c.x[c.n - 1] = xn;
-        for (int k = c.n - 2; k >= 0; --k) {
-          xn = c.bp[k] - c.a3p[k] * xn;
-          c.x[k] = xn;
-        }
-      }
-      atomicAdd(&sy->fallback, 1);
+      chain_sequential_warp(c0, false);
+      if (nchains > 1) chain_sequential_warp(c1, false);
+      if (threadIdx.x == 0) atomicAdd(&sy->fallback, 1);
     }
     if (!grid_sync(sy)) return false;
   }

@@ -82,7 +82,7 @@ struct Sync {
   int fallback;       // chain recurrence needed a sequential pass
   int pad0;
   int halt;           // a step diverged: later stages of the run are skipped
-  int pad1;
+  int max_rounds;     // most verification rounds any chain solve needed
   unsigned long long red[16];  // max-reductions (bit patterns of doubles >= 0):
                                // [0..2] momentum ring, [3..5] PPE ring,
                                // [6..8] step norms, [9..] scratch

@@ -108,6 +108,7 @@ def lib():
     L.wolfd2gpu_stream.argtypes = [vp]
     L.wolfd2gpu_stream.restype = C.c_void_p
     L.wolfd2gpu_profile.argtypes = [vp, C.c_int]
+    L.wolfd2gpu_chain_stats.argtypes = [vp, _ip, _ip]
     L.wolfd2gpu_profile_read.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_longlong)]
     _lib = L
     return L
@@ -269,6 +270,13 @@ class Solver:
         ms, n = C.c_double(), C.c_longlong()
         self._check(self.L.wolfd2gpu_profile_read(self.h, kind, C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def chain_stats(self):
+        """(most verification rounds used, sequential fallbacks) since the
+        previous call."""
+        r, f = C.c_int(), C.c_int()
+        self._check(self.L.wolfd2gpu_chain_stats(self.h, C.byref(r), C.byref(f)))
+        return r.value, f.value
 
     def launch_count(self) -> int:
         return int(self.L.wolfd2gpu_launch_count(self.h))
