@@ -1,0 +1,969 @@
+"""Mechanical Fortran-77 -> C translation of the reference's hot-path source
+(TEST INFRASTRUCTURE ONLY).
+
+No Fortran compiler exists on the build machine or the GPU machines, so the
+reference cannot be compiled as written.  This module reads the reference's
+own source files (src/momentum.f, src/pressure.f, src/utility.f,
+src/bound_cond.f, src/grid.f plus include/config.f and include/wolfd2.h)
+where the reference tree is mounted, and translates the routines of the hot
+path statement by statement into C: same loops, same expressions with the
+Fortran evaluation order made explicit by parentheses, static storage for
+large local arrays (as gfortran places them), arguments by reference.  The
+generated C and its shared libraries go to oracle/_ref/ (git-ignored: they
+are derived from the reference source and are never committed).  They are
+compiled with gcc -O2 -ffp-contract=off, like the oracle, and serve to pin the
+hand-written oracle against the reference source.
+
+The translator handles exactly the Fortran subset these files use: fixed-form
+lines with continuation, INTEGER*4/REAL*8/LOGICAL*4 declarations with
+explicit bounds, PARAMETER constants, DO/END DO, block and logical IF,
+SELECT CASE, CALL, RETURN, STOP, CYCLE, EXIT and assignments.  Anything else
+raises, so an unsupported construct can never be translated silently wrong.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+import subprocess
+from typing import Dict, List, Optional, Tuple
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+REF_ROOT = os.environ.get("WOLFD2_REFERENCE", "/root/reference")
+GEN_C = os.path.join(OUT, "wolfd2_ref.c")
+
+# Routines translated, per file.
+ROUTINES = {
+    "src/momentum.f": ["nauxmomentum", "xmomentum", "ymomentum", "convcoef", "dconvu",
+                       "ddiffu", "dconvv", "ddiffv", "poroscoef", "alttridlu"],
+    "src/pressure.f": ["ppe", "divergence", "rhsppe", "sor", "sorrb", "sorrbp", "slor",
+                       "slorrb", "slorrbp"],
+    "src/utility.f": ["filter", "project", "diffmaxnorm", "dmaxnorm"],
+    "src/bound_cond.f": ["velboundcond", "presboundcond", "veloutflowbcs"],
+    "src/grid.f": ["mirrorpts", "fullgrid", "metric"],
+}
+
+STACK_LIMIT = 65536  # gfortran -fmax-stack-var-size default: larger locals are static
+REF_DEFAULT = {"mnx": "302", "mny": "302"}  # include/config.f:19-20
+
+
+class F77Error(RuntimeError):
+    pass
+
+
+# ---------------------------------------------------------------------------
+# Source reading
+# ---------------------------------------------------------------------------
+
+def _macros() -> Dict[str, str]:
+    m = {}
+    for line in open(os.path.join(REF_ROOT, "include", "wolfd2.h")):
+        mm = re.match(r"\s*#define\s+(\w+)\s+(.+?)\s*$", line)
+        if mm:
+            m[mm.group(1)] = mm.group(2)
+    return m
+
+
+def _statements(path: str, macros: Dict[str, str]) -> List[str]:
+    """Fixed-form lines -> logical statements (lower case, comments and
+    preprocessor lines removed, continuations joined, macros expanded)."""
+    stmts: List[str] = []
+    for raw in open(path, encoding="latin-1"):
+        line = raw.rstrip("\n").expandtabs(6)
+        if not line.strip() or line[0] in "Cc*!" or line.lstrip().startswith("#"):
+            continue
+        if line.lstrip().startswith("/*") or line.lstrip().startswith("*/"):
+            continue
+        body = line[6:72] if len(line) > 6 else ""
+        cont = len(line) > 5 and line[5] not in " 0"
+        # drop trailing ! comments outside strings
+        out, q = [], None
+        for ch in body:
+            if q:
+                out.append(ch)
+                if ch == q:
+                    q = None
+                continue
+            if ch in "'\"":
+                q = ch
+            elif ch == "!":
+                break
+            out.append(ch)
+        body = "".join(out)
+        if cont and stmts:
+            stmts[-1] += " " + body.strip()
+        else:
+            stmts.append(body.strip())
+    res = []
+    for s in stmts:
+        if not s:
+            continue
+        for k, v in macros.items():
+            s = re.sub(r"(?<![\w])" + re.escape(k) + r"(?![\w])", v, s)
+        res.append(s)
+    return res
+
+
+def _lower(s: str) -> str:
+    out, q = [], None
+    for ch in s:
+        if q:
+            out.append(ch)
+            if ch == q:
+                q = None
+        elif ch in "'\"":
+            q = ch
+            out.append(ch)
+        else:
+            out.append(ch.lower())
+    return "".join(out)
+
+
+# ---------------------------------------------------------------------------
+# Expressions
+# ---------------------------------------------------------------------------
+
+TOK = re.compile(r"""\s*(?:
+    (?P<num>\d+\.\d+(?:[de][+-]?\d+)?|\d+\.[de][+-]?\d+|\d+\.(?![a-z])|\.\d+(?:[de][+-]?\d+)?|\d+(?:[de][+-]?\d+)?)|
+    (?P<dot>\.(?:ge|gt|le|lt|eq|ne|and|or|not|true|false)\.)|
+    (?P<id>[a-z_][a-z0-9_]*)|
+    (?P<op>\*\*|[-+*/(),:=<>])|
+    (?P<str>'[^']*')
+)""", re.X)
+
+
+def tokenize(s: str):
+    toks, pos = [], 0
+    s = s.strip()
+    while pos < len(s):
+        m = TOK.match(s, pos)
+        if not m or m.end() == pos:
+            raise F77Error(f"cannot tokenize: {s[pos:]!r}")
+        pos = m.end()
+        for kind in ("num", "dot", "id", "op", "str"):
+            if m.group(kind) is not None:
+                toks.append((kind, m.group(kind)))
+                break
+    return toks
+
+
+class Parser:
+    """Recursive descent over Fortran expression precedence."""
+
+    def __init__(self, toks):
+        self.t = toks
+        self.i = 0
+
+    def peek(self, k=0):
+        return self.t[self.i + k] if self.i + k < len(self.t) else (None, None)
+
+    def take(self, val=None):
+        tok = self.peek()
+        if val is not None and tok[1] != val:
+            raise F77Error(f"expected {val!r}, got {tok!r}")
+        self.i += 1
+        return tok
+
+    def parse(self):
+        e = self.e_or()
+        if self.i != len(self.t):
+            raise F77Error(f"trailing tokens {self.t[self.i:]}")
+        return e
+
+    def e_or(self):
+        a = self.e_and()
+        while self.peek()[1] == ".or.":
+            self.take()
+            a = ("bin", "||", a, self.e_and())
+        return a
+
+    def e_and(self):
+        a = self.e_not()
+        while self.peek()[1] == ".and.":
+            self.take()
+            a = ("bin", "&&", a, self.e_not())
+        return a
+
+    def e_not(self):
+        if self.peek()[1] == ".not.":
+            self.take()
+            return ("un", "!", self.e_not())
+        return self.e_rel()
+
+    REL = {".ge.": ">=", ".gt.": ">", ".le.": "<=", ".lt.": "<", ".eq.": "==", ".ne.": "!="}
+
+    def e_rel(self):
+        a = self.e_add()
+        if self.peek()[1] in self.REL:
+            op = self.REL[self.take()[1]]
+            a = ("bin", op, a, self.e_add())
+        return a
+
+    def e_add(self):
+        # Fortran: [sign] add-operand { add-op add-operand }; the leading sign
+        # applies to the whole first add-operand.
+        if self.peek()[1] in ("+", "-"):
+            sign = self.take()[1]
+            a = self.e_mul()
+            if sign == "-":
+                a = ("un", "-", a)
+        else:
+            a = self.e_mul()
+        while self.peek()[1] in ("+", "-"):
+            op = self.take()[1]
+            if self.peek()[1] in ("+", "-"):  # gfortran extension a + -b
+                s2 = self.take()[1]
+                b = self.e_mul()
+                if s2 == "-":
+                    b = ("un", "-", b)
+            else:
+                b = self.e_mul()
+            a = ("bin", op, a, b)
+        return a
+
+    def e_mul(self):
+        a = self.e_pow()
+        while self.peek()[1] in ("*", "/"):
+            op = self.take()[1]
+            a = ("bin", op, a, self.e_pow())
+        return a
+
+    def e_pow(self):
+        a = self.e_prim()
+        if self.peek()[1] == "**":
+            self.take()
+            if self.peek()[1] in ("+", "-"):
+                s = self.take()[1]
+                b = self.e_pow()
+                b = ("un", "-", b) if s == "-" else b
+            else:
+                b = self.e_pow()
+            return ("pow", a, b)
+        return a
+
+    def e_prim(self):
+        kind, val = self.take()
+        if kind == "num":
+            return ("num", val)
+        if kind == "dot":
+            return ("num", "1" if val == ".true." else "0") if val in (".true.", ".false.") else None
+        if kind == "str":
+            return ("str", val)
+        if kind == "id":
+            if self.peek()[1] == "(":
+                self.take("(")
+                args = []
+                if self.peek()[1] != ")":
+                    while True:
+                        args.append(self.e_or())
+                        if self.peek()[1] == ",":
+                            self.take()
+                            continue
+                        break
+                self.take(")")
+                return ("ref", val, args)
+            return ("id", val)
+        if val == "(":
+            e = self.e_or()
+            self.take(")")
+            return ("par", e)
+        raise F77Error(f"unexpected token {val!r}")
+
+
+def parse_expr(s: str):
+    return Parser(tokenize(s)).parse()
+
+
+# ---------------------------------------------------------------------------
+# Declarations and scopes
+# ---------------------------------------------------------------------------
+
+class Var:
+    def __init__(self, name, ftype, dims=None, dummy=False):
+        self.name = name
+        self.ftype = ftype          # 'int', 'double', 'logical', 'char'
+        self.dims = dims or []      # list of (lo, hi) expression strings (hi may be '*')
+        self.dummy = dummy
+
+    @property
+    def is_array(self):
+        return bool(self.dims)
+
+    def ctype(self):
+        return {"int": "int", "double": "double", "logical": "int", "char": "char"}[self.ftype]
+
+
+def split_top(s: str, sep=",") -> List[str]:
+    parts, depth, cur, q = [], 0, [], None
+    for ch in s:
+        if q:
+            cur.append(ch)
+            if ch == q:
+                q = None
+            continue
+        if ch in "'\"":
+            q = ch
+        if ch == "(":
+            depth += 1
+        elif ch == ")":
+            depth -= 1
+        if ch == sep and depth == 0:
+            parts.append("".join(cur).strip())
+            cur = []
+        else:
+            cur.append(ch)
+    if "".join(cur).strip():
+        parts.append("".join(cur).strip())
+    return parts
+
+
+TYPE_RE = re.compile(r"^(integer\*4|integer|real\*8|double precision|logical\*4|logical|character\*\(\*\)|character\*\d+|character\*\(\w+(?:-\d+)?\))\s+(.*)$")
+
+
+def ftype_of(t: str) -> str:
+    if t.startswith("integer"):
+        return "int"
+    if t.startswith("real") or t.startswith("double"):
+        return "double"
+    if t.startswith("logical"):
+        return "logical"
+    return "char"
+
+
+class Unit:
+    def __init__(self, kind, name, args, rtype=None):
+        self.kind, self.name, self.args, self.rtype = kind, name, args, rtype
+        self.vars: Dict[str, Var] = {}
+        self.params: Dict[str, str] = {}
+        self.body: List[str] = []
+
+
+def parse_units(stmts: List[str], wanted: List[str], config_params: Dict[str, str]) -> List[Unit]:
+    units, cur = [], None
+    for raw in stmts:
+        s = _lower(raw)
+        m = re.match(r"^(subroutine)\s+(\w+)\s*\((.*)\)\s*$", s) or \
+            re.match(r"^(integer\*4|real\*8|integer|logical\*4)\s+function\s+(\w+)\s*\((.*)\)\s*$", s)
+        if m and cur is None:
+            if m.group(1) == "subroutine":
+                cur = Unit("sub", m.group(2), [a.strip() for a in m.group(3).split(",") if a.strip()])
+            else:
+                cur = Unit("fun", m.group(2), [a.strip() for a in m.group(3).split(",") if a.strip()],
+                           ftype_of(m.group(1)))
+            continue
+        if cur is None:
+            continue
+        if s == "end":
+            if cur.name in wanted:
+                units.append(cur)
+            cur = None
+            continue
+        cur.body.append(s)
+    for u in units:
+        _declarations(u, config_params)
+    return units
+
+
+def _declarations(u: Unit, config_params: Dict[str, str]) -> None:
+    body = []
+    decl_done = False
+    for s in u.body:
+        if not decl_done:
+            if s == "implicit none":
+                continue
+            if s.startswith('include "config.f"') or s.startswith("include 'config.f'"):
+                u.params.update(config_params)
+                continue
+            m = re.match(r"^parameter\s*\((.*)\)$", s)
+            if m:
+                for item in split_top(m.group(1)):
+                    k, v = item.split("=", 1)
+                    u.params[k.strip()] = v.strip()
+                continue
+            m = TYPE_RE.match(s)
+            if m:
+                ft = ftype_of(m.group(1))
+                for item in split_top(m.group(2)):
+                    mm = re.match(r"^(\w+)\s*(?:\((.*)\))?$", item)
+                    if not mm:
+                        raise F77Error(f"bad declaration item {item!r} in {u.name}")
+                    name, dims = mm.group(1), mm.group(2)
+                    dl = []
+                    if dims:
+                        for d in split_top(dims):
+                            if ":" in d:
+                                lo, hi = d.split(":", 1)
+                            else:
+                                lo, hi = "1", d
+                            dl.append((lo.strip(), hi.strip()))
+                    u.vars[name] = Var(name, ft, dl, dummy=name in u.args)
+                continue
+            if s.startswith("external"):
+                continue
+            decl_done = True
+        body.append(s)
+    u.body = body
+    if u.kind == "fun" and u.name not in u.vars:
+        u.vars[u.name] = Var(u.name, u.rtype)
+    for a in u.args:
+        if a not in u.vars:
+            raise F77Error(f"undeclared dummy {a} in {u.name}")
+
+
+# ---------------------------------------------------------------------------
+# Code generation
+# ---------------------------------------------------------------------------
+
+INTRINSIC_D = {"dabs": "fabs", "dsqrt": "sqrt", "sqrt": "sqrt", "dlog": "log", "dacos": "acos"}
+
+
+class Gen:
+    def __init__(self, u: Unit, all_units: Dict[str, Unit]):
+        self.u, self.units = u, all_units
+        self.lines: List[str] = []
+        self.tmpn = 0
+        self.loop_labels: List[str] = []
+        self.label_n = 0
+
+    # -- helpers
+    def param_c(self, name):
+        return f"P_{name}"
+
+    def vtype(self, name):
+        if name in self.u.vars:
+            return self.u.vars[name].ftype
+        if name in self.u.params:
+            return "double" if re.search(r"[.]|d[+-]?\d", self.u.params[name]) else "int"
+        raise F77Error(f"unknown name {name} in {self.u.name}")
+
+    def etype(self, e) -> str:
+        k = e[0]
+        if k == "num":
+            return "double" if re.search(r"[.de]", e[1]) else "int"
+        if k == "id":
+            t = self.vtype(e[1])
+            return "int" if t == "logical" else t
+        if k == "par":
+            return self.etype(e[1])
+        if k == "un":
+            return "int" if e[1] == "!" else self.etype(e[2])
+        if k == "bin":
+            if e[1] in ("&&", "||", ">=", ">", "<=", "<", "==", "!="):
+                return "int"
+            a, b = self.etype(e[2]), self.etype(e[3])
+            return "double" if "double" in (a, b) else "int"
+        if k == "pow":
+            return self.etype(e[1])
+        if k == "ref":
+            n = e[1]
+            if n in self.u.vars and self.u.vars[n].is_array:
+                return self.vtype(n)
+            if n in ("mod", "max0", "min0"):
+                return "int"
+            if n in ("max", "min"):
+                ts = [self.etype(a) for a in e[2]]
+                return "double" if "double" in ts else "int"
+            if n in INTRINSIC_D or n in ("dmax1", "dmin1", "dble", "float"):
+                return "double"
+            if n in self.units:
+                return self.units[n].rtype
+            raise F77Error(f"unknown function {n}")
+        raise F77Error(f"type of {e}")
+
+    def index(self, var: Var, args) -> str:
+        if len(args) != len(var.dims):
+            raise F77Error(f"rank mismatch for {var.name}")
+        terms, stride = [], "1"
+        for (lo, hi), a in zip(var.dims, args):
+            lo_c = self.cexpr_str(lo)
+            terms.append(f"((long)({self.expr(a)}) - ({lo_c})) * ({stride})")
+            if hi != "*":
+                stride = f"({stride}) * (({self.cexpr_str(hi)}) - ({lo_c}) + 1)"
+        return " + ".join(terms)
+
+    def cexpr_str(self, s):
+        return self.expr(parse_expr(s))
+
+    def name_ref(self, n):
+        if n in self.u.params:
+            return self.param_c(n)
+        v = self.u.vars[n]
+        if v.dummy and not v.is_array:
+            return f"(*{n})"
+        return n
+
+    def expr(self, e) -> str:
+        k = e[0]
+        if k == "num":
+            s = e[1].replace("d", "e")
+            if re.search(r"[.e]", s):
+                if s.startswith("."):
+                    s = "0" + s
+                if re.match(r"^\d+e", s):
+                    s = s.replace("e", ".e", 1)
+                if s.endswith("."):
+                    s += "0"
+            return s
+        if k == "id":
+            return self.name_ref(e[1])
+        if k == "par":
+            return f"({self.expr(e[1])})"
+        if k == "un":
+            return f"({e[1]}{self.expr(e[2])})"
+        if k == "bin":
+            return f"({self.expr(e[2])} {e[1]} {self.expr(e[3])})"
+        if k == "pow":
+            base, ex = e[1], e[2]
+            if ex[0] == "num" and ex[1] == "2":
+                b = self.expr(base)
+                return f"({b} * {b})"
+            return f"pow((double){self.expr(base)}, (double){self.expr(ex)})"
+        if k == "ref":
+            n, args = e[1], e[2]
+            if n in self.u.vars and self.u.vars[n].is_array:
+                return f"{n}[{self.index(self.u.vars[n], args)}]"
+            if n in INTRINSIC_D:
+                return f"{INTRINSIC_D[n]}({self.expr(args[0])})"
+            if n in ("dmax1", "max", "max0", "dmin1", "min", "min0"):
+                op = ">" if "max" in n else "<"
+                acc = self.expr(args[0])
+                for a in args[1:]:
+                    b = self.expr(a)
+                    acc = f"w2r_sel{op == '>' and 'max' or 'min'}({acc}, {b})"
+                return acc
+            if n == "mod":
+                return f"({self.expr(args[0])} % {self.expr(args[1])})"
+            if n in ("dble", "float"):
+                return f"((double){self.expr(args[0])})"
+            if n in self.units:
+                return self.call(n, args)
+            raise F77Error(f"unknown reference {n}")
+        raise F77Error(f"cannot emit {e}")
+
+    def call(self, n, args) -> str:
+        cu = self.units[n]
+        if len(args) != len(cu.args):
+            raise F77Error(f"call {n}: {len(args)} args, expected {len(cu.args)}")
+        cargs = []
+        for a, formal in zip(args, cu.args):
+            fv = cu.vars[formal]
+            if a[0] == "id" and a[1] in self.u.vars:
+                v = self.u.vars[a[1]]
+                if v.is_array:
+                    cargs.append(a[1])
+                elif v.dummy:
+                    cargs.append(a[1])
+                else:
+                    cargs.append(f"&{a[1]}")
+                continue
+            if a[0] == "ref" and a[1] in self.u.vars and self.u.vars[a[1]].is_array:
+                cargs.append(f"&{self.expr(a)}")
+                continue
+            # expression or parameter: pass a temporary
+            t = f"t_{self.tmpn}"
+            self.tmpn += 1
+            ct = "double" if fv.ftype == "double" else "int"
+            self.emit(f"{ct} {t} = {self.expr(a)};")
+            cargs.append(f"&{t}")
+        return f"{n}_({', '.join(cargs)})"
+
+    def emit(self, s):
+        self.lines.append("  " * (1 + len(self.loop_labels)) + s)
+
+    def gen(self) -> str:
+        u = self.u
+        proto = self.prototype(u)
+        out = [proto + " {"]
+        # parameters
+        for k, v in u.params.items():
+            ct = "double" if re.search(r"[.]|\d[de][+-]?\d", v) else "int"
+            if k in ("mnx", "mny"):
+                out.append(f"  const int P_{k} = W2R_{k.upper()};")
+                continue
+            out.append(f"  const {ct} P_{k} = {self.cexpr_str(v) if not re.match(r'^[-+]?[0-9.]+(?:[de][-+]?[0-9]+)?$', v) else self.expr(('num', v))};")
+        # locals
+        frees = []
+        for name, v in u.vars.items():
+            if v.dummy:
+                continue
+            ct = v.ctype()
+            if name == u.name and u.kind == "fun":
+                out.append(f"  {ct} {name} = 0;")
+                continue
+            if not v.is_array:
+                out.append(f"  {ct} {name};")
+                continue
+            size = " * ".join(f"(({self.cexpr_str(hi)}) - ({self.cexpr_str(lo)}) + 1)" for lo, hi in v.dims)
+            const = all(self._is_const(hi) and self._is_const(lo) for lo, hi in v.dims)
+            if const:
+                # gfortran's stack/static choice is made at the reference's
+                # own compile-time sizes (include/config.f), where every
+                # mnx x mny work array exceeds the stack limit and so lives
+                # in zero-initialised static storage; keep that choice when
+                # the bounds are raised or lowered for a build.
+                nbytes = self._const_val(size, REF_DEFAULT) * (8 if ct == "double" else 4)
+                csize = self._macro_size(size)
+                if nbytes > STACK_LIMIT:
+                    out.append(f"  static {ct} {name}[{csize}];")
+                else:
+                    out.append(f"  {ct} {name}[{csize}];")
+            else:
+                out.append(f"  {ct} *{name} = ({ct} *)malloc(sizeof({ct}) * (size_t)({size}));")
+                frees.append(name)
+        self.frees = frees
+        for s in u.body:
+            self.stmt(s)
+        if self.loop_labels:
+            raise F77Error(f"unclosed block in {u.name}")
+        out.extend(self.lines)
+        out.append("ret:")
+        for f in frees:
+            out.append(f"  free({f});")
+        out.append(f"  return{(' ' + u.name) if u.kind == 'fun' else ''};")
+        out.append("}")
+        return "\n".join(out)
+
+    def _is_const(self, s):
+        e = parse_expr(s)
+        def ok(x):
+            if x[0] == "num":
+                return True
+            if x[0] == "id":
+                return x[1] in self.u.params
+            if x[0] in ("par",):
+                return ok(x[1])
+            if x[0] == "un":
+                return ok(x[2])
+            if x[0] == "bin":
+                return ok(x[2]) and ok(x[3])
+            if x[0] == "ref" and x[1] in ("max0", "max", "min"):
+                return all(ok(a) for a in x[2])
+            return False
+        return ok(e)
+
+    def _const_val(self, cexpr: str, override: Optional[Dict[str, str]] = None) -> int:
+        params = dict(self.u.params)
+        if override:
+            params.update({k: v for k, v in override.items() if k in params})
+        # evaluate parameters recursively in Python
+        def pv(name):
+            e = parse_expr(params[name])
+            return ev(e)
+        def ev(x):
+            if x[0] == "num":
+                return float(x[1].replace("d", "e")) if re.search(r"[.de]", x[1]) else int(x[1])
+            if x[0] == "id":
+                return pv(x[1])
+            if x[0] == "par":
+                return ev(x[1])
+            if x[0] == "un":
+                return -ev(x[2])
+            if x[0] == "bin":
+                a, b = ev(x[2]), ev(x[3])
+                return {"+": a + b, "-": a - b, "*": a * b, "/": a // b}[x[1]]
+            if x[0] == "ref":
+                return max(ev(a) for a in x[2])
+            raise F77Error("const")
+        py = cexpr
+        for k in sorted(params, key=len, reverse=True):
+            py = re.sub(r"\bP_" + k + r"\b", str(pv(k)), py)
+        py = py.replace("(long)", "")
+        return int(eval(py))  # noqa: S307 -- integer arithmetic on literals only
+
+    def _macro_size(self, cexpr: str) -> str:
+        """A C integer constant expression for an array size: parameters
+        expanded, mnx/mny left as the build's W2R_MNX/W2R_MNY macros."""
+        py = cexpr.replace("(long)", "")
+        for _ in range(8):
+            changed = False
+            for k in sorted(self.u.params, key=len, reverse=True):
+                pat = r"\bP_" + k + r"\b"
+                if re.search(pat, py):
+                    if k in ("mnx", "mny"):
+                        rep = f"(W2R_{k.upper()})"
+                    else:
+                        rep = "(" + self.cexpr_str(self.u.params[k]).replace("(long)", "") + ")"
+                    py = re.sub(pat, rep, py)
+                    changed = True
+            if not changed:
+                break
+        return py.replace("w2r_selmax", "W2R_IMAX")
+
+    def prototype(self, u: Unit) -> str:
+        ps = []
+        for a in u.args:
+            v = u.vars[a]
+            ps.append(f"{v.ctype()} *{a}")
+        rt = "void" if u.kind == "sub" else {"int": "int", "double": "double"}[u.rtype]
+        return f"{rt} {u.name}_({', '.join(ps)})"
+
+    # -- statements
+    def stmt(self, s: str):
+        m = re.match(r"^do\s+(\w+)\s*=\s*(.*)$", s)
+        if m:
+            var = m.group(1)
+            parts = split_top(m.group(2))
+            lo, hi = self.cexpr_str(parts[0]), self.cexpr_str(parts[1])
+            step = parts[2] if len(parts) > 2 else "1"
+            st = int(step.replace(" ", ""))
+            cmp = "<=" if st > 0 else ">="
+            v = self.name_ref(var)
+            self.emit(f"for ({v} = {lo}; {v} {cmp} {hi}; {v} += {st}) {{")
+            self.label_n += 1
+            self.loop_labels.append(f"L{self.label_n}")
+            return
+        if s in ("end do", "enddo"):
+            lab = self.loop_labels.pop()
+            self.emit("}")
+            self.emit(f"{lab}_exit:;")
+            return
+        m = re.match(r"^if\s*\((.*)\)\s*then$", s)
+        if m and self._balanced_if(s):
+            self.emit(f"if ({self.cexpr_str(self._if_cond(s))}) {{")
+            self.loop_labels.append("IF")
+            return
+        m = re.match(r"^else\s*if\s*\((.*)\)\s*then$", s)
+        if m:
+            cond = self._if_cond(s[s.index("if"):])
+            self.loop_labels.pop()
+            self.emit(f"}} else if ({self.cexpr_str(cond)}) {{")
+            self.loop_labels.append("IF")
+            return
+        if s == "else":
+            self.loop_labels.pop()
+            self.emit("} else {")
+            self.loop_labels.append("IF")
+            return
+        if s in ("end if", "endif"):
+            self.loop_labels.pop()
+            self.emit("}")
+            return
+        m = re.match(r"^select\s+case\s*\((.*)\)$", s)
+        if m:
+            self.emit(f"switch ({self.cexpr_str(m.group(1))}) {{")
+            self.loop_labels.append("SEL")
+            self.loop_labels.append("CASE0")
+            return
+        m = re.match(r"^case\s*\((.*)\)$", s)
+        if m or s == "case default":
+            top = self.loop_labels.pop()
+            if top != "CASE0":
+                self.emit("  break; }")
+            if s == "case default":
+                self.emit("default: {")
+            else:
+                labels = " ".join(f"case {self.cexpr_str(x)}:" for x in split_top(m.group(1)))
+                self.emit(f"{labels} {{")
+            self.loop_labels.append("CASE")
+            return
+        if s == "end select":
+            top = self.loop_labels.pop()
+            if top == "CASE":
+                self.emit("  break; }")
+            self.loop_labels.pop()
+            self.emit("}")
+            return
+        if s.startswith("if") and self._balanced_if(s) is False:
+            cond = self._if_cond(s)
+            rest = s[self._if_end(s):].strip()
+            self.emit(f"if ({self.cexpr_str(cond)}) {{")
+            self.loop_labels.append("IF")
+            self.stmt(rest)
+            self.loop_labels.pop()
+            self.emit("}")
+            return
+        if s == "return":
+            self.emit("goto ret;")
+            return
+        if s == "stop":
+            self.emit(f'w2r_stop("{self.u.name}");')
+            return
+        if s == "continue":
+            return
+        if s == "cycle":
+            self.emit("continue;")
+            return
+        if s == "exit":
+            loops = [l for l in self.loop_labels if l.startswith("L")]
+            self.emit(f"goto {loops[-1]}_exit;")
+            return
+        if s.startswith("print") or s.startswith("write"):
+            return
+        m = re.match(r"^call\s+(\w+)\s*\((.*)\)$", s)
+        if m:
+            args = [parse_expr(a) for a in split_top(m.group(2))]
+            self.emit(self.call(m.group(1), args) + ";")
+            return
+        # assignment
+        lhs, rhs = self._split_assign(s)
+        le = parse_expr(lhs)
+        self.emit(f"{self.expr(le)} = {self.expr(parse_expr(rhs))};")
+
+    def _if_end(self, s):
+        depth = 0
+        i = s.index("(")
+        for k in range(i, len(s)):
+            if s[k] == "(":
+                depth += 1
+            elif s[k] == ")":
+                depth -= 1
+                if depth == 0:
+                    return k + 1
+        raise F77Error(f"unbalanced if {s}")
+
+    def _if_cond(self, s):
+        i = s.index("(")
+        return s[i + 1:self._if_end(s) - 1]
+
+    def _balanced_if(self, s):
+        if not re.match(r"^if\s*\(", s):
+            return None
+        rest = s[self._if_end(s):].strip()
+        return rest == "then"
+
+    def _split_assign(self, s):
+        depth = 0
+        for k, ch in enumerate(s):
+            if ch == "(":
+                depth += 1
+            elif ch == ")":
+                depth -= 1
+            elif ch == "=" and depth == 0:
+                return s[:k], s[k + 1:]
+        raise F77Error(f"unrecognised statement: {s!r}")
+
+
+def _config_params(mnx: int, mny: int) -> Dict[str, str]:
+    p = {}
+    for raw in open(os.path.join(REF_ROOT, "include", "config.f")):
+        m = re.match(r"\s+parameter\s*\(\s*(\w+)\s*=\s*(\d+)\s*\)", raw, re.I)
+        if m:
+            p[m.group(1).lower()] = m.group(2)
+    # the reference tells the user to raise mnx/mny for larger grids
+    # (src/grid.f:551-575); the translation does the same per build
+    p["mnx"], p["mny"] = str(mnx), str(mny)
+    return p
+
+
+def translate(mnx: int, mny: int, signatures: Optional[dict] = None) -> str:
+    macros = _macros()
+    cfg = _config_params(mnx, mny)
+    all_units: Dict[str, Unit] = {}
+    order: List[Unit] = []
+    for path, names in ROUTINES.items():
+        stmts = _statements(os.path.join(REF_ROOT, path), macros)
+        for u in parse_units(stmts, names, cfg):
+            all_units[u.name] = u
+            order.append(u)
+    missing = {n for ns in ROUTINES.values() for n in ns} - set(all_units)
+    if missing:
+        raise F77Error(f"routines not found: {sorted(missing)}")
+    gens = [Gen(u, all_units) for u in order]
+    if signatures is not None:
+        for u in order:
+            signatures[u.name] = {"kind": u.kind, "rtype": u.rtype,
+                                  "args": [[a, u.vars[a].ftype, u.vars[a].is_array] for a in u.args]}
+    head = ["/* Generated by oracle/f77ref.py from the reference's Fortran source.",
+            " * Derived from the reference: do not commit. */",
+            "#include <math.h>", "#include <stdio.h>", "#include <stdlib.h>",
+            "#ifndef W2R_MNX", "#define W2R_MNX 302", "#endif",
+            "#ifndef W2R_MNY", "#define W2R_MNY 302", "#endif",
+            "#define W2R_IMAX(a, b) ((b) > (a) ? (b) : (a))",
+            "#define w2r_selmax(a, b) ((b) > (a) ? (b) : (a))",
+            "#define w2r_selmin(a, b) ((b) < (a) ? (b) : (a))",
+            "int w2r_stopped = 0;",
+            "static void w2r_stop(const char *w) { fprintf(stderr, \"stop in %s\\n\", w); exit(3); }"]
+    protos = [g.prototype(g.u) + ";" for g in gens]
+    bodies = [g.gen() for g in gens]
+    return "\n".join(head + protos + [""] + bodies) + "\n"
+
+
+def _stale(src: str) -> bool:
+    t = os.path.getmtime(src)
+    deps = [os.path.abspath(__file__)] + [os.path.join(REF_ROOT, p) for p in ROUTINES] + \
+        [os.path.join(REF_ROOT, "include", f) for f in ("config.f", "wolfd2.h")]
+    return any(os.path.exists(d) and os.path.getmtime(d) > t for d in deps)
+
+
+def available() -> bool:
+    return os.path.isdir(os.path.join(REF_ROOT, "src"))
+
+
+def lib_path(mnx: int, mny: int) -> str:
+    return os.path.join(OUT, f"libwolfd2ref_{mnx}x{mny}.so")
+
+
+def build(mnx: int = 0, mny: int = 0) -> Optional[str]:
+    """Generate the C (where the reference source is present) and compile a
+    library for array bounds (0:mnx,0:mny).  Returns its path, or None when
+    neither the source nor previously generated C is available."""
+    os.makedirs(OUT, exist_ok=True)
+    src = GEN_C
+    if available() and (not os.path.exists(src) or _stale(src)):
+        sig = {}
+        with open(src, "w") as f:
+            f.write(translate(mnx or 302, mny or 302, sig))
+        import json
+        with open(os.path.join(OUT, "signatures.json"), "w") as f:
+            json.dump(sig, f, indent=1)
+    if not os.path.exists(src):
+        return None
+    if not mnx:
+        return src
+    out = lib_path(mnx, mny)
+    if not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(src):
+        subprocess.run(["cc", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+                        f"-DW2R_MNX={mnx}", f"-DW2R_MNY={mny}", "-w",
+                        "-o", out, src, "-lm"], check=True)
+    return out
+
+
+def load(mnx: int, mny: int):
+    path = lib_path(mnx, mny)
+    if not os.path.exists(path):
+        path = build(mnx, mny)
+    if not path:
+        return None
+    return C.CDLL(path)
+
+
+class RefLib:
+    """Calls translated reference routines by name with keyword arguments:
+    numpy arrays for array dummies (Fortran layout, float64 or int32) and
+    Python numbers for scalars (passed by reference like Fortran)."""
+
+    def __init__(self, mnx: int, mny: int):
+        import json
+        self.L = load(mnx, mny)
+        if self.L is None:
+            raise FileNotFoundError("reference translation not available")
+        self.sig = json.load(open(os.path.join(OUT, "signatures.json")))
+        self.mnx, self.mny = mnx, mny
+
+    def __call__(self, name: str, **kw):
+        import numpy as np
+        s = self.sig[name]
+        fn = getattr(self.L, name + "_")
+        cargs, keep = [], []
+        for an, ft, is_arr in s["args"]:
+            if an not in kw:
+                raise TypeError(f"{name}: missing argument {an}")
+            v = kw[an]
+            if is_arr:
+                want = np.float64 if ft == "double" else np.int32
+                if not isinstance(v, np.ndarray) or v.dtype != want or not v.flags["F_CONTIGUOUS"]:
+                    raise TypeError(f"{name}: {an} must be a Fortran-ordered {want.__name__} array")
+                cargs.append(C.c_void_p(v.ctypes.data))
+            else:
+                box = C.c_double(float(v)) if ft == "double" else C.c_int(int(v))
+                keep.append(box)
+                cargs.append(C.byref(box))
+        if s["kind"] == "fun":
+            fn.restype = C.c_double if s["rtype"] == "double" else C.c_int
+        else:
+            fn.restype = None
+        r = fn(*cargs)
+        outs = {an: keep[i].value for i, (an, ft, arr) in
+                enumerate([a for a in s["args"] if not a[2]])}
+        return r, outs

@@ -1,0 +1,79 @@
+"""Host-side case setup: the boundary_conditions grammar, SetUpBCs passes,
+restart records and deck writers."""
+import os
+
+import numpy as np
+import pytest
+
+from wolfd2_gb300 import deck
+from wolfd2_gb300.deck import BM_INLET, BM_INTERN, BM_OUTLT1, BM_OUTLT2, BM_WALL1, BM_WALL2
+
+
+def test_cavity_tables():
+    c = deck.cavity(64, 100.0, 0.005)
+    r = c.regions
+    assert (r.n_i, r.n_j) == (1, 1)
+    assert [r.border(1, 1, f) for f in (1, 2, 3, 4)] == [1, 65, 1, 65]
+    assert [r.btype(1, 1, f) for f in (1, 2, 3, 4)] == [BM_WALL1] * 4
+    assert r.dBCVal[0, 0, deck.NORTH - 1, deck.VAR_U - 1] == 1.0
+    assert c.params.re == 100.0 and c.params.npsolver == 1 and c.params.lcartes == 1
+
+
+def test_region_borders_and_consistency():
+    text = """number_of_regions 3 2
+i_borders 10 20
+j_borders 8
+wall 1 1 east no_stress     # internal wall between (1,1) and (2,1)
+inlet 2 2 south nv 0.5
+inlet 1 2 south nv 0.25
+outlet 3 1 east fd p 2.0
+outlet 3 2 east
+blockage 2 1"""
+    r = deck.parse_bc_section(text, 33, 17)
+    assert [r.border(2, 2, f) for f in (1, 2, 3, 4)] == [10, 20, 8, 17]
+    assert r.btype(3, 1, deck.EAST) == BM_OUTLT1 and r.btype(3, 2, deck.EAST) == BM_OUTLT2
+    # blockage makes its faces and the neighbours' shared faces no-slip walls
+    assert r.btype(1, 1, deck.EAST) == BM_WALL1 and r.btype(3, 1, deck.WEST) == BM_WALL1
+    # a later blockage line overrides the earlier inlet on its shared face
+    assert r.btype(2, 2, deck.SOUTH) == BM_WALL1 and r.btype(2, 1, deck.NORTH) == BM_WALL1
+    # an inlet propagates to the neighbour's shared face (bound_cond.f:210-223)
+    assert r.btype(1, 1, deck.NORTH) == BM_INLET
+    assert r.dBCVal[0, 1, deck.SOUTH - 1, deck.VAR_V - 1] == 0.25
+    assert r.dBCVal[2, 0, deck.EAST - 1, deck.VAR_P - 1] == 2.0
+    assert r.btype(2, 2, deck.WEST) == BM_INTERN
+
+
+@pytest.mark.parametrize("bad", [
+    "number_of_regions 2 1\ni_borders 1\nj_borders\n",          # border < 2
+    "number_of_regions 1 1\ni_borders\nj_borders\nwall 1 1 up\n",
+    "number_of_regions 1 1\ni_borders\nj_borders\nwhatever 1 1\n",
+    "i_borders 3\n",
+])
+def test_rejected_decks(bad):
+    with pytest.raises(deck.DeckError):
+        deck.parse_bc_section(bad, 17, 17)
+
+
+def test_restart_round_trip(tmp_path):
+    rng = np.random.default_rng(0)
+    flds = [np.asfortranarray(rng.normal(size=(10, 8))) for _ in range(8)]
+    path = str(tmp_path / "r.rst")
+    deck.write_restart(path, 7, 0.35, 8, 6, flds)
+    k, t, nx, ny, back = deck.read_restart(path)
+    assert (k, t, nx, ny) == (7, 0.35, 8, 6)
+    for a, b in zip(flds, back):
+        assert np.array_equal(a, b)
+
+
+def test_deck_files(tmp_path):
+    c = deck.channel(16, 8, 500.0, 1e-3)
+    deck.write_deck(str(tmp_path / "input.dat"), c, nts=3)
+    deck.write_grid_plot3d(str(tmp_path / "grid.xyz"), c.x, c.y)
+    deck.write_fluid_table(str(tmp_path / "fluidprop.dat"), 1.0, 0.002)
+    txt = open(tmp_path / "input.dat").read()
+    assert "ppe_solver rb_sor" in txt and "outlet 1 1 east fd" in txt
+    first = open(tmp_path / "grid.xyz").readline().split()
+    assert first == ["17", "9"]
+    sec = txt.split("section boundary_conditions")[1].split("end section")[0]
+    r = deck.parse_bc_section(sec, c.nx, c.ny)
+    assert np.array_equal(r.nMomBdTp, c.regions.nMomBdTp)

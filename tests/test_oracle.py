@@ -1,0 +1,96 @@
+"""CPU checks of the oracle against independent restatements (numpy/scipy)
+and against properties the reference's discretisation must have."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+import scipy.linalg
+
+import oracle as O
+from wolfd2_gb300 import deck
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def test_alt_trid_lu_matches_patched_banded_solve():
+    """AltTridLU (momentum.f:1307-1339) divides row 1's super-diagonal by
+    row 2's original diagonal.  Its L*U product is the original matrix with
+    row 1's super-diagonal replaced by a3(1)*a2(1)/a2(2); solving that system
+    with LAPACK must give the same x."""
+    rng = np.random.default_rng(7)
+    for n in (2, 3, 17, 200):
+        a = np.empty((3, n))
+        a[0] = rng.uniform(-0.4, 0.4, n)
+        a[1] = rng.uniform(1.5, 2.5, n)
+        a[2] = rng.uniform(-0.4, 0.4, n)
+        b = rng.normal(size=n)
+        x = O.alt_trid_lu(a, b)
+        ab = np.zeros((3, n))
+        ab[0, 1:] = a[2, :-1]
+        ab[0, 1] = a[2, 0] * a[1, 0] / a[1, 1]
+        ab[1] = a[1]
+        ab[2, :-1] = a[0, 1:]
+        ref = scipy.linalg.solve_banded((1, 1), ab, b)
+        np.testing.assert_allclose(x, ref, rtol=1e-12, atol=1e-14)
+
+
+def test_perturbation_ic_is_discretely_divergence_free():
+    case = deck.cavity(48, 1000.0, 1e-3)
+    u, v, p = deck.perturbation_ic(case, 3)
+    nx, ny = case.nx, case.ny
+    h = 1.0 / 48
+    # Divergence nloc=1 on a Cartesian grid reduces to face differences
+    div = (u[1:nx + 1, 1:ny + 1] - u[0:nx, 1:ny + 1]) * h + (v[1:nx + 1, 1:ny + 1] - v[1:nx + 1, 0:ny]) * h
+    assert np.max(np.abs(div[1:, 1:])) < 1e-15
+    assert np.max(np.abs(u)) > 0.1
+
+
+def test_ppe_operator_symmetric_with_constant_nullspace():
+    """The 5-point operator of pressure.f:97-106 built from the metrics:
+    symmetric, and its interior rows sum to zero."""
+    case = deck.channel(20, 12, 100.0, 1e-3, length=1.7)
+    o = O.Oracle(case.nx + 1, case.ny + 1)
+    m = o.grid(case.nx, case.ny, case.x, case.y)
+    rau, rgv = m["rau"], m["rgv"]
+    nx, ny = case.nx, case.ny
+    for j in range(2, ny + 1):
+        for i in range(2, nx + 1):
+            a1, a2, a4, a5 = rgv[i, j - 1], rau[i - 1, j], rau[i, j], rgv[i, j]
+            a3 = -rau[i, j] - rau[i - 1, j] - rgv[i, j] - rgv[i, j - 1]
+            assert abs(a1 + a2 + a3 + a4 + a5) <= 1e-12 * abs(a3)
+            if i < nx:
+                assert a4 == rau[(i + 1) - 1, j]     # east coefficient = neighbour's west
+            if j < ny:
+                assert a5 == rgv[i, (j + 1) - 1]     # north coefficient = neighbour's south
+
+
+def test_boundary_rules_on_cavity():
+    case = deck.cavity(16, 100.0, 1e-3, lid=1.5)
+    o = O.Oracle(case.nx + 1, case.ny + 1)
+    rng = np.random.default_rng(1)
+    u, v, p = (np.asfortranarray(rng.normal(size=(case.nx + 2, case.ny + 2))) for _ in range(3))
+    o.vel_bound_cond(case.nx, case.ny, case.regions, u, v)
+    o.pres_bound_cond(case.nx, case.ny, case.regions, p)
+    nx, ny = case.nx, case.ny
+    assert np.all(u[1, 1:ny + 1] == 0) and np.all(u[nx, 1:ny + 1] == 0)          # no-slip walls
+    np.testing.assert_array_equal(v[1, 2:ny + 1], -v[2, 2:ny + 1])                  # image points
+    np.testing.assert_array_equal(u[2:nx + 1, ny + 1], 2 * 1.5 - u[2:nx + 1, ny])   # moving lid
+    np.testing.assert_array_equal(u[2:nx, 1], -u[2:nx, 2])
+    np.testing.assert_array_equal(p[1, 2:ny + 1], p[2, 2:ny + 1])                   # Neumann
+    np.testing.assert_array_equal(p[2:nx + 1, ny + 1], p[2:nx + 1, ny])
+
+
+def test_golden_cavity64():
+    """Regression fixture of the 64x64 cavity (config 1) generated by
+    tests/golden/make_golden.py."""
+    g = json.load(open(os.path.join(HERE, "golden", "cavity64_sor.json")))
+    case = deck.cavity(64, 100.0, 0.005, solver="sor")
+    r = O.OracleRun(case)
+    r.step(g["steps"])
+    assert r.cold_nconv == g["cold_nconv"]
+    assert [[h[0], h[1]] for h in r.history] == g["iterations"]
+    for k in ("u", "v", "p"):
+        assert math.fsum(r.f[k].ravel()) == g["sum"][k]
+        assert math.fsum(np.abs(r.f[k]).ravel()) == g["abs_sum"][k]
