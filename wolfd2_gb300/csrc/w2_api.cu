@@ -230,7 +230,10 @@ int pick_blocks(w2_ctx *c, const void *kern, long work) {
   int occ = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, c->threads, 0);
   occ = std::max(1, std::min(occ, c->blocks_per_sm));
+  // tiny grids: one block (grid barriers become __syncthreads); otherwise at
+  // least one block per SM, up to the co-resident limit
   long want = (work + 4095) / 4096;
+  if (want > 1) want = std::max<long>(want, c->nsm);
   long nb = std::max<long>(1, std::min<long>(want, (long)occ * c->nsm));
   return (int)nb;
 }
@@ -530,6 +533,19 @@ int wolfd2gpu_tune(w2_ctx *c, int chain_seg, int chain_warm, int threads, int bl
   return set_segments(c);
 }
 
+static int finish_coefficients(w2_ctx *c) {
+  int *flag = &c->dev.sync->iout[7];
+  CK(cudaMemsetAsync(flag, 0, sizeof(int), c->st));
+  c->launches++;
+  k_ppe_check<<<grid_blocks(c), c->threads, 0, c->st>>>(c->dev, flag);
+  CK(cudaGetLastError());
+  int h = 1;
+  CK(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->dev.ppe_unit = (h == 0) ? 1 : 0;
+  return W2_OK;
+}
+
 int wolfd2gpu_set_metrics(w2_ctx *c, const double *const *metrics) {
   if (!c || !metrics) return W2_E_ARG;
   for (int k = 0; k < W2_NMETRIC; ++k) {
@@ -540,7 +556,8 @@ int wolfd2gpu_set_metrics(w2_ctx *c, const double *const *metrics) {
   c->launches++;
   k_ppe_coef<<<grid_blocks(c), c->threads, 0, c->st>>>(c->dev);
   CK(cudaGetLastError());
-  CK(cudaStreamSynchronize(c->st));
+  int rc = finish_coefficients(c);
+  if (rc) return rc;
   c->metrics_ok = true;
   return W2_OK;
 }
@@ -585,7 +602,8 @@ int wolfd2gpu_grid_metric(w2_ctx *c, const double *gx, const double *gy, double 
   c->launches++;
   k_ppe_coef<<<gb, c->threads, 0, c->st>>>(c->dev);
   CK(cudaGetLastError());
-  CK(cudaStreamSynchronize(c->st));
+  rc = finish_coefficients(c);
+  if (rc) return rc;
   c->metrics_ok = true;
   return W2_OK;
 }

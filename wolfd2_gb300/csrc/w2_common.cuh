@@ -109,6 +109,7 @@ struct Dev {
   Sync *sync;
   int seg, warm;       // chain segment length and warm-up rows
   int has_outflow;     // any OUTLT1/OUTLT2 face (VelOutflowBCs not a no-op)
+  int ppe_unit;        // every PPE row is the unit stencil (1,1,-4,1,1)
 };
 
 __device__ __forceinline__ size_t IX(const Dev &d, int i, int j) {

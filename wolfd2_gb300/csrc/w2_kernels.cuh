@@ -135,6 +135,7 @@ __global__ void k_metric(Dev d, MetricOut m, const double *xn, const double *yn,
 }
 
 __global__ void k_ppe_coef(Dev d) { ppe_coefficients(d); }
+__global__ void k_ppe_check(Dev d, int *flag) { ppe_check_unit(d, flag); }
 
 // ---- field copies -------------------------------------------------------
 __global__ void k_copy3(Dev d, double *a, const double *a0, double *b, const double *b0,
