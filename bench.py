@@ -198,6 +198,8 @@ def run_ours(args):
     case = make_case(args)
     u0, v0, p0 = deck.perturbation_ic(case, args.seed + rank)
     s = Solver.for_case(case)
+    if args.threads or args.blocks_per_sm or args.seg or args.warm:
+        s.tune(seg=args.seg, warm=args.warm, threads=args.threads, blocks_per_sm=args.blocks_per_sm)
     prm = case.params
     st = torch.cuda.ExternalStream(s.stream(), device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -341,6 +343,10 @@ def main():
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--threads", type=int, default=0, help="threads per block (0: library default)")
+    ap.add_argument("--blocks-per-sm", type=int, default=0)
+    ap.add_argument("--seg", type=int, default=0, help="chain segment rows (0: auto)")
+    ap.add_argument("--warm", type=int, default=0, help="chain warm-up rows (0: default)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
