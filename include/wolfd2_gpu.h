@@ -178,6 +178,8 @@ const char *wolfd2gpu_last_error(w2_ctx *ctx);
 
 /* Library configuration knobs (segment length and warm-up of the chain
  * recurrence, threads per block, blocks per SM); 0 keeps the default.
+ * blocks_per_sm = -1 selects the one-colour-per-barrier red/black sweep,
+ * -2 forces the tiled two-sweeps-per-barrier form at any grid size.
  * Takes effect on the next launch. */
 int wolfd2gpu_tune(w2_ctx *ctx, int chain_seg, int chain_warm, int threads,
                    int blocks_per_sm);

@@ -176,3 +176,42 @@ def test_cavity64_lexicographic_sor_500_steps():
     u, v, p = s.store_fields()
     for name, g in (("u", u), ("v", v), ("p", p)):
         assert np.array_equal(g, ref.f[name]), (name, rel_err(g, ref.f[name]))
+
+
+@pytest.mark.parametrize("sortol", [1e-8, 3e-6, 1e-5, 2e-5])
+@pytest.mark.parametrize("msorit", [301, 300])
+def test_tiled_red_black_sweeps(sortol, msorit):
+    """Two sweeps per barrier on shared-memory tiles (forced on a small
+    grid): bit-identical p and nSorConv for stopping points on either sweep
+    of a pair and for odd and even msorit."""
+    case = deck.cavity(128, 400.0, 0.002, solver="rb_sor", ny=64)
+    o, met = oracle_setup(case)
+    s = Solver.for_case(case)
+    s.tune(blocks_per_sm=-2)
+    f = fields_for(case, 9, amp=0.05)
+    u, v = f["u"], f["v"]
+    p = f["p"].copy(order="F")
+    o.vel_bound_cond(case.nx, case.ny, case.regions, u, v)
+    o.pres_bound_cond(case.nx, case.ny, case.regions, p)
+    gp = p.copy(order="F")
+    prm = deck.RunParams(**{**case.params.__dict__, "sortol": sortol})
+    n_o = o.ppe(case.nx, case.ny, case.regions, prm, met, u, v, p, npsolver=5, msorit=msorit)
+    n_g = s.Ppe(True, 5, msorit, prm.dk, sortol, prm.sorrel, u, v, gp)
+    assert n_g == n_o
+    assert np.array_equal(gp, p), rel_err(gp, p)
+
+
+def test_tiled_time_loop_512():
+    """The benchmark's code path (tiled sweeps, unit stencil) over a few
+    steps of a 512x512 cavity from the seeded perturbation."""
+    case = deck.cavity(512, 1000.0, 2.5e-4, solver="rb_sor")
+    u0, v0, p0 = deck.perturbation_ic(case, 1234)
+    ref = O.OracleRun(case, fields={"u": u0, "v": v0, "p": p0}, cold_start=False)
+    ref.step(2)
+    s = Solver.for_case(case)
+    s.load_fields(u0, v0, p0)
+    hist = s.step(case.params, 2)
+    assert [(h[0], h[1]) for h in hist] == [(h[0], h[1]) for h in ref.history]
+    u, v, p = s.store_fields()
+    for name, g in (("u", u), ("v", v), ("p", p)):
+        assert np.array_equal(g, ref.f[name]), (name, rel_err(g, ref.f[name]))

@@ -44,6 +44,12 @@ struct w2_ctx {
   std::vector<cudaEvent_t> ev_pool;
   double prof_ms[W2_K_NKINDS] = {};
   long long prof_n[W2_K_NKINDS] = {};
+  // tiled red/black sweeps
+  bool tiled_ok = false;
+  int tiled_blocks = 0, tiled_threads = 512;
+  size_t tiled_smem = 0;
+  TileGeom tg{};
+  int use_tiled = 1;
 };
 
 namespace {
@@ -337,8 +343,77 @@ int launch_naux(w2_ctx *c, int mqiter, double dk, double re, double qtol, const 
   return coop(c, (const void *)k_naux, blocks, args);
 }
 
+// Tile geometry for the tiled red/black kernel: ntx*nty = k * blocks tiles
+// (k as small as the shared-memory limit allows), choosing the split with
+// the least redundant halo work per block.
+void plan_tiles(w2_ctx *c) {
+  c->tiled_ok = false;
+  int dev = c->device, maxsmem = 0;
+  cudaDeviceGetAttribute(&maxsmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t limit = (size_t)maxsmem - 4096;  // leave room for static shared arrays
+  if (cudaFuncSetAttribute((const void *)k_ppe_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)limit) != cudaSuccess)
+    return;
+  const int NX = c->nx - 1, NY = c->ny - 1;
+  double best = 1e300;
+  // every split into ntx x nty tiles of at least 8 x 8 unknowns; blocks
+  // (one per SM) take ceil(tiles / nsm) tiles each, so the cost of a split is
+  // that count times the area swept per tile over a group of sweeps
+  for (int ntx = 1; ntx <= NX / 8; ++ntx) {
+    const int tx = (NX + ntx - 1) / ntx;
+    if ((NX + tx - 1) / tx != ntx) continue;
+    for (int nty = 1; nty <= NY / 8; ++nty) {
+      const int ty = (NY + nty - 1) / nty;
+      if ((NY + ty - 1) / ty != nty) continue;
+      const size_t smem = (size_t)(tx + 2 * kHalo) * (ty + 2 * kHalo) * 16;
+      if (smem > limit) continue;
+      double area = 0.0;
+      for (int e = kHalo - 1; e >= 0; --e) area += (double)(tx + 2 * e) * (ty + 2 * e);
+      const long per_block = ((long)ntx * nty + c->nsm - 1) / c->nsm;
+      const double cost = per_block * area;
+      if (cost < best) {
+        best = cost;
+        c->tg = TileGeom{tx, ty, ntx, nty};
+        c->tiled_smem = smem;
+      }
+    }
+  }
+  if (best >= 1e300) return;
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void *)k_ppe_tiled, c->tiled_threads,
+                                                c->tiled_smem);
+  if (occ < 1) return;
+  c->tiled_blocks = c->nsm;  // one block per SM, each owning ntiles/nsm tiles
+  c->tiled_ok = true;
+}
+
+// The tiled kernel pays for its halo work only on large grids (one barrier
+// costs about as much as sweeping ~0.15 M points); use_tiled == 2 forces it.
+bool tiled_applies(w2_ctx *c, int npsolver, double sorrel) {
+  const long cells = (long)(c->nx - 1) * (c->ny - 1);
+  const bool big = cells >= (long)c->nsm * 1024;
+  return c->use_tiled && (big || c->use_tiled == 2) && c->tiled_ok && c->dev.ppe_unit &&
+         sorrel == 1.0 && (npsolver == 5 || npsolver == 6);
+}
+
+int launch_ppe_tiled(w2_ctx *c, int lcartes, int msorit, double dk, double sortol,
+                     const double *u, const double *v, double *p, StepOut *out) {
+  Dev d = c->dev;
+  TileGeom g = c->tg;
+  void *args[] = {&d, &g, &lcartes, &msorit, &dk, &sortol, (void *)&u, (void *)&v, &p, &out};
+  c->launches++;
+  cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_ppe_tiled, dim3(c->tiled_blocks),
+                                              dim3(c->tiled_threads), args, c->tiled_smem, c->st);
+  if (e != cudaSuccess) return fail(c, W2_E_CUDA, "tiled PPE launch: %s", cudaGetErrorString(e));
+  return W2_OK;
+}
+
 int launch_ppe(w2_ctx *c, int lcartes, int npsolver, int msorit, double dk, double sortol,
                double sorrel, const double *u, const double *v, double *p) {
+  if (tiled_applies(c, npsolver, sorrel)) {
+    ProfScope ps(c, W2_K_PPE);
+    return launch_ppe_tiled(c, lcartes, msorit, dk, sortol, u, v, p, c->d_out);
+  }
   int blocks = (npsolver == 1 || npsolver == 2) ? 1 : pick_blocks(c, (const void *)k_ppe, (long)c->nx * c->ny);
   ProfScope ps(c, W2_K_PPE);
   Dev d = c->dev;
@@ -521,7 +596,12 @@ int wolfd2gpu_profile_read(w2_ctx *c, int kind, double *total_ms, long long *cou
 
 int wolfd2gpu_tune(w2_ctx *c, int chain_seg, int chain_warm, int threads, int blocks_per_sm) {
   if (!c) return W2_E_ARG;
-  if (chain_seg < 0 || chain_warm < 0 || threads < 0 || blocks_per_sm < 0) return W2_E_ARG;
+  if (blocks_per_sm == -1 || blocks_per_sm == -2) {
+    // -1: one colour per barrier for red/black SOR; -2: tiled sweeps at any size
+    c->use_tiled = blocks_per_sm == -1 ? 0 : 2;
+    blocks_per_sm = 0;
+  }
+  if (chain_seg < 0 || chain_warm < 0 || threads < 0 || blocks_per_sm < -2) return W2_E_ARG;
   if (chain_seg > 0 && chain_seg < 8) return fail(c, W2_E_ARG, "chain segment length must be >= 8");
   if (threads > 0) {
     if (threads % 32 || threads > kMaxThreads) return fail(c, W2_E_ARG, "threads must be a multiple of 32 <= %d", kMaxThreads);
@@ -543,6 +623,7 @@ static int finish_coefficients(w2_ctx *c) {
   CK(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   c->dev.ppe_unit = (h == 0) ? 1 : 0;
+  plan_tiles(c);
   return W2_OK;
 }
 
@@ -851,7 +932,10 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
       }
     }
     if ((rc = launch_bc(c, BC_VEL | BC_PRES, us, vs, p))) break;
-    {
+    if (tiled_applies(c, prm->npsolver, prm->sorrel)) {
+      ProfScope ps(c, W2_K_PPE);
+      if ((rc = launch_ppe_tiled(c, prm->lcartes, prm->msorit, prm->dk, prm->sortol, us, vs, p, o))) break;
+    } else {
       int blocks = (prm->npsolver == 1 || prm->npsolver == 2)
                        ? 1 : pick_blocks(c, (const void *)k_ppe, (long)c->nx * c->ny);
       ProfScope ps(c, W2_K_PPE);

@@ -3,6 +3,7 @@
 #include "w2_bc.cuh"
 #include "w2_momentum.cuh"
 #include "w2_ppe.cuh"
+#include "w2_ppe_tiled.cuh"
 
 namespace w2 {
 
@@ -207,6 +208,23 @@ __global__ void __launch_bounds__(kMaxThreads) k_ppe(Dev d, int lcartes, int nps
     nconv = ppe_parallel(d, p, npsolver, lcartes, msorit, dk, sortol, sorrel);
     if (nconv < 0) return;
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? msorit : nconv;
+}
+
+// Red/black SOR with two sweeps per grid barrier (unit-stencil rows,
+// sorrel = 1); dynamic shared memory holds the staged tile.
+__global__ void __launch_bounds__(kMaxThreads) k_ppe_tiled(Dev d, TileGeom g, int lcartes,
+                                                           int msorit, double dk, double sortol,
+                                                           const double *u, const double *v,
+                                                           double *p, StepOut *out) {
+  if (d.sync->halt) return;
+  Sync *sy = d.sync;
+  ppe_divergence(d, u, v);
+  if (!grid_sync(sy)) return;
+  ppe_rhs_grid(d, lcartes, dk, p);
+  if (!grid_sync(sy)) return;
+  const int nconv = ppe_rb_tiled(d, g, p, d.ppn, d.qh, msorit, sortol);
+  if (nconv < 0) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? msorit : nconv;
 }
 
