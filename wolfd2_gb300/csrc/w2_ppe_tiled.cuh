@@ -31,27 +31,28 @@ struct TileGeom {
 
 // Half-sweep of one colour over box [bi0,bi1] x [bj0,bj1] (grid indices,
 // already clipped to the unknowns) of the shared tile (origin gi0, gj0,
-// row length W).  Returns max |delta| over points inside the own tile.
+// row length W).  Warps take rows, lanes take every other column, so the
+// index arithmetic is adds only.  Returns max |delta| (as IEEE bits) over
+// points inside the own tile.
 __device__ __forceinline__ unsigned long long tile_half_sweep(
     double *P, const double *Bt, int W, int gi0, int gj0, int bi0, int bi1, int bj0, int bj1,
     int parity, int oi0, int oi1, int oj0, int oj1) {
   unsigned long long mx = 0ull;
-  const int rows = bj1 - bj0 + 1;
-  if (rows <= 0 || bi1 < bi0) return 0ull;
-  // points of this colour per row: i from first i >= bi0 with (i+j)%2 == parity
-  const int wmax = (bi1 - bi0) / 2 + 1;
-  for (int t = threadIdx.x; t < rows * wmax; t += blockDim.x) {
-    const int j = bj0 + t / wmax;
-    int i = bi0 + 2 * (t % wmax);
-    if (((i + j) & 1) != parity) ++i;
-    if (i > bi1) continue;
-    const int o = (i - gi0) + (j - gj0) * W;
-    double sum = Bt[o] - P[o - W] - P[o - 1] - P[o + 1] - P[o + W];
-    sum = sum * -0.25 - P[o];
-    P[o] = P[o] + sum;
-    if (i >= oi0 && i <= oi1 && j >= oj0 && j <= oj1) {
-      const unsigned long long b = dbits(fabs(sum));
-      mx = b > mx ? b : mx;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int j = bj0 + warp; j <= bj1; j += nwarps) {
+    const int ist = bi0 + ((bi0 + j + parity) & 1);
+    const bool own_row = j >= oj0 && j <= oj1;
+    const int row = (j - gj0) * W - gi0;
+#pragma unroll 2
+    for (int i = ist + 2 * lane; i <= bi1; i += 64) {
+      const int o = row + i;
+      double sum = Bt[o] - P[o - W] - P[o - 1] - P[o + 1] - P[o + W];
+      sum = sum * -0.25 - P[o];
+      P[o] = P[o] + sum;
+      if (own_row && i >= oi0 && i <= oi1) {
+        const unsigned long long b = dbits(fabs(sum));
+        mx = b > mx ? b : mx;
+      }
     }
   }
   return mx;
