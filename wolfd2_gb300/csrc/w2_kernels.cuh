@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_ppe(Dev d, int lcartes, int nps
 
 // Red/black SOR with two sweeps per grid barrier (unit-stencil rows,
 // sorrel = 1); dynamic shared memory holds the staged tile.
-__global__ void __launch_bounds__(kMaxThreads) k_ppe_tiled(Dev d, TileGeom g, int lcartes,
+__global__ void __launch_bounds__(kMaxThreads, 1) k_ppe_tiled(Dev d, TileGeom g, int lcartes,
                                                            int msorit, double dk, double sortol,
                                                            const double *u, const double *v,
                                                            double *p, StepOut *out) {

@@ -31,27 +31,59 @@ struct TileGeom {
 
 // Half-sweep of one colour over box [bi0,bi1] x [bj0,bj1] (grid indices,
 // already clipped to the unknowns) of the shared tile (origin gi0, gj0,
-// row length W).  Warps take rows, lanes take every other column, so the
-// index arithmetic is adds only.  Returns max |delta| (as IEEE bits) over
-// points inside the own tile.
+// row length W).  The colour's points are numbered row by row; thread t takes
+// points t, t+T, t+2T, ... in batches of four whose operands are all loaded
+// before any is updated (points of one colour never read each other), and the
+// row/column of the next point is advanced incrementally.  Returns max
+// |delta| (as IEEE bits) over points inside the own tile.
 __device__ __forceinline__ unsigned long long tile_half_sweep(
     double *P, const double *Bt, int W, int gi0, int gj0, int bi0, int bi1, int bj0, int bj1,
     int parity, int oi0, int oi1, int oj0, int oj1) {
   unsigned long long mx = 0ull;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  for (int j = bj0 + warp; j <= bj1; j += nwarps) {
-    const int ist = bi0 + ((bi0 + j + parity) & 1);
-    const bool own_row = j >= oj0 && j <= oj1;
-    const int row = (j - gj0) * W - gi0;
-#pragma unroll 2
-    for (int i = ist + 2 * lane; i <= bi1; i += 64) {
-      const int o = row + i;
-      double sum = Bt[o] - P[o - W] - P[o - 1] - P[o + 1] - P[o + W];
-      sum = sum * -0.25 - P[o];
-      P[o] = P[o] + sum;
-      if (own_row && i >= oi0 && i <= oi1) {
-        const unsigned long long b = dbits(fabs(sum));
-        mx = b > mx ? b : mx;
+  const int rows = bj1 - bj0 + 1;
+  if (rows <= 0 || bi1 < bi0) return 0ull;
+  const int wmax = (bi1 - bi0) / 2 + 1;  // slots per row (last may be empty)
+  const int total = rows * wmax;
+  const int T = blockDim.x;
+  const int dj = T / wmax, dk = T % wmax;
+  int t = threadIdx.x;
+  int j = bj0 + t / wmax, k = t % wmax;
+  constexpr int NB = 4;
+  while (t < total) {
+    int o[NB];
+    bool ok[NB], own[NB];
+    double b[NB], s_[NB], w_[NB], e_[NB], n_[NB], c_[NB];
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+      const int i = bi0 + 2 * k + (((bi0 + j + parity) & 1));
+      ok[q] = (t < total) && (i <= bi1);
+      own[q] = ok[q] && i >= oi0 && i <= oi1 && j >= oj0 && j <= oj1;
+      o[q] = ok[q] ? (i - gi0) + (j - gj0) * W : W + 1;
+      t += T;
+      k += dk;
+      j += dj;
+      if (k >= wmax) {
+        k -= wmax;
+        ++j;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+      b[q] = Bt[o[q]];
+      s_[q] = P[o[q] - W];
+      w_[q] = P[o[q] - 1];
+      e_[q] = P[o[q] + 1];
+      n_[q] = P[o[q] + W];
+      c_[q] = P[o[q]];
+    }
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+      double sum = b[q] - s_[q] - w_[q] - e_[q] - n_[q];
+      sum = sum * -0.25 - c_[q];
+      if (ok[q]) P[o[q]] = c_[q] + sum;
+      if (own[q]) {
+        const unsigned long long bb = dbits(fabs(sum));
+        mx = bb > mx ? bb : mx;
       }
     }
   }
