@@ -123,7 +123,7 @@ __device__ __forceinline__ double sor_point(const Dev &d, double *p, int i, int 
                d.pa4[o] * p[IX(d, i + 1, j)] - d.pa5[o] * p[IX(d, i, j + 1)];
   sum = sum / d.pa3[o] - p[o];
   p[o] = p[o] + sorrel * sum;
-  return fabs(sum);
+  return sum;
 }
 
 // Unit-stencil form of sor_point for rows whose coefficients are exactly
@@ -138,7 +138,7 @@ __device__ __forceinline__ double sor_point_unit(const Dev &d, double *p, int i,
                p[IX(d, i, j + 1)];
   sum = sum * -0.25 - p[o];
   p[o] = p[o] + sum;
-  return fabs(sum);
+  return sum;
 }
 
 // Red/black colour sweep over (i+j) % 2 == parity, pressure.f:505-532.
@@ -154,7 +154,7 @@ __device__ double rb_color(const Dev &d, double *p, int parity, double sorrel) {
     const int i = 2 + ((j + parity) & 1) + 2 * (t % nh);
     if (i > nx) continue;
     const double a = UNIT ? sor_point_unit(d, p, i, j) : sor_point(d, p, i, j, sorrel);
-    const unsigned long long b = dbits(a);
+    const unsigned long long b = abs_bits(a);
     mx = b > mx ? b : mx;
   }
   return __longlong_as_double((long long)mx);
@@ -226,7 +226,7 @@ __device__ int sor_lex_block(const Dev &d, double *p, int lcartes, int msorit, d
     for (int s = 0; s < nsteps; ++s) {
       for (int j = 2 + (int)threadIdx.x; j <= ny; j += blockDim.x) {
         const int i = s - j + 4;
-        if (i >= 2 && i <= nx) mx = dmax(mx, sor_point(d, p, i, j, sorrel));
+        if (i >= 2 && i <= nx) mx = dmax(mx, fabs(sor_point(d, p, i, j, sorrel)));
       }
       __syncthreads();
     }

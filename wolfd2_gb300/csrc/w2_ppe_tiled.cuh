@@ -82,7 +82,7 @@ __device__ __forceinline__ unsigned long long tile_half_sweep(
       sum = sum * -0.25 - c_[q];
       if (ok[q]) P[o[q]] = c_[q] + sum;
       if (own[q]) {
-        const unsigned long long bb = dbits(fabs(sum));
+        const unsigned long long bb = abs_bits(sum);
         mx = bb > mx ? bb : mx;
       }
     }
