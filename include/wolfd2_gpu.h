@@ -42,6 +42,8 @@ extern "C" {
 #define W2_E_BCFLAG        5  /* invalid boundary flag (bound_cond.f 'stop')  */
 #define W2_E_UNSUPPORTED   6  /* configuration outside this library's scope   */
 #define W2_E_FALLBACK      7  /* chain recurrence needed the sequential path  */
+#define W2_E_SIZE          8  /* larger than the fixed scratch of the
+                                 allocation-free entry point               */
 
 /* Region / boundary enums, identical to include/wolfd2.h:15-60 of the
  * reference. */
@@ -214,6 +216,34 @@ int wolfd2gpu_profile(w2_ctx *ctx, int enable);
  * wolfd2gpu_profile(ctx, 1); synchronises the context stream. */
 int wolfd2gpu_profile_read(w2_ctx *ctx, int kind, double *total_ms,
                            long long *count);
+
+/* ---- Allocation-free entry point ---------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * -- a driver that gives all device memory to its own pool at start-up, or
+ * code that must not reach the allocator inside its solve loop -- and so
+ * cannot create a w2_ctx.  Runs red/black point SOR (nPpeSolver 5 or 6,
+ * pressure.f:457-656, with the divergence and b = div/dk of Ppe) on device
+ * arrays the caller owns, all in the reference layout with leading dimension
+ * ld (elements) and rows j = 0..ny+1: metrics rau, rgv, xeu, yeu, xzv, yzv,
+ * velocities u, v, and p (updated in place).  The only scratch is a fixed
+ * static device array of W2_NOALLOC_MAX_POINTS doubles plus barrier state
+ * (about 9.6 MB, held by every device that loads the library until the
+ * process exits); the call makes no allocation.  Limits: Cartesian grids,
+ * no blockage regions, ld*(ny+2) <= W2_NOALLOC_MAX_POINTS (else W2_E_SIZE).
+ * The first call on a device looks up the scratch address on that device;
+ * make that first call before any stream capture.  All calls share the
+ * scratch: calls that overlap on the GPU race, so serialise them.
+ * stream is a cudaStream_t (NULL = legacy default stream); the call
+ * synchronises it before returning nSorConv. */
+#define W2_NOALLOC_MAX_POINTS 1200000
+int wolfd2gpu_ppe_rbsor_noalloc(int nx, int ny, int ld, int lCartesGrid,
+                                int nPpeSolver, int msorit, double dk,
+                                double sortol, double sorrel,
+                                const double *rau, const double *rgv,
+                                const double *xeu, const double *yeu,
+                                const double *xzv, const double *yzv,
+                                const double *u, const double *v, double *p,
+                                int *nSorConv, void *stream);
 
 #ifdef __cplusplus
 }

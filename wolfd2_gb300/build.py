@@ -44,7 +44,8 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
     tmp = LIB + ".tmp"
     cmd = [_nvcc(), "-O3", "-std=c++17", *ARCH, "-lineinfo", "--fmad=false",
-           "-Xcompiler", "-fPIC", "-shared", "-o", tmp, os.path.join(CSRC, "w2_api.cu")]
+           "-Xcompiler", "-fPIC", "-shared", "-o", tmp,
+           os.path.join(CSRC, "w2_api.cu"), os.path.join(CSRC, "w2_noalloc.cu")]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     subprocess.run(cmd, check=True)

@@ -137,7 +137,7 @@ __device__ __forceinline__ int read_error(Sync *s) {
 // Grid barrier with a time limit.  All blocks of a cooperative launch call
 // it the same number of times.  On timeout the sticky error is set and every
 // caller returns false; callers then leave the kernel.
-__device__ __noinline__ bool grid_sync(Sync *s) {
+static __device__ __noinline__ bool grid_sync(Sync *s) {
   __shared__ int ok;
   __syncthreads();
   if (gridDim.x == 1) {
@@ -187,7 +187,7 @@ __device__ __forceinline__ unsigned long long abs_bits(double x) {
   return dbits(x) & 0x7fffffffffffffffull;
 }
 
-__device__ __noinline__ void block_max_to(unsigned long long *slot, double v) {
+static __device__ __noinline__ void block_max_to(unsigned long long *slot, double v) {
   __shared__ unsigned long long wmax[32];
   unsigned long long b = dbits(v);
   for (int o = 16; o > 0; o >>= 1) {

@@ -25,7 +25,9 @@ from .deck import Case, Regions, RunParams
 W2_OK = 0
 ERRORS = {1: "bad argument", 2: "CUDA error", 3: "device wait timed out",
           4: "solution diverged", 5: "invalid boundary flag",
-          6: "unsupported configuration", 7: "chain fallback"}
+          6: "unsupported configuration", 7: "chain fallback",
+          8: "larger than the allocation-free scratch"}
+NOALLOC_MAX_POINTS = 1200000
 PREC_FP64, PREC_MIXED = 0, 1
 K_MOMENTUM, K_PPE, K_POST, K_BC, K_COPY = range(5)
 KERNEL_NAMES = {K_MOMENTUM: "k_naux", K_PPE: "k_ppe", K_POST: "k_step_post",
@@ -109,6 +111,8 @@ def lib():
     L.wolfd2gpu_stream.restype = C.c_void_p
     L.wolfd2gpu_profile.argtypes = [vp, C.c_int]
     L.wolfd2gpu_chain_stats.argtypes = [vp, _ip, _ip]
+    L.wolfd2gpu_ppe_rbsor_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                              C.c_double, C.c_double, C.c_double] + [vp] * 9 + [_ip, vp]
     L.wolfd2gpu_profile_read.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_longlong)]
     _lib = L
     return L
@@ -126,6 +130,21 @@ def _i(v: int):
 
 def _d(v: float):
     return C.byref(C.c_double(float(v)))
+
+
+def ppe_rbsor_noalloc(nx, ny, ld, msorit, dk, sortol, sorrel, rau, rgv, xeu, yeu, xzv, yzv,
+                      u, v, p, stream=0, lcartes=1, npsolver=5) -> int:
+    """Allocation-free red/black Ppe on device arrays (integer device
+    addresses in the reference layout with leading dimension ld); returns
+    nSorConv.  See wolfd2gpu_ppe_rbsor_noalloc in include/wolfd2_gpu.h."""
+    L = lib()
+    out = C.c_int()
+    rc = L.wolfd2gpu_ppe_rbsor_noalloc(nx, ny, ld, lcartes, npsolver, msorit, dk, sortol, sorrel,
+                                       rau, rgv, xeu, yeu, xzv, yzv, u, v, p, C.byref(out),
+                                       stream or None)
+    if rc != W2_OK:
+        raise W2Error(rc, "wolfd2gpu_ppe_rbsor_noalloc failed")
+    return out.value
 
 
 class Solver:
