@@ -178,7 +178,7 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": config_of(args, case),
+        "config": config_of(args, case, args.refine_sweeps or 64),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": kind,
                          "sample": f"{args.warmup} + {args.steps} full time steps of the same case; {how}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -187,20 +187,124 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def config_of(args, case):
+def config_of(args, case, inner=None):
+    prec = ("mixed: FP32 red/black Poisson sweeps with FP64 residual and correction "
+            f"({inner} sweeps per refinement pass), FP64 momentum and projection; "
+            "plain FP64 timed beside it" if args.precision == "mixed" else "plain FP64")
     return {"workload": (f"lid-driven cavity {args.n}x{args.n} cells, Re={args.re:g}, "
                          f"dt={args.dt:g} (the named dt={DT_NAMED:g} drives the reference scheme to NaN at this size), "
                          f"seeded 16x16-mode streamfunction perturbation (seed {args.seed}), "
-                         f"ppe_solver {args.solver}, plain FP64"),
+                         f"ppe_solver {args.solver}, {prec}"),
             "cells": case.cells, "nx": case.nx, "ny": case.ny, "re": args.re, "dt": args.dt,
-            "ppe_solver": args.solver,
+            "ppe_solver": args.solver, "precision": args.precision,
             "l2": "flushed between timed steps (256 MiB write); per-step working set > 2x L2"}
+
+
+def mixed_ppe_bytes(cells, nsor, inner):
+    """Algorithmic bytes of one mixed Ppe call: RHS reads us, vs and writes b
+    (FP64, 24 B/cell); per refinement pass the residual reads p, b (FP64) and
+    writes r (FP32) = 20 B, each FP32 sweep reads e, r and writes e = 12 B,
+    the correction reads p, e and writes p = 20 B."""
+    passes = -(-nsor // inner)
+    return cells * (24.0 + passes * 40.0 + 12.0 * nsor)
+
+
+def run_arm(s, prm, args, precision, u0, v0, p0, st, flush, barrier, local, timed=True):
+    """Warm-up then `steps` device-timed steps of one precision mode from the
+    same initial fields; returns the measurements and the final fields."""
+    from wolfd2_gb300.gpu import K_BC, K_COPY, K_MOMENTUM, K_POST, K_PPE
+    import torch
+    kw = {"precision": precision, "refine_sweeps": args.refine_sweeps}
+    s.load_fields(u0, v0, p0)
+    hist = s.step(prm, args.warmup, **kw) if args.warmup else []
+    barrier()
+    s.profile(True)
+    n_launch0 = s.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        barrier()
+        t_wall0 = time.perf_counter()
+        for k in range(args.steps):
+            with torch.cuda.stream(st):
+                flush.fill_(float(k))
+                ev[k][0].record(st)
+            hist += s.step(prm, 1, **kw)
+            with torch.cuda.stream(st):
+                ev[k][1].record(st)
+        barrier()
+        t_wall = time.perf_counter() - t_wall0
+    launches = s.launch_count() - n_launch0
+    t_dev = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+    prof = {k: s.profile_read(k) for k in (K_MOMENTUM, K_PPE, K_POST, K_BC, K_COPY)}
+    s.profile(False)
+    fields = s.store_fields()
+    # end-to-end through the C-ABI with host buffers, copies in the timed region
+    u, v, p = (f.copy(order="F") for f in fields)
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s.load_fields(u, v, p)
+        s.step(prm, 1, **kw)
+        u, v, p = s.store_fields()
+    barrier()
+    t_e2e = time.perf_counter() - t0
+    return {"t_dev": t_dev, "t_e2e": t_e2e, "e2e_steps": e2e_steps, "hist": hist,
+            "timed": hist[-args.steps:], "prof": prof, "launches": launches, "clk": clk,
+            "wall": t_wall, "fields": fields}
+
+
+def roofline_of(arm, cells, precision, inner):
+    """Roofline of the dominant kernel of one arm (HBM view) and the FP64
+    pipe view of the plain red/black sweep."""
+    from wolfd2_gb300.gpu import K_MOMENTUM, K_PPE, KERNEL_NAMES
+    prof, timed = arm["prof"], arm["timed"]
+    hbm_peak, peak_kind = peaks()
+    dom = max((K_MOMENTUM, K_PPE), key=lambda k: prof[k][0])
+    nql = [h[0] if h[0] > 0 else 20 for h in timed]
+    nsor = [h[1] for h in timed]
+    if dom == K_PPE:
+        if precision == "mixed":
+            alg = sum(mixed_ppe_bytes(cells, n, inner) for n in nsor)
+        else:
+            alg = sum(ppe_bytes(cells, n) for n in nsor)
+    else:
+        alg = sum(mom_bytes(cells, n) for n in nql)
+    dom_ms, dom_n = prof[dom]
+    name = KERNEL_NAMES[dom] if not (dom == K_PPE and precision == "mixed") else "k_ppe_mixed"
+    achieved = alg / (dom_ms / 1e3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        tj = json.load(open(tpath)).get(name)
+        if tj:
+            # a captured smaller case, scaled by the algorithmic bytes per launch
+            traffic = tj["bytes_per_alg_byte"] * (alg / dom_n)
+    roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
+            "alg_bytes_per_launch": alg / dom_n, "avg_launch_ms": dom_ms / dom_n}
+    fp64 = None
+    if precision == "fp64" and prof[K_PPE][0] > 0:
+        # unit-stencil red/black point: 4 subtractions, 1 multiply by -1/4,
+        # 1 subtraction and 1 addition per point and sweep
+        ops = sum(cells * n for n in nsor) * 7.0
+        gops = ops / (prof[K_PPE][0] / 1e3) / 1e9
+        fp64 = {"kernel": "k_ppe_tiled", "op_per_point": "7 FP64 add/mul (unit stencil)",
+                "achieved_gops": gops, "peak_gops": 628.0,
+                "peak_kind": "measured DFMA probe on this pool's GB300 (2 DFMA/clk/SM)",
+                "frac": gops / 628.0}
+    return roof, fp64
+
+
+def rel_max(a, b):
+    return float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
 
 
 def run_ours(args):
     import torch
     import torch.distributed as dist
-    from wolfd2_gb300.gpu import K_COPY, K_MOMENTUM, K_POST, K_PPE, K_BC, KERNEL_NAMES, Solver
+    from wolfd2_gb300.gpu import KERNEL_NAMES, PREC_FP64, PREC_MIXED, Solver
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -215,6 +319,9 @@ def run_ours(args):
     s = Solver.for_case(case)
     if args.threads or args.blocks_per_sm or args.seg or args.warm:
         s.tune(seg=args.seg, warm=args.warm, threads=args.threads, blocks_per_sm=args.blocks_per_sm)
+    if args.mixed_k or args.mixed_threads:
+        s.tune_mixed(args.mixed_k, args.mixed_threads)
+    inner = args.refine_sweeps or 16 * (args.mixed_k or 4)
     prm = case.params
     st = torch.cuda.ExternalStream(s.stream(), device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -224,54 +331,17 @@ def run_ours(args):
         if world > 1:
             dist.barrier()
 
-    # warm-up
-    s.load_fields(u0, v0, p0)
-    hist = s.step(prm, args.warmup) if args.warmup else []
-    barrier()
-
-    # device-timed region: fields resident in HBM
-    s.profile(True)
-    n_launch0 = s.launch_count()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
-    with ClockSampler(local) as clk:
-        barrier()
-        t_wall0 = time.perf_counter()
-        for k in range(args.steps):
-            with torch.cuda.stream(st):
-                flush.fill_(float(k))
-                ev[k][0].record(st)
-            hist += s.step(prm, 1)
-            with torch.cuda.stream(st):
-                ev[k][1].record(st)
-        barrier()
-        t_wall = time.perf_counter() - t_wall0
-    launches = s.launch_count() - n_launch0
-    chain_rounds, chain_fallbacks = s.chain_stats()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    t_dev = sum(step_ms) / 1e3
-    prof = {k: s.profile_read(k) for k in (K_MOMENTUM, K_PPE, K_POST, K_BC, K_COPY)}
-    s.profile(False)
-    timed = hist[-args.steps:]
-
-    # end-to-end through the C-ABI with host buffers, copies in the timed region
-    u, v, p = s.store_fields()
-    e2e_steps = max(1, min(args.steps, args.e2e_steps))
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        s.load_fields(u, v, p)
-        s.step(prm, 1)
-        u, v, p = s.store_fields()
-    barrier()
-    t_e2e = time.perf_counter() - t0
-    field_bytes = (case.nx + 2) * (case.ny + 2) * 8
+    arms = {}
+    order = ["fp64", "mixed"] if args.precision == "mixed" else ["fp64"]
+    for name in order:
+        arms[name] = run_arm(s, prm, args, PREC_MIXED if name == "mixed" else PREC_FP64,
+                             u0, v0, p0, st, flush, barrier, local)
+    head = arms[args.precision]
 
     # max over ranks
-    t_max = t_dev
-    t_e2e_max = t_e2e
+    t_max, t_e2e_max = head["t_dev"], head["t_e2e"]
     if world > 1:
-        tt = torch.tensor([t_dev, t_e2e], device=dev, dtype=torch.float64)
+        tt = torch.tensor([t_max, t_e2e_max], device=dev, dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_max, t_e2e_max = float(tt[0]), float(tt[1])
 
@@ -282,62 +352,66 @@ def run_ours(args):
         return
 
     cells = case.cells
+    field_bytes = (case.nx + 2) * (case.ny + 2) * 8
     value = world * cells * args.steps / t_max
-    e2e_value = world * cells * e2e_steps / t_e2e_max
-    hbm_peak, peak_kind = peaks()
-    # dominant kernel: larger share of device time
-    dom = max((K_MOMENTUM, K_PPE), key=lambda k: prof[k][0])
-    nql = [h[0] if h[0] > 0 else 20 for h in timed]
-    nsor = [h[1] for h in timed]
-    if dom == K_PPE:
-        alg = sum(ppe_bytes(cells, n) for n in nsor)
-    else:
-        alg = sum(mom_bytes(cells, n) for n in nql)
-    dom_ms, dom_n = prof[dom]
-    achieved = alg / (dom_ms / 1e3) / 1e9
-    # FP64 pipe view of the red/black sweep: 11 add/mul + 1 divide per point
-    sweep_pts = sum(cells * n for n in nsor)
-    fp64 = None
-    if prof[K_PPE][0] > 0:
-        ops = sweep_pts * (11 + 8.9)
-        fp64 = {"kernel": "k_ppe", "op_per_point": "11 add/mul + 1 div (div = 8.9 FMA slots)",
-                "achieved_gops": ops / (prof[K_PPE][0] / 1e3) / 1e9, "peak_gops": 628.0,
-                "peak_kind": "measured DFMA probe on this pool's GB300 (2 DFMA/clk/SM)",
-                "frac": ops / (prof[K_PPE][0] / 1e3) / 1e9 / 628.0}
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        tj = json.load(open(tpath)).get(KERNEL_NAMES[dom])
-        if tj:
-            # scale a captured small case by the units processed per launch
-            traffic = tj["bytes_per_unit"] * (alg / dom_n) / tj["alg_bytes_per_unit"]
+    e2e_value = world * cells * head["e2e_steps"] / t_e2e_max
+    roof, fp64 = roofline_of(head, cells, args.precision, inner)
+    plain = None
+    accuracy = None
+    if args.precision == "mixed":
+        a64 = arms["fp64"]
+        r64, f64 = roofline_of(a64, cells, "fp64", inner)
+        plain = {"value": world * cells * args.steps / a64["t_dev"], "unit": UNIT,
+                 "ms_per_step": 1e3 * a64["t_dev"] / args.steps,
+                 "e2e": world * cells * a64["e2e_steps"] / a64["t_e2e"],
+                 "roofline": r64, "fp64_roof": f64, "gpu_launches": a64["launches"],
+                 "kernel_ms": {KERNEL_NAMES[k]: {"total_ms": v[0], "launches": v[1]}
+                               for k, v in a64["prof"].items()},
+                 "iterations": [[h[0], h[1]] for h in a64["timed"]],
+                 "clocks": a64["clk"].summary()}
+        fm, fp = head["fields"], a64["fields"]
+        errs = {nm: rel_max(a, b) for nm, a, b in zip("uvp", fm, fp)}
+        div_m = [h[3] for h in head["hist"]]
+        div_p = [h[3] for h in a64["hist"]]
+        accuracy = {
+            "against": "plain FP64 path after the same warm-up + timed steps from the same initial "
+                       "state (bit-identical to the FP64 oracle: parity tests)",
+            "steps": len(head["hist"]),
+            "u_rel_maxnorm": errs["u"], "v_rel_maxnorm": errs["v"], "p_rel_maxnorm": errs["p"],
+            "divmax_mixed": max(div_m), "divmax_fp64": max(div_p),
+            "divmax_rel_diff": abs(max(div_m) - max(div_p)) / max(max(div_p), 1e-300),
+            "velocity_within_1e-5": max(errs["u"], errs["v"]) <= 1e-5,
+            "div_le_1e-10": max(div_m) <= 1e-10,
+        }
     cpu = None
     if not args.no_cpu_baseline:
         cv, csec, cores, kind, how = cpu_step_sample(case, (u0, v0, p0), 1)
         cpu = {"value": cv, "unit": UNIT, "cores": cores, "kind": kind,
                "sample": f"1 full time step of the same {args.n}x{args.n} case from the same initial state "
                          f"({csec:.1f} s); {how}"}
+    chain_rounds, chain_fallbacks = s.chain_stats()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": config_of(args, case),
+        "steps_per_s": world * args.steps / t_max,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+        "data": "synthetic", "config": config_of(args, case, inner),
         "parallelism": "replicas only" if world > 1 else "single GPU",
-        "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[dom], "achieved": achieved,
-                     "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                     "peak_kind": peak_kind, "traffic": traffic,
-                     "alg_bytes_per_launch": alg / dom_n, "avg_launch_ms": dom_ms / dom_n},
+        "roofline": roof,
         "fp64_roof": fp64,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 3 * field_bytes,
-                "d2h_bytes_per_step": 3 * field_bytes, "steps": e2e_steps},
+                "d2h_bytes_per_step": 3 * field_bytes, "steps": head["e2e_steps"]},
+        "plain_fp64": plain,
+        "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
+        "accuracy": accuracy,
         "cpu_baseline": cpu,
-        "clocks": clk.summary(),
-        "gpu_launches": launches,
-        "kernel_ms": {KERNEL_NAMES[k]: {"total_ms": v[0], "launches": v[1]} for k, v in prof.items()},
-        "iterations": [[h[0], h[1]] for h in timed],
-        "chain": {"max_verify_rounds": chain_rounds, "sequential_fallbacks": chain_fallbacks,
-                  "segment_rows": s.seg if hasattr(s, "seg") else None},
-        "wall_s": t_wall,
+        "clocks": head["clk"].summary(),
+        "gpu_launches": head["launches"],
+        "kernel_ms": {KERNEL_NAMES[k]: {"total_ms": v[0], "launches": v[1]} for k, v in head["prof"].items()},
+        "iterations": [[h[0], h[1]] for h in head["timed"]],
+        "chain": {"max_verify_rounds": chain_rounds, "sequential_fallbacks": chain_fallbacks},
+        "wall_s": head["wall"],
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -362,6 +436,12 @@ def main():
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--seg", type=int, default=0, help="chain segment rows (0: auto)")
     ap.add_argument("--warm", type=int, default=0, help="chain warm-up rows (0: default)")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed",
+                    help="headline path; mixed also times plain FP64 beside it")
+    ap.add_argument("--refine-sweeps", type=int, default=0,
+                    help="mixed: FP32 sweeps per refinement pass (0: 16 x sweeps per barrier)")
+    ap.add_argument("--mixed-k", type=int, default=0, help="mixed: sweeps per grid barrier (2/4/8)")
+    ap.add_argument("--mixed-threads", type=int, default=0, help="mixed: threads per block")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

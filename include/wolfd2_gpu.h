@@ -63,8 +63,10 @@ extern "C" {
 
 /* Arithmetic of the hot path. */
 #define W2_PREC_FP64  0   /* plain FP64, op-by-op as the reference source  */
-#define W2_PREC_MIXED 1   /* FP32 momentum + FP32 Poisson sweeps with FP64
-                             residual/correction refinement               */
+#define W2_PREC_MIXED 1   /* red/black Poisson sweeps in FP32 on the
+                             correction equation, FP64 residual and
+                             correction (iterative refinement); npsolver 5
+                             or 6 on Cartesian unit-stencil grids         */
 
 typedef struct w2_ctx w2_ctx;
 
@@ -149,13 +151,16 @@ typedef struct {
   int mqiter, npsolver, msorit, nfiltu, nfiltv, lcartes;
   int precision;      /* W2_PREC_*                                        */
   int refine_sweeps;  /* mixed: FP32 sweeps per refinement pass (0=auto) */
-  double refine_tol;  /* mixed: FP64 residual target (0 = auto)          */
+  double refine_tol;  /* reserved, pass 0                                */
 } w2_params;
 
 /* Per-step results of main.f:753-966. */
 typedef struct {
   int nQLiter, nSorConv;
   double dif[4];      /* DiffMaxNorm of (pn,p), (un,u), (vn,v), (tn,t)  */
+  double divmax;      /* max |Divergence(u,v)| (pressure.f:287-299) over
+                         the pressure cells of the projected field; no
+                         counterpart in the reference                    */
 } w2_stepstat;
 
 /* Copy u, v, p (0:mnx,0:mny host arrays) to / from the device state. */
@@ -185,6 +190,16 @@ const char *wolfd2gpu_last_error(w2_ctx *ctx);
  * Takes effect on the next launch. */
 int wolfd2gpu_tune(w2_ctx *ctx, int chain_seg, int chain_warm, int threads,
                    int blocks_per_sm);
+
+/* Precision of the drop-in wolfd2gpu_ppe on this context (W2_PREC_*) and
+ * FP32 sweeps per refinement pass (0 = auto).  No counterpart in the
+ * reference, whose Ppe is FP64 only. */
+int wolfd2gpu_set_precision(w2_ctx *ctx, int precision, int refine_sweeps);
+
+/* Mixed Poisson kernel shape: sweeps between grid barriers (2, 4 or 8; the
+ * halo is twice that) and threads per block (0 keeps the default).  Tile
+ * sizes are re-planned for the new shape. */
+int wolfd2gpu_tune_mixed(w2_ctx *ctx, int sweeps_per_barrier, int threads);
 
 /* Device pointers of the resident u, v, p fields and the device leading
  * dimension (elements), for callers that bring their own device buffers. */

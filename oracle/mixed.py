@@ -1,0 +1,169 @@
+"""CPU statement of the mixed-precision Ppe (TEST INFRASTRUCTURE ONLY).
+
+The reference's Poisson solve is FP64 only; the mixed form has no
+counterpart there.  It keeps the reference's red/black point iteration
+(SorRB/SorRBP, src/pressure.f:457-656): black points (i+j even) first, then
+red, relaxation factor sorrel, per-sweep dif = max |delta|, stop at the first
+sweep m > 1 with dif < sortol or after msorit sweeps.  It runs that iteration
+on the correction equation A e = r in FP32, where one refinement pass forms
+r = b - A p in FP64, sweeps e from zero `inner` times (or until the stopping
+rule fires), and adds e to p in FP64.  b = div/dk with the divergence of
+src/pressure.f:287-299 (nloc = 1) and RhsPpe's Cartesian form
+(src/pressure.f:354-359).
+
+Every operation is stated in the order the GPU kernel evaluates it, in the
+same IEEE type (numpy float32 elementwise arithmetic, no fused multiply-add),
+and the points of one colour never read each other, so the GPU result is
+expected to equal this model bit for bit.  The model's distance from the FP64
+oracle is the accuracy figure of the mixed path.
+
+``MixedRun`` advances a case with the oracle's FP64 routines for everything
+but the Poisson solve, in the order of main.f:690-972.
+"""
+from __future__ import annotations
+
+from typing import Dict, Optional
+
+import numpy as np
+
+from oracle import FIELD_NAMES, Oracle
+
+
+def divergence(nx: int, ny: int, met: Dict[str, np.ndarray], u: np.ndarray, v: np.ndarray) -> np.ndarray:
+    """Divergence nloc = 1 (src/pressure.f:287-299) on the pressure cells
+    i = 2..nx, j = 2..ny, as an (nx-1, ny-1) array."""
+    def s(a, di, dj):
+        return a[2 + di:nx + 1 + di, 2 + dj:ny + 1 + dj]
+    yeu, xeu, xzv, yzv = met["yeu"], met["xeu"], met["xzv"], met["yzv"]
+    ucij = s(yeu, 0, 0) * s(u, 0, 0) - \
+        s(xeu, 0, 0) * (s(v, 1, 0) + s(v, 0, 0) + s(v, 1, -1) + s(v, 0, -1)) / 4.0
+    uci1j = s(yeu, -1, 0) * s(u, -1, 0) - \
+        s(xeu, -1, 0) * (s(v, 0, 0) + s(v, -1, 0) + s(v, 0, -1) + s(v, -1, -1)) / 4.0
+    vcij = s(xzv, 0, 0) * s(v, 0, 0) - \
+        s(yzv, 0, 0) * (s(u, 0, 1) + s(u, -1, 1) + s(u, 0, 0) + s(u, -1, 0)) / 4.0
+    vcij1 = s(xzv, 0, -1) * s(v, 0, -1) - \
+        s(yzv, 0, -1) * (s(u, 0, 0) + s(u, -1, 0) + s(u, 0, -1) + s(u, -1, -1)) / 4.0
+    return ucij - uci1j + vcij - vcij1
+
+
+def div_check(nx: int, ny: int, met, u, v) -> float:
+    """max |Divergence(u,v)| over the pressure cells (no blockages)."""
+    return float(np.max(np.abs(divergence(nx, ny, met, u, v))))
+
+
+def is_unit_stencil(nx: int, ny: int, met) -> bool:
+    """Every Poisson row is (1, 1, -4, 1, 1) (pressure.f:97-106)."""
+    rau, rgv = met["rau"], met["rgv"]
+    return bool(np.all(rau[1:nx + 1, 2:ny + 1] == 1.0) and np.all(rgv[2:nx + 1, 1:ny + 1] == 1.0))
+
+
+def ppe_mixed(nx: int, ny: int, met, u, v, p, dk: float, msorit: int, sortol: float,
+              sorrel: float, inner: int, dtype=np.float32) -> int:
+    """Mixed Ppe on a Cartesian unit-stencil grid without blockages; p is
+    updated in place on i = 2..nx, j = 2..ny.  Returns nSorConv (msorit when
+    the stopping rule never fired).  dtype = float64 gives the same
+    iteration with FP64 sweeps (equal to the plain solve up to rounding)."""
+    if not is_unit_stencil(nx, ny, met):
+        raise ValueError("mixed Ppe needs the unit stencil")
+    b = divergence(nx, ny, met, u, v) / dk
+    I, J = np.meshgrid(np.arange(2, nx + 1), np.arange(2, ny + 1), indexing="ij")
+    cols = []
+    for c in (0, 1):
+        sel = ((I + J) & 1) == c
+        cols.append((I[sel], J[sel]))
+    relax = dtype(sorrel)
+    quarter = dtype(-0.25)
+    m = 0
+    result = 0
+    done = False
+    while not done:
+        ps = p[2:nx + 1, 2:ny + 1]
+        ap = p[2:nx + 1, 1:ny] + p[1:nx, 2:ny + 1] + p[3:nx + 2, 2:ny + 1] + p[2:nx + 1, 3:ny + 2] - 4.0 * ps
+        R = np.zeros((nx + 2, ny + 2), dtype=dtype)
+        R[2:nx + 1, 2:ny + 1] = (b - ap).astype(dtype)
+        E = np.zeros((nx + 2, ny + 2), dtype=dtype)
+        in_pass = 0
+        while True:
+            m += 1
+            dif = dtype(0.0)
+            for ii, jj in cols:
+                c0 = E[ii, jj]
+                s = R[ii, jj] - E[ii, jj - 1] - E[ii - 1, jj] - E[ii + 1, jj] - E[ii, jj + 1]
+                s = s * quarter - c0
+                E[ii, jj] = c0 + relax * s
+                if s.size:
+                    dif = max(dif, np.max(np.abs(s)))
+            if m > 1 and float(dif) < sortol:
+                result = m
+                done = True
+                break
+            in_pass += 1
+            if m >= msorit:
+                done = True
+                break
+            if in_pass >= inner:
+                break
+        p[2:nx + 1, 2:ny + 1] = ps + E[2:nx + 1, 2:ny + 1].astype(np.float64)
+    return result if result >= 1 else msorit
+
+
+class MixedRun:
+    """A case advanced by the time loop of main.f:690-972 with the mixed
+    Ppe in place of the FP64 one; ``history`` holds (nQLiter, nSorConv,
+    dif(1..4), divmax) per step."""
+
+    def __init__(self, case, fields: Optional[Dict[str, np.ndarray]] = None, cold_start: bool = True,
+                 inner: int = 64):
+        self.case = case
+        self.nx, self.ny = case.nx, case.ny
+        self.prm = case.params
+        self.inner = inner
+        self.o = Oracle(case.nx + 1, case.ny + 1)
+        self.met = self.o.grid(case.nx, case.ny, case.x, case.y)
+        self.f = {n: self.o.field() for n in FIELD_NAMES}
+        if fields:
+            for k, val in fields.items():
+                self.f[k][...] = val
+        self.history = []
+        self.cold_nconv = None
+        if cold_start:
+            f, o, nx, ny, r = self.f, self.o, self.nx, self.ny, case.regions
+            o.vel_bound_cond(nx, ny, r, f["u"], f["v"])
+            self.cold_nconv = self._ppe(f["u"], f["v"], f["p"])
+            o.pres_bound_cond(nx, ny, r, f["p"])
+            o.project(nx, ny, r, self.prm.dk, self.met, f["p"], f["u"], f["v"])
+            o.vel_bound_cond(nx, ny, r, f["u"], f["v"])
+
+    def _ppe(self, u, v, p) -> int:
+        prm = self.prm
+        return ppe_mixed(self.nx, self.ny, self.met, u, v, p, prm.dk, prm.msorit, prm.sortol,
+                         prm.sorrel, self.inner)
+
+    def step(self, n: int = 1):
+        f, o, nx, ny, r, prm = self.f, self.o, self.nx, self.ny, self.case.regions, self.prm
+        for _ in range(n):
+            for a, b in (("pn", "p"), ("un", "u"), ("vn", "v"), ("us", "u"), ("vs", "v")):
+                f[a][...] = f[b]
+            nql = o.naux_momentum(nx, ny, r, prm, self.met, f["d"], f["dn"], f["un"], f["vn"],
+                                  f["us"], f["vs"])
+            if prm.nfiltu == 1:
+                o.filter(nx, ny, 1, r, prm.fpu, f["us"])
+            if prm.nfiltv == 1:
+                o.filter(nx, ny, 2, r, prm.fpv, f["vs"])
+            o.vel_bound_cond(nx, ny, r, f["us"], f["vs"])
+            o.pres_bound_cond(nx, ny, r, f["p"])
+            nsor = self._ppe(f["us"], f["vs"], f["p"])
+            o.pres_bound_cond(nx, ny, r, f["p"])
+            o.project(nx, ny, r, prm.dk, self.met, f["p"], f["us"], f["vs"])
+            o.vel_bound_cond(nx, ny, r, f["us"], f["vs"])
+            o.pres_bound_cond(nx, ny, r, f["p"])
+            f["u"][...] = f["us"]
+            f["v"][...] = f["vs"]
+            o.vel_bound_cond(nx, ny, r, f["u"], f["v"])
+            o.pres_bound_cond(nx, ny, r, f["p"])
+            dif = (o.diff_max_norm(nx, ny, f["pn"], f["p"]), o.diff_max_norm(nx, ny, f["un"], f["u"]),
+                   o.diff_max_norm(nx, ny, f["vn"], f["v"]), 0.0)
+            self.history.append((nql, nsor, dif, div_check(nx, ny, self.met, f["u"], f["v"])))
+            if max(dif) > 1.0e12:
+                raise FloatingPointError("Solution diverged. Please reduce CFL number.")
+        return self.history[-1]

@@ -1,0 +1,91 @@
+"""The mixed-precision Ppe model (FP32 red/black sweeps on the correction
+equation, FP64 residual and correction) against the FP64 oracle: the same
+sweep count at every stopping point, and p within the stated tolerance.
+CPU only; the GPU kernel is held to this model bit for bit in
+test_gpu_mixed.py."""
+import numpy as np
+import pytest
+
+import mixed as M
+import oracle as O
+from wolfd2_gb300 import deck
+
+# p after a mixed solve differs from the FP64 solve by FP32 rounding of one
+# refinement pass's correction at most: 1e-8 of max|p| at these sizes.
+P_REL_TOL = 1e-8
+
+
+def _setup(n=64, seed=3):
+    case = deck.cavity(n, 100.0, 0.005, solver="rb_sor")
+    o = O.Oracle(case.nx + 1, case.ny + 1)
+    met = o.grid(case.nx, case.ny, case.x, case.y)
+    rng = np.random.default_rng(seed)
+    f = [np.asfortranarray(rng.normal(size=(case.nx + 2, case.ny + 2)) * 0.05) for _ in range(3)]
+    u, v, p = f
+    o.vel_bound_cond(case.nx, case.ny, case.regions, u, v)
+    o.pres_bound_cond(case.nx, case.ny, case.regions, p)
+    return case, o, met, u, v, p
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+@pytest.mark.parametrize("sortol", [1e-6, 1e-7, 3e-8])
+@pytest.mark.parametrize("inner", [8, 64])
+def test_mixed_model_stops_where_fp64_stops(sortol, inner):
+    case, o, met, u, v, p = _setup()
+    prm = deck.RunParams(**{**case.params.__dict__, "sortol": sortol})
+    p64 = p.copy(order="F")
+    n64 = o.ppe(case.nx, case.ny, case.regions, prm, met, u, v, p64, npsolver=5, msorit=4000)
+    pm = p.copy(order="F")
+    nm = M.ppe_mixed(case.nx, case.ny, met, u, v, pm, prm.dk, 4000, sortol, prm.sorrel, inner)
+    assert n64 < 4000 and nm == n64
+    assert _rel(pm, p64) <= P_REL_TOL
+
+
+def test_mixed_model_fp64_sweeps_equal_plain_solve():
+    """With FP64 sweeps the refinement form is the plain iteration up to
+    rounding: the algebra of the correction equation is right."""
+    case, o, met, u, v, p = _setup(32, seed=5)
+    prm = case.params
+    p64 = p.copy(order="F")
+    n64 = o.ppe(case.nx, case.ny, case.regions, prm, met, u, v, p64, npsolver=5, msorit=500)
+    pm = p.copy(order="F")
+    nm = M.ppe_mixed(case.nx, case.ny, met, u, v, pm, prm.dk, 500, prm.sortol, prm.sorrel, 37,
+                     dtype=np.float64)
+    assert nm == n64
+    assert _rel(pm, p64) <= 1e-13
+
+
+def test_divergence_matches_oracle_rhs():
+    """The model's divergence is the oracle's b*dk on the pressure cells."""
+    case, o, met, u, v, p = _setup(32, seed=7)
+    div = M.divergence(case.nx, case.ny, met, u, v)
+    # one FP64 sweep from p = b-consistent start: compare through the oracle's
+    # Ppe with msorit = 1 on the unit stencil: p_new - p_old = sum
+    p1 = p.copy(order="F")
+    o.ppe(case.nx, case.ny, case.regions, case.params, met, u, v, p1, npsolver=5, msorit=1)
+    # black points of the first sweep see only old neighbours
+    b = div / case.params.dk
+    i, j = 2, 2  # (i+j) even: black
+    s = b[i - 2, j - 2] - p[i, j - 1] - p[i - 1, j] - p[i + 1, j] - p[i, j + 1]
+    s = s / -4.0 - p[i, j]
+    assert p1[i, j] == p[i, j] + 1.0 * s
+
+
+def test_mixed_time_loop_close_to_fp64():
+    """A few steps of the 64x64 cavity: mixed vs the FP64 oracle, u, v, p
+    within 1e-7 relative, same iteration counts, the divergence check of
+    the same size as the FP64 path's."""
+    case = deck.cavity(64, 100.0, 0.005, solver="rb_sor")
+    ref = O.OracleRun(case)
+    ref.step(4)
+    mx = M.MixedRun(case, inner=32)
+    mx.step(4)
+    assert mx.cold_nconv == ref.cold_nconv
+    assert [(h[0], h[1]) for h in mx.history] == [(h[0], h[1]) for h in ref.history]
+    for name in "uvp":
+        assert _rel(mx.f[name], ref.f[name]) <= 1e-7, name
+    d64 = M.div_check(case.nx, case.ny, ref.met, ref.f["u"], ref.f["v"])
+    assert mx.history[-1][3] <= 2.0 * d64 + 1e-14

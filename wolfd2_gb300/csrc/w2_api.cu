@@ -50,6 +50,13 @@ struct w2_ctx {
   size_t tiled_smem = 0;
   TileGeom tg{};
   int use_tiled = 1;
+  // mixed-precision Poisson sweeps
+  float *e32[2] = {};
+  bool mixed_ok = false;
+  int mixed_K = 4, mixed_threads = 512;
+  size_t mixed_smem = 0;
+  MixedGeom mg{};
+  int prec_dropin = W2_PREC_FP64, refine_dropin = 0;
 };
 
 namespace {
@@ -408,8 +415,97 @@ int launch_ppe_tiled(w2_ctx *c, int lcartes, int msorit, double dk, double sorto
   return W2_OK;
 }
 
+// ---- mixed-precision Poisson sweeps ----------------------------------------
+
+const void *mixed_kernel(int K) {
+  switch (K) {
+    case 2: return (const void *)k_ppe_mixed<2>;
+    case 4: return (const void *)k_ppe_mixed<4>;
+    case 8: return (const void *)k_ppe_mixed<8>;
+  }
+  return nullptr;
+}
+
+// One tile per block (one block per SM): the split of the unknowns into at
+// most nsm tiles, tx even, whose largest tile sweeps the least area per
+// group of K sweeps, within the shared-memory limit.
+void plan_mixed(w2_ctx *c) {
+  c->mixed_ok = false;
+  const int K = c->mixed_K;
+  const void *kf = mixed_kernel(K);
+  if (!kf) return;
+  int maxsmem = 0;
+  cudaDeviceGetAttribute(&maxsmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+  cudaFuncAttributes fa{};
+  if (cudaFuncGetAttributes(&fa, kf) != cudaSuccess || (size_t)maxsmem <= fa.sharedSizeBytes) return;
+  const size_t limit = (size_t)maxsmem - fa.sharedSizeBytes;  // less the static arrays
+  if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit) != cudaSuccess)
+    return;
+  const int NX = c->nx - 1, NY = c->ny - 1, H = 2 * K;
+  double best = 1e300;
+  for (int ntx = 1; ntx <= std::max(1, NX / 8); ++ntx) {
+    int tx = (NX + ntx - 1) / ntx;
+    tx += tx & 1;
+    if ((NX + tx - 1) / tx != ntx) continue;
+    for (int nty = 1; nty <= std::max(1, NY / 8) && ntx * nty <= c->nsm; ++nty) {
+      const int ty = (NY + nty - 1) / nty;
+      if ((NY + ty - 1) / ty != nty) continue;
+      const size_t smem = mixed_smem_bytes(K, tx, ty);
+      if (smem > limit) continue;
+      double area = 0.0;
+      for (int e = H - 1; e >= 0; --e) area += (double)(tx + 2 * e) * (ty + 2 * e);
+      if (area < best) {
+        best = area;
+        c->mg = MixedGeom{tx, ty, ntx, nty};
+        c->mixed_smem = smem;
+      }
+    }
+  }
+  if (best >= 1e300) return;
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kf, c->mixed_threads, c->mixed_smem);
+  if (occ < 1) return;
+  c->mixed_ok = true;
+}
+
+// The mixed path covers npsolver 5/6 on Cartesian grids whose rows are all
+// the unit stencil (no blockages).
+int mixed_check(w2_ctx *c, int lcartes, int npsolver) {
+  if (npsolver != 5 && npsolver != 6)
+    return fail(c, W2_E_UNSUPPORTED, "mixed precision needs ppe_solver rb_sor or rb_sorp (5/6), got %d", npsolver);
+  if (!lcartes || !c->dev.ppe_unit)
+    return fail(c, W2_E_UNSUPPORTED, "mixed precision needs a Cartesian unit-stencil grid without blockages");
+  if (!c->mixed_ok) return fail(c, W2_E_UNSUPPORTED, "no mixed-precision tile plan fits this grid");
+  return W2_OK;
+}
+
+int auto_inner(w2_ctx *c, int req) {
+  if (req > 0) return req;
+  return 16 * c->mixed_K;
+}
+
+int launch_ppe_mixed(w2_ctx *c, int lcartes, int msorit, double dk, double sortol, double sorrel,
+                     int inner, const double *u, const double *v, double *p, StepOut *out) {
+  Dev d = c->dev;
+  MixedGeom g = c->mg;
+  MixedArgs a{lcartes, msorit, auto_inner(c, inner), dk, sortol, (float)sorrel, u, v, p,
+              c->e32[0], c->e32[1]};
+  void *args[] = {&d, &g, &a, &out};
+  c->launches++;
+  cudaError_t e = cudaLaunchCooperativeKernel(mixed_kernel(c->mixed_K), dim3(c->nsm),
+                                              dim3(c->mixed_threads), args, c->mixed_smem, c->st);
+  if (e != cudaSuccess) return fail(c, W2_E_CUDA, "mixed PPE launch: %s", cudaGetErrorString(e));
+  return W2_OK;
+}
+
 int launch_ppe(w2_ctx *c, int lcartes, int npsolver, int msorit, double dk, double sortol,
                double sorrel, const double *u, const double *v, double *p) {
+  if (c->prec_dropin == W2_PREC_MIXED) {
+    int rc = mixed_check(c, lcartes, npsolver);
+    if (rc) return rc;
+    ProfScope ps(c, W2_K_PPE);
+    return launch_ppe_mixed(c, lcartes, msorit, dk, sortol, sorrel, c->refine_dropin, u, v, p, c->d_out);
+  }
   if (tiled_applies(c, npsolver, sorrel)) {
     ProfScope ps(c, W2_K_PPE);
     return launch_ppe_tiled(c, lcartes, msorit, dk, sortol, u, v, p, c->d_out);
@@ -497,6 +593,8 @@ int wolfd2gpu_create(w2_ctx **out, int mnx, int mny, int mgri, int mgrj, int nx,
                    &d.pa5, &d.div, &d.pb, &d.ppn, &d.la3p, &d.lbp, &d.qh};
   for (double **w : wa)
     if (!(*w = dalloc<double>(c, c->nf))) return bad(W2_E_CUDA);
+  for (int k = 0; k < 2; ++k)
+    if (!(c->e32[k] = dalloc<float>(c, c->nf))) return bad(W2_E_CUDA);
   const int nX = nx * (ny - 1), nY = (nx - 1) * ny;
   if (make_chain(c, d.x1, nX, true) || make_chain(c, d.x2, nX, false) ||
       make_chain(c, d.y1, nY, true) || make_chain(c, d.y2, nY, false))
@@ -624,6 +722,29 @@ static int finish_coefficients(w2_ctx *c) {
   CK(cudaStreamSynchronize(c->st));
   c->dev.ppe_unit = (h == 0) ? 1 : 0;
   plan_tiles(c);
+  plan_mixed(c);
+  return W2_OK;
+}
+
+int wolfd2gpu_set_precision(w2_ctx *c, int precision, int refine_sweeps) {
+  if (!c) return W2_E_ARG;
+  if (precision != W2_PREC_FP64 && precision != W2_PREC_MIXED)
+    return fail(c, W2_E_ARG, "unknown precision mode %d", precision);
+  if (refine_sweeps < 0) return fail(c, W2_E_ARG, "refine_sweeps < 0");
+  c->prec_dropin = precision;
+  c->refine_dropin = refine_sweeps;
+  return W2_OK;
+}
+
+int wolfd2gpu_tune_mixed(w2_ctx *c, int sweeps_per_barrier, int threads) {
+  if (!c) return W2_E_ARG;
+  if (sweeps_per_barrier != 0 && !mixed_kernel(sweeps_per_barrier))
+    return fail(c, W2_E_ARG, "sweeps per barrier must be 2, 4 or 8");
+  if (threads != 0 && (threads % 32 || threads < 64 || threads > 1024))
+    return fail(c, W2_E_ARG, "threads must be a multiple of 32 in 64..1024");
+  if (sweeps_per_barrier) c->mixed_K = sweeps_per_barrier;
+  if (threads) c->mixed_threads = threads;
+  if (c->metrics_ok) plan_mixed(c);
   return W2_OK;
 }
 
@@ -864,8 +985,12 @@ static int check_params(w2_ctx *c, const w2_params *prm) {
   if (!prm) return fail(c, W2_E_ARG, "null params");
   if (prm->npsolver < 1 || prm->npsolver > 6 || prm->msorit < 1 || prm->mqiter < 1)
     return fail(c, W2_E_ARG, "bad solver parameters");
+  if (prm->precision == W2_PREC_MIXED) {
+    if (prm->refine_sweeps < 0) return fail(c, W2_E_ARG, "refine_sweeps < 0");
+    return mixed_check(c, prm->lcartes, prm->npsolver);
+  }
   if (prm->precision != W2_PREC_FP64)
-    return fail(c, W2_E_UNSUPPORTED, "precision mode %d not available in this build", prm->precision);
+    return fail(c, W2_E_ARG, "unknown precision mode %d", prm->precision);
   return W2_OK;
 }
 
@@ -875,8 +1000,14 @@ int wolfd2gpu_cold_start(w2_ctx *c, const w2_params *prm, int *nSorConv) {
   if ((rc = check_params(c, prm))) return rc;
   double *u = c->U[c->cur], *v = c->V[c->cur], *p = c->P[c->cur];
   if ((rc = launch_bc(c, BC_VEL, u, v, p))) return rc;
-  if ((rc = launch_ppe(c, prm->lcartes, prm->npsolver, prm->msorit, prm->dk, prm->sortol, prm->sorrel, u, v, p)))
-    return rc;
+  if (prm->precision == W2_PREC_MIXED) {
+    ProfScope ps(c, W2_K_PPE);
+    rc = launch_ppe_mixed(c, prm->lcartes, prm->msorit, prm->dk, prm->sortol, prm->sorrel,
+                          prm->refine_sweeps, u, v, p, c->d_out);
+  } else {
+    rc = launch_ppe(c, prm->lcartes, prm->npsolver, prm->msorit, prm->dk, prm->sortol, prm->sorrel, u, v, p);
+  }
+  if (rc) return rc;
   if ((rc = launch_bc(c, BC_PRES, u, v, p))) return rc;
   c->launches++;
   k_project<<<grid_blocks(c), c->threads, 0, c->st>>>(c->dev, prm->dk, p, u, v);
@@ -932,7 +1063,12 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
       }
     }
     if ((rc = launch_bc(c, BC_VEL | BC_PRES, us, vs, p))) break;
-    if (tiled_applies(c, prm->npsolver, prm->sorrel)) {
+    if (prm->precision == W2_PREC_MIXED) {
+      ProfScope ps(c, W2_K_PPE);
+      if ((rc = launch_ppe_mixed(c, prm->lcartes, prm->msorit, prm->dk, prm->sortol, prm->sorrel,
+                                 prm->refine_sweeps, us, vs, p, o)))
+        break;
+    } else if (tiled_applies(c, prm->npsolver, prm->sorrel)) {
       ProfScope ps(c, W2_K_PPE);
       if ((rc = launch_ppe_tiled(c, prm->lcartes, prm->msorit, prm->dk, prm->sortol, us, vs, p, o))) break;
     } else {
@@ -965,6 +1101,7 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
       stats[s].nQLiter = outs[s].nql;
       stats[s].nSorConv = outs[s].nsor;
       for (int k = 0; k < 4; ++k) stats[s].dif[k] = outs[s].dif[k];
+      stats[s].divmax = outs[s].divmax;
     }
     if (diverged_at < 0 && mx > 1.0e12) diverged_at = s;
   }

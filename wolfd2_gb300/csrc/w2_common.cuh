@@ -83,9 +83,11 @@ struct Sync {
   int pad0;
   int halt;           // a step diverged: later stages of the run are skipped
   int max_rounds;     // most verification rounds any chain solve needed
-  unsigned long long red[16];  // max-reductions (bit patterns of doubles >= 0):
+  unsigned long long red[48];  // max-reductions (bit patterns of doubles >= 0):
                                // [0..2] momentum ring, [3..5] PPE ring,
-                               // [6..8] step norms, [9..] scratch
+                               // [6..8] step norms, [9] scratch, [10..15]
+                               // tiled PPE ring, [16] divergence check,
+                               // [17..40] mixed PPE ring
   int iout[8];                 // chain verification flags ([0..2] fwd, [3..5] bwd)
   double dout[8];              // small double results
 };

@@ -3,6 +3,7 @@
 #include "w2_bc.cuh"
 #include "w2_momentum.cuh"
 #include "w2_ppe.cuh"
+#include "w2_ppe_mixed.cuh"
 #include "w2_ppe_tiled.cuh"
 
 namespace w2 {
@@ -13,6 +14,7 @@ constexpr int kMaxThreads = 512;
 struct StepOut {
   int nql, nsor;
   double dif[4];
+  double divmax;  // max |Divergence(u,v)| on the pressure cells after the step
 };
 
 // ---- grid metrics (grid.f:258-535) ------------------------------------
@@ -228,6 +230,17 @@ __global__ void __launch_bounds__(kMaxThreads, 1) k_ppe_tiled(Dev d, TileGeom g,
   if (blockIdx.x == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? msorit : nconv;
 }
 
+// Mixed-precision red/black SOR (FP32 sweeps, FP64 residual and correction)
+// with K sweeps per grid barrier; one tile per block.
+template <int K>
+__global__ void __launch_bounds__(1024, 1) k_ppe_mixed(Dev d, MixedGeom g, MixedArgs a,
+                                                      StepOut *out) {
+  if (d.sync->halt) return;
+  const int nconv = ppe_mixed<K>(d, g, a);
+  if (nconv < 0) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? a.msorit : nconv;
+}
+
 // ---- Project (utility.f:253-440), masked -------------------------------
 __device__ void project_grid(const Dev &d, double dk, const double *p, double *u, double *v) {
   const int nx = d.nx, ny = d.ny, W = nx + 2, H = ny + 2;
@@ -275,9 +288,22 @@ __global__ void k_diff_norm(Dev d, const double *a, const double *b, unsigned lo
   block_max_to(slot, diff_norm_local(d, a, b));
 }
 
+// Discrete divergence check on the pressure cells (2..nx, 2..ny) outside
+// blockages: max |Divergence(u,v)| of the projected field, FP64.
+__device__ double div_check_local(const Dev &d, const double *u, const double *v) {
+  const int nx = d.nx, ny = d.ny;
+  double mx = 0.0;
+  for (int t = gtid(); t < (nx - 1) * (ny - 1); t += gthreads()) {
+    const int i = t % (nx - 1) + 2, j = t / (nx - 1) + 2;
+    if (d.mask[IX(d, i, j)] & MK_DIVZ) continue;
+    mx = dmax(mx, fabs(div_point(d, u, v, i, j)));
+  }
+  return mx;
+}
+
 // Tail of one step, main.f:813-972: PresBoundCond, Project, boundary
-// conditions of the starred and new fields, the three step norms and the
-// divergence guard.
+// conditions of the starred and new fields, the three step norms, the
+// divergence guard and the discrete divergence check.
 __global__ void __launch_bounds__(kMaxThreads) k_step_post(Dev d, double dk, double *p,
                                                            const double *pn, const double *un,
                                                            const double *vn, double *u,
@@ -287,7 +313,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_step_post(Dev d, double dk, dou
   if (blockIdx.x == 0) {
     if (!pres_bound_cond_block(d, p) && threadIdx.x == 0) set_error(sy, W2_E_BCFLAG);
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) sy->red[6] = sy->red[7] = sy->red[8] = 0ull;
+  if (blockIdx.x == 0 && threadIdx.x == 0) sy->red[6] = sy->red[7] = sy->red[8] = sy->red[16] = 0ull;
   if (!grid_sync(sy)) return;
   project_grid(d, dk, p, u, v);
   if (!grid_sync(sy)) return;
@@ -302,12 +328,14 @@ __global__ void __launch_bounds__(kMaxThreads) k_step_post(Dev d, double dk, dou
   block_max_to(&sy->red[6], diff_norm_local(d, pn, p));
   block_max_to(&sy->red[7], diff_norm_local(d, un, u));
   block_max_to(&sy->red[8], diff_norm_local(d, vn, v));
+  block_max_to(&sy->red[16], div_check_local(d, u, v));
   if (!grid_sync(sy)) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     out->dif[0] = slot_value(&sy->red[6]);
     out->dif[1] = slot_value(&sy->red[7]);
     out->dif[2] = slot_value(&sy->red[8]);
     out->dif[3] = 0.0;
+    out->divmax = slot_value(&sy->red[16]);
     double mx = dmax(dmax(out->dif[0], out->dif[1]), out->dif[2]);
     if (mx > 1.0e12) sy->halt = 1;
   }

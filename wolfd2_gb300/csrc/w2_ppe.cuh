@@ -60,26 +60,29 @@ __device__ void ppe_check_unit(const Dev &d, int *flag) {
   }
 }
 
-// Divergence nloc = 1, pressure.f:287-299, then blockage zeroing.
+// Divergence nloc = 1 at cell (i,j), pressure.f:287-299.
+__device__ __forceinline__ double div_point(const Dev &d, const double *u, const double *v,
+                                            int i, int j) {
+  const Metrics &m = d.m;
+  const size_t o = IX(d, i, j), ow = IX(d, i - 1, j), os = IX(d, i, j - 1);
+  const double ucij = m.yeu[o] * u[o] -
+                      m.xeu[o] * (v[IX(d, i + 1, j)] + v[o] + v[IX(d, i + 1, j - 1)] + v[os]) / 4.0;
+  const double uci1j = m.yeu[ow] * u[ow] -
+                       m.xeu[ow] * (v[o] + v[ow] + v[os] + v[IX(d, i - 1, j - 1)]) / 4.0;
+  const double vcij = m.xzv[o] * v[o] -
+                      m.yzv[o] * (u[IX(d, i, j + 1)] + u[IX(d, i - 1, j + 1)] + u[o] + u[ow]) / 4.0;
+  const double vcij1 = m.xzv[os] * v[os] -
+                       m.yzv[os] * (u[o] + u[ow] + u[os] + u[IX(d, i - 1, j - 1)]) / 4.0;
+  return ucij - uci1j + vcij - vcij1;
+}
+
+// Divergence nloc = 1 on i,j = 1..nx,1..ny, then blockage zeroing.
 __device__ void ppe_divergence(const Dev &d, const double *u, const double *v) {
   const int nx = d.nx, ny = d.ny;
-  const Metrics &m = d.m;
   for (int t = gtid(); t < nx * ny; t += gthreads()) {
     const int i = t % nx + 1, j = t / nx + 1;
-    const size_t o = IX(d, i, j), ow = IX(d, i - 1, j), os = IX(d, i, j - 1);
-    if (d.mask[o] & MK_DIVZ) {
-      d.div[o] = 0.0;
-      continue;
-    }
-    const double ucij = m.yeu[o] * u[o] -
-                        m.xeu[o] * (v[IX(d, i + 1, j)] + v[o] + v[IX(d, i + 1, j - 1)] + v[os]) / 4.0;
-    const double uci1j = m.yeu[ow] * u[ow] -
-                         m.xeu[ow] * (v[o] + v[ow] + v[os] + v[IX(d, i - 1, j - 1)]) / 4.0;
-    const double vcij = m.xzv[o] * v[o] -
-                        m.yzv[o] * (u[IX(d, i, j + 1)] + u[IX(d, i - 1, j + 1)] + u[o] + u[ow]) / 4.0;
-    const double vcij1 = m.xzv[os] * v[os] -
-                         m.yzv[os] * (u[o] + u[ow] + u[os] + u[IX(d, i - 1, j - 1)]) / 4.0;
-    d.div[o] = ucij - uci1j + vcij - vcij1;
+    const size_t o = IX(d, i, j);
+    d.div[o] = (d.mask[o] & MK_DIVZ) ? 0.0 : div_point(d, u, v, i, j);
   }
 }
 

@@ -61,7 +61,8 @@ class Params(C.Structure):
 
 
 class StepStat(C.Structure):
-    _fields_ = [("nQLiter", C.c_int), ("nSorConv", C.c_int), ("dif", C.c_double * 4)]
+    _fields_ = [("nQLiter", C.c_int), ("nSorConv", C.c_int), ("dif", C.c_double * 4),
+                ("divmax", C.c_double)]
 
 
 _lib = None
@@ -104,6 +105,8 @@ def lib():
     L.wolfd2gpu_last_error.argtypes = [vp]
     L.wolfd2gpu_last_error.restype = C.c_char_p
     L.wolfd2gpu_tune.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
+    L.wolfd2gpu_tune_mixed.argtypes = [vp, C.c_int, C.c_int]
+    L.wolfd2gpu_set_precision.argtypes = [vp, C.c_int, C.c_int]
     L.wolfd2gpu_device_fields.argtypes = [vp, C.POINTER(_dp), C.POINTER(_dp), C.POINTER(_dp), _ip]
     L.wolfd2gpu_launch_count.argtypes = [vp]
     L.wolfd2gpu_launch_count.restype = C.c_longlong
@@ -217,6 +220,15 @@ class Solver:
     def tune(self, seg: int = 0, warm: int = 0, threads: int = 0, blocks_per_sm: int = 0):
         self._check(self.L.wolfd2gpu_tune(self.h, seg, warm, threads, blocks_per_sm))
 
+    def tune_mixed(self, sweeps_per_barrier: int = 0, threads: int = 0):
+        """Mixed Poisson kernel shape: sweeps between grid barriers (2, 4, 8)
+        and threads per block; 0 keeps the current value."""
+        self._check(self.L.wolfd2gpu_tune_mixed(self.h, sweeps_per_barrier, threads))
+
+    def set_precision(self, precision: int, refine_sweeps: int = 0):
+        """Precision of the drop-in Ppe (PREC_FP64 or PREC_MIXED)."""
+        self._check(self.L.wolfd2gpu_set_precision(self.h, precision, refine_sweeps))
+
     # ---- reference drop-ins ------------------------------------------------
     def nAuxMomentum(self, mqiter, dk, re, fr, qtol, d, dn, un, vn, us, vs) -> int:
         out = C.c_int()
@@ -273,7 +285,7 @@ class Solver:
         pr = Params.of(prm, **kw)
         st = (StepStat * max(nsteps, 1))()
         self._check(self.L.wolfd2gpu_step(self.h, C.byref(pr), nsteps, st))
-        return [(s.nQLiter, s.nSorConv, tuple(s.dif)) for s in st[:nsteps]]
+        return [(s.nQLiter, s.nSorConv, tuple(s.dif), s.divmax) for s in st[:nsteps]]
 
     def sync(self) -> None:
         self._check(self.L.wolfd2gpu_sync(self.h))
