@@ -178,7 +178,7 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": config_of(args, case, args.refine_sweeps or 64),
+        "config": config_of(args, case, args.refine_sweeps or 128),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": kind,
                          "sample": f"{args.warmup} + {args.steps} full time steps of the same case; {how}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -321,7 +321,7 @@ def run_ours(args):
         s.tune(seg=args.seg, warm=args.warm, threads=args.threads, blocks_per_sm=args.blocks_per_sm)
     if args.mixed_k or args.mixed_threads:
         s.tune_mixed(args.mixed_k, args.mixed_threads)
-    inner = args.refine_sweeps or 16 * (args.mixed_k or 4)
+    inner = args.refine_sweeps or 16 * (args.mixed_k or 8)
     prm = case.params
     st = torch.cuda.ExternalStream(s.stream(), device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -440,7 +440,7 @@ def main():
                     help="headline path; mixed also times plain FP64 beside it")
     ap.add_argument("--refine-sweeps", type=int, default=0,
                     help="mixed: FP32 sweeps per refinement pass (0: 16 x sweeps per barrier)")
-    ap.add_argument("--mixed-k", type=int, default=0, help="mixed: sweeps per grid barrier (2/4/8)")
+    ap.add_argument("--mixed-k", type=int, default=0, help="mixed: sweeps per grid barrier (4/8)")
     ap.add_argument("--mixed-threads", type=int, default=0, help="mixed: threads per block")
     args = ap.parse_args()
     if args.impl == "reference":

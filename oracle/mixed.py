@@ -17,8 +17,11 @@ and the points of one colour never read each other, so the GPU result is
 expected to equal this model bit for bit.  The model's distance from the FP64
 oracle is the accuracy figure of the mixed path.
 
-``MixedRun`` advances a case with the oracle's FP64 routines for everything
-but the Poisson solve, in the order of main.f:690-972.
+``MixedRun`` advances a case in the order of main.f:690-972 with the mixed
+form's precisions: nAuxMomentum in IEEE single (the oracle's FP32 instance of
+its momentum restatement, on FP32 copies of u, v and of the metrics), the
+mixed Ppe above, and the oracle's FP64 routines for the boundary rows, the
+projection and the step norms.
 """
 from __future__ import annotations
 
@@ -120,6 +123,7 @@ class MixedRun:
         self.inner = inner
         self.o = Oracle(case.nx + 1, case.ny + 1)
         self.met = self.o.grid(case.nx, case.ny, case.x, case.y)
+        self.met32 = self.o.metrics32(self.met)
         self.f = {n: self.o.field() for n in FIELD_NAMES}
         if fields:
             for k, val in fields.items():
@@ -144,8 +148,12 @@ class MixedRun:
         for _ in range(n):
             for a, b in (("pn", "p"), ("un", "u"), ("vn", "v"), ("us", "u"), ("vs", "v")):
                 f[a][...] = f[b]
-            nql = o.naux_momentum(nx, ny, r, prm, self.met, f["d"], f["dn"], f["un"], f["vn"],
-                                  f["us"], f["vs"])
+            un32 = np.asfortranarray(f["un"].astype(np.float32))
+            vn32 = np.asfortranarray(f["vn"].astype(np.float32))
+            us32, vs32, z32 = un32.copy(order="F"), vn32.copy(order="F"), o.field32()
+            nql = o.naux_momentum_f32(nx, ny, r, prm, self.met32, z32, z32, un32, vn32, us32, vs32)
+            f["us"][...] = us32.astype(np.float64)
+            f["vs"][...] = vs32.astype(np.float64)
             if prm.nfiltu == 1:
                 o.filter(nx, ny, 1, r, prm.fpu, f["us"])
             if prm.nfiltv == 1:

@@ -39,6 +39,13 @@ class _Metrics(C.Structure):
     _fields_ = [(n, _dp) for n in METRIC_NAMES]
 
 
+_fp = C.POINTER(C.c_float)
+
+
+class _Metrics32(C.Structure):
+    _fields_ = [(n, _fp) for n in METRIC_NAMES]
+
+
 class _Params(C.Structure):
     _fields_ = [(n, C.c_double) for n in "dk re fr qtol sortol sorrel fpu fpv".split()] + \
                [(n, C.c_int) for n in "mqiter npsolver msorit nfiltu nfiltv lcartes".split()]
@@ -50,8 +57,9 @@ class _Fields(C.Structure):
 
 def build(force: bool = False) -> str:
     """Compile the oracle library (gcc, no FMA contraction)."""
+    srcs = ("wolfd2_oracle.c", "wolfd2_oracle.h", "momentum_impl.h")
     if force or not os.path.exists(LIB_PATH) or \
-            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "wolfd2_oracle.c")):
+            os.path.getmtime(LIB_PATH) < max(os.path.getmtime(os.path.join(HERE, f)) for f in srcs):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 
@@ -71,6 +79,11 @@ def lib():
                                             C.POINTER(_Regions), C.c_double, C.c_double,
                                             C.c_double, C.c_double, C.POINTER(_Metrics),
                                             _dp, _dp, _dp, _dp, _dp, _dp]
+            L.w2o_naux_momentum_f32.restype = C.c_int
+            L.w2o_naux_momentum_f32.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                                C.POINTER(_Regions), C.c_double, C.c_double,
+                                                C.c_double, C.c_double, C.POINTER(_Metrics32),
+                                                _fp, _fp, _fp, _fp, _fp, _fp]
             L.w2o_ppe.restype = C.c_int
             L.w2o_ppe.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions), C.c_int,
                                   C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
@@ -170,6 +183,24 @@ class Oracle:
                                         prm.re, prm.fr, prm.qtol,
                                         C.byref(self.metrics_struct(met)),
                                         _ptr(d), _ptr(dn), _ptr(un), _ptr(vn), _ptr(us), _ptr(vs))
+
+    def field32(self) -> np.ndarray:
+        return np.zeros((self.mnx + 1, self.mny + 1), np.float32, order="F")
+
+    @staticmethod
+    def metrics32(met: Dict[str, np.ndarray]) -> Dict[str, np.ndarray]:
+        """The metric arrays rounded to single precision."""
+        return {n: np.asfortranarray(met[n].astype(np.float32)) for n in METRIC_NAMES}
+
+    def naux_momentum_f32(self, nx, ny, regs, prm, met32, d, dn, un, vn, us, vs) -> int:
+        """nAuxMomentum in IEEE single on float32 Fortran-ordered arrays."""
+        rs = self.regions_struct(regs)
+        ms = _Metrics32(*[_ptr(met32[n], C.c_float) for n in METRIC_NAMES])
+        f = [_ptr(a, C.c_float) for a in (d, dn, un, vn, us, vs)]
+        for a in (d, dn, un, vn, us, vs):
+            assert a.dtype == np.float32
+        return self.L.w2o_naux_momentum_f32(self.h, nx, ny, prm.mqiter, C.byref(rs), prm.dk,
+                                            prm.re, prm.fr, prm.qtol, C.byref(ms), *f)
 
     def ppe(self, nx, ny, regs, prm, met, u, v, p, npsolver=None, msorit=None) -> int:
         rs = self.regions_struct(regs)

@@ -31,12 +31,20 @@ typedef struct {
   double *b; /* b(mn)   */
 } w2o_mom_ws;
 
+typedef struct {
+  float *cj1, *cj2, *c1s, *c2s, *c1n, *c2n, *cps, *cpn, *cpj;
+  float *cnvs, *difs, *cnvn, *difn;
+  float *a, *b;
+} w2o_mom_ws32;
+
 struct w2o_ctx {
   int mnx, mny;
   size_t ld, nf; /* leading dimension mnx+1 and field size */
   size_t mn;     /* mnx*mny (chain workspace length) */
   w2o_mom_ws wx, wy;       /* XMomentum / YMomentum statics            */
   double *dus, *dvs;       /* nAuxMomentum statics                     */
+  w2o_mom_ws32 wx32, wy32; /* the same in single precision             */
+  float *dus32, *dvs32;
   double *div, *pa, *pb;   /* Ppe statics: div, a(mn,5), b(mn)         */
   double *rbp_pn;          /* SlorRBP static pn(0:mnx,0:mny)           */
   double *qh;              /* Filter static qh                         */
@@ -82,6 +90,30 @@ static void mom_ws_init(w2o_mom_ws *w, size_t nf, size_t mn) {
   w->a = zalloc(3 * mn); w->b = zalloc(mn);
 }
 
+static float *zalloc32(size_t n) {
+  float *p = (float *)calloc(n ? n : 1, sizeof(float));
+  if (!p) {
+    fprintf(stderr, "oracle: out of memory\n");
+    exit(3);
+  }
+  return p;
+}
+
+static void mom_ws32_init(w2o_mom_ws32 *w, size_t nf, size_t mn) {
+  w->cj1 = zalloc32(nf); w->cj2 = zalloc32(nf); w->c1s = zalloc32(nf);
+  w->c2s = zalloc32(nf); w->c1n = zalloc32(nf); w->c2n = zalloc32(nf);
+  w->cps = zalloc32(nf); w->cpn = zalloc32(nf); w->cpj = zalloc32(nf);
+  w->cnvs = zalloc32(nf); w->difs = zalloc32(nf); w->cnvn = zalloc32(nf);
+  w->difn = zalloc32(nf);
+  w->a = zalloc32(3 * mn); w->b = zalloc32(mn);
+}
+
+static void mom_ws32_free(w2o_mom_ws32 *w) {
+  free(w->cj1); free(w->cj2); free(w->c1s); free(w->c2s); free(w->c1n);
+  free(w->c2n); free(w->cps); free(w->cpn); free(w->cpj); free(w->cnvs);
+  free(w->difs); free(w->cnvn); free(w->difn); free(w->a); free(w->b);
+}
+
 static void mom_ws_free(w2o_mom_ws *w) {
   free(w->cj1); free(w->cj2); free(w->c1s); free(w->c2s); free(w->c1n);
   free(w->c2n); free(w->cps); free(w->cpn); free(w->cpj); free(w->cnvs);
@@ -97,6 +129,9 @@ w2o_ctx *w2o_create(int mnx, int mny) {
   mom_ws_init(&c->wx, c->nf, c->mn);
   mom_ws_init(&c->wy, c->nf, c->mn);
   c->dus = zalloc(c->nf); c->dvs = zalloc(c->nf);
+  mom_ws32_init(&c->wx32, c->nf, c->mn);
+  mom_ws32_init(&c->wy32, c->nf, c->mn);
+  c->dus32 = zalloc32(c->nf); c->dvs32 = zalloc32(c->nf);
   c->div = zalloc(c->nf); c->pa = zalloc(5 * c->mn); c->pb = zalloc(c->mn);
   c->rbp_pn = zalloc(c->nf); c->qh = zalloc(c->nf);
   c->xu = zalloc(c->nf); c->yu = zalloc(c->nf); c->xv = zalloc(c->nf);
@@ -110,6 +145,8 @@ w2o_ctx *w2o_create(int mnx, int mny) {
 void w2o_destroy(w2o_ctx *c) {
   if (!c) return;
   mom_ws_free(&c->wx); mom_ws_free(&c->wy);
+  mom_ws32_free(&c->wx32); mom_ws32_free(&c->wy32);
+  free(c->dus32); free(c->dvs32);
   free(c->dus); free(c->dvs); free(c->div); free(c->pa); free(c->pb);
   free(c->rbp_pn); free(c->qh); free(c->xu); free(c->yu); free(c->xv);
   free(c->yv); free(c->xc); free(c->yc); free(c->lin); free(c->rbp_dif);
@@ -232,437 +269,6 @@ void w2o_grid(w2o_ctx *c, int nx, int ny, double *x, double *y,
 /* momentum.f                                                          */
 /* ------------------------------------------------------------------ */
 
-/* AltTridLU, momentum.f:1307-1339.  a is a(3,n) column-major: a(k,i) at
- * a[(k-1) + 3*(i-1)].  Row 1's super-diagonal is divided by the ORIGINAL
- * diagonal of row 2 (momentum.f:1319). */
-void w2o_alt_trid_lu(int n, double *a, double *b) {
-#define A(k, i) a[((k)-1) + 3 * (size_t)((i)-1)]
-#define B(i) b[(i)-1]
-  int i;
-  A(3, 1) = A(3, 1) / A(2, 2);
-  B(1) = B(1) / A(2, 1);
-  for (i = 2; i <= n - 1; i++) {
-    A(2, i) = A(2, i) - (A(1, i) * A(3, i - 1));
-    A(3, i) = A(3, i) / A(2, i);
-    B(i) = (B(i) - A(1, i) * B(i - 1)) / A(2, i);
-  }
-  A(2, n) = A(2, n) - (A(1, n) * A(3, n - 1));
-  B(n) = (B(n) - A(1, n) * B(n - 1)) / A(2, n);
-  for (i = n - 1; i >= 1; i--) B(i) = B(i) - (A(3, i) * B(i + 1));
-#undef A
-#undef B
-}
-
-/* ConvCoef, momentum.f:864-981 (cases 1, 2, 4, 5). */
-static void conv_coef(w2o_ctx *c, int nx, int ny, int ncomp, int njacob,
-                      const double *xzi, const double *xet, const double *yzi,
-                      const double *yet, const double *u, const double *v,
-                      double *cc1, double *cc2) {
-  int i, j;
-  double djac = 1.0;
-  if (njacob == 1) djac = 2.0;
-  switch (ncomp) {
-    case 1:
-      for (j = 1; j <= ny + 1; j++)
-        for (i = 1; i <= nx + 1; i++)
-          F(cc1, i, j) = (djac * F(yet, i, j) * (F(u, i, j) + F(u, i - 1, j)) -
-                          F(xet, i, j) * (F(v, i, j) + F(v, i, j - 1))) * 0.5;
-      for (j = 1; j <= ny; j++)
-        for (i = 1; i <= nx; i++)
-          F(cc2, i, j) = (F(xzi, i, j) * (F(v, i + 1, j) + F(v, i, j)) -
-                          djac * F(yzi, i, j) * (F(u, i, j + 1) + F(u, i, j))) * 0.5;
-      break;
-    case 2:
-      for (j = 1; j <= ny; j++)
-        for (i = 1; i <= nx; i++)
-          F(cc1, i, j) = (F(yet, i, j) * (F(u, i, j + 1) + F(u, i, j)) -
-                          djac * F(xet, i, j) * (F(v, i + 1, j) + F(v, i, j))) * 0.5;
-      for (j = 1; j <= ny + 1; j++)
-        for (i = 1; i <= nx + 1; i++)
-          F(cc2, i, j) = (djac * F(xzi, i, j) * (F(v, i, j) + F(v, i, j - 1)) -
-                          F(yzi, i, j) * (F(u, i, j) + F(u, i - 1, j))) * 0.5;
-      break;
-    case 4:
-      for (j = 1; j <= ny; j++)
-        for (i = 0; i <= nx; i++) {
-          F(cc1, i, j) = djac * F(yet, i, j) * F(u, i, j) -
-                         F(xet, i, j) * (F(v, i + 1, j) + F(v, i, j) +
-                                         F(v, i + 1, j - 1) + F(v, i, j - 1)) / 4.0;
-          F(cc2, i, j) = F(xzi, i, j) * (F(v, i + 1, j) + F(v, i, j) +
-                                         F(v, i + 1, j - 1) + F(v, i, j - 1)) / 4.0 -
-                         djac * F(yzi, i, j) * F(u, i, j);
-        }
-      break;
-    case 5:
-      for (j = 0; j <= ny; j++)
-        for (i = 1; i <= nx; i++) {
-          F(cc1, i, j) = F(yet, i, j) * (F(u, i, j + 1) + F(u, i - 1, j + 1) +
-                                         F(u, i, j) + F(u, i - 1, j)) / 4.0 -
-                         djac * F(xet, i, j) * F(v, i, j);
-          F(cc2, i, j) = djac * F(xzi, i, j) * F(v, i, j) -
-                         F(yzi, i, j) * (F(u, i, j + 1) + F(u, i - 1, j + 1) +
-                                         F(u, i, j) + F(u, i - 1, j)) / 4.0;
-        }
-      break;
-    default:
-      die("Error: Wrong component flag passed to ConvCoef", ncomp, 0);
-  }
-}
-
-/* DConvU, momentum.f:987-1009 */
-static void dconv_u(w2o_ctx *c, int nx, int ny, const double *c1,
-                    const double *c2, const double *u, double *cv) {
-  for (int j = 2; j <= ny; j++)
-    for (int i = 1; i <= nx; i++)
-      F(cv, i, j) = -F(c2, i, j - 1) * F(u, i, j - 1) - F(c1, i, j) * F(u, i - 1, j) +
-                    (F(c1, i + 1, j) - F(c1, i, j) + F(c2, i, j) - F(c2, i, j - 1)) *
-                        F(u, i, j) +
-                    F(c1, i + 1, j) * F(u, i + 1, j) + F(c2, i, j) * F(u, i, j + 1);
-}
-
-/* DDiffU, momentum.f:1015-1045 */
-static void ddiff_u(w2o_ctx *c, int nx, int ny, const double *ac,
-                    const double *bc, const double *bn, const double *gn,
-                    const double *u, double *d) {
-  double s1, s2;
-  for (int j = 2; j <= ny; j++)
-    for (int i = 1; i <= nx; i++) {
-      s1 = F(ac, i + 1, j) * (F(u, i + 1, j) - F(u, i, j)) -
-           F(ac, i, j) * (F(u, i, j) - F(u, i - 1, j)) +
-           F(bc, i + 1, j) * (F(u, i + 1, j + 1) + F(u, i, j + 1) -
-                              F(u, i + 1, j - 1) - F(u, i, j - 1)) -
-           F(bc, i, j) * (F(u, i, j + 1) + F(u, i - 1, j + 1) - F(u, i, j - 1) -
-                          F(u, i - 1, j - 1));
-      s2 = F(bn, i, j) * (F(u, i + 1, j + 1) + F(u, i + 1, j) -
-                          F(u, i - 1, j + 1) - F(u, i - 1, j)) -
-           F(bn, i, j - 1) * (F(u, i + 1, j) + F(u, i + 1, j - 1) -
-                              F(u, i - 1, j) - F(u, i - 1, j - 1)) +
-           F(gn, i, j) * (F(u, i, j + 1) - F(u, i, j)) -
-           F(gn, i, j - 1) * (F(u, i, j) - F(u, i, j - 1));
-      F(d, i, j) = s1 + s2;
-    }
-}
-
-/* DConvV, momentum.f:1051-1073 */
-static void dconv_v(w2o_ctx *c, int nx, int ny, const double *c1,
-                    const double *c2, const double *v, double *cv) {
-  for (int j = 1; j <= ny; j++)
-    for (int i = 2; i <= nx; i++)
-      F(cv, i, j) = -F(c2, i, j) * F(v, i, j - 1) - F(c1, i - 1, j) * F(v, i - 1, j) +
-                    (F(c1, i, j) - F(c1, i - 1, j) + F(c2, i, j + 1) - F(c2, i, j)) *
-                        F(v, i, j) +
-                    F(c1, i, j) * F(v, i + 1, j) + F(c2, i, j + 1) * F(v, i, j + 1);
-}
-
-/* DDiffV, momentum.f:1079-1109 */
-static void ddiff_v(w2o_ctx *c, int nx, int ny, const double *an,
-                    const double *bc, const double *bn, const double *gc,
-                    const double *v, double *d) {
-  double s1, s2;
-  for (int j = 1; j <= ny; j++)
-    for (int i = 2; i <= nx; i++) {
-      s1 = F(an, i, j) * (F(v, i + 1, j) - F(v, i, j)) -
-           F(an, i - 1, j) * (F(v, i, j) - F(v, i - 1, j)) +
-           F(bn, i, j) * (F(v, i + 1, j + 1) + F(v, i, j + 1) -
-                          F(v, i + 1, j - 1) - F(v, i, j - 1)) -
-           F(bn, i - 1, j) * (F(v, i, j + 1) + F(v, i - 1, j + 1) -
-                              F(v, i, j - 1) - F(v, i - 1, j - 1));
-      s2 = F(bc, i, j + 1) * (F(v, i + 1, j + 1) + F(v, i + 1, j) -
-                              F(v, i - 1, j + 1) - F(v, i - 1, j)) -
-           F(bc, i, j) * (F(v, i + 1, j) + F(v, i + 1, j - 1) - F(v, i - 1, j) -
-                          F(v, i - 1, j - 1)) +
-           F(gc, i, j + 1) * (F(v, i, j + 1) - F(v, i, j)) -
-           F(gc, i, j) * (F(v, i, j) - F(v, i, j - 1));
-      F(d, i, j) = s1 + s2;
-    }
-}
-
-/* PorosCoef, momentum.f:1115-1226 */
-static void poros_coef(w2o_ctx *c, int nx, int ny, int ncomp, int njacob,
-                       const w2o_regions *r, const double *u, const double *v,
-                       double *cp) {
-  (void)nx; (void)ny;
-  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
-    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
-      int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
-      int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
-      if (RTYP(r, ireg, jreg) != RM_POROUS) {
-        for (int j = jS; j <= jN; j++)
-          for (int i = iW; i <= iE; i++) F(cp, i, j) = 0.0;
-        continue;
-      }
-      double porc1 = RPAR(dPRporc1, r, ireg, jreg);
-      double porc2 = RPAR(dPRporc2, r, ireg, jreg);
-      double unorm, unrm1, t;
-      if (ncomp == 1) {
-        for (int j = jS + 1; j <= jN; j++)
-          for (int i = iW; i <= iE; i++) {
-            /* the reference divides only the last v term by 4 */
-            t = F(v, i, j) + F(v, i + 1, j) + F(v, i, j - 1) + F(v, i + 1, j - 1) / 4.0;
-            unorm = sqrt(F(u, i, j) * F(u, i, j) + t * t);
-            unrm1 = 0.0;
-            if (unorm > 1.0e-8) unrm1 = (F(u, i, j) * F(u, i, j)) / unorm;
-            if (njacob == 1) unorm = unrm1 + unorm;
-            F(cp, i, j) = porc1 + porc2 * unorm;
-          }
-      } else if (ncomp == 2) {
-        for (int j = jS; j <= jN; j++)
-          for (int i = iW + 1; i <= iE; i++) {
-            t = (F(u, i - 1, j + 1) + F(u, i, j + 1) + F(u, i - 1, j) + F(u, i, j)) / 4.0;
-            unorm = sqrt(t * t + F(v, i, j) * F(v, i, j));
-            unrm1 = 0.0;
-            if (unorm > 1.0e-8) unrm1 = (F(v, i, j) * F(v, i, j)) / unorm;
-            if (njacob == 1) unorm = unrm1 + unorm;
-            F(cp, i, j) = porc1 + porc2 * unorm;
-          }
-      } else {
-        die("Error: Wrong ncomp flag passed to PorosCoef", ncomp, 0);
-      }
-    }
-}
-
-/* Porosity division of convective coefficients, momentum.f:296-324 (X) and
- * 621-649 (Y). */
-static void poros_scale(w2o_ctx *c, const w2o_regions *r, w2o_mom_ws *w,
-                        int yflag) {
-  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
-    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
-      if (RTYP(r, ireg, jreg) != RM_POROUS) continue;
-      int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
-      int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
-      double por = RPAR(dPRporos, r, ireg, jreg);
-      int j0 = yflag ? jS : jS + 1, i0 = yflag ? iW + 1 : iW;
-      for (int j = j0; j <= jN; j++)
-        for (int i = i0; i <= iE; i++) {
-          F(w->cj1, i, j) = F(w->cj1, i, j) / por;
-          F(w->cj2, i, j) = F(w->cj2, i, j) / por;
-          F(w->c1s, i, j) = F(w->c1s, i, j) / por;
-          F(w->c2s, i, j) = F(w->c2s, i, j) / por;
-          F(w->c1n, i, j) = F(w->c1n, i, j) / por;
-          F(w->c2n, i, j) = F(w->c2n, i, j) / por;
-        }
-    }
-}
-
-#define CA(k, ind) w->a[((k)-1) + 3 * (size_t)((ind)-1)]
-#define CB(ind) w->b[(ind)-1]
-
-static void set_identity_row(w2o_mom_ws *w, int ind) {
-  CA(1, ind) = 0.0; CA(2, ind) = 1.0; CA(3, ind) = 0.0; CB(ind) = 0.0;
-}
-
-/* XMomentum, momentum.f:199-514 */
-static void x_momentum(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
-                       double dk, double re, const w2o_metrics *m,
-                       const double *us, const double *vs, const double *un,
-                       const double *vn, double *dus) {
-  w2o_mom_ws *w = &c->wx;
-  int i, j, ind;
-  double re1 = 1.0 / re, dk2 = dk * 0.5, rkj;
-
-  conv_coef(c, nx, ny, 4, 1, m->xzu, m->xeu, m->yzu, m->yeu, us, vs, w->cj1, w->cj2);
-  conv_coef(c, nx, ny, 1, 0, m->xzn, m->xec, m->yzn, m->yec, us, vs, w->c1s, w->c2s);
-  conv_coef(c, nx, ny, 1, 0, m->xzn, m->xec, m->yzn, m->yec, un, vn, w->c1n, w->c2n);
-  poros_scale(c, r, w, 0);
-
-  dconv_u(c, nx, ny, w->c1s, w->c2s, us, w->cnvs);
-  dconv_u(c, nx, ny, w->c1n, w->c2n, un, w->cnvn);
-  ddiff_u(c, nx, ny, m->rac, m->rbc, m->rbn, m->rgn, us, w->difs);
-  ddiff_u(c, nx, ny, m->rac, m->rbc, m->rbn, m->rgn, un, w->difn);
-
-  poros_coef(c, nx, ny, 1, 1, r, us, vs, w->cpj);
-  poros_coef(c, nx, ny, 1, 0, r, us, vs, w->cps);
-  poros_coef(c, nx, ny, 1, 0, r, un, vn, w->cpn);
-
-  /* First split step, momentum.f:350-384 */
-  for (j = 2; j <= ny; j++)
-    for (i = 1; i <= nx; i++) {
-      ind = (j - 2) * nx + i;
-      rkj = dk2 * F(m->dju, i, j);
-      if (F(w->cj1, i, j) >= 0.0) {
-        CA(1, ind) = rkj * (-F(w->cj1, i - 1, j) - re1 * F(m->rac, i, j));
-        CA(2, ind) = 1.0 + rkj * (F(w->cj1, i, j) +
-                                  re1 * (F(m->rac, i + 1, j) + F(m->rac, i, j))) +
-                     dk2 * F(w->cpj, i, j);
-        CA(3, ind) = rkj * (-re1 * F(m->rac, i + 1, j));
-      } else {
-        CA(1, ind) = rkj * (-re1 * F(m->rac, i, j));
-        CA(2, ind) = 1.0 + rkj * (-F(w->cj1, i, j) +
-                                  re1 * (F(m->rac, i + 1, j) + F(m->rac, i, j))) +
-                     dk2 * F(w->cpj, i, j);
-        CA(3, ind) = rkj * (F(w->cj1, i + 1, j) - re1 * F(m->rac, i + 1, j));
-      }
-      CB(ind) = F(un, i, j) - F(us, i, j) +
-                rkj * (-F(w->cnvs, i, j) - F(w->cnvn, i, j)) +
-                rkj * re1 * (F(w->difs, i, j) + F(w->difn, i, j)) -
-                dk2 * (F(w->cps, i, j) * F(us, i, j) + F(w->cpn, i, j) * F(un, i, j));
-    }
-  w2o_alt_trid_lu(nx * (ny - 1), w->a, w->b);
-
-  /* Second split step, momentum.f:396-428 */
-  for (j = 2; j <= ny; j++)
-    for (i = 1; i <= nx; i++) {
-      ind = (j - 2) * nx + i;
-      rkj = dk2 * F(m->dju, i, j);
-      if (F(w->cj2, i, j) >= 0.0) {
-        CA(1, ind) = rkj * (-F(w->cj2, i, j - 1) - re1 * F(m->rgn, i, j - 1));
-        CA(2, ind) = 1.0 + rkj * (F(w->cj2, i, j) +
-                                  re1 * (F(m->rgn, i, j) + F(m->rgn, i, j - 1))) +
-                     dk2 * F(w->cpj, i, j);
-        CA(3, ind) = rkj * (-re1 * F(m->rgn, i, j));
-      } else {
-        CA(1, ind) = rkj * (-re1 * F(m->rgn, i, j - 1));
-        CA(2, ind) = 1.0 + rkj * (-F(w->cj2, i, j) +
-                                  re1 * (F(m->rgn, i, j) + F(m->rgn, i, j - 1))) +
-                     dk2 * F(w->cpj, i, j);
-        CA(3, ind) = rkj * (F(w->cj2, i, j + 1) - re1 * F(m->rgn, i, j));
-      }
-    }
-
-  /* Blockage and W/E boundary identity rows, momentum.f:434-496 */
-  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
-    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
-      int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
-      int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
-      if (RTYP(r, ireg, jreg) == RM_BLOCKG)
-        for (j = jS + 1; j <= jN; j++)
-          for (i = iW; i <= iE; i++) set_identity_row(w, (j - 2) * nx + i);
-      switch (MBTP(r, ireg, jreg, WEST)) {
-        case BM_INTERN: case BM_OUTLT1: case BM_OUTLT2: break;
-        case BM_WALL1: case BM_WALL2: case BM_INLET:
-          for (j = jS + 1; j <= jN; j++) set_identity_row(w, (j - 2) * nx + iW);
-          break;
-        default: die("Wrong nBdTypeW flag", ireg, jreg);
-      }
-      switch (MBTP(r, ireg, jreg, EAST)) {
-        case BM_INTERN: case BM_OUTLT1: case BM_OUTLT2: break;
-        case BM_WALL1: case BM_WALL2: case BM_INLET:
-          for (j = jS + 1; j <= jN; j++) set_identity_row(w, (j - 2) * nx + iE);
-          break;
-        default: die("Wrong nBdTypeE flag", ireg, jreg);
-      }
-    }
-  w2o_alt_trid_lu(nx * (ny - 1), w->a, w->b);
-
-  for (j = 2; j <= ny; j++)
-    for (i = 1; i <= nx; i++) F(dus, i, j) = CB((j - 2) * nx + i);
-}
-
-/* YMomentum, momentum.f:520-838 */
-static void y_momentum(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
-                       double dk, double re, double fr, const w2o_metrics *m,
-                       const double *d, const double *dn, const double *us,
-                       const double *vs, const double *un, const double *vn,
-                       double *dvs) {
-  w2o_mom_ws *w = &c->wy;
-  int i, j, ind;
-  double re1 = 1.0 / re, dk2 = dk * 0.5, fr1 = 1.0 / fr, rkj, buoy;
-  (void)fr1;
-
-  conv_coef(c, nx, ny, 5, 1, m->xzv, m->xev, m->yzv, m->yev, us, vs, w->cj1, w->cj2);
-  conv_coef(c, nx, ny, 2, 0, m->xzc, m->xen, m->yzc, m->yen, us, vs, w->c1s, w->c2s);
-  conv_coef(c, nx, ny, 2, 0, m->xzc, m->xen, m->yzc, m->yen, un, vn, w->c1n, w->c2n);
-  poros_scale(c, r, w, 1);
-
-  dconv_v(c, nx, ny, w->c1s, w->c2s, vs, w->cnvs);
-  dconv_v(c, nx, ny, w->c1n, w->c2n, vn, w->cnvn);
-  ddiff_v(c, nx, ny, m->ran, m->rbc, m->rbn, m->rgc, vs, w->difs);
-  ddiff_v(c, nx, ny, m->ran, m->rbc, m->rbn, m->rgc, vn, w->difn);
-
-  poros_coef(c, nx, ny, 2, 1, r, us, vs, w->cpj);
-  poros_coef(c, nx, ny, 2, 0, r, us, vs, w->cps);
-  poros_coef(c, nx, ny, 2, 0, r, un, vn, w->cpn);
-
-  /* First split step, momentum.f:675-711 */
-  for (j = 1; j <= ny; j++)
-    for (i = 2; i <= nx; i++) {
-      ind = (j - 1) * (nx - 1) + i - 1;
-      rkj = dk2 * F(m->djv, i, j);
-      if (F(w->cj1, i, j) >= 0.0) {
-        CA(1, ind) = rkj * (-F(w->cj1, i - 1, j) - re1 * F(m->ran, i - 1, j));
-        CA(2, ind) = rkj * (F(w->cj1, i, j) +
-                            re1 * (F(m->ran, i, j) + F(m->ran, i - 1, j))) +
-                     dk2 * F(w->cpj, i, j) + 1.0;
-        CA(3, ind) = rkj * (-re1 * F(m->ran, i, j));
-      } else {
-        CA(1, ind) = rkj * (-re1 * F(m->ran, i - 1, j));
-        CA(2, ind) = rkj * (-F(w->cj1, i, j) +
-                            re1 * (F(m->ran, i, j) + F(m->ran, i - 1, j))) +
-                     dk2 * F(w->cpj, i, j) + 1.0;
-        CA(3, ind) = rkj * (F(w->cj1, i + 1, j) - re1 * F(m->ran, i, j));
-      }
-      buoy = dk * (F(d, i, j + 1) + F(d, i, j) + F(dn, i, j + 1) + F(dn, i, j)) /
-             (4.0 * fr);
-      CB(ind) = F(vn, i, j) - F(vs, i, j) +
-                rkj * (-F(w->cnvs, i, j) - F(w->cnvn, i, j)) +
-                rkj * re1 * (F(w->difs, i, j) + F(w->difn, i, j)) -
-                dk2 * (F(w->cps, i, j) * F(vs, i, j) + F(w->cpn, i, j) * F(vn, i, j)) -
-                buoy;
-    }
-  w2o_alt_trid_lu((nx - 1) * ny, w->a, w->b);
-
-  /* Second split step, momentum.f:723-754 */
-  for (j = 1; j <= ny; j++)
-    for (i = 2; i <= nx; i++) {
-      ind = (j - 1) * (nx - 1) + i - 1;
-      rkj = dk2 * F(m->djv, i, j);
-      if (F(w->cj2, i, j) >= 0.0) {
-        CA(1, ind) = rkj * (-F(w->cj2, i, j - 1) - re1 * F(m->rgc, i, j));
-        CA(2, ind) = rkj * (F(w->cj2, i, j) +
-                            re1 * (F(m->rgc, i, j + 1) + F(m->rgc, i, j))) +
-                     dk2 * F(w->cpj, i, j) + 1.0;
-        CA(3, ind) = rkj * (-re1 * F(m->rgc, i, j + 1));
-      } else {
-        CA(1, ind) = rkj * (-re1 * F(m->rgc, i, j));
-        CA(2, ind) = rkj * (-F(w->cj2, i, j) +
-                            re1 * (F(m->rgc, i, j + 1) + F(m->rgc, i, j))) +
-                     dk2 * F(w->cpj, i, j) + 1.0;
-        CA(3, ind) = rkj * (F(w->cj2, i, j + 1) - re1 * F(m->rgc, i, j + 1));
-      }
-    }
-
-  /* Blockage and S/N boundary identity rows, momentum.f:760-821 */
-  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
-    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
-      int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
-      int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
-      if (RTYP(r, ireg, jreg) == RM_BLOCKG)
-        for (j = jS; j <= jN; j++)
-          for (i = iW + 1; i <= iE; i++) set_identity_row(w, (j - 1) * (nx - 1) + i - 1);
-      switch (MBTP(r, ireg, jreg, SOUTH)) {
-        case BM_INTERN: case BM_OUTLT1: case BM_OUTLT2: break;
-        case BM_WALL1: case BM_WALL2: case BM_INLET:
-          for (i = iW + 1; i <= iE; i++) set_identity_row(w, (jS - 1) * (nx - 1) + i - 1);
-          break;
-        default: die("Wrong nBdTypeS flag", ireg, jreg);
-      }
-      switch (MBTP(r, ireg, jreg, NORTH)) {
-        case BM_INTERN: case BM_OUTLT1: case BM_OUTLT2: break;
-        case BM_WALL1: case BM_WALL2: case BM_INLET:
-          for (i = iW + 1; i <= iE; i++) set_identity_row(w, (jN - 1) * (nx - 1) + i - 1);
-          break;
-        default: die("Wrong nBdTypeN flag", ireg, jreg);
-      }
-    }
-  w2o_alt_trid_lu((nx - 1) * ny, w->a, w->b);
-
-  for (j = 1; j <= ny; j++)
-    for (i = 2; i <= nx; i++) F(dvs, i, j) = CB((j - 1) * (nx - 1) + i - 1);
-}
-#undef CA
-#undef CB
-
-/* DMaxNorm, utility.f:479-507 */
-double w2o_dmax_norm(w2o_ctx *c, int nx, int ny, const double *u) {
-  double diff = fabs(F(u, 5, 5));
-  for (int j = 2; j <= ny - 1; j++)
-    for (int i = 2; i <= nx - 1; i++) {
-      double a = fabs(F(u, i, j));
-      if (a > diff) diff = a;
-    }
-  return diff;
-}
-
 /* DiffMaxNorm, utility.f:446-473 */
 double w2o_diff_max_norm(w2o_ctx *c, int nx, int ny, const double *un,
                          const double *u) {
@@ -675,39 +281,55 @@ double w2o_diff_max_norm(w2o_ctx *c, int nx, int ny, const double *un,
   return diff;
 }
 
-/* nAuxMomentum, momentum.f:33-193 */
-int w2o_naux_momentum(w2o_ctx *c, int nx, int ny, int mqiter,
-                      const w2o_regions *r, double dk, double re, double fr,
-                      double qtol, const w2o_metrics *m, const double *d,
-                      const double *dn, const double *un, const double *vn,
-                      double *us, double *vs) {
-  int i, j, mm;
-  for (j = 1; j <= ny + 1; j++)
-    for (i = 1; i <= nx + 1; i++) {
-      F(us, i, j) = F(un, i, j);
-      F(vs, i, j) = F(vn, i, j);
-    }
-  for (mm = 1; mm <= mqiter; mm++) {
-    w2o_vel_outflow_bcs(c, nx, ny, r, us, vs);
-    for (j = 0; j <= ny + 1; j++)
-      for (i = 0; i <= nx + 1; i++) {
-        F(c->dus, i, j) = 0.0;
-        F(c->dvs, i, j) = 0.0;
-      }
-    x_momentum(c, nx, ny, r, dk, re, m, us, vs, un, vn, c->dus);
-    y_momentum(c, nx, ny, r, dk, re, fr, m, d, dn, us, vs, un, vn, c->dvs);
-    for (j = 1; j <= ny; j++)
-      for (i = 1; i <= nx; i++) {
-        F(us, i, j) = F(us, i, j) + F(c->dus, i, j);
-        F(vs, i, j) = F(vs, i, j) + F(c->dvs, i, j);
-      }
-    double d1 = w2o_dmax_norm(c, nx, ny, c->dus);
-    double d2 = w2o_dmax_norm(c, nx, ny, c->dvs);
-    double difmax = d1 > d2 ? d1 : d2;
-    if (difmax <= qtol) return mm;
-  }
-  return -1;
-}
+/* nAuxMomentum and its helpers in FP64 (the reference's precision) and in
+ * FP32 (the checker of the GPU's single-precision momentum). */
+#define REAL double
+#define R(x) ((double)(x))
+#define FN(x) x
+#define RABS fabs
+#define RSQRT sqrt
+#define MOMWS w2o_mom_ws
+#define METRICS w2o_metrics
+#define MOM_WX wx
+#define MOM_WY wy
+#define MOM_DUS dus
+#define MOM_DVS dvs
+#include "momentum_impl.h"
+#undef REAL
+#undef R
+#undef FN
+#undef RABS
+#undef RSQRT
+#undef MOMWS
+#undef METRICS
+#undef MOM_WX
+#undef MOM_WY
+#undef MOM_DUS
+#undef MOM_DVS
+
+#define REAL float
+#define R(x) ((float)(x))
+#define FN(x) x##_f32
+#define RABS fabsf
+#define RSQRT sqrtf
+#define MOMWS w2o_mom_ws32
+#define METRICS w2o_metrics32
+#define MOM_WX wx32
+#define MOM_WY wy32
+#define MOM_DUS dus32
+#define MOM_DVS dvs32
+#include "momentum_impl.h"
+#undef REAL
+#undef R
+#undef FN
+#undef RABS
+#undef RSQRT
+#undef MOMWS
+#undef METRICS
+#undef MOM_WX
+#undef MOM_WY
+#undef MOM_DUS
+#undef MOM_DVS
 
 /* ------------------------------------------------------------------ */
 /* pressure.f                                                          */
@@ -1295,78 +917,6 @@ void w2o_pres_bound_cond(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
       } else if (t == BM_OUTLT1 || t == BM_OUTLT2) {
         for (i = iW + 1; i <= iE; i++) F(p, i, jN + 1) = 2.0 * BCV(r, ireg, jreg, NORTH, VP) - F(p, i, jN);
       } else if (t != BM_INTERN) die("Wrong nBdTypeN flag", ireg, jreg);
-    }
-}
-
-/* VelOutflowBCs, bound_cond.f:1656-1874 */
-void w2o_vel_outflow_bcs(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
-                         double *u, double *v) {
-  (void)nx; (void)ny;
-  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
-    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
-      int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
-      int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
-      int i, j;
-      switch (MBTP(r, ireg, jreg, WEST)) {
-        case BM_INTERN: case BM_WALL1: case BM_WALL2: case BM_INLET: break;
-        case BM_OUTLT1:
-          for (j = jS; j <= jN; j++) F(u, iW - 1, j) = BCV(r, ireg, jreg, WEST, VU) + F(u, iW, j);
-          for (j = jS + 1; j <= jN; j++) F(v, iW, j) = -F(v, iW + 1, j);
-          break;
-        case BM_OUTLT2:
-          for (j = jS + 1; j <= jN; j++)
-            F(u, iW, j) = F(u, iW + 1, j) - F(v, iW + 1, j) + F(v, iW + 1, j - 1);
-          for (j = jS + 1; j <= jN; j++)
-            F(v, iW, j) = -F(v, iW, j - 1) + 5.0 * (F(v, iW + 1, j) - F(v, iW + 1, j - 1)) +
-                          8.0 * (F(u, iW + 1, j) - F(u, iW, j));
-          break;
-        default: die("Wrong nBdTypeW flag", ireg, jreg);
-      }
-      switch (MBTP(r, ireg, jreg, EAST)) {
-        case BM_INTERN: case BM_WALL1: case BM_WALL2: case BM_INLET: break;
-        case BM_OUTLT1:
-          for (j = jS; j <= jN; j++) F(u, iE + 1, j) = BCV(r, ireg, jreg, EAST, VU) + F(u, iE, j);
-          for (j = jS + 1; j <= jN; j++) F(v, iE + 1, j) = -F(v, iE, j);
-          break;
-        case BM_OUTLT2:
-          for (j = jS + 1; j <= jN; j++)
-            F(u, iE, j) = F(u, iE - 1, j) - (F(v, iE, j) - F(v, iE, j - 1));
-          for (j = jS + 1; j <= jN - 1; j++)
-            F(v, iE + 1, j) = F(v, iE + 1, j - 1) + 3.0 * (F(v, iE, j - 1) - F(v, iE, j)) -
-                              4.0 * (F(u, iE, j) - F(u, iE - 1, j));
-          break;
-        default: die("Wrong nBdTypeE flag", ireg, jreg);
-      }
-      switch (MBTP(r, ireg, jreg, SOUTH)) {
-        case BM_INTERN: case BM_WALL1: case BM_WALL2: case BM_INLET: break;
-        case BM_OUTLT1:
-          for (i = iW + 1; i <= iE; i++) F(u, i, jS) = -F(u, i, jS + 1);
-          for (i = iW; i <= iE; i++) F(v, i, jS) = BCV(r, ireg, jreg, SOUTH, VV) + F(v, i, jS);
-          break;
-        case BM_OUTLT2:
-          for (i = iW + 1; i <= iE; i++)
-            F(v, i, jS) = F(v, i, jS + 1) + (F(u, i, jS + 1) - F(u, i - 1, jS + 1));
-          for (i = iW + 1; i <= iE - 1; i++)
-            F(u, i, jS) = F(u, i - 1, jS) + 3.0 * (F(u, i - 1, jS + 1) - F(u, i, jS + 1)) -
-                          4.0 * (F(v, i, jS + 1) - F(v, i, jS));
-          break;
-        default: die("Wrong nBdTypeS flag", ireg, jreg);
-      }
-      switch (MBTP(r, ireg, jreg, NORTH)) {
-        case BM_INTERN: case BM_WALL1: case BM_WALL2: case BM_INLET: break;
-        case BM_OUTLT1:
-          for (i = iW + 1; i <= iE; i++) F(u, i, jN + 1) = -F(u, i, jN);
-          for (i = iW; i <= iE; i++) F(v, i, jN + 1) = BCV(r, ireg, jreg, NORTH, VV) + F(v, i, jN);
-          break;
-        case BM_OUTLT2:
-          for (i = iW; i <= iE; i++)
-            F(v, i, jN) = F(v, i, jN - 1) - (F(u, i, jN) - F(u, i - 1, jN));
-          for (i = iW + 1; i <= iE - 1; i++)
-            F(u, i, jN + 1) = F(u, i - 1, jN + 1) + 3.0 * (F(u, i - 1, jN) - F(u, i, jN)) -
-                              4.0 * (F(v, i, jN) - F(v, i, jN - 1));
-          break;
-        default: die("Wrong nBdTypeN flag", ireg, jreg);
-      }
     }
 }
 

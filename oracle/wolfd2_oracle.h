@@ -60,6 +60,14 @@ typedef struct {
   double *xeu, *yeu, *xzv, *yzv, *xzu, *yzu, *xev, *yev;
 } w2o_metrics;
 
+/* The metric arrays rounded to single precision (the FP32 momentum's input). */
+typedef struct {
+  float *ran, *rbn, *rgn, *rac, *rbc, *rgc, *rau, *rbu, *rbv, *rgv;
+  float *dju, *djv, *djc, *djn;
+  float *xen, *yen, *xzn, *yzn, *xec, *yec, *xzc, *yzc;
+  float *xeu, *yeu, *xzv, *yzv, *xzu, *yzu, *xev, *yev;
+} w2o_metrics32;
+
 w2o_ctx *w2o_create(int mnx, int mny);
 void w2o_destroy(w2o_ctx *c);
 
@@ -74,6 +82,17 @@ int w2o_naux_momentum(w2o_ctx *c, int nx, int ny, int mqiter,
                       double qtol, const w2o_metrics *m, const double *d,
                       const double *dn, const double *un, const double *vn,
                       double *us, double *vs);
+
+/* nAuxMomentum in single precision: every operation of w2o_naux_momentum in
+ * IEEE single (FP32 fields and metrics, literals and dk, re, fr rounded to
+ * single); the stopping test compares against qtol in double. */
+int w2o_naux_momentum_f32(w2o_ctx *c, int nx, int ny, int mqiter,
+                          const w2o_regions *r, double dk, double re,
+                          double fr, double qtol, const w2o_metrics32 *m,
+                          const float *d, const float *dn, const float *un,
+                          const float *vn, float *us, float *vs);
+void w2o_vel_outflow_bcs_f32(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                             float *u, float *v);
 
 /* pressure.f:30-249; returns nSorConv */
 int w2o_ppe(w2o_ctx *c, int nx, int ny, const w2o_regions *r,

@@ -17,7 +17,7 @@ from wolfd2_gb300.gpu import PREC_MIXED, Solver, W2Error
 pytestmark = pytest.mark.gpu
 
 P_REL_TOL = 1e-8    # one Ppe call, mixed vs FP64 oracle
-UVP_REL_TOL = 1e-7  # a few time steps, mixed vs FP64 oracle
+UVP_REL_TOL = 1e-6  # a few time steps (FP32 momentum), mixed vs FP64 oracle
 
 
 def _rel(a, b):
@@ -36,7 +36,7 @@ def _inputs(case, seed, amp=0.05):
 
 @pytest.mark.parametrize("sortol,msorit", [(1e-8, 301), (1e-8, 300), (2e-6, 2000), (7e-7, 2000),
                                            (3e-7, 2000)])
-@pytest.mark.parametrize("K,threads", [(4, 512), (2, 256), (8, 1024)])
+@pytest.mark.parametrize("K,threads", [(8, 512), (4, 256), (8, 128)])
 def test_mixed_ppe_matches_model(sortol, msorit, K, threads):
     """Drop-in Ppe in mixed mode: bit-identical to the model for stopping
     points on every sweep of a group and for odd/even msorit."""
@@ -139,7 +139,7 @@ def test_mixed_rejects_unsupported():
     with pytest.raises(W2Error):
         s.step(case.params, 1, precision=PREC_MIXED)  # lexicographic SOR
     with pytest.raises(W2Error):
-        s.tune_mixed(3, 0)
+        s.tune_mixed(2, 0)
     odd = deck.cavity(48, 100.0, 0.005, solver="rb_sor")  # h = 1/48: not the unit stencil
     s2 = Solver.for_case(odd)
     z = s2.field()

@@ -51,12 +51,16 @@ struct w2_ctx {
   TileGeom tg{};
   int use_tiled = 1;
   // mixed-precision Poisson sweeps
-  float *e32[2] = {};
+  float *xbuf = nullptr;  // two exchange buffers of 2 colour planes each
+  size_t xbuf_floats = 0;
   bool mixed_ok = false;
-  int mixed_K = 4, mixed_threads = 512;
+  int mixed_K = 8, mixed_threads = kMixedThreads;
   size_t mixed_smem = 0;
   MixedGeom mg{};
   int prec_dropin = W2_PREC_FP64, refine_dropin = 0;
+  // single-precision momentum state (mixed path), made on first use
+  bool f32_alloc = false, f32_metrics_ok = false;
+  float *F32[4] = {};  // un, vn, us, vs
 };
 
 namespace {
@@ -276,17 +280,23 @@ int check_sync(w2_ctx *c) {
 }
 
 // Chain buffers for a chain of n rows.
-int make_chain(w2_ctx *c, Chain &ch, int n, bool with_b) {
+template <class T>
+int make_chain(w2_ctx *c, ChainT<T> &ch, int n, bool with_b) {
   ch.n = n;
-  ch.a1 = dalloc<double>(c, n);
-  ch.a2 = dalloc<double>(c, n);
-  ch.a3 = dalloc<double>(c, n);
-  ch.b = with_b ? dalloc<double>(c, n) : nullptr;
-  ch.a3p = dalloc<double>(c, n);
-  ch.bp = dalloc<double>(c, n);
-  ch.x = dalloc<double>(c, n);
+  ch.a1 = dalloc<T>(c, n);
+  ch.a2 = dalloc<T>(c, n);
+  ch.a3 = dalloc<T>(c, n);
+  ch.b = with_b ? dalloc<T>(c, n) : nullptr;
+  ch.a3p = dalloc<T>(c, n);
+  ch.bp = dalloc<T>(c, n);
+  ch.x = dalloc<T>(c, n);
   ch.bzero = nullptr;
-  if (!ch.a1 || !ch.a2 || !ch.a3 || !ch.a3p || !ch.bp || !ch.x || (with_b && !ch.b))
+  // end-state buffers, sized for the smallest segment length allowed (8)
+  const int ms = (n + 7) / 8;
+  ch.ef = dalloc<T>(c, (size_t)4 * ms);
+  ch.eb = dalloc<T>(c, (size_t)2 * ms);
+  if (!ch.a1 || !ch.a2 || !ch.a3 || !ch.a3p || !ch.bp || !ch.x || (with_b && !ch.b) || !ch.ef ||
+      !ch.eb)
     return fail(c, W2_E_CUDA, "out of device memory (chains)");
   return W2_OK;
 }
@@ -304,6 +314,8 @@ int set_segments(w2_ctx *c) {
     ch.nseg = (n + seg - 1) / seg;
   };
   setn(d.x1, nX); setn(d.x2, nX); setn(d.y1, nY); setn(d.y2, nY);
+  d.f32.x1.nseg = d.x1.nseg; d.f32.x2.nseg = d.x2.nseg;
+  d.f32.y1.nseg = d.y1.nseg; d.f32.y2.nseg = d.y2.nseg;
   // end-state buffers, sized for the smallest segment length we allow (8)
   return W2_OK;
 }
@@ -415,11 +427,62 @@ int launch_ppe_tiled(w2_ctx *c, int lcartes, int msorit, double dk, double sorto
   return W2_OK;
 }
 
+// ---- single-precision momentum state -----------------------------------------
+
+int grid_blocks(w2_ctx *c);
+
+// FP32 copies of the metric arrays the momentum stencils read, FP32 work
+// arrays and chains (the split-2 identity rows shared with the FP64 chains)
+// and the FP32 fields; allocated on the first mixed step, the metrics
+// re-rounded whenever new ones are uploaded.
+int ensure_f32(w2_ctx *c) {
+  Dev &d = c->dev;
+  MomView<float> &v = d.f32;
+  const Metrics &m = d.m;
+  const double *src[] = {m.yeu, m.xeu, m.xzu, m.yzu, m.yec, m.xec, m.xzn, m.yzn,
+                         m.yev, m.xev, m.xzv, m.yzv, m.yen, m.xen, m.xzc, m.yzc,
+                         m.dju, m.djv, m.rac, m.rbc, m.rbn, m.rgn, m.ran, m.rgc};
+  const float **dst[] = {&v.yeu, &v.xeu, &v.xzu, &v.yzu, &v.yec, &v.xec, &v.xzn, &v.yzn,
+                         &v.yev, &v.xev, &v.xzv, &v.yzv, &v.yen, &v.xen, &v.xzc, &v.yzc,
+                         &v.dju, &v.djv, &v.rac, &v.rbc, &v.rbn, &v.rgn, &v.ran, &v.rgc};
+  if (!c->f32_alloc) {
+    for (const float **p : dst)
+      if (!(*p = dalloc<float>(c, c->nf))) return fail(c, W2_E_CUDA, "out of device memory (FP32 metrics)");
+    float **wa[] = {&v.cj1x, &v.cj2x, &v.c1sx, &v.c2sx, &v.c1nx, &v.c2nx,
+                    &v.cj1y, &v.cj2y, &v.c1sy, &v.c2sy, &v.c1ny, &v.c2ny};
+    for (float **p : wa)
+      if (!(*p = dalloc<float>(c, c->nf))) return fail(c, W2_E_CUDA, "out of device memory (FP32 work)");
+    for (int k = 0; k < 4; ++k)
+      if (!(c->F32[k] = dalloc<float>(c, c->nf))) return fail(c, W2_E_CUDA, "out of device memory (FP32 fields)");
+    const int nX = c->nx * (c->ny - 1), nY = (c->nx - 1) * c->ny;
+    int rc;
+    if ((rc = make_chain(c, v.x1, nX, true)) || (rc = make_chain(c, v.x2, nX, false)) ||
+        (rc = make_chain(c, v.y1, nY, true)) || (rc = make_chain(c, v.y2, nY, false)))
+      return rc;
+    v.x2.b = v.x1.x;
+    v.y2.b = v.y1.x;
+    v.x2.bzero = d.x2.bzero;
+    v.y2.bzero = d.y2.bzero;
+    v.x1.nseg = d.x1.nseg; v.x2.nseg = d.x2.nseg;
+    v.y1.nseg = d.y1.nseg; v.y2.nseg = d.y2.nseg;
+    c->f32_alloc = true;
+  }
+  if (!c->f32_metrics_ok) {
+    const int gb = grid_blocks(c);
+    for (int k = 0; k < 24; ++k) {
+      k_to_f32<<<gb, c->threads, 0, c->st>>>(d, src[k], const_cast<float *>(*dst[k]));
+      c->launches++;
+    }
+    CK(cudaGetLastError());
+    c->f32_metrics_ok = true;
+  }
+  return W2_OK;
+}
+
 // ---- mixed-precision Poisson sweeps ----------------------------------------
 
 const void *mixed_kernel(int K) {
   switch (K) {
-    case 2: return (const void *)k_ppe_mixed<2>;
     case 4: return (const void *)k_ppe_mixed<4>;
     case 8: return (const void *)k_ppe_mixed<8>;
   }
@@ -427,11 +490,12 @@ const void *mixed_kernel(int K) {
 }
 
 // One tile per block (one block per SM): the split of the unknowns into at
-// most nsm tiles, tx even, whose largest tile sweeps the least area per
-// group of K sweeps, within the shared-memory limit.
+// most nsm tiles, tx a multiple of 8, whose largest tile sweeps the least
+// area per group of K sweeps, within the shared-memory limit and at most
+// kMixedPmax box positions per thread.
 void plan_mixed(w2_ctx *c) {
   c->mixed_ok = false;
-  const int K = c->mixed_K;
+  const int K = c->mixed_K, T = c->mixed_threads;
   const void *kf = mixed_kernel(K);
   if (!kf) return;
   int maxsmem = 0;
@@ -445,26 +509,42 @@ void plan_mixed(w2_ctx *c) {
   double best = 1e300;
   for (int ntx = 1; ntx <= std::max(1, NX / 8); ++ntx) {
     int tx = (NX + ntx - 1) / ntx;
-    tx += tx & 1;
+    tx = (tx + 7) / 8 * 8;
     if ((NX + tx - 1) / tx != ntx) continue;
-    for (int nty = 1; nty <= std::max(1, NY / 8) && ntx * nty <= c->nsm; ++nty) {
+    for (int nty = 1; nty <= std::max(1, NY / 4) && ntx * nty <= c->nsm; ++nty) {
       const int ty = (NY + nty - 1) / nty;
       if ((NY + ty - 1) / ty != nty) continue;
       const size_t smem = mixed_smem_bytes(K, tx, ty);
       if (smem > limit) continue;
+      const int bw = tx + 2 * H, bh = ty + 2 * H;
+      const int P = ((bh - 2) * (bw / 2 - 1) + T - 1) / T;
+      if (P > kMixedPmax || (size_t)bh * (bw / 2) > 65535) continue;
       double area = 0.0;
       for (int e = H - 1; e >= 0; --e) area += (double)(tx + 2 * e) * (ty + 2 * e);
       if (area < best) {
         best = area;
-        c->mg = MixedGeom{tx, ty, ntx, nty};
+        c->mg = MixedGeom{tx, ty, ntx, nty, ntx * tx / 2 + H, nty * ty + 2 * H, P};
         c->mixed_smem = smem;
       }
     }
   }
   if (best >= 1e300) return;
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kf, c->mixed_threads, c->mixed_smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kf, T, c->mixed_smem);
   if (occ < 1) return;
+  // exchange buffers: zero wherever no tile writes (cells off the unknowns)
+  const size_t need = 4 * (size_t)c->mg.gh * c->mg.gw;
+  if (need > c->xbuf_floats) {
+    if (c->xbuf) {
+      cudaFree(c->xbuf);
+      c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void *)c->xbuf), c->allocs.end());
+      c->xbuf = nullptr;
+      c->xbuf_floats = 0;
+    }
+    if (!(c->xbuf = dalloc<float>(c, need))) return;
+    c->xbuf_floats = need;
+  }
+  if (cudaMemset(c->xbuf, 0, c->xbuf_floats * sizeof(float)) != cudaSuccess) return;
   c->mixed_ok = true;
 }
 
@@ -488,8 +568,9 @@ int launch_ppe_mixed(w2_ctx *c, int lcartes, int msorit, double dk, double sorto
                      int inner, const double *u, const double *v, double *p, StepOut *out) {
   Dev d = c->dev;
   MixedGeom g = c->mg;
+  float *xb1 = c->xbuf + 2 * (size_t)c->mg.gh * c->mg.gw;
   MixedArgs a{lcartes, msorit, auto_inner(c, inner), dk, sortol, (float)sorrel, u, v, p,
-              c->e32[0], c->e32[1]};
+              c->xbuf, xb1};
   void *args[] = {&d, &g, &a, &out};
   c->launches++;
   cudaError_t e = cudaLaunchCooperativeKernel(mixed_kernel(c->mixed_K), dim3(c->nsm),
@@ -593,8 +674,6 @@ int wolfd2gpu_create(w2_ctx **out, int mnx, int mny, int mgri, int mgrj, int nx,
                    &d.pa5, &d.div, &d.pb, &d.ppn, &d.la3p, &d.lbp, &d.qh};
   for (double **w : wa)
     if (!(*w = dalloc<double>(c, c->nf))) return bad(W2_E_CUDA);
-  for (int k = 0; k < 2; ++k)
-    if (!(c->e32[k] = dalloc<float>(c, c->nf))) return bad(W2_E_CUDA);
   const int nX = nx * (ny - 1), nY = (nx - 1) * ny;
   if (make_chain(c, d.x1, nX, true) || make_chain(c, d.x2, nX, false) ||
       make_chain(c, d.y1, nY, true) || make_chain(c, d.y2, nY, false))
@@ -614,17 +693,6 @@ int wolfd2gpu_create(w2_ctx **out, int mnx, int mny, int mgri, int mgrj, int nx,
     cudaMemcpy(dzy, zy.data(), nY, cudaMemcpyHostToDevice);
     d.x2.bzero = dzx;
     d.y2.bzero = dzy;
-  }
-  // end-state buffers for the smallest allowed segment length (8)
-  {
-    const int maxsegX = (nX + 7) / 8, maxsegY = (nY + 7) / 8;
-    Chain *chs[] = {&d.x1, &d.x2, &d.y1, &d.y2};
-    for (Chain *ch : chs) {
-      int ms = ch->n == nX ? maxsegX : maxsegY;
-      ch->ef = dalloc<double>(c, (size_t)4 * ms);
-      ch->eb = dalloc<double>(c, (size_t)2 * ms);
-      if (!ch->ef || !ch->eb) return bad(W2_E_CUDA);
-    }
   }
   d.sync = dalloc<Sync>(c, 1);
   c->d_out = dalloc<StepOut>(c, 1);
@@ -739,9 +807,9 @@ int wolfd2gpu_set_precision(w2_ctx *c, int precision, int refine_sweeps) {
 int wolfd2gpu_tune_mixed(w2_ctx *c, int sweeps_per_barrier, int threads) {
   if (!c) return W2_E_ARG;
   if (sweeps_per_barrier != 0 && !mixed_kernel(sweeps_per_barrier))
-    return fail(c, W2_E_ARG, "sweeps per barrier must be 2, 4 or 8");
-  if (threads != 0 && (threads % 32 || threads < 64 || threads > 1024))
-    return fail(c, W2_E_ARG, "threads must be a multiple of 32 in 64..1024");
+    return fail(c, W2_E_ARG, "sweeps per barrier must be 4 or 8");
+  if (threads != 0 && (threads % 32 || threads < 64 || threads > kMixedThreads))
+    return fail(c, W2_E_ARG, "threads must be a multiple of 32 in 64..%d", kMixedThreads);
   if (sweeps_per_barrier) c->mixed_K = sweeps_per_barrier;
   if (threads) c->mixed_threads = threads;
   if (c->metrics_ok) plan_mixed(c);
@@ -761,6 +829,7 @@ int wolfd2gpu_set_metrics(w2_ctx *c, const double *const *metrics) {
   int rc = finish_coefficients(c);
   if (rc) return rc;
   c->metrics_ok = true;
+  c->f32_metrics_ok = false;
   return W2_OK;
 }
 
@@ -807,6 +876,7 @@ int wolfd2gpu_grid_metric(w2_ctx *c, const double *gx, const double *gy, double 
   rc = finish_coefficients(c);
   if (rc) return rc;
   c->metrics_ok = true;
+  c->f32_metrics_ok = false;
   return W2_OK;
 }
 
@@ -1034,14 +1104,31 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
     double *us = c->U[b], *vs = c->V[b], *p = c->P[b];
     StepOut *o = d_outs + s;
     Dev d = c->dev;
-    {
+    const bool mixed = prm->precision == W2_PREC_MIXED;
+    if (mixed) {
+      if ((rc = ensure_f32(c))) break;
+      d = c->dev;
+      float *un32 = c->F32[0], *vn32 = c->F32[1], *us32 = c->F32[2], *vs32 = c->F32[3];
+      {
+        ProfScope ps(c, W2_K_COPY);
+        c->launches++;
+        k_copy_mixed<<<gb, c->threads, 0, c->st>>>(d, p, pn, un, vn, un32, vn32, us32, vs32);
+        CK(cudaGetLastError());
+      }
+      int blocks = pick_blocks(c, (const void *)k_naux32, (long)c->nx * c->ny);
+      ProfScope ps(c, W2_K_MOMENTUM);
+      int mq = prm->mqiter;
+      double dk = prm->dk, re = prm->re, qtol = prm->qtol;
+      void *args[] = {&d, &mq, &dk, &re, &qtol, &un32, &vn32, &us32, &vs32, &us, &vs, &o};
+      if ((rc = coop(c, (const void *)k_naux32, blocks, args))) break;
+    } else {
       ProfScope ps(c, W2_K_COPY);
       c->launches++;
       k_copy3<<<gb, c->threads, 0, c->st>>>(d, us, un, vs, vn, p, pn);
       CK(cudaGetLastError());
     }
     // nAuxMomentum on (un, vn) -> (us, vs); us = un already (main.f:741-747)
-    {
+    if (!mixed) {
       int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny);
       ProfScope ps(c, W2_K_MOMENTUM);
       int mq = prm->mqiter;

@@ -192,7 +192,9 @@ __device__ bool vel_bound_cond_block(const Dev &d, double *u, double *v) {
 
 // VelOutflowBCs, bound_cond.f:1656-1874 (outlet faces only; note the west
 // mass-conservation u row has the opposite v signs to VelBoundCond's).
-__device__ bool vel_outflow_bcs_block(const Dev &d, double *u, double *v) {
+// T is double on the plain path and float on the mixed one.
+template <class T>
+__device__ bool vel_outflow_bcs_block(const Dev &d, T *u, T *v) {
   const Regions &r = d.r;
   for (int jreg = 1; jreg <= r.nrj; jreg++)
     for (int ireg = 1; ireg <= r.nri; ireg++) {
@@ -200,7 +202,7 @@ __device__ bool vel_outflow_bcs_block(const Dev &d, double *u, double *v) {
       const int jS = r.B(ireg, jreg, SOUTH), jN = r.B(ireg, jreg, NORTH);
       int t = r.BT(ireg, jreg, WEST);
       if (t == BM_OUTLT1) {
-        const double uw = r.BV(ireg, jreg, WEST, VAR_U);
+        const T uw = T(r.BV(ireg, jreg, WEST, VAR_U));
         W2_PFOR(j, jS, jN) UF(iW - 1, j) = uw + UF(iW, j);
         W2_SYNC();
         W2_PFOR(j, jS + 1, jN) VF(iW, j) = -VF(iW + 1, j);
@@ -209,15 +211,15 @@ __device__ bool vel_outflow_bcs_block(const Dev &d, double *u, double *v) {
         W2_PFOR(j, jS + 1, jN) UF(iW, j) = UF(iW + 1, j) - VF(iW + 1, j) + VF(iW + 1, j - 1);
         W2_SYNC();
         W2_SFOR(j, jS + 1, jN)
-        VF(iW, j) = -VF(iW, j - 1) + 5.0 * (VF(iW + 1, j) - VF(iW + 1, j - 1)) +
-                   8.0 * (UF(iW + 1, j) - UF(iW, j));
+        VF(iW, j) = -VF(iW, j - 1) + T(5.0) * (VF(iW + 1, j) - VF(iW + 1, j - 1)) +
+                   T(8.0) * (UF(iW + 1, j) - UF(iW, j));
         W2_SYNC();
       } else if (t < BM_INTERN || t > BM_OUTLT2) {
         return false;
       }
       t = r.BT(ireg, jreg, EAST);
       if (t == BM_OUTLT1) {
-        const double ue = r.BV(ireg, jreg, EAST, VAR_U);
+        const T ue = T(r.BV(ireg, jreg, EAST, VAR_U));
         W2_PFOR(j, jS, jN) UF(iE + 1, j) = ue + UF(iE, j);
         W2_SYNC();
         W2_PFOR(j, jS + 1, jN) VF(iE + 1, j) = -VF(iE, j);
@@ -226,15 +228,15 @@ __device__ bool vel_outflow_bcs_block(const Dev &d, double *u, double *v) {
         W2_PFOR(j, jS + 1, jN) UF(iE, j) = UF(iE - 1, j) - (VF(iE, j) - VF(iE, j - 1));
         W2_SYNC();
         W2_SFOR(j, jS + 1, jN - 1)
-        VF(iE + 1, j) = VF(iE + 1, j - 1) + 3.0 * (VF(iE, j - 1) - VF(iE, j)) -
-                       4.0 * (UF(iE, j) - UF(iE - 1, j));
+        VF(iE + 1, j) = VF(iE + 1, j - 1) + T(3.0) * (VF(iE, j - 1) - VF(iE, j)) -
+                       T(4.0) * (UF(iE, j) - UF(iE - 1, j));
         W2_SYNC();
       } else if (t < BM_INTERN || t > BM_OUTLT2) {
         return false;
       }
       t = r.BT(ireg, jreg, SOUTH);
       if (t == BM_OUTLT1) {
-        const double vs_ = r.BV(ireg, jreg, SOUTH, VAR_V);
+        const T vs_ = T(r.BV(ireg, jreg, SOUTH, VAR_V));
         W2_PFOR(i, iW + 1, iE) UF(i, jS) = -UF(i, jS + 1);
         W2_SYNC();
         W2_PFOR(i, iW, iE) VF(i, jS) = vs_ + VF(i, jS);
@@ -243,15 +245,15 @@ __device__ bool vel_outflow_bcs_block(const Dev &d, double *u, double *v) {
         W2_PFOR(i, iW + 1, iE) VF(i, jS) = VF(i, jS + 1) + (UF(i, jS + 1) - UF(i - 1, jS + 1));
         W2_SYNC();
         W2_SFOR(i, iW + 1, iE - 1)
-        UF(i, jS) = UF(i - 1, jS) + 3.0 * (UF(i - 1, jS + 1) - UF(i, jS + 1)) -
-                   4.0 * (VF(i, jS + 1) - VF(i, jS));
+        UF(i, jS) = UF(i - 1, jS) + T(3.0) * (UF(i - 1, jS + 1) - UF(i, jS + 1)) -
+                   T(4.0) * (VF(i, jS + 1) - VF(i, jS));
         W2_SYNC();
       } else if (t < BM_INTERN || t > BM_OUTLT2) {
         return false;
       }
       t = r.BT(ireg, jreg, NORTH);
       if (t == BM_OUTLT1) {
-        const double vn_ = r.BV(ireg, jreg, NORTH, VAR_V);
+        const T vn_ = T(r.BV(ireg, jreg, NORTH, VAR_V));
         W2_PFOR(i, iW + 1, iE) UF(i, jN + 1) = -UF(i, jN);
         W2_SYNC();
         W2_PFOR(i, iW, iE) VF(i, jN + 1) = vn_ + VF(i, jN);
@@ -260,8 +262,8 @@ __device__ bool vel_outflow_bcs_block(const Dev &d, double *u, double *v) {
         W2_PFOR(i, iW, iE) VF(i, jN) = VF(i, jN - 1) - (UF(i, jN) - UF(i - 1, jN));
         W2_SYNC();
         W2_SFOR(i, iW + 1, iE - 1)
-        UF(i, jN + 1) = UF(i - 1, jN + 1) + 3.0 * (UF(i - 1, jN) - UF(i, jN)) -
-                       4.0 * (VF(i, jN) - VF(i, jN - 1));
+        UF(i, jN + 1) = UF(i - 1, jN + 1) + T(3.0) * (UF(i - 1, jN) - UF(i, jN)) -
+                       T(4.0) * (VF(i, jN) - VF(i, jN - 1));
         W2_SYNC();
       } else if (t < BM_INTERN || t > BM_OUTLT2) {
         return false;

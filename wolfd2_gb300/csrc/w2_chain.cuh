@@ -33,30 +33,37 @@ constexpr int kMaxRounds = 24;
 __device__ __forceinline__ bool same_bits(double a, double b) {
   return __double_as_longlong(a) == __double_as_longlong(b);
 }
+__device__ __forceinline__ bool same_bits(float a, float b) {
+  return __float_as_int(a) == __float_as_int(b);
+}
 
-__device__ __forceinline__ double chain_rhs(const Chain &c, int k) {
-  return (c.bzero != nullptr && c.bzero[k]) ? 0.0 : c.b[k];
+template <class T>
+__device__ __forceinline__ T chain_rhs(const ChainT<T> &c, int k) {
+  return (c.bzero != nullptr && c.bzero[k]) ? T(0) : c.b[k];
 }
 
 // One forward row k >= 1 of AltTridLU: a2' = a2 - a1 a3'(k-1); a3' = a3/a2'
 // (not formed on the last row); b' = (b - a1 b'(k-1)) / a2'.
-__device__ __forceinline__ void fwd_row(const Chain &c, int k, double &a3p, double &bp) {
-  const double a1 = c.a1[k];
-  const double a2p = c.a2[k] - a1 * a3p;
-  const double nb = (chain_rhs(c, k) - a1 * bp) / a2p;
-  a3p = (k < c.n - 1) ? c.a3[k] / a2p : 0.0;
+template <class T>
+__device__ __forceinline__ void fwd_row(const ChainT<T> &c, int k, T &a3p, T &bp) {
+  const T a1 = c.a1[k];
+  const T a2p = c.a2[k] - a1 * a3p;
+  const T nb = (chain_rhs(c, k) - a1 * bp) / a2p;
+  a3p = (k < c.n - 1) ? c.a3[k] / a2p : T(0);
   bp = nb;
 }
 
 // Row 0 with the reference's first-row quirk.
-__device__ __forceinline__ void fwd_row0(const Chain &c, double &a3p, double &bp) {
+template <class T>
+__device__ __forceinline__ void fwd_row0(const ChainT<T> &c, T &a3p, T &bp) {
   a3p = c.a3[0] / c.a2[1];
   bp = chain_rhs(c, 0) / c.a2[0];
 }
 
-__device__ void chain_f1(const Chain &c, int s, int L, int W) {
+template <class T>
+__device__ void chain_f1(const ChainT<T> &c, int s, int L, int W) {
   const int k0 = s * L, k1 = min(c.n, k0 + L);
-  double a3p, bp;
+  T a3p, bp;
   int k;
   if (k0 == 0) {
     fwd_row0(c, a3p, bp);
@@ -69,8 +76,8 @@ __device__ void chain_f1(const Chain &c, int s, int L, int W) {
       fwd_row0(c, a3p, bp);
       for (int q = 1; q < k0; ++q) fwd_row(c, q, a3p, bp);
     } else {
-      a3p = 0.0;
-      bp = 0.0;
+      a3p = T(0);
+      bp = T(0);
       for (int q = kw; q < k0; ++q) fwd_row(c, q, a3p, bp);
     }
     k = k0;
@@ -86,14 +93,15 @@ __device__ void chain_f1(const Chain &c, int s, int L, int W) {
 
 // Verification round; reads end states from `ein`, writes `eout`.
 // Returns true when the segment's end state changed.
-__device__ bool chain_f2(const Chain &c, int s, int L, const double *ein, double *eout) {
+template <class T>
+__device__ bool chain_f2(const ChainT<T> &c, int s, int L, const T *ein, T *eout) {
   if (s == 0) {
     eout[0] = ein[0];
     eout[1] = ein[1];
     return false;
   }
   const int k0 = s * L, k1 = min(c.n, k0 + L);
-  double a3p = ein[2 * (s - 1)], bp = ein[2 * (s - 1) + 1];
+  T a3p = ein[2 * (s - 1)], bp = ein[2 * (s - 1) + 1];
   for (int k = k0; k < k1; ++k) {
     fwd_row(c, k, a3p, bp);
     if (same_bits(a3p, c.a3p[k]) && same_bits(bp, c.bp[k])) {
@@ -109,9 +117,10 @@ __device__ bool chain_f2(const Chain &c, int s, int L, const double *ein, double
   return true;
 }
 
-__device__ void chain_b1(const Chain &c, int s, int L, int W) {
+template <class T>
+__device__ void chain_b1(const ChainT<T> &c, int s, int L, int W) {
   const int k0 = s * L, k1 = min(c.n, k0 + L);
-  double xn;
+  T xn;
   int k;
   if (k1 == c.n) {
     xn = c.bp[c.n - 1];
@@ -123,7 +132,7 @@ __device__ void chain_b1(const Chain &c, int s, int L, int W) {
       xn = c.bp[c.n - 1];
       for (int q = c.n - 2; q >= k1; --q) xn = c.bp[q] - c.a3p[q] * xn;
     } else {
-      xn = 0.0;
+      xn = T(0);
       for (int q = kw; q >= k1; --q) xn = c.bp[q] - c.a3p[q] * xn;
     }
     k = k1 - 1;
@@ -135,13 +144,14 @@ __device__ void chain_b1(const Chain &c, int s, int L, int W) {
   c.eb[s] = c.x[k0];
 }
 
-__device__ bool chain_b2(const Chain &c, int s, int L, const double *ein, double *eout) {
+template <class T>
+__device__ bool chain_b2(const ChainT<T> &c, int s, int L, const T *ein, T *eout) {
   const int k0 = s * L, k1 = min(c.n, k0 + L);
   if (k1 == c.n) {
     eout[s] = ein[s];
     return false;
   }
-  double xn = ein[s + 1];
+  T xn = ein[s + 1];
   for (int k = k1 - 1; k >= k0; --k) {
     xn = c.bp[k] - c.a3p[k] * xn;
     if (same_bits(xn, c.x[k])) {
@@ -158,11 +168,12 @@ __device__ bool chain_b2(const Chain &c, int s, int L, const double *ein, double
 // of block 0 walks the chain in chunks of 32 rows, the lanes staging each
 // chunk's coefficients through shared memory and lane 0 running the
 // recurrence (same arithmetic as fwd_row / the back substitution).
-__device__ void chain_sequential_warp(const Chain &c, bool forward) {
-  __shared__ double s1[32], s2[32], s3[32], sb[32], o3[32], ob[32];
+template <class T>
+__device__ void chain_sequential_warp(const ChainT<T> &c, bool forward) {
+  __shared__ T s1[32], s2[32], s3[32], sb[32], o3[32], ob[32];
   const int lane = threadIdx.x & 31;
   if (forward) {
-    double a3p = 0.0, bp = 0.0;
+    T a3p = T(0), bp = T(0);
     for (int base = 0; base < c.n; base += 32) {
       const int k = base + lane, cnt = min(32, c.n - base);
       if (k < c.n) {
@@ -179,10 +190,10 @@ __device__ void chain_sequential_warp(const Chain &c, bool forward) {
             a3p = s3[0] / c.a2[1];
             bp = sb[0] / s2[0];
           } else {
-            const double a1 = s1[q];
-            const double a2p = s2[q] - a1 * a3p;
-            const double nb = (sb[q] - a1 * bp) / a2p;
-            a3p = (kk < c.n - 1) ? s3[q] / a2p : 0.0;
+            const T a1 = s1[q];
+            const T a2p = s2[q] - a1 * a3p;
+            const T nb = (sb[q] - a1 * bp) / a2p;
+            a3p = (kk < c.n - 1) ? s3[q] / a2p : T(0);
             bp = nb;
           }
           o3[q] = a3p;
@@ -197,7 +208,7 @@ __device__ void chain_sequential_warp(const Chain &c, bool forward) {
       __syncwarp();
     }
   } else {
-    double xn = 0.0;
+    T xn = T(0);
     for (int top = c.n - 1; top >= 0; top -= 32) {
       const int k = top - lane, cnt = min(32, top + 1);
       if (k >= 0) {
@@ -220,16 +231,19 @@ __device__ void chain_sequential_warp(const Chain &c, bool forward) {
 }
 
 // Views of a chain whose end-state buffers are swapped per round.
-__device__ __forceinline__ const double *ef_buf(const Chain &c, int b) {
+template <class T>
+__device__ __forceinline__ const T *ef_buf(const ChainT<T> &c, int b) {
   return c.ef + (size_t)b * 2 * c.nseg;
 }
-__device__ __forceinline__ const double *eb_buf(const Chain &c, int b) {
+template <class T>
+__device__ __forceinline__ const T *eb_buf(const ChainT<T> &c, int b) {
   return c.eb + (size_t)b * c.nseg;
 }
 
 // Solve up to two independent chains together (segments of both share the
 // grid).  Every block must call this.  Returns false if a barrier failed.
-__device__ bool solve_chains(const Dev &d, Chain c0, Chain c1, int nchains) {
+template <class T>
+__device__ bool solve_chains(const Dev &d, ChainT<T> c0, ChainT<T> c1, int nchains) {
   Sync *sy = d.sync;
   const int L = d.seg, W = d.warm;
   const int nseg0 = c0.nseg, nseg1 = nchains > 1 ? c1.nseg : 0;
@@ -250,9 +264,9 @@ __device__ bool solve_chains(const Dev &d, Chain c0, Chain c1, int nchains) {
     if (!grid_sync(sy)) return false;
     int any = 0;
     for (int g = gtid(); g < nsegt; g += gthreads()) {
-      const Chain &c = g < nseg0 ? c0 : c1;
+      const ChainT<T> &c = g < nseg0 ? c0 : c1;
       int s = g < nseg0 ? g : g - nseg0;
-      double *eo = const_cast<double *>(ef_buf(c, cur ^ 1));
+      T *eo = const_cast<T *>(ef_buf(c, cur ^ 1));
       if (chain_f2(c, s, L, ef_buf(c, cur), eo)) any = 1;
     }
     if (any) atomicOr(&sy->iout[round % 3], 1);
@@ -283,12 +297,12 @@ __device__ bool solve_chains(const Dev &d, Chain c0, Chain c1, int nchains) {
   // ---- B1
   for (int g = gtid(); g < nsegt; g += gthreads()) {
     if (g < nseg0) {
-      Chain c = c0;
-      c.eb = const_cast<double *>(eb_buf(c0, 0));
+      ChainT<T> c = c0;
+      c.eb = const_cast<T *>(eb_buf(c0, 0));
       chain_b1(c, g, L, W);
     } else {
-      Chain c = c1;
-      c.eb = const_cast<double *>(eb_buf(c1, 0));
+      ChainT<T> c = c1;
+      c.eb = const_cast<T *>(eb_buf(c1, 0));
       chain_b1(c, g - nseg0, L, W);
     }
   }
@@ -302,9 +316,9 @@ __device__ bool solve_chains(const Dev &d, Chain c0, Chain c1, int nchains) {
     if (!grid_sync(sy)) return false;
     int any = 0;
     for (int g = gtid(); g < nsegt; g += gthreads()) {
-      const Chain &c = g < nseg0 ? c0 : c1;
+      const ChainT<T> &c = g < nseg0 ? c0 : c1;
       int s = g < nseg0 ? g : g - nseg0;
-      if (chain_b2(c, s, L, eb_buf(c, cur), const_cast<double *>(eb_buf(c, cur ^ 1)))) any = 1;
+      if (chain_b2(c, s, L, eb_buf(c, cur), const_cast<T *>(eb_buf(c, cur ^ 1)))) any = 1;
     }
     if (any) atomicOr(&sy->iout[3 + round % 3], 1);
     if (!grid_sync(sy)) return false;

@@ -62,15 +62,30 @@ struct Regions {
 
 // A concatenated tridiagonal chain solved by AltTridLU semantics
 // (momentum.f:1307-1339): forward elimination over all n rows in order,
-// row 1's super-diagonal divided by row 2's original diagonal.
-struct Chain {
+// row 1's super-diagonal divided by row 2's original diagonal.  T is the
+// arithmetic type (double for the plain path, float for the mixed one).
+template <class T>
+struct ChainT {
   int n;           // rows
   int nseg;        // segments of length seg
-  double *a1, *a2, *a3, *b;        // sub, diag, super, rhs
+  T *a1, *a2, *a3, *b;             // sub, diag, super, rhs
   const uint8_t *bzero;            // rows whose rhs is forced to 0 (or null)
-  double *a3p, *bp, *x;            // factorised super, forward rhs, solution
-  double *ef;      // forward end states: 2 per segment x 2 buffers
-  double *eb;      // backward end states: 1 per segment x 2 buffers
+  T *a3p, *bp, *x;                 // factorised super, forward rhs, solution
+  T *ef;           // forward end states: 2 per segment x 2 buffers
+  T *eb;           // backward end states: 1 per segment x 2 buffers
+};
+using Chain = ChainT<double>;
+
+// The momentum step's inputs and work arrays in one arithmetic type: the
+// metric arrays the stencils read, the ConvCoef outputs and the four chains.
+template <class T>
+struct MomView {
+  const T *yeu, *xeu, *xzu, *yzu, *yec, *xec, *xzn, *yzn;
+  const T *yev, *xev, *xzv, *yzv, *yen, *xen, *xzc, *yzc;
+  const T *dju, *djv, *rac, *rbc, *rbn, *rgn, *ran, *rgc;
+  T *cj1x, *cj2x, *c1sx, *c2sx, *c1nx, *c2nx;
+  T *cj1y, *cj2y, *c1sy, *c2sy, *c1ny, *c2ny;
+  ChainT<T> x1, x2, y1, y2;
 };
 
 // Grid-wide synchronisation state in device memory.
@@ -108,6 +123,7 @@ struct Dev {
   double *div, *pb, *ppn;
   double *la3p, *lbp;  // line-solver scratch (field layout)
   double *qh;          // filter scratch
+  MomView<float> f32;  // single-precision momentum (mixed path)
   Sync *sync;
   int seg, warm;       // chain segment length and warm-up rows
   int has_outflow;     // any OUTLT1/OUTLT2 face (VelOutflowBCs not a no-op)

@@ -170,8 +170,53 @@ __global__ void __launch_bounds__(kMaxThreads) k_naux(Dev d, int mqiter, double 
                                                       StepOut *out) {
   if (d.sync->halt) return;
   int res = -1;
-  if (!naux_momentum(d, mqiter, dk, re, qtol, un, vn, us, vs, &res)) return;
+  if (!naux_momentum<double>(d, mom_view64(d), mqiter, dk, re, qtol, un, vn, us, vs, &res)) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) out->nql = res;
+}
+
+// nAuxMomentum in single precision (mixed path) on un32, vn32 -> us32, vs32,
+// then us, vs = the FP32 results widened to FP64 on every cell.
+__global__ void __launch_bounds__(kMaxThreads) k_naux32(Dev d, int mqiter, double dk, double re,
+                                                        double qtol, const float *un,
+                                                        const float *vn, float *us, float *vs,
+                                                        double *us64, double *vs64, StepOut *out) {
+  if (d.sync->halt) return;
+  int res = -1;
+  if (!naux_momentum<float>(d, d.f32, mqiter, dk, re, qtol, un, vn, us, vs, &res)) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) out->nql = res;
+  const int W = d.nx + 2, H = d.ny + 2;
+  for (int t = gtid(); t < W * H; t += gthreads()) {
+    const size_t o = IX(d, t % W, t / W);
+    us64[o] = (double)us[o];
+    vs64[o] = (double)vs[o];
+  }
+}
+
+// Time-level copies of the mixed step: p = pn, and the single-precision
+// momentum inputs un32 = (float)un, vn32 = (float)vn, us32 = un32,
+// vs32 = vn32 on every cell.
+__global__ void k_copy_mixed(Dev d, double *p, const double *pn, const double *un,
+                             const double *vn, float *un32, float *vn32, float *us32,
+                             float *vs32) {
+  const int W = d.nx + 2, H = d.ny + 2;
+  for (int t = gtid(); t < W * H; t += gthreads()) {
+    const size_t o = IX(d, t % W, t / W);
+    p[o] = pn[o];
+    const float a = (float)un[o], b = (float)vn[o];
+    un32[o] = a;
+    us32[o] = a;
+    vn32[o] = b;
+    vs32[o] = b;
+  }
+}
+
+// Metric array rounded to single precision.
+__global__ void k_to_f32(Dev d, const double *src, float *dst) {
+  const int W = d.nx + 2, H = d.ny + 2;
+  for (int t = gtid(); t < W * H; t += gthreads()) {
+    const size_t o = IX(d, t % W, t / W);
+    dst[o] = (float)src[o];
+  }
 }
 
 // ---- boundary programs (one block) -------------------------------------
@@ -233,7 +278,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) k_ppe_tiled(Dev d, TileGeom g,
 // Mixed-precision red/black SOR (FP32 sweeps, FP64 residual and correction)
 // with K sweeps per grid barrier; one tile per block.
 template <int K>
-__global__ void __launch_bounds__(1024, 1) k_ppe_mixed(Dev d, MixedGeom g, MixedArgs a,
+__global__ void __launch_bounds__(kMixedThreads, 1) k_ppe_mixed(Dev d, MixedGeom g, MixedArgs a,
                                                       StepOut *out) {
   if (d.sync->halt) return;
   const int nconv = ppe_mixed<K>(d, g, a);
