@@ -120,10 +120,11 @@ def ppe_bytes(cells, nsor):
     return 8.0 * cells * (3 + 3 * nsor)
 
 
-def mom_bytes(cells, nql):
+def mom_bytes(cells, nql, word=8):
     """Algorithmic bytes of one nAuxMomentum call: per Q-L iteration read us,
-    vs, un, vn and write us, vs (6 words); chain systems stay on chip."""
-    return 8.0 * cells * 6 * nql
+    vs, un, vn and write us, vs (6 words of `word` bytes: 8 plain, 4 in the
+    mixed path's FP32 momentum); chain systems stay on chip."""
+    return float(word) * cells * 6 * nql
 
 
 def step_bytes(cells, nql, nsor):
@@ -239,15 +240,20 @@ def run_arm(s, prm, args, precision, u0, v0, p0, st, flush, barrier, local, time
     prof = {k: s.profile_read(k) for k in (K_MOMENTUM, K_PPE, K_POST, K_BC, K_COPY)}
     s.profile(False)
     fields = s.store_fields()
-    # end-to-end through the C-ABI with host buffers, copies in the timed region
-    u, v, p = (f.copy(order="F") for f in fields)
+    # end-to-end through the C-ABI with pinned host buffers, the copies in
+    # the timed region: each step loads u, v, p, runs, and reads them back
+    pinned = [torch.empty((s.mny + 1, s.mnx + 1), dtype=torch.float64, pin_memory=True)
+              for _ in range(3)]
+    host = [t.numpy().T for t in pinned]  # Fortran-ordered views of pinned memory
+    for h, f in zip(host, fields):
+        h[...] = f
     e2e_steps = max(1, min(args.steps, args.e2e_steps))
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        s.load_fields(u, v, p)
+        s.load_fields(*host)
         s.step(prm, 1, **kw)
-        u, v, p = s.store_fields()
+        s.store_fields(out=host)
     barrier()
     t_e2e = time.perf_counter() - t0
     return {"t_dev": t_dev, "t_e2e": t_e2e, "e2e_steps": e2e_steps, "hist": hist,
@@ -255,10 +261,22 @@ def run_arm(s, prm, args, precision, u0, v0, p0, st, flush, barrier, local, time
             "wall": t_wall, "fields": fields}
 
 
-def roofline_of(arm, cells, precision, inner):
+def kernel_name(kind, precision, tiled):
+    """The kernel a profile kind stands for in this workload."""
+    from wolfd2_gb300.gpu import K_COPY, K_MOMENTUM, K_PPE, KERNEL_NAMES
+    if kind == K_PPE:
+        return "k_ppe_mixed" if precision == "mixed" else ("k_ppe_tiled" if tiled else "k_ppe")
+    if kind == K_MOMENTUM:
+        return "k_naux32" if precision == "mixed" else "k_naux"
+    if kind == K_COPY and precision == "mixed":
+        return "k_copy_mixed"
+    return KERNEL_NAMES[kind]
+
+
+def roofline_of(arm, cells, precision, inner, tiled=True):
     """Roofline of the dominant kernel of one arm (HBM view) and the FP64
     pipe view of the plain red/black sweep."""
-    from wolfd2_gb300.gpu import K_MOMENTUM, K_PPE, KERNEL_NAMES
+    from wolfd2_gb300.gpu import K_MOMENTUM, K_PPE
     prof, timed = arm["prof"], arm["timed"]
     hbm_peak, peak_kind = peaks()
     dom = max((K_MOMENTUM, K_PPE), key=lambda k: prof[k][0])
@@ -270,9 +288,9 @@ def roofline_of(arm, cells, precision, inner):
         else:
             alg = sum(ppe_bytes(cells, n) for n in nsor)
     else:
-        alg = sum(mom_bytes(cells, n) for n in nql)
+        alg = sum(mom_bytes(cells, n, 4 if precision == "mixed" else 8) for n in nql)
     dom_ms, dom_n = prof[dom]
-    name = KERNEL_NAMES[dom] if not (dom == K_PPE and precision == "mixed") else "k_ppe_mixed"
+    name = kernel_name(dom, precision, tiled)
     achieved = alg / (dom_ms / 1e3) / 1e9
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
@@ -290,7 +308,7 @@ def roofline_of(arm, cells, precision, inner):
         # 1 subtraction and 1 addition per point and sweep
         ops = sum(cells * n for n in nsor) * 7.0
         gops = ops / (prof[K_PPE][0] / 1e3) / 1e9
-        fp64 = {"kernel": "k_ppe_tiled", "op_per_point": "7 FP64 add/mul (unit stencil)",
+        fp64 = {"kernel": kernel_name(K_PPE, precision, tiled), "op_per_point": "7 FP64 add/mul (unit stencil)",
                 "achieved_gops": gops, "peak_gops": 628.0,
                 "peak_kind": "measured DFMA probe on this pool's GB300 (2 DFMA/clk/SM)",
                 "frac": gops / 628.0}
@@ -304,7 +322,7 @@ def rel_max(a, b):
 def run_ours(args):
     import torch
     import torch.distributed as dist
-    from wolfd2_gb300.gpu import KERNEL_NAMES, PREC_FP64, PREC_MIXED, Solver
+    from wolfd2_gb300.gpu import PREC_FP64, PREC_MIXED, Solver
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -355,17 +373,19 @@ def run_ours(args):
     field_bytes = (case.nx + 2) * (case.ny + 2) * 8
     value = world * cells * args.steps / t_max
     e2e_value = world * cells * head["e2e_steps"] / t_e2e_max
-    roof, fp64 = roofline_of(head, cells, args.precision, inner)
+    # the plain path's red/black solve runs on shared-memory tiles at this size
+    tiled = args.solver in ("rb_sor", "par_rb_sor") and cells >= 152 * 1024
+    roof, fp64 = roofline_of(head, cells, args.precision, inner, tiled)
     plain = None
     accuracy = None
     if args.precision == "mixed":
         a64 = arms["fp64"]
-        r64, f64 = roofline_of(a64, cells, "fp64", inner)
+        r64, f64 = roofline_of(a64, cells, "fp64", inner, tiled)
         plain = {"value": world * cells * args.steps / a64["t_dev"], "unit": UNIT,
                  "ms_per_step": 1e3 * a64["t_dev"] / args.steps,
                  "e2e": world * cells * a64["e2e_steps"] / a64["t_e2e"],
                  "roofline": r64, "fp64_roof": f64, "gpu_launches": a64["launches"],
-                 "kernel_ms": {KERNEL_NAMES[k]: {"total_ms": v[0], "launches": v[1]}
+                 "kernel_ms": {kernel_name(k, "fp64", tiled): {"total_ms": v[0], "launches": v[1]}
                                for k, v in a64["prof"].items()},
                  "iterations": [[h[0], h[1]] for h in a64["timed"]],
                  "clocks": a64["clk"].summary()}
@@ -401,14 +421,16 @@ def run_ours(args):
         "roofline": roof,
         "fp64_roof": fp64,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 3 * field_bytes,
-                "d2h_bytes_per_step": 3 * field_bytes, "steps": head["e2e_steps"]},
+                "d2h_bytes_per_step": 3 * field_bytes, "steps": head["e2e_steps"],
+                "host_buffers": "pinned"},
         "plain_fp64": plain,
         "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
         "accuracy": accuracy,
         "cpu_baseline": cpu,
         "clocks": head["clk"].summary(),
         "gpu_launches": head["launches"],
-        "kernel_ms": {KERNEL_NAMES[k]: {"total_ms": v[0], "launches": v[1]} for k, v in head["prof"].items()},
+        "kernel_ms": {kernel_name(k, args.precision, tiled): {"total_ms": v[0], "launches": v[1]}
+                      for k, v in head["prof"].items()},
         "iterations": [[h[0], h[1]] for h in head["timed"]],
         "chain": {"max_verify_rounds": chain_rounds, "sequential_fallbacks": chain_fallbacks},
         "wall_s": head["wall"],

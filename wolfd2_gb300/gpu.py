@@ -270,8 +270,10 @@ class Solver:
     def load_fields(self, u, v, p) -> None:
         self._check(self.L.wolfd2gpu_load_fields(self.h, _p(u), _p(v), _p(p)))
 
-    def store_fields(self):
-        u, v, p = self.field(), self.field(), self.field()
+    def store_fields(self, out=None):
+        """Copy u, v, p to host arrays: new ones, or the three Fortran-ordered
+        float64 arrays of `out` (for example pinned buffers)."""
+        u, v, p = out if out is not None else (self.field(), self.field(), self.field())
         self._check(self.L.wolfd2gpu_store_fields(self.h, _p(u), _p(v), _p(p)))
         return u, v, p
 
