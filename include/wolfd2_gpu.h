@@ -197,8 +197,8 @@ int wolfd2gpu_tune(w2_ctx *ctx, int chain_seg, int chain_warm, int threads,
 int wolfd2gpu_set_precision(w2_ctx *ctx, int precision, int refine_sweeps);
 
 /* Mixed Poisson kernel shape: sweeps between grid barriers (4 or 8; the
- * halo is twice that) and threads per block (64..512; 0 keeps the current
- * value).  Tile sizes are re-planned for the new shape. */
+ * halo is twice that) and the largest block the tile planner may use
+ * (64..512 threads; 0 keeps the current value).  Tiles are re-planned. */
 int wolfd2gpu_tune_mixed(w2_ctx *ctx, int sweeps_per_barrier, int threads);
 
 /* Device pointers of the resident u, v, p fields and the device leading

@@ -490,12 +490,13 @@ const void *mixed_kernel(int K) {
 }
 
 // One tile per block (one block per SM): the split of the unknowns into at
-// most nsm tiles, tx a multiple of 8, whose largest tile sweeps the least
-// area per group of K sweeps, within the shared-memory limit and at most
-// kMixedPmax box positions per thread.
+// most nsm tiles, tx a multiple of 8, whose block does the least sweep work
+// per group of K sweeps -- (plane columns rounded to warps) x (box rows
+// active in each half-sweep) -- within the shared-memory limit and
+// mixed_threads <= kMixedThreads threads.
 void plan_mixed(w2_ctx *c) {
   c->mixed_ok = false;
-  const int K = c->mixed_K, T = c->mixed_threads;
+  const int K = c->mixed_K;
   const void *kf = mixed_kernel(K);
   if (!kf) return;
   int maxsmem = 0;
@@ -515,22 +516,23 @@ void plan_mixed(w2_ctx *c) {
       const int ty = (NY + nty - 1) / nty;
       if ((NY + ty - 1) / ty != nty) continue;
       const size_t smem = mixed_smem_bytes(K, tx, ty);
-      if (smem > limit) continue;
-      const int bw = tx + 2 * H, bh = ty + 2 * H;
-      const int P = ((bh - 2) * (bw / 2 - 1) + T - 1) / T;
-      if (P > kMixedPmax || (size_t)bh * (bw / 2) > 65535) continue;
-      double area = 0.0;
-      for (int e = H - 1; e >= 0; --e) area += (double)(tx + 2 * e) * (ty + 2 * e);
-      if (area < best) {
-        best = area;
-        c->mg = MixedGeom{tx, ty, ntx, nty, ntx * tx / 2 + H, nty * ty + 2 * H, P};
+      const int T = mixed_threads(K, tx, ty);
+      if (smem > limit || T > c->mixed_threads) continue;
+      const int bh = ty + 2 * H, hwp = (tx / 2 + H + 31) / 32 * 32;
+      double rows = 0.0;
+      for (int h = 1; h <= 2 * K; ++h) rows += std::max(0, bh - 2 * h);
+      const double cost = (double)hwp * rows;
+      if (cost < best) {
+        best = cost;
+        c->mg = MixedGeom{tx, ty, ntx, nty, ntx * tx / 2 + H, nty * ty + 2 * H, hwp};
         c->mixed_smem = smem;
       }
     }
   }
   if (best >= 1e300) return;
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kf, T, c->mixed_smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kf, mixed_threads(K, c->mg.tx, c->mg.ty),
+                                                c->mixed_smem);
   if (occ < 1) return;
   // exchange buffers: zero wherever no tile writes (cells off the unknowns)
   const size_t need = 4 * (size_t)c->mg.gh * c->mg.gw;
@@ -573,8 +575,9 @@ int launch_ppe_mixed(w2_ctx *c, int lcartes, int msorit, double dk, double sorto
               c->xbuf, xb1};
   void *args[] = {&d, &g, &a, &out};
   c->launches++;
-  cudaError_t e = cudaLaunchCooperativeKernel(mixed_kernel(c->mixed_K), dim3(c->nsm),
-                                              dim3(c->mixed_threads), args, c->mixed_smem, c->st);
+  const int T = mixed_threads(c->mixed_K, g.tx, g.ty);
+  cudaError_t e = cudaLaunchCooperativeKernel(mixed_kernel(c->mixed_K), dim3(c->nsm), dim3(T),
+                                              args, c->mixed_smem, c->st);
   if (e != cudaSuccess) return fail(c, W2_E_CUDA, "mixed PPE launch: %s", cudaGetErrorString(e));
   return W2_OK;
 }
@@ -809,7 +812,7 @@ int wolfd2gpu_tune_mixed(w2_ctx *c, int sweeps_per_barrier, int threads) {
   if (sweeps_per_barrier != 0 && !mixed_kernel(sweeps_per_barrier))
     return fail(c, W2_E_ARG, "sweeps per barrier must be 4 or 8");
   if (threads != 0 && (threads % 32 || threads < 64 || threads > kMixedThreads))
-    return fail(c, W2_E_ARG, "threads must be a multiple of 32 in 64..%d", kMixedThreads);
+    return fail(c, W2_E_ARG, "thread limit must be a multiple of 32 in 64..%d", kMixedThreads);
   if (sweeps_per_barrier) c->mixed_K = sweeps_per_barrier;
   if (threads) c->mixed_threads = threads;
   if (c->metrics_ok) plan_mixed(c);

@@ -13,37 +13,49 @@
 // `inner` sweeps; every pass restarts e from an FP64 residual, so FP32
 // rounding never accumulates beyond one pass.
 //
-// Layout.  Every block owns one tile of tx x ty unknowns and keeps in shared
-// memory the tile grown by a halo of H = 2K cells, K being the sweeps run
-// between grid barriers.  The box is stored as two colour planes (colour 0:
-// i+j even) of hw = bw/2 entries per row: the points of one colour are
-// contiguous and every neighbour of a point sits in the other plane at the
-// same or the adjacent index.  Each thread owns a fixed list of (row, slot)
-// positions of the box, built once per launch, holding per colour the
-// point's distance to the box frame.  Half-sweep h (1-based within a group)
-// updates the points at distance >= h: the frame's values are those of the
-// group start, so after h half-sweeps only the points closer than h to the
-// frame can be stale, and after 2K half-sweeps the tile (distance >= H) is
-// exactly what a global sweep gives.  Between groups only the halo ring
-// changes hands, through a global buffer in the same colour-split layout
-// whose rows are aligned so that the ring and band segments move as 16-byte
-// vectors: each block writes the band of its tile within H of the edge and
-// reads its ring (two buffers, alternating by group).
+// Layout.  Every block owns one tile of tx x ty unknowns; its box is the tile
+// grown by a halo of H = 2K cells, K being the sweeps run between grid
+// barriers.  The box is split into two colour planes (colour 0: i+j even) of
+// hw = bw/2 columns: in every row, column k of a plane holds the point of
+// that colour at i = gi0 + 2k + (row parity), so a point's east/west
+// neighbours are the other plane's columns k and k-1 or k+1, and its
+// north/south neighbours are the other plane's column k one row up or down.
+//
+// Registers.  Thread (k, s) owns column k of both planes over the rows of
+// strip s (kMixedRows rows).  A half-sweep of colour c first reads the
+// strip's column of the other plane into registers, then walks its rows:
+// north/south come from those registers (from shared memory at the strip's
+// first and last row), the
+// column neighbour from the adjacent lane by one warp shuffle whose
+// direction is the row's parity (uniform across the warp; shared memory for
+// the lanes at a warp's edge).  Updates are written through to the
+// shared-memory planes, which are what other threads read and what the halo
+// exchange moves.  Half-sweep h (1-based within a group) updates the points
+// whose distance to the box frame is at least h: the frame keeps its
+// group-start values, so after h half-sweeps only points closer than h to it
+// can be stale, and after 2K half-sweeps the tile (distance >= H) is exactly
+// what a global sweep gives.  Rows closer than h to the frame are skipped
+// whole.
+//
+// Between groups only the halo ring changes hands, through a global buffer
+// in the same colour-split layout whose rows are aligned so that ring and
+// band segments move as 16-byte vectors: each block writes the band of its
+// tile within H of the edge and reads its ring (two buffers, alternating by
+// group).
 #pragma once
 #include "w2_ppe.cuh"
 
 namespace w2 {
 
-constexpr int kMixedPmax = 16;     // box positions per thread
-constexpr int kMixedBatch = 8;     // positions whose operands are loaded together
-constexpr int kMixedThreads = 512;
-constexpr int kMixedRing = 17;     // Sync::red[17 .. 17 + 3K): per-sweep maxima
+constexpr int kMixedRows = 16;      // rows of a thread's strip
+constexpr int kMixedThreads = 512;  // largest block
+constexpr int kMixedRing = 17;      // Sync::red[17 .. 17 + 3K): per-sweep maxima
 
 struct MixedGeom {
   int tx, ty;    // tile size in unknowns (tx a multiple of 8)
   int ntx, nty;  // tiles per direction, ntx*nty <= blocks
   int gw, gh;    // exchange buffer: floats per colour row, rows
-  int P;         // box positions per thread
+  int hwp;       // box columns per plane rounded up to whole warps
 };
 
 struct MixedArgs {
@@ -59,117 +71,121 @@ struct MixedArgs {
 // row j + H - 2, float (i + H - 2) >> 1.  A tile (ti, tj)'s box row jj
 // starts at row tj*ty + jj, float ti*tx/2, both 16-byte aligned.
 struct MixedBox {
-  float *E[2], *E0[2], *R[2];  // colour planes, row stride hw
+  float *E[2], *E0[2], *R[2];  // colour planes in shared memory, row stride hw
   int gi0, gj0, bw, bh, hw;    // box origin (grid indices) and size
   int oi0, oi1, oj0, oj1;      // own tile, clipped to the unknowns
   int ti, tj;
-  __device__ __forceinline__ int at(int i, int j) const {
-    return (j - gj0) * hw + ((i - gi0) >> 1);
-  }
+  int k, lane, jj0;            // this thread's column, lane, first strip row
+  int dcol0, dcol1;            // column k's distance to the frame, per row parity
+  unsigned int vrow;           // bit r: strip row r is a row of unknowns inside the frame
+  bool wedge, eedge;           // west/east neighbour column lives in another warp
+  bool own0, own1;             // column k is in the own tile, per row parity
 };
 
-// Packed position: bits 0-15 row*hw + slot, bit 16 row parity of colour 0,
-// bits 17-21 / 22-26 distance of the colour-0 / colour-1 point to the box
-// frame (0 = not an unknown: never updated).  A thread's unused positions
-// point at row 1, slot 1 with distance 0, so that their (unconditional)
-// operand loads stay inside the box.
-__device__ __forceinline__ unsigned int mixed_unused(const MixedBox &b) {
-  return (unsigned int)(b.hw + 1);
+// Distance of box column ii's cells to the left/right frame (0 when the
+// column is off the unknowns).
+__device__ __forceinline__ int mixed_dcol(const Dev &d, const MixedBox &b, int ii, int H) {
+  const int i = b.gi0 + ii;
+  if (ii < 0 || ii >= b.bw || i < 2 || i > d.nx) return 0;
+  return min(min(ii, b.bw - 1 - ii), H);
 }
 
-__device__ __forceinline__ unsigned int mixed_position(const Dev &d, const MixedBox &b, int n,
-                                                       int H) {
-  const int per_row = b.hw - 1, rows = b.bh - 2;
-  if (n >= rows * per_row) return mixed_unused(b);
-  const int jj = 1 + n / per_row, slot = n % per_row;
-  const int par0 = (b.gj0 + jj) & 1;
-  unsigned int w = (unsigned int)(jj * b.hw + slot) | ((unsigned int)par0 << 16);
-#pragma unroll
-  for (int c = 0; c < 2; ++c) {
-    const int par = par0 ^ c;
-    const int ii = 2 * (slot + 1 - par) + par;
-    const int i = b.gi0 + ii, j = b.gj0 + jj;
-    int dist = 0;
-    if (i >= 2 && i <= d.nx && j >= 2 && j <= d.ny) {
-      dist = min(min(ii, b.bw - 1 - ii), min(jj, b.bh - 1 - jj));
-      dist = min(dist, H);
-    }
-    w |= (unsigned int)dist << (17 + 5 * c);
-  }
-  return w;
+// Distance of box row jj to the top/bottom frame (0 off the unknowns).
+__device__ __forceinline__ int mixed_drow(const Dev &d, const MixedBox &b, int jj, int H) {
+  const int j = b.gj0 + jj;
+  if (jj < 1 || jj > b.bh - 2 || j < 2 || j > d.ny) return 0;
+  return min(min(jj, b.bh - 1 - jj), H);
 }
 
-// Half-sweep h of colour c over the thread's positions; returns the max
-// |delta| over own points (distance >= H) as FP32 bits.  Every position's
-// operands are loaded (all lie inside the box) and only the stores and the
-// maximum are predicated, so the loop has no data-dependent branches.
-template <int K>
-__device__ __forceinline__ unsigned int mixed_half_sweep(const MixedBox &b, const unsigned int *pt,
-                                                         int P, int c, int h, float relax) {
+template <int C, class A>
+__device__ __forceinline__ A &pick(A &a0, A &a1) {
+  if constexpr (C == 0) return a0;
+  else return a1;
+}
+
+// The rows of a half-sweep of colour C for a strip whose first row has
+// parity P0 (so row r has parity P0 ^ (r & 1), known once unrolled).  eo
+// holds the strip's column of the other plane, read from shared memory at
+// the start of the half-sweep.
+template <int K, int C, int P0>
+__device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, int h, bool act0, bool act1,
+                                                   float relax) {
   constexpr int H = 2 * K;
-  constexpr int NB = kMixedBatch;
+  const float *Rc = b.R[C];
+  float *Ec = b.E[C];
+  const float *Eo = b.E[C ^ 1];
+  const int hw = b.hw, base = b.jj0 * hw + b.k;
+  float eo[kMixedRows];
+#pragma unroll
+  for (int r = 0; r < kMixedRows; ++r) eo[r] = Eo[base + r * hw];
   unsigned int mx = 0u;
-  float *Ec = b.E[c];
-  const float *Eo = b.E[c ^ 1];
-  const float *Rc = b.R[c];
-  const int hw = b.hw;
-  const int shift = 17 + 5 * c;
 #pragma unroll
-  for (int q0 = 0; q0 < kMixedPmax; q0 += NB) {
-    if (q0 >= P) break;
-    int o[NB], par[NB], dist[NB];
-    float c_[NB], r_[NB], s_[NB], n_[NB], w_[NB], e_[NB];
-#pragma unroll
-    for (int q = 0; q < NB; ++q) {
-      const unsigned int w = pt[q0 + q];
-      par[q] = (int)((w >> 16) & 1u) ^ c;
-      dist[q] = (int)((w >> shift) & 31u);
-      o[q] = (int)(w & 0xffffu) + 1 - par[q];
-      c_[q] = Ec[o[q]];
-      r_[q] = Rc[o[q]];
-      s_[q] = Eo[o[q] - hw];
-      n_[q] = Eo[o[q] + hw];
-      w_[q] = Eo[o[q] - 1 + par[q]];
-      e_[q] = Eo[o[q] + par[q]];
+  for (int r = 0; r < kMixedRows; ++r) {
+    if (!((b.vrow >> r) & 1u)) continue;  // same for the whole warp
+    const int jj = b.jj0 + r;
+    const int rd = min(jj, b.bh - 1 - jj);
+    if (rd < h) continue;                 // same for the whole warp
+    const int par = P0 ^ (r & 1);         // folded once the loop is unrolled
+    const int o = base + r * hw;
+    const float other = eo[r];
+    float nb;
+    if (par == 0) {
+      nb = __shfl_up_sync(0xffffffffu, other, 1);
+      if (b.wedge) nb = Eo[o - 1];
+    } else {
+      nb = __shfl_down_sync(0xffffffffu, other, 1);
+      if (b.eedge) nb = Eo[o + 1];
     }
-#pragma unroll
-    for (int q = 0; q < NB; ++q) {
-      float sum = r_[q] - s_[q] - w_[q] - e_[q] - n_[q];
-      sum = sum * -0.25f - c_[q];
-      const float nv = c_[q] + relax * sum;
-      if (dist[q] >= h) Ec[o[q]] = nv;
-      const unsigned int bb = (dist[q] >= H) ? __float_as_uint(fabsf(sum)) : 0u;
-      mx = bb > mx ? bb : mx;
+    const float w = par ? other : nb, e = par ? nb : other;
+    const float s = (r == 0) ? Eo[o - hw] : eo[r > 0 ? r - 1 : 0];
+    const float n = (r == kMixedRows - 1) ? Eo[o + hw] : eo[r < kMixedRows - 1 ? r + 1 : r];
+    const float c0 = Ec[o];
+    float sum = Rc[o] - s - w - e - n;
+    sum = sum * -0.25f - c0;
+    if (par ? act1 : act0) {
+      Ec[o] = c0 + relax * sum;
+      if (rd >= H && (par ? b.own1 : b.own0)) {
+        const unsigned int bb = __float_as_uint(fabsf(sum));
+        mx = bb > mx ? bb : mx;
+      }
     }
   }
   return mx;
 }
 
-// ns (<= K) sweeps.  With redm, each warp keeps its running maximum of sweep
-// s in redm[s][warp] (zeroed by the caller).
+// Half-sweep h of colour C over the thread's strip; returns the max |delta|
+// over own points (distance >= H) as FP32 bits.
+template <int K, int C>
+__device__ __forceinline__ unsigned int mixed_half_sweep(const MixedBox &b, int h, float relax) {
+  const bool act0 = b.dcol0 >= h, act1 = b.dcol1 >= h;
+  if ((C + b.gj0 + b.jj0) & 1) return mixed_rows<K, C, 1>(b, h, act0, act1, relax);
+  return mixed_rows<K, C, 0>(b, h, act0, act1, relax);
+}
+
+// ns (<= K) sweeps.  With redm, each warp writes its maximum of sweep s to
+// redm[s][warp].
 template <int K>
-__device__ __forceinline__ void mixed_sweeps(const MixedBox &b, const unsigned int *pt, int P,
-                                             int ns, float relax, unsigned int (*redm)[32]) {
+__device__ __forceinline__ void mixed_sweeps(const MixedBox &b, int ns, float relax,
+                                             unsigned int (*redm)[32]) {
 #pragma unroll 1
   for (int s = 0; s < ns; ++s) {
-#pragma unroll 1
-    for (int c = 0; c < 2; ++c) {
-      const unsigned int m = mixed_half_sweep<K>(b, pt, P, c, 2 * s + c + 1, relax);
-      if (redm) {
-        const unsigned int v = __reduce_max_sync(0xffffffffu, m);
-        if ((threadIdx.x & 31) == 0) {
-          unsigned int &slot = redm[s][threadIdx.x >> 5];
-          slot = v > slot ? v : slot;
-        }
-      }
-      __syncthreads();
+    const unsigned int m0 = mixed_half_sweep<K, 0>(b, 2 * s + 1, relax);
+    __syncthreads();
+    const unsigned int m1 = mixed_half_sweep<K, 1>(b, 2 * s + 2, relax);
+    if (redm) {
+      const unsigned int m = m0 > m1 ? m0 : m1;
+      const unsigned int v = __reduce_max_sync(0xffffffffu, m);
+      if (b.lane == 0) redm[s][threadIdx.x >> 5] = v;
     }
+    __syncthreads();
   }
 }
 
-// r = b - A p in FP64 on the whole box (zero off the unknowns), e = 0.
-__device__ void mixed_residual(const Dev &d, const MixedBox &b, const double *p) {
+// r = b - A p in FP64 on the whole box (zero off the unknowns) into the
+// shared R planes; e = 0 in the shared planes.
+__device__ __noinline__ void mixed_residual(const Dev &d, const MixedBox &b, const double *p) {
   const int n = b.bw * b.bh;
+#pragma unroll 1
   for (int t = threadIdx.x; t < n; t += blockDim.x) {
     const int i = b.gi0 + t % b.bw, j = b.gj0 + t / b.bw;
     float r = 0.0f;
@@ -178,26 +194,26 @@ __device__ void mixed_residual(const Dev &d, const MixedBox &b, const double *p)
       const double ap = p[o - d.ld] + p[o - 1] + p[o + 1] + p[o + d.ld] - 4.0 * p[o];
       r = (float)(d.pb[o] - ap);
     }
-    const int c = (i + j) & 1, x = b.at(i, j);
+    const int c = (i + j) & 1, x = (j - b.gj0) * b.hw + ((i - b.gi0) >> 1);
     b.R[c][x] = r;
     b.E[c][x] = 0.0f;
   }
 }
 
 // p += e on the own tile, FP64.
-__device__ void mixed_correct(const Dev &d, const MixedBox &b, double *p) {
+__device__ __noinline__ void mixed_correct(const Dev &d, const MixedBox &b, double *p) {
   const int tw = b.oi1 - b.oi0 + 1, th = b.oj1 - b.oj0 + 1;
   for (int t = threadIdx.x; t < tw * th; t += blockDim.x) {
     const int i = b.oi0 + t % tw, j = b.oj0 + t / tw;
     const size_t o = IX(d, i, j);
-    p[o] = p[o] + (double)b.E[(i + j) & 1][b.at(i, j)];
+    p[o] = p[o] + (double)b.E[(i + j) & 1][(j - b.gj0) * b.hw + ((i - b.gi0) >> 1)];
   }
 }
 
 // The halo ring from the neighbours' bands: box rows [0,H) and [H+ty,bh)
 // whole, rows [H,H+ty) the K floats at either end of each colour row.
 template <int K>
-__device__ void mixed_ring_load(const MixedGeom &g, const MixedBox &b, const float *G) {
+__device__ __noinline__ void mixed_ring_load(const MixedGeom &g, const MixedBox &b, const float *G) {
   constexpr int H = 2 * K, KV = K / 4;
   const int hv = b.hw / 4;                       // float4 per colour row
   const int n_full = 2 * H * hv, n_side = g.ty * 2 * KV;
@@ -239,7 +255,7 @@ __device__ void mixed_ring_load(const MixedGeom &g, const MixedBox &b, const flo
 
 // The tile's band within H of its edge to the exchange buffer.
 template <int K>
-__device__ void mixed_band_store(const MixedGeom &g, const MixedBox &b, float *G) {
+__device__ __noinline__ void mixed_band_store(const MixedGeom &g, const MixedBox &b, float *G) {
   constexpr int H = 2 * K, KV = K / 4;
   const int tv = g.tx / 8;  // float4 per colour row of the tile
   const int total = 2 * g.ty * tv;
@@ -257,29 +273,34 @@ __device__ void mixed_band_store(const MixedGeom &g, const MixedBox &b, float *G
   }
 }
 
+// Shared-memory plane copy (both colours), 16-byte vectors.
+__device__ __noinline__ void mixed_copy_planes(const MixedBox &b, float *dst0, float *dst1,
+                                               const float *src0, const float *src1) {
+  const int n4 = b.bh * b.hw / 4;
+  float4 *d0 = reinterpret_cast<float4 *>(dst0), *d1 = reinterpret_cast<float4 *>(dst1);
+  const float4 *s0 = reinterpret_cast<const float4 *>(src0);
+  const float4 *s1 = reinterpret_cast<const float4 *>(src1);
+  for (int t = threadIdx.x; t < n4; t += blockDim.x) {
+    d0[t] = s0[t];
+    d1[t] = s1[t];
+  }
+}
+
 // One group of ns sweeps: ring (not in the first group of a pass, when e is
 // still zero everywhere), snapshot, sweeps, band, per-sweep block maxima.
 template <int K>
-__device__ void mixed_group(const MixedGeom &g, const MixedBox &b, const unsigned int *pt,
-                            int ns, float relax, const float *ein, float *eout,
-                            unsigned long long *slots) {
+__device__ __forceinline__ void mixed_group(const MixedGeom &g, const MixedBox &b, int ns,
+                                            float relax, const float *ein, float *eout,
+                                            unsigned long long *slots) {
   __shared__ unsigned int redm[K][32];
   if (ein) {
     mixed_ring_load<K>(g, b, ein);
     __syncthreads();
   }
-  {
-    const int n4 = b.bh * b.hw / 4;
-    float4 *e0 = reinterpret_cast<float4 *>(b.E[0]), *e1 = reinterpret_cast<float4 *>(b.E[1]);
-    float4 *s0 = reinterpret_cast<float4 *>(b.E0[0]), *s1 = reinterpret_cast<float4 *>(b.E0[1]);
-    for (int t = threadIdx.x; t < n4; t += blockDim.x) {
-      s0[t] = e0[t];
-      s1[t] = e1[t];
-    }
-  }
+  mixed_copy_planes(b, b.E0[0], b.E0[1], b.E[0], b.E[1]);
   for (int t = threadIdx.x; t < K * 32; t += blockDim.x) redm[t / 32][t % 32] = 0u;
   __syncthreads();
-  mixed_sweeps<K>(b, pt, g.P, ns, relax, redm);
+  mixed_sweeps<K>(b, ns, relax, redm);
   mixed_band_store<K>(g, b, eout);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
   for (int s = wid; s < ns; s += nw) {
@@ -293,24 +314,25 @@ __device__ void mixed_group(const MixedGeom &g, const MixedBox &b, const unsigne
 // Back to the snapshot taken at the start of the last group, then ns sweeps:
 // the state after sweep ns when the stopping rule fired inside a group.
 template <int K>
-__device__ void mixed_redo(const MixedGeom &g, const MixedBox &b, const unsigned int *pt, int ns,
-                           float relax) {
-  const int n4 = b.bh * b.hw / 4;
-  float4 *e0 = reinterpret_cast<float4 *>(b.E[0]), *e1 = reinterpret_cast<float4 *>(b.E[1]);
-  const float4 *s0 = reinterpret_cast<const float4 *>(b.E0[0]);
-  const float4 *s1 = reinterpret_cast<const float4 *>(b.E0[1]);
-  for (int t = threadIdx.x; t < n4; t += blockDim.x) {
-    e0[t] = s0[t];
-    e1[t] = s1[t];
-  }
+__device__ __forceinline__ void mixed_redo(const MixedBox &b, int ns, float relax) {
+  mixed_copy_planes(b, b.E[0], b.E[1], b.E0[0], b.E0[1]);
   __syncthreads();
-  mixed_sweeps<K>(b, pt, g.P, ns, relax, nullptr);
+  mixed_sweeps<K>(b, ns, relax, nullptr);
 }
 
-// Bytes of dynamic shared memory for a tile of tx x ty unknowns.
+// Bytes of dynamic shared memory for a tile of tx x ty unknowns: the two
+// colour planes of e, their snapshot and the two planes of r.
 __host__ __device__ inline size_t mixed_smem_bytes(int K, int tx, int ty) {
   const size_t bw = (size_t)tx + 4 * K, bh = (size_t)ty + 4 * K;
   return 6 * bh * (bw / 2) * sizeof(float);
+}
+
+// Threads of a block for a tile of tx x ty unknowns: whole warps over the
+// plane columns times strips of kMixedRows rows over the box rows 1..bh-2.
+__host__ __device__ inline int mixed_threads(int K, int tx, int ty) {
+  const int hw = tx / 2 + 2 * K, hwp = (hw + 31) / 32 * 32;
+  const int rows = ty + 4 * K - 2;
+  return hwp * ((rows + kMixedRows - 1) / kMixedRows);
 }
 
 // The whole mixed Ppe: Divergence and b = div/dk in FP64, then refinement
@@ -352,11 +374,18 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
     b.R[0] = fs + 4 * plane;
     b.R[1] = fs + 5 * plane;
   }
-  unsigned int pt[kMixedPmax];
-#pragma unroll
-  for (int q = 0; q < kMixedPmax; ++q)
-    pt[q] = (has && q < g.P) ? mixed_position(d, b, (int)threadIdx.x + q * (int)blockDim.x, H)
-                             : mixed_unused(b);
+  b.k = (int)threadIdx.x % g.hwp;
+  b.lane = (int)threadIdx.x & 31;
+  b.jj0 = 1 + ((int)threadIdx.x / g.hwp) * kMixedRows;
+  b.dcol0 = b.k < b.hw ? mixed_dcol(d, b, 2 * b.k, H) : 0;
+  b.dcol1 = b.k < b.hw ? mixed_dcol(d, b, 2 * b.k + 1, H) : 0;
+  b.own0 = b.dcol0 >= H;
+  b.own1 = b.dcol1 >= H;
+  b.wedge = b.lane == 0 && b.k >= 1 && b.k < b.hw;
+  b.eedge = b.lane == 31 && b.k + 1 < b.hw;
+  b.vrow = 0u;
+  for (int r = 0; r < kMixedRows; ++r)
+    if (mixed_drow(d, b, b.jj0 + r, H) > 0) b.vrow |= 1u << r;
 
   int m = 0, result = 0, grp = 0;
   bool done = false;
@@ -373,7 +402,7 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
       }
       const float *ein = q == 0 ? nullptr : ((q & 1) ? a.xbuf0 : a.xbuf1);
       float *eout = (q & 1) ? a.xbuf1 : a.xbuf0;
-      if (has) mixed_group<K>(g, b, pt, ns, a.relax, ein, eout, slots);
+      if (has) mixed_group<K>(g, b, ns, a.relax, ein, eout, slots);
       if (!grid_sync(sy)) return -1;
       int conv = -1;
       for (int s = 0; s < ns; ++s) {
@@ -386,7 +415,7 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
       ++q;
       if (conv >= 0) {
         result = m + conv + 1;
-        if (has && conv < ns - 1) mixed_redo<K>(g, b, pt, conv + 1, a.relax);
+        if (has && conv < ns - 1) mixed_redo<K>(b, conv + 1, a.relax);
         done = true;
         break;
       }
