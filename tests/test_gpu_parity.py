@@ -215,3 +215,25 @@ def test_tiled_time_loop_512():
     u, v, p = s.store_fields()
     for name, g in (("u", u), ("v", v), ("p", p)):
         assert np.array_equal(g, ref.f[name]), (name, rel_err(g, ref.f[name]))
+
+
+@pytest.mark.parametrize("seg,warm", [(8, 1), (13, 4), (27, 64), (97, 2), (4096, 64)])
+def test_chain_segments_exact(seg, warm):
+    """nAuxMomentum bit-identical for segment lengths that do and do not
+    divide the chains and for warm-ups short enough to need several
+    verification rounds (segment-interleaved chain storage)."""
+    case = deck.channel(48, 16, 500.0, 0.004, length=3.0, solver="rb_sor")
+    o, met = oracle_setup(case)
+    s = Solver.for_case(case)
+    s.tune(seg=seg, warm=warm)
+    f = fields_for(case, 21, amp=0.2)
+    un, vn = f["u"], f["v"]
+    o.vel_bound_cond(case.nx, case.ny, case.regions, un, vn)
+    us, vs = un.copy(order="F"), vn.copy(order="F")
+    gus, gvs = us.copy(order="F"), vs.copy(order="F")
+    z = o.field()
+    prm = case.params
+    n_o = o.naux_momentum(case.nx, case.ny, case.regions, prm, met, z, z, un, vn, us, vs)
+    n_g = s.nAuxMomentum(prm.mqiter, prm.dk, prm.re, prm.fr, prm.qtol, None, None, un, vn, gus, gvs)
+    assert n_g == n_o
+    assert np.array_equal(gus, us) and np.array_equal(gvs, vs)

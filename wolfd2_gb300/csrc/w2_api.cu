@@ -61,6 +61,16 @@ struct w2_ctx {
   // single-precision momentum state (mixed path), made on first use
   bool f32_alloc = false, f32_metrics_ok = false;
   float *F32[4] = {};  // un, vn, us, vs
+  // split-2 identity rows in chain order, and their by-position device copies
+  std::vector<uint8_t> zx, zy;
+  uint8_t *bzx = nullptr, *bzy = nullptr;
+  // how each momentum metric is read (full array, profile over i or j)
+  struct MomMetric {
+    int mode = 0;          // MP_FULL, MP_I, MP_J
+    std::vector<double> host;  // the profile (MP_I: over i, MP_J: over j)
+    double *p64 = nullptr;     // device profile, FP64
+    float *p32 = nullptr;      // device profile or full array, FP32
+  } mm[24];
 };
 
 namespace {
@@ -109,6 +119,20 @@ void bind_metrics(w2_ctx *c) {
   m.xec = a[M_XEC]; m.yec = a[M_YEC]; m.xzc = a[M_XZC]; m.yzc = a[M_YZC];
   m.xeu = a[M_XEU]; m.yeu = a[M_YEU]; m.xzv = a[M_XZV]; m.yzv = a[M_YZV];
   m.xzu = a[M_XZU]; m.yzu = a[M_YZU]; m.xev = a[M_XEV]; m.yev = a[M_YEV];
+}
+
+// The 24 metric arrays the momentum stencils read, in MomView order.
+const int kMomMetric[24] = {M_YEU, M_XEU, M_XZU, M_YZU, M_YEC, M_XEC, M_XZN, M_YZN,
+                            M_YEV, M_XEV, M_XZV, M_YZV, M_YEN, M_XEN, M_XZC, M_YZC,
+                            M_DJU, M_DJV, M_RAC, M_RBC, M_RBN, M_RGN, M_RAN, M_RGC};
+enum { MP_FULL = 0, MP_I = 1, MP_J = 2 };
+
+// The 24 metric references of a momentum view, in MomView order.
+template <class T>
+std::vector<MRef<T> *> mom_refs(MomView<T> &v) {
+  return {&v.yeu, &v.xeu, &v.xzu, &v.yzu, &v.yec, &v.xec, &v.xzn, &v.yzn,
+          &v.yev, &v.xev, &v.xzv, &v.yzv, &v.yen, &v.xen, &v.xzc, &v.yzc,
+          &v.dju, &v.djv, &v.rac, &v.rbc, &v.rbn, &v.rgn, &v.ran, &v.rgc};
 }
 
 // Host replay of the reference's region loops into per-cell mask bits.
@@ -280,16 +304,21 @@ int check_sync(w2_ctx *c) {
 }
 
 // Chain buffers for a chain of n rows.
+// Rows of chain storage: segment-interleaved positions run up to
+// L*nseg - 1 < n + L, and L is at most kMaxSeg.
+constexpr int kMaxSeg = 4096;
+
 template <class T>
 int make_chain(w2_ctx *c, ChainT<T> &ch, int n, bool with_b) {
+  const size_t cap = (size_t)n + kMaxSeg;
   ch.n = n;
-  ch.a1 = dalloc<T>(c, n);
-  ch.a2 = dalloc<T>(c, n);
-  ch.a3 = dalloc<T>(c, n);
-  ch.b = with_b ? dalloc<T>(c, n) : nullptr;
-  ch.a3p = dalloc<T>(c, n);
-  ch.bp = dalloc<T>(c, n);
-  ch.x = dalloc<T>(c, n);
+  ch.a1 = dalloc<T>(c, cap);
+  ch.a2 = dalloc<T>(c, cap);
+  ch.a3 = dalloc<T>(c, cap);
+  ch.b = with_b ? dalloc<T>(c, cap) : nullptr;
+  ch.a3p = dalloc<T>(c, cap);
+  ch.bp = dalloc<T>(c, cap);
+  ch.x = dalloc<T>(c, cap);
   ch.bzero = nullptr;
   // end-state buffers, sized for the smallest segment length allowed (8)
   const int ms = (n + 7) / 8;
@@ -301,21 +330,49 @@ int make_chain(w2_ctx *c, ChainT<T> &ch, int n, bool with_b) {
   return W2_OK;
 }
 
+// Split-2 chain in the storage of split 1: its rows are assembled after the
+// split-1 solve, whose rows and forward states are dead by then; its
+// right-hand side is the split-1 solution; only the solution is its own.
+template <class T>
+int alias_split2(w2_ctx *c, ChainT<T> &c2, const ChainT<T> &c1) {
+  c2.n = c1.n;
+  c2.a1 = c1.a1; c2.a2 = c1.a2; c2.a3 = c1.a3;
+  c2.a3p = c1.a3p; c2.bp = c1.bp;
+  c2.ef = c1.ef; c2.eb = c1.eb;
+  c2.b = c1.x;
+  c2.x = dalloc<T>(c, (size_t)c1.n + kMaxSeg);
+  if (!c2.x) return fail(c, W2_E_CUDA, "out of device memory (chains)");
+  return W2_OK;
+}
+
 int set_segments(w2_ctx *c) {
   Dev &d = c->dev;
   const int nX = c->nx * (c->ny - 1), nY = (c->nx - 1) * c->ny;
   int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny);
   long threads = (long)blocks * c->threads;
   int seg = c->seg_req > 0 ? c->seg_req : (int)std::max<long>(8, (nX + nY + threads - 1) / threads);
-  seg = std::min(seg, 4096);
+  seg = std::min(seg, kMaxSeg);
   d.seg = seg;
   d.warm = c->warm_req > 0 ? c->warm_req : 64;
-  auto setn = [&](Chain &ch, int n) {
-    ch.nseg = (n + seg - 1) / seg;
-  };
-  setn(d.x1, nX); setn(d.x2, nX); setn(d.y1, nY); setn(d.y2, nY);
-  d.f32.x1.nseg = d.x1.nseg; d.f32.x2.nseg = d.x2.nseg;
-  d.f32.y1.nseg = d.y1.nseg; d.f32.y2.nseg = d.y2.nseg;
+  const int nsx = (nX + seg - 1) / seg, nsy = (nY + seg - 1) / seg;
+  ChainT<double> *c64[] = {&d.x1, &d.x2, &d.y1, &d.y2, &d.f64.x1, &d.f64.x2, &d.f64.y1, &d.f64.y2};
+  ChainT<float> *c32[] = {&d.f32.x1, &d.f32.x2, &d.f32.y1, &d.f32.y2};
+  for (int k = 0; k < 8; ++k) {
+    c64[k]->L = seg;
+    c64[k]->nseg = (k % 4) < 2 ? nsx : nsy;
+  }
+  for (int k = 0; k < 4; ++k) {
+    c32[k]->L = seg;
+    c32[k]->nseg = k < 2 ? nsx : nsy;
+  }
+  // split-2 identity rows, stored by position for this segment length
+  if (c->bzx && c->bzy) {
+    std::vector<uint8_t> px((size_t)nX + kMaxSeg, 0), py((size_t)nY + kMaxSeg, 0);
+    for (int t = 0; t < nX; ++t) px[(size_t)(t % seg) * nsx + t / seg] = c->zx[t];
+    for (int t = 0; t < nY; ++t) py[(size_t)(t % seg) * nsy + t / seg] = c->zy[t];
+    CK(cudaMemcpy(c->bzx, px.data(), px.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->bzy, py.data(), py.size(), cudaMemcpyHostToDevice));
+  }
   // end-state buffers, sized for the smallest segment length we allow (8)
   return W2_OK;
 }
@@ -431,51 +488,103 @@ int launch_ppe_tiled(w2_ctx *c, int lcartes, int msorit, double dk, double sorto
 
 int grid_blocks(w2_ctx *c);
 
-// FP32 copies of the metric arrays the momentum stencils read, FP32 work
-// arrays and chains (the split-2 identity rows shared with the FP64 chains)
-// and the FP32 fields; allocated on the first mixed step, the metrics
-// re-rounded whenever new ones are uploaded.
+// FP32 forms of the momentum metrics (profiles where the FP64 ones are,
+// rounded full arrays otherwise), FP32 chains (split 2 in the storage of
+// split 1, the identity rows shared with the FP64 chains) and the FP32
+// fields; allocated on the first mixed step, the metrics re-rounded whenever
+// new ones are uploaded.  The FP32 path forms ConvCoef values where it uses
+// them, so it has no ConvCoef arrays.
 int ensure_f32(w2_ctx *c) {
   Dev &d = c->dev;
   MomView<float> &v = d.f32;
-  const Metrics &m = d.m;
-  const double *src[] = {m.yeu, m.xeu, m.xzu, m.yzu, m.yec, m.xec, m.xzn, m.yzn,
-                         m.yev, m.xev, m.xzv, m.yzv, m.yen, m.xen, m.xzc, m.yzc,
-                         m.dju, m.djv, m.rac, m.rbc, m.rbn, m.rgn, m.ran, m.rgc};
-  const float **dst[] = {&v.yeu, &v.xeu, &v.xzu, &v.yzu, &v.yec, &v.xec, &v.xzn, &v.yzn,
-                         &v.yev, &v.xev, &v.xzv, &v.yzv, &v.yen, &v.xen, &v.xzc, &v.yzc,
-                         &v.dju, &v.djv, &v.rac, &v.rbc, &v.rbn, &v.rgn, &v.ran, &v.rgc};
   if (!c->f32_alloc) {
-    for (const float **p : dst)
-      if (!(*p = dalloc<float>(c, c->nf))) return fail(c, W2_E_CUDA, "out of device memory (FP32 metrics)");
-    float **wa[] = {&v.cj1x, &v.cj2x, &v.c1sx, &v.c2sx, &v.c1nx, &v.c2nx,
-                    &v.cj1y, &v.cj2y, &v.c1sy, &v.c2sy, &v.c1ny, &v.c2ny};
-    for (float **p : wa)
-      if (!(*p = dalloc<float>(c, c->nf))) return fail(c, W2_E_CUDA, "out of device memory (FP32 work)");
     for (int k = 0; k < 4; ++k)
       if (!(c->F32[k] = dalloc<float>(c, c->nf))) return fail(c, W2_E_CUDA, "out of device memory (FP32 fields)");
     const int nX = c->nx * (c->ny - 1), nY = (c->nx - 1) * c->ny;
     int rc;
-    if ((rc = make_chain(c, v.x1, nX, true)) || (rc = make_chain(c, v.x2, nX, false)) ||
-        (rc = make_chain(c, v.y1, nY, true)) || (rc = make_chain(c, v.y2, nY, false)))
+    if ((rc = make_chain(c, v.x1, nX, true)) || (rc = alias_split2(c, v.x2, v.x1)) ||
+        (rc = make_chain(c, v.y1, nY, true)) || (rc = alias_split2(c, v.y2, v.y1)))
       return rc;
-    v.x2.b = v.x1.x;
-    v.y2.b = v.y1.x;
     v.x2.bzero = d.x2.bzero;
     v.y2.bzero = d.y2.bzero;
     v.x1.nseg = d.x1.nseg; v.x2.nseg = d.x2.nseg;
     v.y1.nseg = d.y1.nseg; v.y2.nseg = d.y2.nseg;
+    v.x1.L = v.x2.L = v.y1.L = v.y2.L = d.seg;
     c->f32_alloc = true;
   }
   if (!c->f32_metrics_ok) {
+    std::vector<MRef<float> *> refs = mom_refs(v);
     const int gb = grid_blocks(c);
     for (int k = 0; k < 24; ++k) {
-      k_to_f32<<<gb, c->threads, 0, c->st>>>(d, src[k], const_cast<float *>(*dst[k]));
-      c->launches++;
+      w2_ctx::MomMetric &mm = c->mm[k];
+      if (mm.mode == MP_FULL) {
+        if (!mm.p32 && !(mm.p32 = dalloc<float>(c, c->nf)))
+          return fail(c, W2_E_CUDA, "out of device memory (FP32 metrics)");
+        k_to_f32<<<gb, c->threads, 0, c->st>>>(d, c->met[kMomMetric[k]], mm.p32);
+        c->launches++;
+        *refs[k] = MRef<float>{mm.p32, 1, c->ld};
+      } else {
+        std::vector<float> h(mm.host.size());
+        for (size_t q = 0; q < h.size(); ++q) h[q] = (float)mm.host[q];
+        if (!mm.p32 && !(mm.p32 = dalloc<float>(c, h.size())))
+          return fail(c, W2_E_CUDA, "out of device memory (FP32 metrics)");
+        CK(cudaMemcpy(mm.p32, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+        *refs[k] = mm.mode == MP_I ? MRef<float>{mm.p32, 1, 0} : MRef<float>{mm.p32, 0, 1};
+      }
     }
     CK(cudaGetLastError());
     c->f32_metrics_ok = true;
   }
+  return W2_OK;
+}
+
+// How the momentum stencils read each metric: an array whose value depends
+// on i only (every column identical, bit for bit, over the stored extent) is
+// read as a profile over i, one that depends on j only as a profile over j,
+// anything else in full.  Cartesian grids reduce to profiles, so the
+// stencils stream no metric arrays.  Fills the FP64 view; the FP32 view
+// follows on the next mixed step.
+int momentum_metrics(w2_ctx *c) {
+  Dev &d = c->dev;
+  const int W = c->nx + 2, H = c->ny + 2;
+  const size_t ld = c->ld;
+  std::vector<double> h(c->nf);
+  std::vector<MRef<double> *> refs = mom_refs(d.f64);
+  CK(cudaStreamSynchronize(c->st));
+  for (int k = 0; k < 24; ++k) {
+    const double *src = c->met[kMomMetric[k]];
+    CK(cudaMemcpy(h.data(), src, c->nf * sizeof(double), cudaMemcpyDeviceToHost));
+    auto bits = [&](size_t o) {
+      uint64_t b;
+      memcpy(&b, &h[o], 8);
+      return b;
+    };
+    bool ionly = true, jonly = true;
+    for (int j = 0; j < H && (ionly || jonly); ++j)
+      for (int i = 0; i < W; ++i) {
+        const uint64_t b = bits((size_t)i + (size_t)j * ld);
+        if (ionly && b != bits((size_t)i)) ionly = false;
+        if (jonly && b != bits((size_t)j * ld)) jonly = false;
+      }
+    w2_ctx::MomMetric &mm = c->mm[k];
+    mm.mode = ionly ? MP_I : (jonly ? MP_J : MP_FULL);
+    if (mm.mode == MP_FULL) {
+      mm.host.clear();
+      *refs[k] = MRef<double>{src, 1, (int)ld};
+      continue;
+    }
+    const int len = mm.mode == MP_I ? W : H;
+    mm.host.resize(len);
+    for (int q = 0; q < len; ++q) mm.host[q] = mm.mode == MP_I ? h[q] : h[(size_t)q * ld];
+    if (!mm.p64 && !(mm.p64 = dalloc<double>(c, std::max(W, H))))
+      return fail(c, W2_E_CUDA, "out of device memory (metric profiles)");
+    CK(cudaMemcpy(mm.p64, mm.host.data(), len * sizeof(double), cudaMemcpyHostToDevice));
+    *refs[k] = mm.mode == MP_I ? MRef<double>{mm.p64, 1, 0} : MRef<double>{mm.p64, 0, 1};
+  }
+  // an FP32 buffer was sized for the previous mode (profile or full array):
+  // ensure_f32 makes new ones
+  for (int k = 0; k < 24; ++k) c->mm[k].p32 = nullptr;
+  c->f32_metrics_ok = false;
   return W2_OK;
 }
 
@@ -678,24 +787,30 @@ int wolfd2gpu_create(w2_ctx **out, int mnx, int mny, int mgri, int mgrj, int nx,
   for (double **w : wa)
     if (!(*w = dalloc<double>(c, c->nf))) return bad(W2_E_CUDA);
   const int nX = nx * (ny - 1), nY = (nx - 1) * ny;
-  if (make_chain(c, d.x1, nX, true) || make_chain(c, d.x2, nX, false) ||
-      make_chain(c, d.y1, nY, true) || make_chain(c, d.y2, nY, false))
+  if (make_chain(c, d.x1, nX, true) || alias_split2(c, d.x2, d.x1) ||
+      make_chain(c, d.y1, nY, true) || alias_split2(c, d.y2, d.y1))
     return bad(W2_E_CUDA);
-  // split-2 rhs = split-1 solution, zero on identity rows
-  d.x2.b = d.x1.x;
-  d.y2.b = d.y1.x;
   {
-    std::vector<uint8_t> zx(nX), zy(nY);
+    // split-2 identity rows in chain order; set_segments stores them by position
+    c->zx.assign(nX, 0);
+    c->zy.assign(nY, 0);
     for (int j = 2; j <= ny; ++j)
-      for (int i = 1; i <= nx; ++i) zx[(j - 2) * nx + i - 1] = (mk[i + (size_t)j * c->ld] & MK_XID) ? 1 : 0;
+      for (int i = 1; i <= nx; ++i) c->zx[(j - 2) * nx + i - 1] = (mk[i + (size_t)j * c->ld] & MK_XID) ? 1 : 0;
     for (int j = 1; j <= ny; ++j)
-      for (int i = 2; i <= nx; ++i) zy[(j - 1) * (nx - 1) + i - 2] = (mk[i + (size_t)j * c->ld] & MK_YID) ? 1 : 0;
-    uint8_t *dzx = dalloc<uint8_t>(c, nX), *dzy = dalloc<uint8_t>(c, nY);
-    if (!dzx || !dzy) return bad(W2_E_CUDA);
-    cudaMemcpy(dzx, zx.data(), nX, cudaMemcpyHostToDevice);
-    cudaMemcpy(dzy, zy.data(), nY, cudaMemcpyHostToDevice);
-    d.x2.bzero = dzx;
-    d.y2.bzero = dzy;
+      for (int i = 2; i <= nx; ++i) c->zy[(j - 1) * (nx - 1) + i - 2] = (mk[i + (size_t)j * c->ld] & MK_YID) ? 1 : 0;
+    c->bzx = dalloc<uint8_t>(c, (size_t)nX + kMaxSeg);
+    c->bzy = dalloc<uint8_t>(c, (size_t)nY + kMaxSeg);
+    if (!c->bzx || !c->bzy) return bad(W2_E_CUDA);
+    d.x2.bzero = c->bzx;
+    d.y2.bzero = c->bzy;
+  }
+  d.f64.cj1x = d.cj1x; d.f64.cj2x = d.cj2x; d.f64.c1sx = d.c1sx; d.f64.c2sx = d.c2sx;
+  d.f64.c1nx = d.c1nx; d.f64.c2nx = d.c2nx; d.f64.cj1y = d.cj1y; d.f64.cj2y = d.cj2y;
+  d.f64.c1sy = d.c1sy; d.f64.c2sy = d.c2sy; d.f64.c1ny = d.c1ny; d.f64.c2ny = d.c2ny;
+  d.f64.x1 = d.x1; d.f64.x2 = d.x2; d.f64.y1 = d.y1; d.f64.y2 = d.y2;
+  {
+    std::vector<MRef<double> *> refs = mom_refs(d.f64);
+    for (int k = 0; k < 24; ++k) *refs[k] = MRef<double>{c->met[kMomMetric[k]], 1, (int)c->ld};
   }
   d.sync = dalloc<Sync>(c, 1);
   c->d_out = dalloc<StepOut>(c, 1);
@@ -794,7 +909,7 @@ static int finish_coefficients(w2_ctx *c) {
   c->dev.ppe_unit = (h == 0) ? 1 : 0;
   plan_tiles(c);
   plan_mixed(c);
-  return W2_OK;
+  return momentum_metrics(c);
 }
 
 int wolfd2gpu_set_precision(w2_ctx *c, int precision, int refine_sweeps) {

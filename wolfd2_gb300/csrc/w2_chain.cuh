@@ -7,7 +7,9 @@
 // so a per-line solve would change the numbers.
 //
 // This solver reproduces the sequential recurrence bit for bit with parallel
-// work.  The chain is cut into segments of `seg` rows, one thread each:
+// work.  The chain is cut into segments of L rows, one thread each, and
+// stored segment-interleaved (row r of segment s at r*nseg + s) so that a
+// warp's loads at every step of the walks are consecutive words:
 //   F1  every segment runs the forward recurrence (factorisation + forward
 //       substitution, state (a3', b')) starting `warm` rows early from the
 //       state (0, 0), so by its first own row the state has usually converged
@@ -37,55 +39,92 @@ __device__ __forceinline__ bool same_bits(float a, float b) {
   return __float_as_int(a) == __float_as_int(b);
 }
 
+// Storage position of chain row k: row r of segment s lives at r*nseg + s,
+// so the threads of a warp, one segment each, touch consecutive words at
+// every step of their walks.
 template <class T>
-__device__ __forceinline__ T chain_rhs(const ChainT<T> &c, int k) {
-  return (c.bzero != nullptr && c.bzero[k]) ? T(0) : c.b[k];
+__device__ __forceinline__ int cpos(const ChainT<T> &c, int k) {
+  const int s = k / c.L;
+  return (k - s * c.L) * c.nseg + s;
 }
 
-// One forward row k >= 1 of AltTridLU: a2' = a2 - a1 a3'(k-1); a3' = a3/a2'
-// (not formed on the last row); b' = (b - a1 b'(k-1)) / a2'.
+// A walk over consecutive chain rows with their storage positions.
+struct RowWalk {
+  int k, r, s, p;
+  __device__ __forceinline__ RowWalk(int k0, int L, int nseg)
+      : k(k0), r(k0 % L), s(k0 / L), p((k0 % L) * nseg + k0 / L) {}
+  __device__ __forceinline__ void next(int L, int nseg) {
+    ++k;
+    if (++r == L) {
+      r = 0;
+      p = ++s;
+    } else {
+      p += nseg;
+    }
+  }
+  __device__ __forceinline__ void prev(int L, int nseg) {
+    --k;
+    if (--r < 0) {
+      r = L - 1;
+      --s;
+      p = r * nseg + s;
+    } else {
+      p -= nseg;
+    }
+  }
+};
+
 template <class T>
-__device__ __forceinline__ void fwd_row(const ChainT<T> &c, int k, T &a3p, T &bp) {
-  const T a1 = c.a1[k];
-  const T a2p = c.a2[k] - a1 * a3p;
-  const T nb = (chain_rhs(c, k) - a1 * bp) / a2p;
-  a3p = (k < c.n - 1) ? c.a3[k] / a2p : T(0);
+__device__ __forceinline__ T chain_rhs(const ChainT<T> &c, int p) {
+  return (c.bzero != nullptr && c.bzero[p]) ? T(0) : c.b[p];
+}
+
+// One forward row k >= 1 (stored at p) of AltTridLU: a2' = a2 - a1 a3'(k-1);
+// a3' = a3/a2' (not formed on the last row); b' = (b - a1 b'(k-1)) / a2'.
+template <class T>
+__device__ __forceinline__ void fwd_row(const ChainT<T> &c, int k, int p, T &a3p, T &bp) {
+  const T a1 = c.a1[p];
+  const T a2p = c.a2[p] - a1 * a3p;
+  const T nb = (chain_rhs(c, p) - a1 * bp) / a2p;
+  a3p = (k < c.n - 1) ? c.a3[p] / a2p : T(0);
   bp = nb;
 }
 
 // Row 0 with the reference's first-row quirk.
 template <class T>
 __device__ __forceinline__ void fwd_row0(const ChainT<T> &c, T &a3p, T &bp) {
-  a3p = c.a3[0] / c.a2[1];
+  a3p = c.a3[0] / c.a2[cpos(c, 1)];
   bp = chain_rhs(c, 0) / c.a2[0];
 }
 
 template <class T>
 __device__ void chain_f1(const ChainT<T> &c, int s, int L, int W) {
-  const int k0 = s * L, k1 = min(c.n, k0 + L);
+  const int k0 = s * L, k1 = min(c.n, k0 + L), ns = c.nseg;
   T a3p, bp;
-  int k;
+  int k, p;
   if (k0 == 0) {
     fwd_row0(c, a3p, bp);
     c.a3p[0] = a3p;
     c.bp[0] = bp;
     k = 1;
+    p = ns;
   } else {
-    int kw = k0 - W;
+    const int kw = k0 - W;
+    RowWalk w(kw <= 0 ? 1 : kw, L, ns);
     if (kw <= 0) {
       fwd_row0(c, a3p, bp);
-      for (int q = 1; q < k0; ++q) fwd_row(c, q, a3p, bp);
     } else {
       a3p = T(0);
       bp = T(0);
-      for (int q = kw; q < k0; ++q) fwd_row(c, q, a3p, bp);
     }
+    for (; w.k < k0; w.next(L, ns)) fwd_row(c, w.k, w.p, a3p, bp);
     k = k0;
+    p = s;
   }
-  for (; k < k1; ++k) {
-    fwd_row(c, k, a3p, bp);
-    c.a3p[k] = a3p;
-    c.bp[k] = bp;
+  for (; k < k1; ++k, p += ns) {
+    fwd_row(c, k, p, a3p, bp);
+    c.a3p[p] = a3p;
+    c.bp[p] = bp;
   }
   c.ef[2 * s] = a3p;
   c.ef[2 * s + 1] = bp;
@@ -100,17 +139,17 @@ __device__ bool chain_f2(const ChainT<T> &c, int s, int L, const T *ein, T *eout
     eout[1] = ein[1];
     return false;
   }
-  const int k0 = s * L, k1 = min(c.n, k0 + L);
+  const int k0 = s * L, k1 = min(c.n, k0 + L), ns = c.nseg;
   T a3p = ein[2 * (s - 1)], bp = ein[2 * (s - 1) + 1];
-  for (int k = k0; k < k1; ++k) {
-    fwd_row(c, k, a3p, bp);
-    if (same_bits(a3p, c.a3p[k]) && same_bits(bp, c.bp[k])) {
+  for (int k = k0, p = s; k < k1; ++k, p += ns) {
+    fwd_row(c, k, p, a3p, bp);
+    if (same_bits(a3p, c.a3p[p]) && same_bits(bp, c.bp[p])) {
       eout[2 * s] = ein[2 * s];
       eout[2 * s + 1] = ein[2 * s + 1];
       return false;
     }
-    c.a3p[k] = a3p;
-    c.bp[k] = bp;
+    c.a3p[p] = a3p;
+    c.bp[p] = bp;
   }
   eout[2 * s] = a3p;
   eout[2 * s + 1] = bp;
@@ -119,46 +158,49 @@ __device__ bool chain_f2(const ChainT<T> &c, int s, int L, const T *ein, T *eout
 
 template <class T>
 __device__ void chain_b1(const ChainT<T> &c, int s, int L, int W) {
-  const int k0 = s * L, k1 = min(c.n, k0 + L);
+  const int k0 = s * L, k1 = min(c.n, k0 + L), ns = c.nseg;
+  const int plast = cpos(c, c.n - 1);
   T xn;
   int k;
   if (k1 == c.n) {
-    xn = c.bp[c.n - 1];
-    c.x[c.n - 1] = xn;
+    xn = c.bp[plast];
+    c.x[plast] = xn;
     k = c.n - 2;
   } else {
-    int kw = k1 - 1 + W;
+    const int kw = k1 - 1 + W;
     if (kw >= c.n - 1) {
-      xn = c.bp[c.n - 1];
-      for (int q = c.n - 2; q >= k1; --q) xn = c.bp[q] - c.a3p[q] * xn;
+      xn = c.bp[plast];
+      RowWalk w(c.n - 2, L, ns);
+      for (; w.k >= k1; w.prev(L, ns)) xn = c.bp[w.p] - c.a3p[w.p] * xn;
     } else {
       xn = T(0);
-      for (int q = kw; q >= k1; --q) xn = c.bp[q] - c.a3p[q] * xn;
+      RowWalk w(kw, L, ns);
+      for (; w.k >= k1; w.prev(L, ns)) xn = c.bp[w.p] - c.a3p[w.p] * xn;
     }
     k = k1 - 1;
   }
-  for (; k >= k0; --k) {
-    xn = c.bp[k] - c.a3p[k] * xn;
-    c.x[k] = xn;
+  for (int p = (k - k0) * ns + s; k >= k0; --k, p -= ns) {
+    xn = c.bp[p] - c.a3p[p] * xn;
+    c.x[p] = xn;
   }
-  c.eb[s] = c.x[k0];
+  c.eb[s] = c.x[s];
 }
 
 template <class T>
 __device__ bool chain_b2(const ChainT<T> &c, int s, int L, const T *ein, T *eout) {
-  const int k0 = s * L, k1 = min(c.n, k0 + L);
+  const int k0 = s * L, k1 = min(c.n, k0 + L), ns = c.nseg;
   if (k1 == c.n) {
     eout[s] = ein[s];
     return false;
   }
   T xn = ein[s + 1];
-  for (int k = k1 - 1; k >= k0; --k) {
-    xn = c.bp[k] - c.a3p[k] * xn;
-    if (same_bits(xn, c.x[k])) {
+  for (int k = k1 - 1, p = (k1 - 1 - k0) * ns + s; k >= k0; --k, p -= ns) {
+    xn = c.bp[p] - c.a3p[p] * xn;
+    if (same_bits(xn, c.x[p])) {
       eout[s] = ein[s];
       return false;
     }
-    c.x[k] = xn;
+    c.x[p] = xn;
   }
   eout[s] = xn;
   return true;
@@ -176,18 +218,19 @@ __device__ void chain_sequential_warp(const ChainT<T> &c, bool forward) {
     T a3p = T(0), bp = T(0);
     for (int base = 0; base < c.n; base += 32) {
       const int k = base + lane, cnt = min(32, c.n - base);
+      const int p = k < c.n ? cpos(c, k) : 0;
       if (k < c.n) {
-        s1[lane] = c.a1[k];
-        s2[lane] = c.a2[k];
-        s3[lane] = c.a3[k];
-        sb[lane] = chain_rhs(c, k);
+        s1[lane] = c.a1[p];
+        s2[lane] = c.a2[p];
+        s3[lane] = c.a3[p];
+        sb[lane] = chain_rhs(c, p);
       }
       __syncwarp();
       if (lane == 0) {
         for (int q = 0; q < cnt; ++q) {
           const int kk = base + q;
           if (kk == 0) {
-            a3p = s3[0] / c.a2[1];
+            a3p = s3[0] / c.a2[cpos(c, 1)];
             bp = sb[0] / s2[0];
           } else {
             const T a1 = s1[q];
@@ -202,8 +245,8 @@ __device__ void chain_sequential_warp(const ChainT<T> &c, bool forward) {
       }
       __syncwarp();
       if (k < c.n) {
-        c.a3p[k] = o3[lane];
-        c.bp[k] = ob[lane];
+        c.a3p[p] = o3[lane];
+        c.bp[p] = ob[lane];
       }
       __syncwarp();
     }
@@ -211,9 +254,10 @@ __device__ void chain_sequential_warp(const ChainT<T> &c, bool forward) {
     T xn = T(0);
     for (int top = c.n - 1; top >= 0; top -= 32) {
       const int k = top - lane, cnt = min(32, top + 1);
+      const int p = k >= 0 ? cpos(c, k) : 0;
       if (k >= 0) {
-        s3[lane] = c.a3p[k];
-        sb[lane] = c.bp[k];
+        s3[lane] = c.a3p[p];
+        sb[lane] = c.bp[p];
       }
       __syncwarp();
       if (lane == 0) {
@@ -224,7 +268,7 @@ __device__ void chain_sequential_warp(const ChainT<T> &c, bool forward) {
         }
       }
       __syncwarp();
-      if (k >= 0) c.x[k] = ob[lane];
+      if (k >= 0) c.x[p] = ob[lane];
       __syncwarp();
     }
   }

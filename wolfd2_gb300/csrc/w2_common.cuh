@@ -67,23 +67,38 @@ struct Regions {
 template <class T>
 struct ChainT {
   int n;           // rows
-  int nseg;        // segments of length seg
+  int nseg;        // segments of L rows (the last may be shorter)
+  int L;           // rows per segment; row r of segment s is stored at r*nseg + s
   T *a1, *a2, *a3, *b;             // sub, diag, super, rhs
-  const uint8_t *bzero;            // rows whose rhs is forced to 0 (or null)
+  const uint8_t *bzero;            // rows whose rhs is forced to 0 (or null), by position
   T *a3p, *bp, *x;                 // factorised super, forward rhs, solution
   T *ef;           // forward end states: 2 per segment x 2 buffers
   T *eb;           // backward end states: 1 per segment x 2 buffers
 };
 using Chain = ChainT<double>;
 
+// A metric array as the momentum stencils read it: value(i, j) =
+// p[i*si + j*sj].  A full array has (si, sj) = (1, ld); an array that the
+// host found to depend on i only (every column equal, bit for bit) is a
+// profile over i with sj = 0, one that depends on j only a profile over j
+// with si = 0, a constant has si = sj = 0.  On Cartesian grids most metric
+// arrays collapse this way, so the stencils stream no metric data.
+template <class T>
+struct MRef {
+  const T *p;
+  int si, sj;
+  __device__ __forceinline__ T operator()(int i, int j) const { return p[i * si + j * sj]; }
+};
+
 // The momentum step's inputs and work arrays in one arithmetic type: the
-// metric arrays the stencils read, the ConvCoef outputs and the four chains.
+// metric arrays the stencils read, the ConvCoef outputs and the four chains
+// (split 2 reuses the storage of split 1, whose rows are dead by then).
 template <class T>
 struct MomView {
-  const T *yeu, *xeu, *xzu, *yzu, *yec, *xec, *xzn, *yzn;
-  const T *yev, *xev, *xzv, *yzv, *yen, *xen, *xzc, *yzc;
-  const T *dju, *djv, *rac, *rbc, *rbn, *rgn, *ran, *rgc;
-  T *cj1x, *cj2x, *c1sx, *c2sx, *c1nx, *c2nx;
+  MRef<T> yeu, xeu, xzu, yzu, yec, xec, xzn, yzn;
+  MRef<T> yev, xev, xzv, yzv, yen, xen, xzc, yzc;
+  MRef<T> dju, djv, rac, rbc, rbn, rgn, ran, rgc;
+  T *cj1x, *cj2x, *c1sx, *c2sx, *c1nx, *c2nx;  // ConvCoef outputs (FP64 only)
   T *cj1y, *cj2y, *c1sy, *c2sy, *c1ny, *c2ny;
   ChainT<T> x1, x2, y1, y2;
 };
@@ -123,6 +138,7 @@ struct Dev {
   double *div, *pb, *ppn;
   double *la3p, *lbp;  // line-solver scratch (field layout)
   double *qh;          // filter scratch
+  MomView<double> f64; // momentum view of the plain path
   MomView<float> f32;  // single-precision momentum (mixed path)
   Sync *sync;
   int seg, warm;       // chain segment length and warm-up rows

@@ -164,19 +164,19 @@ __global__ void k_naux_init(Dev d, const double *un, const double *vn, double *u
 }
 
 // ---- nAuxMomentum --------------------------------------------------------
-__global__ void __launch_bounds__(kMaxThreads) k_naux(Dev d, int mqiter, double dk, double re,
+__global__ void __launch_bounds__(kMaxThreads, 1) k_naux(Dev d, int mqiter, double dk, double re,
                                                       double qtol, const double *un,
                                                       const double *vn, double *us, double *vs,
                                                       StepOut *out) {
   if (d.sync->halt) return;
   int res = -1;
-  if (!naux_momentum<double>(d, mom_view64(d), mqiter, dk, re, qtol, un, vn, us, vs, &res)) return;
+  if (!naux_momentum<double>(d, d.f64, mqiter, dk, re, qtol, un, vn, us, vs, &res)) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) out->nql = res;
 }
 
 // nAuxMomentum in single precision (mixed path) on un32, vn32 -> us32, vs32,
 // then us, vs = the FP32 results widened to FP64 on every cell.
-__global__ void __launch_bounds__(kMaxThreads) k_naux32(Dev d, int mqiter, double dk, double re,
+__global__ void __launch_bounds__(kMaxThreads, 1) k_naux32(Dev d, int mqiter, double dk, double re,
                                                         double qtol, const float *un,
                                                         const float *vn, float *us, float *vs,
                                                         double *us64, double *vs64, StepOut *out) {

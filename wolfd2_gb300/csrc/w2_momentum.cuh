@@ -1,22 +1,29 @@
 // w2_momentum.cuh -- nAuxMomentum (momentum.f:33-193) on the device.
 //
-// One Newton-Kantorovich (Q-L) iteration is four phases of a persistent
+// One Newton-Kantorovich (Q-L) iteration is these phases of a persistent
 // kernel:
 //   M1  convective face coefficients of ConvCoef (cases 4, 1 for x; 5, 2 for
-//       y) from us/vs and un/vn, each value computed once;
-//   M2  per row: DConv/DDiff stencils of the starred and time-level-n fields
-//       and the split-1 and split-2 tridiagonal rows of XMomentum
-//       (momentum.f:350-428) and YMomentum (momentum.f:675-754), written in
-//       chain order, with the boundary/blockage identity rows of split 2;
-//   C   the four chain solves (x and y chains together, split 1 then 2);
+//       y) from us/vs and un/vn into arrays -- FP64 path only; the FP32 path
+//       forms each value where a row needs it (same expression, same bits);
+//   M2a per row: DConv/DDiff stencils of the starred and time-level-n fields
+//       and the split-1 tridiagonal rows of XMomentum (momentum.f:350-384)
+//       and YMomentum (momentum.f:675-711), written in chain order;
+//   C1  the split-1 chain solves (x and y together);
+//   M2b the split-2 rows (momentum.f:396-428, 723-754) with the
+//       boundary/blockage identity rows, into the split-1 row storage;
+//   C2  the split-2 chain solves, right-hand side = the split-1 solution;
 //   M4  us += dus, vs += dvs and the DMaxNorm test against qtol.
 // Expressions keep the reference's operand order; the translation unit is
 // compiled without FMA contraction, so every value is the IEEE value of the
 // reference expression in the arithmetic type T: double on the plain path,
-// float (single-precision fields, metrics and chains) on the mixed one.  Non-porous regions contribute exact zeros
-// (PorosCoef writes 0, so dk2*cpj adds +0 to a value >= 1 and the RHS terms
-// vanish); porous decks are rejected on the host.
+// float (single-precision fields, metrics and chains) on the mixed one.
+// Metric arrays are read through MRef, which collapses to 1-D profiles or
+// constants where the host found them so.  Non-porous regions contribute
+// exact zeros (PorosCoef writes 0, so dk2*cpj adds +0 to a value >= 1 and
+// the RHS terms vanish); porous decks are rejected on the host.
 #pragma once
+#include <type_traits>
+
 #include "w2_chain.cuh"
 #include "w2_bc.cuh"
 
@@ -25,124 +32,201 @@ namespace w2 {
 template <class T>
 __device__ __forceinline__ T tmax(T a, T b) { return b > a ? b : a; }
 
-// The FP64 view of the momentum inputs and work arrays held by Dev.
-__device__ __forceinline__ MomView<double> mom_view64(const Dev &d) {
-  const Metrics &m = d.m;
-  MomView<double> v;
-  v.yeu = m.yeu; v.xeu = m.xeu; v.xzu = m.xzu; v.yzu = m.yzu;
-  v.yec = m.yec; v.xec = m.xec; v.xzn = m.xzn; v.yzn = m.yzn;
-  v.yev = m.yev; v.xev = m.xev; v.xzv = m.xzv; v.yzv = m.yzv;
-  v.yen = m.yen; v.xen = m.xen; v.xzc = m.xzc; v.yzc = m.yzc;
-  v.dju = m.dju; v.djv = m.djv; v.rac = m.rac; v.rbc = m.rbc;
-  v.rbn = m.rbn; v.rgn = m.rgn; v.ran = m.ran; v.rgc = m.rgc;
-  v.cj1x = d.cj1x; v.cj2x = d.cj2x; v.c1sx = d.c1sx; v.c2sx = d.c2sx; v.c1nx = d.c1nx; v.c2nx = d.c2nx;
-  v.cj1y = d.cj1y; v.cj2y = d.cj2y; v.c1sy = d.c1sy; v.c2sy = d.c2sy; v.c1ny = d.c1ny; v.c2ny = d.c2ny;
-  v.x1 = d.x1; v.x2 = d.x2; v.y1 = d.y1; v.y2 = d.y2;
-  return v;
+// The FP32 path forms ConvCoef values on the fly (cheap in FP32, and it keeps
+// the working set in L2); the FP64 path stores them once per iteration.
+template <class T>
+constexpr bool kFuseConv = std::is_same<T, float>::value;
+
+// ---- ConvCoef values (momentum.f:864-981) at one point ------------------
+// Each returns the value M1 stores at (i, j), or 0 where M1 never writes
+// (the reference reads such entries of its zero-initialised static arrays,
+// e.g. cj1(nx+1,j) at momentum.f:374).
+
+// XMomentum ConvCoef(4, njacob=1) with xzu, xeu, yzu, yeu: cj1, cj2.
+template <class T>
+__device__ __forceinline__ void conv_x4(const Dev &d, const MomView<T> &V, const T *us,
+                                        const T *vs, int i, int j, T &cj1, T &cj2) {
+  if (i <= d.nx && j >= 1 && j <= d.ny) {
+    const T vsum = vs[IX(d, i + 1, j)] + vs[IX(d, i, j)] + vs[IX(d, i + 1, j - 1)] + vs[IX(d, i, j - 1)];
+    cj1 = T(2.0) * V.yeu(i, j) * us[IX(d, i, j)] - V.xeu(i, j) * vsum / T(4.0);
+    cj2 = V.xzu(i, j) * vsum / T(4.0) - T(2.0) * V.yzu(i, j) * us[IX(d, i, j)];
+  } else {
+    cj1 = T(0);
+    cj2 = T(0);
+  }
 }
 
-// ---- M1: ConvCoef outputs ---------------------------------------------
+// XMomentum ConvCoef(1, njacob=0) with xzn, xec, yzn, yec: c1 (i,j >= 1).
+template <class T>
+__device__ __forceinline__ T conv_x1_c1(const Dev &d, const MomView<T> &V, const T *u, const T *v,
+                                        int i, int j) {
+  if (i < 1 || j < 1) return T(0);
+  return (V.yec(i, j) * (u[IX(d, i, j)] + u[IX(d, i - 1, j)]) -
+          V.xec(i, j) * (v[IX(d, i, j)] + v[IX(d, i, j - 1)])) * T(0.5);
+}
+
+// ... and c2 (1 <= i <= nx, 1 <= j <= ny).
+template <class T>
+__device__ __forceinline__ T conv_x1_c2(const Dev &d, const MomView<T> &V, const T *u, const T *v,
+                                        int i, int j) {
+  if (i < 1 || j < 1 || i > d.nx || j > d.ny) return T(0);
+  return (V.xzn(i, j) * (v[IX(d, i + 1, j)] + v[IX(d, i, j)]) -
+          V.yzn(i, j) * (u[IX(d, i, j + 1)] + u[IX(d, i, j)])) * T(0.5);
+}
+
+// YMomentum ConvCoef(5, njacob=1) with xzv, xev, yzv, yev: cj1, cj2.
+template <class T>
+__device__ __forceinline__ void conv_y5(const Dev &d, const MomView<T> &V, const T *us,
+                                        const T *vs, int i, int j, T &cj1, T &cj2) {
+  if (i >= 1 && i <= d.nx && j <= d.ny) {
+    const T usum = us[IX(d, i, j + 1)] + us[IX(d, i - 1, j + 1)] + us[IX(d, i, j)] + us[IX(d, i - 1, j)];
+    cj1 = V.yev(i, j) * usum / T(4.0) - T(2.0) * V.xev(i, j) * vs[IX(d, i, j)];
+    cj2 = T(2.0) * V.xzv(i, j) * vs[IX(d, i, j)] - V.yzv(i, j) * usum / T(4.0);
+  } else {
+    cj1 = T(0);
+    cj2 = T(0);
+  }
+}
+
+// YMomentum ConvCoef(2, njacob=0) with xzc, xen, yzc, yen: c1 (1 <= i <= nx,
+// 1 <= j <= ny) ...
+template <class T>
+__device__ __forceinline__ T conv_y2_c1(const Dev &d, const MomView<T> &V, const T *u, const T *v,
+                                        int i, int j) {
+  if (i < 1 || j < 1 || i > d.nx || j > d.ny) return T(0);
+  return (V.yen(i, j) * (u[IX(d, i, j + 1)] + u[IX(d, i, j)]) -
+          V.xen(i, j) * (v[IX(d, i + 1, j)] + v[IX(d, i, j)])) * T(0.5);
+}
+
+// ... and c2 (i, j >= 1).
+template <class T>
+__device__ __forceinline__ T conv_y2_c2(const Dev &d, const MomView<T> &V, const T *u, const T *v,
+                                        int i, int j) {
+  if (i < 1 || j < 1) return T(0);
+  return (V.xzc(i, j) * (v[IX(d, i, j)] + v[IX(d, i, j - 1)]) -
+          V.yzc(i, j) * (u[IX(d, i, j)] + u[IX(d, i - 1, j)])) * T(0.5);
+}
+
+// ---- M1: ConvCoef outputs into arrays (FP64 path) -----------------------
 template <class T>
 __device__ void mom_conv_coef(const Dev &d, const MomView<T> &V, const T *us, const T *vs,
                               const T *un, const T *vn) {
-  const int nx = d.nx, ny = d.ny;
-    const int W = nx + 2, H = ny + 2;
+  const int W = d.nx + 2, H = d.ny + 2;
   for (int idx = gtid(); idx < W * H; idx += gthreads()) {
     const int i = idx % W, j = idx / W;
     const size_t o = IX(d, i, j);
-    // XMomentum: ConvCoef(4, njacob=1) with xzu, xeu, yzu, yeu (momentum.f:942-950)
-    if (i <= nx && j >= 1 && j <= ny) {
-      const T vsum = vs[IX(d, i + 1, j)] + vs[o] + vs[IX(d, i + 1, j - 1)] + vs[IX(d, i, j - 1)];
-      V.cj1x[o] = T(2.0) * V.yeu[o] * us[o] - V.xeu[o] * vsum / T(4.0);
-      V.cj2x[o] = V.xzu[o] * vsum / T(4.0) - T(2.0) * V.yzu[o] * us[o];
+    T a, b;
+    conv_x4(d, V, us, vs, i, j, a, b);
+    if (i <= d.nx && j >= 1 && j <= d.ny) {
+      V.cj1x[o] = a;
+      V.cj2x[o] = b;
     }
-    // XMomentum: ConvCoef(1, njacob=0) with xzn, xec, yzn, yec (momentum.f:901-913)
     if (i >= 1 && j >= 1) {
-      V.c1sx[o] = (V.yec[o] * (us[o] + us[IX(d, i - 1, j)]) - V.xec[o] * (vs[o] + vs[IX(d, i, j - 1)])) * T(0.5);
-      V.c1nx[o] = (V.yec[o] * (un[o] + un[IX(d, i - 1, j)]) - V.xec[o] * (vn[o] + vn[IX(d, i, j - 1)])) * T(0.5);
-      if (i <= nx && j <= ny) {
-        V.c2sx[o] = (V.xzn[o] * (vs[IX(d, i + 1, j)] + vs[o]) - V.yzn[o] * (us[IX(d, i, j + 1)] + us[o])) * T(0.5);
-        V.c2nx[o] = (V.xzn[o] * (vn[IX(d, i + 1, j)] + vn[o]) - V.yzn[o] * (un[IX(d, i, j + 1)] + un[o])) * T(0.5);
+      V.c1sx[o] = conv_x1_c1(d, V, us, vs, i, j);
+      V.c1nx[o] = conv_x1_c1(d, V, un, vn, i, j);
+      if (i <= d.nx && j <= d.ny) {
+        V.c2sx[o] = conv_x1_c2(d, V, us, vs, i, j);
+        V.c2nx[o] = conv_x1_c2(d, V, un, vn, i, j);
       }
     }
-    // YMomentum: ConvCoef(5, njacob=1) with xzv, xev, yzv, yev (momentum.f:953-961)
-    if (i >= 1 && i <= nx && j <= ny) {
-      const T usum = us[IX(d, i, j + 1)] + us[IX(d, i - 1, j + 1)] + us[o] + us[IX(d, i - 1, j)];
-      V.cj1y[o] = V.yev[o] * usum / T(4.0) - T(2.0) * V.xev[o] * vs[o];
-      V.cj2y[o] = T(2.0) * V.xzv[o] * vs[o] - V.yzv[o] * usum / T(4.0);
+    conv_y5(d, V, us, vs, i, j, a, b);
+    if (i >= 1 && i <= d.nx && j <= d.ny) {
+      V.cj1y[o] = a;
+      V.cj2y[o] = b;
     }
-    // YMomentum: ConvCoef(2, njacob=0) with xzc, xen, yzc, yen (momentum.f:916-928)
     if (i >= 1 && j >= 1) {
-      if (i <= nx && j <= ny) {
-        V.c1sy[o] = (V.yen[o] * (us[IX(d, i, j + 1)] + us[o]) - V.xen[o] * (vs[IX(d, i + 1, j)] + vs[o])) * T(0.5);
-        V.c1ny[o] = (V.yen[o] * (un[IX(d, i, j + 1)] + un[o]) - V.xen[o] * (vn[IX(d, i + 1, j)] + vn[o])) * T(0.5);
+      if (i <= d.nx && j <= d.ny) {
+        V.c1sy[o] = conv_y2_c1(d, V, us, vs, i, j);
+        V.c1ny[o] = conv_y2_c1(d, V, un, vn, i, j);
       }
-      V.c2sy[o] = (V.xzc[o] * (vs[o] + vs[IX(d, i, j - 1)]) - V.yzc[o] * (us[o] + us[IX(d, i - 1, j)])) * T(0.5);
-      V.c2ny[o] = (V.xzc[o] * (vn[o] + vn[IX(d, i, j - 1)]) - V.yzc[o] * (un[o] + un[IX(d, i - 1, j)])) * T(0.5);
+      V.c2sy[o] = conv_y2_c2(d, V, us, vs, i, j);
+      V.c2ny[o] = conv_y2_c2(d, V, un, vn, i, j);
     }
   }
 }
 
-// DConvU, momentum.f:1000-1006
+// DConvU, momentum.f:1000-1006, on the coefficient values c2(i,j-1),
+// c1(i,j), c1(i+1,j), c2(i,j).
 template <class T>
-__device__ __forceinline__ T dconv_u(const Dev &d, const T *c1, const T *c2,
-                                          const T *u, int i, int j) {
+__device__ __forceinline__ T dconv_u(const Dev &d, T c2s, T c1o, T c1e, T c2o, const T *u, int i,
+                                     int j) {
   const size_t o = IX(d, i, j), os = IX(d, i, j - 1), oe = IX(d, i + 1, j);
-  return -c2[os] * u[os] - c1[o] * u[IX(d, i - 1, j)] +
-         (c1[oe] - c1[o] + c2[o] - c2[os]) * u[o] + c1[oe] * u[oe] + c2[o] * u[IX(d, i, j + 1)];
+  return -c2s * u[os] - c1o * u[IX(d, i - 1, j)] + (c1e - c1o + c2o - c2s) * u[o] + c1e * u[oe] +
+         c2o * u[IX(d, i, j + 1)];
 }
 
 // DDiffU, momentum.f:1030-1042
 template <class T>
-__device__ __forceinline__ T ddiff_u(const Dev &d, const T *ac, const T *bc,
-                                          const T *bn, const T *gn, const T *u,
-                                          int i, int j) {
+__device__ __forceinline__ T ddiff_u(const Dev &d, const MRef<T> &ac, const MRef<T> &bc,
+                                     const MRef<T> &bn, const MRef<T> &gn, const T *u, int i,
+                                     int j) {
 #define Uu(a, b) u[IX(d, a, b)]
-  const T s1 = ac[IX(d, i + 1, j)] * (Uu(i + 1, j) - Uu(i, j)) -
-                    ac[IX(d, i, j)] * (Uu(i, j) - Uu(i - 1, j)) +
-                    bc[IX(d, i + 1, j)] * (Uu(i + 1, j + 1) + Uu(i, j + 1) - Uu(i + 1, j - 1) - Uu(i, j - 1)) -
-                    bc[IX(d, i, j)] * (Uu(i, j + 1) + Uu(i - 1, j + 1) - Uu(i, j - 1) - Uu(i - 1, j - 1));
-  const T s2 = bn[IX(d, i, j)] * (Uu(i + 1, j + 1) + Uu(i + 1, j) - Uu(i - 1, j + 1) - Uu(i - 1, j)) -
-                    bn[IX(d, i, j - 1)] * (Uu(i + 1, j) + Uu(i + 1, j - 1) - Uu(i - 1, j) - Uu(i - 1, j - 1)) +
-                    gn[IX(d, i, j)] * (Uu(i, j + 1) - Uu(i, j)) -
-                    gn[IX(d, i, j - 1)] * (Uu(i, j) - Uu(i, j - 1));
+  const T s1 = ac(i + 1, j) * (Uu(i + 1, j) - Uu(i, j)) - ac(i, j) * (Uu(i, j) - Uu(i - 1, j)) +
+               bc(i + 1, j) * (Uu(i + 1, j + 1) + Uu(i, j + 1) - Uu(i + 1, j - 1) - Uu(i, j - 1)) -
+               bc(i, j) * (Uu(i, j + 1) + Uu(i - 1, j + 1) - Uu(i, j - 1) - Uu(i - 1, j - 1));
+  const T s2 = bn(i, j) * (Uu(i + 1, j + 1) + Uu(i + 1, j) - Uu(i - 1, j + 1) - Uu(i - 1, j)) -
+               bn(i, j - 1) * (Uu(i + 1, j) + Uu(i + 1, j - 1) - Uu(i - 1, j) - Uu(i - 1, j - 1)) +
+               gn(i, j) * (Uu(i, j + 1) - Uu(i, j)) - gn(i, j - 1) * (Uu(i, j) - Uu(i, j - 1));
 #undef Uu
   return s1 + s2;
 }
 
-// DConvV, momentum.f:1064-1070
+// DConvV, momentum.f:1064-1070, on c2(i,j), c1(i-1,j), c1(i,j), c2(i,j+1).
 template <class T>
-__device__ __forceinline__ T dconv_v(const Dev &d, const T *c1, const T *c2,
-                                          const T *v, int i, int j) {
+__device__ __forceinline__ T dconv_v(const Dev &d, T c2o, T c1w, T c1o, T c2n, const T *v, int i,
+                                     int j) {
   const size_t o = IX(d, i, j), ow = IX(d, i - 1, j), on = IX(d, i, j + 1);
-  return -c2[o] * v[IX(d, i, j - 1)] - c1[ow] * v[ow] + (c1[o] - c1[ow] + c2[on] - c2[o]) * v[o] +
-         c1[o] * v[IX(d, i + 1, j)] + c2[on] * v[on];
+  return -c2o * v[IX(d, i, j - 1)] - c1w * v[ow] + (c1o - c1w + c2n - c2o) * v[o] +
+         c1o * v[IX(d, i + 1, j)] + c2n * v[on];
 }
 
 // DDiffV, momentum.f:1094-1106
 template <class T>
-__device__ __forceinline__ T ddiff_v(const Dev &d, const T *an, const T *bc,
-                                          const T *bn, const T *gc, const T *v,
-                                          int i, int j) {
+__device__ __forceinline__ T ddiff_v(const Dev &d, const MRef<T> &an, const MRef<T> &bc,
+                                     const MRef<T> &bn, const MRef<T> &gc, const T *v, int i,
+                                     int j) {
 #define Vv(a, b) v[IX(d, a, b)]
-  const T s1 = an[IX(d, i, j)] * (Vv(i + 1, j) - Vv(i, j)) -
-                    an[IX(d, i - 1, j)] * (Vv(i, j) - Vv(i - 1, j)) +
-                    bn[IX(d, i, j)] * (Vv(i + 1, j + 1) + Vv(i, j + 1) - Vv(i + 1, j - 1) - Vv(i, j - 1)) -
-                    bn[IX(d, i - 1, j)] * (Vv(i, j + 1) + Vv(i - 1, j + 1) - Vv(i, j - 1) - Vv(i - 1, j - 1));
-  const T s2 = bc[IX(d, i, j + 1)] * (Vv(i + 1, j + 1) + Vv(i + 1, j) - Vv(i - 1, j + 1) - Vv(i - 1, j)) -
-                    bc[IX(d, i, j)] * (Vv(i + 1, j) + Vv(i + 1, j - 1) - Vv(i - 1, j) - Vv(i - 1, j - 1)) +
-                    gc[IX(d, i, j + 1)] * (Vv(i, j + 1) - Vv(i, j)) -
-                    gc[IX(d, i, j)] * (Vv(i, j) - Vv(i, j - 1));
+  const T s1 = an(i, j) * (Vv(i + 1, j) - Vv(i, j)) - an(i - 1, j) * (Vv(i, j) - Vv(i - 1, j)) +
+               bn(i, j) * (Vv(i + 1, j + 1) + Vv(i, j + 1) - Vv(i + 1, j - 1) - Vv(i, j - 1)) -
+               bn(i - 1, j) * (Vv(i, j + 1) + Vv(i - 1, j + 1) - Vv(i, j - 1) - Vv(i - 1, j - 1));
+  const T s2 = bc(i, j + 1) * (Vv(i + 1, j + 1) + Vv(i + 1, j) - Vv(i - 1, j + 1) - Vv(i - 1, j)) -
+               bc(i, j) * (Vv(i + 1, j) + Vv(i + 1, j - 1) - Vv(i - 1, j) - Vv(i - 1, j - 1)) +
+               gc(i, j + 1) * (Vv(i, j + 1) - Vv(i, j)) - gc(i, j) * (Vv(i, j) - Vv(i, j - 1));
 #undef Vv
   return s1 + s2;
 }
 
-// ---- M2: stencils and tridiagonal rows --------------------------------
+// cj1/cj2 of X (which = 1, 2) at (i, j): from the arrays or formed here.
 template <class T>
-__device__ void mom_assemble(const Dev &d, const MomView<T> &V, double dk, double re, const T *us,
-                             const T *vs, const T *un, const T *vn) {
+__device__ __forceinline__ T xcj(const Dev &d, const MomView<T> &V, const T *us, const T *vs,
+                                 int which, int i, int j) {
+  if constexpr (kFuseConv<T>) {
+    T a, b;
+    conv_x4(d, V, us, vs, i, j, a, b);
+    return which == 1 ? a : b;
+  } else {
+    return which == 1 ? V.cj1x[IX(d, i, j)] : V.cj2x[IX(d, i, j)];
+  }
+}
+
+template <class T>
+__device__ __forceinline__ T ycj(const Dev &d, const MomView<T> &V, const T *us, const T *vs,
+                                 int which, int i, int j) {
+  if constexpr (kFuseConv<T>) {
+    T a, b;
+    conv_y5(d, V, us, vs, i, j, a, b);
+    return which == 1 ? a : b;
+  } else {
+    return which == 1 ? V.cj1y[IX(d, i, j)] : V.cj2y[IX(d, i, j)];
+  }
+}
+
+// ---- M2a: stencils and split-1 rows ------------------------------------
+template <class T>
+__device__ void mom_assemble1(const Dev &d, const MomView<T> &V, double dk, double re,
+                              const T *us, const T *vs, const T *un, const T *vn) {
   const int nx = d.nx, ny = d.ny;
-    const T re1 = T(1.0) / T(re), dk2 = T(dk) * T(0.5);
+  const T re1 = T(1.0) / T(re), dk2 = T(dk) * T(0.5);
   // X rows: i = 1..nx, j = 2..ny, ind = (j-2)*nx + i-1
   const int nX = nx * (ny - 1);
   const int nY = (nx - 1) * ny;
@@ -150,88 +234,143 @@ __device__ void mom_assemble(const Dev &d, const MomView<T> &V, double dk, doubl
     if (t < nX) {
       const int i = t % nx + 1, j = t / nx + 2;
       const size_t o = IX(d, i, j);
-      const T rkj = dk2 * V.dju[o];
-      const T cnvs = dconv_u(d, V.c1sx, V.c2sx, us, i, j);
-      const T cnvn = dconv_u(d, V.c1nx, V.c2nx, un, i, j);
+      const int px = cpos(V.x1, t);
+      const T rkj = dk2 * V.dju(i, j);
+      T c1s_o, c1s_e, c2s_o, c2s_s, c1n_o, c1n_e, c2n_o, c2n_s;
+      if constexpr (kFuseConv<T>) {
+        c1s_o = conv_x1_c1(d, V, us, vs, i, j);
+        c1s_e = conv_x1_c1(d, V, us, vs, i + 1, j);
+        c2s_o = conv_x1_c2(d, V, us, vs, i, j);
+        c2s_s = conv_x1_c2(d, V, us, vs, i, j - 1);
+        c1n_o = conv_x1_c1(d, V, un, vn, i, j);
+        c1n_e = conv_x1_c1(d, V, un, vn, i + 1, j);
+        c2n_o = conv_x1_c2(d, V, un, vn, i, j);
+        c2n_s = conv_x1_c2(d, V, un, vn, i, j - 1);
+      } else {
+        c1s_o = V.c1sx[o]; c1s_e = V.c1sx[IX(d, i + 1, j)];
+        c2s_o = V.c2sx[o]; c2s_s = V.c2sx[IX(d, i, j - 1)];
+        c1n_o = V.c1nx[o]; c1n_e = V.c1nx[IX(d, i + 1, j)];
+        c2n_o = V.c2nx[o]; c2n_s = V.c2nx[IX(d, i, j - 1)];
+      }
+      const T cnvs = dconv_u(d, c2s_s, c1s_o, c1s_e, c2s_o, us, i, j);
+      const T cnvn = dconv_u(d, c2n_s, c1n_o, c1n_e, c2n_o, un, i, j);
       const T difs = ddiff_u(d, V.rac, V.rbc, V.rbn, V.rgn, us, i, j);
       const T difn = ddiff_u(d, V.rac, V.rbc, V.rbn, V.rgn, un, i, j);
-      const T cj1 = V.cj1x[o], racp = V.rac[IX(d, i + 1, j)], rac0 = V.rac[o];
+      const T cj1 = xcj(d, V, us, vs, 1, i, j), racp = V.rac(i + 1, j), rac0 = V.rac(i, j);
       T a1, a2, a3;
-      if (cj1 >= T(0.0)) {
-        a1 = rkj * (-V.cj1x[IX(d, i - 1, j)] - re1 * rac0);
+      if (cj1 >= T(0)) {
+        a1 = rkj * (-xcj(d, V, us, vs, 1, i - 1, j) - re1 * rac0);
         a2 = T(1.0) + rkj * (cj1 + re1 * (racp + rac0));
         a3 = rkj * (-re1 * racp);
       } else {
         a1 = rkj * (-re1 * rac0);
         a2 = T(1.0) + rkj * (-cj1 + re1 * (racp + rac0));
-        a3 = rkj * (V.cj1x[IX(d, i + 1, j)] - re1 * racp);
+        a3 = rkj * (xcj(d, V, us, vs, 1, i + 1, j) - re1 * racp);
       }
-      V.x1.a1[t] = a1;
-      V.x1.a2[t] = a2;
-      V.x1.a3[t] = a3;
-      V.x1.b[t] =
-          un[o] - us[o] + rkj * (-cnvs - cnvn) + rkj * re1 * (difs + difn);
-      // split 2 (momentum.f:396-428) with identity rows (momentum.f:432-496)
-      if (d.mask[o] & MK_XID) {
-        a1 = T(0.0); a2 = T(1.0); a3 = T(0.0);
-      } else {
-        const T cj2 = V.cj2x[o], rgn0 = V.rgn[o], rgns = V.rgn[IX(d, i, j - 1)];
-        if (cj2 >= T(0.0)) {
-          a1 = rkj * (-V.cj2x[IX(d, i, j - 1)] - re1 * rgns);
-          a2 = T(1.0) + rkj * (cj2 + re1 * (rgn0 + rgns));
-          a3 = rkj * (-re1 * rgn0);
-        } else {
-          a1 = rkj * (-re1 * rgns);
-          a2 = T(1.0) + rkj * (-cj2 + re1 * (rgn0 + rgns));
-          a3 = rkj * (V.cj2x[IX(d, i, j + 1)] - re1 * rgn0);
-        }
-      }
-      V.x2.a1[t] = a1;
-      V.x2.a2[t] = a2;
-      V.x2.a3[t] = a3;
+      V.x1.a1[px] = a1;
+      V.x1.a2[px] = a2;
+      V.x1.a3[px] = a3;
+      V.x1.b[px] = un[o] - us[o] + rkj * (-cnvs - cnvn) + rkj * re1 * (difs + difn);
     } else {
       // Y rows: i = 2..nx, j = 1..ny, ind = (j-1)*(nx-1) + i-2
       const int q = t - nX;
       const int i = q % (nx - 1) + 2, j = q / (nx - 1) + 1;
       const size_t o = IX(d, i, j);
-      const T rkj = dk2 * V.djv[o];
-      const T cnvs = dconv_v(d, V.c1sy, V.c2sy, vs, i, j);
-      const T cnvn = dconv_v(d, V.c1ny, V.c2ny, vn, i, j);
+      const int py = cpos(V.y1, q);
+      const T rkj = dk2 * V.djv(i, j);
+      T c2s_o, c1s_w, c1s_o, c2s_n, c2n_o, c1n_w, c1n_o, c2n_n;
+      if constexpr (kFuseConv<T>) {
+        c2s_o = conv_y2_c2(d, V, us, vs, i, j);
+        c1s_w = conv_y2_c1(d, V, us, vs, i - 1, j);
+        c1s_o = conv_y2_c1(d, V, us, vs, i, j);
+        c2s_n = conv_y2_c2(d, V, us, vs, i, j + 1);
+        c2n_o = conv_y2_c2(d, V, un, vn, i, j);
+        c1n_w = conv_y2_c1(d, V, un, vn, i - 1, j);
+        c1n_o = conv_y2_c1(d, V, un, vn, i, j);
+        c2n_n = conv_y2_c2(d, V, un, vn, i, j + 1);
+      } else {
+        c2s_o = V.c2sy[o]; c1s_w = V.c1sy[IX(d, i - 1, j)];
+        c1s_o = V.c1sy[o]; c2s_n = V.c2sy[IX(d, i, j + 1)];
+        c2n_o = V.c2ny[o]; c1n_w = V.c1ny[IX(d, i - 1, j)];
+        c1n_o = V.c1ny[o]; c2n_n = V.c2ny[IX(d, i, j + 1)];
+      }
+      const T cnvs = dconv_v(d, c2s_o, c1s_w, c1s_o, c2s_n, vs, i, j);
+      const T cnvn = dconv_v(d, c2n_o, c1n_w, c1n_o, c2n_n, vn, i, j);
       const T difs = ddiff_v(d, V.ran, V.rbc, V.rbn, V.rgc, vs, i, j);
       const T difn = ddiff_v(d, V.ran, V.rbc, V.rbn, V.rgc, vn, i, j);
-      const T cj1 = V.cj1y[o], ran0 = V.ran[o], ranw = V.ran[IX(d, i - 1, j)];
+      const T cj1 = ycj(d, V, us, vs, 1, i, j), ran0 = V.ran(i, j), ranw = V.ran(i - 1, j);
       T a1, a2, a3;
-      if (cj1 >= T(0.0)) {
-        a1 = rkj * (-V.cj1y[IX(d, i - 1, j)] - re1 * ranw);
+      if (cj1 >= T(0)) {
+        a1 = rkj * (-ycj(d, V, us, vs, 1, i - 1, j) - re1 * ranw);
         a2 = rkj * (cj1 + re1 * (ran0 + ranw)) + T(1.0);
         a3 = rkj * (-re1 * ran0);
       } else {
         a1 = rkj * (-re1 * ranw);
         a2 = rkj * (-cj1 + re1 * (ran0 + ranw)) + T(1.0);
-        a3 = rkj * (V.cj1y[IX(d, i + 1, j)] - re1 * ran0);
+        a3 = rkj * (ycj(d, V, us, vs, 1, i + 1, j) - re1 * ran0);
       }
-      V.y1.a1[q] = a1;
-      V.y1.a2[q] = a2;
-      V.y1.a3[q] = a3;
-      V.y1.b[q] =
-          vn[o] - vs[o] + rkj * (-cnvs - cnvn) + rkj * re1 * (difs + difn);
-      if (d.mask[o] & MK_YID) {
-        a1 = T(0.0); a2 = T(1.0); a3 = T(0.0);
+      V.y1.a1[py] = a1;
+      V.y1.a2[py] = a2;
+      V.y1.a3[py] = a3;
+      V.y1.b[py] = vn[o] - vs[o] + rkj * (-cnvs - cnvn) + rkj * re1 * (difs + difn);
+    }
+  }
+}
+
+// ---- M2b: split-2 rows (momentum.f:396-428, 723-754) with identity rows
+// (momentum.f:432-496, 760-821), into the split-1 row storage ------------
+template <class T>
+__device__ void mom_assemble2(const Dev &d, const MomView<T> &V, double dk, double re,
+                              const T *us, const T *vs) {
+  const int nx = d.nx, ny = d.ny;
+  const T re1 = T(1.0) / T(re), dk2 = T(dk) * T(0.5);
+  const int nX = nx * (ny - 1);
+  const int nY = (nx - 1) * ny;
+  for (int t = gtid(); t < nX + nY; t += gthreads()) {
+    T a1, a2, a3;
+    if (t < nX) {
+      const int i = t % nx + 1, j = t / nx + 2;
+      const int px = cpos(V.x2, t);
+      if (d.mask[IX(d, i, j)] & MK_XID) {
+        a1 = T(0); a2 = T(1.0); a3 = T(0);
       } else {
-        const T cj2 = V.cj2y[o], rgc0 = V.rgc[o], rgcn = V.rgc[IX(d, i, j + 1)];
-        if (cj2 >= T(0.0)) {
-          a1 = rkj * (-V.cj2y[IX(d, i, j - 1)] - re1 * rgc0);
+        const T rkj = dk2 * V.dju(i, j);
+        const T cj2 = xcj(d, V, us, vs, 2, i, j), rgn0 = V.rgn(i, j), rgns = V.rgn(i, j - 1);
+        if (cj2 >= T(0)) {
+          a1 = rkj * (-xcj(d, V, us, vs, 2, i, j - 1) - re1 * rgns);
+          a2 = T(1.0) + rkj * (cj2 + re1 * (rgn0 + rgns));
+          a3 = rkj * (-re1 * rgn0);
+        } else {
+          a1 = rkj * (-re1 * rgns);
+          a2 = T(1.0) + rkj * (-cj2 + re1 * (rgn0 + rgns));
+          a3 = rkj * (xcj(d, V, us, vs, 2, i, j + 1) - re1 * rgn0);
+        }
+      }
+      V.x2.a1[px] = a1;
+      V.x2.a2[px] = a2;
+      V.x2.a3[px] = a3;
+    } else {
+      const int q = t - nX;
+      const int i = q % (nx - 1) + 2, j = q / (nx - 1) + 1;
+      const int py = cpos(V.y2, q);
+      if (d.mask[IX(d, i, j)] & MK_YID) {
+        a1 = T(0); a2 = T(1.0); a3 = T(0);
+      } else {
+        const T rkj = dk2 * V.djv(i, j);
+        const T cj2 = ycj(d, V, us, vs, 2, i, j), rgc0 = V.rgc(i, j), rgcn = V.rgc(i, j + 1);
+        if (cj2 >= T(0)) {
+          a1 = rkj * (-ycj(d, V, us, vs, 2, i, j - 1) - re1 * rgc0);
           a2 = rkj * (cj2 + re1 * (rgcn + rgc0)) + T(1.0);
           a3 = rkj * (-re1 * rgcn);
         } else {
           a1 = rkj * (-re1 * rgc0);
           a2 = rkj * (-cj2 + re1 * (rgcn + rgc0)) + T(1.0);
-          a3 = rkj * (V.cj2y[IX(d, i, j + 1)] - re1 * rgcn);
+          a3 = rkj * (ycj(d, V, us, vs, 2, i, j + 1) - re1 * rgcn);
         }
       }
-      V.y2.a1[q] = a1;
-      V.y2.a2[q] = a2;
-      V.y2.a3[q] = a3;
+      V.y2.a1[py] = a1;
+      V.y2.a2[py] = a2;
+      V.y2.a3[py] = a3;
     }
   }
 }
@@ -240,12 +379,12 @@ __device__ void mom_assemble(const Dev &d, const MomView<T> &V, double dk, doubl
 template <class T>
 __device__ void mom_update(const Dev &d, const MomView<T> &V, T *us, T *vs, unsigned long long *slot) {
   const int nx = d.nx, ny = d.ny;
-  T mx = T(0.0);
+  T mx = T(0);
   for (int t = gtid(); t < nx * ny; t += gthreads()) {
     const int i = t % nx + 1, j = t / nx + 1;
     const size_t o = IX(d, i, j);
-    const T du = (j >= 2) ? V.x2.x[(j - 2) * nx + i - 1] : T(0.0);
-    const T dv = (i >= 2) ? V.y2.x[(j - 1) * (nx - 1) + i - 2] : T(0.0);
+    const T du = (j >= 2) ? V.x2.x[cpos(V.x2, (j - 2) * nx + i - 1)] : T(0);
+    const T dv = (i >= 2) ? V.y2.x[cpos(V.y2, (j - 1) * (nx - 1) + i - 2)] : T(0);
     us[o] = us[o] + du;
     vs[o] = vs[o] + dv;
     const bool in = (i >= 2 && i <= nx - 1 && j >= 2 && j <= ny - 1) || (i == 5 && j == 5);
@@ -256,9 +395,8 @@ __device__ void mom_update(const Dev &d, const MomView<T> &V, T *us, T *vs, unsi
 
 // The whole nAuxMomentum.  Returns nQLiter (or -1) in *out; false on error.
 template <class T>
-__device__ bool naux_momentum(const Dev &d, const MomView<T> &V, int mqiter, double dk, double re, double qtol,
-                              const T *un, const T *vn, T *us, T *vs,
-                              int *out) {
+__device__ bool naux_momentum(const Dev &d, const MomView<T> &V, int mqiter, double dk, double re,
+                              double qtol, const T *un, const T *vn, T *us, T *vs, int *out) {
   Sync *sy = d.sync;
   int result = -1;
   for (int it = 1; it <= mqiter; ++it) {
@@ -267,15 +405,19 @@ __device__ bool naux_momentum(const Dev &d, const MomView<T> &V, int mqiter, dou
         set_error(sy, W2_E_BCFLAG);
       if (!grid_sync(sy)) return false;
     }
-    mom_conv_coef(d, V, us, vs, un, vn);
+    if constexpr (!kFuseConv<T>) mom_conv_coef(d, V, us, vs, un, vn);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       if (it == 1) sy->red[1] = 0ull;
       sy->red[(it + 1) % 3] = 0ull;
     }
-    if (!grid_sync(sy)) return false;
-    mom_assemble(d, V, dk, re, us, vs, un, vn);
+    if constexpr (!kFuseConv<T>) {
+      if (!grid_sync(sy)) return false;
+    }
+    mom_assemble1(d, V, dk, re, us, vs, un, vn);
     if (!grid_sync(sy)) return false;
     if (!solve_chains(d, V.x1, V.y1, 2)) return false;
+    mom_assemble2(d, V, dk, re, us, vs);
+    if (!grid_sync(sy)) return false;
     if (!solve_chains(d, V.x2, V.y2, 2)) return false;
     mom_update(d, V, us, vs, &sy->red[it % 3]);
     if (!grid_sync(sy)) return false;

@@ -248,9 +248,7 @@ __device__ int sor_lex_block(const Dev &d, double *p, int lcartes, int msorit, d
 // Slor (2), lines in order, by thread 0 of one block.
 __device__ int slor_block(const Dev &d, double *p, int lcartes, int msorit, double dk,
                           double sortol, double sorrel) {
-  __shared__ int result;
   __shared__ double difsh;
-  if (threadIdx.x == 0) result = 0;
   for (int it = 1; it <= msorit; ++it) {
     if (!lcartes) {
       ppe_rhs_block(d, lcartes, dk, p);
