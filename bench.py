@@ -339,7 +339,8 @@ def run_ours(args):
         s.tune(seg=args.seg, warm=args.warm, threads=args.threads, blocks_per_sm=args.blocks_per_sm)
     if args.mixed_k or args.mixed_threads:
         s.tune_mixed(args.mixed_k, args.mixed_threads)
-    inner = args.refine_sweeps or 16 * (args.mixed_k or 8)
+    inner = args.refine_sweeps or s.refine_sweeps or 16 * (args.mixed_k or 8)
+    args.refine_sweeps = inner
     prm = case.params
     st = torch.cuda.ExternalStream(s.stream(), device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)

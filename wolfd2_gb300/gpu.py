@@ -173,11 +173,18 @@ class Solver:
         if rc != W2_OK:
             raise W2Error(rc, "wolfd2gpu_create failed")
         self.h = h
+        self.refine_sweeps = 0  # mixed: FP32 sweeps per refinement pass (0 = library default)
 
     @classmethod
-    def for_case(cls, case: Case, mnx: Optional[int] = None, mny: Optional[int] = None) -> "Solver":
+    def for_case(cls, case: Case, mnx: Optional[int] = None, mny: Optional[int] = None,
+                 tuned: bool = True, precision: str = "mixed") -> "Solver":
+        """Context for a case with its grid metrics; with `tuned`, the kernel
+        shapes the autotuner committed for this grid shape (tuned.json)."""
         s = cls(case.nx, case.ny, case.regions, mnx, mny)
         s.grid_metric(case.x, case.y)
+        if tuned:
+            from . import autotune
+            autotune.apply(s, autotune.lookup(case.nx, case.ny, precision))
         return s
 
     def close(self):
@@ -279,11 +286,15 @@ class Solver:
 
     def cold_start(self, prm: RunParams, **kw) -> int:
         out = C.c_int()
+        if kw.get("precision") == PREC_MIXED and not kw.get("refine_sweeps"):
+            kw["refine_sweeps"] = self.refine_sweeps
         pr = Params.of(prm, **kw)
         self._check(self.L.wolfd2gpu_cold_start(self.h, C.byref(pr), C.byref(out)))
         return out.value
 
     def step(self, prm: RunParams, nsteps: int = 1, **kw) -> List[tuple]:
+        if kw.get("precision") == PREC_MIXED and not kw.get("refine_sweeps"):
+            kw["refine_sweeps"] = self.refine_sweeps
         pr = Params.of(prm, **kw)
         st = (StepStat * max(nsteps, 1))()
         self._check(self.L.wolfd2gpu_step(self.h, C.byref(pr), nsteps, st))
