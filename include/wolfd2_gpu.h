@@ -197,9 +197,13 @@ int wolfd2gpu_tune(w2_ctx *ctx, int chain_seg, int chain_warm, int threads,
 int wolfd2gpu_set_precision(w2_ctx *ctx, int precision, int refine_sweeps);
 
 /* Mixed Poisson kernel shape: sweeps between grid barriers (4 or 8; the
- * halo is twice that) and the largest block the tile planner may use
- * (64..512 threads; 0 keeps the current value).  Tiles are re-planned. */
-int wolfd2gpu_tune_mixed(w2_ctx *ctx, int sweeps_per_barrier, int threads);
+ * halo is twice that), the largest block the tile planner may use
+ * (64..512 threads; 0 keeps the current value), and the tile mode: 0 = one
+ * tile per block when the grid allows it, else several tiles per block;
+ * 1 = always several tiles per block; 2 = the same on at most 16 blocks
+ * (a test shape).  Tiles are re-planned. */
+int wolfd2gpu_tune_mixed(w2_ctx *ctx, int sweeps_per_barrier, int threads,
+                         int mode);
 
 /* Device pointers of the resident u, v, p fields and the device leading
  * dimension (elements), for callers that bring their own device buffers. */

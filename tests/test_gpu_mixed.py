@@ -36,15 +36,17 @@ def _inputs(case, seed, amp=0.05):
 
 @pytest.mark.parametrize("sortol,msorit", [(1e-8, 301), (1e-8, 300), (2e-6, 2000), (7e-7, 2000),
                                            (3e-7, 2000)])
-@pytest.mark.parametrize("K,threads", [(8, 512), (4, 256), (8, 128)])
-def test_mixed_ppe_matches_model(sortol, msorit, K, threads):
+@pytest.mark.parametrize("K,threads,mode", [(8, 512, 0), (4, 256, 0), (8, 128, 0), (8, 512, 2),
+                                            (4, 256, 1)])
+def test_mixed_ppe_matches_model(sortol, msorit, K, threads, mode):
     """Drop-in Ppe in mixed mode: bit-identical to the model for stopping
-    points on every sweep of a group and for odd/even msorit."""
+    points on every sweep of a group and for odd/even msorit, with one tile
+    per block (mode 0) and with several tiles per block (modes 1, 2)."""
     case = deck.cavity(128, 400.0, 0.002, solver="rb_sor", ny=64)
     o, met, u, v, p = _inputs(case, 11)
     inner = 24
     s = Solver.for_case(case)
-    s.tune_mixed(K, threads)
+    s.tune_mixed(K, threads, mode)
     s.set_precision(PREC_MIXED, inner)
     gp = p.copy(order="F")
     n_g = s.Ppe(True, 5, msorit, case.params.dk, sortol, case.params.sorrel, u, v, gp)
@@ -146,3 +148,20 @@ def test_mixed_rejects_unsupported():
     s2.load_fields(z, z, z)
     with pytest.raises(W2Error):
         s2.step(odd.params, 1, precision=PREC_MIXED)
+
+
+def test_mixed_multitile_time_loop_matches_model():
+    """Several tiles per block (16 blocks on a 256x256 cavity): the time
+    loop bit-identical to the model."""
+    case = deck.cavity(256, 1000.0, 0.001, solver="rb_sor")
+    u0, v0, p0 = deck.perturbation_ic(case, 7)
+    model = M.MixedRun(case, fields={"u": u0, "v": v0, "p": p0}, cold_start=False, inner=48)
+    model.step(2)
+    s = Solver.for_case(case)
+    s.tune_mixed(8, 512, 2)
+    s.load_fields(u0, v0, p0)
+    hist = s.step(case.params, 2, precision=PREC_MIXED, refine_sweeps=48)
+    assert [(h[0], h[1]) for h in hist] == [(h[0], h[1]) for h in model.history]
+    u, v, p = s.store_fields()
+    for nm, g in (("u", u), ("v", v), ("p", p)):
+        assert np.array_equal(g, model.f[nm]), (nm, _rel(g, model.f[nm]))

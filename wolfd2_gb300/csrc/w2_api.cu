@@ -54,7 +54,8 @@ struct w2_ctx {
   float *xbuf = nullptr;  // two exchange buffers of 2 colour planes each
   size_t xbuf_floats = 0;
   bool mixed_ok = false;
-  int mixed_K = 8, mixed_threads = kMixedThreads;
+  int mixed_K = 8, mixed_threads = kMixedThreads, mixed_blocks = 0;
+  int mixed_mode = 0;  // 0 auto, 1 multi-tile, 2 multi-tile on at most 16 blocks
   size_t mixed_smem = 0;
   MixedGeom mg{};
   int prec_dropin = W2_PREC_FP64, refine_dropin = 0;
@@ -598,11 +599,14 @@ const void *mixed_kernel(int K) {
   return nullptr;
 }
 
-// One tile per block (one block per SM): the split of the unknowns into at
-// most nsm tiles, tx a multiple of 8, whose block does the least sweep work
-// per group of K sweeps -- (plane columns rounded to warps) x (box rows
-// active in each half-sweep) -- within the shared-memory limit and
-// mixed_threads <= kMixedThreads threads.
+// Tile plan of the mixed Poisson kernel.  Preferred: one tile per block (one
+// block per SM, box resident in shared memory), the split of the unknowns
+// into at most nsm tiles, tx a multiple of 8, whose block does the least
+// sweep work per group of K sweeps -- (plane columns rounded to warps) x (box
+// rows active in each half-sweep).  Grids too large for that run in
+// multi-tile mode: blocks (as many as fit per SM) loop over more tiles,
+// staging each box per group; the split then minimises tiles per block x
+// (sweep work + staging).
 void plan_mixed(w2_ctx *c) {
   c->mixed_ok = false;
   const int K = c->mixed_K;
@@ -616,35 +620,58 @@ void plan_mixed(w2_ctx *c) {
   if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit) != cudaSuccess)
     return;
   const int NX = c->nx - 1, NY = c->ny - 1, H = 2 * K;
-  double best = 1e300;
-  for (int ntx = 1; ntx <= std::max(1, NX / 8); ++ntx) {
-    int tx = (NX + ntx - 1) / ntx;
-    tx = (tx + 7) / 8 * 8;
-    if ((NX + tx - 1) / tx != ntx) continue;
-    for (int nty = 1; nty <= std::max(1, NY / 4) && ntx * nty <= c->nsm; ++nty) {
-      const int ty = (NY + nty - 1) / nty;
-      if ((NY + ty - 1) / ty != nty) continue;
-      const size_t smem = mixed_smem_bytes(K, tx, ty);
-      const int T = mixed_threads(K, tx, ty);
-      if (smem > limit || T > c->mixed_threads) continue;
-      const int bh = ty + 2 * H, hwp = (tx / 2 + H + 31) / 32 * 32;
-      double rows = 0.0;
-      for (int h = 1; h <= 2 * K; ++h) rows += std::max(0, bh - 2 * h);
-      const double cost = (double)hwp * rows;
-      if (cost < best) {
-        best = cost;
-        c->mg = MixedGeom{tx, ty, ntx, nty, ntx * tx / 2 + H, nty * ty + 2 * H, hwp};
-        c->mixed_smem = smem;
+  auto sweep_work = [&](int tx, int ty) {
+    const int bh = ty + 2 * H, hwp = (tx / 2 + H + 31) / 32 * 32;
+    double rows = 0.0;
+    for (int h = 1; h <= 2 * K; ++h) rows += std::max(0, bh - 2 * h);
+    return (double)hwp * rows;
+  };
+  for (int pass = c->mixed_mode ? 1 : 0; pass < 2 && !c->mixed_ok; ++pass) {
+    const bool resident = pass == 0;
+    double best = 1e300;
+    for (int ntx = 1; ntx <= std::max(1, NX / 8); ++ntx) {
+      int tx = (NX + ntx - 1) / ntx;
+      tx = (tx + 7) / 8 * 8;
+      if ((NX + tx - 1) / tx != ntx) continue;
+      for (int nty = 1; nty <= std::max(1, NY / 4); ++nty) {
+        if (resident && ntx * nty > c->nsm) break;
+        const int ty = (NY + nty - 1) / nty;
+        if ((NY + ty - 1) / ty != nty) continue;
+        const size_t smem = mixed_smem_bytes(K, tx, ty, resident);
+        const int T = mixed_threads(K, tx, ty);
+        if (smem > limit || T > c->mixed_threads) continue;
+        double cost = sweep_work(tx, ty);
+        int blocks = c->nsm;
+        if (!resident) {
+          int occ = 0;
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kf, T, smem);
+          if (occ < 1) continue;
+          blocks = c->nsm * occ;
+          if (c->mixed_mode == 2) blocks = std::min(blocks, 16);
+          const int bh = ty + 2 * H, hwp = (tx / 2 + H + 31) / 32 * 32;
+          const int tpb = (ntx * nty + blocks - 1) / blocks;
+          cost = tpb * (cost + 4.0 * K * bh * hwp / 8.0);
+        }
+        if (cost < best) {
+          best = cost;
+          c->mg = MixedGeom{tx, ty, ntx, nty, ntx * tx / 2 + H, nty * ty + 2 * H,
+                            (tx / 2 + H + 31) / 32 * 32, resident ? 1 : 0};
+          c->mixed_smem = smem;
+          c->mixed_blocks = blocks;
+        }
       }
     }
+    if (best >= 1e300) continue;
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kf, mixed_threads(K, c->mg.tx, c->mg.ty),
+                                                  c->mixed_smem);
+    if (occ < 1) continue;
+    c->mixed_ok = true;
   }
-  if (best >= 1e300) return;
-  int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kf, mixed_threads(K, c->mg.tx, c->mg.ty),
-                                                c->mixed_smem);
-  if (occ < 1) return;
-  // exchange buffers: zero wherever no tile writes (cells off the unknowns)
-  const size_t need = 4 * (size_t)c->mg.gh * c->mg.gw;
+  if (!c->mixed_ok) return;
+  // exchange buffers and the r buffer: zero wherever no tile writes (cells
+  // off the unknowns)
+  const size_t need = 6 * (size_t)c->mg.gh * c->mg.gw;
   if (need > c->xbuf_floats) {
     if (c->xbuf) {
       cudaFree(c->xbuf);
@@ -652,11 +679,13 @@ void plan_mixed(w2_ctx *c) {
       c->xbuf = nullptr;
       c->xbuf_floats = 0;
     }
-    if (!(c->xbuf = dalloc<float>(c, need))) return;
+    if (!(c->xbuf = dalloc<float>(c, need))) {
+      c->mixed_ok = false;
+      return;
+    }
     c->xbuf_floats = need;
   }
-  if (cudaMemset(c->xbuf, 0, c->xbuf_floats * sizeof(float)) != cudaSuccess) return;
-  c->mixed_ok = true;
+  if (cudaMemset(c->xbuf, 0, c->xbuf_floats * sizeof(float)) != cudaSuccess) c->mixed_ok = false;
 }
 
 // The mixed path covers npsolver 5/6 on Cartesian grids whose rows are all
@@ -679,14 +708,14 @@ int launch_ppe_mixed(w2_ctx *c, int lcartes, int msorit, double dk, double sorto
                      int inner, const double *u, const double *v, double *p, StepOut *out) {
   Dev d = c->dev;
   MixedGeom g = c->mg;
-  float *xb1 = c->xbuf + 2 * (size_t)c->mg.gh * c->mg.gw;
+  const size_t plane2 = 2 * (size_t)c->mg.gh * c->mg.gw;
   MixedArgs a{lcartes, msorit, auto_inner(c, inner), dk, sortol, (float)sorrel, u, v, p,
-              c->xbuf, xb1};
+              c->xbuf, c->xbuf + plane2, c->xbuf + 2 * plane2};
   void *args[] = {&d, &g, &a, &out};
   c->launches++;
   const int T = mixed_threads(c->mixed_K, g.tx, g.ty);
-  cudaError_t e = cudaLaunchCooperativeKernel(mixed_kernel(c->mixed_K), dim3(c->nsm), dim3(T),
-                                              args, c->mixed_smem, c->st);
+  cudaError_t e = cudaLaunchCooperativeKernel(mixed_kernel(c->mixed_K), dim3(c->mixed_blocks),
+                                              dim3(T), args, c->mixed_smem, c->st);
   if (e != cudaSuccess) return fail(c, W2_E_CUDA, "mixed PPE launch: %s", cudaGetErrorString(e));
   return W2_OK;
 }
@@ -922,8 +951,10 @@ int wolfd2gpu_set_precision(w2_ctx *c, int precision, int refine_sweeps) {
   return W2_OK;
 }
 
-int wolfd2gpu_tune_mixed(w2_ctx *c, int sweeps_per_barrier, int threads) {
+int wolfd2gpu_tune_mixed(w2_ctx *c, int sweeps_per_barrier, int threads, int mode) {
   if (!c) return W2_E_ARG;
+  if (mode < 0 || mode > 2) return fail(c, W2_E_ARG, "tile mode must be 0, 1 or 2");
+  c->mixed_mode = mode;
   if (sweeps_per_barrier != 0 && !mixed_kernel(sweeps_per_barrier))
     return fail(c, W2_E_ARG, "sweeps per barrier must be 4 or 8");
   if (threads != 0 && (threads % 32 || threads < 64 || threads > kMixedThreads))

@@ -56,6 +56,7 @@ struct MixedGeom {
   int ntx, nty;  // tiles per direction, ntx*nty <= blocks
   int gw, gh;    // exchange buffer: floats per colour row, rows
   int hwp;       // box columns per plane rounded up to whole warps
+  int resident;  // one tile per block, box kept in shared memory (else multi-tile)
 };
 
 struct MixedArgs {
@@ -65,6 +66,7 @@ struct MixedArgs {
   const double *u, *v;
   double *p;
   float *xbuf0, *xbuf1;        // exchange buffers: 2 colour planes of gh x gw
+  float *rbuf;                 // r of every unknown, same layout (multi-tile mode)
 };
 
 // Exchange-buffer element of cell (i, j), colour (i+j)&1, for halo H:
@@ -162,8 +164,8 @@ __device__ __forceinline__ unsigned int mixed_half_sweep(const MixedBox &b, int 
   return mixed_rows<K, C, 0>(b, h, act0, act1, relax);
 }
 
-// ns (<= K) sweeps.  With redm, each warp writes its maximum of sweep s to
-// redm[s][warp].
+// ns (<= K) sweeps.  With redm, each warp keeps its running maximum of
+// sweep s in redm[s][warp] (zeroed by the caller).
 template <int K>
 __device__ __forceinline__ void mixed_sweeps(const MixedBox &b, int ns, float relax,
                                              unsigned int (*redm)[32]) {
@@ -175,7 +177,10 @@ __device__ __forceinline__ void mixed_sweeps(const MixedBox &b, int ns, float re
     if (redm) {
       const unsigned int m = m0 > m1 ? m0 : m1;
       const unsigned int v = __reduce_max_sync(0xffffffffu, m);
-      if (b.lane == 0) redm[s][threadIdx.x >> 5] = v;
+      if (b.lane == 0) {
+        unsigned int &slot = redm[s][threadIdx.x >> 5];
+        slot = v > slot ? v : slot;
+      }
     }
     __syncthreads();
   }
@@ -321,10 +326,10 @@ __device__ __forceinline__ void mixed_redo(const MixedBox &b, int ns, float rela
 }
 
 // Bytes of dynamic shared memory for a tile of tx x ty unknowns: the two
-// colour planes of e, their snapshot and the two planes of r.
-__host__ __device__ inline size_t mixed_smem_bytes(int K, int tx, int ty) {
+// colour planes of e and of r, and (resident mode) the snapshot of e.
+__host__ __device__ inline size_t mixed_smem_bytes(int K, int tx, int ty, bool resident = true) {
   const size_t bw = (size_t)tx + 4 * K, bh = (size_t)ty + 4 * K;
-  return 6 * bh * (bw / 2) * sizeof(float);
+  return (resident ? 6 : 4) * bh * (bw / 2) * sizeof(float);
 }
 
 // Threads of a block for a tile of tx x ty unknowns: whole warps over the
@@ -335,27 +340,14 @@ __host__ __device__ inline int mixed_threads(int K, int tx, int ty) {
   return hwp * ((rows + kMixedRows - 1) / kMixedRows);
 }
 
-// The whole mixed Ppe: Divergence and b = div/dk in FP64, then refinement
-// passes until the stopping rule fires or msorit sweeps are done.  Returns
-// nConv (0 = not converged) or -1 on a barrier error.
+// The box of tile `tile` and this thread's place in it.  Resident mode keeps
+// planes E, E0, R; multi-tile mode E and R.
 template <int K>
-__device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
+__device__ __forceinline__ void mixed_setup(const Dev &d, const MixedGeom &g, MixedBox &b,
+                                            int tile, float *fs, bool resident) {
   constexpr int H = 2 * K;
-  Sync *sy = d.sync;
-  unsigned long long *ring = &sy->red[kMixedRing];
-  if (blockIdx.x == 0 && threadIdx.x == 0)
-    for (int k = 0; k < 3 * K; ++k) ring[k] = 0ull;
-  ppe_divergence(d, a.u, a.v);
-  if (!grid_sync(sy)) return -1;
-  ppe_rhs_grid(d, a.lcartes, a.dk, a.p);
-  if (!grid_sync(sy)) return -1;
-
-  extern __shared__ double smem[];
-  float *fs = reinterpret_cast<float *>(smem);
-  const bool has = (int)blockIdx.x < g.ntx * g.nty;
-  MixedBox b;
-  b.ti = blockIdx.x % g.ntx;
-  b.tj = blockIdx.x / g.ntx;
+  b.ti = tile % g.ntx;
+  b.tj = tile / g.ntx;
   b.oi0 = 2 + b.ti * g.tx;
   b.oj0 = 2 + b.tj * g.ty;
   b.oi1 = min(d.nx, b.oi0 + g.tx - 1);
@@ -365,14 +357,18 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
   b.bw = g.tx + 2 * H;
   b.bh = g.ty + 2 * H;
   b.hw = b.bw / 2;
-  {
-    const int plane = b.bh * b.hw;
-    b.E[0] = fs;
-    b.E[1] = fs + plane;
+  const int plane = b.bh * b.hw;
+  b.E[0] = fs;
+  b.E[1] = fs + plane;
+  if (resident) {
     b.E0[0] = fs + 2 * plane;
     b.E0[1] = fs + 3 * plane;
     b.R[0] = fs + 4 * plane;
     b.R[1] = fs + 5 * plane;
+  } else {
+    b.E0[0] = b.E0[1] = nullptr;
+    b.R[0] = fs + 2 * plane;
+    b.R[1] = fs + 3 * plane;
   }
   b.k = (int)threadIdx.x % g.hwp;
   b.lane = (int)threadIdx.x & 31;
@@ -386,13 +382,128 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
   b.vrow = 0u;
   for (int r = 0; r < kMixedRows; ++r)
     if (mixed_drow(d, b, b.jj0 + r, H) > 0) b.vrow |= 1u << r;
+}
+
+// Position of cell (i, j) in a colour-split buffer (see MixedBox).
+template <int K>
+__device__ __forceinline__ size_t mixed_gpos(const MixedGeom &g, int i, int j) {
+  constexpr int H = 2 * K;
+  return (size_t)((i + j) & 1) * g.gh * g.gw + (size_t)(j + H - 2) * g.gw + ((i + H - 2) >> 1);
+}
+
+// ---- multi-tile mode: blocks loop over tiles, staging whole boxes -------
+
+// The whole box of one colour-split buffer into two shared planes (zeros
+// when G is null).
+template <int K>
+__device__ __noinline__ void mixed_box_load(const MixedGeom &g, const MixedBox &b, const float *G,
+                                            float *P0, float *P1) {
+  const int hv = b.hw / 4, total = 2 * b.bh * hv;
+  const size_t plane = (size_t)g.gh * g.gw;
+  const int row0 = b.tj * g.ty, col0 = b.ti * g.tx / 2;
+  for (int f = threadIdx.x; f < total; f += blockDim.x) {
+    const int c = f >= b.bh * hv ? 1 : 0;
+    const int gg = f - c * b.bh * hv;
+    const int jj = gg / hv, kk = 4 * (gg - jj * hv);
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (G) v = *reinterpret_cast<const float4 *>(G + c * plane + (size_t)(row0 + jj) * g.gw + col0 + kk);
+    *reinterpret_cast<float4 *>((c ? P1 : P0) + jj * b.hw + kk) = v;
+  }
+}
+
+// The own tile of the shared e planes to a colour-split buffer.
+template <int K>
+__device__ __noinline__ void mixed_tile_store(const MixedGeom &g, const MixedBox &b, float *G) {
+  const int tv = g.tx / 8, total = 2 * g.ty * tv;
+  const size_t plane = (size_t)g.gh * g.gw;
+  const int row0 = b.tj * g.ty, col0 = b.ti * g.tx / 2;
+  for (int f = threadIdx.x; f < total; f += blockDim.x) {
+    const int c = f >= g.ty * tv ? 1 : 0;
+    const int gg = f - c * g.ty * tv;
+    const int r = gg / tv, seg = gg - r * tv;
+    const int jj = 2 * K + r, kk = K + 4 * seg;
+    *reinterpret_cast<float4 *>(G + c * plane + (size_t)(row0 + jj) * g.gw + col0 + kk) =
+        *reinterpret_cast<const float4 *>(b.E[c] + jj * b.hw + kk);
+  }
+}
+
+// r = b - A p in FP64 on the own unknowns of a tile, into the r buffer.
+template <int K>
+__device__ __noinline__ void mixed_residual_tile(const Dev &d, const MixedGeom &g,
+                                                 const MixedBox &b, const double *p, float *Rg) {
+  const int tw = b.oi1 - b.oi0 + 1, th = b.oj1 - b.oj0 + 1;
+  for (int t = threadIdx.x; t < tw * th; t += blockDim.x) {
+    const int i = b.oi0 + t % tw, j = b.oj0 + t / tw;
+    const size_t o = IX(d, i, j);
+    const double ap = p[o - d.ld] + p[o - 1] + p[o + 1] + p[o + d.ld] - 4.0 * p[o];
+    Rg[mixed_gpos<K>(g, i, j)] = (float)(d.pb[o] - ap);
+  }
+}
+
+// p += e on the own unknowns of a tile, e from a colour-split buffer.
+template <int K>
+__device__ __noinline__ void mixed_correct_tile(const Dev &d, const MixedGeom &g,
+                                                const MixedBox &b, double *p, const float *G) {
+  const int tw = b.oi1 - b.oi0 + 1, th = b.oj1 - b.oj0 + 1;
+  for (int t = threadIdx.x; t < tw * th; t += blockDim.x) {
+    const int i = b.oi0 + t % tw, j = b.oj0 + t / tw;
+    const size_t o = IX(d, i, j);
+    p[o] = p[o] + (double)G[mixed_gpos<K>(g, i, j)];
+  }
+}
+
+// Block maxima of ns sweeps into the global slots.
+__device__ __forceinline__ void mixed_flush_maxima(unsigned int (*redm)[32], int ns,
+                                                   unsigned long long *slots) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  for (int s = wid; s < ns; s += nw) {
+    const unsigned int v = __reduce_max_sync(0xffffffffu, lane < nw ? redm[s][lane] : 0u);
+    if (lane == 0 && v)
+      atomicMax(&slots[s], (unsigned long long)__double_as_longlong((double)__uint_as_float(v)));
+  }
+}
+
+// The whole mixed Ppe: Divergence and b = div/dk in FP64, then refinement
+// passes until the stopping rule fires or msorit sweeps are done.  One tile
+// per block keeps the box resident in shared memory between groups (only the
+// halo ring is exchanged); with more tiles than blocks, each block stages
+// the whole box of each of its tiles every group.  Returns nConv (0 = not
+// converged) or -1 on a barrier error.
+template <int K>
+__device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
+  Sync *sy = d.sync;
+  unsigned long long *ring = &sy->red[kMixedRing];
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+    for (int k = 0; k < 3 * K; ++k) ring[k] = 0ull;
+  ppe_divergence(d, a.u, a.v);
+  if (!grid_sync(sy)) return -1;
+  ppe_rhs_grid(d, a.lcartes, a.dk, a.p);
+  if (!grid_sync(sy)) return -1;
+
+  extern __shared__ double smem[];
+  __shared__ unsigned int redm[K][32];
+  float *fs = reinterpret_cast<float *>(smem);
+  const int ntiles = g.ntx * g.nty;
+  const bool resident = g.resident != 0;
+  const bool has = (int)blockIdx.x < ntiles;
+  MixedBox b;
+  if (resident) mixed_setup<K>(d, g, b, blockIdx.x, fs, true);
 
   int m = 0, result = 0, grp = 0;
   bool done = false;
   while (!done) {
-    if (has) mixed_residual(d, b, a.p);
-    __syncthreads();
+    if (resident) {
+      if (has) mixed_residual(d, b, a.p);
+      __syncthreads();
+    } else {
+      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        mixed_setup<K>(d, g, b, tile, fs, false);
+        mixed_residual_tile<K>(d, g, b, a.p, a.rbuf);
+      }
+      if (!grid_sync(sy)) return -1;
+    }
     int q = 0, in_pass = 0;
+    const float *efinal = nullptr;
     while (true) {
       const int ns = min(K, min(a.inner - in_pass, a.msorit - m));
       unsigned long long *slots = ring + (grp % 3) * K;
@@ -402,7 +513,21 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
       }
       const float *ein = q == 0 ? nullptr : ((q & 1) ? a.xbuf0 : a.xbuf1);
       float *eout = (q & 1) ? a.xbuf1 : a.xbuf0;
-      if (has) mixed_group<K>(g, b, ns, a.relax, ein, eout, slots);
+      if (resident) {
+        if (has) mixed_group<K>(g, b, ns, a.relax, ein, eout, slots);
+      } else {
+        for (int t = threadIdx.x; t < K * 32; t += blockDim.x) redm[t / 32][t % 32] = 0u;
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+          mixed_setup<K>(d, g, b, tile, fs, false);
+          mixed_box_load<K>(g, b, ein, b.E[0], b.E[1]);
+          mixed_box_load<K>(g, b, a.rbuf, b.R[0], b.R[1]);
+          __syncthreads();
+          mixed_sweeps<K>(b, ns, a.relax, redm);
+          mixed_tile_store<K>(g, b, eout);
+          __syncthreads();
+        }
+        mixed_flush_maxima(redm, ns, slots);
+      }
       if (!grid_sync(sy)) return -1;
       int conv = -1;
       for (int s = 0; s < ns; ++s) {
@@ -413,9 +538,25 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
       }
       ++grp;
       ++q;
+      efinal = eout;
       if (conv >= 0) {
         result = m + conv + 1;
-        if (has && conv < ns - 1) mixed_redo<K>(b, conv + 1, a.relax);
+        if (conv < ns - 1) {
+          if (resident) {
+            if (has) mixed_redo<K>(b, conv + 1, a.relax);
+          } else {
+            // the group's input buffer is intact: sweep again from it
+            for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+              mixed_setup<K>(d, g, b, tile, fs, false);
+              mixed_box_load<K>(g, b, ein, b.E[0], b.E[1]);
+              mixed_box_load<K>(g, b, a.rbuf, b.R[0], b.R[1]);
+              __syncthreads();
+              mixed_sweeps<K>(b, conv + 1, a.relax, nullptr);
+              mixed_tile_store<K>(g, b, eout);
+              __syncthreads();
+            }
+          }
+        }
         done = true;
         break;
       }
@@ -427,7 +568,14 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
       }
       if (in_pass >= a.inner) break;
     }
-    if (has) mixed_correct(d, b, a.p);
+    if (resident) {
+      if (has) mixed_correct(d, b, a.p);
+    } else {
+      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        mixed_setup<K>(d, g, b, tile, fs, false);
+        mixed_correct_tile<K>(d, g, b, a.p, efinal);
+      }
+    }
     if (!grid_sync(sy)) return -1;
   }
   return result;

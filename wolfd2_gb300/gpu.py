@@ -105,7 +105,7 @@ def lib():
     L.wolfd2gpu_last_error.argtypes = [vp]
     L.wolfd2gpu_last_error.restype = C.c_char_p
     L.wolfd2gpu_tune.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
-    L.wolfd2gpu_tune_mixed.argtypes = [vp, C.c_int, C.c_int]
+    L.wolfd2gpu_tune_mixed.argtypes = [vp, C.c_int, C.c_int, C.c_int]
     L.wolfd2gpu_set_precision.argtypes = [vp, C.c_int, C.c_int]
     L.wolfd2gpu_device_fields.argtypes = [vp, C.POINTER(_dp), C.POINTER(_dp), C.POINTER(_dp), _ip]
     L.wolfd2gpu_launch_count.argtypes = [vp]
@@ -227,10 +227,11 @@ class Solver:
     def tune(self, seg: int = 0, warm: int = 0, threads: int = 0, blocks_per_sm: int = 0):
         self._check(self.L.wolfd2gpu_tune(self.h, seg, warm, threads, blocks_per_sm))
 
-    def tune_mixed(self, sweeps_per_barrier: int = 0, threads: int = 0):
-        """Mixed Poisson kernel shape: sweeps between grid barriers (2, 4, 8)
-        and threads per block; 0 keeps the current value."""
-        self._check(self.L.wolfd2gpu_tune_mixed(self.h, sweeps_per_barrier, threads))
+    def tune_mixed(self, sweeps_per_barrier: int = 0, threads: int = 0, mode: int = 0):
+        """Mixed Poisson kernel shape: sweeps between grid barriers (4, 8),
+        the block-size limit (0 keeps the current value), and the tile mode
+        (0 auto, 1 several tiles per block, 2 the same on <= 16 blocks)."""
+        self._check(self.L.wolfd2gpu_tune_mixed(self.h, sweeps_per_barrier, threads, mode))
 
     def set_precision(self, precision: int, refine_sweeps: int = 0):
         """Precision of the drop-in Ppe (PREC_FP64 or PREC_MIXED)."""
