@@ -191,6 +191,16 @@ const char *wolfd2gpu_last_error(w2_ctx *ctx);
 int wolfd2gpu_tune(w2_ctx *ctx, int chain_seg, int chain_warm, int threads,
                    int blocks_per_sm);
 
+/* Per-position values on one region face (no counterpart in the reference,
+ * whose faces carry one constant per variable; used for the parabolic
+ * inflow and the lid profile of the benchmark decks): the inlet or
+ * moving-wall value of variable var (1 = u, 2 = v) at position pos along the
+ * face -- j on west/east faces, i on south/north faces -- becomes
+ * values[pos], pos = 0..n-1 (n = ny+2 or nx+2).  values = NULL restores the
+ * region constant dBCVal.  At most 16 profiles per context. */
+int wolfd2gpu_set_face_profile(w2_ctx *ctx, int ireg, int jreg, int face, int var,
+                               const double *values, int n);
+
 /* Precision of the drop-in wolfd2gpu_ppe on this context (W2_PREC_*) and
  * FP32 sweeps per refinement pass (0 = auto).  No counterpart in the
  * reference, whose Ppe is FP64 only. */

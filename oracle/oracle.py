@@ -32,7 +32,7 @@ class _Regions(C.Structure):
     _fields_ = [("mgri", C.c_int), ("mgrj", C.c_int), ("nReg", _ip),
                 ("nRegBrd", _ip), ("nRegType", _ip), ("nMomBdTp", _ip),
                 ("dBCVal", _dp), ("dPRporos", _dp), ("dPRporc1", _dp),
-                ("dPRporc2", _dp)]
+                ("dPRporc2", _dp), ("prof", C.POINTER(_dp))]
 
 
 class _Metrics(C.Structure):
@@ -162,9 +162,19 @@ class Oracle:
                 ("nReg", "nRegBrd", "nRegType", "nMomBdTp")]
         darrs = [np.asfortranarray(getattr(regs, n)) for n in
                  ("dBCVal", "dPRporos", "dPRporc1", "dPRporc2")]
-        s = _Regions(regs.nRegBrd.shape[0], regs.nRegBrd.shape[1],
-                     *[_ptr(a, C.c_int) for a in arrs], *[_ptr(a) for a in darrs])
-        s._keep = (arrs, darrs)
+        mgri, mgrj = regs.nRegBrd.shape[0], regs.nRegBrd.shape[1]
+        profs = getattr(regs, "profiles", None) or {}
+        table, keep = None, []
+        if profs:
+            table = (_dp * (mgri * mgrj * 4 * 2))()
+            for (ir, jr, face, var), vals in profs.items():
+                a = np.ascontiguousarray(vals, np.float64)
+                keep.append(a)
+                table[((ir - 1) + (jr - 1) * mgri + (face - 1) * mgri * mgrj) * 2 + (var - 1)] = \
+                    a.ctypes.data_as(_dp)
+        s = _Regions(mgri, mgrj, *[_ptr(a, C.c_int) for a in arrs], *[_ptr(a) for a in darrs],
+                     C.cast(table, C.POINTER(_dp)) if table is not None else None)
+        s._keep = (arrs, darrs, table, keep)
         return s
 
     @staticmethod

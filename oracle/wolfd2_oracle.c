@@ -66,6 +66,14 @@ struct w2o_ctx {
   (r)->dBCVal[((ir)-1) + ((jr)-1) * (r)->mgri + ((s)-1) * (r)->mgri * (r)->mgrj + \
               ((var)-1) * (r)->mgri * (r)->mgrj * 4]
 #define RPAR(arr, r, ir, jr) (r)->arr[((ir)-1) + ((jr)-1) * (r)->mgri]
+/* A face value at position pos: the per-position profile when one is set
+ * (test shim for inflow and lid profiles), else the region constant. */
+#define PKEY(r, ir, jr, s, var) \
+  ((((ir)-1) + ((jr)-1) * (r)->mgri + ((s)-1) * (r)->mgri * (r)->mgrj) * 2 + ((var)-1))
+#define BCVP(r, ir, jr, s, var, pos)                                   \
+  (((r)->prof && (r)->prof[PKEY(r, ir, jr, s, var)])                   \
+       ? (r)->prof[PKEY(r, ir, jr, s, var)][pos]                       \
+       : BCV(r, ir, jr, s, var))
 
 static void die(const char *msg, int ir, int jr) {
   fprintf(stderr, "%s in region %d,%d\n", msg, ir, jr);
@@ -761,16 +769,16 @@ void w2o_vel_bound_cond(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
         case BM_WALL1:
           for (j = jS; j <= jN; j++) F(u, iW, j) = 0.0;
           for (j = jS + 1; j <= jN; j++)
-            F(v, iW, j) = 2.0 * BCV(r, ireg, jreg, WEST, VV) - F(v, iW + 1, j);
+            F(v, iW, j) = 2.0 * BCVP(r, ireg, jreg, WEST, VV, j) - F(v, iW + 1, j);
           break;
         case BM_WALL2:
           for (j = jS; j <= jN; j++) F(u, iW, j) = 0.0;
           for (j = jS + 1; j <= jN; j++) F(v, iW, j) = F(v, iW + 1, j);
           break;
         case BM_INLET:
-          for (j = jS; j <= jN; j++) F(u, iW, j) = BCV(r, ireg, jreg, WEST, VU);
+          for (j = jS; j <= jN; j++) F(u, iW, j) = BCVP(r, ireg, jreg, WEST, VU, j);
           for (j = jS + 1; j <= jN; j++)
-            F(v, iW, j) = 2.0 * BCV(r, ireg, jreg, WEST, VV) - F(v, iW + 1, j);
+            F(v, iW, j) = 2.0 * BCVP(r, ireg, jreg, WEST, VV, j) - F(v, iW + 1, j);
           break;
         case BM_OUTLT1:
           for (j = jS; j <= jN; j++) F(u, iW - 1, j) = BCV(r, ireg, jreg, WEST, VU) + F(u, iW, j);
@@ -790,16 +798,16 @@ void w2o_vel_bound_cond(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
         case BM_WALL1:
           for (j = jS; j <= jN; j++) F(u, iE, j) = 0.0;
           for (j = jS + 1; j <= jN; j++)
-            F(v, iE + 1, j) = 2.0 * BCV(r, ireg, jreg, EAST, VV) - F(v, iE, j);
+            F(v, iE + 1, j) = 2.0 * BCVP(r, ireg, jreg, EAST, VV, j) - F(v, iE, j);
           break;
         case BM_WALL2:
           for (j = jS; j <= jN; j++) F(u, iE, j) = 0.0;
           for (j = jS + 1; j <= jN; j++) F(v, iE + 1, j) = F(v, iE, j);
           break;
         case BM_INLET:
-          for (j = jS; j <= jN; j++) F(u, iE, j) = BCV(r, ireg, jreg, EAST, VU);
+          for (j = jS; j <= jN; j++) F(u, iE, j) = BCVP(r, ireg, jreg, EAST, VU, j);
           for (j = jS + 1; j <= jN; j++)
-            F(v, iE + 1, j) = 2.0 * BCV(r, ireg, jreg, EAST, VV) - F(v, iE, j);
+            F(v, iE + 1, j) = 2.0 * BCVP(r, ireg, jreg, EAST, VV, j) - F(v, iE, j);
           break;
         case BM_OUTLT1:
           for (j = jS; j <= jN; j++) F(u, iE + 1, j) = BCV(r, ireg, jreg, EAST, VU) + F(u, iE, j);
@@ -818,7 +826,7 @@ void w2o_vel_bound_cond(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
         case BM_INTERN: break;
         case BM_WALL1:
           for (i = iW + 1; i <= iE; i++)
-            F(u, i, jS) = 2.0 * BCV(r, ireg, jreg, SOUTH, VU) - F(u, i, jS + 1);
+            F(u, i, jS) = 2.0 * BCVP(r, ireg, jreg, SOUTH, VU, i) - F(u, i, jS + 1);
           for (i = iW; i <= iE; i++) F(v, i, jS) = 0.0;
           break;
         case BM_WALL2:
@@ -827,8 +835,8 @@ void w2o_vel_bound_cond(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
           break;
         case BM_INLET:
           for (i = iW + 1; i <= iE; i++)
-            F(u, i, jS) = 2.0 * BCV(r, ireg, jreg, SOUTH, VU) - F(u, i, jS + 1);
-          for (i = iW; i <= iE; i++) F(v, i, jS) = BCV(r, ireg, jreg, SOUTH, VV);
+            F(u, i, jS) = 2.0 * BCVP(r, ireg, jreg, SOUTH, VU, i) - F(u, i, jS + 1);
+          for (i = iW; i <= iE; i++) F(v, i, jS) = BCVP(r, ireg, jreg, SOUTH, VV, i);
           break;
         case BM_OUTLT1:
           for (i = iW + 1; i <= iE; i++) F(u, i, jS) = -F(u, i, jS + 1);
@@ -847,7 +855,7 @@ void w2o_vel_bound_cond(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
         case BM_INTERN: break;
         case BM_WALL1:
           for (i = iW + 1; i <= iE; i++)
-            F(u, i, jN + 1) = 2.0 * BCV(r, ireg, jreg, NORTH, VU) - F(u, i, jN);
+            F(u, i, jN + 1) = 2.0 * BCVP(r, ireg, jreg, NORTH, VU, i) - F(u, i, jN);
           for (i = iW; i <= iE; i++) F(v, i, jN) = 0.0;
           break;
         case BM_WALL2:
@@ -856,8 +864,8 @@ void w2o_vel_bound_cond(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
           break;
         case BM_INLET:
           for (i = iW + 1; i <= iE; i++)
-            F(u, i, jN + 1) = 2.0 * BCV(r, ireg, jreg, NORTH, VU) - F(u, i, jN);
-          for (i = iW; i <= iE; i++) F(v, i, jN) = BCV(r, ireg, jreg, NORTH, VV);
+            F(u, i, jN + 1) = 2.0 * BCVP(r, ireg, jreg, NORTH, VU, i) - F(u, i, jN);
+          for (i = iW; i <= iE; i++) F(v, i, jN) = BCVP(r, ireg, jreg, NORTH, VV, i);
           break;
         case BM_OUTLT1:
           for (i = iW + 1; i <= iE; i++) F(u, i, jN + 1) = -F(u, i, jN);

@@ -50,6 +50,12 @@ typedef struct {
   const double *dPRporos;  /* dPRporos(mgri,mgrj)                      */
   const double *dPRporc1;
   const double *dPRporc2;
+  /* Per-position face values (no counterpart in the reference): NULL, or
+   * mgri*mgrj*4*2 pointers, entry ((ir-1) + (jr-1)*mgri + (face-1)*mgri*mgrj)*2
+   * + (var-1) (var 1 = u, 2 = v), each NULL or the values at position pos
+   * along the face (j on west/east, i on south/north faces).  They replace
+   * dBCVal in VelBoundCond's inlet and moving-wall rows. */
+  const double *const *prof;
 } w2o_regions;
 
 /* The 30 metric arrays produced by grid.f:Metric, each (0:mnx,0:mny). */

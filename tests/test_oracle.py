@@ -94,3 +94,47 @@ def test_golden_cavity64():
     for k in ("u", "v", "p"):
         assert math.fsum(r.f[k].ravel()) == g["sum"][k]
         assert math.fsum(np.abs(r.f[k]).ravel()) == g["abs_sum"][k]
+
+
+def test_face_profile_of_constants_equals_region_constant():
+    """The per-position face values (an extension for inflow/lid profiles)
+    reduce to the reference's region constant when every value equals it."""
+    from wolfd2_gb300 import deck as D
+    base = D.channel(48, 16, 500.0, 0.004, length=3.0, solver="rb_sor")
+    prof = D.channel(48, 16, 500.0, 0.004, length=3.0, solver="rb_sor")
+    prof.regions.profiles[(1, 1, D.WEST, 1)] = np.full(prof.ny + 2, 1.0)
+    a, b = O.OracleRun(base), O.OracleRun(prof)
+    a.step(3)
+    b.step(3)
+    assert a.history == b.history
+    for n in "uvp":
+        assert np.array_equal(a.f[n], b.f[n])
+    lid = D.cavity(32, 100.0, 0.005, solver="rb_sor")
+    run0 = O.OracleRun(lid)
+    run0.step(2)
+    lid.regions.profiles[(1, 1, D.NORTH, 1)] = np.full(lid.nx + 2, 1.0)
+    run1 = O.OracleRun(lid)
+    run1.step(2)
+    assert run0.history == run1.history
+
+
+def test_profiled_channel_outlet_types():
+    """Profiled channel at the channel workload's CFL (dx = dy = 1/32,
+    dt = 8e-3, Re = 1e4): with the mass-conserving outlet (BM_OUTLT2) the
+    inflow is balanced and the divergence stays small; with the fully
+    developed outlet (BM_OUTLT1) the all-Neumann pressure problem has no
+    solution and the pressure change grows by a factor > 2 per step."""
+    import mixed as MX
+    from wolfd2_gb300 import deck as D
+    res = {}
+    for outlet in ("mc", "fd"):
+        case = D.channel_inflow(128, 32, 1.0e4, 8.0e-3, seed=1234, outlet=outlet)
+        u0, v0, p0 = D.channel_ic(case)
+        r = O.OracleRun(case, fields={"u": u0, "v": v0, "p": p0}, cold_start=False)
+        r.step(4)
+        res[outlet] = ([h[2][0] for h in r.history],
+                       MX.div_check(case.nx, case.ny, r.met, r.f["u"], r.f["v"]))
+    dp, div = res["mc"]
+    assert div < 1.0e-5 and dp[-1] < dp[0]
+    dp, div = res["fd"]
+    assert all(b > 2.0 * a for a, b in zip(dp, dp[1:])) and div > 1.0e-3

@@ -62,6 +62,11 @@ struct w2_ctx {
   // single-precision momentum state (mixed path), made on first use
   bool f32_alloc = false, f32_metrics_ok = false;
   float *F32[4] = {};  // un, vn, us, vs
+  // per-position face values (wolfd2gpu_set_face_profile)
+  int *prof_idx = nullptr;   // device table, -1 = region constant
+  double *prof = nullptr;    // device values, kMaxProfiles x prof_len
+  int prof_len = 0, prof_used = 0;
+  std::vector<int> prof_host;
   // split-2 identity rows in chain order, and their by-position device copies
   std::vector<uint8_t> zx, zy;
   uint8_t *bzx = nullptr, *bzy = nullptr;
@@ -591,10 +596,10 @@ int momentum_metrics(w2_ctx *c) {
 
 // ---- mixed-precision Poisson sweeps ----------------------------------------
 
-const void *mixed_kernel(int K) {
+const void *mixed_kernel(int K, bool resident) {
   switch (K) {
-    case 4: return (const void *)k_ppe_mixed<4>;
-    case 8: return (const void *)k_ppe_mixed<8>;
+    case 4: return resident ? (const void *)k_ppe_mixed<4, true> : (const void *)k_ppe_mixed<4, false>;
+    case 8: return resident ? (const void *)k_ppe_mixed<8, true> : (const void *)k_ppe_mixed<8, false>;
   }
   return nullptr;
 }
@@ -610,15 +615,9 @@ const void *mixed_kernel(int K) {
 void plan_mixed(w2_ctx *c) {
   c->mixed_ok = false;
   const int K = c->mixed_K;
-  const void *kf = mixed_kernel(K);
-  if (!kf) return;
+  if (!mixed_kernel(K, true)) return;
   int maxsmem = 0;
   cudaDeviceGetAttribute(&maxsmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
-  cudaFuncAttributes fa{};
-  if (cudaFuncGetAttributes(&fa, kf) != cudaSuccess || (size_t)maxsmem <= fa.sharedSizeBytes) return;
-  const size_t limit = (size_t)maxsmem - fa.sharedSizeBytes;  // less the static arrays
-  if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit) != cudaSuccess)
-    return;
   const int NX = c->nx - 1, NY = c->ny - 1, H = 2 * K;
   auto sweep_work = [&](int tx, int ty) {
     const int bh = ty + 2 * H, hwp = (tx / 2 + H + 31) / 32 * 32;
@@ -628,6 +627,12 @@ void plan_mixed(w2_ctx *c) {
   };
   for (int pass = c->mixed_mode ? 1 : 0; pass < 2 && !c->mixed_ok; ++pass) {
     const bool resident = pass == 0;
+    const void *kf = mixed_kernel(K, resident);
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, kf) != cudaSuccess || (size_t)maxsmem <= fa.sharedSizeBytes) continue;
+    const size_t limit = (size_t)maxsmem - fa.sharedSizeBytes;  // less the static arrays
+    if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit) != cudaSuccess)
+      continue;
     double best = 1e300;
     for (int ntx = 1; ntx <= std::max(1, NX / 8); ++ntx) {
       int tx = (NX + ntx - 1) / ntx;
@@ -714,7 +719,7 @@ int launch_ppe_mixed(w2_ctx *c, int lcartes, int msorit, double dk, double sorto
   void *args[] = {&d, &g, &a, &out};
   c->launches++;
   const int T = mixed_threads(c->mixed_K, g.tx, g.ty);
-  cudaError_t e = cudaLaunchCooperativeKernel(mixed_kernel(c->mixed_K), dim3(c->mixed_blocks),
+  cudaError_t e = cudaLaunchCooperativeKernel(mixed_kernel(c->mixed_K, c->mg.resident != 0), dim3(c->mixed_blocks),
                                               dim3(T), args, c->mixed_smem, c->st);
   if (e != cudaSuccess) return fail(c, W2_E_CUDA, "mixed PPE launch: %s", cudaGetErrorString(e));
   return W2_OK;
@@ -941,6 +946,41 @@ static int finish_coefficients(w2_ctx *c) {
   return momentum_metrics(c);
 }
 
+int wolfd2gpu_set_face_profile(w2_ctx *c, int ireg, int jreg, int face, int var,
+                               const double *values, int n) {
+  if (!c) return W2_E_ARG;
+  if (ireg < 1 || ireg > c->mgri || jreg < 1 || jreg > c->mgrj || face < W2_WEST ||
+      face > W2_NORTH || var < 1 || var > 2)
+    return fail(c, W2_E_ARG, "bad face profile key");
+  const int want = (face == W2_WEST || face == W2_EAST) ? c->ny + 2 : c->nx + 2;
+  if (values && n != want) return fail(c, W2_E_ARG, "face profile needs %d values, got %d", want, n);
+  constexpr int kMaxProfiles = 16;
+  const int key = ((ireg - 1) + (jreg - 1) * c->mgri + (face - 1) * c->mgri * c->mgrj) * 2 + (var - 1);
+  if (!c->prof_idx) {
+    c->prof_host.assign((size_t)c->mgri * c->mgrj * 8, -1);
+    c->prof_len = std::max(c->nx, c->ny) + 2;
+    if (!(c->prof_idx = dalloc<int>(c, c->prof_host.size())) ||
+        !(c->prof = dalloc<double>(c, (size_t)kMaxProfiles * c->prof_len)))
+      return fail(c, W2_E_CUDA, "out of device memory (face profiles)");
+  }
+  if (!values) {
+    c->prof_host[key] = -1;
+  } else {
+    int off = c->prof_host[key];
+    if (off < 0) {
+      if (c->prof_used >= kMaxProfiles) return fail(c, W2_E_ARG, "at most %d face profiles", kMaxProfiles);
+      off = c->prof_used++ * c->prof_len;
+      c->prof_host[key] = off;
+    }
+    CK(cudaMemcpy(c->prof + off, values, (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  CK(cudaMemcpy(c->prof_idx, c->prof_host.data(), c->prof_host.size() * sizeof(int),
+                cudaMemcpyHostToDevice));
+  c->dev.prof_idx = c->prof_idx;
+  c->dev.prof = c->prof;
+  return W2_OK;
+}
+
 int wolfd2gpu_set_precision(w2_ctx *c, int precision, int refine_sweeps) {
   if (!c) return W2_E_ARG;
   if (precision != W2_PREC_FP64 && precision != W2_PREC_MIXED)
@@ -955,7 +995,7 @@ int wolfd2gpu_tune_mixed(w2_ctx *c, int sweeps_per_barrier, int threads, int mod
   if (!c) return W2_E_ARG;
   if (mode < 0 || mode > 2) return fail(c, W2_E_ARG, "tile mode must be 0, 1 or 2");
   c->mixed_mode = mode;
-  if (sweeps_per_barrier != 0 && !mixed_kernel(sweeps_per_barrier))
+  if (sweeps_per_barrier != 0 && !mixed_kernel(sweeps_per_barrier, true))
     return fail(c, W2_E_ARG, "sweeps per barrier must be 4 or 8");
   if (threads != 0 && (threads % 32 || threads < 64 || threads > kMixedThreads))
     return fail(c, W2_E_ARG, "thread limit must be a multiple of 32 in 64..%d", kMixedThreads);

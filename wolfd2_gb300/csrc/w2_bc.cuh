@@ -21,6 +21,19 @@ enum { VAR_U = 1, VAR_V = 2, VAR_P = 3 };
 #define W2_SFOR(var, lo, hi) if (threadIdx.x == 0) for (int var = (lo); var <= (hi); ++var)
 #define W2_SYNC() __syncthreads()
 
+// Value of a face's boundary variable (VAR_U, VAR_V) at position pos along
+// the face (j on west/east faces, i on south/north faces): the values set by
+// wolfd2gpu_set_face_profile when there are any (an extension for inflow and
+// lid profiles), else the region constant dBCVal.
+__device__ __forceinline__ double bcv_at(const Dev &d, int ir, int jr, int face, int var, int pos) {
+  if (d.prof_idx) {
+    const int k = d.prof_idx[((ir - 1) + (jr - 1) * d.r.mgri + (face - 1) * d.r.mgri * d.r.mgrj) * 2 +
+                             (var - 1)];
+    if (k >= 0) return d.prof[k + pos];
+  }
+  return d.r.BV(ir, jr, face, var);
+}
+
 // VelBoundCond, bound_cond.f:511-847.  Returns false on an invalid flag.
 __device__ bool vel_bound_cond_block(const Dev &d, double *u, double *v) {
   const Regions &r = d.r;
@@ -33,10 +46,9 @@ __device__ bool vel_bound_cond_block(const Dev &d, double *u, double *v) {
       switch (r.BT(ireg, jreg, WEST)) {
         case BM_INTERN: break;
         case BM_WALL1: {
-          const double vw = r.BV(ireg, jreg, WEST, VAR_V);
           W2_PFOR(j, jS, jN) UF(iW, j) = 0.0;
           W2_SYNC();
-          W2_PFOR(j, jS + 1, jN) VF(iW, j) = 2.0 * vw - VF(iW + 1, j);
+          W2_PFOR(j, jS + 1, jN) VF(iW, j) = 2.0 * bcv_at(d, ireg, jreg, WEST, VAR_V, j) - VF(iW + 1, j);
           W2_SYNC();
         } break;
         case BM_WALL2:
@@ -46,10 +58,9 @@ __device__ bool vel_bound_cond_block(const Dev &d, double *u, double *v) {
           W2_SYNC();
           break;
         case BM_INLET: {
-          const double uw = r.BV(ireg, jreg, WEST, VAR_U), vw = r.BV(ireg, jreg, WEST, VAR_V);
-          W2_PFOR(j, jS, jN) UF(iW, j) = uw;
+          W2_PFOR(j, jS, jN) UF(iW, j) = bcv_at(d, ireg, jreg, WEST, VAR_U, j);
           W2_SYNC();
-          W2_PFOR(j, jS + 1, jN) VF(iW, j) = 2.0 * vw - VF(iW + 1, j);
+          W2_PFOR(j, jS + 1, jN) VF(iW, j) = 2.0 * bcv_at(d, ireg, jreg, WEST, VAR_V, j) - VF(iW + 1, j);
           W2_SYNC();
         } break;
         case BM_OUTLT1: {
@@ -72,10 +83,9 @@ __device__ bool vel_bound_cond_block(const Dev &d, double *u, double *v) {
       switch (r.BT(ireg, jreg, EAST)) {
         case BM_INTERN: break;
         case BM_WALL1: {
-          const double ve = r.BV(ireg, jreg, EAST, VAR_V);
           W2_PFOR(j, jS, jN) UF(iE, j) = 0.0;
           W2_SYNC();
-          W2_PFOR(j, jS + 1, jN) VF(iE + 1, j) = 2.0 * ve - VF(iE, j);
+          W2_PFOR(j, jS + 1, jN) VF(iE + 1, j) = 2.0 * bcv_at(d, ireg, jreg, EAST, VAR_V, j) - VF(iE, j);
           W2_SYNC();
         } break;
         case BM_WALL2:
@@ -85,10 +95,9 @@ __device__ bool vel_bound_cond_block(const Dev &d, double *u, double *v) {
           W2_SYNC();
           break;
         case BM_INLET: {
-          const double ue = r.BV(ireg, jreg, EAST, VAR_U), ve = r.BV(ireg, jreg, EAST, VAR_V);
-          W2_PFOR(j, jS, jN) UF(iE, j) = ue;
+          W2_PFOR(j, jS, jN) UF(iE, j) = bcv_at(d, ireg, jreg, EAST, VAR_U, j);
           W2_SYNC();
-          W2_PFOR(j, jS + 1, jN) VF(iE + 1, j) = 2.0 * ve - VF(iE, j);
+          W2_PFOR(j, jS + 1, jN) VF(iE + 1, j) = 2.0 * bcv_at(d, ireg, jreg, EAST, VAR_V, j) - VF(iE, j);
           W2_SYNC();
         } break;
         case BM_OUTLT1: {
@@ -111,8 +120,7 @@ __device__ bool vel_bound_cond_block(const Dev &d, double *u, double *v) {
       switch (r.BT(ireg, jreg, SOUTH)) {
         case BM_INTERN: break;
         case BM_WALL1: {
-          const double us_ = r.BV(ireg, jreg, SOUTH, VAR_U);
-          W2_PFOR(i, iW + 1, iE) UF(i, jS) = 2.0 * us_ - UF(i, jS + 1);
+          W2_PFOR(i, iW + 1, iE) UF(i, jS) = 2.0 * bcv_at(d, ireg, jreg, SOUTH, VAR_U, i) - UF(i, jS + 1);
           W2_SYNC();
           W2_PFOR(i, iW, iE) VF(i, jS) = 0.0;
           W2_SYNC();
@@ -124,10 +132,9 @@ __device__ bool vel_bound_cond_block(const Dev &d, double *u, double *v) {
           W2_SYNC();
           break;
         case BM_INLET: {
-          const double us_ = r.BV(ireg, jreg, SOUTH, VAR_U), vs_ = r.BV(ireg, jreg, SOUTH, VAR_V);
-          W2_PFOR(i, iW + 1, iE) UF(i, jS) = 2.0 * us_ - UF(i, jS + 1);
+          W2_PFOR(i, iW + 1, iE) UF(i, jS) = 2.0 * bcv_at(d, ireg, jreg, SOUTH, VAR_U, i) - UF(i, jS + 1);
           W2_SYNC();
-          W2_PFOR(i, iW, iE) VF(i, jS) = vs_;
+          W2_PFOR(i, iW, iE) VF(i, jS) = bcv_at(d, ireg, jreg, SOUTH, VAR_V, i);
           W2_SYNC();
         } break;
         case BM_OUTLT1: {
@@ -150,8 +157,7 @@ __device__ bool vel_bound_cond_block(const Dev &d, double *u, double *v) {
       switch (r.BT(ireg, jreg, NORTH)) {
         case BM_INTERN: break;
         case BM_WALL1: {
-          const double un_ = r.BV(ireg, jreg, NORTH, VAR_U);
-          W2_PFOR(i, iW + 1, iE) UF(i, jN + 1) = 2.0 * un_ - UF(i, jN);
+          W2_PFOR(i, iW + 1, iE) UF(i, jN + 1) = 2.0 * bcv_at(d, ireg, jreg, NORTH, VAR_U, i) - UF(i, jN);
           W2_SYNC();
           W2_PFOR(i, iW, iE) VF(i, jN) = 0.0;
           W2_SYNC();
@@ -163,10 +169,9 @@ __device__ bool vel_bound_cond_block(const Dev &d, double *u, double *v) {
           W2_SYNC();
           break;
         case BM_INLET: {
-          const double un_ = r.BV(ireg, jreg, NORTH, VAR_U), vn_ = r.BV(ireg, jreg, NORTH, VAR_V);
-          W2_PFOR(i, iW + 1, iE) UF(i, jN + 1) = 2.0 * un_ - UF(i, jN);
+          W2_PFOR(i, iW + 1, iE) UF(i, jN + 1) = 2.0 * bcv_at(d, ireg, jreg, NORTH, VAR_U, i) - UF(i, jN);
           W2_SYNC();
-          W2_PFOR(i, iW, iE) VF(i, jN) = vn_;
+          W2_PFOR(i, iW, iE) VF(i, jN) = bcv_at(d, ireg, jreg, NORTH, VAR_V, i);
           W2_SYNC();
         } break;
         case BM_OUTLT1: {

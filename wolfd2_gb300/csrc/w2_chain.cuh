@@ -23,20 +23,34 @@
 //       of the sequential recurrence (induction from row 0, which is exact).
 //   B1/B2  the same for the back substitution x(k) = b'(k) - a3'(k) x(k+1),
 //       running from the last row down.
-// If rounds do not settle within kMaxRounds, one thread finishes the
-// recurrence sequentially (always exact, slow) and the fallback flag is set.
+// Round r leaves segments 0..r+1 exact, so at most nseg rounds run before a
+// round changes nothing; the loop is bounded by that count.  A NaN state
+// stays NaN through every later row of the recurrence (only +, -, *, /), so
+// two NaNs count as equal: the solve then matches the sequential one up to
+// NaN payloads, and a diverged flow settles in a few rounds like any other.
+// One warp walking the chain sequentially remains as a guard that a correct
+// build never reaches (it sets the fallback flag).
 #pragma once
 #include "w2_common.cuh"
 
 namespace w2 {
 
-constexpr int kMaxRounds = 24;
-
-__device__ __forceinline__ bool same_bits(double a, double b) {
-  return __double_as_longlong(a) == __double_as_longlong(b);
+// Bound of the verification rounds of one solve: every segment count plus
+// one settling round (see the induction above).
+__device__ __forceinline__ int max_rounds(int nseg0, int nseg1) {
+  return (nseg0 > nseg1 ? nseg0 : nseg1) + 1;
 }
-__device__ __forceinline__ bool same_bits(float a, float b) {
-  return __float_as_int(a) == __float_as_int(b);
+
+// Equal bits, or both NaN (integer tests: no floating-point pipe).
+__device__ __forceinline__ bool same_state(double a, double b) {
+  const unsigned long long x = (unsigned long long)__double_as_longlong(a),
+                           y = (unsigned long long)__double_as_longlong(b);
+  const unsigned long long inf = 0x7ff0000000000000ull, mag = 0x7fffffffffffffffull;
+  return x == y || ((x & mag) > inf && (y & mag) > inf);
+}
+__device__ __forceinline__ bool same_state(float a, float b) {
+  const unsigned x = (unsigned)__float_as_int(a), y = (unsigned)__float_as_int(b);
+  return x == y || ((x & 0x7fffffffu) > 0x7f800000u && (y & 0x7fffffffu) > 0x7f800000u);
 }
 
 // Storage position of chain row k: row r of segment s lives at r*nseg + s,
@@ -143,7 +157,7 @@ __device__ bool chain_f2(const ChainT<T> &c, int s, int L, const T *ein, T *eout
   T a3p = ein[2 * (s - 1)], bp = ein[2 * (s - 1) + 1];
   for (int k = k0, p = s; k < k1; ++k, p += ns) {
     fwd_row(c, k, p, a3p, bp);
-    if (same_bits(a3p, c.a3p[p]) && same_bits(bp, c.bp[p])) {
+    if (same_state(a3p, c.a3p[p]) && same_state(bp, c.bp[p])) {
       eout[2 * s] = ein[2 * s];
       eout[2 * s + 1] = ein[2 * s + 1];
       return false;
@@ -196,7 +210,7 @@ __device__ bool chain_b2(const ChainT<T> &c, int s, int L, const T *ein, T *eout
   T xn = ein[s + 1];
   for (int k = k1 - 1, p = (k1 - 1 - k0) * ns + s; k >= k0; --k, p -= ns) {
     xn = c.bp[p] - c.a3p[p] * xn;
-    if (same_bits(xn, c.x[p])) {
+    if (same_state(xn, c.x[p])) {
       eout[s] = ein[s];
       return false;
     }
@@ -292,6 +306,7 @@ __device__ bool solve_chains(const Dev &d, ChainT<T> c0, ChainT<T> c1, int nchai
   const int L = d.seg, W = d.warm;
   const int nseg0 = c0.nseg, nseg1 = nchains > 1 ? c1.nseg : 0;
   const int nsegt = nseg0 + nseg1;
+  const int nrounds = max_rounds(nseg0, nseg1);
   // ---- F1
   for (int g = gtid(); g < nsegt; g += gthreads()) {
     if (g < nseg0) chain_f1(c0, g, L, W);
@@ -300,7 +315,7 @@ __device__ bool solve_chains(const Dev &d, ChainT<T> c0, ChainT<T> c1, int nchai
   // ---- F2 rounds (end-state buffers alternate 0 -> 1 -> 0 ...)
   int cur = 0;
   bool settled = false;
-  for (int round = 0; round < kMaxRounds; ++round) {
+  for (int round = 0; round < nrounds; ++round) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       if (round == 0) sy->iout[0] = 0;
       sy->iout[(round + 1) % 3] = 0;
@@ -324,7 +339,7 @@ __device__ bool solve_chains(const Dev &d, ChainT<T> c0, ChainT<T> c1, int nchai
       break;
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0 && !settled) atomicMax(&sy->max_rounds, kMaxRounds + 1);
+  if (blockIdx.x == 0 && threadIdx.x == 0 && !settled) atomicMax(&sy->max_rounds, nrounds + 1);
   if (!settled) {
     if (blockIdx.x == 0 && threadIdx.x < 32) {
       chain_sequential_warp(c0, true);
@@ -352,7 +367,7 @@ __device__ bool solve_chains(const Dev &d, ChainT<T> c0, ChainT<T> c1, int nchai
   }
   cur = 0;
   settled = false;
-  for (int round = 0; round < kMaxRounds; ++round) {
+  for (int round = 0; round < nrounds; ++round) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       if (round == 0) sy->iout[3] = 0;
       sy->iout[3 + (round + 1) % 3] = 0;

@@ -127,6 +127,10 @@ struct Dev {
   Metrics m;
   Regions r;
   const uint16_t *mask;
+  // per-position face values: prof_idx[((ir-1) + (jr-1)*mgri + (face-1)*mgri*mgrj)*2
+  // + var-1] is -1 or the offset of the values in prof (null: none set)
+  const int *prof_idx;
+  const double *prof;
   // fields of the device-resident time loop
   double *u, *v, *p, *un, *vn, *pn, *us, *vs;
   // momentum work arrays (X: cj1x..c2nx; Y: cj1y..c2ny)

@@ -276,12 +276,13 @@ __global__ void __launch_bounds__(kMaxThreads, 1) k_ppe_tiled(Dev d, TileGeom g,
 }
 
 // Mixed-precision red/black SOR (FP32 sweeps, FP64 residual and correction)
-// with K sweeps per grid barrier; one tile per block.
-template <int K>
+// with K sweeps per grid barrier; RES: one tile per block resident in shared
+// memory, else blocks loop over tiles.
+template <int K, bool RES>
 __global__ void __launch_bounds__(kMixedThreads, 1) k_ppe_mixed(Dev d, MixedGeom g, MixedArgs a,
                                                       StepOut *out) {
   if (d.sync->halt) return;
-  const int nconv = ppe_mixed<K>(d, g, a);
+  const int nconv = ppe_mixed<K, RES>(d, g, a);
   if (nconv < 0) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? a.msorit : nconv;
 }

@@ -468,8 +468,10 @@ __device__ __forceinline__ void mixed_flush_maxima(unsigned int (*redm)[32], int
 // per block keeps the box resident in shared memory between groups (only the
 // halo ring is exchanged); with more tiles than blocks, each block stages
 // the whole box of each of its tiles every group.  Returns nConv (0 = not
-// converged) or -1 on a barrier error.
-template <int K>
+// converged) or -1 on a barrier error.  RES selects the mode at compile
+// time (each mode is its own kernel: together they would not fit the 128
+// registers a thread of a 512-thread block has).
+template <int K, bool RES>
 __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
   Sync *sy = d.sync;
   unsigned long long *ring = &sy->red[kMixedRing];
@@ -484,15 +486,15 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
   __shared__ unsigned int redm[K][32];
   float *fs = reinterpret_cast<float *>(smem);
   const int ntiles = g.ntx * g.nty;
-  const bool resident = g.resident != 0;
+  constexpr bool resident = RES;
   const bool has = (int)blockIdx.x < ntiles;
   MixedBox b;
-  if (resident) mixed_setup<K>(d, g, b, blockIdx.x, fs, true);
+  if constexpr (resident) mixed_setup<K>(d, g, b, blockIdx.x, fs, true);
 
   int m = 0, result = 0, grp = 0;
   bool done = false;
   while (!done) {
-    if (resident) {
+    if constexpr (resident) {
       if (has) mixed_residual(d, b, a.p);
       __syncthreads();
     } else {
@@ -513,7 +515,7 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
       }
       const float *ein = q == 0 ? nullptr : ((q & 1) ? a.xbuf0 : a.xbuf1);
       float *eout = (q & 1) ? a.xbuf1 : a.xbuf0;
-      if (resident) {
+      if constexpr (resident) {
         if (has) mixed_group<K>(g, b, ns, a.relax, ein, eout, slots);
       } else {
         for (int t = threadIdx.x; t < K * 32; t += blockDim.x) redm[t / 32][t % 32] = 0u;
@@ -542,7 +544,7 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
       if (conv >= 0) {
         result = m + conv + 1;
         if (conv < ns - 1) {
-          if (resident) {
+          if constexpr (resident) {
             if (has) mixed_redo<K>(b, conv + 1, a.relax);
           } else {
             // the group's input buffer is intact: sweep again from it
@@ -568,7 +570,7 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
       }
       if (in_pass >= a.inner) break;
     }
-    if (resident) {
+    if constexpr (resident) {
       if (has) mixed_correct(d, b, a.p);
     } else {
       for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {

@@ -56,6 +56,12 @@ class Regions:
     dPRporos: np.ndarray      # float64 (mgri, mgrj)
     dPRporc1: np.ndarray
     dPRporc2: np.ndarray
+    # Per-position face values (an extension: the reference's faces carry one
+    # constant per variable): {(ireg, jreg, face, var): values}, var 1 = u,
+    # 2 = v, values[pos] at position pos along the face (j on west/east
+    # faces, i on south/north faces); they replace dBCVal in VelBoundCond's
+    # inlet and moving-wall rows.
+    profiles: dict = dataclasses.field(default_factory=dict)
 
     @property
     def n_i(self) -> int:
@@ -402,20 +408,69 @@ def cavity(n: int, re: float, dt: float, *, lid: float = 1.0,
 
 def channel(ncx: int, ncy: int, re: float, dt: float, *, length: float = 4.0,
             height: float = 1.0, u_in: float = 1.0, solver: str = "rb_sor",
-            **kw) -> Case:
+            outlet: str = "fd", **kw) -> Case:
     """Plane channel: inlet on the west face with normal velocity ``u_in``,
-    fully developed outlet on the east face, no-slip south/north walls."""
+    outlet on the east face (``fd`` fully developed, bound_cond.f BM_OUTLT1;
+    ``mc`` mass conservation, BM_OUTLT2), no-slip south/north walls."""
     X, Y = _uniform_nodes(ncx, ncy, length, height)
     nx, ny = ncx + 1, ncy + 1
     bc = ("number_of_regions 1 1\n"
           "i_borders\n"
           "j_borders\n"
           f"inlet 1 1 west nv {u_in!r}\n"
-          "outlet 1 1 east fd\n")
+          f"outlet 1 1 east {outlet}\n")
     prm = RunParams.scaled(dt, 1.0, 1.0, 1.0, 1.0 / re,
                            npsolver=PPE_SOLVERS[solver], lcartes=1, **kw)
     regs = parse_bc_section(bc, nx, ny, re=prm.re)
     return Case(f"channel{ncx}x{ncy}_re{re:g}", nx, ny, X, Y, regs, prm, bc)
+
+
+def inflow_profile(case: Case, seed: int, amp: float = 1.0e-2, modes: int = 16,
+                   u_center: float = 1.0) -> np.ndarray:
+    """Parabolic inflow plus a seeded Fourier perturbation, as the u values
+    of the west face over j = 0..ny+1: at row j (between nodes j-1 and j)
+    with centre height y_c, u = 4 u_center y_c (H - y_c) / H^2 + sum_k a_k
+    sin(k pi y_c / H), a_k ~ N(0, amp^2) from default_rng(seed), k = 1..modes;
+    0 on the rows outside the channel."""
+    y = case.y[0, :]
+    y0, h_ch = y[0], y[-1] - y[0]
+    rng = np.random.default_rng(seed)
+    a = rng.normal(0.0, amp, size=modes)
+    prof = np.zeros(case.ny + 2)
+    for j in range(2, case.ny + 1):
+        yc = 0.5 * (y[j - 2] + y[j - 1]) - y0
+        s = 4.0 * u_center * yc * (h_ch - yc) / h_ch ** 2
+        s += float(np.dot(a, np.sin(np.arange(1, modes + 1) * np.pi * yc / h_ch)))
+        prof[j] = s
+    return prof
+
+
+def channel_inflow(ncx: int, ncy: int, re: float, dt: float, *, seed: int = 1234,
+                   length: float = 4.0, height: float = 1.0, amp: float = 1.0e-2,
+                   solver: str = "rb_sor", outlet: str = "mc", **kw) -> Case:
+    """Plane channel with a parabolic + perturbed inflow profile on the west
+    face (a per-row face profile: the reference's faces carry one constant),
+    outlet on the east face, no-slip walls.
+
+    The default outlet is the mass-conserving one (bound_cond.f BM_OUTLT2:
+    zero-gradient u corrected by continuity, u(iE) = u(iE-1) - (v(iE,j) -
+    v(iE,j-1))).  With the fully developed outlet (``fd``, BM_OUTLT1) the
+    outflow does not balance the inflow, the all-Neumann pressure problem has
+    no solution, and the scheme grows without bound within a few steps."""
+    case = channel(ncx, ncy, re, dt, length=length, height=height, u_in=1.0, solver=solver,
+                   outlet=outlet, **kw)
+    case.regions.profiles[(1, 1, WEST, 1)] = inflow_profile(case, seed, amp)
+    case.name = f"channel{ncx}x{ncy}_re{re:g}_profiled"
+    return case
+
+
+def channel_ic(case: Case):
+    """Initial fields of a profiled channel: u = the inflow profile in every
+    column (divergence-free: u depends on j only, v = 0), p = 0."""
+    prof = case.regions.profiles[(1, 1, WEST, 1)]
+    u = np.zeros((case.nx + 2, case.ny + 2), order="F")
+    u[:, :] = prof[None, :]
+    return u, np.zeros_like(u), np.zeros_like(u)
 
 
 def perturbation_ic(case: Case, seed: int, modes: int = 16, amp: float = 1.0e-3):

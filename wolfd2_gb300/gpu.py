@@ -107,6 +107,7 @@ def lib():
     L.wolfd2gpu_tune.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
     L.wolfd2gpu_tune_mixed.argtypes = [vp, C.c_int, C.c_int, C.c_int]
     L.wolfd2gpu_set_precision.argtypes = [vp, C.c_int, C.c_int]
+    L.wolfd2gpu_set_face_profile.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_int]
     L.wolfd2gpu_device_fields.argtypes = [vp, C.POINTER(_dp), C.POINTER(_dp), C.POINTER(_dp), _ip]
     L.wolfd2gpu_launch_count.argtypes = [vp]
     L.wolfd2gpu_launch_count.restype = C.c_longlong
@@ -182,6 +183,8 @@ class Solver:
         shapes the autotuner committed for this grid shape (tuned.json)."""
         s = cls(case.nx, case.ny, case.regions, mnx, mny)
         s.grid_metric(case.x, case.y)
+        for (ir, jr, face, var), vals in getattr(case.regions, "profiles", {}).items():
+            s.set_face_profile(ir, jr, face, var, vals)
         if tuned:
             from . import autotune
             autotune.apply(s, autotune.lookup(case.nx, case.ny, precision))
@@ -232,6 +235,17 @@ class Solver:
         the block-size limit (0 keeps the current value), and the tile mode
         (0 auto, 1 several tiles per block, 2 the same on <= 16 blocks)."""
         self._check(self.L.wolfd2gpu_tune_mixed(self.h, sweeps_per_barrier, threads, mode))
+
+    def set_face_profile(self, ireg: int, jreg: int, face: int, var: int, values=None):
+        """Per-position inlet / moving-wall values on one region face (var 1 =
+        u, 2 = v; values over j for west/east faces, over i for south/north);
+        None restores the region constant."""
+        if values is None:
+            self._check(self.L.wolfd2gpu_set_face_profile(self.h, ireg, jreg, face, var, None, 0))
+            return
+        a = np.ascontiguousarray(values, np.float64)
+        self._check(self.L.wolfd2gpu_set_face_profile(self.h, ireg, jreg, face, var,
+                                                      a.ctypes.data_as(C.c_void_p), a.size))
 
     def set_precision(self, precision: int, refine_sweeps: int = 0):
         """Precision of the drop-in Ppe (PREC_FP64 or PREC_MIXED)."""
