@@ -9,11 +9,13 @@ re-formed and is therefore searched only over values whose accuracy the tests
 cover (64-256).
 
     python -m wolfd2_gb300.autotune --n 1024 --n 512 [--precision mixed]
+    python -m wolfd2_gb300.autotune --channel 4096x1024
 
 times every candidate on the current GPU (device time of a few steps of the
-seeded-perturbation cavity, CUDA events through the library's profiler) and
-merges the fastest into ``tuned.json`` beside this file.  ``Solver.for_case``
-applies the entry of its grid shape when one exists.
+seeded-perturbation cavity, or of the profiled channel from its initial
+field, CUDA events through the library's profiler) and merges the fastest
+into ``tuned.json`` beside this file.  ``Solver.for_case`` applies the entry
+of its grid shape when one exists.
 """
 from __future__ import annotations
 
@@ -26,10 +28,11 @@ from typing import Dict, Optional
 HERE = os.path.dirname(os.path.abspath(__file__))
 TUNED = os.path.join(HERE, "tuned.json")
 
-CHAIN_SEG = (0, 16, 32, 48)        # 0: the library's default (rows / threads)
+CHAIN_SEG = (0, 16, 32, 48, 128, 512)   # 0: the library's default (rows / threads)
 CHAIN_WARM = (24, 48, 64)
 MIXED_K = (4, 8)
 MIXED_THREADS = (256, 384, 512)
+MIXED_MODE = (0, 1)               # 0: resident tiles when they fit, 1: multi-tile
 REFINE = (64, 128, 256)
 
 
@@ -55,7 +58,7 @@ def apply(solver, cfg: Optional[dict]) -> None:
     solver.tune(seg=cfg.get("seg", 0), warm=cfg.get("warm", 0))
     if cfg.get("mixed_k") or cfg.get("mixed_threads"):
         try:
-            solver.tune_mixed(cfg.get("mixed_k", 0), cfg.get("mixed_threads", 0))
+            solver.tune_mixed(cfg.get("mixed_k", 0), cfg.get("mixed_threads", 0), cfg.get("mixed_mode", 0))
         except Exception:  # a shape the mixed planner rejects: keep its default
             pass
     solver.refine_sweeps = cfg.get("refine_sweeps", 0)
@@ -74,16 +77,19 @@ def _time(solver, case, fields, precision: int, refine: int, steps: int) -> floa
     return ms / steps
 
 
-def tune_case(case, precision: str = "mixed", steps: int = 2, seed: int = 1234, log=print) -> dict:
+def tune_case(case, precision: str = "mixed", steps: int = 2, seed: int = 1234, log=print,
+              fields=None) -> dict:
     """Coordinate search: chain segment shape first, then (mixed) the Poisson
-    kernel shape and the refinement pass length."""
+    kernel shape, tile mode and the refinement pass length."""
     from . import deck
     from .gpu import PREC_FP64, PREC_MIXED, Solver, W2Error
     prec = PREC_MIXED if precision == "mixed" else PREC_FP64
     s = Solver.for_case(case, tuned=False)
-    fields = deck.perturbation_ic(case, seed)
+    if fields is None:
+        fields = deck.perturbation_ic(case, seed)
     best = {"seg": 0, "warm": 64, "mixed_k": 8 if prec == PREC_MIXED else 0,
-            "mixed_threads": 512 if prec == PREC_MIXED else 0, "refine_sweeps": 128 if prec == PREC_MIXED else 0}
+            "mixed_threads": 512 if prec == PREC_MIXED else 0, "mixed_mode": 0,
+            "refine_sweeps": 128 if prec == PREC_MIXED else 0}
 
     def run(cfg):
         apply(s, cfg)
@@ -102,10 +108,10 @@ def tune_case(case, precision: str = "mixed", steps: int = 2, seed: int = 1234, 
         if ms < best_ms:
             best, best_ms = cfg, ms
     if prec == PREC_MIXED:
-        for k, t, r in itertools.product(MIXED_K, MIXED_THREADS, REFINE):
-            cfg = {**best, "mixed_k": k, "mixed_threads": t, "refine_sweeps": r}
+        for k, t, mode, r in itertools.product(MIXED_K, MIXED_THREADS, MIXED_MODE, REFINE):
+            cfg = {**best, "mixed_k": k, "mixed_threads": t, "mixed_mode": mode, "refine_sweeps": r}
             ms = run(cfg)
-            log(f"  mixed K={k} threads<={t} inner={r}: {ms:.3f}")
+            log(f"  mixed K={k} threads<={t} mode={mode} inner={r}: {ms:.3f}")
             if ms < best_ms:
                 best, best_ms = cfg, ms
     best["ms_per_step"] = best_ms
@@ -117,6 +123,8 @@ def tune_case(case, precision: str = "mixed", steps: int = 2, seed: int = 1234, 
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--n", type=int, action="append", help="cavity cells per side (repeatable)")
+    ap.add_argument("--channel", action="append", metavar="NCXxNCY",
+                    help="profiled channel cells, e.g. 4096x1024 (Re 1e4, dt 2.5e-4; repeatable)")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--re", type=float, default=1000.0)
     ap.add_argument("--steps", type=int, default=2)
@@ -127,9 +135,15 @@ def main():
     if os.path.exists(args.out):
         with open(args.out) as f:
             table.update(json.load(f))
-    for n in args.n or [1024]:
-        case = deck.cavity(n, args.re, 0.25 / n, solver="rb_sor")
-        cfg = tune_case(case, args.precision, args.steps)
+    jobs = []
+    for n in args.n or ([] if args.channel else [1024]):
+        jobs.append((deck.cavity(n, args.re, 0.25 / n, solver="rb_sor"), None))
+    for spec in args.channel or []:
+        ncx, ncy = (int(t) for t in spec.lower().split("x"))
+        case = deck.channel_inflow(ncx, ncy, 1.0e4, 2.5e-4)
+        jobs.append((case, deck.channel_ic(case)))
+    for case, fields in jobs:
+        cfg = tune_case(case, args.precision, args.steps, fields=fields)
         table[key(case.nx, case.ny, args.precision)] = cfg
         with open(args.out, "w") as f:
             json.dump(table, f, indent=1, sort_keys=True)

@@ -68,8 +68,6 @@ struct w2_ctx {
   int prof_len = 0, prof_used = 0;
   std::vector<int> prof_host;
   // split-2 identity rows in chain order, and their by-position device copies
-  std::vector<uint8_t> zx, zy;
-  uint8_t *bzx = nullptr, *bzy = nullptr;
   // how each momentum metric is read (full array, profile over i or j)
   struct MomMetric {
     int mode = 0;          // MP_FULL, MP_I, MP_J
@@ -273,9 +271,9 @@ void prof_collect(w2_ctx *c) {
   c->prof_pending.clear();
 }
 
-int pick_blocks(w2_ctx *c, const void *kern, long work) {
+int pick_blocks(w2_ctx *c, const void *kern, long work, size_t smem = 0) {
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, c->threads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, c->threads, smem);
   occ = std::max(1, std::min(occ, c->blocks_per_sm));
   // tiny grids: one block (grid barriers become __syncthreads); otherwise at
   // least one block per SM, up to the co-resident limit
@@ -285,12 +283,16 @@ int pick_blocks(w2_ctx *c, const void *kern, long work) {
   return (int)nb;
 }
 
-int coop(w2_ctx *c, const void *kern, int blocks, void **args) {
+int coop(w2_ctx *c, const void *kern, int blocks, void **args, size_t smem = 0) {
   c->launches++;
-  cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(c->threads), args, 0, c->st);
+  cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(c->threads), args, smem, c->st);
   if (e != cudaSuccess) return fail(c, W2_E_CUDA, "cooperative launch: %s", cudaGetErrorString(e));
   return W2_OK;
 }
+
+// Dynamic shared memory of the momentum kernels: the chain walks' stage
+// (the FP64 and FP32 stages have the same size per thread).
+size_t naux_smem(const w2_ctx *c) { return walk_stage_bytes(sizeof(double), c->threads); }
 
 int check_sync(w2_ctx *c) {
   CK(cudaStreamSynchronize(c->st));
@@ -325,7 +327,6 @@ int make_chain(w2_ctx *c, ChainT<T> &ch, int n, bool with_b) {
   ch.a3p = dalloc<T>(c, cap);
   ch.bp = dalloc<T>(c, cap);
   ch.x = dalloc<T>(c, cap);
-  ch.bzero = nullptr;
   // end-state buffers, sized for the smallest segment length allowed (8)
   const int ms = (n + 7) / 8;
   ch.ef = dalloc<T>(c, (size_t)4 * ms);
@@ -354,7 +355,7 @@ int alias_split2(w2_ctx *c, ChainT<T> &c2, const ChainT<T> &c1) {
 int set_segments(w2_ctx *c) {
   Dev &d = c->dev;
   const int nX = c->nx * (c->ny - 1), nY = (c->nx - 1) * c->ny;
-  int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny);
+  int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny, naux_smem(c));
   long threads = (long)blocks * c->threads;
   int seg = c->seg_req > 0 ? c->seg_req : (int)std::max<long>(8, (nX + nY + threads - 1) / threads);
   seg = std::min(seg, kMaxSeg);
@@ -370,14 +371,6 @@ int set_segments(w2_ctx *c) {
   for (int k = 0; k < 4; ++k) {
     c32[k]->L = seg;
     c32[k]->nseg = k < 2 ? nsx : nsy;
-  }
-  // split-2 identity rows, stored by position for this segment length
-  if (c->bzx && c->bzy) {
-    std::vector<uint8_t> px((size_t)nX + kMaxSeg, 0), py((size_t)nY + kMaxSeg, 0);
-    for (int t = 0; t < nX; ++t) px[(size_t)(t % seg) * nsx + t / seg] = c->zx[t];
-    for (int t = 0; t < nY; ++t) py[(size_t)(t % seg) * nsy + t / seg] = c->zy[t];
-    CK(cudaMemcpy(c->bzx, px.data(), px.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(c->bzy, py.data(), py.size(), cudaMemcpyHostToDevice));
   }
   // end-state buffers, sized for the smallest segment length we allow (8)
   return W2_OK;
@@ -417,12 +410,12 @@ int launch_bc(w2_ctx *c, int ops, double *u, double *v, double *p) {
 
 int launch_naux(w2_ctx *c, int mqiter, double dk, double re, double qtol, const double *un,
                 const double *vn, double *us, double *vs) {
-  int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny);
+  int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny, naux_smem(c));
   ProfScope ps(c, W2_K_MOMENTUM);
   Dev d = c->dev;
   StepOut *out = c->d_out;
   void *args[] = {&d, &mqiter, &dk, &re, &qtol, (void *)&un, (void *)&vn, &us, &vs, &out};
-  return coop(c, (const void *)k_naux, blocks, args);
+  return coop(c, (const void *)k_naux, blocks, args, naux_smem(c));
 }
 
 // Tile geometry for the tiled red/black kernel: ntx*nty = k * blocks tiles
@@ -511,8 +504,6 @@ int ensure_f32(w2_ctx *c) {
     if ((rc = make_chain(c, v.x1, nX, true)) || (rc = alias_split2(c, v.x2, v.x1)) ||
         (rc = make_chain(c, v.y1, nY, true)) || (rc = alias_split2(c, v.y2, v.y1)))
       return rc;
-    v.x2.bzero = d.x2.bzero;
-    v.y2.bzero = d.y2.bzero;
     v.x1.nseg = d.x1.nseg; v.x2.nseg = d.x2.nseg;
     v.y1.nseg = d.y1.nseg; v.y2.nseg = d.y2.nseg;
     v.x1.L = v.x2.L = v.y1.L = v.y2.L = d.seg;
@@ -824,20 +815,6 @@ int wolfd2gpu_create(w2_ctx **out, int mnx, int mny, int mgri, int mgrj, int nx,
   if (make_chain(c, d.x1, nX, true) || alias_split2(c, d.x2, d.x1) ||
       make_chain(c, d.y1, nY, true) || alias_split2(c, d.y2, d.y1))
     return bad(W2_E_CUDA);
-  {
-    // split-2 identity rows in chain order; set_segments stores them by position
-    c->zx.assign(nX, 0);
-    c->zy.assign(nY, 0);
-    for (int j = 2; j <= ny; ++j)
-      for (int i = 1; i <= nx; ++i) c->zx[(j - 2) * nx + i - 1] = (mk[i + (size_t)j * c->ld] & MK_XID) ? 1 : 0;
-    for (int j = 1; j <= ny; ++j)
-      for (int i = 2; i <= nx; ++i) c->zy[(j - 1) * (nx - 1) + i - 2] = (mk[i + (size_t)j * c->ld] & MK_YID) ? 1 : 0;
-    c->bzx = dalloc<uint8_t>(c, (size_t)nX + kMaxSeg);
-    c->bzy = dalloc<uint8_t>(c, (size_t)nY + kMaxSeg);
-    if (!c->bzx || !c->bzy) return bad(W2_E_CUDA);
-    d.x2.bzero = c->bzx;
-    d.y2.bzero = c->bzy;
-  }
   d.f64.cj1x = d.cj1x; d.f64.cj2x = d.cj2x; d.f64.c1sx = d.c1sx; d.f64.c2sx = d.c2sx;
   d.f64.c1nx = d.c1nx; d.f64.c2nx = d.c2nx; d.f64.cj1y = d.cj1y; d.f64.cj2y = d.cj2y;
   d.f64.c1sy = d.c1sy; d.f64.c2sy = d.c2sy; d.f64.c1ny = d.c1ny; d.f64.c2ny = d.c2ny;
@@ -852,6 +829,14 @@ int wolfd2gpu_create(w2_ctx **out, int mnx, int mny, int mgri, int mgrj, int nx,
   if (cudaMallocHost(&c->h_out, sizeof(StepOut)) != cudaSuccess) return bad(W2_E_CUDA);
   c->threads = 256;
   c->blocks_per_sm = 2;
+  {
+    const int wmax = (int)walk_stage_bytes(sizeof(double), kMaxThreads);
+    if (cudaFuncSetAttribute((const void *)k_naux, cudaFuncAttributeMaxDynamicSharedMemorySize, wmax) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute((const void *)k_naux32, cudaFuncAttributeMaxDynamicSharedMemorySize, wmax) !=
+            cudaSuccess)
+      return bad(W2_E_CUDA);
+  }
   set_segments(c);
   d.u = c->U[0]; d.v = c->V[0]; d.p = c->P[0];
   if (cudaDeviceSynchronize() != cudaSuccess) return bad(W2_E_CUDA);
@@ -1304,12 +1289,12 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
         k_copy_mixed<<<gb, c->threads, 0, c->st>>>(d, p, pn, un, vn, un32, vn32, us32, vs32);
         CK(cudaGetLastError());
       }
-      int blocks = pick_blocks(c, (const void *)k_naux32, (long)c->nx * c->ny);
+      int blocks = pick_blocks(c, (const void *)k_naux32, (long)c->nx * c->ny, naux_smem(c));
       ProfScope ps(c, W2_K_MOMENTUM);
       int mq = prm->mqiter;
       double dk = prm->dk, re = prm->re, qtol = prm->qtol;
       void *args[] = {&d, &mq, &dk, &re, &qtol, &un32, &vn32, &us32, &vs32, &us, &vs, &o};
-      if ((rc = coop(c, (const void *)k_naux32, blocks, args))) break;
+      if ((rc = coop(c, (const void *)k_naux32, blocks, args, naux_smem(c)))) break;
     } else {
       ProfScope ps(c, W2_K_COPY);
       c->launches++;
@@ -1318,12 +1303,12 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
     }
     // nAuxMomentum on (un, vn) -> (us, vs); us = un already (main.f:741-747)
     if (!mixed) {
-      int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny);
+      int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny, naux_smem(c));
       ProfScope ps(c, W2_K_MOMENTUM);
       int mq = prm->mqiter;
       double dk = prm->dk, re = prm->re, qtol = prm->qtol;
       void *args[] = {&d, &mq, &dk, &re, &qtol, &un, &vn, &us, &vs, &o};
-      if ((rc = coop(c, (const void *)k_naux, blocks, args))) break;
+      if ((rc = coop(c, (const void *)k_naux, blocks, args, naux_smem(c)))) break;
     }
     if (prm->nfiltu == 1 || prm->nfiltv == 1) {
       double *h = c->stage[5];

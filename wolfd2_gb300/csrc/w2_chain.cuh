@@ -88,9 +88,11 @@ struct RowWalk {
   }
 };
 
+// Right-hand side of a row (the split-2 identity rows find theirs zeroed by
+// the split-2 assembly).
 template <class T>
 __device__ __forceinline__ T chain_rhs(const ChainT<T> &c, int p) {
-  return (c.bzero != nullptr && c.bzero[p]) ? T(0) : c.b[p];
+  return c.b[p];
 }
 
 // One forward row k >= 1 (stored at p) of AltTridLU: a2' = a2 - a1 a3'(k-1);
@@ -111,43 +113,133 @@ __device__ __forceinline__ void fwd_row0(const ChainT<T> &c, T &a3p, T &bp) {
   bp = chain_rhs(c, 0) / c.a2[0];
 }
 
+// Walks load their rows a batch ahead of the recurrence: each thread copies
+// the coefficients of its next rows into its own slots of shared memory with
+// cp.async, waits once, then runs the rows from there.  A walk is a chain of
+// dependent steps, so this pays one memory latency per batch instead of one
+// per row, without holding the batch in registers.  On a uniform stretch of
+// flow no segment re-joins its stored trajectory before the end of the grid
+// line (the rounded recurrence can settle on either of two neighbouring
+// values), so rounds walk whole lines and this latency sets their cost.
+// Each row's arithmetic is fwd_row's, or x = b' - a3' x going back.
+template <class T>
+struct RowBatch {
+  static constexpr int n = sizeof(T) == 4 ? 16 : 8;  // rows per batch
+  static constexpr int arrays = 6;                    // staged arrays at most
+};
+
+// Dynamic shared memory the walks need in a block of `threads` threads.
+inline size_t walk_stage_bytes(size_t elem, int threads) {
+  return elem * (elem == 4 ? 16 : 8) * 6 * (size_t)threads;
+}
+
+// This thread's slots: slot (a, r) at stage[(a * n + r) * blockDim.x].
+template <class T>
+__device__ __forceinline__ T *walk_stage() {
+  extern __shared__ __align__(16) unsigned char w2_walk_smem[];
+  return reinterpret_cast<T *>(w2_walk_smem) + threadIdx.x;
+}
+
+template <class T>
+__device__ __forceinline__ void stage_copy(T *dst, const T *src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(src), "n"((int)sizeof(T))
+               : "memory");
+}
+
+__device__ __forceinline__ void stage_wait() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;\n" ::: "memory");
+}
+
+// Forward rows w.k .. w.k+m-1 (m <= the batch); STORE writes a3' and b'.
+template <class T, bool STORE>
+__device__ __forceinline__ void fwd_batch(const ChainT<T> &c, RowWalk &w, int m, int L, int ns,
+                                          T &a3p, T &bp) {
+  constexpr int R = RowBatch<T>::n;
+  T *st = walk_stage<T>();
+  const int bs = blockDim.x;
+  RowWalk v = w;
+  for (int r = 0; r < m; ++r) {
+    stage_copy(st + (0 * R + r) * bs, c.a1 + v.p);
+    stage_copy(st + (1 * R + r) * bs, c.a2 + v.p);
+    stage_copy(st + (2 * R + r) * bs, c.a3 + v.p);
+    stage_copy(st + (3 * R + r) * bs, c.b + v.p);
+    v.next(L, ns);
+  }
+  stage_wait();
+  RowWalk u = w;
+  for (int r = 0; r < m; ++r) {
+    const T a1 = st[(0 * R + r) * bs];
+    const T a2p = st[(1 * R + r) * bs] - a1 * a3p;
+    const T nb = (st[(3 * R + r) * bs] - a1 * bp) / a2p;
+    a3p = (u.k < c.n - 1) ? st[(2 * R + r) * bs] / a2p : T(0);
+    bp = nb;
+    if (STORE) {
+      c.a3p[u.p] = a3p;
+      c.bp[u.p] = bp;
+    }
+    u.next(L, ns);
+  }
+  w = v;
+}
+
+// Back substitution rows w.k, w.k-1, ... (m of them); STORE writes x.
+template <class T, bool STORE>
+__device__ __forceinline__ void bwd_batch(const ChainT<T> &c, RowWalk &w, int m, int L, int ns, T &xn) {
+  constexpr int R = RowBatch<T>::n;
+  T *st = walk_stage<T>();
+  const int bs = blockDim.x;
+  RowWalk v = w;
+  for (int r = 0; r < m; ++r) {
+    stage_copy(st + (0 * R + r) * bs, c.bp + v.p);
+    stage_copy(st + (1 * R + r) * bs, c.a3p + v.p);
+    v.prev(L, ns);
+  }
+  stage_wait();
+  RowWalk u = w;
+  for (int r = 0; r < m; ++r) {
+    xn = st[(0 * R + r) * bs] - st[(1 * R + r) * bs] * xn;
+    if (STORE) c.x[u.p] = xn;
+    u.prev(L, ns);
+  }
+  w = v;
+}
+
 template <class T>
 __device__ void chain_f1(const ChainT<T> &c, int s, int L, int W) {
+  constexpr int R = RowBatch<T>::n;
   const int k0 = s * L, k1 = min(c.n, k0 + L), ns = c.nseg;
   T a3p, bp;
-  int k, p;
+  int kown = k0;
   if (k0 == 0) {
     fwd_row0(c, a3p, bp);
     c.a3p[0] = a3p;
     c.bp[0] = bp;
-    k = 1;
-    p = ns;
+    kown = 1;
   } else {
     const int kw = k0 - W;
-    RowWalk w(kw <= 0 ? 1 : kw, L, ns);
+    RowWalk u(kw <= 0 ? 1 : kw, L, ns);
     if (kw <= 0) {
       fwd_row0(c, a3p, bp);
     } else {
       a3p = T(0);
       bp = T(0);
     }
-    for (; w.k < k0; w.next(L, ns)) fwd_row(c, w.k, w.p, a3p, bp);
-    k = k0;
-    p = s;
+    while (u.k < k0) fwd_batch<T, false>(c, u, min(R, k0 - u.k), L, ns, a3p, bp);
   }
-  for (; k < k1; ++k, p += ns) {
-    fwd_row(c, k, p, a3p, bp);
-    c.a3p[p] = a3p;
-    c.bp[p] = bp;
-  }
+  RowWalk w(kown, L, ns);
+  while (w.k < k1) fwd_batch<T, true>(c, w, min(R, k1 - w.k), L, ns, a3p, bp);
   c.ef[2 * s] = a3p;
   c.ef[2 * s + 1] = bp;
 }
 
 // Verification round; reads end states from `ein`, writes `eout`.
-// Returns true when the segment's end state changed.
+// Returns true when the segment's end state changed.  The first row runs
+// alone (most segments re-join their stored trajectory there), the rest in
+// batches.
 template <class T>
 __device__ bool chain_f2(const ChainT<T> &c, int s, int L, const T *ein, T *eout) {
+  constexpr int R = RowBatch<T>::n;
   if (s == 0) {
     eout[0] = ein[0];
     eout[1] = ein[1];
@@ -155,15 +247,44 @@ __device__ bool chain_f2(const ChainT<T> &c, int s, int L, const T *ein, T *eout
   }
   const int k0 = s * L, k1 = min(c.n, k0 + L), ns = c.nseg;
   T a3p = ein[2 * (s - 1)], bp = ein[2 * (s - 1) + 1];
-  for (int k = k0, p = s; k < k1; ++k, p += ns) {
-    fwd_row(c, k, p, a3p, bp);
-    if (same_state(a3p, c.a3p[p]) && same_state(bp, c.bp[p])) {
-      eout[2 * s] = ein[2 * s];
-      eout[2 * s + 1] = ein[2 * s + 1];
-      return false;
+  fwd_row(c, k0, s, a3p, bp);
+  if (same_state(a3p, c.a3p[s]) && same_state(bp, c.bp[s])) {
+    eout[2 * s] = ein[2 * s];
+    eout[2 * s + 1] = ein[2 * s + 1];
+    return false;
+  }
+  c.a3p[s] = a3p;
+  c.bp[s] = bp;
+  T *st = walk_stage<T>();
+  const int bs = blockDim.x;
+  for (int k = k0 + 1, p = s + ns; k < k1;) {
+    const int m = min(R, k1 - k);
+    for (int r = 0; r < m; ++r) {
+      const int q = p + r * ns;
+      stage_copy(st + (0 * R + r) * bs, c.a1 + q);
+      stage_copy(st + (1 * R + r) * bs, c.a2 + q);
+      stage_copy(st + (2 * R + r) * bs, c.a3 + q);
+      stage_copy(st + (3 * R + r) * bs, c.b + q);
+      stage_copy(st + (4 * R + r) * bs, c.a3p + q);
+      stage_copy(st + (5 * R + r) * bs, c.bp + q);
     }
-    c.a3p[p] = a3p;
-    c.bp[p] = bp;
+    stage_wait();
+    for (int r = 0; r < m; ++r) {
+      const T a1 = st[(0 * R + r) * bs];
+      const T a2p = st[(1 * R + r) * bs] - a1 * a3p;
+      const T nb = (st[(3 * R + r) * bs] - a1 * bp) / a2p;
+      a3p = (k + r < c.n - 1) ? st[(2 * R + r) * bs] / a2p : T(0);
+      bp = nb;
+      if (same_state(a3p, st[(4 * R + r) * bs]) && same_state(bp, st[(5 * R + r) * bs])) {
+        eout[2 * s] = ein[2 * s];
+        eout[2 * s + 1] = ein[2 * s + 1];
+        return false;
+      }
+      c.a3p[p + r * ns] = a3p;
+      c.bp[p + r * ns] = bp;
+    }
+    k += m;
+    p += m * ns;
   }
   eout[2 * s] = a3p;
   eout[2 * s + 1] = bp;
@@ -171,50 +292,75 @@ __device__ bool chain_f2(const ChainT<T> &c, int s, int L, const T *ein, T *eout
 }
 
 template <class T>
-__device__ void chain_b1(const ChainT<T> &c, int s, int L, int W) {
+__device__ void chain_b1(const ChainT<T> &c, int s, int L, int W, T *eb) {
+  constexpr int R = RowBatch<T>::n;
   const int k0 = s * L, k1 = min(c.n, k0 + L), ns = c.nseg;
   const int plast = cpos(c, c.n - 1);
   T xn;
-  int k;
+  int kown;
   if (k1 == c.n) {
     xn = c.bp[plast];
     c.x[plast] = xn;
-    k = c.n - 2;
+    kown = c.n - 2;
   } else {
     const int kw = k1 - 1 + W;
+    int kstart;
     if (kw >= c.n - 1) {
       xn = c.bp[plast];
-      RowWalk w(c.n - 2, L, ns);
-      for (; w.k >= k1; w.prev(L, ns)) xn = c.bp[w.p] - c.a3p[w.p] * xn;
+      kstart = c.n - 2;
     } else {
       xn = T(0);
-      RowWalk w(kw, L, ns);
-      for (; w.k >= k1; w.prev(L, ns)) xn = c.bp[w.p] - c.a3p[w.p] * xn;
+      kstart = kw;
     }
-    k = k1 - 1;
+    RowWalk u(kstart, L, ns);
+    while (u.k >= k1) bwd_batch<T, false>(c, u, min(R, u.k - k1 + 1), L, ns, xn);
+    kown = k1 - 1;
   }
-  for (int p = (k - k0) * ns + s; k >= k0; --k, p -= ns) {
-    xn = c.bp[p] - c.a3p[p] * xn;
-    c.x[p] = xn;
+  if (kown >= k0) {
+    RowWalk w(kown, L, ns);
+    while (w.k >= k0) bwd_batch<T, true>(c, w, min(R, w.k - k0 + 1), L, ns, xn);
   }
-  c.eb[s] = c.x[s];
+  eb[s] = c.x[s];
 }
 
 template <class T>
 __device__ bool chain_b2(const ChainT<T> &c, int s, int L, const T *ein, T *eout) {
+  constexpr int R = RowBatch<T>::n;
   const int k0 = s * L, k1 = min(c.n, k0 + L), ns = c.nseg;
   if (k1 == c.n) {
     eout[s] = ein[s];
     return false;
   }
   T xn = ein[s + 1];
-  for (int k = k1 - 1, p = (k1 - 1 - k0) * ns + s; k >= k0; --k, p -= ns) {
-    xn = c.bp[p] - c.a3p[p] * xn;
-    if (same_state(xn, c.x[p])) {
-      eout[s] = ein[s];
-      return false;
+  int p = (k1 - 1 - k0) * ns + s;
+  xn = c.bp[p] - c.a3p[p] * xn;
+  if (same_state(xn, c.x[p])) {
+    eout[s] = ein[s];
+    return false;
+  }
+  c.x[p] = xn;
+  p -= ns;
+  T *st = walk_stage<T>();
+  const int bs = blockDim.x;
+  for (int k = k1 - 2; k >= k0;) {
+    const int m = min(R, k - k0 + 1);
+    for (int r = 0; r < m; ++r) {
+      const int q = p - r * ns;
+      stage_copy(st + (0 * R + r) * bs, c.bp + q);
+      stage_copy(st + (1 * R + r) * bs, c.a3p + q);
+      stage_copy(st + (2 * R + r) * bs, c.x + q);
     }
-    c.x[p] = xn;
+    stage_wait();
+    for (int r = 0; r < m; ++r) {
+      xn = st[(0 * R + r) * bs] - st[(1 * R + r) * bs] * xn;
+      if (same_state(xn, st[(2 * R + r) * bs])) {
+        eout[s] = ein[s];
+        return false;
+      }
+      c.x[p - r * ns] = xn;
+    }
+    k -= m;
+    p -= m * ns;
   }
   eout[s] = xn;
   return true;
@@ -300,8 +446,12 @@ __device__ __forceinline__ const T *eb_buf(const ChainT<T> &c, int b) {
 
 // Solve up to two independent chains together (segments of both share the
 // grid).  Every block must call this.  Returns false if a barrier failed.
+// The chains are taken by reference (they live in the kernel's parameter
+// space) and each walk names its chain statically, so the walks read the
+// array pointers from the parameter bank instead of holding them in
+// registers.
 template <class T>
-__device__ bool solve_chains(const Dev &d, ChainT<T> c0, ChainT<T> c1, int nchains) {
+__device__ bool solve_chains(const Dev &d, const ChainT<T> &c0, const ChainT<T> &c1, int nchains) {
   Sync *sy = d.sync;
   const int L = d.seg, W = d.warm;
   const int nseg0 = c0.nseg, nseg1 = nchains > 1 ? c1.nseg : 0;
@@ -323,10 +473,11 @@ __device__ bool solve_chains(const Dev &d, ChainT<T> c0, ChainT<T> c1, int nchai
     if (!grid_sync(sy)) return false;
     int any = 0;
     for (int g = gtid(); g < nsegt; g += gthreads()) {
-      const ChainT<T> &c = g < nseg0 ? c0 : c1;
-      int s = g < nseg0 ? g : g - nseg0;
-      T *eo = const_cast<T *>(ef_buf(c, cur ^ 1));
-      if (chain_f2(c, s, L, ef_buf(c, cur), eo)) any = 1;
+      if (g < nseg0) {
+        if (chain_f2(c0, g, L, ef_buf(c0, cur), const_cast<T *>(ef_buf(c0, cur ^ 1)))) any = 1;
+      } else {
+        if (chain_f2(c1, g - nseg0, L, ef_buf(c1, cur), const_cast<T *>(ef_buf(c1, cur ^ 1)))) any = 1;
+      }
     }
     if (any) atomicOr(&sy->iout[round % 3], 1);
     if (!grid_sync(sy)) return false;
@@ -342,11 +493,13 @@ __device__ bool solve_chains(const Dev &d, ChainT<T> c0, ChainT<T> c1, int nchai
   if (blockIdx.x == 0 && threadIdx.x == 0 && !settled) atomicMax(&sy->max_rounds, nrounds + 1);
   if (!settled) {
     if (blockIdx.x == 0 && threadIdx.x < 32) {
-      chain_sequential_warp(c0, true);
-      chain_sequential_warp(c0, false);
+      // copies: the guard walk must not take the address of parameter space
+      const ChainT<T> t0 = c0, t1 = c1;
+      chain_sequential_warp(t0, true);
+      chain_sequential_warp(t0, false);
       if (nchains > 1) {
-        chain_sequential_warp(c1, true);
-        chain_sequential_warp(c1, false);
+        chain_sequential_warp(t1, true);
+        chain_sequential_warp(t1, false);
       }
       if (threadIdx.x == 0) atomicAdd(&sy->fallback, 1);
     }
@@ -355,15 +508,8 @@ __device__ bool solve_chains(const Dev &d, ChainT<T> c0, ChainT<T> c1, int nchai
   }
   // ---- B1
   for (int g = gtid(); g < nsegt; g += gthreads()) {
-    if (g < nseg0) {
-      ChainT<T> c = c0;
-      c.eb = const_cast<T *>(eb_buf(c0, 0));
-      chain_b1(c, g, L, W);
-    } else {
-      ChainT<T> c = c1;
-      c.eb = const_cast<T *>(eb_buf(c1, 0));
-      chain_b1(c, g - nseg0, L, W);
-    }
+    if (g < nseg0) chain_b1(c0, g, L, W, const_cast<T *>(eb_buf(c0, 0)));
+    else chain_b1(c1, g - nseg0, L, W, const_cast<T *>(eb_buf(c1, 0)));
   }
   cur = 0;
   settled = false;
@@ -375,9 +521,11 @@ __device__ bool solve_chains(const Dev &d, ChainT<T> c0, ChainT<T> c1, int nchai
     if (!grid_sync(sy)) return false;
     int any = 0;
     for (int g = gtid(); g < nsegt; g += gthreads()) {
-      const ChainT<T> &c = g < nseg0 ? c0 : c1;
-      int s = g < nseg0 ? g : g - nseg0;
-      if (chain_b2(c, s, L, eb_buf(c, cur), const_cast<T *>(eb_buf(c, cur ^ 1)))) any = 1;
+      if (g < nseg0) {
+        if (chain_b2(c0, g, L, eb_buf(c0, cur), const_cast<T *>(eb_buf(c0, cur ^ 1)))) any = 1;
+      } else {
+        if (chain_b2(c1, g - nseg0, L, eb_buf(c1, cur), const_cast<T *>(eb_buf(c1, cur ^ 1)))) any = 1;
+      }
     }
     if (any) atomicOr(&sy->iout[3 + round % 3], 1);
     if (!grid_sync(sy)) return false;
@@ -393,8 +541,9 @@ __device__ bool solve_chains(const Dev &d, ChainT<T> c0, ChainT<T> c1, int nchai
   if (!settled) {
     if (blockIdx.x == 0 && threadIdx.x < 32) {
       // forward values are exact here; redo the back substitution serially
-      chain_sequential_warp(c0, false);
-      if (nchains > 1) chain_sequential_warp(c1, false);
+      const ChainT<T> t0 = c0, t1 = c1;
+      chain_sequential_warp(t0, false);
+      if (nchains > 1) chain_sequential_warp(t1, false);
       if (threadIdx.x == 0) atomicAdd(&sy->fallback, 1);
     }
     if (!grid_sync(sy)) return false;

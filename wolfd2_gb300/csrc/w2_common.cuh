@@ -70,7 +70,6 @@ struct ChainT {
   int nseg;        // segments of L rows (the last may be shorter)
   int L;           // rows per segment; row r of segment s is stored at r*nseg + s
   T *a1, *a2, *a3, *b;             // sub, diag, super, rhs
-  const uint8_t *bzero;            // rows whose rhs is forced to 0 (or null), by position
   T *a3p, *bp, *x;                 // factorised super, forward rhs, solution
   T *ef;           // forward end states: 2 per segment x 2 buffers
   T *eb;           // backward end states: 1 per segment x 2 buffers

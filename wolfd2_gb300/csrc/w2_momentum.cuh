@@ -333,6 +333,7 @@ __device__ void mom_assemble2(const Dev &d, const MomView<T> &V, double dk, doub
       const int px = cpos(V.x2, t);
       if (d.mask[IX(d, i, j)] & MK_XID) {
         a1 = T(0); a2 = T(1.0); a3 = T(0);
+        V.x2.b[px] = T(0);  // the split-1 solution, read next only as this rhs
       } else {
         const T rkj = dk2 * V.dju(i, j);
         const T cj2 = xcj(d, V, us, vs, 2, i, j), rgn0 = V.rgn(i, j), rgns = V.rgn(i, j - 1);
@@ -355,6 +356,7 @@ __device__ void mom_assemble2(const Dev &d, const MomView<T> &V, double dk, doub
       const int py = cpos(V.y2, q);
       if (d.mask[IX(d, i, j)] & MK_YID) {
         a1 = T(0); a2 = T(1.0); a3 = T(0);
+        V.y2.b[py] = T(0);
       } else {
         const T rkj = dk2 * V.djv(i, j);
         const T cj2 = ycj(d, V, us, vs, 2, i, j), rgc0 = V.rgc(i, j), rgcn = V.rgc(i, j + 1);
