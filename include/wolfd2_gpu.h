@@ -246,6 +246,39 @@ int wolfd2gpu_profile(w2_ctx *ctx, int enable);
 int wolfd2gpu_profile_read(w2_ctx *ctx, int kind, double *total_ms,
                            long long *count);
 
+/* ---- Ensembles (no reference counterpart) -----------------------------
+ * Many independent cases advanced together by the mixed step
+ * (precision W2_PREC_MIXED): one launch per stage covers every case, each
+ * case on its own group of the launch's blocks (a ragged partition sized
+ * by the cases' cells), with its own barriers, convergence tests and
+ * iteration counts.  Each case is an ordinary context, set up as usual
+ * (metrics, regions, fields; Cartesian unit-stencil grids, rb_sor or
+ * rb_sorp).  Per case, results are bit-identical to wolfd2gpu_step on that
+ * context alone.
+ *
+ * wolfd2gpu_ens_create: cases[n]; threads per block (0: 256) and Poisson
+ *   sweeps per barrier (0: 4) of every launch.  The contexts must outlive
+ *   the ensemble; their own calls must not overlap an ensemble call.
+ * wolfd2gpu_ens_step: prm[n] (one per case), nsteps steps; stats (may be
+ *   NULL) receives n*nsteps records, case-major.  Returns W2_E_DIVERGED if
+ *   a case's max step difference exceeds 1e12 (the case halts; the others
+ *   continue) and the first device error otherwise.
+ * wolfd2gpu_ens_graph: when enabled, one step's launch sequence is captured
+ *   in a CUDA graph on the first call and replayed every step.
+ * wolfd2gpu_ens_info: blocks of the momentum and Poisson launches, device
+ *   milliseconds of the last ens_step call (CUDA events around its steps),
+ *   and kernel launches so far. */
+typedef struct w2_ens w2_ens;
+int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
+                         int sweeps_per_barrier);
+int wolfd2gpu_ens_step(w2_ens *ens, const w2_params *prm, int nsteps,
+                       w2_stepstat *stats);
+int wolfd2gpu_ens_graph(w2_ens *ens, int enable);
+int wolfd2gpu_ens_info(w2_ens *ens, int *blocks_momentum, int *blocks_poisson,
+                       double *last_ms, long long *launches);
+const char *wolfd2gpu_ens_error(w2_ens *ens);
+int wolfd2gpu_ens_destroy(w2_ens *ens);
+
 /* ---- Allocation-free entry point ---------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * -- a driver that gives all device memory to its own pool at start-up, or

@@ -1,0 +1,25 @@
+"""The batched-ensemble workload generator (CPU)."""
+import numpy as np
+
+from wolfd2_gb300 import deck
+
+
+def test_ensemble_workload_draws():
+    m = deck.ensemble_cases(256, seed=2024)
+    assert len(m) == 256
+    assert {x.n for x in m} <= set(deck.ENSEMBLE_SIZES)
+    assert all(100.0 <= x.re <= 5000.0 for x in m)
+    # same seed, same draws
+    assert [(x.n, x.re) for x in m] == [(x.n, x.re) for x in deck.ensemble_cases(256, seed=2024)]
+    for x in m[:20]:
+        c = x.case
+        side = x.n * deck.ENSEMBLE_H
+        hx = np.diff(c.x[:, 0])
+        # power-of-two spacing, exact: every Poisson row is the unit stencil
+        assert np.all(hx == deck.ENSEMBLE_H)
+        assert c.nx == x.n + 1 and c.ny == x.n + 1
+        # similarity: deck Re times the side is the cavity Re; dt in the unit frame
+        assert abs(c.params.re * side - x.re) <= 1e-9 * x.re
+        assert abs(c.params.dk / side - x.dt) <= 1e-15
+        assert x.dt <= x.dt_named == 0.5 / x.n
+        assert x.dt / (x.re / x.n ** 2) <= 0.25 * (1 + 1e-12)

@@ -1,0 +1,84 @@
+"""Ensembles: many cases advanced by one launch per stage must give, per
+case, exactly what the case gives when stepped alone (the same mixed step:
+chain solves are exact for any segment length, the Poisson sweeps exact for
+any tile plan)."""
+import numpy as np
+import pytest
+
+from wolfd2_gb300 import deck
+from wolfd2_gb300.gpu import PREC_MIXED, Ensemble, Solver
+
+pytestmark = pytest.mark.gpu
+
+H = 1.0 / 64.0
+REFINE = 32
+
+
+def _cases():
+    """Cavities of different sizes and Reynolds numbers at spacing 1/64
+    (unit-stencil Poisson rows), one of them rectangular."""
+    spec = [(32, None, 100.0), (48, None, 400.0), (64, None, 1000.0), (96, None, 250.0), (40, 24, 300.0)]
+    out = []
+    for k, (n, ny, re) in enumerate(spec):
+        side = n * H
+        dt = min(0.5 * H, 0.25 * H * H * re)
+        case = deck.cavity(n, re, dt, solver="rb_sor", ny=ny, side=side)
+        out.append((case, deck.perturbation_ic(case, 100 + k)))
+    return out
+
+
+def _alone(case, fields, nsteps):
+    s = Solver.for_case(case, tuned=False)
+    s.load_fields(*fields)
+    hist = s.step(case.params, nsteps, precision=PREC_MIXED, refine_sweeps=REFINE)
+    u, v, p = s.store_fields()
+    s.close()
+    return hist, (u, v, p)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_ensemble_matches_cases_alone(graph):
+    cases = _cases()
+    nsteps = 3
+    solvers = []
+    for case, f in cases:
+        s = Solver.for_case(case, tuned=False)
+        s.load_fields(*f)
+        solvers.append(s)
+    ens = Ensemble(solvers, graph=graph)
+    hist = ens.step([c.params for c, _ in cases], nsteps, refine_sweeps=REFINE)
+    info = ens.info()
+    assert info["blocks_momentum"] >= len(cases) and info["blocks_poisson"] >= len(cases)
+    for k, ((case, f), s) in enumerate(zip(cases, solvers)):
+        ref_hist, ref = _alone(case, f, nsteps)
+        assert [(h[0], h[1]) for h in hist[k]] == [(h[0], h[1]) for h in ref_hist], k
+        assert [h[2][:3] for h in hist[k]] == [h[2][:3] for h in ref_hist], k
+        got = s.store_fields()
+        for name, g, r in zip("uvp", got, ref):
+            assert np.array_equal(g, r), (k, name, float(np.max(np.abs(g - r))))
+    ens.close()
+    for s in solvers:
+        s.close()
+
+
+def test_ensemble_continues_across_calls():
+    """Two calls of 2 steps equal one call of 4 (time levels carried over)."""
+    cases = _cases()[:3]
+    a, b = [], []
+    for case, f in cases:
+        for lst in (a, b):
+            s = Solver.for_case(case, tuned=False)
+            s.load_fields(*f)
+            lst.append(s)
+    ea, eb = Ensemble(a), Ensemble(b, graph=False)
+    prm = [c.params for c, _ in cases]
+    ea.step(prm, 2, refine_sweeps=REFINE)
+    ea.step(prm, 2, refine_sweeps=REFINE)
+    eb.step(prm, 4, refine_sweeps=REFINE)
+    for sa, sb in zip(a, b):
+        for x, y in zip(sa.store_fields(), sb.store_fields()):
+            assert np.array_equal(x, y)
+    ea.close()
+    eb.close()
+    for s in a + b:
+        s.close()

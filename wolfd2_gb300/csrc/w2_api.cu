@@ -13,7 +13,7 @@
 #include <string>
 #include <vector>
 
-#include "w2_kernels.cuh"
+#include "w2_ensemble.cuh"
 
 using namespace w2;
 
@@ -67,7 +67,6 @@ struct w2_ctx {
   double *prof = nullptr;    // device values, kMaxProfiles x prof_len
   int prof_len = 0, prof_used = 0;
   std::vector<int> prof_host;
-  // split-2 identity rows in chain order, and their by-position device copies
   // how each momentum metric is read (full array, profile over i or j)
   struct MomMetric {
     int mode = 0;          // MP_FULL, MP_I, MP_J
@@ -352,15 +351,15 @@ int alias_split2(w2_ctx *c, ChainT<T> &c2, const ChainT<T> &c1) {
   return W2_OK;
 }
 
-int set_segments(w2_ctx *c) {
-  Dev &d = c->dev;
-  const int nX = c->nx * (c->ny - 1), nY = (c->nx - 1) * c->ny;
-  int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny, naux_smem(c));
-  long threads = (long)blocks * c->threads;
-  int seg = c->seg_req > 0 ? c->seg_req : (int)std::max<long>(8, (nX + nY + threads - 1) / threads);
+// Chain segment length and warm-up for `threads` threads walking the chains,
+// applied to every chain view of d (end-state buffers are sized for the
+// shortest segment allowed, 8 rows).
+void chain_views(Dev &d, int nx, int ny, long threads, int seg_req, int warm_req) {
+  const int nX = nx * (ny - 1), nY = (nx - 1) * ny;
+  int seg = seg_req > 0 ? seg_req : (int)std::max<long>(8, (nX + nY + threads - 1) / threads);
   seg = std::min(seg, kMaxSeg);
   d.seg = seg;
-  d.warm = c->warm_req > 0 ? c->warm_req : 64;
+  d.warm = warm_req > 0 ? warm_req : 64;
   const int nsx = (nX + seg - 1) / seg, nsy = (nY + seg - 1) / seg;
   ChainT<double> *c64[] = {&d.x1, &d.x2, &d.y1, &d.y2, &d.f64.x1, &d.f64.x2, &d.f64.y1, &d.f64.y2};
   ChainT<float> *c32[] = {&d.f32.x1, &d.f32.x2, &d.f32.y1, &d.f32.y2};
@@ -372,7 +371,11 @@ int set_segments(w2_ctx *c) {
     c32[k]->L = seg;
     c32[k]->nseg = k < 2 ? nsx : nsy;
   }
-  // end-state buffers, sized for the smallest segment length we allow (8)
+}
+
+int set_segments(w2_ctx *c) {
+  int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny, naux_smem(c));
+  chain_views(c->dev, c->nx, c->ny, (long)blocks * c->threads, c->seg_req, c->warm_req);
   return W2_OK;
 }
 
@@ -595,6 +598,21 @@ const void *mixed_kernel(int K, bool resident) {
   return nullptr;
 }
 
+// Sweep work of one group of K sweeps on a tx x ty tile: (plane columns
+// rounded to warps) x (box rows active in each half-sweep).
+double mixed_sweep_work(int K, int tx, int ty) {
+  const int H = 2 * K, bh = ty + 2 * H, hwp = (tx / 2 + H + 31) / 32 * 32;
+  double rows = 0.0;
+  for (int h = 1; h <= 2 * K; ++h) rows += std::max(0, bh - 2 * h);
+  return (double)hwp * rows;
+}
+
+// Staging work of one group in multi-tile mode (whole box in, tile out).
+double mixed_stage_work(int K, int tx, int ty) {
+  const int H = 2 * K, bh = ty + 2 * H, hwp = (tx / 2 + H + 31) / 32 * 32;
+  return 4.0 * K * bh * hwp / 8.0;
+}
+
 // Tile plan of the mixed Poisson kernel.  Preferred: one tile per block (one
 // block per SM, box resident in shared memory), the split of the unknowns
 // into at most nsm tiles, tx a multiple of 8, whose block does the least
@@ -610,12 +628,7 @@ void plan_mixed(w2_ctx *c) {
   int maxsmem = 0;
   cudaDeviceGetAttribute(&maxsmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
   const int NX = c->nx - 1, NY = c->ny - 1, H = 2 * K;
-  auto sweep_work = [&](int tx, int ty) {
-    const int bh = ty + 2 * H, hwp = (tx / 2 + H + 31) / 32 * 32;
-    double rows = 0.0;
-    for (int h = 1; h <= 2 * K; ++h) rows += std::max(0, bh - 2 * h);
-    return (double)hwp * rows;
-  };
+  auto sweep_work = [&](int tx, int ty) { return mixed_sweep_work(K, tx, ty); };
   for (int pass = c->mixed_mode ? 1 : 0; pass < 2 && !c->mixed_ok; ++pass) {
     const bool resident = pass == 0;
     const void *kf = mixed_kernel(K, resident);
@@ -644,9 +657,8 @@ void plan_mixed(w2_ctx *c) {
           if (occ < 1) continue;
           blocks = c->nsm * occ;
           if (c->mixed_mode == 2) blocks = std::min(blocks, 16);
-          const int bh = ty + 2 * H, hwp = (tx / 2 + H + 31) / 32 * 32;
           const int tpb = (ntx * nty + blocks - 1) / blocks;
-          cost = tpb * (cost + 4.0 * K * bh * hwp / 8.0);
+          cost = tpb * (cost + mixed_stage_work(K, tx, ty));
         }
         if (cost < best) {
           best = cost;
@@ -772,7 +784,11 @@ int wolfd2gpu_create(w2_ctx **out, int mnx, int mny, int mgri, int mgrj, int nx,
   int coopok = 0;
   cudaDeviceGetAttribute(&coopok, cudaDevAttrCooperativeLaunch, c->device);
   if (!coopok) return bad(W2_E_UNSUPPORTED);
-  if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) return bad(W2_E_CUDA);
+  // A blocking stream: set-up work goes through the legacy default stream
+  // (cudaMemset zeroing of every allocation, synchronous uploads whose DMA
+  // may still be in flight when they return), and the kernels on this
+  // stream must run after it.
+  if (cudaStreamCreate(&c->st) != cudaSuccess) return bad(W2_E_CUDA);
   std::vector<uint16_t> mk;
   int rc = build_masks(c, mk);
   if (rc) { fprintf(stderr, "wolfd2gpu_create: %s\n", c->err); return bad(rc); }
@@ -1374,6 +1390,428 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
     return fail(c, W2_E_DIVERGED, "Solution diverged at step %d. Please reduce CFL number.", diverged_at + 1);
   }
   return rc;
+}
+
+}  // extern "C"
+
+// ============================================================================
+// Ensembles: many independent cases advanced together, one launch per stage
+// of the mixed time step (kernels in w2_ensemble.cuh).
+// ============================================================================
+
+struct w2_ens {
+  std::vector<w2_ctx *> cs;
+  int n = 0, K = 4, threads = 256, device = 0, nsm = 0;
+  cudaStream_t st = nullptr;
+  std::vector<void *> allocs;
+  std::vector<EnsCase> h;
+  EnsCase *d_cases = nullptr;
+  int *d_first_m = nullptr, *d_first_p = nullptr, *d_first_1 = nullptr, *d_step = nullptr;
+  std::vector<int> bm, bp;  // blocks per case: momentum/tail launches, Poisson launch
+  int blocks_m = 0, blocks_p = 0;
+  size_t smem_m = 0, smem_p = 0;
+  StepOut *d_outs = nullptr;
+  size_t outs_cap = 0;
+  bool graph_on = false;
+  cudaGraphExec_t gexec = nullptr;
+  int graph_nsteps = -1;
+  long long launches = 0;
+  double last_ms = 0.0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  char err[512] = {0};
+};
+
+namespace {
+
+int efail(w2_ens *e, int code, const char *fmt, ...) {
+  if (e) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(e->err, sizeof(e->err), fmt, ap);
+    va_end(ap);
+  }
+  return code;
+}
+
+#define ECK(call)                                                                  \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess)                                                         \
+      return efail(e, W2_E_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));  \
+  } while (0)
+
+template <class T>
+T *ealloc(w2_ens *e, size_t n) {
+  void *p = nullptr;
+  if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return nullptr;
+  cudaMemset(p, 0, std::max<size_t>(n, 1) * sizeof(T));
+  e->allocs.push_back(p);
+  return (T *)p;
+}
+
+// Blocks per case: every case at least one block, the largest work per
+// block as small as the total allows (bisection on that ratio), leftover
+// blocks to the cases with the most work per block.  Empty if n > total.
+std::vector<int> ens_partition(const std::vector<double> &w, int total) {
+  const int n = (int)w.size();
+  if (n == 0 || n > total) return {};
+  auto blocks_for = [&](double r, std::vector<int> *b) {
+    long sum = 0;
+    for (int k = 0; k < n; ++k) {
+      const long q = std::max(1L, (long)std::ceil(w[k] / r));
+      if (b) (*b)[k] = (int)q;
+      sum += q;
+    }
+    return sum;
+  };
+  double lo = 0.0, hi = *std::max_element(w.begin(), w.end()) + 1.0;
+  for (int it = 0; it < 200; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (blocks_for(mid, nullptr) <= total) hi = mid;
+    else lo = mid;
+  }
+  std::vector<int> b(n, 1);
+  long sum = blocks_for(hi, &b);
+  while (sum < total) {
+    int km = 0;
+    for (int k = 1; k < n; ++k)
+      if (w[k] / b[k] > w[km] / b[km]) km = k;
+    ++b[km];
+    ++sum;
+  }
+  return b;
+}
+
+// Multi-tile plan of one case's Poisson sweeps on `blocks` blocks of at most
+// `tmax` threads and `smax` bytes of dynamic shared memory.
+bool ens_plan(const w2_ctx *c, int K, int blocks, int tmax, size_t smax, MixedGeom *mg, size_t *smem) {
+  const int NX = c->nx - 1, NY = c->ny - 1, H = 2 * K;
+  double best = 1e300;
+  for (int ntx = 1; ntx <= std::max(1, NX / 8); ++ntx) {
+    int tx = (NX + ntx - 1) / ntx;
+    tx = (tx + 7) / 8 * 8;
+    if ((NX + tx - 1) / tx != ntx) continue;
+    for (int nty = 1; nty <= std::max(1, NY / 4); ++nty) {
+      const int ty = (NY + nty - 1) / nty;
+      if ((NY + ty - 1) / ty != nty) continue;
+      const size_t sm = mixed_smem_bytes(K, tx, ty, false);
+      if (sm > smax || mixed_threads(K, tx, ty) > tmax) continue;
+      const int tpb = (ntx * nty + blocks - 1) / blocks;
+      const double cost = tpb * (mixed_sweep_work(K, tx, ty) + mixed_stage_work(K, tx, ty));
+      if (cost < best) {
+        best = cost;
+        *mg = MixedGeom{tx, ty, ntx, nty, ntx * tx / 2 + H, nty * ty + 2 * H, (tx / 2 + H + 31) / 32 * 32, 0};
+        *smem = sm;
+      }
+    }
+  }
+  return best < 1e300;
+}
+
+const void *ens_ppe_kernel(int K) {
+  switch (K) {
+    case 4: return (const void *)ke_ppe_mixed<4>;
+    case 8: return (const void *)ke_ppe_mixed<8>;
+  }
+  return nullptr;
+}
+
+int ens_launch_step(w2_ens *e, const EnsLaunch &Lm, const EnsLaunch &Lp, const EnsLaunch &L1) {
+  EnsLaunch am = Lm, ap = Lp;
+  void *argm[] = {&am}, *argp[] = {&ap};
+  ke_copy_mixed<<<e->blocks_m, e->threads, 0, e->st>>>(Lm);
+  ECK(cudaGetLastError());
+  ECK(cudaLaunchCooperativeKernel((const void *)ke_naux32, dim3(e->blocks_m), dim3(e->threads), argm,
+                                  e->smem_m, e->st));
+  ke_bc<<<e->n, e->threads, 0, e->st>>>(L1);
+  ECK(cudaGetLastError());
+  ECK(cudaLaunchCooperativeKernel(ens_ppe_kernel(e->K), dim3(e->blocks_p), dim3(e->threads), argp,
+                                  e->smem_p, e->st));
+  ECK(cudaLaunchCooperativeKernel((const void *)ke_step_post, dim3(e->blocks_m), dim3(e->threads), argm,
+                                  0, e->st));
+  ke_tick<<<1, 1, 0, e->st>>>(e->d_step);
+  ECK(cudaGetLastError());
+  e->launches += 6;
+  return W2_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads, int sweeps_per_barrier) {
+  if (!out || !cases || n < 1) return W2_E_ARG;
+  *out = nullptr;
+  w2_ens *e = new w2_ens();
+  auto bad = [&](int rc) {
+    if (rc != W2_OK) fprintf(stderr, "wolfd2gpu_ens_create: %s\n", e->err);
+    wolfd2gpu_ens_destroy(e);
+    return rc;
+  };
+  if (threads == 0) threads = 256;
+  if (sweeps_per_barrier == 0) sweeps_per_barrier = 4;
+  if (threads % 32 || threads < 64 || threads > kMaxThreads)
+    return bad(efail(e, W2_E_ARG, "threads must be a multiple of 32 in 64..%d", kMaxThreads));
+  if (!ens_ppe_kernel(sweeps_per_barrier)) return bad(efail(e, W2_E_ARG, "sweeps per barrier must be 4 or 8"));
+  e->n = n;
+  e->threads = threads;
+  e->K = sweeps_per_barrier;
+  e->cs.assign(cases, cases + n);
+  for (int k = 0; k < n; ++k) {
+    w2_ctx *c = e->cs[k];
+    if (!c) return bad(efail(e, W2_E_ARG, "case %d is null", k));
+    if (int rc = ready(c)) return bad(efail(e, rc, "case %d: %s", k, c->err));
+    if (!c->dev.ppe_unit)
+      return bad(efail(e, W2_E_UNSUPPORTED, "case %d: the mixed ensemble needs unit-stencil Poisson rows", k));
+    if (k == 0) e->device = c->device;
+    else if (c->device != e->device) return bad(efail(e, W2_E_ARG, "cases on different devices"));
+    if (int rc = ensure_f32(c)) return bad(efail(e, rc, "case %d: %s", k, c->err));
+    if (cudaStreamSynchronize(c->st) != cudaSuccess) return bad(efail(e, W2_E_CUDA, "case %d: set-up failed", k));
+  }
+  if (cudaSetDevice(e->device) != cudaSuccess) return bad(efail(e, W2_E_CUDA, "cudaSetDevice"));
+  cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, e->device);
+  // blocking, like the contexts' streams (ordered after legacy-stream set-up work)
+  if (cudaStreamCreate(&e->st) != cudaSuccess ||
+      cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess)
+    return bad(efail(e, W2_E_CUDA, "stream or event creation failed"));
+  std::vector<double> work(n);
+  for (int k = 0; k < n; ++k) work[k] = (double)(e->cs[k]->nx - 1) * (e->cs[k]->ny - 1);
+
+  // momentum and step-tail launches: blocks by the co-residency of both
+  e->smem_m = walk_stage_bytes(sizeof(double), threads);
+  if (cudaFuncSetAttribute((const void *)ke_naux32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)e->smem_m) != cudaSuccess)
+    return bad(efail(e, W2_E_CUDA, "shared memory attribute (momentum)"));
+  int occ_m = 0, occ_t = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_m, (const void *)ke_naux32, threads, e->smem_m);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, (const void *)ke_step_post, threads, 0);
+  e->blocks_m = std::min(occ_m, occ_t) * e->nsm;
+  e->bm = ens_partition(work, e->blocks_m);
+  if (e->bm.empty())
+    return bad(efail(e, W2_E_UNSUPPORTED, "%d cases need more blocks than the %d that fit", n, e->blocks_m));
+
+  // Poisson launch: two blocks per SM, each with half an SM's shared memory
+  const void *kp = ens_ppe_kernel(e->K);
+  int smem_sm = 0, smem_optin = 0;
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, e->device);
+  cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device);
+  cudaFuncAttributes fa{};
+  if (cudaFuncGetAttributes(&fa, kp) != cudaSuccess) return bad(efail(e, W2_E_CUDA, "kernel attributes"));
+  for (int per_sm = 2; per_sm >= 1; --per_sm) {
+    const size_t smax = std::min<size_t>((size_t)smem_optin, (size_t)smem_sm / per_sm - 1024) - fa.sharedSizeBytes;
+    const int total = per_sm * e->nsm;
+    std::vector<int> bp = ens_partition(work, total);
+    if (bp.empty()) continue;
+    std::vector<MixedGeom> g(n);
+    size_t smem = 0;
+    bool ok = true;
+    for (int k = 0; k < n && ok; ++k) {
+      size_t sk = 0;
+      ok = ens_plan(e->cs[k], e->K, bp[k], threads, smax, &g[k], &sk);
+      smem = std::max(smem, sk);
+    }
+    if (!ok) continue;
+    if (cudaFuncSetAttribute(kp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      continue;
+    int occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kp, threads, smem);
+    if (occ < per_sm) continue;
+    e->bp = bp;
+    e->blocks_p = total;
+    e->smem_p = smem;
+    e->h.resize(n);
+    for (int k = 0; k < n; ++k) e->h[k].g = g[k];
+    break;
+  }
+  if (e->bp.empty()) return bad(efail(e, W2_E_UNSUPPORTED, "no Poisson tile plan fits the ensemble"));
+
+  // per-case buffers and the parts of the descriptors that do not change
+  for (int k = 0; k < n; ++k) {
+    w2_ctx *c = e->cs[k];
+    EnsCase &h = e->h[k];
+    const MixedGeom &g = h.g;
+    const size_t plane2 = 2 * (size_t)g.gh * g.gw;
+    float *xb = ealloc<float>(e, 3 * plane2);
+    if (!xb) return bad(efail(e, W2_E_CUDA, "out of device memory (case %d Poisson buffers)", k));
+    h.d = c->dev;
+    chain_views(h.d, c->nx, c->ny, (long)e->bm[k] * threads, c->seg_req, c->warm_req);
+    for (int b = 0; b < 2; ++b) {
+      h.U[b] = c->U[b];
+      h.V[b] = c->V[b];
+      h.P[b] = c->P[b];
+      h.a[b] = MixedArgs{};
+      h.a[b].u = c->U[b];
+      h.a[b].v = c->V[b];
+      h.a[b].p = c->P[b];
+      h.a[b].xbuf0 = xb;
+      h.a[b].xbuf1 = xb + plane2;
+      h.a[b].rbuf = xb + 2 * plane2;
+    }
+    for (int q = 0; q < 4; ++q) h.F32[q] = c->F32[q];
+  }
+  std::vector<int> fm(n + 1, 0), fp(n + 1, 0), f1(n + 1, 0);
+  for (int k = 0; k < n; ++k) {
+    fm[k + 1] = fm[k] + e->bm[k];
+    fp[k + 1] = fp[k] + e->bp[k];
+    f1[k + 1] = k + 1;
+  }
+  e->d_cases = ealloc<EnsCase>(e, n);
+  e->d_first_m = ealloc<int>(e, n + 1);
+  e->d_first_p = ealloc<int>(e, n + 1);
+  e->d_first_1 = ealloc<int>(e, n + 1);
+  e->d_step = ealloc<int>(e, 1);
+  if (!e->d_cases || !e->d_first_m || !e->d_first_p || !e->d_first_1 || !e->d_step)
+    return bad(efail(e, W2_E_CUDA, "out of device memory (ensemble tables)"));
+  if (cudaMemcpy(e->d_first_m, fm.data(), fm.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(e->d_first_p, fp.data(), fp.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(e->d_first_1, f1.data(), f1.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+    return bad(efail(e, W2_E_CUDA, "table upload"));
+  if (cudaDeviceSynchronize() != cudaSuccess) return bad(efail(e, W2_E_CUDA, "set-up failed"));
+  *out = e;
+  return W2_OK;
+}
+
+int wolfd2gpu_ens_graph(w2_ens *e, int enable) {
+  if (!e) return W2_E_ARG;
+  e->graph_on = enable != 0;
+  return W2_OK;
+}
+
+int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat *stats) {
+  if (!e || !prm || nsteps < 0) return W2_E_ARG;
+  const int n = e->n;
+  for (int k = 0; k < n; ++k) {
+    const w2_params &q = prm[k];
+    if (q.precision != W2_PREC_MIXED)
+      return efail(e, W2_E_UNSUPPORTED, "case %d: the ensemble runs the mixed step (precision %d)", k, W2_PREC_MIXED);
+    if ((q.npsolver != 5 && q.npsolver != 6) || !q.lcartes)
+      return efail(e, W2_E_UNSUPPORTED, "case %d: the mixed step needs rb_sor/rb_sorp on a Cartesian grid", k);
+    if (q.msorit < 1 || q.mqiter < 1 || q.refine_sweeps < 0) return efail(e, W2_E_ARG, "case %d: bad parameters", k);
+  }
+  if (nsteps == 0) return W2_OK;
+  // descriptors of this call: parameters, starting levels
+  for (int k = 0; k < n; ++k) {
+    const w2_params &q = prm[k];
+    EnsCase &h = e->h[k];
+    h.cur = e->cs[k]->cur;
+    h.mqiter = q.mqiter;
+    h.dk = q.dk;
+    h.re = q.re;
+    h.qtol = q.qtol;
+    for (int b = 0; b < 2; ++b) {
+      MixedArgs &a = h.a[b];
+      a.lcartes = q.lcartes;
+      a.msorit = q.msorit;
+      a.inner = q.refine_sweeps > 0 ? q.refine_sweeps : 16 * e->K;
+      a.dk = q.dk;
+      a.sortol = q.sortol;
+      a.relax = (float)q.sorrel;
+    }
+  }
+  ECK(cudaMemcpyAsync(e->d_cases, e->h.data(), sizeof(EnsCase) * n, cudaMemcpyHostToDevice, e->st));
+  const size_t need = (size_t)n * nsteps;
+  if (need > e->outs_cap) {
+    if (e->d_outs) {
+      cudaFree(e->d_outs);
+      e->allocs.erase(std::remove(e->allocs.begin(), e->allocs.end(), (void *)e->d_outs), e->allocs.end());
+    }
+    e->d_outs = ealloc<StepOut>(e, need);
+    if (!e->d_outs) return efail(e, W2_E_CUDA, "out of device memory (step records)");
+    e->outs_cap = need;
+    e->graph_nsteps = -1;
+  }
+  ECK(cudaMemsetAsync(e->d_step, 0, sizeof(int), e->st));
+  const EnsLaunch Lm{e->d_cases, e->d_first_m, n, e->d_step, e->d_outs, nsteps};
+  const EnsLaunch Lp{e->d_cases, e->d_first_p, n, e->d_step, e->d_outs, nsteps};
+  const EnsLaunch L1{e->d_cases, e->d_first_1, n, e->d_step, e->d_outs, nsteps};
+  if (e->graph_on && e->graph_nsteps != nsteps) {
+    if (e->gexec) {
+      cudaGraphExecDestroy(e->gexec);
+      e->gexec = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    ECK(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
+    const long long l0 = e->launches;
+    int rc = ens_launch_step(e, Lm, Lp, L1);
+    e->launches = l0;
+    cudaError_t ce = cudaStreamEndCapture(e->st, &g);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return efail(e, W2_E_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(&e->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return efail(e, W2_E_CUDA, "graph instantiation: %s", cudaGetErrorString(ce));
+    e->graph_nsteps = nsteps;
+  }
+  ECK(cudaEventRecord(e->ev0, e->st));
+  for (int s = 0; s < nsteps; ++s) {
+    if (e->graph_on) {
+      ECK(cudaGraphLaunch(e->gexec, e->st));
+      e->launches += 6;
+    } else if (int rc = ens_launch_step(e, Lm, Lp, L1)) {
+      return rc;
+    }
+  }
+  ECK(cudaEventRecord(e->ev1, e->st));
+  std::vector<StepOut> outs(need);
+  ECK(cudaMemcpyAsync(outs.data(), e->d_outs, sizeof(StepOut) * need, cudaMemcpyDeviceToHost, e->st));
+  ECK(cudaStreamSynchronize(e->st));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e->ev0, e->ev1);
+  e->last_ms = ms;
+  int rc = W2_OK, diverged = -1;
+  for (int k = 0; k < n; ++k) {
+    w2_ctx *c = e->cs[k];
+    Sync sy;
+    ECK(cudaMemcpy(&sy, c->dev.sync, sizeof(Sync), cudaMemcpyDeviceToHost));
+    if (sy.error || sy.halt) {
+      Sync z;
+      memset(&z, 0, sizeof(z));
+      ECK(cudaMemcpy(c->dev.sync, &z, sizeof(Sync), cudaMemcpyHostToDevice));
+      if (sy.error && rc == W2_OK)
+        rc = efail(e, sy.error, "case %d: device error %d%s", k, sy.error,
+                   sy.error == W2_E_TIMEOUT ? " (device wait exceeded its time limit)" : "");
+    }
+    c->cur = (c->cur + nsteps) & 1;
+    for (int s = 0; s < nsteps; ++s) {
+      const StepOut &o = outs[(size_t)k * nsteps + s];
+      if (stats) {
+        w2_stepstat &t = stats[(size_t)k * nsteps + s];
+        t.nQLiter = o.nql;
+        t.nSorConv = o.nsor;
+        for (int q = 0; q < 4; ++q) t.dif[q] = o.dif[q];
+        t.divmax = o.divmax;
+      }
+      const double mx = std::max(std::max(o.dif[0], o.dif[1]), o.dif[2]);
+      if (diverged < 0 && mx > 1.0e12) diverged = k;
+    }
+  }
+  if (rc == W2_OK && diverged >= 0)
+    return efail(e, W2_E_DIVERGED, "case %d diverged. Please reduce CFL number.", diverged);
+  return rc;
+}
+
+int wolfd2gpu_ens_info(w2_ens *e, int *blocks_momentum, int *blocks_poisson, double *last_ms,
+                       long long *launches) {
+  if (!e) return W2_E_ARG;
+  if (blocks_momentum) *blocks_momentum = e->blocks_m;
+  if (blocks_poisson) *blocks_poisson = e->blocks_p;
+  if (last_ms) *last_ms = e->last_ms;
+  if (launches) *launches = e->launches;
+  return W2_OK;
+}
+
+const char *wolfd2gpu_ens_error(w2_ens *e) { return e ? e->err : "null ensemble"; }
+
+int wolfd2gpu_ens_destroy(w2_ens *e) {
+  if (!e) return W2_OK;
+  if (e->st) cudaStreamSynchronize(e->st);
+  if (e->gexec) cudaGraphExecDestroy(e->gexec);
+  for (void *p : e->allocs) cudaFree(p);
+  if (e->ev0) cudaEventDestroy(e->ev0);
+  if (e->ev1) cudaEventDestroy(e->ev1);
+  if (e->st) cudaStreamDestroy(e->st);
+  delete e;
+  return W2_OK;
 }
 
 }  // extern "C"

@@ -466,7 +466,7 @@ __device__ bool solve_chains(const Dev &d, const ChainT<T> &c0, const ChainT<T> 
   int cur = 0;
   bool settled = false;
   for (int round = 0; round < nrounds; ++round) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (vblock() == 0 && threadIdx.x == 0) {
       if (round == 0) sy->iout[0] = 0;
       sy->iout[(round + 1) % 3] = 0;
     }
@@ -486,13 +486,13 @@ __device__ bool solve_chains(const Dev &d, const ChainT<T> &c0, const ChainT<T> 
     cur ^= 1;
     if (!ch) {
       settled = true;
-      if (blockIdx.x == 0 && threadIdx.x == 0) atomicMax(&sy->max_rounds, round + 1);
+      if (vblock() == 0 && threadIdx.x == 0) atomicMax(&sy->max_rounds, round + 1);
       break;
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0 && !settled) atomicMax(&sy->max_rounds, nrounds + 1);
+  if (vblock() == 0 && threadIdx.x == 0 && !settled) atomicMax(&sy->max_rounds, nrounds + 1);
   if (!settled) {
-    if (blockIdx.x == 0 && threadIdx.x < 32) {
+    if (vblock() == 0 && threadIdx.x < 32) {
       // copies: the guard walk must not take the address of parameter space
       const ChainT<T> t0 = c0, t1 = c1;
       chain_sequential_warp(t0, true);
@@ -514,7 +514,7 @@ __device__ bool solve_chains(const Dev &d, const ChainT<T> &c0, const ChainT<T> 
   cur = 0;
   settled = false;
   for (int round = 0; round < nrounds; ++round) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (vblock() == 0 && threadIdx.x == 0) {
       if (round == 0) sy->iout[3] = 0;
       sy->iout[3 + (round + 1) % 3] = 0;
     }
@@ -534,12 +534,12 @@ __device__ bool solve_chains(const Dev &d, const ChainT<T> &c0, const ChainT<T> 
     cur ^= 1;
     if (!ch) {
       settled = true;
-      if (blockIdx.x == 0 && threadIdx.x == 0) atomicMax(&sy->max_rounds, round + 1);
+      if (vblock() == 0 && threadIdx.x == 0) atomicMax(&sy->max_rounds, round + 1);
       break;
     }
   }
   if (!settled) {
-    if (blockIdx.x == 0 && threadIdx.x < 32) {
+    if (vblock() == 0 && threadIdx.x < 32) {
       // forward values are exact here; redo the back substitution serially
       const ChainT<T> t0 = c0, t1 = c1;
       chain_sequential_warp(t0, false);

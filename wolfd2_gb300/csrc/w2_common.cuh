@@ -171,13 +171,34 @@ __device__ __forceinline__ int read_error(Sync *s) {
       cuda::memory_order_acquire);
 }
 
+// ---- virtual grid ---------------------------------------------------------
+// The blocks that work on one case: a single-case launch is its own virtual
+// grid; an ensemble launch gives each case a group of consecutive blocks.
+// Every kernel sets it at entry (vgrid_set), and device routines index,
+// reduce and synchronise within it (vblock, vblocks, gtid, gthreads,
+// grid_sync).
+struct VGrid {
+  int first, count;
+};
+__device__ __forceinline__ VGrid &vgrid_slot() {
+  __shared__ VGrid g;
+  return g;
+}
+// Every thread of the block writes the same values, so each thread reads
+// back what it wrote without a block barrier.
+__device__ __forceinline__ void vgrid_set(int first, int count) { vgrid_slot() = VGrid{first, count}; }
+__device__ __forceinline__ int vblock() { return (int)blockIdx.x - vgrid_slot().first; }
+__device__ __forceinline__ int vblocks() { return vgrid_slot().count; }
+__device__ __forceinline__ int gtid() { return vblock() * (int)blockDim.x + (int)threadIdx.x; }
+__device__ __forceinline__ int gthreads() { return vblocks() * (int)blockDim.x; }
+
 // Grid barrier with a time limit.  All blocks of a cooperative launch call
 // it the same number of times.  On timeout the sticky error is set and every
 // caller returns false; callers then leave the kernel.
 static __device__ __noinline__ bool grid_sync(Sync *s) {
   __shared__ int ok;
   __syncthreads();
-  if (gridDim.x == 1) {
+  if (vblocks() == 1) {
     if (threadIdx.x == 0) ok = (read_error(s) == 0);
     __syncthreads();
     return ok;
@@ -187,7 +208,7 @@ static __device__ __noinline__ bool grid_sync(Sync *s) {
     __threadfence();
     unsigned g = gen.load(cuda::memory_order_acquire);
     unsigned a = cnt.fetch_add(1u, cuda::memory_order_acq_rel);
-    if (a == gridDim.x - 1) {
+    if (a == (unsigned)vblocks() - 1u) {
       cnt.store(0u, cuda::memory_order_relaxed);
       gen.fetch_add(1u, cuda::memory_order_acq_rel);
     } else {
@@ -255,7 +276,6 @@ __device__ __forceinline__ double slot_value(const unsigned long long *slot) {
 // Max helper matching the reference's dmax1/max on non-NaN values.
 __device__ __forceinline__ double dmax(double a, double b) { return b > a ? b : a; }
 
-__device__ __forceinline__ int gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
-__device__ __forceinline__ int gthreads() { return gridDim.x * blockDim.x; }
+
 
 }  // namespace w2

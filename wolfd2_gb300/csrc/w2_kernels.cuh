@@ -19,6 +19,7 @@ struct StepOut {
 
 // ---- grid metrics (grid.f:258-535) ------------------------------------
 __global__ void k_mirror(Dev d, double *x, double *y) {
+  vgrid_set(0, gridDim.x);
   const int nx = d.nx, ny = d.ny;
 #define X(i, j) x[IX(d, i, j)]
 #define Y(i, j) y[IX(d, i, j)]
@@ -48,6 +49,7 @@ __global__ void k_mirror(Dev d, double *x, double *y) {
 
 __global__ void k_fullgrid_uv(Dev d, const double *x, const double *y, double *xu, double *yu,
                               double *xv, double *yv) {
+  vgrid_set(0, gridDim.x);
   const int nx = d.nx, ny = d.ny, W = nx + 2, H = ny + 2;
   for (int t = gtid(); t < W * H; t += gthreads()) {
     const int i = t % W, j = t / W;
@@ -64,6 +66,7 @@ __global__ void k_fullgrid_uv(Dev d, const double *x, const double *y, double *x
 }
 
 __global__ void k_fullgrid_c(Dev d, const double *xu, const double *yv, double *xc, double *yc) {
+  vgrid_set(0, gridDim.x);
   const int nx = d.nx, ny = d.ny;
   for (int t = gtid(); t < (nx + 1) * (ny + 1); t += gthreads()) {
     const int i = t % (nx + 1) + 1, j = t / (nx + 1) + 1;
@@ -83,6 +86,7 @@ struct MetricOut {
 __global__ void k_metric(Dev d, MetricOut m, const double *xn, const double *yn, const double *xu,
                          const double *yu, const double *xv, const double *yv, const double *xc,
                          const double *yc) {
+  vgrid_set(0, gridDim.x);
   const int nx = d.nx, ny = d.ny;
   for (int t = gtid(); t < nx * ny; t += gthreads()) {
     const int i = t % nx + 1, j = t / nx + 1;
@@ -137,12 +141,19 @@ __global__ void k_metric(Dev d, MetricOut m, const double *xn, const double *yn,
 #undef Y
 }
 
-__global__ void k_ppe_coef(Dev d) { ppe_coefficients(d); }
-__global__ void k_ppe_check(Dev d, int *flag) { ppe_check_unit(d, flag); }
+__global__ void k_ppe_coef(Dev d) {
+  vgrid_set(0, gridDim.x);
+  ppe_coefficients(d);
+}
+__global__ void k_ppe_check(Dev d, int *flag) {
+  vgrid_set(0, gridDim.x);
+  ppe_check_unit(d, flag);
+}
 
 // ---- field copies -------------------------------------------------------
 __global__ void k_copy3(Dev d, double *a, const double *a0, double *b, const double *b0,
                         double *c, const double *c0) {
+  vgrid_set(0, gridDim.x);
   if (d.sync->halt) return;
   const int W = d.nx + 2, H = d.ny + 2;
   for (int t = gtid(); t < W * H; t += gthreads()) {
@@ -155,6 +166,7 @@ __global__ void k_copy3(Dev d, double *a, const double *a0, double *b, const dou
 
 // us(1..nx+1,1..ny+1) = un, vs = vn (momentum.f:114-119)
 __global__ void k_naux_init(Dev d, const double *un, const double *vn, double *us, double *vs) {
+  vgrid_set(0, gridDim.x);
   const int W = d.nx + 1, H = d.ny + 1;
   for (int t = gtid(); t < W * H; t += gthreads()) {
     const size_t o = IX(d, t % W + 1, t / W + 1);
@@ -168,22 +180,21 @@ __global__ void __launch_bounds__(kMaxThreads, 1) k_naux(Dev d, int mqiter, doub
                                                       double qtol, const double *un,
                                                       const double *vn, double *us, double *vs,
                                                       StepOut *out) {
+  vgrid_set(0, gridDim.x);
   if (d.sync->halt) return;
   int res = -1;
   if (!naux_momentum<double>(d, d.f64, mqiter, dk, re, qtol, un, vn, us, vs, &res)) return;
-  if (blockIdx.x == 0 && threadIdx.x == 0) out->nql = res;
+  if (vblock() == 0 && threadIdx.x == 0) out->nql = res;
 }
 
 // nAuxMomentum in single precision (mixed path) on un32, vn32 -> us32, vs32,
 // then us, vs = the FP32 results widened to FP64 on every cell.
-__global__ void __launch_bounds__(kMaxThreads, 1) k_naux32(Dev d, int mqiter, double dk, double re,
-                                                        double qtol, const float *un,
-                                                        const float *vn, float *us, float *vs,
-                                                        double *us64, double *vs64, StepOut *out) {
-  if (d.sync->halt) return;
+__device__ __forceinline__ void naux32_body(const Dev &d, int mqiter, double dk, double re, double qtol,
+                                            const float *un, const float *vn, float *us, float *vs,
+                                            double *us64, double *vs64, StepOut *out) {
   int res = -1;
   if (!naux_momentum<float>(d, d.f32, mqiter, dk, re, qtol, un, vn, us, vs, &res)) return;
-  if (blockIdx.x == 0 && threadIdx.x == 0) out->nql = res;
+  if (vblock() == 0 && threadIdx.x == 0) out->nql = res;
   const int W = d.nx + 2, H = d.ny + 2;
   for (int t = gtid(); t < W * H; t += gthreads()) {
     const size_t o = IX(d, t % W, t / W);
@@ -192,12 +203,21 @@ __global__ void __launch_bounds__(kMaxThreads, 1) k_naux32(Dev d, int mqiter, do
   }
 }
 
+__global__ void __launch_bounds__(kMaxThreads, 1) k_naux32(Dev d, int mqiter, double dk, double re,
+                                                        double qtol, const float *un,
+                                                        const float *vn, float *us, float *vs,
+                                                        double *us64, double *vs64, StepOut *out) {
+  vgrid_set(0, gridDim.x);
+  if (d.sync->halt) return;
+  naux32_body(d, mqiter, dk, re, qtol, un, vn, us, vs, us64, vs64, out);
+}
+
 // Time-level copies of the mixed step: p = pn, and the single-precision
 // momentum inputs un32 = (float)un, vn32 = (float)vn, us32 = un32,
 // vs32 = vn32 on every cell.
-__global__ void k_copy_mixed(Dev d, double *p, const double *pn, const double *un,
-                             const double *vn, float *un32, float *vn32, float *us32,
-                             float *vs32) {
+__device__ __forceinline__ void copy_mixed_body(const Dev &d, double *p, const double *pn,
+                                                const double *un, const double *vn, float *un32,
+                                                float *vn32, float *us32, float *vs32) {
   const int W = d.nx + 2, H = d.ny + 2;
   for (int t = gtid(); t < W * H; t += gthreads()) {
     const size_t o = IX(d, t % W, t / W);
@@ -210,8 +230,16 @@ __global__ void k_copy_mixed(Dev d, double *p, const double *pn, const double *u
   }
 }
 
+__global__ void k_copy_mixed(Dev d, double *p, const double *pn, const double *un,
+                             const double *vn, float *un32, float *vn32, float *us32,
+                             float *vs32) {
+  vgrid_set(0, gridDim.x);
+  copy_mixed_body(d, p, pn, un, vn, un32, vn32, us32, vs32);
+}
+
 // Metric array rounded to single precision.
 __global__ void k_to_f32(Dev d, const double *src, float *dst) {
+  vgrid_set(0, gridDim.x);
   const int W = d.nx + 2, H = d.ny + 2;
   for (int t = gtid(); t < W * H; t += gthreads()) {
     const size_t o = IX(d, t % W, t / W);
@@ -222,13 +250,18 @@ __global__ void k_to_f32(Dev d, const double *src, float *dst) {
 // ---- boundary programs (one block) -------------------------------------
 enum : int { BC_VEL = 1, BC_PRES = 2, BC_OUTFLOW = 4 };
 
-__global__ void k_bc(Dev d, int ops, double *u, double *v, double *p) {
-  if (d.sync->halt) return;
+__device__ __forceinline__ void bc_body(const Dev &d, int ops, double *u, double *v, double *p) {
   bool ok = true;
   if (ops & BC_OUTFLOW) ok = ok && vel_outflow_bcs_block(d, u, v);
   if (ops & BC_VEL) ok = ok && vel_bound_cond_block(d, u, v);
   if (ops & BC_PRES) ok = ok && pres_bound_cond_block(d, p);
   if (!ok && threadIdx.x == 0) set_error(d.sync, W2_E_BCFLAG);
+}
+
+__global__ void k_bc(Dev d, int ops, double *u, double *v, double *p) {
+  vgrid_set(0, gridDim.x);
+  if (d.sync->halt) return;
+  bc_body(d, ops, u, v, p);
 }
 
 // ---- Ppe -----------------------------------------------------------------
@@ -237,6 +270,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_ppe(Dev d, int lcartes, int nps
                                                      double dk, double sortol, double sorrel,
                                                      const double *u, const double *v, double *p,
                                                      StepOut *out) {
+  vgrid_set(0, gridDim.x);
   if (d.sync->halt) return;
   Sync *sy = d.sync;
   ppe_divergence(d, u, v);
@@ -247,7 +281,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_ppe(Dev d, int lcartes, int nps
   }
   int nconv = 0;
   if (npsolver == 1 || npsolver == 2) {
-    if (blockIdx.x == 0) {
+    if (vblock() == 0) {
       nconv = npsolver == 1 ? sor_lex_block(d, p, lcartes, msorit, dk, sortol, sorrel)
                             : slor_block(d, p, lcartes, msorit, dk, sortol, sorrel);
     }
@@ -255,7 +289,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_ppe(Dev d, int lcartes, int nps
     nconv = ppe_parallel(d, p, npsolver, lcartes, msorit, dk, sortol, sorrel);
     if (nconv < 0) return;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? msorit : nconv;
+  if (vblock() == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? msorit : nconv;
 }
 
 // Red/black SOR with two sweeps per grid barrier (unit-stencil rows,
@@ -264,6 +298,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) k_ppe_tiled(Dev d, TileGeom g,
                                                            int msorit, double dk, double sortol,
                                                            const double *u, const double *v,
                                                            double *p, StepOut *out) {
+  vgrid_set(0, gridDim.x);
   if (d.sync->halt) return;
   Sync *sy = d.sync;
   ppe_divergence(d, u, v);
@@ -272,7 +307,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) k_ppe_tiled(Dev d, TileGeom g,
   if (!grid_sync(sy)) return;
   const int nconv = ppe_rb_tiled(d, g, p, d.ppn, d.qh, msorit, sortol);
   if (nconv < 0) return;
-  if (blockIdx.x == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? msorit : nconv;
+  if (vblock() == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? msorit : nconv;
 }
 
 // Mixed-precision red/black SOR (FP32 sweeps, FP64 residual and correction)
@@ -281,10 +316,11 @@ __global__ void __launch_bounds__(kMaxThreads, 1) k_ppe_tiled(Dev d, TileGeom g,
 template <int K, bool RES>
 __global__ void __launch_bounds__(kMixedThreads, 1) k_ppe_mixed(Dev d, MixedGeom g, MixedArgs a,
                                                       StepOut *out) {
+  vgrid_set(0, gridDim.x);
   if (d.sync->halt) return;
   const int nconv = ppe_mixed<K, RES>(d, g, a);
   if (nconv < 0) return;
-  if (blockIdx.x == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? a.msorit : nconv;
+  if (vblock() == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? a.msorit : nconv;
 }
 
 // ---- Project (utility.f:253-440), masked -------------------------------
@@ -313,6 +349,7 @@ __device__ void project_grid(const Dev &d, double dk, const double *p, double *u
 }
 
 __global__ void k_project(Dev d, double dk, const double *p, double *u, double *v) {
+  vgrid_set(0, gridDim.x);
   if (d.sync->halt) return;
   project_grid(d, dk, p, u, v);
 }
@@ -331,6 +368,7 @@ __device__ double diff_norm_local(const Dev &d, const double *a, const double *b
 }
 
 __global__ void k_diff_norm(Dev d, const double *a, const double *b, unsigned long long *slot) {
+  vgrid_set(0, gridDim.x);
   block_max_to(slot, diff_norm_local(d, a, b));
 }
 
@@ -350,20 +388,18 @@ __device__ double div_check_local(const Dev &d, const double *u, const double *v
 // Tail of one step, main.f:813-972: PresBoundCond, Project, boundary
 // conditions of the starred and new fields, the three step norms, the
 // divergence guard and the discrete divergence check.
-__global__ void __launch_bounds__(kMaxThreads) k_step_post(Dev d, double dk, double *p,
-                                                           const double *pn, const double *un,
-                                                           const double *vn, double *u,
-                                                           double *v, StepOut *out) {
-  if (d.sync->halt) return;
+__device__ __forceinline__ void step_post_body(const Dev &d, double dk, double *p, const double *pn,
+                                               const double *un, const double *vn, double *u,
+                                               double *v, StepOut *out) {
   Sync *sy = d.sync;
-  if (blockIdx.x == 0) {
+  if (vblock() == 0) {
     if (!pres_bound_cond_block(d, p) && threadIdx.x == 0) set_error(sy, W2_E_BCFLAG);
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) sy->red[6] = sy->red[7] = sy->red[8] = sy->red[16] = 0ull;
+  if (vblock() == 0 && threadIdx.x == 0) sy->red[6] = sy->red[7] = sy->red[8] = sy->red[16] = 0ull;
   if (!grid_sync(sy)) return;
   project_grid(d, dk, p, u, v);
   if (!grid_sync(sy)) return;
-  if (blockIdx.x == 0) {
+  if (vblock() == 0) {
     bool ok = vel_bound_cond_block(d, u, v) && pres_bound_cond_block(d, p);
     // u = us etc. (main.f:864-870) is a buffer swap on the host; then
     // main.f:946-953 applies the conditions again to the new level.
@@ -376,7 +412,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_step_post(Dev d, double dk, dou
   block_max_to(&sy->red[8], diff_norm_local(d, vn, v));
   block_max_to(&sy->red[16], div_check_local(d, u, v));
   if (!grid_sync(sy)) return;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (vblock() == 0 && threadIdx.x == 0) {
     out->dif[0] = slot_value(&sy->red[6]);
     out->dif[1] = slot_value(&sy->red[7]);
     out->dif[2] = slot_value(&sy->red[8]);
@@ -387,8 +423,18 @@ __global__ void __launch_bounds__(kMaxThreads) k_step_post(Dev d, double dk, dou
   }
 }
 
+__global__ void __launch_bounds__(kMaxThreads) k_step_post(Dev d, double dk, double *p,
+                                                           const double *pn, const double *un,
+                                                           const double *vn, double *u,
+                                                           double *v, StepOut *out) {
+  vgrid_set(0, gridDim.x);
+  if (d.sync->halt) return;
+  step_post_body(d, dk, p, pn, un, vn, u, v, out);
+}
+
 // ---- Filter (utility.f:33-247), velocity components ---------------------
 __global__ void k_filter(Dev d, int bit, double fp, const double *qu, double *qh) {
+  vgrid_set(0, gridDim.x);
   const int W = d.nx + 2, H = d.ny + 2;
   for (int t = gtid(); t < W * H; t += gthreads()) {
     const int i = t % W, j = t / W;

@@ -403,12 +403,12 @@ __device__ bool naux_momentum(const Dev &d, const MomView<T> &V, int mqiter, dou
   int result = -1;
   for (int it = 1; it <= mqiter; ++it) {
     if (d.has_outflow) {
-      if (blockIdx.x == 0 && !vel_outflow_bcs_block(d, us, vs) && threadIdx.x == 0)
+      if (vblock() == 0 && !vel_outflow_bcs_block(d, us, vs) && threadIdx.x == 0)
         set_error(sy, W2_E_BCFLAG);
       if (!grid_sync(sy)) return false;
     }
     if constexpr (!kFuseConv<T>) mom_conv_coef(d, V, us, vs, un, vn);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (vblock() == 0 && threadIdx.x == 0) {
       if (it == 1) sy->red[1] = 0ull;
       sy->red[(it + 1) % 3] = 0ull;
     }

@@ -66,6 +66,7 @@ __device__ __forceinline__ double na_point(const NaArgs &a, const double *b, int
 }
 
 __global__ void __launch_bounds__(512) k_ppe_noalloc(NaArgs a) {
+  w2::vgrid_set(0, gridDim.x);
   w2::Sync *sy = reinterpret_cast<w2::Sync *>(a.scratch);
   double *b = reinterpret_cast<double *>(a.scratch + kSyncBytes);
   const int nx = a.nx, ny = a.ny;
@@ -90,7 +91,7 @@ __global__ void __launch_bounds__(512) k_ppe_noalloc(NaArgs a) {
   const int nh = (nx - 2) / 2 + 1;
   for (int it = 1; it <= a.msorit; ++it) {
     unsigned long long *slot = &sy->red[it % 3];
-    if (blockIdx.x == 0 && threadIdx.x == 0) sy->red[(it + 1) % 3] = 0ull;
+    if (w2::vblock() == 0 && threadIdx.x == 0) sy->red[(it + 1) % 3] = 0ull;
     unsigned long long mx = 0ull;
     for (int parity = 0; parity < 2; ++parity) {
       for (int t = w2::gtid(); t < nh * (ny - 1); t += w2::gthreads()) {
@@ -109,7 +110,7 @@ __global__ void __launch_bounds__(512) k_ppe_noalloc(NaArgs a) {
       break;
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) sy->iout[0] = nconv < 1 ? a.msorit : nconv;
+  if (w2::vblock() == 0 && threadIdx.x == 0) sy->iout[0] = nconv < 1 ? a.msorit : nconv;
 }
 
 std::mutex g_setup_mu;

@@ -274,7 +274,7 @@ __device__ int ppe_parallel(const Dev &d, double *p, int npsolver, int lcartes, 
   const int nx = d.nx, ny = d.ny;
   for (int it = 1; it <= msorit; ++it) {
     unsigned long long *slot = &sy->red[3 + it % 3];
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (vblock() == 0 && threadIdx.x == 0) {
       if (it == 1) sy->red[3 + 1] = 0ull;
       sy->red[3 + (it + 1) % 3] = 0ull;
     }

@@ -113,6 +113,11 @@ template <int K, int C, int P0>
 __device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, int h, bool act0, bool act1,
                                                    float relax) {
   constexpr int H = 2 * K;
+  // A strip wholly below the box (a block with more threads than its tile
+  // plan needs, as in ensemble launches) has nothing to do and must not
+  // load: its rows lie past the shared planes.  Uniform per warp (a strip
+  // spans whole warps).
+  if (b.vrow == 0u) return 0u;
   const float *Rc = b.R[C];
   float *Ec = b.E[C];
   const float *Eo = b.E[C ^ 1];
@@ -475,7 +480,7 @@ template <int K, bool RES>
 __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
   Sync *sy = d.sync;
   unsigned long long *ring = &sy->red[kMixedRing];
-  if (blockIdx.x == 0 && threadIdx.x == 0)
+  if (vblock() == 0 && threadIdx.x == 0)
     for (int k = 0; k < 3 * K; ++k) ring[k] = 0ull;
   ppe_divergence(d, a.u, a.v);
   if (!grid_sync(sy)) return -1;
@@ -487,9 +492,9 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
   float *fs = reinterpret_cast<float *>(smem);
   const int ntiles = g.ntx * g.nty;
   constexpr bool resident = RES;
-  const bool has = (int)blockIdx.x < ntiles;
+  const bool has = vblock() < ntiles;
   MixedBox b;
-  if constexpr (resident) mixed_setup<K>(d, g, b, blockIdx.x, fs, true);
+  if constexpr (resident) mixed_setup<K>(d, g, b, vblock(), fs, true);
 
   int m = 0, result = 0, grp = 0;
   bool done = false;
@@ -498,7 +503,7 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
       if (has) mixed_residual(d, b, a.p);
       __syncthreads();
     } else {
-      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+      for (int tile = vblock(); tile < ntiles; tile += vblocks()) {
         mixed_setup<K>(d, g, b, tile, fs, false);
         mixed_residual_tile<K>(d, g, b, a.p, a.rbuf);
       }
@@ -509,7 +514,7 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
     while (true) {
       const int ns = min(K, min(a.inner - in_pass, a.msorit - m));
       unsigned long long *slots = ring + (grp % 3) * K;
-      if (blockIdx.x == 0 && threadIdx.x == 0) {
+      if (vblock() == 0 && threadIdx.x == 0) {
         unsigned long long *next = ring + ((grp + 1) % 3) * K;
         for (int k = 0; k < K; ++k) next[k] = 0ull;
       }
@@ -519,7 +524,7 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
         if (has) mixed_group<K>(g, b, ns, a.relax, ein, eout, slots);
       } else {
         for (int t = threadIdx.x; t < K * 32; t += blockDim.x) redm[t / 32][t % 32] = 0u;
-        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        for (int tile = vblock(); tile < ntiles; tile += vblocks()) {
           mixed_setup<K>(d, g, b, tile, fs, false);
           mixed_box_load<K>(g, b, ein, b.E[0], b.E[1]);
           mixed_box_load<K>(g, b, a.rbuf, b.R[0], b.R[1]);
@@ -548,7 +553,7 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
             if (has) mixed_redo<K>(b, conv + 1, a.relax);
           } else {
             // the group's input buffer is intact: sweep again from it
-            for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+            for (int tile = vblock(); tile < ntiles; tile += vblocks()) {
               mixed_setup<K>(d, g, b, tile, fs, false);
               mixed_box_load<K>(g, b, ein, b.E[0], b.E[1]);
               mixed_box_load<K>(g, b, a.rbuf, b.R[0], b.R[1]);
@@ -573,7 +578,7 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
     if constexpr (resident) {
       if (has) mixed_correct(d, b, a.p);
     } else {
-      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+      for (int tile = vblock(); tile < ntiles; tile += vblocks()) {
         mixed_setup<K>(d, g, b, tile, fs, false);
         mixed_correct_tile<K>(d, g, b, a.p, efinal);
       }

@@ -99,7 +99,7 @@ __device__ void tiled_group(const Dev &d, const TileGeom &g, const double *pin, 
   double *P = smem, *Bt = smem + W * Hh;
   __shared__ unsigned long long red[kSweepsPerSync][32];
   const int ntiles = g.ntx * g.nty;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  for (int tile = vblock(); tile < ntiles; tile += vblocks()) {
     const int ti = tile % g.ntx, tj = tile / g.ntx;
     const int oi0 = 2 + ti * g.tx, oj0 = 2 + tj * g.ty;
     const int oi1 = min(d.nx, oi0 + g.tx - 1), oj1 = min(d.ny, oj0 + g.ty - 1);
@@ -184,14 +184,14 @@ __device__ int ppe_rb_tiled(const Dev &d, const TileGeom &g, double *p, double *
   // every block before group g-1's barrier -- so one barrier per group
   // orders both the clear and the reads.
   unsigned long long *ring = &sy->red[10];
-  if (blockIdx.x == 0 && threadIdx.x == 0)
+  if (vblock() == 0 && threadIdx.x == 0)
     for (int k = 0; k < 3 * kSweepsPerSync; ++k) ring[k] = 0ull;
   if (!grid_sync(sy)) return -1;
   int grp = 0;
   for (int m0 = 1; m0 <= msorit; m0 += kSweepsPerSync, ++grp) {
     const int ns = min(kSweepsPerSync, msorit - m0 + 1);
     unsigned long long *slots = ring + (grp % 3) * kSweepsPerSync;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (vblock() == 0 && threadIdx.x == 0) {
       unsigned long long *next = ring + ((grp + 1) % 3) * kSweepsPerSync;
       for (int k = 0; k < kSweepsPerSync; ++k) next[k] = 0ull;
     }

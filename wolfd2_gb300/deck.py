@@ -389,12 +389,12 @@ def _uniform_nodes(ncx: int, ncy: int, lx: float, ly: float):
 
 
 def cavity(n: int, re: float, dt: float, *, lid: float = 1.0,
-           solver: str = "sor", ny: Optional[int] = None, **kw) -> Case:
-    """Lid-driven cavity on the unit square with n x n uniform cells: no-slip
-    walls, north wall moving at ``lid`` (``wall 1 1 north tv <lid>``), fluid
-    with rho = 1 and mu = 1/re, dlref = uref = 1."""
+           solver: str = "sor", ny: Optional[int] = None, side: float = 1.0, **kw) -> Case:
+    """Lid-driven cavity of width ``side`` (the unit square by default) with
+    n x n uniform cells: no-slip walls, north wall moving at ``lid`` (``wall
+    1 1 north tv <lid>``), fluid with rho = 1 and mu = 1/re, dlref = uref = 1."""
     ncy = n if ny is None else ny
-    X, Y = _uniform_nodes(n, ncy, 1.0, float(ncy) / n)
+    X, Y = _uniform_nodes(n, ncy, side, side * float(ncy) / n)
     nx, nyy = n + 1, ncy + 1
     bc = ("number_of_regions 1 1\n"
           "i_borders\n"
@@ -471,6 +471,51 @@ def channel_ic(case: Case):
     u = np.zeros((case.nx + 2, case.ny + 2), order="F")
     u[:, :] = prof[None, :]
     return u, np.zeros_like(u), np.zeros_like(u)
+
+
+ENSEMBLE_SIZES = tuple(range(64, 513, 32))
+ENSEMBLE_H = 1.0 / 64.0
+
+
+@dataclasses.dataclass
+class EnsembleMember:
+    case: Case
+    n: int           # cells per side
+    re: float        # cavity Reynolds number U L / nu
+    dt_named: float  # 0.5 h in the unit-cavity frame
+    dt: float        # the step used (unit-cavity frame)
+
+
+def ensemble_cases(count: int = 256, seed: int = 2024, visc_max: float = 0.25,
+                   solver: str = "rb_sor") -> List[EnsembleMember]:
+    """The batched-ensemble workload: ``count`` lid-driven cavities, N cells
+    per side drawn uniformly from {64, 96, ..., 512} and the cavity Reynolds
+    number log-uniform in [100, 5000], both from default_rng(seed), dt = 0.5 h.
+
+    Each cavity is laid out with the same power-of-two spacing h = 1/64 and
+    side L = N/64, with deck Re = Re_cavity / L: the exact similarity image of
+    the unit cavity with h = 1/N at Re_cavity (lengths times L, times times
+    L), so dt = 0.5 h in either frame.  Exact node coordinates give every
+    Poisson row the unit stencil, which the mixed sweeps need.
+
+    The reference's scheme is unstable above a viscous number dt/(h^2 Re)
+    of about 0.3 (0.64 reaches NaN within 8 steps), and 0.5 h / (h^2 Re) =
+    0.5 N / Re exceeds that for small Re and large N, so dt is capped at
+    visc_max h^2 Re; ``dt_named`` and ``dt`` record both."""
+    rng = np.random.default_rng(seed)
+    ns = rng.choice(np.array(ENSEMBLE_SIZES), size=count)
+    res = np.exp(rng.uniform(np.log(100.0), np.log(5000.0), size=count))
+    out = []
+    for n, re in zip(ns.tolist(), res.tolist()):
+        side = n * ENSEMBLE_H
+        h_unit = 1.0 / n
+        dt_named = 0.5 * h_unit
+        dt = min(dt_named, visc_max * h_unit * h_unit * re)
+        # deck frame: lengths x side, time x side, Re_deck = Re / side
+        case = cavity(n, re / side, dt * side, solver=solver, side=side)
+        case.name = f"ens_cavity{n}_re{re:.1f}"
+        out.append(EnsembleMember(case, n, re, dt_named, dt))
+    return out
 
 
 def perturbation_ic(case: Case, seed: int, modes: int = 16, amp: float = 1.0e-3):

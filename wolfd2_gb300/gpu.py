@@ -118,6 +118,13 @@ def lib():
     L.wolfd2gpu_ppe_rbsor_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                               C.c_double, C.c_double, C.c_double] + [vp] * 9 + [_ip, vp]
     L.wolfd2gpu_profile_read.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_longlong)]
+    L.wolfd2gpu_ens_create.argtypes = [C.POINTER(vp), C.POINTER(vp), C.c_int, C.c_int, C.c_int]
+    L.wolfd2gpu_ens_step.argtypes = [vp, C.POINTER(Params), C.c_int, C.POINTER(StepStat)]
+    L.wolfd2gpu_ens_graph.argtypes = [vp, C.c_int]
+    L.wolfd2gpu_ens_info.argtypes = [vp, _ip, _ip, _dp, C.POINTER(C.c_longlong)]
+    L.wolfd2gpu_ens_error.argtypes = [vp]
+    L.wolfd2gpu_ens_error.restype = C.c_char_p
+    L.wolfd2gpu_ens_destroy.argtypes = [vp]
     _lib = L
     return L
 
@@ -346,3 +353,56 @@ class Solver:
         self._check(self.L.wolfd2gpu_device_fields(self.h, C.byref(u), C.byref(v), C.byref(p), C.byref(ld)))
         return (C.cast(u, C.c_void_p).value, C.cast(v, C.c_void_p).value,
                 C.cast(p, C.c_void_p).value, ld.value)
+
+
+class Ensemble:
+    """Many independent cases advanced together by the mixed step, one
+    launch per stage for all of them (wolfd2gpu_ens_*).  Each case is an
+    ordinary Solver, set up and loaded as usual; store_fields on a member
+    reads that case's state.  The members must stay open while the
+    ensemble is used."""
+
+    def __init__(self, solvers: Sequence["Solver"], threads: int = 0, sweeps_per_barrier: int = 0,
+                 graph: bool = True):
+        self.L = lib()
+        self.solvers = list(solvers)
+        hs = (C.c_void_p * len(self.solvers))(*[s.h for s in self.solvers])
+        h = C.c_void_p()
+        rc = self.L.wolfd2gpu_ens_create(C.byref(h), hs, len(self.solvers), threads, sweeps_per_barrier)
+        if rc:
+            raise W2Error(rc, "ensemble creation failed (see stderr)")
+        self.h = h
+        self.L.wolfd2gpu_ens_graph(self.h, 1 if graph else 0)
+
+    def _check(self, rc: int) -> None:
+        if rc:
+            raise W2Error(rc, self.L.wolfd2gpu_ens_error(self.h).decode())
+
+    def step(self, params: Sequence[RunParams], nsteps: int = 1, refine_sweeps: int = 0) -> List[List[tuple]]:
+        """nsteps mixed steps of every case; returns per case the records
+        (nQLiter, nSorConv, dif, divmax) of each step."""
+        n = len(self.solvers)
+        if len(params) != n:
+            raise ValueError("one RunParams per case")
+        pr = (Params * n)(*[Params.of(p, precision=PREC_MIXED, refine_sweeps=refine_sweeps) for p in params])
+        st = (StepStat * max(n * nsteps, 1))()
+        self._check(self.L.wolfd2gpu_ens_step(self.h, pr, nsteps, st))
+        return [[(x.nQLiter, x.nSorConv, tuple(x.dif), x.divmax) for x in st[k * nsteps:(k + 1) * nsteps]]
+                for k in range(n)]
+
+    def info(self) -> dict:
+        bm, bp, ms, nl = C.c_int(), C.c_int(), C.c_double(), C.c_longlong()
+        self._check(self.L.wolfd2gpu_ens_info(self.h, C.byref(bm), C.byref(bp), C.byref(ms), C.byref(nl)))
+        return {"blocks_momentum": bm.value, "blocks_poisson": bp.value, "last_ms": ms.value,
+                "launches": nl.value}
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.L.wolfd2gpu_ens_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
