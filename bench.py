@@ -478,15 +478,196 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+ENSEMBLE = {"count": 256, "seed": 2024}
+
+
+def ensemble_members(args):
+    return deck.ensemble_cases(args.ens_count, seed=args.ens_seed, solver="rb_sor")
+
+
+def ensemble_config(args, members, inner, graph):
+    ns = [m.n for m in members]
+    return {
+        "workload": (f"batched ensemble: {len(members)} lid-driven cavities, N cells per side drawn "
+                     f"uniformly from {{64, 96, ..., 512}} and Re log-uniform in [100, 5000] "
+                     f"(numpy default_rng({args.ens_seed})), dt = 0.5 h capped at the viscous number "
+                     f"dt/(h^2 Re) = 0.25 where the reference scheme is unstable, seeded 16x16-mode "
+                     f"streamfunction perturbation per case, rb_sor, mixed step ({inner} FP32 sweeps per "
+                     f"refinement pass), one launch per stage for all cases"
+                     f"{', step captured in a CUDA graph' if graph else ''}"),
+        "cases": len(members), "cells": int(sum(m.case.cells for m in members)),
+        "n_min": min(ns), "n_max": max(ns), "dt_capped_cases": sum(1 for m in members if m.dt < m.dt_named),
+        "layout": "each cavity at spacing 1/64 with side N/64 and deck Re = Re/side: the exact similarity "
+                  "image of the unit cavity (unit-stencil Poisson rows)",
+        "precision": "mixed", "graph": graph,
+        "l2": "not flushed: the ensemble's fields alone exceed L2 (129 MB) many times over",
+    }
+
+
+def run_ensemble(args):
+    """The batched ensemble (config 3): every case advanced together by one
+    launch per stage; cases are spread over ranks by work, no exchange."""
+    import torch
+    import torch.distributed as dist
+    from wolfd2_gb300 import replicas
+    from wolfd2_gb300.gpu import Ensemble, Solver
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    members = ensemble_members(args)
+    mine = replicas.partition_work([m.case.cells for m in members], world, rank)
+    graph = not args.no_graph
+    inner = args.refine_sweeps or 64
+    solvers, ics = [], []
+    for i in mine:
+        c = members[i].case
+        s = Solver.for_case(c, tuned=False)
+        ic = deck.perturbation_ic(c, args.seed + i)
+        s.load_fields(*ic)
+        solvers.append(s)
+        ics.append(ic)
+    ens = Ensemble(solvers, graph=graph)
+    prm = [members[i].case.params for i in mine]
+    cells = sum(members[i].case.cells for i in mine)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+
+    if args.warmup:
+        ens.step(prm, args.warmup, refine_sweeps=inner)
+    # per-stage split of the same kind of steps (direct launches, events)
+    ens.graph(False)
+    ens.profile(True)
+    prof_hist = ens.step(prm, 1, refine_sweeps=inner)
+    stages = ens.profile_read()
+    ens.profile(False)
+    ens.graph(graph)
+    barrier()
+    l0 = ens.info()["launches"]
+    with ClockSampler(local) as clk:
+        barrier()
+        t0 = time.perf_counter()
+        hist = ens.step(prm, args.steps, refine_sweeps=inner)
+        barrier()
+        wall = time.perf_counter() - t0
+    info = ens.info()
+    t_dev = info["last_ms"] / 1e3
+    launches = info["launches"] - l0
+    # end to end: every step loads all fields from pinned host buffers,
+    # steps, and reads them back
+    pinned, hosts = [], []
+    for s in solvers:
+        ts = [torch.empty((s.mny + 1, s.mnx + 1), dtype=torch.float64, pin_memory=True) for _ in range(3)]
+        hs = [t.numpy().T for t in ts]
+        for h, f in zip(hs, s.store_fields()):
+            h[...] = f
+        pinned.append(ts)
+        hosts.append(hs)
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    field_bytes = sum((s.mnx + 1) * (s.mny + 1) * 8 for s in solvers)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for s, hs in zip(solvers, hosts):
+            s.load_fields(*hs)
+        ens.step(prm, 1, refine_sweeps=inner)
+        for s, hs in zip(solvers, hosts):
+            s.store_fields(out=hs)
+    barrier()
+    t_e2e = time.perf_counter() - t0
+    tt = replicas.max_over_ranks((t_dev, t_e2e), device=dev)
+    t_max, t_e2e_max = tt
+    cells_all = sum(m.case.cells for m in members)
+    if rank != 0:
+        ens.close()
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+    # algorithmic bytes of the dominant stage (the Poisson launch) over its
+    # profiled step, summed over this rank's cases
+    ppe_ms, _ = stages["ke_ppe_mixed"]
+    ppe_bytes = sum(mixed_ppe_bytes(members[i].case.cells, h[0][1], inner)
+                    for i, h in zip(mine, prof_hist))
+    peak_gbs, peak_kind = peaks()
+    traffic_ratio = None
+    try:
+        traffic_ratio = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))[
+            "bytes_per_alg_byte"].get("ke_ppe_mixed")
+    except Exception:
+        traffic_ratio = None
+    achieved = ppe_bytes / (ppe_ms / 1e3) / 1e9 if ppe_ms > 0 else None
+    roof = {"bound": "hbm", "kernel": "ke_ppe_mixed", "achieved": achieved, "peak": peak_gbs,
+            "unit": "GB/s", "frac": achieved / peak_gbs if achieved else None,
+            "peak_kind": peak_kind,
+            "traffic": traffic_ratio * ppe_bytes if traffic_ratio else None,
+            "alg_bytes_per_launch": ppe_bytes, "avg_launch_ms": ppe_ms}
+    cpu = None
+    if not args.no_cpu_baseline:
+        # a bounded sample: one reference step of the first cases in draw
+        # order until about 15 s of host time
+        done, secs, how, kind = 0, 0.0, "", "port"
+        for i, m in enumerate(members):
+            r, kind, how = reference_runner(m.case, deck.perturbation_ic(m.case, args.seed + i))
+            t0 = time.perf_counter()
+            r.step(1)
+            secs += time.perf_counter() - t0
+            done += m.case.cells
+            if secs > 15.0:
+                break
+        cpu = {"value": done / secs, "unit": UNIT, "cores": 1, "kind": kind,
+               "sample": f"1 reference step of each of the first {i + 1} cases ({done} cells, {secs:.1f} s); {how}"}
+    nql = [h[0] for hh in hist for h in hh]
+    nsor = [h[1] for hh in hist for h in hh]
+    line = {
+        "metric": METRIC, "value": cells_all * args.steps / t_max, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
+        "steps_per_s": args.steps / t_max,
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
+        "dtype": "f32+f64", "data": "synthetic",
+        "config": ensemble_config(args, members, inner, graph),
+        "parallelism": f"cases partitioned by work over {world} ranks" if world > 1 else "single GPU",
+        "roofline": roof,
+        "e2e": {"value": cells_all * e2e_steps / t_e2e_max, "unit": UNIT,
+                "h2d_bytes_per_step": 3 * field_bytes, "d2h_bytes_per_step": 3 * field_bytes,
+                "steps": e2e_steps, "host_buffers": "pinned"},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+        "kernel_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in stages.items()},
+        "launch_blocks": {"momentum": info["blocks_momentum"], "poisson": info["blocks_poisson"]},
+        "iterations": {"nql_min": min(nql), "nql_max": max(nql), "nsor_min": min(nsor), "nsor_max": max(nsor)},
+        "divmax_max": max(h[3] for hh in hist for h in hh),
+        "wall_s": wall,
+    }
+    print(json.dumps(line), flush=True)
+    ens.close()
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["cavity", "channel"], default="cavity",
+    ap.add_argument("--workload", choices=["cavity", "channel", "ensemble"], default="cavity",
                     help="cavity: the lid-driven cavity (--n cells per side); channel: the "
-                         "4096x1024 plane channel with a profiled inflow")
+                         "4096x1024 plane channel with a profiled inflow; ensemble: 256 cavities "
+                         "of uneven size and Re advanced together")
+    ap.add_argument("--ens-count", type=int, default=ENSEMBLE["count"])
+    ap.add_argument("--ens-seed", type=int, default=ENSEMBLE["seed"])
+    ap.add_argument("--no-graph", action="store_true", help="ensemble: launch directly, no CUDA graph")
     ap.add_argument("--n", type=int, default=1024, help="cavity cells per side")
     ap.add_argument("--re", type=float, default=1000.0)
     ap.add_argument("--dt", type=float, default=2.5e-4)
@@ -507,6 +688,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "ensemble":
+        run_ensemble(args)
     else:
         run_ours(args)
 

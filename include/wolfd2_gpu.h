@@ -276,6 +276,13 @@ int wolfd2gpu_ens_step(w2_ens *ens, const w2_params *prm, int nsteps,
 int wolfd2gpu_ens_graph(w2_ens *ens, int enable);
 int wolfd2gpu_ens_info(w2_ens *ens, int *blocks_momentum, int *blocks_poisson,
                        double *last_ms, long long *launches);
+/* Per-stage device time of direct (not graph) ensemble launches, CUDA
+ * events on the ensemble's stream: enable (resets the sums), then read the
+ * total milliseconds and launch count of a stage. */
+enum { W2_ENS_COPY = 0, W2_ENS_MOMENTUM = 1, W2_ENS_BC = 2, W2_ENS_PPE = 3, W2_ENS_POST = 4,
+       W2_ENS_NSTAGES = 5 };
+int wolfd2gpu_ens_profile(w2_ens *ens, int enable);
+int wolfd2gpu_ens_profile_read(w2_ens *ens, int stage, double *total_ms, long long *count);
 const char *wolfd2gpu_ens_error(w2_ens *ens);
 int wolfd2gpu_ens_destroy(w2_ens *ens);
 

@@ -23,3 +23,16 @@ def test_ensemble_workload_draws():
         assert abs(c.params.dk / side - x.dt) <= 1e-15
         assert x.dt <= x.dt_named == 0.5 / x.n
         assert x.dt / (x.re / x.n ** 2) <= 0.25 * (1 + 1e-12)
+
+
+def test_partition_work_covers_and_balances():
+    from wolfd2_gb300 import replicas
+    m = deck.ensemble_cases(256, seed=2024)
+    w = [x.case.cells for x in m]
+    for world in (1, 2, 3, 8):
+        parts = [replicas.partition_work(w, world, r) for r in range(world)]
+        owned = sorted(i for p in parts for i in p)
+        assert owned == list(range(len(w)))
+        loads = [sum(w[i] for i in p) for p in parts]
+        # largest-first greedy: every rank within one largest case of the mean
+        assert max(loads) - min(loads) <= max(w)

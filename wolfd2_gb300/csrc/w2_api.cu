@@ -1418,6 +1418,13 @@ struct w2_ens {
   long long launches = 0;
   double last_ms = 0.0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // per-stage event timing of direct (not graph) launches
+  bool prof_on = false;
+  struct Rec { int kind; cudaEvent_t a, b; };
+  std::vector<Rec> prof_pending;
+  std::vector<cudaEvent_t> ev_pool;
+  double prof_ms[W2_ENS_NSTAGES] = {};
+  long long prof_n[W2_ENS_NSTAGES] = {};
   char err[512] = {0};
 };
 
@@ -1516,19 +1523,78 @@ const void *ens_ppe_kernel(int K) {
   return nullptr;
 }
 
-int ens_launch_step(w2_ens *e, const EnsLaunch &Lm, const EnsLaunch &Lp, const EnsLaunch &L1) {
+cudaEvent_t ens_event(w2_ens *e) {
+  if (!e->ev_pool.empty()) {
+    cudaEvent_t v = e->ev_pool.back();
+    e->ev_pool.pop_back();
+    return v;
+  }
+  cudaEvent_t v = nullptr;
+  cudaEventCreate(&v);
+  return v;
+}
+
+// Events around one stage launch when profiling (never inside a capture).
+struct EnsProf {
+  w2_ens *e;
+  int kind;
+  cudaEvent_t a = nullptr;
+  EnsProf(w2_ens *e_, int k, bool capturing) : e(e_), kind(k) {
+    if (e->prof_on && !capturing) {
+      a = ens_event(e);
+      cudaEventRecord(a, e->st);
+    }
+  }
+  ~EnsProf() {
+    if (!a) return;
+    cudaEvent_t b = ens_event(e);
+    cudaEventRecord(b, e->st);
+    e->prof_pending.push_back({kind, a, b});
+  }
+};
+
+void ens_prof_collect(w2_ens *e) {
+  for (auto &r : e->prof_pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+      e->prof_ms[r.kind] += ms;
+      e->prof_n[r.kind] += 1;
+    }
+    e->ev_pool.push_back(r.a);
+    e->ev_pool.push_back(r.b);
+  }
+  e->prof_pending.clear();
+}
+
+int ens_launch_step(w2_ens *e, const EnsLaunch &Lm, const EnsLaunch &Lp, const EnsLaunch &L1,
+                    bool capturing = false) {
   EnsLaunch am = Lm, ap = Lp;
   void *argm[] = {&am}, *argp[] = {&ap};
-  ke_copy_mixed<<<e->blocks_m, e->threads, 0, e->st>>>(Lm);
-  ECK(cudaGetLastError());
-  ECK(cudaLaunchCooperativeKernel((const void *)ke_naux32, dim3(e->blocks_m), dim3(e->threads), argm,
-                                  e->smem_m, e->st));
-  ke_bc<<<e->n, e->threads, 0, e->st>>>(L1);
-  ECK(cudaGetLastError());
-  ECK(cudaLaunchCooperativeKernel(ens_ppe_kernel(e->K), dim3(e->blocks_p), dim3(e->threads), argp,
-                                  e->smem_p, e->st));
-  ECK(cudaLaunchCooperativeKernel((const void *)ke_step_post, dim3(e->blocks_m), dim3(e->threads), argm,
-                                  0, e->st));
+  {
+    EnsProf pr(e, W2_ENS_COPY, capturing);
+    ke_copy_mixed<<<e->blocks_m, e->threads, 0, e->st>>>(Lm);
+    ECK(cudaGetLastError());
+  }
+  {
+    EnsProf pr(e, W2_ENS_MOMENTUM, capturing);
+    ECK(cudaLaunchCooperativeKernel((const void *)ke_naux32, dim3(e->blocks_m), dim3(e->threads), argm,
+                                    e->smem_m, e->st));
+  }
+  {
+    EnsProf pr(e, W2_ENS_BC, capturing);
+    ke_bc<<<e->n, e->threads, 0, e->st>>>(L1);
+    ECK(cudaGetLastError());
+  }
+  {
+    EnsProf pr(e, W2_ENS_PPE, capturing);
+    ECK(cudaLaunchCooperativeKernel(ens_ppe_kernel(e->K), dim3(e->blocks_p), dim3(e->threads), argp,
+                                    e->smem_p, e->st));
+  }
+  {
+    EnsProf pr(e, W2_ENS_POST, capturing);
+    ECK(cudaLaunchCooperativeKernel((const void *)ke_step_post, dim3(e->blocks_m), dim3(e->threads), argm,
+                                    0, e->st));
+  }
   ke_tick<<<1, 1, 0, e->st>>>(e->d_step);
   ECK(cudaGetLastError());
   e->launches += 6;
@@ -1732,7 +1798,7 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
     cudaGraph_t g = nullptr;
     ECK(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
     const long long l0 = e->launches;
-    int rc = ens_launch_step(e, Lm, Lp, L1);
+    int rc = ens_launch_step(e, Lm, Lp, L1, true);
     e->launches = l0;
     cudaError_t ce = cudaStreamEndCapture(e->st, &g);
     if (rc) return rc;
@@ -1758,6 +1824,7 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e->ev0, e->ev1);
   e->last_ms = ms;
+  ens_prof_collect(e);
   int rc = W2_OK, diverged = -1;
   for (int k = 0; k < n; ++k) {
     w2_ctx *c = e->cs[k];
@@ -1800,6 +1867,23 @@ int wolfd2gpu_ens_info(w2_ens *e, int *blocks_momentum, int *blocks_poisson, dou
   return W2_OK;
 }
 
+int wolfd2gpu_ens_profile(w2_ens *e, int enable) {
+  if (!e) return W2_E_ARG;
+  e->prof_on = enable != 0;
+  for (int k = 0; k < W2_ENS_NSTAGES; ++k) {
+    e->prof_ms[k] = 0.0;
+    e->prof_n[k] = 0;
+  }
+  return W2_OK;
+}
+
+int wolfd2gpu_ens_profile_read(w2_ens *e, int stage, double *total_ms, long long *count) {
+  if (!e || stage < 0 || stage >= W2_ENS_NSTAGES) return W2_E_ARG;
+  if (total_ms) *total_ms = e->prof_ms[stage];
+  if (count) *count = e->prof_n[stage];
+  return W2_OK;
+}
+
 const char *wolfd2gpu_ens_error(w2_ens *e) { return e ? e->err : "null ensemble"; }
 
 int wolfd2gpu_ens_destroy(w2_ens *e) {
@@ -1807,6 +1891,11 @@ int wolfd2gpu_ens_destroy(w2_ens *e) {
   if (e->st) cudaStreamSynchronize(e->st);
   if (e->gexec) cudaGraphExecDestroy(e->gexec);
   for (void *p : e->allocs) cudaFree(p);
+  for (auto &r : e->prof_pending) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (cudaEvent_t v : e->ev_pool) cudaEventDestroy(v);
   if (e->ev0) cudaEventDestroy(e->ev0);
   if (e->ev1) cudaEventDestroy(e->ev1);
   if (e->st) cudaStreamDestroy(e->st);

@@ -125,6 +125,8 @@ def lib():
     L.wolfd2gpu_ens_error.argtypes = [vp]
     L.wolfd2gpu_ens_error.restype = C.c_char_p
     L.wolfd2gpu_ens_destroy.argtypes = [vp]
+    L.wolfd2gpu_ens_profile.argtypes = [vp, C.c_int]
+    L.wolfd2gpu_ens_profile_read.argtypes = [vp, C.c_int, _dp, C.POINTER(C.c_longlong)]
     _lib = L
     return L
 
@@ -389,6 +391,24 @@ class Ensemble:
         self._check(self.L.wolfd2gpu_ens_step(self.h, pr, nsteps, st))
         return [[(x.nQLiter, x.nSorConv, tuple(x.dif), x.divmax) for x in st[k * nsteps:(k + 1) * nsteps]]
                 for k in range(n)]
+
+    STAGES = ("ke_copy_mixed", "ke_naux32", "ke_bc", "ke_ppe_mixed", "ke_step_post")
+
+    def profile(self, enable: bool = True) -> None:
+        """Per-stage CUDA-event timing of direct launches (graph replay is
+        not profiled); enabling resets the sums."""
+        self._check(self.L.wolfd2gpu_ens_profile(self.h, 1 if enable else 0))
+
+    def profile_read(self) -> dict:
+        out = {}
+        for k, name in enumerate(self.STAGES):
+            ms, n = C.c_double(), C.c_longlong()
+            self._check(self.L.wolfd2gpu_ens_profile_read(self.h, k, C.byref(ms), C.byref(n)))
+            out[name] = (ms.value, n.value)
+        return out
+
+    def graph(self, enable: bool) -> None:
+        self.L.wolfd2gpu_ens_graph(self.h, 1 if enable else 0)
 
     def info(self) -> dict:
         bm, bp, ms, nl = C.c_int(), C.c_int(), C.c_double(), C.c_longlong()

@@ -8,7 +8,7 @@ max-over-ranks reduction of the elapsed time.
 """
 from __future__ import annotations
 
-from typing import List, Tuple
+from typing import List, Sequence, Tuple
 
 
 def partition(n_items: int, world: int, rank: int) -> List[int]:
@@ -18,6 +18,20 @@ def partition(n_items: int, world: int, rank: int) -> List[int]:
     lo = rank * base + min(rank, extra)
     hi = lo + base + (1 if rank < extra else 0)
     return list(range(lo, hi))
+
+
+def partition_work(weights: Sequence[float], world: int, rank: int) -> List[int]:
+    """Item indices owned by `rank` when items of uneven work (an ensemble's
+    cases, weighted by cells) are spread over `world` ranks: largest first to
+    the least-loaded rank (ties to the lower rank), returned in item order.
+    Every rank computes the same assignment."""
+    load = [0.0] * world
+    owner = [0] * len(weights)
+    for i in sorted(range(len(weights)), key=lambda i: (-weights[i], i)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        owner[i] = r
+        load[r] += weights[i]
+    return [i for i in range(len(weights)) if owner[i] == rank]
 
 
 def max_over_ranks(values: Tuple[float, ...], device=None) -> Tuple[float, ...]:
