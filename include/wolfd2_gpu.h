@@ -177,6 +177,14 @@ int wolfd2gpu_cold_start(w2_ctx *ctx, const w2_params *prm, int *nSorConv);
 int wolfd2gpu_step(w2_ctx *ctx, const w2_params *prm, int nsteps,
                    w2_stepstat *stats);
 
+/* CUDA graphs for wolfd2gpu_step (on by default; no reference counterpart).
+ * When enabled, a call's launch sequence is captured once and replayed by
+ * later calls that bake in the same launches: same starting time level,
+ * step count, parameters, and device state (any re-tuning, metric upload or
+ * face profile makes a new capture).  Profiling (wolfd2gpu_profile) uses
+ * direct launches. */
+int wolfd2gpu_set_graph(w2_ctx *ctx, int enable);
+
 /* Synchronise the context stream; returns the first pending error. */
 int wolfd2gpu_sync(w2_ctx *ctx);
 

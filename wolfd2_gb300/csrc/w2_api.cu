@@ -62,6 +62,15 @@ struct w2_ctx {
   // single-precision momentum state (mixed path), made on first use
   bool f32_alloc = false, f32_metrics_ok = false;
   float *F32[4] = {};  // un, vn, us, vs
+  // step records of wolfd2gpu_step (persistent, so captured graphs keep their address)
+  StepOut *d_outs = nullptr;
+  int outs_cap = 0;
+  // CUDA graphs of whole wolfd2gpu_step calls, keyed by everything their
+  // launches bake in (starting level, step count, parameters, device view,
+  // tile plans, launch shapes)
+  bool graph_on = true;
+  struct Graph { cudaGraphExec_t exec; long long launches; };
+  std::vector<std::pair<std::string, Graph>> graphs;
   // per-position face values (wolfd2gpu_set_face_profile)
   int *prof_idx = nullptr;   // device table, -1 = region constant
   double *prof = nullptr;    // device values, kMaxProfiles x prof_len
@@ -868,6 +877,7 @@ int wolfd2gpu_destroy(w2_ctx *c) {
     cudaEventDestroy(r.b);
   }
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+  for (auto &g : c->graphs) cudaGraphExecDestroy(g.second.exec);
   for (void *p : c->allocs) cudaFree(p);
   if (c->h_out) cudaFreeHost(c->h_out);
   if (c->st) cudaStreamDestroy(c->st);
@@ -1279,14 +1289,14 @@ int wolfd2gpu_cold_start(w2_ctx *c, const w2_params *prm, int *nSorConv) {
   return W2_OK;
 }
 
-int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *stats) {
-  int rc = ready(c);
-  if (rc) return rc;
-  if ((rc = check_params(c, prm))) return rc;
-  if (nsteps < 0) return fail(c, W2_E_ARG, "nsteps < 0");
-  std::vector<StepOut> outs((size_t)std::max(nsteps, 1));
-  StepOut *d_outs = nullptr;
-  CK(cudaMallocAsync((void **)&d_outs, sizeof(StepOut) * std::max(nsteps, 1), c->st));
+}  // extern "C"
+
+namespace {
+
+// The launches of `nsteps` whole steps from time level c->cur (advanced as
+// they are issued), step s writing outs[s].
+int issue_steps(w2_ctx *c, const w2_params *prm, int nsteps, StepOut *d_outs) {
+  int rc = W2_OK;
   const int gb = grid_blocks(c);
   for (int s = 0; s < nsteps && rc == W2_OK; ++s) {
     const int a = c->cur, b = 1 - a;
@@ -1296,8 +1306,6 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
     Dev d = c->dev;
     const bool mixed = prm->precision == W2_PREC_MIXED;
     if (mixed) {
-      if ((rc = ensure_f32(c))) break;
-      d = c->dev;
       float *un32 = c->F32[0], *vn32 = c->F32[1], *us32 = c->F32[2], *vs32 = c->F32[3];
       {
         ProfScope ps(c, W2_K_COPY);
@@ -1366,9 +1374,93 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
     }
     c->cur = b;
   }
+  return rc;
+}
+
+// Cache key of a captured step sequence: the bytes of everything its
+// launches bake in.
+std::string graph_key(const w2_ctx *c, const w2_params *prm, int nsteps) {
+  std::string k;
+  auto add = [&](const void *p, size_t n) { k.append((const char *)p, n); };
+  const int head[] = {c->cur, nsteps, c->threads, c->blocks_per_sm, c->mixed_K, c->mixed_blocks,
+                      c->tiled_blocks, c->tiled_threads, c->use_tiled, (int)c->tiled_ok, (int)c->mixed_ok};
+  add(head, sizeof(head));
+  add(prm, sizeof(*prm));
+  add(&c->dev, sizeof(c->dev));
+  add(&c->mg, sizeof(c->mg));
+  add(&c->tg, sizeof(c->tg));
+  const size_t sm[] = {c->mixed_smem, c->tiled_smem};
+  add(sm, sizeof(sm));
+  return k;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wolfd2gpu_set_graph(w2_ctx *c, int enable) {
+  if (!c) return W2_E_ARG;
+  c->graph_on = enable != 0;
+  return W2_OK;
+}
+
+int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *stats) {
+  int rc = ready(c);
+  if (rc) return rc;
+  if ((rc = check_params(c, prm))) return rc;
+  if (nsteps < 0) return fail(c, W2_E_ARG, "nsteps < 0");
+  if (prm->precision == W2_PREC_MIXED && (rc = ensure_f32(c))) return rc;
+  std::vector<StepOut> outs((size_t)std::max(nsteps, 1));
+  if (nsteps > c->outs_cap) {
+    if (c->d_outs) {
+      CK(cudaStreamSynchronize(c->st));
+      cudaFree(c->d_outs);
+      c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void *)c->d_outs), c->allocs.end());
+      for (auto &g : c->graphs) cudaGraphExecDestroy(g.second.exec);
+      c->graphs.clear();
+    }
+    if (!(c->d_outs = dalloc<StepOut>(c, nsteps))) return fail(c, W2_E_CUDA, "out of device memory (step records)");
+    c->outs_cap = nsteps;
+  }
+  StepOut *d_outs = c->d_outs;
+  if (nsteps > 0 && c->graph_on && !c->prof_on) {
+    const int cur0 = c->cur;
+    const std::string key = graph_key(c, prm, nsteps);
+    const w2_ctx::Graph *hit = nullptr;
+    for (auto &g : c->graphs)
+      if (g.first == key) hit = &g.second;
+    if (!hit) {
+      if (c->graphs.size() >= 8) {
+        for (auto &g : c->graphs) cudaGraphExecDestroy(g.second.exec);
+        c->graphs.clear();
+      }
+      const long long l0 = c->launches;
+      cudaGraph_t g = nullptr;
+      CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+      rc = issue_steps(c, prm, nsteps, d_outs);
+      cudaError_t ce = cudaStreamEndCapture(c->st, &g);
+      c->cur = cur0;
+      if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      if (ce != cudaSuccess) return fail(c, W2_E_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+      cudaGraphExec_t exec = nullptr;
+      ce = cudaGraphInstantiate(&exec, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) return fail(c, W2_E_CUDA, "graph instantiation: %s", cudaGetErrorString(ce));
+      c->graphs.push_back({key, {exec, c->launches - l0}});
+      c->launches = l0;
+      hit = &c->graphs.back().second;
+    }
+    CK(cudaGraphLaunch(hit->exec, c->st));
+    c->launches += hit->launches;
+    c->cur = (cur0 + nsteps) & 1;
+  } else {
+    rc = issue_steps(c, prm, nsteps, d_outs);
+  }
   if (nsteps > 0)
     cudaMemcpyAsync(outs.data(), d_outs, sizeof(StepOut) * nsteps, cudaMemcpyDeviceToHost, c->st);
-  cudaFreeAsync(d_outs, c->st);
   int rs = check_sync(c);
   if (rc == W2_OK) rc = rs;
   int diverged_at = -1;

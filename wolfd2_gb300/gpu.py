@@ -114,6 +114,7 @@ def lib():
     L.wolfd2gpu_stream.argtypes = [vp]
     L.wolfd2gpu_stream.restype = C.c_void_p
     L.wolfd2gpu_profile.argtypes = [vp, C.c_int]
+    L.wolfd2gpu_set_graph.argtypes = [vp, C.c_int]
     L.wolfd2gpu_chain_stats.argtypes = [vp, _ip, _ip]
     L.wolfd2gpu_ppe_rbsor_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                               C.c_double, C.c_double, C.c_double] + [vp] * 9 + [_ip, vp]
@@ -332,7 +333,14 @@ class Solver:
         return int(self.L.wolfd2gpu_stream(self.h) or 0)
 
     def profile(self, enable: bool = True) -> None:
+        """Per-kernel CUDA-event timing (steps then launch directly, not
+        from a captured graph)."""
         self._check(self.L.wolfd2gpu_profile(self.h, 1 if enable else 0))
+
+    def graph(self, enable: bool = True) -> None:
+        """Replay wolfd2gpu_step's launch sequences from captured CUDA graphs
+        (the library default)."""
+        self._check(self.L.wolfd2gpu_set_graph(self.h, 1 if enable else 0))
 
     def profile_read(self, kind: int):
         ms, n = C.c_double(), C.c_longlong()
