@@ -185,6 +185,29 @@ int wolfd2gpu_step(w2_ctx *ctx, const w2_params *prm, int nsteps,
  * direct launches. */
 int wolfd2gpu_set_graph(w2_ctx *ctx, int enable);
 
+/* ---- Adjoint (no reference counterpart) --------------------------------
+ * wolfd2gpu_step_counts: nsteps plain steps with the iteration counts fixed
+ * per step (counts[2s] Q-L iterations, counts[2s+1] SOR sweeps; no
+ * convergence test stops them earlier): the map whose derivative the adjoint
+ * gives, for finite-difference checks.
+ * wolfd2gpu_adjoint: from the loaded fields, runs nsteps plain FP64 steps
+ * (checkpointing the fields every `every` steps and recording each step's
+ * counts into counts[2*nsteps] when not NULL), evaluates
+ *   J = 0.5 * weight * (sum of u^2 over i=1..nx, j=2..ny
+ *                       + sum of v^2 over i=2..nx, j=1..ny)
+ * at the final step, and returns dJ/du, dJ/dv, dJ/dp of the initial fields
+ * ((0:mnx,0:mny) host arrays, any of them may be NULL) and dJ/d(face values)
+ * of the face profile (ireg, jreg, face, var) in gprof[0..nprof) (positions
+ * as wolfd2gpu_set_face_profile).  The derivative is that of the step with
+ * the recorded counts held fixed; the context ends at the final state.
+ * Limits: ppe_solver rb_sor (5), Cartesian grids, no Filter, no outlets. */
+int wolfd2gpu_step_counts(w2_ctx *ctx, const w2_params *prm, int nsteps,
+                          const int *counts, w2_stepstat *stats);
+int wolfd2gpu_adjoint(w2_ctx *ctx, const w2_params *prm, int nsteps, int every,
+                      double weight, double *J, double *gu, double *gv, double *gp,
+                      int ireg, int jreg, int face, int var, double *gprof, int nprof,
+                      int *counts);
+
 /* Synchronise the context stream; returns the first pending error. */
 int wolfd2gpu_sync(w2_ctx *ctx);
 

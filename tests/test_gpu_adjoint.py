@@ -1,0 +1,112 @@
+"""Adjoint of the plain FP64 step against central finite differences of the
+same map (each step's iteration counts held at the recorded values), along
+seeded random directions in the initial u, v, p and the lid profile.
+
+The directions perturb the interior unknowns only: the wall-face velocities
+are exactly 0, where the upwind selector of their momentum rows
+(cj = 2 yeu u on a Cartesian grid) sits on its branch boundary, so a central
+difference there straddles a kink of the map (and the boundary programs
+overwrite those values anyway)."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from wolfd2_gb300 import deck
+from wolfd2_gb300.gpu import Solver
+
+pytestmark = pytest.mark.gpu
+
+NORTH, VAR_U = 4, 1
+
+
+def _setup(n, re, dt, mqiter, msorit, seed=11):
+    case = deck.cavity(n, re, dt, solver="rb_sor")
+    prm = dataclasses.replace(case.params, mqiter=mqiter, msorit=msorit)
+    u, v, p = deck.perturbation_ic(case, seed)
+    rng = np.random.default_rng(seed)
+    p = p + 1e-3 * rng.normal(size=p.shape)
+    p = np.asfortranarray(p)
+    lid = np.ones(case.nx + 2) + 0.05 * np.sin(np.linspace(0, 3, case.nx + 2))
+    return case, prm, (u, v, p), lid
+
+
+def _interior(case):
+    """Masks of the interior unknowns of u, v, p."""
+    nx, ny = case.nx, case.ny
+    mu = np.zeros((nx + 2, ny + 2), bool)
+    mv = np.zeros_like(mu)
+    mp = np.zeros_like(mu)
+    mu[2:nx, 2:ny + 1] = True
+    mv[2:nx + 1, 2:ny] = True
+    mp[2:nx + 1, 2:ny + 1] = True
+    return mu, mv, mp
+
+
+def _objective(case, u, v, w):
+    nx, ny = case.nx, case.ny
+    return 0.5 * w * (np.sum(u[1:nx + 1, 2:ny + 1] ** 2) + np.sum(v[2:nx + 1, 1:ny + 1] ** 2))
+
+
+def _forward(case, prm, fields, lid, counts, w):
+    s = Solver.for_case(case, tuned=False)
+    s.set_face_profile(1, 1, NORTH, VAR_U, lid)
+    s.load_fields(*fields)
+    s.step_counts(prm, counts)
+    u, v, _ = s.store_fields()
+    s.close()
+    return _objective(case, u, v, w)
+
+
+@pytest.mark.parametrize("nsteps,every,mqiter,msorit", [(1, 1, 1, 2), (1, 1, 3, 30), (3, 2, 4, 40), (5, 2, 20, 60)])
+def test_adjoint_matches_finite_differences(nsteps, every, mqiter, msorit):
+    """Along random interior directions (u0, v0, p0 and the lid profile
+    together), the adjoint's directional derivative equals the central
+    difference of the frozen-count map."""
+    case, prm, fields, lid = _setup(32, 200.0, 0.004, mqiter, msorit)
+    w = (1.0 / 32) ** 2
+    s = Solver.for_case(case, tuned=False)
+    s.set_face_profile(1, 1, NORTH, VAR_U, lid)
+    s.load_fields(*fields)
+    J, gu, gv, gp, gl, counts = s.adjoint(prm, nsteps, every, w, profile=(1, 1, NORTH, VAR_U),
+                                          nprof=case.nx + 2)
+    s.close()
+    assert J == pytest.approx(_forward(case, prm, fields, lid, counts, w), rel=1e-14)
+    rng = np.random.default_rng(7)
+    eps = 1e-6
+    masks = _interior(case)
+    for _ in range(3):
+        du, dv, dp = (np.asfortranarray(np.where(m, rng.normal(size=f.shape), 0.0)) for f, m in zip(fields, masks))
+        dl = rng.normal(size=lid.shape)
+        plus = [np.asfortranarray(f + eps * d) for f, d in zip(fields, (du, dv, dp))]
+        minus = [np.asfortranarray(f - eps * d) for f, d in zip(fields, (du, dv, dp))]
+        fd = (_forward(case, prm, plus, lid + eps * dl, counts, w) -
+              _forward(case, prm, minus, lid - eps * dl, counts, w)) / (2 * eps)
+        ad = np.sum(gu * du) + np.sum(gv * dv) + np.sum(gp * dp) + np.sum(gl * dl)
+        assert ad == pytest.approx(fd, rel=1e-5, abs=100 * np.finfo(float).eps * abs(J) / eps), (ad, fd)
+
+
+def test_lid_gradient_reaches_interior_after_two_steps():
+    """The lid's ghost row enters the flow through the next step's momentum
+    rows: one step leaves J independent of it, two do not; the adjoint's lid
+    gradient equals finite differences per lid position."""
+    case, prm, fields, lid = _setup(16, 100.0, 0.004, 6, 20)
+    w = (1.0 / 16) ** 2
+    res = {}
+    for nsteps in (1, 2):
+        s = Solver.for_case(case, tuned=False)
+        s.set_face_profile(1, 1, NORTH, VAR_U, lid)
+        s.load_fields(*fields)
+        res[nsteps] = s.adjoint(prm, nsteps, 1, w, profile=(1, 1, NORTH, VAR_U), nprof=case.nx + 2)
+        s.close()
+    assert not np.any(res[1][4])
+    J, gu, gv, gp, gl, counts = res[2]
+    assert np.any(gl)
+    eps = 1e-6
+    for i in (2, case.nx // 2, case.nx):
+        dl = np.zeros_like(lid)
+        dl[i] = 1.0
+        fd = (_forward(case, prm, fields, lid + eps * dl, counts, w) -
+              _forward(case, prm, fields, lid - eps * dl, counts, w)) / (2 * eps)
+        # a central difference resolves J only to about its rounding over 2 eps
+        assert gl[i] == pytest.approx(fd, rel=1e-5, abs=100 * np.finfo(float).eps * abs(J) / eps), (i, gl[i], fd)

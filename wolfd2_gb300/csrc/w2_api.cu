@@ -13,6 +13,7 @@
 #include <string>
 #include <vector>
 
+#include "w2_adjoint.cuh"
 #include "w2_ensemble.cuh"
 
 using namespace w2;
@@ -71,6 +72,11 @@ struct w2_ctx {
   bool graph_on = true;
   struct Graph { cudaGraphExec_t exec; long long launches; };
   std::vector<std::pair<std::string, Graph>> graphs;
+  // adjoint work state (made on first use): the transposed chains and the
+  // saved split-1 rows and solutions
+  bool adj_alloc = false;
+  Chain adj_tx{}, adj_ty{};
+  double *adj_rows[8] = {};
   // per-position face values (wolfd2gpu_set_face_profile)
   int *prof_idx = nullptr;   // device table, -1 = region constant
   double *prof = nullptr;    // device values, kMaxProfiles x prof_len
@@ -1992,6 +1998,555 @@ int wolfd2gpu_ens_destroy(w2_ens *e) {
   if (e->ev1) cudaEventDestroy(e->ev1);
   if (e->st) cudaStreamDestroy(e->st);
   delete e;
+  return W2_OK;
+}
+
+}  // extern "C"
+
+// ============================================================================
+// Adjoint of the plain FP64 step (kernels in w2_adjoint.cuh)
+// ============================================================================
+
+namespace {
+
+// A boundary program as a list of assignments (see AdjBCList).
+struct BCProg {
+  std::vector<int> stage{0}, tgt, src, nsrc, prof;
+  std::vector<double> coef, pcoef;
+  size_t nf = 0;
+  int ld = 0;
+  int code(int f, int i, int j) const { return (int)((size_t)f * nf + (size_t)i + (size_t)j * ld); }
+  void op(int t, std::initializer_list<std::pair<int, double>> srcs, int pf = -1, double pc = 0.0) {
+    tgt.push_back(t);
+    int q = 0;
+    for (auto &sc : srcs) {
+      src.push_back(sc.first);
+      coef.push_back(sc.second);
+      ++q;
+    }
+    for (; q < kAdjSrc; ++q) {
+      src.push_back(0);
+      coef.push_back(0.0);
+    }
+    nsrc.push_back((int)srcs.size());
+    prof.push_back(pf);
+    pcoef.push_back(pc);
+  }
+  void end_stage() {
+    if ((int)tgt.size() > stage.back()) stage.push_back((int)tgt.size());
+  }
+};
+
+enum { FU = 0, FV = 1, FP = 2 };
+
+// Index into the face-value table of (region, face, var) at pos, or -1.
+int prof_slot(const w2_ctx *c, int ir, int jr, int face, int var, int pos) {
+  if (c->prof_host.empty()) return -1;
+  const int key = ((ir - 1) + (jr - 1) * c->mgri + (face - 1) * c->mgri * c->mgrj) * 2 + (var - 1);
+  const int off = c->prof_host[key];
+  return off < 0 ? -1 : off + pos;
+}
+
+// VelBoundCond (bound_cond.f:511-847) replayed as assignments, in the order
+// of w2_bc.cuh vel_bound_cond_block.
+void emit_vel_bc(const w2_ctx *c, BCProg &g) {
+  const int mgri = c->mgri, mgrj = c->mgrj;
+  auto B = [&](int ir, int jr, int s) { return c->tab_brd[(ir - 1) + (jr - 1) * mgri + (s - 1) * mgri * mgrj]; };
+  auto BT = [&](int ir, int jr, int s) { return c->tab_btype[(ir - 1) + (jr - 1) * mgri + (s - 1) * mgri * mgrj]; };
+  auto U = [&](int i, int j) { return g.code(FU, i, j); };
+  auto V = [&](int i, int j) { return g.code(FV, i, j); };
+  for (int jr = 1; jr <= c->nrj; ++jr)
+    for (int ir = 1; ir <= c->nri; ++ir) {
+      const int iW = B(ir, jr, 1), iE = B(ir, jr, 2), jS = B(ir, jr, 3), jN = B(ir, jr, 4);
+      switch (BT(ir, jr, 1)) {
+        case W2_BM_WALL1:
+          for (int j = jS; j <= jN; ++j) g.op(U(iW, j), {});
+          g.end_stage();
+          for (int j = jS + 1; j <= jN; ++j) g.op(V(iW, j), {{V(iW + 1, j), -1.0}}, prof_slot(c, ir, jr, 1, 2, j), 2.0);
+          g.end_stage();
+          break;
+        case W2_BM_WALL2:
+          for (int j = jS; j <= jN; ++j) g.op(U(iW, j), {});
+          g.end_stage();
+          for (int j = jS + 1; j <= jN; ++j) g.op(V(iW, j), {{V(iW + 1, j), 1.0}});
+          g.end_stage();
+          break;
+        case W2_BM_INLET:
+          for (int j = jS; j <= jN; ++j) g.op(U(iW, j), {}, prof_slot(c, ir, jr, 1, 1, j), 1.0);
+          g.end_stage();
+          for (int j = jS + 1; j <= jN; ++j) g.op(V(iW, j), {{V(iW + 1, j), -1.0}}, prof_slot(c, ir, jr, 1, 2, j), 2.0);
+          g.end_stage();
+          break;
+        case W2_BM_OUTLT1:
+          for (int j = jS; j <= jN; ++j) g.op(U(iW - 1, j), {{U(iW, j), 1.0}});
+          g.end_stage();
+          for (int j = jS + 1; j <= jN; ++j) g.op(V(iW, j), {{V(iW + 1, j), -1.0}});
+          g.end_stage();
+          break;
+        case W2_BM_OUTLT2:
+          for (int j = jS + 1; j <= jN; ++j)
+            g.op(U(iW, j), {{U(iW + 1, j), 1.0}, {V(iW + 1, j), 1.0}, {V(iW + 1, j - 1), -1.0}});
+          g.end_stage();
+          for (int j = jS + 1; j <= jN; ++j) {
+            g.op(V(iW, j), {{V(iW, j - 1), -1.0}, {V(iW + 1, j), 5.0}, {V(iW + 1, j - 1), -5.0},
+                            {U(iW + 1, j), 8.0}, {U(iW, j), -8.0}});
+            g.end_stage();
+          }
+          break;
+        default: break;
+      }
+      switch (BT(ir, jr, 2)) {
+        case W2_BM_WALL1:
+          for (int j = jS; j <= jN; ++j) g.op(U(iE, j), {});
+          g.end_stage();
+          for (int j = jS + 1; j <= jN; ++j) g.op(V(iE + 1, j), {{V(iE, j), -1.0}}, prof_slot(c, ir, jr, 2, 2, j), 2.0);
+          g.end_stage();
+          break;
+        case W2_BM_WALL2:
+          for (int j = jS; j <= jN; ++j) g.op(U(iE, j), {});
+          g.end_stage();
+          for (int j = jS + 1; j <= jN; ++j) g.op(V(iE + 1, j), {{V(iE, j), 1.0}});
+          g.end_stage();
+          break;
+        case W2_BM_INLET:
+          for (int j = jS; j <= jN; ++j) g.op(U(iE, j), {}, prof_slot(c, ir, jr, 2, 1, j), 1.0);
+          g.end_stage();
+          for (int j = jS + 1; j <= jN; ++j) g.op(V(iE + 1, j), {{V(iE, j), -1.0}}, prof_slot(c, ir, jr, 2, 2, j), 2.0);
+          g.end_stage();
+          break;
+        case W2_BM_OUTLT1:
+          for (int j = jS; j <= jN; ++j) g.op(U(iE + 1, j), {{U(iE, j), 1.0}});
+          g.end_stage();
+          for (int j = jS + 1; j <= jN; ++j) g.op(V(iE + 1, j), {{V(iE, j), -1.0}});
+          g.end_stage();
+          break;
+        case W2_BM_OUTLT2:
+          for (int j = jS + 1; j <= jN; ++j)
+            g.op(U(iE, j), {{U(iE - 1, j), 1.0}, {V(iE, j), -1.0}, {V(iE, j - 1), 1.0}});
+          g.end_stage();
+          for (int j = jS + 1; j <= jN - 1; ++j) {
+            g.op(V(iE + 1, j), {{V(iE + 1, j - 1), 1.0}, {V(iE, j - 1), 3.0}, {V(iE, j), -3.0},
+                                {U(iE, j), -4.0}, {U(iE - 1, j), 4.0}});
+            g.end_stage();
+          }
+          break;
+        default: break;
+      }
+      switch (BT(ir, jr, 3)) {
+        case W2_BM_WALL1:
+          for (int i = iW + 1; i <= iE; ++i) g.op(U(i, jS), {{U(i, jS + 1), -1.0}}, prof_slot(c, ir, jr, 3, 1, i), 2.0);
+          g.end_stage();
+          for (int i = iW; i <= iE; ++i) g.op(V(i, jS), {});
+          g.end_stage();
+          break;
+        case W2_BM_WALL2:
+          for (int i = iW + 1; i <= iE; ++i) g.op(U(i, jS), {{U(i, jS + 1), 1.0}});
+          g.end_stage();
+          for (int i = iW; i <= iE; ++i) g.op(V(i, jS), {});
+          g.end_stage();
+          break;
+        case W2_BM_INLET:
+          for (int i = iW + 1; i <= iE; ++i) g.op(U(i, jS), {{U(i, jS + 1), -1.0}}, prof_slot(c, ir, jr, 3, 1, i), 2.0);
+          g.end_stage();
+          for (int i = iW; i <= iE; ++i) g.op(V(i, jS), {}, prof_slot(c, ir, jr, 3, 2, i), 1.0);
+          g.end_stage();
+          break;
+        case W2_BM_OUTLT1:
+          for (int i = iW + 1; i <= iE; ++i) g.op(U(i, jS), {{U(i, jS + 1), -1.0}});
+          g.end_stage();
+          for (int i = iW; i <= iE; ++i) g.op(V(i, jS), {{V(i, jS), 1.0}});
+          g.end_stage();
+          break;
+        case W2_BM_OUTLT2:
+          for (int i = iW + 1; i <= iE; ++i)
+            g.op(V(i, jS), {{V(i, jS + 1), 1.0}, {U(i, jS + 1), 1.0}, {U(i - 1, jS + 1), -1.0}});
+          g.end_stage();
+          for (int i = iW + 1; i <= iE - 1; ++i) {
+            g.op(U(i, jS), {{U(i - 1, jS), 1.0}, {U(i - 1, jS + 1), 3.0}, {U(i, jS + 1), -3.0},
+                            {V(i, jS + 1), -4.0}, {V(i, jS), 4.0}});
+            g.end_stage();
+          }
+          break;
+        default: break;
+      }
+      switch (BT(ir, jr, 4)) {
+        case W2_BM_WALL1:
+          for (int i = iW + 1; i <= iE; ++i) g.op(U(i, jN + 1), {{U(i, jN), -1.0}}, prof_slot(c, ir, jr, 4, 1, i), 2.0);
+          g.end_stage();
+          for (int i = iW; i <= iE; ++i) g.op(V(i, jN), {});
+          g.end_stage();
+          break;
+        case W2_BM_WALL2:
+          for (int i = iW + 1; i <= iE; ++i) g.op(U(i, jN + 1), {{U(i, jN), 1.0}});
+          g.end_stage();
+          for (int i = iW; i <= iE; ++i) g.op(V(i, jN), {});
+          g.end_stage();
+          break;
+        case W2_BM_INLET:
+          for (int i = iW + 1; i <= iE; ++i) g.op(U(i, jN + 1), {{U(i, jN), -1.0}}, prof_slot(c, ir, jr, 4, 1, i), 2.0);
+          g.end_stage();
+          for (int i = iW; i <= iE; ++i) g.op(V(i, jN), {}, prof_slot(c, ir, jr, 4, 2, i), 1.0);
+          g.end_stage();
+          break;
+        case W2_BM_OUTLT1:
+          for (int i = iW + 1; i <= iE; ++i) g.op(U(i, jN + 1), {{U(i, jN), -1.0}});
+          g.end_stage();
+          for (int i = iW; i <= iE; ++i) g.op(V(i, jN + 1), {{V(i, jN), 1.0}});
+          g.end_stage();
+          break;
+        case W2_BM_OUTLT2:
+          for (int i = iW; i <= iE; ++i)
+            g.op(V(i, jN), {{V(i, jN - 1), 1.0}, {U(i, jN), -1.0}, {U(i - 1, jN), 1.0}});
+          g.end_stage();
+          for (int i = iW + 1; i <= iE - 1; ++i) {
+            g.op(U(i, jN + 1), {{U(i - 1, jN + 1), 1.0}, {U(i - 1, jN), 3.0}, {U(i, jN), -3.0},
+                                {V(i, jN), -4.0}, {V(i, jN - 1), 4.0}});
+            g.end_stage();
+          }
+          break;
+        default: break;
+      }
+    }
+}
+
+// PresBoundCond (bound_cond.f:853-1024), in the order of pres_bound_cond_block.
+void emit_pres_bc(const w2_ctx *c, BCProg &g) {
+  const int mgri = c->mgri, mgrj = c->mgrj;
+  auto B = [&](int ir, int jr, int s) { return c->tab_brd[(ir - 1) + (jr - 1) * mgri + (s - 1) * mgri * mgrj]; };
+  auto RT = [&](int ir, int jr) { return c->tab_rtype[(ir - 1) + (jr - 1) * mgri]; };
+  auto BT = [&](int ir, int jr, int s) { return c->tab_btype[(ir - 1) + (jr - 1) * mgri + (s - 1) * mgri * mgrj]; };
+  auto P = [&](int i, int j) { return g.code(FP, i, j); };
+  auto wall = [](int t) { return t == W2_BM_WALL1 || t == W2_BM_WALL2 || t == W2_BM_INLET; };
+  auto outl = [](int t) { return t == W2_BM_OUTLT1 || t == W2_BM_OUTLT2; };
+  for (int jr = 1; jr <= c->nrj; ++jr)
+    for (int ir = 1; ir <= c->nri; ++ir) {
+      const int iW = B(ir, jr, 1), iE = B(ir, jr, 2), jS = B(ir, jr, 3), jN = B(ir, jr, 4);
+      if (RT(ir, jr) == W2_RM_BLOCKG) {
+        for (int j = jS + 1; j <= jN; ++j)
+          for (int i = iW + 1; i <= iE; ++i) g.op(P(i, j), {});
+        g.end_stage();
+        for (int j = jS + 1; j <= jN; ++j) g.op(P(iW + 1, j), {{P(iW, j), 1.0}});
+        g.end_stage();
+        for (int j = jS + 1; j <= jN; ++j) g.op(P(iE, j), {{P(iE + 1, j), 1.0}});
+        g.end_stage();
+        for (int i = iW + 1; i <= iE; ++i) g.op(P(i, jS + 1), {{P(i, jS), 1.0}});
+        g.end_stage();
+        for (int i = iW + 1; i <= iE; ++i) g.op(P(i, jN), {{P(i, jN + 1), 1.0}});
+        g.end_stage();
+        continue;
+      }
+      int t = BT(ir, jr, 1);
+      if (wall(t) || outl(t)) {
+        for (int j = jS + 1; j <= jN; ++j) g.op(P(iW, j), {{P(iW + 1, j), wall(t) ? 1.0 : -1.0}});
+        g.end_stage();
+      }
+      t = BT(ir, jr, 2);
+      if (wall(t) || outl(t)) {
+        for (int j = jS + 1; j <= jN; ++j) g.op(P(iE + 1, j), {{P(iE, j), wall(t) ? 1.0 : -1.0}});
+        g.end_stage();
+      }
+      t = BT(ir, jr, 3);
+      if (wall(t) || outl(t)) {
+        for (int i = iW + 1; i <= iE; ++i) g.op(P(i, jS), {{P(i, jS + 1), wall(t) ? 1.0 : -1.0}});
+        g.end_stage();
+      }
+      t = BT(ir, jr, 4);
+      if (wall(t) || outl(t)) {
+        for (int i = iW + 1; i <= iE; ++i) g.op(P(i, jN + 1), {{P(i, jN), wall(t) ? 1.0 : -1.0}});
+        g.end_stage();
+      }
+    }
+}
+
+// A BCProg on the device for k_adj_bc; buffers recorded in `mem`.
+int upload_bc(w2_ctx *c, const BCProg &g, AdjBCList &L, std::vector<void *> &mem) {
+  auto up = [&](const void *h, size_t bytes) -> void * {
+    void *p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(bytes, 8)) != cudaSuccess) return nullptr;
+    mem.push_back(p);
+    if (h && bytes && cudaMemcpy(p, h, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+    return p;
+  };
+  const size_t n = g.tgt.size();
+  L.nstages = (int)g.stage.size() - 1;
+  L.nf = g.nf;
+  L.stage = (const int *)up(g.stage.data(), g.stage.size() * sizeof(int));
+  L.tgt = (const int *)up(g.tgt.data(), n * sizeof(int));
+  L.src = (const int *)up(g.src.data(), g.src.size() * sizeof(int));
+  L.nsrc = (const int *)up(g.nsrc.data(), n * sizeof(int));
+  L.prof = (const int *)up(g.prof.data(), n * sizeof(int));
+  L.coef = (const double *)up(g.coef.data(), g.coef.size() * sizeof(double));
+  L.pcoef = (const double *)up(g.pcoef.data(), n * sizeof(double));
+  L.tmp = (double *)up(nullptr, n * sizeof(double));
+  if (!L.stage || !L.tgt || !L.src || !L.nsrc || !L.prof || !L.coef || !L.pcoef || !L.tmp)
+    return fail(c, W2_E_CUDA, "out of device memory (boundary adjoint)");
+  return W2_OK;
+}
+
+// Parameters of step s with its counts frozen: exactly m Q-L iterations and
+// n sweeps (no convergence test can stop them earlier).
+w2_params frozen(const w2_params *prm, int m, int n) {
+  w2_params q = *prm;
+  q.mqiter = m;
+  q.qtol = -1.0;
+  q.msorit = n;
+  q.sortol = -1.0;
+  return q;
+}
+
+int adj_check(w2_ctx *c, const w2_params *prm) {
+  int rc = ready(c);
+  if (rc) return rc;
+  if ((rc = check_params(c, prm))) return rc;
+  if (prm->precision != W2_PREC_FP64) return fail(c, W2_E_UNSUPPORTED, "the adjoint runs the plain FP64 step");
+  if (prm->npsolver != 5 || !prm->lcartes)
+    return fail(c, W2_E_UNSUPPORTED, "the adjoint supports ppe_solver rb_sor (5) on Cartesian grids");
+  if (prm->nfiltu == 1 || prm->nfiltv == 1) return fail(c, W2_E_UNSUPPORTED, "the adjoint does not cover Filter");
+  if (c->dev.has_outflow) return fail(c, W2_E_UNSUPPORTED, "the adjoint does not cover VelOutflowBCs (outlets)");
+  return W2_OK;
+}
+
+int adj_alloc(w2_ctx *c) {
+  if (c->adj_alloc) return W2_OK;
+  const int nX = c->nx * (c->ny - 1), nY = (c->nx - 1) * c->ny;
+  int rc;
+  if ((rc = make_chain(c, c->adj_tx, nX, true)) || (rc = make_chain(c, c->adj_ty, nY, true))) return rc;
+  for (int k = 0; k < 8; ++k)
+    if (!(c->adj_rows[k] = dalloc<double>(c, (size_t)(k < 4 ? nX : nY) + kMaxSeg)))
+      return fail(c, W2_E_CUDA, "out of device memory (adjoint rows)");
+  const int wmax = (int)walk_stage_bytes(sizeof(double), kMaxThreads);
+  if (cudaFuncSetAttribute((const void *)k_adj_iter, cudaFuncAttributeMaxDynamicSharedMemorySize, wmax) !=
+      cudaSuccess)
+    return fail(c, W2_E_CUDA, "shared memory attribute (adjoint)");
+  c->adj_alloc = true;
+  return W2_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wolfd2gpu_step_counts(w2_ctx *c, const w2_params *prm, int nsteps, const int *counts, w2_stepstat *stats) {
+  int rc = ready(c);
+  if (rc) return rc;
+  if ((rc = check_params(c, prm))) return rc;
+  if (nsteps < 0 || (nsteps > 0 && !counts)) return fail(c, W2_E_ARG, "counts: 2 per step");
+  const bool g = c->graph_on;
+  c->graph_on = false;
+  for (int s = 0; s < nsteps && rc == W2_OK; ++s) {
+    const w2_params q = frozen(prm, counts[2 * s], counts[2 * s + 1]);
+    w2_stepstat st;
+    rc = wolfd2gpu_step(c, &q, 1, &st);
+    if (stats) stats[s] = st;
+  }
+  c->graph_on = g;
+  return rc;
+}
+
+int wolfd2gpu_adjoint(w2_ctx *c, const w2_params *prm, int nsteps, int every, double weight, double *J,
+                      double *gu, double *gv, double *gp, int ireg, int jreg, int face, int var,
+                      double *gprof, int nprof, int *counts) {
+  int rc = adj_check(c, prm);
+  if (rc) return rc;
+  if (nsteps < 1 || every < 1) return fail(c, W2_E_ARG, "nsteps and checkpoint interval must be >= 1");
+  if ((rc = adj_alloc(c))) return rc;
+  std::vector<void *> mem;
+  struct Free {
+    std::vector<void *> &m;
+    ~Free() {
+      for (void *p : m) cudaFree(p);
+    }
+  } free_mem{mem};
+  auto field = [&]() -> double * {
+    void *p = nullptr;
+    if (cudaMalloc(&p, c->nf * sizeof(double)) != cudaSuccess) return nullptr;
+    cudaMemset(p, 0, c->nf * sizeof(double));
+    mem.push_back(p);
+    return (double *)p;
+  };
+  const size_t fb = c->nf * sizeof(double);
+  const int nck = (nsteps + every - 1) / every, mq = prm->mqiter;
+  std::vector<double *> ck(3 * nck), seg(3 * every), tape(2 * (mq + 1));
+  double *lu = field(), *lv = field(), *lp = field(), *lb = field(), *lun = field(), *lvn = field();
+  double *fin[3] = {field(), field(), field()};
+  for (auto &x : ck) x = field();
+  for (auto &x : seg) x = field();
+  for (auto &x : tape) x = field();
+  double *dJ = nullptr, *lprof = nullptr;
+  const size_t nprof_all = c->prof_host.empty() ? 1 : (size_t)16 * c->prof_len;
+  if (cudaMalloc(&dJ, sizeof(double)) != cudaSuccess) return fail(c, W2_E_CUDA, "out of device memory");
+  mem.push_back(dJ);
+  if (cudaMalloc(&lprof, nprof_all * sizeof(double)) != cudaSuccess) return fail(c, W2_E_CUDA, "out of device memory");
+  mem.push_back(lprof);
+  for (double *x : {lu, lv, lp, lb, lun, lvn, fin[0], fin[1], fin[2]})
+    if (!x) return fail(c, W2_E_CUDA, "out of device memory (adjoint fields)");
+  for (auto *v : {&ck, &seg, &tape})
+    for (double *x : *v)
+      if (!x) return fail(c, W2_E_CUDA, "out of device memory (adjoint checkpoints)");
+  // boundary programs as assignment lists
+  BCProg gv_, gp_;
+  gv_.nf = gp_.nf = c->nf;
+  gv_.ld = gp_.ld = c->ld;
+  emit_vel_bc(c, gv_);
+  emit_pres_bc(c, gp_);
+  AdjBCList Lv{}, Lp{};
+  if ((rc = upload_bc(c, gv_, Lv, mem)) || (rc = upload_bc(c, gp_, Lp, mem))) return rc;
+  CK(cudaDeviceSynchronize());
+  const bool graph0 = c->graph_on;
+  c->graph_on = false;
+  struct Restore {
+    w2_ctx *c;
+    bool g;
+    ~Restore() { c->graph_on = g; }
+  } restore{c, graph0};
+  StepOut so;
+  std::vector<int> cnt(2 * nsteps);
+  auto copy3 = [&](double *du, double *dv, double *dp, const double *su, const double *sv, const double *sp) -> int {
+    CK(cudaMemcpyAsync(du, su, fb, cudaMemcpyDeviceToDevice, c->st));
+    CK(cudaMemcpyAsync(dv, sv, fb, cudaMemcpyDeviceToDevice, c->st));
+    CK(cudaMemcpyAsync(dp, sp, fb, cudaMemcpyDeviceToDevice, c->st));
+    return W2_OK;
+  };
+  // ---- forward: checkpoints and the iteration counts of every step
+  if (nsteps > c->outs_cap) {
+    if (c->d_outs) {
+      cudaFree(c->d_outs);
+      c->allocs.erase(std::remove(c->allocs.begin(), c->allocs.end(), (void *)c->d_outs), c->allocs.end());
+      for (auto &gr : c->graphs) cudaGraphExecDestroy(gr.second.exec);
+      c->graphs.clear();
+    }
+    if (!(c->d_outs = dalloc<StepOut>(c, nsteps))) return fail(c, W2_E_CUDA, "out of device memory (step records)");
+    c->outs_cap = nsteps;
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    if (s % every == 0) {
+      const int k = s / every;
+      if ((rc = copy3(ck[3 * k], ck[3 * k + 1], ck[3 * k + 2], c->U[c->cur], c->V[c->cur], c->P[c->cur]))) return rc;
+    }
+    if ((rc = issue_steps(c, prm, 1, c->d_outs))) return rc;
+    CK(cudaMemcpyAsync(&so, c->d_outs, sizeof(StepOut), cudaMemcpyDeviceToHost, c->st));
+    if ((rc = check_sync(c))) return rc;
+    cnt[2 * s] = so.nql > 0 ? so.nql : prm->mqiter;
+    cnt[2 * s + 1] = so.nsor;
+    const double mx = std::max(std::max(so.dif[0], so.dif[1]), so.dif[2]);
+    if (!(mx <= 1.0e12)) return fail(c, W2_E_DIVERGED, "forward run diverged at step %d", s + 1);
+  }
+  if ((rc = copy3(fin[0], fin[1], fin[2], c->U[c->cur], c->V[c->cur], c->P[c->cur]))) return rc;
+  // ---- objective and its gradient at the final step
+  Dev d = c->dev;
+  const int gb = grid_blocks(c);
+  CK(cudaMemsetAsync(dJ, 0, sizeof(double), c->st));
+  CK(cudaMemsetAsync(lp, 0, fb, c->st));
+  CK(cudaMemsetAsync(lprof, 0, nprof_all * sizeof(double), c->st));
+  k_adj_objective<<<gb, c->threads, 0, c->st>>>(d, weight, fin[0], fin[1], lu, lv, dJ);
+  CK(cudaGetLastError());
+  // ---- backward, segment by segment
+  const int nX = c->nx * (c->ny - 1);
+  (void)nX;
+  Chain tx = c->adj_tx, ty = c->adj_ty;
+  tx.L = ty.L = d.seg;
+  tx.nseg = d.f64.x1.nseg;
+  ty.nseg = d.f64.y1.nseg;
+  const int bl_iter = pick_blocks(c, (const void *)k_adj_iter, (long)c->nx * c->ny, naux_smem(c));
+  const int bl_ppe = pick_blocks(c, (const void *)k_adj_ppe, (long)c->nx * c->ny);
+  const int bl_naux = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny, naux_smem(c));
+  double *lprof_arg = c->prof_host.empty() ? nullptr : lprof;
+  auto adj_bc = [&](AdjBCList &L) -> int {
+    c->launches++;
+    k_adj_bc<<<1, 512, 0, c->st>>>(L, lu, lv, lp, lprof_arg);
+    CK(cudaGetLastError());
+    return W2_OK;
+  };
+  for (int k = nck - 1; k >= 0; --k) {
+    const int s0 = k * every, s1 = std::min(nsteps, s0 + every);
+    // recompute the segment's step inputs
+    if ((rc = copy3(c->U[c->cur], c->V[c->cur], c->P[c->cur], ck[3 * k], ck[3 * k + 1], ck[3 * k + 2]))) return rc;
+    for (int s = s0; s < s1; ++s) {
+      const int q = s - s0;
+      if ((rc = copy3(seg[3 * q], seg[3 * q + 1], seg[3 * q + 2], c->U[c->cur], c->V[c->cur], c->P[c->cur]))) return rc;
+      if (s + 1 < s1) {
+        const w2_params f = frozen(prm, cnt[2 * s], cnt[2 * s + 1]);
+        if ((rc = issue_steps(c, &f, 1, c->d_outs))) return rc;
+      }
+    }
+    for (int s = s1 - 1; s >= s0; --s) {
+      const int q = s - s0, m = cnt[2 * s], ns = cnt[2 * s + 1];
+      double *un = seg[3 * q], *vn = seg[3 * q + 1];
+      double dk = prm->dk;
+      // tail: PresBC, Project, VelBC, PresBC, VelBC, PresBC reversed
+      if ((rc = adj_bc(Lp)) || (rc = adj_bc(Lv)) || (rc = adj_bc(Lp)) || (rc = adj_bc(Lv))) return rc;
+      c->launches++;
+      k_adj_project<<<gb, c->threads, 0, c->st>>>(d, dk, lu, lv, lp);
+      CK(cudaGetLastError());
+      if ((rc = adj_bc(Lp))) return rc;
+      // Ppe (fixed sweep count) and Divergence
+      {
+        double sr = prm->sorrel;
+        int nsv = ns;
+        void *args[] = {&d, &nsv, &sr, &dk, &lp, &lb, &lu, &lv};
+        if ((rc = coop(c, (const void *)k_adj_ppe, bl_ppe, args))) return rc;
+      }
+      // the boundary rows before Ppe: VelBC then PresBC, reversed
+      if ((rc = adj_bc(Lp)) || (rc = adj_bc(Lv))) return rc;
+      // Q-L iterations: tape the iterates, then transpose them in reverse
+      CK(cudaMemcpyAsync(tape[0], un, fb, cudaMemcpyDeviceToDevice, c->st));
+      CK(cudaMemcpyAsync(tape[1], vn, fb, cudaMemcpyDeviceToDevice, c->st));
+      for (int it = 1; it <= m; ++it) {
+        double *us = tape[2 * it], *vs = tape[2 * it + 1];
+        CK(cudaMemcpyAsync(us, tape[2 * it - 2], fb, cudaMemcpyDeviceToDevice, c->st));
+        CK(cudaMemcpyAsync(vs, tape[2 * it - 1], fb, cudaMemcpyDeviceToDevice, c->st));
+        int one = 1;
+        double re = prm->re, qt = -1.0;
+        StepOut *o = c->d_out;
+        void *args[] = {&d, &one, &dk, &re, &qt, &un, &vn, &us, &vs, &o};
+        if ((rc = coop(c, (const void *)k_naux, bl_naux, args, naux_smem(c)))) return rc;
+      }
+      CK(cudaMemsetAsync(lun, 0, fb, c->st));
+      CK(cudaMemsetAsync(lvn, 0, fb, c->st));
+      for (int it = m; it >= 1; --it) {
+        AdjIter A{};
+        A.us = tape[2 * it - 2];
+        A.vs = tape[2 * it - 1];
+        A.un = un;
+        A.vn = vn;
+        A.lus = lu;
+        A.lvs = lv;
+        A.lun = lun;
+        A.lvn = lvn;
+        A.sa1x = c->adj_rows[0]; A.sa2x = c->adj_rows[1]; A.sa3x = c->adj_rows[2]; A.sx1 = c->adj_rows[3];
+        A.sa1y = c->adj_rows[4]; A.sa2y = c->adj_rows[5]; A.sa3y = c->adj_rows[6]; A.sy1 = c->adj_rows[7];
+        A.tx = tx;
+        A.ty = ty;
+        A.dk = dk;
+        A.re = prm->re;
+        void *args[] = {&d, &A};
+        if ((rc = coop(c, (const void *)k_adj_iter, bl_iter, args, naux_smem(c)))) return rc;
+      }
+      // us = un, vs = vn at the start of the step: the level-n adjoint
+      k_axpy2<<<gb, c->threads, 0, c->st>>>(d, lu, lun, lv, lvn);
+      c->launches++;
+      CK(cudaGetLastError());
+    }
+  }
+  if ((rc = check_sync(c))) return rc;
+  // outputs
+  CK(cudaMemcpy(J, dJ, sizeof(double), cudaMemcpyDeviceToHost));
+  if (gu && (rc = copy_out(c, gu, lu))) return rc;
+  if (gv && (rc = copy_out(c, gv, lv))) return rc;
+  if (gp && (rc = copy_out(c, gp, lp))) return rc;
+  if (gprof && nprof > 0) {
+    const int slot = prof_slot(c, ireg, jreg, face, var, 0);
+    std::vector<double> h(nprof, 0.0);
+    if (slot >= 0) {
+      const int n = std::min(nprof, c->prof_len);
+      CK(cudaMemcpy(h.data(), lprof + slot, n * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    memcpy(gprof, h.data(), nprof * sizeof(double));
+  }
+  if (counts) memcpy(counts, cnt.data(), cnt.size() * sizeof(int));
+  // leave the context at the final state of the run
+  if ((rc = copy3(c->U[c->cur], c->V[c->cur], c->P[c->cur], fin[0], fin[1], fin[2]))) return rc;
+  CK(cudaStreamSynchronize(c->st));
   return W2_OK;
 }
 

@@ -115,6 +115,9 @@ def lib():
     L.wolfd2gpu_stream.restype = C.c_void_p
     L.wolfd2gpu_profile.argtypes = [vp, C.c_int]
     L.wolfd2gpu_set_graph.argtypes = [vp, C.c_int]
+    L.wolfd2gpu_step_counts.argtypes = [vp, C.POINTER(Params), C.c_int, _ip, C.POINTER(StepStat)]
+    L.wolfd2gpu_adjoint.argtypes = [vp, C.POINTER(Params), C.c_int, C.c_int, C.c_double, _dp, _dp, _dp,
+                                    _dp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.c_int, _ip]
     L.wolfd2gpu_chain_stats.argtypes = [vp, _ip, _ip]
     L.wolfd2gpu_ppe_rbsor_noalloc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                               C.c_double, C.c_double, C.c_double] + [vp] * 9 + [_ip, vp]
@@ -324,6 +327,34 @@ class Solver:
         st = (StepStat * max(nsteps, 1))()
         self._check(self.L.wolfd2gpu_step(self.h, C.byref(pr), nsteps, st))
         return [(s.nQLiter, s.nSorConv, tuple(s.dif), s.divmax) for s in st[:nsteps]]
+
+    def step_counts(self, prm: RunParams, counts) -> List[tuple]:
+        """Plain steps with each step's (Q-L iterations, SOR sweeps) fixed."""
+        counts = np.ascontiguousarray(np.asarray(counts, dtype=np.int32).ravel())
+        n = counts.size // 2
+        pr = Params.of(prm)
+        st = (StepStat * max(n, 1))()
+        self._check(self.L.wolfd2gpu_step_counts(self.h, C.byref(pr), n, counts.ctypes.data_as(_ip), st))
+        return [(s.nQLiter, s.nSorConv, tuple(s.dif), s.divmax) for s in st[:n]]
+
+    def adjoint(self, prm: RunParams, nsteps: int, every: int = 20, weight: float = 1.0,
+                profile=None, nprof: int = 0):
+        """J = 0.5 * weight * sum(u^2 + v^2) over the momentum unknowns after
+        nsteps plain steps from the loaded fields, and its gradient with the
+        recorded iteration counts held fixed.  profile = (ireg, jreg, face,
+        var) selects the face profile whose gradient is returned.  Returns
+        (J, du, dv, dp, dprof, counts)."""
+        gu, gv, gp = self.field(), self.field(), self.field()
+        ir, jr, fc, vr = profile if profile else (0, 0, 0, 0)
+        npf = nprof if profile else 0
+        gprof = np.zeros(max(npf, 1))
+        counts = np.zeros(2 * nsteps, dtype=np.int32)
+        J = C.c_double()
+        pr = Params.of(prm)
+        self._check(self.L.wolfd2gpu_adjoint(self.h, C.byref(pr), nsteps, every, weight, C.byref(J), _p(gu),
+                                             _p(gv), _p(gp), ir, jr, fc, vr, gprof.ctypes.data_as(_dp), npf,
+                                             counts.ctypes.data_as(_ip)))
+        return J.value, gu, gv, gp, gprof[:npf], counts.reshape(nsteps, 2)
 
     def sync(self) -> None:
         self._check(self.L.wolfd2gpu_sync(self.h))
