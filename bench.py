@@ -487,6 +487,120 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+ADJOINT = {"n": 256, "re": 400.0, "dt": 2.0e-3, "steps": 400, "every": 20, "eps": 1.0e-6}
+
+
+def run_adjoint(args):
+    """Config 4: gradient of J = 0.5 h^2 sum(u^2 + v^2) at the final step
+    with respect to the initial u, v and the 256-point lid profile, by the
+    library's discrete adjoint (checkpoint and recompute), checked against
+    central finite differences of the same map along seeded directions."""
+    import torch
+    from wolfd2_gb300.gpu import Solver
+
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    n, nsteps = ADJOINT["n"], args.adj_steps
+    case = deck.cavity(n, ADJOINT["re"], ADJOINT["dt"], solver="rb_sor")
+    prm = case.params
+    u0, v0, p0 = deck.perturbation_ic(case, args.seed)
+    lid = np.ones(case.nx + 2)
+    w = (1.0 / n) ** 2
+    NORTH, VAR_U = 4, 1
+
+    def solver():
+        s = Solver.for_case(case, tuned=False)
+        s.set_face_profile(1, 1, NORTH, VAR_U, lid)
+        return s
+
+    s = solver()
+    s.load_fields(u0, v0, p0)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        J, gu, gv, gp, gl, counts = s.adjoint(prm, nsteps, ADJOINT["every"], w, profile=(1, 1, NORTH, VAR_U),
+                                              nprof=case.nx + 2)
+        t_adj = time.perf_counter() - t0
+    launches = s.launch_count()
+    # forward alone, the same steps (frozen counts), for the adjoint's cost ratio
+    s.load_fields(u0, v0, p0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.step_counts(prm, counts)
+    t_fwd = time.perf_counter() - t0
+
+    def objective(u, v):
+        nx, ny = case.nx, case.ny
+        return 0.5 * w * (np.sum(u[1:nx + 1, 2:ny + 1] ** 2) + np.sum(v[2:nx + 1, 1:ny + 1] ** 2))
+
+    def J_at(u, v, lidv):
+        s.set_face_profile(1, 1, NORTH, VAR_U, lidv)
+        s.load_fields(np.asfortranarray(u), np.asfortranarray(v), p0)
+        s.step_counts(prm, counts)
+        uu, vv, _ = s.store_fields()
+        return objective(uu, vv)
+
+    # seeded directions in the interior unknowns of u0, v0 and in the lid
+    rng = np.random.default_rng(args.seed + 1)
+    nx, ny = case.nx, case.ny
+    mu = np.zeros_like(u0, dtype=bool)
+    mv = np.zeros_like(mu)
+    mu[2:nx, 2:ny + 1] = True
+    mv[2:nx + 1, 2:ny] = True
+    eps = ADJOINT["eps"]
+    errs, pairs = [], []
+    t0 = time.perf_counter()
+    for _ in range(args.fd_dirs):
+        du = np.where(mu, rng.normal(size=u0.shape), 0.0)
+        dv = np.where(mv, rng.normal(size=v0.shape), 0.0)
+        dl = rng.normal(size=lid.shape)
+        fd = (J_at(u0 + eps * du, v0 + eps * dv, lid + eps * dl) -
+              J_at(u0 - eps * du, v0 - eps * dv, lid - eps * dl)) / (2 * eps)
+        ad = float(np.sum(gu * du) + np.sum(gv * dv) + np.sum(gl * dl))
+        pairs.append((ad, fd))
+        errs.append(abs(ad - fd) / max(abs(fd), 1e-300))
+    t_fd = time.perf_counter() - t0
+    s.close()
+    if rank != 0:
+        return
+    cells = case.cells
+    cpu = None
+    if not args.no_cpu_baseline:
+        cv, csec, cores, kind, how = cpu_step_sample(case, (u0, v0, p0), 1)
+        cpu = {"value": cv, "unit": UNIT, "cores": cores, "kind": kind,
+               "sample": f"1 forward reference step of the same {n}x{n} case ({csec:.1f} s); {how}; the reference "
+                         f"has no adjoint: one finite-difference gradient component costs two such {nsteps}-step runs"}
+    line = {
+        "metric": METRIC, "value": cells * nsteps / t_adj, "unit": UNIT, "n_gpus": 1,
+        "steps": nsteps, "warmup": 0, "ms_per_step": 1e3 * t_adj / nsteps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": (f"adjoint: lid-driven cavity {n}x{n}, Re={ADJOINT['re']:g}, dt={ADJOINT['dt']:g}, "
+                                f"{nsteps} steps from the seeded 16x16-mode perturbation (seed {args.seed}), rb_sor, "
+                                f"plain FP64; J = 0.5 h^2 sum(u^2+v^2) at the final step; gradient with respect to "
+                                f"the initial u, v, p and the {case.nx + 2}-value lid profile (256 moving-wall "
+                                f"positions), checkpoint every {ADJOINT['every']} steps, iteration counts of the "
+                                f"forward run held fixed"),
+                   "value_is": "cell-steps of the forward horizon per second of the whole gradient "
+                               "(forward with checkpoints + recompute + adjoint)"},
+        "gradient_s": t_adj, "forward_s": t_fwd, "adjoint_over_forward": t_adj / t_fwd,
+        "J": J, "fd_check": {"directions": args.fd_dirs, "eps": eps, "max_rel_err": max(errs) if errs else None,
+                             "median_rel_err": float(np.median(errs)) if errs else None,
+                             "pairs": pairs[:8], "seconds": t_fd},
+        "iterations": {"nql_min": int(counts[:, 0].min()), "nql_max": int(counts[:, 0].max()),
+                       "nsor_min": int(counts[:, 1].min()), "nsor_max": int(counts[:, 1].max())},
+        "lid_grad_norm": float(np.linalg.norm(gl)),
+        "e2e": {"value": cells * nsteps / t_adj, "unit": UNIT, "h2d_bytes_per_step": 3 * (nx + 2) * (ny + 2) * 8 / nsteps,
+                "d2h_bytes_per_step": 3 * (nx + 2) * (ny + 2) * 8 / nsteps,
+                "note": "the gradient call takes host fields in and returns host gradients; value already end to end"},
+        "roofline": None,
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+
+
 ENSEMBLE = {"count": 256, "seed": 2024}
 
 
@@ -670,13 +784,15 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["cavity", "channel", "ensemble"], default="cavity",
+    ap.add_argument("--workload", choices=["cavity", "channel", "ensemble", "adjoint"], default="cavity",
                     help="cavity: the lid-driven cavity (--n cells per side); channel: the "
                          "4096x1024 plane channel with a profiled inflow; ensemble: 256 cavities "
                          "of uneven size and Re advanced together")
     ap.add_argument("--ens-count", type=int, default=ENSEMBLE["count"])
     ap.add_argument("--ens-seed", type=int, default=ENSEMBLE["seed"])
     ap.add_argument("--no-graph", action="store_true", help="ensemble: launch directly, no CUDA graph")
+    ap.add_argument("--adj-steps", type=int, default=ADJOINT["steps"], help="adjoint: steps of the horizon")
+    ap.add_argument("--fd-dirs", type=int, default=4, help="adjoint: finite-difference directions checked")
     ap.add_argument("--n", type=int, default=1024, help="cavity cells per side")
     ap.add_argument("--re", type=float, default=1000.0)
     ap.add_argument("--dt", type=float, default=2.5e-4)
@@ -699,6 +815,8 @@ def main():
         run_reference(args)
     elif args.workload == "ensemble":
         run_ensemble(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
     else:
         run_ours(args)
 
