@@ -110,3 +110,60 @@ def test_lid_gradient_reaches_interior_after_two_steps():
               _forward(case, prm, fields, lid - eps * dl, counts, w)) / (2 * eps)
         # a central difference resolves J only to about its rounding over 2 eps
         assert gl[i] == pytest.approx(fd, rel=1e-5, abs=100 * np.finfo(float).eps * abs(J) / eps), (i, gl[i], fd)
+
+
+def test_adjoint_matches_reference_finite_differences():
+    """The GPU adjoint against central differences of the CPU reference
+    restatement (the oracle, bit-identical to the GPU forward), run step by
+    step with the same frozen counts."""
+    import oracle as O
+    case, prm, fields, lid = _setup(16, 100.0, 0.004, 6, 20)
+    case.regions.profiles[(1, 1, NORTH, VAR_U)] = lid
+    w = (1.0 / 16) ** 2
+    nsteps = 3
+    s = Solver.for_case(case, tuned=False)
+    s.load_fields(*fields)
+    J, gu, gv, gp, gl, counts = s.adjoint(prm, nsteps, 2, w, profile=(1, 1, NORTH, VAR_U), nprof=case.nx + 2)
+    s.close()
+
+    def ref_J(flds, lidv):
+        case.regions.profiles[(1, 1, NORTH, VAR_U)] = lidv
+        r = O.OracleRun(case, fields={"u": flds[0], "v": flds[1], "p": flds[2]}, cold_start=False)
+        for m, ns in counts:
+            r._ps = O.Oracle.params_struct(dataclasses.replace(prm, mqiter=int(m), qtol=-1.0,
+                                                               msorit=int(ns), sortol=-1.0))
+            r.step(1)
+        return _objective(case, r.f["u"], r.f["v"], w)
+
+    assert ref_J(fields, lid) == pytest.approx(J, rel=1e-13)
+    rng = np.random.default_rng(5)
+    eps = 1e-6
+    masks = _interior(case)
+    du, dv, dp = (np.where(m, rng.normal(size=f.shape), 0.0) for f, m in zip(fields, masks))
+    dl = rng.normal(size=lid.shape)
+    fd = (ref_J([f + eps * d for f, d in zip(fields, (du, dv, dp))], lid + eps * dl) -
+          ref_J([f - eps * d for f, d in zip(fields, (du, dv, dp))], lid - eps * dl)) / (2 * eps)
+    ad = np.sum(gu * du) + np.sum(gv * dv) + np.sum(gp * dp) + np.sum(gl * dl)
+    assert ad == pytest.approx(fd, rel=1e-5, abs=100 * np.finfo(float).eps * abs(J) / eps)
+
+
+def test_autograd_wrapper():
+    import torch
+    from wolfd2_gb300.autograd import KineticEnergy
+    case, prm, fields, lid = _setup(16, 100.0, 0.004, 6, 20)
+    w = (1.0 / 16) ** 2
+    s = Solver.for_case(case, tuned=False)
+    u0 = torch.tensor(np.ascontiguousarray(fields[0].T)).T.requires_grad_()
+    v0 = torch.tensor(np.ascontiguousarray(fields[1].T)).T.requires_grad_()
+    lt = torch.tensor(lid, requires_grad=True)
+    p0 = torch.tensor(np.ascontiguousarray(fields[2].T)).T
+    J = KineticEnergy.apply(u0, v0, lt, s, prm, 2, 1, w, p0)
+    J.backward()
+    s.load_fields(*fields)
+    s.set_face_profile(1, 1, NORTH, VAR_U, lid)
+    J2, gu, gv, _, gl, _ = s.adjoint(prm, 2, 1, w, profile=(1, 1, NORTH, VAR_U), nprof=case.nx + 2)
+    s.close()
+    # J and the gradients are sums of FP64 atomics: equal up to their order
+    assert float(J) == pytest.approx(J2, rel=1e-13)
+    for g, ref in ((u0.grad, gu), (v0.grad, gv), (lt.grad, gl)):
+        assert np.allclose(g.numpy(), ref, rtol=1e-11, atol=1e-12 * np.max(np.abs(ref)))
