@@ -200,7 +200,7 @@ int wolfd2gpu_set_graph(w2_ctx *ctx, int enable);
  * of the face profile (ireg, jreg, face, var) in gprof[0..nprof) (positions
  * as wolfd2gpu_set_face_profile).  The derivative is that of the step with
  * the recorded counts held fixed; the context ends at the final state.
- * Limits: ppe_solver rb_sor (5), Cartesian grids, no Filter, no outlets. */
+ * Limits: ppe_solver rb_sor (5), Cartesian grids, no Filter. */
 int wolfd2gpu_step_counts(w2_ctx *ctx, const w2_params *prm, int nsteps,
                           const int *counts, w2_stepstat *stats);
 int wolfd2gpu_adjoint(w2_ctx *ctx, const w2_params *prm, int nsteps, int every,

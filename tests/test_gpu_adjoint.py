@@ -167,3 +167,49 @@ def test_autograd_wrapper():
     assert float(J) == pytest.approx(J2, rel=1e-13)
     for g, ref in ((u0.grad, gu), (v0.grad, gv), (lt.grad, gl)):
         assert np.allclose(g.numpy(), ref, rtol=1e-11, atol=1e-12 * np.max(np.abs(ref)))
+
+
+@pytest.mark.parametrize("outlet", ["mc", "fd"])
+def test_channel_adjoint_inflow_profile(outlet):
+    """Channel with a per-row inflow profile and an outlet (VelOutflowBCs
+    inside every Q-L iteration): gradient with respect to the initial fields
+    and the inflow profile against central differences.  The start is the
+    flow after two steps: the initial field has v = 0 everywhere, where every
+    v-driven upwind selector sits on its branch point."""
+    WEST = 1
+    case = deck.channel_inflow(48, 16, 500.0, 0.004, seed=3, length=3.0, outlet=outlet)
+    prm = dataclasses.replace(case.params, mqiter=8, msorit=40)
+    s = Solver.for_case(case, tuned=False)
+    s.load_fields(*deck.channel_ic(case))
+    s.step(prm, 2)
+    fields = s.store_fields()
+    s.close()
+    prof = case.regions.profiles[(1, 1, WEST, VAR_U)].copy()
+    w = (1.0 / 16) ** 2
+    s = Solver.for_case(case, tuned=False)
+    s.load_fields(*fields)
+    J, gu, gv, gp, gl, counts = s.adjoint(prm, 3, 2, w, profile=(1, 1, WEST, VAR_U), nprof=case.ny + 2)
+    s.close()
+    assert np.any(gl)
+
+    def J_at(flds, pr):
+        s = Solver.for_case(case, tuned=False)
+        s.set_face_profile(1, 1, WEST, VAR_U, pr)
+        s.load_fields(*[np.asfortranarray(f) for f in flds])
+        s.step_counts(prm, counts)
+        u, v, _ = s.store_fields()
+        s.close()
+        return _objective(case, u, v, w)
+
+    assert J_at(fields, prof) == pytest.approx(J, rel=1e-13)
+    rng = np.random.default_rng(9)
+    eps = 1e-6
+    masks = _interior(case)
+    for _ in range(2):
+        du, dv, dp = (np.where(m, rng.normal(size=f.shape), 0.0) for f, m in zip(fields, masks))
+        dl = np.zeros_like(prof)
+        dl[2:case.ny + 1] = rng.normal(size=case.ny - 1)
+        fd = (J_at([f + eps * d for f, d in zip(fields, (du, dv, dp))], prof + eps * dl) -
+              J_at([f - eps * d for f, d in zip(fields, (du, dv, dp))], prof - eps * dl)) / (2 * eps)
+        ad = np.sum(gu * du) + np.sum(gv * dv) + np.sum(gp * dp) + np.sum(gl * dl)
+        assert ad == pytest.approx(fd, rel=1e-5, abs=100 * np.finfo(float).eps * abs(J) / eps), (ad, fd)

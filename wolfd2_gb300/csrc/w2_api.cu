@@ -2209,6 +2209,84 @@ void emit_vel_bc(const w2_ctx *c, BCProg &g) {
     }
 }
 
+// VelOutflowBCs (bound_cond.f:1656-1874), in the order of
+// vel_outflow_bcs_block: outlet faces only.
+void emit_outflow_bc(const w2_ctx *c, BCProg &g) {
+  const int mgri = c->mgri, mgrj = c->mgrj;
+  auto B = [&](int ir, int jr, int s) { return c->tab_brd[(ir - 1) + (jr - 1) * mgri + (s - 1) * mgri * mgrj]; };
+  auto BT = [&](int ir, int jr, int s) { return c->tab_btype[(ir - 1) + (jr - 1) * mgri + (s - 1) * mgri * mgrj]; };
+  auto U = [&](int i, int j) { return g.code(FU, i, j); };
+  auto V = [&](int i, int j) { return g.code(FV, i, j); };
+  for (int jr = 1; jr <= c->nrj; ++jr)
+    for (int ir = 1; ir <= c->nri; ++ir) {
+      const int iW = B(ir, jr, 1), iE = B(ir, jr, 2), jS = B(ir, jr, 3), jN = B(ir, jr, 4);
+      int t = BT(ir, jr, 1);
+      if (t == W2_BM_OUTLT1) {
+        for (int j = jS; j <= jN; ++j) g.op(U(iW - 1, j), {{U(iW, j), 1.0}});
+        g.end_stage();
+        for (int j = jS + 1; j <= jN; ++j) g.op(V(iW, j), {{V(iW + 1, j), -1.0}});
+        g.end_stage();
+      } else if (t == W2_BM_OUTLT2) {
+        for (int j = jS + 1; j <= jN; ++j)
+          g.op(U(iW, j), {{U(iW + 1, j), 1.0}, {V(iW + 1, j), -1.0}, {V(iW + 1, j - 1), 1.0}});
+        g.end_stage();
+        for (int j = jS + 1; j <= jN; ++j) {
+          g.op(V(iW, j), {{V(iW, j - 1), -1.0}, {V(iW + 1, j), 5.0}, {V(iW + 1, j - 1), -5.0},
+                          {U(iW + 1, j), 8.0}, {U(iW, j), -8.0}});
+          g.end_stage();
+        }
+      }
+      t = BT(ir, jr, 2);
+      if (t == W2_BM_OUTLT1) {
+        for (int j = jS; j <= jN; ++j) g.op(U(iE + 1, j), {{U(iE, j), 1.0}});
+        g.end_stage();
+        for (int j = jS + 1; j <= jN; ++j) g.op(V(iE + 1, j), {{V(iE, j), -1.0}});
+        g.end_stage();
+      } else if (t == W2_BM_OUTLT2) {
+        for (int j = jS + 1; j <= jN; ++j)
+          g.op(U(iE, j), {{U(iE - 1, j), 1.0}, {V(iE, j), -1.0}, {V(iE, j - 1), 1.0}});
+        g.end_stage();
+        for (int j = jS + 1; j <= jN - 1; ++j) {
+          g.op(V(iE + 1, j), {{V(iE + 1, j - 1), 1.0}, {V(iE, j - 1), 3.0}, {V(iE, j), -3.0},
+                              {U(iE, j), -4.0}, {U(iE - 1, j), 4.0}});
+          g.end_stage();
+        }
+      }
+      t = BT(ir, jr, 3);
+      if (t == W2_BM_OUTLT1) {
+        for (int i = iW + 1; i <= iE; ++i) g.op(U(i, jS), {{U(i, jS + 1), -1.0}});
+        g.end_stage();
+        for (int i = iW; i <= iE; ++i) g.op(V(i, jS), {{V(i, jS), 1.0}});
+        g.end_stage();
+      } else if (t == W2_BM_OUTLT2) {
+        for (int i = iW + 1; i <= iE; ++i)
+          g.op(V(i, jS), {{V(i, jS + 1), 1.0}, {U(i, jS + 1), 1.0}, {U(i - 1, jS + 1), -1.0}});
+        g.end_stage();
+        for (int i = iW + 1; i <= iE - 1; ++i) {
+          g.op(U(i, jS), {{U(i - 1, jS), 1.0}, {U(i - 1, jS + 1), 3.0}, {U(i, jS + 1), -3.0},
+                          {V(i, jS + 1), -4.0}, {V(i, jS), 4.0}});
+          g.end_stage();
+        }
+      }
+      t = BT(ir, jr, 4);
+      if (t == W2_BM_OUTLT1) {
+        for (int i = iW + 1; i <= iE; ++i) g.op(U(i, jN + 1), {{U(i, jN), -1.0}});
+        g.end_stage();
+        for (int i = iW; i <= iE; ++i) g.op(V(i, jN + 1), {{V(i, jN), 1.0}});
+        g.end_stage();
+      } else if (t == W2_BM_OUTLT2) {
+        for (int i = iW; i <= iE; ++i)
+          g.op(V(i, jN), {{V(i, jN - 1), 1.0}, {U(i, jN), -1.0}, {U(i - 1, jN), 1.0}});
+        g.end_stage();
+        for (int i = iW + 1; i <= iE - 1; ++i) {
+          g.op(U(i, jN + 1), {{U(i - 1, jN + 1), 1.0}, {U(i - 1, jN), 3.0}, {U(i, jN), -3.0},
+                              {V(i, jN), -4.0}, {V(i, jN - 1), 4.0}});
+          g.end_stage();
+        }
+      }
+    }
+}
+
 // PresBoundCond (bound_cond.f:853-1024), in the order of pres_bound_cond_block.
 void emit_pres_bc(const w2_ctx *c, BCProg &g) {
   const int mgri = c->mgri, mgrj = c->mgrj;
@@ -2302,7 +2380,6 @@ int adj_check(w2_ctx *c, const w2_params *prm) {
   if (prm->npsolver != 5 || !prm->lcartes)
     return fail(c, W2_E_UNSUPPORTED, "the adjoint supports ppe_solver rb_sor (5) on Cartesian grids");
   if (prm->nfiltu == 1 || prm->nfiltv == 1) return fail(c, W2_E_UNSUPPORTED, "the adjoint does not cover Filter");
-  if (c->dev.has_outflow) return fail(c, W2_E_UNSUPPORTED, "the adjoint does not cover VelOutflowBCs (outlets)");
   return W2_OK;
 }
 
@@ -2384,13 +2461,18 @@ int wolfd2gpu_adjoint(w2_ctx *c, const w2_params *prm, int nsteps, int every, do
     for (double *x : *v)
       if (!x) return fail(c, W2_E_CUDA, "out of device memory (adjoint checkpoints)");
   // boundary programs as assignment lists
-  BCProg gv_, gp_;
-  gv_.nf = gp_.nf = c->nf;
-  gv_.ld = gp_.ld = c->ld;
+  BCProg gv_, gp_, go_;
+  gv_.nf = gp_.nf = go_.nf = c->nf;
+  gv_.ld = gp_.ld = go_.ld = c->ld;
   emit_vel_bc(c, gv_);
   emit_pres_bc(c, gp_);
-  AdjBCList Lv{}, Lp{};
-  if ((rc = upload_bc(c, gv_, Lv, mem)) || (rc = upload_bc(c, gp_, Lp, mem))) return rc;
+  emit_outflow_bc(c, go_);
+  AdjBCList Lv{}, Lp{}, Lo{};
+  if ((rc = upload_bc(c, gv_, Lv, mem)) || (rc = upload_bc(c, gp_, Lp, mem)) || (rc = upload_bc(c, go_, Lo, mem)))
+    return rc;
+  const bool outflow = c->dev.has_outflow != 0;
+  double *wu = field(), *wv = field();
+  if (!wu || !wv) return fail(c, W2_E_CUDA, "out of device memory (adjoint fields)");
   CK(cudaDeviceSynchronize());
   const bool graph0 = c->graph_on;
   c->graph_on = false;
@@ -2504,9 +2586,18 @@ int wolfd2gpu_adjoint(w2_ctx *c, const w2_params *prm, int nsteps, int every, do
       CK(cudaMemsetAsync(lun, 0, fb, c->st));
       CK(cudaMemsetAsync(lvn, 0, fb, c->st));
       for (int it = m; it >= 1; --it) {
+        // the iteration starts by VelOutflowBCs on the iterate (outlets)
+        const double *us_it = tape[2 * it - 2], *vs_it = tape[2 * it - 1];
+        if (outflow) {
+          CK(cudaMemcpyAsync(wu, us_it, fb, cudaMemcpyDeviceToDevice, c->st));
+          CK(cudaMemcpyAsync(wv, vs_it, fb, cudaMemcpyDeviceToDevice, c->st));
+          if ((rc = launch_bc(c, BC_OUTFLOW, wu, wv, c->P[c->cur]))) return rc;
+          us_it = wu;
+          vs_it = wv;
+        }
         AdjIter A{};
-        A.us = tape[2 * it - 2];
-        A.vs = tape[2 * it - 1];
+        A.us = us_it;
+        A.vs = vs_it;
         A.un = un;
         A.vn = vn;
         A.lus = lu;
@@ -2521,6 +2612,7 @@ int wolfd2gpu_adjoint(w2_ctx *c, const w2_params *prm, int nsteps, int every, do
         A.re = prm->re;
         void *args[] = {&d, &A};
         if ((rc = coop(c, (const void *)k_adj_iter, bl_iter, args, naux_smem(c)))) return rc;
+        if (outflow && (rc = adj_bc(Lo))) return rc;
       }
       // us = un, vs = vn at the start of the step: the level-n adjoint
       k_axpy2<<<gb, c->threads, 0, c->st>>>(d, lu, lun, lv, lvn);
