@@ -181,9 +181,52 @@ def cpu_step_sample(case, ic, nsteps=1):
     return case.cells * nsteps / dt, dt, 1, kind, how
 
 
+def run_reference_sampled(args):
+    """Reference arm of the ensemble and adjoint workloads: the reference's
+    forward steps on one host core over a bounded sample of the workload
+    (the reference has neither batching nor an adjoint)."""
+    if args.workload == "ensemble":
+        members = ensemble_members(args)
+        cases = [(m.case, deck.perturbation_ic(m.case, args.seed + i)) for i, m in enumerate(members)]
+        config = ensemble_config(args, members, args.refine_sweeps or 64, not args.no_graph)
+    else:
+        case = deck.cavity(ADJOINT["n"], ADJOINT["re"], ADJOINT["dt"], solver="rb_sor")
+        cases = [(case, deck.perturbation_ic(case, args.seed))]
+        config = {"workload": f"adjoint workload's forward: lid-driven cavity {ADJOINT['n']}x{ADJOINT['n']}, "
+                              f"Re={ADJOINT['re']:g}, dt={ADJOINT['dt']:g}, rb_sor, plain FP64"}
+    done, secs, steps_run, kind, how = 0, 0.0, 0, "port", ""
+    for step_round in range(max(1, args.steps)):
+        for c, ic in cases:
+            r, kind, how = reference_runner(c, ic)
+            t0 = time.perf_counter()
+            r.step(1)
+            secs += time.perf_counter() - t0
+            done += c.cells
+            steps_run += 1
+            if secs > 15.0 * max(1, args.steps):
+                break
+        if secs > 15.0 * max(1, args.steps):
+            break
+    value = done / secs
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * secs / max(1, steps_run), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": kind,
+                         "sample": f"{steps_run} single reference steps over the workload's cases in order "
+                                   f"({done} cell-steps, {secs:.1f} s); {how}"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
+        return
+    if args.workload in ("ensemble", "adjoint"):
+        run_reference_sampled(args)
         return
     case = make_case(args)
     ic = make_ic(args, case)
