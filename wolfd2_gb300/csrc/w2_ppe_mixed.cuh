@@ -80,6 +80,7 @@ struct MixedBox {
   int k, lane, jj0;            // this thread's column, lane, first strip row
   int dcol0, dcol1;            // column k's distance to the frame, per row parity
   unsigned int vrow;           // bit r: strip row r is a row of unknowns inside the frame
+  unsigned int orow;           // bit r: ... at distance >= H from the frame (own rows)
   bool wedge, eedge;           // west/east neighbour column lives in another warp
   bool own0, own1;             // column k is in the own tile, per row parity
 };
@@ -110,9 +111,8 @@ __device__ __forceinline__ A &pick(A &a0, A &a1) {
 // holds the strip's column of the other plane, read from shared memory at
 // the start of the half-sweep.
 template <int K, int C, int P0>
-__device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, int h, bool act0, bool act1,
-                                                   float relax) {
-  constexpr int H = 2 * K;
+__device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, unsigned int amask, bool act0,
+                                                   bool act1, float relax) {
   // A strip wholly below the box (a block with more threads than its tile
   // plan needs, as in ensemble launches) has nothing to do and must not
   // load: its rows lie past the shared planes.  Uniform per warp (a strip
@@ -128,10 +128,7 @@ __device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, int h, boo
   unsigned int mx = 0u;
 #pragma unroll
   for (int r = 0; r < kMixedRows; ++r) {
-    if (!((b.vrow >> r) & 1u)) continue;  // same for the whole warp
-    const int jj = b.jj0 + r;
-    const int rd = min(jj, b.bh - 1 - jj);
-    if (rd < h) continue;                 // same for the whole warp
+    if (!((amask >> r) & 1u)) continue;   // same for the whole warp
     const int par = P0 ^ (r & 1);         // folded once the loop is unrolled
     const int o = base + r * hw;
     const float other = eo[r];
@@ -151,7 +148,7 @@ __device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, int h, boo
     sum = sum * -0.25f - c0;
     if (par ? act1 : act0) {
       Ec[o] = c0 + relax * sum;
-      if (rd >= H && (par ? b.own1 : b.own0)) {
+      if (((b.orow >> r) & 1u) && (par ? b.own1 : b.own0)) {
         const unsigned int bb = __float_as_uint(fabsf(sum));
         mx = bb > mx ? bb : mx;
       }
@@ -165,8 +162,13 @@ __device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, int h, boo
 template <int K, int C>
 __device__ __forceinline__ unsigned int mixed_half_sweep(const MixedBox &b, int h, float relax) {
   const bool act0 = b.dcol0 >= h, act1 = b.dcol1 >= h;
-  if ((C + b.gj0 + b.jj0) & 1) return mixed_rows<K, C, 1>(b, h, act0, act1, relax);
-  return mixed_rows<K, C, 0>(b, h, act0, act1, relax);
+  // rows at distance >= h from the frame: r in [h - jj0, bh - 1 - h - jj0]
+  const int lo = max(0, h - b.jj0), hi = min(kMixedRows - 1, b.bh - 1 - h - b.jj0);
+  unsigned int amask = 0u;
+  if (hi >= lo) amask = ((2u << hi) - 1u) & ~((1u << lo) - 1u);
+  amask &= b.vrow;
+  if ((C + b.gj0 + b.jj0) & 1) return mixed_rows<K, C, 1>(b, amask, act0, act1, relax);
+  return mixed_rows<K, C, 0>(b, amask, act0, act1, relax);
 }
 
 // ns (<= K) sweeps.  With redm, each warp keeps its running maximum of
@@ -385,8 +387,12 @@ __device__ __forceinline__ void mixed_setup(const Dev &d, const MixedGeom &g, Mi
   b.wedge = b.lane == 0 && b.k >= 1 && b.k < b.hw;
   b.eedge = b.lane == 31 && b.k + 1 < b.hw;
   b.vrow = 0u;
-  for (int r = 0; r < kMixedRows; ++r)
-    if (mixed_drow(d, b, b.jj0 + r, H) > 0) b.vrow |= 1u << r;
+  b.orow = 0u;
+  for (int r = 0; r < kMixedRows; ++r) {
+    const int dr = mixed_drow(d, b, b.jj0 + r, H);
+    if (dr > 0) b.vrow |= 1u << r;
+    if (dr >= H) b.orow |= 1u << r;
+  }
 }
 
 // Position of cell (i, j) in a colour-split buffer (see MixedBox).
