@@ -698,7 +698,7 @@ def run_ensemble(args):
         s.load_fields(*ic)
         solvers.append(s)
         ics.append(ic)
-    ens = Ensemble(solvers, graph=graph)
+    ens = Ensemble(solvers, threads=args.ens_threads, graph=graph)
     prm = [members[i].case.params for i in mine]
     cells = sum(members[i].case.cells for i in mine)
 
@@ -834,6 +834,7 @@ def main():
     ap.add_argument("--ens-count", type=int, default=ENSEMBLE["count"])
     ap.add_argument("--ens-seed", type=int, default=ENSEMBLE["seed"])
     ap.add_argument("--no-graph", action="store_true", help="ensemble: launch directly, no CUDA graph")
+    ap.add_argument("--ens-threads", type=int, default=0, help="ensemble: threads per block (0: library default)")
     ap.add_argument("--adj-steps", type=int, default=ADJOINT["steps"], help="adjoint: steps of the horizon")
     ap.add_argument("--fd-dirs", type=int, default=4, help="adjoint: finite-difference directions checked")
     ap.add_argument("--n", type=int, default=1024, help="cavity cells per side")

@@ -287,7 +287,7 @@ int wolfd2gpu_profile_read(w2_ctx *ctx, int kind, double *total_ms,
  * rb_sorp).  Per case, results are bit-identical to wolfd2gpu_step on that
  * context alone.
  *
- * wolfd2gpu_ens_create: cases[n]; threads per block (0: 256) and Poisson
+ * wolfd2gpu_ens_create: cases[n]; threads per block (0: 128) and Poisson
  *   sweeps per barrier (0: 4) of every launch.  The contexts must outlive
  *   the ensemble; their own calls must not overlap an ensemble call.
  * wolfd2gpu_ens_step: prm[n] (one per case), nsteps steps; stats (may be

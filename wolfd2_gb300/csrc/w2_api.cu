@@ -1712,7 +1712,10 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
     wolfd2gpu_ens_destroy(e);
     return rc;
   };
-  if (threads == 0) threads = 256;
+  // 128-thread blocks: four per SM, so the ragged partition has 4 x SMs
+  // groups to size (with at least one per case, coarser blocks leave the
+  // largest cases with too few)
+  if (threads == 0) threads = 128;
   if (sweeps_per_barrier == 0) sweeps_per_barrier = 4;
   if (threads % 32 || threads < 64 || threads > kMaxThreads)
     return bad(efail(e, W2_E_ARG, "threads must be a multiple of 32 in 64..%d", kMaxThreads));
@@ -1754,14 +1757,15 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
   if (e->bm.empty())
     return bad(efail(e, W2_E_UNSUPPORTED, "%d cases need more blocks than the %d that fit", n, e->blocks_m));
 
-  // Poisson launch: two blocks per SM, each with half an SM's shared memory
+  // Poisson launch: as many blocks per SM (up to four) as registers and
+  // shared memory allow, each with that share of an SM's shared memory
   const void *kp = ens_ppe_kernel(e->K);
   int smem_sm = 0, smem_optin = 0;
   cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, e->device);
   cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device);
   cudaFuncAttributes fa{};
   if (cudaFuncGetAttributes(&fa, kp) != cudaSuccess) return bad(efail(e, W2_E_CUDA, "kernel attributes"));
-  for (int per_sm = 2; per_sm >= 1; --per_sm) {
+  for (int per_sm = 4; per_sm >= 1; --per_sm) {
     const size_t smax = std::min<size_t>((size_t)smem_optin, (size_t)smem_sm / per_sm - 1024) - fa.sharedSizeBytes;
     const int total = per_sm * e->nsm;
     std::vector<int> bp = ens_partition(work, total);
