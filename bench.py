@@ -544,17 +544,34 @@ def run_adjoint(args):
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    n, nsteps = ADJOINT["n"], args.adj_steps
-    case = deck.cavity(n, ADJOINT["re"], ADJOINT["dt"], solver="rb_sor")
+    NORTH, WEST, VAR_U = 4, 1, 1
+    if args.adj_case == "channel":
+        # config 5's gradient: final kinetic energy w.r.t. the inflow profile;
+        # the start is the flow after two steps (v = 0 everywhere at the
+        # initial field puts every v-driven upwind selector on its branch point)
+        case = deck.channel_inflow(CHANNEL["ncx"], CHANNEL["ncy"], CHANNEL["re"], CHANNEL["dt"], seed=args.seed)
+        n = CHANNEL["ncy"]
+        nsteps = args.adj_steps if args.adj_steps != ADJOINT["steps"] else 10
+        every = 5
+        face = (1, 1, WEST, VAR_U)
+        lid = case.regions.profiles[(1, 1, WEST, VAR_U)].copy()
+        s0 = Solver.for_case(case, tuned=False)
+        s0.load_fields(*deck.channel_ic(case))
+        s0.step(case.params, 2)
+        u0, v0, p0 = s0.store_fields()
+        s0.close()
+    else:
+        n, nsteps, every = ADJOINT["n"], args.adj_steps, ADJOINT["every"]
+        case = deck.cavity(n, ADJOINT["re"], ADJOINT["dt"], solver="rb_sor")
+        u0, v0, p0 = deck.perturbation_ic(case, args.seed)
+        lid = np.ones(case.nx + 2)
+        face = (1, 1, NORTH, VAR_U)
     prm = case.params
-    u0, v0, p0 = deck.perturbation_ic(case, args.seed)
-    lid = np.ones(case.nx + 2)
     w = (1.0 / n) ** 2
-    NORTH, VAR_U = 4, 1
 
     def solver():
         s = Solver.for_case(case, tuned=False)
-        s.set_face_profile(1, 1, NORTH, VAR_U, lid)
+        s.set_face_profile(*face, lid)
         return s
 
     s = solver()
@@ -562,8 +579,7 @@ def run_adjoint(args):
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
-        J, gu, gv, gp, gl, counts = s.adjoint(prm, nsteps, ADJOINT["every"], w, profile=(1, 1, NORTH, VAR_U),
-                                              nprof=case.nx + 2)
+        J, gu, gv, gp, gl, counts = s.adjoint(prm, nsteps, every, w, profile=face, nprof=lid.size)
         t_adj = time.perf_counter() - t0
     launches = s.launch_count()
     # forward alone, the same steps (frozen counts), for the adjoint's cost ratio
@@ -578,7 +594,7 @@ def run_adjoint(args):
         return 0.5 * w * (np.sum(u[1:nx + 1, 2:ny + 1] ** 2) + np.sum(v[2:nx + 1, 1:ny + 1] ** 2))
 
     def J_at(u, v, lidv):
-        s.set_face_profile(1, 1, NORTH, VAR_U, lidv)
+        s.set_face_profile(*face, lidv)
         s.load_fields(np.asfortranarray(u), np.asfortranarray(v), p0)
         s.step_counts(prm, counts)
         uu, vv, _ = s.store_fields()
@@ -598,6 +614,9 @@ def run_adjoint(args):
         du = np.where(mu, rng.normal(size=u0.shape), 0.0)
         dv = np.where(mv, rng.normal(size=v0.shape), 0.0)
         dl = rng.normal(size=lid.shape)
+        if args.adj_case == "channel":
+            dl[:2] = 0.0          # rows outside the channel carry no inflow
+            dl[case.ny + 1:] = 0.0
         fd = (J_at(u0 + eps * du, v0 + eps * dv, lid + eps * dl) -
               J_at(u0 - eps * du, v0 - eps * dv, lid - eps * dl)) / (2 * eps)
         ad = float(np.sum(gu * du) + np.sum(gv * dv) + np.sum(gl * dl))
@@ -618,12 +637,18 @@ def run_adjoint(args):
         "metric": METRIC, "value": cells * nsteps / t_adj, "unit": UNIT, "n_gpus": 1,
         "steps": nsteps, "warmup": 0, "ms_per_step": 1e3 * t_adj / nsteps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": (f"adjoint: lid-driven cavity {n}x{n}, Re={ADJOINT['re']:g}, dt={ADJOINT['dt']:g}, "
-                                f"{nsteps} steps from the seeded 16x16-mode perturbation (seed {args.seed}), rb_sor, "
-                                f"plain FP64; J = 0.5 h^2 sum(u^2+v^2) at the final step; gradient with respect to "
-                                f"the initial u, v, p and the {case.nx + 2}-value lid profile (256 moving-wall "
-                                f"positions), checkpoint every {ADJOINT['every']} steps, iteration counts of the "
-                                f"forward run held fixed"),
+        "config": {"workload": (
+            (f"adjoint: lid-driven cavity {n}x{n}, Re={ADJOINT['re']:g}, dt={ADJOINT['dt']:g}, "
+             f"{nsteps} steps from the seeded 16x16-mode perturbation (seed {args.seed}), rb_sor, "
+             f"plain FP64; J = 0.5 h^2 sum(u^2+v^2) at the final step; gradient with respect to "
+             f"the initial u, v, p and the {case.nx + 2}-value lid profile (256 moving-wall "
+             f"positions), checkpoint every {every} steps, iteration counts of the forward run held fixed")
+            if args.adj_case != "channel" else
+            (f"adjoint: profiled channel {CHANNEL['ncx']}x{CHANNEL['ncy']} (mass-conserving outlet), "
+             f"deck Re={CHANNEL['re']:g}, dt={CHANNEL['dt']:g}, {nsteps} steps (a reduced horizon of the "
+             f"configuration's 1000) from the flow after two steps, plain FP64; J = 0.5 h^2 sum(u^2+v^2) at "
+             f"the final step; gradient with respect to the initial u, v, p and the {lid.size}-value inflow "
+             f"profile, checkpoint every {every} steps, iteration counts held fixed")),
                    "value_is": "cell-steps of the forward horizon per second of the whole gradient "
                                "(forward with checkpoints + recompute + adjoint)"},
         "gradient_s": t_adj, "forward_s": t_fwd, "adjoint_over_forward": t_adj / t_fwd,
@@ -836,6 +861,8 @@ def main():
     ap.add_argument("--no-graph", action="store_true", help="ensemble: launch directly, no CUDA graph")
     ap.add_argument("--ens-threads", type=int, default=0, help="ensemble: threads per block (0: library default)")
     ap.add_argument("--adj-steps", type=int, default=ADJOINT["steps"], help="adjoint: steps of the horizon")
+    ap.add_argument("--adj-case", choices=["cavity", "channel"], default="cavity",
+                    help="adjoint: the 256x256 cavity (lid profile) or the profiled channel (inflow profile)")
     ap.add_argument("--fd-dirs", type=int, default=4, help="adjoint: finite-difference directions checked")
     ap.add_argument("--n", type=int, default=1024, help="cavity cells per side")
     ap.add_argument("--re", type=float, default=1000.0)
