@@ -255,8 +255,9 @@ int wolfd2gpu_device_fields(w2_ctx *ctx, double **u, double **v, double **p,
 long long wolfd2gpu_launch_count(w2_ctx *ctx);
 
 /* Chain-solver statistics since the last call (then reset): the most
- * verification rounds any chain solve needed (kMaxRounds+1 = it fell back to
- * the sequential walk) and the number of sequential fallbacks. */
+ * verification rounds any chain solve needed (at most the segment count;
+ * one more than that would mean the sequential guard walk ran) and the
+ * number of such guard walks (0 in a correct build). */
 int wolfd2gpu_chain_stats(w2_ctx *ctx, int *max_rounds, int *fallbacks);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that time or
