@@ -678,19 +678,22 @@ def ensemble_members(args):
 
 def ensemble_config(args, members, inner, graph):
     ns = [m.n for m in members]
+    mixed = args.precision == "mixed"
+    step = (f"mixed step ({inner} FP32 sweeps per refinement pass)" if mixed
+            else "plain FP64 step (bit-identical per case to the case stepped alone)")
     return {
         "workload": (f"batched ensemble: {len(members)} lid-driven cavities, N cells per side drawn "
                      f"uniformly from {{64, 96, ..., 512}} and Re log-uniform in [100, 5000] "
                      f"(numpy default_rng({args.ens_seed})), dt = 0.5 h capped at the viscous number "
                      f"dt/(h^2 Re) = 0.25 where the reference scheme is unstable, seeded 16x16-mode "
-                     f"streamfunction perturbation per case, rb_sor, mixed step ({inner} FP32 sweeps per "
-                     f"refinement pass), one launch per stage for all cases"
+                     f"streamfunction perturbation per case, rb_sor, {step}, one launch per stage for "
+                     f"all cases"
                      f"{', step captured in a CUDA graph' if graph else ''}"),
         "cases": len(members), "cells": int(sum(m.case.cells for m in members)),
         "n_min": min(ns), "n_max": max(ns), "dt_capped_cases": sum(1 for m in members if m.dt < m.dt_named),
         "layout": "each cavity at spacing 1/64 with side N/64 and deck Re = Re/side: the exact similarity "
                   "image of the unit cavity (unit-stencil Poisson rows)",
-        "precision": "mixed", "graph": graph,
+        "precision": args.precision, "graph": graph,
         "l2": "not flushed: the ensemble's fields alone exceed L2 (129 MB) many times over",
     }
 
@@ -701,7 +704,7 @@ def run_ensemble(args):
     import torch
     import torch.distributed as dist
     from wolfd2_gb300 import replicas
-    from wolfd2_gb300.gpu import Ensemble, Solver
+    from wolfd2_gb300.gpu import PREC_FP64, PREC_MIXED, Ensemble, Solver
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -715,6 +718,8 @@ def run_ensemble(args):
     mine = replicas.partition_work([m.case.cells for m in members], world, rank)
     graph = not args.no_graph
     inner = args.refine_sweeps or 64
+    mixed = args.precision == "mixed"
+    kw = {"refine_sweeps": inner, "precision": PREC_MIXED if mixed else PREC_FP64}
     solvers, ics = [], []
     for i in mine:
         c = members[i].case
@@ -733,12 +738,12 @@ def run_ensemble(args):
             dist.barrier()
 
     if args.warmup:
-        ens.step(prm, args.warmup, refine_sweeps=inner)
+        ens.step(prm, args.warmup, **kw)
     # per-stage split of the same kind of steps (direct launches, events)
     ens.graph(False)
     ens.profile(True)
-    prof_hist = ens.step(prm, 1, refine_sweeps=inner)
-    stages = ens.profile_read()
+    prof_hist = ens.step(prm, 1, **kw)
+    stages = ens.profile_read(mixed)
     ens.profile(False)
     ens.graph(graph)
     barrier()
@@ -746,7 +751,7 @@ def run_ensemble(args):
     with ClockSampler(local) as clk:
         barrier()
         t0 = time.perf_counter()
-        hist = ens.step(prm, args.steps, refine_sweeps=inner)
+        hist = ens.step(prm, args.steps, **kw)
         barrier()
         wall = time.perf_counter() - t0
     info = ens.info()
@@ -769,7 +774,7 @@ def run_ensemble(args):
     for _ in range(e2e_steps):
         for s, hs in zip(solvers, hosts):
             s.load_fields(*hs)
-        ens.step(prm, 1, refine_sweeps=inner)
+        ens.step(prm, 1, **kw)
         for s, hs in zip(solvers, hosts):
             s.store_fields(out=hs)
     barrier()
@@ -785,22 +790,25 @@ def run_ensemble(args):
         return
     # algorithmic bytes of the dominant stage (the Poisson launch) over its
     # profiled step, summed over this rank's cases
-    ppe_ms, _ = stages["ke_ppe_mixed"]
-    ppe_bytes = sum(mixed_ppe_bytes(members[i].case.cells, h[0][1], inner)
-                    for i, h in zip(mine, prof_hist))
+    kname = "ke_ppe_mixed" if mixed else "ke_ppe"
+    ppe_ms, _ = stages[kname]
+    if mixed:
+        alg = sum(mixed_ppe_bytes(members[i].case.cells, h[0][1], inner) for i, h in zip(mine, prof_hist))
+    else:
+        alg = sum(ppe_bytes(members[i].case.cells, h[0][1]) for i, h in zip(mine, prof_hist))
     peak_gbs, peak_kind = peaks()
     traffic_ratio = None
     try:
         traffic_ratio = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))[
-            "bytes_per_alg_byte"].get("ke_ppe_mixed")
+            "bytes_per_alg_byte"].get(kname)
     except Exception:
         traffic_ratio = None
-    achieved = ppe_bytes / (ppe_ms / 1e3) / 1e9 if ppe_ms > 0 else None
-    roof = {"bound": "hbm", "kernel": "ke_ppe_mixed", "achieved": achieved, "peak": peak_gbs,
+    achieved = alg / (ppe_ms / 1e3) / 1e9 if ppe_ms > 0 else None
+    roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak_gbs,
             "unit": "GB/s", "frac": achieved / peak_gbs if achieved else None,
             "peak_kind": peak_kind,
-            "traffic": traffic_ratio * ppe_bytes if traffic_ratio else None,
-            "alg_bytes_per_launch": ppe_bytes, "avg_launch_ms": ppe_ms}
+            "traffic": traffic_ratio * alg if traffic_ratio else None,
+            "alg_bytes_per_launch": alg, "avg_launch_ms": ppe_ms}
     cpu = None
     if not args.no_cpu_baseline:
         # a bounded sample: one reference step of the first cases in draw
@@ -823,7 +831,7 @@ def run_ensemble(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
         "steps_per_s": args.steps / t_max,
         "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
-        "dtype": "f32+f64", "data": "synthetic",
+        "dtype": "f32+f64" if mixed else "f64", "data": "synthetic",
         "config": ensemble_config(args, members, inner, graph),
         "parallelism": f"cases partitioned by work over {world} ranks" if world > 1 else "single GPU",
         "roofline": roof,

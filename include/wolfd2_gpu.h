@@ -279,14 +279,16 @@ int wolfd2gpu_profile_read(w2_ctx *ctx, int kind, double *total_ms,
                            long long *count);
 
 /* ---- Ensembles (no reference counterpart) -----------------------------
- * Many independent cases advanced together by the mixed step
- * (precision W2_PREC_MIXED): one launch per stage covers every case, each
- * case on its own group of the launch's blocks (a ragged partition sized
- * by the cases' cells), with its own barriers, convergence tests and
- * iteration counts.  Each case is an ordinary context, set up as usual
- * (metrics, regions, fields; Cartesian unit-stencil grids, rb_sor or
- * rb_sorp).  Per case, results are bit-identical to wolfd2gpu_step on that
- * context alone.
+ * Many independent cases advanced together: one launch per stage covers
+ * every case, each case on its own group of the launch's blocks (a ragged
+ * partition sized by the cases' cells), with its own barriers, convergence
+ * tests and iteration counts.  Each case is an ordinary context, set up as
+ * usual (metrics, regions, fields).  One call steps every case in the same
+ * precision: W2_PREC_MIXED (Cartesian unit-stencil grids, rb_sor or
+ * rb_sorp, in every case) or W2_PREC_FP64 (any grid and any of the six
+ * Poisson solvers, per case).  Filter is not applied (W2_E_UNSUPPORTED).
+ * Per case, results are bit-identical to wolfd2gpu_step on that context
+ * alone.
  *
  * wolfd2gpu_ens_create: cases[n]; threads per block (0: 128) and Poisson
  *   sweeps per barrier (0: 4) of every launch.  The contexts must outlive
@@ -297,7 +299,8 @@ int wolfd2gpu_profile_read(w2_ctx *ctx, int kind, double *total_ms,
  *   continue) and the first device error otherwise.
  * wolfd2gpu_ens_graph: when enabled, one step's launch sequence is captured
  *   in a CUDA graph on the first call and replayed every step.
- * wolfd2gpu_ens_info: blocks of the momentum and Poisson launches, device
+ * wolfd2gpu_ens_info: blocks of the momentum and (mixed) Poisson launches
+ *   (the plain Poisson launch uses the momentum partition), device
  *   milliseconds of the last ens_step call (CUDA events around its steps),
  *   and kernel launches so far. */
 typedef struct w2_ens w2_ens;

@@ -1,12 +1,12 @@
 """Ensembles: many cases advanced by one launch per stage must give, per
-case, exactly what the case gives when stepped alone (the same mixed step:
-chain solves are exact for any segment length, the Poisson sweeps exact for
-any tile plan)."""
+case, exactly what the case gives when stepped alone (the same mixed or
+plain step: chain solves are exact for any segment length, the Poisson
+sweeps exact for any tile plan or block count)."""
 import numpy as np
 import pytest
 
 from wolfd2_gb300 import deck
-from wolfd2_gb300.gpu import PREC_MIXED, Ensemble, Solver
+from wolfd2_gb300.gpu import PREC_FP64, PREC_MIXED, Ensemble, Solver
 
 pytestmark = pytest.mark.gpu
 
@@ -27,10 +27,28 @@ def _cases():
     return out
 
 
-def _alone(case, fields, nsteps):
+def _plain_cases():
+    """One case per Poisson solver, on grids the mixed step does not take:
+    spacings that are not powers of two, a rectangle, and a channel with an
+    outlet."""
+    out = []
+    spec = [(32, None, 100.0, "sor", 0.5), (40, None, 400.0, "lsor", 1.0),
+            (48, 32, 300.0, "rb_lsor", 1.0), (36, None, 200.0, "par_rb_lsor", 1.0),
+            (64, None, 1000.0, "rb_sor", 1.0)]
+    for k, (n, ny, re, solver, side) in enumerate(spec):
+        h = side / n
+        dt = min(0.5 * h, 0.25 * h * h * re)
+        case = deck.cavity(n, re, dt, solver=solver, ny=ny, side=side)
+        out.append((case, deck.perturbation_ic(case, 200 + k)))
+    ch = deck.channel_inflow(64, 16, 100.0, 0.01, solver="par_rb_sor", outlet="mc", seed=7)
+    out.append((ch, deck.channel_ic(ch)))
+    return out
+
+
+def _alone(case, fields, nsteps, precision=PREC_MIXED):
     s = Solver.for_case(case, tuned=False)
     s.load_fields(*fields)
-    hist = s.step(case.params, nsteps, precision=PREC_MIXED, refine_sweeps=REFINE)
+    hist = s.step(case.params, nsteps, precision=precision, refine_sweeps=REFINE)
     u, v, p = s.store_fields()
     s.close()
     return hist, (u, v, p)
@@ -81,4 +99,58 @@ def test_ensemble_continues_across_calls():
     ea.close()
     eb.close()
     for s in a + b:
+        s.close()
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_plain_ensemble_matches_cases_alone(graph):
+    """The plain FP64 ensemble: every solver, non-unit grids, an outlet;
+    bit-identical fields and equal iteration counts per case."""
+    cases = _plain_cases()
+    nsteps = 3
+    solvers = []
+    for case, f in cases:
+        s = Solver.for_case(case, tuned=False)
+        s.load_fields(*f)
+        solvers.append(s)
+    ens = Ensemble(solvers, graph=graph)
+    hist = ens.step([c.params for c, _ in cases], nsteps, precision=PREC_FP64)
+    for k, ((case, f), s) in enumerate(zip(cases, solvers)):
+        ref_hist, ref = _alone(case, f, nsteps, precision=PREC_FP64)
+        assert [(h[0], h[1]) for h in hist[k]] == [(h[0], h[1]) for h in ref_hist], k
+        assert [h[2][:3] for h in hist[k]] == [h[2][:3] for h in ref_hist], k
+        got = s.store_fields()
+        for name, g, r in zip("uvp", got, ref):
+            assert np.array_equal(g, r), (k, name, float(np.max(np.abs(g - r))))
+    # these grids have no mixed Poisson plan
+    with pytest.raises(Exception):
+        ens.step([c.params for c, _ in cases], 1, precision=PREC_MIXED)
+    ens.close()
+    for s in solvers:
+        s.close()
+
+
+def test_ensemble_switches_precision():
+    """Unit-stencil cases: plain steps then mixed steps in one ensemble equal
+    the same sequence on each case alone."""
+    cases = _cases()[:3]
+    solvers = []
+    for case, f in cases:
+        s = Solver.for_case(case, tuned=False)
+        s.load_fields(*f)
+        solvers.append(s)
+    ens = Ensemble(solvers)
+    prm = [c.params for c, _ in cases]
+    ens.step(prm, 2, precision=PREC_FP64)
+    ens.step(prm, 2, precision=PREC_MIXED, refine_sweeps=REFINE)
+    for (case, f), s in zip(cases, solvers):
+        a = Solver.for_case(case, tuned=False)
+        a.load_fields(*f)
+        a.step(case.params, 2)
+        a.step(case.params, 2, precision=PREC_MIXED, refine_sweeps=REFINE)
+        for x, y in zip(s.store_fields(), a.store_fields()):
+            assert np.array_equal(x, y)
+        a.close()
+    ens.close()
+    for s in solvers:
         s.close()

@@ -115,31 +115,54 @@ __global__ void k_adj_project(Dev d, double dk, const double *lu, const double *
 
 // ---- Ppe: red/black SOR (pressure.f:457-532) and Divergence ---------------
 
-// Gather of point (i, j) from the unknowns of colour `par` that it
-// neighbours: sum over such x of dp_x_new/dp_y * lambda_x.
-__device__ __forceinline__ double adj_rb_gather(const Dev &d, const double *lp, int i, int j, int par,
-                                                double sorrel) {
+// Transposed SOR coefficients, fixed for a call: for each unknown x,
+// q3 = sorrel/a3(x) and qk = sorrel*ak(x)/a3(x) (k = 1, 2, 4, 5), the
+// factors by which x's update reads b and each neighbour.  Evaluated as the
+// sweep itself groups them, so the products below round as before.
+struct AdjPpeCoef {
+  double *q1, *q2, *q3, *q4, *q5;
+};
+
+__global__ void k_adj_ppe_coef(Dev d, double sorrel, AdjPpeCoef q) {
+  vgrid_set(0, gridDim.x);
+  const int nx = d.nx, ny = d.ny;
+  for (int t = gtid(); t < (nx - 1) * (ny - 1); t += gthreads()) {
+    const int i = t % (nx - 1) + 2, j = t / (nx - 1) + 2;
+    const size_t x = IX(d, i, j);
+    const double a3 = d.pa3[x];
+    q.q3[x] = sorrel / a3;
+    q.q1[x] = sorrel * d.pa1[x] / a3;
+    q.q2[x] = sorrel * d.pa2[x] / a3;
+    q.q4[x] = sorrel * d.pa4[x] / a3;
+    q.q5[x] = sorrel * d.pa5[x] / a3;
+  }
+}
+
+// Gather of point (i, j), whose colour is not `par`, from the unknowns of
+// colour `par` that it neighbours: sum over such x of dp_x_new/dp_y * lambda_x.
+__device__ __forceinline__ double adj_rb_gather(const Dev &d, const AdjPpeCoef &q, const double *lp, int i,
+                                                int j) {
   double g = 0.0;
-  auto unk = [&](int a, int b) { return a >= 2 && a <= d.nx && b >= 2 && b <= d.ny && ((a + b) & 1) == par; };
+  auto unk = [&](int a, int b) { return a >= 2 && a <= d.nx && b >= 2 && b <= d.ny; };
   // x north of y: y is x's south, coefficient a1(x)
   if (unk(i, j + 1)) {
     const size_t x = IX(d, i, j + 1);
-    g -= sorrel * d.pa1[x] / d.pa3[x] * lp[x];
+    g -= q.q1[x] * lp[x];
   }
   // x east of y: y is x's west, a2(x)
   if (unk(i + 1, j)) {
     const size_t x = IX(d, i + 1, j);
-    g -= sorrel * d.pa2[x] / d.pa3[x] * lp[x];
+    g -= q.q2[x] * lp[x];
   }
   // x west of y: y is x's east, a4(x)
   if (unk(i - 1, j)) {
     const size_t x = IX(d, i - 1, j);
-    g -= sorrel * d.pa4[x] / d.pa3[x] * lp[x];
+    g -= q.q4[x] * lp[x];
   }
   // x south of y: y is x's north, a5(x)
   if (unk(i, j - 1)) {
     const size_t x = IX(d, i, j - 1);
-    g -= sorrel * d.pa5[x] / d.pa3[x] * lp[x];
+    g -= q.q5[x] * lp[x];
   }
   return g;
 }
@@ -147,9 +170,11 @@ __device__ __forceinline__ double adj_rb_gather(const Dev &d, const double *lp, 
 // Transpose of nsor red/black sweeps (colour 0 then 1 per sweep) with fixed
 // count, then of b = div/dk and Divergence.  lp: in, the adjoint of p after
 // the sweeps; out, of p before them.  lb: scratch (the adjoint of b).
-// lus, lvs: += the divergence's transpose.
+// lus, lvs: += the divergence's transpose.  q: from k_adj_ppe_coef with the
+// same sorrel.
 __global__ void __launch_bounds__(kMaxThreads) k_adj_ppe(Dev d, int nsor, double sorrel, double dk,
-                                                         double *lp, double *lb, double *lus, double *lvs) {
+                                                         AdjPpeCoef q, double *lp, double *lb, double *lus,
+                                                         double *lvs) {
   vgrid_set(0, gridDim.x);
   Sync *sy = d.sync;
   const int nx = d.nx, ny = d.ny, W = nx + 1, H = ny + 1;  // points i, j = 1..nx+1, 1..ny+1
@@ -163,10 +188,12 @@ __global__ void __launch_bounds__(kMaxThreads) k_adj_ppe(Dev d, int nsor, double
       const int i = t % W + 1, j = t / W + 1;
       const size_t o = IX(d, i, j);
       const bool isu = i >= 2 && i <= nx && j >= 2 && j <= ny;
-      if (isu && ((i + j) & 1) == par) {
-        lb[o] += sorrel / d.pa3[o] * lp[o];
+      if (((i + j) & 1) == par) {
+        // the colour's own points: an unknown's update read b; a boundary
+        // point of this colour neighbours no unknown of it
+        if (isu) lb[o] += q.q3[o] * lp[o];
       } else {
-        const double g = adj_rb_gather(d, lp, i, j, par, sorrel);
+        const double g = adj_rb_gather(d, q, lp, i, j);
         if (isu) lp[o] = (first ? lp[o] : om * lp[o]) + g;
         else lp[o] += g;
       }

@@ -1494,7 +1494,7 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
 
 // ============================================================================
 // Ensembles: many independent cases advanced together, one launch per stage
-// of the mixed time step (kernels in w2_ensemble.cuh).
+// of the mixed or plain time step (kernels in w2_ensemble.cuh).
 // ============================================================================
 
 struct w2_ens {
@@ -1510,9 +1510,10 @@ struct w2_ens {
   size_t smem_m = 0, smem_p = 0;
   StepOut *d_outs = nullptr;
   size_t outs_cap = 0;
+  bool mixed_ok = false;    // every case has a mixed Poisson plan
   bool graph_on = false;
   cudaGraphExec_t gexec = nullptr;
-  int graph_nsteps = -1;
+  int graph_nsteps = -1, graph_prec = -1;
   long long launches = 0;
   double last_ms = 0.0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1664,29 +1665,54 @@ void ens_prof_collect(w2_ens *e) {
   e->prof_pending.clear();
 }
 
-int ens_launch_step(w2_ens *e, const EnsLaunch &Lm, const EnsLaunch &Lp, const EnsLaunch &L1,
+// One step's launches: mixed (Lp: the Poisson partition) or plain FP64
+// (every stage on the momentum partition Lm).
+int ens_launch_step(w2_ens *e, bool mixed, const EnsLaunch &Lm, const EnsLaunch &Lp, const EnsLaunch &L1,
                     bool capturing = false) {
   EnsLaunch am = Lm, ap = Lp;
   void *argm[] = {&am}, *argp[] = {&ap};
-  {
-    EnsProf pr(e, W2_ENS_COPY, capturing);
-    ke_copy_mixed<<<e->blocks_m, e->threads, 0, e->st>>>(Lm);
-    ECK(cudaGetLastError());
-  }
-  {
-    EnsProf pr(e, W2_ENS_MOMENTUM, capturing);
-    ECK(cudaLaunchCooperativeKernel((const void *)ke_naux32, dim3(e->blocks_m), dim3(e->threads), argm,
-                                    e->smem_m, e->st));
-  }
-  {
-    EnsProf pr(e, W2_ENS_BC, capturing);
-    ke_bc<<<e->n, e->threads, 0, e->st>>>(L1);
-    ECK(cudaGetLastError());
-  }
-  {
-    EnsProf pr(e, W2_ENS_PPE, capturing);
-    ECK(cudaLaunchCooperativeKernel(ens_ppe_kernel(e->K), dim3(e->blocks_p), dim3(e->threads), argp,
-                                    e->smem_p, e->st));
+  if (!mixed) {
+    {
+      EnsProf pr(e, W2_ENS_COPY, capturing);
+      ke_copy3<<<e->blocks_m, e->threads, 0, e->st>>>(Lm);
+      ECK(cudaGetLastError());
+    }
+    {
+      EnsProf pr(e, W2_ENS_MOMENTUM, capturing);
+      ECK(cudaLaunchCooperativeKernel((const void *)ke_naux, dim3(e->blocks_m), dim3(e->threads), argm,
+                                      e->smem_m, e->st));
+    }
+    {
+      EnsProf pr(e, W2_ENS_BC, capturing);
+      ke_bc<<<e->n, e->threads, 0, e->st>>>(L1);
+      ECK(cudaGetLastError());
+    }
+    {
+      EnsProf pr(e, W2_ENS_PPE, capturing);
+      ECK(cudaLaunchCooperativeKernel((const void *)ke_ppe, dim3(e->blocks_m), dim3(e->threads), argm, 0,
+                                      e->st));
+    }
+  } else {
+    {
+      EnsProf pr(e, W2_ENS_COPY, capturing);
+      ke_copy_mixed<<<e->blocks_m, e->threads, 0, e->st>>>(Lm);
+      ECK(cudaGetLastError());
+    }
+    {
+      EnsProf pr(e, W2_ENS_MOMENTUM, capturing);
+      ECK(cudaLaunchCooperativeKernel((const void *)ke_naux32, dim3(e->blocks_m), dim3(e->threads), argm,
+                                      e->smem_m, e->st));
+    }
+    {
+      EnsProf pr(e, W2_ENS_BC, capturing);
+      ke_bc<<<e->n, e->threads, 0, e->st>>>(L1);
+      ECK(cudaGetLastError());
+    }
+    {
+      EnsProf pr(e, W2_ENS_PPE, capturing);
+      ECK(cudaLaunchCooperativeKernel(ens_ppe_kernel(e->K), dim3(e->blocks_p), dim3(e->threads), argp,
+                                      e->smem_p, e->st));
+    }
   }
   {
     EnsProf pr(e, W2_ENS_POST, capturing);
@@ -1724,15 +1750,20 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
   e->threads = threads;
   e->K = sweeps_per_barrier;
   e->cs.assign(cases, cases + n);
+  // the mixed step needs unit-stencil Poisson rows in every case
+  bool unit = true;
   for (int k = 0; k < n; ++k) {
     w2_ctx *c = e->cs[k];
     if (!c) return bad(efail(e, W2_E_ARG, "case %d is null", k));
     if (int rc = ready(c)) return bad(efail(e, rc, "case %d: %s", k, c->err));
-    if (!c->dev.ppe_unit)
-      return bad(efail(e, W2_E_UNSUPPORTED, "case %d: the mixed ensemble needs unit-stencil Poisson rows", k));
+    unit = unit && c->dev.ppe_unit;
     if (k == 0) e->device = c->device;
     else if (c->device != e->device) return bad(efail(e, W2_E_ARG, "cases on different devices"));
-    if (int rc = ensure_f32(c)) return bad(efail(e, rc, "case %d: %s", k, c->err));
+  }
+  for (int k = 0; k < n; ++k) {
+    w2_ctx *c = e->cs[k];
+    if (unit)
+      if (int rc = ensure_f32(c)) return bad(efail(e, rc, "case %d: %s", k, c->err));
     if (cudaStreamSynchronize(c->st) != cudaSuccess) return bad(efail(e, W2_E_CUDA, "case %d: set-up failed", k));
   }
   if (cudaSetDevice(e->device) != cudaSuccess) return bad(efail(e, W2_E_CUDA, "cudaSetDevice"));
@@ -1744,28 +1775,37 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
   std::vector<double> work(n);
   for (int k = 0; k < n; ++k) work[k] = (double)(e->cs[k]->nx - 1) * (e->cs[k]->ny - 1);
 
-  // momentum and step-tail launches: blocks by the co-residency of both
+  // momentum and step-tail launches (and the plain Poisson launch): blocks
+  // by the co-residency of all of them
   e->smem_m = walk_stage_bytes(sizeof(double), threads);
-  if (cudaFuncSetAttribute((const void *)ke_naux32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)e->smem_m) != cudaSuccess)
-    return bad(efail(e, W2_E_CUDA, "shared memory attribute (momentum)"));
-  int occ_m = 0, occ_t = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_m, (const void *)ke_naux32, threads, e->smem_m);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_t, (const void *)ke_step_post, threads, 0);
-  e->blocks_m = std::min(occ_m, occ_t) * e->nsm;
+  int occ = 1 << 20;
+  for (const void *kf : {(const void *)ke_naux32, (const void *)ke_naux}) {
+    if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem_m) != cudaSuccess)
+      return bad(efail(e, W2_E_CUDA, "shared memory attribute (momentum)"));
+    int o = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kf, threads, e->smem_m);
+    occ = std::min(occ, o);
+  }
+  for (const void *kf : {(const void *)ke_step_post, (const void *)ke_ppe}) {
+    int o = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kf, threads, 0);
+    occ = std::min(occ, o);
+  }
+  e->blocks_m = occ * e->nsm;
   e->bm = ens_partition(work, e->blocks_m);
   if (e->bm.empty())
     return bad(efail(e, W2_E_UNSUPPORTED, "%d cases need more blocks than the %d that fit", n, e->blocks_m));
 
-  // Poisson launch: as many blocks per SM (up to four) as registers and
-  // shared memory allow, each with that share of an SM's shared memory
+  // mixed Poisson launch: as many blocks per SM (up to four) as registers
+  // and shared memory allow, each with that share of an SM's shared memory
   const void *kp = ens_ppe_kernel(e->K);
+  e->h.resize(n);
   int smem_sm = 0, smem_optin = 0;
   cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, e->device);
   cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device);
   cudaFuncAttributes fa{};
   if (cudaFuncGetAttributes(&fa, kp) != cudaSuccess) return bad(efail(e, W2_E_CUDA, "kernel attributes"));
-  for (int per_sm = 4; per_sm >= 1; --per_sm) {
+  for (int per_sm = 4; unit && per_sm >= 1; --per_sm) {
     const size_t smax = std::min<size_t>((size_t)smem_optin, (size_t)smem_sm / per_sm - 1024) - fa.sharedSizeBytes;
     const int total = per_sm * e->nsm;
     std::vector<int> bp = ens_partition(work, total);
@@ -1787,11 +1827,15 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
     e->bp = bp;
     e->blocks_p = total;
     e->smem_p = smem;
-    e->h.resize(n);
     for (int k = 0; k < n; ++k) e->h[k].g = g[k];
     break;
   }
-  if (e->bp.empty()) return bad(efail(e, W2_E_UNSUPPORTED, "no Poisson tile plan fits the ensemble"));
+  e->mixed_ok = !e->bp.empty();
+  if (!e->mixed_ok) {
+    // plain steps only: the Poisson table is unused
+    e->bp = e->bm;
+    e->blocks_p = e->blocks_m;
+  }
 
   // per-case buffers and the parts of the descriptors that do not change
   for (int k = 0; k < n; ++k) {
@@ -1799,8 +1843,9 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
     EnsCase &h = e->h[k];
     const MixedGeom &g = h.g;
     const size_t plane2 = 2 * (size_t)g.gh * g.gw;
-    float *xb = ealloc<float>(e, 3 * plane2);
-    if (!xb) return bad(efail(e, W2_E_CUDA, "out of device memory (case %d Poisson buffers)", k));
+    float *xb = nullptr;
+    if (e->mixed_ok && !(xb = ealloc<float>(e, 3 * plane2)))
+      return bad(efail(e, W2_E_CUDA, "out of device memory (case %d Poisson buffers)", k));
     h.d = c->dev;
     chain_views(h.d, c->nx, c->ny, (long)e->bm[k] * threads, c->seg_req, c->warm_req);
     for (int b = 0; b < 2; ++b) {
@@ -1848,12 +1893,19 @@ int wolfd2gpu_ens_graph(w2_ens *e, int enable) {
 int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat *stats) {
   if (!e || !prm || nsteps < 0) return W2_E_ARG;
   const int n = e->n;
+  const bool mixed = prm[0].precision == W2_PREC_MIXED;
   for (int k = 0; k < n; ++k) {
     const w2_params &q = prm[k];
-    if (q.precision != W2_PREC_MIXED)
-      return efail(e, W2_E_UNSUPPORTED, "case %d: the ensemble runs the mixed step (precision %d)", k, W2_PREC_MIXED);
-    if ((q.npsolver != 5 && q.npsolver != 6) || !q.lcartes)
+    if (q.precision != W2_PREC_MIXED && q.precision != W2_PREC_FP64)
+      return efail(e, W2_E_ARG, "case %d: bad precision %d", k, q.precision);
+    if ((q.precision == W2_PREC_MIXED) != mixed)
+      return efail(e, W2_E_UNSUPPORTED, "case %d: every case of one call runs in the same precision", k);
+    if (mixed && !e->mixed_ok)
+      return efail(e, W2_E_UNSUPPORTED, "the mixed step needs unit-stencil Poisson rows in every case");
+    if (mixed && ((q.npsolver != 5 && q.npsolver != 6) || !q.lcartes))
       return efail(e, W2_E_UNSUPPORTED, "case %d: the mixed step needs rb_sor/rb_sorp on a Cartesian grid", k);
+    if (q.npsolver < 1 || q.npsolver > 6) return efail(e, W2_E_ARG, "case %d: bad Poisson solver %d", k, q.npsolver);
+    if (q.nfiltu == 1 || q.nfiltv == 1) return efail(e, W2_E_UNSUPPORTED, "case %d: the ensemble does not apply Filter", k);
     if (q.msorit < 1 || q.mqiter < 1 || q.refine_sweeps < 0) return efail(e, W2_E_ARG, "case %d: bad parameters", k);
   }
   if (nsteps == 0) return W2_OK;
@@ -1866,6 +1918,11 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
     h.dk = q.dk;
     h.re = q.re;
     h.qtol = q.qtol;
+    h.npsolver = q.npsolver;
+    h.lcartes = q.lcartes;
+    h.msorit = q.msorit;
+    h.sortol = q.sortol;
+    h.sorrel = q.sorrel;
     for (int b = 0; b < 2; ++b) {
       MixedArgs &a = h.a[b];
       a.lcartes = q.lcartes;
@@ -1892,7 +1949,8 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
   const EnsLaunch Lm{e->d_cases, e->d_first_m, n, e->d_step, e->d_outs, nsteps};
   const EnsLaunch Lp{e->d_cases, e->d_first_p, n, e->d_step, e->d_outs, nsteps};
   const EnsLaunch L1{e->d_cases, e->d_first_1, n, e->d_step, e->d_outs, nsteps};
-  if (e->graph_on && e->graph_nsteps != nsteps) {
+  const int prec = mixed ? W2_PREC_MIXED : W2_PREC_FP64;
+  if (e->graph_on && (e->graph_nsteps != nsteps || e->graph_prec != prec)) {
     if (e->gexec) {
       cudaGraphExecDestroy(e->gexec);
       e->gexec = nullptr;
@@ -1900,7 +1958,7 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
     cudaGraph_t g = nullptr;
     ECK(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
     const long long l0 = e->launches;
-    int rc = ens_launch_step(e, Lm, Lp, L1, true);
+    int rc = ens_launch_step(e, mixed, Lm, Lp, L1, true);
     e->launches = l0;
     cudaError_t ce = cudaStreamEndCapture(e->st, &g);
     if (rc) return rc;
@@ -1909,13 +1967,14 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
     cudaGraphDestroy(g);
     if (ce != cudaSuccess) return efail(e, W2_E_CUDA, "graph instantiation: %s", cudaGetErrorString(ce));
     e->graph_nsteps = nsteps;
+    e->graph_prec = prec;
   }
   ECK(cudaEventRecord(e->ev0, e->st));
   for (int s = 0; s < nsteps; ++s) {
     if (e->graph_on) {
       ECK(cudaGraphLaunch(e->gexec, e->st));
       e->launches += 6;
-    } else if (int rc = ens_launch_step(e, Lm, Lp, L1)) {
+    } else if (int rc = ens_launch_step(e, mixed, Lm, Lp, L1)) {
       return rc;
     }
   }
@@ -2526,6 +2585,13 @@ int wolfd2gpu_adjoint(w2_ctx *c, const w2_params *prm, int nsteps, int every, do
   CK(cudaMemsetAsync(lprof, 0, nprof_all * sizeof(double), c->st));
   k_adj_objective<<<gb, c->threads, 0, c->st>>>(d, weight, fin[0], fin[1], lu, lv, dJ);
   CK(cudaGetLastError());
+  // transposed SOR coefficients, fixed for the call
+  AdjPpeCoef pq{field(), field(), field(), field(), field()};
+  for (double *x : {pq.q1, pq.q2, pq.q3, pq.q4, pq.q5})
+    if (!x) return fail(c, W2_E_CUDA, "out of device memory (adjoint fields)");
+  c->launches += 2;
+  k_adj_ppe_coef<<<gb, c->threads, 0, c->st>>>(d, prm->sorrel, pq);
+  CK(cudaGetLastError());
   // ---- backward, segment by segment
   const int nX = c->nx * (c->ny - 1);
   (void)nX;
@@ -2569,7 +2635,7 @@ int wolfd2gpu_adjoint(w2_ctx *c, const w2_params *prm, int nsteps, int every, do
       {
         double sr = prm->sorrel;
         int nsv = ns;
-        void *args[] = {&d, &nsv, &sr, &dk, &lp, &lb, &lu, &lv};
+        void *args[] = {&d, &nsv, &sr, &dk, &pq, &lp, &lb, &lu, &lv};
         if ((rc = coop(c, (const void *)k_adj_ppe, bl_ppe, args))) return rc;
       }
       // the boundary rows before Ppe: VelBC then PresBC, reversed

@@ -1,5 +1,5 @@
 // w2_ensemble.cuh -- many independent cases advanced together: one launch per
-// stage of the mixed time step covers every case.
+// stage of the time step (mixed, or plain FP64) covers every case.
 //
 // The launch's blocks are split into one group of consecutive blocks per
 // case (a ragged partition, sized by the host to each case's cells).  A block
@@ -29,6 +29,8 @@ struct EnsCase {
   int cur;                 // time level holding the fields when the call starts
   int mqiter;
   double dk, re, qtol;
+  int npsolver, lcartes, msorit;  // plain step's Ppe
+  double sortol, sorrel;
 };
 
 // Arguments shared by the launches of one ensemble step.
@@ -107,6 +109,36 @@ __global__ void __launch_bounds__(kMaxThreads) ke_step_post(EnsLaunch L) {
   if (e.d.sync->halt) return;
   const int a = ens_level(e, L), b = a ^ 1;
   step_post_body(e.d, e.dk, e.P[b], e.P[a], e.U[a], e.V[a], e.U[b], e.V[b], ens_out(L, k));
+}
+
+// ---- plain FP64 step: the single-case stage bodies on each case's group --
+
+__global__ void ke_copy3(EnsLaunch L) {
+  const int k = ens_enter(L.first, L.n);
+  const EnsCase &e = L.cs[k];
+  if (e.d.sync->halt) return;
+  const int a = ens_level(e, L), b = a ^ 1;
+  copy3_body(e.d, e.U[b], e.U[a], e.V[b], e.V[a], e.P[b], e.P[a]);
+}
+
+__global__ void __launch_bounds__(kMaxThreads, 1) ke_naux(EnsLaunch L) {
+  const int k = ens_enter(L.first, L.n);
+  const EnsCase &e = L.cs[k];
+  if (e.d.sync->halt) return;
+  const int a = ens_level(e, L), b = a ^ 1;
+  int res = -1;
+  if (!naux_momentum<double>(e.d, e.d.f64, e.mqiter, e.dk, e.re, e.qtol, e.U[a], e.V[a], e.U[b], e.V[b], &res))
+    return;
+  if (vblock() == 0 && threadIdx.x == 0) ens_out(L, k)->nql = res;
+}
+
+__global__ void __launch_bounds__(kMaxThreads) ke_ppe(EnsLaunch L) {
+  const int k = ens_enter(L.first, L.n);
+  const EnsCase &e = L.cs[k];
+  if (e.d.sync->halt) return;
+  const int b = ens_level(e, L) ^ 1;
+  ppe_body(e.d, e.lcartes, e.npsolver, e.msorit, e.dk, e.sortol, e.sorrel, e.U[b], e.V[b], e.P[b],
+           ens_out(L, k));
 }
 
 __global__ void ke_tick(int *step) { ++*step; }

@@ -151,10 +151,8 @@ __global__ void k_ppe_check(Dev d, int *flag) {
 }
 
 // ---- field copies -------------------------------------------------------
-__global__ void k_copy3(Dev d, double *a, const double *a0, double *b, const double *b0,
-                        double *c, const double *c0) {
-  vgrid_set(0, gridDim.x);
-  if (d.sync->halt) return;
+__device__ __forceinline__ void copy3_body(const Dev &d, double *a, const double *a0, double *b,
+                                           const double *b0, double *c, const double *c0) {
   const int W = d.nx + 2, H = d.ny + 2;
   for (int t = gtid(); t < W * H; t += gthreads()) {
     const size_t o = IX(d, t % W, t / W);
@@ -162,6 +160,13 @@ __global__ void k_copy3(Dev d, double *a, const double *a0, double *b, const dou
     b[o] = b0[o];
     if (c) c[o] = c0[o];
   }
+}
+
+__global__ void k_copy3(Dev d, double *a, const double *a0, double *b, const double *b0,
+                        double *c, const double *c0) {
+  vgrid_set(0, gridDim.x);
+  if (d.sync->halt) return;
+  copy3_body(d, a, a0, b, b0, c, c0);
 }
 
 // us(1..nx+1,1..ny+1) = un, vs = vn (momentum.f:114-119)
@@ -265,13 +270,12 @@ __global__ void k_bc(Dev d, int ops, double *u, double *v, double *p) {
 }
 
 // ---- Ppe -----------------------------------------------------------------
-// Multi-block form (solvers 3, 4, 5, 6) and single-block form (1, 2).
-__global__ void __launch_bounds__(kMaxThreads) k_ppe(Dev d, int lcartes, int npsolver, int msorit,
-                                                     double dk, double sortol, double sorrel,
-                                                     const double *u, const double *v, double *p,
-                                                     StepOut *out) {
-  vgrid_set(0, gridDim.x);
-  if (d.sync->halt) return;
+// Multi-block form (solvers 3, 4, 5, 6) and single-block form (1, 2: the
+// first block of the virtual grid solves, the others only help with the
+// divergence and right-hand side).
+__device__ __forceinline__ void ppe_body(const Dev &d, int lcartes, int npsolver, int msorit, double dk,
+                                         double sortol, double sorrel, const double *u, const double *v,
+                                         double *p, StepOut *out) {
   Sync *sy = d.sync;
   ppe_divergence(d, u, v);
   if (!grid_sync(sy)) return;
@@ -290,6 +294,15 @@ __global__ void __launch_bounds__(kMaxThreads) k_ppe(Dev d, int lcartes, int nps
     if (nconv < 0) return;
   }
   if (vblock() == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? msorit : nconv;
+}
+
+__global__ void __launch_bounds__(kMaxThreads) k_ppe(Dev d, int lcartes, int npsolver, int msorit,
+                                                     double dk, double sortol, double sorrel,
+                                                     const double *u, const double *v, double *p,
+                                                     StepOut *out) {
+  vgrid_set(0, gridDim.x);
+  if (d.sync->halt) return;
+  ppe_body(d, lcartes, npsolver, msorit, dk, sortol, sorrel, u, v, p, out);
 }
 
 // Red/black SOR with two sweeps per grid barrier (unit-stencil rows,

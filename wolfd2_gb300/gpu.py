@@ -397,11 +397,11 @@ class Solver:
 
 
 class Ensemble:
-    """Many independent cases advanced together by the mixed step, one
-    launch per stage for all of them (wolfd2gpu_ens_*).  Each case is an
-    ordinary Solver, set up and loaded as usual; store_fields on a member
-    reads that case's state.  The members must stay open while the
-    ensemble is used."""
+    """Many independent cases advanced together, one launch per stage for
+    all of them (wolfd2gpu_ens_*), by the mixed step or the plain FP64 step.
+    Each case is an ordinary Solver, set up and loaded as usual;
+    store_fields on a member reads that case's state.  The members must
+    stay open while the ensemble is used."""
 
     def __init__(self, solvers: Sequence["Solver"], threads: int = 0, sweeps_per_barrier: int = 0,
                  graph: bool = True):
@@ -419,28 +419,32 @@ class Ensemble:
         if rc:
             raise W2Error(rc, self.L.wolfd2gpu_ens_error(self.h).decode())
 
-    def step(self, params: Sequence[RunParams], nsteps: int = 1, refine_sweeps: int = 0) -> List[List[tuple]]:
-        """nsteps mixed steps of every case; returns per case the records
-        (nQLiter, nSorConv, dif, divmax) of each step."""
+    def step(self, params: Sequence[RunParams], nsteps: int = 1, refine_sweeps: int = 0,
+             precision: int = PREC_MIXED) -> List[List[tuple]]:
+        """nsteps steps of every case in `precision` (PREC_MIXED or
+        PREC_FP64); returns per case the records (nQLiter, nSorConv, dif,
+        divmax) of each step."""
         n = len(self.solvers)
         if len(params) != n:
             raise ValueError("one RunParams per case")
-        pr = (Params * n)(*[Params.of(p, precision=PREC_MIXED, refine_sweeps=refine_sweeps) for p in params])
+        pr = (Params * n)(*[Params.of(p, precision=precision, refine_sweeps=refine_sweeps) for p in params])
         st = (StepStat * max(n * nsteps, 1))()
         self._check(self.L.wolfd2gpu_ens_step(self.h, pr, nsteps, st))
         return [[(x.nQLiter, x.nSorConv, tuple(x.dif), x.divmax) for x in st[k * nsteps:(k + 1) * nsteps]]
                 for k in range(n)]
 
     STAGES = ("ke_copy_mixed", "ke_naux32", "ke_bc", "ke_ppe_mixed", "ke_step_post")
+    STAGES_FP64 = ("ke_copy3", "ke_naux", "ke_bc", "ke_ppe", "ke_step_post")
 
     def profile(self, enable: bool = True) -> None:
         """Per-stage CUDA-event timing of direct launches (graph replay is
         not profiled); enabling resets the sums."""
         self._check(self.L.wolfd2gpu_ens_profile(self.h, 1 if enable else 0))
 
-    def profile_read(self) -> dict:
+    def profile_read(self, mixed: bool = True) -> dict:
+        """Stage sums keyed by the kernel names of the mixed or plain step."""
         out = {}
-        for k, name in enumerate(self.STAGES):
+        for k, name in enumerate(self.STAGES if mixed else self.STAGES_FP64):
             ms, n = C.c_double(), C.c_longlong()
             self._check(self.L.wolfd2gpu_ens_profile_read(self.h, k, C.byref(ms), C.byref(n)))
             out[name] = (ms.value, n.value)
