@@ -101,7 +101,9 @@ int wolfd2gpu_grid_metric(w2_ctx *ctx, const double *gx, const double *gy,
 
 /* nAuxMomentum, src/momentum.f:33-48: returns the number of Q-L iterations
  * (or -1) through *nQLiter.  Metric arguments are accepted for signature
- * parity and ignored: the copies uploaded at set-up are used. */
+ * parity and ignored: the copies uploaded at set-up are used.  Non-zero
+ * density d, dn (EqState output) adds the buoyancy term of YMomentum
+ * (momentum.f:703, divided by fr); d = dn = NULL means zero density. */
 int wolfd2gpu_naux_momentum(w2_ctx *ctx, const int *nx, const int *ny,
                             const int *mqiter, const double *dk,
                             const double *re, const double *fr,
@@ -142,6 +144,35 @@ int wolfd2gpu_diff_max_norm(w2_ctx *ctx, const int *nx, const int *ny,
 /* Filter, src/utility.f:33-36, velocity components (ncomp 1 = u, 2 = v). */
 int wolfd2gpu_filter(w2_ctx *ctx, const int *nx, const int *ny,
                      const int *ncomp, const double *fp, double *qu);
+
+/* ---- Thermal energy (drop-ins; main.f:839-855 with nthermen = 1) --------
+ * Thermal region tables as the reference passes them: nTRgType(mgri,mgrj)
+ * (0 no source, 1 heat generation, 2 fixed temperature), nTemBdTp(mgri,mgrj,4)
+ * (0 interface, 1 fixed temperature, 2 heat flux), dTRgVal(mgri,mgrj),
+ * dHGSTval(mgri,mgrj); face temperatures are dBCVal(...,4) given to
+ * wolfd2gpu_create.  An unknown flag returns W2_E_BCFLAG (the reference
+ * stops).  Metric arguments are the uploaded ones. */
+
+/* TempBoundCond, src/bound_cond.f:1030-1033. */
+int wolfd2gpu_temp_bound_cond(w2_ctx *ctx, const int *nx, const int *ny,
+                              const int *nTRgType, const int *nTemBdTp,
+                              const double *dTRgVal, double *t);
+
+/* ThermEnergy, src/thermal.f:24-34: t (the starred temperature) updated in
+ * place from un, vn, u, v, tn. */
+int wolfd2gpu_therm_energy(w2_ctx *ctx, const int *nx, const int *ny,
+                           const int *nTRgType, const int *nTemBdTp,
+                           const double *dk, const double *pe,
+                           const double *dTRgVal, const double *dHGSTval,
+                           const double *un, const double *vn, const double *u,
+                           const double *v, const double *tn, double *t);
+
+/* EqState, src/thermal.f:288-290: den on i, j = 2..n (other entries kept). */
+int wolfd2gpu_eq_state(w2_ctx *ctx, const int *nx, const int *ny,
+                       const double *uref, const double *densref,
+                       const double *tmax, const double *tref,
+                       const double *rconst, const double *p, const double *t,
+                       double *den);
 
 /* ---- Device-resident time loop ---------------------------------------- */
 

@@ -4,7 +4,8 @@
 No Fortran compiler exists on the build machine or the GPU machines, so the
 reference cannot be compiled as written.  This module reads the reference's
 own source files (src/momentum.f, src/pressure.f, src/utility.f,
-src/bound_cond.f, src/grid.f plus include/config.f and include/wolfd2.h)
+src/bound_cond.f, src/grid.f, src/thermal.f plus include/config.f and
+include/wolfd2.h)
 where the reference tree is mounted, and translates the routines of the hot
 path statement by statement into C: same loops, same expressions with the
 Fortran evaluation order made explicit by parentheses, static storage for
@@ -40,8 +41,9 @@ ROUTINES = {
     "src/pressure.f": ["ppe", "divergence", "rhsppe", "sor", "sorrb", "sorrbp", "slor",
                        "slorrb", "slorrbp"],
     "src/utility.f": ["filter", "project", "diffmaxnorm", "dmaxnorm"],
-    "src/bound_cond.f": ["velboundcond", "presboundcond", "veloutflowbcs"],
+    "src/bound_cond.f": ["velboundcond", "presboundcond", "veloutflowbcs", "tempboundcond"],
     "src/grid.f": ["mirrorpts", "fullgrid", "metric"],
+    "src/thermal.f": ["thermenergy", "eqstate"],
 }
 
 STACK_LIMIT = 65536  # gfortran -fmax-stack-var-size default: larger locals are static

@@ -110,7 +110,8 @@ void FN(w2o_alt_trid_lu)(int n, REAL *a, REAL *b) {
 #undef B
 }
 
-/* ConvCoef, momentum.f:864-981 (cases 1, 2, 4, 5). */
+/* ConvCoef, momentum.f:864-981 (cases 1, 2, 4, 5 of the momentum
+ * equations; 3 and 6 of the thermal energy equation). */
 static void FN(conv_coef)(w2o_ctx *c, int nx, int ny, int ncomp, int njacob,
                       const REAL *xzi, const REAL *xet, const REAL *yzi,
                       const REAL *yet, const REAL *u, const REAL *v,
@@ -159,6 +160,26 @@ static void FN(conv_coef)(w2o_ctx *c, int nx, int ny, int ncomp, int njacob,
           F(cc2, i, j) = djac * F(xzi, i, j) * F(v, i, j) -
                          F(yzi, i, j) * (F(u, i, j + 1) + F(u, i - 1, j + 1) +
                                          F(u, i, j) + F(u, i - 1, j)) / R(4.0);
+        }
+      break;
+    case 3:
+      for (j = 1; j <= ny; j++)
+        for (i = 1; i <= nx; i++) {
+          F(cc1, i, j) = (F(yet, i, j) * F(u, i, j) -
+                          F(xet, i, j) * (F(v, i + 1, j) + F(v, i, j) + F(v, i + 1, j - 1) +
+                                          F(v, i, j - 1)) / R(4.0)) * R(0.5);
+          F(cc2, i, j) = (F(xzi, i, j) * F(v, i, j) -
+                          F(yzi, i, j) * (F(u, i, j + 1) + F(u, i - 1, j + 1) + F(u, i, j) +
+                                          F(u, i - 1, j)) / R(4.0)) * R(0.5);
+        }
+      break;
+    case 6:
+      for (j = 1; j <= ny + 1; j++)
+        for (i = 1; i <= nx + 1; i++) {
+          F(cc1, i, j) = (F(yet, i, j) * (F(u, i, j) + F(u, i - 1, j)) -
+                          F(xet, i, j) * (F(v, i, j) + F(v, i, j - 1))) * R(0.5);
+          F(cc2, i, j) = (F(xzi, i, j) * (F(v, i, j) + F(v, i, j - 1)) -
+                          F(yzi, i, j) * (F(u, i, j) + F(u, i - 1, j))) * R(0.5);
         }
       break;
     default:
@@ -548,7 +569,7 @@ int FN(w2o_naux_momentum)(w2o_ctx *c, int nx, int ny, int mqiter,
       }
     REAL d1 = FN(w2o_dmax_norm)(c, nx, ny, c->MOM_DUS);
     REAL d2 = FN(w2o_dmax_norm)(c, nx, ny, c->MOM_DVS);
-    REAL difmax = d1 > d2 ? d1 : d2;
+    REAL difmax = d2 > d1 ? d2 : d1;  /* max(dif(1),dif(2)): dif(1) unless dif(2) is larger */
     if (difmax <= qtol) return mm;
   }
   return -1;

@@ -39,6 +39,10 @@ class _Metrics(C.Structure):
     _fields_ = [(n, _dp) for n in METRIC_NAMES]
 
 
+class _Thermal(C.Structure):
+    _fields_ = [("nTRgType", _ip), ("nTemBdTp", _ip), ("dTRgVal", _dp), ("dHGSTval", _dp)]
+
+
 _fp = C.POINTER(C.c_float)
 
 
@@ -100,6 +104,12 @@ def lib():
             L.w2o_dmax_norm.restype = C.c_double
             L.w2o_dmax_norm.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp]
             L.w2o_alt_trid_lu.argtypes = [C.c_int, _dp, _dp]
+            L.w2o_temp_bound_cond.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions),
+                                              C.POINTER(_Thermal), _dp]
+            L.w2o_therm_energy.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions),
+                                           C.POINTER(_Thermal), C.c_double, C.c_double,
+                                           C.POINTER(_Metrics), _dp, _dp, _dp, _dp, _dp, _dp]
+            L.w2o_eq_state.argtypes = [C.c_void_p, C.c_int, C.c_int] + [C.c_double] * 5 + [_dp, _dp, _dp]
             L.w2o_cold_start.restype = C.c_int
             L.w2o_cold_start.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions),
                                          C.POINTER(_Params), C.POINTER(_Metrics), C.POINTER(_Fields)]
@@ -240,6 +250,29 @@ class Oracle:
     def filter(self, nx, ny, ncomp, regs, fp, q) -> None:
         rs = self.regions_struct(regs)
         self.L.w2o_filter(self.h, nx, ny, ncomp, C.byref(rs), fp, _ptr(q))
+
+    @staticmethod
+    def thermal_struct(th) -> _Thermal:
+        """th: an object with nTRgType (mgri, mgrj), nTemBdTp (mgri, mgrj, 4),
+        dTRgVal and dHGSTval (mgri, mgrj), Fortran-ordered."""
+        ia = [np.asfortranarray(getattr(th, n), np.int32) for n in ("nTRgType", "nTemBdTp")]
+        da = [np.asfortranarray(getattr(th, n), np.float64) for n in ("dTRgVal", "dHGSTval")]
+        s = _Thermal(*[_ptr(a, C.c_int) for a in ia], *[_ptr(a) for a in da])
+        s._keep = (ia, da)
+        return s
+
+    def temp_bound_cond(self, nx, ny, regs, th, t) -> None:
+        rs, ts = self.regions_struct(regs), self.thermal_struct(th)
+        self.L.w2o_temp_bound_cond(self.h, nx, ny, C.byref(rs), C.byref(ts), _ptr(t))
+
+    def therm_energy(self, nx, ny, regs, th, dk, pe, met, un, vn, u, v, tn, t) -> None:
+        rs, ts = self.regions_struct(regs), self.thermal_struct(th)
+        self.L.w2o_therm_energy(self.h, nx, ny, C.byref(rs), C.byref(ts), dk, pe,
+                                C.byref(self.metrics_struct(met)), _ptr(un), _ptr(vn), _ptr(u),
+                                _ptr(v), _ptr(tn), _ptr(t))
+
+    def eq_state(self, nx, ny, uref, densref, tmax, tref, rconst, p, t, den) -> None:
+        self.L.w2o_eq_state(self.h, nx, ny, uref, densref, tmax, tref, rconst, _ptr(p), _ptr(t), _ptr(den))
 
     def diff_max_norm(self, nx, ny, un, u) -> float:
         return self.L.w2o_diff_max_norm(self.h, nx, ny, _ptr(un), _ptr(u))

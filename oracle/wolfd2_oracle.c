@@ -22,6 +22,8 @@ enum { BM_INTERN = 0, BM_WALL1 = 1, BM_WALL2 = 2, BM_INLET = 3,
        BM_OUTLT1 = 4, BM_OUTLT2 = 5 };
 enum { WEST = 1, EAST = 2, SOUTH = 3, NORTH = 4 };
 enum { VU = 1, VV = 2, VP = 3, VT = 4 };
+enum { RT_NOSRCE = 0, RT_HEATGN = 1, RT_TEMPER = 2 };
+enum { BT_INTERN = 0, BT_TEMPER = 1, BT_HTFLUX = 2 };
 
 /* Persistent work storage (the reference's static locals). */
 typedef struct {
@@ -51,6 +53,8 @@ struct w2o_ctx {
   double *xu, *yu, *xv, *yv, *xc, *yc; /* Grid statics              */
   double *lin;             /* aline/bline/plold for the line solvers   */
   double *rbp_dif;         /* SorRBP dif(0:nx+1,0:ny+1)                */
+  double *th_cu1, *th_cv1, *th_cun, *th_cvn, *th_s; /* ThermEnergy statics */
+  double *th_a, *th_b;     /* ThermEnergy a(3,mn), b(mn)               */
 };
 
 #define IX(i, j) ((size_t)(i) + (size_t)(j) * c->ld)
@@ -147,6 +151,10 @@ w2o_ctx *w2o_create(int mnx, int mny) {
   size_t mnl = (size_t)(mnx > mny ? mnx : mny);
   c->lin = zalloc(5 * mnl);
   c->rbp_dif = zalloc(c->nf);
+  c->th_cu1 = zalloc(c->nf); c->th_cv1 = zalloc(c->nf);
+  c->th_cun = zalloc(c->nf); c->th_cvn = zalloc(c->nf);
+  c->th_s = zalloc(c->nf);
+  c->th_a = zalloc(3 * c->mn); c->th_b = zalloc(c->mn);
   return c;
 }
 
@@ -158,6 +166,8 @@ void w2o_destroy(w2o_ctx *c) {
   free(c->dus); free(c->dvs); free(c->div); free(c->pa); free(c->pb);
   free(c->rbp_pn); free(c->qh); free(c->xu); free(c->yu); free(c->xv);
   free(c->yv); free(c->xc); free(c->yc); free(c->lin); free(c->rbp_dif);
+  free(c->th_cu1); free(c->th_cv1); free(c->th_cun); free(c->th_cvn);
+  free(c->th_s); free(c->th_a); free(c->th_b);
   free(c);
 }
 
@@ -338,6 +348,188 @@ double w2o_diff_max_norm(w2o_ctx *c, int nx, int ny, const double *un,
 #undef MOM_WY
 #undef MOM_DUS
 #undef MOM_DVS
+
+/* ------------------------------------------------------------------ */
+/* thermal.f and TempBoundCond                                         */
+/* ------------------------------------------------------------------ */
+
+#define TRT(t, r, ir, jr) (t)->nTRgType[((ir)-1) + ((jr)-1) * (r)->mgri]
+#define TBT(t, r, ir, jr, s) \
+  (t)->nTemBdTp[((ir)-1) + ((jr)-1) * (r)->mgri + ((s)-1) * (r)->mgri * (r)->mgrj]
+#define TRV(arr, r, ir, jr) (arr)[((ir)-1) + ((jr)-1) * (r)->mgri]
+
+/* TempBoundCond, bound_cond.f:1030-1186: fixed-temperature regions (interior
+ * value, then image points across each face), else per face: interface,
+ * fixed temperature (image) or heat flux (ghost = value + inner). */
+void w2o_temp_bound_cond(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                         const w2o_thermal *th, double *t) {
+  (void)nx; (void)ny;
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      const int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      const int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      int i, j;
+      if (TRT(th, r, ireg, jreg) == RT_TEMPER) {
+        const double tv = TRV(th->dTRgVal, r, ireg, jreg);
+        for (j = jS + 1; j <= jN; j++)
+          for (i = iW + 1; i <= iE; i++) F(t, i, j) = tv;
+        for (j = jS + 1; j <= jN; j++) F(t, iW + 1, j) = 2.0 * BCV(r, ireg, jreg, WEST, VT) - F(t, iW, j);
+        for (j = jS + 1; j <= jN; j++) F(t, iE, j) = 2.0 * BCV(r, ireg, jreg, EAST, VT) - F(t, iE + 1, j);
+        for (i = iW + 1; i <= iE; i++) F(t, i, jS + 1) = 2.0 * BCV(r, ireg, jreg, SOUTH, VT) - F(t, i, jS);
+        for (i = iW + 1; i <= iE; i++) F(t, i, jN) = 2.0 * BCV(r, ireg, jreg, NORTH, VT) - F(t, i, jN + 1);
+        continue;
+      }
+      switch (TBT(th, r, ireg, jreg, WEST)) {
+        case BT_INTERN: break;
+        case BT_TEMPER:
+          for (j = jS + 1; j <= jN; j++) F(t, iW, j) = 2.0 * BCV(r, ireg, jreg, WEST, VT) - F(t, iW + 1, j);
+          break;
+        case BT_HTFLUX:
+          for (j = jS + 1; j <= jN; j++) F(t, iW, j) = BCV(r, ireg, jreg, WEST, VT) + F(t, iW + 1, j);
+          break;
+        default: die("Wrong nTemBdTp W flag", ireg, jreg);
+      }
+      switch (TBT(th, r, ireg, jreg, EAST)) {
+        case BT_INTERN: break;
+        case BT_TEMPER:
+          for (j = jS + 1; j <= jN; j++) F(t, iE + 1, j) = 2.0 * BCV(r, ireg, jreg, EAST, VT) - F(t, iE, j);
+          break;
+        case BT_HTFLUX:
+          for (j = jS + 1; j <= jN; j++) F(t, iE + 1, j) = BCV(r, ireg, jreg, EAST, VT) + F(t, iE, j);
+          break;
+        default: die("Wrong nTemBdTp E flag", ireg, jreg);
+      }
+      switch (TBT(th, r, ireg, jreg, SOUTH)) {
+        case BT_INTERN: break;
+        case BT_TEMPER:
+          for (i = iW + 1; i <= iE; i++) F(t, i, jS) = 2.0 * BCV(r, ireg, jreg, SOUTH, VT) - F(t, i, jS + 1);
+          break;
+        case BT_HTFLUX:
+          for (i = iW + 1; i <= iE; i++) F(t, i, jS) = BCV(r, ireg, jreg, SOUTH, VT) + F(t, i, jS + 1);
+          break;
+        default: die("Wrong nTemBdTp S flag", ireg, jreg);
+      }
+      switch (TBT(th, r, ireg, jreg, NORTH)) {
+        case BT_INTERN: break;
+        case BT_TEMPER:
+          for (i = iW + 1; i <= iE; i++) F(t, i, jN + 1) = 2.0 * BCV(r, ireg, jreg, NORTH, VT) - F(t, i, jN);
+          break;
+        case BT_HTFLUX:
+          for (i = iW + 1; i <= iE; i++) F(t, i, jN + 1) = BCV(r, ireg, jreg, NORTH, VT) + F(t, i, jN);
+          break;
+        default: die("Wrong nTemBdTp N flag", ireg, jreg);
+      }
+    }
+}
+
+/* ThermEnergy, thermal.f:24-280.  Two split steps on ONE chain of the
+ * (nx-1)(ny-1) interior points in i-fastest order (ind = (j-2)(nx-1)+i-1)
+ * for both splits: split 1 holds the upwinded i-direction rows, split 2 the
+ * j-direction coefficients on the same i-fastest chain, as the reference
+ * writes them, with identity rows in fixed-temperature regions. */
+void w2o_therm_energy(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                      const w2o_thermal *th, double dk, double pe,
+                      const w2o_metrics *m, const double *un, const double *vn,
+                      const double *u, const double *v, const double *tn,
+                      double *t) {
+  double *cu1 = c->th_cu1, *cv1 = c->th_cv1, *cun = c->th_cun, *cvn = c->th_cvn, *sg = c->th_s;
+  double *a = c->th_a, *b = c->th_b;
+#define TA(k, ind) a[((k)-1) + 3 * (size_t)((ind)-1)]
+#define TB(ind) b[(ind)-1]
+  const double pe1 = 1.0 / pe;
+  int i, j;
+  w2o_temp_bound_cond(c, nx, ny, r, th, t);
+  conv_coef(c, nx, ny, 6, 0, m->xzc, m->xec, m->yzc, m->yec, u, v, cu1, cv1);
+  conv_coef(c, nx, ny, 3, 0, m->xzv, m->xeu, m->yzv, m->yeu, un, vn, cun, cvn);
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      const int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      const int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      const double sv = TRT(th, r, ireg, jreg) == RT_HEATGN ? TRV(th->dHGSTval, r, ireg, jreg) : 0.0;
+      for (j = jS + 1; j <= jN; j++)
+        for (i = iW + 1; i <= iE; i++) F(sg, i, j) = sv;
+    }
+  /* split 1 */
+  for (j = 2; j <= ny; j++)
+    for (i = 2; i <= nx; i++) {
+      const int ind = (j - 2) * (nx - 1) + i - 1;
+      const double rkj = dk * F(m->djc, i, j) * 0.5;
+      const double rw = F(m->rau, i - 1, j), ro = F(m->rau, i, j);
+      if (F(cu1, i, j) >= 0.0) {
+        TA(1, ind) = rkj * (-F(cu1, i - 1, j) - pe1 * rw);
+        TA(2, ind) = 1.0 + rkj * (F(cu1, i, j) + pe1 * (ro + rw));
+        TA(3, ind) = rkj * (-pe1 * ro);
+      } else {
+        TA(1, ind) = rkj * (-pe1 * rw);
+        TA(2, ind) = 1.0 + rkj * (-F(cu1, i, j) + pe1 * (ro + rw));
+        TA(3, ind) = rkj * (F(cu1, i + 1, j) - pe1 * ro);
+      }
+      const double cc = -F(cvn, i, j - 1) * F(tn, i, j - 1) - F(cun, i - 1, j) * F(tn, i - 1, j) +
+                        (F(cun, i, j) - F(cun, i - 1, j) + F(cvn, i, j) - F(cvn, i, j - 1)) * F(tn, i, j) +
+                        F(cun, i, j) * F(tn, i + 1, j) + F(cvn, i, j) * F(tn, i, j + 1);
+      const double dd =
+          F(m->rau, i, j) * (F(tn, i + 1, j) - F(tn, i, j)) -
+          F(m->rau, i - 1, j) * (F(tn, i, j) - F(tn, i - 1, j)) +
+          F(m->rbu, i, j) * (F(tn, i + 1, j + 1) + F(tn, i, j + 1) - F(tn, i + 1, j - 1) - F(tn, i, j - 1)) -
+          F(m->rbu, i - 1, j) * (F(tn, i, j + 1) + F(tn, i - 1, j + 1) - F(tn, i, j - 1) - F(tn, i - 1, j - 1)) +
+          F(m->rbv, i, j) * (F(tn, i + 1, j + 1) + F(tn, i + 1, j) - F(tn, i - 1, j + 1) - F(tn, i - 1, j)) -
+          F(m->rbv, i, j - 1) * (F(tn, i + 1, j) + F(tn, i + 1, j - 1) - F(tn, i - 1, j) - F(tn, i - 1, j - 1)) +
+          F(m->rgv, i, j) * (F(tn, i, j + 1) - F(tn, i, j)) -
+          F(m->rgv, i, j - 1) * (F(tn, i, j) - F(tn, i, j - 1));
+      TB(ind) = dk * F(sg, i, j) * 0.5 + 2.0 * rkj * (-cc + pe1 * dd);
+    }
+  w2o_alt_trid_lu((nx - 1) * (ny - 1), a, b);
+  /* split 2: same chain order, j-direction coefficients */
+  for (j = 2; j <= ny; j++)
+    for (i = 2; i <= nx; i++) {
+      const int ind = (j - 2) * (nx - 1) + i - 1;
+      const double rkj = dk * F(m->djc, i, j) * 0.5;
+      const double rs = F(m->rgv, i, j - 1), ro = F(m->rgv, i, j);
+      if (F(cv1, i, j) >= 0.0) {
+        TA(1, ind) = rkj * (-F(cv1, i, j - 1) - pe1 * rs);
+        TA(2, ind) = 1.0 + rkj * (F(cv1, i, j) + pe1 * (ro + rs));
+        TA(3, ind) = rkj * (-pe1 * ro);
+      } else {
+        TA(1, ind) = rkj * (-pe1 * rs);
+        TA(2, ind) = 1.0 + rkj * (-F(cv1, i, j) + pe1 * (ro + rs));
+        TA(3, ind) = rkj * (F(cv1, i, j + 1) - pe1 * ro);
+      }
+    }
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      if (TRT(th, r, ireg, jreg) != RT_TEMPER) continue;
+      const int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      const int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      for (j = jS + 1; j <= jN; j++)
+        for (i = iW + 1; i <= iE; i++) {
+          const int ind = (j - 2) * (nx - 1) + i - 1;
+          TA(1, ind) = 0.0;
+          TA(2, ind) = 1.0;
+          TA(3, ind) = 0.0;
+          TB(ind) = 0.0;
+        }
+    }
+  w2o_alt_trid_lu((nx - 1) * (ny - 1), a, b);
+  for (j = 2; j <= ny; j++)
+    for (i = 2; i <= nx; i++) F(t, i, j) = F(t, i, j) + TB((j - 2) * (nx - 1) + i - 1);
+#undef TA
+#undef TB
+}
+
+/* EqState, thermal.f:288-329: den = (p densref uref^2 + pref) /
+ * (densref rconst (t (tmax - tref) + tref)) - 1 on i, j = 2..n, flushed to
+ * zero below 1e-10 in magnitude. */
+void w2o_eq_state(w2o_ctx *c, int nx, int ny, double uref, double densref, double tmax,
+                  double tref, double rconst, const double *p, const double *t, double *den) {
+  const double pref = densref * rconst * tref;
+  for (int j = 2; j <= ny; j++)
+    for (int i = 2; i <= nx; i++) {
+      const double c1 = F(p, i, j) * densref * (uref * uref) + pref;
+      const double c2 = densref * rconst * (F(t, i, j) * (tmax - tref) + tref);
+      F(den, i, j) = c1 / c2 - 1.0;
+      if (fabs(F(den, i, j)) < 1.0e-10) F(den, i, j) = 0.0;
+    }
+}
 
 /* ------------------------------------------------------------------ */
 /* pressure.f                                                          */

@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
  * Fortran routines on the hot path (momentum.f, pressure.f, utility.f,
- * bound_cond.f and the time-loop body of main.f).  It exists so the tests,
+ * bound_cond.f, thermal.f and the time-loop body of main.f).  It exists so the tests,
  * the smoke check and the CPU-baseline leg of the benchmark can check the
  * CUDA library against an independent implementation.  Nothing in the
  * product (wolfd2_gb300/, include/) links or calls it.
@@ -126,6 +126,33 @@ void w2o_filter(w2o_ctx *c, int nx, int ny, int ncomp, const w2o_regions *r,
 double w2o_diff_max_norm(w2o_ctx *c, int nx, int ny, const double *un,
                          const double *u);
 double w2o_dmax_norm(w2o_ctx *c, int nx, int ny, const double *u);
+
+/* Thermal region and boundary tables, Fortran layout (mgri, mgrj of the
+ * regions): nTRgType(mgri,mgrj) (RT_NOSRCE 0, RT_HEATGN 1, RT_TEMPER 2),
+ * nTemBdTp(mgri,mgrj,4) (BT_INTERN 0, BT_TEMPER 1, BT_HTFLUX 2),
+ * dTRgVal(mgri,mgrj), dHGSTval(mgri,mgrj).  Face values are dBCVal's
+ * variable 4 (_T_). */
+typedef struct {
+  const int *nTRgType;
+  const int *nTemBdTp;
+  const double *dTRgVal;
+  const double *dHGSTval;
+} w2o_thermal;
+
+/* bound_cond.f:1030-1186 */
+void w2o_temp_bound_cond(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                         const w2o_thermal *th, double *t);
+
+/* thermal.f:24-280 (t: the starred temperature, updated in place) */
+void w2o_therm_energy(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                      const w2o_thermal *th, double dk, double pe,
+                      const w2o_metrics *m, const double *un, const double *vn,
+                      const double *u, const double *v, const double *tn,
+                      double *t);
+
+/* thermal.f:288-329 */
+void w2o_eq_state(w2o_ctx *c, int nx, int ny, double uref, double densref, double tmax,
+                  double tref, double rconst, const double *p, const double *t, double *den);
 
 /* momentum.f:1307-1339 (exported for unit tests) */
 void w2o_alt_trid_lu(int n, double *a /* a(3,n) */, double *b);

@@ -1,0 +1,139 @@
+"""GPU parity of the thermal drop-ins (ThermEnergy, TempBoundCond, EqState)
+and of the buoyancy term of nAuxMomentum against the CPU oracle: bit-for-bit
+equal fields on a curvilinear 3 x 2 region layout with fixed-temperature and
+heat-generating regions and fixed-temperature / heat-flux faces."""
+import numpy as np
+import pytest
+
+import oracle as O
+import thermal_setup
+from wolfd2_gb300 import deck
+from wolfd2_gb300.gpu import Solver, W2Error
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(seed=5):
+    case, th, f = thermal_setup.problem(seed=seed)
+    s = Solver.for_case(case, tuned=False)
+    o = O.Oracle(case.nx + 1, case.ny + 1)
+    met = o.grid(case.nx, case.ny, case.x, case.y)
+    return case, th, f, s, o, met
+
+
+@pytest.mark.parametrize("pe,dk", [(50.0, 0.004), (3.0, 0.02)])
+def test_therm_energy_bitwise(pe, dk):
+    case, th, f, s, o, met = _setup()
+    tg, to = f["t"].copy(order="F"), f["t"].copy(order="F")
+    s.ThermEnergy(th, dk, pe, f["un"], f["vn"], f["u"], f["v"], f["tn"], tg)
+    o.therm_energy(case.nx, case.ny, case.regions, th, dk, pe, met, f["un"], f["vn"], f["u"], f["v"],
+                   f["tn"], to)
+    assert np.isfinite(to).all()
+    assert np.array_equal(tg, to), float(np.max(np.abs(tg - to)))
+    s.close()
+
+
+def test_therm_energy_single_region_cavity():
+    """One region (the whole cavity), hot west wall, adiabatic others, a heat
+    source everywhere: the chain couples every row through its end rows."""
+    case = deck.cavity(48, 100.0, 0.005, solver="rb_sor")
+    th = deck.Thermal.empty()
+    th.nTRgType[0, 0] = deck.RT_HEATGN
+    th.dHGSTval[0, 0] = 0.05
+    th.nTemBdTp[0, 0, :] = (deck.BT_TEMPER, deck.BT_HTFLUX, deck.BT_HTFLUX, deck.BT_HTFLUX)
+    case.regions.dBCVal[0, 0, deck.WEST - 1, deck.VAR_T - 1] = 1.0
+    s = Solver.for_case(case, tuned=False)
+    o = O.Oracle(case.nx + 1, case.ny + 1)
+    met = o.grid(case.nx, case.ny, case.x, case.y)
+    u, v, p = deck.perturbation_ic(case, 3, amp=0.05)
+    rng = np.random.default_rng(4)
+    tn = np.asfortranarray(rng.uniform(0.0, 1.0, size=u.shape))
+    tg, to = tn.copy(order="F"), tn.copy(order="F")
+    s.ThermEnergy(th, 0.005, 70.0, u, v, u, v, tn, tg)
+    o.therm_energy(case.nx, case.ny, case.regions, th, 0.005, 70.0, met, u, v, u, v, tn, to)
+    assert np.array_equal(tg, to)
+    s.close()
+
+
+def test_temp_bound_cond_and_eq_state_bitwise():
+    case, th, f, s, o, met = _setup(seed=9)
+    a, b = f["t"].copy(order="F"), f["t"].copy(order="F")
+    s.TempBoundCond(th, a)
+    o.temp_bound_cond(case.nx, case.ny, case.regions, th, b)
+    assert np.array_equal(a, b)
+    t = np.asfortranarray(0.5 + 0.4 * np.tanh(f["tn"]))
+    kw = (1.3, 1.1, 350.0, 290.0, 287.0)
+    dg, do = np.asfortranarray(f["u"].copy()), np.asfortranarray(f["u"].copy())
+    s.EqState(*kw, f["p"], t, dg)
+    o.eq_state(case.nx, case.ny, *kw, f["p"], t, do)
+    assert np.array_equal(dg, do) and np.count_nonzero(do[2:case.nx + 1, 2:case.ny + 1]) > 0
+    s.close()
+
+
+def test_bad_thermal_flag_is_an_error():
+    case, th, f, s, o, met = _setup()
+    th.nTemBdTp[0, 0, 0] = 7
+    with pytest.raises(W2Error):
+        s.TempBoundCond(th, f["t"].copy(order="F"))
+    s.close()
+
+
+def _momentum_inputs(o, case, f, amp=0.1):
+    """Smooth velocities made consistent with the boundary conditions, and
+    the densities of EqState at two temperatures."""
+    nx, ny = case.nx, case.ny
+    u, v = np.asfortranarray(amp * f["u"]), np.asfortranarray(amp * f["v"])
+    o.vel_bound_cond(nx, ny, case.regions, u, v)
+    t = np.asfortranarray(0.5 + 0.4 * np.tanh(f["tn"]))
+    tn = np.asfortranarray(0.5 + 0.4 * np.tanh(f["t"]))
+    den, denn = o.field(), o.field()
+    o.eq_state(nx, ny, 1.0, 1.0, 320.0, 290.0, 287.0, f["p"], t, den)
+    o.eq_state(nx, ny, 1.0, 1.0, 320.0, 290.0, 287.0, f["p"], tn, denn)
+    return u, v, den, denn
+
+
+@pytest.mark.parametrize("buoyant", [False, True])
+def test_momentum_multiregion_curvilinear(buoyant):
+    """nAuxMomentum on the 3 x 2 curvilinear layout, with and without the
+    buoyancy term of the density from EqState."""
+    case, th, f, s, o, met = _setup()
+    nx, ny = case.nx, case.ny
+    u, v, den, denn = _momentum_inputs(o, case, f)
+    assert np.count_nonzero(den) > 0
+    prm = dataclasses_replace(case.params, fr=0.37)
+    dg, dng = (den, denn) if buoyant else (None, None)
+    do, dno = (den, denn) if buoyant else (o.field(), o.field())
+    usg, vsg = u.copy(order="F"), v.copy(order="F")
+    uso, vso = u.copy(order="F"), v.copy(order="F")
+    ng = s.nAuxMomentum(prm.mqiter, prm.dk, prm.re, prm.fr, prm.qtol, dg, dng, u, v, usg, vsg)
+    no = o.naux_momentum(nx, ny, case.regions, prm, met, do, dno, u, v, uso, vso)
+    assert ng == no and ng > 0
+    assert np.array_equal(usg, uso) and np.array_equal(vsg, vso)
+    if buoyant:
+        # the term is live: zero density gives a different v
+        us0, vs0 = u.copy(order="F"), v.copy(order="F")
+        s.nAuxMomentum(prm.mqiter, prm.dk, prm.re, prm.fr, prm.qtol, None, None, u, v, us0, vs0)
+        assert not np.array_equal(vs0, vsg)
+    s.close()
+
+
+def test_momentum_divergence_reported_like_reference():
+    """Velocities far from their boundary values drive the Newton-Kantorovich
+    iteration to NaN: the run is not converged (-1), as in the reference,
+    and the NaN fields agree with the oracle's."""
+    case, th, f, s, o, met = _setup()
+    nx, ny = case.nx, case.ny
+    u, v, p = deck.perturbation_ic(case, 11, amp=0.05)
+    prm = case.params
+    usg, vsg = u.copy(order="F"), v.copy(order="F")
+    uso, vso = u.copy(order="F"), v.copy(order="F")
+    ng = s.nAuxMomentum(prm.mqiter, prm.dk, prm.re, prm.fr, prm.qtol, None, None, u, v, usg, vsg)
+    no = o.naux_momentum(nx, ny, case.regions, prm, met, o.field(), o.field(), u, v, uso, vso)
+    assert no == -1 and ng == -1
+    assert np.array_equal(usg, uso, equal_nan=True) and np.array_equal(vsg, vso, equal_nan=True)
+    s.close()
+
+
+def dataclasses_replace(p, **kw):
+    import dataclasses
+    return dataclasses.replace(p, **kw)

@@ -73,3 +73,57 @@ def test_named_dt_diverges_at_1024():
     r = refrun.RefRun(case, fields={"u": u, "v": v, "p": p}, cold_start=False)
     h = r.step(1)
     assert h[0] == -1 and not np.isfinite(r.f["u"]).all()
+
+
+def _thermal_tables(th):
+    return dict(ntrgtype=np.asfortranarray(th.nTRgType, np.int32),
+                ntembdtp=np.asfortranarray(th.nTemBdTp, np.int32),
+                dtrgval=np.asfortranarray(th.dTRgVal), dhgstval=np.asfortranarray(th.dHGSTval))
+
+
+@pytest.mark.parametrize("pe", [50.0, 7.0])
+def test_thermal_energy_bitwise(pe):
+    """ThermEnergy (with its TempBoundCond and ConvCoef cases 3 and 6) on a
+    curvilinear 3 x 2 region layout with fixed-temperature and heat-generating
+    regions, fixed-temperature and heat-flux faces."""
+    import thermal_setup
+    case, th, f = thermal_setup.problem()
+    f77ref.build(case.nx + 1, case.ny + 1)
+    r = refrun.RefRun(case, cold_start=False)
+    o = O.Oracle(case.nx + 1, case.ny + 1)
+    met = o.grid(case.nx, case.ny, case.x, case.y)
+    for k in refrun.METRICS:
+        assert np.array_equal(met[k], r.m[k]), k
+    t_ref, t_or = f["t"].copy(order="F"), f["t"].copy(order="F")
+    m = r.m
+    r.R("thermenergy", nx=case.nx, ny=case.ny, nreg=r.tab["nreg"], nregbrd=r.tab["nregbrd"],
+        **_thermal_tables(th), dk=0.004, pe=pe, dbcval=r.tab["dbcval"],
+        rau=m["rau"], rbu=m["rbu"], rbv=m["rbv"], rgv=m["rgv"], djc=m["djc"],
+        xeu=m["xeu"], yeu=m["yeu"], xzv=m["xzv"], yzv=m["yzv"],
+        xec=m["xec"], yec=m["yec"], xzc=m["xzc"], yzc=m["yzc"],
+        un=f["un"], vn=f["vn"], u=f["u"], v=f["v"], tn=f["tn"], t=t_ref)
+    o.therm_energy(case.nx, case.ny, case.regions, th, 0.004, pe, met, f["un"], f["vn"], f["u"], f["v"],
+                   f["tn"], t_or)
+    assert np.isfinite(t_or).all()
+    assert np.array_equal(t_ref, t_or)
+
+
+def test_temp_bound_cond_and_eq_state_bitwise():
+    import thermal_setup
+    case, th, f = thermal_setup.problem(seed=9)
+    f77ref.build(case.nx + 1, case.ny + 1)
+    r = refrun.RefRun(case, cold_start=False)
+    o = O.Oracle(case.nx + 1, case.ny + 1)
+    a, b = f["t"].copy(order="F"), f["t"].copy(order="F")
+    r.R("tempboundcond", nx=case.nx, ny=case.ny, nreg=r.tab["nreg"], nregbrd=r.tab["nregbrd"],
+        **{k: v for k, v in _thermal_tables(th).items() if k != "dhgstval"}, dbcval=r.tab["dbcval"], t=a)
+    o.temp_bound_cond(case.nx, case.ny, case.regions, th, b)
+    assert np.array_equal(a, b)
+    da, db = r.z(), r.z()
+    # temperatures in [0, 1] of the reference scale, pressure of either sign
+    t = np.asfortranarray(0.5 + 0.4 * np.tanh(f["tn"]))
+    kw = dict(uref=1.3, densref=1.1, tmax=350.0, tref=290.0, rconst=287.0)
+    r.R("eqstate", nx=case.nx, ny=case.ny, **kw, p=f["p"], t=t, den=da)
+    o.eq_state(case.nx, case.ny, kw["uref"], kw["densref"], kw["tmax"], kw["tref"], kw["rconst"],
+               f["p"], t, db)
+    assert np.array_equal(da, db) and np.count_nonzero(da) > 0

@@ -15,6 +15,7 @@
 
 #include "w2_adjoint.cuh"
 #include "w2_ensemble.cuh"
+#include "w2_thermal.cuh"
 
 using namespace w2;
 
@@ -77,6 +78,12 @@ struct w2_ctx {
   bool adj_alloc = false;
   Chain adj_tx{}, adj_ty{};
   double *adj_rows[8] = {};
+  // thermal energy (made on first use): the chain of the (nx-1)(ny-1)
+  // interior points and the thermal region tables of the current call
+  bool therm_alloc = false;
+  Chain therm_ch{};
+  int *d_ttab = nullptr;     // nTRgType(mgri,mgrj) then nTemBdTp(mgri,mgrj,4)
+  double *d_tval = nullptr;  // dTRgVal(mgri,mgrj) then dHGSTval(mgri,mgrj)
   // per-position face values (wolfd2gpu_set_face_profile)
   int *prof_idx = nullptr;   // device table, -1 = region constant
   double *prof = nullptr;    // device values, kMaxProfiles x prof_len
@@ -427,10 +434,14 @@ int launch_bc(w2_ctx *c, int ops, double *u, double *v, double *p) {
 }
 
 int launch_naux(w2_ctx *c, int mqiter, double dk, double re, double qtol, const double *un,
-                const double *vn, double *us, double *vs) {
+                const double *vn, double *us, double *vs, const double *den = nullptr,
+                const double *denn = nullptr, double fr = 0.0) {
   int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny, naux_smem(c));
   ProfScope ps(c, W2_K_MOMENTUM);
   Dev d = c->dev;
+  d.den = den;
+  d.denn = denn;
+  d.fr = fr;
   StepOut *out = c->d_out;
   void *args[] = {&d, &mqiter, &dk, &re, &qtol, (void *)&un, (void *)&vn, &us, &vs, &out};
   return coop(c, (const void *)k_naux, blocks, args, naux_smem(c));
@@ -1093,30 +1104,37 @@ int wolfd2gpu_naux_momentum(w2_ctx *c, const int *nx, const int *ny, const int *
                             const double *qtol, const double *d, const double *dn,
                             const double *un, const double *vn, double *us, double *vs,
                             int *nQLiter) {
-  (void)fr;
   int rc = ready(c);
   if (rc) return rc;
   if (!dims_match(c, nx, ny) || !mqiter || !dk || !re || !qtol || !un || !vn || !us || !vs || !nQLiter)
     return fail(c, W2_E_ARG, "bad argument");
-  if (d || dn) {
-    // density enters only through the buoyancy term (momentum.f:703), which
-    // needs the equation of state (thermal energy, outside this library)
+  // density enters only through the buoyancy term of YMomentum
+  // (momentum.f:703); all-zero (or absent) density arrays leave it out
+  bool buoy = false;
+  {
     const double *arrs[2] = {d, dn};
     for (const double *a : arrs)
       if (a)
-        for (int j = 0; j <= c->ny + 1; ++j)
+        for (int j = 0; j <= c->ny + 1 && !buoy; ++j)
           for (int i = 0; i <= c->nx + 1; ++i)
-            if (a[i + (size_t)j * (c->mnx + 1)] != 0.0)
-              return fail(c, W2_E_UNSUPPORTED, "nonzero density (buoyancy) is not supported");
+            if (a[i + (size_t)j * (c->mnx + 1)] != 0.0) {
+              buoy = true;
+              break;
+            }
   }
+  if (buoy && (!d || !dn || !fr)) return fail(c, W2_E_ARG, "buoyancy needs d, dn and fr");
   double *dun = c->stage[0], *dvn = c->stage[1], *dus = c->stage[2], *dvs = c->stage[3];
+  double *dd = c->stage[4], *ddn = c->stage[5];
   if ((rc = copy_in(c, dun, un)) || (rc = copy_in(c, dvn, vn)) || (rc = copy_in(c, dus, us)) ||
       (rc = copy_in(c, dvs, vs)))
     return rc;
+  if (buoy && ((rc = copy_in(c, dd, d)) || (rc = copy_in(c, ddn, dn)))) return rc;
   c->launches++;
   k_naux_init<<<grid_blocks(c), c->threads, 0, c->st>>>(c->dev, dun, dvn, dus, dvs);
   CK(cudaGetLastError());
-  if ((rc = launch_naux(c, *mqiter, *dk, *re, *qtol, dun, dvn, dus, dvs))) return rc;
+  if ((rc = launch_naux(c, *mqiter, *dk, *re, *qtol, dun, dvn, dus, dvs, buoy ? dd : nullptr,
+                        buoy ? ddn : nullptr, buoy ? *fr : 0.0)))
+    return rc;
   if ((rc = copy_out(c, us, dus)) || (rc = copy_out(c, vs, dvs))) return rc;
   CK(cudaMemcpyAsync(c->h_out, c->d_out, sizeof(StepOut), cudaMemcpyDeviceToHost, c->st));
   if ((rc = check_sync(c))) return rc;
@@ -1219,6 +1237,118 @@ int wolfd2gpu_filter(w2_ctx *c, const int *nx, const int *ny, const int *ncomp, 
   k_filter<<<grid_blocks(c), c->threads, 0, c->st>>>(c->dev, *ncomp == 1 ? MK_FU : MK_FV, *fp, dq, dh);
   CK(cudaGetLastError());
   if ((rc = copy_out(c, qu, dh))) return rc;
+  return check_sync(c);
+}
+
+}  // extern "C"
+
+namespace {
+
+// Thermal tables of a call: every flag checked as TempBoundCond's select
+// cases do (bound_cond.f:1098-1183, 'stop' on an unknown flag), then
+// uploaded.  The chain of the interior points is made on first use.
+int therm_prepare(w2_ctx *c, const int *nTRgType, const int *nTemBdTp, const double *dTRgVal,
+                  const double *dHGSTval, ThermTables *tt) {
+  const int mg = c->mgri * c->mgrj;
+  for (int jr = 1; jr <= c->nrj; ++jr)
+    for (int ir = 1; ir <= c->nri; ++ir) {
+      const int rt = nTRgType[(ir - 1) + (jr - 1) * c->mgri];
+      if (rt < RT_NOSRCE || rt > RT_TEMPER)
+        return fail(c, W2_E_BCFLAG, "Wrong nTRgType flag in region %d,%d", ir, jr);
+      if (rt == RT_TEMPER) continue;
+      for (int s = 1; s <= 4; ++s) {
+        const int bt = nTemBdTp[(ir - 1) + (jr - 1) * c->mgri + (s - 1) * mg];
+        if (bt < BT_INTERN || bt > BT_HTFLUX)
+          return fail(c, W2_E_BCFLAG, "Wrong nTemBdTp %c flag in region %d,%d", "WESN"[s - 1], ir, jr);
+      }
+    }
+  if (!c->therm_alloc) {
+    const int n = (c->nx - 1) * (c->ny - 1);
+    int rc;
+    if ((rc = make_chain(c, c->therm_ch, n, true))) return rc;
+    if (!(c->d_ttab = dalloc<int>(c, (size_t)5 * mg)) || !(c->d_tval = dalloc<double>(c, (size_t)2 * mg)))
+      return fail(c, W2_E_CUDA, "out of device memory (thermal tables)");
+    const int wmax = (int)walk_stage_bytes(sizeof(double), kMaxThreads);
+    if (cudaFuncSetAttribute((const void *)k_therm, cudaFuncAttributeMaxDynamicSharedMemorySize, wmax) !=
+        cudaSuccess)
+      return fail(c, W2_E_CUDA, "shared memory attribute (thermal)");
+    c->therm_alloc = true;
+  }
+  CK(cudaMemcpyAsync(c->d_ttab, nTRgType, sizeof(int) * mg, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->d_ttab + mg, nTemBdTp, sizeof(int) * 4 * mg, cudaMemcpyHostToDevice, c->st));
+  if (dTRgVal) CK(cudaMemcpyAsync(c->d_tval, dTRgVal, sizeof(double) * mg, cudaMemcpyHostToDevice, c->st));
+  if (dHGSTval)
+    CK(cudaMemcpyAsync(c->d_tval + mg, dHGSTval, sizeof(double) * mg, cudaMemcpyHostToDevice, c->st));
+  // the uploads read pageable host memory: finish them before the caller's
+  // arrays can change
+  CK(cudaStreamSynchronize(c->st));
+  *tt = ThermTables{c->d_ttab, c->d_ttab + mg, c->d_tval, c->d_tval + mg};
+  c->therm_ch.L = c->dev.seg;
+  c->therm_ch.nseg = (c->therm_ch.n + c->dev.seg - 1) / c->dev.seg;
+  return W2_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wolfd2gpu_temp_bound_cond(w2_ctx *c, const int *nx, const int *ny, const int *nTRgType,
+                              const int *nTemBdTp, const double *dTRgVal, double *t) {
+  int rc = ready(c);
+  if (rc) return rc;
+  if (!dims_match(c, nx, ny) || !nTRgType || !nTemBdTp || !dTRgVal || !t)
+    return fail(c, W2_E_ARG, "bad argument");
+  ThermTables tt;
+  if ((rc = therm_prepare(c, nTRgType, nTemBdTp, dTRgVal, nullptr, &tt))) return rc;
+  double *dt = c->stage[0];
+  if ((rc = copy_in(c, dt, t))) return rc;
+  c->launches++;
+  k_temp_bc<<<1, c->threads, 0, c->st>>>(c->dev, tt, dt);
+  CK(cudaGetLastError());
+  if ((rc = copy_out(c, t, dt))) return rc;
+  return check_sync(c);
+}
+
+int wolfd2gpu_therm_energy(w2_ctx *c, const int *nx, const int *ny, const int *nTRgType,
+                           const int *nTemBdTp, const double *dk, const double *pe,
+                           const double *dTRgVal, const double *dHGSTval, const double *un,
+                           const double *vn, const double *u, const double *v, const double *tn,
+                           double *t) {
+  int rc = ready(c);
+  if (rc) return rc;
+  if (!dims_match(c, nx, ny) || !nTRgType || !nTemBdTp || !dk || !pe || !dTRgVal || !dHGSTval || !un ||
+      !vn || !u || !v || !tn || !t)
+    return fail(c, W2_E_ARG, "bad argument");
+  ThermTables tt;
+  if ((rc = therm_prepare(c, nTRgType, nTemBdTp, dTRgVal, dHGSTval, &tt))) return rc;
+  double *s[6] = {c->stage[0], c->stage[1], c->stage[2], c->stage[3], c->stage[4], c->stage[5]};
+  const double *h[6] = {un, vn, u, v, tn, t};
+  for (int k = 0; k < 6; ++k)
+    if ((rc = copy_in(c, s[k], h[k]))) return rc;
+  const Dev &d = c->dev;
+  ThermArgs A{tt, *dk, *pe, s[0], s[1], s[2], s[3], s[4], s[5], d.cj1x, d.cj2x, d.c1sx, d.c2sx, c->therm_ch};
+  Dev dv = d;
+  int blocks = pick_blocks(c, (const void *)k_therm, (long)c->nx * c->ny, naux_smem(c));
+  void *args[] = {&dv, &A};
+  if ((rc = coop(c, (const void *)k_therm, blocks, args, naux_smem(c)))) return rc;
+  if ((rc = copy_out(c, t, s[5]))) return rc;
+  return check_sync(c);
+}
+
+int wolfd2gpu_eq_state(w2_ctx *c, const int *nx, const int *ny, const double *uref,
+                       const double *densref, const double *tmax, const double *tref,
+                       const double *rconst, const double *p, const double *t, double *den) {
+  int rc = ready(c);
+  if (rc) return rc;
+  if (!dims_match(c, nx, ny) || !uref || !densref || !tmax || !tref || !rconst || !p || !t || !den)
+    return fail(c, W2_E_ARG, "bad argument");
+  double *dp = c->stage[0], *dt = c->stage[1], *dd = c->stage[2];
+  if ((rc = copy_in(c, dp, p)) || (rc = copy_in(c, dt, t)) || (rc = copy_in(c, dd, den))) return rc;
+  c->launches++;
+  k_eq_state<<<grid_blocks(c), c->threads, 0, c->st>>>(c->dev, *uref, *densref, *tmax, *tref, *rconst, dp, dt,
+                                                       dd);
+  CK(cudaGetLastError());
+  if ((rc = copy_out(c, den, dd))) return rc;
   return check_sync(c);
 }
 

@@ -147,6 +147,10 @@ struct Dev {
   int seg, warm;       // chain segment length and warm-up rows
   int has_outflow;     // any OUTLT1/OUTLT2 face (VelOutflowBCs not a no-op)
   int ppe_unit;        // every PPE row is the unit stencil (1,1,-4,1,1)
+  // density at the starred and time-level-n states for the buoyancy term of
+  // YMomentum (momentum.f:703), FP64 path; null when the density is zero
+  const double *den, *denn;
+  double fr;
 };
 
 __device__ __forceinline__ size_t IX(const Dev &d, int i, int j) {

@@ -20,7 +20,9 @@
 // Metric arrays are read through MRef, which collapses to 1-D profiles or
 // constants where the host found them so.  Non-porous regions contribute
 // exact zeros (PorosCoef writes 0, so dk2*cpj adds +0 to a value >= 1 and
-// the RHS terms vanish); porous decks are rejected on the host.
+// the RHS terms vanish); porous decks are rejected on the host.  The
+// buoyancy term of the y rows (momentum.f:703) is formed when the host gives
+// a density (FP64 path); with zero density it is zero and left out.
 #pragma once
 #include <type_traits>
 
@@ -31,6 +33,8 @@ namespace w2 {
 
 template <class T>
 __device__ __forceinline__ T tmax(T a, T b) { return b > a ? b : a; }
+template <class T>
+__device__ __forceinline__ T tmax_nan(T a, T b) { return (b > a || b != b) ? b : a; }
 
 // The FP32 path forms ConvCoef values on the fly (cheap in FP32, and it keeps
 // the working set in L2); the FP64 path stores them once per iteration.
@@ -312,7 +316,16 @@ __device__ void mom_assemble1(const Dev &d, const MomView<T> &V, double dk, doub
       V.y1.a1[py] = a1;
       V.y1.a2[py] = a2;
       V.y1.a3[py] = a3;
-      V.y1.b[py] = vn[o] - vs[o] + rkj * (-cnvs - cnvn) + rkj * re1 * (difs + difn);
+      T rhs = vn[o] - vs[o] + rkj * (-cnvs - cnvn) + rkj * re1 * (difs + difn);
+      if constexpr (std::is_same<T, double>::value) {
+        if (d.den) {
+          // buoy = dk (d(i,j+1) + d(i,j) + dn(i,j+1) + dn(i,j)) / (4 fr)
+          const size_t on = IX(d, i, j + 1);
+          const double buoy = dk * (d.den[on] + d.den[o] + d.denn[on] + d.denn[o]) / (4.0 * d.fr);
+          rhs = rhs - buoy;
+        }
+      }
+      V.y1.b[py] = rhs;
     }
   }
 }
@@ -390,7 +403,10 @@ __device__ void mom_update(const Dev &d, const MomView<T> &V, T *us, T *vs, unsi
     us[o] = us[o] + du;
     vs[o] = vs[o] + dv;
     const bool in = (i >= 2 && i <= nx - 1 && j >= 2 && j <= ny - 1) || (i == 5 && j == 5);
-    if (in) mx = tmax(tmax(mx, fabs(du)), fabs(dv));
+    // a NaN increment keeps the norm NaN (NaN's bits rank above every finite
+    // value in the slot's atomic max), so a NaN iterate never passes the qtol
+    // test: the reference reports such a run as not converged (-1)
+    if (in) mx = tmax_nan(tmax_nan(mx, fabs(du)), fabs(dv));
   }
   block_max_to(slot, mx);
 }

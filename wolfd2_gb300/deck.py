@@ -363,6 +363,28 @@ class RunParams:
         return RunParams(dk=dt * uref / dlref, re=re, fr=fr, **kw)
 
 
+# include/wolfd2.h: thermal region and boundary types
+RT_NOSRCE, RT_HEATGN, RT_TEMPER = 0, 1, 2
+BT_INTERN, BT_TEMPER, BT_HTFLUX = 0, 1, 2
+
+
+@dataclasses.dataclass
+class Thermal:
+    """Thermal region/boundary tables of ThermEnergy and TempBoundCond
+    (src/thermal.f:24-73, src/bound_cond.f:1030-1063), Fortran layout like
+    Regions; face temperatures are dBCVal(..., VAR_T)."""
+    nTRgType: np.ndarray      # int32 (mgri, mgrj): RT_*
+    nTemBdTp: np.ndarray      # int32 (mgri, mgrj, 4): BT_*
+    dTRgVal: np.ndarray       # float64 (mgri, mgrj): fixed-region temperature
+    dHGSTval: np.ndarray      # float64 (mgri, mgrj): heat generation source
+
+    @classmethod
+    def empty(cls) -> "Thermal":
+        f = dict(order="F")
+        return cls(np.zeros((MGRI, MGRJ), np.int32, **f), np.zeros((MGRI, MGRJ, 4), np.int32, **f),
+                   np.zeros((MGRI, MGRJ), np.float64, **f), np.zeros((MGRI, MGRJ), np.float64, **f))
+
+
 @dataclasses.dataclass
 class Case:
     """Everything the hot path needs for one instance."""

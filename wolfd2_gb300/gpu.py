@@ -97,6 +97,9 @@ def lib():
     L.wolfd2gpu_vel_outflow_bcs.argtypes = [vp, _ip, _ip, _dp, _dp]
     L.wolfd2gpu_diff_max_norm.argtypes = [vp, _ip, _ip, _dp, _dp, _dp]
     L.wolfd2gpu_filter.argtypes = [vp, _ip, _ip, _ip, _dp, _dp]
+    L.wolfd2gpu_temp_bound_cond.argtypes = [vp, _ip, _ip, _ip, _ip, _dp, _dp]
+    L.wolfd2gpu_therm_energy.argtypes = [vp, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp] + [_dp] * 6
+    L.wolfd2gpu_eq_state.argtypes = [vp, _ip, _ip] + [_dp] * 8
     L.wolfd2gpu_load_fields.argtypes = [vp, _dp, _dp, _dp]
     L.wolfd2gpu_store_fields.argtypes = [vp, _dp, _dp, _dp]
     L.wolfd2gpu_cold_start.argtypes = [vp, C.POINTER(Params), _ip]
@@ -300,6 +303,32 @@ class Solver:
 
     def Filter(self, ncomp, fp, qu) -> None:
         self._check(self.L.wolfd2gpu_filter(self.h, _i(self.nx), _i(self.ny), _i(ncomp), _d(fp), _p(qu)))
+
+    @staticmethod
+    def _ttab(a, dtype):
+        a = np.asfortranarray(a, dtype)
+        return a, a.ctypes.data_as(C.POINTER(C.c_int if dtype == np.int32 else C.c_double))
+
+    def TempBoundCond(self, th, t) -> None:
+        """th: deck.Thermal tables; t updated in place."""
+        rt, prt = self._ttab(th.nTRgType, np.int32)
+        bt, pbt = self._ttab(th.nTemBdTp, np.int32)
+        tv, ptv = self._ttab(th.dTRgVal, np.float64)
+        self._check(self.L.wolfd2gpu_temp_bound_cond(self.h, _i(self.nx), _i(self.ny), prt, pbt, ptv, _p(t)))
+
+    def ThermEnergy(self, th, dk, pe, un, vn, u, v, tn, t) -> None:
+        """ThermEnergy with deck.Thermal tables; t updated in place."""
+        rt, prt = self._ttab(th.nTRgType, np.int32)
+        bt, pbt = self._ttab(th.nTemBdTp, np.int32)
+        tv, ptv = self._ttab(th.dTRgVal, np.float64)
+        hg, phg = self._ttab(th.dHGSTval, np.float64)
+        self._check(self.L.wolfd2gpu_therm_energy(
+            self.h, _i(self.nx), _i(self.ny), prt, pbt, _d(dk), _d(pe), ptv, phg,
+            _p(un), _p(vn), _p(u), _p(v), _p(tn), _p(t)))
+
+    def EqState(self, uref, densref, tmax, tref, rconst, p, t, den) -> None:
+        self._check(self.L.wolfd2gpu_eq_state(self.h, _i(self.nx), _i(self.ny), _d(uref), _d(densref),
+                                              _d(tmax), _d(tref), _d(rconst), _p(p), _p(t), _p(den)))
 
     # ---- device-resident time loop ---------------------------------------
     def load_fields(self, u, v, p) -> None:
