@@ -176,6 +176,28 @@ int wolfd2gpu_eq_state(w2_ctx *ctx, const int *nx, const int *ny,
 
 /* ---- Device-resident time loop ---------------------------------------- */
 
+/* Thermal switches and constants of the time loop (ReadParam, parse.f:118-159;
+ * pe = re * Prandtl, file_manip.f:158; EqState's uref, densref, tmax, tref,
+ * rconst). */
+typedef struct {
+  int nthermen, neqstate, nmeiter;
+  double dmeittol, pe, uref, densref, tmax, tref, rconst;
+} w2_thermal;
+
+/* Switch the device-resident time loop to main.f's path with the energy
+ * equation (nthermen = 1) and/or the equation of state (neqstate = 1):
+ * momentum/energy iterations (up to nmeiter, ended by dmeittol, main.f:736-879)
+ * with ThermEnergy, EqState and the buoyancy term of YMomentum, then
+ * TempBoundCond.  Tables as for wolfd2gpu_therm_energy.  tp = NULL (or both
+ * switches 0) returns to the plain loop.  The temperature and density start
+ * at zero; wolfd2gpu_load_thermal / wolfd2gpu_store_thermal move them
+ * ((0:mnx,0:mny) host arrays, d may be NULL).  Plain FP64 only, no Filter. */
+int wolfd2gpu_set_thermal(w2_ctx *ctx, const w2_thermal *tp, const int *nTRgType,
+                          const int *nTemBdTp, const double *dTRgVal,
+                          const double *dHGSTval);
+int wolfd2gpu_load_thermal(w2_ctx *ctx, const double *t, const double *d);
+int wolfd2gpu_store_thermal(w2_ctx *ctx, double *t, double *d);
+
 /* Run parameters of the time loop (main.f with nthermen = 0). */
 typedef struct {
   double dk, re, fr, qtol, sortol, sorrel, fpu, fpv;
@@ -302,7 +324,8 @@ void *wolfd2gpu_stream(w2_ctx *ctx);
 #define W2_K_POST     2  /* Project + boundary rows + step norms  */
 #define W2_K_BC       3  /* one-block boundary programs           */
 #define W2_K_COPY     4  /* time-level copies                     */
-#define W2_K_NKINDS   5
+#define W2_K_THERM    5  /* ThermEnergy and EqState               */
+#define W2_K_NKINDS   6
 int wolfd2gpu_profile(w2_ctx *ctx, int enable);
 /* Accumulated device time (ms) and launch count of one kind since the last
  * wolfd2gpu_profile(ctx, 1); synchronises the context stream. */

@@ -59,6 +59,11 @@ class _Fields(C.Structure):
     _fields_ = [(n, _dp) for n in FIELD_NAMES]
 
 
+class _ThermalParams(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("nthermen", "neqstate", "nmeiter")] + \
+               [(n, C.c_double) for n in ("dmeittol", "pe", "uref", "densref", "tmax", "tref", "rconst")]
+
+
 def build(force: bool = False) -> str:
     """Compile the oracle library (gcc, no FMA contraction)."""
     srcs = ("wolfd2_oracle.c", "wolfd2_oracle.h", "momentum_impl.h")
@@ -113,6 +118,11 @@ def lib():
             L.w2o_cold_start.restype = C.c_int
             L.w2o_cold_start.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions),
                                          C.POINTER(_Params), C.POINTER(_Metrics), C.POINTER(_Fields)]
+            L.w2o_step_thermal.restype = C.c_int
+            L.w2o_step_thermal.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions),
+                                           C.POINTER(_Thermal), C.POINTER(_ThermalParams),
+                                           C.POINTER(_Params), C.POINTER(_Metrics), C.POINTER(_Fields),
+                                           _ip, _ip, _dp]
             L.w2o_step.restype = C.c_int
             L.w2o_step.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions),
                                    C.POINTER(_Params), C.POINTER(_Metrics), C.POINTER(_Fields),
@@ -297,6 +307,12 @@ class OracleRun:
         self._ms = Oracle.metrics_struct(self.met)
         self._ps = Oracle.params_struct(case.params)
         self._fs = _Fields(*[_ptr(self.f[n]) for n in FIELD_NAMES])
+        self._th = self._tp = None
+        if getattr(case, "thermal", None) is not None and getattr(case, "tparams", None) is not None:
+            self._th = Oracle.thermal_struct(case.thermal)
+            tp = case.tparams
+            self._tp = _ThermalParams(tp.nthermen, tp.neqstate, tp.nmeiter, tp.dmeittol, tp.pe, tp.uref,
+                                      tp.densref, tp.tmax, tp.tref, tp.rconst)
         self.history = []
         self.cold_nconv = None
         if cold_start:
@@ -308,9 +324,15 @@ class OracleRun:
         nql, nsor = C.c_int(), C.c_int()
         dif = (C.c_double * 4)()
         for _ in range(n):
-            rc = self.o.L.w2o_step(self.o.h, self.nx, self.ny, C.byref(self._rs), C.byref(self._ps),
-                                   C.byref(self._ms), C.byref(self._fs), C.byref(nql),
-                                   C.byref(nsor), dif)
+            if self._th is not None:
+                rc = self.o.L.w2o_step_thermal(self.o.h, self.nx, self.ny, C.byref(self._rs),
+                                               C.byref(self._th), C.byref(self._tp), C.byref(self._ps),
+                                               C.byref(self._ms), C.byref(self._fs), C.byref(nql),
+                                               C.byref(nsor), dif)
+            else:
+                rc = self.o.L.w2o_step(self.o.h, self.nx, self.ny, C.byref(self._rs), C.byref(self._ps),
+                                       C.byref(self._ms), C.byref(self._fs), C.byref(nql),
+                                       C.byref(nsor), dif)
             self.history.append((nql.value, nsor.value, tuple(dif)))
             if rc:
                 raise FloatingPointError("Solution diverged. Please reduce CFL number.")

@@ -3,8 +3,10 @@ INFRASTRUCTURE ONLY).
 
 The routines come from oracle/f77ref.py's translation of the reference
 source; this module only sequences them exactly as the reference's main
-program does for nthermen = nsmallscl = 0 (src/main.f:606-641 cold start,
-src/main.f:690-972 one time step), using the reference's own argument names.
+program does for nsmallscl = 0 (src/main.f:606-641 cold start,
+src/main.f:690-972 one time step, with the momentum/energy iterations when
+the case carries thermal parameters), using the reference's own argument
+names.
 """
 from __future__ import annotations
 
@@ -109,25 +111,72 @@ class RefRun:
         self.vel_bc(f["u"], f["v"])
         return n
 
+    # -- thermal (case.thermal: deck.Thermal, case.tparams: deck.ThermalParams)
+    def _ttab(self):
+        th = self.case.thermal
+        return dict(ntrgtype=np.asfortranarray(th.nTRgType, np.int32),
+                    ntembdtp=np.asfortranarray(th.nTemBdTp, np.int32),
+                    dtrgval=np.asfortranarray(th.dTRgVal, np.float64))
+
+    def temp_bc(self, t):
+        tb = self.tab
+        self.R("tempboundcond", nx=self.nx, ny=self.ny, nreg=tb["nreg"], nregbrd=tb["nregbrd"],
+               **self._ttab(), dbcval=tb["dbcval"], t=t)
+
+    def therm(self, un, vn, u, v, tn, t):
+        tb, m, tp = self.tab, self.m, self.case.tparams
+        self.R("thermenergy", nx=self.nx, ny=self.ny, nreg=tb["nreg"], nregbrd=tb["nregbrd"],
+               **self._ttab(), dhgstval=np.asfortranarray(self.case.thermal.dHGSTval, np.float64),
+               dk=self.case.params.dk, pe=tp.pe, dbcval=tb["dbcval"],
+               **{k: m[k] for k in ("rau", "rbu", "rbv", "rgv", "djc", "xeu", "yeu", "xzv", "yzv",
+                                    "xec", "yec", "xzc", "yzc")},
+               un=un, vn=vn, u=u, v=v, tn=tn, t=t)
+
+    def eq_state(self, p, t, den):
+        tp = self.case.tparams
+        self.R("eqstate", nx=self.nx, ny=self.ny, uref=tp.uref, densref=tp.densref, tmax=tp.tmax,
+               tref=tp.tref, rconst=tp.rconst, p=p, t=t, den=den)
+
     def step(self, n: int = 1):
+        """main.f:690-972: with case.tparams.nthermen = 1 the momentum/energy
+        iterations (main.f:736-879) run ThermEnergy and EqState."""
         f = self.f
+        tp = getattr(self.case, "tparams", None)
+        therm = tp is not None and tp.nthermen == 1
+        eqs = tp is not None and tp.neqstate == 1
+        nme = tp.nmeiter if tp is not None else 1
+        if not therm and nme > 0:
+            nme = 1
         for _ in range(n):
             for a, b in (("pn", "p"), ("un", "u"), ("vn", "v"), ("tn", "t"), ("dn", "d")):
                 f[a][...] = f[b]
-            for a, b in (("us", "u"), ("vs", "v"), ("ts", "t")):
-                f[a][...] = f[b]
-            nql = self.naux(f["un"], f["vn"], f["us"], f["vs"])
-            self.vel_bc(f["us"], f["vs"])
-            self.pres_bc(f["p"])
-            nsor = self.ppe(f["us"], f["vs"], f["p"])
-            self.pres_bc(f["p"])
-            self.project(f["p"], f["us"], f["vs"])
-            self.vel_bc(f["us"], f["vs"])
-            self.pres_bc(f["p"])
-            for a, b in (("u", "us"), ("v", "vs"), ("t", "ts")):
-                f[a][...] = f[b]
+            for l in range(1, nme + 1):
+                for a, b in (("us", "u"), ("vs", "v"), ("ts", "t")):
+                    f[a][...] = f[b]
+                nql = self.naux(f["un"], f["vn"], f["us"], f["vs"])
+                self.vel_bc(f["us"], f["vs"])
+                self.pres_bc(f["p"])
+                nsor = self.ppe(f["us"], f["vs"], f["p"])
+                self.pres_bc(f["p"])
+                self.project(f["p"], f["us"], f["vs"])
+                self.vel_bc(f["us"], f["vs"])
+                self.pres_bc(f["p"])
+                if therm:
+                    self.therm(f["un"], f["vn"], f["us"], f["vs"], f["tn"], f["ts"])
+                if eqs:
+                    self.eq_state(f["p"], f["ts"], f["d"])
+                me = (self.diff(f["u"], f["us"]), self.diff(f["v"], f["vs"]), self.diff(f["t"], f["ts"]))
+                for a, b in (("u", "us"), ("v", "vs"), ("t", "ts")):
+                    f[a][...] = f[b]
+                mx = me[0]
+                for x in me[1:]:
+                    mx = x if x > mx else mx
+                if l > 1 and mx < tp.dmeittol:
+                    break
             self.vel_bc(f["u"], f["v"])
             self.pres_bc(f["p"])
+            if therm:
+                self.temp_bc(f["t"])
             dif = (self.diff(f["pn"], f["p"]), self.diff(f["un"], f["u"]),
                    self.diff(f["vn"], f["v"]), self.diff(f["tn"], f["t"]))
             self.history.append((nql, nsor, dif))

@@ -1142,43 +1142,71 @@ int w2o_cold_start(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
 int w2o_step(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
              const w2o_params *prm, const w2o_metrics *m, w2o_fields *f,
              int *nQLiter, int *nSorConv, double dif[4]) {
+  return w2o_step_thermal(c, nx, ny, r, NULL, NULL, prm, m, f, nQLiter, nSorConv, dif);
+}
+
+int w2o_step_thermal(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                     const w2o_thermal *th, const w2o_thermal_params *tp,
+                     const w2o_params *prm, const w2o_metrics *m, w2o_fields *f,
+                     int *nQLiter, int *nSorConv, double dif[4]) {
   int i, j;
+  const int therm = th && tp && tp->nthermen == 1;
+  const int eqs = th && tp && tp->neqstate == 1;
+  /* main.f:736: without the energy equation one pass */
+  int nme = tp ? tp->nmeiter : 1;
+  if (!therm && nme > 0) nme = 1;
   for (j = 0; j <= ny + 1; j++)
     for (i = 0; i <= nx + 1; i++) {
       F(f->pn, i, j) = F(f->p, i, j);
       F(f->un, i, j) = F(f->u, i, j);
       F(f->vn, i, j) = F(f->v, i, j);
       F(f->tn, i, j) = F(f->t, i, j);
+      F(f->dn, i, j) = F(f->d, i, j);
     }
-  for (j = 0; j <= ny + 1; j++)
-    for (i = 0; i <= nx + 1; i++) {
-      F(f->us, i, j) = F(f->u, i, j);
-      F(f->vs, i, j) = F(f->v, i, j);
-      F(f->ts, i, j) = F(f->t, i, j);
-    }
-  *nQLiter = w2o_naux_momentum(c, nx, ny, prm->mqiter, r, prm->dk, prm->re,
-                               prm->fr, prm->qtol, m, f->d, f->dn, f->un,
-                               f->vn, f->us, f->vs);
-  if (prm->nfiltu == 1) w2o_filter(c, nx, ny, VU, r, prm->fpu, f->us);
-  if (prm->nfiltv == 1) w2o_filter(c, nx, ny, VV, r, prm->fpv, f->vs);
-  w2o_vel_bound_cond(c, nx, ny, r, f->us, f->vs);
-  w2o_pres_bound_cond(c, nx, ny, r, f->p);
-  *nSorConv = w2o_ppe(c, nx, ny, r, prm->lcartes, prm->npsolver, prm->msorit,
-                      prm->dk, prm->sortol, prm->sorrel, m, f->us, f->vs, f->p);
-  w2o_pres_bound_cond(c, nx, ny, r, f->p);
-  w2o_project(c, nx, ny, r, prm->dk, m, f->p, f->us, f->vs);
-  w2o_vel_bound_cond(c, nx, ny, r, f->us, f->vs);
-  w2o_pres_bound_cond(c, nx, ny, r, f->p);
-  /* main.f:857-859 computes dif(1..3) here; with one momentum/energy pass
-   * they are overwritten below before any use. */
-  for (j = 0; j <= ny + 1; j++)
-    for (i = 0; i <= nx + 1; i++) {
-      F(f->u, i, j) = F(f->us, i, j);
-      F(f->v, i, j) = F(f->vs, i, j);
-      F(f->t, i, j) = F(f->ts, i, j);
-    }
+  for (int l = 1; l <= nme; l++) {
+    for (j = 0; j <= ny + 1; j++)
+      for (i = 0; i <= nx + 1; i++) {
+        F(f->us, i, j) = F(f->u, i, j);
+        F(f->vs, i, j) = F(f->v, i, j);
+        F(f->ts, i, j) = F(f->t, i, j);
+      }
+    *nQLiter = w2o_naux_momentum(c, nx, ny, prm->mqiter, r, prm->dk, prm->re,
+                                 prm->fr, prm->qtol, m, f->d, f->dn, f->un,
+                                 f->vn, f->us, f->vs);
+    if (prm->nfiltu == 1) w2o_filter(c, nx, ny, VU, r, prm->fpu, f->us);
+    if (prm->nfiltv == 1) w2o_filter(c, nx, ny, VV, r, prm->fpv, f->vs);
+    w2o_vel_bound_cond(c, nx, ny, r, f->us, f->vs);
+    w2o_pres_bound_cond(c, nx, ny, r, f->p);
+    *nSorConv = w2o_ppe(c, nx, ny, r, prm->lcartes, prm->npsolver, prm->msorit,
+                        prm->dk, prm->sortol, prm->sorrel, m, f->us, f->vs, f->p);
+    w2o_pres_bound_cond(c, nx, ny, r, f->p);
+    w2o_project(c, nx, ny, r, prm->dk, m, f->p, f->us, f->vs);
+    w2o_vel_bound_cond(c, nx, ny, r, f->us, f->vs);
+    w2o_pres_bound_cond(c, nx, ny, r, f->p);
+    if (therm)
+      w2o_therm_energy(c, nx, ny, r, th, prm->dk, tp->pe, m, f->un, f->vn, f->us, f->vs, f->tn, f->ts);
+    if (eqs)
+      w2o_eq_state(c, nx, ny, tp->uref, tp->densref, tp->tmax, tp->tref, tp->rconst, f->p, f->ts, f->d);
+    /* main.f:857-859, the momentum/energy convergence test's norms */
+    double me[3];
+    me[0] = w2o_diff_max_norm(c, nx, ny, f->u, f->us);
+    me[1] = w2o_diff_max_norm(c, nx, ny, f->v, f->vs);
+    me[2] = w2o_diff_max_norm(c, nx, ny, f->t, f->ts);
+    for (j = 0; j <= ny + 1; j++)
+      for (i = 0; i <= nx + 1; i++) {
+        F(f->u, i, j) = F(f->us, i, j);
+        F(f->v, i, j) = F(f->vs, i, j);
+        F(f->t, i, j) = F(f->ts, i, j);
+      }
+    /* difmax = max(dif(1),dif(2),dif(3)) (main.f:873) */
+    double mx = me[0];
+    if (me[1] > mx) mx = me[1];
+    if (me[2] > mx) mx = me[2];
+    if (l > 1 && mx < tp->dmeittol) break;
+  }
   w2o_vel_bound_cond(c, nx, ny, r, f->u, f->v);
   w2o_pres_bound_cond(c, nx, ny, r, f->p);
+  if (therm) w2o_temp_bound_cond(c, nx, ny, r, th, f->t);
   dif[0] = w2o_diff_max_norm(c, nx, ny, f->pn, f->p);
   dif[1] = w2o_diff_max_norm(c, nx, ny, f->un, f->u);
   dif[2] = w2o_diff_max_norm(c, nx, ny, f->vn, f->v);

@@ -157,11 +157,18 @@ void w2o_eq_state(w2o_ctx *c, int nx, int ny, double uref, double densref, doubl
 /* momentum.f:1307-1339 (exported for unit tests) */
 void w2o_alt_trid_lu(int n, double *a /* a(3,n) */, double *b);
 
-/* Time-loop parameters (main.f with nthermen = nsmallscl = 0). */
+/* Time-loop parameters (main.f with nsmallscl = 0). */
 typedef struct {
   double dk, re, fr, qtol, sortol, sorrel, fpu, fpv;
   int mqiter, npsolver, msorit, nfiltu, nfiltv, lcartes;
 } w2o_params;
+
+/* Thermal switches and constants of the time loop (ReadParam, parse.f:118-159
+ * defaults; pe = re * Prandtl, file_manip.f:158). */
+typedef struct {
+  int nthermen, neqstate, nmeiter;
+  double dmeittol, pe, uref, densref, tmax, tref, rconst;
+} w2o_thermal_params;
 
 /* Fields of the time loop, each (0:mnx,0:mny). */
 typedef struct {
@@ -177,6 +184,14 @@ int w2o_cold_start(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
 int w2o_step(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
              const w2o_params *prm, const w2o_metrics *m, w2o_fields *f,
              int *nQLiter, int *nSorConv, double dif[4]);
+
+/* The same with the thermal energy equation: momentum/energy iterations
+ * (main.f:736-879: ThermEnergy, EqState, the ME convergence test), and
+ * TempBoundCond after them.  th/tp NULL or nthermen = 0 is w2o_step. */
+int w2o_step_thermal(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                     const w2o_thermal *th, const w2o_thermal_params *tp,
+                     const w2o_params *prm, const w2o_metrics *m, w2o_fields *f,
+                     int *nQLiter, int *nSorConv, double dif[4]);
 
 #ifdef __cplusplus
 }

@@ -137,3 +137,39 @@ def test_momentum_divergence_reported_like_reference():
 def dataclasses_replace(p, **kw):
     import dataclasses
     return dataclasses.replace(p, **kw)
+
+
+def _loop_cases():
+    return {
+        "heated1": lambda: deck.heated_cavity(32, 500.0, 0.004, nmeiter=1, eqstate=False),
+        "heated3": lambda: deck.heated_cavity(32, 500.0, 0.004, nmeiter=3, dmeittol=1e-7),
+        "heated6_lid": lambda: deck.heated_cavity(40, 300.0, 0.004, nmeiter=6, dmeittol=1e-6, lid=1.0),
+        "multiregion": lambda: thermal_setup.loop_case(),
+    }
+
+
+@pytest.mark.parametrize("name", sorted(_loop_cases()))
+@pytest.mark.parametrize("graph", [False, True])
+def test_thermal_time_loop_matches_oracle(name, graph):
+    """The device-resident step with the energy equation (momentum/energy
+    iterations ending on the device, ThermEnergy, EqState, buoyancy,
+    TempBoundCond) against the oracle's time loop: bit-identical fields,
+    temperatures, densities and iteration counts."""
+    case = _loop_cases()[name]()
+    o = O.OracleRun(case)
+    s = Solver.for_case(case, tuned=False)
+    s.graph(graph)
+    s.load_fields(o.f["u"], o.f["v"], o.f["p"])
+    s.load_thermal(o.f["t"], o.f["d"])
+    nsteps = 6
+    hist = s.step(case.params, 3) + s.step(case.params, 3)
+    o.step(nsteps)
+    assert [(h[0], h[1]) for h in hist] == [h[:2] for h in o.history]
+    for h, oh in zip(hist, o.history):
+        assert tuple(h[2]) == tuple(oh[2])
+    u, v, p = s.store_fields()
+    t, dd = s.store_thermal()
+    for name_, g, r in zip("uvptd", (u, v, p, t, dd), (o.f["u"], o.f["v"], o.f["p"], o.f["t"], o.f["d"])):
+        assert np.array_equal(g, r), (name_, float(np.max(np.abs(g - r))))
+    assert np.abs(t).max() > 0.1
+    s.close()

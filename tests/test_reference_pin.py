@@ -127,3 +127,41 @@ def test_temp_bound_cond_and_eq_state_bitwise():
     o.eq_state(case.nx, case.ny, kw["uref"], kw["densref"], kw["tmax"], kw["tref"], kw["rconst"],
                f["p"], t, db)
     assert np.array_equal(da, db) and np.count_nonzero(da) > 0
+
+
+@pytest.mark.parametrize("nmeiter,eqstate", [(1, False), (3, True), (6, True)])
+def test_heated_cavity_time_loop_bitwise(nmeiter, eqstate):
+    """The time loop with the energy equation: momentum/energy iterations
+    (main.f:736-879) with ThermEnergy, EqState feeding the buoyancy term of
+    YMomentum, and TempBoundCond after them."""
+    case = deck.heated_cavity(24, 500.0, 0.004, nmeiter=nmeiter, dmeittol=1e-7, eqstate=eqstate)
+    f77ref.build(case.nx + 1, case.ny + 1)
+    r = refrun.RefRun(case)
+    o = O.OracleRun(case)
+    r.step(8)
+    o.step(8)
+    assert [h[:2] for h in r.history] == [h[:2] for h in o.history]
+    for a, b in zip(r.history, o.history):
+        assert a[2] == b[2]
+    for k in ("u", "v", "p", "t", "d"):
+        assert np.array_equal(r.f[k], o.f[k]), k
+    assert np.abs(o.f["t"]).max() > 0.1
+    if eqstate:
+        assert np.abs(o.f["d"]).max() > 1e-3
+
+
+def test_multiregion_thermal_time_loop_bitwise():
+    """The time loop with the energy equation on the curvilinear 3 x 2
+    layout (fixed-temperature and heat-generating regions)."""
+    import thermal_setup
+    case = thermal_setup.loop_case()
+    f77ref.build(case.nx + 1, case.ny + 1)
+    r = refrun.RefRun(case)
+    o = O.OracleRun(case)
+    r.step(5)
+    o.step(5)
+    assert [h[:2] for h in r.history] == [h[:2] for h in o.history]
+    for a, b in zip(r.history, o.history):
+        assert a[2] == b[2]
+    for k in ("u", "v", "p", "t", "d"):
+        assert np.array_equal(r.f[k], o.f[k]), k

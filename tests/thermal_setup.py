@@ -56,3 +56,14 @@ def problem(ncx: int = 36, ncy: int = 24, seed: int = 5):
     fields = {n: smooth(k) for k, n in enumerate(["u", "v", "un", "vn", "tn", "t", "p"])}
     fields["t"] = np.asfortranarray(fields["tn"] + 0.01 * fields["t"])
     return case, th, fields
+
+
+def loop_case(nmeiter: int = 3):
+    """The 3 x 2 thermal layout as a time-loop case: energy equation and
+    EqState on (buoyancy at Froude number 0.05), momentum/energy iterations."""
+    case, th, f = problem()
+    case.thermal = th
+    case.tparams = deck.ThermalParams(nthermen=1, neqstate=1, nmeiter=nmeiter, dmeittol=1e-7, pe=100.0,
+                                      tmax=330.0, tref=300.0, rconst=287.0)
+    case.params.fr = 0.05
+    return case

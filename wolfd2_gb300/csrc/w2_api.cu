@@ -84,6 +84,13 @@ struct w2_ctx {
   Chain therm_ch{};
   int *d_ttab = nullptr;     // nTRgType(mgri,mgrj) then nTemBdTp(mgri,mgrj,4)
   double *d_tval = nullptr;  // dTRgVal(mgri,mgrj) then dHGSTval(mgri,mgrj)
+  // the time loop with the energy equation (wolfd2gpu_set_thermal): its
+  // switches, tables, temperature levels, density d / dn, and the previous
+  // iterates of the momentum/energy iterations
+  bool therm_on = false;
+  w2_thermal therm_p{};
+  ThermTables therm_tt{};
+  double *T[2] = {}, *Dd = nullptr, *Ddn = nullptr, *Up = nullptr, *Vp = nullptr, *Tp = nullptr;
   // per-position face values (wolfd2gpu_set_face_profile)
   int *prof_idx = nullptr;   // device table, -1 = region constant
   double *prof = nullptr;    // device values, kMaxProfiles x prof_len
@@ -501,8 +508,8 @@ bool tiled_applies(w2_ctx *c, int npsolver, double sorrel) {
 }
 
 int launch_ppe_tiled(w2_ctx *c, int lcartes, int msorit, double dk, double sortol,
-                     const double *u, const double *v, double *p, StepOut *out) {
-  Dev d = c->dev;
+                     const double *u, const double *v, double *p, StepOut *out, const Dev *dv = nullptr) {
+  Dev d = dv ? *dv : c->dev;
   TileGeom g = c->tg;
   void *args[] = {&d, &g, &lcartes, &msorit, &dk, &sortol, (void *)&u, (void *)&v, &p, &out};
   c->launches++;
@@ -1352,6 +1359,47 @@ int wolfd2gpu_eq_state(w2_ctx *c, const int *nx, const int *ny, const double *ur
   return check_sync(c);
 }
 
+int wolfd2gpu_set_thermal(w2_ctx *c, const w2_thermal *tp, const int *nTRgType, const int *nTemBdTp,
+                          const double *dTRgVal, const double *dHGSTval) {
+  int rc = ready(c);
+  if (rc) return rc;
+  if (!tp || (tp->nthermen != 1 && tp->neqstate != 1)) {
+    c->therm_on = false;
+    return W2_OK;
+  }
+  if (!nTRgType || !nTemBdTp || !dTRgVal || !dHGSTval) return fail(c, W2_E_ARG, "bad argument");
+  if (tp->nmeiter < 1 || (tp->nthermen == 1 && !(tp->pe != 0.0)))
+    return fail(c, W2_E_ARG, "nmeiter must be >= 1 and pe non-zero");
+  if ((rc = therm_prepare(c, nTRgType, nTemBdTp, dTRgVal, dHGSTval, &c->therm_tt))) return rc;
+  double **bufs[] = {&c->T[0], &c->T[1], &c->Dd, &c->Ddn, &c->Up, &c->Vp, &c->Tp};
+  for (double **b : bufs)
+    if (!*b && !(*b = dalloc<double>(c, c->nf))) return fail(c, W2_E_CUDA, "out of device memory (thermal fields)");
+  c->therm_p = *tp;
+  c->therm_on = true;
+  return W2_OK;
+}
+
+int wolfd2gpu_load_thermal(w2_ctx *c, const double *t, const double *d) {
+  if (!c || !c->therm_on || !t) return fail(c, W2_E_ARG, "thermal loop not set, or t missing");
+  int rc;
+  if ((rc = copy_in(c, c->T[c->cur], t))) return rc;
+  if (d) {
+    if ((rc = copy_in(c, c->Dd, d))) return rc;
+  } else {
+    CK(cudaMemsetAsync(c->Dd, 0, c->nf * sizeof(double), c->st));
+  }
+  return W2_OK;
+}
+
+int wolfd2gpu_store_thermal(w2_ctx *c, double *t, double *d) {
+  if (!c || !c->therm_on) return fail(c, W2_E_ARG, "thermal loop not set");
+  int rc;
+  if (t && (rc = copy_out(c, t, c->T[c->cur]))) return rc;
+  if (d && (rc = copy_out(c, d, c->Dd))) return rc;
+  CK(cudaStreamSynchronize(c->st));
+  return W2_OK;
+}
+
 // ---- device-resident time loop ----------------------------------------------
 
 int wolfd2gpu_load_fields(w2_ctx *c, const double *u, const double *v, const double *p) {
@@ -1431,6 +1479,110 @@ namespace {
 
 // The launches of `nsteps` whole steps from time level c->cur (advanced as
 // they are issued), step s writing outs[s].
+// One step of main.f:690-972 with the energy equation: momentum/energy
+// iterations (main.f:736-879) whose launches after convergence skip on the
+// device, then the step tail (kernels in w2_thermal.cuh).
+int issue_thermal_step(w2_ctx *c, const w2_params *prm, const double *un, const double *vn,
+                       const double *pn, double *us, double *vs, double *p, StepOut *o) {
+  const w2_thermal &tp = c->therm_p;
+  const bool therm = tp.nthermen == 1, eqs = tp.neqstate == 1;
+  int nme = tp.nmeiter;
+  if (!therm && nme > 0) nme = 1;  // main.f:736
+  const int gb = grid_blocks(c);
+  const int a = c->cur, b = 1 - a;
+  double *tn = c->T[a], *ts = c->T[b];
+  Dev d = c->dev;
+  int rc = W2_OK;
+  {
+    ProfScope ps(c, W2_K_COPY);
+    c->launches++;
+    k_copy_th<<<gb, c->threads, 0, c->st>>>(d, us, un, vs, vn, p, pn, ts, tn, c->Ddn, c->Dd);
+    CK(cudaGetLastError());
+  }
+  for (int l = 1; l <= nme; ++l) {
+    Dev dl = d;
+    dl.me_gate = l >= 2 ? 1 : 0;
+    dl.den = c->Dd;
+    dl.denn = c->Ddn;
+    dl.fr = prm->fr;
+    if (l >= 2) {
+      c->launches++;
+      k_me_begin<<<gb, c->threads, 0, c->st>>>(dl, un, vn, us, vs, ts, c->Up, c->Vp, c->Tp);
+      CK(cudaGetLastError());
+    }
+    {
+      int blocks = pick_blocks(c, (const void *)k_naux, (long)c->nx * c->ny, naux_smem(c));
+      ProfScope ps(c, W2_K_MOMENTUM);
+      int mq = prm->mqiter;
+      double dk = prm->dk, re = prm->re, qtol = prm->qtol;
+      void *args[] = {&dl, &mq, &dk, &re, &qtol, (void *)&un, (void *)&vn, &us, &vs, &o};
+      if ((rc = coop(c, (const void *)k_naux, blocks, args, naux_smem(c)))) return rc;
+    }
+    {
+      ProfScope ps(c, W2_K_BC);
+      c->launches++;
+      k_bc<<<1, c->threads, 0, c->st>>>(dl, BC_VEL | BC_PRES, us, vs, p);
+      CK(cudaGetLastError());
+    }
+    {
+      ProfScope ps(c, W2_K_PPE);
+      if (tiled_applies(c, prm->npsolver, prm->sorrel)) {
+        if ((rc = launch_ppe_tiled(c, prm->lcartes, prm->msorit, prm->dk, prm->sortol, us, vs, p, o, &dl)))
+          return rc;
+      } else {
+        int blocks = (prm->npsolver == 1 || prm->npsolver == 2)
+                         ? 1 : pick_blocks(c, (const void *)k_ppe, (long)c->nx * c->ny);
+        int lc = prm->lcartes, ns = prm->npsolver, ms = prm->msorit;
+        double dk = prm->dk, st = prm->sortol, sr = prm->sorrel;
+        void *args[] = {&dl, &lc, &ns, &ms, &dk, &st, &sr, &us, &vs, &p, &o};
+        if ((rc = coop(c, (const void *)k_ppe, blocks, args))) return rc;
+      }
+    }
+    {
+      ProfScope ps(c, W2_K_POST);
+      int blocks = pick_blocks(c, (const void *)k_me_post, (long)c->nx * c->ny);
+      double dk = prm->dk;
+      void *args[] = {&dl, &dk, &p, &us, &vs};
+      if ((rc = coop(c, (const void *)k_me_post, blocks, args))) return rc;
+    }
+    if (therm) {
+      ProfScope ps(c, W2_K_THERM);
+      Chain ch = c->therm_ch;  // segments of the current chain view
+      ch.L = d.seg;
+      ch.nseg = (ch.n + d.seg - 1) / d.seg;
+      ThermArgs A{c->therm_tt, prm->dk, tp.pe, un, vn, us, vs, tn, ts, d.cj1x, d.cj2x, d.c1sx, d.c2sx, ch};
+      int blocks = pick_blocks(c, (const void *)k_therm, (long)c->nx * c->ny, naux_smem(c));
+      void *args[] = {&dl, &A};
+      if ((rc = coop(c, (const void *)k_therm, blocks, args, naux_smem(c)))) return rc;
+    }
+    if (eqs) {
+      ProfScope ps(c, W2_K_THERM);
+      c->launches++;
+      k_eq_state<<<gb, c->threads, 0, c->st>>>(dl, tp.uref, tp.densref, tp.tmax, tp.tref, tp.rconst, p, ts,
+                                               c->Dd);
+      CK(cudaGetLastError());
+    }
+    if (l >= 2 && l < nme) {
+      ProfScope ps(c, W2_K_POST);
+      int blocks = pick_blocks(c, (const void *)k_me_norms, (long)c->nx * c->ny);
+      int ll = l;
+      double tol = tp.dmeittol;
+      const double *up = c->Up, *vp = c->Vp, *tpv = c->Tp;
+      void *args[] = {&dl, &ll, &tol, (void *)&up, (void *)&vp, (void *)&tpv, &us, &vs, &ts};
+      if ((rc = coop(c, (const void *)k_me_norms, blocks, args))) return rc;
+    }
+  }
+  {
+    ProfScope ps(c, W2_K_POST);
+    int blocks = pick_blocks(c, (const void *)k_step_tail_th, (long)c->nx * c->ny);
+    ThermTables tt = c->therm_tt;
+    int th = therm ? 1 : 0;
+    void *args[] = {&d, &tt, &th, &p, (void *)&pn, (void *)&un, (void *)&vn, &us, &vs, &tn, &ts, &o};
+    if ((rc = coop(c, (const void *)k_step_tail_th, blocks, args))) return rc;
+  }
+  return rc;
+}
+
 int issue_steps(w2_ctx *c, const w2_params *prm, int nsteps, StepOut *d_outs) {
   int rc = W2_OK;
   const int gb = grid_blocks(c);
@@ -1441,6 +1593,11 @@ int issue_steps(w2_ctx *c, const w2_params *prm, int nsteps, StepOut *d_outs) {
     StepOut *o = d_outs + s;
     Dev d = c->dev;
     const bool mixed = prm->precision == W2_PREC_MIXED;
+    if (c->therm_on) {
+      if ((rc = issue_thermal_step(c, prm, un, vn, pn, us, vs, p, o))) break;
+      c->cur = b;
+      continue;
+    }
     if (mixed) {
       float *un32 = c->F32[0], *vn32 = c->F32[1], *us32 = c->F32[2], *vs32 = c->F32[3];
       {
@@ -1527,6 +1684,14 @@ std::string graph_key(const w2_ctx *c, const w2_params *prm, int nsteps) {
   add(&c->tg, sizeof(c->tg));
   const size_t sm[] = {c->mixed_smem, c->tiled_smem};
   add(sm, sizeof(sm));
+  add(&c->therm_on, sizeof(c->therm_on));
+  if (c->therm_on) {
+    add(&c->therm_p, sizeof(c->therm_p));
+    add(&c->therm_tt, sizeof(c->therm_tt));
+    add(&c->therm_ch, sizeof(c->therm_ch));
+    const double *bufs[] = {c->T[0], c->T[1], c->Dd, c->Ddn, c->Up, c->Vp, c->Tp};
+    add(bufs, sizeof(bufs));
+  }
   return k;
 }
 
@@ -1545,6 +1710,8 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
   if (rc) return rc;
   if ((rc = check_params(c, prm))) return rc;
   if (nsteps < 0) return fail(c, W2_E_ARG, "nsteps < 0");
+  if (c->therm_on && (prm->precision != W2_PREC_FP64 || prm->nfiltu == 1 || prm->nfiltv == 1))
+    return fail(c, W2_E_UNSUPPORTED, "the time loop with the energy equation runs plain FP64 without Filter");
   if (prm->precision == W2_PREC_MIXED && (rc = ensure_f32(c))) return rc;
   std::vector<StepOut> outs((size_t)std::max(nsteps, 1));
   if (nsteps > c->outs_cap) {
@@ -1601,7 +1768,7 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
   if (rc == W2_OK) rc = rs;
   int diverged_at = -1;
   for (int s = 0; s < nsteps; ++s) {
-    double mx = std::max(std::max(outs[s].dif[0], outs[s].dif[1]), outs[s].dif[2]);
+    double mx = std::max(std::max(std::max(outs[s].dif[0], outs[s].dif[1]), outs[s].dif[2]), outs[s].dif[3]);
     if (stats) {
       stats[s].nQLiter = outs[s].nql;
       stats[s].nSorConv = outs[s].nsor;
@@ -1886,6 +2053,8 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
     w2_ctx *c = e->cs[k];
     if (!c) return bad(efail(e, W2_E_ARG, "case %d is null", k));
     if (int rc = ready(c)) return bad(efail(e, rc, "case %d: %s", k, c->err));
+    if (c->therm_on)
+      return bad(efail(e, W2_E_UNSUPPORTED, "case %d: ensembles do not run the energy equation", k));
     unit = unit && c->dev.ppe_unit;
     if (k == 0) e->device = c->device;
     else if (c->device != e->device) return bad(efail(e, W2_E_ARG, "cases on different devices"));
@@ -2573,6 +2742,7 @@ int adj_check(w2_ctx *c, const w2_params *prm) {
   if (prm->npsolver != 5 || !prm->lcartes)
     return fail(c, W2_E_UNSUPPORTED, "the adjoint supports ppe_solver rb_sor (5) on Cartesian grids");
   if (prm->nfiltu == 1 || prm->nfiltv == 1) return fail(c, W2_E_UNSUPPORTED, "the adjoint does not cover Filter");
+  if (c->therm_on) return fail(c, W2_E_UNSUPPORTED, "the adjoint does not cover the energy equation");
   return W2_OK;
 }
 

@@ -119,6 +119,7 @@ struct Sync {
                                // [17..40] mixed PPE ring
   int iout[8];                 // chain verification flags ([0..2] fwd, [3..5] bwd)
   double dout[8];              // small double results
+  int me_done;                 // the momentum/energy iterations of this step converged
 };
 
 struct Dev {
@@ -151,6 +152,7 @@ struct Dev {
   // YMomentum (momentum.f:703), FP64 path; null when the density is zero
   const double *den, *denn;
   double fr;
+  int me_gate;         // a launch of momentum/energy iteration >= 2: skipped once they converged
 };
 
 __device__ __forceinline__ size_t IX(const Dev &d, int i, int j) {
@@ -173,6 +175,12 @@ __device__ __forceinline__ void set_error(Sync *s, int code) {
 __device__ __forceinline__ int read_error(Sync *s) {
   return cuda::atomic_ref<int, cuda::thread_scope_device>(s->error).load(
       cuda::memory_order_acquire);
+}
+
+// A launch of the time step skips its work once the run has halted (a step
+// diverged) or, inside momentum/energy iterations 2.., once they converged.
+__device__ __forceinline__ bool step_skip(const Dev &d) {
+  return d.sync->halt || (d.me_gate && d.sync->me_done);
 }
 
 // ---- virtual grid ---------------------------------------------------------

@@ -165,7 +165,7 @@ __device__ __forceinline__ void copy3_body(const Dev &d, double *a, const double
 __global__ void k_copy3(Dev d, double *a, const double *a0, double *b, const double *b0,
                         double *c, const double *c0) {
   vgrid_set(0, gridDim.x);
-  if (d.sync->halt) return;
+  if (step_skip(d)) return;
   copy3_body(d, a, a0, b, b0, c, c0);
 }
 
@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) k_naux(Dev d, int mqiter, doub
                                                       const double *vn, double *us, double *vs,
                                                       StepOut *out) {
   vgrid_set(0, gridDim.x);
-  if (d.sync->halt) return;
+  if (step_skip(d)) return;
   int res = -1;
   if (!naux_momentum<double>(d, d.f64, mqiter, dk, re, qtol, un, vn, us, vs, &res)) return;
   if (vblock() == 0 && threadIdx.x == 0) out->nql = res;
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) k_naux32(Dev d, int mqiter, do
                                                         const float *vn, float *us, float *vs,
                                                         double *us64, double *vs64, StepOut *out) {
   vgrid_set(0, gridDim.x);
-  if (d.sync->halt) return;
+  if (step_skip(d)) return;
   naux32_body(d, mqiter, dk, re, qtol, un, vn, us, vs, us64, vs64, out);
 }
 
@@ -265,7 +265,8 @@ __device__ __forceinline__ void bc_body(const Dev &d, int ops, double *u, double
 
 __global__ void k_bc(Dev d, int ops, double *u, double *v, double *p) {
   vgrid_set(0, gridDim.x);
-  if (d.sync->halt) return;
+  if (step_skip(d)) return;
+  if (step_skip(d)) return;
   bc_body(d, ops, u, v, p);
 }
 
@@ -301,7 +302,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_ppe(Dev d, int lcartes, int nps
                                                      const double *u, const double *v, double *p,
                                                      StepOut *out) {
   vgrid_set(0, gridDim.x);
-  if (d.sync->halt) return;
+  if (step_skip(d)) return;
   ppe_body(d, lcartes, npsolver, msorit, dk, sortol, sorrel, u, v, p, out);
 }
 
@@ -312,7 +313,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) k_ppe_tiled(Dev d, TileGeom g,
                                                            const double *u, const double *v,
                                                            double *p, StepOut *out) {
   vgrid_set(0, gridDim.x);
-  if (d.sync->halt) return;
+  if (step_skip(d)) return;
   Sync *sy = d.sync;
   ppe_divergence(d, u, v);
   if (!grid_sync(sy)) return;
@@ -330,7 +331,7 @@ template <int K, bool RES>
 __global__ void __launch_bounds__(kMixedThreads, 1) k_ppe_mixed(Dev d, MixedGeom g, MixedArgs a,
                                                       StepOut *out) {
   vgrid_set(0, gridDim.x);
-  if (d.sync->halt) return;
+  if (step_skip(d)) return;
   const int nconv = ppe_mixed<K, RES>(d, g, a);
   if (nconv < 0) return;
   if (vblock() == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? a.msorit : nconv;
@@ -363,7 +364,7 @@ __device__ void project_grid(const Dev &d, double dk, const double *p, double *u
 
 __global__ void k_project(Dev d, double dk, const double *p, double *u, double *v) {
   vgrid_set(0, gridDim.x);
-  if (d.sync->halt) return;
+  if (step_skip(d)) return;
   project_grid(d, dk, p, u, v);
 }
 
@@ -441,7 +442,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_step_post(Dev d, double dk, dou
                                                            const double *vn, double *u,
                                                            double *v, StepOut *out) {
   vgrid_set(0, gridDim.x);
-  if (d.sync->halt) return;
+  if (step_skip(d)) return;
   step_post_body(d, dk, p, pn, un, vn, u, v, out);
 }
 

@@ -20,8 +20,16 @@
 //   T3  t += solution on the interior.
 // Expressions keep the reference's operand order (no FMA contraction in
 // this translation unit), so t matches the reference bit for bit.
+//
+// The time step with the energy equation (main.f:690-972, nthermen = 1) is
+// the plain step's launches inside momentum/energy iterations: k_copy_th,
+// then per iteration [k_me_begin from the second on] k_naux, k_bc, the Ppe
+// kernel, k_me_post, k_therm, k_eq_state, k_me_norms; then k_step_tail_th.
+// Iterations after the convergence test fired skip their launches on the
+// device (Dev::me_gate, Sync::me_done), so a step is one fixed launch
+// sequence and can be captured in a CUDA graph.
 #pragma once
-#include "w2_chain.cuh"
+#include "w2_kernels.cuh"
 
 namespace w2 {
 
@@ -116,6 +124,7 @@ __device__ __forceinline__ void region_of(const Dev &d, int i, int j, int &ir, i
 
 __global__ void __launch_bounds__(kMaxThreads, 1) k_therm(Dev d, ThermArgs A) {
   vgrid_set(0, gridDim.x);
+  if (step_skip(d)) return;
   Sync *sy = d.sync;
   const int nx = d.nx, ny = d.ny;
   const Metrics &m = d.m;
@@ -241,6 +250,7 @@ __global__ void k_temp_bc(Dev d, ThermTables tt, double *t) {
 __global__ void k_eq_state(Dev d, double uref, double densref, double tmax, double tref, double rconst,
                            const double *p, const double *t, double *den) {
   vgrid_set(0, gridDim.x);
+  if (step_skip(d)) return;
   const int nx = d.nx, ny = d.ny;
   const double pref = densref * rconst * tref;
   for (int q = gtid(); q < (nx - 1) * (ny - 1); q += gthreads()) {
@@ -251,6 +261,123 @@ __global__ void k_eq_state(Dev d, double uref, double densref, double tmax, doub
     double r = c1 / c2 - 1.0;
     if (fabs(r) < 1.0e-10) r = 0.0;
     den[o] = r;
+  }
+}
+
+// ---- the time step with the energy equation --------------------------------
+
+// Time levels (main.f:696-704) and the first iterates (main.f:741-747, with
+// nAuxMomentum's us = un): us = un, vs = vn, p = pn, ts = tn on the whole
+// array, dn = d; the momentum/energy iterations start unconverged.
+__global__ void k_copy_th(Dev d, double *us, const double *un, double *vs, const double *vn, double *p,
+                          const double *pn, double *ts, const double *tn, double *dn, const double *den) {
+  vgrid_set(0, gridDim.x);
+  if (d.sync->halt) return;
+  if (vblock() == 0 && threadIdx.x == 0) d.sync->me_done = 0;
+  const int W = d.nx + 2, H = d.ny + 2;
+  for (int q = gtid(); q < W * H; q += gthreads()) {
+    const size_t o = IX(d, q % W, q / W);
+    us[o] = un[o];
+    vs[o] = vn[o];
+    p[o] = pn[o];
+    ts[o] = tn[o];
+    dn[o] = den[o];
+  }
+}
+
+// Iteration l >= 2: keep the previous iterates (u, v, t before this pass,
+// for the convergence norms), then nAuxMomentum's us(1..nx+1,1..ny+1) = un
+// (momentum.f:114-119); ts = t is the array itself.
+__global__ void k_me_begin(Dev d, const double *un, const double *vn, double *us, double *vs,
+                           const double *ts, double *up, double *vp, double *tp) {
+  vgrid_set(0, gridDim.x);
+  if (step_skip(d)) return;
+  const int W = d.nx + 2, H = d.ny + 2;
+  for (int q = gtid(); q < W * H; q += gthreads()) {
+    const int i = q % W, j = q / W;
+    const size_t o = IX(d, i, j);
+    up[o] = us[o];
+    vp[o] = vs[o];
+    tp[o] = ts[o];
+    if (i >= 1 && j >= 1) {
+      us[o] = un[o];
+      vs[o] = vn[o];
+    }
+  }
+}
+
+// After Ppe in an iteration (main.f:818-836): PresBoundCond, Project,
+// VelBoundCond, PresBoundCond.
+__global__ void __launch_bounds__(kMaxThreads) k_me_post(Dev d, double dk, double *p, double *u, double *v) {
+  vgrid_set(0, gridDim.x);
+  if (step_skip(d)) return;
+  Sync *sy = d.sync;
+  if (vblock() == 0 && !pres_bound_cond_block(d, p) && threadIdx.x == 0) set_error(sy, W2_E_BCFLAG);
+  if (!grid_sync(sy)) return;
+  project_grid(d, dk, p, u, v);
+  if (!grid_sync(sy)) return;
+  if (vblock() == 0) {
+    const bool ok = vel_bound_cond_block(d, u, v) && pres_bound_cond_block(d, p);
+    if (!ok && threadIdx.x == 0) set_error(sy, W2_E_BCFLAG);
+  }
+}
+
+// The iteration's convergence norms (main.f:857-877): DiffMaxNorm of the
+// previous and new u, v, t; from iteration 2 on, max < dmeittol ends the
+// iterations.
+__global__ void __launch_bounds__(kMaxThreads) k_me_norms(Dev d, int l, double tol, const double *up,
+                                                         const double *vp, const double *tp,
+                                                         const double *us, const double *vs,
+                                                         const double *ts) {
+  vgrid_set(0, gridDim.x);
+  if (step_skip(d)) return;
+  Sync *sy = d.sync;
+  if (vblock() == 0 && threadIdx.x == 0) sy->red[41] = sy->red[42] = sy->red[43] = 0ull;
+  if (!grid_sync(sy)) return;
+  block_max_to(&sy->red[41], diff_norm_local(d, up, us));
+  block_max_to(&sy->red[42], diff_norm_local(d, vp, vs));
+  block_max_to(&sy->red[43], diff_norm_local(d, tp, ts));
+  if (!grid_sync(sy)) return;
+  if (vblock() == 0 && threadIdx.x == 0) {
+    double mx = slot_value(&sy->red[41]);
+    const double m2 = slot_value(&sy->red[42]), m3 = slot_value(&sy->red[43]);
+    if (m2 > mx) mx = m2;
+    if (m3 > mx) mx = m3;
+    if (l > 1 && mx < tol) sy->me_done = 1;
+  }
+}
+
+// After the iterations (main.f:881-972 without Filter of t): VelBoundCond,
+// PresBoundCond, TempBoundCond on the new level, the step norms of p, u, v, t
+// and the divergence test.
+__global__ void __launch_bounds__(kMaxThreads) k_step_tail_th(Dev d, ThermTables tt, int therm, double *p,
+                                                             const double *pn, const double *un,
+                                                             const double *vn, double *u, double *v,
+                                                             const double *tn, double *t, StepOut *out) {
+  vgrid_set(0, gridDim.x);
+  if (d.sync->halt) return;
+  Sync *sy = d.sync;
+  if (vblock() == 0) {
+    const bool ok = vel_bound_cond_block(d, u, v) && pres_bound_cond_block(d, p);
+    if (!ok && threadIdx.x == 0) set_error(sy, W2_E_BCFLAG);
+    if (therm) temp_bc_block(d, tt, t);
+    if (threadIdx.x == 0) sy->red[6] = sy->red[7] = sy->red[8] = sy->red[16] = sy->red[44] = 0ull;
+  }
+  if (!grid_sync(sy)) return;
+  block_max_to(&sy->red[6], diff_norm_local(d, pn, p));
+  block_max_to(&sy->red[7], diff_norm_local(d, un, u));
+  block_max_to(&sy->red[8], diff_norm_local(d, vn, v));
+  block_max_to(&sy->red[44], diff_norm_local(d, tn, t));
+  block_max_to(&sy->red[16], div_check_local(d, u, v));
+  if (!grid_sync(sy)) return;
+  if (vblock() == 0 && threadIdx.x == 0) {
+    out->dif[0] = slot_value(&sy->red[6]);
+    out->dif[1] = slot_value(&sy->red[7]);
+    out->dif[2] = slot_value(&sy->red[8]);
+    out->dif[3] = slot_value(&sy->red[44]);
+    out->divmax = slot_value(&sy->red[16]);
+    const double mx = dmax(dmax(dmax(out->dif[0], out->dif[1]), out->dif[2]), out->dif[3]);
+    if (mx > 1.0e12) sy->halt = 1;
   }
 }
 

@@ -386,6 +386,23 @@ class Thermal:
 
 
 @dataclasses.dataclass
+class ThermalParams:
+    """Thermal switches and constants of the time loop: ReadParam's
+    nthermen, neqstate, nmeiter, dmeittol (defaults src/parse.f:118-159),
+    pe = re * Prandtl (src/file_manip.f:158) and EqState's constants."""
+    nthermen: int = 1
+    neqstate: int = 0
+    nmeiter: int = 1
+    dmeittol: float = 1.0e-4
+    pe: float = 1.0
+    uref: float = 1.0
+    densref: float = 1.0
+    tmax: float = 1.0
+    tref: float = 0.0
+    rconst: float = 1.0
+
+
+@dataclasses.dataclass
 class Case:
     """Everything the hot path needs for one instance."""
     name: str
@@ -396,6 +413,8 @@ class Case:
     regions: Regions
     params: RunParams
     bc_text: str = ""
+    thermal: Optional[Thermal] = None        # thermal tables (nthermen = 1)
+    tparams: Optional[ThermalParams] = None
 
     @property
     def cells(self) -> int:
@@ -426,6 +445,30 @@ def cavity(n: int, re: float, dt: float, *, lid: float = 1.0,
                            npsolver=PPE_SOLVERS[solver], lcartes=1, **kw)
     regs = parse_bc_section(bc, nx, nyy, re=prm.re)
     return Case(f"cavity{n}x{ncy}_re{re:g}", nx, nyy, X, Y, regs, prm, bc)
+
+
+def heated_cavity(n: int, re: float, dt: float, *, pr: float = 0.71, fr: float = 0.05,
+                  lid: float = 0.0, nmeiter: int = 3, dmeittol: float = 1.0e-6,
+                  eqstate: bool = True, solver: str = "rb_sor", t_hot: float = 1.0,
+                  t_cold: float = 0.0, **kw) -> Case:
+    """Differentially heated cavity: the cavity of :func:`cavity` (moving
+    lid optional) with the energy equation on (nthermen = 1, pe = re * pr):
+    west wall at t_hot, east wall at t_cold (fixed temperature), adiabatic
+    south and north walls (zero heat flux); with ``eqstate`` the density of
+    the ideal-gas EqState (tref = 300, tmax = 330, so d ~ -0.1 t) drives the
+    buoyancy term of YMomentum at Froude number ``fr``."""
+    case = cavity(n, re, dt, lid=lid, solver=solver, **kw)
+    case.params.fr = fr
+    th = Thermal.empty()
+    th.nTemBdTp[0, 0, :] = (BT_TEMPER, BT_TEMPER, BT_HTFLUX, BT_HTFLUX)
+    case.regions.dBCVal[0, 0, WEST - 1, VAR_T - 1] = t_hot
+    case.regions.dBCVal[0, 0, EAST - 1, VAR_T - 1] = t_cold
+    case.thermal = th
+    case.tparams = ThermalParams(nthermen=1, neqstate=1 if eqstate else 0, nmeiter=nmeiter,
+                                 dmeittol=dmeittol, pe=case.params.re * pr, uref=1.0, densref=1.0,
+                                 tmax=330.0, tref=300.0, rconst=287.0)
+    case.name = f"heated_{case.name}"
+    return case
 
 
 def channel(ncx: int, ncy: int, re: float, dt: float, *, length: float = 4.0,

@@ -29,9 +29,15 @@ ERRORS = {1: "bad argument", 2: "CUDA error", 3: "device wait timed out",
           8: "larger than the allocation-free scratch"}
 NOALLOC_MAX_POINTS = 1200000
 PREC_FP64, PREC_MIXED = 0, 1
-K_MOMENTUM, K_PPE, K_POST, K_BC, K_COPY = range(5)
+K_MOMENTUM, K_PPE, K_POST, K_BC, K_COPY, K_THERM = range(6)
 KERNEL_NAMES = {K_MOMENTUM: "k_naux", K_PPE: "k_ppe", K_POST: "k_step_post",
-                K_BC: "k_bc", K_COPY: "k_copy3"}
+                K_BC: "k_bc", K_COPY: "k_copy3", K_THERM: "k_therm"}
+
+
+class ThermalC(C.Structure):
+    """w2_thermal of include/wolfd2_gpu.h."""
+    _fields_ = [(n, C.c_int) for n in ("nthermen", "neqstate", "nmeiter")] + \
+               [(n, C.c_double) for n in ("dmeittol", "pe", "uref", "densref", "tmax", "tref", "rconst")]
 
 # metric order of the C-ABI = argument order of grid.f:Grid
 METRIC_ORDER = ("rau rbu rbv rgv ran rbn rgn rac rbc rgc dju djv djc djn xen yen xzn yzn "
@@ -100,6 +106,9 @@ def lib():
     L.wolfd2gpu_temp_bound_cond.argtypes = [vp, _ip, _ip, _ip, _ip, _dp, _dp]
     L.wolfd2gpu_therm_energy.argtypes = [vp, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp] + [_dp] * 6
     L.wolfd2gpu_eq_state.argtypes = [vp, _ip, _ip] + [_dp] * 8
+    L.wolfd2gpu_set_thermal.argtypes = [vp, C.POINTER(ThermalC), _ip, _ip, _dp, _dp]
+    L.wolfd2gpu_load_thermal.argtypes = [vp, _dp, _dp]
+    L.wolfd2gpu_store_thermal.argtypes = [vp, _dp, _dp]
     L.wolfd2gpu_load_fields.argtypes = [vp, _dp, _dp, _dp]
     L.wolfd2gpu_store_fields.argtypes = [vp, _dp, _dp, _dp]
     L.wolfd2gpu_cold_start.argtypes = [vp, C.POINTER(Params), _ip]
@@ -201,6 +210,8 @@ class Solver:
         s.grid_metric(case.x, case.y)
         for (ir, jr, face, var), vals in getattr(case.regions, "profiles", {}).items():
             s.set_face_profile(ir, jr, face, var, vals)
+        if getattr(case, "tparams", None) is not None and getattr(case, "thermal", None) is not None:
+            s.set_thermal(case.tparams, case.thermal)
         if tuned:
             from . import autotune
             autotune.apply(s, autotune.lookup(case.nx, case.ny, precision))
@@ -331,6 +342,30 @@ class Solver:
                                               _d(tmax), _d(tref), _d(rconst), _p(p), _p(t), _p(den)))
 
     # ---- device-resident time loop ---------------------------------------
+    def set_thermal(self, tparams=None, th=None) -> None:
+        """Time loop with the energy equation (deck.ThermalParams and
+        deck.Thermal tables); None returns to the plain loop."""
+        if tparams is None:
+            self._check(self.L.wolfd2gpu_set_thermal(self.h, None, None, None, None, None))
+            return
+        tp = tparams
+        c = ThermalC(tp.nthermen, tp.neqstate, tp.nmeiter, tp.dmeittol, tp.pe, tp.uref, tp.densref,
+                     tp.tmax, tp.tref, tp.rconst)
+        rt, prt = self._ttab(th.nTRgType, np.int32)
+        bt, pbt = self._ttab(th.nTemBdTp, np.int32)
+        tv, ptv = self._ttab(th.dTRgVal, np.float64)
+        hg, phg = self._ttab(th.dHGSTval, np.float64)
+        self._check(self.L.wolfd2gpu_set_thermal(self.h, C.byref(c), prt, pbt, ptv, phg))
+
+    def load_thermal(self, t, d=None) -> None:
+        self._check(self.L.wolfd2gpu_load_thermal(self.h, _p(t), None if d is None else _p(d)))
+
+    def store_thermal(self):
+        t = np.zeros((self.mnx + 1, self.mny + 1), order="F")
+        d = np.zeros_like(t)
+        self._check(self.L.wolfd2gpu_store_thermal(self.h, _p(t), _p(d)))
+        return t, d
+
     def load_fields(self, u, v, p) -> None:
         self._check(self.L.wolfd2gpu_load_fields(self.h, _p(u), _p(v), _p(p)))
 
