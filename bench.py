@@ -116,10 +116,16 @@ class ClockSampler:
 CHANNEL = {"ncx": 4096, "ncy": 1024, "re": 10000.0, "dt": 2.5e-4}
 
 
+THERMAL = {"nmeiter": 2, "dmeittol": 0.0, "pr": 0.71, "fr": 0.05}
+
+
 def make_case(args):
     if args.workload == "channel":
         return deck.channel_inflow(CHANNEL["ncx"], CHANNEL["ncy"], CHANNEL["re"], CHANNEL["dt"],
                                    seed=args.seed, solver=args.solver)
+    if args.workload == "thermal":
+        return deck.heated_cavity(args.n, args.re, args.dt, solver=args.solver, pr=THERMAL["pr"],
+                                  fr=THERMAL["fr"], nmeiter=THERMAL["nmeiter"], dmeittol=THERMAL["dmeittol"])
     return deck.cavity(args.n, args.re, args.dt, solver=args.solver)
 
 
@@ -127,6 +133,14 @@ def make_ic(args, case, rank=0):
     if args.workload == "channel":
         return deck.channel_ic(case)
     return deck.perturbation_ic(case, args.seed + rank)
+
+
+def make_t0(case):
+    """Initial temperature of the heated cavity: linear from the hot west
+    wall (1) to the cold east wall (0) over the cell centres."""
+    t = np.zeros((case.nx + 2, case.ny + 2), order="F")
+    t[...] = (1.0 - (np.arange(case.nx + 2) - 0.5) / (case.nx - 1))[:, None]
+    return np.asfortranarray(np.clip(t, 0.0, 1.0))
 
 
 def ppe_bytes(cells, nsor):
@@ -146,7 +160,7 @@ def step_bytes(cells, nql, nsor):
     return 8.0 * cells * (6 * nql + 3 + 3 * nsor + 5 + 3)
 
 
-def reference_runner(case, ic):
+def reference_runner(case, ic, t0=None):
     """The host-side reference run: the mechanical translation of the
     reference's Fortran source (oracle/f77ref.py, kind "reference") when its
     generated C is present, else the oracle's restatement (kind "port").
@@ -156,6 +170,8 @@ def reference_runner(case, ic):
     import oracle as O
     u, v, p = ic
     fields = {"u": u, "v": v, "p": p}
+    if t0 is not None:
+        fields["t"] = t0
     if getattr(case.regions, "profiles", None):
         # the reference has no per-row inflow: time the restatement with the shim
         return O.OracleRun(case, fields=fields, cold_start=False), "port", \
@@ -171,10 +187,10 @@ def reference_runner(case, ic):
         "C restatement of the reference (oracle), gcc -O2, 1 thread"
 
 
-def cpu_step_sample(case, ic, nsteps=1):
+def cpu_step_sample(case, ic, nsteps=1, t0=None):
     """Time `nsteps` full reference steps on the host; returns
     (cell-steps/s, seconds, threads, kind, how)."""
-    r, kind, how = reference_runner(case, ic)
+    r, kind, how = reference_runner(case, ic, t0)
     t0 = time.perf_counter()
     r.step(nsteps)
     dt = time.perf_counter() - t0
@@ -230,7 +246,7 @@ def run_reference(args):
         return
     case = make_case(args)
     ic = make_ic(args, case)
-    r, kind, how = reference_runner(case, ic)
+    r, kind, how = reference_runner(case, ic, make_t0(case) if args.workload == "thermal" else None)
     r.step(args.warmup)
     t0 = time.perf_counter()
     r.step(args.steps)
@@ -255,7 +271,15 @@ def config_of(args, case, inner=None):
             f"FP64 Poisson residual and correction ({inner} sweeps per refinement pass), FP64 "
             "divergence check, projection and norms; plain FP64 timed beside it"
             if args.precision == "mixed" else "plain FP64")
-    if args.workload == "channel":
+    if args.workload == "thermal":
+        work = (f"differentially heated cavity {args.n}x{args.n} cells, Re={args.re:g}, dt={args.dt:g}, "
+                f"energy equation on (Pe = Re x {THERMAL['pr']}), west wall t=1, east wall t=0, adiabatic "
+                f"south/north, ideal-gas EqState density (tref 300, tmax 330) driving the buoyancy term at "
+                f"Fr={THERMAL['fr']}, {THERMAL['nmeiter']} momentum/energy iterations per step "
+                f"(dmeittol {THERMAL['dmeittol']:g}: all run), seeded 16x16-mode velocity perturbation "
+                f"(seed {args.seed}), linear initial temperature, ppe_solver {args.solver}, plain FP64")
+        re, dt = args.re, args.dt
+    elif args.workload == "channel":
         work = (f"plane channel {CHANNEL['ncx']}x{CHANNEL['ncy']} cells, length 4 x height 1, "
                 f"Re=5000 on the half-height (deck Re={CHANNEL['re']:g}), dt={CHANNEL['dt']:g}, "
                 f"parabolic inflow + seeded 16-mode Fourier perturbation (amplitude 1e-2, seed {args.seed}) "
@@ -282,13 +306,16 @@ def mixed_ppe_bytes(cells, nsor, inner):
     return cells * (24.0 + passes * 40.0 + 12.0 * nsor)
 
 
-def run_arm(s, prm, args, precision, u0, v0, p0, st, flush, barrier, local, timed=True):
+def run_arm(s, prm, args, precision, u0, v0, p0, st, flush, barrier, local, timed=True, t0=None):
     """Warm-up then `steps` device-timed steps of one precision mode from the
-    same initial fields; returns the measurements and the final fields."""
-    from wolfd2_gb300.gpu import K_BC, K_COPY, K_MOMENTUM, K_POST, K_PPE
+    same initial fields (and temperature t0 with the energy equation);
+    returns the measurements and the final fields."""
+    from wolfd2_gb300.gpu import K_BC, K_COPY, K_MOMENTUM, K_POST, K_PPE, K_THERM
     import torch
     kw = {"precision": precision, "refine_sweeps": args.refine_sweeps}
     s.load_fields(u0, v0, p0)
+    if t0 is not None:
+        s.load_thermal(t0)
     # single-step warm-up calls: the step's CUDA graphs (one per time-level
     # parity) are captured here, outside the timed region
     hist = []
@@ -316,25 +343,32 @@ def run_arm(s, prm, args, precision, u0, v0, p0, st, flush, barrier, local, time
     s.profile(True)
     for _ in range(args.steps):
         hist += s.step(prm, 1, **kw)
-    prof = {k: s.profile_read(k) for k in (K_MOMENTUM, K_PPE, K_POST, K_BC, K_COPY)}
+    kinds = (K_MOMENTUM, K_PPE, K_POST, K_BC, K_COPY) + ((K_THERM,) if t0 is not None else ())
+    prof = {k: s.profile_read(k) for k in kinds}
     s.profile(False)
     fields = s.store_fields()
+    if t0 is not None:
+        fields = tuple(fields) + (s.store_thermal()[0],)
     # end-to-end through the C-ABI with pinned host buffers, the copies in
     # the timed region: each step loads u, v, p, runs, and reads them back
     pinned = [torch.empty((s.mny + 1, s.mnx + 1), dtype=torch.float64, pin_memory=True)
-              for _ in range(3)]
+              for _ in range(len(fields))]
     host = [t.numpy().T for t in pinned]  # Fortran-ordered views of pinned memory
     for h, f in zip(host, fields):
         h[...] = f
     e2e_steps = max(1, min(args.steps, args.e2e_steps))
     barrier()
-    t0 = time.perf_counter()
+    tw0 = time.perf_counter()
     for _ in range(e2e_steps):
-        s.load_fields(*host)
+        s.load_fields(*host[:3])
+        if t0 is not None:
+            s.load_thermal(host[3])
         s.step(prm, 1, **kw)
-        s.store_fields(out=host)
+        s.store_fields(out=host[:3])
+        if t0 is not None:
+            s.store_thermal(out=host[3])
     barrier()
-    t_e2e = time.perf_counter() - t0
+    t_e2e = time.perf_counter() - tw0
     return {"t_dev": t_dev, "t_e2e": t_e2e, "e2e_steps": e2e_steps, "hist": hist,
             "timed": hist[args.warmup:args.warmup + args.steps], "profiled": hist[-args.steps:],
             "prof": prof, "launches": launches,
@@ -371,6 +405,9 @@ def roofline_of(arm, cells, precision, inner, tiled=True):
     else:
         alg = sum(mom_bytes(cells, n, 4 if precision == "mixed" else 8) for n in nql)
     dom_ms, dom_n = prof[dom]
+    # with momentum/energy iterations a step launches the kernel once per
+    # iteration; the step record holds the last iteration's counts
+    alg *= dom_n / max(1, len(timed))
     name = kernel_name(dom, precision, tiled)
     achieved = alg / (dom_ms / 1e3) / 1e9
     traffic = None
@@ -415,6 +452,10 @@ def run_ours(args):
 
     case = make_case(args)
     u0, v0, p0 = make_ic(args, case, rank)
+    t0 = None
+    if args.workload == "thermal":
+        args.precision = "fp64"  # the loop with the energy equation is plain FP64
+        t0 = make_t0(case)
     s = Solver.for_case(case)
     if args.threads or args.blocks_per_sm or args.seg or args.warm:
         s.tune(seg=args.seg, warm=args.warm, threads=args.threads, blocks_per_sm=args.blocks_per_sm)
@@ -435,7 +476,7 @@ def run_ours(args):
     order = ["fp64", "mixed"] if args.precision == "mixed" else ["fp64"]
     for name in order:
         arms[name] = run_arm(s, prm, args, PREC_MIXED if name == "mixed" else PREC_FP64,
-                             u0, v0, p0, st, flush, barrier, local)
+                             u0, v0, p0, st, flush, barrier, local, t0=t0)
     head = arms[args.precision]
 
     # max over ranks
@@ -453,6 +494,7 @@ def run_ours(args):
 
     cells = case.cells
     field_bytes = (case.nx + 2) * (case.ny + 2) * 8
+    nfields = 4 if t0 is not None else 3
     value = world * cells * args.steps / t_max
     e2e_value = world * cells * head["e2e_steps"] / t_e2e_max
     # the plain path's red/black solve runs on shared-memory tiles at this size
@@ -494,7 +536,7 @@ def run_ours(args):
         }
     cpu = None
     if not args.no_cpu_baseline:
-        cv, csec, cores, kind, how = cpu_step_sample(case, (u0, v0, p0), 1)
+        cv, csec, cores, kind, how = cpu_step_sample(case, (u0, v0, p0), 1, t0)
         cpu = {"value": cv, "unit": UNIT, "cores": cores, "kind": kind,
                "sample": f"1 full time step of the same {case.nx - 1}x{case.ny - 1} case from the same initial "
                          f"state ({csec:.1f} s); {how}"}
@@ -509,8 +551,8 @@ def run_ours(args):
         "parallelism": "replicas only" if world > 1 else "single GPU",
         "roofline": roof,
         "fp64_roof": fp64,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 3 * field_bytes,
-                "d2h_bytes_per_step": 3 * field_bytes, "steps": head["e2e_steps"],
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nfields * field_bytes,
+                "d2h_bytes_per_step": nfields * field_bytes, "steps": head["e2e_steps"],
                 "host_buffers": "pinned"},
         "plain_fp64": plain,
         "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
@@ -860,10 +902,12 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["cavity", "channel", "ensemble", "adjoint"], default="cavity",
+    ap.add_argument("--workload", choices=["cavity", "channel", "ensemble", "adjoint", "thermal"],
+                    default="cavity",
                     help="cavity: the lid-driven cavity (--n cells per side); channel: the "
                          "4096x1024 plane channel with a profiled inflow; ensemble: 256 cavities "
-                         "of uneven size and Re advanced together")
+                         "of uneven size and Re advanced together; thermal: the differentially "
+                         "heated cavity with the energy equation (--n cells per side)")
     ap.add_argument("--ens-count", type=int, default=ENSEMBLE["count"])
     ap.add_argument("--ens-seed", type=int, default=ENSEMBLE["seed"])
     ap.add_argument("--no-graph", action="store_true", help="ensemble: launch directly, no CUDA graph")

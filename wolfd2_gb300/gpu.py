@@ -360,7 +360,12 @@ class Solver:
     def load_thermal(self, t, d=None) -> None:
         self._check(self.L.wolfd2gpu_load_thermal(self.h, _p(t), None if d is None else _p(d)))
 
-    def store_thermal(self):
+    def store_thermal(self, out=None):
+        """(t, d) to new host arrays, or t alone into `out` (a Fortran-ordered
+        float64 array, for example a pinned buffer); returns (t, d)."""
+        if out is not None:
+            self._check(self.L.wolfd2gpu_store_thermal(self.h, _p(out), None))
+            return out, None
         t = np.zeros((self.mnx + 1, self.mny + 1), order="F")
         d = np.zeros_like(t)
         self._check(self.L.wolfd2gpu_store_thermal(self.h, _p(t), _p(d)))
