@@ -77,3 +77,34 @@ def test_deck_files(tmp_path):
     sec = txt.split("section boundary_conditions")[1].split("end section")[0]
     r = deck.parse_bc_section(sec, c.nx, c.ny)
     assert np.array_equal(r.nMomBdTp, c.regions.nMomBdTp)
+
+
+def test_thermal_keywords():
+    """parse.f's thermal keywords: defaults (adiabatic outer walls,
+    interfaces inside), temperatures on walls scaled to (T - tref)/(tmax -
+    tref), fixed-temperature blocks with their neighbours' faces, heat
+    generation regions and the coinciding-face pairing of SetUpBCs."""
+    from wolfd2_gb300.deck import (BT_HTFLUX, BT_INTERN, BT_TEMPER, RT_HEATGN, RT_TEMPER, VAR_T,
+                                   heat_sources, parse_bc_section)
+    text = ("number_of_regions 3 2\n i_borders 10 20\n j_borders 8\n"
+            "wall 1 1 west t 350\n blockage 2 1 temper 320\n"
+            "heat_generation_region 3 2 5.0\n fixed_temperature_wall 1 2 north 330\n"
+            "heat_flux_wall 3 1 east\n")
+    r = parse_bc_section(text, 31, 17, tref=300.0, tmax=400.0)
+    th = r.thermal
+    assert th.nTemBdTp[0, 0, deck.WEST - 1] == BT_TEMPER
+    assert r.dBCVal[0, 0, deck.WEST - 1, VAR_T - 1] == (350.0 - 300.0) / 100.0
+    assert th.nTRgType[1, 0] == RT_TEMPER and th.dTRgVal[1, 0] == 0.2
+    assert (th.nTemBdTp[1, 0, :] == BT_TEMPER).all()
+    # the block's neighbours see its temperature on their coinciding faces
+    assert th.nTemBdTp[0, 0, deck.EAST - 1] == BT_TEMPER and th.nTemBdTp[2, 0, deck.WEST - 1] == BT_TEMPER
+    assert th.nTemBdTp[1, 1, deck.SOUTH - 1] == BT_TEMPER
+    assert r.dBCVal[1, 1, deck.SOUTH - 1, VAR_T - 1] == 0.2
+    assert th.nTRgType[2, 1] == RT_HEATGN and th.dTRgVal[2, 1] == 5.0
+    assert th.nTemBdTp[0, 1, deck.NORTH - 1] == BT_TEMPER
+    assert th.nTemBdTp[2, 0, deck.EAST - 1] == BT_HTFLUX
+    # interfaces stay interfaces, outer walls default to adiabatic
+    assert th.nTemBdTp[0, 1, deck.EAST - 1] == BT_INTERN
+    assert th.nTemBdTp[2, 1, deck.NORTH - 1] == BT_HTFLUX
+    heat_sources(r, 1.0, 300.0, 400.0, 2.0, 10.0)
+    assert th.dHGSTval[2, 1] == 5.0 / (10.0 * 2.0 * 100.0)

@@ -62,6 +62,9 @@ class Regions:
     # faces, i on south/north faces); they replace dBCVal in VelBoundCond's
     # inlet and moving-wall rows.
     profiles: dict = dataclasses.field(default_factory=dict)
+    # thermal tables of the same section (parse.f's thermal keywords); face
+    # temperatures are dBCVal(..., VAR_T)
+    thermal: Optional["Thermal"] = None
 
     @property
     def n_i(self) -> int:
@@ -100,7 +103,7 @@ class DeckError(ValueError):
 
 
 def _init_bc_flags(t: Regions) -> None:
-    """InitBCFlags, src/parse.f:2257-2380 (momentum part)."""
+    """InitBCFlags, src/parse.f:2257-2380: momentum and temperature."""
     ni, nj = t.n_i, t.n_j
     t.dBCVal[:ni, :nj, :, :] = 0.0
     t.nRegType[:ni, :nj] = RM_INTERN
@@ -109,16 +112,51 @@ def _init_bc_flags(t: Regions) -> None:
     t.nMomBdTp[ni - 1, :nj, EAST - 1] = BM_WALL1
     t.nMomBdTp[:ni, 0, SOUTH - 1] = BM_WALL1
     t.nMomBdTp[:ni, nj - 1, NORTH - 1] = BM_WALL1
+    # temperature: no sources, interfaces inside, adiabatic outer walls
+    th = t.thermal
+    th.nTRgType[:ni, :nj] = RT_NOSRCE
+    th.nTemBdTp[:ni, :nj, :] = BT_INTERN
+    th.nTemBdTp[0, :nj, WEST - 1] = BT_HTFLUX
+    th.nTemBdTp[ni - 1, :nj, EAST - 1] = BT_HTFLUX
+    th.nTemBdTp[:ni, 0, SOUTH - 1] = BT_HTFLUX
+    th.nTemBdTp[:ni, nj - 1, NORTH - 1] = BT_HTFLUX
 
 
 def parse_bc_section(text: str, nx: int, ny: int, *, uref: float = 1.0,
                      densref: float = 1.0, dlref: float = 1.0,
-                     re: float = 1.0) -> Regions:
+                     re: float = 1.0, tref: float = 0.0, tmax: float = 1.0) -> Regions:
     """Parse a ``boundary_conditions`` section body (lines between
     ``section boundary_conditions`` and ``end section``) and run the
     ``SetUpBCs`` passes.  Keywords are case-insensitive; ``#`` starts a
-    comment (src/parse.f:1168-1210)."""
+    comment (src/parse.f:1168-1210).  Temperatures are scaled to
+    (T - tref) / (tmax - tref) (src/parse.f:1366, 1565, 1834); the thermal
+    tables land in ``Regions.thermal`` (heat generation values stay as read:
+    :func:`heat_sources` scales them)."""
     t = _empty_tables()
+    t.thermal = Thermal.empty()
+    th = t.thermal
+
+    def temp_of(word: str) -> float:
+        try:
+            return (float(word) - tref) / (tmax - tref)
+        except ValueError as exc:
+            raise DeckError(f"expected a temperature, got {word!r}") from exc
+
+    def fixed_temperature(ir: int, jr: int, val: float, neighbours: bool) -> None:
+        """A fixed-temperature region: its faces (and with `neighbours` the
+        coinciding faces of its neighbours) at that temperature."""
+        i0, j0 = ir - 1, jr - 1
+        th.nTRgType[i0, j0] = RT_TEMPER
+        th.dTRgVal[i0, j0] = val
+        th.nTemBdTp[i0, j0, :] = BT_TEMPER
+        t.dBCVal[i0, j0, :, VAR_T - 1] = val
+        if not neighbours:
+            return
+        for di, dj, face in ((-1, 0, EAST), (1, 0, WEST), (0, -1, NORTH), (0, 1, SOUTH)):
+            a, b = i0 + di, j0 + dj
+            if 0 <= a < t.n_i and 0 <= b < t.n_j:
+                th.nTemBdTp[a, b, face - 1] = BT_TEMPER
+                t.dBCVal[a, b, face - 1, VAR_T - 1] = val
     found_nreg = def_i = def_j = False
     perm_eq = np.zeros((MGRI, MGRJ), np.int32, order="F")
     dim_coef = np.zeros((MGRI, MGRJ, 3), np.float64, order="F")
@@ -173,14 +211,27 @@ def parse_bc_section(text: str, nx: int, ny: int, *, uref: float = 1.0,
             ir, jr = need_ij(w, 1)
             t.nRegType[ir - 1, jr - 1] = RM_BLOCKG
             t.nMomBdTp[ir - 1, jr - 1, :] = BM_WALL1
+            th.nTemBdTp[ir - 1, jr - 1, :] = BT_HTFLUX
             if ir > 1:
                 t.nMomBdTp[ir - 2, jr - 1, EAST - 1] = BM_WALL1
+                th.nTemBdTp[ir - 2, jr - 1, EAST - 1] = BT_HTFLUX
             if ir < t.n_i:
                 t.nMomBdTp[ir, jr - 1, WEST - 1] = BM_WALL1
+                th.nTemBdTp[ir, jr - 1, WEST - 1] = BT_HTFLUX
             if jr > 1:
                 t.nMomBdTp[ir - 1, jr - 2, NORTH - 1] = BM_WALL1
+                th.nTemBdTp[ir - 1, jr - 2, NORTH - 1] = BT_HTFLUX
             if jr < t.n_j:
                 t.nMomBdTp[ir - 1, jr, SOUTH - 1] = BM_WALL1
+                th.nTemBdTp[ir - 1, jr, SOUTH - 1] = BT_HTFLUX
+            # src/parse.f:1347-1400: "temper <T>" makes it a fixed-temperature block
+            k = 3
+            while k < len(w):
+                if w[k] in ("temper", "t") and k + 1 < len(w):
+                    fixed_temperature(ir, jr, temp_of(w[k + 1]), True)
+                    k += 2
+                else:
+                    raise DeckError(f"blockage: unrecognized word {w[k]!r}")
         elif key == "porous_region":
             ir, jr = need_ij(w, 1)
             t.nRegType[ir - 1, jr - 1] = RM_POROUS
@@ -229,13 +280,38 @@ def parse_bc_section(text: str, nx: int, ny: int, *, uref: float = 1.0,
                     t.dBCVal[i0, j0, face - 1, VAR_P - 1] = float(rest[k + 1]) / (densref * uref * uref)
                     k += 1
                 elif word in ("temper", "t"):
-                    k += 1  # thermal boundary values: thermal energy is not on this path
+                    if k + 1 >= len(rest):
+                        raise DeckError(f"{key}: temperature value missing")
+                    th.nTemBdTp[i0, j0, face - 1] = BT_TEMPER
+                    t.dBCVal[i0, j0, face - 1, VAR_T - 1] = temp_of(rest[k + 1])
+                    k += 1
                 else:
                     raise DeckError(f"{key}: unrecognized word {word!r}")
                 k += 1
-        elif key in ("heat_generation_region", "fixed_temperature_region",
-                     "fixed_temperature_wall"):
-            continue  # thermal keywords: accepted, not on the momentum path
+        elif key == "heat_generation_region":
+            ir, jr = need_ij(w, 1)
+            if len(w) < 4:
+                raise DeckError("heat_generation_region: value missing")
+            th.nTRgType[ir - 1, jr - 1] = RT_HEATGN
+            th.dTRgVal[ir - 1, jr - 1] = float(w[3])
+        elif key == "fixed_temperature_region":
+            ir, jr = need_ij(w, 1)
+            if len(w) < 4:
+                raise DeckError("fixed_temperature_region: value missing")
+            fixed_temperature(ir, jr, temp_of(w[3]), False)
+        elif key in ("fixed_temperature_wall", "heat_flux_wall"):
+            ir, jr = need_ij(w, 1)
+            if len(w) < 4:
+                raise DeckError(f"{key}: missing face")
+            face = face_of(w[3])
+            if key == "heat_flux_wall":
+                # only adiabatic walls (src/parse.f:1924-1926)
+                th.nTemBdTp[ir - 1, jr - 1, face - 1] = BT_HTFLUX
+            else:
+                if len(w) < 5:
+                    raise DeckError("fixed_temperature_wall: value missing")
+                th.nTemBdTp[ir - 1, jr - 1, face - 1] = BT_TEMPER
+                t.dBCVal[ir - 1, jr - 1, face - 1, VAR_T - 1] = temp_of(w[4])
         else:
             raise DeckError(f"Unrecognized keyword: [{key}]")
 
@@ -302,6 +378,35 @@ def _setup_bcs(t: Regions, nx: int, ny: int) -> None:
                 T[ir, jr, NORTH - 1] = BM_WALL1
             if T[ir, jr, NORTH - 1] == BM_WALL1:
                 T[ir, jr + 1, SOUTH - 1] = BM_WALL1
+    if t.thermal is None:
+        return
+    # the same pairing of coinciding faces for temperature (src/bound_cond.f:226-258)
+    Q = t.thermal.nTemBdTp
+    for jr in range(nj):
+        for ir in range(ni - 1):
+            for bt in (BT_TEMPER, BT_HTFLUX):
+                if Q[ir, jr, EAST - 1] == bt:
+                    Q[ir + 1, jr, WEST - 1] = bt
+                if Q[ir + 1, jr, WEST - 1] == bt:
+                    Q[ir, jr, EAST - 1] = bt
+    for jr in range(nj - 1):
+        for ir in range(ni):
+            for bt in (BT_TEMPER, BT_HTFLUX):
+                if Q[ir, jr + 1, SOUTH - 1] == bt:
+                    Q[ir, jr, NORTH - 1] = bt
+                if Q[ir, jr, NORTH - 1] == bt:
+                    Q[ir, jr + 1, SOUTH - 1] = bt
+
+
+def heat_sources(regions: Regions, dlref: float, tref: float, tmax: float, dconduct: float,
+                 pe: float) -> None:
+    """dHGSTval of the heat-generating regions from the values the deck gave
+    (src/bound_cond.f:2018-2029): s = q dlref^2 / (pe dconduct (tmax - tref))."""
+    th = regions.thermal
+    for jr in range(regions.n_j):
+        for ir in range(regions.n_i):
+            if th.nTRgType[ir, jr] == RT_HEATGN:
+                th.dHGSTval[ir, jr] = (th.dTRgVal[ir, jr] * dlref ** 2) / (pe * dconduct * (tmax - tref))
 
 
 def _por_reg_cnst(t: Regions, perm_eq, dim_coef, dlref: float, re: float) -> None:
