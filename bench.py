@@ -375,9 +375,15 @@ def run_arm(s, prm, args, precision, u0, v0, p0, st, flush, barrier, local, time
             "clk": clk, "wall": t_wall, "fields": fields}
 
 
-def kernel_name(kind, precision, tiled):
+def kernel_name(kind, precision, tiled, thermal=False):
     """The kernel a profile kind stands for in this workload."""
-    from wolfd2_gb300.gpu import K_COPY, K_MOMENTUM, K_PPE, KERNEL_NAMES
+    from wolfd2_gb300.gpu import K_COPY, K_MOMENTUM, K_POST, K_PPE, K_THERM, KERNEL_NAMES
+    if thermal and kind == K_POST:
+        return "k_me_post+k_step_tail_th"
+    if thermal and kind == K_COPY:
+        return "k_copy_th"
+    if kind == K_THERM:
+        return "k_therm+k_eq_state"
     if kind == K_PPE:
         return "k_ppe_mixed" if precision == "mixed" else ("k_ppe_tiled" if tiled else "k_ppe")
     if kind == K_MOMENTUM:
@@ -560,7 +566,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "clocks": head["clk"].summary(),
         "gpu_launches": head["launches"],
-        "kernel_ms": {kernel_name(k, args.precision, tiled): {"total_ms": v[0], "launches": v[1]}
+        "kernel_ms": {kernel_name(k, args.precision, tiled, t0 is not None): {"total_ms": v[0], "launches": v[1]}
                       for k, v in head["prof"].items()},
         "iterations": [[h[0], h[1]] for h in head["timed"]],
         "chain": {"max_verify_rounds": chain_rounds, "sequential_fallbacks": chain_fallbacks},

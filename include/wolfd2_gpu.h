@@ -198,6 +198,19 @@ int wolfd2gpu_set_thermal(w2_ctx *ctx, const w2_thermal *tp, const int *nTRgType
 int wolfd2gpu_load_thermal(w2_ctx *ctx, const double *t, const double *d);
 int wolfd2gpu_store_thermal(w2_ctx *ctx, double *t, double *d);
 
+/* Snapshots streamed from the device (no reference counterpart; the output
+ * and restart path of main.f copies the host arrays).  wolfd2gpu_snapshot
+ * queues copies of the current time level -- u, v, p, and t, d (may be NULL)
+ * with the energy equation -- into (0:mnx,0:mny) host arrays on a copy stream
+ * and returns at once; steps called after it run while the copy proceeds,
+ * and the first work that overwrites that level waits for it.  Use
+ * page-locked host arrays for a copy that overlaps the steps.
+ * wolfd2gpu_snapshot_wait blocks until the arrays are filled (then write
+ * the Plot3D solution or restart file from them). */
+int wolfd2gpu_snapshot(w2_ctx *ctx, double *u, double *v, double *p, double *t,
+                       double *d);
+int wolfd2gpu_snapshot_wait(w2_ctx *ctx);
+
 /* Run parameters of the time loop (main.f with nthermen = 0). */
 typedef struct {
   double dk, re, fr, qtol, sortol, sorrel, fpu, fpv;

@@ -108,3 +108,21 @@ def test_thermal_keywords():
     assert th.nTemBdTp[2, 1, deck.NORTH - 1] == BT_HTFLUX
     heat_sources(r, 1.0, 300.0, 400.0, 2.0, 10.0)
     assert th.dHGSTval[2, 1] == 5.0 / (10.0 * 2.0 * 100.0)
+
+
+def test_plot3d_solution_layout(tmp_path):
+    """SaveStdVarsP3D's unformatted solution file: (nx, ny, nVars), then
+    p, u, v, w = 0 (and t) over i = 1..nx, j = 1..ny, i fastest."""
+    import numpy as np
+    nx, ny = 7, 5
+    rng = np.random.default_rng(0)
+    u, v, p, t = (np.asfortranarray(rng.normal(size=(nx + 2, ny + 2))) for _ in range(4))
+    pre = str(tmp_path / "snap")
+    deck.write_plot3d_solution(pre, nx, ny, u, v, p, t)
+    n1, n2, f = deck.read_plot3d_solution(pre + ".qqq")
+    assert (n1, n2, f.shape[2]) == (nx, ny, 5)
+    for l, a in enumerate((p, u, v, np.zeros_like(p), t)):
+        assert np.array_equal(f[:, :, l], a[1:nx + 1, 1:ny + 1])
+    raw = open(pre + ".qqq", "rb").read()
+    assert np.frombuffer(raw[:4], "<i4")[0] == 12 and len(raw) == 4 + 12 + 4 + 4 + nx * ny * 5 * 8 + 4
+    assert open(pre + ".nam").read().splitlines()[-1] == " Complete Temperature"

@@ -87,6 +87,11 @@ struct w2_ctx {
   // the time loop with the energy equation (wolfd2gpu_set_thermal): its
   // switches, tables, temperature levels, density d / dn, and the previous
   // iterates of the momentum/energy iterations
+  // snapshots (wolfd2gpu_snapshot): a copy stream, the events ordering it
+  // after the step that made the level and before the step that overwrites it
+  cudaStream_t cst = nullptr;
+  cudaEvent_t ev_snap_src = nullptr, ev_snap_done = nullptr;
+  int snap_level = -1;  // time level a copy may still be reading, or -1
   bool therm_on = false;
   w2_thermal therm_p{};
   ThermTables therm_tt{};
@@ -429,6 +434,16 @@ int ready(w2_ctx *c) {
   if (!c->metrics_ok) return fail(c, W2_E_ARG, "metrics not set (wolfd2gpu_set_metrics or wolfd2gpu_grid_metric)");
   if (c->porous) return fail(c, W2_E_UNSUPPORTED, "porous regions are not supported by the GPU path");
   return W2_OK;
+}
+
+// A snapshot copy may still read time level snap_level: work on the context
+// stream that writes that level (or any level, when `level` is -1) first
+// waits for the copy.
+void snap_fence(w2_ctx *c, int level = -1) {
+  if (c->snap_level < 0) return;
+  if (level >= 0 && level != c->snap_level) return;
+  cudaStreamWaitEvent(c->st, c->ev_snap_done, 0);
+  c->snap_level = -1;
 }
 
 // ---- launch helpers on explicit device buffers ---------------------------
@@ -904,6 +919,12 @@ int wolfd2gpu_destroy(w2_ctx *c) {
   for (auto &g : c->graphs) cudaGraphExecDestroy(g.second.exec);
   for (void *p : c->allocs) cudaFree(p);
   if (c->h_out) cudaFreeHost(c->h_out);
+  if (c->cst) {
+    cudaStreamSynchronize(c->cst);
+    cudaStreamDestroy(c->cst);
+  }
+  if (c->ev_snap_src) cudaEventDestroy(c->ev_snap_src);
+  if (c->ev_snap_done) cudaEventDestroy(c->ev_snap_done);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
   return W2_OK;
@@ -1382,6 +1403,7 @@ int wolfd2gpu_set_thermal(w2_ctx *c, const w2_thermal *tp, const int *nTRgType, 
 int wolfd2gpu_load_thermal(w2_ctx *c, const double *t, const double *d) {
   if (!c || !c->therm_on || !t) return fail(c, W2_E_ARG, "thermal loop not set, or t missing");
   int rc;
+  snap_fence(c);
   if ((rc = copy_in(c, c->T[c->cur], t))) return rc;
   if (d) {
     if ((rc = copy_in(c, c->Dd, d))) return rc;
@@ -1405,9 +1427,47 @@ int wolfd2gpu_store_thermal(w2_ctx *c, double *t, double *d) {
 int wolfd2gpu_load_fields(w2_ctx *c, const double *u, const double *v, const double *p) {
   if (!c || !u || !v || !p) return W2_E_ARG;
   int rc;
+  snap_fence(c);
   if ((rc = copy_in(c, c->U[c->cur], u)) || (rc = copy_in(c, c->V[c->cur], v)) ||
       (rc = copy_in(c, c->P[c->cur], p)))
     return rc;
+  return W2_OK;
+}
+
+// Snapshot of the current time level (u, v, p; t and d with the energy
+// equation) into host arrays on a copy stream, ordered after the work issued
+// so far; the next steps run meanwhile (the copy engines work beside the
+// SMs), and the first launch that overwrites the level waits for the copy.
+int wolfd2gpu_snapshot(w2_ctx *c, double *u, double *v, double *p, double *t, double *d) {
+  if (!c || !u || !v || !p) return W2_E_ARG;
+  if ((t || d) && !c->therm_on) return fail(c, W2_E_ARG, "t, d snapshots need the thermal loop");
+  if (!c->cst) {
+    if (cudaStreamCreateWithFlags(&c->cst, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_snap_src, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_snap_done, cudaEventDisableTiming) != cudaSuccess)
+      return fail(c, W2_E_CUDA, "snapshot stream or events");
+  }
+  // a previous snapshot into other host buffers must be complete
+  if (c->snap_level >= 0) CK(cudaEventSynchronize(c->ev_snap_done));
+  CK(cudaEventRecord(c->ev_snap_src, c->st));
+  CK(cudaStreamWaitEvent(c->cst, c->ev_snap_src, 0));
+  const int L = c->cur;
+  const double *src[5] = {c->U[L], c->V[L], c->P[L], c->therm_on ? c->T[L] : nullptr, c->Dd};
+  double *dst[5] = {u, v, p, t, d};
+  for (int k = 0; k < 5; ++k) {
+    if (!dst[k]) continue;
+    CK(cudaMemcpy2DAsync(dst[k], (size_t)(c->mnx + 1) * 8, src[k], (size_t)c->ld * 8, (size_t)(c->nx + 2) * 8,
+                         c->ny + 2, cudaMemcpyDeviceToHost, c->cst));
+  }
+  CK(cudaEventRecord(c->ev_snap_done, c->cst));
+  c->snap_level = L;
+  return W2_OK;
+}
+
+// Wait until the last snapshot's host arrays are filled.
+int wolfd2gpu_snapshot_wait(w2_ctx *c) {
+  if (!c) return W2_E_ARG;
+  if (c->ev_snap_done) CK(cudaEventSynchronize(c->ev_snap_done));
   return W2_OK;
 }
 
@@ -1452,6 +1512,7 @@ int wolfd2gpu_cold_start(w2_ctx *c, const w2_params *prm, int *nSorConv) {
   int rc = ready(c);
   if (rc) return rc;
   if ((rc = check_params(c, prm))) return rc;
+  snap_fence(c);
   double *u = c->U[c->cur], *v = c->V[c->cur], *p = c->P[c->cur];
   if ((rc = launch_bc(c, BC_VEL, u, v, p))) return rc;
   if (prm->precision == W2_PREC_MIXED) {
@@ -1713,6 +1774,9 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
   if (c->therm_on && (prm->precision != W2_PREC_FP64 || prm->nfiltu == 1 || prm->nfiltv == 1))
     return fail(c, W2_E_UNSUPPORTED, "the time loop with the energy equation runs plain FP64 without Filter");
   if (prm->precision == W2_PREC_MIXED && (rc = ensure_f32(c))) return rc;
+  // one step writes the other level; two or more write both
+  if (nsteps >= 2) snap_fence(c);
+  else if (nsteps == 1) snap_fence(c, 1 - c->cur);
   std::vector<StepOut> outs((size_t)std::max(nsteps, 1));
   if (nsteps > c->outs_cap) {
     if (c->d_outs) {
@@ -2208,6 +2272,14 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
     if (q.msorit < 1 || q.mqiter < 1 || q.refine_sweeps < 0) return efail(e, W2_E_ARG, "case %d: bad parameters", k);
   }
   if (nsteps == 0) return W2_OK;
+  // a snapshot copy of a case must finish before the ensemble's stream writes its fields
+  for (int k = 0; k < n; ++k) {
+    w2_ctx *c = e->cs[k];
+    if (c->snap_level >= 0) {
+      ECK(cudaStreamWaitEvent(e->st, c->ev_snap_done, 0));
+      c->snap_level = -1;
+    }
+  }
   // descriptors of this call: parameters, starting levels
   for (int k = 0; k < n; ++k) {
     const w2_params &q = prm[k];
@@ -2790,6 +2862,7 @@ int wolfd2gpu_adjoint(w2_ctx *c, const w2_params *prm, int nsteps, int every, do
   if (rc) return rc;
   if (nsteps < 1 || every < 1) return fail(c, W2_E_ARG, "nsteps and checkpoint interval must be >= 1");
   if ((rc = adj_alloc(c))) return rc;
+  snap_fence(c);
   std::vector<void *> mem;
   struct Free {
     std::vector<void *> &m;

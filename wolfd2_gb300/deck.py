@@ -785,6 +785,42 @@ def write_restart(path: str, k: int, dtime: float, nx: int, ny: int,
         f.write(b"".join(body))
 
 
+def write_plot3d_solution(prefix: str, nx: int, ny: int, u: np.ndarray, v: np.ndarray,
+                          p: np.ndarray, t: Optional[np.ndarray] = None,
+                          names: bool = True) -> None:
+    """The standard-variable output of SaveStdVarsP3D (src/file_manip.f:1024-1175)
+    in its unformatted form: ``<prefix>.qqq`` holds record 1 ``nx, ny, nVars``
+    and record 2 the REAL*8 functions f(i, j, l) over i = 1..nx, j = 1..ny
+    (i fastest) for l = p, u, v, w = 0 (and t with the energy equation);
+    ``<prefix>.nam`` the FieldView names, one list-directed line each."""
+    def rec(buf: bytes) -> bytes:
+        n = np.array([len(buf)], "<i4").tobytes()
+        return n + buf + n
+    funcs = [p, u, v, np.zeros_like(p)] + ([t] if t is not None else [])
+    body = rec(np.array([nx, ny, len(funcs)], "<i4").tobytes())
+    data = b"".join(np.asarray(f[1:nx + 1, 1:ny + 1], "<f8").ravel(order="F").tobytes() for f in funcs)
+    with open(prefix + ".qqq", "wb") as fh:
+        fh.write(body + rec(data))
+    if names:
+        lines = ["Complete Pressure", "Complete U ; Complete Velocity", "Complete V", "Complete W"]
+        if t is not None:
+            lines.append("Complete Temperature")
+        with open(prefix + ".nam", "w") as fh:
+            fh.write("".join(f" {x}\n" for x in lines))
+
+
+def read_plot3d_solution(path: str):
+    """Inverse of :func:`write_plot3d_solution` for the .qqq file: returns
+    (nx, ny, f) with f of shape (nx, ny, nVars)."""
+    b = open(path, "rb").read()
+    n0 = int(np.frombuffer(b[:4], "<i4")[0])
+    nx, ny, nv = (int(x) for x in np.frombuffer(b[4:4 + n0], "<i4"))
+    o = 4 + n0 + 4
+    n1 = int(np.frombuffer(b[o:o + 4], "<i4")[0])
+    f = np.frombuffer(b[o + 4:o + 4 + n1], "<f8").reshape((nx, ny, nv), order="F")
+    return nx, ny, f
+
+
 def read_restart(path: str):
     """Inverse of :func:`write_restart`; returns (k, dtime, nx, ny, fields)."""
     data = open(path, "rb").read()

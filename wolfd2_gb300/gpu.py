@@ -109,6 +109,8 @@ def lib():
     L.wolfd2gpu_set_thermal.argtypes = [vp, C.POINTER(ThermalC), _ip, _ip, _dp, _dp]
     L.wolfd2gpu_load_thermal.argtypes = [vp, _dp, _dp]
     L.wolfd2gpu_store_thermal.argtypes = [vp, _dp, _dp]
+    L.wolfd2gpu_snapshot.argtypes = [vp, _dp, _dp, _dp, _dp, _dp]
+    L.wolfd2gpu_snapshot_wait.argtypes = [vp]
     L.wolfd2gpu_load_fields.argtypes = [vp, _dp, _dp, _dp]
     L.wolfd2gpu_store_fields.argtypes = [vp, _dp, _dp, _dp]
     L.wolfd2gpu_cold_start.argtypes = [vp, C.POINTER(Params), _ip]
@@ -370,6 +372,17 @@ class Solver:
         d = np.zeros_like(t)
         self._check(self.L.wolfd2gpu_store_thermal(self.h, _p(t), _p(d)))
         return t, d
+
+    def snapshot(self, out) -> None:
+        """Queue a copy of the current level into the host arrays of `out`
+        ((u, v, p) or (u, v, p, t, d), Fortran-ordered float64, page-locked
+        for a copy that overlaps later steps) and return at once;
+        snapshot_wait() blocks until they are filled."""
+        arrs = list(out) + [None] * (5 - len(out))
+        self._check(self.L.wolfd2gpu_snapshot(self.h, *[None if a is None else _p(a) for a in arrs]))
+
+    def snapshot_wait(self) -> None:
+        self._check(self.L.wolfd2gpu_snapshot_wait(self.h))
 
     def load_fields(self, u, v, p) -> None:
         self._check(self.L.wolfd2gpu_load_fields(self.h, _p(u), _p(v), _p(p)))
