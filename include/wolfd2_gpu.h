@@ -167,6 +167,11 @@ int wolfd2gpu_therm_energy(w2_ctx *ctx, const int *nx, const int *ny,
                            const double *un, const double *vn, const double *u,
                            const double *v, const double *tn, double *t);
 
+/* Filter, src/utility.f:33-36, of the temperature (ncomp = _T_): the
+ * Shuman filter on every region whose nTRgType is not 1. */
+int wolfd2gpu_filter_t(w2_ctx *ctx, const int *nx, const int *ny, const int *nTRgType,
+                       const double *fp, double *t);
+
 /* EqState, src/thermal.f:288-290: den on i, j = 2..n (other entries kept). */
 int wolfd2gpu_eq_state(w2_ctx *ctx, const int *nx, const int *ny,
                        const double *uref, const double *densref,
@@ -182,14 +187,17 @@ int wolfd2gpu_eq_state(w2_ctx *ctx, const int *nx, const int *ny,
 typedef struct {
   int nthermen, neqstate, nmeiter;
   double dmeittol, pe, uref, densref, tmax, tref, rconst;
+  int nfiltt;         /* Filter of t after the iterations (main.f:889-893) */
+  double fpt;
 } w2_thermal;
 
 /* Switch the device-resident time loop to main.f's path with the energy
  * equation (nthermen = 1) and/or the equation of state (neqstate = 1):
  * momentum/energy iterations (up to nmeiter, ended by dmeittol, main.f:736-879)
  * with ThermEnergy, EqState and the buoyancy term of YMomentum, then
- * TempBoundCond.  Tables as for wolfd2gpu_therm_energy.  tp = NULL (or both
- * switches 0) returns to the plain loop.  The temperature and density start
+ * TempBoundCond (and Filter of t with nfiltt = 1).  Tables as for
+ * wolfd2gpu_therm_energy.  tp = NULL (or both switches 0) returns to the
+ * plain loop.  The temperature and density start
  * at zero; wolfd2gpu_load_thermal / wolfd2gpu_store_thermal move them
  * ((0:mnx,0:mny) host arrays, d may be NULL).  Plain FP64 only, no Filter. */
 int wolfd2gpu_set_thermal(w2_ctx *ctx, const w2_thermal *tp, const int *nTRgType,

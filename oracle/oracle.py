@@ -61,7 +61,8 @@ class _Fields(C.Structure):
 
 class _ThermalParams(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("nthermen", "neqstate", "nmeiter")] + \
-               [(n, C.c_double) for n in ("dmeittol", "pe", "uref", "densref", "tmax", "tref", "rconst")]
+               [(n, C.c_double) for n in ("dmeittol", "pe", "uref", "densref", "tmax", "tref", "rconst")] + \
+               [("nfiltt", C.c_int), ("fpt", C.c_double)]
 
 
 def build(force: bool = False) -> str:
@@ -115,6 +116,8 @@ def lib():
                                            C.POINTER(_Thermal), C.c_double, C.c_double,
                                            C.POINTER(_Metrics), _dp, _dp, _dp, _dp, _dp, _dp]
             L.w2o_eq_state.argtypes = [C.c_void_p, C.c_int, C.c_int] + [C.c_double] * 5 + [_dp, _dp, _dp]
+            L.w2o_filter_t.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions),
+                                       C.POINTER(_Thermal), C.c_double, _dp]
             L.w2o_cold_start.restype = C.c_int
             L.w2o_cold_start.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions),
                                          C.POINTER(_Params), C.POINTER(_Metrics), C.POINTER(_Fields)]
@@ -281,6 +284,10 @@ class Oracle:
                                 C.byref(self.metrics_struct(met)), _ptr(un), _ptr(vn), _ptr(u),
                                 _ptr(v), _ptr(tn), _ptr(t))
 
+    def filter_t(self, nx, ny, regs, th, fp, q) -> None:
+        rs, ts = self.regions_struct(regs), self.thermal_struct(th)
+        self.L.w2o_filter_t(self.h, nx, ny, C.byref(rs), C.byref(ts), fp, _ptr(q))
+
     def eq_state(self, nx, ny, uref, densref, tmax, tref, rconst, p, t, den) -> None:
         self.L.w2o_eq_state(self.h, nx, ny, uref, densref, tmax, tref, rconst, _ptr(p), _ptr(t), _ptr(den))
 
@@ -312,7 +319,7 @@ class OracleRun:
             self._th = Oracle.thermal_struct(case.thermal)
             tp = case.tparams
             self._tp = _ThermalParams(tp.nthermen, tp.neqstate, tp.nmeiter, tp.dmeittol, tp.pe, tp.uref,
-                                      tp.densref, tp.tmax, tp.tref, tp.rconst)
+                                      tp.densref, tp.tmax, tp.tref, tp.rconst, tp.nfiltt, tp.fpt)
         self.history = []
         self.cold_nconv = None
         if cold_start:

@@ -173,6 +173,11 @@ class RefRun:
                     mx = x if x > mx else mx
                 if l > 1 and mx < tp.dmeittol:
                     break
+            if therm and tp.nfiltt == 1:
+                tb = self.tab
+                self.R("filter", nx=self.nx, ny=self.ny, ncomp=4, nreg=tb["nreg"], nregbrd=tb["nregbrd"],
+                       nregtype=tb["nregtype"], nmombdtp=tb["nmombdtp"],
+                       ntrgtype=self._ttab()["ntrgtype"], fp=tp.fpt, qu=f["t"])
             self.vel_bc(f["u"], f["v"])
             self.pres_bc(f["p"])
             if therm:

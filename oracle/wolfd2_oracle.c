@@ -943,6 +943,25 @@ void w2o_filter(w2o_ctx *c, int nx, int ny, int ncomp, const w2o_regions *r,
     for (int i = 0; i <= nx + 1; i++) F(qu, i, j) = F(qh, i, j);
 }
 
+void w2o_filter_t(w2o_ctx *c, int nx, int ny, const w2o_regions *r, const w2o_thermal *th,
+                  double fp, double *qu) {
+  double *qh = c->qh;
+  for (int j = 0; j <= ny + 1; j++)
+    for (int i = 0; i <= nx + 1; i++) F(qh, i, j) = F(qu, i, j);
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      if (th->nTRgType[(ireg - 1) + (jreg - 1) * r->mgri] == BT_TEMPER) continue;
+      const int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      const int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      for (int j = jS + 1; j <= jN; j++)
+        for (int i = iW + 1; i <= iE; i++)
+          F(qh, i, j) = (F(qu, i, j - 1) + F(qu, i - 1, j) + F(qu, i, j + 1) + F(qu, i + 1, j) +
+                         fp * F(qu, i, j)) / (fp + 4.0);
+    }
+  for (int j = 0; j <= ny + 1; j++)
+    for (int i = 0; i <= nx + 1; i++) F(qu, i, j) = F(qh, i, j);
+}
+
 /* ------------------------------------------------------------------ */
 /* bound_cond.f                                                        */
 /* ------------------------------------------------------------------ */
@@ -1204,6 +1223,7 @@ int w2o_step_thermal(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
     if (me[2] > mx) mx = me[2];
     if (l > 1 && mx < tp->dmeittol) break;
   }
+  if (therm && tp->nfiltt == 1) w2o_filter_t(c, nx, ny, r, th, tp->fpt, f->t);
   w2o_vel_bound_cond(c, nx, ny, r, f->u, f->v);
   w2o_pres_bound_cond(c, nx, ny, r, f->p);
   if (therm) w2o_temp_bound_cond(c, nx, ny, r, th, f->t);

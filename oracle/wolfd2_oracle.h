@@ -168,7 +168,14 @@ typedef struct {
 typedef struct {
   int nthermen, neqstate, nmeiter;
   double dmeittol, pe, uref, densref, tmax, tref, rconst;
+  int nfiltt;    /* Filter of t after the iterations (main.f:889-893) */
+  double fpt;
 } w2o_thermal_params;
+
+/* Filter of a scalar (utility.f:33-247, ncomp = _T_): every region whose
+ * nTRgType is not 1 (the reference compares with BT_TEMPER = 1). */
+void w2o_filter_t(w2o_ctx *c, int nx, int ny, const w2o_regions *r, const w2o_thermal *th,
+                  double fp, double *q);
 
 /* Fields of the time loop, each (0:mnx,0:mny). */
 typedef struct {

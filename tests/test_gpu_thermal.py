@@ -139,13 +139,31 @@ def dataclasses_replace(p, **kw):
     return dataclasses.replace(p, **kw)
 
 
+def _filtered(case):
+    case.tparams.nfiltt = 1
+    case.tparams.fpt = 20.0
+    return case
+
+
 def _loop_cases():
     return {
         "heated1": lambda: deck.heated_cavity(32, 500.0, 0.004, nmeiter=1, eqstate=False),
         "heated3": lambda: deck.heated_cavity(32, 500.0, 0.004, nmeiter=3, dmeittol=1e-7),
         "heated6_lid": lambda: deck.heated_cavity(40, 300.0, 0.004, nmeiter=6, dmeittol=1e-6, lid=1.0),
         "multiregion": lambda: thermal_setup.loop_case(),
+        "multiregion_filter_t": lambda: _filtered(thermal_setup.loop_case(nmeiter=2)),
     }
+
+
+def test_filter_t_bitwise():
+    """Filter of the temperature on the 3 x 2 layout: the heat-generating
+    region (nTRgType 1) is skipped, as the reference's test skips it."""
+    case, th, f, s, o, met = _setup()
+    tg, to = f["t"].copy(order="F"), f["t"].copy(order="F")
+    s.FilterT(th, 20.0, tg)
+    o.filter_t(case.nx, case.ny, case.regions, th, 20.0, to)
+    assert np.array_equal(tg, to) and not np.array_equal(tg, f["t"])
+    s.close()
 
 
 @pytest.mark.parametrize("name", sorted(_loop_cases()))

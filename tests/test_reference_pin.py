@@ -165,3 +165,26 @@ def test_multiregion_thermal_time_loop_bitwise():
         assert a[2] == b[2]
     for k in ("u", "v", "p", "t", "d"):
         assert np.array_equal(r.f[k], o.f[k]), k
+
+
+@pytest.mark.parametrize("layout", ["heated", "multiregion"])
+def test_thermal_loop_with_filter_bitwise(layout):
+    """Filter of t after the momentum/energy iterations (main.f:889-893;
+    utility.f's scalar branch skips the regions whose nTRgType equals 1)."""
+    import thermal_setup
+    if layout == "heated":
+        case = deck.heated_cavity(24, 500.0, 0.004, nmeiter=2, dmeittol=1e-7)
+    else:
+        case = thermal_setup.loop_case(nmeiter=2)
+    case.tparams.nfiltt = 1
+    case.tparams.fpt = 20.0
+    f77ref.build(case.nx + 1, case.ny + 1)
+    r = refrun.RefRun(case)
+    o = O.OracleRun(case)
+    r.step(5)
+    o.step(5)
+    assert [h[:2] for h in r.history] == [h[:2] for h in o.history]
+    for a, b in zip(r.history, o.history):
+        assert a[2] == b[2]
+    for k in ("u", "v", "p", "t", "d"):
+        assert np.array_equal(r.f[k], o.f[k]), k

@@ -84,6 +84,7 @@ struct w2_ctx {
   Chain therm_ch{};
   int *d_ttab = nullptr;     // nTRgType(mgri,mgrj) then nTemBdTp(mgri,mgrj,4)
   double *d_tval = nullptr;  // dTRgVal(mgri,mgrj) then dHGSTval(mgri,mgrj)
+  int *d_trt_filter = nullptr;  // nTRgType of the drop-in Filter of t
   // the time loop with the energy equation (wolfd2gpu_set_thermal): its
   // switches, tables, temperature levels, density d / dn, and the previous
   // iterates of the momentum/energy iterations
@@ -1363,6 +1364,28 @@ int wolfd2gpu_therm_energy(w2_ctx *c, const int *nx, const int *ny, const int *n
   return check_sync(c);
 }
 
+int wolfd2gpu_filter_t(w2_ctx *c, const int *nx, const int *ny, const int *nTRgType, const double *fp,
+                       double *t) {
+  int rc = ready(c);
+  if (rc) return rc;
+  if (!dims_match(c, nx, ny) || !nTRgType || !fp || !t) return fail(c, W2_E_ARG, "bad argument");
+  // only nTRgType matters here; it goes to a table of its own, so the
+  // tables of the thermal loop stay as they were
+  const int mg = c->mgri * c->mgrj;
+  if (!c->d_trt_filter && !(c->d_trt_filter = dalloc<int>(c, mg)))
+    return fail(c, W2_E_CUDA, "out of device memory (thermal tables)");
+  CK(cudaMemcpyAsync(c->d_trt_filter, nTRgType, sizeof(int) * mg, cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  ThermTables tt{c->d_trt_filter, nullptr, nullptr, nullptr};
+  double *dq = c->stage[0], *dh = c->stage[1];
+  if ((rc = copy_in(c, dq, t))) return rc;
+  c->launches++;
+  k_filter_t<<<grid_blocks(c), c->threads, 0, c->st>>>(c->dev, tt, *fp, dq, dh);
+  CK(cudaGetLastError());
+  if ((rc = copy_out(c, t, dh))) return rc;
+  return check_sync(c);
+}
+
 int wolfd2gpu_eq_state(w2_ctx *c, const int *nx, const int *ny, const double *uref,
                        const double *densref, const double *tmax, const double *tref,
                        const double *rconst, const double *p, const double *t, double *den) {
@@ -1632,6 +1655,14 @@ int issue_thermal_step(w2_ctx *c, const w2_params *prm, const double *un, const 
       void *args[] = {&dl, &ll, &tol, (void *)&up, (void *)&vp, (void *)&tpv, &us, &vs, &ts};
       if ((rc = coop(c, (const void *)k_me_norms, blocks, args))) return rc;
     }
+  }
+  if (therm && tp.nfiltt == 1) {
+    // main.f:889-893: Filter of t after the iterations
+    ProfScope ps(c, W2_K_THERM);
+    c->launches++;
+    k_filter_t<<<gb, c->threads, 0, c->st>>>(d, c->therm_tt, tp.fpt, ts, d.qh);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ts, d.qh, c->nf * sizeof(double), cudaMemcpyDeviceToDevice, c->st));
   }
   {
     ProfScope ps(c, W2_K_POST);

@@ -264,6 +264,29 @@ __global__ void k_eq_state(Dev d, double uref, double densref, double tmax, doub
   }
 }
 
+// Filter of a scalar (utility.f:33-247 with ncomp = _T_): the Shuman filter
+// on the interior of every region whose nTRgType is not 1 (the reference
+// compares nTRgType with BT_TEMPER, whose value is 1), from qu into qh; the
+// other points copy qu.  The caller copies qh back to qu.
+__global__ void k_filter_t(Dev d, ThermTables tt, double fp, const double *qu, double *qh) {
+  vgrid_set(0, gridDim.x);
+  if (d.sync->halt) return;
+  const int W = d.nx + 2, H = d.ny + 2;
+  for (int q = gtid(); q < W * H; q += gthreads()) {
+    const int i = q % W, j = q / W;
+    const size_t o = IX(d, i, j);
+    double r = qu[o];
+    if (i >= 2 && i <= d.nx && j >= 2 && j <= d.ny) {
+      int ir, jr;
+      region_of(d, i, j, ir, jr);
+      if (t_rt(d, tt, ir, jr) != BT_TEMPER)
+        r = (qu[IX(d, i, j - 1)] + qu[IX(d, i - 1, j)] + qu[IX(d, i, j + 1)] + qu[IX(d, i + 1, j)] + fp * qu[o]) /
+            (fp + 4.0);
+    }
+    qh[o] = r;
+  }
+}
+
 // ---- the time step with the energy equation --------------------------------
 
 // Time levels (main.f:696-704) and the first iterates (main.f:741-747, with

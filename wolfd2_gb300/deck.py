@@ -505,6 +505,8 @@ class ThermalParams:
     tmax: float = 1.0
     tref: float = 0.0
     rconst: float = 1.0
+    nfiltt: int = 0             # Filter of t after the iterations (filter_t)
+    fpt: float = 5.0            # its parameter (src/parse.f:159 default)
 
 
 @dataclasses.dataclass

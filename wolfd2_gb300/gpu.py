@@ -37,7 +37,8 @@ KERNEL_NAMES = {K_MOMENTUM: "k_naux", K_PPE: "k_ppe", K_POST: "k_step_post",
 class ThermalC(C.Structure):
     """w2_thermal of include/wolfd2_gpu.h."""
     _fields_ = [(n, C.c_int) for n in ("nthermen", "neqstate", "nmeiter")] + \
-               [(n, C.c_double) for n in ("dmeittol", "pe", "uref", "densref", "tmax", "tref", "rconst")]
+               [(n, C.c_double) for n in ("dmeittol", "pe", "uref", "densref", "tmax", "tref", "rconst")] + \
+               [("nfiltt", C.c_int), ("fpt", C.c_double)]
 
 # metric order of the C-ABI = argument order of grid.f:Grid
 METRIC_ORDER = ("rau rbu rbv rgv ran rbn rgn rac rbc rgc dju djv djc djn xen yen xzn yzn "
@@ -106,6 +107,7 @@ def lib():
     L.wolfd2gpu_temp_bound_cond.argtypes = [vp, _ip, _ip, _ip, _ip, _dp, _dp]
     L.wolfd2gpu_therm_energy.argtypes = [vp, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp] + [_dp] * 6
     L.wolfd2gpu_eq_state.argtypes = [vp, _ip, _ip] + [_dp] * 8
+    L.wolfd2gpu_filter_t.argtypes = [vp, _ip, _ip, _ip, _dp, _dp]
     L.wolfd2gpu_set_thermal.argtypes = [vp, C.POINTER(ThermalC), _ip, _ip, _dp, _dp]
     L.wolfd2gpu_load_thermal.argtypes = [vp, _dp, _dp]
     L.wolfd2gpu_store_thermal.argtypes = [vp, _dp, _dp]
@@ -339,6 +341,11 @@ class Solver:
             self.h, _i(self.nx), _i(self.ny), prt, pbt, _d(dk), _d(pe), ptv, phg,
             _p(un), _p(vn), _p(u), _p(v), _p(tn), _p(t)))
 
+    def FilterT(self, th, fp, t) -> None:
+        """Filter of the temperature (utility.f, ncomp = _T_) in place."""
+        rt, prt = self._ttab(th.nTRgType, np.int32)
+        self._check(self.L.wolfd2gpu_filter_t(self.h, _i(self.nx), _i(self.ny), prt, _d(fp), _p(t)))
+
     def EqState(self, uref, densref, tmax, tref, rconst, p, t, den) -> None:
         self._check(self.L.wolfd2gpu_eq_state(self.h, _i(self.nx), _i(self.ny), _d(uref), _d(densref),
                                               _d(tmax), _d(tref), _d(rconst), _p(p), _p(t), _p(den)))
@@ -352,7 +359,7 @@ class Solver:
             return
         tp = tparams
         c = ThermalC(tp.nthermen, tp.neqstate, tp.nmeiter, tp.dmeittol, tp.pe, tp.uref, tp.densref,
-                     tp.tmax, tp.tref, tp.rconst)
+                     tp.tmax, tp.tref, tp.rconst, tp.nfiltt, tp.fpt)
         rt, prt = self._ttab(th.nTRgType, np.int32)
         bt, pbt = self._ttab(th.nTemBdTp, np.int32)
         tv, ptv = self._ttab(th.dTRgVal, np.float64)
