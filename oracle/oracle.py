@@ -343,7 +343,7 @@ class OracleRun:
             self.history.append((nql.value, nsor.value, tuple(dif)))
             if rc:
                 raise FloatingPointError("Solution diverged. Please reduce CFL number.")
-        return self.history[-1]
+        return self.history[-1] if self.history else None
 
 
 def threads() -> int:

@@ -185,4 +185,4 @@ class RefRun:
             dif = (self.diff(f["pn"], f["p"]), self.diff(f["un"], f["u"]),
                    self.diff(f["vn"], f["v"]), self.diff(f["tn"], f["t"]))
             self.history.append((nql, nsor, dif))
-        return self.history[-1]
+        return self.history[-1] if self.history else None
