@@ -188,3 +188,21 @@ def test_thermal_loop_with_filter_bitwise(layout):
         assert a[2] == b[2]
     for k in ("u", "v", "p", "t", "d"):
         assert np.array_equal(r.f[k], o.f[k]), k
+
+
+@pytest.mark.parametrize("solver", ["rb_sor", "rb_lsor"])
+def test_curvilinear_multiregion_time_loop_bitwise(solver):
+    """The plain time loop on the curvilinear 3 x 2 layout with lcartes = 0:
+    RhsPpe forms the cross terms before every sweep (pressure.f:362-375)."""
+    import thermal_setup
+    case = thermal_setup.curvilinear_case()
+    case.params.npsolver = deck.PPE_SOLVERS[solver]
+    case.params.msorit = 300
+    f77ref.build(case.nx + 1, case.ny + 1)
+    r = refrun.RefRun(case)
+    o = O.OracleRun(case)
+    r.step(5)
+    o.step(5)
+    assert [h[:2] for h in r.history] == [h[:2] for h in o.history]
+    for k in "uvp":
+        assert np.array_equal(r.f[k], o.f[k]), k

@@ -67,3 +67,22 @@ def loop_case(nmeiter: int = 3):
                                       tmax=330.0, tref=300.0, rconst=287.0)
     case.params.fr = 0.05
     return case
+
+
+def curvilinear_case(lcartes: int = 0):
+    """The 3 x 2 curvilinear layout without the energy equation, for the
+    plain time loop on a non-Cartesian grid (RhsPpe's cross terms every
+    sweep when lcartes = 0)."""
+    case, th, f = problem()
+    case.params.lcartes = lcartes
+    return case
+
+
+def blockage_case():
+    """Three regions in i with an internal blockage, an inlet and an outlet."""
+    text = ("number_of_regions 3 1\n i_borders 12 20\n j_borders\n"
+            "blockage 2 1\n inlet 1 1 west nv 1.0\n outlet 3 1 east fd\n")
+    case = deck.channel(32, 14, 300.0, 0.003, length=2.0, solver="rb_sor")
+    case.regions = deck.parse_bc_section(text, case.nx, case.ny, re=case.params.re)
+    case.bc_text = text
+    return case
