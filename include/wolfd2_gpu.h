@@ -282,6 +282,12 @@ int wolfd2gpu_adjoint(w2_ctx *ctx, const w2_params *prm, int nsteps, int every,
                       int ireg, int jreg, int face, int var, double *gprof, int nprof,
                       int *counts);
 
+/* Self-test of the device-wait limit (no reference counterpart): runs a
+ * grid barrier that one of its two blocks never reaches; the waiting block
+ * gives up after the limit (4 s) and the call returns W2_E_TIMEOUT with the
+ * barrier state cleared, the context still usable.  Nothing faults or hangs. */
+int wolfd2gpu_selftest_wait(w2_ctx *ctx);
+
 /* Synchronise the context stream; returns the first pending error. */
 int wolfd2gpu_sync(w2_ctx *ctx);
 

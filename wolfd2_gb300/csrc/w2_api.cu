@@ -1487,6 +1487,21 @@ int wolfd2gpu_snapshot(w2_ctx *c, double *u, double *v, double *p, double *t, do
   return W2_OK;
 }
 
+// Self-test of the device-wait limit (k_selftest_wait): returns the status
+// the host reads after a grid barrier that one block never reaches, which is
+// W2_E_TIMEOUT after the limit (4 s); the barrier state is cleared, so the
+// context stays usable.
+int wolfd2gpu_selftest_wait(w2_ctx *c) {
+  if (!c) return W2_E_ARG;
+  CK(cudaStreamSynchronize(c->st));
+  Dev d = c->dev;
+  void *args[] = {&d};
+  c->launches++;
+  cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_selftest_wait, dim3(2), dim3(32), args, 0, c->st);
+  if (e != cudaSuccess) return fail(c, W2_E_CUDA, "cooperative launch: %s", cudaGetErrorString(e));
+  return check_sync(c);
+}
+
 // Wait until the last snapshot's host arrays are filled.
 int wolfd2gpu_snapshot_wait(w2_ctx *c) {
   if (!c) return W2_E_ARG;

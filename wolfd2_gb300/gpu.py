@@ -113,6 +113,7 @@ def lib():
     L.wolfd2gpu_store_thermal.argtypes = [vp, _dp, _dp]
     L.wolfd2gpu_snapshot.argtypes = [vp, _dp, _dp, _dp, _dp, _dp]
     L.wolfd2gpu_snapshot_wait.argtypes = [vp]
+    L.wolfd2gpu_selftest_wait.argtypes = [vp]
     L.wolfd2gpu_load_fields.argtypes = [vp, _dp, _dp, _dp]
     L.wolfd2gpu_store_fields.argtypes = [vp, _dp, _dp, _dp]
     L.wolfd2gpu_cold_start.argtypes = [vp, C.POINTER(Params), _ip]
@@ -390,6 +391,11 @@ class Solver:
 
     def snapshot_wait(self) -> None:
         self._check(self.L.wolfd2gpu_snapshot_wait(self.h))
+
+    def selftest_wait(self) -> int:
+        """Status of a grid barrier one block never reaches (W2_E_TIMEOUT
+        after the device-wait limit); the context stays usable."""
+        return int(self.L.wolfd2gpu_selftest_wait(self.h))
 
     def load_fields(self, u, v, p) -> None:
         self._check(self.L.wolfd2gpu_load_fields(self.h, _p(u), _p(v), _p(p)))
