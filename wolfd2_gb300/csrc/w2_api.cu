@@ -5,6 +5,7 @@
 // reference expression operation by operation, so their results are the
 // IEEE-double results of the reference source as written.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cstdarg>
@@ -18,6 +19,13 @@
 #include "w2_thermal.cuh"
 
 using namespace w2;
+
+// NVTX range over a public call (header-only NVTX v3: a no-op unless a
+// profiler or tracer is attached).
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
 
 struct w2_ctx {
   int mnx = 0, mny = 0, mgri = 0, mgrj = 0, nx = 0, ny = 0, ld = 0;
@@ -1547,6 +1555,7 @@ static int check_params(w2_ctx *c, const w2_params *prm) {
 }
 
 int wolfd2gpu_cold_start(w2_ctx *c, const w2_params *prm, int *nSorConv) {
+  NvtxRange nv("wolfd2gpu_cold_start");
   int rc = ready(c);
   if (rc) return rc;
   if ((rc = check_params(c, prm))) return rc;
@@ -1813,6 +1822,7 @@ int wolfd2gpu_set_graph(w2_ctx *c, int enable) {
 }
 
 int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *stats) {
+  NvtxRange nv("wolfd2gpu_step");
   int rc = ready(c);
   if (rc) return rc;
   if ((rc = check_params(c, prm))) return rc;
@@ -2300,6 +2310,7 @@ int wolfd2gpu_ens_graph(w2_ens *e, int enable) {
 }
 
 int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat *stats) {
+  NvtxRange nv("wolfd2gpu_ens_step");
   if (!e || !prm || nsteps < 0) return W2_E_ARG;
   const int n = e->n;
   const bool mixed = prm[0].precision == W2_PREC_MIXED;
@@ -2904,6 +2915,7 @@ int wolfd2gpu_step_counts(w2_ctx *c, const w2_params *prm, int nsteps, const int
 int wolfd2gpu_adjoint(w2_ctx *c, const w2_params *prm, int nsteps, int every, double weight, double *J,
                       double *gu, double *gv, double *gp, int ireg, int jreg, int face, int var,
                       double *gprof, int nprof, int *counts) {
+  NvtxRange nv("wolfd2gpu_adjoint");
   int rc = adj_check(c, prm);
   if (rc) return rc;
   if (nsteps < 1 || every < 1) return fail(c, W2_E_ARG, "nsteps and checkpoint interval must be >= 1");

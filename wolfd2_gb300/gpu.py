@@ -423,6 +423,22 @@ class Solver:
         self._check(self.L.wolfd2gpu_step(self.h, C.byref(pr), nsteps, st))
         return [(s.nQLiter, s.nSorConv, tuple(s.dif), s.divmax) for s in st[:nsteps]]
 
+    def step_log(self, prm: RunParams, nsteps: int, path: str, k0: int = 0, dtime0: float = 0.0,
+                 **kw) -> List[tuple]:
+        """nsteps steps, then one JSON line per step appended to `path` with
+        the fields of the reference's PrintDiff table (src/string.f:467-566):
+        step k, dimensionless time, nQLiter, nSorConv and the max-norm
+        differences of p, u, v (and t), plus the divergence check."""
+        import json
+        import math
+        hist = self.step(prm, nsteps, **kw)
+        with open(path, "a") as fh:
+            for n, (nql, nsor, dif, divmax) in enumerate(hist, 1):
+                rec = {"k": k0 + n, "time": dtime0 + n * prm.dk, "nQLiter": nql, "nSorConv": nsor,
+                       "dif": [None if math.isnan(x) else x for x in dif], "divmax": divmax}
+                fh.write(json.dumps(rec) + "\n")
+        return hist
+
     def step_counts(self, prm: RunParams, counts) -> List[tuple]:
         """Plain steps with each step's (Q-L iterations, SOR sweeps) fixed."""
         counts = np.ascontiguousarray(np.asarray(counts, dtype=np.int32).ravel())
