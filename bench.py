@@ -656,7 +656,8 @@ def run_adjoint(args):
     mu[2:nx, 2:ny + 1] = True
     mv[2:nx + 1, 2:ny] = True
     eps = ADJOINT["eps"]
-    errs, pairs = [], []
+    extra_eps = [float(x) for x in args.fd_eps.split(",") if x] if args.fd_eps else []
+    errs, errs4, pairs, sweep = [], [], [], {}
     t0 = time.perf_counter()
     for _ in range(args.fd_dirs):
         du = np.where(mu, rng.normal(size=u0.shape), 0.0)
@@ -665,11 +666,27 @@ def run_adjoint(args):
         if args.adj_case == "channel":
             dl[:2] = 0.0          # rows outside the channel carry no inflow
             dl[case.ny + 1:] = 0.0
-        fd = (J_at(u0 + eps * du, v0 + eps * dv, lid + eps * dl) -
-              J_at(u0 - eps * du, v0 - eps * dv, lid - eps * dl)) / (2 * eps)
         ad = float(np.sum(gu * du) + np.sum(gv * dv) + np.sum(gl * dl))
-        pairs.append((ad, fd))
-        errs.append(abs(ad - fd) / max(abs(fd), 1e-300))
+        for e_ in [eps] + extra_eps:
+            Jp = J_at(u0 + e_ * du, v0 + e_ * dv, lid + e_ * dl)
+            Jm = J_at(u0 - e_ * du, v0 - e_ * dv, lid - e_ * dl)
+            fd = (Jp - Jm) / (2 * e_)
+            fd4 = None
+            if args.fd_order == 4:
+                # fourth-order central difference: cancels the eps^2
+                # truncation term of the two-point one
+                J2p = J_at(u0 + 2 * e_ * du, v0 + 2 * e_ * dv, lid + 2 * e_ * dl)
+                J2m = J_at(u0 - 2 * e_ * du, v0 - 2 * e_ * dv, lid - 2 * e_ * dl)
+                fd4 = (8.0 * (Jp - Jm) - (J2p - J2m)) / (12 * e_)
+            if e_ == eps:
+                pairs.append((ad, fd))
+                errs.append(abs(ad - fd) / max(abs(fd), 1e-300))
+                if fd4 is not None:
+                    errs4.append(abs(ad - fd4) / max(abs(fd4), 1e-300))
+            else:
+                sweep.setdefault(e_, []).append(
+                    (abs(ad - fd) / max(abs(fd), 1e-300),
+                     None if fd4 is None else abs(ad - fd4) / max(abs(fd4), 1e-300)))
     t_fd = time.perf_counter() - t0
     s.close()
     if rank != 0:
@@ -702,6 +719,12 @@ def run_adjoint(args):
         "gradient_s": t_adj, "forward_s": t_fwd, "adjoint_over_forward": t_adj / t_fwd,
         "J": J, "fd_check": {"directions": args.fd_dirs, "eps": eps, "max_rel_err": max(errs) if errs else None,
                              "median_rel_err": float(np.median(errs)) if errs else None,
+                             "order4_max_rel_err": max(errs4) if errs4 else None,
+                             "order4_median_rel_err": float(np.median(errs4)) if errs4 else None,
+                             "eps_sweep": {f"{e_:g}": {"order2_max_rel_err": max(x[0] for x in v),
+                                                      "order4_max_rel_err": (max(x[1] for x in v)
+                                                                             if v[0][1] is not None else None)}
+                                           for e_, v in sweep.items()},
                              "pairs": pairs[:8], "seconds": t_fd},
         "iterations": {"nql_min": int(counts[:, 0].min()), "nql_max": int(counts[:, 0].max()),
                        "nsor_min": int(counts[:, 1].min()), "nsor_max": int(counts[:, 1].max())},
@@ -922,6 +945,10 @@ def main():
     ap.add_argument("--adj-case", choices=["cavity", "channel"], default="cavity",
                     help="adjoint: the 256x256 cavity (lid profile) or the profiled channel (inflow profile)")
     ap.add_argument("--fd-dirs", type=int, default=4, help="adjoint: finite-difference directions checked")
+    ap.add_argument("--fd-eps", default="", help="adjoint: further eps values for the same directions, "
+                    "comma-separated (the configuration's eps=1e-6 is always checked)")
+    ap.add_argument("--fd-order", type=int, choices=[2, 4], default=4,
+                    help="adjoint: also check against the fourth-order central difference (4 runs per direction)")
     ap.add_argument("--n", type=int, default=1024, help="cavity cells per side")
     ap.add_argument("--re", type=float, default=1000.0)
     ap.add_argument("--dt", type=float, default=2.5e-4)

@@ -57,3 +57,19 @@ def test_snapshot_overlaps_steps(thermal):
     s.snapshot(host)
     s.snapshot_wait()
     s.close()
+
+
+def test_step_log(tmp_path):
+    """The per-step JSONL log carries PrintDiff's fields, one line a step."""
+    import json
+    case = deck.cavity(32, 100.0, 0.005, solver="rb_sor")
+    s = Solver.for_case(case, tuned=False)
+    s.load_fields(*deck.perturbation_ic(case, 3))
+    path = str(tmp_path / "steps.jsonl")
+    hist = s.step_log(case.params, 3, path, k0=10, dtime0=1.0)
+    s.close()
+    recs = [json.loads(x) for x in open(path)]
+    assert [r["k"] for r in recs] == [11, 12, 13]
+    assert [(r["nQLiter"], r["nSorConv"]) for r in recs] == [(h[0], h[1]) for h in hist]
+    assert recs[-1]["time"] == pytest.approx(1.0 + 3 * case.params.dk)
+    assert len(recs[0]["dif"]) == 4
