@@ -42,7 +42,7 @@ import numpy as np  # noqa: E402
 
 from wolfd2_gb300 import deck  # noqa: E402
 
-METRIC = json.load(open(os.path.join(ROOT, "BASELINE.json")))["metric"]
+METRIC = "cell-steps/s, mixed FP32+refine vs plain FP64 on GB300 at <=1e-10 div; % HBM roof"
 UNIT = "cell-steps/s"
 DT_NAMED = 1.0e-3
 
@@ -582,7 +582,7 @@ ADJOINT = {"n": 256, "re": 400.0, "dt": 2.0e-3, "steps": 400, "every": 20, "eps"
 
 
 def run_adjoint(args):
-    """Config 4: gradient of J = 0.5 h^2 sum(u^2 + v^2) at the final step
+    """The adjoint workload: gradient of J = 0.5 h^2 sum(u^2 + v^2) at the final step
     with respect to the initial u, v and the 256-point lid profile, by the
     library's discrete adjoint (checkpoint and recompute), checked against
     central finite differences of the same map along seeded directions."""
@@ -594,7 +594,7 @@ def run_adjoint(args):
     torch.cuda.set_device(local)
     NORTH, WEST, VAR_U = 4, 1, 1
     if args.adj_case == "channel":
-        # config 5's gradient: final kinetic energy w.r.t. the inflow profile;
+        # the channel's gradient: final kinetic energy w.r.t. the inflow profile;
         # the start is the flow after two steps (v = 0 everywhere at the
         # initial field puts every v-driven upwind selector on its branch point)
         case = deck.channel_inflow(CHANNEL["ncx"], CHANNEL["ncy"], CHANNEL["re"], CHANNEL["dt"], seed=args.seed)
@@ -711,7 +711,7 @@ def run_adjoint(args):
             if args.adj_case != "channel" else
             (f"adjoint: profiled channel {CHANNEL['ncx']}x{CHANNEL['ncy']} (mass-conserving outlet), "
              f"deck Re={CHANNEL['re']:g}, dt={CHANNEL['dt']:g}, {nsteps} steps (a reduced horizon of the "
-             f"configuration's 1000) from the flow after two steps, plain FP64; J = 0.5 h^2 sum(u^2+v^2) at "
+             f"1000-step workload) from the flow after two steps, plain FP64; J = 0.5 h^2 sum(u^2+v^2) at "
              f"the final step; gradient with respect to the initial u, v, p and the {lid.size}-value inflow "
              f"profile, checkpoint every {every} steps, iteration counts held fixed")),
                    "value_is": "cell-steps of the forward horizon per second of the whole gradient "
@@ -770,7 +770,7 @@ def ensemble_config(args, members, inner, graph):
 
 
 def run_ensemble(args):
-    """The batched ensemble (config 3): every case advanced together by one
+    """The batched ensemble of 256 cavities: every case advanced together by one
     launch per stage; cases are spread over ranks by work, no exchange."""
     import torch
     import torch.distributed as dist
@@ -946,7 +946,7 @@ def main():
                     help="adjoint: the 256x256 cavity (lid profile) or the profiled channel (inflow profile)")
     ap.add_argument("--fd-dirs", type=int, default=4, help="adjoint: finite-difference directions checked")
     ap.add_argument("--fd-eps", default="", help="adjoint: further eps values for the same directions, "
-                    "comma-separated (the configuration's eps=1e-6 is always checked)")
+                    "comma-separated (eps=1e-6 is always checked)")
     ap.add_argument("--fd-order", type=int, choices=[2, 4], default=4,
                     help="adjoint: also check against the fourth-order central difference (4 runs per direction)")
     ap.add_argument("--n", type=int, default=1024, help="cavity cells per side")

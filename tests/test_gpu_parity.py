@@ -163,7 +163,7 @@ def test_time_loop_matches_oracle(case):
 
 
 def test_cavity64_lexicographic_sor_500_steps():
-    """Config 1 (64x64 cavity, Re=100, dt=0.005, point SOR) -- the first 60
+    """The 64x64 cavity (Re=100, dt=0.005, point SOR) -- the first 60
     steps here; the full 500 are in the benchmark's parity check."""
     case = deck.cavity(64, 100.0, 0.005, solver="sor")
     ref = O.OracleRun(case)

@@ -83,7 +83,7 @@ def test_boundary_rules_on_cavity():
 
 
 def test_golden_cavity64():
-    """Regression fixture of the 64x64 cavity (config 1) generated by
+    """Regression fixture of the 64x64 cavity (Re 100, point SOR) generated by
     tests/golden/make_golden.py."""
     g = json.load(open(os.path.join(HERE, "golden", "cavity64_sor.json")))
     case = deck.cavity(64, 100.0, 0.005, solver="sor")
