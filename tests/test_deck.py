@@ -126,3 +126,54 @@ def test_plot3d_solution_layout(tmp_path):
     raw = open(pre + ".qqq", "rb").read()
     assert np.frombuffer(raw[:4], "<i4")[0] == 12 and len(raw) == 4 + 12 + 4 + 4 + nx * ny * 5 * 8 + 4
     assert open(pre + ".nam").read().splitlines()[-1] == " Complete Temperature"
+
+
+def test_read_deck_round_trip(tmp_path):
+    """A deck written by write_deck (with its grid and fluid files) reads back
+    into the same case: ReadParam's scaling gives the same dk and Re, the grid
+    and the region tables are the same."""
+    c = deck.channel(16, 8, 500.0, 1e-3, solver="par_rb_sor")
+    deck.write_deck(str(tmp_path / "input.dat"), c, nts=3)
+    deck.write_grid_plot3d(str(tmp_path / "grid.xyz"), c.x, c.y)
+    deck.write_fluid_table(str(tmp_path / "fluidprop.dat"), 1.0, 1.0 / c.params.re)
+    r = deck.read_deck(str(tmp_path / "input.dat"))
+    assert (r.nx, r.ny) == (c.nx, c.ny)
+    assert np.array_equal(r.x, c.x) and np.array_equal(r.y, c.y)
+    for k in ("dk", "npsolver", "msorit", "sortol", "sorrel", "mqiter", "qtol", "lcartes"):
+        assert getattr(r.params, k) == getattr(c.params, k), k
+    assert r.params.re == pytest.approx(c.params.re, rel=1e-15)
+    assert r.params.nts == 3
+    for k in ("nRegBrd", "nRegType", "nMomBdTp", "dBCVal"):
+        assert np.array_equal(getattr(r.regions, k), getattr(c.regions, k)), k
+    assert r.thermal is None
+
+
+def test_read_deck_thermal_and_fluid_interpolation(tmp_path):
+    """thermal_energy / buoyancy decks: Pe = Re Pr and Fr from the reference
+    quantities, the fluid row interpolated at ref_temperature, temperatures
+    scaled to (T - tref)/(tmax - tref), heat sources scaled."""
+    (tmp_path / "grid.xyz").write_text("")
+    c = deck.cavity(8, 100.0, 0.01)
+    deck.write_grid_plot3d(str(tmp_path / "grid.xyz"), c.x, c.y)
+    (tmp_path / "fluid.dat").write_text(
+        "# two fluids\nfluid water\n250 2.0 4.0 0.02 0.6 7.0\n350 2.0 4.0 0.02 0.6 7.0\nend\n"
+        "fluid air01 gasconstant 287.0\n280 1.2 1000 0.010 0.025 0.70\n320 1.0 1000 0.012 0.027 0.72\nend\n")
+    (tmp_path / "input.dat").write_text(
+        "section input_parameters\n grid_file grid.xyz cartesian_grid\n thermal_energy\n buoyancy\n"
+        " time_step_size 0.02\n ref_length 2.0\n ref_velocity 0.5\n ref_temperature 300\n"
+        " max_ref_temperature 400\n fluid_prop_file fluid.dat\n max_me_iter 3\n me_tolerance 1d-6\n"
+        " filter_t 8.0\n ppe_solver rb_sor\nend section\n\n"
+        "section boundary_conditions\n number_of_regions 1 1\n i_borders\n j_borders\n"
+        " wall 1 1 west t 350\n heat_generation_region 1 1 5.0\nend section\n")
+    r = deck.read_deck(str(tmp_path / "input.dat"))
+    rho, mu, k, pr = 1.1, 0.011, 0.026, 0.71      # the rows at 300 K
+    assert r.params.dk == pytest.approx(0.02 * 0.5 / 2.0)
+    assert r.params.re == pytest.approx(2.0 * 0.5 / (mu / rho), rel=1e-12)
+    assert r.params.fr == pytest.approx(0.25 / (2.0 * 9.81))
+    tp = r.tparams
+    assert (tp.nthermen, tp.neqstate, tp.nmeiter, tp.nfiltt) == (1, 1, 3, 1)
+    assert tp.dmeittol == 1e-6 and tp.fpt == 8.0 and tp.rconst == 287.0
+    assert tp.pe == pytest.approx(r.params.re * pr, rel=1e-12)
+    assert r.regions.dBCVal[0, 0, deck.WEST - 1, deck.VAR_T - 1] == pytest.approx(0.5)
+    assert r.thermal.dHGSTval[0, 0] == pytest.approx(5.0 * 4.0 / (tp.pe * k * 100.0), rel=1e-12)
+    assert r.x.max() == pytest.approx(c.x.max() / 2.0)

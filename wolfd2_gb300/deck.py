@@ -838,3 +838,230 @@ def read_restart(path: str):
     arr = np.frombuffer(recs[2], "<f8").reshape(8, ny + 2, nx + 2)
     fields = [np.asfortranarray(a.T) for a in arr]
     return k, dtime, nx, ny, fields
+
+
+# ---- input_parameters section and fluid table (ReadParam) -----------------
+
+@dataclasses.dataclass
+class DeckInput:
+    """The input_parameters section as ReadParam leaves it (src/parse.f:117-193
+    defaults, src/parse.f:261-903 keywords), before the reference scaling."""
+    grid_file: str = ""
+    lcartes: int = 0
+    nthermen: int = 0
+    neqstate: int = 0
+    nts: int = 0
+    dt: float = 0.0                 # physical time step (time_step_size)
+    mqiter: int = 20
+    qtol: float = 1.0e-4
+    nmeiter: int = 1
+    dmeittol: float = 1.0e-4
+    nfiltu: int = 0
+    nfiltv: int = 0
+    nfiltt: int = 0
+    fpu: float = 5.0e2
+    fpv: float = 5.0e2
+    fpt: float = 5.0
+    npsolver: int = 1
+    msorit: int = 2000
+    sortol: float = 1.0e-8
+    sorrel: float = 1.0
+    dlref: float = 1.0
+    uref: float = 1.0
+    tref: float = 283.57
+    tmax: float = 1.0e3
+    fluid_file: str = "fluidprop.dat"
+    fluid_name: str = "air01"
+    restart: Optional[str] = None
+    write_restart: Optional[str] = None
+    write_restart_freq: int = 0     # 0: at the end only
+    print_diff_freq: int = 1
+    other: dict = dataclasses.field(default_factory=dict)  # keywords off the hot path, as read
+
+
+_INT_KEYS = {"n_time_steps": "nts", "max_ql_iter": "mqiter", "max_me_iter": "nmeiter",
+             "max_sor_iter": "msorit", "print_diff_freq": "print_diff_freq"}
+_REAL_KEYS = {"time_step_size": "dt", "ql_tolerance": "qtol", "me_tolerance": "dmeittol",
+              "sor_tolerance": "sortol", "sor_relaxation": "sorrel", "ref_length": "dlref",
+              "ref_velocity": "uref", "ref_temperature": "tref", "max_ref_temperature": "tmax"}
+_FILTER_KEYS = {"filter_u": ("nfiltu", "fpu"), "filter_v": ("nfiltv", "fpv"), "filter_t": ("nfiltt", "fpt")}
+# accepted and kept as read: ATD, time averaging, trajectories and output control
+_OTHER_KEYS = {"small_scale", "trajectories", "atd_cu0", "atd_tscf", "atd_hscf", "atd_bnumcrit",
+               "atd_rmapmax", "atd_rmapexp", "atd_temcf", "atd_ppe_solver", "atd_max_sor_iter",
+               "atd_sor_tolerance", "atd_sor_relaxation", "atd_filter_u", "atd_filter_v", "atd_filter_t",
+               "time_average_mode", "output_format", "output_prefix", "snapshots_prefix", "snapshots_freq",
+               "snapshots_first", "time_series_prefix", "time_series_freq", "time_series_point",
+               "print_bann_freq"}
+
+
+def _sections(text: str):
+    """{section name: body text} of a deck (``section <name>`` ... ``end
+    section``, case-insensitive keywords, ``#`` comments)."""
+    out, cur, body = {}, None, []
+    for raw in text.splitlines():
+        line = raw.split("#", 1)[0].strip()
+        w = line.lower().split()
+        if not w:
+            continue
+        if w[0] == "section":
+            if cur is not None or len(w) < 2:
+                raise DeckError("SECTION keyword misplaced")
+            cur, body = w[1], []
+        elif w[0] == "end" and len(w) > 1 and w[1] == "section":
+            if cur is None:
+                raise DeckError("END SECTION without SECTION")
+            out[cur] = "\n".join(body)
+            cur = None
+        elif cur is not None:
+            body.append(line)
+    if cur is not None:
+        raise DeckError(f"section {cur} not closed")
+    return out
+
+
+def parse_input_section(text: str) -> DeckInput:
+    """The input_parameters keywords (src/parse.f:261-903)."""
+    d = DeckInput()
+    for raw in text.splitlines():
+        w = raw.split("#", 1)[0].split()
+        if not w:
+            continue
+        key = w[0].lower()
+
+        def arg(k=1):
+            if len(w) <= k:
+                raise DeckError(f"{key}: value missing")
+            return w[k]
+        try:
+            if key == "grid_file":
+                d.grid_file = arg()
+                if len(w) > 2:
+                    if w[2].lower() != "cartesian_grid":
+                        raise DeckError(f"Unrecognized keyword: [{w[2]}]")
+                    d.lcartes = 1
+            elif key == "thermal_energy":
+                d.nthermen = 1
+            elif key == "buoyancy":
+                d.neqstate = 1
+            elif key in _INT_KEYS:
+                setattr(d, _INT_KEYS[key], int(arg()))
+            elif key in _REAL_KEYS:
+                setattr(d, _REAL_KEYS[key], float(arg().replace("d", "e").replace("D", "e")))
+            elif key in _FILTER_KEYS:
+                flag, par = _FILTER_KEYS[key]
+                setattr(d, flag, 1)
+                setattr(d, par, float(arg().replace("d", "e").replace("D", "e")))
+            elif key == "ppe_solver":
+                name = arg().lower()
+                if name not in PPE_SOLVERS:
+                    raise DeckError(f"Unrecognized ppe_solver: [{name}]")
+                d.npsolver = PPE_SOLVERS[name]
+            elif key == "fluid_prop_file":
+                d.fluid_file = arg()
+            elif key == "fluid_prop_table":
+                d.fluid_name = arg()
+            elif key == "restart":
+                d.restart = arg()
+            elif key == "write_restart":
+                d.write_restart = arg()
+                d.write_restart_freq = int(w[2]) if len(w) > 2 else 0
+            elif key in _OTHER_KEYS:
+                d.other[key] = w[1:]
+            else:
+                raise DeckError(f"Unrecognized keyword: [{key}]")
+        except ValueError as exc:
+            raise DeckError(f"{key}: bad value {' '.join(w[1:])!r}") from exc
+    return d
+
+
+def read_fluid_props(path: str, name: str, tref: float) -> dict:
+    """lReadFldProps (src/parse.f:2027-2250): the rows ``T rho c mu k Pr`` of
+    fluid ``name`` (optional ``gasconstant R`` on its ``fluid`` line), linearly
+    interpolated at tref between the bracketing rows as dLinInterp does
+    (src/utility.f:654-662: y1 + (y2 - y1)(x - x1)/(x2 - x1), with the
+    current row as point 1 and the previous one as point 2)."""
+    found, inside, prev, rconst = False, False, None, 0.0
+    nrow = 0
+    for raw in open(path):
+        line = raw.strip()
+        if not line:
+            continue
+        if line.startswith("#"):
+            if inside:
+                raise DeckError("Comments not allowed inside Fluid Def.")
+            continue
+        w = line.lower().split()
+        if w[0] == "fluid" and not inside:
+            inside, nrow, prev = True, 0, None
+            found = len(w) > 1 and w[1] == name.lower()
+            if found and len(w) > 3 and w[2] == "gasconstant":
+                rconst = float(w[3])
+            continue
+        if w[0] == "end" and inside:
+            inside = False
+            if found:
+                raise DeckError("Did not find requested interval")
+            continue
+        if inside and found:
+            nrow += 1
+            row = [float(x) for x in w[:6]]
+            if nrow == 1 and row[0] > tref:
+                raise DeckError(f"Searched value ({tref}) is lower than first entry in table")
+            p = prev if prev is not None else [0.0] * 6
+            if nrow > 1 and p[0] > row[0]:
+                raise DeckError("Entries should be arranged in ascending order with respect to temperature")
+            if p[0] <= tref <= row[0]:
+                vals = [row[k] + (p[k] - row[k]) * (tref - row[0]) / (p[0] - row[0]) for k in range(1, 6)]
+                return {"tref": tref, "densref": vals[0], "c": vals[1], "mu": vals[2],
+                        "dconduct": vals[3], "prandtl": vals[4], "rconst": rconst}
+            prev = row
+    raise DeckError(f"fluid {name!r} not found in {path}")
+
+
+def read_grid_plot3d(path: str):
+    """2-D formatted Plot3D grid as ReadGrid reads it (src/grid.f:189-228):
+    ``nx ny``, then every x (i fastest), then every y; returns (nx, ny, X, Y)
+    with X, Y of shape (nx, ny)."""
+    vals = open(path).read().replace("d", "e").replace("D", "e").split()
+    nx, ny = int(vals[0]), int(vals[1])
+    a = np.array([float(v) for v in vals[2:2 + 2 * nx * ny]])
+    X = a[:nx * ny].reshape((nx, ny), order="F")
+    Y = a[nx * ny:].reshape((nx, ny), order="F")
+    return nx, ny, X, Y
+
+
+def read_deck(path: str, base: Optional[str] = None) -> Case:
+    """A reference input deck (both sections, src/main.f:311-312) with its grid
+    and fluid files (relative to ``base``, default the deck's folder) as a
+    Case: ReadParam's scaling (src/file_manip.f:130-157: dk = dt uref/dlref,
+    Re = dlref uref rho/mu, Pe = Re Pr, Fr = uref^2/(9.81 dlref)), the grid
+    nodes divided by dlref, the boundary section with its thermal tables, and
+    the heat sources of bound_cond.f:2018-2029."""
+    import os
+    base = base if base is not None else os.path.dirname(os.path.abspath(path))
+    sec = _sections(open(path).read())
+    if "input_parameters" not in sec or "boundary_conditions" not in sec:
+        raise DeckError("a deck needs input_parameters and boundary_conditions sections")
+    d = parse_input_section(sec["input_parameters"])
+    fl = read_fluid_props(os.path.join(base, d.fluid_file), d.fluid_name, d.tref)
+    kinvisc = fl["mu"] / fl["densref"]
+    re = d.dlref * d.uref / kinvisc
+    fr = d.uref ** 2.0 / (d.dlref * 9.81)
+    prm = RunParams(dk=d.dt * d.uref / d.dlref, re=re, fr=fr, nts=d.nts, mqiter=d.mqiter, qtol=d.qtol,
+                    npsolver=d.npsolver, msorit=d.msorit, sortol=d.sortol, sorrel=d.sorrel,
+                    nfiltu=d.nfiltu, nfiltv=d.nfiltv, fpu=d.fpu, fpv=d.fpv, lcartes=d.lcartes)
+    nx, ny, X, Y = read_grid_plot3d(os.path.join(base, d.grid_file))
+    regs = parse_bc_section(sec["boundary_conditions"], nx, ny, uref=d.uref, densref=fl["densref"],
+                            dlref=d.dlref, re=re, tref=fl["tref"], tmax=d.tmax)
+    case = Case(os.path.splitext(os.path.basename(path))[0], nx, ny, X / d.dlref, Y / d.dlref, regs, prm,
+                sec["boundary_conditions"])
+    if d.nthermen or d.neqstate:
+        pe = re * fl["prandtl"]
+        if d.nthermen:
+            heat_sources(regs, d.dlref, fl["tref"], d.tmax, fl["dconduct"], pe)
+        case.thermal = regs.thermal
+        case.tparams = ThermalParams(nthermen=d.nthermen, neqstate=d.neqstate, nmeiter=d.nmeiter,
+                                     dmeittol=d.dmeittol, pe=pe, uref=d.uref, densref=fl["densref"],
+                                     tmax=d.tmax, tref=fl["tref"], rconst=fl["rconst"], nfiltt=d.nfiltt,
+                                     fpt=d.fpt)
+    return case
