@@ -191,3 +191,35 @@ def test_thermal_time_loop_matches_oracle(name, graph):
         assert np.array_equal(g, r), (name_, float(np.max(np.abs(g - r))))
     assert np.abs(t).max() > 0.1
     s.close()
+
+
+def test_deck_driven_thermal_run(tmp_path):
+    """A reference-style deck (thermal energy, buoyancy, Filter of t, a fluid
+    table) read by read_deck and stepped on the device equals the oracle's
+    time loop on the same case."""
+    c = deck.cavity(32, 100.0, 0.01)
+    deck.write_grid_plot3d(str(tmp_path / "grid.xyz"), c.x, c.y)
+    (tmp_path / "fluid.dat").write_text(
+        "fluid air01 gasconstant 287.0\n280 1.2 1000 0.010 0.025 0.70\n320 1.0 1000 0.012 0.027 0.72\nend\n")
+    (tmp_path / "input.dat").write_text(
+        "section input_parameters\n grid_file grid.xyz cartesian_grid\n thermal_energy\n buoyancy\n"
+        " time_step_size 0.004\n ref_temperature 300\n max_ref_temperature 330\n"
+        " fluid_prop_file fluid.dat\n max_me_iter 2\n me_tolerance 1d-9\n filter_t 50.0\n"
+        " ppe_solver rb_sor\n max_sor_iter 400\nend section\n\n"
+        "section boundary_conditions\n number_of_regions 1 1\n i_borders\n j_borders\n"
+        " wall 1 1 north tv 1.0\n wall 1 1 west t 330\n wall 1 1 east t 300\nend section\n")
+    case = deck.read_deck(str(tmp_path / "input.dat"))
+    o = O.OracleRun(case)
+    o.step(4)
+    s = Solver.for_case(case, tuned=False)
+    z = s.field()
+    s.load_fields(z, z, z)
+    s.cold_start(case.params)
+    hist = s.step(case.params, 4)
+    assert [(h[0], h[1]) for h in hist] == [h[:2] for h in o.history]
+    u, v, p = s.store_fields()
+    t, d = s.store_thermal()
+    for nm, g in zip("uvptd", (u, v, p, t, d)):
+        assert np.array_equal(g, o.f[nm]), nm
+    assert np.abs(t).max() > 0.1
+    s.close()
