@@ -1,10 +1,21 @@
-"""Generate tests/golden/cavity64_sor.json: the first 40 steps of the 64x64
-lid-driven cavity (Re=100, dt=0.005, point SOR, cold start).
+"""Generate the golden fixtures under tests/golden/: short time loops of the
+oracle, each checked against the mechanical translation of the reference's
+own Fortran source (oracle/f77ref.py) when the reference tree is present.
 
-The fixture is produced by the mechanical translation of the reference's own
-Fortran source (oracle/f77ref.py) when the reference tree is present, and
-must agree with the oracle (the script asserts it); the file records which
-produced it."""
+  cavity64_sor.json          64x64 lid-driven cavity, Re=100, dt=0.005,
+                             point SOR, cold start, 40 steps
+  heated24_filter.json       24x24 differentially heated cavity (energy
+                             equation, EqState, buoyancy), two momentum /
+                             energy iterations, Filter of t, 6 steps
+  thermal_multiregion.json   the curvilinear 3 x 2 region layout with a
+                             fixed-temperature and a heat-generating region,
+                             3 momentum / energy iterations, 5 steps
+  curvilinear_rb_lsor.json   the curvilinear 3 x 2 layout, plain step,
+                             lcartes = 0 (cross terms in every sweep),
+                             red-black line SOR, 5 steps
+
+Each file records which produced it: the oracle alone, or the translated
+reference source with the oracle equal to it bit for bit."""
 import json
 import math
 import os
@@ -14,38 +25,84 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle")]
+sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle"), os.path.dirname(HERE)]
 
 import f77ref  # noqa: E402
 import oracle as O  # noqa: E402
+import thermal_setup  # noqa: E402
 from wolfd2_gb300 import deck  # noqa: E402
 
-STEPS = 40
+
+def _cavity64():
+    return deck.cavity(64, 100.0, 0.005, solver="sor")
 
 
-def main():
-    case = deck.cavity(64, 100.0, 0.005, solver="sor")
+def _heated24():
+    case = deck.heated_cavity(24, 500.0, 0.004, nmeiter=2, dmeittol=1e-7)
+    case.tparams.nfiltt = 1
+    case.tparams.fpt = 20.0
+    return case
+
+
+def _curvilinear_rb_lsor():
+    case = thermal_setup.curvilinear_case()
+    case.params.npsolver = deck.PPE_SOLVERS["rb_lsor"]
+    case.params.msorit = 300
+    return case
+
+
+# name -> (case factory, steps, description, fields)
+FIXTURES = {
+    "cavity64_sor": (_cavity64, 40, "cavity 64x64, Re=100, dt=0.005, ppe_solver sor, cold start",
+                     "uvp"),
+    "heated24_filter": (_heated24, 6, "heated cavity 24x24, Re=500, Pr=0.71, Fr=0.05, dt=0.004, "
+                        "nmeiter 2, EqState + buoyancy, filter_t 20, rb_sor", "uvptd"),
+    "thermal_multiregion": (lambda: thermal_setup.loop_case(), 5,
+                            "curvilinear 3 x 2 regions, fixed-temperature and heat-generating "
+                            "regions, energy equation with EqState and buoyancy", "uvptd"),
+    "curvilinear_rb_lsor": (_curvilinear_rb_lsor, 5, "curvilinear 3 x 2 regions, lcartes 0, "
+                            "ppe_solver rb_lsor, msorit 300", "uvp"),
+}
+
+
+def summary(o, fields):
+    """The size-independent record a fixture keeps of an oracle run."""
+    out = {"cold_nconv": o.cold_nconv,
+           "iterations": [[h[0], h[1]] for h in o.history],
+           "dif_last": list(o.history[-1][2]),
+           "sum": {k: math.fsum(o.f[k].ravel()) for k in fields},
+           "abs_sum": {k: math.fsum(np.abs(o.f[k]).ravel()) for k in fields}}
+    return out
+
+
+def make(name):
+    factory, steps, desc, fields = FIXTURES[name]
+    case = factory()
     o = O.OracleRun(case)
-    o.step(STEPS)
+    o.step(steps)
     src = "oracle"
     if f77ref.available():
         import refrun
         f77ref.build(case.nx + 1, case.ny + 1)
         r = refrun.RefRun(case)
-        r.step(STEPS)
-        for k in "uvp":
-            assert np.array_equal(r.f[k], o.f[k]), k
-        assert [h[:2] for h in r.history] == [h[:2] for h in o.history]
+        r.step(steps)
+        for k in fields:
+            assert np.array_equal(r.f[k], o.f[k]), (name, k)
+        assert [h[:2] for h in r.history] == [h[:2] for h in o.history], name
+        assert [h[2] for h in r.history] == [h[2] for h in o.history], name
         src = "translated reference source (oracle/f77ref.py), equal to the oracle"
-    out = {"case": "cavity 64x64, Re=100, dt=0.005, ppe_solver sor, cold start",
-           "steps": STEPS, "source": src, "cold_nconv": o.cold_nconv,
-           "iterations": [[h[0], h[1]] for h in o.history],
-           "dif_last": list(o.history[-1][2]),
-           "sum": {k: math.fsum(o.f[k].ravel()) for k in "uvp"},
-           "abs_sum": {k: math.fsum(np.abs(o.f[k]).ravel()) for k in "uvp"}}
-    with open(os.path.join(HERE, "cavity64_sor.json"), "w") as f:
+    out = {"case": desc, "steps": steps, "source": src}
+    out.update(summary(o, fields))
+    if name != "cavity64_sor":
+        out["fields"] = fields
+    with open(os.path.join(HERE, name + ".json"), "w") as f:
         json.dump(out, f, indent=1)
-    print("wrote", out["source"])
+    print("wrote", name, "from", out["source"])
+
+
+def main():
+    for name in (sys.argv[1:] or FIXTURES):
+        make(name)
 
 
 if __name__ == "__main__":
