@@ -41,11 +41,14 @@ ROUTINES = {
     "src/pressure.f": ["ppe", "divergence", "rhsppe", "sor", "sorrb", "sorrbp", "slor",
                        "slorrb", "slorrbp"],
     "src/utility.f": ["filter", "project", "diffmaxnorm", "dmaxnorm"],
-    "src/bound_cond.f": ["velboundcond", "presboundcond", "veloutflowbcs", "tempboundcond"],
+    "src/bound_cond.f": ["velboundcond", "presboundcond", "veloutflowbcs", "tempboundcond",
+                         "smlsclbc"],
     "src/grid.f": ["mirrorpts", "fullgrid", "metric"],
     "src/thermal.f": ["thermenergy", "eqstate"],
+    "src/small_scale.f": ["smallscale"],
 }
 
+FPPDEFS = {"_SMALLSCL_", "_TIMEAVG_", "_TRAJECT_"}  # Makefile:47, the default build
 STACK_LIMIT = 65536  # gfortran -fmax-stack-var-size default: larger locals are static
 REF_DEFAULT = {"mnx": "302", "mny": "302"}  # include/config.f:19-20
 
@@ -71,11 +74,28 @@ def _statements(path: str, macros: Dict[str, str]) -> List[str]:
     """Fixed-form lines -> logical statements (lower case, comments and
     preprocessor lines removed, continuations joined, macros expanded)."""
     stmts: List[str] = []
+    active: List[bool] = []     # one entry per open #ifdef / #ifndef
+    in_comment = False          # inside a C comment (the build runs cpp)
     for raw in open(path, encoding="latin-1"):
         line = raw.rstrip("\n").expandtabs(6)
-        if not line.strip() or line[0] in "Cc*!" or line.lstrip().startswith("#"):
+        if in_comment:
+            in_comment = "*/" not in line
             continue
-        if line.lstrip().startswith("/*") or line.lstrip().startswith("*/"):
+        if line.lstrip().startswith("/*"):
+            in_comment = "*/" not in line
+            continue
+        d = re.match(r"^\s*#\s*(ifdef|ifndef|else|endif)\b\s*(\w*)", line)
+        if d:
+            if d.group(1) in ("ifdef", "ifndef"):
+                active.append((d.group(2) in FPPDEFS) == (d.group(1) == "ifdef"))
+            elif d.group(1) == "else":
+                active[-1] = not active[-1]
+            else:
+                active.pop()
+            continue
+        if not all(active):
+            continue
+        if not line.strip() or line[0] in "Cc*!" or line.lstrip().startswith("#"):
             continue
         body = line[6:72] if len(line) > 6 else ""
         cont = len(line) > 5 and line[5] not in " 0"
@@ -339,6 +359,7 @@ class Unit:
         self.vars: Dict[str, Var] = {}
         self.params: Dict[str, str] = {}
         self.body: List[str] = []
+        self.save_all = False   # a bare SAVE: every local keeps its value between calls
 
 
 def parse_units(stmts: List[str], wanted: List[str], config_params: Dict[str, str]) -> List[Unit]:
@@ -403,6 +424,9 @@ def _declarations(u: Unit, config_params: Dict[str, str]) -> None:
                 continue
             if s.startswith("external"):
                 continue
+            if s == "save":
+                u.save_all = True
+                continue
             decl_done = True
         body.append(s)
     u.body = body
@@ -417,7 +441,10 @@ def _declarations(u: Unit, config_params: Dict[str, str]) -> None:
 # Code generation
 # ---------------------------------------------------------------------------
 
-INTRINSIC_D = {"dabs": "fabs", "dsqrt": "sqrt", "sqrt": "sqrt", "dlog": "log", "dacos": "acos"}
+# double intrinsics -> libm (gfortran calls the same libm entries; datanh is
+# gfortran's intrinsic in the default build, which leaves _DATANH_ undefined)
+INTRINSIC_D = {"dabs": "fabs", "dsqrt": "sqrt", "sqrt": "sqrt", "dlog": "log", "dacos": "acos",
+               "dtanh": "tanh", "datanh": "atanh"}
 
 
 class Gen:
@@ -498,6 +525,7 @@ class Gen:
     def expr(self, e) -> str:
         k = e[0]
         if k == "num":
+            single = "d" not in e[1] and re.search(r"[.e]", e[1]) is not None
             s = e[1].replace("d", "e")
             if re.search(r"[.e]", s):
                 if s.startswith("."):
@@ -506,7 +534,9 @@ class Gen:
                     s = s.replace("e", ".e", 1)
                 if s.endswith("."):
                     s += "0"
-            return s
+            # a literal without a d exponent is default REAL (REAL*4: the
+            # build has no -fdefault-real-8), widened where it meets REAL*8
+            return f"((double){s}f)" if single else s
         if k == "id":
             return self.name_ref(e[1])
         if k == "par":
@@ -594,7 +624,7 @@ class Gen:
                 out.append(f"  {ct} {name} = 0;")
                 continue
             if not v.is_array:
-                out.append(f"  {ct} {name};")
+                out.append(f"  {'static ' if u.save_all else ''}{ct} {name};")
                 continue
             size = " * ".join(f"(({self.cexpr_str(hi)}) - ({self.cexpr_str(lo)}) + 1)" for lo, hi in v.dims)
             const = all(self._is_const(hi) and self._is_const(lo) for lo, hi in v.dims)
@@ -606,7 +636,7 @@ class Gen:
                 # the bounds are raised or lowered for a build.
                 nbytes = self._const_val(size, REF_DEFAULT) * (8 if ct == "double" else 4)
                 csize = self._macro_size(size)
-                if nbytes > STACK_LIMIT:
+                if nbytes > STACK_LIMIT or u.save_all:
                     out.append(f"  static {ct} {name}[{csize}];")
                 else:
                     out.append(f"  {ct} {name}[{csize}];")

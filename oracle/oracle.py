@@ -39,6 +39,22 @@ class _Metrics(C.Structure):
     _fields_ = [(n, _dp) for n in METRIC_NAMES]
 
 
+class AtdParams(C.Structure):
+    """w2o_atd_params: SmallScale's parameters (parse.f:144-178 defaults)."""
+    _fields_ = [(n, C.c_int) for n in ("npsolver", "msorit", "lcartes")] + \
+        [(n, C.c_double) for n in ("dlref", "uref", "tref", "tmax", "dka", "re", "pe", "sortol",
+                                   "sorrel")] + \
+        [("fp", C.c_double * 4)] + \
+        [(n, C.c_double) for n in ("cu0", "tscoef", "hscoef", "temcoef", "bnumc", "rmax", "rlc")]
+
+    @classmethod
+    def make(cls, *, dka, re, pe, npsolver=1, msorit=2000, lcartes=1, dlref=1.0, uref=1.0,
+             tref=300.0, tmax=330.0, sortol=1e-8, sorrel=1.0, fp=(500.0, 500.0, 0.0, 500.0),
+             cu0=0.0, tscoef=1.0, hscoef=1.0, temcoef=1.0, bnumc=200.0, rmax=0.95, rlc=5.0):
+        return cls(npsolver, msorit, lcartes, dlref, uref, tref, tmax, dka, re, pe, sortol, sorrel,
+                   (C.c_double * 4)(*fp), cu0, tscoef, hscoef, temcoef, bnumc, rmax, rlc)
+
+
 class _Thermal(C.Structure):
     _fields_ = [("nTRgType", _ip), ("nTemBdTp", _ip), ("dTRgVal", _dp), ("dHGSTval", _dp)]
 
@@ -116,6 +132,15 @@ def lib():
                                            C.POINTER(_Thermal), C.c_double, C.c_double,
                                            C.POINTER(_Metrics), _dp, _dp, _dp, _dp, _dp, _dp]
             L.w2o_eq_state.argtypes = [C.c_void_p, C.c_int, C.c_int] + [C.c_double] * 5 + [_dp, _dp, _dp]
+            L.w2o_atd_create.argtypes = [C.c_int, C.c_int]
+            L.w2o_atd_create.restype = C.c_void_p
+            L.w2o_atd_destroy.argtypes = [C.c_void_p]
+            L.w2o_sml_scl_bc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions),
+                                         C.POINTER(_Thermal), _dp, _dp, _dp, _dp]
+            L.w2o_small_scale.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                          C.POINTER(_Regions), C.POINTER(_Thermal),
+                                          C.POINTER(AtdParams), C.POINTER(_Metrics)] + [_dp] * 7
+            L.w2o_small_scale.restype = C.c_int
             L.w2o_filter_t.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions),
                                        C.POINTER(_Thermal), C.c_double, _dp]
             L.w2o_cold_start.restype = C.c_int
@@ -284,6 +309,11 @@ class Oracle:
                                 C.byref(self.metrics_struct(met)), _ptr(un), _ptr(vn), _ptr(u),
                                 _ptr(v), _ptr(tn), _ptr(t))
 
+    def sml_scl_bc(self, nx, ny, regs, th, u, v, p, t) -> None:
+        rs, ts = self.regions_struct(regs), self.thermal_struct(th)
+        self.L.w2o_sml_scl_bc(self.h, nx, ny, C.byref(rs), C.byref(ts), _ptr(u), _ptr(v), _ptr(p),
+                              _ptr(t))
+
     def filter_t(self, nx, ny, regs, th, fp, q) -> None:
         rs, ts = self.regions_struct(regs), self.thermal_struct(th)
         self.L.w2o_filter_t(self.h, nx, ny, C.byref(rs), C.byref(ts), fp, _ptr(q))
@@ -350,3 +380,27 @@ def threads() -> int:
     """Host threads the oracle library runs on (1: the restatement is serial,
     like the reference)."""
     return 1
+
+
+class SmallScale:
+    """small_scale.f's SmallScale with its saved state (the map iterates,
+    cell areas and work arrays) held by this object instead of static
+    storage; one object per run."""
+
+    def __init__(self, o: "Oracle", nx: int, ny: int, regs, th, met, ap: AtdParams):
+        self.o, self.nx, self.ny = o, nx, ny
+        self.s = o.L.w2o_atd_create(o.mnx, o.mny)
+        self._rs, self._ts = Oracle.regions_struct(regs), Oracle.thermal_struct(th)
+        self._ms = Oracle.metrics_struct(met)
+        self.ap = ap
+
+    def __call__(self, initflg, u1, v1, t1, uss, vss, pss, tss) -> int:
+        return self.o.L.w2o_small_scale(self.o.h, self.s, self.nx, self.ny, initflg,
+                                        C.byref(self._rs), C.byref(self._ts), C.byref(self.ap),
+                                        C.byref(self._ms), _ptr(u1), _ptr(v1), _ptr(t1), _ptr(uss),
+                                        _ptr(vss), _ptr(pss), _ptr(tss))
+
+    def __del__(self):
+        if getattr(self, "s", None):
+            self.o.L.w2o_atd_destroy(self.s)
+            self.s = None

@@ -1235,3 +1235,355 @@ int w2o_step_thermal(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
   for (int k = 1; k < 4; k++) difmax = dif[k] > difmax ? dif[k] : difmax;
   return difmax > 1.0e12 ? 1 : 0;
 }
+
+/* ------------------------------------------------------------------------
+ * Small-scale (ATD) model: SmlSclBC (bound_cond.f:1211-1500) and SmallScale
+ * (small_scale.f:31-578), the second caller of Ppe and Project.
+ * ---------------------------------------------------------------------- */
+
+void w2o_sml_scl_bc(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                    const w2o_thermal *th, double *u, double *v, double *p,
+                    double *t) {
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      const int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      const int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      int i, j;
+      /* image points: wall faces mirror (no-slip) or copy (no-stress) the
+       * tangential component and zero the normal one */
+      switch (MBTP(r, ireg, jreg, WEST)) {
+        case BM_INTERN: break;
+        case BM_WALL1: case BM_INLET:
+          for (j = jS; j <= jN; j++) F(u, iW, j) = 0.0;
+          for (j = jS + 1; j <= jN; j++) F(v, iW, j) = -F(v, iW + 1, j);
+          break;
+        case BM_WALL2:
+          for (j = jS; j <= jN; j++) F(u, iW, j) = 0.0;
+          for (j = jS + 1; j <= jN; j++) F(v, iW, j) = F(v, iW + 1, j);
+          break;
+        case BM_OUTLT1:
+          if (iW < 1) die("SmlSclBC: west outlet writes column iW-1 outside the array", ireg, jreg);
+          for (j = jS; j <= jN; j++) F(u, iW - 1, j) = F(u, iW, j);
+          for (j = jS + 1; j <= jN; j++) F(v, iW, j) = -F(v, iW + 1, j);
+          break;
+        case BM_OUTLT2:
+          for (j = jS; j <= jN; j++) {
+            if (j < 1) die("SmlSclBC: west outlet reads row j-1 outside the array", ireg, jreg);
+            F(u, iW, j) = F(u, iW + 1, j) - F(v, iW, j) + F(v, iW, j - 1);
+          }
+          for (j = jS + 1; j <= jN; j++)
+            F(v, iW, j) = -F(v, iW, j - 1) + 5.0 * (F(v, iW + 1, j) - F(v, iW + 1, j - 1)) +
+                          8.0 * (F(u, iW + 1, j) - F(u, iW, j));
+          break;
+        default: die("Wrong nBdTypeW flag", ireg, jreg);
+      }
+      switch (MBTP(r, ireg, jreg, EAST)) {
+        case BM_INTERN: break;
+        case BM_WALL1: case BM_INLET:
+          for (j = jS; j <= jN; j++) F(u, iE, j) = 0.0;
+          for (j = jS + 1; j <= jN; j++) F(v, iE + 1, j) = -F(v, iE, j);
+          break;
+        case BM_WALL2:
+          for (j = jS; j <= jN; j++) F(u, iE, j) = 0.0;
+          for (j = jS + 1; j <= jN; j++) F(v, iE + 1, j) = F(v, iE, j);
+          break;
+        case BM_OUTLT1: /* the u row assigns u(iE+1,j) to itself */
+          for (j = jS + 1; j <= jN; j++) F(v, iE + 1, j) = -F(v, iE, j);
+          break;
+        case BM_OUTLT2:
+          for (j = jS + 1; j <= jN; j++) F(u, iE, j) = F(u, iE - 1, j) - (F(v, iE, j) - F(v, iE, j - 1));
+          for (j = jS + 1; j <= jN - 1; j++)
+            F(v, iE + 1, j) = F(v, iE + 1, j - 1) + 3.0 * (F(v, iE, j - 1) - F(v, iE, j)) -
+                              4.0 * (F(u, iE, j) - F(u, iE - 1, j));
+          break;
+        default: die("Wrong nBdTypeE flag", ireg, jreg);
+      }
+      switch (MBTP(r, ireg, jreg, SOUTH)) {
+        case BM_INTERN: break;
+        case BM_WALL1: case BM_INLET:
+          for (i = iW + 1; i <= iE; i++) F(u, i, jS) = -F(u, i, jS + 1);
+          for (i = iW; i <= iE; i++) F(v, i, jS) = 0.0;
+          break;
+        case BM_WALL2:
+          for (i = iW + 1; i <= iE; i++) F(u, i, jS) = F(u, i, jS + 1);
+          for (i = iW; i <= iE; i++) F(v, i, jS) = 0.0;
+          break;
+        case BM_OUTLT1:
+          if (jS < 1) die("SmlSclBC: south outlet writes row jS-1 outside the array", ireg, jreg);
+          for (i = iW + 1; i <= iE; i++) F(u, i, jS) = -F(u, i, jS + 1);
+          for (i = iW; i <= iE; i++) F(v, i, jS - 1) = F(v, i, jS);
+          break;
+        case BM_OUTLT2:
+          if (jS < 1 || iW < 1) die("SmlSclBC: south outlet reaches outside the array", ireg, jreg);
+          for (i = iW + 1; i <= iE; i++)
+            F(u, i, jS - 1) = F(u, i - 1, jS - 1) + 5.0 * (F(u, i, jS) - F(u, i - 1, jS)) +
+                              8.0 * (F(v, i, jS) - F(v, i - 1, jS - 1));
+          for (i = iW; i <= iE; i++) F(v, i, jS - 1) = F(v, i, jS) - F(u, i, jS) - F(u, i - 1, jS);
+          break;
+        default: die("Wrong nBdTypeS flag", ireg, jreg);
+      }
+      switch (MBTP(r, ireg, jreg, NORTH)) {
+        case BM_INTERN: break;
+        case BM_WALL1: case BM_INLET:
+          for (i = iW + 1; i <= iE; i++) F(u, i, jN + 1) = -F(u, i, jN);
+          for (i = iW; i <= iE; i++) F(v, i, jN) = 0.0;
+          break;
+        case BM_WALL2:
+          for (i = iW + 1; i <= iE; i++) F(u, i, jN + 1) = F(u, i, jN);
+          for (i = iW; i <= iE; i++) F(v, i, jN) = 0.0;
+          break;
+        case BM_OUTLT1:
+          for (i = iW + 1; i <= iE; i++) F(u, i, jN + 1) = -F(u, i, jN);
+          for (i = iW; i <= iE; i++) F(v, i, jN + 1) = F(v, i, jN);
+          break;
+        case BM_OUTLT2:
+          if (iW < 1) die("SmlSclBC: north outlet reads column iW-1 outside the array", ireg, jreg);
+          for (i = iW; i <= iE; i++) F(v, i, jN) = F(v, i, jN - 1) - (F(u, i, jN) - F(u, i - 1, jN));
+          for (i = iW + 1; i <= iE - 1; i++)
+            F(u, i, jN + 1) = F(u, i - 1, jN + 1) + 3.0 * (F(u, i - 1, jN) - F(u, i, jN)) -
+                              4.0 * (F(v, i, jN) - F(v, i, jN - 1));
+          break;
+        default: die("Wrong nBdTypeN flag", ireg, jreg);
+      }
+    }
+  /* the pressure takes the large-scale pressure conditions */
+  w2o_pres_bound_cond(c, nx, ny, r, p);
+  /* small-scale temperature: homogeneous image conditions */
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      const int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      const int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      int i, j;
+      if (TRT(th, r, ireg, jreg) == RT_TEMPER) {
+        for (j = jS + 1; j <= jN; j++)
+          for (i = iW + 1; i <= iE; i++) F(t, i, j) = 0.0;
+        for (j = jS + 1; j <= jN; j++) F(t, iW + 1, j) = -F(t, iW, j);
+        for (j = jS + 1; j <= jN; j++) F(t, iE, j) = -F(t, iE + 1, j);
+        for (i = iW + 1; i <= iE; i++) F(t, i, jS + 1) = -F(t, i, jS);
+        for (i = iW + 1; i <= iE; i++) F(t, i, jN) = -F(t, i, jN + 1);
+        continue;
+      }
+      for (int face = WEST; face <= NORTH; face++) {
+        const int bt = TBT(th, r, ireg, jreg, face);
+        if (bt == BT_INTERN) continue;
+        if (bt != BT_TEMPER && bt != BT_HTFLUX) die("Wrong nTemBdTp flag", ireg, jreg);
+        const double sg = bt == BT_TEMPER ? -1.0 : 1.0;
+        if (face == WEST)
+          for (j = jS + 1; j <= jN; j++) F(t, iW, j) = sg * F(t, iW + 1, j);
+        else if (face == EAST)
+          for (j = jS + 1; j <= jN; j++) F(t, iE + 1, j) = sg * F(t, iE, j);
+        else if (face == SOUTH)
+          for (i = iW + 1; i <= iE; i++) F(t, i, jS) = sg * F(t, i, jS + 1);
+        else
+          for (i = iW + 1; i <= iE; i++) F(t, i, jN + 1) = sg * F(t, i, jN);
+      }
+    }
+}
+
+/* small_scale.f keeps every local between calls (a bare SAVE): the map
+ * iterates and the cell areas carry information from call to call, and the
+ * work arrays keep whatever their never-written borders hold (zero). */
+struct w2o_atd {
+  size_t nf;
+  double *umap, *vmap, *tmap;  /* (0:mnx,0:mny,3) */
+  double *area, tarea;
+  double *xz, *xe, *yz, *ye, *rj, *ul, *vl, *tl, *uc, *vc, *uf, *vf, *tf;
+};
+
+w2o_atd *w2o_atd_create(int mnx, int mny) {
+  w2o_atd *s = (w2o_atd *)calloc(1, sizeof(w2o_atd));
+  s->nf = (size_t)(mnx + 1) * (size_t)(mny + 1);
+  double **arr[] = {&s->area, &s->xz, &s->xe, &s->yz, &s->ye, &s->rj, &s->ul, &s->vl,
+                    &s->tl, &s->uc, &s->vc, &s->uf, &s->vf, &s->tf};
+  for (size_t k = 0; k < sizeof(arr) / sizeof(arr[0]); k++) *arr[k] = (double *)calloc(s->nf, sizeof(double));
+  s->umap = (double *)calloc(3 * s->nf, sizeof(double));
+  s->vmap = (double *)calloc(3 * s->nf, sizeof(double));
+  s->tmap = (double *)calloc(3 * s->nf, sizeof(double));
+  return s;
+}
+
+void w2o_atd_destroy(w2o_atd *s) {
+  if (!s) return;
+  double *arr[] = {s->area, s->xz, s->xe, s->yz, s->ye, s->rj, s->ul, s->vl, s->tl,
+                   s->uc, s->vc, s->uf, s->vf, s->tf, s->umap, s->vmap, s->tmap};
+  for (size_t k = 0; k < sizeof(arr) / sizeof(arr[0]); k++) free(arr[k]);
+  free(s);
+}
+
+/* one step of the logistic map x <- r A x (1 - B |x|) of small_scale.f */
+static inline double atd_map(double rm, double x) {
+  const double A = 4.82842712474, B = 1.47839783948;
+  return rm * A * x * (1.0 - B * fabs(x));
+}
+
+int w2o_small_scale(w2o_ctx *c, w2o_atd *s, int nx, int ny, int initflg,
+                    const w2o_regions *r, const w2o_thermal *th,
+                    const w2o_atd_params *ap, const w2o_metrics *m,
+                    const double *u1, const double *v1, const double *t1,
+                    double *uss, double *vss, double *pss, double *tss) {
+  const double rc = 0.20710678119;
+  const double third = 1.0 / 3.0, sixth = 1.0 / 6.0;
+  const double piosr2 = acos(-1.0) / sqrt(2.0);
+  const double hs = ap->dlref * ap->hscoef, dk = ap->dka * ap->dlref / ap->uref;
+  const double pr = ap->pe / ap->re, rnu = ap->uref * ap->dlref / ap->re, dkappa = rnu / pr;
+  const double dl = ap->dlref;
+  const size_t nf = s->nf;
+  if (initflg <= 0) {
+    /* seed the three maps per variable, sweeping j fastest */
+    double um = 0.92, vm = 0.31, tm = 0.50;
+    for (int i = 0; i <= nx + 1; i++)
+      for (int j = 0; j <= ny + 1; j++) {
+        for (int l = 0; l < 3; l++) {
+          um = atd_map(rc, um);
+          vm = atd_map(rc, vm);
+          tm = atd_map(rc, tm);
+          s->umap[IX(i, j) + l * nf] = um;
+          s->vmap[IX(i, j) + l * nf] = vm;
+          s->tmap[IX(i, j) + l * nf] = tm;
+        }
+        F(uss, i, j) = 0.0;
+        F(vss, i, j) = 0.0;
+        F(tss, i, j) = 0.0;
+      }
+    s->tarea = 0.0;
+    for (int i = 1; i <= nx; i++)
+      for (int j = 1; j <= ny; j++) {
+        F(s->area, i, j) = 1.0 / F(m->djc, i, j);
+        s->tarea = s->tarea + F(s->area, i, j);
+      }
+    if (initflg < 0) return 0;
+  }
+  /* dimensional metrics, cell-centred large-scale fields, contravariant
+   * velocity; the copies that will be low-pass filtered */
+  for (int i = 1; i <= nx; i++)
+    for (int j = 1; j <= ny; j++) {
+      F(s->xz, i, j) = dl * F(m->xzc, i, j);
+      F(s->xe, i, j) = dl * F(m->xec, i, j);
+      F(s->yz, i, j) = dl * F(m->yzc, i, j);
+      F(s->ye, i, j) = dl * F(m->yec, i, j);
+      F(s->rj, i, j) = F(m->djc, i, j) / (dl * dl);
+      F(s->vl, i, j) = ap->uref * (F(v1, i, j) + F(v1, i, j - 1)) * 0.5;
+      F(s->ul, i, j) = ap->uref * (F(u1, i, j) + F(u1, i - 1, j)) * 0.5;
+      F(s->tl, i, j) = (ap->tmax - ap->tref) * F(t1, i, j) + ap->tref;
+      F(s->uc, i, j) = F(s->ye, i, j) * F(s->ul, i, j) - F(s->xe, i, j) * F(s->vl, i, j);
+      F(s->vc, i, j) = F(s->xz, i, j) * F(s->vl, i, j) - F(s->yz, i, j) * F(s->ul, i, j);
+      F(s->uf, i, j) = F(s->uc, i, j);
+      F(s->vf, i, j) = F(s->vc, i, j);
+      F(s->tf, i, j) = F(s->tl, i, j);
+    }
+  w2o_temp_bound_cond(c, nx, ny, r, th, s->tf);
+  w2o_filter(c, nx, ny, VU, r, ap->fp[0], s->uf);
+  w2o_filter(c, nx, ny, VV, r, ap->fp[1], s->vf);
+  w2o_filter_t(c, nx, ny, r, th, ap->fp[3], s->tf);
+  /* high-pass parts: field minus its Shuman-filtered copy */
+  for (int i = 1; i <= nx; i++)
+    for (int j = 1; j <= ny; j++) {
+      F(s->uf, i, j) = F(s->uc, i, j) - F(s->uf, i, j);
+      F(s->vf, i, j) = F(s->vc, i, j) - F(s->vf, i, j);
+      F(s->tf, i, j) = F(s->tl, i, j) - F(s->tf, i, j);
+    }
+#define CD_I(a) ((F(a, i + 1, j) - F(a, i - 1, j)) * 0.5)
+#define CD_J(a) ((F(a, i, j + 1) - F(a, i, j - 1)) * 0.5)
+  for (int jreg = 1; jreg <= r->nReg[1]; jreg++)
+    for (int ireg = 1; ireg <= r->nReg[0]; ireg++) {
+      const int iW = RBRD(r, ireg, jreg, WEST), iE = RBRD(r, ireg, jreg, EAST);
+      const int jS = RBRD(r, ireg, jreg, SOUTH), jN = RBRD(r, ireg, jreg, NORTH);
+      if (RTYP(r, ireg, jreg) == RM_BLOCKG || TRT(th, r, ireg, jreg) == RT_TEMPER) continue;
+      for (int i = iW + 1; i <= iE; i++)
+        for (int j = jS + 1; j <= jN; j++) {
+          const double xz = F(s->xz, i, j), xe = F(s->xe, i, j), yz = F(s->yz, i, j);
+          const double ye = F(s->ye, i, j), rj = F(s->rj, i, j);
+          const double hxy = sqrt(xz * xz + yz * yz + xe * xe + ye * ye);
+          /* |grad u| and |grad T| of the unfiltered large scales (physical
+           * derivatives through the inverse Jacobian) */
+          double uz = CD_I(s->ul), ue = CD_J(s->ul), vz = CD_I(s->vl), ve = CD_J(s->vl);
+          double q1 = rj * (ye * uz - yz * ue), q2 = rj * (xz * ue - xe * uz);
+          double q3 = rj * (ye * vz - yz * ve), q4 = rj * (xz * ve - xe * vz);
+          const double delu2n = sqrt(q1 * q1 + q2 * q2 + q3 * q3 + q4 * q4);
+          double tz = CD_I(s->tl), te = CD_J(s->tl);
+          q1 = rj * (ye * tz - yz * te);
+          q2 = rj * (xz * te - xe * tz);
+          const double delt2n = sqrt(q1 * q1 + q2 * q2);
+          const double reh = delu2n * (hxy * hxy) / rnu, peh = pr * reh;
+          if (!(peh > 3.0)) continue;
+          const double cuU = ap->cu0 * ap->temcoef, cuV = ap->cu0, cuT = ap->cu0;
+          int nmap = 0;
+          if (ap->cu0 > (double)1.0e-10f) {
+            const double ts = ap->tscoef * piosr2 * pow(reh, third) / (ap->cu0 * delu2n);
+            nmap = (int)(1.0 + dk / ts);
+          }
+          if (nmap > 50) nmap = 50;
+          const double bnum = sqrt(15.0) * pow((hs * hs) * delu2n / rnu, sixth);
+          const double rmap = ap->rmax * tanh(pow(bnum / ap->bnumc, ap->rlc) * atanh(rc / ap->rmax));
+          /* anisotropy: gradients of the high-pass parts */
+          uz = CD_I(s->uf); ue = CD_J(s->uf);
+          vz = CD_I(s->vf); ve = CD_J(s->vf);
+          tz = CD_I(s->tf); te = CD_J(s->tf);
+          const double gu1 = rj * (ye * uz - yz * ue), gu2 = rj * (xz * ue - xe * uz);
+          const double gv1 = rj * (ye * vz - yz * ve), gv2 = rj * (xz * ve - xe * vz);
+          const double gt1 = rj * (ye * tz - yz * te), gt2 = rj * (xz * te - xe * tz);
+          const double gu = sqrt(gu1 * gu1 + gu2 * gu2), gv = sqrt(gv1 * gv1 + gv2 * gv2);
+          const double gt = sqrt(gt1 * gt1 + gt2 * gt2);
+          const double grd = sqrt(gu * gu + gv * gv + gt * gt);
+          const double s1 = gu / grd, s2 = gv / grd;
+          const double a1 = xz * s1 + xe * s2, a2 = yz * s1 + ye * s2;
+          const double rnrmjs = sqrt(a1 * a1 + a2 * a2);
+          const double zeta1 = sqrt(2.0) * s1 / rnrmjs, zeta2 = sqrt(2.0) * s2 / rnrmjs;
+          double alf11 = 0.0, alf12 = 0.0, alf21 = 0.0, alf22 = 0.0;
+          double alf31 = 0.0, alf32 = 0.0, alf33 = 0.0;
+          if (fabs(gu) > 0.0) { alf11 = gu1 / gu; alf12 = gu2 / gu; }
+          if (fabs(gv) > 0.0) { alf21 = gv1 / gv; alf22 = gv2 / gv; }
+          if (fabs(gt) > 0.0) {
+            alf31 = gu1 / gt;
+            alf32 = gu2 / gt;
+            alf33 = sqrt(gt1 * gt1 + gt2 * gt2) / gt;
+          }
+          /* advance the nine chaotic maps nmap times and keep them */
+          double mp[9];
+          for (int l = 0; l < 3; l++) {
+            mp[l] = s->umap[IX(i, j) + l * nf];
+            mp[3 + l] = s->vmap[IX(i, j) + l * nf];
+            mp[6 + l] = s->tmap[IX(i, j) + l * nf];
+          }
+          for (int k = 0; k < nmap; k++)
+            for (int l = 0; l < 9; l++) mp[l] = atd_map(rmap, mp[l]);
+          for (int l = 0; l < 3; l++) {
+            s->umap[IX(i, j) + l * nf] = mp[l];
+            s->vmap[IX(i, j) + l * nf] = mp[3 + l];
+            s->tmap[IX(i, j) + l * nf] = mp[6 + l];
+          }
+          /* both velocity combinations draw on the u maps */
+          const double um = alf11 * mp[0] + alf12 * mp[1];
+          const double vm = alf21 * mp[0] + alf22 * mp[1];
+          const double tm = alf31 * mp[6] + alf32 * mp[7] + alf33 * mp[8];
+          const double sq = sqrt(rnu * delu2n), r6 = pow(reh, sixth);
+          double av = cuV * r6 * sq;
+          double at = pow(3.0 * pow(cuT, 4.0) * peh / pr, sixth) * sqrt(dkappa);
+          at = at * delt2n / sqrt(delu2n) * ap->temcoef;
+          const double ascale = sqrt(F(s->area, i, j) / s->tarea);
+          const double h3 = pow(hxy, third);
+          (void)cuU; /* its amplitude is computed and not used */
+          av = av * ascale * h3;
+          at = at * ascale * h3;
+          /* the u component takes av, as the v component does */
+          const double uscon = av * zeta1 * um, vscon = av * zeta2 * vm;
+          double us = rj * (xz * uscon + ye * vscon) / ap->uref;
+          double vs = rj * (ye * vscon + yz * uscon) / ap->uref;
+          double tsv = (at * tm * 1.0) / (ap->tmax - ap->tref);
+          F(uss, i, j) = fabs(us) < 1.0e-14 ? 0.0 : us;
+          F(vss, i, j) = fabs(vs) < 1.0e-14 ? 0.0 : vs;
+          F(tss, i, j) = fabs(tsv) < 1.0e-14 ? 0.0 : tsv;
+        }
+    }
+#undef CD_I
+#undef CD_J
+  w2o_sml_scl_bc(c, nx, ny, r, th, uss, vss, pss, tss);
+  for (int j = 0; j <= ny; j++)
+    for (int i = 0; i <= nx; i++) F(pss, i, j) = 0.0;
+  w2o_sml_scl_bc(c, nx, ny, r, th, uss, vss, pss, tss);
+  const int nsor = w2o_ppe(c, nx, ny, r, ap->lcartes, ap->npsolver, ap->msorit, ap->dka,
+                           ap->sortol, ap->sorrel, m, uss, vss, pss);
+  w2o_sml_scl_bc(c, nx, ny, r, th, uss, vss, pss, tss);
+  w2o_project(c, nx, ny, r, ap->dka, m, pss, uss, vss);
+  return nsor;
+}

@@ -200,6 +200,38 @@ int w2o_step_thermal(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
                      const w2o_params *prm, const w2o_metrics *m, w2o_fields *f,
                      int *nQLiter, int *nSorConv, double dif[4]);
 
+/* Small-scale (ATD) model parameters: parse.f's ss* keywords (defaults
+ * parse.f:144-178), the reference scales, and main.f's dk passed as dka. */
+typedef struct {
+  int npsolver, msorit, lcartes;   /* nssPpeSlvr, mssSorIt, lCartesGrid   */
+  double dlref, uref, tref, tmax, dka, re, pe, sortol, sorrel;
+  double fp[4];                    /* ssFiltPar(_U_.._T_); fp[2] unused   */
+  double cu0, tscoef, hscoef, temcoef, bnumc, rmax, rlc;
+} w2o_atd_params;
+
+/* What small_scale.f keeps between calls (its SAVE): the three logistic-map
+ * iterates per cell for each of u, v, t, the cell areas and their sum, and
+ * the work arrays (whose unwritten borders stay zero). */
+typedef struct w2o_atd w2o_atd;
+w2o_atd *w2o_atd_create(int mnx, int mny);
+void w2o_atd_destroy(w2o_atd *s);
+
+/* bound_cond.f:1211-1500 (image-point conditions of the small scales;
+ * PresBoundCond for p).  A west or south outlet on the grid's edge, where
+ * the reference writes outside its arrays, stops with a message. */
+void w2o_sml_scl_bc(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                    const w2o_thermal *th, double *u, double *v, double *p,
+                    double *t);
+
+/* small_scale.f:31-578.  initflg <= 0 seeds the maps and the areas and
+ * zeroes uss, vss, tss (initflg < 0 stops there); u1, v1, t1 are the large
+ * scales.  Returns the small-scale Ppe's nSorConv (0 when initflg < 0). */
+int w2o_small_scale(w2o_ctx *c, w2o_atd *s, int nx, int ny, int initflg,
+                    const w2o_regions *r, const w2o_thermal *th,
+                    const w2o_atd_params *ap, const w2o_metrics *m,
+                    const double *u1, const double *v1, const double *t1,
+                    double *uss, double *vss, double *pss, double *tss);
+
 #ifdef __cplusplus
 }
 #endif

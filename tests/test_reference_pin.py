@@ -206,3 +206,101 @@ def test_curvilinear_multiregion_time_loop_bitwise(solver):
     assert [h[:2] for h in r.history] == [h[:2] for h in o.history]
     for k in "uvp":
         assert np.array_equal(r.f[k], o.f[k]), k
+
+
+def _atd_layout(name):
+    """(case, thermal tables, large-scale u, v, t) for the small-scale pin."""
+    import thermal_setup
+    if name == "blockage":
+        case = thermal_setup.blockage_case()
+        th = deck.Thermal.empty()
+        rng = np.random.default_rng(3)
+        o = O.Oracle(case.nx + 1, case.ny + 1)
+        u, v, p = deck.perturbation_ic(case, 5, amp=0.3)
+        t = np.asfortranarray(rng.uniform(0.0, 1.0, size=u.shape))
+        return case, th, u, v, t
+    case, th, f = thermal_setup.problem()
+    case.params.lcartes = 0
+    t = np.asfortranarray(0.5 + 0.4 * np.tanh(f["tn"]))
+    return case, th, np.asfortranarray(f["u"]), np.asfortranarray(f["v"]), t
+
+
+@pytest.mark.parametrize("layout,solver,cu0,dka,bnumc", [
+    ("curvilinear", "rb_sor", 5.0, 0.3, 5.0),
+    ("curvilinear", "sor", 0.8, 0.05, 8.0),
+    ("curvilinear", "rb_sor", 2.0, 0.1, 200.0),   # parse.f's bnumc: rmap ~ 1e-6
+    ("curvilinear", "rb_lsor", 0.0, 0.004, 200.0),   # parse.f's cu0 = 0: no maps
+    ("blockage", "rb_sor", 3.0, 0.2, 5.0),
+])
+def test_small_scale_bitwise(layout, solver, cu0, dka, bnumc):
+    """SmallScale (small_scale.f:31-578) with SmlSclBC, its Filters, Ppe and
+    Project: the initial call and three more, against the translated source;
+    the map iterates and cell areas carry over between calls in both.  A
+    small bnumc drives the maps into their chaotic range (rmap near rmax)."""
+    case, th, u, v, t = _atd_layout(layout)
+    f77ref.build(case.nx + 1, case.ny + 1)
+    r = refrun.RefRun(case, cold_start=False)
+    o = O.Oracle(case.nx + 1, case.ny + 1)
+    met = o.grid(case.nx, case.ny, case.x, case.y)
+    re, pe, npsolver = 1000.0, 700.0, deck.PPE_SOLVERS[solver]
+    ap = O.AtdParams.make(dka=dka, re=re, pe=pe, npsolver=npsolver, msorit=300,
+                          lcartes=case.params.lcartes, cu0=cu0, sortol=1e-9, sorrel=1.2,
+                          fp=(400.0, 300.0, 0.0, 200.0), bnumc=bnumc)
+    atd = O.SmallScale(o, case.nx, case.ny, case.regions, th, met, ap)
+    tb, m = r.tab, r.m
+    ref = {k: o.field() for k in ("uss", "vss", "pss", "tss")}
+    orc = {k: o.field() for k in ("uss", "vss", "pss", "tss")}
+    rng = np.random.default_rng(11)
+    for call in range(4):
+        r.R("smallscale", nx=case.nx, ny=case.ny, initflg=0 if call == 0 else 1, nthermen=1,
+            lcartesgrid=case.params.lcartes, nreg=tb["nreg"], nregbrd=tb["nregbrd"],
+            nregtype=tb["nregtype"], nmombdtp=tb["nmombdtp"], **{k: w for k, w in
+                                                                 _thermal_tables(th).items()
+                                                                 if k != "dhgstval"},
+            nppesolver=npsolver, msorit=300, dlref=1.0, uref=1.0, tref=300.0, tmax=330.0,
+            dka=dka, re=re, pe=pe, sortol=1e-9, sorrel=1.2,
+            fp=np.array([400.0, 300.0, 0.0, 200.0]), cu0=cu0, tscoef=1.0, hscoef=1.0,
+            temcoef=1.0, bnumc=bnumc, rmax=0.95, rlc=5.0, dbcval=tb["dbcval"],
+            **{k: m[k] for k in ("rau", "rbu", "rbv", "rgv", "dju", "djv", "djc", "xeu", "yeu",
+                                 "xzv", "yzv", "xzu", "yzu", "xev", "yev", "xec", "yec", "xzc",
+                                 "yzc")},
+            u1=u, v1=v, t1=t, **ref)
+        atd(0 if call == 0 else 1, u, v, t, orc["uss"], orc["vss"], orc["pss"], orc["tss"])
+        for k in ref:
+            assert np.array_equal(ref[k], orc[k], equal_nan=True), (call, k)
+        # the next call sees slightly different large scales
+        u = np.asfortranarray(u + 0.02 * rng.standard_normal(u.shape))
+        v = np.asfortranarray(v + 0.02 * rng.standard_normal(v.shape))
+    if cu0 > 0 and bnumc < 10:
+        assert np.count_nonzero(orc["uss"]) > 0 and np.count_nonzero(orc["tss"]) > 0
+        assert np.abs(orc["tss"]).max() > 1e-6
+    elif cu0 == 0:
+        assert not orc["uss"].any() and not orc["tss"].any()
+
+
+@pytest.mark.parametrize("outlet", ["fd", "mc"])
+def test_sml_scl_bc_bitwise(outlet):
+    """SmlSclBC (bound_cond.f:1211-1500) on a channel with either outlet
+    type (BM_OUTLT1, BM_OUTLT2) and the heated cavity's temperature faces,
+    and on the thermal 3 x 2 layout (a fixed-temperature region)."""
+    import thermal_setup
+    rng = np.random.default_rng(7)
+    hc = deck.heated_cavity(8, 100.0, 0.01)
+    for case, th in ((deck.channel(30, 12, 200.0, 0.003, outlet=outlet), hc.thermal),
+                     thermal_setup.problem()[:2]):
+        f77ref.build(case.nx + 1, case.ny + 1)
+        r = refrun.RefRun(case, cold_start=False)
+        o = O.Oracle(case.nx + 1, case.ny + 1)
+        if case.regions.nReg[0] * case.regions.nReg[1] == 1:
+            th = deck.Thermal.empty()
+            th.nTemBdTp[0, 0, :] = hc.thermal.nTemBdTp[0, 0, :]
+        a = {k: np.asfortranarray(rng.standard_normal((case.nx + 2, case.ny + 2))) for k in "uvpt"}
+        b = {k: w.copy(order="F") for k, w in a.items()}
+        tb = r.tab
+        tt = _thermal_tables(th)
+        r.R("smlsclbc", nx=case.nx, ny=case.ny, nreg=tb["nreg"], nregbrd=tb["nregbrd"],
+            nregtype=tb["nregtype"], nmombdtp=tb["nmombdtp"], ntrgtype=tt["ntrgtype"],
+            ntembdtp=tt["ntembdtp"], dbcval=tb["dbcval"], u=a["u"], v=a["v"], p=a["p"], t=a["t"])
+        o.sml_scl_bc(case.nx, case.ny, case.regions, th, b["u"], b["v"], b["p"], b["t"])
+        for k in "uvpt":
+            assert np.array_equal(a[k], b[k]), k
