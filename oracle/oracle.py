@@ -141,6 +141,11 @@ def lib():
                                           C.POINTER(_Regions), C.POINTER(_Thermal),
                                           C.POINTER(AtdParams), C.POINTER(_Metrics)] + [_dp] * 7
             L.w2o_small_scale.restype = C.c_int
+            L.w2o_step_atd.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions),
+                                       C.POINTER(_Thermal), C.c_void_p, C.c_void_p,
+                                       C.POINTER(_Metrics), C.c_void_p, C.c_void_p,
+                                       C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double)]
+            L.w2o_step_atd.restype = C.c_int
             L.w2o_filter_t.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_Regions),
                                        C.POINTER(_Thermal), C.c_double, _dp]
             L.w2o_cold_start.restype = C.c_int
@@ -356,12 +361,39 @@ class OracleRun:
             self.cold_nconv = self.o.L.w2o_cold_start(self.o.h, self.nx, self.ny, C.byref(self._rs),
                                                       C.byref(self._ps), C.byref(self._ms),
                                                       C.byref(self._fs))
+        self.atd = None
+        a = getattr(case, "atd", None)
+        if a is not None:
+            # main.f:645-664: the small scales seeded after the cold start
+            from wolfd2_gb300.deck import Thermal
+            th = case.thermal if case.thermal is not None else Thermal.empty()
+            self._th_atd = Oracle.thermal_struct(th)
+            p = case.params
+            self._ap = AtdParams.make(dka=p.dk, re=p.re, pe=a.pe, npsolver=a.npsolver, msorit=a.msorit,
+                                      lcartes=p.lcartes, dlref=a.dlref, uref=a.uref, tref=a.tref,
+                                      tmax=a.tmax, sortol=a.sortol, sorrel=a.sorrel,
+                                      fp=(a.fpu, a.fpv, 0.0, a.fpt), cu0=a.cu0, tscoef=a.tscoef,
+                                      hscoef=a.hscoef, temcoef=a.temcoef, bnumc=a.bnumc,
+                                      rmax=a.rmax, rlc=a.rlc)
+            self.atd = SmallScale(self.o, self.nx, self.ny, case.regions, th, self.met, self._ap)
+            for k in ("uss", "vss", "pss", "tss", "usn", "vsn", "tsn"):
+                self.f[k] = self.o.field()
+            f = self.f
+            self.atd_nsor = [self.atd(0, f["u"], f["v"], f["t"], f["uss"], f["vss"], f["pss"], f["tss"])]
+            self._run = _AtdRun(self.atd.s, C.pointer(self._ap),
+                                *[_ptr(f[k]) for k in ("uss", "vss", "pss", "tss", "usn", "vsn", "tsn")])
 
     def step(self, n: int = 1):
         nql, nsor = C.c_int(), C.c_int()
         dif = (C.c_double * 4)()
         for _ in range(n):
-            if self._th is not None:
+            if self.atd is not None:
+                tp = C.byref(self._tp) if self._tp is not None else None
+                rc = self.o.L.w2o_step_atd(self.o.h, self.nx, self.ny, C.byref(self._rs),
+                                           C.byref(self._th_atd), tp, C.byref(self._ps),
+                                           C.byref(self._ms), C.byref(self._fs), C.byref(self._run),
+                                           C.byref(nql), C.byref(nsor), dif)
+            elif self._th is not None:
                 rc = self.o.L.w2o_step_thermal(self.o.h, self.nx, self.ny, C.byref(self._rs),
                                                C.byref(self._th), C.byref(self._tp), C.byref(self._ps),
                                                C.byref(self._ms), C.byref(self._fs), C.byref(nql),
@@ -380,6 +412,11 @@ def threads() -> int:
     """Host threads the oracle library runs on (1: the restatement is serial,
     like the reference)."""
     return 1
+
+
+class _AtdRun(C.Structure):
+    _fields_ = [("state", C.c_void_p), ("ap", C.POINTER(AtdParams))] + \
+        [(k, _dp) for k in ("uss", "vss", "pss", "tss", "usn", "vsn", "tsn")]
 
 
 class SmallScale:

@@ -55,6 +55,29 @@ class RefRun:
         self.cold_nconv = None
         if cold_start:
             self.cold_nconv = self._cold_start()
+        self.atd = getattr(case, "atd", None)
+        if self.atd is not None:
+            for k in ("uss", "vss", "pss", "tss", "usn", "vsn", "tsn"):
+                self.f[k] = z()
+            self.small_scale(0)   # main.f:645-664
+
+    def small_scale(self, initflg):
+        """SmallScale(initflg) on the fields u, v, t (main.f:645-664, 911-930)."""
+        a, p, tb, m, f = self.atd, self.case.params, self.tab, self.m, self.f
+        tt = self._ttab()
+        self.R("smallscale", nx=self.nx, ny=self.ny, initflg=initflg, nthermen=0,
+               lcartesgrid=p.lcartes, nreg=tb["nreg"], nregbrd=tb["nregbrd"], nregtype=tb["nregtype"],
+               ntrgtype=tt["ntrgtype"], nmombdtp=tb["nmombdtp"], ntembdtp=tt["ntembdtp"],
+               nppesolver=a.npsolver, msorit=a.msorit, dlref=a.dlref, uref=a.uref, tref=a.tref,
+               tmax=a.tmax, dka=p.dk, re=p.re, pe=a.pe, sortol=a.sortol, sorrel=a.sorrel,
+               fp=np.array([a.fpu, a.fpv, 0.0, a.fpt]), cu0=a.cu0, tscoef=a.tscoef,
+               hscoef=a.hscoef, temcoef=a.temcoef, bnumc=a.bnumc, rmax=a.rmax, rlc=a.rlc,
+               dtrgval=tt["dtrgval"], dbcval=tb["dbcval"],
+               **{k: m[k] for k in ("rau", "rbu", "rbv", "rgv", "dju", "djv", "djc", "xeu", "yeu",
+                                    "xzv", "yzv", "xzu", "yzu", "xev", "yev", "xec", "yec", "xzc",
+                                    "yzc")},
+               u1=f["u"], v1=f["v"], t1=f["t"], uss=f["uss"], vss=f["vss"], pss=f["pss"],
+               tss=f["tss"])
 
     # -- wrappers with the reference's argument names --------------------
     def vel_bc(self, u, v):
@@ -114,6 +137,9 @@ class RefRun:
     # -- thermal (case.thermal: deck.Thermal, case.tparams: deck.ThermalParams)
     def _ttab(self):
         th = self.case.thermal
+        if th is None:
+            from wolfd2_gb300.deck import Thermal
+            th = Thermal.empty()
         return dict(ntrgtype=np.asfortranarray(th.nTRgType, np.int32),
                     ntembdtp=np.asfortranarray(th.nTemBdTp, np.int32),
                     dtrgval=np.asfortranarray(th.dTRgVal, np.float64))
@@ -150,6 +176,11 @@ class RefRun:
         for _ in range(n):
             for a, b in (("pn", "p"), ("un", "u"), ("vn", "v"), ("tn", "t"), ("dn", "d")):
                 f[a][...] = f[b]
+            if self.atd is not None:   # main.f:708-730
+                for a, b in (("usn", "uss"), ("vsn", "vss"), ("tsn", "tss")):
+                    f[a][...] = f[b]
+                for a, b in (("un", "uss"), ("vn", "vss"), ("tn", "tss")):
+                    f[a][...] = f[a] + f[b]
             for l in range(1, nme + 1):
                 for a, b in (("us", "u"), ("vs", "v"), ("ts", "t")):
                     f[a][...] = f[b]
@@ -178,6 +209,12 @@ class RefRun:
                 self.R("filter", nx=self.nx, ny=self.ny, ncomp=4, nreg=tb["nreg"], nregbrd=tb["nregbrd"],
                        nregtype=tb["nregtype"], nmombdtp=tb["nmombdtp"],
                        ntrgtype=self._ttab()["ntrgtype"], fp=tp.fpt, qu=f["t"])
+            if self.atd is not None:   # main.f:898-940
+                for a, b in (("u", "usn"), ("v", "vsn"), ("t", "tsn")):
+                    f[a][...] = f[a] - f[b]
+                self.small_scale(1)
+                for a, b in (("u", "uss"), ("v", "vss"), ("t", "tss")):
+                    f[a][...] = f[a] + f[b]
             self.vel_bc(f["u"], f["v"])
             self.pres_bc(f["p"])
             if therm:

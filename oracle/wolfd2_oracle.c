@@ -1168,6 +1168,13 @@ int w2o_step_thermal(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
                      const w2o_thermal *th, const w2o_thermal_params *tp,
                      const w2o_params *prm, const w2o_metrics *m, w2o_fields *f,
                      int *nQLiter, int *nSorConv, double dif[4]) {
+  return w2o_step_atd(c, nx, ny, r, th, tp, prm, m, f, NULL, nQLiter, nSorConv, dif);
+}
+
+int w2o_step_atd(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                 const w2o_thermal *th, const w2o_thermal_params *tp,
+                 const w2o_params *prm, const w2o_metrics *m, w2o_fields *f,
+                 const w2o_atd_run *a, int *nQLiter, int *nSorConv, double dif[4]) {
   int i, j;
   const int therm = th && tp && tp->nthermen == 1;
   const int eqs = th && tp && tp->neqstate == 1;
@@ -1182,6 +1189,16 @@ int w2o_step_thermal(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
       F(f->tn, i, j) = F(f->t, i, j);
       F(f->dn, i, j) = F(f->d, i, j);
     }
+  if (a) /* main.f:708-730: keep the small scales of level n, add them to it */
+    for (j = 0; j <= ny + 1; j++)
+      for (i = 0; i <= nx + 1; i++) {
+        F(a->usn, i, j) = F(a->uss, i, j);
+        F(a->vsn, i, j) = F(a->vss, i, j);
+        F(a->tsn, i, j) = F(a->tss, i, j);
+        F(f->un, i, j) = F(f->un, i, j) + F(a->uss, i, j);
+        F(f->vn, i, j) = F(f->vn, i, j) + F(a->vss, i, j);
+        F(f->tn, i, j) = F(f->tn, i, j) + F(a->tss, i, j);
+      }
   for (int l = 1; l <= nme; l++) {
     for (j = 0; j <= ny + 1; j++)
       for (i = 0; i <= nx + 1; i++) {
@@ -1224,6 +1241,22 @@ int w2o_step_thermal(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
     if (l > 1 && mx < tp->dmeittol) break;
   }
   if (therm && tp->nfiltt == 1) w2o_filter_t(c, nx, ny, r, th, tp->fpt, f->t);
+  if (a) { /* main.f:898-940: small scales of level n+1 from the large scales */
+    for (j = 0; j <= ny + 1; j++)
+      for (i = 0; i <= nx + 1; i++) {
+        F(f->u, i, j) = F(f->u, i, j) - F(a->usn, i, j);
+        F(f->v, i, j) = F(f->v, i, j) - F(a->vsn, i, j);
+        F(f->t, i, j) = F(f->t, i, j) - F(a->tsn, i, j);
+      }
+    w2o_small_scale(c, a->state, nx, ny, 1, r, th, a->ap, m, f->u, f->v, f->t, a->uss,
+                    a->vss, a->pss, a->tss);
+    for (j = 0; j <= ny + 1; j++)
+      for (i = 0; i <= nx + 1; i++) {
+        F(f->u, i, j) = F(f->u, i, j) + F(a->uss, i, j);
+        F(f->v, i, j) = F(f->v, i, j) + F(a->vss, i, j);
+        F(f->t, i, j) = F(f->t, i, j) + F(a->tss, i, j);
+      }
+  }
   w2o_vel_bound_cond(c, nx, ny, r, f->u, f->v);
   w2o_pres_bound_cond(c, nx, ny, r, f->p);
   if (therm) w2o_temp_bound_cond(c, nx, ny, r, th, f->t);

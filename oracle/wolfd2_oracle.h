@@ -232,6 +232,25 @@ int w2o_small_scale(w2o_ctx *c, w2o_atd *s, int nx, int ny, int initflg,
                     const double *u1, const double *v1, const double *t1,
                     double *uss, double *vss, double *pss, double *tss);
 
+/* The small scales carried by the time loop (main.f's nsmallscl = 1): the
+ * model's saved state and parameters, uss, vss, pss, tss and their level-n
+ * copies usn, vsn, tsn, each (0:mnx,0:mny).  Seed them after the cold start
+ * with w2o_small_scale(initflg 0) on u, v, t. */
+typedef struct {
+  w2o_atd *state;
+  const w2o_atd_params *ap;
+  double *uss, *vss, *pss, *tss, *usn, *vsn, *tsn;
+} w2o_atd_run;
+
+/* w2o_step_thermal with the small scales (main.f:708-730, 898-940): added to
+ * the level-n fields before the iterations, removed from the new fields and
+ * recomputed by SmallScale after them, then added back; a NULL run is
+ * w2o_step_thermal.  The thermal tables th are required with a run. */
+int w2o_step_atd(w2o_ctx *c, int nx, int ny, const w2o_regions *r,
+                 const w2o_thermal *th, const w2o_thermal_params *tp,
+                 const w2o_params *prm, const w2o_metrics *m, w2o_fields *f,
+                 const w2o_atd_run *a, int *nQLiter, int *nSorConv, double dif[4]);
+
 #ifdef __cplusplus
 }
 #endif

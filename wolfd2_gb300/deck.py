@@ -491,6 +491,35 @@ class Thermal:
 
 
 @dataclasses.dataclass
+class SmallScaleParams:
+    """Switch and constants of the small-scale (ATD) model, SmallScale
+    (src/small_scale.f:31-578), with ReadParam's defaults (src/parse.f:
+    144-178): its own Ppe solver and sweep limit, the chaotic-map constants
+    and the Shuman filter parameters of u, v and t.  SmallScale also reads
+    dlref, uref, tref, tmax and pe (pe / re is its Prandtl number); it
+    always takes the thermal tables of the case (TempBoundCond, Filter of t)."""
+    npsolver: int = 1           # nssPpeSlvr
+    msorit: int = 2000          # mssSorIt
+    sortol: float = 1.0e-8      # ssSorTol
+    sorrel: float = 1.0         # ssSorRel
+    cu0: float = 0.0            # ssCu0
+    tscoef: float = 1.0         # ssTsCoef
+    hscoef: float = 1.0         # ssHsCoef
+    temcoef: float = 1.0        # ssTemCoef
+    bnumc: float = 200.0        # ssBnCrit
+    rmax: float = 0.95          # ssRMpMax
+    rlc: float = 5.0            # ssRMpExp
+    fpu: float = 500.0          # ssFiltPar(_U_)
+    fpv: float = 500.0          # ssFiltPar(_V_)
+    fpt: float = 500.0          # ssFiltPar(_T_)
+    dlref: float = 1.0
+    uref: float = 1.0
+    tref: float = 300.0
+    tmax: float = 330.0
+    pe: float = 0.0             # re * Prandtl
+
+
+@dataclasses.dataclass
 class ThermalParams:
     """Thermal switches and constants of the time loop: ReadParam's
     nthermen, neqstate, nmeiter, dmeittol (defaults src/parse.f:118-159),
@@ -522,6 +551,7 @@ class Case:
     bc_text: str = ""
     thermal: Optional[Thermal] = None        # thermal tables (nthermen = 1)
     tparams: Optional[ThermalParams] = None
+    atd: Optional[SmallScaleParams] = None   # nsmallscl = 1 (needs the thermal tables)
 
     @property
     def cells(self) -> int:
