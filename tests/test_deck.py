@@ -177,3 +177,27 @@ def test_read_deck_thermal_and_fluid_interpolation(tmp_path):
     assert r.regions.dBCVal[0, 0, deck.WEST - 1, deck.VAR_T - 1] == pytest.approx(0.5)
     assert r.thermal.dHGSTval[0, 0] == pytest.approx(5.0 * 4.0 / (tp.pe * k * 100.0), rel=1e-12)
     assert r.x.max() == pytest.approx(c.x.max() / 2.0)
+
+
+def test_read_deck_small_scale_keywords(tmp_path):
+    """small_scale and the atd_* keywords (src/parse.f:342-344, 491-620)
+    become the case's SmallScale parameters; unset ones keep parse.f's
+    defaults, and the case carries thermal tables for the model."""
+    c = deck.cavity(8, 100.0, 0.01)
+    deck.write_grid_plot3d(str(tmp_path / "grid.xyz"), c.x, c.y)
+    (tmp_path / "fluid.dat").write_text(
+        "fluid air01 gasconstant 287.0\n280 1.2 1000 0.010 0.025 0.70\n320 1.0 1000 0.012 0.027 0.72\nend\n")
+    (tmp_path / "input.dat").write_text(
+        "section input_parameters\n grid_file grid.xyz cartesian_grid\n small_scale\n"
+        " time_step_size 0.01\n ref_temperature 300\n fluid_prop_file fluid.dat\n"
+        " atd_cu0 0.7\n atd_bnumcrit 12.5\n atd_rmapmax 0.9\n atd_ppe_solver rb_lsor\n"
+        " atd_max_sor_iter 500\n atd_sor_tolerance 1d-9\n atd_filter_t 250\nend section\n\n"
+        "section boundary_conditions\n number_of_regions 1 1\n i_borders\n j_borders\n"
+        " wall 1 1 north tv 1.0\nend section\n")
+    r = deck.read_deck(str(tmp_path / "input.dat"))
+    a = r.atd
+    assert (a.cu0, a.bnumc, a.rmax, a.msorit, a.sortol, a.fpt) == (0.7, 12.5, 0.9, 500, 1e-9, 250.0)
+    assert a.npsolver == deck.PPE_SOLVERS["rb_lsor"]
+    assert (a.tscoef, a.hscoef, a.temcoef, a.rlc, a.fpu, a.sorrel) == (1.0, 1.0, 1.0, 5.0, 500.0, 1.0)
+    assert a.pe == pytest.approx(r.params.re * 0.71, rel=1e-12) and a.tref == 300.0
+    assert r.thermal is not None and r.tparams is None

@@ -1094,4 +1094,32 @@ def read_deck(path: str, base: Optional[str] = None) -> Case:
                                      dmeittol=d.dmeittol, pe=pe, uref=d.uref, densref=fl["densref"],
                                      tmax=d.tmax, tref=fl["tref"], rconst=fl["rconst"], nfiltt=d.nfiltt,
                                      fpt=d.fpt)
+    if "small_scale" in d.other:
+        case.thermal = case.thermal if case.thermal is not None else regs.thermal
+        case.atd = small_scale_params(d, pe=re * fl["prandtl"], tref=fl["tref"])
     return case
+
+
+_ATD_REAL = {"atd_cu0": "cu0", "atd_tscf": "tscoef", "atd_hscf": "hscoef", "atd_bnumcrit": "bnumc",
+             "atd_rmapmax": "rmax", "atd_rmapexp": "rlc", "atd_temcf": "temcoef",
+             "atd_sor_tolerance": "sortol", "atd_sor_relaxation": "sorrel", "atd_filter_u": "fpu",
+             "atd_filter_v": "fpv", "atd_filter_t": "fpt"}
+
+
+def small_scale_params(d: DeckInput, pe: float, tref: float) -> SmallScaleParams:
+    """SmallScale's parameters from the atd_* keywords of a deck (src/parse.f:
+    491-620, defaults 144-178) and the deck's reference scales."""
+    a = SmallScaleParams(dlref=d.dlref, uref=d.uref, tref=tref, tmax=d.tmax, pe=pe)
+    for key, w in d.other.items():
+        try:
+            if key in _ATD_REAL:
+                setattr(a, _ATD_REAL[key], float(w[0].replace("d", "e").replace("D", "e")))
+            elif key == "atd_max_sor_iter":
+                a.msorit = int(w[0])
+            elif key == "atd_ppe_solver":
+                if w[0].lower() not in PPE_SOLVERS:
+                    raise DeckError(f"Unrecognized atd_ppe_solver: [{w[0]}]")
+                a.npsolver = PPE_SOLVERS[w[0].lower()]
+        except (IndexError, ValueError) as exc:
+            raise DeckError(f"{key}: bad value {' '.join(w)!r}") from exc
+    return a
