@@ -4,21 +4,28 @@
 Workload (one "step" = one pass of main.f:690-972, the whole time step):
 lid-driven cavity, 1024 x 1024 uniform cells, Re = 1000, seeded divergence-
 free perturbation (16 x 16 streamfunction modes, N(0, 1e-3) amplitudes),
-red/black point SOR, plain FP64.  dt = 2.5e-4: at the named dt = 1e-3 the
-reference's own Newton-Kantorovich iteration diverges to NaN in the first
-step at this resolution (the mechanical translation of the reference source,
-the CPU oracle and the GPU path all agree on that), and at 5e-4 it drifts
-unstable within ten steps; dt = 2.5e-4 keeps the viscous number
-dt/(h^2 Re) of the stable 512x512 case and runs the reference algorithm
-cleanly (7-11 Q-L iterations and the full 2000 SOR sweeps per step).
+red/black point SOR with the Poisson solve converged: sor_relaxation at the
+model problem's optimum 2/(1 + sin(pi/1024)) (rounded to FP32, so both
+precisions relax by the same factor), sor_tolerance 1e-9, max_sor_iter
+20000 -- the reference's own keywords -- which brings the interior
+divergence (dk times the Poisson residual) below 1e-10 in both precisions.
+dt = 2.5e-4: at the named dt = 1e-3 the reference's own Newton-Kantorovich
+iteration diverges to NaN in the first step at this resolution (the
+mechanical translation of the reference source, the CPU oracle and the GPU
+path all agree on that), and at 5e-4 it drifts unstable within ten steps;
+dt = 2.5e-4 keeps the viscous number dt/(h^2 Re) of the stable 512x512 case.
+--ppe-defaults runs the reference's default Poisson settings instead
+(sorrel 1, sortol 1e-8, 2000 sweeps: unconverged at this size).
 
 Arms:
   --impl ours       the CUDA library through its C-ABI (value: device-timed
                     with CUDA events on the library stream; e2e: host buffers
                     with the H2D/D2H copies inside the timed region)
-  --impl reference  the reference algorithm on the host cores (the CPU
-                    oracle's restatement; no Fortran compiler exists on the
-                    GPU machines to build the reference itself)
+  --impl reference  the reference algorithm on one host core: the
+                    mechanical translation of the reference's Fortran source
+                    to C (no Fortran compiler exists on the GPU machines),
+                    full time steps of the same case, as many as fit a
+                    bounded time
 
 Multi-GPU: the single-case path does not shard (per-sweep halos, global
 max-norms and domain-long chains), so N GPUs run N independent replicas and
@@ -119,14 +126,34 @@ CHANNEL = {"ncx": 4096, "ncy": 1024, "re": 10000.0, "dt": 2.5e-4}
 THERMAL = {"nmeiter": 2, "dmeittol": 0.0, "pr": 0.71, "fr": 0.05}
 
 
+def optimal_relaxation(n):
+    """SOR's optimal relaxation for the n x n model Poisson problem,
+    2/(1 + sin(pi/n)), rounded to the nearest FP32 value so that the FP64
+    and FP32 sweeps relax by the same factor."""
+    return float(np.float32(2.0 / (1.0 + np.sin(np.pi / n))))
+
+
+def poisson_settings(args):
+    """(sorrel, sortol, msorit) of the run: converged by default for the
+    cavity workload, the reference's defaults (parse.f:136,160-161) with
+    --ppe-defaults or for the other workloads."""
+    if args.workload == "cavity" and not args.ppe_defaults:
+        sorrel = args.sorrel or optimal_relaxation(args.n)
+        return sorrel, args.sortol or 1.0e-9, args.msorit or 20000
+    return args.sorrel or 1.0, args.sortol or 1.0e-8, args.msorit or 2000
+
+
 def make_case(args):
     if args.workload == "channel":
-        return deck.channel_inflow(CHANNEL["ncx"], CHANNEL["ncy"], CHANNEL["re"], CHANNEL["dt"],
+        case = deck.channel_inflow(CHANNEL["ncx"], CHANNEL["ncy"], CHANNEL["re"], CHANNEL["dt"],
                                    seed=args.seed, solver=args.solver)
-    if args.workload == "thermal":
-        return deck.heated_cavity(args.n, args.re, args.dt, solver=args.solver, pr=THERMAL["pr"],
+    elif args.workload == "thermal":
+        case = deck.heated_cavity(args.n, args.re, args.dt, solver=args.solver, pr=THERMAL["pr"],
                                   fr=THERMAL["fr"], nmeiter=THERMAL["nmeiter"], dmeittol=THERMAL["dmeittol"])
-    return deck.cavity(args.n, args.re, args.dt, solver=args.solver)
+    else:
+        case = deck.cavity(args.n, args.re, args.dt, solver=args.solver)
+    case.params.sorrel, case.params.sortol, case.params.msorit = poisson_settings(args)
+    return case
 
 
 def make_ic(args, case, rank=0):
@@ -187,14 +214,16 @@ def reference_runner(case, ic, t0=None):
         "C restatement of the reference (oracle), gcc -O2, 1 thread"
 
 
-def cpu_step_sample(case, ic, nsteps=1, t0=None):
+def cpu_step_sample(case, ic, nsteps=1, t0=None, with_run=False):
     """Time `nsteps` full reference steps on the host; returns
-    (cell-steps/s, seconds, threads, kind, how)."""
+    (cell-steps/s, seconds, threads, kind, how) and, with_run, the run
+    itself (its fields and per-step counts)."""
     r, kind, how = reference_runner(case, ic, t0)
     t0 = time.perf_counter()
     r.step(nsteps)
     dt = time.perf_counter() - t0
-    return case.cells * nsteps / dt, dt, 1, kind, how
+    out = (case.cells * nsteps / dt, dt, 1, kind, how)
+    return out + (r,) if with_run else out
 
 
 def run_reference_sampled(args):
@@ -247,21 +276,31 @@ def run_reference(args):
     case = make_case(args)
     ic = make_ic(args, case)
     r, kind, how = reference_runner(case, ic, make_t0(case) if args.workload == "thermal" else None)
-    r.step(args.warmup)
+    # a bounded sample: whole time steps from the initial state until the
+    # step budget (--steps) or the time budget is used up; the host run
+    # needs no warm-up
+    budget = args.ref_seconds
     t0 = time.perf_counter()
-    r.step(args.steps)
+    steps = 0
+    while steps < max(1, args.steps):
+        r.step(1)
+        steps += 1
+        if time.perf_counter() - t0 > budget:
+            break
     dt = time.perf_counter() - t0
-    value = case.cells * args.steps / dt
+    value = case.cells * steps / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+        "n_gpus": args.gpus, "steps": steps, "warmup": 0,
+        "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": config_of(args, case, args.refine_sweeps or 128),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": kind,
-                         "sample": f"{args.warmup} + {args.steps} full time steps of the same case; {how}"},
+                         "sample": f"the first {steps} full time steps of the same case from the same "
+                                   f"initial state ({dt:.1f} s, a budget of {budget:g} s or --steps "
+                                   f"{args.steps}); {how}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "iterations": [[h[0], h[1]] for h in r.history[-args.steps:]],
+        "iterations": [[h[0], h[1]] for h in r.history[-steps:]],
     }
     print(json.dumps(line), flush=True)
 
@@ -287,13 +326,19 @@ def config_of(args, case, inner=None):
                 f"no-slip walls, ppe_solver {args.solver}, {prec}")
         re, dt = CHANNEL["re"], CHANNEL["dt"]
     else:
+        prm = case.params
+        conv = ("" if args.ppe_defaults else
+                f" (the Poisson solve converged: interior divergence <= 1e-10 in both precisions)")
         work = (f"lid-driven cavity {args.n}x{args.n} cells, Re={args.re:g}, "
                 f"dt={args.dt:g} (the named dt={DT_NAMED:g} drives the reference scheme to NaN at this size), "
                 f"seeded 16x16-mode streamfunction perturbation (seed {args.seed}), "
-                f"ppe_solver {args.solver}, {prec}")
+                f"ppe_solver {args.solver}, sor_relaxation {prm.sorrel!r}, sor_tolerance {prm.sortol:g}, "
+                f"max_sor_iter {prm.msorit}{conv}, {prec}")
         re, dt = args.re, args.dt
+    prm = case.params
     return {"workload": work, "cells": case.cells, "nx": case.nx, "ny": case.ny, "re": re, "dt": dt,
-            "ppe_solver": args.solver, "precision": args.precision,
+            "ppe_solver": args.solver, "sor_relaxation": prm.sorrel, "sor_tolerance": prm.sortol,
+            "max_sor_iter": prm.msorit, "precision": args.precision,
             "l2": "flushed between timed steps (256 MiB write); per-step working set > 2x L2"}
 
 
@@ -393,7 +438,10 @@ def kernel_name(kind, precision, tiled, thermal=False):
     return KERNEL_NAMES[kind]
 
 
-def roofline_of(arm, cells, precision, inner, tiled=True):
+FP64_PEAK_GOPS = 628.0
+
+
+def roofline_of(arm, cells, precision, inner, tiled=True, sorrel=1.0):
     """Roofline of the dominant kernel of one arm (HBM view) and the FP64
     pipe view of the plain red/black sweep."""
     from wolfd2_gb300.gpu import K_MOMENTUM, K_PPE
@@ -429,13 +477,21 @@ def roofline_of(arm, cells, precision, inner, tiled=True):
     fp64 = None
     if precision == "fp64" and prof[K_PPE][0] > 0:
         # unit-stencil red/black point: 4 subtractions, 1 multiply by -1/4,
-        # 1 subtraction and 1 addition per point and sweep
-        ops = sum(cells * n for n in nsor) * 7.0
+        # 1 subtraction, the product by sorrel (when it is not 1) and 1
+        # addition per point and sweep; the sweeps are the FP64 pipe's work
+        relax = sorrel != 1.0
+        per_point = 8.0 if relax else 7.0
+        ops = sum(cells * n for n in nsor) * per_point
         gops = ops / (prof[K_PPE][0] / 1e3) / 1e9
-        fp64 = {"kernel": kernel_name(K_PPE, precision, tiled), "op_per_point": "7 FP64 add/mul (unit stencil)",
-                "achieved_gops": gops, "peak_gops": 628.0,
-                "peak_kind": "measured DFMA probe on this pool's GB300 (2 DFMA/clk/SM)",
-                "frac": gops / 628.0}
+        fp64 = {"bound": "fp64", "kernel": kernel_name(K_PPE, precision, tiled),
+                "op_per_point": f"{per_point:g} FP64 add/mul (unit stencil{', relaxed' if relax else ''})",
+                "achieved_gops": gops, "peak_gops": FP64_PEAK_GOPS,
+                "peak_kind": "measured: FP64 fused multiply-add issue rate of the GB300 (2 per clock per SM "
+                             "at 2070 MHz on 152 SMs), a probe run on the same hardware",
+                "frac": gops / FP64_PEAK_GOPS,
+                "roof_note": "the plain sweep's FP64 work per point takes longer than its 24 bytes of "
+                             "traffic at the HBM rate, and its working set stays in L2: min(HBM, FP64) "
+                             "is this roof"}
     return roof, fp64
 
 
@@ -505,12 +561,12 @@ def run_ours(args):
     e2e_value = world * cells * head["e2e_steps"] / t_e2e_max
     # the plain path's red/black solve runs on shared-memory tiles at this size
     tiled = args.solver in ("rb_sor", "par_rb_sor") and cells >= 152 * 1024
-    roof, fp64 = roofline_of(head, cells, args.precision, inner, tiled)
+    roof, fp64 = roofline_of(head, cells, args.precision, inner, tiled, prm.sorrel)
     plain = None
     accuracy = None
     if args.precision == "mixed":
         a64 = arms["fp64"]
-        r64, f64 = roofline_of(a64, cells, "fp64", inner, tiled)
+        r64, f64 = roofline_of(a64, cells, "fp64", inner, tiled, prm.sorrel)
         plain = {"value": world * cells * args.steps / a64["t_dev"], "unit": UNIT,
                  "ms_per_step": 1e3 * a64["t_dev"] / args.steps,
                  "e2e": world * cells * a64["e2e_steps"] / a64["t_e2e"],
@@ -528,6 +584,8 @@ def run_ours(args):
         p_dyn = float(np.max(np.abs(fm[2] - fp[2]))) / pscale
         div_m = [h[3] for h in head["hist"]]
         div_p = [h[3] for h in a64["hist"]]
+        divi_m = max(h[4] for h in head["hist"])
+        divi_p = max(h[4] for h in a64["hist"])
         accuracy = {
             "against": "plain FP64 path after the same warm-up + timed steps from the same initial "
                        "state (bit-identical to the FP64 oracle: parity tests)",
@@ -535,17 +593,36 @@ def run_ours(args):
             "velocity_rel_maxnorm": vel_rel,
             "u_rel_maxnorm": errs["u"], "v_rel_maxnorm": errs["v"], "p_rel_maxnorm": errs["p"],
             "p_rel_dynamic": p_dyn,
+            "divmax_interior_mixed": divi_m, "divmax_interior_fp64": divi_p,
             "divmax_mixed": max(div_m), "divmax_fp64": max(div_p),
             "divmax_rel_diff": abs(max(div_m) - max(div_p)) / max(max(div_p), 1e-300),
+            "divergence_note": "interior: cells whose four neighbours are Poisson unknowns and whose "
+                               "faces Project sets, where the divergence is dk times the Poisson "
+                               "residual; divmax: all pressure cells, which adds at the boundary "
+                               "dk * coefficient * (change of the ghost pressure Ppe holds frozen "
+                               "during the solve) -- the reference scheme's, in both precisions",
             "velocity_within_1e-5": vel_rel <= 1e-5,
-            "div_le_1e-10": max(div_m) <= 1e-10,
+            "div_le_1e-10": divi_m <= 1e-10 and divi_p <= 1e-10,
         }
     cpu = None
+    parity = None
     if not args.no_cpu_baseline:
-        cv, csec, cores, kind, how = cpu_step_sample(case, (u0, v0, p0), 1, t0)
+        cv, csec, cores, kind, how, ref = cpu_step_sample(case, (u0, v0, p0), 1, t0, with_run=True)
         cpu = {"value": cv, "unit": UNIT, "cores": cores, "kind": kind,
                "sample": f"1 full time step of the same {case.nx - 1}x{case.ny - 1} case from the same initial "
                          f"state ({csec:.1f} s); {how}"}
+        if t0 is None:
+            # the same first step on the GPU's plain FP64 path, field for field
+            s.load_fields(u0, v0, p0)
+            h1 = s.step(prm, 1, precision=PREC_FP64)
+            g = s.store_fields()
+            parity = {"against": f"{how.split(',')[0]} ({kind}): 1 time step of this case from the same "
+                                 "initial state, plain FP64 path",
+                      "iterations_equal": [h1[0][0], h1[0][1]] == list(ref.history[0][:2]),
+                      "iterations": [h1[0][0], h1[0][1]]}
+            for nm, a in zip("uvp", g):
+                parity[nm] = rel_max(a, ref.f[nm])
+            parity["bitwise"] = all(np.array_equal(a, ref.f[nm]) for nm, a in zip("uvp", g))
     chain_rounds, chain_fallbacks = s.chain_stats()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -563,6 +640,7 @@ def run_ours(args):
         "plain_fp64": plain,
         "speedup_vs_plain_fp64": (value / plain["value"]) if plain else None,
         "accuracy": accuracy,
+        "parity": parity,
         "cpu_baseline": cpu,
         "clocks": head["clk"].summary(),
         "gpu_launches": head["launches"],
@@ -955,6 +1033,14 @@ def main():
     ap.add_argument("--solver", default="rb_sor", choices=sorted(deck.PPE_SOLVERS))
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--sorrel", type=float, default=0.0,
+                    help="sor_relaxation (0: the optimum 2/(1+sin(pi/n)) for the cavity, else 1)")
+    ap.add_argument("--sortol", type=float, default=0.0, help="sor_tolerance (0: 1e-9 cavity, else 1e-8)")
+    ap.add_argument("--msorit", type=int, default=0, help="max_sor_iter (0: 20000 cavity, else 2000)")
+    ap.add_argument("--ppe-defaults", action="store_true",
+                    help="the reference's default Poisson settings (sorrel 1, sortol 1e-8, 2000 sweeps)")
+    ap.add_argument("--ref-seconds", type=float, default=100.0,
+                    help="reference arm: time budget of its sample of whole steps")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--threads", type=int, default=0, help="threads per block (0: library default)")
     ap.add_argument("--blocks-per-sm", type=int, default=0)

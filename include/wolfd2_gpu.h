@@ -100,8 +100,9 @@ int wolfd2gpu_grid_metric(w2_ctx *ctx, const double *gx, const double *gy,
 /* ---- Drop-in replacements (arguments as in the reference) ------------ */
 
 /* nAuxMomentum, src/momentum.f:33-48: returns the number of Q-L iterations
- * (or -1) through *nQLiter.  Metric arguments are accepted for signature
- * parity and ignored: the copies uploaded at set-up are used.  Non-zero
+ * (or -1) through *nQLiter.  The reference's metric arguments are not in
+ * this signature: the copies uploaded at set-up are used (the Fortran
+ * replacement routine accepts and drops them).  Non-zero
  * density d, dn (EqState output) adds the buoyancy term of YMomentum
  * (momentum.f:703, divided by fr); d = dn = NULL means zero density. */
 int wolfd2gpu_naux_momentum(w2_ctx *ctx, const int *nx, const int *ny,
@@ -235,6 +236,13 @@ typedef struct {
   double divmax;      /* max |Divergence(u,v)| (pressure.f:287-299) over
                          the pressure cells of the projected field; no
                          counterpart in the reference                    */
+  double divmax_int;  /* the same over the interior cells: the four
+                         neighbours are Poisson unknowns and the four
+                         faces are set by Project, so the divergence is
+                         dk times the Poisson residual.  Cells touching a
+                         boundary also carry the fixed face values and
+                         the ghost pressures Ppe holds frozen during the
+                         solve, which no tolerance removes             */
 } w2_stepstat;
 
 /* Copy u, v, p (0:mnx,0:mny host arrays) to / from the device state. */
@@ -415,11 +423,12 @@ int wolfd2gpu_ens_destroy(w2_ens *ens);
  * (about 9.6 MB, held by every device that loads the library until the
  * process exits); the call makes no allocation.  Limits: Cartesian grids,
  * no blockage regions, ld*(ny+2) <= W2_NOALLOC_MAX_POINTS (else W2_E_SIZE).
- * The first call on a device looks up the scratch address on that device;
- * make that first call before any stream capture.  All calls share the
+ * Every call looks up the scratch's address on the current device
+ * (cudaGetSymbolAddress, which allocates nothing).  All calls share the
  * scratch: calls that overlap on the GPU race, so serialise them.
  * stream is a cudaStream_t (NULL = legacy default stream); the call
- * synchronises it before returning nSorConv. */
+ * synchronises it and copies its status to the host before returning
+ * nSorConv, so it cannot be used inside stream or graph capture. */
 #define W2_NOALLOC_MAX_POINTS 1200000
 int wolfd2gpu_ppe_rbsor_noalloc(int nx, int ny, int ld, int lCartesGrid,
                                 int nPpeSolver, int msorit, double dk,

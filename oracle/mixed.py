@@ -54,6 +54,14 @@ def div_check(nx: int, ny: int, met, u, v) -> float:
     return float(np.max(np.abs(divergence(nx, ny, met, u, v))))
 
 
+def div_check_interior(nx: int, ny: int, met, u, v) -> float:
+    """max |Divergence(u,v)| over the interior cells i, j = 3..n-1 (every
+    neighbour an unknown of the Poisson equation; on a one-region layout
+    also every face updated by Project), where the divergence is dk times
+    the Poisson residual."""
+    return float(np.max(np.abs(divergence(nx, ny, met, u, v)[1:-1, 1:-1])))
+
+
 def is_unit_stencil(nx: int, ny: int, met) -> bool:
     """Every Poisson row is (1, 1, -4, 1, 1) (pressure.f:97-106)."""
     rau, rgv = met["rau"], met["rgv"]
@@ -113,7 +121,7 @@ def ppe_mixed(nx: int, ny: int, met, u, v, p, dk: float, msorit: int, sortol: fl
 class MixedRun:
     """A case advanced by the time loop of main.f:690-972 with the mixed
     Ppe in place of the FP64 one; ``history`` holds (nQLiter, nSorConv,
-    dif(1..4), divmax) per step."""
+    dif(1..4), divmax, divmax over the interior cells) per step."""
 
     def __init__(self, case, fields: Optional[Dict[str, np.ndarray]] = None, cold_start: bool = True,
                  inner: int = 64):
@@ -171,7 +179,8 @@ class MixedRun:
             o.pres_bound_cond(nx, ny, r, f["p"])
             dif = (o.diff_max_norm(nx, ny, f["pn"], f["p"]), o.diff_max_norm(nx, ny, f["un"], f["u"]),
                    o.diff_max_norm(nx, ny, f["vn"], f["v"]), 0.0)
-            self.history.append((nql, nsor, dif, div_check(nx, ny, self.met, f["u"], f["v"])))
+            self.history.append((nql, nsor, dif, div_check(nx, ny, self.met, f["u"], f["v"]),
+                                 div_check_interior(nx, ny, self.met, f["u"], f["v"])))
             if max(dif) > 1.0e12:
                 raise FloatingPointError("Solution diverged. Please reduce CFL number.")
         return self.history[-1]

@@ -3,7 +3,8 @@ oracle, each checked against the mechanical translation of the reference's
 own Fortran source (oracle/f77ref.py) when the reference tree is present.
 
   cavity64_sor.json          64x64 lid-driven cavity, Re=100, dt=0.005,
-                             point SOR, cold start, 40 steps
+                             point SOR, cold start, all 500 steps of the
+                             configuration
   heated24_filter.json       24x24 differentially heated cavity (energy
                              equation, EqState, buoyancy), two momentum /
                              energy iterations, Filter of t, 6 steps
@@ -15,7 +16,11 @@ own Fortran source (oracle/f77ref.py) when the reference tree is present.
                              red-black line SOR, 5 steps
 
 Each file records which produced it: the oracle alone, or the translated
-reference source with the oracle equal to it bit for bit."""
+reference source with the oracle equal to it bit for bit.  Besides the
+iteration counts, the last step's differences and the exact sums, it keeps
+the SHA-256 of every final field's bytes ((nx+2) x (ny+2) doubles,
+Fortran order), so a run matches a fixture only if every value matches."""
+import hashlib
 import json
 import math
 import os
@@ -53,7 +58,7 @@ def _curvilinear_rb_lsor():
 
 # name -> (case factory, steps, description, fields)
 FIXTURES = {
-    "cavity64_sor": (_cavity64, 40, "cavity 64x64, Re=100, dt=0.005, ppe_solver sor, cold start",
+    "cavity64_sor": (_cavity64, 500, "cavity 64x64, Re=100, dt=0.005, ppe_solver sor, cold start",
                      "uvp"),
     "heated24_filter": (_heated24, 6, "heated cavity 24x24, Re=500, Pr=0.71, Fr=0.05, dt=0.004, "
                         "nmeiter 2, EqState + buoyancy, filter_t 20, rb_sor", "uvptd"),
@@ -65,13 +70,19 @@ FIXTURES = {
 }
 
 
-def summary(o, fields):
-    """The size-independent record a fixture keeps of an oracle run."""
+def field_hash(a, nx, ny):
+    """SHA-256 of the (0:nx+1, 0:ny+1) part of a field, Fortran order."""
+    return hashlib.sha256(np.asfortranarray(a[:nx + 2, :ny + 2]).tobytes(order="F")).hexdigest()
+
+
+def summary(o, fields, nx, ny):
+    """The record a fixture keeps of a run."""
     out = {"cold_nconv": o.cold_nconv,
            "iterations": [[h[0], h[1]] for h in o.history],
            "dif_last": list(o.history[-1][2]),
            "sum": {k: math.fsum(o.f[k].ravel()) for k in fields},
-           "abs_sum": {k: math.fsum(np.abs(o.f[k]).ravel()) for k in fields}}
+           "abs_sum": {k: math.fsum(np.abs(o.f[k]).ravel()) for k in fields},
+           "sha256": {k: field_hash(o.f[k], nx, ny) for k in fields}}
     return out
 
 
@@ -92,11 +103,11 @@ def make(name):
         assert [h[2] for h in r.history] == [h[2] for h in o.history], name
         src = "translated reference source (oracle/f77ref.py), equal to the oracle"
     out = {"case": desc, "steps": steps, "source": src}
-    out.update(summary(o, fields))
-    if name != "cavity64_sor":
-        out["fields"] = fields
+    out.update(summary(o, fields, case.nx, case.ny))
+    out["fields"] = fields
     with open(os.path.join(HERE, name + ".json"), "w") as f:
-        json.dump(out, f, indent=1)
+        f.write(json.dumps(out, indent=1, separators=(",", ": "))
+                .replace("[\n   ", "[").replace(",\n   ", ", ").replace("\n  ]", "]"))
     print("wrote", name, "from", out["source"])
 
 

@@ -1,8 +1,9 @@
 """The device time loop against the golden fixtures of tests/golden (made
 from the translated reference source), with no oracle in the loop: zero
 fields, cold start, then the fixture's steps through the C-ABI; iteration
-counts, the last step's differences and the exact sums of every field must
-equal the fixture's."""
+counts, the last step's differences, the exact sums and the SHA-256 of
+every field must equal the fixture's.  The 64x64 cavity fixture is the
+whole 500-step run of that configuration (lexicographic point SOR)."""
 import json
 import os
 import sys
@@ -40,6 +41,7 @@ def test_device_matches_golden(name):
     if "t" in fields:
         f["t"], f["d"] = s.store_thermal()
     s.close()
-    got = make_golden.summary(_Run(nconv, [(h[0], h[1], tuple(h[2])) for h in hist], f), fields)
-    for k in ("cold_nconv", "iterations", "dif_last", "sum", "abs_sum"):
+    got = make_golden.summary(_Run(nconv, [(h[0], h[1], tuple(h[2])) for h in hist], f), fields,
+                              case.nx, case.ny)
+    for k in ("cold_nconv", "iterations", "dif_last", "sum", "abs_sum", "sha256"):
         assert got[k] == g[k], (name, k, got[k], g[k])

@@ -90,17 +90,18 @@ GOLDEN = ("cavity64_sor", "heated24_filter", "thermal_multiregion", "curvilinear
 def test_golden_fixture(name):
     """The oracle's time loop reproduces each fixture of
     tests/golden/make_golden.py (generated from the translated reference
-    source): iteration counts, the last step's differences and the exact
-    sums of every field."""
+    source): iteration counts, the last step's differences, the exact
+    sums and the SHA-256 of every field."""
     sys.path.insert(0, os.path.join(HERE, "golden"))
     import make_golden
     g = json.load(open(os.path.join(HERE, "golden", name + ".json")))
     factory, steps, _, fields = make_golden.FIXTURES[name]
-    assert g["steps"] == steps and g.get("fields", "uvp") == fields
-    r = O.OracleRun(factory())
+    assert g["steps"] == steps and g["fields"] == fields
+    case = factory()
+    r = O.OracleRun(case)
     r.step(g["steps"])
-    assert make_golden.summary(r, fields) == {k: g[k] for k in
-                                              ("cold_nconv", "iterations", "dif_last", "sum", "abs_sum")}
+    keys = ("cold_nconv", "iterations", "dif_last", "sum", "abs_sum", "sha256")
+    assert make_golden.summary(r, fields, case.nx, case.ny) == {k: g[k] for k in keys}
 
 
 def test_face_profile_of_constants_equals_region_constant():

@@ -527,15 +527,16 @@ void plan_tiles(w2_ctx *c) {
 bool tiled_applies(w2_ctx *c, int npsolver, double sorrel) {
   const long cells = (long)(c->nx - 1) * (c->ny - 1);
   const bool big = cells >= (long)c->nsm * 1024;
+  (void)sorrel;
   return c->use_tiled && (big || c->use_tiled == 2) && c->tiled_ok && c->dev.ppe_unit &&
-         sorrel == 1.0 && (npsolver == 5 || npsolver == 6);
+         (npsolver == 5 || npsolver == 6);
 }
 
-int launch_ppe_tiled(w2_ctx *c, int lcartes, int msorit, double dk, double sortol,
+int launch_ppe_tiled(w2_ctx *c, int lcartes, int msorit, double dk, double sortol, double sorrel,
                      const double *u, const double *v, double *p, StepOut *out, const Dev *dv = nullptr) {
   Dev d = dv ? *dv : c->dev;
   TileGeom g = c->tg;
-  void *args[] = {&d, &g, &lcartes, &msorit, &dk, &sortol, (void *)&u, (void *)&v, &p, &out};
+  void *args[] = {&d, &g, &lcartes, &msorit, &dk, &sortol, &sorrel, (void *)&u, (void *)&v, &p, &out};
   c->launches++;
   cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_ppe_tiled, dim3(c->tiled_blocks),
                                               dim3(c->tiled_threads), args, c->tiled_smem, c->st);
@@ -795,7 +796,7 @@ int launch_ppe(w2_ctx *c, int lcartes, int npsolver, int msorit, double dk, doub
   }
   if (tiled_applies(c, npsolver, sorrel)) {
     ProfScope ps(c, W2_K_PPE);
-    return launch_ppe_tiled(c, lcartes, msorit, dk, sortol, u, v, p, c->d_out);
+    return launch_ppe_tiled(c, lcartes, msorit, dk, sortol, sorrel, u, v, p, c->d_out);
   }
   int blocks = (npsolver == 1 || npsolver == 2) ? 1 : pick_blocks(c, (const void *)k_ppe, (long)c->nx * c->ny);
   ProfScope ps(c, W2_K_PPE);
@@ -1635,7 +1636,7 @@ int issue_thermal_step(w2_ctx *c, const w2_params *prm, const double *un, const 
     {
       ProfScope ps(c, W2_K_PPE);
       if (tiled_applies(c, prm->npsolver, prm->sorrel)) {
-        if ((rc = launch_ppe_tiled(c, prm->lcartes, prm->msorit, prm->dk, prm->sortol, us, vs, p, o, &dl)))
+        if ((rc = launch_ppe_tiled(c, prm->lcartes, prm->msorit, prm->dk, prm->sortol, prm->sorrel, us, vs, p, o, &dl)))
           return rc;
       } else {
         int blocks = (prm->npsolver == 1 || prm->npsolver == 2)
@@ -1764,7 +1765,7 @@ int issue_steps(w2_ctx *c, const w2_params *prm, int nsteps, StepOut *d_outs) {
         break;
     } else if (tiled_applies(c, prm->npsolver, prm->sorrel)) {
       ProfScope ps(c, W2_K_PPE);
-      if ((rc = launch_ppe_tiled(c, prm->lcartes, prm->msorit, prm->dk, prm->sortol, us, vs, p, o))) break;
+      if ((rc = launch_ppe_tiled(c, prm->lcartes, prm->msorit, prm->dk, prm->sortol, prm->sorrel, us, vs, p, o))) break;
     } else {
       int blocks = (prm->npsolver == 1 || prm->npsolver == 2)
                        ? 1 : pick_blocks(c, (const void *)k_ppe, (long)c->nx * c->ny);
@@ -1894,6 +1895,7 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
       stats[s].nSorConv = outs[s].nsor;
       for (int k = 0; k < 4; ++k) stats[s].dif[k] = outs[s].dif[k];
       stats[s].divmax = outs[s].divmax;
+      stats[s].divmax_int = outs[s].divmax_int;
     }
     if (diverged_at < 0 && mx > 1.0e12) diverged_at = s;
   }
@@ -2436,6 +2438,7 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
         t.nSorConv = o.nsor;
         for (int q = 0; q < 4; ++q) t.dif[q] = o.dif[q];
         t.divmax = o.divmax;
+        t.divmax_int = o.divmax_int;
       }
       const double mx = std::max(std::max(o.dif[0], o.dif[1]), o.dif[2]);
       if (diverged < 0 && mx > 1.0e12) diverged = k;

@@ -116,7 +116,9 @@ struct Sync {
                                // [0..2] momentum ring, [3..5] PPE ring,
                                // [6..8] step norms, [9] scratch, [10..15]
                                // tiled PPE ring, [16] divergence check,
-                               // [17..40] mixed PPE ring
+                               // [17..40] mixed PPE ring, [41..44]
+                               // momentum/energy norms, [45] interior
+                               // divergence check
   int iout[8];                 // chain verification flags ([0..2] fwd, [3..5] bwd)
   double dout[8];              // small double results
   int me_done;                 // the momentum/energy iterations of this step converged

@@ -15,6 +15,7 @@ struct StepOut {
   int nql, nsor;
   double dif[4];
   double divmax;  // max |Divergence(u,v)| on the pressure cells after the step
+  double divmax_int;  // the same over the interior cells (div_check_local)
 };
 
 // ---- grid metrics (grid.f:258-535) ------------------------------------
@@ -310,7 +311,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_ppe(Dev d, int lcartes, int nps
 // sorrel = 1); dynamic shared memory holds the staged tile.
 __global__ void __launch_bounds__(kMaxThreads, 1) k_ppe_tiled(Dev d, TileGeom g, int lcartes,
                                                            int msorit, double dk, double sortol,
-                                                           const double *u, const double *v,
+                                                           double sorrel, const double *u, const double *v,
                                                            double *p, StepOut *out) {
   vgrid_set(0, gridDim.x);
   if (step_skip(d)) return;
@@ -319,7 +320,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1) k_ppe_tiled(Dev d, TileGeom g,
   if (!grid_sync(sy)) return;
   ppe_rhs_grid(d, lcartes, dk, p);
   if (!grid_sync(sy)) return;
-  const int nconv = ppe_rb_tiled(d, g, p, d.ppn, d.qh, msorit, sortol);
+  const int nconv = ppe_rb_tiled(d, g, p, d.ppn, d.qh, msorit, sortol, sorrel);
   if (nconv < 0) return;
   if (vblock() == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? msorit : nconv;
 }
@@ -394,16 +395,41 @@ __global__ void k_diff_norm(Dev d, const double *a, const double *b, unsigned lo
 }
 
 // Discrete divergence check on the pressure cells (2..nx, 2..ny) outside
-// blockages: max |Divergence(u,v)| of the projected field, FP64.
-__device__ double div_check_local(const Dev &d, const double *u, const double *v) {
+// blockages: max |Divergence(u,v)| of the projected field, FP64, into
+// `all`; into `inner`, the same over the interior cells -- those whose four
+// neighbours are unknowns of the Poisson equation (i, j = 3..n-1) and whose
+// four faces are all updated by Project.  There the divergence is dk times
+// the Poisson residual, the part a converged solve drives to zero.  In a
+// cell touching a boundary it also holds the face value the boundary
+// conditions fix and the change of the ghost pressure that Ppe keeps frozen
+// during the solve (PresBoundCond runs before and after it, main.f:793-816),
+// which no solver tolerance removes.
+__device__ void div_check_local(const Dev &d, const double *u, const double *v, double &all,
+                                double &inner) {
   const int nx = d.nx, ny = d.ny;
-  double mx = 0.0;
+  double mx = 0.0, mi = 0.0;
   for (int t = gtid(); t < (nx - 1) * (ny - 1); t += gthreads()) {
     const int i = t % (nx - 1) + 2, j = t / (nx - 1) + 2;
-    if (d.mask[IX(d, i, j)] & MK_DIVZ) continue;
-    mx = dmax(mx, fabs(div_point(d, u, v, i, j)));
+    const size_t o = IX(d, i, j);
+    const uint16_t mk = d.mask[o];
+    if (mk & MK_DIVZ) continue;
+    const double a = fabs(div_point(d, u, v, i, j));
+    mx = dmax(mx, a);
+    if (i >= 3 && i <= nx - 1 && j >= 3 && j <= ny - 1 && (mk & MK_PU) && (mk & MK_PV) &&
+        (d.mask[IX(d, i - 1, j)] & MK_PU) && (d.mask[IX(d, i, j - 1)] & MK_PV))
+      mi = dmax(mi, a);
   }
-  return mx;
+  all = mx;
+  inner = mi;
+}
+
+// Both divergence maxima of the projected field into slots 16 (all cells)
+// and 45 (interior cells).
+__device__ __forceinline__ void div_check_to(const Dev &d, const double *u, const double *v) {
+  double all, inner;
+  div_check_local(d, u, v, all, inner);
+  block_max_to(&d.sync->red[16], all);
+  block_max_to(&d.sync->red[45], inner);
 }
 
 // Tail of one step, main.f:813-972: PresBoundCond, Project, boundary
@@ -416,7 +442,7 @@ __device__ __forceinline__ void step_post_body(const Dev &d, double dk, double *
   if (vblock() == 0) {
     if (!pres_bound_cond_block(d, p) && threadIdx.x == 0) set_error(sy, W2_E_BCFLAG);
   }
-  if (vblock() == 0 && threadIdx.x == 0) sy->red[6] = sy->red[7] = sy->red[8] = sy->red[16] = 0ull;
+  if (vblock() == 0 && threadIdx.x == 0) sy->red[6] = sy->red[7] = sy->red[8] = sy->red[16] = sy->red[45] = 0ull;
   if (!grid_sync(sy)) return;
   project_grid(d, dk, p, u, v);
   if (!grid_sync(sy)) return;
@@ -431,7 +457,7 @@ __device__ __forceinline__ void step_post_body(const Dev &d, double dk, double *
   block_max_to(&sy->red[6], diff_norm_local(d, pn, p));
   block_max_to(&sy->red[7], diff_norm_local(d, un, u));
   block_max_to(&sy->red[8], diff_norm_local(d, vn, v));
-  block_max_to(&sy->red[16], div_check_local(d, u, v));
+  div_check_to(d, u, v);
   if (!grid_sync(sy)) return;
   if (vblock() == 0 && threadIdx.x == 0) {
     out->dif[0] = slot_value(&sy->red[6]);
@@ -439,6 +465,7 @@ __device__ __forceinline__ void step_post_body(const Dev &d, double dk, double *
     out->dif[2] = slot_value(&sy->red[8]);
     out->dif[3] = 0.0;
     out->divmax = slot_value(&sy->red[16]);
+    out->divmax_int = slot_value(&sy->red[45]);
     double mx = dmax(dmax(out->dif[0], out->dif[1]), out->dif[2]);
     if (mx > 1.0e12) sy->halt = 1;
   }

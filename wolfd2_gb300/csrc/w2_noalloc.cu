@@ -17,11 +17,12 @@
 // contents behind; each call clears the barrier and reduction state before
 // use.  Two calls whose kernels overlap on the GPU (different streams, or
 // different host threads) race on that array and give wrong results, so
-// callers serialise them.
+// callers serialise them.  A call waits for its stream and copies its result
+// to the host before returning, so it cannot be recorded into a CUDA graph
+// by stream capture.
 #include <cuda_runtime.h>
 
 #include <cstdio>
-#include <mutex>
 
 #include "w2_common.cuh"
 
@@ -113,26 +114,23 @@ __global__ void __launch_bounds__(512) k_ppe_noalloc(NaArgs a) {
   if (w2::vblock() == 0 && threadIdx.x == 0) sy->iout[0] = nconv < 1 ? a.msorit : nconv;
 }
 
-std::mutex g_setup_mu;
-void *g_scratch_addr[128] = {};  // per device, from cudaGetSymbolAddress
-
-// Once per device, with that device current: the device address of the
-// scratch array.  In host code the array's name is only a host-side stand-in
-// for the symbol, so the kernel is given this address instead.
-int scratch_address(int dev, void **out) {
-  std::lock_guard<std::mutex> lk(g_setup_mu);
-  if (dev < 0 || dev >= 128) return W2_E_ARG;
-  if (!g_scratch_addr[dev]) {
-    void *ptr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&ptr, w2_noalloc_scratch);
-    if (e != cudaSuccess || ptr == nullptr) {
-      fprintf(stderr, "wolfd2gpu_ppe_rbsor_noalloc: cudaGetSymbolAddress failed: %s\n",
-              cudaGetErrorString(e));
-      return W2_E_CUDA;
-    }
-    g_scratch_addr[dev] = ptr;
+// The device address of the scratch array on the current device.  In host
+// code the array's name is only a host-side stand-in for the symbol, so the
+// kernel is given this address instead.  It is looked up on every call (the
+// call's set-up, with the caller's device current): the lookup allocates
+// nothing and is cheap, and an address cached across calls would go stale
+// if the device's primary context were reset in between (cudaDeviceReset
+// by anyone in the process), after which the module -- and the array with
+// it -- can be loaded at another address.
+int scratch_address(void **out) {
+  void *ptr = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&ptr, w2_noalloc_scratch);
+  if (e != cudaSuccess || ptr == nullptr) {
+    fprintf(stderr, "wolfd2gpu_ppe_rbsor_noalloc: cudaGetSymbolAddress failed: %s\n",
+            cudaGetErrorString(e));
+    return W2_E_CUDA;
   }
-  *out = g_scratch_addr[dev];
+  *out = ptr;
   return W2_OK;
 }
 
@@ -161,7 +159,7 @@ extern "C" int wolfd2gpu_ppe_rbsor_noalloc(int nx, int ny, int ld, int lCartesGr
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return W2_E_CUDA;
   void *scr = nullptr;
-  int rc = scratch_address(dev, &scr);
+  int rc = scratch_address(&scr);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   // clear the barrier/reduction state left by the previous call

@@ -35,10 +35,13 @@ struct TileGeom {
 // points t, t+T, t+2T, ... in batches of four whose operands are all loaded
 // before any is updated (points of one colour never read each other), and the
 // row/column of the next point is advanced incrementally.  Returns max
-// |delta| (as IEEE bits) over points inside the own tile.
+// |delta| (as IEEE bits) over points inside the own tile.  RELAX: the
+// update is p + sorrel*sum (pressure.f:531); without it sorrel is 1 and
+// 1*sum == sum bit for bit, so the product is left out.
+template <bool RELAX>
 __device__ __forceinline__ unsigned long long tile_half_sweep(
     double *P, const double *Bt, int W, int gi0, int gj0, int bi0, int bi1, int bj0, int bj1,
-    int parity, int oi0, int oi1, int oj0, int oj1) {
+    int parity, int oi0, int oi1, int oj0, int oj1, double relax) {
   unsigned long long mx = 0ull;
   const int rows = bj1 - bj0 + 1;
   if (rows <= 0 || bi1 < bi0) return 0ull;
@@ -80,7 +83,7 @@ __device__ __forceinline__ unsigned long long tile_half_sweep(
     for (int q = 0; q < NB; ++q) {
       double sum = b[q] - s_[q] - w_[q] - e_[q] - n_[q];
       sum = sum * -0.25 - c_[q];
-      if (ok[q]) P[o[q]] = c_[q] + sum;
+      if (ok[q]) P[o[q]] = RELAX ? c_[q] + relax * sum : c_[q] + sum;
       if (own[q]) {
         const unsigned long long bb = abs_bits(sum);
         mx = bb > mx ? bb : mx;
@@ -92,8 +95,9 @@ __device__ __forceinline__ unsigned long long tile_half_sweep(
 
 // One group of up to K sweeps on every tile this block owns: read pin,
 // write pout (and pmid after the first sweep), record per-sweep maxima.
+template <bool RELAX>
 __device__ void tiled_group(const Dev &d, const TileGeom &g, const double *pin, double *pout,
-                            double *pmid, int nsweeps, unsigned long long *slots) {
+                            double *pmid, int nsweeps, unsigned long long *slots, double relax) {
   extern __shared__ double smem[];
   const int W = g.tx + 2 * kHalo, Hh = g.ty + 2 * kHalo;
   double *P = smem, *Bt = smem + W * Hh;
@@ -121,8 +125,8 @@ __device__ void tiled_group(const Dev &d, const TileGeom &g, const double *pin, 
         const int e = kHalo - 1 - 2 * s - c;  // box growth for this half-sweep
         const int bi0 = max(2, oi0 - e), bi1 = min(d.nx, oi1 + e);
         const int bj0 = max(2, oj0 - e), bj1 = min(d.ny, oj1 + e);
-        const unsigned long long m = tile_half_sweep(P, Bt, W, gi0, gj0, bi0, bi1, bj0, bj1,
-                                                     c, oi0, oi1, oj0, oj1);
+        const unsigned long long m = tile_half_sweep<RELAX>(P, Bt, W, gi0, gj0, bi0, bi1, bj0, bj1,
+                                                            c, oi0, oi1, oj0, oj1, relax);
         mxs[s] = m > mxs[s] ? m : mxs[s];
         __syncthreads();
       }
@@ -167,7 +171,7 @@ __device__ void tiled_group(const Dev &d, const TileGeom &g, const double *pin, 
 // Red/black SOR by groups of K sweeps.  p is the caller's field; pb2 and pm
 // are scratch fields.  Returns nConv (0 = not converged) or -1 on error.
 __device__ int ppe_rb_tiled(const Dev &d, const TileGeom &g, double *p, double *p2, double *pm,
-                            int msorit, double sortol) {
+                            int msorit, double sortol, double sorrel) {
   Sync *sy = d.sync;
   const int W = d.nx + 2, H = d.ny + 2;
   // scratch buffers start as copies of p (ghost values included)
@@ -195,7 +199,10 @@ __device__ int ppe_rb_tiled(const Dev &d, const TileGeom &g, double *p, double *
       unsigned long long *next = ring + ((grp + 1) % 3) * kSweepsPerSync;
       for (int k = 0; k < kSweepsPerSync; ++k) next[k] = 0ull;
     }
-    tiled_group(d, g, bufs[cur], bufs[cur ^ 1], pm, ns, slots);
+    if (sorrel == 1.0)
+      tiled_group<false>(d, g, bufs[cur], bufs[cur ^ 1], pm, ns, slots, sorrel);
+    else
+      tiled_group<true>(d, g, bufs[cur], bufs[cur ^ 1], pm, ns, slots, sorrel);
     if (!grid_sync(sy)) return -1;
     int conv_s = -1;
     for (int s2 = 0; s2 < ns; ++s2) {

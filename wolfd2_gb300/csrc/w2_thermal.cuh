@@ -384,14 +384,14 @@ __global__ void __launch_bounds__(kMaxThreads) k_step_tail_th(Dev d, ThermTables
     const bool ok = vel_bound_cond_block(d, u, v) && pres_bound_cond_block(d, p);
     if (!ok && threadIdx.x == 0) set_error(sy, W2_E_BCFLAG);
     if (therm) temp_bc_block(d, tt, t);
-    if (threadIdx.x == 0) sy->red[6] = sy->red[7] = sy->red[8] = sy->red[16] = sy->red[44] = 0ull;
+    if (threadIdx.x == 0) sy->red[6] = sy->red[7] = sy->red[8] = sy->red[16] = sy->red[44] = sy->red[45] = 0ull;
   }
   if (!grid_sync(sy)) return;
   block_max_to(&sy->red[6], diff_norm_local(d, pn, p));
   block_max_to(&sy->red[7], diff_norm_local(d, un, u));
   block_max_to(&sy->red[8], diff_norm_local(d, vn, v));
   block_max_to(&sy->red[44], diff_norm_local(d, tn, t));
-  block_max_to(&sy->red[16], div_check_local(d, u, v));
+  div_check_to(d, u, v);
   if (!grid_sync(sy)) return;
   if (vblock() == 0 && threadIdx.x == 0) {
     out->dif[0] = slot_value(&sy->red[6]);
@@ -399,6 +399,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_step_tail_th(Dev d, ThermTables
     out->dif[2] = slot_value(&sy->red[8]);
     out->dif[3] = slot_value(&sy->red[44]);
     out->divmax = slot_value(&sy->red[16]);
+    out->divmax_int = slot_value(&sy->red[45]);
     const double mx = dmax(dmax(dmax(out->dif[0], out->dif[1]), out->dif[2]), out->dif[3]);
     if (mx > 1.0e12) sy->halt = 1;
   }

@@ -69,7 +69,7 @@ class Params(C.Structure):
 
 class StepStat(C.Structure):
     _fields_ = [("nQLiter", C.c_int), ("nSorConv", C.c_int), ("dif", C.c_double * 4),
-                ("divmax", C.c_double)]
+                ("divmax", C.c_double), ("divmax_int", C.c_double)]
 
 
 _lib = None
@@ -421,7 +421,7 @@ class Solver:
         pr = Params.of(prm, **kw)
         st = (StepStat * max(nsteps, 1))()
         self._check(self.L.wolfd2gpu_step(self.h, C.byref(pr), nsteps, st))
-        return [(s.nQLiter, s.nSorConv, tuple(s.dif), s.divmax) for s in st[:nsteps]]
+        return [(s.nQLiter, s.nSorConv, tuple(s.dif), s.divmax, s.divmax_int) for s in st[:nsteps]]
 
     def step_log(self, prm: RunParams, nsteps: int, path: str, k0: int = 0, dtime0: float = 0.0,
                  **kw) -> List[tuple]:
@@ -433,9 +433,10 @@ class Solver:
         import math
         hist = self.step(prm, nsteps, **kw)
         with open(path, "a") as fh:
-            for n, (nql, nsor, dif, divmax) in enumerate(hist, 1):
+            for n, (nql, nsor, dif, divmax, divmax_int) in enumerate(hist, 1):
                 rec = {"k": k0 + n, "time": dtime0 + n * prm.dk, "nQLiter": nql, "nSorConv": nsor,
-                       "dif": [None if math.isnan(x) else x for x in dif], "divmax": divmax}
+                       "dif": [None if math.isnan(x) else x for x in dif], "divmax": divmax,
+                       "divmax_interior": divmax_int}
                 fh.write(json.dumps(rec) + "\n")
         return hist
 
@@ -446,7 +447,7 @@ class Solver:
         pr = Params.of(prm)
         st = (StepStat * max(n, 1))()
         self._check(self.L.wolfd2gpu_step_counts(self.h, C.byref(pr), n, counts.ctypes.data_as(_ip), st))
-        return [(s.nQLiter, s.nSorConv, tuple(s.dif), s.divmax) for s in st[:n]]
+        return [(s.nQLiter, s.nSorConv, tuple(s.dif), s.divmax, s.divmax_int) for s in st[:n]]
 
     def adjoint(self, prm: RunParams, nsteps: int, every: int = 20, weight: float = 1.0,
                 profile=None, nprof: int = 0):
@@ -534,14 +535,14 @@ class Ensemble:
              precision: int = PREC_MIXED) -> List[List[tuple]]:
         """nsteps steps of every case in `precision` (PREC_MIXED or
         PREC_FP64); returns per case the records (nQLiter, nSorConv, dif,
-        divmax) of each step."""
+        divmax, divmax_int) of each step."""
         n = len(self.solvers)
         if len(params) != n:
             raise ValueError("one RunParams per case")
         pr = (Params * n)(*[Params.of(p, precision=precision, refine_sweeps=refine_sweeps) for p in params])
         st = (StepStat * max(n * nsteps, 1))()
         self._check(self.L.wolfd2gpu_ens_step(self.h, pr, nsteps, st))
-        return [[(x.nQLiter, x.nSorConv, tuple(x.dif), x.divmax) for x in st[k * nsteps:(k + 1) * nsteps]]
+        return [[(x.nQLiter, x.nSorConv, tuple(x.dif), x.divmax, x.divmax_int) for x in st[k * nsteps:(k + 1) * nsteps]]
                 for k in range(n)]
 
     STAGES = ("ke_copy_mixed", "ke_naux32", "ke_bc", "ke_ppe_mixed", "ke_step_post")
