@@ -840,8 +840,8 @@ def ensemble_config(args, members, inner, graph):
                      f"{', step captured in a CUDA graph' if graph else ''}"),
         "cases": len(members), "cells": int(sum(m.case.cells for m in members)),
         "n_min": min(ns), "n_max": max(ns), "dt_capped_cases": sum(1 for m in members if m.dt < m.dt_named),
-        "layout": "each cavity at spacing 1/64 with side N/64 and deck Re = Re/side: the exact similarity "
-                  "image of the unit cavity (unit-stencil Poisson rows)",
+        "layout": "each cavity the unit square with h = 1/N; the Poisson rows of every member round to "
+                  "the unit stencil in FP32 (exactly unit only for N a power of two)",
         "precision": args.precision, "graph": graph,
         "l2": "not flushed: the ensemble's fields alone exceed L2 (129 MB) many times over",
     }

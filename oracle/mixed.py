@@ -62,20 +62,43 @@ def div_check_interior(nx: int, ny: int, met, u, v) -> float:
     return float(np.max(np.abs(divergence(nx, ny, met, u, v)[1:-1, 1:-1])))
 
 
+def ppe_rows(nx: int, ny: int, met):
+    """The Poisson rows a1..a5 of pressure.f:97-106 on i, j = 2..nx, 2..ny,
+    each an (nx-1, ny-1) array, a3 formed in the reference's order."""
+    rau, rgv = met["rau"], met["rgv"]
+    I, J, Im, Jm = slice(2, nx + 1), slice(2, ny + 1), slice(1, nx), slice(1, ny)
+    a1, a2, a4, a5 = rgv[I, Jm], rau[Im, J], rau[I, J], rgv[I, J]
+    a3 = -rau[I, J] - rau[Im, J] - rgv[I, J] - rgv[I, Jm]
+    return a1, a2, a3, a4, a5
+
+
 def is_unit_stencil(nx: int, ny: int, met) -> bool:
     """Every Poisson row is (1, 1, -4, 1, 1) (pressure.f:97-106)."""
-    rau, rgv = met["rau"], met["rgv"]
-    return bool(np.all(rau[1:nx + 1, 2:ny + 1] == 1.0) and np.all(rgv[2:nx + 1, 1:ny + 1] == 1.0))
+    a1, a2, a3, a4, a5 = ppe_rows(nx, ny, met)
+    return bool(np.all(a1 == 1.0) and np.all(a2 == 1.0) and np.all(a3 == -4.0) and
+                np.all(a4 == 1.0) and np.all(a5 == 1.0))
+
+
+def is_unit_stencil32(nx: int, ny: int, met) -> bool:
+    """Every Poisson row rounds to (1, 1, -4, 1, 1) in FP32: the rows of any
+    uniform square-cell Cartesian grid."""
+    a = [x.astype(np.float32) for x in ppe_rows(nx, ny, met)]
+    return bool(np.all(a[0] == 1) and np.all(a[1] == 1) and np.all(a[2] == -4) and
+                np.all(a[3] == 1) and np.all(a[4] == 1))
 
 
 def ppe_mixed(nx: int, ny: int, met, u, v, p, dk: float, msorit: int, sortol: float,
               sorrel: float, inner: int, dtype=np.float32) -> int:
-    """Mixed Ppe on a Cartesian unit-stencil grid without blockages; p is
-    updated in place on i = 2..nx, j = 2..ny.  Returns nSorConv (msorit when
-    the stopping rule never fired).  dtype = float64 gives the same
-    iteration with FP64 sweeps (equal to the plain solve up to rounding)."""
-    if not is_unit_stencil(nx, ny, met):
-        raise ValueError("mixed Ppe needs the unit stencil")
+    """Mixed Ppe on a Cartesian grid without blockages whose Poisson rows
+    round to the unit stencil in FP32; p is updated in place on i = 2..nx,
+    j = 2..ny.  The FP32 sweeps run the unit stencil, each pass's FP64
+    residual the grid's own rows (the unit form when they are exactly
+    unit).  Returns nSorConv (msorit when the stopping rule never fired).
+    dtype = float64 gives the same iteration with FP64 sweeps."""
+    if not is_unit_stencil32(nx, ny, met):
+        raise ValueError("mixed Ppe needs rows that round to the unit stencil in FP32")
+    unit = is_unit_stencil(nx, ny, met)
+    a1, a2, a3, a4, a5 = ppe_rows(nx, ny, met)
     b = divergence(nx, ny, met, u, v) / dk
     I, J = np.meshgrid(np.arange(2, nx + 1), np.arange(2, ny + 1), indexing="ij")
     cols = []
@@ -89,7 +112,11 @@ def ppe_mixed(nx: int, ny: int, met, u, v, p, dk: float, msorit: int, sortol: fl
     done = False
     while not done:
         ps = p[2:nx + 1, 2:ny + 1]
-        ap = p[2:nx + 1, 1:ny] + p[1:nx, 2:ny + 1] + p[3:nx + 2, 2:ny + 1] + p[2:nx + 1, 3:ny + 2] - 4.0 * ps
+        if unit:
+            ap = p[2:nx + 1, 1:ny] + p[1:nx, 2:ny + 1] + p[3:nx + 2, 2:ny + 1] + p[2:nx + 1, 3:ny + 2] - 4.0 * ps
+        else:
+            ap = (a1 * p[2:nx + 1, 1:ny] + a2 * p[1:nx, 2:ny + 1] + a4 * p[3:nx + 2, 2:ny + 1] +
+                  a5 * p[2:nx + 1, 3:ny + 2] + a3 * ps)
         R = np.zeros((nx + 2, ny + 2), dtype=dtype)
         R[2:nx + 1, 2:ny + 1] = (b - ap).astype(dtype)
         E = np.zeros((nx + 2, ny + 2), dtype=dtype)

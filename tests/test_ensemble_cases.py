@@ -13,14 +13,13 @@ def test_ensemble_workload_draws():
     assert [(x.n, x.re) for x in m] == [(x.n, x.re) for x in deck.ensemble_cases(256, seed=2024)]
     for x in m[:20]:
         c = x.case
-        side = x.n * deck.ENSEMBLE_H
+        # the unit square, h = 1/N, the drawn Re and dt = 0.5 h (capped)
         hx = np.diff(c.x[:, 0])
-        # power-of-two spacing, exact: every Poisson row is the unit stencil
-        assert np.all(hx == deck.ENSEMBLE_H)
+        assert np.allclose(hx, 1.0 / x.n, rtol=1e-12, atol=0)
+        assert c.x[-1, 0] == 1.0 and c.y[0, -1] == 1.0
         assert c.nx == x.n + 1 and c.ny == x.n + 1
-        # similarity: deck Re times the side is the cavity Re; dt in the unit frame
-        assert abs(c.params.re * side - x.re) <= 1e-9 * x.re
-        assert abs(c.params.dk / side - x.dt) <= 1e-15
+        assert abs(c.params.re - x.re) <= 1e-9 * x.re
+        assert c.params.dk == x.dt
         assert x.dt <= x.dt_named == 0.5 / x.n
         assert x.dt / (x.re / x.n ** 2) <= 0.25 * (1 + 1e-12)
 

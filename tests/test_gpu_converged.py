@@ -67,8 +67,11 @@ def test_converged_plain_step_matches_oracle(n):
     div = M.divergence(nx, ny, ref.met, u, v)
     assert hist[-1][3] == float(np.max(np.abs(div)))
     assert hist[-1][4] == float(np.max(np.abs(div[1:-1, 1:-1])))
+    # the boundary part is the frozen-ghost term, up to the remaining
+    # Poisson residual (the size of the interior divergence)
     term = frozen_ghost_term(case, ref.met, p1, p)
-    assert np.max(np.abs(div - term)) <= 1e-12 * max(1.0, float(np.max(np.abs(div))))
+    assert np.max(np.abs(div)) > 1e3 * hist[-1][4]
+    assert np.max(np.abs(div - term)) <= 10.0 * hist[-1][4] + 1e-13
 
 
 def test_converged_mixed_step_matches_model():

@@ -161,12 +161,38 @@ def test_mixed_rejects_unsupported():
         s.step(case.params, 1, precision=PREC_MIXED)  # lexicographic SOR
     with pytest.raises(W2Error):
         s.tune_mixed(2, 0)
-    odd = deck.cavity(48, 100.0, 0.005, solver="rb_sor")  # h = 1/48: not the unit stencil
+    # cells 0.0625 x 0.05: Poisson rows (1.25, 0.8, -4.1, 0.8, 1.25), not the unit stencil in FP32
+    odd = deck.channel(40, 20, 800.0, 0.004, length=2.5, solver="rb_sor", outlet="mc")
     s2 = Solver.for_case(odd)
     z = s2.field()
     s2.load_fields(z, z, z)
     with pytest.raises(W2Error):
         s2.step(odd.params, 1, precision=PREC_MIXED)
+
+
+@pytest.mark.parametrize("n", [48, 96])
+def test_mixed_non_dyadic_grid_matches_model(n):
+    """h = 1/n with n not a power of two: the Poisson rows miss the unit
+    stencil by rounding in FP64 but round to it in FP32, so the FP32 sweeps
+    run the unit stencil and every pass's FP64 residual the grid's own
+    rows.  Bit-identical to the model, close to the FP64 oracle."""
+    case = deck.cavity(n, 400.0, 0.25 / n, solver="rb_sor")
+    u0, v0, p0 = deck.perturbation_ic(case, 3)
+    fields = {"u": u0, "v": v0, "p": p0}
+    model = M.MixedRun(case, fields=fields, cold_start=False, inner=32)
+    model.step(3)
+    s = Solver.for_case(case)
+    s.load_fields(u0, v0, p0)
+    hist = s.step(case.params, 3, precision=PREC_MIXED, refine_sweeps=32)
+    assert [(h[0], h[1]) for h in hist] == [(h[0], h[1]) for h in model.history]
+    u, v, p = s.store_fields()
+    for nm, g in (("u", u), ("v", v), ("p", p)):
+        assert np.array_equal(g, model.f[nm]), (nm, _rel(g, model.f[nm]))
+    ref = O.OracleRun(case, fields=fields, cold_start=False)
+    ref.step(3)
+    assert [h[1] for h in hist] == [h[1] for h in ref.history]
+    assert _vel_rel(u, v, ref.f["u"], ref.f["v"]) <= UVP_REL_TOL
+    assert _p_rel(p, ref.f["p"], ref.f["u"], ref.f["v"]) <= P_DYN_TOL
 
 
 def test_mixed_multitile_time_loop_matches_model():

@@ -755,12 +755,14 @@ void plan_mixed(w2_ctx *c) {
 }
 
 // The mixed path covers npsolver 5/6 on Cartesian grids whose rows are all
-// the unit stencil (no blockages).
+// the unit stencil in FP32 (no blockages): every uniform square-cell grid.
 int mixed_check(w2_ctx *c, int lcartes, int npsolver) {
   if (npsolver != 5 && npsolver != 6)
     return fail(c, W2_E_UNSUPPORTED, "mixed precision needs ppe_solver rb_sor or rb_sorp (5/6), got %d", npsolver);
-  if (!lcartes || !c->dev.ppe_unit)
-    return fail(c, W2_E_UNSUPPORTED, "mixed precision needs a Cartesian unit-stencil grid without blockages");
+  if (!lcartes || !c->dev.ppe_unit32)
+    return fail(c, W2_E_UNSUPPORTED,
+                "mixed precision needs a Cartesian grid whose Poisson rows round to the unit stencil in FP32 "
+                "(uniform square cells, no blockages)");
   if (!c->mixed_ok) return fail(c, W2_E_UNSUPPORTED, "no mixed-precision tile plan fits this grid");
   return W2_OK;
 }
@@ -1006,7 +1008,8 @@ static int finish_coefficients(w2_ctx *c) {
   int h = 1;
   CK(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
-  c->dev.ppe_unit = (h == 0) ? 1 : 0;
+  c->dev.ppe_unit = (h & 1) ? 0 : 1;
+  c->dev.ppe_unit32 = (h & 2) ? 0 : 1;
   plan_tiles(c);
   plan_mixed(c);
   return momentum_metrics(c);
@@ -2169,7 +2172,8 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
   e->threads = threads;
   e->K = sweeps_per_barrier;
   e->cs.assign(cases, cases + n);
-  // the mixed step needs unit-stencil Poisson rows in every case
+  // the mixed step needs Poisson rows that round to the unit stencil in
+  // FP32 in every case
   bool unit = true;
   for (int k = 0; k < n; ++k) {
     w2_ctx *c = e->cs[k];
@@ -2177,7 +2181,7 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
     if (int rc = ready(c)) return bad(efail(e, rc, "case %d: %s", k, c->err));
     if (c->therm_on)
       return bad(efail(e, W2_E_UNSUPPORTED, "case %d: ensembles do not run the energy equation", k));
-    unit = unit && c->dev.ppe_unit;
+    unit = unit && c->dev.ppe_unit32;
     if (k == 0) e->device = c->device;
     else if (c->device != e->device) return bad(efail(e, W2_E_ARG, "cases on different devices"));
   }
@@ -2323,7 +2327,8 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
     if ((q.precision == W2_PREC_MIXED) != mixed)
       return efail(e, W2_E_UNSUPPORTED, "case %d: every case of one call runs in the same precision", k);
     if (mixed && !e->mixed_ok)
-      return efail(e, W2_E_UNSUPPORTED, "the mixed step needs unit-stencil Poisson rows in every case");
+      return efail(e, W2_E_UNSUPPORTED, "the mixed step needs Poisson rows that round to the unit stencil "
+                                        "in FP32 in every case");
     if (mixed && ((q.npsolver != 5 && q.npsolver != 6) || !q.lcartes))
       return efail(e, W2_E_UNSUPPORTED, "case %d: the mixed step needs rb_sor/rb_sorp on a Cartesian grid", k);
     if (q.npsolver < 1 || q.npsolver > 6) return efail(e, W2_E_ARG, "case %d: bad Poisson solver %d", k, q.npsolver);

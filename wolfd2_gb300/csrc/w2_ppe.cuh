@@ -49,14 +49,20 @@ __device__ void ppe_coefficients(const Dev &d) {
 // Flags any row whose coefficients are not the unit stencil (identity rows
 // of blockages excluded from the check; the unit form is used only when
 // there are none).
+// flag bit 0: some row is not exactly (1,1,-4,1,1) (or is an identity row);
+// bit 1: some row does not round to it in FP32 (or is an identity row).
 __device__ void ppe_check_unit(const Dev &d, int *flag) {
   const int nx = d.nx, ny = d.ny;
   for (int t = gtid(); t < (nx - 1) * (ny - 1); t += gthreads()) {
     const int i = t % (nx - 1) + 2, j = t / (nx - 1) + 2;
     const size_t o = IX(d, i, j);
-    if ((d.mask[o] & MK_PID) || d.pa1[o] != 1.0 || d.pa2[o] != 1.0 || d.pa3[o] != -4.0 ||
-        d.pa4[o] != 1.0 || d.pa5[o] != 1.0)
+    const bool id = (d.mask[o] & MK_PID) != 0;
+    if (id || d.pa1[o] != 1.0 || d.pa2[o] != 1.0 || d.pa3[o] != -4.0 || d.pa4[o] != 1.0 ||
+        d.pa5[o] != 1.0)
       atomicOr(flag, 1);
+    if (id || (float)d.pa1[o] != 1.0f || (float)d.pa2[o] != 1.0f || (float)d.pa3[o] != -4.0f ||
+        (float)d.pa4[o] != 1.0f || (float)d.pa5[o] != 1.0f)
+      atomicOr(flag, 2);
   }
 }
 

@@ -193,6 +193,20 @@ __device__ __forceinline__ void mixed_sweeps(const MixedBox &b, int ns, float re
   }
 }
 
+// (A p) at point o in FP64 for the residual of a refinement pass: on
+// unit-stencil rows p_s + p_w + p_e + p_n - 4 p, otherwise the coefficients
+// of pressure.f:97-106 in the same order, (((a1 p_s + a2 p_w) + a4 p_e) +
+// a5 p_n) + a3 p, which is the unit form bit for bit when the a's are
+// (1, 1, -4, 1, 1).  The FP32 sweeps run the unit stencil: the rows of any
+// uniform square-cell grid round to it in FP32 (ppe_unit32), and the
+// residual of the next pass, formed with the FP64 rows, corrects the
+// difference.
+__device__ __forceinline__ double mixed_ap(const Dev &d, const double *p, size_t o) {
+  if (d.ppe_unit) return p[o - d.ld] + p[o - 1] + p[o + 1] + p[o + d.ld] - 4.0 * p[o];
+  return d.pa1[o] * p[o - d.ld] + d.pa2[o] * p[o - 1] + d.pa4[o] * p[o + 1] + d.pa5[o] * p[o + d.ld] +
+         d.pa3[o] * p[o];
+}
+
 // r = b - A p in FP64 on the whole box (zero off the unknowns) into the
 // shared R planes; e = 0 in the shared planes.
 __device__ __noinline__ void mixed_residual(const Dev &d, const MixedBox &b, const double *p) {
@@ -203,8 +217,7 @@ __device__ __noinline__ void mixed_residual(const Dev &d, const MixedBox &b, con
     float r = 0.0f;
     if (i >= 2 && i <= d.nx && j >= 2 && j <= d.ny) {
       const size_t o = IX(d, i, j);
-      const double ap = p[o - d.ld] + p[o - 1] + p[o + 1] + p[o + d.ld] - 4.0 * p[o];
-      r = (float)(d.pb[o] - ap);
+      r = (float)(d.pb[o] - mixed_ap(d, p, o));
     }
     const int c = (i + j) & 1, x = (j - b.gj0) * b.hw + ((i - b.gi0) >> 1);
     b.R[c][x] = r;
@@ -446,8 +459,7 @@ __device__ __noinline__ void mixed_residual_tile(const Dev &d, const MixedGeom &
   for (int t = threadIdx.x; t < tw * th; t += blockDim.x) {
     const int i = b.oi0 + t % tw, j = b.oj0 + t / tw;
     const size_t o = IX(d, i, j);
-    const double ap = p[o - d.ld] + p[o - 1] + p[o + 1] + p[o + d.ld] - 4.0 * p[o];
-    Rg[mixed_gpos<K>(g, i, j)] = (float)(d.pb[o] - ap);
+    Rg[mixed_gpos<K>(g, i, j)] = (float)(d.pb[o] - mixed_ap(d, p, o));
   }
 }
 

@@ -676,7 +676,6 @@ def channel_ic(case: Case):
 
 
 ENSEMBLE_SIZES = tuple(range(64, 513, 32))
-ENSEMBLE_H = 1.0 / 64.0
 
 
 @dataclasses.dataclass
@@ -684,21 +683,16 @@ class EnsembleMember:
     case: Case
     n: int           # cells per side
     re: float        # cavity Reynolds number U L / nu
-    dt_named: float  # 0.5 h in the unit-cavity frame
-    dt: float        # the step used (unit-cavity frame)
+    dt_named: float  # 0.5 h
+    dt: float        # the step used
 
 
 def ensemble_cases(count: int = 256, seed: int = 2024, visc_max: float = 0.25,
                    solver: str = "rb_sor") -> List[EnsembleMember]:
-    """The batched-ensemble workload: ``count`` lid-driven cavities, N cells
-    per side drawn uniformly from {64, 96, ..., 512} and the cavity Reynolds
-    number log-uniform in [100, 5000], both from default_rng(seed), dt = 0.5 h.
-
-    Each cavity is laid out with the same power-of-two spacing h = 1/64 and
-    side L = N/64, with deck Re = Re_cavity / L: the exact similarity image of
-    the unit cavity with h = 1/N at Re_cavity (lengths times L, times times
-    L), so dt = 0.5 h in either frame.  Exact node coordinates give every
-    Poisson row the unit stencil, which the mixed sweeps need.
+    """The batched-ensemble workload: ``count`` lid-driven cavities on the
+    unit square, N cells per side drawn uniformly from {64, 96, ..., 512}
+    and the cavity Reynolds number log-uniform in [100, 5000], both from
+    default_rng(seed), h = 1/N, dt = 0.5 h.
 
     The reference's scheme is unstable above a viscous number dt/(h^2 Re)
     of about 0.3 (0.64 reaches NaN within 8 steps), and 0.5 h / (h^2 Re) =
@@ -709,12 +703,10 @@ def ensemble_cases(count: int = 256, seed: int = 2024, visc_max: float = 0.25,
     res = np.exp(rng.uniform(np.log(100.0), np.log(5000.0), size=count))
     out = []
     for n, re in zip(ns.tolist(), res.tolist()):
-        side = n * ENSEMBLE_H
-        h_unit = 1.0 / n
-        dt_named = 0.5 * h_unit
-        dt = min(dt_named, visc_max * h_unit * h_unit * re)
-        # deck frame: lengths x side, time x side, Re_deck = Re / side
-        case = cavity(n, re / side, dt * side, solver=solver, side=side)
+        h = 1.0 / n
+        dt_named = 0.5 * h
+        dt = min(dt_named, visc_max * h * h * re)
+        case = cavity(n, re, dt, solver=solver)
         case.name = f"ens_cavity{n}_re{re:.1f}"
         out.append(EnsembleMember(case, n, re, dt_named, dt))
     return out
