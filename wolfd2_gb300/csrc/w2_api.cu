@@ -508,7 +508,7 @@ void plan_tiles(w2_ctx *c) {
       const double cost = per_block * area;
       if (cost < best) {
         best = cost;
-        c->tg = TileGeom{tx, ty, ntx, nty};
+        c->tg = TileGeom{tx, ty, ntx, nty, 1.0, -1.0};
         c->tiled_smem = smem;
       }
     }

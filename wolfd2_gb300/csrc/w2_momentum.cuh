@@ -226,6 +226,104 @@ __device__ __forceinline__ T ycj(const Dev &d, const MomView<T> &V, const T *us,
 }
 
 // ---- M2a: stencils and split-1 rows ------------------------------------
+// X row t of split 1 (i = t % nx + 1, j = t / nx + 2; momentum.f:350-384).
+template <class T>
+__device__ __forceinline__ ChainRow<T> x_row1(const Dev &d, const MomView<T> &V, T re1, T dk2,
+                                              const T *us, const T *vs, const T *un, const T *vn,
+                                              int t) {
+  const int nx = d.nx;
+  const int i = t % nx + 1, j = t / nx + 2;
+  const size_t o = IX(d, i, j);
+  const T rkj = dk2 * V.dju(i, j);
+  T c1s_o, c1s_e, c2s_o, c2s_s, c1n_o, c1n_e, c2n_o, c2n_s;
+  if constexpr (kFuseConv<T>) {
+    c1s_o = conv_x1_c1(d, V, us, vs, i, j);
+    c1s_e = conv_x1_c1(d, V, us, vs, i + 1, j);
+    c2s_o = conv_x1_c2(d, V, us, vs, i, j);
+    c2s_s = conv_x1_c2(d, V, us, vs, i, j - 1);
+    c1n_o = conv_x1_c1(d, V, un, vn, i, j);
+    c1n_e = conv_x1_c1(d, V, un, vn, i + 1, j);
+    c2n_o = conv_x1_c2(d, V, un, vn, i, j);
+    c2n_s = conv_x1_c2(d, V, un, vn, i, j - 1);
+  } else {
+    c1s_o = V.c1sx[o]; c1s_e = V.c1sx[IX(d, i + 1, j)];
+    c2s_o = V.c2sx[o]; c2s_s = V.c2sx[IX(d, i, j - 1)];
+    c1n_o = V.c1nx[o]; c1n_e = V.c1nx[IX(d, i + 1, j)];
+    c2n_o = V.c2nx[o]; c2n_s = V.c2nx[IX(d, i, j - 1)];
+  }
+  const T cnvs = dconv_u(d, c2s_s, c1s_o, c1s_e, c2s_o, us, i, j);
+  const T cnvn = dconv_u(d, c2n_s, c1n_o, c1n_e, c2n_o, un, i, j);
+  const T difs = ddiff_u(d, V.rac, V.rbc, V.rbn, V.rgn, us, i, j);
+  const T difn = ddiff_u(d, V.rac, V.rbc, V.rbn, V.rgn, un, i, j);
+  const T cj1 = xcj(d, V, us, vs, 1, i, j), racp = V.rac(i + 1, j), rac0 = V.rac(i, j);
+  ChainRow<T> r;
+  if (cj1 >= T(0)) {
+    r.a1 = rkj * (-xcj(d, V, us, vs, 1, i - 1, j) - re1 * rac0);
+    r.a2 = T(1.0) + rkj * (cj1 + re1 * (racp + rac0));
+    r.a3 = rkj * (-re1 * racp);
+  } else {
+    r.a1 = rkj * (-re1 * rac0);
+    r.a2 = T(1.0) + rkj * (-cj1 + re1 * (racp + rac0));
+    r.a3 = rkj * (xcj(d, V, us, vs, 1, i + 1, j) - re1 * racp);
+  }
+  r.b = un[o] - us[o] + rkj * (-cnvs - cnvn) + rkj * re1 * (difs + difn);
+  return r;
+}
+
+// Y row q of split 1 (i = q % (nx-1) + 2, j = q / (nx-1) + 1; momentum.f:675-711),
+// with the buoyancy term of momentum.f:703 when a density is given (FP64).
+template <class T>
+__device__ __forceinline__ ChainRow<T> y_row1(const Dev &d, const MomView<T> &V, T re1, T dk2,
+                                              double dk, const T *us, const T *vs, const T *un,
+                                              const T *vn, int q) {
+  const int nx = d.nx;
+  const int i = q % (nx - 1) + 2, j = q / (nx - 1) + 1;
+  const size_t o = IX(d, i, j);
+  const T rkj = dk2 * V.djv(i, j);
+  T c2s_o, c1s_w, c1s_o, c2s_n, c2n_o, c1n_w, c1n_o, c2n_n;
+  if constexpr (kFuseConv<T>) {
+    c2s_o = conv_y2_c2(d, V, us, vs, i, j);
+    c1s_w = conv_y2_c1(d, V, us, vs, i - 1, j);
+    c1s_o = conv_y2_c1(d, V, us, vs, i, j);
+    c2s_n = conv_y2_c2(d, V, us, vs, i, j + 1);
+    c2n_o = conv_y2_c2(d, V, un, vn, i, j);
+    c1n_w = conv_y2_c1(d, V, un, vn, i - 1, j);
+    c1n_o = conv_y2_c1(d, V, un, vn, i, j);
+    c2n_n = conv_y2_c2(d, V, un, vn, i, j + 1);
+  } else {
+    c2s_o = V.c2sy[o]; c1s_w = V.c1sy[IX(d, i - 1, j)];
+    c1s_o = V.c1sy[o]; c2s_n = V.c2sy[IX(d, i, j + 1)];
+    c2n_o = V.c2ny[o]; c1n_w = V.c1ny[IX(d, i - 1, j)];
+    c1n_o = V.c1ny[o]; c2n_n = V.c2ny[IX(d, i, j + 1)];
+  }
+  const T cnvs = dconv_v(d, c2s_o, c1s_w, c1s_o, c2s_n, vs, i, j);
+  const T cnvn = dconv_v(d, c2n_o, c1n_w, c1n_o, c2n_n, vn, i, j);
+  const T difs = ddiff_v(d, V.ran, V.rbc, V.rbn, V.rgc, vs, i, j);
+  const T difn = ddiff_v(d, V.ran, V.rbc, V.rbn, V.rgc, vn, i, j);
+  const T cj1 = ycj(d, V, us, vs, 1, i, j), ran0 = V.ran(i, j), ranw = V.ran(i - 1, j);
+  ChainRow<T> r;
+  if (cj1 >= T(0)) {
+    r.a1 = rkj * (-ycj(d, V, us, vs, 1, i - 1, j) - re1 * ranw);
+    r.a2 = rkj * (cj1 + re1 * (ran0 + ranw)) + T(1.0);
+    r.a3 = rkj * (-re1 * ran0);
+  } else {
+    r.a1 = rkj * (-re1 * ranw);
+    r.a2 = rkj * (-cj1 + re1 * (ran0 + ranw)) + T(1.0);
+    r.a3 = rkj * (ycj(d, V, us, vs, 1, i + 1, j) - re1 * ran0);
+  }
+  T rhs = vn[o] - vs[o] + rkj * (-cnvs - cnvn) + rkj * re1 * (difs + difn);
+  if constexpr (std::is_same<T, double>::value) {
+    if (d.den) {
+      // buoy = dk (d(i,j+1) + d(i,j) + dn(i,j+1) + dn(i,j)) / (4 fr)
+      const size_t on = IX(d, i, j + 1);
+      const double buoy = dk * (d.den[on] + d.den[o] + d.denn[on] + d.denn[o]) / (4.0 * d.fr);
+      rhs = rhs - buoy;
+    }
+  }
+  r.b = rhs;
+  return r;
+}
+
 template <class T>
 __device__ void mom_assemble1(const Dev &d, const MomView<T> &V, double dk, double re,
                               const T *us, const T *vs, const T *un, const T *vn) {
@@ -236,102 +334,79 @@ __device__ void mom_assemble1(const Dev &d, const MomView<T> &V, double dk, doub
   const int nY = (nx - 1) * ny;
   for (int t = gtid(); t < nX + nY; t += gthreads()) {
     if (t < nX) {
-      const int i = t % nx + 1, j = t / nx + 2;
-      const size_t o = IX(d, i, j);
       const int px = cpos(V.x1, t);
-      const T rkj = dk2 * V.dju(i, j);
-      T c1s_o, c1s_e, c2s_o, c2s_s, c1n_o, c1n_e, c2n_o, c2n_s;
-      if constexpr (kFuseConv<T>) {
-        c1s_o = conv_x1_c1(d, V, us, vs, i, j);
-        c1s_e = conv_x1_c1(d, V, us, vs, i + 1, j);
-        c2s_o = conv_x1_c2(d, V, us, vs, i, j);
-        c2s_s = conv_x1_c2(d, V, us, vs, i, j - 1);
-        c1n_o = conv_x1_c1(d, V, un, vn, i, j);
-        c1n_e = conv_x1_c1(d, V, un, vn, i + 1, j);
-        c2n_o = conv_x1_c2(d, V, un, vn, i, j);
-        c2n_s = conv_x1_c2(d, V, un, vn, i, j - 1);
-      } else {
-        c1s_o = V.c1sx[o]; c1s_e = V.c1sx[IX(d, i + 1, j)];
-        c2s_o = V.c2sx[o]; c2s_s = V.c2sx[IX(d, i, j - 1)];
-        c1n_o = V.c1nx[o]; c1n_e = V.c1nx[IX(d, i + 1, j)];
-        c2n_o = V.c2nx[o]; c2n_s = V.c2nx[IX(d, i, j - 1)];
-      }
-      const T cnvs = dconv_u(d, c2s_s, c1s_o, c1s_e, c2s_o, us, i, j);
-      const T cnvn = dconv_u(d, c2n_s, c1n_o, c1n_e, c2n_o, un, i, j);
-      const T difs = ddiff_u(d, V.rac, V.rbc, V.rbn, V.rgn, us, i, j);
-      const T difn = ddiff_u(d, V.rac, V.rbc, V.rbn, V.rgn, un, i, j);
-      const T cj1 = xcj(d, V, us, vs, 1, i, j), racp = V.rac(i + 1, j), rac0 = V.rac(i, j);
-      T a1, a2, a3;
-      if (cj1 >= T(0)) {
-        a1 = rkj * (-xcj(d, V, us, vs, 1, i - 1, j) - re1 * rac0);
-        a2 = T(1.0) + rkj * (cj1 + re1 * (racp + rac0));
-        a3 = rkj * (-re1 * racp);
-      } else {
-        a1 = rkj * (-re1 * rac0);
-        a2 = T(1.0) + rkj * (-cj1 + re1 * (racp + rac0));
-        a3 = rkj * (xcj(d, V, us, vs, 1, i + 1, j) - re1 * racp);
-      }
-      V.x1.a1[px] = a1;
-      V.x1.a2[px] = a2;
-      V.x1.a3[px] = a3;
-      V.x1.b[px] = un[o] - us[o] + rkj * (-cnvs - cnvn) + rkj * re1 * (difs + difn);
+      const ChainRow<T> r = x_row1(d, V, re1, dk2, us, vs, un, vn, t);
+      V.x1.a1[px] = r.a1;
+      V.x1.a2[px] = r.a2;
+      V.x1.a3[px] = r.a3;
+      V.x1.b[px] = r.b;
     } else {
       // Y rows: i = 2..nx, j = 1..ny, ind = (j-1)*(nx-1) + i-2
       const int q = t - nX;
-      const int i = q % (nx - 1) + 2, j = q / (nx - 1) + 1;
-      const size_t o = IX(d, i, j);
       const int py = cpos(V.y1, q);
-      const T rkj = dk2 * V.djv(i, j);
-      T c2s_o, c1s_w, c1s_o, c2s_n, c2n_o, c1n_w, c1n_o, c2n_n;
-      if constexpr (kFuseConv<T>) {
-        c2s_o = conv_y2_c2(d, V, us, vs, i, j);
-        c1s_w = conv_y2_c1(d, V, us, vs, i - 1, j);
-        c1s_o = conv_y2_c1(d, V, us, vs, i, j);
-        c2s_n = conv_y2_c2(d, V, us, vs, i, j + 1);
-        c2n_o = conv_y2_c2(d, V, un, vn, i, j);
-        c1n_w = conv_y2_c1(d, V, un, vn, i - 1, j);
-        c1n_o = conv_y2_c1(d, V, un, vn, i, j);
-        c2n_n = conv_y2_c2(d, V, un, vn, i, j + 1);
-      } else {
-        c2s_o = V.c2sy[o]; c1s_w = V.c1sy[IX(d, i - 1, j)];
-        c1s_o = V.c1sy[o]; c2s_n = V.c2sy[IX(d, i, j + 1)];
-        c2n_o = V.c2ny[o]; c1n_w = V.c1ny[IX(d, i - 1, j)];
-        c1n_o = V.c1ny[o]; c2n_n = V.c2ny[IX(d, i, j + 1)];
-      }
-      const T cnvs = dconv_v(d, c2s_o, c1s_w, c1s_o, c2s_n, vs, i, j);
-      const T cnvn = dconv_v(d, c2n_o, c1n_w, c1n_o, c2n_n, vn, i, j);
-      const T difs = ddiff_v(d, V.ran, V.rbc, V.rbn, V.rgc, vs, i, j);
-      const T difn = ddiff_v(d, V.ran, V.rbc, V.rbn, V.rgc, vn, i, j);
-      const T cj1 = ycj(d, V, us, vs, 1, i, j), ran0 = V.ran(i, j), ranw = V.ran(i - 1, j);
-      T a1, a2, a3;
-      if (cj1 >= T(0)) {
-        a1 = rkj * (-ycj(d, V, us, vs, 1, i - 1, j) - re1 * ranw);
-        a2 = rkj * (cj1 + re1 * (ran0 + ranw)) + T(1.0);
-        a3 = rkj * (-re1 * ran0);
-      } else {
-        a1 = rkj * (-re1 * ranw);
-        a2 = rkj * (-cj1 + re1 * (ran0 + ranw)) + T(1.0);
-        a3 = rkj * (ycj(d, V, us, vs, 1, i + 1, j) - re1 * ran0);
-      }
-      V.y1.a1[py] = a1;
-      V.y1.a2[py] = a2;
-      V.y1.a3[py] = a3;
-      T rhs = vn[o] - vs[o] + rkj * (-cnvs - cnvn) + rkj * re1 * (difs + difn);
-      if constexpr (std::is_same<T, double>::value) {
-        if (d.den) {
-          // buoy = dk (d(i,j+1) + d(i,j) + dn(i,j+1) + dn(i,j)) / (4 fr)
-          const size_t on = IX(d, i, j + 1);
-          const double buoy = dk * (d.den[on] + d.den[o] + d.denn[on] + d.denn[o]) / (4.0 * d.fr);
-          rhs = rhs - buoy;
-        }
-      }
-      V.y1.b[py] = rhs;
+      const ChainRow<T> r = y_row1(d, V, re1, dk2, dk, us, vs, un, vn, q);
+      V.y1.a1[py] = r.a1;
+      V.y1.a2[py] = r.a2;
+      V.y1.a3[py] = r.a3;
+      V.y1.b[py] = r.b;
     }
   }
 }
 
 // ---- M2b: split-2 rows (momentum.f:396-428, 723-754) with identity rows
 // (momentum.f:432-496, 760-821), into the split-1 row storage ------------
+// X row t of split 2; x1 is the split-1 solution, the right-hand side (0 on
+// identity rows).
+template <class T>
+__device__ __forceinline__ ChainRow<T> x_row2(const Dev &d, const MomView<T> &V, T re1, T dk2,
+                                              const T *us, const T *vs, const T *x1, int t) {
+  const int nx = d.nx;
+  const int i = t % nx + 1, j = t / nx + 2;
+  ChainRow<T> r;
+  if (d.mask[IX(d, i, j)] & MK_XID) {
+    r.a1 = T(0); r.a2 = T(1.0); r.a3 = T(0); r.b = T(0);
+    return r;
+  }
+  const T rkj = dk2 * V.dju(i, j);
+  const T cj2 = xcj(d, V, us, vs, 2, i, j), rgn0 = V.rgn(i, j), rgns = V.rgn(i, j - 1);
+  if (cj2 >= T(0)) {
+    r.a1 = rkj * (-xcj(d, V, us, vs, 2, i, j - 1) - re1 * rgns);
+    r.a2 = T(1.0) + rkj * (cj2 + re1 * (rgn0 + rgns));
+    r.a3 = rkj * (-re1 * rgn0);
+  } else {
+    r.a1 = rkj * (-re1 * rgns);
+    r.a2 = T(1.0) + rkj * (-cj2 + re1 * (rgn0 + rgns));
+    r.a3 = rkj * (xcj(d, V, us, vs, 2, i, j + 1) - re1 * rgn0);
+  }
+  r.b = x1 ? x1[cpos(V.x2, t)] : T(0);
+  return r;
+}
+
+template <class T>
+__device__ __forceinline__ ChainRow<T> y_row2(const Dev &d, const MomView<T> &V, T re1, T dk2,
+                                              const T *us, const T *vs, const T *x1, int q) {
+  const int nx = d.nx;
+  const int i = q % (nx - 1) + 2, j = q / (nx - 1) + 1;
+  ChainRow<T> r;
+  if (d.mask[IX(d, i, j)] & MK_YID) {
+    r.a1 = T(0); r.a2 = T(1.0); r.a3 = T(0); r.b = T(0);
+    return r;
+  }
+  const T rkj = dk2 * V.djv(i, j);
+  const T cj2 = ycj(d, V, us, vs, 2, i, j), rgc0 = V.rgc(i, j), rgcn = V.rgc(i, j + 1);
+  if (cj2 >= T(0)) {
+    r.a1 = rkj * (-ycj(d, V, us, vs, 2, i, j - 1) - re1 * rgc0);
+    r.a2 = rkj * (cj2 + re1 * (rgcn + rgc0)) + T(1.0);
+    r.a3 = rkj * (-re1 * rgcn);
+  } else {
+    r.a1 = rkj * (-re1 * rgc0);
+    r.a2 = rkj * (-cj2 + re1 * (rgcn + rgc0)) + T(1.0);
+    r.a3 = rkj * (ycj(d, V, us, vs, 2, i, j + 1) - re1 * rgcn);
+  }
+  r.b = x1 ? x1[cpos(V.y2, q)] : T(0);
+  return r;
+}
+
 template <class T>
 __device__ void mom_assemble2(const Dev &d, const MomView<T> &V, double dk, double re,
                               const T *us, const T *vs) {
@@ -340,55 +415,56 @@ __device__ void mom_assemble2(const Dev &d, const MomView<T> &V, double dk, doub
   const int nX = nx * (ny - 1);
   const int nY = (nx - 1) * ny;
   for (int t = gtid(); t < nX + nY; t += gthreads()) {
-    T a1, a2, a3;
     if (t < nX) {
-      const int i = t % nx + 1, j = t / nx + 2;
       const int px = cpos(V.x2, t);
-      if (d.mask[IX(d, i, j)] & MK_XID) {
-        a1 = T(0); a2 = T(1.0); a3 = T(0);
-        V.x2.b[px] = T(0);  // the split-1 solution, read next only as this rhs
-      } else {
-        const T rkj = dk2 * V.dju(i, j);
-        const T cj2 = xcj(d, V, us, vs, 2, i, j), rgn0 = V.rgn(i, j), rgns = V.rgn(i, j - 1);
-        if (cj2 >= T(0)) {
-          a1 = rkj * (-xcj(d, V, us, vs, 2, i, j - 1) - re1 * rgns);
-          a2 = T(1.0) + rkj * (cj2 + re1 * (rgn0 + rgns));
-          a3 = rkj * (-re1 * rgn0);
-        } else {
-          a1 = rkj * (-re1 * rgns);
-          a2 = T(1.0) + rkj * (-cj2 + re1 * (rgn0 + rgns));
-          a3 = rkj * (xcj(d, V, us, vs, 2, i, j + 1) - re1 * rgn0);
-        }
-      }
-      V.x2.a1[px] = a1;
-      V.x2.a2[px] = a2;
-      V.x2.a3[px] = a3;
+      const ChainRow<T> r = x_row2(d, V, re1, dk2, us, vs, (const T *)nullptr, t);
+      // identity rows: the split-1 solution, read next only as this rhs
+      if (d.mask[IX(d, t % nx + 1, t / nx + 2)] & MK_XID) V.x2.b[px] = T(0);
+      V.x2.a1[px] = r.a1;
+      V.x2.a2[px] = r.a2;
+      V.x2.a3[px] = r.a3;
     } else {
       const int q = t - nX;
-      const int i = q % (nx - 1) + 2, j = q / (nx - 1) + 1;
       const int py = cpos(V.y2, q);
-      if (d.mask[IX(d, i, j)] & MK_YID) {
-        a1 = T(0); a2 = T(1.0); a3 = T(0);
-        V.y2.b[py] = T(0);
-      } else {
-        const T rkj = dk2 * V.djv(i, j);
-        const T cj2 = ycj(d, V, us, vs, 2, i, j), rgc0 = V.rgc(i, j), rgcn = V.rgc(i, j + 1);
-        if (cj2 >= T(0)) {
-          a1 = rkj * (-ycj(d, V, us, vs, 2, i, j - 1) - re1 * rgc0);
-          a2 = rkj * (cj2 + re1 * (rgcn + rgc0)) + T(1.0);
-          a3 = rkj * (-re1 * rgcn);
-        } else {
-          a1 = rkj * (-re1 * rgc0);
-          a2 = rkj * (-cj2 + re1 * (rgcn + rgc0)) + T(1.0);
-          a3 = rkj * (ycj(d, V, us, vs, 2, i, j + 1) - re1 * rgcn);
-        }
-      }
-      V.y2.a1[py] = a1;
-      V.y2.a2[py] = a2;
-      V.y2.a3[py] = a3;
+      const ChainRow<T> r = y_row2(d, V, re1, dk2, us, vs, (const T *)nullptr, q);
+      if (d.mask[IX(d, q % (nx - 1) + 2, q / (nx - 1) + 1)] & MK_YID) V.y2.b[py] = T(0);
+      V.y2.a1[py] = r.a1;
+      V.y2.a2[py] = r.a2;
+      V.y2.a3[py] = r.a3;
     }
   }
 }
+
+// Rows of the split-1 chains (0: X, 1: Y) formed where the chain walks use
+// them: the FP32 path never stores its rows, so the walks read only the
+// fields (cached) and the forward states, and the chains' working set stays
+// small enough for L2.
+template <class T>
+struct Split1Rows {
+  const Dev &d;
+  const MomView<T> &V;
+  T re1, dk2;
+  double dk;
+  const T *us, *vs, *un, *vn;
+  __device__ __forceinline__ ChainRow<T> operator()(int ch, int k) const {
+    return ch == 0 ? x_row1(d, V, re1, dk2, us, vs, un, vn, k)
+                   : y_row1(d, V, re1, dk2, dk, us, vs, un, vn, k);
+  }
+};
+
+// Rows of the split-2 chains; their right-hand side is the split-1
+// solution, read from the split-1 chains' x arrays.
+template <class T>
+struct Split2Rows {
+  const Dev &d;
+  const MomView<T> &V;
+  T re1, dk2;
+  const T *us, *vs;
+  __device__ __forceinline__ ChainRow<T> operator()(int ch, int k) const {
+    return ch == 0 ? x_row2(d, V, re1, dk2, us, vs, V.x1.x, k)
+                   : y_row2(d, V, re1, dk2, us, vs, V.y1.x, k);
+  }
+};
 
 // ---- M4: update and DMaxNorm (momentum.f:171-188, utility.f:479-507) --
 template <class T>
@@ -431,12 +507,22 @@ __device__ bool naux_momentum(const Dev &d, const MomView<T> &V, int mqiter, dou
     if constexpr (!kFuseConv<T>) {
       if (!grid_sync(sy)) return false;
     }
-    mom_assemble1(d, V, dk, re, us, vs, un, vn);
-    if (!grid_sync(sy)) return false;
-    if (!solve_chains(d, V.x1, V.y1, 2)) return false;
-    mom_assemble2(d, V, dk, re, us, vs);
-    if (!grid_sync(sy)) return false;
-    if (!solve_chains(d, V.x2, V.y2, 2)) return false;
+    if constexpr (kFuseConv<T>) {
+      // FP32: the chain walks form their rows (split-2 rows read the split-1
+      // solution, complete after the first solve's last barrier)
+      const T re1 = T(1.0) / T(re), dk2 = T(dk) * T(0.5);
+      const Split1Rows<T> r1{d, V, re1, dk2, dk, us, vs, un, vn};
+      if (!solve_chains_rows(d, V.x1, V.y1, r1)) return false;
+      const Split2Rows<T> r2{d, V, re1, dk2, us, vs};
+      if (!solve_chains_rows(d, V.x2, V.y2, r2)) return false;
+    } else {
+      mom_assemble1(d, V, dk, re, us, vs, un, vn);
+      if (!grid_sync(sy)) return false;
+      if (!solve_chains(d, V.x1, V.y1, 2)) return false;
+      mom_assemble2(d, V, dk, re, us, vs);
+      if (!grid_sync(sy)) return false;
+      if (!solve_chains(d, V.x2, V.y2, 2)) return false;
+    }
     mom_update(d, V, us, vs, &sy->red[it % 3]);
     if (!grid_sync(sy)) return false;
     const double difmax = slot_value(&sy->red[it % 3]);
