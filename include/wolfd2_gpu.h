@@ -334,6 +334,12 @@ int wolfd2gpu_set_precision(w2_ctx *ctx, int precision, int refine_sweeps);
 int wolfd2gpu_tune_mixed(w2_ctx *ctx, int sweeps_per_barrier, int threads,
                          int mode);
 
+/* Staging of the mixed Poisson boxes in the several-tiles-per-block mode
+ * (the 4096 x 1024 channel, ensembles): enable = 1 (default) loads each
+ * tile's boxes with TMA tensor copies, 0 with per-thread vector loads.  The
+ * results are the same bit for bit.  No counterpart in the reference. */
+int wolfd2gpu_set_tma(w2_ctx *ctx, int enable);
+
 /* Device pointers of the resident u, v, p fields and the device leading
  * dimension (elements), for callers that bring their own device buffers. */
 int wolfd2gpu_device_fields(w2_ctx *ctx, double **u, double **v, double **p,

@@ -112,18 +112,21 @@ def test_lid_gradient_reaches_interior_after_two_steps():
         assert gl[i] == pytest.approx(fd, rel=1e-5, abs=100 * np.finfo(float).eps * abs(J) / eps), (i, gl[i], fd)
 
 
-def test_adjoint_matches_reference_finite_differences():
+@pytest.mark.parametrize("n,re,dt,mqiter,msorit,nsteps,every", [(16, 100.0, 0.004, 6, 20, 3, 2),
+                                                                  (64, 400.0, 0.002, 8, 60, 20, 5)])
+def test_adjoint_matches_reference_finite_differences(n, re, dt, mqiter, msorit, nsteps, every):
     """The GPU adjoint against central differences of the CPU reference
     restatement (the oracle, bit-identical to the GPU forward), run step by
-    step with the same frozen counts."""
+    step with the same frozen counts: a 16x16 cavity over 3 steps and a
+    64x64 cavity over 20 steps with checkpoints every 5."""
     import oracle as O
-    case, prm, fields, lid = _setup(16, 100.0, 0.004, 6, 20)
+    case, prm, fields, lid = _setup(n, re, dt, mqiter, msorit)
     case.regions.profiles[(1, 1, NORTH, VAR_U)] = lid
-    w = (1.0 / 16) ** 2
-    nsteps = 3
+    w = (1.0 / n) ** 2
     s = Solver.for_case(case, tuned=False)
     s.load_fields(*fields)
-    J, gu, gv, gp, gl, counts = s.adjoint(prm, nsteps, 2, w, profile=(1, 1, NORTH, VAR_U), nprof=case.nx + 2)
+    J, gu, gv, gp, gl, counts = s.adjoint(prm, nsteps, every, w, profile=(1, 1, NORTH, VAR_U),
+                                          nprof=case.nx + 2)
     s.close()
 
     def ref_J(flds, lidv):

@@ -195,14 +195,17 @@ def test_mixed_non_dyadic_grid_matches_model(n):
     assert _p_rel(p, ref.f["p"], ref.f["u"], ref.f["v"]) <= P_DYN_TOL
 
 
-def test_mixed_multitile_time_loop_matches_model():
-    """Several tiles per block (16 blocks on a 256x256 cavity): the time
-    loop bit-identical to the model."""
+@pytest.mark.parametrize("tma", [True, False])
+def test_mixed_multitile_time_loop_matches_model(tma):
+    """Several tiles per block (16 blocks on a 256x256 cavity), the boxes
+    staged by TMA tensor copies or by vector loads: the time loop
+    bit-identical to the model."""
     case = deck.cavity(256, 1000.0, 0.001, solver="rb_sor")
     u0, v0, p0 = deck.perturbation_ic(case, 7)
     model = M.MixedRun(case, fields={"u": u0, "v": v0, "p": p0}, cold_start=False, inner=48)
     model.step(2)
     s = Solver.for_case(case)
+    s.set_tma(tma)
     s.tune_mixed(8, 512, 2)
     s.load_fields(u0, v0, p0)
     hist = s.step(case.params, 2, precision=PREC_MIXED, refine_sweeps=48)

@@ -5,6 +5,7 @@
 // reference expression operation by operation, so their results are the
 // IEEE-double results of the reference source as written.
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 #include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
@@ -60,9 +61,12 @@ struct w2_ctx {
   size_t tiled_smem = 0;
   TileGeom tg{};
   int use_tiled = 1;
+  int use_tma = 1;        // TMA staging of multi-tile mixed Poisson boxes
   // mixed-precision Poisson sweeps
   float *xbuf = nullptr;  // two exchange buffers of 2 colour planes each
   size_t xbuf_floats = 0;
+  CUtensorMap *d_tm = nullptr;  // TMA maps of the two exchange buffers and r (multi-tile plans)
+  bool tm_ok = false;
   bool mixed_ok = false;
   int mixed_K = 8, mixed_threads = kMixedThreads, mixed_blocks = 0;
   int mixed_mode = 0;  // 0 auto, 1 multi-tile, 2 multi-tile on at most 16 blocks
@@ -118,6 +122,53 @@ struct w2_ctx {
     float *p32 = nullptr;      // device profile or full array, FP32
   } mm[24];
 };
+
+// cuTensorMapEncodeTiled from the driver the runtime uses (no link to
+// libcuda), fetched once.
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+bool w2_encode_plane_map(CUtensorMap *map, const float *base, int gw, int gh, int hw, int bh) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc || !base || ((uintptr_t)base & 15u) || (gw % 4) || (hw % 4) || hw < 4 || hw > 256 || bh < 1 ||
+      bh > 256 || hw > gw || bh > gh)
+    return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)gw, (cuuint64_t)gh, 2};
+  const cuuint64_t strides[2] = {(cuuint64_t)gw * 4, (cuuint64_t)gw * gh * 4};
+  const cuuint32_t box[3] = {(cuuint32_t)hw, (cuuint32_t)bh, 2};
+  const cuuint32_t es[3] = {1, 1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The three maps (exchange buffers 0 and 1, r) of a multi-tile mixed plan
+// over the buffer xb (3 x 2 planes of gh x gw), into dev[0..2].  False when
+// a box breaks the TMA rules.
+static bool encode_mixed_maps(CUtensorMap *dev, const float *xb, const MixedGeom &g, int K, cudaStream_t st) {
+  // a box's x origin (tile column ti * tx/2 floats) must be a multiple of
+  // 16 bytes: tx a multiple of 8, as both planners make it
+  if (g.resident || g.tx % 8 != 0) return false;
+  const size_t plane2 = 2 * (size_t)g.gh * g.gw;
+  const int hw = g.tx / 2 + 2 * K, bh = g.ty + 4 * K;
+  CUtensorMap h[3];
+  for (int k = 0; k < 3; ++k)
+    if (!w2_encode_plane_map(&h[k], xb + k * plane2, g.gw, g.gh, hw, bh)) return false;
+  return cudaMemcpyAsync(dev, h, sizeof h, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+         cudaStreamSynchronize(st) == cudaSuccess;
+}
 
 namespace {
 
@@ -573,9 +624,36 @@ int ensure_f32(w2_ctx *c) {
   if (!c->f32_metrics_ok) {
     std::vector<MRef<float> *> refs = mom_refs(v);
     const int gb = grid_blocks(c);
+    const int W = c->nx + 2, H = c->ny + 2;
+    std::vector<double> h64;
     for (int k = 0; k < 24; ++k) {
       w2_ctx::MomMetric &mm = c->mm[k];
       if (mm.mode == MP_FULL) {
+        // An array that varies only in its last FP64 bits (a uniform grid
+        // whose spacing is not a power of two) can be constant along i or j
+        // once rounded to FP32: the FP32 view then reads a profile of the
+        // rounded values, which are the values it would read in full.
+        if (h64.size() != c->nf) h64.resize(c->nf);
+        CK(cudaStreamSynchronize(c->st));
+        CK(cudaMemcpy(h64.data(), c->met[kMomMetric[k]], c->nf * sizeof(double), cudaMemcpyDeviceToHost));
+        auto f32 = [&](int i, int j) { return (float)h64[(size_t)i + (size_t)j * c->ld]; };
+        bool ionly = true, jonly = true;
+        for (int j = 0; j < H && (ionly || jonly); ++j)
+          for (int i = 0; i < W; ++i) {
+            const float x = f32(i, j), xi = f32(i, 0), xj = f32(0, j);
+            if (ionly && memcmp(&x, &xi, 4) != 0) ionly = false;
+            if (jonly && memcmp(&x, &xj, 4) != 0) jonly = false;
+          }
+        if (ionly || jonly) {
+          const int len = ionly ? W : H;
+          std::vector<float> h(len);
+          for (int q = 0; q < len; ++q) h[q] = ionly ? f32(q, 0) : f32(0, q);
+          if (!(mm.p32 = dalloc<float>(c, std::max(W, H))))
+            return fail(c, W2_E_CUDA, "out of device memory (FP32 metrics)");
+          CK(cudaMemcpy(mm.p32, h.data(), len * sizeof(float), cudaMemcpyHostToDevice));
+          *refs[k] = ionly ? MRef<float>{mm.p32, 1, 0} : MRef<float>{mm.p32, 0, 1};
+          continue;
+        }
         if (!mm.p32 && !(mm.p32 = dalloc<float>(c, c->nf)))
           return fail(c, W2_E_CUDA, "out of device memory (FP32 metrics)");
         k_to_f32<<<gb, c->threads, 0, c->st>>>(d, c->met[kMomMetric[k]], mm.p32);
@@ -752,6 +830,12 @@ void plan_mixed(w2_ctx *c) {
     c->xbuf_floats = need;
   }
   if (cudaMemset(c->xbuf, 0, c->xbuf_floats * sizeof(float)) != cudaSuccess) c->mixed_ok = false;
+  // multi-tile plans stage their boxes with TMA when the maps can be made
+  c->tm_ok = false;
+  if (c->mixed_ok && !c->mg.resident && c->use_tma) {
+    if (!c->d_tm) c->d_tm = dalloc<CUtensorMap>(c, 3);
+    c->tm_ok = c->d_tm && encode_mixed_maps(c->d_tm, c->xbuf, c->mg, c->mixed_K, c->st);
+  }
 }
 
 // The mixed path covers npsolver 5/6 on Cartesian grids whose rows are all
@@ -778,7 +862,7 @@ int launch_ppe_mixed(w2_ctx *c, int lcartes, int msorit, double dk, double sorto
   MixedGeom g = c->mg;
   const size_t plane2 = 2 * (size_t)c->mg.gh * c->mg.gw;
   MixedArgs a{lcartes, msorit, auto_inner(c, inner), dk, sortol, (float)sorrel, u, v, p,
-              c->xbuf, c->xbuf + plane2, c->xbuf + 2 * plane2};
+              c->xbuf, c->xbuf + plane2, c->xbuf + 2 * plane2, c->tm_ok ? c->d_tm : nullptr};
   void *args[] = {&d, &g, &a, &out};
   c->launches++;
   const int T = mixed_threads(c->mixed_K, g.tx, g.ty);
@@ -1070,6 +1154,13 @@ int wolfd2gpu_tune_mixed(w2_ctx *c, int sweeps_per_barrier, int threads, int mod
     return fail(c, W2_E_ARG, "thread limit must be a multiple of 32 in 64..%d", kMixedThreads);
   if (sweeps_per_barrier) c->mixed_K = sweeps_per_barrier;
   if (threads) c->mixed_threads = threads;
+  if (c->metrics_ok) plan_mixed(c);
+  return W2_OK;
+}
+
+int wolfd2gpu_set_tma(w2_ctx *c, int enable) {
+  if (!c) return W2_E_ARG;
+  c->use_tma = enable ? 1 : 0;
   if (c->metrics_ok) plan_mixed(c);
   return W2_OK;
 }
@@ -1926,6 +2017,7 @@ struct w2_ens {
   std::vector<void *> allocs;
   std::vector<EnsCase> h;
   EnsCase *d_cases = nullptr;
+  CUtensorMap *d_tm = nullptr;  // 3 TMA maps per case (multi-tile Poisson boxes)
   int *d_first_m = nullptr, *d_first_p = nullptr, *d_first_1 = nullptr, *d_step = nullptr;
   std::vector<int> bm, bp;  // blocks per case: momentum/tail launches, Poisson launch
   int blocks_m = 0, blocks_p = 0;
@@ -2271,6 +2363,12 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
     float *xb = nullptr;
     if (e->mixed_ok && !(xb = ealloc<float>(e, 3 * plane2)))
       return bad(efail(e, W2_E_CUDA, "out of device memory (case %d Poisson buffers)", k));
+    const CUtensorMap *tm = nullptr;
+    if (e->mixed_ok && c->use_tma) {
+      if (!e->d_tm && !(e->d_tm = ealloc<CUtensorMap>(e, 3 * (size_t)n)))
+        return bad(efail(e, W2_E_CUDA, "out of device memory (tensor maps)"));
+      if (encode_mixed_maps(e->d_tm + 3 * k, xb, g, e->K, c->st)) tm = e->d_tm + 3 * k;
+    }
     h.d = c->dev;
     chain_views(h.d, c->nx, c->ny, (long)e->bm[k] * threads, c->seg_req, c->warm_req);
     for (int b = 0; b < 2; ++b) {
@@ -2284,6 +2382,7 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
       h.a[b].xbuf0 = xb;
       h.a[b].xbuf1 = xb + plane2;
       h.a[b].rbuf = xb + 2 * plane2;
+      h.a[b].tm = tm;
     }
     for (int q = 0; q < 4; ++q) h.F32[q] = c->F32[q];
   }

@@ -376,13 +376,32 @@ __device__ bool chain_b2(const ChainT<T> &c, int s, int L, const T *ein, T *eout
 // of block 0 walks the chain in chunks of 32 rows, the lanes staging each
 // chunk's coefficients through shared memory and lane 0 running the
 // recurrence (same arithmetic as fwd_row / the back substitution).
+// The guard walk gives up after kGuardLimitNs, well inside the other blocks'
+// barrier wait (kWaitLimitNs): it sets W2_E_FALLBACK, which those blocks see
+// while they wait, so a chain too long to walk in time ends the launch with
+// that status instead of a barrier timeout.
+constexpr unsigned long long kGuardLimitNs = 1000000000ull;
+
+// true (on every lane) once the guard walk started at t0 is out of time;
+// the first lane to see it sets W2_E_FALLBACK.
+__device__ __forceinline__ bool guard_out_of_time(Sync *sy, unsigned long long t0) {
+  int late = 0;
+  if ((threadIdx.x & 31) == 0 && gtime_ns() - t0 > kGuardLimitNs) {
+    set_error(sy, W2_E_FALLBACK);
+    late = 1;
+  }
+  return __shfl_sync(0xffffffffu, late, 0) != 0;
+}
+
 template <class T>
-__device__ void chain_sequential_warp(const ChainT<T> &c, bool forward) {
+__device__ void chain_sequential_warp(const ChainT<T> &c, bool forward, Sync *sy) {
   __shared__ T s1[32], s2[32], s3[32], sb[32], o3[32], ob[32];
   const int lane = threadIdx.x & 31;
+  const unsigned long long t0 = gtime_ns();
   if (forward) {
     T a3p = T(0), bp = T(0);
     for (int base = 0; base < c.n; base += 32) {
+      if (guard_out_of_time(sy, t0)) return;
       const int k = base + lane, cnt = min(32, c.n - base);
       const int p = k < c.n ? cpos(c, k) : 0;
       if (k < c.n) {
@@ -419,6 +438,7 @@ __device__ void chain_sequential_warp(const ChainT<T> &c, bool forward) {
   } else {
     T xn = T(0);
     for (int top = c.n - 1; top >= 0; top -= 32) {
+      if (guard_out_of_time(sy, t0)) return;
       const int k = top - lane, cnt = min(32, top + 1);
       const int p = k >= 0 ? cpos(c, k) : 0;
       if (k >= 0) {
@@ -501,11 +521,11 @@ __device__ bool solve_chains(const Dev &d, const ChainT<T> &c0, const ChainT<T> 
     if (vblock() == 0 && threadIdx.x < 32) {
       // copies: the guard walk must not take the address of parameter space
       const ChainT<T> t0 = c0, t1 = c1;
-      chain_sequential_warp(t0, true);
-      chain_sequential_warp(t0, false);
+      chain_sequential_warp(t0, true, sy);
+      chain_sequential_warp(t0, false, sy);
       if (nchains > 1) {
-        chain_sequential_warp(t1, true);
-        chain_sequential_warp(t1, false);
+        chain_sequential_warp(t1, true, sy);
+        chain_sequential_warp(t1, false, sy);
       }
       if (threadIdx.x == 0) atomicAdd(&sy->fallback, 1);
     }
@@ -548,8 +568,8 @@ __device__ bool solve_chains(const Dev &d, const ChainT<T> &c0, const ChainT<T> 
     if (vblock() == 0 && threadIdx.x < 32) {
       // forward values are exact here; redo the back substitution serially
       const ChainT<T> t0 = c0, t1 = c1;
-      chain_sequential_warp(t0, false);
-      if (nchains > 1) chain_sequential_warp(t1, false);
+      chain_sequential_warp(t0, false, sy);
+      if (nchains > 1) chain_sequential_warp(t1, false, sy);
       if (threadIdx.x == 0) atomicAdd(&sy->fallback, 1);
     }
     if (!grid_sync(sy)) return false;
@@ -638,13 +658,18 @@ __device__ bool chain_f2_rows(const ChainT<T> &c, int ch, int s, int L, const T 
 // Guard walk for chains with a row source: lane 0 of warp 0 of block 0
 // runs the forward recurrence over the whole chain.
 template <class T, class Rows>
-__device__ void chain_sequential_rows(const ChainT<T> &c, int ch, const Rows &rows) {
+__device__ void chain_sequential_rows(const ChainT<T> &c, int ch, const Rows &rows, Sync *sy) {
   if ((threadIdx.x & 31) != 0) return;
+  const unsigned long long t0 = gtime_ns();
   T a3p, bp;
   fwd_first<T>(rows, ch, a3p, bp);
   c.a3p[0] = a3p;
   c.bp[0] = bp;
   for (int k = 1; k < c.n; ++k) {
+    if ((k & 255) == 0 && gtime_ns() - t0 > kGuardLimitNs) {
+      set_error(sy, W2_E_FALLBACK);
+      return;
+    }
     fwd_step(rows(ch, k), k == c.n - 1, a3p, bp);
     const int p = cpos(c, k);
     c.a3p[p] = a3p;
@@ -698,11 +723,11 @@ __device__ bool solve_chains_rows(const Dev &d, const ChainT<T> &c0, const Chain
   if (!settled) {
     if (vblock() == 0 && threadIdx.x < 32) {
       const ChainT<T> t0 = c0, t1 = c1;
-      chain_sequential_rows(t0, 0, rows);
-      chain_sequential_rows(t1, 1, rows);
+      chain_sequential_rows(t0, 0, rows, sy);
+      chain_sequential_rows(t1, 1, rows, sy);
       __syncwarp();
-      chain_sequential_warp(t0, false);
-      chain_sequential_warp(t1, false);
+      chain_sequential_warp(t0, false, sy);
+      chain_sequential_warp(t1, false, sy);
       if (threadIdx.x == 0) atomicAdd(&sy->fallback, 1);
     }
     if (!grid_sync(sy)) return false;
@@ -743,8 +768,8 @@ __device__ bool solve_chains_rows(const Dev &d, const ChainT<T> &c0, const Chain
   if (!settled) {
     if (vblock() == 0 && threadIdx.x < 32) {
       const ChainT<T> t0 = c0, t1 = c1;
-      chain_sequential_warp(t0, false);
-      chain_sequential_warp(t1, false);
+      chain_sequential_warp(t0, false, sy);
+      chain_sequential_warp(t1, false, sy);
       if (threadIdx.x == 0) atomicAdd(&sy->fallback, 1);
     }
     if (!grid_sync(sy)) return false;

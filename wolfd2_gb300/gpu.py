@@ -124,6 +124,7 @@ def lib():
     L.wolfd2gpu_tune.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
     L.wolfd2gpu_tune_mixed.argtypes = [vp, C.c_int, C.c_int, C.c_int]
     L.wolfd2gpu_set_precision.argtypes = [vp, C.c_int, C.c_int]
+    L.wolfd2gpu_set_tma.argtypes = [vp, C.c_int]
     L.wolfd2gpu_set_face_profile.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_int]
     L.wolfd2gpu_device_fields.argtypes = [vp, C.POINTER(_dp), C.POINTER(_dp), C.POINTER(_dp), _ip]
     L.wolfd2gpu_launch_count.argtypes = [vp]
@@ -267,6 +268,11 @@ class Solver:
         the block-size limit (0 keeps the current value), and the tile mode
         (0 auto, 1 several tiles per block, 2 the same on <= 16 blocks)."""
         self._check(self.L.wolfd2gpu_tune_mixed(self.h, sweeps_per_barrier, threads, mode))
+
+    def set_tma(self, enable: bool = True):
+        """TMA staging of the mixed Poisson boxes in the several-tiles-per-
+        block mode (default on; off: vector loads, same results)."""
+        self._check(self.L.wolfd2gpu_set_tma(self.h, 1 if enable else 0))
 
     def set_face_profile(self, ireg: int, jreg: int, face: int, var: int, values=None):
         """Per-position inlet / moving-wall values on one region face (var 1 =
