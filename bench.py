@@ -519,6 +519,8 @@ def run_ours(args):
         args.precision = "fp64"  # the loop with the energy equation is plain FP64
         t0 = make_t0(case)
     s = Solver.for_case(case)
+    if args.no_tma:
+        s.set_tma(False)
     if args.threads or args.blocks_per_sm or args.seg or args.warm:
         s.tune(seg=args.seg, warm=args.warm, threads=args.threads, blocks_per_sm=args.blocks_per_sm)
     if args.mixed_k or args.mixed_threads:
@@ -873,6 +875,8 @@ def run_ensemble(args):
     for i in mine:
         c = members[i].case
         s = Solver.for_case(c, tuned=False)
+        if args.no_tma:
+            s.set_tma(False)
         ic = deck.perturbation_ic(c, args.seed + i)
         s.load_fields(*ic)
         solvers.append(s)
@@ -1019,6 +1023,8 @@ def main():
     ap.add_argument("--ens-seed", type=int, default=ENSEMBLE["seed"])
     ap.add_argument("--no-graph", action="store_true", help="ensemble: launch directly, no CUDA graph")
     ap.add_argument("--ens-threads", type=int, default=0, help="ensemble: threads per block (0: library default)")
+    ap.add_argument("--no-tma", action="store_true",
+                    help="stage the several-tiles-per-block Poisson boxes with vector loads, not TMA")
     ap.add_argument("--adj-steps", type=int, default=ADJOINT["steps"], help="adjoint: steps of the horizon")
     ap.add_argument("--adj-case", choices=["cavity", "channel"], default="cavity",
                     help="adjoint: the 256x256 cavity (lid profile) or the profiled channel (inflow profile)")

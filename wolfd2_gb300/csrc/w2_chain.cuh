@@ -577,204 +577,4 @@ __device__ bool solve_chains(const Dev &d, const ChainT<T> &c0, const ChainT<T> 
   return true;
 }
 
-// ---- chains whose rows are formed where they are used ---------------------
-// The same solve as solve_chains with the rows taken from a source rows(ch,
-// k) (ch 0: the first chain, 1: the second) instead of the a1, a2, a3, b
-// arrays: the forward walks (F1, F2, the guard walk) form each row when they
-// reach it, so no row is stored or re-read.  Every row value is the one the
-// assembly would have stored, so the solution is the same bit for bit.
-
-template <class T>
-__device__ __forceinline__ void fwd_step(const ChainRow<T> &r, bool last, T &a3p, T &bp) {
-  const T a2p = r.a2 - r.a1 * a3p;
-  const T nb = (r.b - r.a1 * bp) / a2p;
-  a3p = last ? T(0) : r.a3 / a2p;
-  bp = nb;
-}
-
-// Row 0 with the first-row quirk: a3' = a3(0) / a2(1), b' = b(0) / a2(0).
-template <class T, class Rows>
-__device__ __forceinline__ void fwd_first(const Rows &rows, int ch, T &a3p, T &bp) {
-  const ChainRow<T> r0 = rows(ch, 0), r1 = rows(ch, 1);
-  a3p = r0.a3 / r1.a2;
-  bp = r0.b / r0.a2;
-}
-
-template <class T, class Rows>
-__device__ void chain_f1_rows(const ChainT<T> &c, int ch, int s, int L, int W, const Rows &rows) {
-  const int k0 = s * L, k1 = min(c.n, k0 + L), ns = c.nseg;
-  T a3p, bp;
-  int k = k0;
-  if (k0 == 0) {
-    fwd_first<T>(rows, ch, a3p, bp);
-    c.a3p[0] = a3p;
-    c.bp[0] = bp;
-    k = 1;
-  } else {
-    int kw = k0 - W;
-    if (kw <= 0) {
-      fwd_first<T>(rows, ch, a3p, bp);
-      kw = 1;
-    } else {
-      a3p = T(0);
-      bp = T(0);
-    }
-    for (int q = kw; q < k0; ++q) fwd_step(rows(ch, q), q == c.n - 1, a3p, bp);
-  }
-  for (int p = (k - k0) * ns + s; k < k1; ++k, p += ns) {
-    fwd_step(rows(ch, k), k == c.n - 1, a3p, bp);
-    c.a3p[p] = a3p;
-    c.bp[p] = bp;
-  }
-  c.ef[2 * s] = a3p;
-  c.ef[2 * s + 1] = bp;
-}
-
-template <class T, class Rows>
-__device__ bool chain_f2_rows(const ChainT<T> &c, int ch, int s, int L, const T *ein, T *eout,
-                              const Rows &rows) {
-  if (s == 0) {
-    eout[0] = ein[0];
-    eout[1] = ein[1];
-    return false;
-  }
-  const int k0 = s * L, k1 = min(c.n, k0 + L), ns = c.nseg;
-  T a3p = ein[2 * (s - 1)], bp = ein[2 * (s - 1) + 1];
-  for (int k = k0, p = s; k < k1; ++k, p += ns) {
-    fwd_step(rows(ch, k), k == c.n - 1, a3p, bp);
-    if (same_state(a3p, c.a3p[p]) && same_state(bp, c.bp[p])) {
-      eout[2 * s] = ein[2 * s];
-      eout[2 * s + 1] = ein[2 * s + 1];
-      return false;
-    }
-    c.a3p[p] = a3p;
-    c.bp[p] = bp;
-  }
-  eout[2 * s] = a3p;
-  eout[2 * s + 1] = bp;
-  return true;
-}
-
-// Guard walk for chains with a row source: lane 0 of warp 0 of block 0
-// runs the forward recurrence over the whole chain.
-template <class T, class Rows>
-__device__ void chain_sequential_rows(const ChainT<T> &c, int ch, const Rows &rows, Sync *sy) {
-  if ((threadIdx.x & 31) != 0) return;
-  const unsigned long long t0 = gtime_ns();
-  T a3p, bp;
-  fwd_first<T>(rows, ch, a3p, bp);
-  c.a3p[0] = a3p;
-  c.bp[0] = bp;
-  for (int k = 1; k < c.n; ++k) {
-    if ((k & 255) == 0 && gtime_ns() - t0 > kGuardLimitNs) {
-      set_error(sy, W2_E_FALLBACK);
-      return;
-    }
-    fwd_step(rows(ch, k), k == c.n - 1, a3p, bp);
-    const int p = cpos(c, k);
-    c.a3p[p] = a3p;
-    c.bp[p] = bp;
-  }
-}
-
-template <class T, class Rows>
-__device__ bool solve_chains_rows(const Dev &d, const ChainT<T> &c0, const ChainT<T> &c1,
-                                  const Rows &rows) {
-  Sync *sy = d.sync;
-  const int L = d.seg, W = d.warm;
-  const int nseg0 = c0.nseg, nseg1 = c1.nseg;
-  const int nsegt = nseg0 + nseg1;
-  const int nrounds = max_rounds(nseg0, nseg1);
-  // ---- F1
-  for (int g = gtid(); g < nsegt; g += gthreads()) {
-    if (g < nseg0) chain_f1_rows(c0, 0, g, L, W, rows);
-    else chain_f1_rows(c1, 1, g - nseg0, L, W, rows);
-  }
-  // ---- F2 rounds
-  int cur = 0;
-  bool settled = false;
-  for (int round = 0; round < nrounds; ++round) {
-    if (vblock() == 0 && threadIdx.x == 0) {
-      if (round == 0) sy->iout[0] = 0;
-      sy->iout[(round + 1) % 3] = 0;
-    }
-    if (!grid_sync(sy)) return false;
-    int any = 0;
-    for (int g = gtid(); g < nsegt; g += gthreads()) {
-      if (g < nseg0) {
-        if (chain_f2_rows(c0, 0, g, L, ef_buf(c0, cur), const_cast<T *>(ef_buf(c0, cur ^ 1)), rows)) any = 1;
-      } else {
-        if (chain_f2_rows(c1, 1, g - nseg0, L, ef_buf(c1, cur), const_cast<T *>(ef_buf(c1, cur ^ 1)), rows))
-          any = 1;
-      }
-    }
-    if (any) atomicOr(&sy->iout[round % 3], 1);
-    if (!grid_sync(sy)) return false;
-    int chg = cuda::atomic_ref<int, cuda::thread_scope_device>(sy->iout[round % 3])
-                  .load(cuda::memory_order_acquire);
-    cur ^= 1;
-    if (!chg) {
-      settled = true;
-      if (vblock() == 0 && threadIdx.x == 0) atomicMax(&sy->max_rounds, round + 1);
-      break;
-    }
-  }
-  if (vblock() == 0 && threadIdx.x == 0 && !settled) atomicMax(&sy->max_rounds, nrounds + 1);
-  if (!settled) {
-    if (vblock() == 0 && threadIdx.x < 32) {
-      const ChainT<T> t0 = c0, t1 = c1;
-      chain_sequential_rows(t0, 0, rows, sy);
-      chain_sequential_rows(t1, 1, rows, sy);
-      __syncwarp();
-      chain_sequential_warp(t0, false, sy);
-      chain_sequential_warp(t1, false, sy);
-      if (threadIdx.x == 0) atomicAdd(&sy->fallback, 1);
-    }
-    if (!grid_sync(sy)) return false;
-    return true;
-  }
-  // ---- B1, B2: the back substitution reads only a3', b'
-  for (int g = gtid(); g < nsegt; g += gthreads()) {
-    if (g < nseg0) chain_b1(c0, g, L, W, const_cast<T *>(eb_buf(c0, 0)));
-    else chain_b1(c1, g - nseg0, L, W, const_cast<T *>(eb_buf(c1, 0)));
-  }
-  cur = 0;
-  settled = false;
-  for (int round = 0; round < nrounds; ++round) {
-    if (vblock() == 0 && threadIdx.x == 0) {
-      if (round == 0) sy->iout[3] = 0;
-      sy->iout[3 + (round + 1) % 3] = 0;
-    }
-    if (!grid_sync(sy)) return false;
-    int any = 0;
-    for (int g = gtid(); g < nsegt; g += gthreads()) {
-      if (g < nseg0) {
-        if (chain_b2(c0, g, L, eb_buf(c0, cur), const_cast<T *>(eb_buf(c0, cur ^ 1)))) any = 1;
-      } else {
-        if (chain_b2(c1, g - nseg0, L, eb_buf(c1, cur), const_cast<T *>(eb_buf(c1, cur ^ 1)))) any = 1;
-      }
-    }
-    if (any) atomicOr(&sy->iout[3 + round % 3], 1);
-    if (!grid_sync(sy)) return false;
-    int chg = cuda::atomic_ref<int, cuda::thread_scope_device>(sy->iout[3 + round % 3])
-                  .load(cuda::memory_order_acquire);
-    cur ^= 1;
-    if (!chg) {
-      settled = true;
-      if (vblock() == 0 && threadIdx.x == 0) atomicMax(&sy->max_rounds, round + 1);
-      break;
-    }
-  }
-  if (!settled) {
-    if (vblock() == 0 && threadIdx.x < 32) {
-      const ChainT<T> t0 = c0, t1 = c1;
-      chain_sequential_warp(t0, false, sy);
-      chain_sequential_warp(t1, false, sy);
-      if (threadIdx.x == 0) atomicAdd(&sy->fallback, 1);
-    }
-    if (!grid_sync(sy)) return false;
-  }
-  return true;
-}
-
 }  // namespace w2

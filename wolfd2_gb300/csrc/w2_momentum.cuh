@@ -355,11 +355,11 @@ __device__ void mom_assemble1(const Dev &d, const MomView<T> &V, double dk, doub
 
 // ---- M2b: split-2 rows (momentum.f:396-428, 723-754) with identity rows
 // (momentum.f:432-496, 760-821), into the split-1 row storage ------------
-// X row t of split 2; x1 is the split-1 solution, the right-hand side (0 on
-// identity rows).
+// X row t of split 2 (its right-hand side, the split-1 solution, stays in
+// place; b is left 0).
 template <class T>
 __device__ __forceinline__ ChainRow<T> x_row2(const Dev &d, const MomView<T> &V, T re1, T dk2,
-                                              const T *us, const T *vs, const T *x1, int t) {
+                                              const T *us, const T *vs, int t) {
   const int nx = d.nx;
   const int i = t % nx + 1, j = t / nx + 2;
   ChainRow<T> r;
@@ -378,13 +378,13 @@ __device__ __forceinline__ ChainRow<T> x_row2(const Dev &d, const MomView<T> &V,
     r.a2 = T(1.0) + rkj * (-cj2 + re1 * (rgn0 + rgns));
     r.a3 = rkj * (xcj(d, V, us, vs, 2, i, j + 1) - re1 * rgn0);
   }
-  r.b = x1 ? x1[cpos(V.x2, t)] : T(0);
+  r.b = T(0);
   return r;
 }
 
 template <class T>
 __device__ __forceinline__ ChainRow<T> y_row2(const Dev &d, const MomView<T> &V, T re1, T dk2,
-                                              const T *us, const T *vs, const T *x1, int q) {
+                                              const T *us, const T *vs, int q) {
   const int nx = d.nx;
   const int i = q % (nx - 1) + 2, j = q / (nx - 1) + 1;
   ChainRow<T> r;
@@ -403,7 +403,7 @@ __device__ __forceinline__ ChainRow<T> y_row2(const Dev &d, const MomView<T> &V,
     r.a2 = rkj * (-cj2 + re1 * (rgcn + rgc0)) + T(1.0);
     r.a3 = rkj * (ycj(d, V, us, vs, 2, i, j + 1) - re1 * rgcn);
   }
-  r.b = x1 ? x1[cpos(V.y2, q)] : T(0);
+  r.b = T(0);
   return r;
 }
 
@@ -417,7 +417,7 @@ __device__ void mom_assemble2(const Dev &d, const MomView<T> &V, double dk, doub
   for (int t = gtid(); t < nX + nY; t += gthreads()) {
     if (t < nX) {
       const int px = cpos(V.x2, t);
-      const ChainRow<T> r = x_row2(d, V, re1, dk2, us, vs, (const T *)nullptr, t);
+      const ChainRow<T> r = x_row2(d, V, re1, dk2, us, vs, t);
       // identity rows: the split-1 solution, read next only as this rhs
       if (d.mask[IX(d, t % nx + 1, t / nx + 2)] & MK_XID) V.x2.b[px] = T(0);
       V.x2.a1[px] = r.a1;
@@ -426,7 +426,7 @@ __device__ void mom_assemble2(const Dev &d, const MomView<T> &V, double dk, doub
     } else {
       const int q = t - nX;
       const int py = cpos(V.y2, q);
-      const ChainRow<T> r = y_row2(d, V, re1, dk2, us, vs, (const T *)nullptr, q);
+      const ChainRow<T> r = y_row2(d, V, re1, dk2, us, vs, q);
       if (d.mask[IX(d, q % (nx - 1) + 2, q / (nx - 1) + 1)] & MK_YID) V.y2.b[py] = T(0);
       V.y2.a1[py] = r.a1;
       V.y2.a2[py] = r.a2;
@@ -434,37 +434,6 @@ __device__ void mom_assemble2(const Dev &d, const MomView<T> &V, double dk, doub
     }
   }
 }
-
-// Rows of the split-1 chains (0: X, 1: Y) formed where the chain walks use
-// them: the FP32 path never stores its rows, so the walks read only the
-// fields (cached) and the forward states, and the chains' working set stays
-// small enough for L2.
-template <class T>
-struct Split1Rows {
-  const Dev &d;
-  const MomView<T> &V;
-  T re1, dk2;
-  double dk;
-  const T *us, *vs, *un, *vn;
-  __device__ __forceinline__ ChainRow<T> operator()(int ch, int k) const {
-    return ch == 0 ? x_row1(d, V, re1, dk2, us, vs, un, vn, k)
-                   : y_row1(d, V, re1, dk2, dk, us, vs, un, vn, k);
-  }
-};
-
-// Rows of the split-2 chains; their right-hand side is the split-1
-// solution, read from the split-1 chains' x arrays.
-template <class T>
-struct Split2Rows {
-  const Dev &d;
-  const MomView<T> &V;
-  T re1, dk2;
-  const T *us, *vs;
-  __device__ __forceinline__ ChainRow<T> operator()(int ch, int k) const {
-    return ch == 0 ? x_row2(d, V, re1, dk2, us, vs, V.x1.x, k)
-                   : y_row2(d, V, re1, dk2, us, vs, V.y1.x, k);
-  }
-};
 
 // ---- M4: update and DMaxNorm (momentum.f:171-188, utility.f:479-507) --
 template <class T>
@@ -507,22 +476,12 @@ __device__ bool naux_momentum(const Dev &d, const MomView<T> &V, int mqiter, dou
     if constexpr (!kFuseConv<T>) {
       if (!grid_sync(sy)) return false;
     }
-    if constexpr (kFuseConv<T>) {
-      // FP32: the chain walks form their rows (split-2 rows read the split-1
-      // solution, complete after the first solve's last barrier)
-      const T re1 = T(1.0) / T(re), dk2 = T(dk) * T(0.5);
-      const Split1Rows<T> r1{d, V, re1, dk2, dk, us, vs, un, vn};
-      if (!solve_chains_rows(d, V.x1, V.y1, r1)) return false;
-      const Split2Rows<T> r2{d, V, re1, dk2, us, vs};
-      if (!solve_chains_rows(d, V.x2, V.y2, r2)) return false;
-    } else {
-      mom_assemble1(d, V, dk, re, us, vs, un, vn);
-      if (!grid_sync(sy)) return false;
-      if (!solve_chains(d, V.x1, V.y1, 2)) return false;
-      mom_assemble2(d, V, dk, re, us, vs);
-      if (!grid_sync(sy)) return false;
-      if (!solve_chains(d, V.x2, V.y2, 2)) return false;
-    }
+    mom_assemble1(d, V, dk, re, us, vs, un, vn);
+    if (!grid_sync(sy)) return false;
+    if (!solve_chains(d, V.x1, V.y1, 2)) return false;
+    mom_assemble2(d, V, dk, re, us, vs);
+    if (!grid_sync(sy)) return false;
+    if (!solve_chains(d, V.x2, V.y2, 2)) return false;
     mom_update(d, V, us, vs, &sy->red[it % 3]);
     if (!grid_sync(sy)) return false;
     const double difmax = slot_value(&sy->red[it % 3]);

@@ -22,15 +22,15 @@
 // north/south neighbours are the other plane's column k one row up or down.
 //
 // Registers.  Thread (k, s) owns column k of both planes over the rows of
-// strip s (kMixedRows rows) and holds both columns in registers for a whole
-// group of sweeps.  A half-sweep of colour c walks the strip's rows:
-// north/south come from the registers of the other plane (from shared
-// memory at the strip's first and last row), the column neighbour from the
-// adjacent lane by one warp shuffle whose direction is the row's parity
-// (uniform across the warp; shared memory for the lanes at a warp's edge),
-// the point's own value from the registers.  Updates are written through to
-// the shared-memory planes, which are what other warps read and what the
-// halo exchange moves.  Half-sweep h (1-based within a group) updates the points
+// strip s (kMixedRows rows).  A half-sweep of colour c first reads the
+// strip's column of the other plane into registers, then walks its rows:
+// north/south come from those registers (from shared memory at the strip's
+// first and last row), the
+// column neighbour from the adjacent lane by one warp shuffle whose
+// direction is the row's parity (uniform across the warp; shared memory for
+// the lanes at a warp's edge).  Updates are written through to the
+// shared-memory planes, which are what other threads read and what the halo
+// exchange moves.  Half-sweep h (1-based within a group) updates the points
 // whose distance to the box frame is at least h: the frame keeps its
 // group-start values, so after h half-sweeps only points closer than h to it
 // can be stale, and after 2K half-sweeps the tile (distance >= H) is exactly
@@ -109,39 +109,13 @@ __device__ __forceinline__ A &pick(A &a0, A &a1) {
   else return a1;
 }
 
-// The e values of a thread's strip column, both colour planes, held in
-// registers across the half-sweeps of a group: a half-sweep reads its own
-// column of the other plane and the values it updates from here, not from
-// shared memory.
-struct MixedCol {
-  float e[2][kMixedRows];
-};
-
-// The strip column of both planes from shared memory (rows and columns that
-// exist in the box; the rest read as 0 and are never used).
-__device__ __forceinline__ void mixed_col_load(const MixedBox &b, MixedCol &cv) {
-  const int hw = b.hw, base = b.jj0 * hw + b.k;
-  const int nr = min(kMixedRows, b.bh - b.jj0);
-  const bool col = b.k < hw;
-#pragma unroll
-  for (int r = 0; r < kMixedRows; ++r) {
-    const bool in = col && r < nr;
-    cv.e[0][r] = in ? b.E[0][base + r * hw] : 0.0f;
-    cv.e[1][r] = in ? b.E[1][base + r * hw] : 0.0f;
-  }
-}
-
 // The rows of a half-sweep of colour C for a strip whose first row has
-// parity P0 (so row r has parity P0 ^ (r & 1), known once unrolled).  The
-// other plane's column comes from the registers (cv), the column
-// neighbour from the adjacent lane by one warp shuffle (shared memory for
-// the lanes at a warp's edge), the north/south neighbour from the
-// registers (shared memory at the strip's first and last row).  Updates go
-// to the registers and through to the shared-memory plane, which is what
-// other warps and strips read after the block barrier.
+// parity P0 (so row r has parity P0 ^ (r & 1), known once unrolled).  eo
+// holds the strip's column of the other plane, read from shared memory at
+// the start of the half-sweep.
 template <int K, int C, int P0>
-__device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, MixedCol &cv, unsigned int amask,
-                                                   bool act0, bool act1, float relax) {
+__device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, unsigned int amask, bool act0,
+                                                   bool act1, float relax) {
   // A strip wholly below the box (a block with more threads than its tile
   // plan needs, as in ensemble launches) has nothing to do and must not
   // load: its rows lie past the shared planes.  Uniform per warp (a strip
@@ -151,13 +125,16 @@ __device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, MixedCol &
   float *Ec = b.E[C];
   const float *Eo = b.E[C ^ 1];
   const int hw = b.hw, base = b.jj0 * hw + b.k;
+  float eo[kMixedRows];
+#pragma unroll
+  for (int r = 0; r < kMixedRows; ++r) eo[r] = Eo[base + r * hw];
   unsigned int mx = 0u;
 #pragma unroll
   for (int r = 0; r < kMixedRows; ++r) {
     if (!((amask >> r) & 1u)) continue;   // same for the whole warp
     const int par = P0 ^ (r & 1);         // folded once the loop is unrolled
     const int o = base + r * hw;
-    const float other = cv.e[C ^ 1][r];
+    const float other = eo[r];
     float nb;
     if (par == 0) {
       nb = __shfl_up_sync(0xffffffffu, other, 1);
@@ -167,15 +144,13 @@ __device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, MixedCol &
       if (b.eedge) nb = Eo[o + 1];
     }
     const float w = par ? other : nb, e = par ? nb : other;
-    const float s = (r == 0) ? Eo[o - hw] : cv.e[C ^ 1][r > 0 ? r - 1 : 0];
-    const float n = (r == kMixedRows - 1) ? Eo[o + hw] : cv.e[C ^ 1][r < kMixedRows - 1 ? r + 1 : r];
-    const float c0 = cv.e[C][r];
+    const float s = (r == 0) ? Eo[o - hw] : eo[r > 0 ? r - 1 : 0];
+    const float n = (r == kMixedRows - 1) ? Eo[o + hw] : eo[r < kMixedRows - 1 ? r + 1 : r];
+    const float c0 = Ec[o];
     float sum = Rc[o] - s - w - e - n;
     sum = sum * -0.25f - c0;
     if (par ? act1 : act0) {
-      const float nv = c0 + relax * sum;
-      cv.e[C][r] = nv;
-      Ec[o] = nv;
+      Ec[o] = c0 + relax * sum;
       if (((b.orow >> r) & 1u) && (par ? b.own1 : b.own0)) {
         const unsigned int bb = __float_as_uint(fabsf(sum));
         mx = bb > mx ? bb : mx;
@@ -188,30 +163,27 @@ __device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, MixedCol &
 // Half-sweep h of colour C over the thread's strip; returns the max |delta|
 // over own points (distance >= H) as FP32 bits.
 template <int K, int C>
-__device__ __forceinline__ unsigned int mixed_half_sweep(const MixedBox &b, MixedCol &cv, int h, float relax) {
+__device__ __forceinline__ unsigned int mixed_half_sweep(const MixedBox &b, int h, float relax) {
   const bool act0 = b.dcol0 >= h, act1 = b.dcol1 >= h;
   // rows at distance >= h from the frame: r in [h - jj0, bh - 1 - h - jj0]
   const int lo = max(0, h - b.jj0), hi = min(kMixedRows - 1, b.bh - 1 - h - b.jj0);
   unsigned int amask = 0u;
   if (hi >= lo) amask = ((2u << hi) - 1u) & ~((1u << lo) - 1u);
   amask &= b.vrow;
-  if ((C + b.gj0 + b.jj0) & 1) return mixed_rows<K, C, 1>(b, cv, amask, act0, act1, relax);
-  return mixed_rows<K, C, 0>(b, cv, amask, act0, act1, relax);
+  if ((C + b.gj0 + b.jj0) & 1) return mixed_rows<K, C, 1>(b, amask, act0, act1, relax);
+  return mixed_rows<K, C, 0>(b, amask, act0, act1, relax);
 }
 
-// ns (<= K) sweeps from the shared planes (the caller has synchronised the
-// block after filling them).  With redm, each warp keeps its running maximum
-// of sweep s in redm[s][warp] (zeroed by the caller).
+// ns (<= K) sweeps.  With redm, each warp keeps its running maximum of
+// sweep s in redm[s][warp] (zeroed by the caller).
 template <int K>
 __device__ __forceinline__ void mixed_sweeps(const MixedBox &b, int ns, float relax,
                                              unsigned int (*redm)[32]) {
-  MixedCol cv;
-  mixed_col_load(b, cv);
 #pragma unroll 1
   for (int s = 0; s < ns; ++s) {
-    const unsigned int m0 = mixed_half_sweep<K, 0>(b, cv, 2 * s + 1, relax);
+    const unsigned int m0 = mixed_half_sweep<K, 0>(b, 2 * s + 1, relax);
     __syncthreads();
-    const unsigned int m1 = mixed_half_sweep<K, 1>(b, cv, 2 * s + 2, relax);
+    const unsigned int m1 = mixed_half_sweep<K, 1>(b, 2 * s + 2, relax);
     if (redm) {
       const unsigned int m = m0 > m1 ? m0 : m1;
       const unsigned int v = __reduce_max_sync(0xffffffffu, m);
@@ -575,11 +547,15 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
 
   extern __shared__ double smem[];
   __shared__ unsigned int redm[K][32];
-  __shared__ unsigned long long tbar;  // completion of the TMA box loads
+  __shared__ unsigned long long tbar;  // completion of the TMA box loads (multi-tile mode)
   unsigned tphase = 0u;
-  float *fs = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smem) + 127) & ~(uintptr_t)127);
-  if (!RES && a.tm && threadIdx.x == 0) mbar_init(&tbar, 1);
-  __syncthreads();
+  float *fs = reinterpret_cast<float *>(smem);
+  if constexpr (!RES) {
+    // TMA destinations start on 128-byte boundaries
+    fs = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smem) + 127) & ~(uintptr_t)127);
+    if (a.tm && threadIdx.x == 0) mbar_init(&tbar, 1);
+    __syncthreads();
+  }
   const int ntiles = g.ntx * g.nty;
   constexpr bool resident = RES;
   const bool has = vblock() < ntiles;
