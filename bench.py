@@ -523,8 +523,8 @@ def run_ours(args):
         s.set_tma(False)
     if args.threads or args.blocks_per_sm or args.seg or args.warm:
         s.tune(seg=args.seg, warm=args.warm, threads=args.threads, blocks_per_sm=args.blocks_per_sm)
-    if args.mixed_k or args.mixed_threads:
-        s.tune_mixed(args.mixed_k, args.mixed_threads)
+    if args.mixed_k or args.mixed_threads or args.mixed_mode:
+        s.tune_mixed(args.mixed_k, args.mixed_threads, args.mixed_mode)
     inner = args.refine_sweeps or s.refine_sweeps or 16 * (args.mixed_k or 8)
     args.refine_sweeps = inner
     prm = case.params
@@ -1058,6 +1058,8 @@ def main():
                     help="mixed: FP32 sweeps per refinement pass (0: 16 x sweeps per barrier)")
     ap.add_argument("--mixed-k", type=int, default=0, help="mixed: sweeps per grid barrier (4/8)")
     ap.add_argument("--mixed-threads", type=int, default=0, help="mixed: threads per block")
+    ap.add_argument("--mixed-mode", type=int, default=0,
+                    help="mixed: tile mode (0 auto, 1 several tiles per block, 3 two resident blocks per SM)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -66,7 +66,9 @@ extern "C" {
 #define W2_PREC_MIXED 1   /* red/black Poisson sweeps in FP32 on the
                              correction equation, FP64 residual and
                              correction (iterative refinement); npsolver 5
-                             or 6 on Cartesian unit-stencil grids         */
+                             or 6 on Cartesian grids whose Poisson rows
+                             round to the unit stencil in FP32 (uniform
+                             square cells, no blockages)                 */
 
 typedef struct w2_ctx w2_ctx;
 
@@ -330,7 +332,8 @@ int wolfd2gpu_set_precision(w2_ctx *ctx, int precision, int refine_sweeps);
  * (64..512 threads; 0 keeps the current value), and the tile mode: 0 = one
  * tile per block when the grid allows it, else several tiles per block;
  * 1 = always several tiles per block; 2 = the same on at most 16 blocks
- * (a test shape).  Tiles are re-planned. */
+ * (a test shape); 3 = one tile per block, two blocks per SM (at most 256
+ * threads each).  Tiles are re-planned. */
 int wolfd2gpu_tune_mixed(w2_ctx *ctx, int sweeps_per_barrier, int threads,
                          int mode);
 

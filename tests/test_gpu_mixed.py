@@ -56,11 +56,12 @@ def _inputs(case, seed, amp=0.05):
 @pytest.mark.parametrize("sortol,msorit", [(1e-8, 301), (1e-8, 300), (2e-6, 2000), (7e-7, 2000),
                                            (3e-7, 2000)])
 @pytest.mark.parametrize("K,threads,mode", [(8, 512, 0), (4, 256, 0), (8, 128, 0), (8, 512, 2),
-                                            (4, 256, 1)])
+                                            (4, 256, 1), (8, 256, 3), (4, 256, 3)])
 def test_mixed_ppe_matches_model(sortol, msorit, K, threads, mode):
     """Drop-in Ppe in mixed mode: bit-identical to the model for stopping
     points on every sweep of a group and for odd/even msorit, with one tile
-    per block (mode 0) and with several tiles per block (modes 1, 2)."""
+    per block (mode 0; mode 3 two such blocks per SM) and with several tiles
+    per block (modes 1, 2)."""
     case = deck.cavity(128, 400.0, 0.002, solver="rb_sor", ny=64)
     o, met, u, v, p = _inputs(case, 11)
     inner = 24

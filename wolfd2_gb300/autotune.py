@@ -32,7 +32,7 @@ CHAIN_SEG = (0, 16, 32, 48, 128, 512)   # 0: the library's default (rows / threa
 CHAIN_WARM = (24, 48, 64)
 MIXED_K = (4, 8)
 MIXED_THREADS = (256, 384, 512)
-MIXED_MODE = (0, 1)               # 0: resident tiles when they fit, 1: multi-tile
+MIXED_MODE = (0, 1, 3)            # 0: resident tiles when they fit, 1: multi-tile, 3: two resident tiles per SM
 REFINE = (64, 128, 256)
 
 

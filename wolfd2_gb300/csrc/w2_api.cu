@@ -69,7 +69,8 @@ struct w2_ctx {
   bool tm_ok = false;
   bool mixed_ok = false;
   int mixed_K = 8, mixed_threads = kMixedThreads, mixed_blocks = 0;
-  int mixed_mode = 0;  // 0 auto, 1 multi-tile, 2 multi-tile on at most 16 blocks
+  int mixed_mode = 0;  // 0 auto, 1 multi-tile, 2 multi-tile on at most 16 blocks,
+                       // 3 one tile per block with two blocks per SM
   size_t mixed_smem = 0;
   MixedGeom mg{};
   int prec_dropin = W2_PREC_FP64, refine_dropin = 0;
@@ -765,8 +766,12 @@ void plan_mixed(w2_ctx *c) {
   cudaDeviceGetAttribute(&maxsmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
   const int NX = c->nx - 1, NY = c->ny - 1, H = 2 * K;
   auto sweep_work = [&](int tx, int ty) { return mixed_sweep_work(K, tx, ty); };
-  for (int pass = c->mixed_mode ? 1 : 0; pass < 2 && !c->mixed_ok; ++pass) {
+  for (int pass = (c->mixed_mode == 1 || c->mixed_mode == 2) ? 1 : 0; pass < 2 && !c->mixed_ok; ++pass) {
     const bool resident = pass == 0;
+    // mode 3: resident tiles two to an SM (at most 256 threads each, so the
+    // two blocks' 128-register threads fit one SM's register file)
+    const int per_sm = (resident && c->mixed_mode == 3) ? 2 : 1;
+    const int tmax = per_sm == 2 ? std::min(c->mixed_threads, 256) : c->mixed_threads;
     const void *kf = mixed_kernel(K, resident);
     cudaFuncAttributes fa{};
     if (cudaFuncGetAttributes(&fa, kf) != cudaSuccess || (size_t)maxsmem <= fa.sharedSizeBytes) continue;
@@ -779,14 +784,20 @@ void plan_mixed(w2_ctx *c) {
       tx = (tx + 7) / 8 * 8;
       if ((NX + tx - 1) / tx != ntx) continue;
       for (int nty = 1; nty <= std::max(1, NY / 4); ++nty) {
-        if (resident && ntx * nty > c->nsm) break;
+        if (resident && ntx * nty > per_sm * c->nsm) break;
         const int ty = (NY + nty - 1) / nty;
         if ((NY + ty - 1) / ty != nty) continue;
         const size_t smem = mixed_smem_bytes(K, tx, ty, resident);
         const int T = mixed_threads(K, tx, ty);
-        if (smem > limit || T > c->mixed_threads) continue;
+        if (smem > limit || T > tmax) continue;
         double cost = sweep_work(tx, ty);
         int blocks = c->nsm;
+        if (per_sm == 2) {
+          int occ = 0;
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kf, T, smem);
+          if (occ < 2) continue;
+          blocks = 2 * c->nsm;
+        }
         if (!resident) {
           int occ = 0;
           cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kf, T, smem);
@@ -1146,7 +1157,7 @@ int wolfd2gpu_set_precision(w2_ctx *c, int precision, int refine_sweeps) {
 
 int wolfd2gpu_tune_mixed(w2_ctx *c, int sweeps_per_barrier, int threads, int mode) {
   if (!c) return W2_E_ARG;
-  if (mode < 0 || mode > 2) return fail(c, W2_E_ARG, "tile mode must be 0, 1 or 2");
+  if (mode < 0 || mode > 3) return fail(c, W2_E_ARG, "tile mode must be 0, 1, 2 or 3");
   c->mixed_mode = mode;
   if (sweeps_per_barrier != 0 && !mixed_kernel(sweeps_per_barrier, true))
     return fail(c, W2_E_ARG, "sweeps per barrier must be 4 or 8");

@@ -266,7 +266,8 @@ class Solver:
     def tune_mixed(self, sweeps_per_barrier: int = 0, threads: int = 0, mode: int = 0):
         """Mixed Poisson kernel shape: sweeps between grid barriers (4, 8),
         the block-size limit (0 keeps the current value), and the tile mode
-        (0 auto, 1 several tiles per block, 2 the same on <= 16 blocks)."""
+        (0 auto, 1 several tiles per block, 2 the same on <= 16 blocks, 3 one
+        tile per block with two blocks per SM)."""
         self._check(self.L.wolfd2gpu_tune_mixed(self.h, sweeps_per_barrier, threads, mode))
 
     def set_tma(self, enable: bool = True):
