@@ -350,11 +350,12 @@ __device__ __forceinline__ void mixed_redo(const MixedBox &b, int ns, float rela
 
 // Bytes of dynamic shared memory for a tile of tx x ty unknowns: the two
 // colour planes of e and of r, and (resident mode) the snapshot of e.
-// 256 bytes more cover the 128-byte alignment of the planes' base and of
-// the r planes (TMA destinations).
+// Multi-tile mode: the r planes start on a 128-byte boundary (a TMA
+// destination), after the e planes rounded up to 32 floats.
+__host__ __device__ inline size_t mixed_r_offset(size_t plane) { return (2 * plane + 31) & ~(size_t)31; }
 __host__ __device__ inline size_t mixed_smem_bytes(int K, int tx, int ty, bool resident = true) {
-  const size_t bw = (size_t)tx + 4 * K, bh = (size_t)ty + 4 * K;
-  return (resident ? 6 : 4) * bh * (bw / 2) * sizeof(float) + 256;
+  const size_t bw = (size_t)tx + 4 * K, bh = (size_t)ty + 4 * K, plane = bh * (bw / 2);
+  return (resident ? 6 * plane : mixed_r_offset(plane) + 2 * plane) * sizeof(float);
 }
 
 // Threads of a block for a tile of tx x ty unknowns: whole warps over the
@@ -391,8 +392,7 @@ __device__ __forceinline__ void mixed_setup(const Dev &d, const MixedGeom &g, Mi
     b.R[0] = fs + 4 * plane;
     b.R[1] = fs + 5 * plane;
   } else {
-    // the r planes start on a 128-byte boundary (a TMA destination)
-    const int r0 = (2 * plane + 31) & ~31;
+    const int r0 = (int)mixed_r_offset((size_t)plane);
     b.E0[0] = b.E0[1] = nullptr;
     b.R[0] = fs + r0;
     b.R[1] = fs + r0 + plane;
@@ -500,9 +500,9 @@ __device__ __forceinline__ void mixed_flush_maxima(unsigned int (*redm)[32], int
 // ran out its time limit (the error is set).
 template <int K>
 __device__ __forceinline__ bool mixed_stage(const MixedGeom &g, const MixedBox &b, const MixedArgs &a,
-                                            const float *ein, unsigned long long *bar, unsigned &phase,
-                                            Sync *sy) {
-  if (!a.tm) {
+                                            bool tma, const float *ein, unsigned long long *bar,
+                                            unsigned &phase, Sync *sy) {
+  if (!tma) {
     mixed_box_load<K>(g, b, ein, b.E[0], b.E[1]);
     mixed_box_load<K>(g, b, a.rbuf, b.R[0], b.R[1]);
     __syncthreads();
@@ -545,15 +545,17 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
   ppe_rhs_grid(d, a.lcartes, a.dk, a.p);
   if (!grid_sync(sy)) return -1;
 
-  extern __shared__ double smem[];
+  extern __shared__ __align__(128) double smem[];
   __shared__ unsigned int redm[K][32];
   __shared__ unsigned long long tbar;  // completion of the TMA box loads (multi-tile mode)
   unsigned tphase = 0u;
   float *fs = reinterpret_cast<float *>(smem);
+  // TMA destinations must start on 128-byte boundaries: the declaration
+  // asks for that alignment of the dynamic base; should a base ever lack
+  // it, the boxes are staged with vector loads instead
+  const bool tma = !RES && a.tm && (smem_addr(smem) & 127u) == 0u;
   if constexpr (!RES) {
-    // TMA destinations start on 128-byte boundaries
-    fs = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smem) + 127) & ~(uintptr_t)127);
-    if (a.tm && threadIdx.x == 0) mbar_init(&tbar, 1);
+    if (tma && threadIdx.x == 0) mbar_init(&tbar, 1);
     __syncthreads();
   }
   const int ntiles = g.ntx * g.nty;
@@ -592,7 +594,7 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
         for (int t = threadIdx.x; t < K * 32; t += blockDim.x) redm[t / 32][t % 32] = 0u;
         for (int tile = vblock(); tile < ntiles; tile += vblocks()) {
           mixed_setup<K>(d, g, b, tile, fs, false);
-          if (!mixed_stage<K>(g, b, a, ein, &tbar, tphase, sy)) return -1;
+          if (!mixed_stage<K>(g, b, a, tma, ein, &tbar, tphase, sy)) return -1;
           mixed_sweeps<K>(b, ns, a.relax, redm);
           mixed_tile_store<K>(g, b, eout);
           __syncthreads();
@@ -619,7 +621,7 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
             // the group's input buffer is intact: sweep again from it
             for (int tile = vblock(); tile < ntiles; tile += vblocks()) {
               mixed_setup<K>(d, g, b, tile, fs, false);
-              if (!mixed_stage<K>(g, b, a, ein, &tbar, tphase, sy)) return -1;
+              if (!mixed_stage<K>(g, b, a, tma, ein, &tbar, tphase, sy)) return -1;
               mixed_sweeps<K>(b, conv + 1, a.relax, nullptr);
               mixed_tile_store<K>(g, b, eout);
               __syncthreads();
