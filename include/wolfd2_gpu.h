@@ -182,6 +182,31 @@ int wolfd2gpu_eq_state(w2_ctx *ctx, const int *nx, const int *ny,
                        const double *rconst, const double *p, const double *t,
                        double *den);
 
+/* SmallScale, src/small_scale.f:31-49 (Additive Turbulent Decomposition):
+ * the small-scale fields uss, vss, pss, tss, updated in place, from the
+ * large-scale u1, v1, t1 (all (0:mnx,0:mny) host arrays); arguments in the
+ * reference's order without the region tables, dBCVal and metrics (the ones
+ * given to wolfd2gpu_create and uploaded); fp is fp(1..4) of the reference
+ * (u, v, unused, t).  The map iterates and cell areas persist in the
+ * context between calls, as the reference keeps them (SAVE); initflg <= 0
+ * seeds them (and zeroes uss, vss, tss), initflg < 0 returns after that.
+ * nSorConv (no counterpart in the reference's argument list) receives the
+ * small-scale Ppe's count.  pow, tanh and atanh are CUDA's, an ulp or so
+ * from the host's, and the chaotic maps amplify such differences.  An
+ * outlet on the grid's edge, where the reference's SmlSclBC would write
+ * outside its arrays, returns W2_E_UNSUPPORTED. */
+int wolfd2gpu_small_scale(w2_ctx *ctx, const int *nx, const int *ny, const int *initflg,
+                          const int *nthermen, const int *lCartesGrid, const int *nTRgType,
+                          const int *nTemBdTp, const int *nPpeSolver, const int *msorit,
+                          const double *dlref, const double *uref, const double *tref,
+                          const double *tmax, const double *dka, const double *re,
+                          const double *pe, const double *sortol, const double *sorrel,
+                          const double *fp, const double *cu0, const double *TsCoef,
+                          const double *HsCoef, const double *TemCoef, const double *bnumc,
+                          const double *rmax, const double *rlc, const double *dTRgVal,
+                          const double *u1, const double *v1, const double *t1, double *uss,
+                          double *vss, double *pss, double *tss, int *nSorConv);
+
 /* ---- Device-resident time loop ---------------------------------------- */
 
 /* Thermal switches and constants of the time loop (ReadParam, parse.f:118-159;
@@ -307,7 +332,9 @@ const char *wolfd2gpu_last_error(w2_ctx *ctx);
 /* Library configuration knobs (segment length and warm-up of the chain
  * recurrence, threads per block, blocks per SM); 0 keeps the default.
  * blocks_per_sm = -1 selects the one-colour-per-barrier red/black sweep,
- * -2 forces the tiled two-sweeps-per-barrier form at any grid size.
+ * -2 forces the tiled two-sweeps-per-barrier form at any grid size, -3 runs
+ * that form in 1024-thread blocks (two points in flight per thread instead
+ * of four in 512-thread blocks), -4 returns to 512-thread blocks.
  * Takes effect on the next launch. */
 int wolfd2gpu_tune(w2_ctx *ctx, int chain_seg, int chain_warm, int threads,
                    int blocks_per_sm);

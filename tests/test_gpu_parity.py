@@ -216,17 +216,21 @@ def test_time_loop_with_velocity_filter(case):
         assert np.array_equal(g, ref.f[name]), (name, rel_err(g, ref.f[name]))
 
 
+@pytest.mark.parametrize("wide", [False, True])
 @pytest.mark.parametrize("sorrel", [1.0, 1.9])
 @pytest.mark.parametrize("sortol", [1e-8, 3e-6, 1e-5, 2e-5])
 @pytest.mark.parametrize("msorit", [301, 300])
-def test_tiled_red_black_sweeps(sortol, msorit, sorrel):
+def test_tiled_red_black_sweeps(sortol, msorit, sorrel, wide):
     """Two sweeps per barrier on shared-memory tiles (forced on a small
     grid): bit-identical p and nSorConv for stopping points on either sweep
-    of a pair, for odd and even msorit, with and without over-relaxation."""
+    of a pair, for odd and even msorit, with and without over-relaxation, in
+    512- and 1024-thread blocks."""
     case = deck.cavity(128, 400.0, 0.002, solver="rb_sor", ny=64)
     o, met = oracle_setup(case)
     s = Solver.for_case(case)
     s.tune(blocks_per_sm=-2)
+    if wide:
+        s.tune(blocks_per_sm=-3)   # 1024-thread blocks
     f = fields_for(case, 9, amp=0.05)
     u, v = f["u"], f["v"]
     p = f["p"].copy(order="F")

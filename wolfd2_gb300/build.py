@@ -43,7 +43,7 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
         return LIB
     os.makedirs(LIBDIR, exist_ok=True)
     tmp = LIB + ".tmp"
-    cmd = [_nvcc(), "-O3", "-std=c++17", *ARCH, "-lineinfo", "--fmad=false",
+    cmd = [_nvcc(), "-O3", "-std=c++17", *ARCH, "-lineinfo", "--fmad=false", "-Xcompiler", "-ffp-contract=off",
            "-Xcompiler", "-fPIC", "-shared", "-o", tmp,
            os.path.join(CSRC, "w2_api.cu"), os.path.join(CSRC, "w2_noalloc.cu")]
     if verbose:

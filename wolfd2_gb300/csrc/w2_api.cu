@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "w2_adjoint.cuh"
+#include "w2_atd.cuh"
 #include "w2_ensemble.cuh"
 #include "w2_thermal.cuh"
 
@@ -39,6 +40,8 @@ struct w2_ctx {
   double *U[2] = {}, *V[2] = {}, *P[2] = {};
   int cur = 0;
   double *stage[6] = {};  // drop-in staging: a, b, c, d, e, f
+  AtdState atd{};         // SmallScale's saved state (allocated on its first call)
+  double *atd_io[4] = {}; // SmallScale's uss, vss, pss, tss on the device
   StepOut *d_out = nullptr;
   StepOut *h_out = nullptr;  // pinned
   int threads = 256, blocks_per_sm = 2, seg_req = 0, warm_req = 0;
@@ -58,6 +61,7 @@ struct w2_ctx {
   // tiled red/black sweeps
   bool tiled_ok = false;
   int tiled_blocks = 0, tiled_threads = 512;
+  int tiled_wide = 0;     // 1024-thread blocks, two points in flight per thread
   size_t tiled_smem = 0;
   TileGeom tg{};
   int use_tiled = 1;
@@ -533,12 +537,17 @@ int launch_naux(w2_ctx *c, int mqiter, double dk, double re, double qtol, const 
 // Tile geometry for the tiled red/black kernel: ntx*nty = k * blocks tiles
 // (k as small as the shared-memory limit allows), choosing the split with
 // the least redundant halo work per block.
+const void *tiled_kernel(const w2_ctx *c) {
+  return c->tiled_wide ? (const void *)k_ppe_tiled_w : (const void *)k_ppe_tiled;
+}
+
 void plan_tiles(w2_ctx *c) {
   c->tiled_ok = false;
+  c->tiled_threads = c->tiled_wide ? 1024 : 512;
   int dev = c->device, maxsmem = 0;
   cudaDeviceGetAttribute(&maxsmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const size_t limit = (size_t)maxsmem - 4096;  // leave room for static shared arrays
-  if (cudaFuncSetAttribute((const void *)k_ppe_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (cudaFuncSetAttribute(tiled_kernel(c), cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)limit) != cudaSuccess)
     return;
   const int NX = c->nx - 1, NY = c->ny - 1;
@@ -567,7 +576,7 @@ void plan_tiles(w2_ctx *c) {
   }
   if (best >= 1e300) return;
   int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void *)k_ppe_tiled, c->tiled_threads,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, tiled_kernel(c), c->tiled_threads,
                                                 c->tiled_smem);
   if (occ < 1) return;
   c->tiled_blocks = c->nsm;  // one block per SM, each owning ntiles/nsm tiles
@@ -590,7 +599,7 @@ int launch_ppe_tiled(w2_ctx *c, int lcartes, int msorit, double dk, double sorto
   TileGeom g = c->tg;
   void *args[] = {&d, &g, &lcartes, &msorit, &dk, &sortol, &sorrel, (void *)&u, (void *)&v, &p, &out};
   c->launches++;
-  cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_ppe_tiled, dim3(c->tiled_blocks),
+  cudaError_t e = cudaLaunchCooperativeKernel(tiled_kernel(c), dim3(c->tiled_blocks),
                                               dim3(c->tiled_threads), args, c->tiled_smem, c->st);
   if (e != cudaSuccess) return fail(c, W2_E_CUDA, "tiled PPE launch: %s", cudaGetErrorString(e));
   return W2_OK;
@@ -1081,6 +1090,11 @@ int wolfd2gpu_tune(w2_ctx *c, int chain_seg, int chain_warm, int threads, int bl
     // -1: one colour per barrier for red/black SOR; -2: tiled sweeps at any size
     c->use_tiled = blocks_per_sm == -1 ? 0 : 2;
     blocks_per_sm = 0;
+  } else if (blocks_per_sm == -3 || blocks_per_sm == -4) {
+    // tiled sweeps in 1024-thread blocks (-3) or back to 512-thread blocks (-4)
+    c->tiled_wide = blocks_per_sm == -3 ? 1 : 0;
+    blocks_per_sm = 0;
+    if (c->metrics_ok) plan_tiles(c);
   }
   if (chain_seg < 0 || chain_warm < 0 || threads < 0 || blocks_per_sm < -2) return W2_E_ARG;
   if (chain_seg > 0 && chain_seg < 8) return fail(c, W2_E_ARG, "chain segment length must be >= 8");
@@ -1498,6 +1512,124 @@ int wolfd2gpu_filter_t(w2_ctx *c, const int *nx, const int *ny, const int *nTRgT
   CK(cudaGetLastError());
   if ((rc = copy_out(c, t, dh))) return rc;
   return check_sync(c);
+}
+
+int wolfd2gpu_small_scale(w2_ctx *c, const int *nx, const int *ny, const int *initflg,
+                          const int *nthermen, const int *lCartesGrid, const int *nTRgType,
+                          const int *nTemBdTp, const int *nPpeSolver, const int *msorit,
+                          const double *dlref, const double *uref, const double *tref,
+                          const double *tmax, const double *dka, const double *re, const double *pe,
+                          const double *sortol, const double *sorrel, const double *fp,
+                          const double *cu0, const double *TsCoef, const double *HsCoef,
+                          const double *TemCoef, const double *bnumc, const double *rmax,
+                          const double *rlc, const double *dTRgVal, const double *u1, const double *v1,
+                          const double *t1, double *uss, double *vss, double *pss, double *tss,
+                          int *nSorConv) {
+  (void)nthermen;  // the reference passes it and does not use it
+  int rc = ready(c);
+  if (rc) return rc;
+  if (!dims_match(c, nx, ny) || !initflg || !lCartesGrid || !nTRgType || !nTemBdTp || !nPpeSolver ||
+      !msorit || !dlref || !uref || !tref || !tmax || !dka || !re || !pe || !sortol || !sorrel || !fp ||
+      !cu0 || !TsCoef || !HsCoef || !TemCoef || !bnumc || !rmax || !rlc || !dTRgVal || !u1 || !v1 || !t1 ||
+      !uss || !vss || !pss || !tss || !nSorConv)
+    return fail(c, W2_E_ARG, "bad argument");
+  if (*nPpeSolver < 1 || *nPpeSolver > 6) return fail(c, W2_E_ARG, "nPpeSolver must be 1..6");
+  ThermTables tt;
+  if ((rc = therm_prepare(c, nTRgType, nTemBdTp, dTRgVal, nullptr, &tt))) return rc;
+  AtdState &S = c->atd;
+  if (!S.area) {
+    double **arr[] = {&S.area, &S.xz, &S.xe, &S.yz, &S.ye, &S.rj, &S.ul, &S.vl, &S.tl,
+                      &S.uc, &S.vc, &S.uf, &S.vf, &S.tf, &S.ff};
+    for (double **a : arr)
+      if (!(*a = dalloc<double>(c, c->nf))) return fail(c, W2_E_CUDA, "out of device memory (small scales)");
+    for (int l = 0; l < 9; ++l)
+      if (!(S.map[l] = dalloc<double>(c, c->nf))) return fail(c, W2_E_CUDA, "out of device memory (maps)");
+    for (int k = 0; k < 4; ++k)
+      if (!(c->atd_io[k] = dalloc<double>(c, c->nf))) return fail(c, W2_E_CUDA, "out of device memory");
+    if (!(S.tarea = dalloc<double>(c, 1))) return fail(c, W2_E_CUDA, "out of device memory");
+  }
+  double *dus = c->atd_io[0], *dvs = c->atd_io[1], *dps = c->atd_io[2], *dts = c->atd_io[3];
+  const int NX = c->nx, NY = c->ny;
+  const size_t ld = c->ld;
+  if (*initflg <= 0) {
+    // small_scale.f:198-243 on the host: the maps are seeded along one
+    // sequential chain (j fastest), the areas summed in the reference's order
+    const double rc0 = 0.20710678119, A = 4.82842712474, B = 1.47839783948;
+    double um = 0.92, vm = 0.31, tm = 0.50;
+    std::vector<double> h(9 * c->nf, 0.0);
+    for (int i = 0; i <= NX + 1; i++)
+      for (int j = 0; j <= NY + 1; j++)
+        for (int l = 0; l < 3; l++) {
+          um = rc0 * A * um * (1.0 - B * std::fabs(um));
+          vm = rc0 * A * vm * (1.0 - B * std::fabs(vm));
+          tm = rc0 * A * tm * (1.0 - B * std::fabs(tm));
+          const size_t o = (size_t)i + (size_t)j * ld;
+          h[(size_t)l * c->nf + o] = um;
+          h[(size_t)(3 + l) * c->nf + o] = vm;
+          h[(size_t)(6 + l) * c->nf + o] = tm;
+        }
+    for (int l = 0; l < 9; ++l)
+      CK(cudaMemcpy(S.map[l], h.data() + (size_t)l * c->nf, c->nf * sizeof(double), cudaMemcpyHostToDevice));
+    std::vector<double> djc(c->nf), area(c->nf, 0.0);
+    CK(cudaStreamSynchronize(c->st));
+    CK(cudaMemcpy(djc.data(), c->met[M_DJC], c->nf * sizeof(double), cudaMemcpyDeviceToHost));
+    double tarea = 0.0;
+    for (int i = 1; i <= NX; i++)
+      for (int j = 1; j <= NY; j++) {
+        const size_t o = (size_t)i + (size_t)j * ld;
+        area[o] = 1.0 / djc[o];
+        tarea = tarea + area[o];
+      }
+    CK(cudaMemcpy(S.area, area.data(), c->nf * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(S.tarea, &tarea, sizeof(double), cudaMemcpyHostToDevice));
+    for (size_t k = 0; k < (size_t)(c->mnx + 1) * (size_t)(c->mny + 1); ++k) {
+      const size_t i = k % (size_t)(c->mnx + 1), j = k / (size_t)(c->mnx + 1);
+      if (i <= (size_t)NX + 1 && j <= (size_t)NY + 1) uss[k] = vss[k] = tss[k] = 0.0;
+    }
+    if (*initflg < 0) {
+      *nSorConv = 0;
+      return W2_OK;
+    }
+  }
+  const AtdParams P{*dlref, *uref, *tref, *tmax, *dka, *re, *pe, fp[0], fp[1], fp[3],
+                    *cu0, *TsCoef, *HsCoef, *TemCoef, *bnumc, *rmax, *rlc};
+  double *d1 = c->stage[0], *d2 = c->stage[1], *d3 = c->stage[2];
+  if ((rc = copy_in(c, d1, u1)) || (rc = copy_in(c, d2, v1)) || (rc = copy_in(c, d3, t1)) ||
+      (rc = copy_in(c, dus, uss)) || (rc = copy_in(c, dvs, vss)) || (rc = copy_in(c, dps, pss)) ||
+      (rc = copy_in(c, dts, tss)))
+    return rc;
+  const Dev &d = c->dev;
+  const int gb = grid_blocks(c), T = c->threads;
+  cudaStream_t st = c->st;
+  c->launches += 13;
+  k_atd_prep<<<gb, T, 0, st>>>(d, S, P, d1, d2, d3);
+  k_temp_bc<<<1, T, 0, st>>>(d, tt, S.tf);
+  // the high-pass parts: the field minus its Shuman-filtered copy
+  k_filter<<<gb, T, 0, st>>>(d, MK_FU, P.fpu, S.uc, S.ff);
+  k_atd_highpass<<<gb, T, 0, st>>>(d, S.uc, S.ff, S.uf);
+  k_filter<<<gb, T, 0, st>>>(d, MK_FV, P.fpv, S.vc, S.ff);
+  k_atd_highpass<<<gb, T, 0, st>>>(d, S.vc, S.ff, S.vf);
+  k_filter_t<<<gb, T, 0, st>>>(d, tt, P.fpt, S.tf, S.ff);
+  k_atd_highpass<<<gb, T, 0, st>>>(d, S.tl, S.ff, S.tf);
+  k_atd_cells<<<gb, T, 0, st>>>(d, S, P, tt, dus, dvs, dts);
+  k_atd_bc<<<1, T, 0, st>>>(d, tt, dus, dvs, dps, dts);
+  k_atd_zero_p<<<gb, T, 0, st>>>(d, dps);
+  k_atd_bc<<<1, T, 0, st>>>(d, tt, dus, dvs, dps, dts);
+  CK(cudaGetLastError());
+  if ((rc = check_sync(c))) return rc;
+  if ((rc = launch_ppe(c, *lCartesGrid ? 1 : 0, *nPpeSolver, *msorit, *dka, *sortol, *sorrel, dus, dvs, dps)))
+    return rc;
+  CK(cudaMemcpyAsync(c->h_out, c->d_out, sizeof(StepOut), cudaMemcpyDeviceToHost, st));
+  c->launches += 2;
+  k_atd_bc<<<1, T, 0, st>>>(d, tt, dus, dvs, dps, dts);
+  k_project<<<gb, T, 0, st>>>(d, *dka, dps, dus, dvs);
+  CK(cudaGetLastError());
+  if ((rc = copy_out(c, uss, dus)) || (rc = copy_out(c, vss, dvs)) || (rc = copy_out(c, pss, dps)) ||
+      (rc = copy_out(c, tss, dts)))
+    return rc;
+  if ((rc = check_sync(c))) return rc;
+  *nSorConv = c->h_out->nsor;
+  return W2_OK;
 }
 
 int wolfd2gpu_eq_state(w2_ctx *c, const int *nx, const int *ny, const double *uref,

@@ -309,20 +309,36 @@ __global__ void __launch_bounds__(kMaxThreads) k_ppe(Dev d, int lcartes, int nps
 
 // Red/black SOR with two sweeps per grid barrier (unit-stencil rows,
 // sorrel = 1); dynamic shared memory holds the staged tile.
-__global__ void __launch_bounds__(kMaxThreads, 1) k_ppe_tiled(Dev d, TileGeom g, int lcartes,
-                                                           int msorit, double dk, double sortol,
-                                                           double sorrel, const double *u, const double *v,
-                                                           double *p, StepOut *out) {
-  vgrid_set(0, gridDim.x);
+template <int NB>
+__device__ __forceinline__ void ppe_tiled_body(const Dev &d, const TileGeom &g, int lcartes, int msorit,
+                                               double dk, double sortol, double sorrel, const double *u,
+                                               const double *v, double *p, StepOut *out) {
   if (step_skip(d)) return;
   Sync *sy = d.sync;
   ppe_divergence(d, u, v);
   if (!grid_sync(sy)) return;
   ppe_rhs_grid(d, lcartes, dk, p);
   if (!grid_sync(sy)) return;
-  const int nconv = ppe_rb_tiled(d, g, p, d.ppn, d.qh, msorit, sortol, sorrel);
+  const int nconv = ppe_rb_tiled<NB>(d, g, p, d.ppn, d.qh, msorit, sortol, sorrel);
   if (nconv < 0) return;
   if (vblock() == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? msorit : nconv;
+}
+
+// Red/black SOR on shared-memory tiles: 512-thread blocks with four points
+// of a thread in flight, or (k_ppe_tiled_w) 1024-thread blocks with two.
+__global__ void __launch_bounds__(kMaxThreads, 1) k_ppe_tiled(Dev d, TileGeom g, int lcartes,
+                                                           int msorit, double dk, double sortol,
+                                                           double sorrel, const double *u, const double *v,
+                                                           double *p, StepOut *out) {
+  vgrid_set(0, gridDim.x);
+  ppe_tiled_body<4>(d, g, lcartes, msorit, dk, sortol, sorrel, u, v, p, out);
+}
+__global__ void __launch_bounds__(1024, 1) k_ppe_tiled_w(Dev d, TileGeom g, int lcartes, int msorit,
+                                                         double dk, double sortol, double sorrel,
+                                                         const double *u, const double *v, double *p,
+                                                         StepOut *out) {
+  vgrid_set(0, gridDim.x);
+  ppe_tiled_body<2>(d, g, lcartes, msorit, dk, sortol, sorrel, u, v, p, out);
 }
 
 // Mixed-precision red/black SOR (FP32 sweeps, FP64 residual and correction)

@@ -58,7 +58,7 @@ __device__ __forceinline__ double mul_neg_quarter(double x) {
 // fma(x, -1, y) rounds exactly as y - x and fma(x, 1, y) as y + x, and the
 // GB300 issues FP64 FMAs at a higher rate than FP64 adds.  The product by
 // -1/4 is an exponent edit (mul_neg_quarter).
-template <bool RELAX>
+template <bool RELAX, int NB>
 __device__ __forceinline__ unsigned long long tile_half_sweep(
     double *P, const double *Bt, int W, int gi0, int gj0, int bi0, int bi1, int bj0, int bj1,
     int parity, int oi0, int oi1, int oj0, int oj1, double relax, double one, double mone) {
@@ -71,7 +71,6 @@ __device__ __forceinline__ unsigned long long tile_half_sweep(
   const int dj = T / wmax, dk = T % wmax;
   int t = threadIdx.x;
   int j = bj0 + t / wmax, k = t % wmax;
-  constexpr int NB = 4;
   while (t < total) {
     int o[NB];
     bool ok[NB], own[NB];
@@ -119,7 +118,8 @@ __device__ __forceinline__ unsigned long long tile_half_sweep(
 
 // One group of up to K sweeps on every tile this block owns: read pin,
 // write pout (and pmid after the first sweep), record per-sweep maxima.
-template <bool RELAX>
+// NB points of a thread are in flight at once.
+template <bool RELAX, int NB>
 __device__ void tiled_group(const Dev &d, const TileGeom &g, const double *pin, double *pout,
                             double *pmid, int nsweeps, unsigned long long *slots, double relax) {
   extern __shared__ double smem[];
@@ -149,7 +149,7 @@ __device__ void tiled_group(const Dev &d, const TileGeom &g, const double *pin, 
         const int e = kHalo - 1 - 2 * s - c;  // box growth for this half-sweep
         const int bi0 = max(2, oi0 - e), bi1 = min(d.nx, oi1 + e);
         const int bj0 = max(2, oj0 - e), bj1 = min(d.ny, oj1 + e);
-        const unsigned long long m = tile_half_sweep<RELAX>(P, Bt, W, gi0, gj0, bi0, bi1, bj0, bj1,
+        const unsigned long long m = tile_half_sweep<RELAX, NB>(P, Bt, W, gi0, gj0, bi0, bi1, bj0, bj1,
                                                             c, oi0, oi1, oj0, oj1, relax, g.one,
                                                             g.mone);
         mxs[s] = m > mxs[s] ? m : mxs[s];
@@ -195,6 +195,7 @@ __device__ void tiled_group(const Dev &d, const TileGeom &g, const double *pin, 
 
 // Red/black SOR by groups of K sweeps.  p is the caller's field; pb2 and pm
 // are scratch fields.  Returns nConv (0 = not converged) or -1 on error.
+template <int NB>
 __device__ int ppe_rb_tiled(const Dev &d, const TileGeom &g, double *p, double *p2, double *pm,
                             int msorit, double sortol, double sorrel) {
   Sync *sy = d.sync;
@@ -225,9 +226,9 @@ __device__ int ppe_rb_tiled(const Dev &d, const TileGeom &g, double *p, double *
       for (int k = 0; k < kSweepsPerSync; ++k) next[k] = 0ull;
     }
     if (sorrel == 1.0)
-      tiled_group<false>(d, g, bufs[cur], bufs[cur ^ 1], pm, ns, slots, sorrel);
+      tiled_group<false, NB>(d, g, bufs[cur], bufs[cur ^ 1], pm, ns, slots, sorrel);
     else
-      tiled_group<true>(d, g, bufs[cur], bufs[cur ^ 1], pm, ns, slots, sorrel);
+      tiled_group<true, NB>(d, g, bufs[cur], bufs[cur ^ 1], pm, ns, slots, sorrel);
     if (!grid_sync(sy)) return -1;
     int conv_s = -1;
     for (int s2 = 0; s2 < ns; ++s2) {

@@ -107,6 +107,11 @@ def lib():
     L.wolfd2gpu_temp_bound_cond.argtypes = [vp, _ip, _ip, _ip, _ip, _dp, _dp]
     L.wolfd2gpu_therm_energy.argtypes = [vp, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp] + [_dp] * 6
     L.wolfd2gpu_eq_state.argtypes = [vp, _ip, _ip] + [_dp] * 8
+    # ctx; nx ny initflg nthermen lCartesGrid nTRgType nTemBdTp nPpeSolver msorit;
+    # dlref uref tref tmax dka re pe sortol sorrel; fp; cu0 TsCoef HsCoef TemCoef
+    # bnumc rmax rlc; dTRgVal; u1 v1 t1 uss vss pss tss; nSorConv
+    L.wolfd2gpu_small_scale.argtypes = [vp] + [_ip] * 9 + [_dp] * 9 + [_dp] + [_dp] * 7 + [_dp] + \
+        [_dp] * 7 + [_ip]
     L.wolfd2gpu_filter_t.argtypes = [vp, _ip, _ip, _ip, _dp, _dp]
     L.wolfd2gpu_set_thermal.argtypes = [vp, C.POINTER(ThermalC), _ip, _ip, _dp, _dp]
     L.wolfd2gpu_load_thermal.argtypes = [vp, _dp, _dp]
@@ -353,6 +358,28 @@ class Solver:
         """Filter of the temperature (utility.f, ncomp = _T_) in place."""
         rt, prt = self._ttab(th.nTRgType, np.int32)
         self._check(self.L.wolfd2gpu_filter_t(self.h, _i(self.nx), _i(self.ny), prt, _d(fp), _p(t)))
+
+    def SmallScale(self, initflg, th, ap, u1, v1, t1, uss, vss, pss, tss, nthermen=1) -> int:
+        """SmallScale (small_scale.f:31-49) on the device: the small-scale
+        fields uss, vss, pss, tss (updated in place) from the large-scale u1,
+        v1, t1.  th: deck.Thermal tables; ap: the routine's parameters
+        (npsolver, msorit, lcartes, dlref, uref, tref, tmax, dka, re, pe,
+        sortol, sorrel, fp[4], cu0, tscoef, hscoef, temcoef, bnumc, rmax,
+        rlc).  The maps and cell areas persist in the context between calls,
+        as the reference's SAVE keeps them.  Returns the Ppe's nSorConv."""
+        rt, prt = self._ttab(th.nTRgType, np.int32)
+        bt, pbt = self._ttab(th.nTemBdTp, np.int32)
+        tv, ptv = self._ttab(th.dTRgVal, np.float64)
+        fp = np.ascontiguousarray([float(x) for x in ap.fp], dtype=np.float64)
+        out = C.c_int()
+        self._check(self.L.wolfd2gpu_small_scale(
+            self.h, _i(self.nx), _i(self.ny), _i(initflg), _i(nthermen), _i(ap.lcartes), prt, pbt,
+            _i(ap.npsolver), _i(ap.msorit), _d(ap.dlref), _d(ap.uref), _d(ap.tref), _d(ap.tmax),
+            _d(ap.dka), _d(ap.re), _d(ap.pe), _d(ap.sortol), _d(ap.sorrel),
+            fp.ctypes.data_as(_dp), _d(ap.cu0), _d(ap.tscoef), _d(ap.hscoef), _d(ap.temcoef),
+            _d(ap.bnumc), _d(ap.rmax), _d(ap.rlc), ptv, _p(u1), _p(v1), _p(t1), _p(uss), _p(vss),
+            _p(pss), _p(tss), C.byref(out)))
+        return out.value
 
     def EqState(self, uref, densref, tmax, tref, rconst, p, t, den) -> None:
         self._check(self.L.wolfd2gpu_eq_state(self.h, _i(self.nx), _i(self.ny), _d(uref), _d(densref),
