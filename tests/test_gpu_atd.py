@@ -106,3 +106,35 @@ def test_small_scale_chaotic_maps():
             ro = float(np.sqrt(np.mean(orc[k] ** 2)))
             rd = float(np.sqrt(np.mean(dev[k] ** 2)))
             assert ro > 0 and 0.5 * ro <= rd <= 2.0 * ro, (k, ro, rd)
+
+
+@pytest.mark.parametrize("cu0,bnumc,tol", [(0.0, 200.0, 0.0), (2.0, 200.0, 1e-9)])
+def test_small_scale_time_loop(cu0, bnumc, tol):
+    """main.f's loop with nsmallscl = 1 driven through the drop-ins
+    (wolfd2_gb300.atd.AtdLoop, the calling pattern of the Fortran driver)
+    against the oracle's loop, from a developed lid-driven flow: bit for bit
+    with the maps off (cu0 = 0), within 1e-9 of each field's size with
+    contracting maps (bnumc = 200)."""
+    from wolfd2_gb300.atd import AtdLoop
+    case = deck.cavity(32, 800.0, 0.004, solver="rb_sor")
+    dev = O.OracleRun(case)
+    dev.step(40)
+    fields = {k: dev.f[k].copy(order="F") for k in ("u", "v", "p", "t", "d")}
+    case.atd = deck.SmallScaleParams(cu0=cu0, bnumc=bnumc, npsolver=deck.PPE_SOLVERS["rb_sor"], msorit=400,
+                                     sorrel=1.3, fpu=300.0, fpv=300.0, fpt=200.0, pe=560.0)
+    ref = O.OracleRun(case, fields=fields)
+    s = Solver.for_case(case, tuned=False)
+    loop = AtdLoop(s, case, fields, ref._ap)
+    assert loop.nsor_seed == ref.atd_nsor[0]
+    ref.step(4)
+    loop.step(4)
+    assert [h[:2] for h in loop.history] == [h[:2] for h in ref.history]
+    for k in ("u", "v", "p", "uss", "vss", "pss", "tss"):
+        if tol == 0.0:
+            assert np.array_equal(loop.f[k], ref.f[k]), k
+        else:
+            scale = max(float(np.max(np.abs(ref.f[k]))), 1e-300)
+            assert float(np.max(np.abs(loop.f[k] - ref.f[k]))) <= tol * scale, k
+    if cu0 > 0:
+        assert np.abs(ref.f["uss"]).max() > 0
+    s.close()
