@@ -334,7 +334,10 @@ const char *wolfd2gpu_last_error(w2_ctx *ctx);
  * blocks_per_sm = -1 selects the one-colour-per-barrier red/black sweep,
  * -2 forces the tiled two-sweeps-per-barrier form at any grid size, -3 runs
  * that form in 1024-thread blocks (two points in flight per thread instead
- * of four in 512-thread blocks), -4 returns to 512-thread blocks.
+ * of four in 512-thread blocks), -4 returns to 512-thread blocks; -5 has
+ * nAuxMomentum solve its X and Y chains one after the other (half the
+ * working set, twice the barriers), -6 both together (the default).  None
+ * changes a result bit.
  * Takes effect on the next launch. */
 int wolfd2gpu_tune(w2_ctx *ctx, int chain_seg, int chain_warm, int threads,
                    int blocks_per_sm);

@@ -78,12 +78,15 @@ def test_small_scale_without_maps_bitwise(layout):
             assert np.array_equal(dev[k], orc[k]), k
 
 
-@pytest.mark.parametrize("layout", ["curvilinear", "blockage"])
-def test_small_scale_contracting_maps(layout):
-    """bnumc = 200 (parse.f's value): rmap is about 1e-6, the maps contract,
-    and the libm differences stay at rounding level: the small scales agree
-    to 1e-11 of their largest value and the sweep counts are equal."""
-    res = _run(layout, 2.0, 200.0, 0.1)
+@pytest.mark.parametrize("layout,bnumc,dka", [("curvilinear", 200.0, 0.1), ("blockage", 50.0, 0.05)])
+def test_small_scale_contracting_maps(layout, bnumc, dka):
+    """Maps that contract (bnumc = 200, parse.f's value, on the curvilinear
+    grid; bnumc = 50 on the blockage grid, whose weaker gradients leave the
+    model idle at 200): the libm differences stay at rounding level, the
+    small scales agree to 1e-11 of their largest value and the sweep counts
+    are equal.  (On the oracle a 1e-15 relative change of u moves these
+    outputs by under 1e-14 of their size.)"""
+    res = _run(layout, 2.0, bnumc, dka)
     for n_o, n_d, orc, dev in res:
         assert n_d == n_o
         for k in orc:
@@ -122,7 +125,7 @@ def test_small_scale_time_loop(cu0, bnumc, tol):
     fields = {k: dev.f[k].copy(order="F") for k in ("u", "v", "p", "t", "d")}
     case.atd = deck.SmallScaleParams(cu0=cu0, bnumc=bnumc, npsolver=deck.PPE_SOLVERS["rb_sor"], msorit=400,
                                      sorrel=1.3, fpu=300.0, fpv=300.0, fpt=200.0, pe=560.0)
-    ref = O.OracleRun(case, fields=fields)
+    ref = O.OracleRun(case, fields=fields, cold_start=False)
     s = Solver.for_case(case, tuned=False)
     loop = AtdLoop(s, case, fields, ref._ap)
     assert loop.nsor_seed == ref.atd_nsor[0]

@@ -1090,6 +1090,10 @@ int wolfd2gpu_tune(w2_ctx *c, int chain_seg, int chain_warm, int threads, int bl
     // -1: one colour per barrier for red/black SOR; -2: tiled sweeps at any size
     c->use_tiled = blocks_per_sm == -1 ? 0 : 2;
     blocks_per_sm = 0;
+  } else if (blocks_per_sm == -5 || blocks_per_sm == -6) {
+    // nAuxMomentum's X and Y chains solved one after the other (-5) or together (-6)
+    c->dev.chains_apart = blocks_per_sm == -5 ? 1 : 0;
+    blocks_per_sm = 0;
   } else if (blocks_per_sm == -3 || blocks_per_sm == -4) {
     // tiled sweeps in 1024-thread blocks (-3) or back to 512-thread blocks (-4)
     c->tiled_wide = blocks_per_sm == -3 ? 1 : 0;

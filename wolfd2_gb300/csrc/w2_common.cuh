@@ -150,6 +150,8 @@ struct Dev {
   int seg, warm;       // chain segment length and warm-up rows
   int has_outflow;     // any OUTLT1/OUTLT2 face (VelOutflowBCs not a no-op)
   int ppe_unit;        // every PPE row is the unit stencil (1,1,-4,1,1)
+  int chains_apart;    // nAuxMomentum solves the X and the Y chain one after
+                       // the other (half the working set, twice the barriers)
   int ppe_unit32;      // every PPE row rounds to the unit stencil in FP32 (no
                        // identity rows): any uniform square-cell Cartesian grid
   // density at the starred and time-level-n states for the buoyancy term of

@@ -478,10 +478,18 @@ __device__ bool naux_momentum(const Dev &d, const MomView<T> &V, int mqiter, dou
     }
     mom_assemble1(d, V, dk, re, us, vs, un, vn);
     if (!grid_sync(sy)) return false;
-    if (!solve_chains(d, V.x1, V.y1, 2)) return false;
+    if (d.chains_apart) {
+      if (!solve_chains(d, V.x1, V.x1, 1) || !solve_chains(d, V.y1, V.y1, 1)) return false;
+    } else if (!solve_chains(d, V.x1, V.y1, 2)) {
+      return false;
+    }
     mom_assemble2(d, V, dk, re, us, vs);
     if (!grid_sync(sy)) return false;
-    if (!solve_chains(d, V.x2, V.y2, 2)) return false;
+    if (d.chains_apart) {
+      if (!solve_chains(d, V.x2, V.x2, 1) || !solve_chains(d, V.y2, V.y2, 1)) return false;
+    } else if (!solve_chains(d, V.x2, V.y2, 2)) {
+      return false;
+    }
     mom_update(d, V, us, vs, &sy->red[it % 3]);
     if (!grid_sync(sy)) return false;
     const double difmax = slot_value(&sy->red[it % 3]);
