@@ -79,8 +79,14 @@ typedef struct w2_ctx w2_ctx;
 #define W2_NMETRIC 30
 
 /* Create a context for an nx x ny natural-point grid.  Uploads the region
- * tables (output of SetUpBCs, src/bound_cond.f:34-443).  Fields are zero.
- * No reference counterpart (the reference keeps these as static arrays). */
+ * tables (output of SetUpBCs, src/bound_cond.f:34-443) and, where nRegType
+ * has porous regions, their porosity and Dupuit-Forchheimer constants
+ * (output of PorRegCnst, src/bound_cond.f:1883-1986; may be NULL without
+ * porous regions).  Porous regions run on the plain FP64 momentum path
+ * (the drop-in nAuxMomentum and the FP64 step); the mixed step, the
+ * ensemble and the adjoint return W2_E_UNSUPPORTED for them.  Fields are
+ * zero.  No reference counterpart (the reference keeps these as static
+ * arrays). */
 int wolfd2gpu_create(w2_ctx **ctx, int mnx, int mny, int mgri, int mgrj,
                      int nx, int ny, const int *nReg, const int *nRegBrd,
                      const int *nRegType, const int *nMomBdTp,
@@ -334,10 +340,7 @@ const char *wolfd2gpu_last_error(w2_ctx *ctx);
  * blocks_per_sm = -1 selects the one-colour-per-barrier red/black sweep,
  * -2 forces the tiled two-sweeps-per-barrier form at any grid size, -3 runs
  * that form in 1024-thread blocks (two points in flight per thread instead
- * of four in 512-thread blocks), -4 returns to 512-thread blocks; -5 has
- * nAuxMomentum solve its X and Y chains one after the other (half the
- * working set, twice the barriers), -6 both together (the default).  None
- * changes a result bit.
+ * of four in 512-thread blocks), -4 returns to 512-thread blocks.
  * Takes effect on the next launch. */
 int wolfd2gpu_tune(w2_ctx *ctx, int chain_seg, int chain_warm, int threads,
                    int blocks_per_sm);

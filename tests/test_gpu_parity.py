@@ -260,17 +260,15 @@ def test_tiled_time_loop_512():
         assert np.array_equal(g, ref.f[name]), (name, rel_err(g, ref.f[name]))
 
 
-@pytest.mark.parametrize("seg,warm,apart", [(8, 1, False), (13, 4, False), (27, 64, False), (97, 2, False),
-                                            (4096, 64, False), (8, 1, True), (97, 2, True)])
-def test_chain_segments_exact(seg, warm, apart):
+@pytest.mark.parametrize("seg,warm", [(8, 1), (13, 4), (27, 64), (97, 2), (4096, 64)])
+def test_chain_segments_exact(seg, warm):
     """nAuxMomentum bit-identical for segment lengths that do and do not
     divide the chains and for warm-ups short enough to need several
-    verification rounds (segment-interleaved chain storage), with the X
-    and Y chains solved together or one after the other."""
+    verification rounds (segment-interleaved chain storage)."""
     case = deck.channel(48, 16, 500.0, 0.004, length=3.0, solver="rb_sor")
     o, met = oracle_setup(case)
     s = Solver.for_case(case)
-    s.tune(seg=seg, warm=warm, blocks_per_sm=-5 if apart else -6)
+    s.tune(seg=seg, warm=warm)
     f = fields_for(case, 21, amp=0.2)
     un, vn = f["u"], f["v"]
     o.vel_bound_cond(case.nx, case.ny, case.regions, un, vn)

@@ -63,6 +63,24 @@ def test_blockage_and_porous_free_multiregion():
         assert np.array_equal(r.f[k], o.f[k]), k
 
 
+@pytest.mark.parametrize("layout", ["row", "quad"])
+def test_porous_regions_bitwise(layout):
+    """PorosCoef and the porosity division of the convective coefficients
+    (momentum.f:296-324, 621-649, 1115-1226): the oracle's time loop equals
+    the translated reference's on porous layouts."""
+    import porous_setup
+    case = porous_setup.case(layout)
+    assert (case.regions.nRegType == deck.RM_POROUS).sum() >= 2
+    f77ref.build(case.nx + 1, case.ny + 1)
+    r = refrun.RefRun(case)
+    o = O.OracleRun(case)
+    r.step(6)
+    o.step(6)
+    assert [h[:2] for h in r.history] == [h[:2] for h in o.history]
+    for k in "uvp":
+        assert np.array_equal(r.f[k], o.f[k]), k
+
+
 def test_named_dt_diverges_at_1024():
     """At 1024x1024, Re=1000 the named dt=1e-3 drives the reference's own
     Newton-Kantorovich iteration to NaN in the first step (both in the

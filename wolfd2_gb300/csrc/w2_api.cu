@@ -50,6 +50,7 @@ struct w2_ctx {
   char err[512] = {0};
   std::vector<int> tab_brd, tab_rtype, tab_btype;
   std::vector<double> tab_bcv;
+  std::vector<double> tab_por, tab_porc1, tab_porc2;  // dPRporos, dPRporc1, dPRporc2
   int nri = 0, nrj = 0;
   // per-kernel event timing (wolfd2gpu_profile)
   bool prof_on = false;
@@ -323,6 +324,60 @@ int build_masks(w2_ctx *c, std::vector<uint16_t> &mk) {
   return W2_OK;
 }
 
+// Host replay of the porous region loops of XMomentum/YMomentum
+// (momentum.f:296-324, 621-649) and PorosCoef (momentum.f:1157-1214) into
+// the per-cell tables of Porous (planes: X divisors 0-1, Y divisors 2-3,
+// porc1 X, porc2 X, porc1 Y, porc2 Y) and the MK_PCX / MK_PCY bits.
+int build_porous(w2_ctx *c, std::vector<uint16_t> &mk, std::vector<double> &tab) {
+  const int mgri = c->mgri, mgrj = c->mgrj, ld = c->ld;
+  const size_t nf = c->nf;
+  tab.assign(8 * nf, 0.0);
+  std::fill(tab.begin(), tab.begin() + 4 * nf, 1.0);
+  std::vector<uint8_t> nxd(nf, 0), nyd(nf, 0);
+  std::vector<int> wx(nf, 0), wy(nf, 0);  // last PorosCoef writer: 0 zero, else region + 1
+  auto B = [&](int ir, int jr, int s) { return c->tab_brd[(ir - 1) + (jr - 1) * mgri + (s - 1) * mgri * mgrj]; };
+  auto id = [&](int ir, int jr) { return (ir - 1) + (jr - 1) * mgri; };
+  auto o = [&](int i, int j) { return (size_t)i + (size_t)j * ld; };
+  for (int jr = 1; jr <= c->nrj; jr++)
+    for (int ir = 1; ir <= c->nri; ir++) {
+      const int iW = B(ir, jr, W2_WEST), iE = B(ir, jr, W2_EAST);
+      const int jS = B(ir, jr, W2_SOUTH), jN = B(ir, jr, W2_NORTH);
+      if (c->tab_rtype[id(ir, jr)] != W2_RM_POROUS) {
+        for (int j = jS; j <= jN; j++)
+          for (int i = iW; i <= iE; i++) wx[o(i, j)] = wy[o(i, j)] = 0;
+        continue;
+      }
+      const double por = c->tab_por[id(ir, jr)];
+      for (int j = jS + 1; j <= jN; j++)
+        for (int i = iW; i <= iE; i++) {
+          const size_t k = o(i, j);
+          if (nxd[k] == 2) return fail(c, W2_E_UNSUPPORTED, "a cell in three porous regions");
+          tab[nxd[k]++ * nf + k] = por;
+          wx[k] = id(ir, jr) + 1;
+        }
+      for (int j = jS; j <= jN; j++)
+        for (int i = iW + 1; i <= iE; i++) {
+          const size_t k = o(i, j);
+          if (nyd[k] == 2) return fail(c, W2_E_UNSUPPORTED, "a cell in three porous regions");
+          tab[(2 + nyd[k]++) * nf + k] = por;
+          wy[k] = id(ir, jr) + 1;
+        }
+    }
+  for (size_t k = 0; k < nf; ++k) {
+    if (wx[k]) {
+      mk[k] |= MK_PCX;
+      tab[4 * nf + k] = c->tab_porc1[wx[k] - 1];
+      tab[5 * nf + k] = c->tab_porc2[wx[k] - 1];
+    }
+    if (wy[k]) {
+      mk[k] |= MK_PCY;
+      tab[6 * nf + k] = c->tab_porc1[wy[k] - 1];
+      tab[7 * nf + k] = c->tab_porc2[wy[k] - 1];
+    }
+  }
+  return W2_OK;
+}
+
 cudaEvent_t ev_get(w2_ctx *c) {
   if (!c->ev_pool.empty()) {
     cudaEvent_t e = c->ev_pool.back();
@@ -497,7 +552,6 @@ bool dims_match(w2_ctx *c, const int *nx, const int *ny) {
 int ready(w2_ctx *c) {
   if (!c) return W2_E_ARG;
   if (!c->metrics_ok) return fail(c, W2_E_ARG, "metrics not set (wolfd2gpu_set_metrics or wolfd2gpu_grid_metric)");
-  if (c->porous) return fail(c, W2_E_UNSUPPORTED, "porous regions are not supported by the GPU path");
   return W2_OK;
 }
 
@@ -925,7 +979,6 @@ int wolfd2gpu_create(w2_ctx **out, int mnx, int mny, int mgri, int mgrj, int nx,
                      const int *nReg, const int *nRegBrd, const int *nRegType,
                      const int *nMomBdTp, const double *dBCVal, const double *dPRporos,
                      const double *dPRporc1, const double *dPRporc2) {
-  (void)dPRporos; (void)dPRporc1; (void)dPRporc2;
   if (!out) return W2_E_ARG;
   *out = nullptr;
   if (nx < 6 || ny < 6 || nx + 1 > mnx || ny + 1 > mny || mgri < 1 || mgrj < 1 || !nReg ||
@@ -943,6 +996,13 @@ int wolfd2gpu_create(w2_ctx **out, int mnx, int mny, int mgri, int mgrj, int nx,
   c->tab_btype.assign(nMomBdTp, nMomBdTp + nt * 4);
   c->tab_bcv.assign(dBCVal, dBCVal + nt * 16);
   auto bad = [&](int code) { int r = code; wolfd2gpu_destroy(c); return r; };
+  for (size_t k = 0; k < nt; ++k)
+    if (nRegType[k] == W2_RM_POROUS && (!dPRporos || !dPRporc1 || !dPRporc2)) return bad(W2_E_ARG);
+  if (dPRporos && dPRporc1 && dPRporc2) {
+    c->tab_por.assign(dPRporos, dPRporos + nt);
+    c->tab_porc1.assign(dPRporc1, dPRporc1 + nt);
+    c->tab_porc2.assign(dPRporc2, dPRporc2 + nt);
+  }
   if (cudaGetDevice(&c->device) != cudaSuccess) return bad(W2_E_CUDA);
   cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device);
   int coopok = 0;
@@ -955,8 +1015,21 @@ int wolfd2gpu_create(w2_ctx **out, int mnx, int mny, int mgri, int mgrj, int nx,
   if (cudaStreamCreate(&c->st) != cudaSuccess) return bad(W2_E_CUDA);
   std::vector<uint16_t> mk;
   int rc = build_masks(c, mk);
+  std::vector<double> ptab;
+  if (!rc && c->porous) rc = build_porous(c, mk, ptab);
   if (rc) { fprintf(stderr, "wolfd2gpu_create: %s\n", c->err); return bad(rc); }
   Dev &d = c->dev;
+  if (c->porous) {
+    double *pt = dalloc<double>(c, 8 * c->nf);
+    if (!pt) return bad(W2_E_CUDA);
+    cudaMemcpy(pt, ptab.data(), 8 * c->nf * sizeof(double), cudaMemcpyHostToDevice);
+    d.porous = 1;
+    for (int k = 0; k < 4; ++k) d.por.div[k] = pt + k * c->nf;
+    for (int k = 0; k < 2; ++k) {
+      d.por.c1[k] = pt + (4 + 2 * k) * c->nf;
+      d.por.c2[k] = pt + (5 + 2 * k) * c->nf;
+    }
+  }
   d.nx = nx; d.ny = ny; d.ld = c->ld;
   for (int k = 0; k < W2_NMETRIC; ++k)
     if (!(c->met[k] = dalloc<double>(c, c->nf))) return bad(W2_E_CUDA);
@@ -1089,10 +1162,6 @@ int wolfd2gpu_tune(w2_ctx *c, int chain_seg, int chain_warm, int threads, int bl
   if (blocks_per_sm == -1 || blocks_per_sm == -2) {
     // -1: one colour per barrier for red/black SOR; -2: tiled sweeps at any size
     c->use_tiled = blocks_per_sm == -1 ? 0 : 2;
-    blocks_per_sm = 0;
-  } else if (blocks_per_sm == -5 || blocks_per_sm == -6) {
-    // nAuxMomentum's X and Y chains solved one after the other (-5) or together (-6)
-    c->dev.chains_apart = blocks_per_sm == -5 ? 1 : 0;
     blocks_per_sm = 0;
   } else if (blocks_per_sm == -3 || blocks_per_sm == -4) {
     // tiled sweeps in 1024-thread blocks (-3) or back to 512-thread blocks (-4)
@@ -1789,6 +1858,7 @@ static int check_params(w2_ctx *c, const w2_params *prm) {
     return fail(c, W2_E_ARG, "bad solver parameters");
   if (prm->precision == W2_PREC_MIXED) {
     if (prm->refine_sweeps < 0) return fail(c, W2_E_ARG, "refine_sweeps < 0");
+    if (c->porous) return fail(c, W2_E_UNSUPPORTED, "porous regions run the plain FP64 step");
     return mixed_check(c, prm->lcartes, prm->npsolver);
   }
   if (prm->precision != W2_PREC_FP64)
@@ -2418,6 +2488,7 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
     w2_ctx *c = e->cs[k];
     if (!c) return bad(efail(e, W2_E_ARG, "case %d is null", k));
     if (int rc = ready(c)) return bad(efail(e, rc, "case %d: %s", k, c->err));
+    if (c->porous) return bad(efail(e, W2_E_UNSUPPORTED, "case %d: porous regions run single-case steps", k));
     if (c->therm_on)
       return bad(efail(e, W2_E_UNSUPPORTED, "case %d: ensembles do not run the energy equation", k));
     unit = unit && c->dev.ppe_unit32;
@@ -3126,6 +3197,7 @@ int adj_check(w2_ctx *c, const w2_params *prm) {
     return fail(c, W2_E_UNSUPPORTED, "the adjoint supports ppe_solver rb_sor (5) on Cartesian grids");
   if (prm->nfiltu == 1 || prm->nfiltv == 1) return fail(c, W2_E_UNSUPPORTED, "the adjoint does not cover Filter");
   if (c->therm_on) return fail(c, W2_E_UNSUPPORTED, "the adjoint does not cover the energy equation");
+  if (c->porous) return fail(c, W2_E_UNSUPPORTED, "the adjoint does not cover porous regions");
   return W2_OK;
 }
 

@@ -28,6 +28,20 @@ enum : uint16_t {
   MK_DIVZ = 1u << 5,  // div(i,j) zeroed          (pressure.f:109-196)
   MK_FU = 1u << 6,    // Filter u at (i,j)        (utility.f:79-140)
   MK_FV = 1u << 7,    // Filter v at (i,j)        (utility.f:142-204)
+  MK_PCX = 1u << 8,   // X PorosCoef value from a porous region (momentum.f:1186-1196)
+  MK_PCY = 1u << 9,   // Y PorosCoef value from a porous region (momentum.f:1200-1209)
+};
+
+// Porous regions on the FP64 momentum path, from a host replay of the
+// region loops: div[0..1] are the porosities the X division loop
+// (momentum.f:296-324) applies to a cell, first and second (1 where it
+// applies fewer: a cell on the shared border of two porous regions is
+// divided twice), div[2..3] those of the Y loop (momentum.f:621-649);
+// c1[k], c2[k] are porc1, porc2 of the porous region whose PorosCoef loop
+// writes the cell last (k = 0 X, 1 Y; read where MK_PCX / MK_PCY is set).
+struct Porous {
+  const double *div[4];
+  const double *c1[2], *c2[2];
 };
 
 // Metric arrays (grid.f:368-535), device copies in the padded layout.
@@ -150,14 +164,14 @@ struct Dev {
   int seg, warm;       // chain segment length and warm-up rows
   int has_outflow;     // any OUTLT1/OUTLT2 face (VelOutflowBCs not a no-op)
   int ppe_unit;        // every PPE row is the unit stencil (1,1,-4,1,1)
-  int chains_apart;    // nAuxMomentum solves the X and the Y chain one after
-                       // the other (half the working set, twice the barriers)
   int ppe_unit32;      // every PPE row rounds to the unit stencil in FP32 (no
                        // identity rows): any uniform square-cell Cartesian grid
   // density at the starred and time-level-n states for the buoyancy term of
   // YMomentum (momentum.f:703), FP64 path; null when the density is zero
   const double *den, *denn;
   double fr;
+  int porous;          // porous regions present (tables in por)
+  Porous por;
   int me_gate;         // a launch of momentum/energy iteration >= 2: skipped once they converged
 };
 

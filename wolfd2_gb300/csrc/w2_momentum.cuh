@@ -20,7 +20,9 @@
 // Metric arrays are read through MRef, which collapses to 1-D profiles or
 // constants where the host found them so.  Non-porous regions contribute
 // exact zeros (PorosCoef writes 0, so dk2*cpj adds +0 to a value >= 1 and
-// the RHS terms vanish); porous decks are rejected on the host.  The
+// the RHS terms vanish), and the rows leave those terms out; with porous
+// regions (FP64 path) M1 divides the ConvCoef values by the porosities and
+// the rows add the PorosCoef terms, formed where they are used.  The
 // buoyancy term of the y rows (momentum.f:703) is formed when the host gives
 // a density (FP64 path); with zero density it is zero and left out.
 #pragma once
@@ -111,6 +113,56 @@ __device__ __forceinline__ T conv_y2_c2(const Dev &d, const MomView<T> &V, const
           V.yzc(i, j) * (u[IX(d, i, j)] + u[IX(d, i - 1, j)])) * T(0.5);
 }
 
+// ---- porous regions (FP64 path) -----------------------------------------
+// The porosity division of the six ConvCoef arrays of X (momentum.f:296-324)
+// and of Y (momentum.f:621-649) at one cell, in the order of the region
+// loops; a divisor of 1 leaves a value's bits unchanged.  Every cell the
+// loops divide lies inside the ranges M1 writes.
+__device__ __forceinline__ void poros_divide(const Dev &d, const MomView<double> &V, size_t o) {
+  const double x0 = d.por.div[0][o], x1 = d.por.div[1][o];
+  const double y0 = d.por.div[2][o], y1 = d.por.div[3][o];
+  double *xs[6] = {V.cj1x, V.cj2x, V.c1sx, V.c2sx, V.c1nx, V.c2nx};
+  double *ys[6] = {V.cj1y, V.cj2y, V.c1sy, V.c2sy, V.c1ny, V.c2ny};
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    xs[k][o] = xs[k][o] / x0 / x1;
+    ys[k][o] = ys[k][o] / y0 / y1;
+  }
+}
+
+// PorosCoef (momentum.f:1115-1226) at (i, j) for X (momentum.f:1186-1196;
+// as there, only the last v of the four is divided by 4) ...
+__device__ __forceinline__ double poros_cp_x(const Dev &d, int njacob, const double *u, const double *v,
+                                             int i, int j) {
+  const size_t o = IX(d, i, j);
+  if (!(d.mask[o] & MK_PCX)) return 0.0;
+  const double t = v[o] + v[IX(d, i + 1, j)] + v[IX(d, i, j - 1)] + v[IX(d, i + 1, j - 1)] / 4.0;
+  double unorm = sqrt(u[o] * u[o] + t * t);
+  double unrm1 = 0.0;
+  if (unorm > 1.0e-8) unrm1 = (u[o] * u[o]) / unorm;
+  if (njacob == 1) unorm = unrm1 + unorm;
+  return d.por.c1[0][o] + d.por.c2[0][o] * unorm;
+}
+
+// ... and for Y (momentum.f:1200-1209).
+__device__ __forceinline__ double poros_cp_y(const Dev &d, int njacob, const double *u, const double *v,
+                                             int i, int j) {
+  const size_t o = IX(d, i, j);
+  if (!(d.mask[o] & MK_PCY)) return 0.0;
+  const double t = (u[IX(d, i - 1, j + 1)] + u[IX(d, i, j + 1)] + u[IX(d, i - 1, j)] + u[o]) / 4.0;
+  double unorm = sqrt(t * t + v[o] * v[o]);
+  double unrm1 = 0.0;
+  if (unorm > 1.0e-8) unrm1 = (v[o] * v[o]) / unorm;
+  if (njacob == 1) unorm = unrm1 + unorm;
+  return d.por.c1[1][o] + d.por.c2[1][o] * unorm;
+}
+
+template <class T>
+__device__ __forceinline__ bool porous_on(const Dev &d) {
+  if constexpr (std::is_same<T, double>::value) return d.porous != 0;
+  return false;
+}
+
 // ---- M1: ConvCoef outputs into arrays (FP64 path) -----------------------
 template <class T>
 __device__ void mom_conv_coef(const Dev &d, const MomView<T> &V, const T *us, const T *vs,
@@ -145,6 +197,9 @@ __device__ void mom_conv_coef(const Dev &d, const MomView<T> &V, const T *us, co
       }
       V.c2sy[o] = conv_y2_c2(d, V, us, vs, i, j);
       V.c2ny[o] = conv_y2_c2(d, V, un, vn, i, j);
+    }
+    if constexpr (std::is_same<T, double>::value) {
+      if (d.porous) poros_divide(d, V, o);
     }
   }
 }
@@ -267,6 +322,13 @@ __device__ __forceinline__ ChainRow<T> x_row1(const Dev &d, const MomView<T> &V,
     r.a3 = rkj * (xcj(d, V, us, vs, 1, i + 1, j) - re1 * racp);
   }
   r.b = un[o] - us[o] + rkj * (-cnvs - cnvn) + rkj * re1 * (difs + difn);
+  if constexpr (std::is_same<T, double>::value) {
+    if (d.porous) {
+      // + dk2 cpj on the diagonal, - dk2 (cps us + cpn un) on the right
+      r.a2 = r.a2 + dk2 * poros_cp_x(d, 1, us, vs, i, j);
+      r.b = r.b - dk2 * (poros_cp_x(d, 0, us, vs, i, j) * us[o] + poros_cp_x(d, 0, un, vn, i, j) * un[o]);
+    }
+  }
   return r;
 }
 
@@ -302,17 +364,27 @@ __device__ __forceinline__ ChainRow<T> y_row1(const Dev &d, const MomView<T> &V,
   const T difn = ddiff_v(d, V.ran, V.rbc, V.rbn, V.rgc, vn, i, j);
   const T cj1 = ycj(d, V, us, vs, 1, i, j), ran0 = V.ran(i, j), ranw = V.ran(i - 1, j);
   ChainRow<T> r;
+  // dk2 cpj enters before the 1 (momentum.f:689-697); rows without porous
+  // regions leave the (zero) term out
+  T pj = T(0);
+  if constexpr (std::is_same<T, double>::value) {
+    if (d.porous) pj = dk2 * poros_cp_y(d, 1, us, vs, i, j);
+  }
   if (cj1 >= T(0)) {
     r.a1 = rkj * (-ycj(d, V, us, vs, 1, i - 1, j) - re1 * ranw);
-    r.a2 = rkj * (cj1 + re1 * (ran0 + ranw)) + T(1.0);
+    r.a2 = porous_on<T>(d) ? rkj * (cj1 + re1 * (ran0 + ranw)) + pj + T(1.0)
+                           : rkj * (cj1 + re1 * (ran0 + ranw)) + T(1.0);
     r.a3 = rkj * (-re1 * ran0);
   } else {
     r.a1 = rkj * (-re1 * ranw);
-    r.a2 = rkj * (-cj1 + re1 * (ran0 + ranw)) + T(1.0);
+    r.a2 = porous_on<T>(d) ? rkj * (-cj1 + re1 * (ran0 + ranw)) + pj + T(1.0)
+                           : rkj * (-cj1 + re1 * (ran0 + ranw)) + T(1.0);
     r.a3 = rkj * (ycj(d, V, us, vs, 1, i + 1, j) - re1 * ran0);
   }
   T rhs = vn[o] - vs[o] + rkj * (-cnvs - cnvn) + rkj * re1 * (difs + difn);
   if constexpr (std::is_same<T, double>::value) {
+    if (d.porous)
+      rhs = rhs - dk2 * (poros_cp_y(d, 0, us, vs, i, j) * vs[o] + poros_cp_y(d, 0, un, vn, i, j) * vn[o]);
     if (d.den) {
       // buoy = dk (d(i,j+1) + d(i,j) + dn(i,j+1) + dn(i,j)) / (4 fr)
       const size_t on = IX(d, i, j + 1);
@@ -378,6 +450,9 @@ __device__ __forceinline__ ChainRow<T> x_row2(const Dev &d, const MomView<T> &V,
     r.a2 = T(1.0) + rkj * (-cj2 + re1 * (rgn0 + rgns));
     r.a3 = rkj * (xcj(d, V, us, vs, 2, i, j + 1) - re1 * rgn0);
   }
+  if constexpr (std::is_same<T, double>::value) {
+    if (d.porous) r.a2 = r.a2 + dk2 * poros_cp_x(d, 1, us, vs, i, j);
+  }
   r.b = T(0);
   return r;
 }
@@ -394,13 +469,19 @@ __device__ __forceinline__ ChainRow<T> y_row2(const Dev &d, const MomView<T> &V,
   }
   const T rkj = dk2 * V.djv(i, j);
   const T cj2 = ycj(d, V, us, vs, 2, i, j), rgc0 = V.rgc(i, j), rgcn = V.rgc(i, j + 1);
+  T pj = T(0);
+  if constexpr (std::is_same<T, double>::value) {
+    if (d.porous) pj = dk2 * poros_cp_y(d, 1, us, vs, i, j);
+  }
   if (cj2 >= T(0)) {
     r.a1 = rkj * (-ycj(d, V, us, vs, 2, i, j - 1) - re1 * rgc0);
-    r.a2 = rkj * (cj2 + re1 * (rgcn + rgc0)) + T(1.0);
+    r.a2 = porous_on<T>(d) ? rkj * (cj2 + re1 * (rgcn + rgc0)) + pj + T(1.0)
+                           : rkj * (cj2 + re1 * (rgcn + rgc0)) + T(1.0);
     r.a3 = rkj * (-re1 * rgcn);
   } else {
     r.a1 = rkj * (-re1 * rgc0);
-    r.a2 = rkj * (-cj2 + re1 * (rgcn + rgc0)) + T(1.0);
+    r.a2 = porous_on<T>(d) ? rkj * (-cj2 + re1 * (rgcn + rgc0)) + pj + T(1.0)
+                           : rkj * (-cj2 + re1 * (rgcn + rgc0)) + T(1.0);
     r.a3 = rkj * (ycj(d, V, us, vs, 2, i, j + 1) - re1 * rgcn);
   }
   r.b = T(0);
@@ -478,18 +559,10 @@ __device__ bool naux_momentum(const Dev &d, const MomView<T> &V, int mqiter, dou
     }
     mom_assemble1(d, V, dk, re, us, vs, un, vn);
     if (!grid_sync(sy)) return false;
-    if (d.chains_apart) {
-      if (!solve_chains(d, V.x1, V.x1, 1) || !solve_chains(d, V.y1, V.y1, 1)) return false;
-    } else if (!solve_chains(d, V.x1, V.y1, 2)) {
-      return false;
-    }
+    if (!solve_chains(d, V.x1, V.y1, 2)) return false;
     mom_assemble2(d, V, dk, re, us, vs);
     if (!grid_sync(sy)) return false;
-    if (d.chains_apart) {
-      if (!solve_chains(d, V.x2, V.x2, 1) || !solve_chains(d, V.y2, V.y2, 1)) return false;
-    } else if (!solve_chains(d, V.x2, V.y2, 2)) {
-      return false;
-    }
+    if (!solve_chains(d, V.x2, V.y2, 2)) return false;
     mom_update(d, V, us, vs, &sy->red[it % 3]);
     if (!grid_sync(sy)) return false;
     const double difmax = slot_value(&sy->red[it % 3]);
