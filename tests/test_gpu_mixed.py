@@ -55,7 +55,7 @@ def _inputs(case, seed, amp=0.05):
 
 @pytest.mark.parametrize("sortol,msorit", [(1e-8, 301), (1e-8, 300), (2e-6, 2000), (7e-7, 2000),
                                            (3e-7, 2000)])
-@pytest.mark.parametrize("K,threads,mode", [(8, 512, 0), (4, 256, 0), (8, 128, 0), (8, 512, 2),
+@pytest.mark.parametrize("K,threads,mode", [(8, 512, 0), (4, 256, 0), (4, 128, 0), (8, 512, 2),
                                             (4, 256, 1), (8, 256, 3), (4, 256, 3)])
 def test_mixed_ppe_matches_model(sortol, msorit, K, threads, mode):
     """Drop-in Ppe in mixed mode: bit-identical to the model for stopping
@@ -80,6 +80,25 @@ def test_mixed_ppe_matches_model(sortol, msorit, K, threads, mode):
     n64 = o.ppe(case.nx, case.ny, case.regions, prm, met, u, v, p64, npsolver=5, msorit=msorit)
     assert n_g == n64
     assert _rel(gp, p64) <= P_REL_TOL
+
+
+@pytest.mark.parametrize("sorrel", [1.25, 1.9757, 0.7])
+@pytest.mark.parametrize("K,threads,mode", [(8, 512, 0), (4, 256, 1)])
+def test_mixed_ppe_relaxed(sorrel, K, threads, mode):
+    """Relaxation factors other than 1 (the update c + sorrel * sum rounds
+    the product before the sum, pressure.f:531): bit-identical to the model
+    in both tile modes."""
+    case = deck.cavity(128, 400.0, 0.002, solver="rb_sor", ny=64)
+    o, met, u, v, p = _inputs(case, 17)
+    s = Solver.for_case(case)
+    s.tune_mixed(K, threads, mode)
+    s.set_precision(PREC_MIXED, 48)
+    gp = p.copy(order="F")
+    n_g = s.Ppe(True, 5, 700, case.params.dk, 1e-9, sorrel, u, v, gp)
+    pm = p.copy(order="F")
+    n_m = M.ppe_mixed(case.nx, case.ny, met, u, v, pm, case.params.dk, 700, 1e-9, sorrel, 48)
+    assert n_g == n_m
+    assert np.array_equal(gp, pm), _rel(gp, pm)
 
 
 @pytest.mark.parametrize("inner", [1, 7, 64, 5000])

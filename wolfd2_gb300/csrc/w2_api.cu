@@ -801,7 +801,7 @@ const void *mixed_kernel(int K, bool resident) {
 // Sweep work of one group of K sweeps on a tx x ty tile: (plane columns
 // rounded to warps) x (box rows active in each half-sweep).
 double mixed_sweep_work(int K, int tx, int ty) {
-  const int H = 2 * K, bh = ty + 2 * H, hwp = (tx / 2 + H + 31) / 32 * 32;
+  const int H = 2 * K, bh = ty + 2 * H, hwp = mixed_lanes(K, tx);
   double rows = 0.0;
   for (int h = 1; h <= 2 * K; ++h) rows += std::max(0, bh - 2 * h);
   return (double)hwp * rows;
@@ -809,7 +809,7 @@ double mixed_sweep_work(int K, int tx, int ty) {
 
 // Staging work of one group in multi-tile mode (whole box in, tile out).
 double mixed_stage_work(int K, int tx, int ty) {
-  const int H = 2 * K, bh = ty + 2 * H, hwp = (tx / 2 + H + 31) / 32 * 32;
+  const int H = 2 * K, bh = ty + 2 * H, hwp = (tx / 2 + H + 31) / 32 * 32;  // plane columns in warps
   return 4.0 * K * bh * hwp / 8.0;
 }
 
@@ -873,7 +873,7 @@ void plan_mixed(w2_ctx *c) {
         if (cost < best) {
           best = cost;
           c->mg = MixedGeom{tx, ty, ntx, nty, ntx * tx / 2 + H, nty * ty + 2 * H,
-                            (tx / 2 + H + 31) / 32 * 32, resident ? 1 : 0};
+                            mixed_lanes(K, tx), resident ? 1 : 0};
           c->mixed_smem = smem;
           c->mixed_blocks = blocks;
         }
@@ -2337,7 +2337,7 @@ bool ens_plan(const w2_ctx *c, int K, int blocks, int tmax, size_t smax, MixedGe
       const double cost = tpb * (mixed_sweep_work(K, tx, ty) + mixed_stage_work(K, tx, ty));
       if (cost < best) {
         best = cost;
-        *mg = MixedGeom{tx, ty, ntx, nty, ntx * tx / 2 + H, nty * ty + 2 * H, (tx / 2 + H + 31) / 32 * 32, 0};
+        *mg = MixedGeom{tx, ty, ntx, nty, ntx * tx / 2 + H, nty * ty + 2 * H, mixed_lanes(K, tx), 0};
         *smem = sm;
       }
     }

@@ -21,14 +21,16 @@
 // neighbours are the other plane's columns k and k-1 or k+1, and its
 // north/south neighbours are the other plane's column k one row up or down.
 //
-// Registers.  Thread (k, s) owns column k of both planes over the rows of
-// strip s (kMixedRows rows).  A half-sweep of colour c first reads the
-// strip's column of the other plane into registers, then walks its rows:
-// north/south come from those registers (from shared memory at the strip's
-// first and last row), the
-// column neighbour from the adjacent lane by one warp shuffle whose
+// Registers.  Thread (t, s) owns the column pair k = 2t, 2t+1 of both planes
+// over the rows of strip s (kMixedRows rows).  A half-sweep of colour c
+// first reads the strip's column pair of the other plane into registers (8
+// bytes a row), then walks its rows: north/south come from those registers
+// (from shared memory at the strip's first and last row), the neighbour
+// column beyond the pair from the adjacent lane by one warp shuffle whose
 // direction is the row's parity (uniform across the warp; shared memory for
-// the lanes at a warp's edge).  Updates are written through to the
+// the lanes at a warp's edge).  The two points of a row are updated
+// together by the packed FP32 instructions (add/sub/mul.rn.f32x2), which
+// round each lane as the scalar instruction does.  Updates are written through to the
 // shared-memory planes, which are what other threads read and what the halo
 // exchange moves.  Half-sweep h (1-based within a group) updates the points
 // whose distance to the box frame is at least h: the frame keeps its
@@ -48,7 +50,7 @@
 
 namespace w2 {
 
-constexpr int kMixedRows = 16;      // rows of a thread's strip
+constexpr int kMixedRows = 8;       // rows of a thread's strip
 constexpr int kMixedThreads = 512;  // largest block
 constexpr int kMixedRing = 17;      // Sync::red[17 .. 17 + 3K): per-sweep maxima
 
@@ -56,7 +58,7 @@ struct MixedGeom {
   int tx, ty;    // tile size in unknowns (tx a multiple of 8)
   int ntx, nty;  // tiles per direction, ntx*nty <= blocks
   int gw, gh;    // exchange buffer: floats per colour row, rows
-  int hwp;       // box columns per plane rounded up to whole warps
+  int hwp;       // threads over one strip row (mixed_lanes)
   int resident;  // one tile per block, box kept in shared memory (else multi-tile)
 };
 
@@ -80,12 +82,13 @@ struct MixedBox {
   int gi0, gj0, bw, bh, hw;    // box origin (grid indices) and size
   int oi0, oi1, oj0, oj1;      // own tile, clipped to the unknowns
   int ti, tj;
-  int k, lane, jj0;            // this thread's column, lane, first strip row
-  int dcol0, dcol1;            // column k's distance to the frame, per row parity
+  int k, lane, jj0;            // this thread's first column (pair k, k+1), lane, first strip row
+  int dc[4];                   // distance to the frame of box columns 2k .. 2k+3
+                               // (column k + q/2 in rows of parity q&1)
+  unsigned int own4;           // bit q: dc[q] >= H (own tile)
   unsigned int vrow;           // bit r: strip row r is a row of unknowns inside the frame
   unsigned int orow;           // bit r: ... at distance >= H from the frame (own rows)
   bool wedge, eedge;           // west/east neighbour column lives in another warp
-  bool own0, own1;             // column k is in the own tile, per row parity
 };
 
 // Distance of box column ii's cells to the left/right frame (0 when the
@@ -109,13 +112,35 @@ __device__ __forceinline__ A &pick(A &a0, A &a1) {
   else return a1;
 }
 
+// Packed FP32 pairs: each lane rounds as the scalar instruction does.
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) {
+  float2 r;
+  asm("{\n\t.reg .b64 x, y, z;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\t"
+      "sub.rn.f32x2 z, x, y;\n\tmov.b64 {%0, %1}, z;\n\t}"
+      : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b) {
+  float2 r;
+  asm("{\n\t.reg .b64 x, y, z;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\t"
+      "mul.rn.f32x2 z, x, y;\n\tmov.b64 {%0, %1}, z;\n\t}"
+      : "=f"(r.x), "=f"(r.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+}
+
+__device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
+
 // The rows of a half-sweep of colour C for a strip whose first row has
 // parity P0 (so row r has parity P0 ^ (r & 1), known once unrolled).  eo
-// holds the strip's column of the other plane, read from shared memory at
-// the start of the half-sweep.
+// holds the strip's column pair of the other plane, read from shared memory
+// at the start of the half-sweep.  In a row of parity 0 the pair's points
+// sit at box columns 2k and 2k+2 with west neighbours (k-1, k) and east
+// neighbours (k, k+1) of the other plane; in a row of parity 1 at 2k+1 and
+// 2k+3 with west (k, k+1) and east (k+1, k+2).  actm bit q: the point at box
+// column 2k+q is updated in this half-sweep.
 template <int K, int C, int P0>
-__device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, unsigned int amask, bool act0,
-                                                   bool act1, float relax) {
+__device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, unsigned int amask, unsigned int actm,
+                                                   float relax) {
   // A strip wholly below the box (a block with more threads than its tile
   // plan needs, as in ensemble launches) has nothing to do and must not
   // load: its rows lie past the shared planes.  Uniform per warp (a strip
@@ -125,34 +150,52 @@ __device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, unsigned i
   float *Ec = b.E[C];
   const float *Eo = b.E[C ^ 1];
   const int hw = b.hw, base = b.jj0 * hw + b.k;
-  float eo[kMixedRows];
+  const float2 q4 = make_float2(-0.25f, -0.25f);
+  float2 eo[kMixedRows];
 #pragma unroll
-  for (int r = 0; r < kMixedRows; ++r) eo[r] = Eo[base + r * hw];
+  for (int r = 0; r < kMixedRows; ++r) eo[r] = ld2(Eo + base + r * hw);
   unsigned int mx = 0u;
 #pragma unroll
   for (int r = 0; r < kMixedRows; ++r) {
     if (!((amask >> r) & 1u)) continue;   // same for the whole warp
     const int par = P0 ^ (r & 1);         // folded once the loop is unrolled
     const int o = base + r * hw;
-    const float other = eo[r];
-    float nb;
+    const float2 ot = eo[r];
+    float2 w, e;
     if (par == 0) {
-      nb = __shfl_up_sync(0xffffffffu, other, 1);
+      float nb = __shfl_up_sync(0xffffffffu, ot.y, 1);
       if (b.wedge) nb = Eo[o - 1];
+      w = make_float2(nb, ot.x);
+      e = ot;
     } else {
-      nb = __shfl_down_sync(0xffffffffu, other, 1);
-      if (b.eedge) nb = Eo[o + 1];
+      float nb = __shfl_down_sync(0xffffffffu, ot.x, 1);
+      if (b.eedge) nb = Eo[o + 2];
+      w = ot;
+      e = make_float2(ot.y, nb);
     }
-    const float w = par ? other : nb, e = par ? nb : other;
-    const float s = (r == 0) ? Eo[o - hw] : eo[r > 0 ? r - 1 : 0];
-    const float n = (r == kMixedRows - 1) ? Eo[o + hw] : eo[r < kMixedRows - 1 ? r + 1 : r];
-    const float c0 = Ec[o];
-    float sum = Rc[o] - s - w - e - n;
-    sum = sum * -0.25f - c0;
-    if (par ? act1 : act0) {
-      Ec[o] = c0 + relax * sum;
-      if (((b.orow >> r) & 1u) && (par ? b.own1 : b.own0)) {
-        const unsigned int bb = __float_as_uint(fabsf(sum));
+    const float2 sv = (r == 0) ? ld2(Eo + o - hw) : eo[r > 0 ? r - 1 : 0];
+    const float2 nv = (r == kMixedRows - 1) ? ld2(Eo + o + hw) : eo[r < kMixedRows - 1 ? r + 1 : r];
+    const float2 c0 = ld2(Ec + o);
+    float2 sum = f2sub(f2sub(f2sub(f2sub(ld2(Rc + o), sv), w), e), nv);
+    sum = f2sub(f2mul(sum, q4), c0);
+    // c0 + relax*sum in two roundings, as scalar intrinsics: a packed
+    // multiply followed by a packed add came out fused
+    const float2 nw = make_float2(__fadd_rn(c0.x, __fmul_rn(relax, sum.x)),
+                                  __fadd_rn(c0.y, __fmul_rn(relax, sum.y)));
+    const bool a0 = (actm >> par) & 1u, a1 = (actm >> (2 + par)) & 1u;
+    if (a0 && a1) {
+      *reinterpret_cast<float2 *>(Ec + o) = nw;
+    } else {
+      if (a0) Ec[o] = nw.x;
+      if (a1) Ec[o + 1] = nw.y;
+    }
+    if ((b.orow >> r) & 1u) {
+      if (a0 && ((b.own4 >> par) & 1u)) {
+        const unsigned int bb = __float_as_uint(fabsf(sum.x));
+        mx = bb > mx ? bb : mx;
+      }
+      if (a1 && ((b.own4 >> (2 + par)) & 1u)) {
+        const unsigned int bb = __float_as_uint(fabsf(sum.y));
         mx = bb > mx ? bb : mx;
       }
     }
@@ -164,14 +207,16 @@ __device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, unsigned i
 // over own points (distance >= H) as FP32 bits.
 template <int K, int C>
 __device__ __forceinline__ unsigned int mixed_half_sweep(const MixedBox &b, int h, float relax) {
-  const bool act0 = b.dcol0 >= h, act1 = b.dcol1 >= h;
+  unsigned int actm = 0u;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) actm |= (b.dc[q] >= h ? 1u : 0u) << q;
   // rows at distance >= h from the frame: r in [h - jj0, bh - 1 - h - jj0]
   const int lo = max(0, h - b.jj0), hi = min(kMixedRows - 1, b.bh - 1 - h - b.jj0);
   unsigned int amask = 0u;
   if (hi >= lo) amask = ((2u << hi) - 1u) & ~((1u << lo) - 1u);
   amask &= b.vrow;
-  if ((C + b.gj0 + b.jj0) & 1) return mixed_rows<K, C, 1>(b, amask, act0, act1, relax);
-  return mixed_rows<K, C, 0>(b, amask, act0, act1, relax);
+  if ((C + b.gj0 + b.jj0) & 1) return mixed_rows<K, C, 1>(b, amask, actm, relax);
+  return mixed_rows<K, C, 0>(b, amask, actm, relax);
 }
 
 // ns (<= K) sweeps.  With redm, each warp keeps its running maximum of
@@ -358,12 +403,19 @@ __host__ __device__ inline size_t mixed_smem_bytes(int K, int tx, int ty, bool r
   return (resident ? 6 * plane : mixed_r_offset(plane) + 2 * plane) * sizeof(float);
 }
 
+// Threads over one strip row of a tile's box: the plane column pairs
+// rounded up to whole warps.
+__host__ __device__ inline int mixed_lanes(int K, int tx) {
+  const int hw = tx / 2 + 2 * K;  // a multiple of 4: tx is a multiple of 8
+  return (hw / 2 + 31) / 32 * 32;
+}
+
 // Threads of a block for a tile of tx x ty unknowns: whole warps over the
-// plane columns times strips of kMixedRows rows over the box rows 1..bh-2.
+// plane column pairs times strips of kMixedRows rows over the box rows
+// 1..bh-2.
 __host__ __device__ inline int mixed_threads(int K, int tx, int ty) {
-  const int hw = tx / 2 + 2 * K, hwp = (hw + 31) / 32 * 32;
   const int rows = ty + 4 * K - 2;
-  return hwp * ((rows + kMixedRows - 1) / kMixedRows);
+  return mixed_lanes(K, tx) * ((rows + kMixedRows - 1) / kMixedRows);
 }
 
 // The box of tile `tile` and this thread's place in it.  Resident mode keeps
@@ -397,15 +449,20 @@ __device__ __forceinline__ void mixed_setup(const Dev &d, const MixedGeom &g, Mi
     b.R[0] = fs + r0;
     b.R[1] = fs + r0 + plane;
   }
-  b.k = (int)threadIdx.x % g.hwp;
+  // lanes past the box's column pairs read the last pair (their values
+  // reach only the frame column, which is never updated) and update nothing
+  const int t = (int)threadIdx.x % g.hwp, np = b.hw / 2;
+  const bool valid = t < np;
+  b.k = 2 * min(t, np - 1);
   b.lane = (int)threadIdx.x & 31;
   b.jj0 = 1 + ((int)threadIdx.x / g.hwp) * kMixedRows;
-  b.dcol0 = b.k < b.hw ? mixed_dcol(d, b, 2 * b.k, H) : 0;
-  b.dcol1 = b.k < b.hw ? mixed_dcol(d, b, 2 * b.k + 1, H) : 0;
-  b.own0 = b.dcol0 >= H;
-  b.own1 = b.dcol1 >= H;
-  b.wedge = b.lane == 0 && b.k >= 1 && b.k < b.hw;
-  b.eedge = b.lane == 31 && b.k + 1 < b.hw;
+  b.own4 = 0u;
+  for (int q = 0; q < 4; ++q) {
+    b.dc[q] = valid ? mixed_dcol(d, b, 2 * b.k + q, H) : 0;
+    if (b.dc[q] >= H) b.own4 |= 1u << q;
+  }
+  b.wedge = b.lane == 0 && valid && b.k >= 2;
+  b.eedge = b.lane == 31 && valid && b.k + 2 < b.hw;
   b.vrow = 0u;
   b.orow = 0u;
   for (int r = 0; r < kMixedRows; ++r) {
