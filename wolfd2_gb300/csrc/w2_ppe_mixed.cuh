@@ -128,7 +128,28 @@ __device__ __forceinline__ float2 f2mul(float2 a, float2 b) {
   return r;
 }
 
-__device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
+// The planes by 32-bit shared-window address (byte offsets).  Reached
+// through the box's pointers, the resident kernel's sweeps came out as
+// generic loads and stores (the compiler did not trace the pointers back to
+// the shared window there); the multi-tile and ensemble kernels get shared
+// loads from the pointers and run faster with them than with these
+// volatile forms, so the access form is a template choice (SH).
+__device__ __forceinline__ float2 lds2(unsigned a) {
+  float2 v;
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ float lds1(unsigned a) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
+  return v;
+}
+__device__ __forceinline__ void sts2(unsigned a, float2 v) {
+  asm volatile("st.shared.v2.f32 [%0], {%1, %2};" ::"r"(a), "f"(v.x), "f"(v.y) : "memory");
+}
+__device__ __forceinline__ void sts1(unsigned a, float v) {
+  asm volatile("st.shared.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
 
 // The rows of a half-sweep of colour C for a strip whose first row has
 // parity P0 (so row r has parity P0 ^ (r & 1), known once unrolled).  eo
@@ -138,7 +159,7 @@ __device__ __forceinline__ float2 ld2(const float *p) { return *reinterpret_cast
 // neighbours (k, k+1) of the other plane; in a row of parity 1 at 2k+1 and
 // 2k+3 with west (k, k+1) and east (k+1, k+2).  actm bit q: the point at box
 // column 2k+q is updated in this half-sweep.
-template <int K, int C, int P0>
+template <int K, int C, int P0, bool SH>
 __device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, unsigned int amask, unsigned int actm,
                                                    float relax) {
   // A strip wholly below the box (a block with more threads than its tile
@@ -146,37 +167,62 @@ __device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, unsigned i
   // load: its rows lie past the shared planes.  Uniform per warp (a strip
   // spans whole warps).
   if (b.vrow == 0u) return 0u;
-  const float *Rc = b.R[C];
-  float *Ec = b.E[C];
-  const float *Eo = b.E[C ^ 1];
-  const int hw = b.hw, base = b.jj0 * hw + b.k;
+  const unsigned sR = smem_addr(b.R[C]), sE = smem_addr(b.E[C]), sO = smem_addr(b.E[C ^ 1]);
+  const char *pR = reinterpret_cast<const char *>(b.R[C]), *pO = reinterpret_cast<const char *>(b.E[C ^ 1]);
+  char *pE = reinterpret_cast<char *>(b.E[C]);
+  // plane accesses at byte offset o: shared-window forms or through the pointers
+  auto ldO2 = [&](unsigned o) {
+    if constexpr (SH) return lds2(sO + o);
+    else return *reinterpret_cast<const float2 *>(pO + o);
+  };
+  auto ldO1 = [&](unsigned o) {
+    if constexpr (SH) return lds1(sO + o);
+    else return *reinterpret_cast<const float *>(pO + o);
+  };
+  auto ldE2 = [&](unsigned o) {
+    if constexpr (SH) return lds2(sE + o);
+    else return *reinterpret_cast<const float2 *>(pE + o);
+  };
+  auto ldR2 = [&](unsigned o) {
+    if constexpr (SH) return lds2(sR + o);
+    else return *reinterpret_cast<const float2 *>(pR + o);
+  };
+  auto stE2 = [&](unsigned o, float2 v) {
+    if constexpr (SH) sts2(sE + o, v);
+    else *reinterpret_cast<float2 *>(pE + o) = v;
+  };
+  auto stE1 = [&](unsigned o, float v) {
+    if constexpr (SH) sts1(sE + o, v);
+    else *reinterpret_cast<float *>(pE + o) = v;
+  };
+  const unsigned hb = 4u * (unsigned)b.hw, base = 4u * (unsigned)(b.jj0 * b.hw + b.k);
   const float2 q4 = make_float2(-0.25f, -0.25f);
   float2 eo[kMixedRows];
 #pragma unroll
-  for (int r = 0; r < kMixedRows; ++r) eo[r] = ld2(Eo + base + r * hw);
+  for (int r = 0; r < kMixedRows; ++r) eo[r] = ldO2(base + r * hb);
   unsigned int mx = 0u;
 #pragma unroll
   for (int r = 0; r < kMixedRows; ++r) {
     if (!((amask >> r) & 1u)) continue;   // same for the whole warp
     const int par = P0 ^ (r & 1);         // folded once the loop is unrolled
-    const int o = base + r * hw;
+    const unsigned o = base + r * hb;     // byte offset of the pair in a plane
     const float2 ot = eo[r];
     float2 w, e;
     if (par == 0) {
       float nb = __shfl_up_sync(0xffffffffu, ot.y, 1);
-      if (b.wedge) nb = Eo[o - 1];
+      if (b.wedge) nb = ldO1(o - 4u);
       w = make_float2(nb, ot.x);
       e = ot;
     } else {
       float nb = __shfl_down_sync(0xffffffffu, ot.x, 1);
-      if (b.eedge) nb = Eo[o + 2];
+      if (b.eedge) nb = ldO1(o + 8u);
       w = ot;
       e = make_float2(ot.y, nb);
     }
-    const float2 sv = (r == 0) ? ld2(Eo + o - hw) : eo[r > 0 ? r - 1 : 0];
-    const float2 nv = (r == kMixedRows - 1) ? ld2(Eo + o + hw) : eo[r < kMixedRows - 1 ? r + 1 : r];
-    const float2 c0 = ld2(Ec + o);
-    float2 sum = f2sub(f2sub(f2sub(f2sub(ld2(Rc + o), sv), w), e), nv);
+    const float2 sv = (r == 0) ? ldO2(o - hb) : eo[r > 0 ? r - 1 : 0];
+    const float2 nv = (r == kMixedRows - 1) ? ldO2(o + hb) : eo[r < kMixedRows - 1 ? r + 1 : r];
+    const float2 c0 = ldE2(o);
+    float2 sum = f2sub(f2sub(f2sub(f2sub(ldR2(o), sv), w), e), nv);
     sum = f2sub(f2mul(sum, q4), c0);
     // c0 + relax*sum in two roundings, as scalar intrinsics: a packed
     // multiply followed by a packed add came out fused
@@ -184,10 +230,10 @@ __device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, unsigned i
                                   __fadd_rn(c0.y, __fmul_rn(relax, sum.y)));
     const bool a0 = (actm >> par) & 1u, a1 = (actm >> (2 + par)) & 1u;
     if (a0 && a1) {
-      *reinterpret_cast<float2 *>(Ec + o) = nw;
+      stE2(o, nw);
     } else {
-      if (a0) Ec[o] = nw.x;
-      if (a1) Ec[o + 1] = nw.y;
+      if (a0) stE1(o, nw.x);
+      if (a1) stE1(o + 4u, nw.y);
     }
     if ((b.orow >> r) & 1u) {
       if (a0 && ((b.own4 >> par) & 1u)) {
@@ -205,7 +251,7 @@ __device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, unsigned i
 
 // Half-sweep h of colour C over the thread's strip; returns the max |delta|
 // over own points (distance >= H) as FP32 bits.
-template <int K, int C>
+template <int K, int C, bool SH>
 __device__ __forceinline__ unsigned int mixed_half_sweep(const MixedBox &b, int h, float relax) {
   unsigned int actm = 0u;
 #pragma unroll
@@ -215,20 +261,21 @@ __device__ __forceinline__ unsigned int mixed_half_sweep(const MixedBox &b, int 
   unsigned int amask = 0u;
   if (hi >= lo) amask = ((2u << hi) - 1u) & ~((1u << lo) - 1u);
   amask &= b.vrow;
-  if ((C + b.gj0 + b.jj0) & 1) return mixed_rows<K, C, 1>(b, amask, actm, relax);
-  return mixed_rows<K, C, 0>(b, amask, actm, relax);
+  if ((C + b.gj0 + b.jj0) & 1) return mixed_rows<K, C, 1, SH>(b, amask, actm, relax);
+  return mixed_rows<K, C, 0, SH>(b, amask, actm, relax);
 }
 
 // ns (<= K) sweeps.  With redm, each warp keeps its running maximum of
-// sweep s in redm[s][warp] (zeroed by the caller).
-template <int K>
+// sweep s in redm[s][warp] (zeroed by the caller).  SH: plane accesses in
+// the shared-window forms (resident kernel) or through the box's pointers.
+template <int K, bool SH>
 __device__ __forceinline__ void mixed_sweeps(const MixedBox &b, int ns, float relax,
                                              unsigned int (*redm)[32]) {
 #pragma unroll 1
   for (int s = 0; s < ns; ++s) {
-    const unsigned int m0 = mixed_half_sweep<K, 0>(b, 2 * s + 1, relax);
+    const unsigned int m0 = mixed_half_sweep<K, 0, SH>(b, 2 * s + 1, relax);
     __syncthreads();
-    const unsigned int m1 = mixed_half_sweep<K, 1>(b, 2 * s + 2, relax);
+    const unsigned int m1 = mixed_half_sweep<K, 1, SH>(b, 2 * s + 2, relax);
     if (redm) {
       const unsigned int m = m0 > m1 ? m0 : m1;
       const unsigned int v = __reduce_max_sync(0xffffffffu, m);
@@ -373,7 +420,7 @@ __device__ __forceinline__ void mixed_group(const MixedGeom &g, const MixedBox &
   mixed_copy_planes(b, b.E0[0], b.E0[1], b.E[0], b.E[1]);
   for (int t = threadIdx.x; t < K * 32; t += blockDim.x) redm[t / 32][t % 32] = 0u;
   __syncthreads();
-  mixed_sweeps<K>(b, ns, relax, redm);
+  mixed_sweeps<K, true>(b, ns, relax, redm);
   mixed_band_store<K>(g, b, eout);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
   for (int s = wid; s < ns; s += nw) {
@@ -390,7 +437,7 @@ template <int K>
 __device__ __forceinline__ void mixed_redo(const MixedBox &b, int ns, float relax) {
   mixed_copy_planes(b, b.E[0], b.E[1], b.E0[0], b.E0[1]);
   __syncthreads();
-  mixed_sweeps<K>(b, ns, relax, nullptr);
+  mixed_sweeps<K, true>(b, ns, relax, nullptr);
 }
 
 // Bytes of dynamic shared memory for a tile of tx x ty unknowns: the two
@@ -652,7 +699,7 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
         for (int tile = vblock(); tile < ntiles; tile += vblocks()) {
           mixed_setup<K>(d, g, b, tile, fs, false);
           if (!mixed_stage<K>(g, b, a, tma, ein, &tbar, tphase, sy)) return -1;
-          mixed_sweeps<K>(b, ns, a.relax, redm);
+          mixed_sweeps<K, false>(b, ns, a.relax, redm);
           mixed_tile_store<K>(g, b, eout);
           __syncthreads();
         }
@@ -679,7 +726,7 @@ __device__ int ppe_mixed(const Dev &d, const MixedGeom &g, const MixedArgs &a) {
             for (int tile = vblock(); tile < ntiles; tile += vblocks()) {
               mixed_setup<K>(d, g, b, tile, fs, false);
               if (!mixed_stage<K>(g, b, a, tma, ein, &tbar, tphase, sy)) return -1;
-              mixed_sweeps<K>(b, conv + 1, a.relax, nullptr);
+              mixed_sweeps<K, false>(b, conv + 1, a.relax, nullptr);
               mixed_tile_store<K>(g, b, eout);
               __syncthreads();
             }
