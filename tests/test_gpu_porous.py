@@ -12,7 +12,7 @@ from wolfd2_gb300.gpu import PREC_MIXED, Solver, W2Error
 
 pytestmark = pytest.mark.gpu
 
-LAYOUTS = ["row", "quad"]
+LAYOUTS = ["row", "quad", "curvi"]
 
 
 def _smooth(case, seed, amp):

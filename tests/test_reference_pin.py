@@ -63,7 +63,7 @@ def test_blockage_and_porous_free_multiregion():
         assert np.array_equal(r.f[k], o.f[k]), k
 
 
-@pytest.mark.parametrize("layout", ["row", "quad"])
+@pytest.mark.parametrize("layout", ["row", "quad", "curvi"])
 def test_porous_regions_bitwise(layout):
     """PorosCoef and the porosity division of the convective coefficients
     (momentum.f:296-324, 621-649, 1115-1226): the oracle's time loop equals
