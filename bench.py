@@ -845,6 +845,7 @@ def ensemble_config(args, members, inner, graph):
         "layout": "each cavity the unit square with h = 1/N; the Poisson rows of every member round to "
                   "the unit stencil in FP32 (exactly unit only for N a power of two)",
         "precision": args.precision, "graph": graph,
+        "threads_per_block": args.ens_threads or 128, "sweeps_per_barrier": args.ens_k or 4,
         "l2": "not flushed: the ensemble's fields alone exceed L2 (129 MB) many times over",
     }
 
@@ -881,7 +882,7 @@ def run_ensemble(args):
         s.load_fields(*ic)
         solvers.append(s)
         ics.append(ic)
-    ens = Ensemble(solvers, threads=args.ens_threads, graph=graph)
+    ens = Ensemble(solvers, threads=args.ens_threads, sweeps_per_barrier=args.ens_k, graph=graph)
     prm = [members[i].case.params for i in mine]
     cells = sum(members[i].case.cells for i in mine)
 
@@ -1023,6 +1024,8 @@ def main():
     ap.add_argument("--ens-seed", type=int, default=ENSEMBLE["seed"])
     ap.add_argument("--no-graph", action="store_true", help="ensemble: launch directly, no CUDA graph")
     ap.add_argument("--ens-threads", type=int, default=0, help="ensemble: threads per block (0: library default)")
+    ap.add_argument("--ens-k", type=int, default=0, choices=[0, 4, 8],
+                    help="ensemble: Poisson sweeps per grid barrier (0: library default)")
     ap.add_argument("--no-tma", action="store_true",
                     help="stage the several-tiles-per-block Poisson boxes with vector loads, not TMA")
     ap.add_argument("--adj-steps", type=int, default=ADJOINT["steps"], help="adjoint: steps of the horizon")

@@ -22,7 +22,8 @@
 // north/south neighbours are the other plane's column k one row up or down.
 //
 // Registers.  Thread (t, s) owns the column pair k = 2t, 2t+1 of both planes
-// over the rows of strip s (kMixedRows rows).  A half-sweep of colour c
+// over the rows of strip s (at most kMixedRows rows; which rows depends on
+// the kernel, see mixed_half_sweep).  A half-sweep of colour c
 // first reads the strip's column pair of the other plane into registers (8
 // bytes a row), then walks its rows: north/south come from those registers
 // (from shared memory at the strip's first and last row), the neighbour
@@ -82,12 +83,12 @@ struct MixedBox {
   int gi0, gj0, bw, bh, hw;    // box origin (grid indices) and size
   int oi0, oi1, oj0, oj1;      // own tile, clipped to the unknowns
   int ti, tj;
-  int k, lane, jj0;            // this thread's first column (pair k, k+1), lane, first strip row
+  int k, lane;                 // this thread's first column (pair k, k+1), lane
+  int strip, nstrips;          // this thread's strip and the block's strips
+  int jlo, jhi;                // box rows of unknowns
   int dc[4];                   // distance to the frame of box columns 2k .. 2k+3
                                // (column k + q/2 in rows of parity q&1)
   unsigned int own4;           // bit q: dc[q] >= H (own tile)
-  unsigned int vrow;           // bit r: strip row r is a row of unknowns inside the frame
-  unsigned int orow;           // bit r: ... at distance >= H from the frame (own rows)
   bool wedge, eedge;           // west/east neighbour column lives in another warp
 };
 
@@ -97,13 +98,6 @@ __device__ __forceinline__ int mixed_dcol(const Dev &d, const MixedBox &b, int i
   const int i = b.gi0 + ii;
   if (ii < 0 || ii >= b.bw || i < 2 || i > d.nx) return 0;
   return min(min(ii, b.bw - 1 - ii), H);
-}
-
-// Distance of box row jj to the top/bottom frame (0 off the unknowns).
-__device__ __forceinline__ int mixed_drow(const Dev &d, const MixedBox &b, int jj, int H) {
-  const int j = b.gj0 + jj;
-  if (jj < 1 || jj > b.bh - 2 || j < 2 || j > d.ny) return 0;
-  return min(min(jj, b.bh - 1 - jj), H);
 }
 
 template <int C, class A>
@@ -160,13 +154,8 @@ __device__ __forceinline__ void sts1(unsigned a, float v) {
 // 2k+3 with west (k, k+1) and east (k+1, k+2).  actm bit q: the point at box
 // column 2k+q is updated in this half-sweep.
 template <int K, int C, int P0, bool SH>
-__device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, unsigned int amask, unsigned int actm,
-                                                   float relax) {
-  // A strip wholly below the box (a block with more threads than its tile
-  // plan needs, as in ensemble launches) has nothing to do and must not
-  // load: its rows lie past the shared planes.  Uniform per warp (a strip
-  // spans whole warps).
-  if (b.vrow == 0u) return 0u;
+__device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, int jj0, unsigned int amask,
+                                                   unsigned int orow, unsigned int actm, float relax) {
   const unsigned sR = smem_addr(b.R[C]), sE = smem_addr(b.E[C]), sO = smem_addr(b.E[C ^ 1]);
   const char *pR = reinterpret_cast<const char *>(b.R[C]), *pO = reinterpret_cast<const char *>(b.E[C ^ 1]);
   char *pE = reinterpret_cast<char *>(b.E[C]);
@@ -195,7 +184,7 @@ __device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, unsigned i
     if constexpr (SH) sts1(sE + o, v);
     else *reinterpret_cast<float *>(pE + o) = v;
   };
-  const unsigned hb = 4u * (unsigned)b.hw, base = 4u * (unsigned)(b.jj0 * b.hw + b.k);
+  const unsigned hb = 4u * (unsigned)b.hw, base = 4u * (unsigned)(jj0 * b.hw + b.k);
   const float2 q4 = make_float2(-0.25f, -0.25f);
   float2 eo[kMixedRows];
 #pragma unroll
@@ -235,7 +224,7 @@ __device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, unsigned i
       if (a0) stE1(o, nw.x);
       if (a1) stE1(o + 4u, nw.y);
     }
-    if ((b.orow >> r) & 1u) {
+    if ((orow >> r) & 1u) {
       if (a0 && ((b.own4 >> par) & 1u)) {
         const unsigned int bb = __float_as_uint(fabsf(sum.x));
         mx = bb > mx ? bb : mx;
@@ -250,19 +239,41 @@ __device__ __forceinline__ unsigned int mixed_rows(const MixedBox &b, unsigned i
 }
 
 // Half-sweep h of colour C over the thread's strip; returns the max |delta|
-// over own points (distance >= H) as FP32 bits.
+// over own points (distance >= H) as FP32 bits.  It updates the rows at
+// distance >= h from the frame (h .. bh-1-h).  In the multi-tile and
+// ensemble kernels (!SH) those rows are dealt out to the block's strips in
+// equal runs, so every warp has about the same number of rows whatever h is
+// (fixed strips would leave the warps near the frame idle at the barrier
+// while the shrinking box passes them by): 27.0 against 32.9 ms per channel
+// solve.  The resident kernel keeps fixed strips of kMixedRows rows (1 +
+// strip * kMixedRows ..), measured faster there (10.7 against 11.0 ms).  A
+// strip's run is uniform per warp and at most kMixedRows rows long: the
+// block has enough strips of kMixedRows rows to cover rows 1 .. bh-2.
 template <int K, int C, bool SH>
 __device__ __forceinline__ unsigned int mixed_half_sweep(const MixedBox &b, int h, float relax) {
+  constexpr int H = 2 * K;
+  const int span = b.bh - 2 * h;
+  if (span <= 0) return 0u;
+  int run, jj0;
+  if constexpr (SH) {
+    run = kMixedRows;
+    jj0 = 1 + b.strip * kMixedRows;
+  } else {
+    run = (span + b.nstrips - 1) / b.nstrips;
+    jj0 = h + b.strip * run;
+  }
+  // rows of unknowns among the run inside h .. bh-1-h, and own rows
+  // (distance >= H)
+  const int ulo = max(max(b.jlo, jj0), h), uhi = min(min(b.jhi, jj0 + run - 1), b.bh - 1 - h);
+  if (uhi < ulo) return 0u;
+  const unsigned int amask = ((2u << (uhi - jj0)) - 1u) & ~((1u << (ulo - jj0)) - 1u);
+  const int olo = max(ulo, H), ohi = min(uhi, b.bh - 1 - H);
+  const unsigned int orow = ohi < olo ? 0u : ((2u << (ohi - jj0)) - 1u) & ~((1u << (olo - jj0)) - 1u);
   unsigned int actm = 0u;
 #pragma unroll
   for (int q = 0; q < 4; ++q) actm |= (b.dc[q] >= h ? 1u : 0u) << q;
-  // rows at distance >= h from the frame: r in [h - jj0, bh - 1 - h - jj0]
-  const int lo = max(0, h - b.jj0), hi = min(kMixedRows - 1, b.bh - 1 - h - b.jj0);
-  unsigned int amask = 0u;
-  if (hi >= lo) amask = ((2u << hi) - 1u) & ~((1u << lo) - 1u);
-  amask &= b.vrow;
-  if ((C + b.gj0 + b.jj0) & 1) return mixed_rows<K, C, 1, SH>(b, amask, actm, relax);
-  return mixed_rows<K, C, 0, SH>(b, amask, actm, relax);
+  if ((C + b.gj0 + jj0) & 1) return mixed_rows<K, C, 1, SH>(b, jj0, amask, orow, actm, relax);
+  return mixed_rows<K, C, 0, SH>(b, jj0, amask, orow, actm, relax);
 }
 
 // ns (<= K) sweeps.  With redm, each warp keeps its running maximum of
@@ -502,7 +513,10 @@ __device__ __forceinline__ void mixed_setup(const Dev &d, const MixedGeom &g, Mi
   const bool valid = t < np;
   b.k = 2 * min(t, np - 1);
   b.lane = (int)threadIdx.x & 31;
-  b.jj0 = 1 + ((int)threadIdx.x / g.hwp) * kMixedRows;
+  b.strip = (int)threadIdx.x / g.hwp;
+  b.nstrips = (int)blockDim.x / g.hwp;
+  b.jlo = max(1, 2 - b.gj0);
+  b.jhi = min(b.bh - 2, d.ny - b.gj0);
   b.own4 = 0u;
   for (int q = 0; q < 4; ++q) {
     b.dc[q] = valid ? mixed_dcol(d, b, 2 * b.k + q, H) : 0;
@@ -510,13 +524,6 @@ __device__ __forceinline__ void mixed_setup(const Dev &d, const MixedGeom &g, Mi
   }
   b.wedge = b.lane == 0 && valid && b.k >= 2;
   b.eedge = b.lane == 31 && valid && b.k + 2 < b.hw;
-  b.vrow = 0u;
-  b.orow = 0u;
-  for (int r = 0; r < kMixedRows; ++r) {
-    const int dr = mixed_drow(d, b, b.jj0 + r, H);
-    if (dr > 0) b.vrow |= 1u << r;
-    if (dr >= H) b.orow |= 1u << r;
-  }
 }
 
 // Position of cell (i, j) in a colour-split buffer (see MixedBox).
