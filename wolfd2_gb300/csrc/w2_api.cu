@@ -2242,6 +2242,7 @@ struct w2_ens {
   StepOut *d_outs = nullptr;
   size_t outs_cap = 0;
   bool mixed_ok = false;    // every case has a mixed Poisson plan
+  const char *mixed_why = "";  // why not, when not
   bool graph_on = false;
   cudaGraphExec_t gexec = nullptr;
   int graph_nsteps = -1, graph_prec = -1;
@@ -2566,6 +2567,9 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
     break;
   }
   e->mixed_ok = !e->bp.empty();
+  if (!e->mixed_ok)
+    e->mixed_why = unit ? "no Poisson tile plan fits every case in blocks of this many threads and sweeps per barrier"
+                        : "the mixed step needs Poisson rows that round to the unit stencil in FP32 in every case";
   if (!e->mixed_ok) {
     // plain steps only: the Poisson table is unused
     e->bp = e->bm;
@@ -2643,9 +2647,7 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
       return efail(e, W2_E_ARG, "case %d: bad precision %d", k, q.precision);
     if ((q.precision == W2_PREC_MIXED) != mixed)
       return efail(e, W2_E_UNSUPPORTED, "case %d: every case of one call runs in the same precision", k);
-    if (mixed && !e->mixed_ok)
-      return efail(e, W2_E_UNSUPPORTED, "the mixed step needs Poisson rows that round to the unit stencil "
-                                        "in FP32 in every case");
+    if (mixed && !e->mixed_ok) return efail(e, W2_E_UNSUPPORTED, "%s", e->mixed_why);
     if (mixed && ((q.npsolver != 5 && q.npsolver != 6) || !q.lcartes))
       return efail(e, W2_E_UNSUPPORTED, "case %d: the mixed step needs rb_sor/rb_sorp on a Cartesian grid", k);
     if (q.npsolver < 1 || q.npsolver > 6) return efail(e, W2_E_ARG, "case %d: bad Poisson solver %d", k, q.npsolver);
