@@ -665,10 +665,9 @@ int grid_blocks(w2_ctx *c);
 
 // FP32 forms of the momentum metrics (profiles where the FP64 ones are,
 // rounded full arrays otherwise), FP32 chains (split 2 in the storage of
-// split 1, the identity rows shared with the FP64 chains) and the FP32
-// fields; allocated on the first mixed step, the metrics re-rounded whenever
-// new ones are uploaded.  The FP32 path forms ConvCoef values where it uses
-// them, so it has no ConvCoef arrays.
+// split 1, the identity rows shared with the FP64 chains), the FP32 ConvCoef
+// arrays and the FP32 fields; allocated on the first mixed step, the metrics
+// re-rounded whenever new ones are uploaded.
 int ensure_f32(w2_ctx *c) {
   Dev &d = c->dev;
   MomView<float> &v = d.f32;
@@ -683,6 +682,10 @@ int ensure_f32(w2_ctx *c) {
     v.x1.nseg = d.x1.nseg; v.x2.nseg = d.x2.nseg;
     v.y1.nseg = d.y1.nseg; v.y2.nseg = d.y2.nseg;
     v.x1.L = v.x2.L = v.y1.L = v.y2.L = d.seg;
+    float **cc[] = {&v.cj1x, &v.cj2x, &v.c1sx, &v.c2sx, &v.c1nx, &v.c2nx,
+                    &v.cj1y, &v.cj2y, &v.c1sy, &v.c2sy, &v.c1ny, &v.c2ny};
+    for (float **a : cc)
+      if (!(*a = dalloc<float>(c, c->nf))) return fail(c, W2_E_CUDA, "out of device memory (FP32 ConvCoef arrays)");
     c->f32_alloc = true;
   }
   if (!c->f32_metrics_ok) {

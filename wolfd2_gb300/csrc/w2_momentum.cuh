@@ -3,8 +3,10 @@
 // One Newton-Kantorovich (Q-L) iteration is these phases of a persistent
 // kernel:
 //   M1  convective face coefficients of ConvCoef (cases 4, 1 for x; 5, 2 for
-//       y) from us/vs and un/vn into arrays -- FP64 path only; the FP32 path
-//       forms each value where a row needs it (same expression, same bits);
+//       y) from us/vs and un/vn into arrays, in both precisions (forming
+//       them in the rows instead gives the same bits and measured slower:
+//       2.86 against 2.75 ms per FP32 call at 1024^2, 138 against 124 ms in
+//       the 256-case ensemble);
 //   M2a per row: DConv/DDiff stencils of the starred and time-level-n fields
 //       and the split-1 tridiagonal rows of XMomentum (momentum.f:350-384)
 //       and YMomentum (momentum.f:675-711), written in chain order;
@@ -38,10 +40,10 @@ __device__ __forceinline__ T tmax(T a, T b) { return b > a ? b : a; }
 template <class T>
 __device__ __forceinline__ T tmax_nan(T a, T b) { return (b > a || b != b) ? b : a; }
 
-// The FP32 path forms ConvCoef values on the fly (cheap in FP32, and it keeps
-// the working set in L2); the FP64 path stores them once per iteration.
+// Whether the rows form ConvCoef values themselves instead of reading M1's
+// arrays (same bits either way); both paths read the arrays.
 template <class T>
-constexpr bool kFuseConv = std::is_same<T, float>::value;
+constexpr bool kFuseConv = false;
 
 // ---- ConvCoef values (momentum.f:864-981) at one point ------------------
 // Each returns the value M1 stores at (i, j), or 0 where M1 never writes

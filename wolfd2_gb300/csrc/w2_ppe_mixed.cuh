@@ -128,14 +128,16 @@ __device__ __forceinline__ float2 f2mul(float2 a, float2 b) {
 // the shared window there); the multi-tile and ensemble kernels get shared
 // loads from the pointers and run faster with them than with these
 // volatile forms, so the access form is a template choice (SH).
+// The loads name memory too, so that no compiler pass moves them across
+// the block barriers or across the other accesses of the planes.
 __device__ __forceinline__ float2 lds2(unsigned a) {
   float2 v;
-  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a) : "memory");
   return v;
 }
 __device__ __forceinline__ float lds1(unsigned a) {
   float v;
-  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
+  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a) : "memory");
   return v;
 }
 __device__ __forceinline__ void sts2(unsigned a, float2 v) {
