@@ -147,6 +147,8 @@ def make_case(args):
     if args.workload == "channel":
         case = deck.channel_inflow(CHANNEL["ncx"], CHANNEL["ncy"], CHANNEL["re"], CHANNEL["dt"],
                                    seed=args.seed, solver=args.solver)
+    elif args.workload == "clustered":
+        case = deck.clustered_cavity(args.n, args.re, args.dt, solver=args.solver)
     elif args.workload == "thermal":
         case = deck.heated_cavity(args.n, args.re, args.dt, solver=args.solver, pr=THERMAL["pr"],
                                   fr=THERMAL["fr"], nmeiter=THERMAL["nmeiter"], dmeittol=THERMAL["dmeittol"])
@@ -325,6 +327,14 @@ def config_of(args, case, inner=None):
                 f"as a per-row inlet profile, zero-gradient mass-conserving outlet (bound_cond.f BM_OUTLT2), "
                 f"no-slip walls, ppe_solver {args.solver}, {prec}")
         re, dt = CHANNEL["re"], CHANNEL["dt"]
+    elif args.workload == "clustered":
+        work = (f"lid-driven cavity {args.n}x{args.n} cells clustered towards the walls (nodes s - 0.5 "
+                f"sin(2 pi s)/(2 pi): cell widths 0.5/n to 1.5/n, no Poisson row the unit stencil), "
+                f"Re={args.re:g}, dt={args.dt:g} (2.5e-4 drives the reference scheme to NaN on these cells), "
+                f"seeded 16x16-mode streamfunction perturbation "
+                f"(seed {args.seed}), ppe_solver {args.solver}, the reference's default Poisson settings, "
+                f"{prec}; the mixed Poisson solve runs the general-row kernel")
+        re, dt = args.re, args.dt
     else:
         prm = case.params
         conv = ("" if args.ppe_defaults else
@@ -340,6 +350,23 @@ def config_of(args, case, inner=None):
             "ppe_solver": args.solver, "sor_relaxation": prm.sorrel, "sor_tolerance": prm.sortol,
             "max_sor_iter": prm.msorit, "precision": args.precision,
             "l2": "flushed between timed steps (256 MiB write); per-step working set > 2x L2"}
+
+
+def ppe_bytes_general(cells, nsor):
+    """Algorithmic bytes of one plain Ppe call with general rows: RHS reads
+    us, vs and writes b (3 words); each sweep reads p, b, a1..a5 and writes p
+    (8 words)."""
+    return 8.0 * cells * (3 + 8 * nsor)
+
+
+def mixed_ppe_bytes_general(cells, nsor, inner):
+    """Algorithmic bytes of one mixed Ppe call with general rows: RHS reads
+    us, vs and writes div (FP64, 24 B/cell); per refinement pass the residual
+    reads p, div, a1..a5 (FP64) and writes r, e (FP32) = 64 B, the correction
+    reads p, e and writes p = 20 B; each FP32 sweep reads e, r, c1..c5 and
+    writes e = 32 B."""
+    passes = -(-nsor // inner)
+    return cells * (24.0 + passes * 84.0 + 32.0 * nsor)
 
 
 def mixed_ppe_bytes(cells, nsor, inner):
@@ -420,8 +447,9 @@ def run_arm(s, prm, args, precision, u0, v0, p0, st, flush, barrier, local, time
             "clk": clk, "wall": t_wall, "fields": fields}
 
 
-def kernel_name(kind, precision, tiled, thermal=False):
-    """The kernel a profile kind stands for in this workload."""
+def kernel_name(kind, precision, tiled, thermal=False, general=False):
+    """The kernel a profile kind stands for in this workload (general: the
+    Poisson rows are not the unit stencil)."""
     from wolfd2_gb300.gpu import K_COPY, K_MOMENTUM, K_POST, K_PPE, K_THERM, KERNEL_NAMES
     if thermal and kind == K_POST:
         return "k_me_post+k_step_tail_th"
@@ -430,7 +458,9 @@ def kernel_name(kind, precision, tiled, thermal=False):
     if kind == K_THERM:
         return "k_therm+k_eq_state"
     if kind == K_PPE:
-        return "k_ppe_mixed" if precision == "mixed" else ("k_ppe_tiled" if tiled else "k_ppe")
+        if precision == "mixed":
+            return "k_ppe_mixg" if general else "k_ppe_mixed"
+        return "k_ppe_tiled" if tiled else "k_ppe"
     if kind == K_MOMENTUM:
         return "k_naux32" if precision == "mixed" else "k_naux"
     if kind == K_COPY and precision == "mixed":
@@ -441,7 +471,7 @@ def kernel_name(kind, precision, tiled, thermal=False):
 FP64_PEAK_GOPS = 628.0
 
 
-def roofline_of(arm, cells, precision, inner, tiled=True, sorrel=1.0):
+def roofline_of(arm, cells, precision, inner, tiled=True, sorrel=1.0, general=False):
     """Roofline of the dominant kernel of one arm (HBM view) and the FP64
     pipe view of the plain red/black sweep."""
     from wolfd2_gb300.gpu import K_MOMENTUM, K_PPE
@@ -453,16 +483,17 @@ def roofline_of(arm, cells, precision, inner, tiled=True, sorrel=1.0):
     nsor = [h[1] for h in timed]
     if dom == K_PPE:
         if precision == "mixed":
-            alg = sum(mixed_ppe_bytes(cells, n, inner) for n in nsor)
+            mb = mixed_ppe_bytes_general if general else mixed_ppe_bytes
+            alg = sum(mb(cells, n, inner) for n in nsor)
         else:
-            alg = sum(ppe_bytes(cells, n) for n in nsor)
+            alg = sum((ppe_bytes_general if general else ppe_bytes)(cells, n) for n in nsor)
     else:
         alg = sum(mom_bytes(cells, n, 4 if precision == "mixed" else 8) for n in nql)
     dom_ms, dom_n = prof[dom]
     # with momentum/energy iterations a step launches the kernel once per
     # iteration; the step record holds the last iteration's counts
     alg *= dom_n / max(1, len(timed))
-    name = kernel_name(dom, precision, tiled)
+    name = kernel_name(dom, precision, tiled, general=general)
     achieved = alg / (dom_ms / 1e3) / 1e9
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
@@ -475,7 +506,7 @@ def roofline_of(arm, cells, precision, inner, tiled=True, sorrel=1.0):
             "frac": achieved / hbm_peak, "peak_kind": peak_kind, "traffic": traffic,
             "alg_bytes_per_launch": alg / dom_n, "avg_launch_ms": dom_ms / dom_n}
     fp64 = None
-    if precision == "fp64" and prof[K_PPE][0] > 0:
+    if precision == "fp64" and prof[K_PPE][0] > 0 and not general:
         # unit-stencil red/black point: 4 subtractions, 1 multiply by -1/4,
         # 1 subtraction, the product by sorrel (when it is not 1) and 1
         # addition per point and sweep; the sweeps are the FP64 pipe's work
@@ -562,18 +593,19 @@ def run_ours(args):
     value = world * cells * args.steps / t_max
     e2e_value = world * cells * head["e2e_steps"] / t_e2e_max
     # the plain path's red/black solve runs on shared-memory tiles at this size
-    tiled = args.solver in ("rb_sor", "par_rb_sor") and cells >= 152 * 1024
-    roof, fp64 = roofline_of(head, cells, args.precision, inner, tiled, prm.sorrel)
+    tiled = args.solver in ("rb_sor", "par_rb_sor") and cells >= 152 * 1024 and args.workload != "clustered"
+    general = args.workload == "clustered"
+    roof, fp64 = roofline_of(head, cells, args.precision, inner, tiled, prm.sorrel, general)
     plain = None
     accuracy = None
     if args.precision == "mixed":
         a64 = arms["fp64"]
-        r64, f64 = roofline_of(a64, cells, "fp64", inner, tiled, prm.sorrel)
+        r64, f64 = roofline_of(a64, cells, "fp64", inner, tiled, prm.sorrel, general)
         plain = {"value": world * cells * args.steps / a64["t_dev"], "unit": UNIT,
                  "ms_per_step": 1e3 * a64["t_dev"] / args.steps,
                  "e2e": world * cells * a64["e2e_steps"] / a64["t_e2e"],
                  "roofline": r64, "fp64_roof": f64, "gpu_launches": a64["launches"],
-                 "kernel_ms": {kernel_name(k, "fp64", tiled): {"total_ms": v[0], "launches": v[1]}
+                 "kernel_ms": {kernel_name(k, "fp64", tiled, general=general): {"total_ms": v[0], "launches": v[1]}
                                for k, v in a64["prof"].items()},
                  "iterations": [[h[0], h[1]] for h in a64["timed"]],
                  "clocks": a64["clk"].summary()}
@@ -646,7 +678,8 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "clocks": head["clk"].summary(),
         "gpu_launches": head["launches"],
-        "kernel_ms": {kernel_name(k, args.precision, tiled, t0 is not None): {"total_ms": v[0], "launches": v[1]}
+        "kernel_ms": {kernel_name(k, args.precision, tiled, t0 is not None, general): {"total_ms": v[0],
+                                                                                      "launches": v[1]}
                       for k, v in head["prof"].items()},
         "iterations": [[h[0], h[1]] for h in head["timed"]],
         "chain": {"max_verify_rounds": chain_rounds, "sequential_fallbacks": chain_fallbacks},
@@ -1014,12 +1047,13 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["cavity", "channel", "ensemble", "adjoint", "thermal"],
+    ap.add_argument("--workload", choices=["cavity", "channel", "ensemble", "adjoint", "thermal", "clustered"],
                     default="cavity",
                     help="cavity: the lid-driven cavity (--n cells per side); channel: the "
                          "4096x1024 plane channel with a profiled inflow; ensemble: 256 cavities "
                          "of uneven size and Re advanced together; thermal: the differentially "
-                         "heated cavity with the energy equation (--n cells per side)")
+                         "heated cavity with the energy equation (--n cells per side); clustered: "
+                         "the lid-driven cavity on a wall-clustered Cartesian grid (--n cells per side)")
     ap.add_argument("--ens-count", type=int, default=ENSEMBLE["count"])
     ap.add_argument("--ens-seed", type=int, default=ENSEMBLE["seed"])
     ap.add_argument("--no-graph", action="store_true", help="ensemble: launch directly, no CUDA graph")
@@ -1038,7 +1072,9 @@ def main():
                     help="adjoint: also check against the fourth-order central difference (4 runs per direction)")
     ap.add_argument("--n", type=int, default=1024, help="cavity cells per side")
     ap.add_argument("--re", type=float, default=1000.0)
-    ap.add_argument("--dt", type=float, default=2.5e-4)
+    ap.add_argument("--dt", type=float, default=0.0,
+                    help="time step (0: 2.5e-4; the clustered cavity 6.25e-5, the same CFL number on its "
+                         "smallest cells, where 2.5e-4 drives the reference scheme to NaN)")
     ap.add_argument("--solver", default="rb_sor", choices=sorted(deck.PPE_SOLVERS))
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--e2e-steps", type=int, default=3)
@@ -1064,6 +1100,8 @@ def main():
     ap.add_argument("--mixed-mode", type=int, default=0,
                     help="mixed: tile mode (0 auto, 1 several tiles per block, 3 two resident blocks per SM)")
     args = ap.parse_args()
+    if not args.dt:
+        args.dt = 6.25e-5 if args.workload == "clustered" else 2.5e-4
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "ensemble":

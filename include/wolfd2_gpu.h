@@ -66,9 +66,11 @@ extern "C" {
 #define W2_PREC_MIXED 1   /* red/black Poisson sweeps in FP32 on the
                              correction equation, FP64 residual and
                              correction (iterative refinement); npsolver 5
-                             or 6 on Cartesian grids whose Poisson rows
-                             round to the unit stencil in FP32 (uniform
-                             square cells, no blockages)                 */
+                             or 6 on any grid (rows that round to the unit
+                             stencil in FP32 take the tile kernel, others
+                             -- non-square cells, blockages, curvilinear
+                             grids -- the general-row kernel); porous
+                             decks run plain FP64                        */
 
 typedef struct w2_ctx w2_ctx;
 

@@ -87,6 +87,116 @@ def is_unit_stencil32(nx: int, ny: int, met) -> bool:
                 np.all(a[3] == 1) and np.all(a[4] == 1))
 
 
+def blockage_rows(nx: int, ny: int, regions) -> np.ndarray:
+    """The cells whose Poisson row becomes the identity (0, 0, 1, 0, 0) and
+    whose divergence is zeroed, by the blockage loops of pressure.f:109-196:
+    a boolean (nx+2, ny+2) array indexed (i, j)."""
+    idn = np.zeros((nx + 2, ny + 2), dtype=bool)
+    if regions is None:
+        return idn
+    ni, nj = regions.n_i, regions.n_j
+    blk = 0  # RM_BLOCKG
+    W, E, S, N = 1, 2, 3, 4
+    for jr in range(1, nj + 1):
+        for ir in range(1, ni + 1):
+            if regions.rtype(ir, jr) != blk:
+                continue
+            iw, ie = regions.border(ir, jr, W), regions.border(ir, jr, E)
+            js, jn = regions.border(ir, jr, S), regions.border(ir, jr, N)
+            idn[iw + 2:ie, js + 2:jn] = True
+            if ir > 1 and regions.rtype(ir - 1, jr) == blk:
+                idn[iw + 1, js + 1:jn + 1] = True
+            if ir < ni and regions.rtype(ir + 1, jr) == blk:
+                idn[ie, js + 1:jn + 1] = True
+            if jr > 1 and regions.rtype(ir, jr - 1) == blk:
+                idn[iw + 1:ie + 1, js + 1] = True
+            if jr < nj and regions.rtype(ir, jr + 1) == blk:
+                idn[iw + 1:ie + 1, jn] = True
+    return idn
+
+
+def _cross(nx: int, ny: int, rbu, rbv, P):
+    """RhsPpe's non-Cartesian cross terms (src/pressure.f:360-375) on the
+    unknowns, in its operand order and in the type of P and the metric
+    arrays: rbu(i,j) (...) - rbu(i-1,j) (...) + rbv(i,j) (...) - rbv(i,j-1) (...)."""
+    def s(a, di, dj):
+        return a[2 + di:nx + 1 + di, 2 + dj:ny + 1 + dj]
+    return (s(rbu, 0, 0) * (s(P, 1, 1) + s(P, 0, 1) - s(P, 1, -1) - s(P, 0, -1)) -
+            s(rbu, -1, 0) * (s(P, 0, 1) + s(P, -1, 1) - s(P, 0, -1) - s(P, -1, -1)) +
+            s(rbv, 0, 0) * (s(P, 1, 1) + s(P, 1, 0) - s(P, -1, 1) - s(P, -1, 0)) -
+            s(rbv, 0, -1) * (s(P, 1, 0) + s(P, 1, -1) - s(P, -1, 0) - s(P, -1, -1)))
+
+
+def ppe_mixed_general(nx: int, ny: int, met, u, v, p, dk: float, msorit: int, sortol: float,
+                      sorrel: float, inner: int, regions=None, lcartes: int = 1) -> int:
+    """Mixed Ppe with the grid's own Poisson rows in the FP32 sweeps: any
+    Cartesian grid (cells of any shape and spacing, blockage identity rows)
+    and, with lcartes = 0, curvilinear grids.
+
+    Each refinement pass forms r = RhsPpe(p) - A p in FP64 with the rows of
+    pressure.f:97-196 (RhsPpe's cross terms of the current p when lcartes =
+    0), then relaxes A e = r from e = 0 in FP32 with the rows rounded to
+    FP32 (c_k = a_k): per sweep (lcartes = 0: r' = r - the cross terms of e
+    in FP32, with rbu, rbv rounded to FP32, formed before the sweep as the
+    reference forms its right-hand side), black points then red,
+    s = r' - c1 eS - c2 eW - c4 eE - c5 eN, s = s / c3 - e, e = e + sorrel s,
+    dif = max |s|.  Stopping rule and pass lengths as ppe_mixed.  On unit
+    rows every operation equals the unit form's bit for bit (1 x == x,
+    x / -4 == x * -0.25)."""
+    f32 = np.float32
+    a1, a2, a3, a4, a5 = (a.copy() for a in ppe_rows(nx, ny, met))
+    idn = blockage_rows(nx, ny, regions)[2:nx + 1, 2:ny + 1]
+    for a in (a1, a2, a4, a5):
+        a[idn] = 0.0
+    a3[idn] = 1.0
+    div = divergence(nx, ny, met, u, v)
+    div[idn] = 0.0
+    b = div / dk
+    c1, c2, c3, c4, c5 = (a.astype(f32) for a in (a1, a2, a3, a4, a5))
+    rbu32, rbv32 = met["rbu"].astype(f32), met["rbv"].astype(f32)
+    I, J = np.meshgrid(np.arange(2, nx + 1), np.arange(2, ny + 1), indexing="ij")
+    cols = []
+    for c in (0, 1):
+        sel = ((I + J) & 1) == c
+        cols.append((I[sel], J[sel], sel))
+    relax = f32(sorrel)
+    m = 0
+    result = 0
+    done = False
+    while not done:
+        ps = p[2:nx + 1, 2:ny + 1]
+        bb = b if lcartes else b - _cross(nx, ny, met["rbu"], met["rbv"], p)
+        ap = (a1 * p[2:nx + 1, 1:ny] + a2 * p[1:nx, 2:ny + 1] + a4 * p[3:nx + 2, 2:ny + 1] +
+              a5 * p[2:nx + 1, 3:ny + 2] + a3 * ps)
+        R = (bb - ap).astype(f32)
+        E = np.zeros((nx + 2, ny + 2), dtype=f32)
+        in_pass = 0
+        while True:
+            m += 1
+            RR = R if lcartes else R - _cross(nx, ny, rbu32, rbv32, E)
+            dif = f32(0.0)
+            for ii, jj, sel in cols:
+                c0 = E[ii, jj]
+                s = RR[sel] - c1[sel] * E[ii, jj - 1] - c2[sel] * E[ii - 1, jj] - \
+                    c4[sel] * E[ii + 1, jj] - c5[sel] * E[ii, jj + 1]
+                s = s / c3[sel] - c0
+                E[ii, jj] = c0 + relax * s
+                if s.size:
+                    dif = max(dif, np.max(np.abs(s)))
+            if m > 1 and float(dif) < sortol:
+                result = m
+                done = True
+                break
+            in_pass += 1
+            if m >= msorit:
+                done = True
+                break
+            if in_pass >= inner:
+                break
+        p[2:nx + 1, 2:ny + 1] = ps + E[2:nx + 1, 2:ny + 1].astype(np.float64)
+    return result if result >= 1 else msorit
+
+
 def ppe_mixed(nx: int, ny: int, met, u, v, p, dk: float, msorit: int, sortol: float,
               sorrel: float, inner: int, dtype=np.float32) -> int:
     """Mixed Ppe on a Cartesian grid without blockages whose Poisson rows
@@ -165,6 +275,10 @@ class MixedRun:
                 self.f[k][...] = val
         self.history = []
         self.cold_nconv = None
+        # the unit-stencil sweeps where every row rounds to it in FP32 on a
+        # Cartesian grid without blockages, else the grid's own rows
+        self.general = not (self.prm.lcartes and is_unit_stencil32(self.nx, self.ny, self.met) and
+                            not blockage_rows(self.nx, self.ny, case.regions).any())
         if cold_start:
             f, o, nx, ny, r = self.f, self.o, self.nx, self.ny, case.regions
             o.vel_bound_cond(nx, ny, r, f["u"], f["v"])
@@ -175,6 +289,9 @@ class MixedRun:
 
     def _ppe(self, u, v, p) -> int:
         prm = self.prm
+        if self.general:
+            return ppe_mixed_general(self.nx, self.ny, self.met, u, v, p, prm.dk, prm.msorit, prm.sortol,
+                                     prm.sorrel, self.inner, regions=self.case.regions, lcartes=prm.lcartes)
         return ppe_mixed(self.nx, self.ny, self.met, u, v, p, prm.dk, prm.msorit, prm.sortol,
                          prm.sorrel, self.inner)
 

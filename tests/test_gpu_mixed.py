@@ -181,13 +181,6 @@ def test_mixed_rejects_unsupported():
         s.step(case.params, 1, precision=PREC_MIXED)  # lexicographic SOR
     with pytest.raises(W2Error):
         s.tune_mixed(2, 0)
-    # cells 0.0625 x 0.05: Poisson rows (1.25, 0.8, -4.1, 0.8, 1.25), not the unit stencil in FP32
-    odd = deck.channel(40, 20, 800.0, 0.004, length=2.5, solver="rb_sor", outlet="mc")
-    s2 = Solver.for_case(odd)
-    z = s2.field()
-    s2.load_fields(z, z, z)
-    with pytest.raises(W2Error):
-        s2.step(odd.params, 1, precision=PREC_MIXED)
 
 
 @pytest.mark.parametrize("n", [48, 96])

@@ -109,3 +109,52 @@ def test_mixed_time_loop_close_to_fp64():
         assert _rel(mx.f[name], ref.f[name]) <= 1e-6, name
     d64 = M.div_check(case.nx, case.ny, ref.met, ref.f["u"], ref.f["v"])
     assert mx.history[-1][3] <= 2.0 * d64 + 1e-14
+
+
+def _general_layouts():
+    import thermal_setup
+    case_c, _, _ = thermal_setup.problem()
+    case_c.params.lcartes = 0
+    st = deck.cavity(40, 400.0, 0.001, solver="rb_sor")
+    st.x = 0.5 * (1.0 - np.cos(np.pi * st.x))
+    st.y = 0.5 * (1.0 - np.cos(np.pi * st.y))
+    return {"nonsquare": deck.channel(40, 20, 800.0, 0.004, length=2.5, solver="rb_sor", outlet="mc"),
+            "stretched": st, "blockage": thermal_setup.blockage_case(), "curvilinear": case_c}
+
+
+@pytest.mark.parametrize("sorrel", [1.0, 1.7])
+def test_general_model_equals_unit_model_on_unit_rows(sorrel):
+    """On unit rows every operation of the general-row sweep rounds as the
+    unit form's (1 x == x, x / -4 == x * -0.25): the same p bit for bit."""
+    case, o, met, u, v, p = _setup(48, seed=9)
+    p1, p2 = p.copy(order="F"), p.copy(order="F")
+    n1 = M.ppe_mixed(case.nx, case.ny, met, u, v, p1, case.params.dk, 500, 1e-7, sorrel, 32)
+    n2 = M.ppe_mixed_general(case.nx, case.ny, met, u, v, p2, case.params.dk, 500, 1e-7, sorrel, 32,
+                             regions=case.regions)
+    assert n1 == n2 and np.array_equal(p1, p2)
+
+
+@pytest.mark.parametrize("layout", ["nonsquare", "stretched", "blockage", "curvilinear"])
+@pytest.mark.parametrize("sortol", [1e-6, 1e-9])
+def test_general_model_stops_where_fp64_stops(layout, sortol):
+    """General rows (non-square and unequal cells, blockage identity rows,
+    RhsPpe's cross terms on a curvilinear grid): the FP32 sweeps with FP64
+    refinement stop on the oracle's sweep and land within P_REL_TOL of its
+    p; at the tight tolerance the two agree to 1e-12."""
+    case = _general_layouts()[layout]
+    o = O.Oracle(case.nx + 1, case.ny + 1)
+    met = o.grid(case.nx, case.ny, case.x, case.y)
+    rng = np.random.default_rng(2)
+    u, v, p = (np.asfortranarray(rng.normal(size=(case.nx + 2, case.ny + 2)) * 0.05) for _ in range(3))
+    o.vel_bound_cond(case.nx, case.ny, case.regions, u, v)
+    o.pres_bound_cond(case.nx, case.ny, case.regions, p)
+    assert not (case.params.lcartes and M.is_unit_stencil32(case.nx, case.ny, met)
+                and not M.blockage_rows(case.nx, case.ny, case.regions).any())
+    prm = deck.RunParams(**{**case.params.__dict__, "sortol": sortol})
+    p64 = p.copy(order="F")
+    n64 = o.ppe(case.nx, case.ny, case.regions, prm, met, u, v, p64, npsolver=5, msorit=3000)
+    pm = p.copy(order="F")
+    nm = M.ppe_mixed_general(case.nx, case.ny, met, u, v, pm, prm.dk, 3000, sortol, prm.sorrel, 32,
+                             regions=case.regions, lcartes=prm.lcartes)
+    assert n64 < 3000 and nm == n64
+    assert _rel(pm, p64) <= (1e-12 if sortol < 1e-8 else P_REL_TOL)

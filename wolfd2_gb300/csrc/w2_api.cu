@@ -78,6 +78,11 @@ struct w2_ctx {
                        // 3 one tile per block with two blocks per SM
   size_t mixed_smem = 0;
   MixedGeom mg{};
+  // mixed Poisson sweeps with the grid's own rows (grids whose rows are not
+  // the unit stencil in FP32, blockages, curvilinear grids), made on first use
+  float *mgbuf = nullptr;       // MG_PLANES colour-split planes
+  float *mg_rb = nullptr;       // FP32 rbu, rbv in field layout
+  bool mg_coef_ok = false;      // coefficient planes of the current metrics
   int prec_dropin = W2_PREC_FP64, refine_dropin = 0;
   // single-precision momentum state (mixed path), made on first use
   bool f32_alloc = false, f32_metrics_ok = false;
@@ -915,16 +920,47 @@ void plan_mixed(w2_ctx *c) {
   }
 }
 
-// The mixed path covers npsolver 5/6 on Cartesian grids whose rows are all
-// the unit stencil in FP32 (no blockages): every uniform square-cell grid.
+// The mixed Poisson solve takes npsolver 5/6 on every grid: the unit-stencil
+// kernel where the rows round to (1,1,-4,1,1) in FP32 on a Cartesian grid
+// without blockages (every uniform square-cell grid), the general-row kernel
+// everywhere else.
+bool mixed_general(const w2_ctx *c, int lcartes) { return !lcartes || !c->dev.ppe_unit32; }
+
 int mixed_check(w2_ctx *c, int lcartes, int npsolver) {
   if (npsolver != 5 && npsolver != 6)
     return fail(c, W2_E_UNSUPPORTED, "mixed precision needs ppe_solver rb_sor or rb_sorp (5/6), got %d", npsolver);
-  if (!lcartes || !c->dev.ppe_unit32)
-    return fail(c, W2_E_UNSUPPORTED,
-                "mixed precision needs a Cartesian grid whose Poisson rows round to the unit stencil in FP32 "
-                "(uniform square cells, no blockages)");
+  if (mixed_general(c, lcartes)) return W2_OK;
   if (!c->mixed_ok) return fail(c, W2_E_UNSUPPORTED, "no mixed-precision tile plan fits this grid");
+  return W2_OK;
+}
+
+MixgArgs mixg_args(w2_ctx *c, int lcartes, int msorit, double dk, double sortol, double sorrel, int inner,
+                   const double *u, const double *v, double *p) {
+  return MixgArgs{lcartes, msorit, inner, dk, sortol, (float)sorrel, u, v, p, c->mgbuf, mixg_gw(c->nx),
+                  c->mg_rb, c->mg_rb + c->nf};
+}
+
+// The general-row kernel's planes (zeroed: cells off the unknowns keep e =
+// 0), its FP32 rbu and rbv, and its coefficient planes for the current
+// metrics.
+int ensure_mixg(w2_ctx *c) {
+  const size_t plane = (size_t)mixg_gw(c->nx) * (c->ny + 2);
+  if (!c->mgbuf) {
+    if (!(c->mgbuf = dalloc<float>(c, MG_PLANES * plane)) || !(c->mg_rb = dalloc<float>(c, 2 * c->nf)))
+      return fail(c, W2_E_CUDA, "out of device memory (mixed Poisson planes)");
+    CK(cudaMemsetAsync(c->mgbuf, 0, MG_PLANES * plane * sizeof(float), c->st));
+    c->mg_coef_ok = false;
+  }
+  if (!c->mg_coef_ok) {
+    const int gb = grid_blocks(c);
+    MixgArgs a = mixg_args(c, 1, 0, 1.0, 0.0, 1.0, 1, nullptr, nullptr, nullptr);
+    k_mixg_coef<<<gb, c->threads, 0, c->st>>>(c->dev, a);
+    k_to_f32<<<gb, c->threads, 0, c->st>>>(c->dev, c->met[M_RBU], c->mg_rb);
+    k_to_f32<<<gb, c->threads, 0, c->st>>>(c->dev, c->met[M_RBV], c->mg_rb + c->nf);
+    c->launches += 3;
+    CK(cudaGetLastError());
+    c->mg_coef_ok = true;
+  }
   return W2_OK;
 }
 
@@ -935,6 +971,14 @@ int auto_inner(w2_ctx *c, int req) {
 
 int launch_ppe_mixed(w2_ctx *c, int lcartes, int msorit, double dk, double sortol, double sorrel,
                      int inner, const double *u, const double *v, double *p, StepOut *out) {
+  if (mixed_general(c, lcartes)) {
+    if (int rc = ensure_mixg(c)) return rc;
+    Dev d = c->dev;
+    MixgArgs a = mixg_args(c, lcartes, msorit, dk, sortol, sorrel, auto_inner(c, inner), u, v, p);
+    void *args[] = {&d, &a, &out};
+    return coop(c, (const void *)k_ppe_mixg, pick_blocks(c, (const void *)k_ppe_mixg, (long)c->nx * c->ny),
+                args);
+  }
   Dev d = c->dev;
   MixedGeom g = c->mg;
   const size_t plane2 = 2 * (size_t)c->mg.gh * c->mg.gw;
@@ -1195,6 +1239,7 @@ static int finish_coefficients(w2_ctx *c) {
   CK(cudaStreamSynchronize(c->st));
   c->dev.ppe_unit = (h & 1) ? 0 : 1;
   c->dev.ppe_unit32 = (h & 2) ? 0 : 1;
+  c->mg_coef_ok = false;
   plan_tiles(c);
   plan_mixed(c);
   return momentum_metrics(c);
@@ -2145,6 +2190,8 @@ int wolfd2gpu_step(w2_ctx *c, const w2_params *prm, int nsteps, w2_stepstat *sta
   if (c->therm_on && (prm->precision != W2_PREC_FP64 || prm->nfiltu == 1 || prm->nfiltv == 1))
     return fail(c, W2_E_UNSUPPORTED, "the time loop with the energy equation runs plain FP64 without Filter");
   if (prm->precision == W2_PREC_MIXED && (rc = ensure_f32(c))) return rc;
+  // the general-row Poisson planes are made before any launch is captured
+  if (prm->precision == W2_PREC_MIXED && mixed_general(c, prm->lcartes) && (rc = ensure_mixg(c))) return rc;
   // one step writes the other level; two or more write both
   if (nsteps >= 2) snap_fence(c);
   else if (nsteps == 1) snap_fence(c, 1 - c->cur);

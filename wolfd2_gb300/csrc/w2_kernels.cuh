@@ -4,6 +4,7 @@
 #include "w2_momentum.cuh"
 #include "w2_ppe.cuh"
 #include "w2_ppe_mixed.cuh"
+#include "w2_ppe_mixg.cuh"
 #include "w2_ppe_tiled.cuh"
 
 namespace w2 {
@@ -352,6 +353,22 @@ __global__ void __launch_bounds__(kMixedThreads, 1) k_ppe_mixed(Dev d, MixedGeom
   const int nconv = ppe_mixed<K, RES>(d, g, a);
   if (nconv < 0) return;
   if (vblock() == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? a.msorit : nconv;
+}
+
+// Mixed-precision red/black SOR with the grid's own rows (any Cartesian
+// grid, blockages, curvilinear grids): one grid barrier per colour.
+__global__ void __launch_bounds__(kMaxThreads) k_ppe_mixg(Dev d, MixgArgs a, StepOut *out) {
+  vgrid_set(0, gridDim.x);
+  if (step_skip(d)) return;
+  const int nconv = ppe_mixg(d, a);
+  if (nconv < 0) return;
+  if (vblock() == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? a.msorit : nconv;
+}
+
+// Its FP32 coefficient planes, formed once per metric upload.
+__global__ void k_mixg_coef(Dev d, MixgArgs a) {
+  vgrid_set(0, gridDim.x);
+  mixg_coefficients(d, a);
 }
 
 // ---- Project (utility.f:253-440), masked -------------------------------

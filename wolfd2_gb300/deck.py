@@ -584,6 +584,20 @@ def cavity(n: int, re: float, dt: float, *, lid: float = 1.0,
     return Case(f"cavity{n}x{ncy}_re{re:g}", nx, nyy, X, Y, regs, prm, bc)
 
 
+def clustered_cavity(n: int, re: float, dt: float, *, beta: float = 0.5, **kw) -> Case:
+    """The lid-driven cavity of ``cavity`` on a Cartesian grid whose cells
+    cluster towards the walls: node k of either direction at
+    s - beta sin(2 pi s) / (2 pi), s = k / n, so cell widths run from (1 -
+    beta) / n at the walls to (1 + beta) / n in the middle and no Poisson
+    row is the unit stencil."""
+    case = cavity(n, re, dt, **kw)
+    warp = lambda s: s - beta * np.sin(2.0 * np.pi * s) / (2.0 * np.pi)
+    case.x = np.asfortranarray(warp(case.x))
+    case.y = np.asfortranarray(warp(case.y))
+    case.name = f"clustered{n}_re{re:g}"
+    return case
+
+
 def heated_cavity(n: int, re: float, dt: float, *, pr: float = 0.71, fr: float = 0.05,
                   lid: float = 0.0, nmeiter: int = 3, dmeittol: float = 1.0e-6,
                   eqstate: bool = True, solver: str = "rb_sor", t_hot: float = 1.0,
