@@ -459,7 +459,8 @@ def kernel_name(kind, precision, tiled, thermal=False, general=False):
         return "k_therm+k_eq_state"
     if kind == K_PPE:
         if precision == "mixed":
-            return "k_ppe_mixg" if general else "k_ppe_mixed"
+            # general rows on a Cartesian grid: the tiled general-row form
+            return "k_ppe_mixgt" if general else "k_ppe_mixed"
         return "k_ppe_tiled" if tiled else "k_ppe"
     if kind == K_MOMENTUM:
         return "k_naux32" if precision == "mixed" else "k_naux"

@@ -342,7 +342,10 @@ const char *wolfd2gpu_last_error(w2_ctx *ctx);
  * blocks_per_sm = -1 selects the one-colour-per-barrier red/black sweep,
  * -2 forces the tiled two-sweeps-per-barrier form at any grid size, -3 runs
  * that form in 1024-thread blocks (two points in flight per thread instead
- * of four in 512-thread blocks), -4 returns to 512-thread blocks.
+ * of four in 512-thread blocks), -4 returns to 512-thread blocks.  For the
+ * mixed Poisson solve with general rows, -5 selects the form with one grid
+ * barrier per colour on Cartesian grids too, -6 returns to the tiled form
+ * (four sweeps per grid barrier; the default on Cartesian grids).
  * Takes effect on the next launch. */
 int wolfd2gpu_tune(w2_ctx *ctx, int chain_seg, int chain_warm, int threads,
                    int blocks_per_sm);

@@ -133,3 +133,26 @@ def test_mixed_general_cold_start_matches_model():
     u, v, p = s.store_fields()
     for nm, g in (("u", u), ("v", v), ("p", p)):
         assert np.array_equal(g, model.f[nm]), nm
+
+
+@pytest.mark.parametrize("layout", ["nonsquare", "blockage", "nonsquare_big"])
+@pytest.mark.parametrize("sortol,inner", [(1e-9, 24), (2e-7, 7)])
+def test_mixed_general_forms_agree(layout, sortol, inner):
+    """Cartesian grids run the tiled form (four sweeps per grid barrier on
+    halo'd tiles) by default; the one-grid-barrier-per-colour form gives
+    the same bits, and both equal the model."""
+    case = LAYOUTS[layout]()
+    o, met, u, v, p = _inputs(case, 31)
+    out = []
+    for form in (-6, -5):  # tiled, then one barrier per colour
+        s = Solver.for_case(case)
+        s.tune(blocks_per_sm=form)
+        s.set_precision(PREC_MIXED, inner)
+        gp = p.copy(order="F")
+        out.append((s.Ppe(True, 5, 3000, case.params.dk, sortol, 1.0, u, v, gp), gp))
+    pm = p.copy(order="F")
+    n_m = M.ppe_mixed_general(case.nx, case.ny, met, u, v, pm, case.params.dk, 3000, sortol, 1.0, inner,
+                              regions=case.regions)
+    for n_g, gp in out:
+        assert n_g == n_m
+        assert np.array_equal(gp, pm), _rel(gp, pm)

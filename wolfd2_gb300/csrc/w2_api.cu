@@ -83,6 +83,14 @@ struct w2_ctx {
   float *mgbuf = nullptr;       // MG_PLANES colour-split planes
   float *mg_rb = nullptr;       // FP32 rbu, rbv in field layout
   bool mg_coef_ok = false;      // coefficient planes of the current metrics
+  // its tiled form (Cartesian grids): tile plan, buffers (c1..c5, r, e0, e1
+  // in field layout), and the switch between the two forms
+  bool mgt_ok = false;
+  MixgtGeom mgt{};
+  int mgt_blocks = 0;
+  size_t mgt_smem = 0;
+  float *mgt_buf = nullptr;
+  int use_mixgt = 1;
   int prec_dropin = W2_PREC_FP64, refine_dropin = 0;
   // single-precision momentum state (mixed path), made on first use
   bool f32_alloc = false, f32_metrics_ok = false;
@@ -926,6 +934,48 @@ void plan_mixed(w2_ctx *c) {
 // everywhere else.
 bool mixed_general(const w2_ctx *c, int lcartes) { return !lcartes || !c->dev.ppe_unit32; }
 
+// Tile plan of the general-row kernel's tiled form: one or more blocks of
+// kMixgtThreads per SM, as many as shared memory allows; the split of the
+// unknowns into tiles minimising tiles per block x (sweep work of a group
+// on the shrinking boxes + staging of the box).
+void plan_mixgt(w2_ctx *c) {
+  c->mgt_ok = false;
+  int maxsmem = 0;
+  cudaDeviceGetAttribute(&maxsmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+  const void *kf = (const void *)k_ppe_mixgt;
+  cudaFuncAttributes fa{};
+  if (cudaFuncGetAttributes(&fa, kf) != cudaSuccess || (size_t)maxsmem <= fa.sharedSizeBytes) return;
+  const size_t limit = (size_t)maxsmem - fa.sharedSizeBytes;
+  if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit) != cudaSuccess) return;
+  const int NX = c->nx - 1, NY = c->ny - 1, H = kMixgtH, K = kMixgtK;
+  double best = 1e300;
+  for (int ntx = 1; ntx <= NX; ++ntx) {
+    const int tx = (NX + ntx - 1) / ntx;
+    if ((NX + tx - 1) / tx != ntx) continue;
+    for (int nty = 1; nty <= NY; ++nty) {
+      const int ty = (NY + nty - 1) / nty;
+      if ((NY + ty - 1) / ty != nty) continue;
+      const size_t smem = mixgt_smem_bytes(tx, ty);
+      if (smem > limit) continue;
+      int occ = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kf, kMixgtThreads, smem);
+      if (occ < 1) continue;
+      const int tiles = ntx * nty, cap = c->nsm * occ;
+      const int tpb = (tiles + cap - 1) / cap;
+      const double cost = tpb * ((double)K * (tx + H) * (ty + H) + 2.0 * (tx + 2 * H) * (ty + 2 * H));
+      if (cost < best) {
+        best = cost;
+        c->mgt = MixgtGeom{tx, ty, ntx, nty};
+        c->mgt_smem = smem;
+        c->mgt_blocks = (tiles + tpb - 1) / tpb;
+      }
+    }
+  }
+  c->mgt_ok = best < 1e300;
+}
+
+bool mixgt_applies(const w2_ctx *c, int lcartes) { return lcartes && c->use_mixgt && c->mgt_ok; }
+
 int mixed_check(w2_ctx *c, int lcartes, int npsolver) {
   if (npsolver != 5 && npsolver != 6)
     return fail(c, W2_E_UNSUPPORTED, "mixed precision needs ppe_solver rb_sor or rb_sorp (5/6), got %d", npsolver);
@@ -958,6 +1008,15 @@ int ensure_mixg(w2_ctx *c) {
     k_to_f32<<<gb, c->threads, 0, c->st>>>(c->dev, c->met[M_RBU], c->mg_rb);
     k_to_f32<<<gb, c->threads, 0, c->st>>>(c->dev, c->met[M_RBV], c->mg_rb + c->nf);
     c->launches += 3;
+    if (!c->mgt_buf) {
+      if (!(c->mgt_buf = dalloc<float>(c, 8 * c->nf)))
+        return fail(c, W2_E_CUDA, "out of device memory (tiled mixed Poisson buffers)");
+      CK(cudaMemsetAsync(c->mgt_buf, 0, 8 * c->nf * sizeof(float), c->st));
+    }
+    float *b = c->mgt_buf;
+    const size_t nf = c->nf;
+    k_mixgt_coef<<<gb, c->threads, 0, c->st>>>(c->dev, b, b + nf, b + 2 * nf, b + 3 * nf, b + 4 * nf);
+    c->launches++;
     CK(cudaGetLastError());
     c->mg_coef_ok = true;
   }
@@ -974,6 +1033,19 @@ int launch_ppe_mixed(w2_ctx *c, int lcartes, int msorit, double dk, double sorto
   if (mixed_general(c, lcartes)) {
     if (int rc = ensure_mixg(c)) return rc;
     Dev d = c->dev;
+    if (mixgt_applies(c, lcartes)) {
+      float *b = c->mgt_buf;
+      const size_t nf = c->nf;
+      MixgtGeom g = c->mgt;
+      MixgtArgs a{msorit, auto_inner(c, inner), dk, sortol, (float)sorrel, u, v, p,
+                  {b, b + nf, b + 2 * nf, b + 3 * nf, b + 4 * nf}, b + 5 * nf, {b + 6 * nf, b + 7 * nf}};
+      void *args[] = {&d, &g, &a, &out};
+      c->launches++;
+      cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_ppe_mixgt, dim3(c->mgt_blocks),
+                                                  dim3(kMixgtThreads), args, c->mgt_smem, c->st);
+      if (e != cudaSuccess) return fail(c, W2_E_CUDA, "tiled mixed PPE launch: %s", cudaGetErrorString(e));
+      return W2_OK;
+    }
     MixgArgs a = mixg_args(c, lcartes, msorit, dk, sortol, sorrel, auto_inner(c, inner), u, v, p);
     void *args[] = {&d, &a, &out};
     return coop(c, (const void *)k_ppe_mixg, pick_blocks(c, (const void *)k_ppe_mixg, (long)c->nx * c->ny),
@@ -1210,6 +1282,11 @@ int wolfd2gpu_tune(w2_ctx *c, int chain_seg, int chain_warm, int threads, int bl
     // -1: one colour per barrier for red/black SOR; -2: tiled sweeps at any size
     c->use_tiled = blocks_per_sm == -1 ? 0 : 2;
     blocks_per_sm = 0;
+  } else if (blocks_per_sm == -5 || blocks_per_sm == -6) {
+    // general-row mixed Poisson: one grid barrier per colour (-5) or the
+    // tiled form on Cartesian grids (-6, the default)
+    c->use_mixgt = blocks_per_sm == -6 ? 1 : 0;
+    blocks_per_sm = 0;
   } else if (blocks_per_sm == -3 || blocks_per_sm == -4) {
     // tiled sweeps in 1024-thread blocks (-3) or back to 512-thread blocks (-4)
     c->tiled_wide = blocks_per_sm == -3 ? 1 : 0;
@@ -1241,6 +1318,7 @@ static int finish_coefficients(w2_ctx *c) {
   c->dev.ppe_unit32 = (h & 2) ? 0 : 1;
   c->mg_coef_ok = false;
   plan_tiles(c);
+  plan_mixgt(c);
   plan_mixed(c);
   return momentum_metrics(c);
 }
@@ -2152,11 +2230,13 @@ std::string graph_key(const w2_ctx *c, const w2_params *prm, int nsteps) {
   std::string k;
   auto add = [&](const void *p, size_t n) { k.append((const char *)p, n); };
   const int head[] = {c->cur, nsteps, c->threads, c->blocks_per_sm, c->mixed_K, c->mixed_blocks,
-                      c->tiled_blocks, c->tiled_threads, c->use_tiled, (int)c->tiled_ok, (int)c->mixed_ok};
+                      c->tiled_blocks, c->tiled_threads, c->use_tiled, (int)c->tiled_ok, (int)c->mixed_ok,
+                      c->use_mixgt, (int)c->mgt_ok, c->mgt_blocks};
   add(head, sizeof(head));
   add(prm, sizeof(*prm));
   add(&c->dev, sizeof(c->dev));
   add(&c->mg, sizeof(c->mg));
+  add(&c->mgt, sizeof(c->mgt));
   add(&c->tg, sizeof(c->tg));
   const size_t sm[] = {c->mixed_smem, c->tiled_smem};
   add(sm, sizeof(sm));

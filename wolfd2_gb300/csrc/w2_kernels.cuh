@@ -371,6 +371,31 @@ __global__ void k_mixg_coef(Dev d, MixgArgs a) {
   mixg_coefficients(d, a);
 }
 
+// The tiled form for Cartesian grids: kMixgtK sweeps per grid barrier on
+// halo'd tiles in shared memory.
+__global__ void __launch_bounds__(kMixgtThreads, 1) k_ppe_mixgt(Dev d, MixgtGeom g, MixgtArgs a, StepOut *out) {
+  vgrid_set(0, gridDim.x);
+  if (step_skip(d)) return;
+  const int nconv = ppe_mixgt(d, g, a);
+  if (nconv < 0) return;
+  if (vblock() == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? a.msorit : nconv;
+}
+
+// Its FP32 rows c1..c5 in field layout (every unknown; zeros elsewhere
+// from the allocation).
+__global__ void k_mixgt_coef(Dev d, float *c1, float *c2, float *c3, float *c4, float *c5) {
+  vgrid_set(0, gridDim.x);
+  const int nx = d.nx, ny = d.ny;
+  for (int t = gtid(); t < (nx - 1) * (ny - 1); t += gthreads()) {
+    const size_t o = IX(d, t % (nx - 1) + 2, t / (nx - 1) + 2);
+    c1[o] = (float)d.pa1[o];
+    c2[o] = (float)d.pa2[o];
+    c3[o] = (float)d.pa3[o];
+    c4[o] = (float)d.pa4[o];
+    c5[o] = (float)d.pa5[o];
+  }
+}
+
 // ---- Project (utility.f:253-440), masked -------------------------------
 __device__ void project_grid(const Dev &d, double dk, const double *p, double *u, double *v) {
   const int nx = d.nx, ny = d.ny, W = nx + 2, H = ny + 2;

@@ -25,9 +25,11 @@
 // k+1.  Cells off the unknowns hold e = 0 (the ghost pressures stay frozen
 // during the iteration, so their correction is zero) and are never written.
 // One grid barrier separates the colours, one ends the sweep (and, with
-// lcartes = 0, one follows the cross-term pass).
+// lcartes = 0, one follows the cross-term pass).  Cartesian grids run the
+// tiled form at the end of this file instead, K sweeps per grid barrier.
 #pragma once
 #include "w2_ppe.cuh"
+#include "w2_ppe_mixed.cuh"
 
 namespace w2 {
 
@@ -149,17 +151,25 @@ __device__ unsigned int mixg_half(const Dev &d, const MixgArgs &a, int c, float 
   const float *__restrict__ Eo = mixg_plane(a, ny, MG_E + (c ^ 1));
   float *__restrict__ Ec = mixg_plane(a, ny, MG_E + c);
   unsigned int mx = 0u;
-  for (int t0 = gtid(); t0 < total; t0 += kMixgBatch * T) {
+  // (j, k) of point t, advanced by T points at a time without a division
+  const int dj = T / nk, dk = T % nk;
+  int t = gtid(), j = 2 + t / nk, k = 1 + t % nk;
+  while (t < total) {
     int x[kMixgBatch], par[kMixgBatch];
     bool ok[kMixgBatch];
 #pragma unroll
     for (int q = 0; q < kMixgBatch; ++q) {
-      const int t = t0 + q * T;
-      const int j = 2 + t / nk, k = 1 + t % nk;
       par[q] = (c + j) & 1;
       ok[q] = t < total && 2 * k + par[q] <= nx;
       x[q] = ok[q] ? j * gw + k : gw + 1;
       if (!ok[q]) par[q] = 0;
+      t += T;
+      k += dk;
+      j += dj;
+      if (k > nk) {
+        k -= nk;
+        ++j;
+      }
     }
     float r[kMixgBatch], c1[kMixgBatch], c2[kMixgBatch], c3[kMixgBatch], c4[kMixgBatch], c5[kMixgBatch];
     float e0[kMixgBatch], es[kMixgBatch], ew[kMixgBatch], ee[kMixgBatch], en[kMixgBatch];
@@ -255,6 +265,292 @@ __device__ int ppe_mixg(const Dev &d, const MixgArgs &a) {
       if (in_pass >= a.inner) break;
     }
     mixg_correct(d, a);
+    if (!grid_sync(sy)) return -1;
+  }
+  return result;
+}
+
+
+// ---- tiled form (Cartesian grids) ------------------------------------------
+// The same iteration on halo'd tiles in shared memory, K sweeps per grid
+// barrier, as the plain tiled sweep does it (w2_ppe_tiled.cuh): each block
+// stages, for every tile it owns, the tile grown by H = 2K cells of e, r and
+// c1..c5 (natural (i, j) layout, FP32), runs the colour half-sweeps on
+// boxes that shrink by one cell per half-sweep -- black on the tile grown
+// by H-1, red on H-2, ... -- so that every point of the box it covers sees
+// exactly the values a global sweep would, then writes its tile's e.  e is
+// double-buffered in global memory between groups.  lcartes = 0 keeps the
+// one-colour-per-barrier kernel above (its cross terms need e on the
+// diagonals of every point at the start of each sweep).
+constexpr int kMixgtK = 4;
+constexpr int kMixgtH = 2 * kMixgtK;
+constexpr int kMixgtThreads = 512;
+constexpr int kMixgtPlanes = 7;  // e, r, c1..c5
+
+struct MixgtGeom {
+  int tx, ty;    // tile size in unknowns
+  int ntx, nty;  // tiles per direction
+};
+
+struct MixgtArgs {
+  int msorit, inner;
+  double dk, sortol;
+  float relax;
+  const double *u, *v;
+  double *p;
+  const float *c[5];  // c1..c5 in field layout, zero off the unknowns
+  float *r;           // r in field layout, zero off the unknowns
+  float *e[2];        // e, double-buffered, zero off the unknowns
+};
+
+__host__ __device__ inline size_t mixgt_smem_bytes(int tx, int ty) {
+  return (size_t)kMixgtPlanes * (tx + 2 * kMixgtH) * (ty + 2 * kMixgtH) * sizeof(float);
+}
+
+// r = RhsPpe(p) - A p (Cartesian: div/dk - A p) in FP64 on the unknowns.
+__device__ void mixgt_residual(const Dev &d, const MixgtArgs &a) {
+  const int nx = d.nx, ny = d.ny;
+  for (int t = gtid(); t < (nx - 1) * (ny - 1); t += gthreads()) {
+    const int i = t % (nx - 1) + 2, j = t / (nx - 1) + 2;
+    const size_t o = IX(d, i, j);
+    const double bb = rhs_point(d, 1, a.dk, a.p, i, j);
+    const double ap = d.pa1[o] * a.p[o - d.ld] + d.pa2[o] * a.p[o - 1] + d.pa4[o] * a.p[o + 1] +
+                      d.pa5[o] * a.p[o + d.ld] + d.pa3[o] * a.p[o];
+    a.r[o] = (float)(bb - ap);
+  }
+}
+
+// A tile's own unknowns and its box.
+struct MixgtBox {
+  int oi0, oi1, oj0, oj1;  // own tile, clipped to the unknowns
+  int gi0, gj0, bw, bh;    // box origin and size
+};
+
+__device__ __forceinline__ MixgtBox mixgt_box(const Dev &d, const MixgtGeom &g, int tile) {
+  MixgtBox b;
+  const int ti = tile % g.ntx, tj = tile / g.ntx;
+  b.oi0 = 2 + ti * g.tx;
+  b.oj0 = 2 + tj * g.ty;
+  b.oi1 = min(d.nx, b.oi0 + g.tx - 1);
+  b.oj1 = min(d.ny, b.oj0 + g.ty - 1);
+  b.gi0 = b.oi0 - kMixgtH;
+  b.gj0 = b.oj0 - kMixgtH;
+  b.bw = g.tx + 2 * kMixgtH;
+  b.bh = g.ty + 2 * kMixgtH;
+  return b;
+}
+
+// Stage the box: e from ein (zeros when ein is null), r, c1..c5; zeros
+// outside the stored field.
+__device__ void mixgt_stage(const Dev &d, const MixgtArgs &a, const MixgtBox &b, const float *ein,
+                            float *S) {
+  const int n = b.bw * b.bh, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const float *c1 = a.c[0], *c2 = a.c[1], *c3 = a.c[2], *c4 = a.c[3], *c5 = a.c[4], *r = a.r;
+  for (int jj = threadIdx.x >> 5; jj < b.bh; jj += nw) {
+    const int j = b.gj0 + jj;
+    const bool jin = j >= 0 && j <= d.ny + 1;
+    for (int ii = lane; ii < b.bw; ii += 32) {
+      const int i = b.gi0 + ii, t = jj * b.bw + ii;
+      const bool in = jin && i >= 0 && i <= d.nx + 1;
+      const size_t o = in ? IX(d, i, j) : 0;
+      S[t] = (in && ein) ? ein[o] : 0.0f;
+      S[n + t] = in ? r[o] : 0.0f;
+      S[2 * n + t] = in ? c1[o] : 0.0f;
+      S[3 * n + t] = in ? c2[o] : 0.0f;
+      S[4 * n + t] = in ? c3[o] : 0.0f;
+      S[5 * n + t] = in ? c4[o] : 0.0f;
+      S[6 * n + t] = in ? c5[o] : 0.0f;
+    }
+  }
+}
+
+// Half-sweep of colour c over the box [bi0,bi1] x [bj0,bj1] (clipped to the
+// unknowns) of the staged planes; the colour's points numbered row by row,
+// kMixgBatch of a thread's points loaded before any is updated.  Returns
+// max |s| (IEEE bits) over the own tile's points.
+__device__ unsigned int mixgt_half(float *S, const MixgtBox &b, int bi0, int bi1, int bj0, int bj1, int c,
+                                   float relax) {
+  unsigned int mx = 0u;
+  const int rows = bj1 - bj0 + 1;
+  if (rows <= 0 || bi1 < bi0) return 0u;
+  const int n = b.bw * b.bh, bw = b.bw;
+  float *E = S;
+  const float *R = S + n, *C1 = S + 2 * n, *C2 = S + 3 * n, *C3 = S + 4 * n, *C4 = S + 5 * n,
+              *C5 = S + 6 * n;
+  const int wmax = (bi1 - bi0) / 2 + 1, total = rows * wmax, T = blockDim.x;
+  // (j, k) of point t, advanced by T points at a time without a division
+  const int dj = T / wmax, dk = T % wmax;
+  int t = threadIdx.x, j = bj0 + t / wmax, k = t % wmax;
+  while (t < total) {
+    int x[kMixgBatch];
+    bool ok[kMixgBatch], own[kMixgBatch];
+#pragma unroll
+    for (int q = 0; q < kMixgBatch; ++q) {
+      const int i = bi0 + 2 * k + ((bi0 + j + c) & 1);
+      ok[q] = t < total && i <= bi1;
+      own[q] = ok[q] && i >= b.oi0 && i <= b.oi1 && j >= b.oj0 && j <= b.oj1;
+      x[q] = ok[q] ? (i - b.gi0) + (j - b.gj0) * bw : bw + 1;
+      t += T;
+      k += dk;
+      j += dj;
+      if (k >= wmax) {
+        k -= wmax;
+        ++j;
+      }
+    }
+    float r[kMixgBatch], c1[kMixgBatch], c2[kMixgBatch], c3[kMixgBatch], c4[kMixgBatch], c5[kMixgBatch];
+    float e0[kMixgBatch], es[kMixgBatch], ew[kMixgBatch], ee[kMixgBatch], en[kMixgBatch];
+#pragma unroll
+    for (int q = 0; q < kMixgBatch; ++q) {
+      r[q] = R[x[q]];
+      c1[q] = C1[x[q]];
+      c2[q] = C2[x[q]];
+      c3[q] = C3[x[q]];
+      c4[q] = C4[x[q]];
+      c5[q] = C5[x[q]];
+      e0[q] = E[x[q]];
+      es[q] = E[x[q] - bw];
+      ew[q] = E[x[q] - 1];
+      ee[q] = E[x[q] + 1];
+      en[q] = E[x[q] + bw];
+    }
+#pragma unroll
+    for (int q = 0; q < kMixgBatch; ++q) {
+      float s = r[q] - c1[q] * es[q];
+      s = s - c2[q] * ew[q];
+      s = s - c4[q] * ee[q];
+      s = s - c5[q] * en[q];
+      s = s / c3[q];
+      s = s - e0[q];
+      if (ok[q]) E[x[q]] = e0[q] + relax * s;
+      if (own[q]) {
+        const unsigned int bb = __float_as_uint(s) & 0x7fffffffu;
+        mx = bb > mx ? bb : mx;
+      }
+    }
+  }
+  return mx;
+}
+
+// ns sweeps of every tile this block owns, from ein (null: e = 0) to eout;
+// per-sweep maxima into slots (null: not recorded).
+__device__ void mixgt_group(const Dev &d, const MixgtGeom &g, const MixgtArgs &a, int ns, const float *ein,
+                            float *eout, unsigned long long *slots) {
+  extern __shared__ __align__(16) float mgt_smem[];
+  __shared__ unsigned int redm[kMixgtK][32];
+  unsigned int mxs[kMixgtK];
+#pragma unroll
+  for (int s = 0; s < kMixgtK; ++s) mxs[s] = 0u;
+  const int ntiles = g.ntx * g.nty;
+  for (int tile = vblock(); tile < ntiles; tile += vblocks()) {
+    const MixgtBox b = mixgt_box(d, g, tile);
+    mixgt_stage(d, a, b, ein, mgt_smem);
+    __syncthreads();
+    for (int s = 0; s < ns; ++s) {
+      for (int c = 0; c < 2; ++c) {
+        const int grow = kMixgtH - 1 - 2 * s - c;
+        const int bi0 = max(2, b.oi0 - grow), bi1 = min(d.nx, b.oi1 + grow);
+        const int bj0 = max(2, b.oj0 - grow), bj1 = min(d.ny, b.oj1 + grow);
+        const unsigned int m = mixgt_half(mgt_smem, b, bi0, bi1, bj0, bj1, c, a.relax);
+#pragma unroll
+        for (int q = 0; q < kMixgtK; ++q)
+          if (q == s) mxs[q] = m > mxs[q] ? m : mxs[q];
+        __syncthreads();
+      }
+    }
+    const int tw = b.oi1 - b.oi0 + 1, th = b.oj1 - b.oj0 + 1;
+    for (int t = threadIdx.x; t < tw * th; t += blockDim.x) {
+      const int i = b.oi0 + t % tw, j = b.oj0 + t / tw;
+      eout[IX(d, i, j)] = mgt_smem[(i - b.gi0) + (j - b.gj0) * b.bw];
+    }
+    __syncthreads();
+  }
+  if (!slots) return;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int s = 0; s < kMixgtK; ++s) {
+    const unsigned int v = __reduce_max_sync(0xffffffffu, mxs[s]);
+    if (lane == 0) redm[s][w] = v;
+  }
+  __syncthreads();
+  if (w < ns) {
+    const unsigned int v = __reduce_max_sync(0xffffffffu, lane < nw ? redm[w][lane] : 0u);
+    if (lane == 0 && v)
+      atomicMax(&slots[w], (unsigned long long)__double_as_longlong((double)__uint_as_float(v)));
+  }
+  __syncthreads();
+}
+
+// p += e on the own tiles of this block, FP64.
+__device__ void mixgt_correct(const Dev &d, const MixgtGeom &g, const MixgtArgs &a, const float *e) {
+  const int ntiles = g.ntx * g.nty;
+  for (int tile = vblock(); tile < ntiles; tile += vblocks()) {
+    const MixgtBox b = mixgt_box(d, g, tile);
+    const int tw = b.oi1 - b.oi0 + 1, th = b.oj1 - b.oj0 + 1;
+    for (int t = threadIdx.x; t < tw * th; t += blockDim.x) {
+      const size_t o = IX(d, b.oi0 + t % tw, b.oj0 + t / tw);
+      a.p[o] = a.p[o] + (double)e[o];
+    }
+  }
+}
+
+// The whole Ppe on tiles (Cartesian grids).  Per-sweep maxima in the ring
+// red[kMixedRing ..] of three groups of kMixgtK slots: group q writes set
+// q % 3 and, before its barrier, block 0 clears set (q + 1) % 3, last read
+// by every block before the barrier of group q - 1.  When the stopping rule
+// fires on sweep s < ns of a group, the group's input buffer is intact and
+// the tiles are swept again from it for s + 1 sweeps.  Returns nConv (0 =
+// not converged) or -1 on a barrier error.
+__device__ int ppe_mixgt(const Dev &d, const MixgtGeom &g, const MixgtArgs &a) {
+  Sync *sy = d.sync;
+  unsigned long long *ring = &sy->red[kMixedRing];
+  if (vblock() == 0 && threadIdx.x == 0)
+    for (int k = 0; k < 3 * kMixgtK; ++k) ring[k] = 0ull;
+  ppe_divergence(d, a.u, a.v);
+  if (!grid_sync(sy)) return -1;
+  int m = 0, result = 0, grp = 0;
+  bool done = false;
+  while (!done) {
+    mixgt_residual(d, a);
+    if (!grid_sync(sy)) return -1;
+    int q = 0, in_pass = 0;
+    const float *efinal = nullptr;
+    while (true) {
+      const int ns = min(kMixgtK, min(a.inner - in_pass, a.msorit - m));
+      unsigned long long *slots = ring + (grp % 3) * kMixgtK;
+      if (vblock() == 0 && threadIdx.x == 0) {
+        unsigned long long *next = ring + ((grp + 1) % 3) * kMixgtK;
+        for (int k = 0; k < kMixgtK; ++k) next[k] = 0ull;
+      }
+      const float *ein = q == 0 ? nullptr : a.e[(q + 1) & 1];
+      float *eout = a.e[q & 1];
+      mixgt_group(d, g, a, ns, ein, eout, slots);
+      if (!grid_sync(sy)) return -1;
+      int conv = -1;
+      for (int s = 0; s < ns; ++s) {
+        if (m + s + 1 > 1 && slot_value(&slots[s]) < a.sortol) {
+          conv = s;
+          break;
+        }
+      }
+      ++grp;
+      ++q;
+      efinal = eout;
+      if (conv >= 0) {
+        result = m + conv + 1;
+        if (conv < ns - 1) mixgt_group(d, g, a, conv + 1, ein, eout, nullptr);
+        done = true;
+        break;
+      }
+      m += ns;
+      in_pass += ns;
+      if (m >= a.msorit) {
+        done = true;
+        break;
+      }
+      if (in_pass >= a.inner) break;
+    }
+    mixgt_correct(d, g, a, efinal);
     if (!grid_sync(sy)) return -1;
   }
   return result;
