@@ -940,6 +940,8 @@ bool mixed_general(const w2_ctx *c, int lcartes) { return !lcartes || !c->dev.pp
 // on the shrinking boxes + staging of the box).
 void plan_mixgt(w2_ctx *c) {
   c->mgt_ok = false;
+  // rows that round to the unit stencil take the unit kernel on Cartesian grids
+  if (c->dev.ppe_unit32) return;
   int maxsmem = 0;
   cudaDeviceGetAttribute(&maxsmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
   const void *kf = (const void *)k_ppe_mixgt;
