@@ -420,8 +420,9 @@ int wolfd2gpu_profile_read(w2_ctx *ctx, int kind, double *total_ms,
  * partition sized by the cases' cells), with its own barriers, convergence
  * tests and iteration counts.  Each case is an ordinary context, set up as
  * usual (metrics, regions, fields).  One call steps every case in the same
- * precision: W2_PREC_MIXED (Cartesian unit-stencil grids, rb_sor or
- * rb_sorp, in every case) or W2_PREC_FP64 (any grid and any of the six
+ * precision: W2_PREC_MIXED (rb_sor or rb_sorp in every case; unit-row
+ * cases on the multi-tile kernel, which needs a Cartesian grid, the others
+ * on the general-row kernel) or W2_PREC_FP64 (any grid and any of the six
  * Poisson solvers, per case).  Filter is not applied (W2_E_UNSUPPORTED).
  * Per case, results are bit-identical to wolfd2gpu_step on that context
  * alone.

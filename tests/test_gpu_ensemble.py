@@ -122,7 +122,7 @@ def test_plain_ensemble_matches_cases_alone(graph):
         got = s.store_fields()
         for name, g, r in zip("uvp", got, ref):
             assert np.array_equal(g, r), (k, name, float(np.max(np.abs(g - r))))
-    # these grids have no mixed Poisson plan
+    # lexicographic and line solvers have no mixed form
     with pytest.raises(Exception):
         ens.step([c.params for c, _ in cases], 1, precision=PREC_MIXED)
     ens.close()
@@ -151,6 +151,49 @@ def test_ensemble_switches_precision():
         for x, y in zip(s.store_fields(), a.store_fields()):
             assert np.array_equal(x, y)
         a.close()
+    ens.close()
+    for s in solvers:
+        s.close()
+
+
+def _general_cases():
+    """Cases whose Poisson rows are not the unit stencil in FP32 beside
+    unit-row ones: a channel with non-square cells, a blockage, a
+    wall-clustered cavity, a curvilinear layout with RhsPpe's cross terms
+    (lCartesGrid = 0), and two unit-row cavities."""
+    import thermal_setup
+    curv, _, _ = thermal_setup.problem(36, 24)
+    curv.params.lcartes = 0
+    gen = [deck.channel(40, 20, 800.0, 0.004, length=2.5, solver="rb_sor", outlet="mc"),
+           thermal_setup.blockage_case(),
+           deck.clustered_cavity(48, 400.0, 0.002, solver="rb_sor"),
+           curv]
+    out = [(c, deck.perturbation_ic(c, 300 + k)) for k, c in enumerate(gen)]
+    return out + _cases()[:2]
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_mixed_ensemble_general_rows_matches_cases_alone(graph):
+    """The mixed step of an ensemble mixing general-row cases (the
+    general-row Poisson kernel on their block groups) with unit-row ones
+    (the multi-tile unit kernel): per case bit-identical to the case alone
+    (which runs the tiled general-row form on Cartesian grids)."""
+    cases = _general_cases()
+    nsteps = 3
+    solvers = []
+    for case, f in cases:
+        s = Solver.for_case(case, tuned=False)
+        s.load_fields(*f)
+        solvers.append(s)
+    ens = Ensemble(solvers, graph=graph)
+    hist = ens.step([c.params for c, _ in cases], nsteps, refine_sweeps=REFINE)
+    for k, ((case, f), s) in enumerate(zip(cases, solvers)):
+        ref_hist, ref = _alone(case, f, nsteps)
+        assert [(h[0], h[1]) for h in hist[k]] == [(h[0], h[1]) for h in ref_hist], k
+        assert [h[2][:3] for h in hist[k]] == [h[2][:3] for h in ref_hist], k
+        got = s.store_fields()
+        for name, g, r in zip("uvp", got, ref):
+            assert np.array_equal(g, r), (k, name, float(np.max(np.abs(g - r))))
     ens.close()
     for s in solvers:
         s.close()

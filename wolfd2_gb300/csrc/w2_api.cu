@@ -2614,9 +2614,8 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
   e->threads = threads;
   e->K = sweeps_per_barrier;
   e->cs.assign(cases, cases + n);
-  // the mixed step needs Poisson rows that round to the unit stencil in
-  // FP32 in every case
-  bool unit = true;
+  // cases whose Poisson rows round to the unit stencil in FP32 take the
+  // multi-tile unit kernel in the mixed step, the others the general-row one
   for (int k = 0; k < n; ++k) {
     w2_ctx *c = e->cs[k];
     if (!c) return bad(efail(e, W2_E_ARG, "case %d is null", k));
@@ -2624,14 +2623,14 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
     if (c->porous) return bad(efail(e, W2_E_UNSUPPORTED, "case %d: porous regions run single-case steps", k));
     if (c->therm_on)
       return bad(efail(e, W2_E_UNSUPPORTED, "case %d: ensembles do not run the energy equation", k));
-    unit = unit && c->dev.ppe_unit32;
     if (k == 0) e->device = c->device;
     else if (c->device != e->device) return bad(efail(e, W2_E_ARG, "cases on different devices"));
   }
   for (int k = 0; k < n; ++k) {
     w2_ctx *c = e->cs[k];
-    if (unit)
-      if (int rc = ensure_f32(c)) return bad(efail(e, rc, "case %d: %s", k, c->err));
+    if (int rc = ensure_f32(c)) return bad(efail(e, rc, "case %d: %s", k, c->err));
+    if (!c->dev.ppe_unit32)
+      if (int rc = ensure_mixg(c)) return bad(efail(e, rc, "case %d: %s", k, c->err));
     if (cudaStreamSynchronize(c->st) != cudaSuccess) return bad(efail(e, W2_E_CUDA, "case %d: set-up failed", k));
   }
   if (cudaSetDevice(e->device) != cudaSuccess) return bad(efail(e, W2_E_CUDA, "cudaSetDevice"));
@@ -2673,7 +2672,7 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
   cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device);
   cudaFuncAttributes fa{};
   if (cudaFuncGetAttributes(&fa, kp) != cudaSuccess) return bad(efail(e, W2_E_CUDA, "kernel attributes"));
-  for (int per_sm = 4; unit && per_sm >= 1; --per_sm) {
+  for (int per_sm = 4; per_sm >= 1; --per_sm) {
     const size_t smax = std::min<size_t>((size_t)smem_optin, (size_t)smem_sm / per_sm - 1024) - fa.sharedSizeBytes;
     const int total = per_sm * e->nsm;
     std::vector<int> bp = ens_partition(work, total);
@@ -2682,6 +2681,7 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
     size_t smem = 0;
     bool ok = true;
     for (int k = 0; k < n && ok; ++k) {
+      if (!e->cs[k]->dev.ppe_unit32) continue;  // general rows: no tiles, no dynamic shared memory
       size_t sk = 0;
       ok = ens_plan(e->cs[k], e->K, bp[k], threads, smax, &g[k], &sk);
       smem = std::max(smem, sk);
@@ -2700,8 +2700,7 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
   }
   e->mixed_ok = !e->bp.empty();
   if (!e->mixed_ok)
-    e->mixed_why = unit ? "no Poisson tile plan fits every case in blocks of this many threads and sweeps per barrier"
-                        : "the mixed step needs Poisson rows that round to the unit stencil in FP32 in every case";
+    e->mixed_why = "no Poisson tile plan fits every case in blocks of this many threads and sweeps per barrier";
   if (!e->mixed_ok) {
     // plain steps only: the Poisson table is unused
     e->bp = e->bm;
@@ -2714,11 +2713,12 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
     EnsCase &h = e->h[k];
     const MixedGeom &g = h.g;
     const size_t plane2 = 2 * (size_t)g.gh * g.gw;
+    h.general = c->dev.ppe_unit32 ? 0 : 1;
     float *xb = nullptr;
-    if (e->mixed_ok && !(xb = ealloc<float>(e, 3 * plane2)))
+    if (e->mixed_ok && !h.general && !(xb = ealloc<float>(e, 3 * plane2)))
       return bad(efail(e, W2_E_CUDA, "out of device memory (case %d Poisson buffers)", k));
     const CUtensorMap *tm = nullptr;
-    if (e->mixed_ok && c->use_tma) {
+    if (e->mixed_ok && !h.general && c->use_tma) {
       if (!e->d_tm && !(e->d_tm = ealloc<CUtensorMap>(e, 3 * (size_t)n)))
         return bad(efail(e, W2_E_CUDA, "out of device memory (tensor maps)"));
       if (encode_mixed_maps(e->d_tm + 3 * k, xb, g, e->K, c->st)) tm = e->d_tm + 3 * k;
@@ -2737,6 +2737,7 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
       h.a[b].xbuf1 = xb + plane2;
       h.a[b].rbuf = xb + 2 * plane2;
       h.a[b].tm = tm;
+      h.ga[b] = h.general ? mixg_args(c, 1, 0, 1.0, 0.0, 1.0, 1, c->U[b], c->V[b], c->P[b]) : MixgArgs{};
     }
     for (int q = 0; q < 4; ++q) h.F32[q] = c->F32[q];
   }
@@ -2780,8 +2781,12 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
     if ((q.precision == W2_PREC_MIXED) != mixed)
       return efail(e, W2_E_UNSUPPORTED, "case %d: every case of one call runs in the same precision", k);
     if (mixed && !e->mixed_ok) return efail(e, W2_E_UNSUPPORTED, "%s", e->mixed_why);
-    if (mixed && ((q.npsolver != 5 && q.npsolver != 6) || !q.lcartes))
-      return efail(e, W2_E_UNSUPPORTED, "case %d: the mixed step needs rb_sor/rb_sorp on a Cartesian grid", k);
+    if (mixed && q.npsolver != 5 && q.npsolver != 6)
+      return efail(e, W2_E_UNSUPPORTED, "case %d: the mixed step needs rb_sor or rb_sorp", k);
+    if (mixed && !q.lcartes && !e->h[k].general)
+      return efail(e, W2_E_UNSUPPORTED,
+                   "case %d: in an ensemble the mixed step takes lCartesGrid = 0 only on grids whose rows are not "
+                   "the unit stencil", k);
     if (q.npsolver < 1 || q.npsolver > 6) return efail(e, W2_E_ARG, "case %d: bad Poisson solver %d", k, q.npsolver);
     if (q.nfiltu == 1 || q.nfiltv == 1) return efail(e, W2_E_UNSUPPORTED, "case %d: the ensemble does not apply Filter", k);
     if (q.msorit < 1 || q.mqiter < 1 || q.refine_sweeps < 0) return efail(e, W2_E_ARG, "case %d: bad parameters", k);
@@ -2817,6 +2822,13 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
       a.dk = q.dk;
       a.sortol = q.sortol;
       a.relax = (float)q.sorrel;
+      MixgArgs &ga = h.ga[b];
+      ga.lcartes = q.lcartes;
+      ga.msorit = q.msorit;
+      ga.inner = a.inner;
+      ga.dk = q.dk;
+      ga.sortol = q.sortol;
+      ga.relax = (float)q.sorrel;
     }
   }
   ECK(cudaMemcpyAsync(e->d_cases, e->h.data(), sizeof(EnsCase) * n, cudaMemcpyHostToDevice, e->st));

@@ -31,6 +31,8 @@ struct EnsCase {
   double dk, re, qtol;
   int npsolver, lcartes, msorit;  // plain step's Ppe
   double sortol, sorrel;
+  int general;             // Poisson rows not the unit stencil in FP32: the
+  MixgArgs ga[2];          // general-row mixed Ppe, forming level 0 / 1
 };
 
 // Arguments shared by the launches of one ensemble step.
@@ -97,10 +99,10 @@ __global__ void __launch_bounds__(kMixedThreads, 1) ke_ppe_mixed(EnsLaunch L) {
   const EnsCase &e = L.cs[k];
   if (e.d.sync->halt) return;
   const int b = ens_level(e, L) ^ 1;
-  const MixedArgs &a = e.a[b];
-  const int nconv = ppe_mixed<K, false>(e.d, e.g, a);
+  const int msorit = e.general ? e.ga[b].msorit : e.a[b].msorit;
+  const int nconv = e.general ? ppe_mixg(e.d, e.ga[b]) : ppe_mixed<K, false>(e.d, e.g, e.a[b]);
   if (nconv < 0) return;
-  if (vblock() == 0 && threadIdx.x == 0) ens_out(L, k)->nsor = nconv < 1 ? a.msorit : nconv;
+  if (vblock() == 0 && threadIdx.x == 0) ens_out(L, k)->nsor = nconv < 1 ? msorit : nconv;
 }
 
 __global__ void __launch_bounds__(kMaxThreads) ke_step_post(EnsLaunch L) {
