@@ -69,8 +69,7 @@ extern "C" {
                              or 6 on any grid (rows that round to the unit
                              stencil in FP32 take the tile kernel, others
                              -- non-square cells, blockages, curvilinear
-                             grids -- the general-row kernel); porous
-                             decks run plain FP64                        */
+                             grids -- the general-row kernel)            */
 
 typedef struct w2_ctx w2_ctx;
 
@@ -84,9 +83,9 @@ typedef struct w2_ctx w2_ctx;
  * tables (output of SetUpBCs, src/bound_cond.f:34-443) and, where nRegType
  * has porous regions, their porosity and Dupuit-Forchheimer constants
  * (output of PorRegCnst, src/bound_cond.f:1883-1986; may be NULL without
- * porous regions).  Porous regions run on the plain FP64 momentum path
- * (the drop-in nAuxMomentum and the FP64 step); the mixed step, the
- * ensemble and the adjoint return W2_E_UNSUPPORTED for them.  Fields are
+ * porous regions).  Porous regions run in the drop-in nAuxMomentum, the
+ * FP64 step and the mixed step (its FP32 momentum on the tables rounded to
+ * FP32); the ensemble and the adjoint return W2_E_UNSUPPORTED for them.  Fields are
  * zero.  No reference counterpart (the reference keeps these as static
  * arrays). */
 int wolfd2gpu_create(w2_ctx **ctx, int mnx, int mny, int mgri, int mgrj,

@@ -1,14 +1,16 @@
-"""Porous regions on the device (FP64 momentum path): the porosity division
-of the convective coefficients (momentum.f:296-324, 621-649) and the
-PorosCoef terms of both split steps (momentum.f:1115-1226), against the
-oracle (itself pinned to the translated reference on the same layouts).
-The bar is bit-for-bit equality."""
+"""Porous regions on the device: the porosity division of the convective
+coefficients (momentum.f:296-324, 621-649) and the PorosCoef terms of both
+split steps (momentum.f:1115-1226).  The FP64 path against the oracle
+(itself pinned to the translated reference on the same layouts), the mixed
+step against its model (oracle/mixed.py); the bar is bit-for-bit
+equality."""
 import numpy as np
 import pytest
 
+import mixed as M
 import oracle as O
 import porous_setup
-from wolfd2_gb300.gpu import PREC_MIXED, Solver, W2Error
+from wolfd2_gb300.gpu import PREC_MIXED, Solver
 
 pytestmark = pytest.mark.gpu
 
@@ -69,14 +71,38 @@ def test_porous_time_loop(layout):
     s.close()
 
 
-def test_porous_mixed_step_rejected():
-    """The FP32 momentum of the mixed step has no porous terms: the step
-    reports W2_E_UNSUPPORTED (6) instead of running without them."""
-    case = porous_setup.case("row")
+UVP_REL_TOL = 1e-6  # a few mixed steps, velocity on max(|u|, |v|)
+P_DYN_TOL = 4e-6    # p on max(max |p|, U^2)
+
+
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_porous_mixed_time_loop_matches_model(layout):
+    """The mixed step on porous layouts: the FP32 momentum divides its
+    ConvCoef values by the porosities and adds the PorosCoef terms in single
+    precision (the tables rounded to FP32, as the oracle's single-precision
+    statement rounds them); the Poisson solve takes the unit-stencil kernel
+    ("quad": square cells) or the general-row one ("row": non-square cells;
+    "curvi": curvilinear with cross terms).  Cold start and five steps
+    bit-identical to the model, within the mixed path's tolerances of the
+    FP64 oracle."""
+    case = porous_setup.case(layout)
+    model = M.MixedRun(case, inner=32)
+    model.step(5)
     s = Solver.for_case(case, tuned=False)
     z = s.field()
     s.load_fields(z, z, z)
-    with pytest.raises(W2Error) as e:
-        s.step(case.params, 1, precision=PREC_MIXED)
-    assert e.value.code == 6
+    assert s.cold_start(case.params, precision=PREC_MIXED, refine_sweeps=32) == model.cold_nconv
+    hist = s.step(case.params, 5, precision=PREC_MIXED, refine_sweeps=32)
+    assert [(h[0], h[1]) for h in hist] == [(h[0], h[1]) for h in model.history]
+    for a, b in zip(hist, model.history):
+        assert a[2][:3] == b[2][:3]
+    u, v, p = s.store_fields()
+    for nm, g in (("u", u), ("v", v), ("p", p)):
+        assert np.array_equal(g, model.f[nm]), nm
+    ref = O.OracleRun(case)
+    ref.step(5)
+    assert [h[1] for h in hist] == [h[1] for h in ref.history]
+    scale = max(float(np.max(np.abs(ref.f["u"]))), float(np.max(np.abs(ref.f["v"]))))
+    assert max(float(np.max(np.abs(u - ref.f["u"]))), float(np.max(np.abs(v - ref.f["v"])))) / scale <= UVP_REL_TOL
+    assert float(np.max(np.abs(p - ref.f["p"]))) / max(float(np.max(np.abs(ref.f["p"]))), scale ** 2) <= P_DYN_TOL
     s.close()

@@ -1144,11 +1144,22 @@ int wolfd2gpu_create(w2_ctx **out, int mnx, int mny, int mgri, int mgrj, int nx,
     double *pt = dalloc<double>(c, 8 * c->nf);
     if (!pt) return bad(W2_E_CUDA);
     cudaMemcpy(pt, ptab.data(), 8 * c->nf * sizeof(double), cudaMemcpyHostToDevice);
+    // the same tables rounded to FP32 for the mixed step's momentum
+    std::vector<float> pt32(ptab.size());
+    for (size_t q = 0; q < ptab.size(); ++q) pt32[q] = (float)ptab[q];
+    float *pf = dalloc<float>(c, 8 * c->nf);
+    if (!pf) return bad(W2_E_CUDA);
+    cudaMemcpy(pf, pt32.data(), 8 * c->nf * sizeof(float), cudaMemcpyHostToDevice);
     d.porous = 1;
-    for (int k = 0; k < 4; ++k) d.por.div[k] = pt + k * c->nf;
+    for (int k = 0; k < 4; ++k) {
+      d.por.div[k] = pt + k * c->nf;
+      d.por.div32[k] = pf + k * c->nf;
+    }
     for (int k = 0; k < 2; ++k) {
       d.por.c1[k] = pt + (4 + 2 * k) * c->nf;
       d.por.c2[k] = pt + (5 + 2 * k) * c->nf;
+      d.por.c1_32[k] = pf + (4 + 2 * k) * c->nf;
+      d.por.c2_32[k] = pf + (5 + 2 * k) * c->nf;
     }
   }
   d.nx = nx; d.ny = ny; d.ld = c->ld;
@@ -1208,6 +1219,8 @@ int wolfd2gpu_create(w2_ctx **out, int mnx, int mny, int mgri, int mgrj, int nx,
     if (cudaFuncSetAttribute((const void *)k_naux, cudaFuncAttributeMaxDynamicSharedMemorySize, wmax) !=
             cudaSuccess ||
         cudaFuncSetAttribute((const void *)k_naux32, cudaFuncAttributeMaxDynamicSharedMemorySize, wmax) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute((const void *)k_naux32_por, cudaFuncAttributeMaxDynamicSharedMemorySize, wmax) !=
             cudaSuccess)
       return bad(W2_E_CUDA);
   }
@@ -1986,7 +1999,6 @@ static int check_params(w2_ctx *c, const w2_params *prm) {
     return fail(c, W2_E_ARG, "bad solver parameters");
   if (prm->precision == W2_PREC_MIXED) {
     if (prm->refine_sweeps < 0) return fail(c, W2_E_ARG, "refine_sweeps < 0");
-    if (c->porous) return fail(c, W2_E_UNSUPPORTED, "porous regions run the plain FP64 step");
     return mixed_check(c, prm->lcartes, prm->npsolver);
   }
   if (prm->precision != W2_PREC_FP64)
@@ -2162,12 +2174,14 @@ int issue_steps(w2_ctx *c, const w2_params *prm, int nsteps, StepOut *d_outs) {
         k_copy_mixed<<<gb, c->threads, 0, c->st>>>(d, p, pn, un, vn, un32, vn32, us32, vs32);
         CK(cudaGetLastError());
       }
-      int blocks = pick_blocks(c, (const void *)k_naux32, (long)c->nx * c->ny, naux_smem(c));
+      // porous regions: the instance with the porous terms compiled in
+      const void *kn = c->porous ? (const void *)k_naux32_por : (const void *)k_naux32;
+      int blocks = pick_blocks(c, kn, (long)c->nx * c->ny, naux_smem(c));
       ProfScope ps(c, W2_K_MOMENTUM);
       int mq = prm->mqiter;
       double dk = prm->dk, re = prm->re, qtol = prm->qtol;
       void *args[] = {&d, &mq, &dk, &re, &qtol, &un32, &vn32, &us32, &vs32, &us, &vs, &o};
-      if ((rc = coop(c, (const void *)k_naux32, blocks, args, naux_smem(c)))) break;
+      if ((rc = coop(c, kn, blocks, args, naux_smem(c)))) break;
     } else {
       ProfScope ps(c, W2_K_COPY);
       c->launches++;

@@ -32,8 +32,8 @@ enum : uint16_t {
   MK_PCY = 1u << 9,   // Y PorosCoef value from a porous region (momentum.f:1200-1209)
 };
 
-// Porous regions on the FP64 momentum path, from a host replay of the
-// region loops: div[0..1] are the porosities the X division loop
+// Porous regions on the momentum path (FP64, and FP32 in the mixed step),
+// from a host replay of the region loops: div[0..1] are the porosities the X division loop
 // (momentum.f:296-324) applies to a cell, first and second (1 where it
 // applies fewer: a cell on the shared border of two porous regions is
 // divided twice), div[2..3] those of the Y loop (momentum.f:621-649);
@@ -42,6 +42,9 @@ enum : uint16_t {
 struct Porous {
   const double *div[4];
   const double *c1[2], *c2[2];
+  // the same tables rounded to FP32, for the mixed path's FP32 momentum
+  const float *div32[4];
+  const float *c1_32[2], *c2_32[2];
 };
 
 // Metric arrays (grid.f:368-535), device copies in the padded layout.

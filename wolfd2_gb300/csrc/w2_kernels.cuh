@@ -195,12 +195,15 @@ __global__ void __launch_bounds__(kMaxThreads, 1) k_naux(Dev d, int mqiter, doub
 }
 
 // nAuxMomentum in single precision (mixed path) on un32, vn32 -> us32, vs32,
-// then us, vs = the FP32 results widened to FP64 on every cell.
+// then us, vs = the FP32 results widened to FP64 on every cell.  POR: the
+// porous terms are compiled in (a case with porous regions; without them
+// the kernel keeps the registers those terms would take).
+template <bool POR = false>
 __device__ __forceinline__ void naux32_body(const Dev &d, int mqiter, double dk, double re, double qtol,
                                             const float *un, const float *vn, float *us, float *vs,
                                             double *us64, double *vs64, StepOut *out) {
   int res = -1;
-  if (!naux_momentum<float>(d, d.f32, mqiter, dk, re, qtol, un, vn, us, vs, &res)) return;
+  if (!naux_momentum<float, POR>(d, d.f32, mqiter, dk, re, qtol, un, vn, us, vs, &res)) return;
   if (vblock() == 0 && threadIdx.x == 0) out->nql = res;
   const int W = d.nx + 2, H = d.ny + 2;
   for (int t = gtid(); t < W * H; t += gthreads()) {
@@ -217,6 +220,17 @@ __global__ void __launch_bounds__(kMaxThreads, 1) k_naux32(Dev d, int mqiter, do
   vgrid_set(0, gridDim.x);
   if (step_skip(d)) return;
   naux32_body(d, mqiter, dk, re, qtol, un, vn, us, vs, us64, vs64, out);
+}
+
+// The same with the porous terms of momentum.f:296-324, 621-649 and
+// 1115-1226 in single precision.
+__global__ void __launch_bounds__(kMaxThreads, 1) k_naux32_por(Dev d, int mqiter, double dk, double re,
+                                                            double qtol, const float *un,
+                                                            const float *vn, float *us, float *vs,
+                                                            double *us64, double *vs64, StepOut *out) {
+  vgrid_set(0, gridDim.x);
+  if (step_skip(d)) return;
+  naux32_body<true>(d, mqiter, dk, re, qtol, un, vn, us, vs, us64, vs64, out);
 }
 
 // Time-level copies of the mixed step: p = pn, and the single-precision

@@ -23,8 +23,9 @@
 // constants where the host found them so.  Non-porous regions contribute
 // exact zeros (PorosCoef writes 0, so dk2*cpj adds +0 to a value >= 1 and
 // the RHS terms vanish), and the rows leave those terms out; with porous
-// regions (FP64 path) M1 divides the ConvCoef values by the porosities and
-// the rows add the PorosCoef terms, formed where they are used.  The
+// regions (either path, the tables rounded to FP32 on the mixed one) M1
+// divides the ConvCoef values by the porosities and the rows add the
+// PorosCoef terms, formed where they are used.  The
 // buoyancy term of the y rows (momentum.f:703) is formed when the host gives
 // a density (FP64 path); with zero density it is zero and left out.
 #pragma once
@@ -115,16 +116,37 @@ __device__ __forceinline__ T conv_y2_c2(const Dev &d, const MomView<T> &V, const
           V.yzc(i, j) * (u[IX(d, i, j)] + u[IX(d, i - 1, j)])) * T(0.5);
 }
 
-// ---- porous regions (FP64 path) -----------------------------------------
+// ---- porous regions ------------------------------------------------------
+// The host-replayed tables in the arithmetic type of the step: the FP64
+// tables, or their FP32 roundings (the reference's porosities and porous
+// constants rounded to single, as the single-precision statement rounds
+// them).
+template <class T>
+__device__ __forceinline__ const T *por_div(const Dev &d, int k) {
+  if constexpr (std::is_same<T, double>::value) return d.por.div[k];
+  else return d.por.div32[k];
+}
+template <class T>
+__device__ __forceinline__ const T *por_c1(const Dev &d, int k) {
+  if constexpr (std::is_same<T, double>::value) return d.por.c1[k];
+  else return d.por.c1_32[k];
+}
+template <class T>
+__device__ __forceinline__ const T *por_c2(const Dev &d, int k) {
+  if constexpr (std::is_same<T, double>::value) return d.por.c2[k];
+  else return d.por.c2_32[k];
+}
+
 // The porosity division of the six ConvCoef arrays of X (momentum.f:296-324)
 // and of Y (momentum.f:621-649) at one cell, in the order of the region
 // loops; a divisor of 1 leaves a value's bits unchanged.  Every cell the
 // loops divide lies inside the ranges M1 writes.
-__device__ __forceinline__ void poros_divide(const Dev &d, const MomView<double> &V, size_t o) {
-  const double x0 = d.por.div[0][o], x1 = d.por.div[1][o];
-  const double y0 = d.por.div[2][o], y1 = d.por.div[3][o];
-  double *xs[6] = {V.cj1x, V.cj2x, V.c1sx, V.c2sx, V.c1nx, V.c2nx};
-  double *ys[6] = {V.cj1y, V.cj2y, V.c1sy, V.c2sy, V.c1ny, V.c2ny};
+template <class T>
+__device__ __forceinline__ void poros_divide(const Dev &d, const MomView<T> &V, size_t o) {
+  const T x0 = por_div<T>(d, 0)[o], x1 = por_div<T>(d, 1)[o];
+  const T y0 = por_div<T>(d, 2)[o], y1 = por_div<T>(d, 3)[o];
+  T *xs[6] = {V.cj1x, V.cj2x, V.c1sx, V.c2sx, V.c1nx, V.c2nx};
+  T *ys[6] = {V.cj1y, V.cj2y, V.c1sy, V.c2sy, V.c1ny, V.c2ny};
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
     xs[k][o] = xs[k][o] / x0 / x1;
@@ -134,39 +156,39 @@ __device__ __forceinline__ void poros_divide(const Dev &d, const MomView<double>
 
 // PorosCoef (momentum.f:1115-1226) at (i, j) for X (momentum.f:1186-1196;
 // as there, only the last v of the four is divided by 4) ...
-__device__ __forceinline__ double poros_cp_x(const Dev &d, int njacob, const double *u, const double *v,
-                                             int i, int j) {
+template <class T>
+__device__ __forceinline__ T poros_cp_x(const Dev &d, int njacob, const T *u, const T *v, int i, int j) {
   const size_t o = IX(d, i, j);
-  if (!(d.mask[o] & MK_PCX)) return 0.0;
-  const double t = v[o] + v[IX(d, i + 1, j)] + v[IX(d, i, j - 1)] + v[IX(d, i + 1, j - 1)] / 4.0;
-  double unorm = sqrt(u[o] * u[o] + t * t);
-  double unrm1 = 0.0;
-  if (unorm > 1.0e-8) unrm1 = (u[o] * u[o]) / unorm;
+  if (!(d.mask[o] & MK_PCX)) return T(0);
+  const T t = v[o] + v[IX(d, i + 1, j)] + v[IX(d, i, j - 1)] + v[IX(d, i + 1, j - 1)] / T(4.0);
+  T unorm = sqrt(u[o] * u[o] + t * t);
+  T unrm1 = T(0);
+  if (unorm > T(1.0e-8)) unrm1 = (u[o] * u[o]) / unorm;
   if (njacob == 1) unorm = unrm1 + unorm;
-  return d.por.c1[0][o] + d.por.c2[0][o] * unorm;
+  return por_c1<T>(d, 0)[o] + por_c2<T>(d, 0)[o] * unorm;
 }
 
 // ... and for Y (momentum.f:1200-1209).
-__device__ __forceinline__ double poros_cp_y(const Dev &d, int njacob, const double *u, const double *v,
-                                             int i, int j) {
+template <class T>
+__device__ __forceinline__ T poros_cp_y(const Dev &d, int njacob, const T *u, const T *v, int i, int j) {
   const size_t o = IX(d, i, j);
-  if (!(d.mask[o] & MK_PCY)) return 0.0;
-  const double t = (u[IX(d, i - 1, j + 1)] + u[IX(d, i, j + 1)] + u[IX(d, i - 1, j)] + u[o]) / 4.0;
-  double unorm = sqrt(t * t + v[o] * v[o]);
-  double unrm1 = 0.0;
-  if (unorm > 1.0e-8) unrm1 = (v[o] * v[o]) / unorm;
+  if (!(d.mask[o] & MK_PCY)) return T(0);
+  const T t = (u[IX(d, i - 1, j + 1)] + u[IX(d, i, j + 1)] + u[IX(d, i - 1, j)] + u[o]) / T(4.0);
+  T unorm = sqrt(t * t + v[o] * v[o]);
+  T unrm1 = T(0);
+  if (unorm > T(1.0e-8)) unrm1 = (v[o] * v[o]) / unorm;
   if (njacob == 1) unorm = unrm1 + unorm;
-  return d.por.c1[1][o] + d.por.c2[1][o] * unorm;
+  return por_c1<T>(d, 1)[o] + por_c2<T>(d, 1)[o] * unorm;
 }
 
-template <class T>
+template <bool POR>
 __device__ __forceinline__ bool porous_on(const Dev &d) {
-  if constexpr (std::is_same<T, double>::value) return d.porous != 0;
+  if constexpr (POR) return d.porous != 0;
   return false;
 }
 
 // ---- M1: ConvCoef outputs into arrays (FP64 path) -----------------------
-template <class T>
+template <class T, bool POR = std::is_same<T, double>::value>
 __device__ void mom_conv_coef(const Dev &d, const MomView<T> &V, const T *us, const T *vs,
                               const T *un, const T *vn) {
   const int W = d.nx + 2, H = d.ny + 2;
@@ -200,8 +222,8 @@ __device__ void mom_conv_coef(const Dev &d, const MomView<T> &V, const T *us, co
       V.c2sy[o] = conv_y2_c2(d, V, us, vs, i, j);
       V.c2ny[o] = conv_y2_c2(d, V, un, vn, i, j);
     }
-    if constexpr (std::is_same<T, double>::value) {
-      if (d.porous) poros_divide(d, V, o);
+    if constexpr (POR) {
+      if (d.porous) poros_divide<T>(d, V, o);
     }
   }
 }
@@ -284,7 +306,7 @@ __device__ __forceinline__ T ycj(const Dev &d, const MomView<T> &V, const T *us,
 
 // ---- M2a: stencils and split-1 rows ------------------------------------
 // X row t of split 1 (i = t % nx + 1, j = t / nx + 2; momentum.f:350-384).
-template <class T>
+template <class T, bool POR = std::is_same<T, double>::value>
 __device__ __forceinline__ ChainRow<T> x_row1(const Dev &d, const MomView<T> &V, T re1, T dk2,
                                               const T *us, const T *vs, const T *un, const T *vn,
                                               int t) {
@@ -324,19 +346,17 @@ __device__ __forceinline__ ChainRow<T> x_row1(const Dev &d, const MomView<T> &V,
     r.a3 = rkj * (xcj(d, V, us, vs, 1, i + 1, j) - re1 * racp);
   }
   r.b = un[o] - us[o] + rkj * (-cnvs - cnvn) + rkj * re1 * (difs + difn);
-  if constexpr (std::is_same<T, double>::value) {
-    if (d.porous) {
-      // + dk2 cpj on the diagonal, - dk2 (cps us + cpn un) on the right
-      r.a2 = r.a2 + dk2 * poros_cp_x(d, 1, us, vs, i, j);
-      r.b = r.b - dk2 * (poros_cp_x(d, 0, us, vs, i, j) * us[o] + poros_cp_x(d, 0, un, vn, i, j) * un[o]);
-    }
+  if (porous_on<POR>(d)) {
+    // + dk2 cpj on the diagonal, - dk2 (cps us + cpn un) on the right
+    r.a2 = r.a2 + dk2 * poros_cp_x<T>(d, 1, us, vs, i, j);
+    r.b = r.b - dk2 * (poros_cp_x<T>(d, 0, us, vs, i, j) * us[o] + poros_cp_x<T>(d, 0, un, vn, i, j) * un[o]);
   }
   return r;
 }
 
 // Y row q of split 1 (i = q % (nx-1) + 2, j = q / (nx-1) + 1; momentum.f:675-711),
 // with the buoyancy term of momentum.f:703 when a density is given (FP64).
-template <class T>
+template <class T, bool POR = std::is_same<T, double>::value>
 __device__ __forceinline__ ChainRow<T> y_row1(const Dev &d, const MomView<T> &V, T re1, T dk2,
                                               double dk, const T *us, const T *vs, const T *un,
                                               const T *vn, int q) {
@@ -369,24 +389,22 @@ __device__ __forceinline__ ChainRow<T> y_row1(const Dev &d, const MomView<T> &V,
   // dk2 cpj enters before the 1 (momentum.f:689-697); rows without porous
   // regions leave the (zero) term out
   T pj = T(0);
-  if constexpr (std::is_same<T, double>::value) {
-    if (d.porous) pj = dk2 * poros_cp_y(d, 1, us, vs, i, j);
-  }
+  if (porous_on<POR>(d)) pj = dk2 * poros_cp_y<T>(d, 1, us, vs, i, j);
   if (cj1 >= T(0)) {
     r.a1 = rkj * (-ycj(d, V, us, vs, 1, i - 1, j) - re1 * ranw);
-    r.a2 = porous_on<T>(d) ? rkj * (cj1 + re1 * (ran0 + ranw)) + pj + T(1.0)
+    r.a2 = porous_on<POR>(d) ? rkj * (cj1 + re1 * (ran0 + ranw)) + pj + T(1.0)
                            : rkj * (cj1 + re1 * (ran0 + ranw)) + T(1.0);
     r.a3 = rkj * (-re1 * ran0);
   } else {
     r.a1 = rkj * (-re1 * ranw);
-    r.a2 = porous_on<T>(d) ? rkj * (-cj1 + re1 * (ran0 + ranw)) + pj + T(1.0)
+    r.a2 = porous_on<POR>(d) ? rkj * (-cj1 + re1 * (ran0 + ranw)) + pj + T(1.0)
                            : rkj * (-cj1 + re1 * (ran0 + ranw)) + T(1.0);
     r.a3 = rkj * (ycj(d, V, us, vs, 1, i + 1, j) - re1 * ran0);
   }
   T rhs = vn[o] - vs[o] + rkj * (-cnvs - cnvn) + rkj * re1 * (difs + difn);
+  if (porous_on<POR>(d))
+    rhs = rhs - dk2 * (poros_cp_y<T>(d, 0, us, vs, i, j) * vs[o] + poros_cp_y<T>(d, 0, un, vn, i, j) * vn[o]);
   if constexpr (std::is_same<T, double>::value) {
-    if (d.porous)
-      rhs = rhs - dk2 * (poros_cp_y(d, 0, us, vs, i, j) * vs[o] + poros_cp_y(d, 0, un, vn, i, j) * vn[o]);
     if (d.den) {
       // buoy = dk (d(i,j+1) + d(i,j) + dn(i,j+1) + dn(i,j)) / (4 fr)
       const size_t on = IX(d, i, j + 1);
@@ -398,7 +416,7 @@ __device__ __forceinline__ ChainRow<T> y_row1(const Dev &d, const MomView<T> &V,
   return r;
 }
 
-template <class T>
+template <class T, bool POR = std::is_same<T, double>::value>
 __device__ void mom_assemble1(const Dev &d, const MomView<T> &V, double dk, double re,
                               const T *us, const T *vs, const T *un, const T *vn) {
   const int nx = d.nx, ny = d.ny;
@@ -409,7 +427,7 @@ __device__ void mom_assemble1(const Dev &d, const MomView<T> &V, double dk, doub
   for (int t = gtid(); t < nX + nY; t += gthreads()) {
     if (t < nX) {
       const int px = cpos(V.x1, t);
-      const ChainRow<T> r = x_row1(d, V, re1, dk2, us, vs, un, vn, t);
+      const ChainRow<T> r = x_row1<T, POR>(d, V, re1, dk2, us, vs, un, vn, t);
       V.x1.a1[px] = r.a1;
       V.x1.a2[px] = r.a2;
       V.x1.a3[px] = r.a3;
@@ -418,7 +436,7 @@ __device__ void mom_assemble1(const Dev &d, const MomView<T> &V, double dk, doub
       // Y rows: i = 2..nx, j = 1..ny, ind = (j-1)*(nx-1) + i-2
       const int q = t - nX;
       const int py = cpos(V.y1, q);
-      const ChainRow<T> r = y_row1(d, V, re1, dk2, dk, us, vs, un, vn, q);
+      const ChainRow<T> r = y_row1<T, POR>(d, V, re1, dk2, dk, us, vs, un, vn, q);
       V.y1.a1[py] = r.a1;
       V.y1.a2[py] = r.a2;
       V.y1.a3[py] = r.a3;
@@ -431,7 +449,7 @@ __device__ void mom_assemble1(const Dev &d, const MomView<T> &V, double dk, doub
 // (momentum.f:432-496, 760-821), into the split-1 row storage ------------
 // X row t of split 2 (its right-hand side, the split-1 solution, stays in
 // place; b is left 0).
-template <class T>
+template <class T, bool POR = std::is_same<T, double>::value>
 __device__ __forceinline__ ChainRow<T> x_row2(const Dev &d, const MomView<T> &V, T re1, T dk2,
                                               const T *us, const T *vs, int t) {
   const int nx = d.nx;
@@ -452,14 +470,12 @@ __device__ __forceinline__ ChainRow<T> x_row2(const Dev &d, const MomView<T> &V,
     r.a2 = T(1.0) + rkj * (-cj2 + re1 * (rgn0 + rgns));
     r.a3 = rkj * (xcj(d, V, us, vs, 2, i, j + 1) - re1 * rgn0);
   }
-  if constexpr (std::is_same<T, double>::value) {
-    if (d.porous) r.a2 = r.a2 + dk2 * poros_cp_x(d, 1, us, vs, i, j);
-  }
+  if (porous_on<POR>(d)) r.a2 = r.a2 + dk2 * poros_cp_x<T>(d, 1, us, vs, i, j);
   r.b = T(0);
   return r;
 }
 
-template <class T>
+template <class T, bool POR = std::is_same<T, double>::value>
 __device__ __forceinline__ ChainRow<T> y_row2(const Dev &d, const MomView<T> &V, T re1, T dk2,
                                               const T *us, const T *vs, int q) {
   const int nx = d.nx;
@@ -472,17 +488,15 @@ __device__ __forceinline__ ChainRow<T> y_row2(const Dev &d, const MomView<T> &V,
   const T rkj = dk2 * V.djv(i, j);
   const T cj2 = ycj(d, V, us, vs, 2, i, j), rgc0 = V.rgc(i, j), rgcn = V.rgc(i, j + 1);
   T pj = T(0);
-  if constexpr (std::is_same<T, double>::value) {
-    if (d.porous) pj = dk2 * poros_cp_y(d, 1, us, vs, i, j);
-  }
+  if (porous_on<POR>(d)) pj = dk2 * poros_cp_y<T>(d, 1, us, vs, i, j);
   if (cj2 >= T(0)) {
     r.a1 = rkj * (-ycj(d, V, us, vs, 2, i, j - 1) - re1 * rgc0);
-    r.a2 = porous_on<T>(d) ? rkj * (cj2 + re1 * (rgcn + rgc0)) + pj + T(1.0)
+    r.a2 = porous_on<POR>(d) ? rkj * (cj2 + re1 * (rgcn + rgc0)) + pj + T(1.0)
                            : rkj * (cj2 + re1 * (rgcn + rgc0)) + T(1.0);
     r.a3 = rkj * (-re1 * rgcn);
   } else {
     r.a1 = rkj * (-re1 * rgc0);
-    r.a2 = porous_on<T>(d) ? rkj * (-cj2 + re1 * (rgcn + rgc0)) + pj + T(1.0)
+    r.a2 = porous_on<POR>(d) ? rkj * (-cj2 + re1 * (rgcn + rgc0)) + pj + T(1.0)
                            : rkj * (-cj2 + re1 * (rgcn + rgc0)) + T(1.0);
     r.a3 = rkj * (ycj(d, V, us, vs, 2, i, j + 1) - re1 * rgcn);
   }
@@ -490,7 +504,7 @@ __device__ __forceinline__ ChainRow<T> y_row2(const Dev &d, const MomView<T> &V,
   return r;
 }
 
-template <class T>
+template <class T, bool POR = std::is_same<T, double>::value>
 __device__ void mom_assemble2(const Dev &d, const MomView<T> &V, double dk, double re,
                               const T *us, const T *vs) {
   const int nx = d.nx, ny = d.ny;
@@ -500,7 +514,7 @@ __device__ void mom_assemble2(const Dev &d, const MomView<T> &V, double dk, doub
   for (int t = gtid(); t < nX + nY; t += gthreads()) {
     if (t < nX) {
       const int px = cpos(V.x2, t);
-      const ChainRow<T> r = x_row2(d, V, re1, dk2, us, vs, t);
+      const ChainRow<T> r = x_row2<T, POR>(d, V, re1, dk2, us, vs, t);
       // identity rows: the split-1 solution, read next only as this rhs
       if (d.mask[IX(d, t % nx + 1, t / nx + 2)] & MK_XID) V.x2.b[px] = T(0);
       V.x2.a1[px] = r.a1;
@@ -509,7 +523,7 @@ __device__ void mom_assemble2(const Dev &d, const MomView<T> &V, double dk, doub
     } else {
       const int q = t - nX;
       const int py = cpos(V.y2, q);
-      const ChainRow<T> r = y_row2(d, V, re1, dk2, us, vs, q);
+      const ChainRow<T> r = y_row2<T, POR>(d, V, re1, dk2, us, vs, q);
       if (d.mask[IX(d, q % (nx - 1) + 2, q / (nx - 1) + 1)] & MK_YID) V.y2.b[py] = T(0);
       V.y2.a1[py] = r.a1;
       V.y2.a2[py] = r.a2;
@@ -540,7 +554,7 @@ __device__ void mom_update(const Dev &d, const MomView<T> &V, T *us, T *vs, unsi
 }
 
 // The whole nAuxMomentum.  Returns nQLiter (or -1) in *out; false on error.
-template <class T>
+template <class T, bool POR = std::is_same<T, double>::value>
 __device__ bool naux_momentum(const Dev &d, const MomView<T> &V, int mqiter, double dk, double re,
                               double qtol, const T *un, const T *vn, T *us, T *vs, int *out) {
   Sync *sy = d.sync;
@@ -551,7 +565,7 @@ __device__ bool naux_momentum(const Dev &d, const MomView<T> &V, int mqiter, dou
         set_error(sy, W2_E_BCFLAG);
       if (!grid_sync(sy)) return false;
     }
-    if constexpr (!kFuseConv<T>) mom_conv_coef(d, V, us, vs, un, vn);
+    if constexpr (!kFuseConv<T>) mom_conv_coef<T, POR>(d, V, us, vs, un, vn);
     if (vblock() == 0 && threadIdx.x == 0) {
       if (it == 1) sy->red[1] = 0ull;
       sy->red[(it + 1) % 3] = 0ull;
@@ -559,10 +573,10 @@ __device__ bool naux_momentum(const Dev &d, const MomView<T> &V, int mqiter, dou
     if constexpr (!kFuseConv<T>) {
       if (!grid_sync(sy)) return false;
     }
-    mom_assemble1(d, V, dk, re, us, vs, un, vn);
+    mom_assemble1<T, POR>(d, V, dk, re, us, vs, un, vn);
     if (!grid_sync(sy)) return false;
     if (!solve_chains(d, V.x1, V.y1, 2)) return false;
-    mom_assemble2(d, V, dk, re, us, vs);
+    mom_assemble2<T, POR>(d, V, dk, re, us, vs);
     if (!grid_sync(sy)) return false;
     if (!solve_chains(d, V.x2, V.y2, 2)) return false;
     mom_update(d, V, us, vs, &sy->red[it % 3]);
