@@ -201,3 +201,18 @@ def test_read_deck_small_scale_keywords(tmp_path):
     assert (a.tscoef, a.hscoef, a.temcoef, a.rlc, a.fpu, a.sorrel) == (1.0, 1.0, 1.0, 5.0, 500.0, 1.0)
     assert a.pe == pytest.approx(r.params.re * 0.71, rel=1e-12) and a.tref == 300.0
     assert r.thermal is not None and r.tparams is None
+
+
+def test_clustered_cavity_cells():
+    """The wall-clustered cavity: monotone nodes on the unit square, cell
+    widths from (1 - beta)/n at the walls to (1 + beta)/n in the middle,
+    the same in x and y."""
+    n = 64
+    case = deck.clustered_cavity(n, 1000.0, 1e-4, solver="rb_sor")
+    x = case.x[:, 0]
+    y = case.y[0, :]
+    dx = np.diff(x)
+    assert x[0] == 0.0 and abs(x[-1] - 1.0) < 1e-15
+    assert np.all(dx > 0)
+    assert abs(dx.min() * n - 0.5) < 0.01 and abs(dx.max() * n - 1.5) < 0.01
+    assert np.allclose(x, y)

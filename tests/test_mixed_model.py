@@ -158,3 +158,23 @@ def test_general_model_stops_where_fp64_stops(layout, sortol):
                              regions=case.regions, lcartes=prm.lcartes)
     assert n64 < 3000 and nm == n64
     assert _rel(pm, p64) <= (1e-12 if sortol < 1e-8 else P_REL_TOL)
+
+
+@pytest.mark.parametrize("layout", ["nonsquare", "blockage", "curvilinear"])
+def test_general_model_time_loop_close_to_fp64(layout):
+    """The mixed time loop with general Poisson rows (FP32 momentum, general
+    FP32 sweeps with FP64 refinement): the oracle's Q-L and sweep counts
+    over three steps, velocity within 1e-6 of the FP64 oracle."""
+    case = _general_layouts()[layout]
+    case.params.sortol = 1e-9
+    u0, v0, p0 = deck.perturbation_ic(case, 5)
+    fields = {"u": u0, "v": v0, "p": p0}
+    mx = M.MixedRun(case, fields=fields, cold_start=False, inner=32)
+    assert mx.general
+    mx.step(3)
+    ref = O.OracleRun(case, fields=fields, cold_start=False)
+    ref.step(3)
+    assert [h[:2] for h in mx.history] == [h[:2] for h in ref.history]
+    scale = max(float(np.max(np.abs(ref.f["u"]))), float(np.max(np.abs(ref.f["v"]))))
+    err = max(float(np.max(np.abs(mx.f["u"] - ref.f["u"]))), float(np.max(np.abs(mx.f["v"] - ref.f["v"]))))
+    assert err / scale <= 1e-6
