@@ -282,7 +282,6 @@ __device__ __forceinline__ void bc_body(const Dev &d, int ops, double *u, double
 __global__ void k_bc(Dev d, int ops, double *u, double *v, double *p) {
   vgrid_set(0, gridDim.x);
   if (step_skip(d)) return;
-  if (step_skip(d)) return;
   bc_body(d, ops, u, v, p);
 }
 
