@@ -422,7 +422,7 @@ int wolfd2gpu_profile_read(w2_ctx *ctx, int kind, double *total_ms,
  * precision: W2_PREC_MIXED (rb_sor or rb_sorp in every case; unit-row
  * cases on the multi-tile kernel, which needs a Cartesian grid, the others
  * on the general-row kernel) or W2_PREC_FP64 (any grid and any of the six
- * Poisson solvers, per case).  Filter is not applied (W2_E_UNSUPPORTED).
+ * Poisson solvers, per case).  Filter (nfiltu, nfiltv) runs per case.
  * Per case, results are bit-identical to wolfd2gpu_step on that context
  * alone.
  *

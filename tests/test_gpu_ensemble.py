@@ -197,3 +197,33 @@ def test_mixed_ensemble_general_rows_matches_cases_alone(graph):
     ens.close()
     for s in solvers:
         s.close()
+
+
+@pytest.mark.parametrize("precision", [PREC_MIXED, PREC_FP64])
+def test_ensemble_filter_matches_cases_alone(precision):
+    """Filter of us and/or vs after nAuxMomentum (utility.f:33-247, main.f:
+    783-791) in some cases of an ensemble, none in others: per case
+    bit-identical to the case alone."""
+    cases = _cases()[:3] + [_general_cases()[1]]
+    flags = [(1, 1, 4.0), (1, 0, 2.5), (0, 0, 0.0), (0, 1, 6.0)]
+    for (case, _), (fu, fv, fp) in zip(cases, flags):
+        case.params.nfiltu, case.params.nfiltv = fu, fv
+        case.params.fpu = case.params.fpv = fp
+    nsteps = 3
+    solvers = []
+    for case, f in cases:
+        s = Solver.for_case(case, tuned=False)
+        s.load_fields(*f)
+        solvers.append(s)
+    ens = Ensemble(solvers)
+    hist = ens.step([c.params for c, _ in cases], nsteps, refine_sweeps=REFINE, precision=precision)
+    for k, ((case, f), s) in enumerate(zip(cases, solvers)):
+        ref_hist, ref = _alone(case, f, nsteps, precision=precision)
+        assert [(h[0], h[1]) for h in hist[k]] == [(h[0], h[1]) for h in ref_hist], k
+        assert [h[2][:3] for h in hist[k]] == [h[2][:3] for h in ref_hist], k
+        got = s.store_fields()
+        for name, g, r in zip("uvp", got, ref):
+            assert np.array_equal(g, r), (k, name, float(np.max(np.abs(g - r))))
+    ens.close()
+    for s in solvers:
+        s.close()

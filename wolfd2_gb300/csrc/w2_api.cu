@@ -2391,7 +2391,7 @@ struct w2_ens {
   const char *mixed_why = "";  // why not, when not
   bool graph_on = false;
   cudaGraphExec_t gexec = nullptr;
-  int graph_nsteps = -1, graph_prec = -1;
+  int graph_nsteps = -1, graph_prec = -1, graph_filter = -1;
   long long launches = 0;
   double last_ms = 0.0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -2545,10 +2545,19 @@ void ens_prof_collect(w2_ens *e) {
 
 // One step's launches: mixed (Lp: the Poisson partition) or plain FP64
 // (every stage on the momentum partition Lm).
-int ens_launch_step(w2_ens *e, bool mixed, const EnsLaunch &Lm, const EnsLaunch &Lp, const EnsLaunch &L1,
-                    bool capturing = false) {
+int ens_launch_step(w2_ens *e, bool mixed, bool filt, const EnsLaunch &Lm, const EnsLaunch &Lp,
+                    const EnsLaunch &L1, bool capturing = false) {
   EnsLaunch am = Lm, ap = Lp;
   void *argm[] = {&am}, *argp[] = {&ap};
+  // Filter of us, vs in the cases that ask for it, after nAuxMomentum
+  auto filter = [&]() -> int {
+    if (!filt) return W2_OK;
+    ke_filter<<<e->blocks_m, e->threads, 0, e->st>>>(Lm, 0);
+    ke_filter<<<e->blocks_m, e->threads, 0, e->st>>>(Lm, 1);
+    ECK(cudaGetLastError());
+    if (!capturing) e->launches += 2;
+    return W2_OK;
+  };
   if (!mixed) {
     {
       EnsProf pr(e, W2_ENS_COPY, capturing);
@@ -2560,6 +2569,7 @@ int ens_launch_step(w2_ens *e, bool mixed, const EnsLaunch &Lm, const EnsLaunch 
       ECK(cudaLaunchCooperativeKernel((const void *)ke_naux, dim3(e->blocks_m), dim3(e->threads), argm,
                                       e->smem_m, e->st));
     }
+    if (int rc = filter()) return rc;
     {
       EnsProf pr(e, W2_ENS_BC, capturing);
       ke_bc<<<e->n, e->threads, 0, e->st>>>(L1);
@@ -2581,6 +2591,7 @@ int ens_launch_step(w2_ens *e, bool mixed, const EnsLaunch &Lm, const EnsLaunch 
       ECK(cudaLaunchCooperativeKernel((const void *)ke_naux32, dim3(e->blocks_m), dim3(e->threads), argm,
                                       e->smem_m, e->st));
     }
+    if (int rc = filter()) return rc;
     {
       EnsProf pr(e, W2_ENS_BC, capturing);
       ke_bc<<<e->n, e->threads, 0, e->st>>>(L1);
@@ -2802,7 +2813,6 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
                    "case %d: in an ensemble the mixed step takes lCartesGrid = 0 only on grids whose rows are not "
                    "the unit stencil", k);
     if (q.npsolver < 1 || q.npsolver > 6) return efail(e, W2_E_ARG, "case %d: bad Poisson solver %d", k, q.npsolver);
-    if (q.nfiltu == 1 || q.nfiltv == 1) return efail(e, W2_E_UNSUPPORTED, "case %d: the ensemble does not apply Filter", k);
     if (q.msorit < 1 || q.mqiter < 1 || q.refine_sweeps < 0) return efail(e, W2_E_ARG, "case %d: bad parameters", k);
   }
   if (nsteps == 0) return W2_OK;
@@ -2815,6 +2825,7 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
     }
   }
   // descriptors of this call: parameters, starting levels
+  bool filt = false;
   for (int k = 0; k < n; ++k) {
     const w2_params &q = prm[k];
     EnsCase &h = e->h[k];
@@ -2828,6 +2839,13 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
     h.msorit = q.msorit;
     h.sortol = q.sortol;
     h.sorrel = q.sorrel;
+    h.nfiltu = q.nfiltu == 1;
+    h.nfiltv = q.nfiltv == 1;
+    h.fpu = q.fpu;
+    h.fpv = q.fpv;
+    h.hu = e->cs[k]->stage[4];
+    h.hv = e->cs[k]->stage[5];
+    filt = filt || h.nfiltu || h.nfiltv;
     for (int b = 0; b < 2; ++b) {
       MixedArgs &a = h.a[b];
       a.lcartes = q.lcartes;
@@ -2862,7 +2880,7 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
   const EnsLaunch Lp{e->d_cases, e->d_first_p, n, e->d_step, e->d_outs, nsteps};
   const EnsLaunch L1{e->d_cases, e->d_first_1, n, e->d_step, e->d_outs, nsteps};
   const int prec = mixed ? W2_PREC_MIXED : W2_PREC_FP64;
-  if (e->graph_on && (e->graph_nsteps != nsteps || e->graph_prec != prec)) {
+  if (e->graph_on && (e->graph_nsteps != nsteps || e->graph_prec != prec || e->graph_filter != (int)filt)) {
     if (e->gexec) {
       cudaGraphExecDestroy(e->gexec);
       e->gexec = nullptr;
@@ -2870,7 +2888,7 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
     cudaGraph_t g = nullptr;
     ECK(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
     const long long l0 = e->launches;
-    int rc = ens_launch_step(e, mixed, Lm, Lp, L1, true);
+    int rc = ens_launch_step(e, mixed, filt, Lm, Lp, L1, true);
     e->launches = l0;
     cudaError_t ce = cudaStreamEndCapture(e->st, &g);
     if (rc) return rc;
@@ -2880,13 +2898,14 @@ int wolfd2gpu_ens_step(w2_ens *e, const w2_params *prm, int nsteps, w2_stepstat 
     if (ce != cudaSuccess) return efail(e, W2_E_CUDA, "graph instantiation: %s", cudaGetErrorString(ce));
     e->graph_nsteps = nsteps;
     e->graph_prec = prec;
+    e->graph_filter = (int)filt;
   }
   ECK(cudaEventRecord(e->ev0, e->st));
   for (int s = 0; s < nsteps; ++s) {
     if (e->graph_on) {
       ECK(cudaGraphLaunch(e->gexec, e->st));
-      e->launches += 6;
-    } else if (int rc = ens_launch_step(e, mixed, Lm, Lp, L1)) {
+      e->launches += filt ? 8 : 6;
+    } else if (int rc = ens_launch_step(e, mixed, filt, Lm, Lp, L1)) {
       return rc;
     }
   }

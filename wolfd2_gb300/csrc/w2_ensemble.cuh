@@ -33,6 +33,9 @@ struct EnsCase {
   double sortol, sorrel;
   int general;             // Poisson rows not the unit stencil in FP32: the
   MixgArgs ga[2];          // general-row mixed Ppe, forming level 0 / 1
+  int nfiltu, nfiltv;      // Filter of us, vs after nAuxMomentum (main.f:783-791)
+  double fpu, fpv;
+  double *hu, *hv;         // its results before they replace us, vs
 };
 
 // Arguments shared by the launches of one ensemble step.
@@ -82,6 +85,30 @@ __global__ void __launch_bounds__(kMaxThreads, 1) ke_naux32(EnsLaunch L) {
   const int b = ens_level(e, L) ^ 1;
   naux32_body(e.d, e.mqiter, e.dk, e.re, e.qtol, e.F32[0], e.F32[1], e.F32[2], e.F32[3], e.U[b],
               e.V[b], ens_out(L, k));
+}
+
+// Filter of us and vs after nAuxMomentum (utility.f:33-247, main.f:783-791):
+// phase 0 filters into the scratch fields, phase 1 copies them back (the
+// filter of a cell reads its neighbours' unfiltered values, so the copy
+// waits for the launch boundary).  Cases without Filter do nothing.
+__global__ void ke_filter(EnsLaunch L, int phase) {
+  const int k = ens_enter(L.first, L.n);
+  const EnsCase &e = L.cs[k];
+  if (e.d.sync->halt || !(e.nfiltu || e.nfiltv)) return;
+  const int b = ens_level(e, L) ^ 1;
+  const Dev &d = e.d;
+  const int W = d.nx + 2, H = d.ny + 2;
+  for (int t = gtid(); t < W * H; t += gthreads()) {
+    const int i = t % W, j = t / W;
+    const size_t o = IX(d, i, j);
+    if (phase == 0) {
+      if (e.nfiltu) e.hu[o] = filter_point(d, MK_FU, e.fpu, e.U[b], i, j);
+      if (e.nfiltv) e.hv[o] = filter_point(d, MK_FV, e.fpv, e.V[b], i, j);
+    } else {
+      if (e.nfiltu) e.U[b][o] = e.hu[o];
+      if (e.nfiltv) e.V[b][o] = e.hv[o];
+    }
+  }
 }
 
 // Boundary rows before the Poisson solve (one block per case).

@@ -562,17 +562,23 @@ __global__ void k_selftest_wait(Dev d) {
 }
 
 // ---- Filter (utility.f:33-247), velocity components ---------------------
+// The filtered value of cell (i, j) where the mask bit is set, else the
+// value itself.
+__device__ __forceinline__ double filter_point(const Dev &d, int bit, double fp, const double *qu, int i,
+                                               int j) {
+  const size_t o = IX(d, i, j);
+  if (d.mask[o] & bit)
+    return (qu[IX(d, i, j - 1)] + qu[IX(d, i - 1, j)] + qu[IX(d, i, j + 1)] + qu[IX(d, i + 1, j)] +
+            fp * qu[o]) / (fp + 4.0);
+  return qu[o];
+}
+
 __global__ void k_filter(Dev d, int bit, double fp, const double *qu, double *qh) {
   vgrid_set(0, gridDim.x);
   const int W = d.nx + 2, H = d.ny + 2;
   for (int t = gtid(); t < W * H; t += gthreads()) {
     const int i = t % W, j = t / W;
-    const size_t o = IX(d, i, j);
-    if (d.mask[o] & bit)
-      qh[o] = (qu[IX(d, i, j - 1)] + qu[IX(d, i - 1, j)] + qu[IX(d, i, j + 1)] + qu[IX(d, i + 1, j)] +
-               fp * qu[o]) / (fp + 4.0);
-    else
-      qh[o] = qu[o];
+    qh[IX(d, i, j)] = filter_point(d, bit, fp, qu, i, j);
   }
 }
 
