@@ -84,8 +84,8 @@ typedef struct w2_ctx w2_ctx;
  * has porous regions, their porosity and Dupuit-Forchheimer constants
  * (output of PorRegCnst, src/bound_cond.f:1883-1986; may be NULL without
  * porous regions).  Porous regions run in the drop-in nAuxMomentum, the
- * FP64 step and the mixed step (its FP32 momentum on the tables rounded to
- * FP32); the ensemble and the adjoint return W2_E_UNSUPPORTED for them.  Fields are
+ * FP64 step, the mixed step (its FP32 momentum on the tables rounded to
+ * FP32) and ensembles; the adjoint returns W2_E_UNSUPPORTED for them.  Fields are
  * zero.  No reference counterpart (the reference keeps these as static
  * arrays). */
 int wolfd2gpu_create(w2_ctx **ctx, int mnx, int mny, int mgri, int mgrj,

@@ -227,3 +227,33 @@ def test_ensemble_filter_matches_cases_alone(precision):
     ens.close()
     for s in solvers:
         s.close()
+
+
+@pytest.mark.parametrize("precision", [PREC_MIXED, PREC_FP64])
+def test_ensemble_porous_matches_cases_alone(precision):
+    """Porous layouts (two regions sharing a border, three around a
+    non-porous one, a curvilinear pair) beside a plain cavity in one
+    ensemble: per case bit-identical to the case alone, in both
+    precisions."""
+    import porous_setup
+    cases = [(c, deck.perturbation_ic(c, 400 + k))
+             for k, c in enumerate(porous_setup.case(n) for n in ("row", "quad", "curvi"))]
+    cases += _cases()[:1]
+    nsteps = 3
+    solvers = []
+    for case, f in cases:
+        s = Solver.for_case(case, tuned=False)
+        s.load_fields(*f)
+        solvers.append(s)
+    ens = Ensemble(solvers)
+    hist = ens.step([c.params for c, _ in cases], nsteps, refine_sweeps=REFINE, precision=precision)
+    for k, ((case, f), s) in enumerate(zip(cases, solvers)):
+        ref_hist, ref = _alone(case, f, nsteps, precision=precision)
+        assert [(h[0], h[1]) for h in hist[k]] == [(h[0], h[1]) for h in ref_hist], k
+        assert [h[2][:3] for h in hist[k]] == [h[2][:3] for h in ref_hist], k
+        got = s.store_fields()
+        for name, g, r in zip("uvp", got, ref):
+            assert np.array_equal(g, r), (k, name, float(np.max(np.abs(g - r))))
+    ens.close()
+    for s in solvers:
+        s.close()

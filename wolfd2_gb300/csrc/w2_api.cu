@@ -2392,6 +2392,7 @@ struct w2_ens {
   bool graph_on = false;
   cudaGraphExec_t gexec = nullptr;
   int graph_nsteps = -1, graph_prec = -1, graph_filter = -1;
+  bool porous = false;     // some case has porous regions (momentum with the porous terms)
   long long launches = 0;
   double last_ms = 0.0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -2588,7 +2589,8 @@ int ens_launch_step(w2_ens *e, bool mixed, bool filt, const EnsLaunch &Lm, const
     }
     {
       EnsProf pr(e, W2_ENS_MOMENTUM, capturing);
-      ECK(cudaLaunchCooperativeKernel((const void *)ke_naux32, dim3(e->blocks_m), dim3(e->threads), argm,
+      ECK(cudaLaunchCooperativeKernel(e->porous ? (const void *)ke_naux32_por : (const void *)ke_naux32,
+                                      dim3(e->blocks_m), dim3(e->threads), argm,
                                       e->smem_m, e->st));
     }
     if (int rc = filter()) return rc;
@@ -2645,7 +2647,7 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
     w2_ctx *c = e->cs[k];
     if (!c) return bad(efail(e, W2_E_ARG, "case %d is null", k));
     if (int rc = ready(c)) return bad(efail(e, rc, "case %d: %s", k, c->err));
-    if (c->porous) return bad(efail(e, W2_E_UNSUPPORTED, "case %d: porous regions run single-case steps", k));
+    if (c->porous) e->porous = true;
     if (c->therm_on)
       return bad(efail(e, W2_E_UNSUPPORTED, "case %d: ensembles do not run the energy equation", k));
     if (k == 0) e->device = c->device;
@@ -2671,7 +2673,7 @@ int wolfd2gpu_ens_create(w2_ens **out, w2_ctx *const *cases, int n, int threads,
   // by the co-residency of all of them
   e->smem_m = walk_stage_bytes(sizeof(double), threads);
   int occ = 1 << 20;
-  for (const void *kf : {(const void *)ke_naux32, (const void *)ke_naux}) {
+  for (const void *kf : {(const void *)ke_naux32, (const void *)ke_naux32_por, (const void *)ke_naux}) {
     if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem_m) != cudaSuccess)
       return bad(efail(e, W2_E_CUDA, "shared memory attribute (momentum)"));
     int o = 0;

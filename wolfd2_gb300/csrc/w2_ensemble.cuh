@@ -78,14 +78,21 @@ __global__ void ke_copy_mixed(EnsLaunch L) {
   copy_mixed_body(e.d, e.P[b], e.P[a], e.U[a], e.V[a], e.F32[0], e.F32[1], e.F32[2], e.F32[3]);
 }
 
-__global__ void __launch_bounds__(kMaxThreads, 1) ke_naux32(EnsLaunch L) {
+template <bool POR>
+__device__ __forceinline__ void ens_naux32(const EnsLaunch &L) {
   const int k = ens_enter(L.first, L.n);
   const EnsCase &e = L.cs[k];
   if (e.d.sync->halt) return;
   const int b = ens_level(e, L) ^ 1;
-  naux32_body(e.d, e.mqiter, e.dk, e.re, e.qtol, e.F32[0], e.F32[1], e.F32[2], e.F32[3], e.U[b],
-              e.V[b], ens_out(L, k));
+  naux32_body<POR>(e.d, e.mqiter, e.dk, e.re, e.qtol, e.F32[0], e.F32[1], e.F32[2], e.F32[3], e.U[b],
+                   e.V[b], ens_out(L, k));
 }
+
+__global__ void __launch_bounds__(kMaxThreads, 1) ke_naux32(EnsLaunch L) { ens_naux32<false>(L); }
+
+// With the porous terms compiled in: launched when some case has porous
+// regions (the others skip the terms at run time).
+__global__ void __launch_bounds__(kMaxThreads, 1) ke_naux32_por(EnsLaunch L) { ens_naux32<true>(L); }
 
 // Filter of us and vs after nAuxMomentum (utility.f:33-247, main.f:783-791):
 // phase 0 filters into the scratch fields, phase 1 copies them back (the
