@@ -18,15 +18,16 @@
 // kernel; on unit rows every operation rounds as the unit form does (1 x ==
 // x, x / -4 == x * -0.25).
 //
-// Layout: colour-split FP32 planes in global memory (they stay in L2: 16
-// floats a cell).  Cell (i, j) lives in the plane of its colour (i+j)&1 at
+// Layout: colour-split FP32 planes in global memory (they stay in L2: 8
+// floats a cell, each in the plane of the cell's colour).  Cell (i, j) lives in the plane of its colour (i+j)&1 at
 // j*gw + (i >> 1), so the points of one colour in a row are contiguous and
 // a point's east/west neighbours are the other plane's entries k and k-1 or
 // k+1.  Cells off the unknowns hold e = 0 (the ghost pressures stay frozen
 // during the iteration, so their correction is zero) and are never written.
 // One grid barrier separates the colours, one ends the sweep (and, with
-// lcartes = 0, one follows the cross-term pass).  Cartesian grids run the
-// tiled form at the end of this file instead, K sweeps per grid barrier.
+// lcartes = 0, one follows the cross-term pass).  Single cases on Cartesian
+// grids run the tiled form at the end of this file by default, K sweeps
+// per grid barrier; ensembles run this form on every general-row case.
 #pragma once
 #include "w2_ppe.cuh"
 #include "w2_ppe_mixed.cuh"
