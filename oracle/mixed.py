@@ -139,10 +139,13 @@ def ppe_mixed_general(nx: int, ny: int, met, u, v, p, dk: float, msorit: int, so
     FP32 (c_k = a_k): per sweep (lcartes = 0: r' = r - the cross terms of e
     in FP32, with rbu, rbv rounded to FP32, formed before the sweep as the
     reference forms its right-hand side), black points then red,
-    s = r' - c1 eS - c2 eW - c4 eE - c5 eN, s = s / c3 - e, e = e + sorrel s,
-    dif = max |s|.  Stopping rule and pass lengths as ppe_mixed.  On unit
-    rows every operation equals the unit form's bit for bit (1 x == x,
-    x / -4 == x * -0.25)."""
+    s = r' - c1 eS - c2 eW - c4 eE - c5 eN, s = s * (1/c3) - e,
+    e = e + sorrel s, dif = max |s|, where 1/c3 is the FP32 reciprocal of
+    the rounded diagonal (the reference divides, pressure.f:437; a product
+    by the reciprocal is one rounding of a different operator, which the
+    FP64 residual of the next pass corrects like any FP32 error).  Stopping
+    rule and pass lengths as ppe_mixed.  On unit rows every operation
+    equals the unit form's bit for bit (1 x == x, 1/-4 == -0.25 exactly)."""
     f32 = np.float32
     a1, a2, a3, a4, a5 = (a.copy() for a in ppe_rows(nx, ny, met))
     idn = blockage_rows(nx, ny, regions)[2:nx + 1, 2:ny + 1]
@@ -153,6 +156,7 @@ def ppe_mixed_general(nx: int, ny: int, met, u, v, p, dk: float, msorit: int, so
     div[idn] = 0.0
     b = div / dk
     c1, c2, c3, c4, c5 = (a.astype(f32) for a in (a1, a2, a3, a4, a5))
+    rc3 = f32(1.0) / c3
     rbu32, rbv32 = met["rbu"].astype(f32), met["rbv"].astype(f32)
     I, J = np.meshgrid(np.arange(2, nx + 1), np.arange(2, ny + 1), indexing="ij")
     cols = []
@@ -179,7 +183,7 @@ def ppe_mixed_general(nx: int, ny: int, met, u, v, p, dk: float, msorit: int, so
                 c0 = E[ii, jj]
                 s = RR[sel] - c1[sel] * E[ii, jj - 1] - c2[sel] * E[ii - 1, jj] - \
                     c4[sel] * E[ii + 1, jj] - c5[sel] * E[ii, jj + 1]
-                s = s / c3[sel] - c0
+                s = s * rc3[sel] - c0
                 E[ii, jj] = c0 + relax * s
                 if s.size:
                     dif = max(dif, np.max(np.abs(s)))

@@ -394,8 +394,8 @@ __global__ void __launch_bounds__(kMixgtThreads, 1) k_ppe_mixgt(Dev d, MixgtGeom
   if (vblock() == 0 && threadIdx.x == 0) out->nsor = nconv < 1 ? a.msorit : nconv;
 }
 
-// Its FP32 rows c1..c5 in field layout (every unknown; zeros elsewhere
-// from the allocation).
+// Its FP32 rows c1..c5 in field layout, the diagonal as its FP32
+// reciprocal (every unknown; zeros elsewhere from the allocation).
 __global__ void k_mixgt_coef(Dev d, float *c1, float *c2, float *c3, float *c4, float *c5) {
   vgrid_set(0, gridDim.x);
   const int nx = d.nx, ny = d.ny;
@@ -403,7 +403,7 @@ __global__ void k_mixgt_coef(Dev d, float *c1, float *c2, float *c3, float *c4, 
     const size_t o = IX(d, t % (nx - 1) + 2, t / (nx - 1) + 2);
     c1[o] = (float)d.pa1[o];
     c2[o] = (float)d.pa2[o];
-    c3[o] = (float)d.pa3[o];
+    c3[o] = 1.0f / (float)d.pa3[o];
     c4[o] = (float)d.pa4[o];
     c5[o] = (float)d.pa5[o];
   }

@@ -12,11 +12,14 @@
 // first forms r' = r - (cross terms of e, FP32) when lcartes = 0 -- the
 // reference forms its right-hand side once per sweep from the current p --
 // then updates the black points, then the red ones:
-//   s = r' - c1 eS - c2 eW - c4 eE - c5 eN;  s = s / c3 - e;  e = e + sorrel s
-// with max |s| as the sweep's dif.  Sweep counts, the stopping rule (sweep
-// m > 1 and dif < sortol) and the pass lengths are those of the unit-stencil
-// kernel; on unit rows every operation rounds as the unit form does (1 x ==
-// x, x / -4 == x * -0.25).
+//   s = r' - c1 eS - c2 eW - c4 eE - c5 eN;  s = s * (1/c3) - e;  e = e + sorrel s
+// with max |s| as the sweep's dif, 1/c3 the FP32 reciprocal of the rounded
+// diagonal, formed once with the coefficients (the reference divides; the
+// product is one rounding of a slightly different FP32 operator, and the
+// next pass's FP64 residual corrects it like any FP32 error).  Sweep counts,
+// the stopping rule (sweep m > 1 and dif < sortol) and the pass lengths are
+// those of the unit-stencil kernel; on unit rows every operation rounds as
+// the unit form does (1 x == x, 1/-4 == -0.25 exactly).
 //
 // Layout: colour-split FP32 planes in global memory (they stay in L2: 8
 // floats a cell, each in the plane of the cell's colour).  Cell (i, j) lives in the plane of its colour (i+j)&1 at
@@ -56,8 +59,9 @@ __device__ __forceinline__ float *mixg_plane(const MixgArgs &a, int ny, int q) {
 }
 __device__ __forceinline__ int mixg_pos(const MixgArgs &a, int i, int j) { return j * a.gw + (i >> 1); }
 
-// The rows rounded to FP32 into the coefficient planes (every unknown; the
-// planes' other cells stay as the allocation's zeros).
+// The rows rounded to FP32 into the coefficient planes, the diagonal as its
+// FP32 reciprocal (every unknown; the planes' other cells stay as the
+// allocation's zeros).
 __device__ void mixg_coefficients(const Dev &d, const MixgArgs &a) {
   const int nx = d.nx, ny = d.ny;
   for (int t = gtid(); t < (nx - 1) * (ny - 1); t += gthreads()) {
@@ -66,7 +70,7 @@ __device__ void mixg_coefficients(const Dev &d, const MixgArgs &a) {
     const int c = (i + j) & 1, x = mixg_pos(a, i, j);
     mixg_plane(a, ny, MG_C1 + c)[x] = (float)d.pa1[o];
     mixg_plane(a, ny, MG_C2 + c)[x] = (float)d.pa2[o];
-    mixg_plane(a, ny, MG_C3 + c)[x] = (float)d.pa3[o];
+    mixg_plane(a, ny, MG_C3 + c)[x] = 1.0f / (float)d.pa3[o];
     mixg_plane(a, ny, MG_C4 + c)[x] = (float)d.pa4[o];
     mixg_plane(a, ny, MG_C5 + c)[x] = (float)d.pa5[o];
   }
@@ -194,7 +198,7 @@ __device__ unsigned int mixg_half(const Dev &d, const MixgArgs &a, int c, float 
       s = s - c2[q] * ew[q];
       s = s - c4[q] * ee[q];
       s = s - c5[q] * en[q];
-      s = s / c3[q];
+      s = s * c3[q];
       s = s - e0[q];
       if (ok[q]) {
         Ec[x[q]] = e0[q] + relax * s;
@@ -421,7 +425,7 @@ __device__ unsigned int mixgt_half(float *S, const MixgtBox &b, int bi0, int bi1
       s = s - c2[q] * ew[q];
       s = s - c4[q] * ee[q];
       s = s - c5[q] * en[q];
-      s = s / c3[q];
+      s = s * c3[q];
       s = s - e0[q];
       if (ok[q]) E[x[q]] = e0[q] + relax * s;
       if (own[q]) {
